@@ -1,0 +1,58 @@
+"""Extract golden vectors from the reference's own unit tests.
+
+Reads ``test/unit/test_gfn2_xtb.f90`` of the reference repository (as text;
+nothing is compiled or run) and writes ``atoms_gfn2.json`` next to this
+file: GFN2-xTB total energies of isolated atoms Z = 1..86 for the neutral,
+cation and anion cases, with the unpaired-electron counts the reference
+uses, the accuracy (0.01) and the tolerance (10*sqrt(eps)) of that test
+(reference ``test/unit/test_gfn2_xtb.f90:34-36,61-272``).
+
+Isolated atoms need no coordination-number or dispersion data, so these
+energies pin the basis, the on-site integrals, the self energies, the
+shell-resolved Coulomb / third-order terms, Fermi smearing, the entropy term
+and the Broyden-mixed SCF of the oracle and of the CUDA engine.
+
+Usage: ``python tests/golden/make_golden.py [REFERENCE_ROOT]``
+"""
+from __future__ import annotations
+
+import json
+import re
+import sys
+from pathlib import Path
+
+
+def _array(block: str, name: str):
+    m = re.search(name + r"\(86\) = \[(.*?)\]", block, re.S)
+    body = re.sub(r"[&\s]", "", m.group(1))
+    return [v.replace("_wp", "") for v in body.split(",")]
+
+
+def main():
+    root = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+    text = (root / "test/unit/test_gfn2_xtb.f90").read_text()
+    out = {"source": "reference test/unit/test_gfn2_xtb.f90:61-272", "accuracy": 0.01,
+           "kt": 300.0 * 3.166808578545117e-06, "thr": 10 * (2.220446049250313e-16) ** 0.5,
+           "cases": {}}
+    for key, sub, charge in (("neutral", "test_e_pse(", 0), ("cation", "test_e_pse_cation(", 1),
+                             ("anion", "test_e_pse_anion(", -1)):
+        i = text.index("subroutine " + sub)
+        j = text.index("end subroutine", i)
+        block = text[i:j]
+        uhf = [int(v) for v in _array(block, "uhf")]
+        ref = [float(v) for v in _array(block, "ref")]
+        skip = []
+        m = re.search(r"if \(any\(izp == \[([\d, ]+)\]\)\) cycle", block)
+        if m:
+            skip = [int(v) for v in m.group(1).split(",")]
+        m = re.search(r"if \(izp == (\d+)\) cycle", block)
+        if m:
+            skip.append(int(m.group(1)))
+        out["cases"][key] = {"charge": charge, "uhf": uhf, "energy": ref, "skip": skip}
+    dst = Path(__file__).resolve().parent / "atoms_gfn2.json"
+    dst.write_text(json.dumps(out, indent=1))
+    print("wrote", dst)
+
+
+if __name__ == "__main__":
+    main()
