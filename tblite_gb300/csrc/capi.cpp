@@ -1,0 +1,949 @@
+// C ABI of the GB300 engine: error / context / structure / calculator / result objects and the
+// single-point driver (reference src/tblite/api/*.f90 for the object conventions and
+// src/tblite/xtb/singlepoint.f90:73-433 for the driver).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/tblite.h"
+#include "element_data.inc"
+#include "engine.h"
+#include "params_gfn2.inc"
+
+using namespace tb;
+
+// --------------------------------------------------------------------------------------
+// objects
+// --------------------------------------------------------------------------------------
+struct _tblite_error {
+  std::string msg;
+  bool set = false;
+};
+
+struct _tblite_context {
+  std::vector<std::string> errors;
+  tblite_logger_callback logger = nullptr;
+  void* userdata = nullptr;
+  int verbosity = 1;
+  int color = 0;
+  void push(const std::string& m) { errors.push_back(m); }
+  void message(const std::string& m) {
+    if (logger) {
+      std::string tmp = m;
+      logger(nullptr, tmp.data(), (int)tmp.size(), userdata);
+    } else if (verbosity > 0) {
+      printf("%s\n", m.c_str());
+    }
+  }
+};
+
+struct _tblite_structure {
+  int nat = 0;
+  std::vector<int> num;
+  std::vector<double> xyz;  // [nat][3] Bohr
+  double charge = 0.0;
+  int uhf = 0;
+};
+
+namespace {
+
+void cuda_check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess)
+    throw std::runtime_error(std::string("CUDA error '") + cudaGetErrorString(e) + "' in " + what);
+}
+
+template <class T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  void alloc(size_t count) {
+    if (count <= n && p) return;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cuda_check(cudaMalloc(&p, sizeof(T) * std::max<size_t>(count, 1)), "cudaMalloc");
+    n = count;
+  }
+  void upload(const std::vector<T>& h, cudaStream_t s) {
+    alloc(h.size());
+    if (!h.empty())
+      cuda_check(cudaMemcpyAsync(p, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice, s),
+                 "upload");
+  }
+  void download(std::vector<T>& h, size_t count, cudaStream_t s) const {
+    h.resize(count);
+    if (count)
+      cuda_check(cudaMemcpyAsync(h.data(), p, sizeof(T) * count, cudaMemcpyDeviceToHost, s),
+                 "download");
+  }
+  ~DBuf() {
+    if (p) cudaFree(p);
+  }
+};
+
+}  // namespace
+
+struct Workspace {
+  cudaStream_t stream = nullptr;
+  int nat = -1, nsh = -1, nao = -1, memory = -1;
+  // static molecule/basis data
+  DBuf<double> xyz, sh_alpha, sh_coeff, sh_se0, sh_kcn, sh_shpoly, sh_zeta, sh_hub, sh_gam3,
+      sh_refocc, at_en, at_rad, at_rcov, at_mprad, at_vcn, at_dkern, at_qkern, at_repa, at_repz;
+  DBuf<int> at_z, at_sh, sh_atom, sh_l, sh_nprim, sh_ao, ao_sh, ao_at;
+  // geometry dependent
+  DBuf<double> cn, se, mrad, dmrdcn, S, H, D, Q, F, C, P, W, emo, focc, scratch;
+  // SCF state
+  DBuf<double> qsh, qat, dpat, qpat, qsh_o, qat_o, dpat_o, qpat_o, vsh, vat, vdp, vqp, vao;
+  DBuf<double> mull, eband, eelec, erep, vec_out, scal;
+  DBuf<int> icount;
+  // Broyden
+  DBuf<double> b_q, b_qlast, b_dq, b_dqlast, b_df, b_u, b_a, b_omega, b_work;
+  DBuf<int> b_status;
+  // gradient
+  DBuf<double> grad, sigma, sig_at, dEdcn;
+  EigenSolver* eig = nullptr;
+  ~Workspace() {
+    if (eig) eigen_destroy(eig);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+struct _tblite_calculator {
+  // molecule-bound basis (built at construction)
+  int nat = 0, nsh = 0, nao = 0;
+  std::vector<int> at_z, at_sh, sh_atom, sh_l, sh_nprim, sh_ao, ao_sh, ao_at;
+  std::vector<double> sh_alpha, sh_coeff, sh_se0, sh_kcn, sh_shpoly, sh_zeta, sh_hub, sh_gam3,
+      sh_refocc, at_en, at_rad, at_rcov, at_mprad, at_vcn, at_dkern, at_qkern, at_repa, at_repz;
+  double min_alpha = 1e300;
+  // settings (reference api/calculator.f90:78-89, scf/mixer/input.f90:28-34)
+  double accuracy = 1.0;
+  double etemp = 300.0 * 3.166808578545117e-06;
+  int max_iter = 250;
+  double damping = 0.4;
+  int memory = 0;
+  int guess = TBLITE_GUESS_SAD;
+  int save_integrals = 0;
+  bool anneal = false;
+  double anneal_kt = 0.0;
+  int anneal_hold = 50, anneal_cycles = 50;
+  std::unique_ptr<Workspace> ws;
+};
+
+struct _tblite_result {
+  int nat = 0, nsh = 0, nao = 0;
+  bool has_energy = false, has_wfn = false;
+  double energy = 0.0;
+  std::vector<double> energies, gradient, sigma, qat, qsh, dpat, qpat, emo, focc, P, C, S, H, wbo;
+  double dipole[3] = {0, 0, 0}, quadrupole[6] = {0, 0, 0, 0, 0, 0};
+};
+
+// --------------------------------------------------------------------------------------
+// STO-nG expansion, reference src/tblite/basis/slater.f90:409-511
+// --------------------------------------------------------------------------------------
+static void slater_to_gauss(int ng, int n, int l, double zeta, double* alpha, double* coeff) {
+  int ityp;
+  if (l == 0) ityp = n;
+  else if (l == 1) ityp = 4 + n;
+  else if (l == 2) ityp = 7 + n;
+  else throw std::runtime_error("angular momentum above d is not supported");
+  const double* pa = nullptr;
+  const double* pc = nullptr;
+  if (ng == 1) {
+    alpha[0] = STO_ALPHA1[ityp - 1] * zeta * zeta;
+    coeff[0] = 1.0;
+  } else {
+    if (ng == 6 && n == 6) {
+      pa = l == 0 ? STO_ALPHA6S : STO_ALPHA6P;
+      pc = l == 0 ? STO_COEFF6S : STO_COEFF6P;
+    } else {
+      const double* A[] = {nullptr, nullptr, STO_ALPHA2, STO_ALPHA3, STO_ALPHA4, STO_ALPHA5, STO_ALPHA6};
+      const double* Cc[] = {nullptr, nullptr, STO_COEFF2, STO_COEFF3, STO_COEFF4, STO_COEFF5, STO_COEFF6};
+      pa = A[ng] + (ityp - 1) * ng;
+      pc = Cc[ng] + (ityp - 1) * ng;
+    }
+    for (int k = 0; k < ng; ++k) {
+      alpha[k] = pa[k] * zeta * zeta;
+      coeff[k] = pc[k];
+    }
+  }
+  static const double dfac[8] = {1, 1, 3, 15, 105, 945, 10395, 135135};  // (2l-1)!!
+  const double top = 2.0 / M_PI;
+  for (int k = 0; k < ng; ++k)
+    coeff[k] = coeff[k] * pow(top * alpha[k], 0.75) * pow(sqrt(4 * alpha[k]), l) / sqrt(dfac[l]);
+}
+
+static void build_calculator(_tblite_calculator* c, const _tblite_structure* mol) {
+  c->nat = mol->nat;
+  c->at_z = mol->num;
+  c->at_sh.assign(1, 0);
+  c->nsh = 0;
+  c->nao = 0;
+  for (int i = 0; i < mol->nat; ++i) {
+    const int z = mol->num[i];
+    if (z < 1 || z > 86) throw std::runtime_error("No support for elements with Z > 86.");
+    const int ns = GFN2_NSHELL[z - 1];
+    for (int s = 0; s < ns; ++s) {
+      const int l = GFN2_ANG_SHELL[(z - 1) * 3 + s];
+      if (l > 1)
+        throw std::runtime_error("element Z=" + std::to_string(z) +
+                                 " has d shells, which the CUDA integral kernels do not handle yet");
+      const int pqn = GFN2_PRINCIPAL_QUANTUM_NUMBER[(z - 1) * 3 + s];
+      const int ng = GFN2_NUMBER_OF_PRIMITIVES[(z - 1) * 3 + s];
+      const double zeta = GFN2_SLATER_EXPONENT[(z - 1) * 3 + s];
+      double a[MAXG] = {0}, cc[MAXG] = {0};
+      slater_to_gauss(ng, pqn, l, zeta, a, cc);
+      for (int k = 0; k < MAXG; ++k) {
+        c->sh_alpha.push_back(a[k]);
+        c->sh_coeff.push_back(cc[k]);
+        if (k < ng) c->min_alpha = std::min(c->min_alpha, a[k]);
+      }
+      c->sh_atom.push_back(i);
+      c->sh_l.push_back(l);
+      c->sh_nprim.push_back(ng);
+      c->sh_ao.push_back(c->nao);
+      c->sh_zeta.push_back(zeta);
+      c->sh_se0.push_back(GFN2_P_SELFENERGY[(z - 1) * 3 + s]);
+      c->sh_kcn.push_back(GFN2_P_KCN[(z - 1) * 3 + l]);
+      c->sh_shpoly.push_back(GFN2_P_SHPOLY[(z - 1) * 3 + l]);
+      c->sh_hub.push_back(GFN2_HUBBARD_PARAMETER[z - 1] * GFN2_SHELL_HUBBARD[(z - 1) * 3 + l]);
+      c->sh_gam3.push_back(GFN2_P_HUBBARD_DERIVS[z - 1] * GFN2_SHELL_HUBBARD_DERIVS[l]);
+      c->sh_refocc.push_back(GFN2_REFERENCE_OCC[(z - 1) * 3 + l]);
+      for (int m = 0; m < 2 * l + 1; ++m) {
+        c->ao_sh.push_back(c->nsh);
+        c->ao_at.push_back(i);
+      }
+      c->nao += 2 * l + 1;
+      c->nsh += 1;
+    }
+    c->at_sh.push_back(c->nsh);
+    // external element data: needed only when the molecule has pairs
+    const bool need = mol->nat > 1;
+    const double en = EXT_EN[z - 1], rad = EXT_RAD[z - 1], rcov = EXT_RCOV[z - 1];
+    if (need && (std::isnan(en) || std::isnan(rad) || std::isnan(rcov)))
+      throw std::runtime_error(std::string("element data pack '") + EXT_PACK_NAME +
+                               "' has no entry for Z=" + std::to_string(z));
+    c->at_en.push_back(need ? en : 0.0);
+    c->at_rad.push_back(need ? rad : 1.0);
+    c->at_rcov.push_back(need ? rcov : 1.0);
+    c->at_mprad.push_back(GFN2_P_RAD[z - 1]);
+    c->at_vcn.push_back(GFN2_P_VCN[z - 1]);
+    c->at_dkern.push_back(GFN2_P_DKERNEL[z - 1]);
+    c->at_qkern.push_back(GFN2_P_QKERNEL[z - 1]);
+    c->at_repa.push_back(GFN2_REP_ALPHA[z - 1]);
+    c->at_repz.push_back(GFN2_REP_ZEFF[z - 1]);
+  }
+}
+
+static Gfn2Scalars gfn2_scalars(const _tblite_calculator* c) {
+  Gfn2Scalars p{};
+  p.wexp = GFN2_WEXP;
+  p.enscale = GFN2_ENSCALE;
+  p.gexp = GFN2_GEXP;
+  for (int a = 0; a < 5; ++a)
+    for (int b = 0; b < 5; ++b) p.kshell[a][b] = GFN2_KSHELL[a * 5 + b];
+  p.mp_dmp3 = GFN2_MP_DMP3;
+  p.mp_dmp5 = GFN2_MP_DMP5;
+  p.mp_shift = GFN2_MP_SHIFT;
+  p.mp_kexp = GFN2_MP_KEXP;
+  p.mp_rmax = GFN2_MP_RMAX;
+  p.rep_kexp = GFN2_REP_KEXP;
+  p.rep_kexp_light = GFN2_REP_KEXP_LIGHT;
+  p.rep_rexp = GFN2_REP_REXP;
+  p.rep_cutoff = 25.0;
+  p.cn_ka = EXT_CN_KA;
+  p.cn_kb = EXT_CN_KB;
+  p.cn_rshift = EXT_CN_RSHIFT;
+  p.cn_cutoff = EXT_CN_CUTOFF;
+  // get_cutoff, reference basis/type.f90:227-247
+  p.h0_cutoff = std::min(sqrt(2.0 * INTCUT / c->min_alpha), 40.0);
+  return p;
+}
+
+// --------------------------------------------------------------------------------------
+// single point driver
+// --------------------------------------------------------------------------------------
+static void ensure_workspace(_tblite_calculator* c) {
+  if (!c->ws) {
+    c->ws.reset(new Workspace());
+    cuda_check(cudaStreamCreateWithFlags(&c->ws->stream, cudaStreamNonBlocking), "stream");
+  }
+  Workspace& w = *c->ws;
+  const int memory = c->memory > 0 ? std::min(c->memory, c->max_iter) : c->max_iter;
+  cudaStream_t s = w.stream;
+  if (w.nat != c->nat || w.nao != c->nao || w.nsh != c->nsh) {
+    const size_t n = c->nao, nn = n * n;
+    w.sh_alpha.upload(c->sh_alpha, s);
+    w.sh_coeff.upload(c->sh_coeff, s);
+    w.sh_se0.upload(c->sh_se0, s);
+    w.sh_kcn.upload(c->sh_kcn, s);
+    w.sh_shpoly.upload(c->sh_shpoly, s);
+    w.sh_zeta.upload(c->sh_zeta, s);
+    w.sh_hub.upload(c->sh_hub, s);
+    w.sh_gam3.upload(c->sh_gam3, s);
+    w.sh_refocc.upload(c->sh_refocc, s);
+    w.at_en.upload(c->at_en, s);
+    w.at_rad.upload(c->at_rad, s);
+    w.at_rcov.upload(c->at_rcov, s);
+    w.at_mprad.upload(c->at_mprad, s);
+    w.at_vcn.upload(c->at_vcn, s);
+    w.at_dkern.upload(c->at_dkern, s);
+    w.at_qkern.upload(c->at_qkern, s);
+    w.at_repa.upload(c->at_repa, s);
+    w.at_repz.upload(c->at_repz, s);
+    w.at_z.upload(c->at_z, s);
+    w.at_sh.upload(c->at_sh, s);
+    w.sh_atom.upload(c->sh_atom, s);
+    w.sh_l.upload(c->sh_l, s);
+    w.sh_nprim.upload(c->sh_nprim, s);
+    w.sh_ao.upload(c->sh_ao, s);
+    w.ao_sh.upload(c->ao_sh, s);
+    w.ao_at.upload(c->ao_at, s);
+    const size_t nat = c->nat, nsh = c->nsh;
+    w.xyz.alloc(3 * nat);
+    w.cn.alloc(nat);
+    w.se.alloc(nsh);
+    w.mrad.alloc(nat);
+    w.dmrdcn.alloc(nat);
+    w.S.alloc(nn);
+    w.H.alloc(nn);
+    w.D.alloc(3 * nn);
+    w.Q.alloc(6 * nn);
+    w.F.alloc(nn);
+    w.C.alloc(nn);
+    w.P.alloc(nn);
+    w.W.alloc(nn);
+    w.emo.alloc(n);
+    w.focc.alloc(3 * n);
+    w.scratch.alloc(nn);
+    for (auto* b : {&w.qsh, &w.qsh_o, &w.vsh}) b->alloc(nsh);
+    for (auto* b : {&w.qat, &w.qat_o, &w.vat, &w.eband, &w.eelec, &w.erep, &w.dEdcn}) b->alloc(nat);
+    for (auto* b : {&w.dpat, &w.dpat_o, &w.vdp, &w.grad}) b->alloc(3 * nat);
+    for (auto* b : {&w.qpat, &w.qpat_o, &w.vqp}) b->alloc(6 * nat);
+    w.sig_at.alloc(9 * nat);
+    w.sigma.alloc(9);
+    w.vao.alloc(n);
+    w.mull.alloc((size_t)mulliken_chunks((int)n) * 11 * n);
+    w.scal.alloc(8);
+    w.icount.alloc(4);
+    const size_t nd = nsh + 9 * nat;
+    w.vec_out.alloc(nd);
+    if (w.eig) eigen_destroy(w.eig);
+    w.eig = eigen_create((int)n, s);
+    w.nat = c->nat;
+    w.nsh = c->nsh;
+    w.nao = c->nao;
+    w.memory = -1;
+  }
+  if (w.memory != memory) {
+    const size_t nd = c->nsh + 9 * c->nat;
+    for (auto* b : {&w.b_q, &w.b_qlast, &w.b_dq, &w.b_dqlast}) b->alloc(nd);
+    w.b_df.alloc(nd * memory);
+    w.b_u.alloc(nd * memory);
+    w.b_a.alloc((size_t)memory * memory);
+    w.b_omega.alloc(memory);
+    w.b_work.alloc((size_t)memory * memory + 2 * memory + 64);
+    w.b_status.alloc(1);
+    w.memory = memory;
+  }
+}
+
+static DevMol dev_mol(const _tblite_calculator* c) {
+  const Workspace& w = *c->ws;
+  DevMol m{};
+  m.nat = c->nat;
+  m.nsh = c->nsh;
+  m.nao = c->nao;
+  m.xyz = w.xyz.p;
+  m.at_z = w.at_z.p;
+  m.at_sh = w.at_sh.p;
+  m.sh_atom = w.sh_atom.p;
+  m.sh_l = w.sh_l.p;
+  m.sh_nprim = w.sh_nprim.p;
+  m.sh_alpha = w.sh_alpha.p;
+  m.sh_coeff = w.sh_coeff.p;
+  m.sh_ao = w.sh_ao.p;
+  m.ao_sh = w.ao_sh.p;
+  m.ao_at = w.ao_at.p;
+  m.sh_se0 = w.sh_se0.p;
+  m.sh_kcn = w.sh_kcn.p;
+  m.sh_shpoly = w.sh_shpoly.p;
+  m.sh_zeta = w.sh_zeta.p;
+  m.sh_hub = w.sh_hub.p;
+  m.sh_gam3 = w.sh_gam3.p;
+  m.sh_refocc = w.sh_refocc.p;
+  m.at_en = w.at_en.p;
+  m.at_rad = w.at_rad.p;
+  m.at_rcov = w.at_rcov.p;
+  m.at_mprad = w.at_mprad.p;
+  m.at_vcn = w.at_vcn.p;
+  m.at_dkern = w.at_dkern.p;
+  m.at_qkern = w.at_qkern.p;
+  m.at_repa = w.at_repa.p;
+  m.at_repz = w.at_repz.p;
+  return m;
+}
+
+static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
+                        _tblite_calculator* c, _tblite_result* res) {
+  if (mol->nat != c->nat) throw std::runtime_error("structure does not match calculator");
+  ensure_workspace(c);
+  Workspace& w = *c->ws;
+  cudaStream_t s = w.stream;
+  const int nat = c->nat, nsh = c->nsh, n = c->nao;
+  const size_t nd = nsh + 9 * (size_t)nat;
+  const Gfn2Scalars p = gfn2_scalars(c);
+  cuda_check(cudaMemcpyAsync(w.xyz.p, mol->xyz.data(), sizeof(double) * 3 * nat,
+                             cudaMemcpyHostToDevice, s),
+             "xyz");
+  DevMol m = dev_mol(c);
+  // occupation, reference xtb/singlepoint.f90:140-156
+  double nocc = -mol->charge, nel_ref = 0.0;
+  for (int i = 0; i < nsh; ++i) nocc += c->sh_refocc[i];
+  nel_ref = nocc;
+  int nuhf;
+  const int nel_i = (int)lround(nel_ref);
+  if ((mol->uhf % 2) == (nel_i % 2)) {
+    nuhf = mol->uhf;
+  } else {
+    if (mol->uhf != 0)
+      throw std::runtime_error("Total number of electrons (" + std::to_string(nel_i) +
+                               ") and number unpaired electrons (" + std::to_string(mol->uhf) +
+                               ") is not compatible");
+    nuhf = nel_i % 2;
+  }
+  const double diff = std::min((double)nuhf, nocc);
+  const double nalp = (nocc - diff) / 2 + diff, nbet = (nocc - diff) / 2;
+
+  // geometry-dependent setup
+  launch_cn(m, p, w.cn.p, s);
+  launch_setup_levels(m, p, w.cn.p, w.se.p, w.mrad.p, w.dmrdcn.p, s);
+  launch_build_h0(m, p, w.se.p, w.S.p, w.H.p, w.D.p, w.Q.p, s);
+  cuda_check(cudaMemsetAsync(w.grad.p, 0, sizeof(double) * 3 * nat, s), "zero");
+  cuda_check(cudaMemsetAsync(w.sig_at.p, 0, sizeof(double) * 9 * nat, s), "zero");
+  cuda_check(cudaMemsetAsync(w.sigma.p, 0, sizeof(double) * 9, s), "zero");
+  cuda_check(cudaMemsetAsync(w.dEdcn.p, 0, sizeof(double) * nat, s), "zero");
+  launch_repulsion(m, p, w.erep.p, w.grad.p, w.sig_at.p, s);
+  const int chol = eigen_set_overlap(w.eig, w.S.p);
+  if (chol != 0) throw std::runtime_error("overlap matrix is not positive definite");
+
+  // initial guess: restart from a compatible result, else SAD (wavefunction/guess.f90:51-120)
+  std::vector<double> qsh0(nsh), dp0(3 * nat, 0.0), qp0(6 * nat, 0.0), qat0(nat);
+  if (res->has_wfn && res->nat == nat && res->nsh == nsh && res->nao == n) {
+    qsh0 = res->qsh;
+    dp0 = res->dpat;
+    qp0 = res->qpat;
+    qat0 = res->qat;
+  } else {
+    std::vector<double> n0at(nat, 0.0);
+    for (int i = 0; i < nsh; ++i) n0at[c->sh_atom[i]] += c->sh_refocc[i];
+    for (int i = 0; i < nat; ++i) qat0[i] = mol->charge / nat;
+    for (int i = 0; i < nsh; ++i)
+      qsh0[i] = c->sh_refocc[i] / n0at[c->sh_atom[i]] * qat0[c->sh_atom[i]];
+  }
+  w.qsh.upload(qsh0, s);
+  w.dpat.upload(dp0, s);
+  w.qpat.upload(qp0, s);
+  w.qat.upload(qat0, s);
+
+  BroydenState b{};
+  b.ndim = (int)nd;
+  b.memory = w.memory;
+  b.iter = 0;
+  b.damp = c->damping;
+  b.q = w.b_q.p;
+  b.qlast = w.b_qlast.p;
+  b.dq = w.b_dq.p;
+  b.dqlast = w.b_dqlast.p;
+  b.df = w.b_df.p;
+  b.u = w.b_u.p;
+  b.a = w.b_a.p;
+  b.omega = w.b_omega.p;
+  b.work = w.b_work.p;
+  b.status = w.b_status.p;
+
+  const double econv = 1.0e-6 * c->accuracy, pconv = 2.0e-5 * c->accuracy;
+  const double target_kt = c->etemp;
+  double elevated_kt = target_kt;
+  int anneal_hold = 50, anneal_steps = 50;
+  if (c->anneal) {
+    elevated_kt = c->anneal_kt;
+    anneal_hold = std::max(0, c->anneal_hold);
+    anneal_steps = std::max(0, c->anneal_cycles);
+  }
+  std::vector<double> h_eelec(nat, 0.0), h_scal(2);
+  int iscf = 0;
+  bool converged = false;
+  double eelec_sum = 0.0;
+  if (ctx->verbosity > 0) {
+    ctx->message(std::string(60, '-'));
+    ctx->message("  cycle        total energy    energy error   density error");
+    ctx->message(std::string(60, '-'));
+  }
+  std::vector<double> h_erep;
+  w.erep.download(h_erep, nat, s);
+  std::vector<int> h_cnt(1);
+  double kt = target_kt;
+  while (!converged && iscf < c->max_iter) {
+    const double elast = eelec_sum;
+    if (elevated_kt > target_kt) {  // singlepoint.f90:286-296
+      if (iscf < anneal_hold) kt = elevated_kt;
+      else if (anneal_steps > 0 && iscf < anneal_hold + anneal_steps)
+        kt = elevated_kt + (double)(iscf - anneal_hold + 1) / anneal_steps * (target_kt - elevated_kt);
+      else kt = target_kt;
+    }
+    if (iscf > 0) {
+      launch_broyden_next(b, s);
+      int st = 0;
+      cuda_check(cudaMemcpyAsync(&st, w.b_status.p, sizeof(int), cudaMemcpyDeviceToHost, s), "st");
+      cuda_check(cudaStreamSynchronize(s), "sync");
+      if (st != 0) throw std::runtime_error("Broyden mixing failed to obtain next iteration");
+      launch_unpack(m, w.b_q.p, w.qsh.p, w.qat.p, w.dpat.p, w.qpat.p, s);
+    }
+    ++iscf;
+    launch_coulomb_potential(m, p, w.mrad.p, w.qsh.p, w.qat.p, w.dpat.p, w.qpat.p, w.vsh.p, w.vat.p,
+                             w.vdp.p, w.vqp.p, s);
+    launch_vao(m, w.vsh.p, w.vat.p, w.vao.p, s);
+    launch_fock(n, w.ao_at.p, w.H.p, w.S.p, w.D.p, w.Q.p, w.vao.p, w.vdp.p, w.vqp.p, w.F.p, s);
+    launch_pack(m, w.qsh.p, w.dpat.p, w.qpat.p, w.b_q.p, s);  // mixer%set
+    const int info = eigen_solve(w.eig, w.F.p, w.C.p, w.emo.p);
+    if (info != 0)
+      throw std::runtime_error("(sygvd) failed to solve eigenvalue problem. info=" +
+                               std::to_string(info));
+    launch_fermi(n, w.emo.p, nalp, nbet, kt, w.focc.p, w.scal.p, w.icount.p, s);
+    w.icount.download(h_cnt, 1, s);
+    cuda_check(cudaStreamSynchronize(s), "sync");
+    density_matrix(n, h_cnt[0], w.C.p, w.focc.p, w.P.p, w.scratch.p, s);
+    launch_mulliken(m, w.P.p, w.S.p, w.H.p, w.D.p, w.Q.p, w.mull.p, mulliken_chunks(n), w.qsh_o.p,
+                    w.qat_o.p, w.dpat_o.p, w.qpat_o.p, w.eband.p, s);
+    launch_pack(m, w.qsh_o.p, w.dpat_o.p, w.qpat_o.p, w.vec_out.p, s);
+    launch_diff((int)nd, w.vec_out.p, w.b_q.p, w.b_dq.p, w.scal.p + 1, s);  // mixer%diff
+    launch_eelec_init(nat, w.scal.p, w.eband.p, w.eelec.p, s);
+    launch_coulomb_energy(m, p, w.mrad.p, w.qsh_o.p, w.qat_o.p, w.dpat_o.p, w.qpat_o.p, w.eelec.p,
+                          s);
+    w.eelec.download(h_eelec, nat, s);
+    w.scal.download(h_scal, 2, s);
+    cuda_check(cudaStreamSynchronize(s), "sync");
+    eelec_sum = 0.0;
+    for (int i = 0; i < nat; ++i) eelec_sum += h_eelec[i];
+    const bool econv_ok = fabs(eelec_sum - elast) < econv;
+    const bool pconv_ok = h_scal[1] < pconv;
+    converged = econv_ok && pconv_ok && kt <= target_kt;
+    if (ctx->verbosity > 0) {
+      double etot = eelec_sum;
+      for (int i = 0; i < nat; ++i) etot += h_erep[i];
+      char buf[128];
+      snprintf(buf, sizeof(buf), "%7d%24.13g%16.7e%16.7e", iscf, etot, eelec_sum - elast, h_scal[1]);
+      ctx->message(buf);
+    }
+  }
+  // results (singlepoint.f90:315-322)
+  res->nat = nat;
+  res->nsh = nsh;
+  res->nao = n;
+  res->energies.resize(nat);
+  res->energy = 0.0;
+  for (int i = 0; i < nat; ++i) {
+    res->energies[i] = h_erep[i] + h_eelec[i];
+    res->energy += res->energies[i];
+  }
+  res->has_energy = true;
+
+  // gradient (singlepoint.f90:343-381): Coulomb at output moments, H0 with last potential
+  launch_coulomb_gradient(m, p, w.mrad.p, w.dmrdcn.p, w.qsh_o.p, w.qat_o.p, w.dpat_o.p, w.qpat_o.p,
+                          w.grad.p, w.sig_at.p, w.dEdcn.p, s);
+  // W = C diag(f e) C^T  (scf/diag.f90:110-143)
+  launch_fe(n, w.focc.p, w.emo.p, w.vec_out.p, s);
+  density_matrix(n, h_cnt[0], w.C.p, w.vec_out.p, w.W.p, w.scratch.p, s);
+  launch_h0_gradient(m, p, w.se.p, w.P.p, w.W.p, w.vao.p, w.vdp.p, w.vqp.p, w.grad.p, w.sigma.p,
+                     w.dEdcn.p, s);
+  launch_cn_grad(m, p, w.dEdcn.p, w.grad.p, w.sig_at.p, s);
+  w.grad.download(res->gradient, 3 * nat, s);
+  std::vector<double> h_sig_at, h_sigma;
+  w.sig_at.download(h_sig_at, 9 * nat, s);
+  w.sigma.download(h_sigma, 9, s);
+  w.qsh_o.download(res->qsh, nsh, s);
+  w.qat_o.download(res->qat, nat, s);
+  w.dpat_o.download(res->dpat, 3 * nat, s);
+  w.qpat_o.download(res->qpat, 6 * nat, s);
+  w.emo.download(res->emo, n, s);
+  w.focc.download(res->focc, n, s);
+  w.P.download(res->P, (size_t)n * n, s);
+  if (c->save_integrals) {
+    w.S.download(res->S, (size_t)n * n, s);
+    w.H.download(res->H, (size_t)n * n, s);
+  }
+  cuda_check(cudaStreamSynchronize(s), "sync results");
+  res->sigma.assign(9, 0.0);
+  for (int k = 0; k < 9; ++k) {
+    double acc = h_sigma[k];
+    for (int i = 0; i < nat; ++i) acc += h_sig_at[9 * i + k];
+    res->sigma[k] = acc;
+  }
+  res->has_wfn = true;
+  // molecular multipoles (post_processing/molmom.f90)
+  for (int k = 0; k < 3; ++k) res->dipole[k] = 0.0;
+  for (int i = 0; i < nat; ++i)
+    for (int k = 0; k < 3; ++k)
+      res->dipole[k] += mol->xyz[3 * i + k] * res->qat[i] + res->dpat[3 * i + k];
+  if (!converged)
+    throw std::runtime_error("SCF not converged in " + std::to_string(iscf) + " cycles");
+}
+
+// --------------------------------------------------------------------------------------
+// C ABI
+// --------------------------------------------------------------------------------------
+static void copy_msg(const std::string& msg, char* buffer, const int* buffersize) {
+  if (!buffer) return;
+  size_t cap = buffersize ? (size_t)std::max(*buffersize, 0) : msg.size() + 1;
+  if (cap == 0) return;
+  const size_t len = std::min(cap - 1, msg.size());
+  memcpy(buffer, msg.data(), len);
+  buffer[len] = '\0';
+}
+
+static void set_err(tblite_error e, const std::string& m) {
+  if (e) {
+    e->msg = m;
+    e->set = true;
+  }
+}
+
+extern "C" {
+
+int tblite_get_version(void) { return 7 * 100 + 0; }  // 0.7.0 -> 700 (reference version.h)
+
+int tblite_get_feature(const char* flag) {
+  if (!flag) return 0;
+  return 0;
+}
+
+tblite_error tblite_new_error(void) { return new _tblite_error(); }
+void tblite_delete_error(tblite_error* e) {
+  if (e && *e) {
+    delete *e;
+    *e = nullptr;
+  }
+}
+int tblite_check_error(tblite_error e) { return e && e->set ? 1 : 0; }
+void tblite_clear_error(tblite_error e) {
+  if (e) {
+    e->set = false;
+    e->msg.clear();
+  }
+}
+void tblite_get_error(tblite_error e, char* buffer, const int* buffersize) {
+  if (e && e->set) copy_msg(e->msg, buffer, buffersize);
+}
+void tblite_set_error(tblite_error e, char* buffer, const int* buffersize) {
+  if (!e || !buffer) return;
+  std::string m = buffersize ? std::string(buffer, strnlen(buffer, *buffersize)) : std::string(buffer);
+  set_err(e, m);
+}
+
+tblite_context tblite_new_context(void) { return new _tblite_context(); }
+void tblite_delete_context(tblite_context* c) {
+  if (c && *c) {
+    delete *c;
+    *c = nullptr;
+  }
+}
+int tblite_check_context(tblite_context c) { return c && !c->errors.empty() ? 1 : 0; }
+void tblite_get_context_error(tblite_context c, char* buffer, const int* buffersize) {
+  if (!c || c->errors.empty()) return;
+  std::string m = c->errors.front();
+  c->errors.erase(c->errors.begin());
+  copy_msg(m, buffer, buffersize);
+}
+void tblite_set_context_logger(tblite_context c, tblite_logger_callback cb, void* ud) {
+  if (!c) return;
+  c->logger = cb;
+  c->userdata = ud;
+}
+void tblite_set_context_color(tblite_context c, int color) {
+  if (c) c->color = color;
+}
+void tblite_set_context_verbosity(tblite_context c, int v) {
+  if (c) c->verbosity = v;
+}
+
+tblite_structure tblite_new_structure(tblite_error error, const int natoms, const int* numbers,
+                                      const double* positions, const double* charge, const int* uhf,
+                                      const double* lattice, const bool* periodic) {
+  if (natoms <= 0 || !numbers || !positions) {
+    set_err(error, "Invalid molecular structure data");
+    return nullptr;
+  }
+  if (periodic) {
+    for (int k = 0; k < 3; ++k)
+      if (periodic[k]) {
+        set_err(error, "Periodic systems are not supported by the GPU engine");
+        return nullptr;
+      }
+  }
+  (void)lattice;
+  auto* m = new _tblite_structure();
+  m->nat = natoms;
+  m->num.assign(numbers, numbers + natoms);
+  m->xyz.assign(positions, positions + 3 * natoms);
+  for (double x : m->xyz)
+    if (!std::isfinite(x)) {
+      delete m;
+      set_err(error, "Non-finite atomic coordinates");
+      return nullptr;
+    }
+  m->charge = charge ? *charge : 0.0;
+  m->uhf = uhf ? *uhf : 0;
+  return m;
+}
+void tblite_delete_structure(tblite_structure* m) {
+  if (m && *m) {
+    delete *m;
+    *m = nullptr;
+  }
+}
+void tblite_update_structure_geometry(tblite_error error, tblite_structure m,
+                                      const double* positions, const double* lattice) {
+  (void)lattice;
+  if (!m) {
+    set_err(error, "Molecular structure data is missing");
+    return;
+  }
+  if (!positions) {
+    set_err(error, "Position array is missing");
+    return;
+  }
+  m->xyz.assign(positions, positions + 3 * m->nat);
+}
+void tblite_update_structure_charge(tblite_error error, tblite_structure m, const double* charge) {
+  if (!m) {
+    set_err(error, "Molecular structure data is missing");
+    return;
+  }
+  m->charge = charge ? *charge : 0.0;
+}
+void tblite_update_structure_uhf(tblite_error error, tblite_structure m, const int* uhf) {
+  if (!m) {
+    set_err(error, "Molecular structure data is missing");
+    return;
+  }
+  m->uhf = uhf ? *uhf : 0;
+}
+
+tblite_result tblite_new_result(void) { return new _tblite_result(); }
+tblite_result tblite_copy_result(tblite_result r) { return r ? new _tblite_result(*r) : nullptr; }
+void tblite_delete_result(tblite_result* r) {
+  if (r && *r) {
+    delete *r;
+    *r = nullptr;
+  }
+}
+
+#define RESULT_GUARD(cond, msg)  \
+  if (!res) {                    \
+    set_err(error, "Result container is missing"); \
+    return;                      \
+  }                              \
+  if (!(cond)) {                 \
+    set_err(error, msg);         \
+    return;                      \
+  }
+
+void tblite_get_result_number_of_atoms(tblite_error error, tblite_result res, int* nat) {
+  RESULT_GUARD(res->has_energy, "Result does not contain number of atoms");
+  *nat = res->nat;
+}
+void tblite_get_result_number_of_shells(tblite_error error, tblite_result res, int* nsh) {
+  RESULT_GUARD(res->has_wfn, "Result does not contain number of shells");
+  *nsh = res->nsh;
+}
+void tblite_get_result_number_of_orbitals(tblite_error error, tblite_result res, int* nao) {
+  RESULT_GUARD(res->has_wfn, "Result does not contain number of orbitals");
+  *nao = res->nao;
+}
+void tblite_get_result_number_of_spins(tblite_error error, tblite_result res, int* nspin) {
+  RESULT_GUARD(res->has_wfn, "Result does not contain number of spins");
+  *nspin = 1;
+}
+void tblite_get_result_energy(tblite_error error, tblite_result res, double* energy) {
+  RESULT_GUARD(res->has_energy, "Result does not contain energy");
+  *energy = res->energy;
+}
+void tblite_get_result_energies(tblite_error error, tblite_result res, double* energies) {
+  RESULT_GUARD(res->has_energy, "Result does not contain atom-resolved energies");
+  std::copy(res->energies.begin(), res->energies.end(), energies);
+}
+void tblite_get_result_gradient(tblite_error error, tblite_result res, double* gradient) {
+  RESULT_GUARD(!res->gradient.empty(), "Result does not contain gradient");
+  std::copy(res->gradient.begin(), res->gradient.end(), gradient);
+}
+void tblite_get_result_virial(tblite_error error, tblite_result res, double* sigma) {
+  RESULT_GUARD(!res->sigma.empty(), "Result does not contain virial");
+  std::copy(res->sigma.begin(), res->sigma.end(), sigma);
+}
+void tblite_get_result_charges(tblite_error error, tblite_result res, double* charges) {
+  RESULT_GUARD(res->has_wfn, "Result does not contain atomic charges");
+  std::copy(res->qat.begin(), res->qat.end(), charges);
+}
+void tblite_get_result_bond_orders(tblite_error error, tblite_result res, double* mbo) {
+  RESULT_GUARD(!res->wbo.empty(), "Result does not contain bond orders");
+  std::copy(res->wbo.begin(), res->wbo.end(), mbo);
+}
+void tblite_get_result_dipole(tblite_error error, tblite_result res, double dipole[3]) {
+  RESULT_GUARD(res->has_wfn, "Result does not contain dipole moment");
+  for (int k = 0; k < 3; ++k) dipole[k] = res->dipole[k];
+}
+void tblite_get_result_quadrupole(tblite_error error, tblite_result res, double quadrupole[6]) {
+  RESULT_GUARD(res->has_wfn, "Result does not contain quadrupole moment");
+  for (int k = 0; k < 6; ++k) quadrupole[k] = res->quadrupole[k];
+}
+void tblite_get_result_orbital_energies(tblite_error error, tblite_result res, double* emo) {
+  RESULT_GUARD(res->has_wfn, "Result does not contain orbital energies");
+  std::copy(res->emo.begin(), res->emo.end(), emo);
+}
+void tblite_get_result_orbital_occupations(tblite_error error, tblite_result res, double* occ) {
+  RESULT_GUARD(res->has_wfn, "Result does not contain orbital occupations");
+  std::copy(res->focc.begin(), res->focc.end(), occ);
+}
+void tblite_get_result_orbital_coefficients(tblite_error error, tblite_result res, double* cmat) {
+  RESULT_GUARD(!res->C.empty(), "Result does not contain orbital coefficients");
+  std::copy(res->C.begin(), res->C.end(), cmat);
+}
+void tblite_get_result_density_matrix(tblite_error error, tblite_result res, double* pmat) {
+  RESULT_GUARD(!res->P.empty(), "Result does not contain density matrix");
+  std::copy(res->P.begin(), res->P.end(), pmat);
+}
+void tblite_get_result_overlap_matrix(tblite_error error, tblite_result res, double* smat) {
+  RESULT_GUARD(!res->S.empty(), "Result does not contain overlap matrix");
+  std::copy(res->S.begin(), res->S.end(), smat);
+}
+void tblite_get_result_hamiltonian_matrix(tblite_error error, tblite_result res, double* hmat) {
+  RESULT_GUARD(!res->H.empty(), "Result does not contain Hamiltonian matrix");
+  std::copy(res->H.begin(), res->H.end(), hmat);
+}
+
+tblite_calculator tblite_new_gfn2_calculator(tblite_context ctx, tblite_structure mol,
+                                            tblite_xtb_config* config) {
+  (void)config;
+  if (!ctx) return nullptr;
+  if (!mol) {
+    ctx->push("Molecular structure data is missing");
+    return nullptr;
+  }
+  auto* c = new _tblite_calculator();
+  try {
+    build_calculator(c, mol);
+  } catch (const std::exception& e) {
+    ctx->push(e.what());
+    delete c;
+    return nullptr;
+  }
+  return c;
+}
+void tblite_delete_calculator(tblite_calculator* c) {
+  if (c && *c) {
+    delete *c;
+    *c = nullptr;
+  }
+}
+
+#define CALC_GUARD                                   \
+  if (!ctx) return;                                  \
+  if (!calc) {                                       \
+    ctx->push("Calculator object is missing");       \
+    return;                                          \
+  }
+
+void tblite_set_calculator_accuracy(tblite_context ctx, tblite_calculator calc, double acc) {
+  CALC_GUARD;
+  calc->accuracy = acc;
+}
+void tblite_set_calculator_max_iter(tblite_context ctx, tblite_calculator calc, int max_iter) {
+  CALC_GUARD;
+  calc->max_iter = max_iter;
+}
+void tblite_set_calculator_mixer_damping(tblite_context ctx, tblite_calculator calc, double d) {
+  CALC_GUARD;
+  calc->damping = d;
+}
+void tblite_set_calculator_mixer_memory(tblite_context ctx, tblite_calculator calc, int memory) {
+  CALC_GUARD;
+  calc->memory = memory;
+}
+void tblite_set_calculator_mixer(tblite_context ctx, tblite_calculator calc, tblite_mixer mixer) {
+  CALC_GUARD;
+  if (mixer != TBLITE_MIXER_BROYDEN) ctx->push("Unknown mixer selected");
+}
+void tblite_set_calculator_temperature_annealing(tblite_context ctx, tblite_calculator calc,
+                                                 double initial_etemp, int hold, int cycles) {
+  CALC_GUARD;
+  calc->anneal = true;
+  calc->anneal_kt = initial_etemp;
+  calc->anneal_hold = hold;
+  calc->anneal_cycles = cycles;
+}
+void tblite_set_calculator_guess(tblite_context ctx, tblite_calculator calc, tblite_guess guess) {
+  CALC_GUARD;
+  if (guess != TBLITE_GUESS_SAD) {
+    ctx->push("Only the SAD guess is available in the GPU engine");
+    return;
+  }
+  calc->guess = guess;
+}
+void tblite_set_calculator_temperature(tblite_context ctx, tblite_calculator calc, double etemp) {
+  CALC_GUARD;
+  calc->etemp = etemp;
+}
+void tblite_set_calculator_save_integrals(tblite_context ctx, tblite_calculator calc, int v) {
+  CALC_GUARD;
+  calc->save_integrals = v;
+}
+void tblite_get_calculator_shell_count(tblite_context ctx, tblite_calculator calc, int* nsh) {
+  CALC_GUARD;
+  *nsh = calc->nsh;
+}
+void tblite_get_calculator_shell_map(tblite_context ctx, tblite_calculator calc, int* sh2at) {
+  CALC_GUARD;
+  std::copy(calc->sh_atom.begin(), calc->sh_atom.end(), sh2at);
+}
+void tblite_get_calculator_angular_momenta(tblite_context ctx, tblite_calculator calc, int* am) {
+  CALC_GUARD;
+  std::copy(calc->sh_l.begin(), calc->sh_l.end(), am);
+}
+void tblite_get_calculator_orbital_count(tblite_context ctx, tblite_calculator calc, int* nao) {
+  CALC_GUARD;
+  *nao = calc->nao;
+}
+void tblite_get_calculator_orbital_map(tblite_context ctx, tblite_calculator calc, int* ao2sh) {
+  CALC_GUARD;
+  std::copy(calc->ao_sh.begin(), calc->ao_sh.end(), ao2sh);
+}
+
+void tblite_get_singlepoint(tblite_context ctx, tblite_structure mol, tblite_calculator calc,
+                            tblite_result res) {
+  if (!ctx) return;
+  if (!mol) {
+    ctx->push("Molecular structure data is missing");
+    return;
+  }
+  if (!calc) {
+    ctx->push("Calculator object is missing");
+    return;
+  }
+  if (!res) {
+    ctx->push("Result container is missing");
+    return;
+  }
+  try {
+    singlepoint(ctx, mol, calc, res);
+  } catch (const std::exception& e) {
+    ctx->push(e.what());
+  }
+}
+
+}  // extern "C"

@@ -1,0 +1,143 @@
+// Internal interfaces of the GB300 GFN2-xTB engine (not part of the public C ABI).
+//
+// Layout conventions shared by all kernels (row-major, FP64):
+//   S[n][n], H[n][n], F[n][n], P[n][n]   symmetric AO matrices
+//   D[3][n][n], Q[6][n][n]              multipole integrals, operator on the atom of the
+//                                       COLUMN index (the reference stores dpint(k, j, i)
+//                                       with the operator on the atom of i)
+//   C (eigenvectors) column-major: C[m*n + r] = coefficient of AO r in orbital m
+//   Q components: xx, xy, yy, xz, yz, zz (traceless, 3/2 M - 1/2 tr M)
+//   spherical p order (y, z, x); spherical d order (xy, yz, z2, xz, x2-y2)
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace tb {
+
+constexpr int MAXG = 12;    // max primitives per shell
+constexpr int MAXL = 2;     // max angular momentum handled by the kernels
+constexpr double INTCUT = 25.0;  // integral_cutoff(acc) is always 25 in the reference
+
+// Device view of one molecule + GFN2 parameters (all pointers are device pointers).
+struct DevMol {
+  int nat, nsh, nao;
+  const double* xyz;       // [nat][3]
+  const int* at_z;         // [nat]
+  const int* at_sh;        // [nat+1]
+  const int* sh_atom;      // [nsh]
+  const int* sh_l;         // [nsh]
+  const int* sh_nprim;     // [nsh]
+  const double* sh_alpha;  // [nsh][MAXG]
+  const double* sh_coeff;  // [nsh][MAXG]
+  const int* sh_ao;        // [nsh]
+  const int* ao_sh;        // [nao]
+  const int* ao_at;        // [nao]
+  const double* sh_se0;    // base self energy
+  const double* sh_kcn;    // CN shift (Hartree per CN)
+  const double* sh_shpoly; // shell polynomial
+  const double* sh_zeta;   // Slater exponent
+  const double* sh_hub;    // shell hardness
+  const double* sh_gam3;   // shell Hubbard derivative
+  const double* sh_refocc; // reference occupation
+  const double* at_en;     // Pauling EN (external data)
+  const double* at_rad;    // atomic radius for the H0 polynomial (external data)
+  const double* at_rcov;   // covalent radius for the CN (external data)
+  const double* at_mprad;  // AES base radius
+  const double* at_vcn;    // AES valence CN
+  const double* at_dkern;  // AES dipole kernel
+  const double* at_qkern;  // AES quadrupole kernel
+  const double* at_repa;   // repulsion alpha
+  const double* at_repz;   // repulsion zeff
+};
+
+struct Gfn2Scalars {
+  double wexp, enscale, gexp;
+  double kshell[5][5];
+  double mp_dmp3, mp_dmp5, mp_shift, mp_kexp, mp_rmax;
+  double rep_kexp, rep_kexp_light, rep_rexp, rep_cutoff;
+  double cn_ka, cn_kb, cn_rshift, cn_cutoff;
+  double h0_cutoff;  // real-space cutoff of the integral pair list
+};
+
+// Kernel launchers (defined in the .cu files).  All run on `stream`.
+void launch_cn(const DevMol& m, const Gfn2Scalars& p, double* cn, cudaStream_t s);
+void launch_cn_grad(const DevMol& m, const Gfn2Scalars& p, const double* dEdcn, double* grad,
+                    double* sigma, cudaStream_t s);
+void launch_setup_levels(const DevMol& m, const Gfn2Scalars& p, const double* cn,
+                         double* selfenergy, double* mrad, double* dmrdcn, cudaStream_t s);
+void launch_build_h0(const DevMol& m, const Gfn2Scalars& p, const double* selfenergy, double* S,
+                     double* H, double* D, double* Q, cudaStream_t s);
+void launch_h0_gradient(const DevMol& m, const Gfn2Scalars& p, const double* selfenergy,
+                        const double* P, const double* W, const double* vao, const double* vdp,
+                        const double* vqp, double* grad, double* sigma, double* dEdcn,
+                        cudaStream_t s);
+void launch_repulsion(const DevMol& m, const Gfn2Scalars& p, double* erep, double* grad,
+                      double* sigma, cudaStream_t s);
+// electrostatics: potentials from (qsh, qat, dpat, qpat)
+void launch_coulomb_potential(const DevMol& m, const Gfn2Scalars& p, const double* mrad,
+                              const double* qsh, const double* qat, const double* dpat,
+                              const double* qpat, double* vsh, double* vat, double* vdp,
+                              double* vqp, cudaStream_t s);
+// per-atom electrostatic energy (es2 + es3 + AES incl. kernels), added into eat
+void launch_coulomb_energy(const DevMol& m, const Gfn2Scalars& p, const double* mrad,
+                           const double* qsh, const double* qat, const double* dpat,
+                           const double* qpat, double* eat, cudaStream_t s);
+void launch_coulomb_gradient(const DevMol& m, const Gfn2Scalars& p, const double* mrad,
+                             const double* dmrdcn, const double* qsh, const double* qat,
+                             const double* dpat, const double* qpat, double* grad, double* sigma,
+                             double* dEdcn, cudaStream_t s);
+void launch_vao(const DevMol& m, const double* vsh, const double* vat, double* vao, cudaStream_t s);
+void launch_fock(int n, const int* ao_at, const double* H, const double* S, const double* D,
+                 const double* Q, const double* vao, const double* vdp, const double* vqp,
+                 double* F, cudaStream_t s);
+// Mulliken analysis + band energy: column partial sums then per-shell/atom reduction
+void launch_mulliken(const DevMol& m, const double* P, const double* S, const double* H,
+                     const double* D, const double* Q, double* partial, int nchunk,
+                     double* qsh, double* qat, double* dpat, double* qpat, double* eat_band,
+                     cudaStream_t s);
+int mulliken_chunks(int n);
+
+// Fermi filling of both spin channels; writes focc (alpha+beta), ts (entropy term) to scal[0]
+void launch_fermi(int n, const double* emo, double nalp, double nbet, double kt, double* focc,
+                  double* ts, int* nocc_cols, cudaStream_t s);
+
+// Broyden mixer (reference scf/mixer/broyden.f90)
+struct BroydenState {
+  int ndim, memory, iter;
+  double damp;
+  double *q, *qlast, *dq, *dqlast, *df, *u, *a, *omega;  // device
+  double* work;   // device scratch [memory*memory + 2*memory + 64]
+  int* status;    // device status word (0 ok, !=0 singular)
+};
+void launch_broyden_next(BroydenState& b, cudaStream_t s);
+void launch_pack(const DevMol& m, const double* qsh, const double* dpat, const double* qpat,
+                 double* vec, cudaStream_t s);
+void launch_unpack(const DevMol& m, const double* vec, double* qsh, double* qat, double* dpat,
+                   double* qpat, cudaStream_t s);
+// dq = vec_out - q ; err2 = sum(dq^2)/ndim (into *err)
+void launch_diff(int ndim, const double* vec_out, const double* q, double* dq, double* err,
+                 cudaStream_t s);
+
+// eigen solver (generalised, Cholesky reduced)
+struct EigenSolver;
+EigenSolver* eigen_create(int n, cudaStream_t s);
+void eigen_destroy(EigenSolver*);
+// factorise S once per geometry; returns 0 on success, >0 if S is not positive definite
+int eigen_set_overlap(EigenSolver*, const double* S);
+// solve F C = S C e ; F is destroyed, C column-major [n][n], e ascending. returns 0 on success
+int eigen_solve(EigenSolver*, double* F, double* C, double* e);
+
+// eelec[i] = ts/nat + eband[i]
+void launch_eelec_init(int nat, const double* ts, const double* eband, double* eelec,
+                       cudaStream_t s);
+// out[m] = f[m] * e[m]
+void launch_fe(int n, const double* f, const double* e, double* out, cudaStream_t s);
+
+// dense helpers
+void density_matrix(int n, int k, const double* C, const double* f, double* P, double* work,
+                    cudaStream_t s);
+
+}  // namespace tb

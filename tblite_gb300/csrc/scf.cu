@@ -1,0 +1,903 @@
+// SCF kernels: coordination number, self energies, electrostatics (isotropic, third order,
+// anisotropic multipoles), repulsion, Fock assembly, Mulliken analysis, Fermi filling,
+// Broyden mixing, and the pair gradients.
+//
+// Restated from the reference:
+//   self energies            src/tblite/xtb/h0.f90:113-217
+//   AES radii                src/tblite/coulomb/multipole.f90:389-420
+//   isotropic Coulomb        src/tblite/coulomb/charge/effective.f90:238-286, 487-556
+//   third order              src/tblite/coulomb/thirdorder.f90:109-172
+//   AES matrices/potential   src/tblite/coulomb/multipole.f90:197-350, 488-535, 746-852
+//   repulsion                src/tblite/repulsion/effective.f90:187-247
+//   Fock assembly            src/tblite/scf/potential.f90:122-255
+//   Mulliken                 src/tblite/wavefunction/mulliken.f90:37-100
+//   Fermi filling            src/tblite/wavefunction/fermi.f90:31-106, scf/iterator.f90:347-353
+//   Broyden                  src/tblite/scf/mixer/broyden.f90:148-278
+// Interaction matrices (gamma, AES) are evaluated on the fly inside the potential kernels
+// instead of being stored: one warp per atom walks all partners.
+#include <cuda_runtime.h>
+
+#include "engine.h"
+
+namespace tb {
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// ------------------------------------------------------------------------------------
+// coordination number (double exponential counting function, see oracle for the form)
+// ------------------------------------------------------------------------------------
+__device__ __forceinline__ void dexp_count(double r, double r0, const Gfn2Scalars& p, double& c,
+                                           double& dc) {
+  const double e1 = exp(-p.cn_ka * (r0 / r - 1.0));
+  const double e2 = exp(-p.cn_kb * ((r0 + p.cn_rshift) / r - 1.0));
+  const double f1 = 1.0 / (1.0 + e1), f2 = 1.0 / (1.0 + e2);
+  c = f1 * f2;
+  const double d1 = -f1 * f1 * e1 * p.cn_ka * r0 / (r * r);
+  const double d2 = -f2 * f2 * e2 * p.cn_kb * (r0 + p.cn_rshift) / (r * r);
+  dc = d1 * f2 + f1 * d2;
+}
+
+__global__ void k_cn(DevMol m, Gfn2Scalars p, double* cn) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= m.nat) return;
+  const int i = warp;
+  const double xi = m.xyz[3 * i], yi = m.xyz[3 * i + 1], zi = m.xyz[3 * i + 2];
+  const double cut2 = p.cn_cutoff * p.cn_cutoff;
+  double acc = 0.0;
+  for (int j = lane; j < m.nat; j += 32) {
+    if (j == i) continue;
+    const double dx = xi - m.xyz[3 * j], dy = yi - m.xyz[3 * j + 1], dz = zi - m.xyz[3 * j + 2];
+    const double r2 = dx * dx + dy * dy + dz * dz;
+    if (r2 > cut2 || r2 < 1e-12) continue;
+    double c, dc;
+    dexp_count(sqrt(r2), m.at_rcov[i] + m.at_rcov[j], p, c, dc);
+    acc += c;
+  }
+  acc = warp_sum(acc);
+  if (lane == 0) cn[i] = acc;
+}
+
+void launch_cn(const DevMol& m, const Gfn2Scalars& p, double* cn, cudaStream_t s) {
+  if (m.nat == 1) {
+    cudaMemsetAsync(cn, 0, sizeof(double), s);
+    return;
+  }
+  k_cn<<<(m.nat * 32 + 255) / 256, 256, 0, s>>>(m, p, cn);
+}
+
+// grad_i += sum_j (dEdcn_i + dEdcn_j) dcount/dr (R_i - R_j)/r ; per-atom sigma partials
+__global__ void k_cn_grad(DevMol m, Gfn2Scalars p, const double* __restrict__ dEdcn, double* grad,
+                          double* sig_at) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= m.nat) return;
+  const int i = warp;
+  const double cut2 = p.cn_cutoff * p.cn_cutoff;
+  double g[3] = {0, 0, 0}, sg[9] = {0};
+  for (int j = lane; j < m.nat; j += 32) {
+    if (j == i) continue;
+    double v[3], r2 = 0;
+    for (int k = 0; k < 3; ++k) {
+      v[k] = m.xyz[3 * i + k] - m.xyz[3 * j + k];
+      r2 += v[k] * v[k];
+    }
+    if (r2 > cut2 || r2 < 1e-12) continue;
+    const double r = sqrt(r2);
+    double c, dc;
+    dexp_count(r, m.at_rcov[i] + m.at_rcov[j], p, c, dc);
+    const double f = (dEdcn[i] + dEdcn[j]) * dc / r;
+    for (int k = 0; k < 3; ++k) g[k] += f * v[k];
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) sg[3 * a + b] += 0.5 * f * v[a] * v[b];
+  }
+  for (int k = 0; k < 3; ++k) {
+    g[k] = warp_sum(g[k]);
+  }
+  for (int k = 0; k < 9; ++k) sg[k] = warp_sum(sg[k]);
+  if (lane == 0) {
+    for (int k = 0; k < 3; ++k) grad[3 * i + k] += g[k];
+    for (int k = 0; k < 9; ++k) sig_at[9 * i + k] += sg[k];
+  }
+}
+
+void launch_cn_grad(const DevMol& m, const Gfn2Scalars& p, const double* dEdcn, double* grad,
+                    double* sig_at, cudaStream_t s) {
+  if (m.nat == 1) return;
+  k_cn_grad<<<(m.nat * 32 + 255) / 256, 256, 0, s>>>(m, p, dEdcn, grad, sig_at);
+}
+
+// ------------------------------------------------------------------------------------
+// self energies and AES damping radii
+// ------------------------------------------------------------------------------------
+__global__ void k_levels(DevMol m, Gfn2Scalars p, const double* __restrict__ cn, double* se,
+                         double* mrad, double* dmrdcn) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < m.nsh) se[t] = m.sh_se0[t] - m.sh_kcn[t] * cn[m.sh_atom[t]];
+  if (t < m.nat) {
+    const double arg = cn[t] - m.at_vcn[t] - p.mp_shift;
+    const double t1 = exp(-p.mp_kexp * arg);
+    const double t2 = (p.mp_rmax - m.at_mprad[t]) / (1.0 + t1);
+    mrad[t] = m.at_mprad[t] + t2;
+    dmrdcn[t] = -t2 * p.mp_kexp * t1 / (1.0 + t1);
+  }
+}
+
+void launch_setup_levels(const DevMol& m, const Gfn2Scalars& p, const double* cn, double* se,
+                         double* mrad, double* dmrdcn, cudaStream_t s) {
+  const int nt = m.nsh > m.nat ? m.nsh : m.nat;
+  k_levels<<<(nt + 127) / 128, 128, 0, s>>>(m, p, cn, se, mrad, dmrdcn);
+}
+
+// ------------------------------------------------------------------------------------
+// electrostatics: one warp per atom i, partners j strided over lanes
+// MODE 0: potentials (vsh, vat, vdp, vqp);  MODE 1: per-atom energy (added to eat)
+// ------------------------------------------------------------------------------------
+constexpr int MAXSH = 3;
+
+template <int MODE>
+__global__ void k_coulomb(DevMol m, Gfn2Scalars p, const double* __restrict__ mrad,
+                          const double* __restrict__ qsh, const double* __restrict__ qat,
+                          const double* __restrict__ dpat, const double* __restrict__ qpat,
+                          double* vsh, double* vat, double* vdp, double* vqp, double* eat) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= m.nat) return;
+  const int i = warp;
+  const int is0 = m.at_sh[i], nsi = m.at_sh[i + 1] - is0;
+  double xi[3], di[3], qi[6];
+  for (int k = 0; k < 3; ++k) {
+    xi[k] = m.xyz[3 * i + k];
+    di[k] = dpat[3 * i + k];
+  }
+  for (int k = 0; k < 6; ++k) qi[k] = qpat[6 * i + k];
+  const double qa_i = qat[i], ri = mrad[i];
+  double ush[MAXSH] = {0, 0, 0};     // sum_j gamma q_j for shells of i
+  double uat = 0.0;                  // vat_i
+  double ud[3] = {0, 0, 0};          // vdp_i: sd + dd parts
+  double udd[3] = {0, 0, 0};         // dd part only (energy needs 1/2 of it)
+  double uq[6] = {0, 0, 0, 0, 0, 0};  // vqp_i
+  for (int j = lane; j < m.nat; j += 32) {
+    if (j == i) continue;
+    double v[3];
+    for (int k = 0; k < 3; ++k) v[k] = xi[k] - m.xyz[3 * j + k];  // R_i - R_j
+    const double r2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+    const double r1 = sqrt(r2);
+    // isotropic: gamma = 1/sqrt(r^2 + eta^-2) for gexp = 2; general form kept
+    const int js0 = m.at_sh[j], nsj = m.at_sh[j + 1] - js0;
+    for (int a = 0; a < nsi; ++a) {
+      const double hi = m.sh_hub[is0 + a];
+      double acc = 0.0;
+      for (int b = 0; b < nsj; ++b) {
+        const double g = 0.5 * (hi + m.sh_hub[js0 + b]);
+        const double t = 1.0 / pow(pow(r1, p.gexp) + pow(g, -p.gexp), 1.0 / p.gexp);
+        acc += t * qsh[js0 + b];
+      }
+      ush[a] += acc;
+    }
+    // AES (multipole.f90:488-535), amat(:, jat, iat) with vec = R_iat - R_jat
+    const double g1 = 1.0 / r1, g3 = g1 * g1 * g1, g5 = g3 * g1 * g1;
+    const double rr = 0.5 * (mrad[j] + ri) * g1;
+    const double rr3 = rr * rr * rr;
+    const double f3 = 1.0 / (1.0 + 6.0 * pow(rr, p.mp_dmp3));
+    const double f5 = 1.0 / (1.0 + 6.0 * pow(rr, p.mp_dmp5));
+    (void)rr3;
+    const double* dj = dpat + 3 * j;
+    const double* qj = qpat + 6 * j;
+    const double qa_j = qat[j];
+    // vat_i += sum_j amat_sd(:, j, i) . dpat_j + amat_sq(:, j, i) . qpat_j   (v = R_i - R_j)
+    const double sq[6] = {v[0] * v[0] * g5 * f5, 2 * v[0] * v[1] * g5 * f5, v[1] * v[1] * g5 * f5,
+                          2 * v[0] * v[2] * g5 * f5, 2 * v[1] * v[2] * g5 * f5,
+                          v[2] * v[2] * g5 * f5};
+    uat += (v[0] * dj[0] + v[1] * dj[1] + v[2] * dj[2]) * g3 * f3;
+    for (int k = 0; k < 6; ++k) uat += sq[k] * qj[k];
+    // vdp_i += sum_j amat_sd(:, i, j) q_j + amat_dd(:, i, :, j) dpat_j ; amat_sd(:, i, j) = -v g3 f3
+    const double vd = v[0] * dj[0] + v[1] * dj[1] + v[2] * dj[2];
+    for (int k = 0; k < 3; ++k) {
+      ud[k] += -v[k] * g3 * f3 * qa_j;
+      const double dd = dj[k] * g3 * f5 - v[k] * vd * 3.0 * g5 * f5;
+      udd[k] += dd;
+    }
+    for (int k = 0; k < 6; ++k) uq[k] += sq[k] * qa_j;
+  }
+  for (int a = 0; a < MAXSH; ++a) ush[a] = warp_sum(ush[a]);
+  uat = warp_sum(uat);
+  for (int k = 0; k < 3; ++k) {
+    ud[k] = warp_sum(ud[k]);
+    udd[k] = warp_sum(udd[k]);
+  }
+  for (int k = 0; k < 6; ++k) uq[k] = warp_sum(uq[k]);
+  if (lane != 0) return;
+  // on-site gamma block
+  double gsh[MAXSH];
+  for (int a = 0; a < nsi; ++a) {
+    double acc = ush[a];
+    for (int b = 0; b < nsi; ++b)
+      acc += 0.5 * (m.sh_hub[is0 + a] + m.sh_hub[is0 + b]) * qsh[is0 + b];
+    gsh[a] = acc;
+  }
+  const double mpscale[6] = {1, 2, 1, 2, 2, 1};
+  if (MODE == 0) {
+    for (int a = 0; a < nsi; ++a) {
+      const double q = qsh[is0 + a];
+      vsh[is0 + a] = gsh[a] + q * q * m.sh_gam3[is0 + a];
+    }
+    vat[i] = uat;
+    for (int k = 0; k < 3; ++k) vdp[3 * i + k] = ud[k] + udd[k] + 2.0 * m.at_dkern[i] * di[k];
+    for (int k = 0; k < 6; ++k) vqp[6 * i + k] = uq[k] + 2.0 * m.at_qkern[i] * qi[k] * mpscale[k];
+  } else {
+    double e = 0.0;
+    for (int a = 0; a < nsi; ++a) {
+      const double q = qsh[is0 + a];
+      e += 0.5 * gsh[a] * q + q * q * q * m.sh_gam3[is0 + a] / 3.0;
+    }
+    for (int k = 0; k < 3; ++k) e += di[k] * (ud[k] + 0.5 * udd[k]);
+    for (int k = 0; k < 6; ++k) e += qi[k] * uq[k];
+    double d2 = 0.0, q2 = 0.0;
+    for (int k = 0; k < 3; ++k) d2 += di[k] * di[k];
+    for (int k = 0; k < 6; ++k) q2 += qi[k] * qi[k] * mpscale[k];
+    e += m.at_dkern[i] * d2 + m.at_qkern[i] * q2;
+    eat[i] += e;
+  }
+}
+
+void launch_coulomb_potential(const DevMol& m, const Gfn2Scalars& p, const double* mrad,
+                              const double* qsh, const double* qat, const double* dpat,
+                              const double* qpat, double* vsh, double* vat, double* vdp,
+                              double* vqp, cudaStream_t s) {
+  k_coulomb<0><<<(m.nat * 32 + 255) / 256, 256, 0, s>>>(m, p, mrad, qsh, qat, dpat, qpat, vsh, vat,
+                                                         vdp, vqp, nullptr);
+}
+
+void launch_coulomb_energy(const DevMol& m, const Gfn2Scalars& p, const double* mrad,
+                           const double* qsh, const double* qat, const double* dpat,
+                           const double* qpat, double* eat, cudaStream_t s) {
+  k_coulomb<1><<<(m.nat * 32 + 255) / 256, 256, 0, s>>>(m, p, mrad, qsh, qat, dpat, qpat, nullptr,
+                                                         nullptr, nullptr, nullptr, eat);
+}
+
+// ------------------------------------------------------------------------------------
+// electrostatic gradient at fixed charges/moments (es2 + AES); dEdcn += dEdr dmrdcn
+// per-atom formulation: atom i sums its own share of every pair (no atomics)
+// ------------------------------------------------------------------------------------
+__global__ void k_coulomb_grad(DevMol m, Gfn2Scalars p, const double* __restrict__ mrad,
+                               const double* __restrict__ dmrdcn, const double* __restrict__ qsh,
+                               const double* __restrict__ qat, const double* __restrict__ dpat,
+                               const double* __restrict__ qpat, double* grad, double* sig_at,
+                               double* dEdcn) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= m.nat) return;
+  const int i = warp;
+  const int is0 = m.at_sh[i], nsi = m.at_sh[i + 1] - is0;
+  double g[3] = {0, 0, 0}, sg[9] = {0}, dEdr = 0.0;
+  const double* di = dpat + 3 * i;
+  const double* qi = qpat + 6 * i;
+  for (int j = lane; j < m.nat; j += 32) {
+    if (j == i) continue;
+    double w[3];
+    for (int k = 0; k < 3; ++k) w[k] = m.xyz[3 * i + k] - m.xyz[3 * j + k];  // R_i - R_j
+    const double r2 = w[0] * w[0] + w[1] * w[1] + w[2] * w[2], r1 = sqrt(r2);
+    // es2: d/dR_i of 1/2 sum q gamma q  (pair counted once per atom)
+    const int js0 = m.at_sh[j], nsj = m.at_sh[j + 1] - js0;
+    double f = 0.0;
+    for (int a = 0; a < nsi; ++a)
+      for (int b = 0; b < nsj; ++b) {
+        const double gm = 0.5 * (m.sh_hub[is0 + a] + m.sh_hub[js0 + b]);
+        double d = 1.0 / (pow(r1, p.gexp) + pow(gm, -p.gexp));
+        d = -pow(r1, p.gexp - 2.0) * d * pow(d, 1.0 / p.gexp);
+        f += d * qsh[is0 + a] * qsh[js0 + b];
+      }
+    double gp[3];
+    for (int k = 0; k < 3; ++k) gp[k] = f * w[k];
+    // AES pair term written as in the reference with (iat, jat) = (i, j), vec = R_j - R_i
+    const double* dj = dpat + 3 * j;
+    const double* qj = qpat + 6 * j;
+    const double qai = qat[i], qaj = qat[j];
+    double v[3] = {-w[0], -w[1], -w[2]};
+    const double rr = 0.5 * (mrad[i] + mrad[j]);
+    const double g1 = 1.0 / r1, g3 = g1 * g1 * g1, g5 = g3 * g1 * g1, g7 = g5 * g1 * g1;
+    const double f3 = 1.0 / (1.0 + 6.0 * pow(rr * g1, p.mp_dmp3));
+    const double d3 = -3 * g5 * f3 - p.mp_dmp3 * f3 * (f3 - 1.0) * g5;
+    const double f5 = 1.0 / (1.0 + 6.0 * pow(rr * g1, p.mp_dmp5));
+    const double d5 = -5 * f5 - p.mp_dmp5 * (f5 * f5 - f5);
+    const double dpiqj = (v[0] * di[0] + v[1] * di[1] + v[2] * di[2]) * qaj;
+    const double qidpj = (v[0] * dj[0] + v[1] * dj[1] + v[2] * dj[2]) * qai;
+    double fddr = 3.0 * (dpiqj - qidpj) * p.mp_dmp3 * f3 * g3 * (f3 / rr) * pow(rr * g1, p.mp_dmp3);
+    double ga[3];
+    for (int k = 0; k < 3; ++k)
+      ga[k] = -d3 * v[k] * (dpiqj - qidpj) + f3 * g3 * (qai * dj[k] - qaj * di[k]);
+    const double dpidpj = di[0] * dj[0] + di[1] * dj[1] + di[2] * dj[2];
+    const double dpiv = di[0] * v[0] + di[1] * v[1] + di[2] * v[2];
+    const double dpjv = dj[0] * v[0] + dj[1] * v[1] + dj[2] * v[2];
+    const double edd = dpidpj * r2 - 3 * dpjv * dpiv;
+    fddr += 3.0 * edd * p.mp_dmp5 * f5 * g5 * (f5 / rr) * pow(rr * g1, p.mp_dmp5);
+    for (int k = 0; k < 3; ++k)
+      ga[k] += -2.0 * f5 * g5 * dpidpj * v[k] + 3.0 * f5 * g5 * (dpiv * dj[k] + dpjv * di[k])
+               - edd * d5 * g7 * v[k];
+    const double eq = 2 * (qaj * qi[1] + qj[1] * qai) * v[0] * v[1]
+                      + 2 * (qaj * qi[3] + qj[3] * qai) * v[0] * v[2]
+                      + 2 * (qaj * qi[4] + qj[4] * qai) * v[1] * v[2]
+                      + (qaj * qi[0] + qj[0] * qai) * v[0] * v[0]
+                      + (qaj * qi[2] + qj[2] * qai) * v[1] * v[1]
+                      + (qaj * qi[5] + qj[5] * qai) * v[2] * v[2];
+    fddr += eq * 3.0 * p.mp_dmp5 * f5 * g5 * f5 / rr * pow(rr * g1, p.mp_dmp5);
+    const double qjv[3] = {v[0] * qj[0] + v[1] * qj[1] + v[2] * qj[3],
+                           v[0] * qj[1] + v[1] * qj[2] + v[2] * qj[4],
+                           v[0] * qj[3] + v[1] * qj[4] + v[2] * qj[5]};
+    const double qiv[3] = {v[0] * qi[0] + v[1] * qi[1] + v[2] * qi[3],
+                           v[0] * qi[1] + v[1] * qi[2] + v[2] * qi[4],
+                           v[0] * qi[3] + v[1] * qi[4] + v[2] * qi[5]};
+    for (int k = 0; k < 3; ++k)
+      ga[k] += -eq * d5 * g7 * v[k] - 2.0 * f5 * g5 * qai * qjv[k] - 2.0 * f5 * g5 * qaj * qiv[k];
+    dEdr += fddr;
+    for (int k = 0; k < 3; ++k) g[k] += gp[k] + ga[k];
+    // virial, half of each pair per atom
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b)
+        sg[3 * a + b] += 0.5 * gp[a] * w[b] - 0.25 * (v[a] * ga[b] + ga[a] * v[b]);
+  }
+  for (int k = 0; k < 3; ++k) g[k] = warp_sum(g[k]);
+  for (int k = 0; k < 9; ++k) sg[k] = warp_sum(sg[k]);
+  dEdr = warp_sum(dEdr);
+  if (lane == 0) {
+    for (int k = 0; k < 3; ++k) grad[3 * i + k] += g[k];
+    for (int k = 0; k < 9; ++k) sig_at[9 * i + k] += sg[k];
+    dEdcn[i] += dEdr * dmrdcn[i];
+  }
+}
+
+void launch_coulomb_gradient(const DevMol& m, const Gfn2Scalars& p, const double* mrad,
+                             const double* dmrdcn, const double* qsh, const double* qat,
+                             const double* dpat, const double* qpat, double* grad, double* sig_at,
+                             double* dEdcn, cudaStream_t s) {
+  if (m.nat == 1) return;
+  k_coulomb_grad<<<(m.nat * 32 + 255) / 256, 256, 0, s>>>(m, p, mrad, dmrdcn, qsh, qat, dpat, qpat,
+                                                          grad, sig_at, dEdcn);
+}
+
+// ------------------------------------------------------------------------------------
+// repulsion energy + gradient (per atom, each pair seen from both atoms)
+// ------------------------------------------------------------------------------------
+__global__ void k_repulsion(DevMol m, Gfn2Scalars p, double* erep, double* grad, double* sig_at) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= m.nat) return;
+  const int i = warp;
+  const double cut2 = p.rep_cutoff * p.rep_cutoff;
+  double e = 0.0, g[3] = {0, 0, 0}, sg[9] = {0};
+  for (int j = lane; j < m.nat; j += 32) {
+    if (j == i) continue;
+    double v[3], r2 = 0;
+    for (int k = 0; k < 3; ++k) {
+      v[k] = m.xyz[3 * i + k] - m.xyz[3 * j + k];
+      r2 += v[k] * v[k];
+    }
+    if (r2 > cut2 || r2 < 1e-12) continue;
+    const double r1 = sqrt(r2);
+    const double ke = (m.at_z[i] > 2 || m.at_z[j] > 2) ? p.rep_kexp : p.rep_kexp_light;
+    const double a = sqrt(m.at_repa[i] * m.at_repa[j]), z = m.at_repz[i] * m.at_repz[j];
+    const double r1k = pow(r1, ke), exa = exp(-a * r1k), r1r = pow(r1, p.rep_rexp);
+    const double dE = z * exa / r1r;
+    e += 0.5 * dE;
+    const double f = -(a * r1k * ke + p.rep_rexp) * dE / r2;
+    for (int k = 0; k < 3; ++k) g[k] += f * v[k];
+    for (int a2 = 0; a2 < 3; ++a2)
+      for (int c = 0; c < 3; ++c) sg[3 * a2 + c] += 0.5 * f * v[a2] * v[c];
+  }
+  e = warp_sum(e);
+  for (int k = 0; k < 3; ++k) g[k] = warp_sum(g[k]);
+  for (int k = 0; k < 9; ++k) sg[k] = warp_sum(sg[k]);
+  if (lane == 0) {
+    erep[i] = e;
+    if (grad) {
+      for (int k = 0; k < 3; ++k) grad[3 * i + k] += g[k];
+      for (int k = 0; k < 9; ++k) sig_at[9 * i + k] += sg[k];
+    }
+  }
+}
+
+void launch_repulsion(const DevMol& m, const Gfn2Scalars& p, double* erep, double* grad,
+                      double* sig_at, cudaStream_t s) {
+  k_repulsion<<<(m.nat * 32 + 255) / 256, 256, 0, s>>>(m, p, erep, grad, sig_at);
+}
+
+// ------------------------------------------------------------------------------------
+// orbital potential: vao = vsh(ao) + vat(atom)
+// ------------------------------------------------------------------------------------
+__global__ void k_vao(DevMol m, const double* vsh, const double* vat, double* vao) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m.nao) return;
+  vao[t] = vsh[m.ao_sh[t]] + vat[m.ao_at[t]];
+}
+
+void launch_vao(const DevMol& m, const double* vsh, const double* vat, double* vao,
+                cudaStream_t s) {
+  k_vao<<<(m.nao + 255) / 256, 256, 0, s>>>(m, vsh, vat, vao);
+}
+
+// ------------------------------------------------------------------------------------
+// Fock assembly, tiles of 32x32; block (32, 8).  For a tile pair (I <= J) the block reads
+// the (I,J) tiles of H, S, D, Q and the (J,I) tiles of D, Q (staged through shared memory),
+// writes F(I,J) and its transpose F(J,I).  Every input element is read once.
+//   F_rc = H_rc - 1/2 S_rc (v_r + v_c) - 1/2 sum_k (M_k,rc u_k,A(c) + M_k,cr u_k,A(r))
+// The two multipole products are summed in an order that depends only on min/max(r,c),
+// so F is exactly symmetric.
+// ------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_fock(int n, const int* __restrict__ ao_at,
+                                              const double* __restrict__ H,
+                                              const double* __restrict__ S,
+                                              const double* __restrict__ D,
+                                              const double* __restrict__ Q,
+                                              const double* __restrict__ vao,
+                                              const double* __restrict__ vdp,
+                                              const double* __restrict__ vqp, double* F) {
+  const int I = blockIdx.y, J = blockIdx.x;
+  if (I > J) return;
+  __shared__ double sh[32][33];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const size_t nn = (size_t)n * n;
+  const int c = J * 32 + tx;
+  const bool cin = c < n;
+  double acc[4];
+  int rows[4];
+  const int atc = cin ? ao_at[c] : 0;
+  const double vc = cin ? vao[c] : 0.0;
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    const int r = I * 32 + ty + 8 * s;
+    rows[s] = r;
+    acc[s] = 0.0;
+    if (r < n && cin) {
+      const size_t rc = (size_t)r * n + c;
+      acc[s] = H[rc] - 0.5 * S[rc] * (vao[r] + vc);
+    }
+  }
+  // multipole terms
+  for (int k = 0; k < 9; ++k) {
+    const double* M = k < 3 ? D + k * nn : Q + (k - 3) * nn;
+    const double* u = k < 3 ? vdp : vqp;
+    const int ku = k < 3 ? k : k - 3, su = k < 3 ? 3 : 6;
+    // stage tile (J, I) of M: sh[a][b] = M[J*32 + a][I*32 + b]
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      const int a = ty + 8 * s;
+      const int rr = J * 32 + a, cc = I * 32 + tx;
+      sh[a][tx] = (rr < n && cc < n) ? M[(size_t)rr * n + cc] : 0.0;
+    }
+    __syncthreads();
+    const double uc = cin ? u[su * atc + ku] : 0.0;
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      const int r = rows[s];
+      if (r < n && cin) {
+        const double t1 = M[(size_t)r * n + c] * uc;          // M_rc u_A(c)
+        const double t2 = sh[tx][ty + 8 * s] * u[su * ao_at[r] + ku];  // M_cr u_A(r)
+        acc[s] -= 0.5 * (r <= c ? (t1 + t2) : (t2 + t1));
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    const int r = rows[s];
+    if (r < n && cin) F[(size_t)r * n + c] = acc[s];
+  }
+  if (I == J) return;
+  // transpose write of F(J,I)
+#pragma unroll
+  for (int s = 0; s < 4; ++s) sh[ty + 8 * s][tx] = acc[s];
+  __syncthreads();
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+    const int rr = J * 32 + ty + 8 * s, cc = I * 32 + tx;
+    if (rr < n && cc < n) F[(size_t)rr * n + cc] = sh[tx][ty + 8 * s];
+  }
+}
+
+void launch_fock(int n, const int* ao_at, const double* H, const double* S, const double* D,
+                 const double* Q, const double* vao, const double* vdp, const double* vqp, double* F,
+                 cudaStream_t s) {
+  const int nt = (n + 31) / 32;
+  k_fock<<<dim3(nt, nt), dim3(32, 8), 0, s>>>(n, ao_at, H, S, D, Q, vao, vdp, vqp, F);
+}
+
+// ------------------------------------------------------------------------------------
+// Mulliken: column sums over row chunks.  partial[chunk][11][n]:
+//   0: sum_r P S, 1-3: sum_r P D_k, 4-9: sum_r P Q_q, 10: sum_r P H
+// ------------------------------------------------------------------------------------
+constexpr int MULL_ROWS = 64;
+
+int mulliken_chunks(int n) { return (n + MULL_ROWS - 1) / MULL_ROWS; }
+
+__global__ void __launch_bounds__(128) k_mull_partial(int n, const double* __restrict__ P,
+                                                      const double* __restrict__ S,
+                                                      const double* __restrict__ H,
+                                                      const double* __restrict__ D,
+                                                      const double* __restrict__ Q,
+                                                      double* partial) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int chunk = blockIdx.y;
+  if (c >= n) return;
+  const size_t nn = (size_t)n * n;
+  double acc[11];
+#pragma unroll
+  for (int k = 0; k < 11; ++k) acc[k] = 0.0;
+  const int r0 = chunk * MULL_ROWS, r1 = min(n, r0 + MULL_ROWS);
+  for (int r = r0; r < r1; ++r) {
+    const size_t rc = (size_t)r * n + c;
+    const double pv = P[rc];
+    acc[0] += pv * S[rc];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) acc[1 + k] += pv * D[k * nn + rc];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) acc[4 + q] += pv * Q[q * nn + rc];
+    acc[10] += pv * H[rc];
+  }
+#pragma unroll
+  for (int k = 0; k < 11; ++k) partial[((size_t)chunk * 11 + k) * n + c] = acc[k];
+}
+
+// one thread per atom: reduce chunks for its orbitals, fill shells/atoms
+__global__ void k_mull_reduce(DevMol m, const double* __restrict__ partial, int nchunk,
+                              double* qsh, double* qat, double* dpat, double* qpat,
+                              double* eband) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m.nat) return;
+  const int n = m.nao;
+  double d[3] = {0, 0, 0}, q[6] = {0, 0, 0, 0, 0, 0}, e = 0.0, qa = 0.0;
+  for (int s = m.at_sh[i]; s < m.at_sh[i + 1]; ++s) {
+    double ps = 0.0;
+    const int o = m.sh_ao[s], no = 2 * m.sh_l[s] + 1;
+    for (int mu = o; mu < o + no; ++mu) {
+      for (int ch = 0; ch < nchunk; ++ch) {
+        const double* pp = partial + (size_t)ch * 11 * n;
+        ps += pp[mu];
+        for (int k = 0; k < 3; ++k) d[k] += pp[(1 + k) * (size_t)n + mu];
+        for (int k = 0; k < 6; ++k) q[k] += pp[(4 + k) * (size_t)n + mu];
+        e += pp[10 * (size_t)n + mu];
+      }
+    }
+    const double v = m.sh_refocc[s] - ps;
+    qsh[s] = v;
+    qa += v;
+  }
+  qat[i] = qa;
+  for (int k = 0; k < 3; ++k) dpat[3 * i + k] = -d[k];
+  for (int k = 0; k < 6; ++k) qpat[6 * i + k] = -q[k];
+  eband[i] = e;
+}
+
+void launch_mulliken(const DevMol& m, const double* P, const double* S, const double* H,
+                     const double* D, const double* Q, double* partial, int nchunk, double* qsh,
+                     double* qat, double* dpat, double* qpat, double* eband, cudaStream_t s) {
+  const int n = m.nao;
+  k_mull_partial<<<dim3((n + 127) / 128, nchunk), 128, 0, s>>>(n, P, S, H, D, Q, partial);
+  k_mull_reduce<<<(m.nat + 127) / 128, 128, 0, s>>>(m, partial, nchunk, qsh, qat, dpat, qpat,
+                                                    eband);
+}
+
+// ------------------------------------------------------------------------------------
+// Fermi filling (one block).  Both spin channels share the eigenvalues.
+// ------------------------------------------------------------------------------------
+__device__ double block_sum(double v, double* red) {
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  const int nw = blockDim.x >> 5;
+  double t = threadIdx.x < nw ? red[threadIdx.x] : 0.0;
+  if (w == 0) t = warp_sum(t);
+  __syncthreads();
+  if (threadIdx.x == 0) red[0] = t;
+  __syncthreads();
+  const double r = red[0];
+  __syncthreads();
+  return r;
+}
+
+__device__ void fermi_channel(int n, const double* emo, double nel, double kt, double* occ,
+                              double* red, double* ts) {
+  // Aufbau
+  int homo = (int)floor(nel);
+  const double frac = fmod(nel, 1.0);
+  for (int k = threadIdx.x; k < n; k += blockDim.x)
+    occ[k] = k < homo ? 1.0 : (k == homo ? frac : 0.0);
+  __syncthreads();
+  homo = frac > 0.5 ? homo + 1 : homo;
+  if (homo > 0) {
+    double ef = 0.5 * (emo[max(homo, 1) - 1] + emo[min(homo + 1, n) - 1]);
+    const double occt = homo;
+    const double thr = 1.4901161193847656e-08;      // sqrt(epsilon)
+    const double sqrttiny = 1.4916681462400413e-154;  // sqrt(tiny)
+    for (int cyc = 0; cyc < 200; ++cyc) {
+      double tn = 0.0, td = 0.0;
+      for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const double x = (emo[k] - ef) / kt;
+        double f = 0.0, df = 0.0;
+        if (x < 50.0) {
+          const double ex = exp(x);
+          f = 1.0 / (ex + 1.0);
+          df = ex / (kt * (ex + 1.0) * (ex + 1.0));
+        }
+        occ[k] = f;
+        tn += f;
+        td += df;
+      }
+      tn = block_sum(tn, red);
+      td = block_sum(td, red);
+      const double change = td > sqrttiny ? (occt - tn) / td : 0.0;
+      ef += change;
+      if (fabs(occt - tn) <= thr) break;
+    }
+  }
+  __syncthreads();
+  double s = 0.0;
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    const double o = occ[k];
+    s += log(pow(o, o) * pow(1.0 - o, 1.0 - o));
+  }
+  s = block_sum(s, red);
+  if (threadIdx.x == 0) *ts += s * kt;
+  __syncthreads();
+}
+
+__global__ void k_fermi(int n, const double* emo, double nalp, double nbet, double kt, double* fa,
+                        double* fb, double* focc, double* ts, int* ncols) {
+  __shared__ double red[32];
+  if (threadIdx.x == 0) *ts = 0.0;
+  __syncthreads();
+  fermi_channel(n, emo, nalp, kt, fa, red, ts);
+  fermi_channel(n, emo, nbet, kt, fb, red, ts);
+  int last = -1;
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    const double f = fa[k] + fb[k];
+    focc[k] = f;
+    if (f != 0.0) last = max(last, k);
+  }
+  // block max
+  __shared__ int mx;
+  if (threadIdx.x == 0) mx = -1;
+  __syncthreads();
+  atomicMax(&mx, last);
+  __syncthreads();
+  if (threadIdx.x == 0) *ncols = mx + 1;
+}
+
+void launch_fermi(int n, const double* emo, double nalp, double nbet, double kt, double* focc,
+                  double* ts, int* ncols, cudaStream_t s) {
+  // fa, fb scratch follow focc in memory: focc[n], fa[n], fb[n]
+  k_fermi<<<1, 1024, 0, s>>>(n, emo, nalp, nbet, kt, focc + n, focc + 2 * n, focc, ts, ncols);
+}
+
+// ------------------------------------------------------------------------------------
+// mixer vector packing  [qsh | dpat | qpat]
+// ------------------------------------------------------------------------------------
+__global__ void k_pack(int nsh, int nat, const double* qsh, const double* dpat, const double* qpat,
+                       double* vec) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nd = nsh + 9 * nat;
+  if (t >= nd) return;
+  if (t < nsh) vec[t] = qsh[t];
+  else if (t < nsh + 3 * nat) vec[t] = dpat[t - nsh];
+  else vec[t] = qpat[t - nsh - 3 * nat];
+}
+
+void launch_pack(const DevMol& m, const double* qsh, const double* dpat, const double* qpat,
+                 double* vec, cudaStream_t s) {
+  const int nd = m.nsh + 9 * m.nat;
+  k_pack<<<(nd + 255) / 256, 256, 0, s>>>(m.nsh, m.nat, qsh, dpat, qpat, vec);
+}
+
+__global__ void k_unpack(DevMol m, const double* vec, double* qsh, double* qat, double* dpat,
+                         double* qpat) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nsh = m.nsh, nat = m.nat;
+  if (t < nsh) qsh[t] = vec[t];
+  if (t < 3 * nat) dpat[t] = vec[nsh + t];
+  if (t < 6 * nat) qpat[t] = vec[nsh + 3 * nat + t];
+  if (t < nat) {
+    double a = 0.0;
+    for (int s = m.at_sh[t]; s < m.at_sh[t + 1]; ++s) a += vec[s];
+    qat[t] = a;
+  }
+}
+
+void launch_unpack(const DevMol& m, const double* vec, double* qsh, double* qat, double* dpat,
+                   double* qpat, cudaStream_t s) {
+  const int nt = m.nsh > 6 * m.nat ? m.nsh : 6 * m.nat;
+  k_unpack<<<(nt + 255) / 256, 256, 0, s>>>(m, vec, qsh, qat, dpat, qpat);
+}
+
+__global__ void k_diff(int nd, const double* vout, const double* q, double* dq, double* err) {
+  __shared__ double red[32];
+  double s = 0.0;
+  for (int t = threadIdx.x; t < nd; t += blockDim.x) {
+    const double d = vout[t] - q[t];
+    dq[t] = d;
+    s += d * d / nd;
+  }
+  s = block_sum(s, red);
+  if (threadIdx.x == 0) *err = sqrt(s);
+}
+
+void launch_diff(int nd, const double* vout, const double* q, double* dq, double* err,
+                 cudaStream_t s) {
+  k_diff<<<1, 1024, 0, s>>>(nd, vout, q, dq, err);
+}
+
+// ------------------------------------------------------------------------------------
+// Broyden step (one block).  Same recurrences as the reference; the overlap matrix a(i,j)
+// is kept between calls and only the row of the newest history vector is recomputed
+// (the other rows are unchanged dot products).
+// ------------------------------------------------------------------------------------
+__device__ double block_dot(int nd, const double* x, const double* y, double* red) {
+  double s = 0.0;
+  for (int t = threadIdx.x; t < nd; t += blockDim.x) s += x[t] * y[t];
+  return block_sum(s, red);
+}
+
+__global__ void k_broyden(int nd, int memory, int iter, double alpha, double* q, double* qlast,
+                          const double* dq, double* dqlast, double* df, double* u, double* a,
+                          double* omega, double* work, int* status) {
+  __shared__ double red[32];
+  if (iter == 1) {
+    for (int t = threadIdx.x; t < nd; t += blockDim.x) {
+      dqlast[t] = dq[t];
+      qlast[t] = q[t];
+      q[t] = q[t] + alpha * dq[t];
+    }
+    if (threadIdx.x == 0) *status = 0;
+    return;
+  }
+  const int itn = iter - 1;
+  const int it1 = (itn - 1) % memory;
+  const int nhist = min(memory, itn);
+  const int first = max(1, itn - memory + 1);
+  const double omega0 = 0.01, minw = 1.0, maxw = 100000.0, wfac = 0.01;
+  double w = sqrt(block_dot(nd, dq, dq, red));
+  w = w > wfac / maxw ? wfac / w : maxw;
+  if (w < minw) w = minw;
+  if (threadIdx.x == 0) omega[it1] = w;
+  double* dfn = df + (size_t)it1 * nd;
+  for (int t = threadIdx.x; t < nd; t += blockDim.x) dfn[t] = dq[t] - dqlast[t];
+  __syncthreads();
+  double inv = sqrt(block_dot(nd, dfn, dfn, red));
+  inv = inv > 2.220446049250313e-16 ? inv : 2.220446049250313e-16;
+  inv = 1.0 / inv;
+  for (int t = threadIdx.x; t < nd; t += blockDim.x) dfn[t] *= inv;
+  __syncthreads();
+  // history indices, c vector, a row
+  double* beta = work;                      // [nhist][nhist]
+  double* cvec = work + memory * memory;    // [nhist]
+  for (int ih = 0; ih < nhist; ++ih) {
+    const int i = (first + ih - 1) % memory;
+    const double dfi_dq = block_dot(nd, df + (size_t)i * nd, dq, red);
+    const double aij = block_dot(nd, df + (size_t)i * nd, dfn, red);
+    if (threadIdx.x == 0) {
+      cvec[ih] = omega[i] * dfi_dq;
+      a[(size_t)i * memory + it1] = aij;
+      a[(size_t)it1 * memory + i] = aij;
+    }
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < nhist * nhist; t += blockDim.x) {
+    const int ih = t / nhist, jh = t % nhist;
+    const int i = (first + ih - 1) % memory, j = (first + jh - 1) % memory;
+    beta[t] = omega[i] * omega[j] * a[(size_t)i * memory + j] + (ih == jh ? omega0 * omega0 : 0.0);
+  }
+  __syncthreads();
+  // solve beta^T x = c by Gaussian elimination with partial pivoting (getrf + getrs 't')
+  __shared__ int piv;
+  __shared__ int fail;
+  if (threadIdx.x == 0) fail = 0;
+  __syncthreads();
+  // transpose in place to solve beta^T
+  for (int t = threadIdx.x; t < nhist * nhist; t += blockDim.x) {
+    const int i = t / nhist, j = t % nhist;
+    if (i < j) {
+      const double x = beta[i * nhist + j];
+      beta[i * nhist + j] = beta[j * nhist + i];
+      beta[j * nhist + i] = x;
+    }
+  }
+  __syncthreads();
+  for (int k = 0; k < nhist; ++k) {
+    if (threadIdx.x == 0) {
+      int p = k;
+      double best = fabs(beta[k * nhist + k]);
+      for (int i = k + 1; i < nhist; ++i) {
+        const double v = fabs(beta[i * nhist + k]);
+        if (v > best) {
+          best = v;
+          p = i;
+        }
+      }
+      piv = p;
+      if (best == 0.0) fail = k + 1;
+    }
+    __syncthreads();
+    if (fail) break;
+    const int p = piv;
+    if (p != k) {
+      for (int j = threadIdx.x; j < nhist; j += blockDim.x) {
+        const double x = beta[k * nhist + j];
+        beta[k * nhist + j] = beta[p * nhist + j];
+        beta[p * nhist + j] = x;
+      }
+      if (threadIdx.x == 0) {
+        const double x = cvec[k];
+        cvec[k] = cvec[p];
+        cvec[p] = x;
+      }
+    }
+    __syncthreads();
+    const double pivv = beta[k * nhist + k];
+    for (int t = threadIdx.x; t < (nhist - k - 1) * (nhist - k); t += blockDim.x) {
+      const int i = k + 1 + t / (nhist - k), j = k + t % (nhist - k);
+      const double f = beta[i * nhist + k] / pivv;
+      if (j > k) beta[i * nhist + j] -= f * beta[k * nhist + j];
+    }
+    __syncthreads();
+    for (int i = k + 1 + threadIdx.x; i < nhist; i += blockDim.x) {
+      cvec[i] -= beta[i * nhist + k] / pivv * cvec[k];
+    }
+    __syncthreads();
+  }
+  if (fail) {
+    if (threadIdx.x == 0) *status = fail;
+    return;
+  }
+  if (threadIdx.x == 0) {
+    for (int i = nhist - 1; i >= 0; --i) {
+      double s = cvec[i];
+      for (int j = i + 1; j < nhist; ++j) s -= beta[i * nhist + j] * cvec[j];
+      cvec[i] = s / beta[i * nhist + i];
+    }
+    *status = 0;
+  }
+  __syncthreads();
+  double* un = u + (size_t)it1 * nd;
+  for (int t = threadIdx.x; t < nd; t += blockDim.x) {
+    un[t] = alpha * dfn[t] + inv * (q[t] - qlast[t]);
+    dqlast[t] = dq[t];
+    qlast[t] = q[t];
+    q[t] = q[t] + alpha * dq[t];
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < nd; t += blockDim.x) {
+    double v = q[t];
+    for (int ih = 0; ih < nhist; ++ih) {
+      const int i = (first + ih - 1) % memory;
+      v -= omega[i] * cvec[ih] * u[(size_t)i * nd + t];
+    }
+    q[t] = v;
+  }
+}
+
+__global__ void k_eelec_init(int nat, const double* ts, const double* eband, double* eelec) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nat) eelec[i] = *ts / nat + eband[i];
+}
+
+void launch_eelec_init(int nat, const double* ts, const double* eband, double* eelec,
+                       cudaStream_t s) {
+  k_eelec_init<<<(nat + 127) / 128, 128, 0, s>>>(nat, ts, eband, eelec);
+}
+
+__global__ void k_fe(int n, const double* f, const double* e, double* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = f[i] * e[i];
+}
+
+void launch_fe(int n, const double* f, const double* e, double* out, cudaStream_t s) {
+  k_fe<<<(n + 255) / 256, 256, 0, s>>>(n, f, e, out);
+}
+
+void launch_broyden_next(BroydenState& b, cudaStream_t s) {
+  b.iter += 1;
+  k_broyden<<<1, 1024, 0, s>>>(b.ndim, b.memory, b.iter, b.damp, b.q, b.qlast, b.dq, b.dqlast,
+                               b.df, b.u, b.a, b.omega, b.work, b.status);
+}
+
+}  // namespace tb

@@ -1,0 +1,183 @@
+"""Python surface of the engine: ``Structure``, ``Calculator`` and ``Result``.
+
+Same class names, constructor arguments, ``set``/``get`` keys and
+``singlepoint(res=None, copy=False)`` semantics as the reference's
+``tblite.interface`` (python/tblite/interface.py:31-685), implemented on the
+C ABI of ``libtblite_gb300.so`` (CUDA, FP64).  Inputs and outputs are in
+atomic units (Bohr, Hartree).
+"""
+from __future__ import annotations
+
+from ctypes import byref, c_int, c_void_p
+from typing import Optional
+
+import numpy as np
+
+from . import library
+from .exceptions import TBLiteRuntimeError, TBLiteTypeError, TBLiteValueError
+
+
+class Structure:
+    """Molecular structure (reference interface.py:31-172)."""
+
+    def __init__(self, numbers, positions, charge: Optional[float] = None,
+                 uhf: Optional[int] = None, lattice=None, periodic=None):
+        numbers = np.asarray(numbers)
+        positions = np.asarray(positions, dtype=np.float64)
+        if numbers.ndim != 1:
+            raise TBLiteValueError("Expected one dimensional numbers array")
+        if positions.shape != (len(numbers), 3):
+            raise TBLiteValueError("Expected tripels of cartesian coordinates")
+        if lattice is not None or (periodic is not None and np.any(periodic)):
+            raise TBLiteValueError("Periodic systems are not supported by the GPU engine")
+        self._natoms = len(numbers)
+        self._mol = library.new_structure(numbers, positions, charge, uhf)
+
+    def __len__(self):
+        return self._natoms
+
+    def update(self, positions, lattice=None):
+        positions = np.asarray(positions, dtype=np.float64)
+        if positions.shape != (self._natoms, 3):
+            raise TBLiteValueError("Dimension missmatch for position")
+        library.update_geometry(self._mol, positions)
+
+    def __del__(self):
+        mol = getattr(self, "_mol", None)
+        if mol is not None and mol.value:
+            library.load().tblite_delete_structure(byref(mol))
+
+
+class Result:
+    """Calculation result and restart data (reference interface.py:175-380)."""
+
+    _shapes = {
+        "energy": (), "energies": ("nat",), "gradient": ("nat", 3), "virial": (3, 3),
+        "charges": ("nat",), "bond-orders": ("nat", "nat"), "dipole": (3,), "quadrupole": (6,),
+        "orbital-energies": ("nao",), "orbital-occupations": ("nao",),
+        "orbital-coefficients": ("nao", "nao"), "density-matrix": ("nao", "nao"),
+        "overlap-matrix": ("nao", "nao"), "hamiltonian-matrix": ("nao", "nao"),
+    }
+
+    def __init__(self, other: Optional["Result"] = None):
+        lib = library.load()
+        if other is not None:
+            self._res = c_void_p(lib.tblite_copy_result(other._res))
+        else:
+            self._res = c_void_p(lib.tblite_new_result())
+
+    def __del__(self):
+        res = getattr(self, "_res", None)
+        if res is not None and res.value:
+            library.load().tblite_delete_result(byref(res))
+
+    def get(self, attribute: str):
+        if attribute == "natoms":
+            return library.result_int(self._res, "number_of_atoms")
+        if attribute == "norbitals":
+            return library.result_int(self._res, "number_of_orbitals")
+        if attribute not in self._shapes:
+            raise TBLiteValueError(f"Attribute '{attribute}' is not available in this container")
+        dims = {"nat": None, "nao": None}
+        shape = self._shapes[attribute]
+        if "nat" in shape:
+            dims["nat"] = library.result_int(self._res, "number_of_atoms")
+        if "nao" in shape:
+            dims["nao"] = library.result_int(self._res, "number_of_orbitals")
+        real = tuple(dims[s] if isinstance(s, str) else s for s in shape)
+        name = attribute.replace("-", "_")
+        if attribute == "energy":
+            return float(library.result_array(self._res, name, (1,))[0])
+        return library.result_array(self._res, name, real)
+
+    def dict(self):
+        out = {}
+        for key in ("energy", "gradient", "virial", "charges", "dipole", "orbital-energies",
+                    "orbital-occupations", "density-matrix"):
+            try:
+                out[key] = self.get(key)
+            except TBLiteRuntimeError:
+                pass
+        return out
+
+
+class Calculator(Structure):
+    """Single point calculator (reference interface.py:382-685)."""
+
+    _methods = ("GFN2-xTB",)
+
+    def __init__(self, method: str, numbers, positions, charge: Optional[float] = None,
+                 uhf: Optional[int] = None, lattice=None, periodic=None, xtb_config=None,
+                 **context_kwargs):
+        Structure.__init__(self, numbers, positions, charge, uhf, lattice, periodic)
+        if method not in self._methods:
+            raise TBLiteValueError(f"Method '{method}' is not available for this calculator")
+        self._ctx = library.new_context(**context_kwargs)
+        self._calc = library.new_gfn2_calculator(self._ctx, self._mol)
+        self._method = method
+
+    def __del__(self):
+        lib = library.load()
+        calc = getattr(self, "_calc", None)
+        if calc is not None and calc.value:
+            lib.tblite_delete_calculator(byref(calc))
+        ctx = getattr(self, "_ctx", None)
+        if ctx is not None and ctx.value:
+            lib.tblite_delete_context(byref(ctx))
+        Structure.__del__(self)
+
+    def set(self, attribute: str, value) -> None:
+        lib = library.load()
+        setters = {
+            "accuracy": lambda v: lib.tblite_set_calculator_accuracy(self._ctx, self._calc, float(v)),
+            "max-iter": lambda v: lib.tblite_set_calculator_max_iter(self._ctx, self._calc, int(v)),
+            "mixer-damping": lambda v: lib.tblite_set_calculator_mixer_damping(self._ctx, self._calc,
+                                                                               float(v)),
+            "mixer-memory": lambda v: lib.tblite_set_calculator_mixer_memory(self._ctx, self._calc,
+                                                                             int(v)),
+            "temperature": lambda v: lib.tblite_set_calculator_temperature(self._ctx, self._calc,
+                                                                           float(v)),
+            "save-integrals": lambda v: lib.tblite_set_calculator_save_integrals(
+                self._ctx, self._calc, int(bool(v))),
+            "guess": lambda v: lib.tblite_set_calculator_guess(
+                self._ctx, self._calc, {"sad": 0, "eeq": 1, "eeqbc": 2}.get(v, v)
+                if isinstance(v, str) else int(v)),
+            "annealing": lambda v: lib.tblite_set_calculator_temperature_annealing(
+                self._ctx, self._calc, float(v[0]), int(v[1]), int(v[2])),
+            "verbosity": lambda v: lib.tblite_set_context_verbosity(self._ctx, int(v)),
+        }
+        if attribute not in setters:
+            raise TBLiteValueError(f"Attribute '{attribute}' is not supported in this calculator")
+        setters[attribute](value)
+        library.context_check(self._ctx)
+
+    def get(self, attribute: str):
+        lib = library.load()
+        if attribute in ("shell-map", "angular-momenta"):
+            nsh = c_int(0)
+            lib.tblite_get_calculator_shell_count(self._ctx, self._calc, byref(nsh))
+            out = np.zeros(nsh.value, dtype=np.int32)
+            fn = (lib.tblite_get_calculator_shell_map if attribute == "shell-map"
+                  else lib.tblite_get_calculator_angular_momenta)
+            fn(self._ctx, self._calc, library._ip(out))
+            library.context_check(self._ctx)
+            return out
+        if attribute == "orbital-map":
+            nao = c_int(0)
+            lib.tblite_get_calculator_orbital_count(self._ctx, self._calc, byref(nao))
+            out = np.zeros(nao.value, dtype=np.int32)
+            lib.tblite_get_calculator_orbital_map(self._ctx, self._calc, library._ip(out))
+            library.context_check(self._ctx)
+            return out
+        raise TBLiteValueError(f"Attribute '{attribute}' is not available in this calculator")
+
+    def add(self, interaction: str, *args) -> None:
+        raise TBLiteValueError(f"Interaction '{interaction}' is not available in the GPU engine")
+
+    def singlepoint(self, res: Optional[Result] = None, copy: bool = False) -> Result:
+        if res is not None and not isinstance(res, Result):
+            raise TBLiteTypeError("Restart data must be a Result object")
+        _res = Result(res) if copy or res is None else res
+        library.load().tblite_get_singlepoint(self._ctx, self._mol, self._calc, _res._res)
+        library.context_check(self._ctx)
+        return _res

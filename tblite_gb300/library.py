@@ -1,0 +1,193 @@
+"""ctypes binding of the C ABI in ``include/tblite.h`` (libtblite_gb300.so).
+
+Mirrors the role of the reference's CFFI layer (python/tblite/library.py):
+every wrapper checks the error handle / context after the call and raises
+``TBLiteRuntimeError`` with the library's message.  The shared library is the
+in-tree CUDA build; if it is missing or fails to load, importing the wrappers
+raises -- there is no CPU implementation behind this module.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from ctypes import POINTER, byref, c_bool, c_char_p, c_double, c_int, c_void_p
+from pathlib import Path
+
+import numpy as np
+
+from .exceptions import TBLiteRuntimeError
+
+_LIB = None
+_dbl_p = POINTER(c_double)
+_int_p = POINTER(c_int)
+
+
+def library_path() -> Path:
+    env = os.environ.get("TBLITE_GB300_LIBRARY")
+    if env:
+        return Path(env)
+    return Path(__file__).resolve().parent / "lib" / "libtblite_gb300.so"
+
+
+_SIGNATURES = {
+    "tblite_get_version": (c_int, []),
+    "tblite_get_feature": (c_int, [c_char_p]),
+    "tblite_new_error": (c_void_p, []),
+    "tblite_delete_error": (None, [POINTER(c_void_p)]),
+    "tblite_check_error": (c_int, [c_void_p]),
+    "tblite_clear_error": (None, [c_void_p]),
+    "tblite_get_error": (None, [c_void_p, c_char_p, _int_p]),
+    "tblite_set_error": (None, [c_void_p, c_char_p, _int_p]),
+    "tblite_new_context": (c_void_p, []),
+    "tblite_delete_context": (None, [POINTER(c_void_p)]),
+    "tblite_check_context": (c_int, [c_void_p]),
+    "tblite_get_context_error": (None, [c_void_p, c_char_p, _int_p]),
+    "tblite_set_context_logger": (None, [c_void_p, c_void_p, c_void_p]),
+    "tblite_set_context_color": (None, [c_void_p, c_int]),
+    "tblite_set_context_verbosity": (None, [c_void_p, c_int]),
+    "tblite_new_structure": (c_void_p, [c_void_p, c_int, _int_p, _dbl_p, _dbl_p, _int_p, _dbl_p,
+                                        POINTER(c_bool)]),
+    "tblite_delete_structure": (None, [POINTER(c_void_p)]),
+    "tblite_update_structure_geometry": (None, [c_void_p, c_void_p, _dbl_p, _dbl_p]),
+    "tblite_update_structure_charge": (None, [c_void_p, c_void_p, _dbl_p]),
+    "tblite_update_structure_uhf": (None, [c_void_p, c_void_p, _int_p]),
+    "tblite_new_result": (c_void_p, []),
+    "tblite_copy_result": (c_void_p, [c_void_p]),
+    "tblite_delete_result": (None, [POINTER(c_void_p)]),
+    "tblite_new_gfn2_calculator": (c_void_p, [c_void_p, c_void_p, c_void_p]),
+    "tblite_delete_calculator": (None, [POINTER(c_void_p)]),
+    "tblite_set_calculator_accuracy": (None, [c_void_p, c_void_p, c_double]),
+    "tblite_set_calculator_max_iter": (None, [c_void_p, c_void_p, c_int]),
+    "tblite_set_calculator_mixer_damping": (None, [c_void_p, c_void_p, c_double]),
+    "tblite_set_calculator_mixer_memory": (None, [c_void_p, c_void_p, c_int]),
+    "tblite_set_calculator_mixer": (None, [c_void_p, c_void_p, c_int]),
+    "tblite_set_calculator_temperature_annealing": (None, [c_void_p, c_void_p, c_double, c_int,
+                                                           c_int]),
+    "tblite_set_calculator_guess": (None, [c_void_p, c_void_p, c_int]),
+    "tblite_set_calculator_temperature": (None, [c_void_p, c_void_p, c_double]),
+    "tblite_set_calculator_save_integrals": (None, [c_void_p, c_void_p, c_int]),
+    "tblite_get_calculator_shell_count": (None, [c_void_p, c_void_p, _int_p]),
+    "tblite_get_calculator_shell_map": (None, [c_void_p, c_void_p, _int_p]),
+    "tblite_get_calculator_angular_momenta": (None, [c_void_p, c_void_p, _int_p]),
+    "tblite_get_calculator_orbital_count": (None, [c_void_p, c_void_p, _int_p]),
+    "tblite_get_calculator_orbital_map": (None, [c_void_p, c_void_p, _int_p]),
+    "tblite_get_singlepoint": (None, [c_void_p, c_void_p, c_void_p, c_void_p]),
+}
+for _name in ("number_of_atoms", "number_of_shells", "number_of_orbitals", "number_of_spins"):
+    _SIGNATURES[f"tblite_get_result_{_name}"] = (None, [c_void_p, c_void_p, _int_p])
+for _name in ("energy", "energies", "gradient", "virial", "charges", "bond_orders", "dipole",
+              "quadrupole", "orbital_energies", "orbital_occupations", "orbital_coefficients",
+              "density_matrix", "overlap_matrix", "hamiltonian_matrix"):
+    _SIGNATURES[f"tblite_get_result_{_name}"] = (None, [c_void_p, c_void_p, _dbl_p])
+
+
+def load():
+    """Load the CUDA engine; raises if the in-tree build is missing."""
+    global _LIB
+    if _LIB is None:
+        path = library_path()
+        if not path.exists():
+            raise TBLiteRuntimeError(
+                f"CUDA engine library not found at {path}; run tblite_gb300._build.build()")
+        lib = ctypes.CDLL(str(path))
+        for name, (res, args) in _SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = lib
+    return _LIB
+
+
+def exported_symbols():
+    return list(_SIGNATURES)
+
+
+# ----------------------------------------------------------------------------- helpers
+def _dp(a):
+    return a.ctypes.data_as(_dbl_p)
+
+
+def _ip(a):
+    return a.ctypes.data_as(_int_p)
+
+
+class _Error:
+    def __init__(self):
+        self.lib = load()
+        self.h = c_void_p(self.lib.tblite_new_error())
+
+    def check(self):
+        if self.lib.tblite_check_error(self.h):
+            buf = ctypes.create_string_buffer(512)
+            size = c_int(512)
+            self.lib.tblite_get_error(self.h, buf, byref(size))
+            self.lib.tblite_clear_error(self.h)
+            raise TBLiteRuntimeError(buf.value.decode())
+
+    def __del__(self):
+        if getattr(self, "h", None) and self.h.value:
+            self.lib.tblite_delete_error(byref(self.h))
+
+
+def context_check(ctx):
+    lib = load()
+    if lib.tblite_check_context(ctx):
+        buf = ctypes.create_string_buffer(512)
+        size = c_int(512)
+        msgs = []
+        while lib.tblite_check_context(ctx):
+            lib.tblite_get_context_error(ctx, buf, byref(size))
+            msgs.append(buf.value.decode())
+        raise TBLiteRuntimeError("\n".join(msgs))
+
+
+def new_context(verbosity: int = 0):
+    lib = load()
+    ctx = c_void_p(lib.tblite_new_context())
+    lib.tblite_set_context_verbosity(ctx, int(verbosity))
+    return ctx
+
+
+def new_structure(numbers, positions, charge=None, uhf=None):
+    lib = load()
+    err = _Error()
+    num = np.ascontiguousarray(numbers, dtype=np.int32)
+    pos = np.ascontiguousarray(positions, dtype=np.float64)
+    ch = None if charge is None else byref(c_double(float(charge)))
+    u = None if uhf is None else byref(c_int(int(uhf)))
+    mol = c_void_p(lib.tblite_new_structure(err.h, len(num), _ip(num), _dp(pos), ch, u, None, None))
+    err.check()
+    return mol
+
+
+def update_geometry(mol, positions):
+    lib = load()
+    err = _Error()
+    pos = np.ascontiguousarray(positions, dtype=np.float64)
+    lib.tblite_update_structure_geometry(err.h, mol, _dp(pos), None)
+    err.check()
+
+
+def new_gfn2_calculator(ctx, mol):
+    lib = load()
+    calc = c_void_p(lib.tblite_new_gfn2_calculator(ctx, mol, None))
+    context_check(ctx)
+    return calc
+
+
+def result_array(res, name, shape):
+    lib = load()
+    err = _Error()
+    out = np.zeros(shape, dtype=np.float64)
+    getattr(lib, f"tblite_get_result_{name}")(err.h, res, _dp(out))
+    err.check()
+    return out
+
+
+def result_int(res, name):
+    lib = load()
+    err = _Error()
+    v = c_int(0)
+    getattr(lib, f"tblite_get_result_{name}")(err.h, res, byref(v))
+    err.check()
+    return v.value

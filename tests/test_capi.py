@@ -1,0 +1,89 @@
+"""Host-side checks of the C ABI (no GPU needed): exports, handles, errors, basis maps."""
+import re
+from ctypes import byref, c_int, c_void_p
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from tblite_gb300 import _build, library
+from tblite_gb300.exceptions import TBLiteRuntimeError
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+@pytest.fixture(scope="module")
+def lib():
+    _build.build()
+    return library.load()
+
+
+def test_header_symbols_exported(lib):
+    header = (ROOT / "include" / "tblite.h").read_text()
+    names = sorted(set(re.findall(r"\b(tblite_[a-z0-9_]+)\s*\(", header)))
+    assert len(names) > 50
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_error_roundtrip(lib):
+    err = c_void_p(lib.tblite_new_error())
+    assert lib.tblite_check_error(err) == 0
+    msg = b"some failure"
+    size = c_int(len(msg))
+    lib.tblite_set_error(err, msg, byref(size))
+    assert lib.tblite_check_error(err) == 1
+    import ctypes
+    buf = ctypes.create_string_buffer(64)
+    cap = c_int(64)
+    lib.tblite_get_error(err, buf, byref(cap))
+    assert buf.value == msg
+    lib.tblite_clear_error(err)
+    assert lib.tblite_check_error(err) == 0
+    lib.tblite_delete_error(byref(err))
+    assert err.value is None
+
+
+def test_null_handles_report_errors(lib):
+    ctx = c_void_p(lib.tblite_new_context())
+    res = c_void_p(lib.tblite_new_result())
+    lib.tblite_get_singlepoint(ctx, None, None, res)
+    assert lib.tblite_check_context(ctx) == 1
+    with pytest.raises(TBLiteRuntimeError, match="structure data is missing"):
+        library.context_check(ctx)
+    lib.tblite_delete_result(byref(res))
+    lib.tblite_delete_context(byref(ctx))
+
+
+def test_structure_validation():
+    with pytest.raises(TBLiteRuntimeError, match="Non-finite"):
+        library.new_structure([8, 1], [[0, 0, 0], [np.nan, 0, 0]])
+    with pytest.raises(TBLiteRuntimeError, match="Invalid"):
+        library.new_structure([], np.zeros((0, 3)))
+
+
+def test_result_without_data(lib):
+    res = c_void_p(lib.tblite_new_result())
+    with pytest.raises(TBLiteRuntimeError, match="does not contain energy"):
+        library.result_array(res, "energy", (1,))
+    lib.tblite_delete_result(byref(res))
+
+
+def test_basis_maps_match_oracle():
+    from oracle import gfn2
+    from tblite_gb300 import interface, workloads
+
+    z, x = workloads.water_cluster((2, 1, 1), seed=5)
+    calc = interface.Calculator("GFN2-xTB", z, x)
+    ref = gfn2.new_calc(gfn2.Molecule(z, x))
+    assert np.array_equal(calc.get("shell-map"), ref.sh_atom)
+    assert np.array_equal(calc.get("angular-momenta"), ref.sh_l)
+    ao2sh = np.repeat(np.arange(len(ref.sh_l)), 2 * ref.sh_l + 1)
+    assert np.array_equal(calc.get("orbital-map"), ao2sh)
+
+
+def test_unsupported_element_message():
+    from tblite_gb300 import interface
+
+    with pytest.raises(TBLiteRuntimeError, match="d shells"):
+        interface.Calculator("GFN2-xTB", [26, 1], [[0, 0, 0], [0, 0, 3.0]])
