@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "../../include/tblite.h"
+#include "../../include/tblite_gb300_ext.h"
 #include "element_data.inc"
 #include "engine.h"
 #include "params_gfn2.inc"
@@ -389,6 +390,71 @@ static DevMol dev_mol(const _tblite_calculator* c) {
   return m;
 }
 
+// --------------------------------------------------------------------------------------
+// optional per-phase timing with CUDA events on the engine stream
+// --------------------------------------------------------------------------------------
+enum Phase { PH_SETUP, PH_POTENTIAL, PH_FOCK, PH_EIGEN, PH_DENSITY, PH_MULLIKEN, PH_MIXER,
+             PH_GRADIENT, PH_TRANSFER, PH_COUNT };
+
+struct Profiler {
+  bool enabled = false;
+  std::vector<cudaEvent_t> pool;
+  std::vector<std::pair<int, std::pair<int, int>>> marks;  // phase, (event a, event b)
+  int used = 0;
+  double phase_ms[PH_COUNT] = {0};
+  int phase_n[PH_COUNT] = {0};
+  double total_ms = 0.0;
+  int iterations = 0;
+  int open_phase = -1, open_event = -1;
+  cudaEvent_t ev() {
+    if (used == (int)pool.size()) {
+      cudaEvent_t e;
+      cuda_check(cudaEventCreate(&e), "event");
+      pool.push_back(e);
+    }
+    return pool[used++];
+  }
+  void reset() {
+    used = 0;
+    marks.clear();
+    for (int k = 0; k < PH_COUNT; ++k) {
+      phase_ms[k] = 0.0;
+      phase_n[k] = 0;
+    }
+    total_ms = 0.0;
+  }
+  void begin(int ph, cudaStream_t s) {
+    if (!enabled) return;
+    const int a = used;
+    cuda_check(cudaEventRecord(ev(), s), "record");
+    open_phase = ph;
+    open_event = a;
+  }
+  void end(cudaStream_t s) {
+    if (!enabled || open_phase < 0) return;
+    const int b = used;
+    cuda_check(cudaEventRecord(ev(), s), "record");
+    marks.push_back({open_phase, {open_event, b}});
+    open_phase = -1;
+  }
+  void collect() {
+    if (!enabled || marks.empty()) return;
+    for (auto& mk : marks) {
+      float ms = 0.f;
+      cuda_check(cudaEventElapsedTime(&ms, pool[mk.second.first], pool[mk.second.second]),
+                 "elapsed");
+      phase_ms[mk.first] += ms;
+      phase_n[mk.first] += 1;
+    }
+    float tot = 0.f;
+    cuda_check(cudaEventElapsedTime(&tot, pool[marks.front().second.first],
+                                    pool[marks.back().second.second]),
+               "elapsed");
+    total_ms = tot;
+  }
+};
+static Profiler g_prof;
+
 static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
                         _tblite_calculator* c, _tblite_result* res) {
   if (mol->nat != c->nat) throw std::runtime_error("structure does not match calculator");
@@ -420,7 +486,9 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
   const double diff = std::min((double)nuhf, nocc);
   const double nalp = (nocc - diff) / 2 + diff, nbet = (nocc - diff) / 2;
 
+  g_prof.reset();
   // geometry-dependent setup
+  g_prof.begin(PH_SETUP, s);
   launch_cn(m, p, w.cn.p, s);
   launch_setup_levels(m, p, w.cn.p, w.se.p, w.mrad.p, w.dmrdcn.p, s);
   launch_build_h0(m, p, w.se.p, w.S.p, w.H.p, w.D.p, w.Q.p, s);
@@ -430,6 +498,7 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
   cuda_check(cudaMemsetAsync(w.dEdcn.p, 0, sizeof(double) * nat, s), "zero");
   launch_repulsion(m, p, w.erep.p, w.grad.p, w.sig_at.p, s);
   const int chol = eigen_set_overlap(w.eig, w.S.p);
+  g_prof.end(s);
   if (chol != 0) throw std::runtime_error("overlap matrix is not positive definite");
 
   // initial guess: restart from a compatible result, else SAD (wavefunction/guess.f90:51-120)
@@ -498,27 +567,38 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
       else kt = target_kt;
     }
     if (iscf > 0) {
+      g_prof.begin(PH_MIXER, s);
       launch_broyden_next(b, s);
       int st = 0;
       cuda_check(cudaMemcpyAsync(&st, w.b_status.p, sizeof(int), cudaMemcpyDeviceToHost, s), "st");
       cuda_check(cudaStreamSynchronize(s), "sync");
       if (st != 0) throw std::runtime_error("Broyden mixing failed to obtain next iteration");
       launch_unpack(m, w.b_q.p, w.qsh.p, w.qat.p, w.dpat.p, w.qpat.p, s);
+      g_prof.end(s);
     }
     ++iscf;
+    g_prof.begin(PH_POTENTIAL, s);
     launch_coulomb_potential(m, p, w.mrad.p, w.qsh.p, w.qat.p, w.dpat.p, w.qpat.p, w.vsh.p, w.vat.p,
                              w.vdp.p, w.vqp.p, s);
     launch_vao(m, w.vsh.p, w.vat.p, w.vao.p, s);
+    g_prof.end(s);
+    g_prof.begin(PH_FOCK, s);
     launch_fock(n, w.ao_at.p, w.H.p, w.S.p, w.D.p, w.Q.p, w.vao.p, w.vdp.p, w.vqp.p, w.F.p, s);
     launch_pack(m, w.qsh.p, w.dpat.p, w.qpat.p, w.b_q.p, s);  // mixer%set
+    g_prof.end(s);
+    g_prof.begin(PH_EIGEN, s);
     const int info = eigen_solve(w.eig, w.F.p, w.C.p, w.emo.p);
+    g_prof.end(s);
     if (info != 0)
       throw std::runtime_error("(sygvd) failed to solve eigenvalue problem. info=" +
                                std::to_string(info));
+    g_prof.begin(PH_DENSITY, s);
     launch_fermi(n, w.emo.p, nalp, nbet, kt, w.focc.p, w.scal.p, w.icount.p, s);
     w.icount.download(h_cnt, 1, s);
     cuda_check(cudaStreamSynchronize(s), "sync");
     density_matrix(n, h_cnt[0], w.C.p, w.focc.p, w.P.p, w.scratch.p, s);
+    g_prof.end(s);
+    g_prof.begin(PH_MULLIKEN, s);
     launch_mulliken(m, w.P.p, w.S.p, w.H.p, w.D.p, w.Q.p, w.mull.p, mulliken_chunks(n), w.qsh_o.p,
                     w.qat_o.p, w.dpat_o.p, w.qpat_o.p, w.eband.p, s);
     launch_pack(m, w.qsh_o.p, w.dpat_o.p, w.qpat_o.p, w.vec_out.p, s);
@@ -526,6 +606,7 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
     launch_eelec_init(nat, w.scal.p, w.eband.p, w.eelec.p, s);
     launch_coulomb_energy(m, p, w.mrad.p, w.qsh_o.p, w.qat_o.p, w.dpat_o.p, w.qpat_o.p, w.eelec.p,
                           s);
+    g_prof.end(s);
     w.eelec.download(h_eelec, nat, s);
     w.scal.download(h_scal, 2, s);
     cuda_check(cudaStreamSynchronize(s), "sync");
@@ -555,6 +636,7 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
   res->has_energy = true;
 
   // gradient (singlepoint.f90:343-381): Coulomb at output moments, H0 with last potential
+  g_prof.begin(PH_GRADIENT, s);
   launch_coulomb_gradient(m, p, w.mrad.p, w.dmrdcn.p, w.qsh_o.p, w.qat_o.p, w.dpat_o.p, w.qpat_o.p,
                           w.grad.p, w.sig_at.p, w.dEdcn.p, s);
   // W = C diag(f e) C^T  (scf/diag.f90:110-143)
@@ -563,6 +645,8 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
   launch_h0_gradient(m, p, w.se.p, w.P.p, w.W.p, w.vao.p, w.vdp.p, w.vqp.p, w.grad.p, w.sigma.p,
                      w.dEdcn.p, s);
   launch_cn_grad(m, p, w.dEdcn.p, w.grad.p, w.sig_at.p, s);
+  g_prof.end(s);
+  g_prof.begin(PH_TRANSFER, s);
   w.grad.download(res->gradient, 3 * nat, s);
   std::vector<double> h_sig_at, h_sigma;
   w.sig_at.download(h_sig_at, 9 * nat, s);
@@ -578,7 +662,10 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
     w.S.download(res->S, (size_t)n * n, s);
     w.H.download(res->H, (size_t)n * n, s);
   }
+  g_prof.end(s);
   cuda_check(cudaStreamSynchronize(s), "sync results");
+  g_prof.collect();
+  g_prof.iterations = iscf;
   res->sigma.assign(9, 0.0);
   for (int k = 0; k < 9; ++k) {
     double acc = h_sigma[k];
@@ -615,6 +702,22 @@ static void set_err(tblite_error e, const std::string& m) {
 }
 
 extern "C" {
+
+void tblite_gb300_set_profiling(int enable) { g_prof.enabled = enable != 0; }
+
+int tblite_gb300_get_profile(double* phase_ms, int* phase_count, int nphase, double* total_ms,
+                             int* iterations) {
+  const int m = std::min(nphase, (int)PH_COUNT);
+  for (int k = 0; k < m; ++k) {
+    if (phase_ms) phase_ms[k] = g_prof.phase_ms[k];
+    if (phase_count) phase_count[k] = g_prof.phase_n[k];
+  }
+  if (total_ms) *total_ms = g_prof.total_ms;
+  if (iterations) *iterations = g_prof.iterations;
+  return PH_COUNT;
+}
+
+unsigned long long tblite_gb300_get_launch_count(void) { return g_kernel_launches; }
 
 int tblite_get_version(void) { return 7 * 100 + 0; }  // 0.7.0 -> 700 (reference version.h)
 

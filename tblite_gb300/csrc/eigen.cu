@@ -148,6 +148,7 @@ void density_matrix(int n, int k, const double* C, const double* f, double* P, d
     return;
   }
   const size_t tot = (size_t)n * k;
+  ++g_kernel_launches;
   k_scale_cols<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(n, k, C, f, work);
   const double one = 1.0, zero = 0.0;
   // P(n x n) = work(n x k) * C(n x k)^T

@@ -17,6 +17,9 @@
 
 namespace tb {
 
+// number of engine kernels launched since library load (instrumentation)
+extern unsigned long long g_kernel_launches;
+
 constexpr int MAXG = 12;    // max primitives per shell
 constexpr int MAXL = 2;     // max angular momentum handled by the kernels
 constexpr double INTCUT = 25.0;  // integral_cutoff(acc) is always 25 in the reference

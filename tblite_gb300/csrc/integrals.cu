@@ -194,6 +194,7 @@ void launch_build_h0(const DevMol& m, const Gfn2Scalars& p, const double* se, do
   const long long npair = (long long)m.nsh * (m.nsh + 1) / 2;
   const long long nthr = npair * 3;
   const int bs = 128;
+  ++g_kernel_launches;
   k_build_h0<<<(unsigned)((nthr + bs - 1) / bs), bs, 0, s>>>(m, p, se, S, H, D, Q, npair);
 }
 
@@ -377,8 +378,10 @@ void launch_h0_gradient(const DevMol& m, const Gfn2Scalars& p, const double* se,
                         double* grad, double* sigma, double* dEdcn, cudaStream_t s) {
   const long long npair = (long long)m.nsh * (m.nsh + 1) / 2;
   const int bs = 128;
+  ++g_kernel_launches;
   k_h0_gradient<<<(unsigned)((npair + bs - 1) / bs), bs, 0, s>>>(m, p, se, P, W, vao, vdp, vqp,
                                                                    grad, sigma, dEdcn, npair);
+  ++g_kernel_launches;
   k_h0_onsite_dcn<<<(m.nat + 127) / 128, 128, 0, s>>>(m, P, dEdcn);
 }
 

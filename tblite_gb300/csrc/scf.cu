@@ -21,6 +21,8 @@
 
 namespace tb {
 
+unsigned long long g_kernel_launches = 0;
+
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -66,6 +68,7 @@ void launch_cn(const DevMol& m, const Gfn2Scalars& p, double* cn, cudaStream_t s
     cudaMemsetAsync(cn, 0, sizeof(double), s);
     return;
   }
+  ++g_kernel_launches;
   k_cn<<<(m.nat * 32 + 255) / 256, 256, 0, s>>>(m, p, cn);
 }
 
@@ -106,6 +109,7 @@ __global__ void k_cn_grad(DevMol m, Gfn2Scalars p, const double* __restrict__ dE
 void launch_cn_grad(const DevMol& m, const Gfn2Scalars& p, const double* dEdcn, double* grad,
                     double* sig_at, cudaStream_t s) {
   if (m.nat == 1) return;
+  ++g_kernel_launches;
   k_cn_grad<<<(m.nat * 32 + 255) / 256, 256, 0, s>>>(m, p, dEdcn, grad, sig_at);
 }
 
@@ -128,6 +132,7 @@ __global__ void k_levels(DevMol m, Gfn2Scalars p, const double* __restrict__ cn,
 void launch_setup_levels(const DevMol& m, const Gfn2Scalars& p, const double* cn, double* se,
                          double* mrad, double* dmrdcn, cudaStream_t s) {
   const int nt = m.nsh > m.nat ? m.nsh : m.nat;
+  ++g_kernel_launches;
   k_levels<<<(nt + 127) / 128, 128, 0, s>>>(m, p, cn, se, mrad, dmrdcn);
 }
 
@@ -246,6 +251,7 @@ void launch_coulomb_potential(const DevMol& m, const Gfn2Scalars& p, const doubl
                               const double* qsh, const double* qat, const double* dpat,
                               const double* qpat, double* vsh, double* vat, double* vdp,
                               double* vqp, cudaStream_t s) {
+  ++g_kernel_launches;
   k_coulomb<0><<<(m.nat * 32 + 255) / 256, 256, 0, s>>>(m, p, mrad, qsh, qat, dpat, qpat, vsh, vat,
                                                          vdp, vqp, nullptr);
 }
@@ -253,6 +259,7 @@ void launch_coulomb_potential(const DevMol& m, const Gfn2Scalars& p, const doubl
 void launch_coulomb_energy(const DevMol& m, const Gfn2Scalars& p, const double* mrad,
                            const double* qsh, const double* qat, const double* dpat,
                            const double* qpat, double* eat, cudaStream_t s) {
+  ++g_kernel_launches;
   k_coulomb<1><<<(m.nat * 32 + 255) / 256, 256, 0, s>>>(m, p, mrad, qsh, qat, dpat, qpat, nullptr,
                                                          nullptr, nullptr, nullptr, eat);
 }
@@ -352,6 +359,7 @@ void launch_coulomb_gradient(const DevMol& m, const Gfn2Scalars& p, const double
                              const double* dpat, const double* qpat, double* grad, double* sig_at,
                              double* dEdcn, cudaStream_t s) {
   if (m.nat == 1) return;
+  ++g_kernel_launches;
   k_coulomb_grad<<<(m.nat * 32 + 255) / 256, 256, 0, s>>>(m, p, mrad, dmrdcn, qsh, qat, dpat, qpat,
                                                           grad, sig_at, dEdcn);
 }
@@ -398,6 +406,7 @@ __global__ void k_repulsion(DevMol m, Gfn2Scalars p, double* erep, double* grad,
 
 void launch_repulsion(const DevMol& m, const Gfn2Scalars& p, double* erep, double* grad,
                       double* sig_at, cudaStream_t s) {
+  ++g_kernel_launches;
   k_repulsion<<<(m.nat * 32 + 255) / 256, 256, 0, s>>>(m, p, erep, grad, sig_at);
 }
 
@@ -412,6 +421,7 @@ __global__ void k_vao(DevMol m, const double* vsh, const double* vat, double* va
 
 void launch_vao(const DevMol& m, const double* vsh, const double* vat, double* vao,
                 cudaStream_t s) {
+  ++g_kernel_launches;
   k_vao<<<(m.nao + 255) / 256, 256, 0, s>>>(m, vsh, vat, vao);
 }
 
@@ -498,6 +508,7 @@ void launch_fock(int n, const int* ao_at, const double* H, const double* S, cons
                  const double* Q, const double* vao, const double* vdp, const double* vqp, double* F,
                  cudaStream_t s) {
   const int nt = (n + 31) / 32;
+  ++g_kernel_launches;
   k_fock<<<dim3(nt, nt), dim3(32, 8), 0, s>>>(n, ao_at, H, S, D, Q, vao, vdp, vqp, F);
 }
 
@@ -571,7 +582,9 @@ void launch_mulliken(const DevMol& m, const double* P, const double* S, const do
                      const double* D, const double* Q, double* partial, int nchunk, double* qsh,
                      double* qat, double* dpat, double* qpat, double* eband, cudaStream_t s) {
   const int n = m.nao;
+  ++g_kernel_launches;
   k_mull_partial<<<dim3((n + 127) / 128, nchunk), 128, 0, s>>>(n, P, S, H, D, Q, partial);
+  ++g_kernel_launches;
   k_mull_reduce<<<(m.nat + 127) / 128, 128, 0, s>>>(m, partial, nchunk, qsh, qat, dpat, qpat,
                                                     eband);
 }
@@ -667,6 +680,7 @@ __global__ void k_fermi(int n, const double* emo, double nalp, double nbet, doub
 void launch_fermi(int n, const double* emo, double nalp, double nbet, double kt, double* focc,
                   double* ts, int* ncols, cudaStream_t s) {
   // fa, fb scratch follow focc in memory: focc[n], fa[n], fb[n]
+  ++g_kernel_launches;
   k_fermi<<<1, 1024, 0, s>>>(n, emo, nalp, nbet, kt, focc + n, focc + 2 * n, focc, ts, ncols);
 }
 
@@ -686,6 +700,7 @@ __global__ void k_pack(int nsh, int nat, const double* qsh, const double* dpat, 
 void launch_pack(const DevMol& m, const double* qsh, const double* dpat, const double* qpat,
                  double* vec, cudaStream_t s) {
   const int nd = m.nsh + 9 * m.nat;
+  ++g_kernel_launches;
   k_pack<<<(nd + 255) / 256, 256, 0, s>>>(m.nsh, m.nat, qsh, dpat, qpat, vec);
 }
 
@@ -706,6 +721,7 @@ __global__ void k_unpack(DevMol m, const double* vec, double* qsh, double* qat, 
 void launch_unpack(const DevMol& m, const double* vec, double* qsh, double* qat, double* dpat,
                    double* qpat, cudaStream_t s) {
   const int nt = m.nsh > 6 * m.nat ? m.nsh : 6 * m.nat;
+  ++g_kernel_launches;
   k_unpack<<<(nt + 255) / 256, 256, 0, s>>>(m, vec, qsh, qat, dpat, qpat);
 }
 
@@ -723,6 +739,7 @@ __global__ void k_diff(int nd, const double* vout, const double* q, double* dq, 
 
 void launch_diff(int nd, const double* vout, const double* q, double* dq, double* err,
                  cudaStream_t s) {
+  ++g_kernel_launches;
   k_diff<<<1, 1024, 0, s>>>(nd, vout, q, dq, err);
 }
 
@@ -882,6 +899,7 @@ __global__ void k_eelec_init(int nat, const double* ts, const double* eband, dou
 
 void launch_eelec_init(int nat, const double* ts, const double* eband, double* eelec,
                        cudaStream_t s) {
+  ++g_kernel_launches;
   k_eelec_init<<<(nat + 127) / 128, 128, 0, s>>>(nat, ts, eband, eelec);
 }
 
@@ -891,11 +909,13 @@ __global__ void k_fe(int n, const double* f, const double* e, double* out) {
 }
 
 void launch_fe(int n, const double* f, const double* e, double* out, cudaStream_t s) {
+  ++g_kernel_launches;
   k_fe<<<(n + 255) / 256, 256, 0, s>>>(n, f, e, out);
 }
 
 void launch_broyden_next(BroydenState& b, cudaStream_t s) {
   b.iter += 1;
+  ++g_kernel_launches;
   k_broyden<<<1, 1024, 0, s>>>(b.ndim, b.memory, b.iter, b.damp, b.q, b.qlast, b.dq, b.dqlast,
                                b.df, b.u, b.a, b.omega, b.work, b.status);
 }

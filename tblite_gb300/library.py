@@ -72,6 +72,10 @@ _SIGNATURES = {
     "tblite_get_calculator_orbital_count": (None, [c_void_p, c_void_p, _int_p]),
     "tblite_get_calculator_orbital_map": (None, [c_void_p, c_void_p, _int_p]),
     "tblite_get_singlepoint": (None, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    # extensions (include/tblite_gb300_ext.h)
+    "tblite_gb300_set_profiling": (None, [c_int]),
+    "tblite_gb300_get_profile": (c_int, [_dbl_p, _int_p, c_int, _dbl_p, _int_p]),
+    "tblite_gb300_get_launch_count": (ctypes.c_ulonglong, []),
 }
 for _name in ("number_of_atoms", "number_of_shells", "number_of_orbitals", "number_of_spins"):
     _SIGNATURES[f"tblite_get_result_{_name}"] = (None, [c_void_p, c_void_p, _int_p])
@@ -96,6 +100,30 @@ def load():
             fn.argtypes = args
         _LIB = lib
     return _LIB
+
+
+PHASES = ("setup", "potential", "fock", "eigensolve", "density", "mulliken", "mixer",
+          "gradient", "transfer")
+
+
+def set_profiling(enable: bool) -> None:
+    load().tblite_gb300_set_profiling(int(bool(enable)))
+
+
+def get_profile():
+    """Per-phase device times (ms) of the last single point, from CUDA events."""
+    lib = load()
+    ms = np.zeros(len(PHASES))
+    cnt = np.zeros(len(PHASES), dtype=np.int32)
+    tot = c_double(0.0)
+    it = c_int(0)
+    lib.tblite_gb300_get_profile(_dp(ms), _ip(cnt), len(PHASES), byref(tot), byref(it))
+    return {"phase_ms": dict(zip(PHASES, ms.tolist())), "phase_count": dict(zip(PHASES, cnt.tolist())),
+            "total_ms": tot.value, "iterations": it.value}
+
+
+def launch_count() -> int:
+    return int(load().tblite_gb300_get_launch_count())
 
 
 def exported_symbols():

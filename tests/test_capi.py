@@ -19,7 +19,7 @@ def lib():
 
 
 def test_header_symbols_exported(lib):
-    header = (ROOT / "include" / "tblite.h").read_text()
+    header = "".join(p.read_text() for p in sorted((ROOT / "include").glob("*.h")))
     names = sorted(set(re.findall(r"\b(tblite_[a-z0-9_]+)\s*\(", header)))
     assert len(names) > 50
     missing = [n for n in names if not hasattr(lib, n)]
