@@ -105,7 +105,7 @@ def _cpu_baseline(numbers, positions, sample_evals=1):
     threads = os.cpu_count() or 1
     for var in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS"):
         os.environ.setdefault(var, str(threads))
-    calc = gfn2.new_calc(gfn2.Molecule(numbers, positions), include_dispersion=False)
+    calc = gfn2.new_calc(gfn2.Molecule(numbers, positions))
     gfn2.lib()
     t0 = time.perf_counter()
     for _ in range(sample_evals):
@@ -230,7 +230,7 @@ def run_reference(args):
     threads = os.cpu_count() or 1
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        calc = gfn2.new_calc(gfn2.Molecule(numbers, positions), include_dispersion=False)
+        calc = gfn2.new_calc(gfn2.Molecule(numbers, positions))
         gfn2.singlepoint(calc, grad=True)
     dt = time.perf_counter() - t0
     value = args.steps / dt

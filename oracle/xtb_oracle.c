@@ -749,3 +749,188 @@ void orc_repulsion(int nat, const double *xyz, const int *num, const double *alp
             }
         }
 }
+
+/* ------------------------------------------------------------------ */
+/* D4 dispersion.  The model is part of dftd4 (not in the reference tree); the
+ * reference calls it from src/tblite/disp/d4.f90:105-474.  Restated from the
+ * published D4 model: EN-weighted error-function coordination number,
+ * Gaussian reference weights with charge scaling, rational (BJ) damping for the
+ * two-body term, Axilrod-Teller-Muto three-body term with the same radii.
+ * c6ref[ia][r][ib][s] is a table over the atoms' species (nsp species, MREF refs). */
+/* ------------------------------------------------------------------ */
+#define MREF 7
+
+void orc_d4_cn(int nat, const double *xyz, const double *rcov, const double *en, double kn,
+               double k4, double k5, double k6, double cutoff, const double *dEdcn, double *cn,
+               double *gradient, double *sigma) {
+    const double cut2 = cutoff * cutoff;
+    if (cn) memset(cn, 0, nat * sizeof(double));
+    for (int i = 0; i < nat; ++i)
+        for (int j = 0; j < i; ++j) {
+            double v[3], r2 = 0;
+            for (int k = 0; k < 3; ++k) { v[k] = xyz[3 * i + k] - xyz[3 * j + k]; r2 += v[k] * v[k]; }
+            if (r2 > cut2 || r2 < 1e-12) continue;
+            const double r = sqrt(r2), rc = rcov[i] + rcov[j];
+            const double den = k4 * exp(-pow(fabs(en[i] - en[j]) + k5, 2) / k6);
+            const double arg = -kn * (r - rc) / rc;
+            if (cn) {
+                const double c = den * 0.5 * (1.0 + erf(arg));
+                cn[i] += c;
+                cn[j] += c;
+            }
+            if (gradient) {
+                const double dc = -den * kn / rc * exp(-arg * arg) / sqrt(M_PI);
+                const double f = (dEdcn[i] + dEdcn[j]) * dc / r;
+                for (int k = 0; k < 3; ++k) {
+                    gradient[3 * i + k] += f * v[k];
+                    gradient[3 * j + k] -= f * v[k];
+                }
+                for (int a = 0; a < 3; ++a)
+                    for (int b = 0; b < 3; ++b) sigma[3 * a + b] += f * v[a] * v[b];
+            }
+        }
+}
+
+static double d4_pair_de(double r2, double rrij, double r0, double s6, double s8, double *ddedr) {
+    const double r6 = r2 * r2 * r2, r8 = r6 * r2, r0_6 = pow(r0, 6), r0_8 = pow(r0, 8);
+    const double t6 = 1.0 / (r6 + r0_6), t8 = 1.0 / (r8 + r0_8);
+    if (ddedr) {
+        const double r = sqrt(r2);
+        *ddedr = s6 * 6.0 * r6 / r * t6 * t6 + s8 * rrij * 8.0 * r8 / r * t8 * t8;
+    }
+    return -(s6 * t6 + s8 * rrij * t8);
+}
+
+/* Two-body term with atom-wise weights gw[nat][MREF].
+ * mode 0: u[nat][MREF] = sum_B dE_AB sum_s c6ref(rA,sB) gw_sB   (for potential / energy)
+ * mode 1: gradient at fixed weights + dEdcn via dgwdcn (dE/dgw chain) */
+void orc_d4_twobody(int nat, const double *xyz, const int *sp, int nsp, const double *c6ref,
+                    const double *r4r2, double a1, double a2, double s6, double s8, double cutoff,
+                    const double *gw, const double *dgwdcn, int mode, double *u, double *gradient,
+                    double *sigma, double *dEdcn) {
+    const double cut2 = cutoff * cutoff;
+    const int ld = nsp * MREF;
+    if (mode == 0) memset(u, 0, (size_t)nat * MREF * sizeof(double));
+    for (int i = 0; i < nat; ++i)
+        for (int j = 0; j < nat; ++j) {
+            if (i == j) continue;
+            double v[3], r2 = 0;
+            for (int k = 0; k < 3; ++k) { v[k] = xyz[3 * i + k] - xyz[3 * j + k]; r2 += v[k] * v[k]; }
+            if (r2 > cut2 || r2 < 1e-12) continue;
+            const double rrij = 3.0 * r4r2[i] * r4r2[j];
+            const double r0 = a1 * sqrt(rrij) + a2;
+            double dd;
+            const double de = d4_pair_de(r2, rrij, r0, s6, s8, &dd);
+            const double *tab = c6ref + (size_t)sp[i] * MREF * ld + sp[j] * MREF;
+            if (mode == 0) {
+                for (int r = 0; r < MREF; ++r) {
+                    double acc = 0.0;
+                    for (int s = 0; s < MREF; ++s) acc += tab[(size_t)r * ld + s] * gw[j * MREF + s];
+                    u[i * MREF + r] += de * acc;
+                }
+            } else if (j < i) {
+                double c6 = 0.0, dc6i = 0.0, dc6j = 0.0;
+                for (int r = 0; r < MREF; ++r)
+                    for (int s = 0; s < MREF; ++s) {
+                        const double t = tab[(size_t)r * ld + s];
+                        c6 += gw[i * MREF + r] * gw[j * MREF + s] * t;
+                        dc6i += dgwdcn[i * MREF + r] * gw[j * MREF + s] * t;
+                        dc6j += gw[i * MREF + r] * dgwdcn[j * MREF + s] * t;
+                    }
+                dEdcn[i] += de * dc6i;
+                dEdcn[j] += de * dc6j;
+                const double f = dd * c6 / sqrt(r2);  /* d(de c6)/dR_i = dd c6 v/r */
+                for (int k = 0; k < 3; ++k) {
+                    gradient[3 * i + k] += f * v[k];
+                    gradient[3 * j + k] -= f * v[k];
+                }
+                for (int a = 0; a < 3; ++a)
+                    for (int b = 0; b < 3; ++b) sigma[3 * a + b] += f * v[a] * v[b];
+            }
+        }
+}
+
+/* Three-body ATM term at fixed atomic C6 (c6[nat][nat]); energies split in thirds.
+ * dEdc6[nat][nat] accumulates dE/dC6_ij (symmetric use) for the CN chain rule. */
+void orc_d4_atm(int nat, const double *xyz, const double *c6, const double *r4r2, double a1,
+                double a2, double s9, double alp, double cutoff, double *energies, double *dEdc6,
+                double *gradient, double *sigma) {
+    const double cut2 = cutoff * cutoff;
+    for (int i = 0; i < nat; ++i)
+        for (int j = 0; j < i; ++j) {
+            double vij[3], r2ij = 0;
+            for (int k = 0; k < 3; ++k) { vij[k] = xyz[3 * j + k] - xyz[3 * i + k]; r2ij += vij[k] * vij[k]; }
+            if (r2ij > cut2 || r2ij < 1e-12) continue;
+            const double r0ij = a1 * sqrt(3.0 * r4r2[i] * r4r2[j]) + a2;
+            for (int l = 0; l < j; ++l) {
+                double vik[3], vjk[3], r2ik = 0, r2jk = 0;
+                for (int k = 0; k < 3; ++k) {
+                    vik[k] = xyz[3 * l + k] - xyz[3 * i + k];
+                    vjk[k] = xyz[3 * l + k] - xyz[3 * j + k];
+                    r2ik += vik[k] * vik[k];
+                    r2jk += vjk[k] * vjk[k];
+                }
+                if (r2ik > cut2 || r2jk > cut2 || r2ik < 1e-12 || r2jk < 1e-12) continue;
+                const double r0ik = a1 * sqrt(3.0 * r4r2[i] * r4r2[l]) + a2;
+                const double r0jk = a1 * sqrt(3.0 * r4r2[j] * r4r2[l]) + a2;
+                const double c6ij = c6[i * nat + j], c6ik = c6[i * nat + l], c6jk = c6[j * nat + l];
+                const double c9 = -s9 * sqrt(fabs(c6ij * c6ik * c6jk));
+                const double r0 = r0ij * r0ik * r0jk;
+                const double r2 = r2ij * r2ik * r2jk, r1 = sqrt(r2), r3 = r2 * r1, r5 = r3 * r2;
+                const double fdmp = 1.0 / (1.0 + 6.0 * pow(r0 / r1, alp / 3.0));
+                const double ang = 0.375 * (r2ij + r2jk - r2ik) * (r2ij - r2jk + r2ik)
+                                       * (-r2ij + r2jk + r2ik) / r5 + 1.0 / r3;
+                const double rr = ang * fdmp;
+                const double dE = rr * c9;
+                energies[i] += dE / 3.0;
+                energies[j] += dE / 3.0;
+                energies[l] += dE / 3.0;
+                /* derivatives w.r.t. the three squared distances (x = r2ij etc.) */
+                const double dfdmp = -2.0 * alp * pow(r0 / r1, alp / 3.0) * fdmp * fdmp;
+                /* d ang / d r2ij (chain through the product terms), as in the published form */
+                double dang[3];
+                {
+                    const double a = r2ij, b = r2jk, c = r2ik;
+                    const double P = (a + b - c) * (a - b + c) * (-a + b + c);
+                    const double dPa = (a - b + c) * (-a + b + c) + (a + b - c) * (-a + b + c)
+                                       - (a + b - c) * (a - b + c);
+                    const double dPb = (a - b + c) * (-a + b + c) - (a + b - c) * (-a + b + c)
+                                       + (a + b - c) * (a - b + c);
+                    const double dPc = -(a - b + c) * (-a + b + c) + (a + b - c) * (-a + b + c)
+                                       + (a + b - c) * (a - b + c);
+                    /* r5 = (abc)^(5/2), r3 = (abc)^(3/2) */
+                    dang[0] = 0.375 * (dPa / r5 - 2.5 * P / (r5 * a)) - 1.5 / (r3 * a);
+                    dang[1] = 0.375 * (dPb / r5 - 2.5 * P / (r5 * b)) - 1.5 / (r3 * b);
+                    dang[2] = 0.375 * (dPc / r5 - 2.5 * P / (r5 * c)) - 1.5 / (r3 * c);
+                }
+                /* d fdmp / d r2x = dfdmp/6 * (-1/(2 r2x)) ... fdmp depends on r1 = sqrt(abc) */
+                const double dfd[3] = {dfdmp / 6.0 * (-0.5 / r2ij) * -1.0, 0, 0};
+                (void)dfd;
+                /* fdmp = 1/(1+6 t), t = (r0/r1)^(alp/3); dt/d r2x = -(alp/6) t / r2x */
+                const double t = pow(r0 / r1, alp / 3.0);
+                const double dfdt = -6.0 * fdmp * fdmp;
+                const double dx[3] = {r2ij, r2jk, r2ik};
+                double dEd[3];
+                for (int q = 0; q < 3; ++q) {
+                    const double dtdx = -(alp / 6.0) * t / dx[q];
+                    dEd[q] = c9 * (dang[q] * fdmp + ang * dfdt * dtdx);
+                }
+                /* gradient: d r2ij / dR_i = -2 vij (vij = R_j - R_i) */
+                for (int k = 0; k < 3; ++k) {
+                    const double gij = 2.0 * dEd[0] * vij[k], gjk = 2.0 * dEd[1] * vjk[k],
+                                 gik = 2.0 * dEd[2] * vik[k];
+                    gradient[3 * i + k] += -gij - gik;
+                    gradient[3 * j + k] += gij - gjk;
+                    gradient[3 * l + k] += gjk + gik;
+                }
+                for (int a = 0; a < 3; ++a)
+                    for (int b = 0; b < 3; ++b)
+                        sigma[3 * a + b] += 2.0 * (dEd[0] * vij[a] * vij[b] + dEd[1] * vjk[a] * vjk[b]
+                                                   + dEd[2] * vik[a] * vik[b]);
+                /* dE/dc6: c9 = -s9 sqrt(c6ij c6ik c6jk) -> dc9/dc6ij = c9 / (2 c6ij) */
+                dEdc6[i * nat + j] += rr * c9 / (2.0 * c6ij);
+                dEdc6[i * nat + l] += rr * c9 / (2.0 * c6ik);
+                dEdc6[j * nat + l] += rr * c9 / (2.0 * c6jk);
+            }
+        }
+}

@@ -108,6 +108,10 @@ struct Workspace {
   DBuf<int> b_status;
   // gradient
   DBuf<double> grad, sigma, sig_at, dEdcn;
+  // D4 dispersion
+  DBuf<int> d4_sp, d4_nref, d4_ngw;
+  DBuf<double> d4_refcn, d4_refq, d4_zeff, d4_gam, d4_r4r2, d4_rcov, d4_en, d4_c6ref;
+  DBuf<double> d4_cn, d4_gw, d4_dgw, d4_gwv, d4_dgwdq, d4_dgwv_cn, d4_c6, d4_dc6, d4_e3, d4_dEdcn;
   EigenSolver* eig = nullptr;
   ~Workspace() {
     if (eig) eigen_destroy(eig);
@@ -119,6 +123,11 @@ struct _tblite_calculator {
   // molecule-bound basis (built at construction)
   int nat = 0, nsh = 0, nao = 0;
   std::vector<int> at_z, at_sh, sh_atom, sh_l, sh_nprim, sh_ao, ao_sh, ao_at;
+  // D4 data per atom (empty for a single atom: no pairs, no dispersion)
+  bool has_d4 = false;
+  int d4_nsp = 0;
+  std::vector<int> d4_sp, d4_nref, d4_ngw;
+  std::vector<double> d4_refcn, d4_refq, d4_zeff, d4_gam, d4_r4r2, d4_rcov, d4_en, d4_c6ref;
   std::vector<double> sh_alpha, sh_coeff, sh_se0, sh_kcn, sh_shpoly, sh_zeta, sh_hub, sh_gam3,
       sh_refocc, at_en, at_rad, at_rcov, at_mprad, at_vcn, at_dkern, at_qkern, at_repa, at_repz;
   double min_alpha = 1e300;
@@ -239,6 +248,42 @@ static void build_calculator(_tblite_calculator* c, const _tblite_structure* mol
     c->at_repa.push_back(GFN2_REP_ALPHA[z - 1]);
     c->at_repz.push_back(GFN2_REP_ZEFF[z - 1]);
   }
+  // D4 model data (element-data pack), only for molecules with pairs
+  if (mol->nat > 1) {
+    std::vector<int> species;
+    for (int z : mol->num)
+      if (std::find(species.begin(), species.end(), z) == species.end()) species.push_back(z);
+    c->has_d4 = true;
+    c->d4_nsp = (int)species.size();
+    for (int z : species)
+      if (EXT_D4_NREF[z - 1] <= 0 || std::isnan(EXT_D4_ZEFF[z - 1]))
+        throw std::runtime_error(std::string("element data pack '") + EXT_PACK_NAME +
+                                 "' has no D4 data for Z=" + std::to_string(z));
+    for (int i = 0; i < mol->nat; ++i) {
+      const int z = mol->num[i];
+      c->d4_sp.push_back((int)(std::find(species.begin(), species.end(), z) - species.begin()));
+      c->d4_nref.push_back(EXT_D4_NREF[z - 1]);
+      for (int r = 0; r < D4_MREF; ++r) {
+        c->d4_ngw.push_back(EXT_D4_NGW[(z - 1) * D4_MREF + r]);
+        c->d4_refcn.push_back(EXT_D4_REFCN[(z - 1) * D4_MREF + r]);
+        c->d4_refq.push_back(EXT_D4_REFQ[(z - 1) * D4_MREF + r]);
+      }
+      c->d4_zeff.push_back(EXT_D4_ZEFF[z - 1]);
+      c->d4_gam.push_back(EXT_D4_GAM[z - 1]);
+      c->d4_r4r2.push_back(EXT_D4_R4R2[z - 1]);
+      c->d4_rcov.push_back(EXT_D4_RCOV[z - 1]);
+      c->d4_en.push_back(EXT_D4_EN[z - 1]);
+    }
+    const int nsp = c->d4_nsp, ld = nsp * D4_MREF;
+    c->d4_c6ref.assign((size_t)ld * ld, 0.0);
+    for (int a = 0; a < nsp; ++a)
+      for (int r = 0; r < EXT_D4_NREF[species[a] - 1]; ++r)
+        for (int b = 0; b < nsp; ++b)
+          for (int q = 0; q < EXT_D4_NREF[species[b] - 1]; ++q)
+            c->d4_c6ref[(size_t)(a * D4_MREF + r) * ld + b * D4_MREF + q] =
+                sqrt(EXT_D4_REFC6[(species[a] - 1) * D4_MREF + r] *
+                     EXT_D4_REFC6[(species[b] - 1) * D4_MREF + q]);
+  }
 }
 
 static Gfn2Scalars gfn2_scalars(const _tblite_calculator* c) {
@@ -297,6 +342,24 @@ static void ensure_workspace(_tblite_calculator* c) {
     w.at_qkern.upload(c->at_qkern, s);
     w.at_repa.upload(c->at_repa, s);
     w.at_repz.upload(c->at_repz, s);
+    if (c->has_d4) {
+      w.d4_sp.upload(c->d4_sp, s);
+      w.d4_nref.upload(c->d4_nref, s);
+      w.d4_ngw.upload(c->d4_ngw, s);
+      w.d4_refcn.upload(c->d4_refcn, s);
+      w.d4_refq.upload(c->d4_refq, s);
+      w.d4_zeff.upload(c->d4_zeff, s);
+      w.d4_gam.upload(c->d4_gam, s);
+      w.d4_r4r2.upload(c->d4_r4r2, s);
+      w.d4_rcov.upload(c->d4_rcov, s);
+      w.d4_en.upload(c->d4_en, s);
+      w.d4_c6ref.upload(c->d4_c6ref, s);
+      const size_t na = c->nat, nr = na * D4_MREF;
+      for (auto* b : {&w.d4_gw, &w.d4_dgw, &w.d4_gwv, &w.d4_dgwdq, &w.d4_dgwv_cn}) b->alloc(nr);
+      for (auto* b : {&w.d4_cn, &w.d4_e3, &w.d4_dEdcn}) b->alloc(na);
+      w.d4_c6.alloc(na * na);
+      w.d4_dc6.alloc(na * na);
+    }
     w.at_z.upload(c->at_z, s);
     w.at_sh.upload(c->at_sh, s);
     w.sh_atom.upload(c->sh_atom, s);
@@ -352,6 +415,50 @@ static void ensure_workspace(_tblite_calculator* c) {
     w.b_status.alloc(1);
     w.memory = memory;
   }
+}
+
+static DevD4 dev_d4(const _tblite_calculator* c, D4Work& wk) {
+  Workspace& w = *c->ws;
+  DevD4 d{};
+  d.nsp = c->d4_nsp;
+  d.sp = w.d4_sp.p;
+  d.nref = w.d4_nref.p;
+  d.ngw = w.d4_ngw.p;
+  d.refcn = w.d4_refcn.p;
+  d.refq = w.d4_refq.p;
+  d.zeff = w.d4_zeff.p;
+  d.gam = w.d4_gam.p;
+  d.r4r2 = w.d4_r4r2.p;
+  d.rcov = w.d4_rcov.p;
+  d.en = w.d4_en.p;
+  d.c6ref = w.d4_c6ref.p;
+  d.ga = EXT_D4_GA;
+  d.gc = EXT_D4_GC;
+  d.wf = EXT_D4_WF;
+  d.kn = EXT_D4_CN_KN;
+  d.k4 = EXT_D4_CN_K4;
+  d.k5 = EXT_D4_CN_K5;
+  d.k6 = EXT_D4_CN_K6;
+  d.cn_cutoff = EXT_D4_CN_CUTOFF;
+  d.disp2_cutoff = EXT_D4_DISP2_CUTOFF;
+  d.disp3_cutoff = EXT_D4_DISP3_CUTOFF;
+  d.atm_alpha = EXT_D4_ATM_ALPHA;
+  d.s6 = GFN2_S6;
+  d.s8 = GFN2_S8;
+  d.a1 = GFN2_A1;
+  d.a2 = GFN2_A2;
+  d.s9 = GFN2_S9;
+  wk.cn = w.d4_cn.p;
+  wk.gw = w.d4_gw.p;
+  wk.dgw = w.d4_dgw.p;
+  wk.gwv = w.d4_gwv.p;
+  wk.dgwdq = w.d4_dgwdq.p;
+  wk.dgwv_cn = w.d4_dgwv_cn.p;
+  wk.c6 = w.d4_c6.p;
+  wk.dc6 = w.d4_dc6.p;
+  wk.e3 = w.d4_e3.p;
+  wk.dEdcn = w.d4_dEdcn.p;
+  return d;
 }
 
 static DevMol dev_mol(const _tblite_calculator* c) {
@@ -497,6 +604,9 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
   cuda_check(cudaMemsetAsync(w.sigma.p, 0, sizeof(double) * 9, s), "zero");
   cuda_check(cudaMemsetAsync(w.dEdcn.p, 0, sizeof(double) * nat, s), "zero");
   launch_repulsion(m, p, w.erep.p, w.grad.p, w.sig_at.p, s);
+  D4Work d4w{};
+  DevD4 d4 = c->has_d4 ? dev_d4(c, d4w) : DevD4{};
+  if (c->has_d4) d4_setup(m, d4, d4w, true, w.grad.p, w.sig_at.p, s);
   const int chol = eigen_set_overlap(w.eig, w.S.p);
   g_prof.end(s);
   if (chol != 0) throw std::runtime_error("overlap matrix is not positive definite");
@@ -556,6 +666,12 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
   }
   std::vector<double> h_erep;
   w.erep.download(h_erep, nat, s);
+  if (c->has_d4) {  // non-self-consistent energies: repulsion + three-body dispersion
+    std::vector<double> h_e3;
+    w.d4_e3.download(h_e3, nat, s);
+    cuda_check(cudaStreamSynchronize(s), "sync e3");
+    for (int i = 0; i < nat; ++i) h_erep[i] += h_e3[i];
+  }
   std::vector<int> h_cnt(1);
   double kt = target_kt;
   while (!converged && iscf < c->max_iter) {
@@ -580,6 +696,7 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
     g_prof.begin(PH_POTENTIAL, s);
     launch_coulomb_potential(m, p, w.mrad.p, w.qsh.p, w.qat.p, w.dpat.p, w.qpat.p, w.vsh.p, w.vat.p,
                              w.vdp.p, w.vqp.p, s);
+    if (c->has_d4) d4_potential(m, d4, d4w, w.qat.p, w.vat.p, s);
     launch_vao(m, w.vsh.p, w.vat.p, w.vao.p, s);
     g_prof.end(s);
     g_prof.begin(PH_FOCK, s);
@@ -606,6 +723,7 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
     launch_eelec_init(nat, w.scal.p, w.eband.p, w.eelec.p, s);
     launch_coulomb_energy(m, p, w.mrad.p, w.qsh_o.p, w.qat_o.p, w.dpat_o.p, w.qpat_o.p, w.eelec.p,
                           s);
+    if (c->has_d4) d4_energy(m, d4, d4w, w.qat_o.p, w.eelec.p, s);
     g_prof.end(s);
     w.eelec.download(h_eelec, nat, s);
     w.scal.download(h_scal, 2, s);
@@ -639,6 +757,7 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
   g_prof.begin(PH_GRADIENT, s);
   launch_coulomb_gradient(m, p, w.mrad.p, w.dmrdcn.p, w.qsh_o.p, w.qat_o.p, w.dpat_o.p, w.qpat_o.p,
                           w.grad.p, w.sig_at.p, w.dEdcn.p, s);
+  if (c->has_d4) d4_gradient(m, d4, d4w, w.qat_o.p, w.grad.p, w.sig_at.p, s);
   // W = C diag(f e) C^T  (scf/diag.f90:110-143)
   launch_fe(n, w.focc.p, w.emo.p, w.vec_out.p, s);
   density_matrix(n, h_cnt[0], w.C.p, w.vec_out.p, w.W.p, w.scratch.p, s);

@@ -1,0 +1,383 @@
+// Self-consistent D4 dispersion on the GPU (two-body, charge dependent) and the charge-free
+// Axilrod-Teller-Muto three-body term.
+//
+// The reference calls dftd4 v4.2.0 through src/tblite/disp/d4.f90:105-474 (update:
+// coordination number + dispersion matrix; get_engrad: three-body; get_energy /
+// get_potential / get_gradient: two-body).  The D4 model is restated from its published
+// form; its element data come from the element-data pack compiled into the library.
+//
+// GPU formulation: the (mref N)^2 dispersion matrix of the reference is never stored.  One
+// warp per atom walks its partners and contracts the reference C6 table with the partner's
+// weights on the fly; every per-atom kernel sums only its own atom's share of each pair or
+// triple, so all reductions are deterministic (no atomics).
+#include <cuda_runtime.h>
+
+#include "engine.h"
+
+namespace tb {
+
+__device__ __forceinline__ double wsum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// D4 coordination number, dcount/dr
+__device__ __forceinline__ void d4_count(const DevD4& d, int i, int j, double r, double& c,
+                                         double& dc) {
+  const double rc = d.rcov[i] + d.rcov[j];
+  const double den = d.k4 * exp(-(fabs(d.en[i] - d.en[j]) + d.k5) * (fabs(d.en[i] - d.en[j]) + d.k5) / d.k6);
+  const double arg = -d.kn * (r - rc) / rc;
+  c = den * 0.5 * (1.0 + erf(arg));
+  dc = -den * d.kn / rc * exp(-arg * arg) * 0.5641895835477563;  // 1/sqrt(pi)
+}
+
+__global__ void k_d4_cn(DevMol m, DevD4 d, double* cn) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= m.nat) return;
+  const int i = warp;
+  const double cut2 = d.cn_cutoff * d.cn_cutoff;
+  double acc = 0.0;
+  for (int j = lane; j < m.nat; j += 32) {
+    if (j == i) continue;
+    double r2 = 0.0;
+    for (int k = 0; k < 3; ++k) {
+      const double t = m.xyz[3 * i + k] - m.xyz[3 * j + k];
+      r2 += t * t;
+    }
+    if (r2 > cut2 || r2 < 1e-12) continue;
+    double c, dc;
+    d4_count(d, i, j, sqrt(r2), c, dc);
+    acc += c;
+  }
+  acc = wsum(acc);
+  if (lane == 0) cn[i] = acc;
+}
+
+// Gaussian reference weights in CN and their CN derivative (charge independent part)
+__global__ void k_d4_weights(int nat, DevD4 d, const double* __restrict__ cn, double* gw,
+                             double* dgw) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nat) return;
+  const int nr = d.nref[i];
+  double num[D4_MREF], dnum[D4_MREF], norm = 0.0, dnorm = 0.0;
+  for (int r = 0; r < D4_MREF; ++r) {
+    num[r] = 0.0;
+    dnum[r] = 0.0;
+    if (r >= nr) continue;
+    const double dcn = cn[i] - d.refcn[i * D4_MREF + r];
+    for (int k = 1; k <= d.ngw[i * D4_MREF + r]; ++k) {
+      const double w = exp(-d.wf * k * dcn * dcn);
+      num[r] += w;
+      dnum[r] += -2.0 * d.wf * k * dcn * w;
+    }
+    norm += num[r];
+    dnorm += dnum[r];
+  }
+  for (int r = 0; r < D4_MREF; ++r) {
+    gw[i * D4_MREF + r] = r < nr ? num[r] / norm : 0.0;
+    dgw[i * D4_MREF + r] = r < nr ? dnum[r] / norm - num[r] * dnorm / (norm * norm) : 0.0;
+  }
+}
+
+// charge scaling: gwv = gw zeta(q), dgwdq = gw dzeta/dq, dgwv_cn = dgw/dcn zeta(q)
+__global__ void k_d4_zeta(int nat, DevD4 d, const double* __restrict__ q,
+                          const double* __restrict__ gw, const double* __restrict__ dgw,
+                          double* gwv, double* dgwdq, double* dgwv_cn) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nat) return;
+  const double qi = q ? q[i] : 0.0;
+  const double z = d.zeff[i] + qi;
+  for (int r = 0; r < D4_MREF; ++r) {
+    double zeta = 0.0, dzeta = 0.0;
+    if (r < d.nref[i]) {
+      const double zr = d.zeff[i] + d.refq[i * D4_MREF + r];
+      if (z > 0.0) {
+        const double t = exp(d.gc * d.gam[i] * (1.0 - zr / z));
+        zeta = exp(d.ga * (1.0 - t));
+        dzeta = zeta * (-d.ga * t) * d.gc * d.gam[i] * zr / (z * z);
+      } else {
+        zeta = exp(d.ga);
+      }
+    }
+    const int k = i * D4_MREF + r;
+    gwv[k] = gw[k] * zeta;
+    if (dgwdq) dgwdq[k] = gw[k] * dzeta;
+    if (dgwv_cn) dgwv_cn[k] = dgw[k] * zeta;
+  }
+}
+
+__device__ __forceinline__ double d4_de(double r2, double rrij, double r0, double s6, double s8,
+                                        double& dd) {
+  const double r6 = r2 * r2 * r2, r8 = r6 * r2;
+  const double r02 = r0 * r0, r06 = r02 * r02 * r02, r08 = r06 * r02;
+  const double t6 = 1.0 / (r6 + r06), t8 = 1.0 / (r8 + r08);
+  const double r = sqrt(r2);
+  dd = s6 * 6.0 * r6 / r * t6 * t6 + s8 * rrij * 8.0 * r8 / r * t8 * t8;
+  return -(s6 * t6 + s8 * rrij * t8);
+}
+
+// MODE 0: vat += sum_r dgwdq_r u_r ; MODE 1: eat += 1/2 sum_r gwv_r u_r ;
+// MODE 2: gradient at fixed weights + dEdcn (own atom share), per-atom sigma partials
+template <int MODE>
+__global__ void k_d4_pair(DevMol m, DevD4 d, const double* __restrict__ gwv,
+                          const double* __restrict__ dgwdq, const double* __restrict__ dgwv_cn,
+                          double* vat, double* eat, double* grad, double* sig_at, double* dEdcn) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= m.nat) return;
+  const int i = warp;
+  const double cut2 = d.disp2_cutoff * d.disp2_cutoff;
+  const int ld = d.nsp * D4_MREF;
+  const double* tab_i = d.c6ref + (size_t)d.sp[i] * D4_MREF * ld;
+  double gi[D4_MREF], dci[D4_MREF];
+  for (int r = 0; r < D4_MREF; ++r) {
+    gi[r] = gwv[i * D4_MREF + r];
+    dci[r] = MODE == 2 ? dgwv_cn[i * D4_MREF + r] : 0.0;
+  }
+  double u[D4_MREF] = {0, 0, 0, 0, 0, 0, 0};
+  double g[3] = {0, 0, 0}, sg[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, dcn = 0.0;
+  for (int j = lane; j < m.nat; j += 32) {
+    if (j == i) continue;
+    double v[3], r2 = 0.0;
+    for (int k = 0; k < 3; ++k) {
+      v[k] = m.xyz[3 * i + k] - m.xyz[3 * j + k];
+      r2 += v[k] * v[k];
+    }
+    if (r2 > cut2 || r2 < 1e-12) continue;
+    const double rrij = 3.0 * d.r4r2[i] * d.r4r2[j];
+    const double r0 = d.a1 * sqrt(rrij) + d.a2;
+    double dd;
+    const double de = d4_de(r2, rrij, r0, d.s6, d.s8, dd);
+    const double* tab = tab_i + d.sp[j] * D4_MREF;
+    const double* gj = gwv + j * D4_MREF;
+    if (MODE < 2) {
+      for (int r = 0; r < D4_MREF; ++r) {
+        double acc = 0.0;
+        for (int s = 0; s < D4_MREF; ++s) acc += tab[(size_t)r * ld + s] * gj[s];
+        u[r] += de * acc;
+      }
+    } else {
+      double c6 = 0.0, dc6 = 0.0;
+      for (int r = 0; r < D4_MREF; ++r) {
+        double acc = 0.0;
+        for (int s = 0; s < D4_MREF; ++s) acc += tab[(size_t)r * ld + s] * gj[s];
+        c6 += gi[r] * acc;
+        dc6 += dci[r] * acc;
+      }
+      dcn += de * dc6;
+      const double f = dd * c6 / sqrt(r2);
+      for (int k = 0; k < 3; ++k) g[k] += f * v[k];
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) sg[3 * a + b] += 0.5 * f * v[a] * v[b];
+    }
+  }
+  if (MODE < 2) {
+    for (int r = 0; r < D4_MREF; ++r) u[r] = wsum(u[r]);
+    if (lane == 0) {
+      double acc = 0.0;
+      if (MODE == 0) {
+        for (int r = 0; r < D4_MREF; ++r) acc += dgwdq[i * D4_MREF + r] * u[r];
+        vat[i] += acc;
+      } else {
+        for (int r = 0; r < D4_MREF; ++r) acc += gi[r] * u[r];
+        eat[i] += 0.5 * acc;
+      }
+    }
+  } else {
+    for (int k = 0; k < 3; ++k) g[k] = wsum(g[k]);
+    for (int k = 0; k < 9; ++k) sg[k] = wsum(sg[k]);
+    dcn = wsum(dcn);
+    if (lane == 0) {
+      for (int k = 0; k < 3; ++k) grad[3 * i + k] += g[k];
+      for (int k = 0; k < 9; ++k) sig_at[9 * i + k] += sg[k];
+      dEdcn[i] += dcn;
+    }
+  }
+}
+
+// atomic C6 at the given weights and d c6_ij / d cn_i
+__global__ void k_d4_c6(int nat, DevD4 d, const double* __restrict__ gwv,
+                        const double* __restrict__ dgwv_cn, double* c6, double* dc6) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)nat * nat) return;
+  const int i = (int)(t / nat), j = (int)(t % nat);
+  const int ld = d.nsp * D4_MREF;
+  const double* tab = d.c6ref + (size_t)d.sp[i] * D4_MREF * ld + d.sp[j] * D4_MREF;
+  double c = 0.0, dc = 0.0;
+  for (int r = 0; r < D4_MREF; ++r) {
+    double acc = 0.0;
+    for (int s = 0; s < D4_MREF; ++s) acc += tab[(size_t)r * ld + s] * gwv[j * D4_MREF + s];
+    c += gwv[i * D4_MREF + r] * acc;
+    dc += dgwv_cn[i * D4_MREF + r] * acc;
+  }
+  c6[t] = c;
+  dc6[t] = dc;
+}
+
+// Axilrod-Teller-Muto term, one warp per atom i, triples (i, j, l) with j < l, both != i.
+// Atom i collects 1/3 of each triple energy, its own force, 1/3 of the virial and the
+// CN derivative through c6_ij and c6_il.
+__global__ void k_d4_atm(DevMol m, DevD4 d, const double* __restrict__ c6,
+                         const double* __restrict__ dc6, double* eat, double* grad, double* sig_at,
+                         double* dEdcn) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= m.nat) return;
+  const int i = warp, nat = m.nat;
+  const double cut2 = d.disp3_cutoff * d.disp3_cutoff;
+  const double alp3 = d.atm_alpha / 3.0;
+  double e = 0.0, g[3] = {0, 0, 0}, sg[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, dcn = 0.0;
+  const double* xi = m.xyz + 3 * i;
+  for (int j = lane; j < nat; j += 32) {
+    if (j == i) continue;
+    double vij[3], r2ij = 0.0;
+    for (int k = 0; k < 3; ++k) {
+      vij[k] = m.xyz[3 * j + k] - xi[k];
+      r2ij += vij[k] * vij[k];
+    }
+    if (r2ij > cut2 || r2ij < 1e-12) continue;
+    const double r0ij = d.a1 * sqrt(3.0 * d.r4r2[i] * d.r4r2[j]) + d.a2;
+    const double c6ij = c6[(size_t)i * nat + j];
+    for (int l = j + 1; l < nat; ++l) {
+      if (l == i) continue;
+      double vil[3], vjl[3], r2il = 0.0, r2jl = 0.0;
+      for (int k = 0; k < 3; ++k) {
+        vil[k] = m.xyz[3 * l + k] - xi[k];
+        vjl[k] = m.xyz[3 * l + k] - m.xyz[3 * j + k];
+        r2il += vil[k] * vil[k];
+        r2jl += vjl[k] * vjl[k];
+      }
+      if (r2il > cut2 || r2jl > cut2 || r2il < 1e-12 || r2jl < 1e-12) continue;
+      const double r0il = d.a1 * sqrt(3.0 * d.r4r2[i] * d.r4r2[l]) + d.a2;
+      const double r0jl = d.a1 * sqrt(3.0 * d.r4r2[j] * d.r4r2[l]) + d.a2;
+      const double c6il = c6[(size_t)i * nat + l], c6jl = c6[(size_t)j * nat + l];
+      const double c9 = -d.s9 * sqrt(fabs(c6ij * c6il * c6jl));
+      const double r0 = r0ij * r0il * r0jl;
+      const double r2 = r2ij * r2il * r2jl, r1 = sqrt(r2), r3 = r2 * r1, r5 = r3 * r2;
+      const double t = pow(r0 / r1, alp3);
+      const double fdmp = 1.0 / (1.0 + 6.0 * t);
+      // angular factor in the squared distances a = r2ij, b = r2jl, c = r2il
+      const double a = r2ij, b = r2jl, c = r2il;
+      const double P = (a + b - c) * (a - b + c) * (-a + b + c);
+      const double ang = 0.375 * P / r5 + 1.0 / r3;
+      const double rr = ang * fdmp;
+      e += rr * c9 / 3.0;
+      const double dPa = (a - b + c) * (-a + b + c) + (a + b - c) * (-a + b + c) - (a + b - c) * (a - b + c);
+      const double dPc = -(a - b + c) * (-a + b + c) + (a + b - c) * (-a + b + c) + (a + b - c) * (a - b + c);
+      const double dPb = (a - b + c) * (-a + b + c) - (a + b - c) * (-a + b + c) + (a + b - c) * (a - b + c);
+      const double dfdt = -6.0 * fdmp * fdmp;
+      const double dEa = c9 * ((0.375 * (dPa / r5 - 2.5 * P / (r5 * a)) - 1.5 / (r3 * a)) * fdmp
+                               + ang * dfdt * (-(d.atm_alpha / 6.0) * t / a));
+      const double dEb = c9 * ((0.375 * (dPb / r5 - 2.5 * P / (r5 * b)) - 1.5 / (r3 * b)) * fdmp
+                               + ang * dfdt * (-(d.atm_alpha / 6.0) * t / b));
+      const double dEc = c9 * ((0.375 * (dPc / r5 - 2.5 * P / (r5 * c)) - 1.5 / (r3 * c)) * fdmp
+                               + ang * dfdt * (-(d.atm_alpha / 6.0) * t / c));
+      // r2ij = |R_j - R_i|^2 -> d/dR_i = -2 vij ; r2il -> -2 vil
+      for (int k = 0; k < 3; ++k) g[k] += -2.0 * dEa * vij[k] - 2.0 * dEc * vil[k];
+      for (int p = 0; p < 3; ++p)
+        for (int q = 0; q < 3; ++q)
+          sg[3 * p + q] += 2.0 / 3.0 * (dEa * vij[p] * vij[q] + dEb * vjl[p] * vjl[q]
+                                        + dEc * vil[p] * vil[q]);
+      // dE/dc6 = rr c9 / (2 c6)
+      dcn += rr * c9 / (2.0 * c6ij) * dc6[(size_t)i * nat + j]
+             + rr * c9 / (2.0 * c6il) * dc6[(size_t)i * nat + l];
+    }
+  }
+  e = wsum(e);
+  for (int k = 0; k < 3; ++k) g[k] = wsum(g[k]);
+  for (int k = 0; k < 9; ++k) sg[k] = wsum(sg[k]);
+  dcn = wsum(dcn);
+  if (lane == 0) {
+    eat[i] = e;
+    if (grad) {
+      for (int k = 0; k < 3; ++k) grad[3 * i + k] += g[k];
+      for (int k = 0; k < 9; ++k) sig_at[9 * i + k] += sg[k];
+      dEdcn[i] += dcn;
+    }
+  }
+}
+
+__global__ void k_d4_cn_grad(DevMol m, DevD4 d, const double* __restrict__ dEdcn, double* grad,
+                             double* sig_at) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= m.nat) return;
+  const int i = warp;
+  const double cut2 = d.cn_cutoff * d.cn_cutoff;
+  double g[3] = {0, 0, 0}, sg[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  for (int j = lane; j < m.nat; j += 32) {
+    if (j == i) continue;
+    double v[3], r2 = 0.0;
+    for (int k = 0; k < 3; ++k) {
+      v[k] = m.xyz[3 * i + k] - m.xyz[3 * j + k];
+      r2 += v[k] * v[k];
+    }
+    if (r2 > cut2 || r2 < 1e-12) continue;
+    const double r = sqrt(r2);
+    double c, dc;
+    d4_count(d, i, j, r, c, dc);
+    const double f = (dEdcn[i] + dEdcn[j]) * dc / r;
+    for (int k = 0; k < 3; ++k) g[k] += f * v[k];
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) sg[3 * a + b] += 0.5 * f * v[a] * v[b];
+  }
+  for (int k = 0; k < 3; ++k) g[k] = wsum(g[k]);
+  for (int k = 0; k < 9; ++k) sg[k] = wsum(sg[k]);
+  if (lane == 0) {
+    for (int k = 0; k < 3; ++k) grad[3 * i + k] += g[k];
+    for (int k = 0; k < 9; ++k) sig_at[9 * i + k] += sg[k];
+  }
+}
+
+static inline unsigned warps_grid(int nat) { return (unsigned)((nat * 32 + 255) / 256); }
+
+void d4_setup(const DevMol& m, const DevD4& d, D4Work& w, bool grad, double* grad_out,
+              double* sig_at, cudaStream_t s) {
+  ++g_kernel_launches;
+  k_d4_cn<<<warps_grid(m.nat), 256, 0, s>>>(m, d, w.cn);
+  ++g_kernel_launches;
+  k_d4_weights<<<(m.nat + 127) / 128, 128, 0, s>>>(m.nat, d, w.cn, w.gw, w.dgw);
+  // charge-free weights for the three-body term
+  ++g_kernel_launches;
+  k_d4_zeta<<<(m.nat + 127) / 128, 128, 0, s>>>(m.nat, d, nullptr, w.gw, w.dgw, w.gwv, nullptr,
+                                                 w.dgwv_cn);
+  const long long nn = (long long)m.nat * m.nat;
+  ++g_kernel_launches;
+  k_d4_c6<<<(unsigned)((nn + 255) / 256), 256, 0, s>>>(m.nat, d, w.gwv, w.dgwv_cn, w.c6, w.dc6);
+  cudaMemsetAsync(w.dEdcn, 0, sizeof(double) * m.nat, s);
+  ++g_kernel_launches;
+  k_d4_atm<<<warps_grid(m.nat), 256, 0, s>>>(m, d, w.c6, w.dc6, w.e3, grad ? grad_out : nullptr,
+                                             sig_at, w.dEdcn);
+}
+
+void d4_potential(const DevMol& m, const DevD4& d, D4Work& w, const double* qat, double* vat,
+                  cudaStream_t s) {
+  ++g_kernel_launches;
+  k_d4_zeta<<<(m.nat + 127) / 128, 128, 0, s>>>(m.nat, d, qat, w.gw, w.dgw, w.gwv, w.dgwdq,
+                                                 nullptr);
+  ++g_kernel_launches;
+  k_d4_pair<0><<<warps_grid(m.nat), 256, 0, s>>>(m, d, w.gwv, w.dgwdq, nullptr, vat, nullptr,
+                                                 nullptr, nullptr, nullptr);
+}
+
+void d4_energy(const DevMol& m, const DevD4& d, D4Work& w, const double* qat, double* eat,
+               cudaStream_t s) {
+  ++g_kernel_launches;
+  k_d4_zeta<<<(m.nat + 127) / 128, 128, 0, s>>>(m.nat, d, qat, w.gw, w.dgw, w.gwv, nullptr,
+                                                 nullptr);
+  ++g_kernel_launches;
+  k_d4_pair<1><<<warps_grid(m.nat), 256, 0, s>>>(m, d, w.gwv, nullptr, nullptr, nullptr, eat,
+                                                 nullptr, nullptr, nullptr);
+}
+
+void d4_gradient(const DevMol& m, const DevD4& d, D4Work& w, const double* qat, double* grad,
+                 double* sig_at, cudaStream_t s) {
+  ++g_kernel_launches;
+  k_d4_zeta<<<(m.nat + 127) / 128, 128, 0, s>>>(m.nat, d, qat, w.gw, w.dgw, w.gwv, nullptr,
+                                                 w.dgwv_cn);
+  ++g_kernel_launches;
+  k_d4_pair<2><<<warps_grid(m.nat), 256, 0, s>>>(m, d, w.gwv, nullptr, w.dgwv_cn, nullptr, nullptr,
+                                                 grad, sig_at, w.dEdcn);
+  ++g_kernel_launches;
+  k_d4_cn_grad<<<warps_grid(m.nat), 256, 0, s>>>(m, d, w.dEdcn, grad, sig_at);
+}
+
+}  // namespace tb

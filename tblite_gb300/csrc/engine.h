@@ -65,6 +65,39 @@ struct Gfn2Scalars {
   double h0_cutoff;  // real-space cutoff of the integral pair list
 };
 
+// D4 dispersion data, per atom (device pointers) + model constants
+constexpr int D4_MREF = 7;
+struct DevD4 {
+  int nsp;
+  const int* sp;          // [nat] species index
+  const int* nref;        // [nat]
+  const int* ngw;         // [nat][MREF]
+  const double* refcn;    // [nat][MREF]
+  const double* refq;     // [nat][MREF]
+  const double* zeff;     // [nat]
+  const double* gam;      // [nat]
+  const double* r4r2;     // [nat]
+  const double* rcov;     // [nat]
+  const double* en;       // [nat]
+  const double* c6ref;    // [nsp][MREF][nsp][MREF]
+  double ga, gc, wf, kn, k4, k5, k6, cn_cutoff, disp2_cutoff, disp3_cutoff, atm_alpha;
+  double s6, s8, a1, a2, s9;
+};
+struct D4Work {  // device scratch
+  double *cn, *gw, *dgw, *gwv, *dgwdq, *dgwv_cn, *c6, *dc6, *e3, *dEdcn;
+};
+// geometry setup: CN, weights, atomic C6 at q = 0, three-body energy (e3) and, with grad,
+// its gradient and dEdcn (w.dEdcn is reset here)
+void d4_setup(const DevMol& m, const DevD4& d, D4Work& w, bool grad, double* grad_out,
+              double* sig_at, cudaStream_t s);
+void d4_potential(const DevMol& m, const DevD4& d, D4Work& w, const double* qat, double* vat,
+                  cudaStream_t s);
+void d4_energy(const DevMol& m, const DevD4& d, D4Work& w, const double* qat, double* eat,
+               cudaStream_t s);
+// two-body gradient at the final charges + the D4 CN chain rule (uses w.dEdcn from setup)
+void d4_gradient(const DevMol& m, const DevD4& d, D4Work& w, const double* qat, double* grad,
+                 double* sig_at, cudaStream_t s);
+
 // Kernel launchers (defined in the .cu files).  All run on `stream`.
 void launch_cn(const DevMol& m, const Gfn2Scalars& p, double* cn, cudaStream_t s);
 void launch_cn_grad(const DevMol& m, const Gfn2Scalars& p, const double* dEdcn, double* grad,

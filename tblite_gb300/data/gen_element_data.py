@@ -1,10 +1,15 @@
 """Compile an element-data pack (JSON) into ``../csrc/element_data.inc``.
 
 The element-data pack carries the per-element numbers that GFN2-xTB takes from
-libraries outside the reference tree (mctc-lib covalent radii, Pauling
-electronegativities, atomic radii and the coordination-number constants).
-Elements absent from the pack are stored as NaN; the library rejects molecules
-that need them with an error naming the element.
+libraries outside the reference tree: mctc-lib covalent radii, Pauling
+electronegativities, atomic radii and coordination-number constants, and the
+dftd4 model data (reference coordination numbers and charges, Gaussian weight
+counts, reference C6 values, effective charges, hardnesses, <r4>/<r2> ratios).
+Elements absent from the pack are stored as NaN (nref = 0); the library rejects
+molecules that need them with an error naming the element.
+
+Reference C6 values for a pair of references (r of element A, s of element B)
+are formed as sqrt(c6_A[r] * c6_B[s]) -- the combining rule of the pack format.
 
 Usage: ``python tblite_gb300/data/gen_element_data.py [PACK.json]``
 (default: ``element_data_synthetic.json``).
@@ -15,24 +20,29 @@ import sys
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
+MREF = 7
 
 
-def table(d):
-    out = [math.nan] * 86
+def table(d, default=math.nan):
+    out = [default] * 86
     for k, v in d.items():
         out[int(k) - 1] = float(v)
     return out
 
 
-def fmt(name, vals):
-    body = ", ".join("NAN" if math.isnan(v) else repr(v) for v in vals)
-    return f"static const double {name}[86] = {{{body}}};\n"
+def fmt(name, vals, ctype="double"):
+    if ctype == "int":
+        body = ", ".join(str(int(v)) for v in vals)
+    else:
+        body = ", ".join("NAN" if math.isnan(v) else repr(float(v)) for v in vals)
+    return f"static const {ctype} {name}[{len(vals)}] = {{{body}}};\n"
 
 
 def main():
     src = Path(sys.argv[1]) if len(sys.argv) > 1 else HERE / "element_data_synthetic.json"
     pack = json.loads(src.read_text())
     cn = pack["cn"]
+    d4 = pack["d4"]
     lines = ["// Generated by tblite_gb300/data/gen_element_data.py -- do not edit.\n",
              f"// pack: {pack['name']}\n", "#pragma once\n#include <cmath>\n",
              f'static const char* const EXT_PACK_NAME = "{pack["name"]}";\n',
@@ -41,7 +51,29 @@ def main():
              f"static const double EXT_CN_RSHIFT = {cn['rshift']!r};\n",
              f"static const double EXT_CN_CUTOFF = {cn['cutoff']!r};\n",
              fmt("EXT_RCOV", table(cn["rcov"])), fmt("EXT_EN", table(pack["pauling_en"])),
-             fmt("EXT_RAD", table(pack["atomic_rad"]))]
+             fmt("EXT_RAD", table(pack["atomic_rad"])),
+             f"static const int EXT_D4_MREF = {MREF};\n"]
+    for key in ("ga", "gc", "wf", "cn_kn", "cn_k4", "cn_k5", "cn_k6", "cn_cutoff", "disp2_cutoff",
+                "disp3_cutoff", "atm_alpha"):
+        lines.append(f"static const double EXT_D4_{key.upper()} = {float(d4[key])!r};\n")
+    nref = [0] * 86
+    refcn = [0.0] * (86 * MREF)
+    refq = [0.0] * (86 * MREF)
+    ngw = [0] * (86 * MREF)
+    refc6 = [0.0] * (86 * MREF)
+    for k, v in d4["refcn"].items():
+        z = int(k) - 1
+        nref[z] = len(v)
+        for r in range(len(v)):
+            refcn[z * MREF + r] = v[r]
+            refq[z * MREF + r] = d4["refq"][k][r]
+            ngw[z * MREF + r] = d4["ngw"][k][r]
+            refc6[z * MREF + r] = d4["refc6"][k][r]
+    lines += [fmt("EXT_D4_NREF", nref, "int"), fmt("EXT_D4_REFCN", refcn), fmt("EXT_D4_REFQ", refq),
+              fmt("EXT_D4_NGW", ngw, "int"), fmt("EXT_D4_REFC6", refc6),
+              fmt("EXT_D4_ZEFF", table(d4["zeff"])), fmt("EXT_D4_GAM", table(d4["gam"])),
+              fmt("EXT_D4_R4R2", table(d4["r4r2"])), fmt("EXT_D4_RCOV", table(d4["rcov"])),
+              fmt("EXT_D4_EN", table(d4["en"]))]
     (HERE.parent / "csrc" / "element_data.inc").write_text("".join(lines))
     print("wrote element_data.inc from", src.name)
 

@@ -36,7 +36,7 @@ def _oracle(z, x, charge=0.0, uhf=0, acc=1.0, grad=True):
     from oracle import gfn2
 
     calc = gfn2.new_calc(gfn2.Molecule(np.asarray(z), np.asarray(x), charge=charge, uhf=uhf),
-                         accuracy=acc, include_dispersion=False)
+                         accuracy=acc)
     return gfn2.singlepoint(calc, grad=grad)
 
 

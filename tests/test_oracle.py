@@ -99,7 +99,7 @@ WATER_DIMER = np.array([[0, 0, 0], [0.96, 0, 0], [-0.24, 0.93, 0], [2.9, 0.1, 0.
                         [3.5, 0.8, 0.3], [3.3, -0.7, -0.2]]) / 0.52917721092
 
 
-@pytest.mark.parametrize("dispersion", [False])
+@pytest.mark.parametrize("dispersion", [False, True])
 def test_molecular_gradient_fd(dispersion):
     """Analytic gradient vs central differences of the SCF energy (pattern of
     reference test/unit/test_gfn2_xtb.f90:365-416)."""
