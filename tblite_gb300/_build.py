@@ -18,7 +18,7 @@ OUT = PKG / "lib"
 OBJ = PKG / "_build"
 LIBNAME = "libtblite_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-UNITS = ["integrals.cu", "scf.cu", "disp.cu", "eigen.cu", "capi.cpp"]
+UNITS = ["integrals.cu", "scf.cu", "disp.cu", "linalg.cu", "eigen.cu", "capi.cpp"]
 HEADERS = ["engine.h", "params_gfn2.inc", "element_data.inc"]
 
 
@@ -62,7 +62,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     if force or not lib.exists() or lib.stat().st_mtime < newest:
         tmp = OUT / f".{LIBNAME}.{os.getpid()}"
         cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *[str(o) for _, o, _ in jobs],
-               "-lcusolver", "-lcublas", "-lcudart"]
+               "-lcudart"]
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")

@@ -704,15 +704,16 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
     launch_pack(m, w.qsh.p, w.dpat.p, w.qpat.p, w.b_q.p, s);  // mixer%set
     g_prof.end(s);
     g_prof.begin(PH_EIGEN, s);
-    const int info = eigen_solve(w.eig, w.F.p, w.C.p, w.emo.p);
-    g_prof.end(s);
+    const int info = eigen_values(w.eig, w.F.p, w.emo.p);
     if (info != 0)
       throw std::runtime_error("(sygvd) failed to solve eigenvalue problem. info=" +
                                std::to_string(info));
-    g_prof.begin(PH_DENSITY, s);
     launch_fermi(n, w.emo.p, nalp, nbet, kt, w.focc.p, w.scal.p, w.icount.p, s);
     w.icount.download(h_cnt, 1, s);
     cuda_check(cudaStreamSynchronize(s), "sync");
+    eigen_vectors(w.eig, h_cnt[0], w.C.p);
+    g_prof.end(s);
+    g_prof.begin(PH_DENSITY, s);
     density_matrix(n, h_cnt[0], w.C.p, w.focc.p, w.P.p, w.scratch.p, s);
     g_prof.end(s);
     g_prof.begin(PH_MULLIKEN, s);

@@ -327,12 +327,12 @@ __global__ void k_d4_cn_grad(DevMol m, DevD4 d, const double* __restrict__ dEdcn
   }
 }
 
-static inline unsigned warps_grid(int nat) { return (unsigned)((nat * 32 + 255) / 256); }
+static inline unsigned warps_grid(int nat) { return (unsigned)((nat * 32 + 63) / 64); }
 
 void d4_setup(const DevMol& m, const DevD4& d, D4Work& w, bool grad, double* grad_out,
               double* sig_at, cudaStream_t s) {
   ++g_kernel_launches;
-  k_d4_cn<<<warps_grid(m.nat), 256, 0, s>>>(m, d, w.cn);
+  k_d4_cn<<<warps_grid(m.nat), 64, 0, s>>>(m, d, w.cn);
   ++g_kernel_launches;
   k_d4_weights<<<(m.nat + 127) / 128, 128, 0, s>>>(m.nat, d, w.cn, w.gw, w.dgw);
   // charge-free weights for the three-body term
@@ -344,7 +344,7 @@ void d4_setup(const DevMol& m, const DevD4& d, D4Work& w, bool grad, double* gra
   k_d4_c6<<<(unsigned)((nn + 255) / 256), 256, 0, s>>>(m.nat, d, w.gwv, w.dgwv_cn, w.c6, w.dc6);
   cudaMemsetAsync(w.dEdcn, 0, sizeof(double) * m.nat, s);
   ++g_kernel_launches;
-  k_d4_atm<<<warps_grid(m.nat), 256, 0, s>>>(m, d, w.c6, w.dc6, w.e3, grad ? grad_out : nullptr,
+  k_d4_atm<<<warps_grid(m.nat), 64, 0, s>>>(m, d, w.c6, w.dc6, w.e3, grad ? grad_out : nullptr,
                                              sig_at, w.dEdcn);
 }
 
@@ -354,7 +354,7 @@ void d4_potential(const DevMol& m, const DevD4& d, D4Work& w, const double* qat,
   k_d4_zeta<<<(m.nat + 127) / 128, 128, 0, s>>>(m.nat, d, qat, w.gw, w.dgw, w.gwv, w.dgwdq,
                                                  nullptr);
   ++g_kernel_launches;
-  k_d4_pair<0><<<warps_grid(m.nat), 256, 0, s>>>(m, d, w.gwv, w.dgwdq, nullptr, vat, nullptr,
+  k_d4_pair<0><<<warps_grid(m.nat), 64, 0, s>>>(m, d, w.gwv, w.dgwdq, nullptr, vat, nullptr,
                                                  nullptr, nullptr, nullptr);
 }
 
@@ -364,7 +364,7 @@ void d4_energy(const DevMol& m, const DevD4& d, D4Work& w, const double* qat, do
   k_d4_zeta<<<(m.nat + 127) / 128, 128, 0, s>>>(m.nat, d, qat, w.gw, w.dgw, w.gwv, nullptr,
                                                  nullptr);
   ++g_kernel_launches;
-  k_d4_pair<1><<<warps_grid(m.nat), 256, 0, s>>>(m, d, w.gwv, nullptr, nullptr, nullptr, eat,
+  k_d4_pair<1><<<warps_grid(m.nat), 64, 0, s>>>(m, d, w.gwv, nullptr, nullptr, nullptr, eat,
                                                  nullptr, nullptr, nullptr);
 }
 
@@ -374,10 +374,10 @@ void d4_gradient(const DevMol& m, const DevD4& d, D4Work& w, const double* qat, 
   k_d4_zeta<<<(m.nat + 127) / 128, 128, 0, s>>>(m.nat, d, qat, w.gw, w.dgw, w.gwv, nullptr,
                                                  w.dgwv_cn);
   ++g_kernel_launches;
-  k_d4_pair<2><<<warps_grid(m.nat), 256, 0, s>>>(m, d, w.gwv, nullptr, w.dgwv_cn, nullptr, nullptr,
+  k_d4_pair<2><<<warps_grid(m.nat), 64, 0, s>>>(m, d, w.gwv, nullptr, w.dgwv_cn, nullptr, nullptr,
                                                  grad, sig_at, w.dEdcn);
   ++g_kernel_launches;
-  k_d4_cn_grad<<<warps_grid(m.nat), 256, 0, s>>>(m, d, w.dEdcn, grad, sig_at);
+  k_d4_cn_grad<<<warps_grid(m.nat), 64, 0, s>>>(m, d, w.dEdcn, grad, sig_at);
 }
 
 }  // namespace tb

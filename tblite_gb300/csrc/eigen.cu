@@ -1,148 +1,668 @@
-// Generalised symmetric eigenproblem  F C = S C e  (reference src/tblite/lapack/sygvd.f90:125-151,
-// LAPACK dsygvd itype 1, jobz V).
+// Generalised symmetric eigenproblem  F C = S C e  of the SCF (reference
+// src/tblite/lapack/sygvd.f90:125-151, LAPACK dsygvd itype 1, jobz V), written for GB300.
 //
-// Cholesky reduction: S = L L^T is factorised once per geometry (the reference refactorises S
-// on every SCF iteration; the factor is the same).  Per iteration
-//   A = L^-1 F L^-T  (two triangular solves),  A Y = Y e,  C = L^-T Y.
-// The triangular solves and the dense tridiagonal eigensolver run on cuBLAS / cuSOLVER;
-// the density matrix GEMM uses cuBLAS.
-#include <cublas_v2.h>
+//   once per geometry   S = L L^T (Cholesky), X = L^-T                      (linalg.cu)
+//   every iteration     A = X^T F X            two triangle-aware GEMMs
+//                       A = Q T Q^T            Householder tridiagonalisation, one cooperative
+//                                              kernel, two grid barriers per column
+//                       T y = y e              all eigenvalues by Sturm-count bisection
+//   after Fermi filling eigenvectors only for the occupied orbitals: inverse iteration on T,
+//                       clusters of close eigenvalues re-orthonormalised + Rayleigh-Ritz,
+//                       back-transformation Z = Q Y (column blocks per CTA, reflectors
+//                       staged in shared memory), C = X Z (triangular GEMM).
+//
+// The reference refactorises S on every call of dsygvd; the factor is identical, so it is
+// computed once here.  Eigenvector signs are arbitrary in both codes; every quantity the
+// engine derives (density, energy weighted density, charges) is sign invariant.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
-#include <cusolverDn.h>
 
+#include <cmath>
 #include <cstdio>
 #include <stdexcept>
+#include <vector>
 
 #include "engine.h"
 
+namespace cg = cooperative_groups;
+
 namespace tb {
+
+static void ck(cudaError_t e, const char* what) {
+  if (e != cudaSuccess)
+    throw std::runtime_error(std::string("CUDA error '") + cudaGetErrorString(e) + "' in " + what);
+}
 
 struct EigenSolver {
   int n = 0;
   cudaStream_t stream = nullptr;
-  cusolverDnHandle_t sol = nullptr;
-  cublasHandle_t blas = nullptr;
-  double* L = nullptr;     // Cholesky factor (lower, column-major == upper of row-major)
-  double* work = nullptr;  // cuSOLVER workspace
-  int lwork = 0;
-  int* info = nullptr;     // device
-  int* hinfo = nullptr;    // pinned host
+  double *L = nullptr, *X = nullptr, *A = nullptr, *T1 = nullptr;
+  double *d = nullptr, *e = nullptr, *tau = nullptr, *w = nullptr, *pv = nullptr, *scal = nullptr;
+  double *lu = nullptr;   // inverse iteration scratch [5][n][n]
+  double *Y = nullptr;    // eigenvectors of T, column-major [k][n]
+  int* status = nullptr;  // device
+  int* hstatus = nullptr; // pinned
+  int coop_blocks = 0;
 };
 
-static void check_cusolver(cusolverStatus_t st, const char* what) {
-  if (st != CUSOLVER_STATUS_SUCCESS) {
-    char buf[160];
-    snprintf(buf, sizeof(buf), "cuSOLVER error %d in %s", (int)st, what);
-    throw std::runtime_error(buf);
-  }
+// ------------------------------------------------------------------------------------------
+// Householder tridiagonalisation of the symmetric A (column-major, full storage), lower form
+// as LAPACK dsytd2('L'): for column i, v = [1; A(i+2:n, i)], tau_i, e_i = beta, d_i = A(i,i).
+// Warp 0 of block 0 owns the column that becomes the next pivot column: it updates that column
+// during the rank-2 update of step i and immediately builds reflector i+1 from it, so every
+// step needs two grid barriers (after the reflector, after the symmetric matrix-vector product).
+// ------------------------------------------------------------------------------------------
+// 1/x from the hardware approximation refined by two Newton steps (relative error ~1e-16);
+// used where x is bounded away from zero and denormals (pivots, Sturm quotients).
+__device__ __forceinline__ double frcp(double x) {
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+  double e = fma(-x, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-x, r, 1.0);
+  return fma(r, e, r);
 }
-static void check_cublas(cublasStatus_t st, const char* what) {
-  if (st != CUBLAS_STATUS_SUCCESS) {
-    char buf[160];
-    snprintf(buf, sizeof(buf), "cuBLAS error %d in %s", (int)st, what);
-    throw std::runtime_error(buf);
-  }
+
+__device__ __forceinline__ double wred(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
 }
-static void check_cuda(cudaError_t st, const char* what) {
-  if (st != cudaSuccess) {
-    char buf[200];
-    snprintf(buf, sizeof(buf), "CUDA error '%s' in %s", cudaGetErrorString(st), what);
-    throw std::runtime_error(buf);
+
+__device__ double block_sum256(double v, double* red) {
+  v = wred(v);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+  for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[k];
+  __syncthreads();
+  return t;
+}
+
+// reflector for column i, built by all threads of one block; writes tau[i], e[i], scaled v
+__device__ void make_reflector(int n, int i, double* A, double* tau, double* e, double* red) {
+  double* col = A + (size_t)i * n;
+  const double alpha = col[i + 1];
+  double s = 0.0;
+#pragma unroll 4
+  for (int r = i + 2 + threadIdx.x; r < n; r += blockDim.x) s += col[r] * col[r];
+  s = block_sum256(s, red);
+  double t = 0.0, beta = alpha;
+  if (s > 0.0) {
+    beta = -copysign(sqrt(alpha * alpha + s), alpha);
+    t = (beta - alpha) / beta;
+    const double sc = 1.0 / (alpha - beta);
+#pragma unroll 4
+    for (int r = i + 2 + threadIdx.x; r < n; r += blockDim.x) col[r] *= sc;
+  }
+  if (threadIdx.x == 0) {
+    tau[i] = t;
+    e[i] = beta;
   }
 }
 
+__global__ void __launch_bounds__(256) k_tridiag(int n, double* A, double* d, double* e,
+                                                 double* tau, double* pv, double* scal) {
+  cg::grid_group grid = cg::this_grid();
+  const int lane = threadIdx.x & 31;
+  const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarp = (gridDim.x * blockDim.x) >> 5;
+  const int bw = blockDim.x >> 5;  // warps per block
+  // warps that update trailing columns 1..m-1 (block 0 owns column 0 and the next reflector)
+  const bool solo = gridDim.x == 1;
+  const int uw = solo ? gwarp : gwarp - bw, nuw = solo ? nwarp : nwarp - bw;
+  __shared__ double red[32];
+  __shared__ double sK;
+  (void)scal;
+  if (blockIdx.x == 0 && n > 1) make_reflector(n, 0, A, tau, e, red);
+  grid.sync();
+  for (int i = 0; i < n - 1; ++i) {
+    const int m = n - i - 1;  // size of the trailing block A22 = A(i+1:n, i+1:n)
+    const double* v = A + (size_t)i * n + (i + 1);  // v[0] is implicitly 1
+    const double t = tau[i];
+    // p = t * A22 v  (rows of A22 via its columns, symmetric), also p_r v_r
+    for (int r = gwarp; r < m; r += nwarp) {
+      const double* colr = A + (size_t)(i + 1 + r) * n + (i + 1);
+      double s = 0.0;
+      if (lane < m) s = lane == 0 ? colr[0] : colr[lane] * v[lane];
+#pragma unroll 8
+      for (int c = lane + 32; c < m; c += 32) s += colr[c] * v[c];
+      s = wred(s) * t;
+      if (lane == 0) {
+        pv[r] = s;
+        pv[n + r] = s * (r == 0 ? 1.0 : v[r]);
+      }
+    }
+    grid.sync();
+    // K = -1/2 t (p . v), reduced by every block in the same order
+    {
+      double s = 0.0;
+      for (int r = threadIdx.x; r < m; r += blockDim.x) s += pv[n + r];
+      s = block_sum256(s, red);
+      if (threadIdx.x == 0) sK = -0.5 * t * s;
+      __syncthreads();
+    }
+    const double K = sK;
+    if (blockIdx.x == 0) {
+      if (threadIdx.x == 0) d[i] = A[i + (size_t)i * n];
+      // column 0 of A22 (global column i+1), then reflector i+1 from it
+      if (t != 0.0) {
+        const double wc = pv[0] + K;
+        double* colc = A + (size_t)(i + 1) * n + (i + 1);
+#pragma unroll 4
+        for (int r = threadIdx.x; r < m; r += blockDim.x) {
+          const double vr = r == 0 ? 1.0 : v[r];
+          const double wr = pv[r] + K * vr;
+          colc[r] -= vr * wc + wr;
+        }
+      }
+      __syncthreads();
+      if (i + 1 < n - 1) make_reflector(n, i + 1, A, tau, e, red);
+      else if (threadIdx.x == 0) d[n - 1] = A[(n - 1) + (size_t)(n - 1) * n];
+    }
+    // rank-2 update of the remaining columns: A22 -= v w^T + w v^T, w = p + K v
+    if (t != 0.0 && uw >= 0) {
+      for (int c = 1 + uw; c < m; c += nuw) {
+        const double vc = v[c];
+        const double wc = pv[c] + K * vc;
+        double* colc = A + (size_t)(i + 1 + c) * n + (i + 1);
+        if (lane == 0) colc[0] -= wc + (pv[0] + K) * vc;
+#pragma unroll 8
+        for (int r = 1 + lane; r < m; r += 32) {
+          const double vr = v[r];
+          colc[r] -= vr * wc + (pv[r] + K * vr) * vc;
+        }
+      }
+    }
+    grid.sync();
+  }
+  if (n == 1 && gwarp == 0 && lane == 0) d[0] = A[0];
+}
+
+// ------------------------------------------------------------------------------------------
+// eigenvalues of T by bisection on the Sturm count (one thread per eigenvalue, ascending)
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ int sturm(int n, const double* __restrict__ d,
+                                     const double* __restrict__ e2, double x, double pivmin) {
+  int cnt = 0;
+  double q = d[0] - x;
+  if (fabs(q) < pivmin) q = -pivmin;
+  cnt += q < 0.0;
+  for (int i = 1; i < n; ++i) {
+    q = d[i] - x - e2[i - 1] / q;
+    if (fabs(q) < pivmin) q = -pivmin;
+    cnt += q < 0.0;
+  }
+  return cnt;
+}
+
+__global__ void k_bisect(int n, const double* __restrict__ d, const double* __restrict__ e,
+                         double* e2, double* w, double* scal) {
+  __shared__ double bounds[3];
+  // Gershgorin bounds and pivmin (each block recomputes, O(n))
+  if (threadIdx.x == 0) {
+    double lo = 1e300, hi = -1e300, emax = 0.0;
+    for (int i = 0; i < n; ++i) {
+      const double r = (i > 0 ? fabs(e[i - 1]) : 0.0) + (i < n - 1 ? fabs(e[i]) : 0.0);
+      lo = fmin(lo, d[i] - r);
+      hi = fmax(hi, d[i] + r);
+      if (i < n - 1) emax = fmax(emax, e[i] * e[i]);
+    }
+    const double tnorm = fmax(fabs(lo), fabs(hi));
+    bounds[0] = lo - 2.2e-16 * tnorm * 4 - 1e-300;
+    bounds[1] = hi + 2.2e-16 * tnorm * 4 + 1e-300;
+    bounds[2] = fmax(2.2250738585072014e-308 * fmax(1.0, emax), 1e-300);
+  }
+  __syncthreads();
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  (void)e2;
+  if (j >= n) return;
+  double lo = bounds[0], hi = bounds[1];
+  const double pivmin = bounds[2];
+  for (int it = 0; it < 200; ++it) {
+    const double mid = 0.5 * (lo + hi);
+    if (hi - lo <= 2.0 * 2.220446049250313e-16 * fmax(fabs(lo), fabs(hi)) + 4.0 * pivmin ||
+        mid == lo || mid == hi)
+      break;
+    int cnt = 0;
+    double q = d[0] - mid;
+    if (fabs(q) < pivmin) q = -pivmin;
+    cnt += q < 0.0;
+    for (int i = 1; i < n; ++i) {
+      q = d[i] - mid - (e[i - 1] * e[i - 1]) / q;
+      if (fabs(q) < pivmin) q = -pivmin;
+      cnt += q < 0.0;
+    }
+    if (cnt > j) hi = mid;
+    else lo = mid;
+  }
+  w[j] = 0.5 * (lo + hi);
+  if (j == 0) scal[1] = fmax(fabs(bounds[0]), fabs(bounds[1]));  // |T| estimate
+}
+
+// Multisection: four lanes per eigenvalue evaluate the Sturm count at four interior points of
+// the current bracket (a 5-way split per round), so 8 eigenvalues fill a warp and the n
+// eigenvalues spread over all SMs.  The Sturm recurrence uses the correctly rounded FP64
+// reciprocal; the count stays backward stable.
+__global__ void __launch_bounds__(64) k_multisect(int n, const double* __restrict__ d,
+                                                  const double* __restrict__ e, double* w,
+                                                  double* scal) {
+  __shared__ double bounds[3];
+  if (threadIdx.x == 0) {
+    double lo = 1e300, hi = -1e300, emax = 0.0;
+    for (int i = 0; i < n; ++i) {
+      const double r = (i > 0 ? fabs(e[i - 1]) : 0.0) + (i < n - 1 ? fabs(e[i]) : 0.0);
+      lo = fmin(lo, d[i] - r);
+      hi = fmax(hi, d[i] + r);
+      if (i < n - 1) emax = fmax(emax, e[i] * e[i]);
+    }
+    const double tnorm = fmax(fabs(lo), fabs(hi));
+    bounds[0] = lo - 8.9e-16 * tnorm - 1e-300;
+    bounds[1] = hi + 8.9e-16 * tnorm + 1e-300;
+    bounds[2] = fmax(2.2250738585072014e-308 * fmax(1.0, emax), 1e-300);
+  }
+  __syncthreads();
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = gt >> 2, sub = gt & 3;
+  const unsigned grp = 0xFu << (threadIdx.x & 28);
+  const bool active = j < n;
+  double lo = bounds[0], hi = bounds[1];
+  const double pivmin = bounds[2];
+  for (int it = 0; it < 64; ++it) {
+    const bool done = !active || hi - lo <= 2.0 * 2.220446049250313e-16 * fmax(fabs(lo), fabs(hi)) + 4.0 * pivmin;
+    if (__all_sync(0xffffffffu, done)) break;
+    const double step = (hi - lo) * 0.2;
+    const double x = lo + (sub + 1) * step;
+    int cnt = 0;
+    if (!done) {
+      double q = d[0] - x;
+      if (fabs(q) < pivmin) q = -pivmin;
+      cnt += q < 0.0;
+      for (int i = 1; i < n; ++i) {
+        const double ee = e[i - 1];
+        q = d[i] - x - (ee * ee) * frcp(q);
+        if (fabs(q) < pivmin) q = -pivmin;
+        cnt += q < 0.0;
+      }
+    }
+    // gather the four counts of this eigenvalue's group
+    const int base = threadIdx.x & 28;
+    const int c0 = __shfl_sync(0xffffffffu, cnt, base + 0);
+    const int c1 = __shfl_sync(0xffffffffu, cnt, base + 1);
+    const int c2 = __shfl_sync(0xffffffffu, cnt, base + 2);
+    const int c3 = __shfl_sync(0xffffffffu, cnt, base + 3);
+    (void)grp;
+    if (!done) {
+      const double x0 = lo + step, x1 = lo + 2 * step, x2 = lo + 3 * step, x3 = lo + 4 * step;
+      if (c0 > j) hi = x0;
+      else if (c1 > j) { lo = x0; hi = x1; }
+      else if (c2 > j) { lo = x1; hi = x2; }
+      else if (c3 > j) { lo = x2; hi = x3; }
+      else lo = x3;
+    }
+  }
+  if (active && sub == 0) w[j] = 0.5 * (lo + hi);
+  if (gt == 0) scal[1] = fmax(fabs(bounds[0]), fabs(bounds[1]));
+}
+
+// ------------------------------------------------------------------------------------------
+// inverse iteration: one thread per eigenvector (column j < k), Gaussian elimination with
+// partial pivoting of the tridiagonal T - w_j I, three solves from a pseudo-random start.
+// scratch layout [array][row][j] keeps the per-row accesses of a warp contiguous.
+// Y is written column-major [j][n].
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ double hash_uniform(unsigned a, unsigned b) {
+  unsigned h = a * 0x9E3779B1u ^ (b + 0x7F4A7C15u) * 0x85EBCA77u;
+  h ^= h >> 15;
+  h *= 0x2C1B3C6Du;
+  h ^= h >> 12;
+  h *= 0x297A2D39u;
+  h ^= h >> 15;
+  return (double)h / 4294967296.0 * 2.0 - 1.0;
+}
+
+__global__ void k_invit(int n, int k, const double* __restrict__ d, const double* __restrict__ e,
+                        const double* __restrict__ w, const double* __restrict__ scal, double* lu,
+                        double* Y) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= k) return;
+  const size_t nk = (size_t)n * k;
+  double* U0 = lu;
+  double* U1 = lu + nk;
+  double* U2 = lu + 2 * nk;
+  double* Lm = lu + 3 * nk;
+  double* PV = lu + 4 * nk;  // pivot flag stored as double
+#define AT(arr, r) arr[(size_t)(r) * k + j]
+  const double lam = w[j];
+  const double tnorm = scal[1] > 0 ? scal[1] : 1.0;
+  const double tiny = 2.220446049250313e-16 * tnorm;
+  // factorise T - lam I
+  double u0 = d[0] - lam, u1 = n > 1 ? e[0] : 0.0, u2 = 0.0;
+  for (int r = 0; r < n - 1; ++r) {
+    const double c = e[r];                                  // sub-diagonal of row r+1
+    const double a1 = d[r + 1] - lam, b1 = r + 1 < n - 1 ? e[r + 1] : 0.0;
+    if (fabs(u0) >= fabs(c)) {
+      if (fabs(u0) < tiny) u0 = copysign(tiny, u0 == 0.0 ? 1.0 : u0);
+      const double l = c / u0;
+      AT(U0, r) = u0; AT(U1, r) = u1; AT(U2, r) = u2; AT(Lm, r) = l; AT(PV, r) = 0.0;
+      u0 = a1 - l * u1;
+      u1 = b1 - l * u2;
+      u2 = 0.0;
+    } else {
+      const double l = u0 / c;
+      AT(U0, r) = c; AT(U1, r) = a1; AT(U2, r) = b1; AT(Lm, r) = l; AT(PV, r) = 1.0;
+      const double n0 = u1 - l * a1, n1 = u2 - l * b1;
+      u0 = n0;
+      u1 = n1;
+      u2 = 0.0;
+    }
+  }
+  if (fabs(u0) < tiny) u0 = copysign(tiny, u0 == 0.0 ? 1.0 : u0);
+  AT(U0, n - 1) = u0; AT(U1, n - 1) = 0.0; AT(U2, n - 1) = 0.0;
+  double* y = Y + (size_t)j * n;
+  for (int r = 0; r < n; ++r) y[r] = hash_uniform(j + 1, r + 1);
+  for (int iter = 0; iter < 2; ++iter) {
+    // forward: apply row operations to the right-hand side
+    for (int r = 0; r < n - 1; ++r) {
+      const double l = AT(Lm, r);
+      if (AT(PV, r) == 0.0) {
+        y[r + 1] -= l * y[r];
+      } else {
+        const double t = y[r];
+        y[r] = y[r + 1];
+        y[r + 1] = t - l * y[r];
+      }
+    }
+    // backward: U x = y
+    double x1 = 0.0, x2 = 0.0;
+    for (int r = n - 1; r >= 0; --r) {
+      const double v = (y[r] - AT(U1, r) * x1 - AT(U2, r) * x2) * frcp(AT(U0, r));
+      y[r] = v;
+      x2 = x1;
+      x1 = v;
+    }
+    double nrm = 0.0;
+    for (int r = 0; r < n; ++r) nrm += y[r] * y[r];
+    nrm = 1.0 / sqrt(nrm);
+    for (int r = 0; r < n; ++r) y[r] *= nrm;
+  }
+#undef AT
+}
+
+// Clusters of close eigenvalues (gap < tol |T|): modified Gram-Schmidt, then Rayleigh-Ritz
+// with T inside the cluster (Jacobi on the small projected matrix).  One block per cluster
+// start; vectors of a cluster are consecutive columns of Y.
+constexpr int MAXCL = 32;
+__global__ void k_clusters(int n, int k, const double* __restrict__ d,
+                           const double* __restrict__ e, const double* __restrict__ w,
+                           const double* __restrict__ scal, double tolrel, double* Y) {
+  const int j0 = blockIdx.x;
+  if (j0 >= k) return;
+  const double tol = tolrel * (scal[1] > 0 ? scal[1] : 1.0);
+  if (j0 > 0 && w[j0] - w[j0 - 1] < tol) return;  // not a cluster start
+  int c = 1;
+  while (j0 + c < k && w[j0 + c] - w[j0 + c - 1] < tol) ++c;
+  if (c == 1) return;
+  __shared__ double red[32];
+  __shared__ double H[MAXCL][MAXCL], V[MAXCL][MAXCL];
+  auto bsum = [&](double v) {
+    v = wred(v);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x < 32) {
+      t = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+      t = wred(t);
+      if (threadIdx.x == 0) red[0] = t;
+    }
+    __syncthreads();
+    t = red[0];
+    __syncthreads();
+    return t;
+  };
+  // MGS
+  for (int a = 0; a < c; ++a) {
+    double* ya = Y + (size_t)(j0 + a) * n;
+    for (int b = 0; b < a; ++b) {
+      const double* yb = Y + (size_t)(j0 + b) * n;
+      double s = 0.0;
+      for (int r = threadIdx.x; r < n; r += blockDim.x) s += ya[r] * yb[r];
+      s = bsum(s);
+      for (int r = threadIdx.x; r < n; r += blockDim.x) ya[r] -= s * yb[r];
+      __syncthreads();
+    }
+    double s = 0.0;
+    for (int r = threadIdx.x; r < n; r += blockDim.x) s += ya[r] * ya[r];
+    s = 1.0 / sqrt(bsum(s));
+    for (int r = threadIdx.x; r < n; r += blockDim.x) ya[r] *= s;
+    __syncthreads();
+  }
+  if (c > MAXCL) return;
+  // H = Y_c^T T Y_c
+  for (int a = 0; a < c; ++a)
+    for (int b = a; b < c; ++b) {
+      const double* ya = Y + (size_t)(j0 + a) * n;
+      const double* yb = Y + (size_t)(j0 + b) * n;
+      double s = 0.0;
+      for (int r = threadIdx.x; r < n; r += blockDim.x) {
+        double ty = d[r] * yb[r];
+        if (r > 0) ty += e[r - 1] * yb[r - 1];
+        if (r < n - 1) ty += e[r] * yb[r + 1];
+        s += ya[r] * ty;
+      }
+      s = bsum(s);
+      if (threadIdx.x == 0) {
+        H[a][b] = s;
+        H[b][a] = s;
+      }
+    }
+  __syncthreads();
+  // cyclic Jacobi on H (thread 0), V accumulates rotations
+  if (threadIdx.x == 0) {
+    for (int a = 0; a < c; ++a)
+      for (int b = 0; b < c; ++b) V[a][b] = a == b ? 1.0 : 0.0;
+    for (int sweep = 0; sweep < 30; ++sweep) {
+      double off = 0.0;
+      for (int a = 0; a < c; ++a)
+        for (int b = a + 1; b < c; ++b) off += H[a][b] * H[a][b];
+      if (off < 1e-60) break;
+      for (int p = 0; p < c; ++p)
+        for (int q = p + 1; q < c; ++q) {
+          if (H[p][q] == 0.0) continue;
+          const double th = (H[q][q] - H[p][p]) / (2.0 * H[p][q]);
+          const double t = copysign(1.0, th) / (fabs(th) + sqrt(th * th + 1.0));
+          const double cs = 1.0 / sqrt(t * t + 1.0), sn = t * cs;
+          for (int r = 0; r < c; ++r) {
+            const double hp = H[r][p], hq = H[r][q];
+            H[r][p] = cs * hp - sn * hq;
+            H[r][q] = sn * hp + cs * hq;
+          }
+          for (int r = 0; r < c; ++r) {
+            const double hp = H[p][r], hq = H[q][r];
+            H[p][r] = cs * hp - sn * hq;
+            H[q][r] = sn * hp + cs * hq;
+          }
+          for (int r = 0; r < c; ++r) {
+            const double vp = V[r][p], vq = V[r][q];
+            V[r][p] = cs * vp - sn * vq;
+            V[r][q] = sn * vp + cs * vq;
+          }
+        }
+    }
+    // sort by Ritz value (ascending) -- columns of V
+    for (int a = 0; a < c; ++a) {
+      int mn = a;
+      for (int b = a + 1; b < c; ++b)
+        if (H[b][b] < H[mn][mn]) mn = b;
+      if (mn != a) {
+        const double t = H[a][a];
+        H[a][a] = H[mn][mn];
+        H[mn][mn] = t;
+        for (int r = 0; r < c; ++r) {
+          const double v = V[r][a];
+          V[r][a] = V[r][mn];
+          V[r][mn] = v;
+        }
+      }
+    }
+  }
+  __syncthreads();
+  // Y_c <- Y_c V (row by row through registers)
+  for (int r = threadIdx.x; r < n; r += blockDim.x) {
+    double row[MAXCL];
+    for (int a = 0; a < c; ++a) row[a] = Y[(size_t)(j0 + a) * n + r];
+    for (int b = 0; b < c; ++b) {
+      double s = 0.0;
+      for (int a = 0; a < c; ++a) s += row[a] * V[a][b];
+      Y[(size_t)(j0 + b) * n + r] = s;
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// back-transformation Z = Q Y = H_0 H_1 ... H_{n-2} Y  (apply H_{n-2} first).  Each block owns
+// a set of columns (one warp per column); reflectors are staged in shared memory in chunks.
+// ------------------------------------------------------------------------------------------
+constexpr int BT_WARPS = 4;
+constexpr int BT_CHUNK_MAX = 16;
+constexpr size_t BT_SMEM_MAX = 200 * 1024;
+static int bt_chunk(int n) {
+  int c = (int)(BT_SMEM_MAX / (sizeof(double) * (size_t)n));
+  return c < 1 ? 1 : (c > BT_CHUNK_MAX ? BT_CHUNK_MAX : c);
+}
+
+__global__ void __launch_bounds__(BT_WARPS * 32) k_backtransform(int n, int k, int chunk,
+                                                                 const double* __restrict__ A,
+                                                                 const double* __restrict__ tau,
+                                                                 double* Y) {
+  extern __shared__ double smem[];  // [chunk][n]
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int col = blockIdx.x * BT_WARPS + wid;
+  double* y = col < k ? Y + (size_t)col * n : nullptr;
+  // reflectors i = n-2 .. 0 ; reflector i acts on rows i+1..n-1, v[0] = 1
+  for (int top = n - 2; top >= 0; top -= chunk) {
+    const int bot = max(0, top - chunk + 1);
+    __syncthreads();
+    for (int i = top; i >= bot; --i) {
+      double* sv = smem + (size_t)(top - i) * n;
+      for (int r = i + 1 + threadIdx.x; r < n; r += blockDim.x)
+        sv[r] = r == i + 1 ? 1.0 : A[r + (size_t)i * n];
+    }
+    __syncthreads();
+    if (y) {
+      for (int i = top; i >= bot; --i) {
+        const double t = tau[i];
+        if (t == 0.0) continue;
+        const double* sv = smem + (size_t)(top - i) * n;
+        double s = 0.0;
+        for (int r = i + 1 + lane; r < n; r += 32) s += sv[r] * y[r];
+        s = wred(s) * t;
+        for (int r = i + 1 + lane; r < n; r += 32) y[r] -= s * sv[r];
+        __syncwarp();
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------
 EigenSolver* eigen_create(int n, cudaStream_t s) {
   auto* e = new EigenSolver();
   e->n = n;
   e->stream = s;
-  check_cusolver(cusolverDnCreate(&e->sol), "create");
-  check_cusolver(cusolverDnSetStream(e->sol, s), "set stream");
-  check_cublas(cublasCreate(&e->blas), "cublas create");
-  check_cublas(cublasSetStream(e->blas, s), "cublas stream");
-  check_cuda(cudaMalloc(&e->L, sizeof(double) * (size_t)n * n), "alloc L");
-  check_cuda(cudaMalloc(&e->info, sizeof(int)), "alloc info");
-  check_cuda(cudaMallocHost(&e->hinfo, sizeof(int)), "alloc hinfo");
-  int lw1 = 0, lw2 = 0;
-  check_cusolver(cusolverDnDpotrf_bufferSize(e->sol, CUBLAS_FILL_MODE_LOWER, n, e->L, n, &lw1),
-                 "potrf ws");
-  check_cusolver(cusolverDnDsyevd_bufferSize(e->sol, CUSOLVER_EIG_MODE_VECTOR,
-                                             CUBLAS_FILL_MODE_LOWER, n, e->L, n, nullptr, &lw2),
-                 "syevd ws");
-  e->lwork = lw1 > lw2 ? lw1 : lw2;
-  check_cuda(cudaMalloc(&e->work, sizeof(double) * (size_t)e->lwork), "alloc work");
+  const size_t nn = (size_t)n * n;
+  ck(cudaMalloc(&e->L, sizeof(double) * nn), "L");
+  ck(cudaMalloc(&e->X, sizeof(double) * nn), "X");
+  ck(cudaMalloc(&e->A, sizeof(double) * nn), "A");
+  ck(cudaMalloc(&e->T1, sizeof(double) * nn), "T1");
+  ck(cudaMalloc(&e->Y, sizeof(double) * nn), "Y");
+  ck(cudaMalloc(&e->lu, sizeof(double) * 5 * nn), "lu");
+  ck(cudaMalloc(&e->d, sizeof(double) * (n + 1)), "d");
+  ck(cudaMalloc(&e->e, sizeof(double) * (n + 1)), "e");
+  ck(cudaMalloc(&e->tau, sizeof(double) * (n + 1)), "tau");
+  ck(cudaMalloc(&e->w, sizeof(double) * (n + 1)), "w");
+  ck(cudaMalloc(&e->pv, sizeof(double) * 2 * (n + 1)), "pv");
+  ck(cudaMalloc(&e->scal, sizeof(double) * 8), "scal");
+  ck(cudaMalloc(&e->status, sizeof(int)), "status");
+  ck(cudaMallocHost(&e->hstatus, sizeof(int)), "hstatus");
+  int dev = 0, nsm = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tridiag, 256, 0);
+  (void)per_sm;
+  e->coop_blocks = nsm;  // one block per SM keeps the grid barrier cheap
+  // shared memory of the back-transformation
+  ck(cudaFuncSetAttribute(k_backtransform, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          (int)(sizeof(double) * bt_chunk(n) * n)),
+     "smem attr");
   return e;
 }
 
 void eigen_destroy(EigenSolver* e) {
   if (!e) return;
-  cudaFree(e->L);
-  cudaFree(e->work);
-  cudaFree(e->info);
-  cudaFreeHost(e->hinfo);
-  cublasDestroy(e->blas);
-  cusolverDnDestroy(e->sol);
+  for (double* p : {e->L, e->X, e->A, e->T1, e->Y, e->lu, e->d, e->e, e->tau, e->w, e->pv, e->scal})
+    cudaFree(p);
+  cudaFree(e->status);
+  cudaFreeHost(e->hstatus);
   delete e;
 }
 
+int cholesky_inverse(int n, double* L, double* X, int* d_status, int* h_status, cudaStream_t s);
+
 int eigen_set_overlap(EigenSolver* e, const double* S) {
   const int n = e->n;
-  check_cuda(cudaMemcpyAsync(e->L, S, sizeof(double) * (size_t)n * n, cudaMemcpyDeviceToDevice,
-                             e->stream),
-             "copy S");
-  check_cusolver(cusolverDnDpotrf(e->sol, CUBLAS_FILL_MODE_LOWER, n, e->L, n, e->work, e->lwork,
-                                  e->info),
-                 "potrf");
-  check_cuda(cudaMemcpyAsync(e->hinfo, e->info, sizeof(int), cudaMemcpyDeviceToHost, e->stream),
-             "info");
-  check_cuda(cudaStreamSynchronize(e->stream), "sync potrf");
-  return *e->hinfo;
+  ck(cudaMemcpyAsync(e->L, S, sizeof(double) * (size_t)n * n, cudaMemcpyDeviceToDevice, e->stream),
+     "copy S");
+  return cholesky_inverse(n, e->L, e->X, e->status, e->hstatus, e->stream);
 }
 
-int eigen_solve(EigenSolver* e, double* F, double* C, double* w) {
-  const int n = e->n;
-  const double one = 1.0;
-  // A = L^-1 F   (column-major view; F symmetric)
-  check_cublas(cublasDtrsm(e->blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N,
-                           CUBLAS_DIAG_NON_UNIT, n, n, &one, e->L, n, F, n),
-               "trsm 1");
-  // A = A L^-T
-  check_cublas(cublasDtrsm(e->blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T,
-                           CUBLAS_DIAG_NON_UNIT, n, n, &one, e->L, n, F, n),
-               "trsm 2");
-  check_cusolver(cusolverDnDsyevd(e->sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, F,
-                                  n, w, e->work, e->lwork, e->info),
-                 "syevd");
-  // C = L^-T Y
-  check_cublas(cublasDtrsm(e->blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T,
-                           CUBLAS_DIAG_NON_UNIT, n, n, &one, e->L, n, F, n),
-               "trsm 3");
-  if (C != F)
-    check_cuda(cudaMemcpyAsync(C, F, sizeof(double) * (size_t)n * n, cudaMemcpyDeviceToDevice,
-                               e->stream),
-               "copy C");
-  check_cuda(cudaMemcpyAsync(e->hinfo, e->info, sizeof(int), cudaMemcpyDeviceToHost, e->stream),
-             "info");
-  check_cuda(cudaStreamSynchronize(e->stream), "sync syevd");
-  return *e->hinfo;
+int eigen_values(EigenSolver* es, const double* F, double* w_out) {
+  const int n = es->n;
+  cudaStream_t s = es->stream;
+  // A = X^T (F X): X upper triangular
+  gemm64(false, false, n, n, n, 1.0, F, n, es->X, n, 0.0, es->T1, n, KM_LT_COLEND, s);
+  gemm64(true, false, n, n, n, 1.0, es->X, n, es->T1, n, 0.0, es->A, n, KM_LT_ROWEND, s);
+  // tridiagonalise
+  {
+    int nn = n;
+    int blocks = es->coop_blocks;
+    const int need = (n * 32 + 255) / 256;
+    if (blocks > need) blocks = need > 0 ? need : 1;
+    void* args[] = {&nn, &es->A, &es->d, &es->e, &es->tau, &es->pv, &es->scal};
+    ++g_kernel_launches;
+    ck(cudaLaunchCooperativeKernel((void*)k_tridiag, blocks, 256, args, 0, s), "tridiag");
+  }
+  ++g_kernel_launches;
+  k_multisect<<<(4 * n + 63) / 64, 64, 0, s>>>(n, es->d, es->e, es->w, es->scal);
+  ck(cudaMemcpyAsync(w_out, es->w, sizeof(double) * n, cudaMemcpyDeviceToDevice, s), "w");
+  return 0;
 }
 
-// P = sum_{m<k} f_m C_m C_m^T  (C column-major): scale columns into work, then one GEMM
+void eigen_vectors(EigenSolver* es, int k, double* C) {
+  const int n = es->n;
+  cudaStream_t s = es->stream;
+  if (k <= 0) return;
+  ++g_kernel_launches;
+  k_invit<<<(k + 15) / 16, 16, 0, s>>>(n, k, es->d, es->e, es->w, es->scal, es->lu, es->Y);
+  ++g_kernel_launches;
+  k_clusters<<<k, 256, 0, s>>>(n, k, es->d, es->e, es->w, es->scal, 1e-5, es->Y);
+  const int chunk = bt_chunk(n);
+  const size_t smem = sizeof(double) * chunk * n;
+  ++g_kernel_launches;
+  k_backtransform<<<(k + BT_WARPS - 1) / BT_WARPS, BT_WARPS * 32, smem, s>>>(n, k, chunk, es->A,
+                                                                           es->tau, es->Y);
+  // C = X Y (X upper triangular)
+  gemm64(false, false, n, k, n, 1.0, es->X, n, es->Y, n, 0.0, C, n, KM_GE_ROWBEG, s);
+}
+
+// P = sum_{m<k} f_m C_m C_m^T: scale columns into work, then one GEMM
 __global__ void k_scale_cols(int n, int k, const double* C, const double* f, double* out) {
   const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (t >= (size_t)n * k) return;
   out[t] = C[t] * f[t / n];
 }
 
-static cublasHandle_t g_blas = nullptr;
-static cudaStream_t g_blas_stream = nullptr;
-
 void density_matrix(int n, int k, const double* C, const double* f, double* P, double* work,
                     cudaStream_t s) {
-  if (!g_blas) check_cublas(cublasCreate(&g_blas), "create");
-  if (g_blas_stream != s) {
-    check_cublas(cublasSetStream(g_blas, s), "stream");
-    g_blas_stream = s;
-  }
   if (k <= 0) {
     cudaMemsetAsync(P, 0, sizeof(double) * (size_t)n * n, s);
     return;
@@ -150,11 +670,7 @@ void density_matrix(int n, int k, const double* C, const double* f, double* P, d
   const size_t tot = (size_t)n * k;
   ++g_kernel_launches;
   k_scale_cols<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(n, k, C, f, work);
-  const double one = 1.0, zero = 0.0;
-  // P(n x n) = work(n x k) * C(n x k)^T
-  check_cublas(cublasDgemm(g_blas, CUBLAS_OP_N, CUBLAS_OP_T, n, n, k, &one, work, n, C, n, &zero,
-                           P, n),
-               "gemm P");
+  gemm64(false, true, n, n, k, 1.0, work, n, C, n, 0.0, P, n, KM_NONE, s);
 }
 
 }  // namespace tb

@@ -163,8 +163,15 @@ EigenSolver* eigen_create(int n, cudaStream_t s);
 void eigen_destroy(EigenSolver*);
 // factorise S once per geometry; returns 0 on success, >0 if S is not positive definite
 int eigen_set_overlap(EigenSolver*, const double* S);
-// solve F C = S C e ; F is destroyed, C column-major [n][n], e ascending. returns 0 on success
-int eigen_solve(EigenSolver*, double* F, double* C, double* e);
+// all eigenvalues (ascending) of F C = S C e; keeps the tridiagonal form for eigen_vectors
+int eigen_values(EigenSolver*, const double* F, double* e);
+// the k lowest eigenvectors, C column-major [k][n] (S-orthonormal)
+void eigen_vectors(EigenSolver*, int k, double* C);
+
+// dense FP64 GEMM (column-major, BLAS semantics); kmode skips zero triangles
+enum { KM_NONE = 0, KM_LT_COLEND = 1, KM_LT_ROWEND = 2, KM_GE_ROWBEG = 3 };
+void gemm64(bool ta, bool tb, int M, int N, int K, double alpha, const double* A, int lda,
+            const double* B, int ldb, double beta, double* C, int ldc, int kmode, cudaStream_t s);
 
 // eelec[i] = ts/nat + eband[i]
 void launch_eelec_init(int nat, const double* ts, const double* eband, double* eelec,

@@ -1,0 +1,192 @@
+// Dense FP64 linear algebra kernels of the engine: tiled GEMM with triangle-aware k ranges,
+// Cholesky factorisation and the inverse of its transpose (once per geometry).
+//
+// GB300 executes FP64 at ~2 FMA/clk/SM, so these kernels are arithmetic bound even from L2;
+// the tiling only has to keep every SM busy (small tiles, many CTAs) and avoid wasted work on
+// the zero triangles of triangular operands.  All matrices are column-major
+// (element (i, j) at p[i + j*ld]) as in BLAS.
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+
+#include "engine.h"
+
+namespace cg = cooperative_groups;
+
+namespace tb {
+
+// ------------------------------------------------------------------------------------------
+// GEMM:  C = alpha op(A) op(B) + beta C ,  op(A): M x K,  op(B): K x N
+// kmode restricts the summation range when an operand is triangular:
+//   KM_NONE        0 <= k < K
+//   KM_LT_COLEND   k <  column tile end   (op(B) upper triangular:  B(k,j) = 0 for k > j)
+//   KM_LT_ROWEND   k <  row tile end      (op(A) lower triangular:  A(i,k) = 0 for k > i)
+//   KM_GE_ROWBEG   k >= row tile begin    (op(A) upper triangular:  A(i,k) = 0 for k < i)
+// ------------------------------------------------------------------------------------------
+template <int BM, int BN, int BK, int TM, int TN>
+__global__ void __launch_bounds__((BM / TM) * (BN / TN))
+    k_gemm(int M, int N, int K, double alpha, const double* __restrict__ A, int lda, bool ta,
+           const double* __restrict__ B, int ldb, bool tb, double beta, double* __restrict__ C,
+           int ldc, int kmode) {
+  constexpr int NT = (BM / TM) * (BN / TN);
+  __shared__ double As[BK][BM + 1];
+  __shared__ double Bs[BK][BN + 1];
+  const int i0 = blockIdx.y * BM, j0 = blockIdx.x * BN;
+  const int tid = threadIdx.x;
+  const int tr = tid / (BN / TN), tc = tid % (BN / TN);
+  int kbeg = 0, kend = K;
+  if (kmode == KM_LT_COLEND) kend = min(K, j0 + BN);
+  else if (kmode == KM_LT_ROWEND) kend = min(K, i0 + BM);
+  else if (kmode == KM_GE_ROWBEG) kbeg = (i0 / BK) * BK;
+  double acc[TM][TN];
+#pragma unroll
+  for (int a = 0; a < TM; ++a)
+#pragma unroll
+    for (int b = 0; b < TN; ++b) acc[a][b] = 0.0;
+  for (int k0 = kbeg; k0 < kend; k0 += BK) {
+    for (int t = tid; t < BM * BK; t += NT) {
+      const int ii = ta ? t / BK : t % BM, kk = ta ? t % BK : t / BM;
+      const int gi = i0 + ii, gk = k0 + kk;
+      double v = 0.0;
+      if (gi < M && gk < kend) v = ta ? A[gk + (size_t)gi * lda] : A[gi + (size_t)gk * lda];
+      As[kk][ii] = v;
+    }
+    for (int t = tid; t < BK * BN; t += NT) {
+      const int kk = tb ? t / BN : t % BK, jj = tb ? t % BN : t / BK;
+      const int gk = k0 + kk, gj = j0 + jj;
+      double v = 0.0;
+      if (gj < N && gk < kend) v = tb ? B[gj + (size_t)gk * ldb] : B[gk + (size_t)gj * ldb];
+      Bs[kk][jj] = v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) {
+      double a[TM], b[TN];
+#pragma unroll
+      for (int x = 0; x < TM; ++x) a[x] = As[kk][tr * TM + x];
+#pragma unroll
+      for (int y = 0; y < TN; ++y) b[y] = Bs[kk][tc * TN + y];
+#pragma unroll
+      for (int x = 0; x < TM; ++x)
+#pragma unroll
+        for (int y = 0; y < TN; ++y) acc[x][y] = fma(a[x], b[y], acc[x][y]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int x = 0; x < TM; ++x) {
+    const int gi = i0 + tr * TM + x;
+    if (gi >= M) continue;
+#pragma unroll
+    for (int y = 0; y < TN; ++y) {
+      const int gj = j0 + tc * TN + y;
+      if (gj >= N) continue;
+      double* c = C + gi + (size_t)gj * ldc;
+      *c = beta == 0.0 ? alpha * acc[x][y] : alpha * acc[x][y] + beta * *c;
+    }
+  }
+}
+
+void gemm64(bool ta, bool tb, int M, int N, int K, double alpha, const double* A, int lda,
+            const double* B, int ldb, double beta, double* C, int ldc, int kmode, cudaStream_t s) {
+  if (M <= 0 || N <= 0) return;
+  // small problems: 16x16 tiles keep enough CTAs in flight on 152 SMs
+  if ((long long)((M + 31) / 32) * ((N + 31) / 32) < 2 * 152) {
+    dim3 grid((N + 15) / 16, (M + 15) / 16);
+    ++g_kernel_launches;
+    k_gemm<16, 16, 16, 2, 2><<<grid, 64, 0, s>>>(M, N, K, alpha, A, lda, ta, B, ldb, tb, beta, C,
+                                                 ldc, kmode);
+  } else {
+    dim3 grid((N + 31) / 32, (M + 31) / 32);
+    ++g_kernel_launches;
+    k_gemm<32, 32, 16, 4, 4><<<grid, 64, 0, s>>>(M, N, K, alpha, A, lda, ta, B, ldb, tb, beta, C,
+                                                  ldc, kmode);
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// Cholesky S = L L^T (lower, in place, column-major), right looking, one grid barrier per
+// column: warps own trailing columns and update them with the (not yet scaled) pivot column.
+// status: 0 ok, j+1 if the j-th pivot is not positive.
+// ------------------------------------------------------------------------------------------
+__global__ void k_cholesky(int n, double* A, int* status) {
+  cg::grid_group grid = cg::this_grid();
+  const int lane = threadIdx.x & 31;
+  const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarp = (gridDim.x * blockDim.x) >> 5;
+  for (int j = 0; j < n; ++j) {
+    const double piv = A[j + (size_t)j * n];
+    if (!(piv > 0.0)) {
+      if (gwarp == 0 && lane == 0) *status = j + 1;
+      return;  // every thread reads the same pivot and leaves together
+    }
+    const double inv = 1.0 / piv;
+    for (int c = j + 1 + gwarp; c < n; c += nwarp) {
+      const double ljc = A[c + (size_t)j * n] * inv;
+      double* col = A + (size_t)c * n;
+      const double* pj = A + (size_t)j * n;
+      for (int i = c + lane; i < n; i += 32) col[i] -= pj[i] * ljc;
+    }
+    grid.sync();
+  }
+  if (gwarp == 0 && lane == 0) *status = 0;
+}
+
+// scale columns: L(i,j) = A(i,j)/sqrt(A(j,j)), zero the strict upper triangle
+__global__ void k_chol_scale(int n, double* A) {
+  const int j = blockIdx.x;
+  const double d = sqrt(A[j + (size_t)j * n]);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    double* p = A + i + (size_t)j * n;
+    if (i < j) *p = 0.0;
+    else if (i > j) *p = *p / d;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) A[j + (size_t)j * n] = d;
+}
+
+// X = L^-T (upper triangular): column j solves L^T x = e_j by back substitution; the dot
+// products read columns of L, which are contiguous.  One warp per column.
+__global__ void k_tri_inv_t(int n, const double* __restrict__ L, double* X) {
+  const int lane = threadIdx.x & 31;
+  const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (j >= n) return;
+  double* x = X + (size_t)j * n;
+  for (int i = lane; i < n; i += 32) x[i] = 0.0;
+  __syncwarp();
+  if (lane == 0) x[j] = 1.0 / L[j + (size_t)j * n];
+  __syncwarp();
+  for (int i = j - 1; i >= 0; --i) {
+    const double* li = L + (size_t)i * n;  // column i of L
+    double s = 0.0;
+    for (int k = i + 1 + lane; k <= j; k += 32) s += li[k] * x[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) x[i] = -s / li[i];
+    __syncwarp();
+  }
+}
+
+int cholesky_inverse(int n, double* L, double* X, int* d_status, int* h_status, cudaStream_t s) {
+  int dev = 0, nsm = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cholesky, 256, 0);
+  (void)per_sm;
+  int blocks = nsm;  // one block per SM keeps the grid barrier cheap
+  const int need = (n * 32 + 255) / 256;
+  if (blocks > need) blocks = need > 0 ? need : 1;
+  void* args[] = {&n, &L, &d_status};
+  ++g_kernel_launches;
+  cudaError_t e = cudaLaunchCooperativeKernel((void*)k_cholesky, blocks, 256, args, 0, s);
+  if (e != cudaSuccess) return -1;
+  cudaMemcpyAsync(h_status, d_status, sizeof(int), cudaMemcpyDeviceToHost, s);
+  cudaStreamSynchronize(s);
+  if (*h_status != 0) return *h_status;
+  ++g_kernel_launches;
+  k_chol_scale<<<n, 256, 0, s>>>(n, L);
+  ++g_kernel_launches;
+  k_tri_inv_t<<<(n * 32 + 255) / 256, 256, 0, s>>>(n, L, X);
+  return 0;
+}
+
+}  // namespace tb

@@ -29,6 +29,20 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
+// x^e for the small integer exponents of the damping functions, pow() otherwise
+__device__ __forceinline__ double powe(double x, double e) {
+  if (e == 2.0) return x * x;
+  if (e == 3.0) return x * x * x;
+  if (e == 4.0) { const double x2 = x * x; return x2 * x2; }
+  return pow(x, e);
+}
+
+// isotropic kernel 1/(r^g + eta^-g)^(1/g); g = 2 is the GFN2 case
+__device__ __forceinline__ double gam_kernel(double r1, double eta, double g) {
+  if (g == 2.0) return rsqrt(r1 * r1 + 1.0 / (eta * eta));
+  return 1.0 / pow(pow(r1, g) + pow(eta, -g), 1.0 / g);
+}
+
 // ------------------------------------------------------------------------------------
 // coordination number (double exponential counting function, see oracle for the form)
 // ------------------------------------------------------------------------------------
@@ -69,7 +83,7 @@ void launch_cn(const DevMol& m, const Gfn2Scalars& p, double* cn, cudaStream_t s
     return;
   }
   ++g_kernel_launches;
-  k_cn<<<(m.nat * 32 + 255) / 256, 256, 0, s>>>(m, p, cn);
+  k_cn<<<(m.nat * 32 + 63) / 64, 64, 0, s>>>(m, p, cn);
 }
 
 // grad_i += sum_j (dEdcn_i + dEdcn_j) dcount/dr (R_i - R_j)/r ; per-atom sigma partials
@@ -110,7 +124,7 @@ void launch_cn_grad(const DevMol& m, const Gfn2Scalars& p, const double* dEdcn, 
                     double* sig_at, cudaStream_t s) {
   if (m.nat == 1) return;
   ++g_kernel_launches;
-  k_cn_grad<<<(m.nat * 32 + 255) / 256, 256, 0, s>>>(m, p, dEdcn, grad, sig_at);
+  k_cn_grad<<<(m.nat * 32 + 63) / 64, 64, 0, s>>>(m, p, dEdcn, grad, sig_at);
 }
 
 // ------------------------------------------------------------------------------------
@@ -176,7 +190,7 @@ __global__ void k_coulomb(DevMol m, Gfn2Scalars p, const double* __restrict__ mr
       double acc = 0.0;
       for (int b = 0; b < nsj; ++b) {
         const double g = 0.5 * (hi + m.sh_hub[js0 + b]);
-        const double t = 1.0 / pow(pow(r1, p.gexp) + pow(g, -p.gexp), 1.0 / p.gexp);
+        const double t = gam_kernel(r1, g, p.gexp);
         acc += t * qsh[js0 + b];
       }
       ush[a] += acc;
@@ -185,8 +199,8 @@ __global__ void k_coulomb(DevMol m, Gfn2Scalars p, const double* __restrict__ mr
     const double g1 = 1.0 / r1, g3 = g1 * g1 * g1, g5 = g3 * g1 * g1;
     const double rr = 0.5 * (mrad[j] + ri) * g1;
     const double rr3 = rr * rr * rr;
-    const double f3 = 1.0 / (1.0 + 6.0 * pow(rr, p.mp_dmp3));
-    const double f5 = 1.0 / (1.0 + 6.0 * pow(rr, p.mp_dmp5));
+    const double f3 = 1.0 / (1.0 + 6.0 * powe(rr, p.mp_dmp3));
+    const double f5 = 1.0 / (1.0 + 6.0 * powe(rr, p.mp_dmp5));
     (void)rr3;
     const double* dj = dpat + 3 * j;
     const double* qj = qpat + 6 * j;
@@ -252,7 +266,7 @@ void launch_coulomb_potential(const DevMol& m, const Gfn2Scalars& p, const doubl
                               const double* qpat, double* vsh, double* vat, double* vdp,
                               double* vqp, cudaStream_t s) {
   ++g_kernel_launches;
-  k_coulomb<0><<<(m.nat * 32 + 255) / 256, 256, 0, s>>>(m, p, mrad, qsh, qat, dpat, qpat, vsh, vat,
+  k_coulomb<0><<<(m.nat * 32 + 63) / 64, 64, 0, s>>>(m, p, mrad, qsh, qat, dpat, qpat, vsh, vat,
                                                          vdp, vqp, nullptr);
 }
 
@@ -260,7 +274,7 @@ void launch_coulomb_energy(const DevMol& m, const Gfn2Scalars& p, const double* 
                            const double* qsh, const double* qat, const double* dpat,
                            const double* qpat, double* eat, cudaStream_t s) {
   ++g_kernel_launches;
-  k_coulomb<1><<<(m.nat * 32 + 255) / 256, 256, 0, s>>>(m, p, mrad, qsh, qat, dpat, qpat, nullptr,
+  k_coulomb<1><<<(m.nat * 32 + 63) / 64, 64, 0, s>>>(m, p, mrad, qsh, qat, dpat, qpat, nullptr,
                                                          nullptr, nullptr, nullptr, eat);
 }
 
@@ -291,8 +305,14 @@ __global__ void k_coulomb_grad(DevMol m, Gfn2Scalars p, const double* __restrict
     for (int a = 0; a < nsi; ++a)
       for (int b = 0; b < nsj; ++b) {
         const double gm = 0.5 * (m.sh_hub[is0 + a] + m.sh_hub[js0 + b]);
-        double d = 1.0 / (pow(r1, p.gexp) + pow(gm, -p.gexp));
-        d = -pow(r1, p.gexp - 2.0) * d * pow(d, 1.0 / p.gexp);
+        double d;
+        if (p.gexp == 2.0) {
+          d = 1.0 / (r2 + 1.0 / (gm * gm));
+          d = -d * sqrt(d);
+        } else {
+          d = 1.0 / (pow(r1, p.gexp) + pow(gm, -p.gexp));
+          d = -pow(r1, p.gexp - 2.0) * d * pow(d, 1.0 / p.gexp);
+        }
         f += d * qsh[is0 + a] * qsh[js0 + b];
       }
     double gp[3];
@@ -304,13 +324,13 @@ __global__ void k_coulomb_grad(DevMol m, Gfn2Scalars p, const double* __restrict
     double v[3] = {-w[0], -w[1], -w[2]};
     const double rr = 0.5 * (mrad[i] + mrad[j]);
     const double g1 = 1.0 / r1, g3 = g1 * g1 * g1, g5 = g3 * g1 * g1, g7 = g5 * g1 * g1;
-    const double f3 = 1.0 / (1.0 + 6.0 * pow(rr * g1, p.mp_dmp3));
+    const double f3 = 1.0 / (1.0 + 6.0 * powe(rr * g1, p.mp_dmp3));
     const double d3 = -3 * g5 * f3 - p.mp_dmp3 * f3 * (f3 - 1.0) * g5;
-    const double f5 = 1.0 / (1.0 + 6.0 * pow(rr * g1, p.mp_dmp5));
+    const double f5 = 1.0 / (1.0 + 6.0 * powe(rr * g1, p.mp_dmp5));
     const double d5 = -5 * f5 - p.mp_dmp5 * (f5 * f5 - f5);
     const double dpiqj = (v[0] * di[0] + v[1] * di[1] + v[2] * di[2]) * qaj;
     const double qidpj = (v[0] * dj[0] + v[1] * dj[1] + v[2] * dj[2]) * qai;
-    double fddr = 3.0 * (dpiqj - qidpj) * p.mp_dmp3 * f3 * g3 * (f3 / rr) * pow(rr * g1, p.mp_dmp3);
+    double fddr = 3.0 * (dpiqj - qidpj) * p.mp_dmp3 * f3 * g3 * (f3 / rr) * powe(rr * g1, p.mp_dmp3);
     double ga[3];
     for (int k = 0; k < 3; ++k)
       ga[k] = -d3 * v[k] * (dpiqj - qidpj) + f3 * g3 * (qai * dj[k] - qaj * di[k]);
@@ -318,7 +338,7 @@ __global__ void k_coulomb_grad(DevMol m, Gfn2Scalars p, const double* __restrict
     const double dpiv = di[0] * v[0] + di[1] * v[1] + di[2] * v[2];
     const double dpjv = dj[0] * v[0] + dj[1] * v[1] + dj[2] * v[2];
     const double edd = dpidpj * r2 - 3 * dpjv * dpiv;
-    fddr += 3.0 * edd * p.mp_dmp5 * f5 * g5 * (f5 / rr) * pow(rr * g1, p.mp_dmp5);
+    fddr += 3.0 * edd * p.mp_dmp5 * f5 * g5 * (f5 / rr) * powe(rr * g1, p.mp_dmp5);
     for (int k = 0; k < 3; ++k)
       ga[k] += -2.0 * f5 * g5 * dpidpj * v[k] + 3.0 * f5 * g5 * (dpiv * dj[k] + dpjv * di[k])
                - edd * d5 * g7 * v[k];
@@ -328,7 +348,7 @@ __global__ void k_coulomb_grad(DevMol m, Gfn2Scalars p, const double* __restrict
                       + (qaj * qi[0] + qj[0] * qai) * v[0] * v[0]
                       + (qaj * qi[2] + qj[2] * qai) * v[1] * v[1]
                       + (qaj * qi[5] + qj[5] * qai) * v[2] * v[2];
-    fddr += eq * 3.0 * p.mp_dmp5 * f5 * g5 * f5 / rr * pow(rr * g1, p.mp_dmp5);
+    fddr += eq * 3.0 * p.mp_dmp5 * f5 * g5 * f5 / rr * powe(rr * g1, p.mp_dmp5);
     const double qjv[3] = {v[0] * qj[0] + v[1] * qj[1] + v[2] * qj[3],
                            v[0] * qj[1] + v[1] * qj[2] + v[2] * qj[4],
                            v[0] * qj[3] + v[1] * qj[4] + v[2] * qj[5]};
@@ -360,7 +380,7 @@ void launch_coulomb_gradient(const DevMol& m, const Gfn2Scalars& p, const double
                              double* dEdcn, cudaStream_t s) {
   if (m.nat == 1) return;
   ++g_kernel_launches;
-  k_coulomb_grad<<<(m.nat * 32 + 255) / 256, 256, 0, s>>>(m, p, mrad, dmrdcn, qsh, qat, dpat, qpat,
+  k_coulomb_grad<<<(m.nat * 32 + 63) / 64, 64, 0, s>>>(m, p, mrad, dmrdcn, qsh, qat, dpat, qpat,
                                                           grad, sig_at, dEdcn);
 }
 
@@ -407,7 +427,7 @@ __global__ void k_repulsion(DevMol m, Gfn2Scalars p, double* erep, double* grad,
 void launch_repulsion(const DevMol& m, const Gfn2Scalars& p, double* erep, double* grad,
                       double* sig_at, cudaStream_t s) {
   ++g_kernel_launches;
-  k_repulsion<<<(m.nat * 32 + 255) / 256, 256, 0, s>>>(m, p, erep, grad, sig_at);
+  k_repulsion<<<(m.nat * 32 + 63) / 64, 64, 0, s>>>(m, p, erep, grad, sig_at);
 }
 
 // ------------------------------------------------------------------------------------
