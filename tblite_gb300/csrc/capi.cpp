@@ -397,8 +397,12 @@ static void ensure_workspace(_tblite_calculator* c) {
     w.icount.alloc(4);
     const size_t nd = nsh + 9 * nat;
     w.vec_out.alloc(nd);
-    if (w.eig) eigen_destroy(w.eig);
-    w.eig = eigen_create((int)n, s);
+    if (w.eig && eigen_capacity(w.eig) >= (int)n) {
+      eigen_resize(w.eig, (int)n);
+    } else {
+      if (w.eig) eigen_destroy(w.eig);
+      w.eig = eigen_create((int)n, s);
+    }
     w.nat = c->nat;
     w.nsh = c->nsh;
     w.nao = c->nao;
@@ -669,7 +673,7 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
   if (c->has_d4) {  // non-self-consistent energies: repulsion + three-body dispersion
     std::vector<double> h_e3;
     w.d4_e3.download(h_e3, nat, s);
-    cuda_check(cudaStreamSynchronize(s), "sync e3");
+    stream_wait(s);
     for (int i = 0; i < nat; ++i) h_erep[i] += h_e3[i];
   }
   std::vector<int> h_cnt(1);
@@ -687,7 +691,7 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
       launch_broyden_next(b, s);
       int st = 0;
       cuda_check(cudaMemcpyAsync(&st, w.b_status.p, sizeof(int), cudaMemcpyDeviceToHost, s), "st");
-      cuda_check(cudaStreamSynchronize(s), "sync");
+      stream_wait(s);
       if (st != 0) throw std::runtime_error("Broyden mixing failed to obtain next iteration");
       launch_unpack(m, w.b_q.p, w.qsh.p, w.qat.p, w.dpat.p, w.qpat.p, s);
       g_prof.end(s);
@@ -710,7 +714,7 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
                                std::to_string(info));
     launch_fermi(n, w.emo.p, nalp, nbet, kt, w.focc.p, w.scal.p, w.icount.p, s);
     w.icount.download(h_cnt, 1, s);
-    cuda_check(cudaStreamSynchronize(s), "sync");
+    stream_wait(s);
     eigen_vectors(w.eig, h_cnt[0], w.C.p);
     g_prof.end(s);
     g_prof.begin(PH_DENSITY, s);
@@ -728,7 +732,7 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
     g_prof.end(s);
     w.eelec.download(h_eelec, nat, s);
     w.scal.download(h_scal, 2, s);
-    cuda_check(cudaStreamSynchronize(s), "sync");
+    stream_wait(s);
     eelec_sum = 0.0;
     for (int i = 0; i < nat; ++i) eelec_sum += h_eelec[i];
     const bool econv_ok = fabs(eelec_sum - elast) < econv;
@@ -783,7 +787,8 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
     w.H.download(res->H, (size_t)n * n, s);
   }
   g_prof.end(s);
-  cuda_check(cudaStreamSynchronize(s), "sync results");
+  stream_wait(s);
+  cuda_check(cudaGetLastError(), "results");
   g_prof.collect();
   g_prof.iterations = iscf;
   res->sigma.assign(9, 0.0);

@@ -43,7 +43,14 @@ struct EigenSolver {
   int* status = nullptr;  // device
   int* hstatus = nullptr; // pinned
   int coop_blocks = 0;
+  int cap = 0;  // buffers hold problems up to this order
 };
+
+int eigen_capacity(const EigenSolver* e) { return e ? e->cap : 0; }
+void eigen_resize(EigenSolver* e, int n) {
+  if (n > e->cap) throw std::runtime_error("eigen solver capacity exceeded");
+  e->n = n;
+}
 
 // ------------------------------------------------------------------------------------------
 // Householder tridiagonalisation of the symmetric A (column-major, full storage), lower form
@@ -179,6 +186,113 @@ __global__ void __launch_bounds__(256) k_tridiag(int n, double* A, double* d, do
   if (n == 1 && gwarp == 0 && lane == 0) d[0] = A[0];
 }
 
+constexpr size_t TRIDIAG_SMEM_MAX = 200 * 1024;
+
+// Shared-memory resident variant for n where every block can hold its columns: global column j
+// lives in block j % nb (slot j / nb) for the whole reduction, so the symmetric matrix-vector
+// product, the rank-2 update and the next reflector read and write shared memory only; just the
+// reflector v and the product p travel through L2.  Two grid barriers per column.
+__global__ void __launch_bounds__(256) k_tridiag_smem(int n, double* A, double* d, double* e,
+                                                      double* tau, double* vbuf, double* pbuf) {
+  cg::grid_group grid = cg::this_grid();
+  extern __shared__ double sm[];
+  const int nb = gridDim.x, b = blockIdx.x;
+  const int ncpb = (n + nb - 1) / nb;
+  double* scol = sm;                    // [ncpb][n]
+  double* sv = sm + (size_t)ncpb * n;   // [n]  reflector of the current step
+  double* sp = sv + n;                  // [n]  p of the current step
+  __shared__ double red[32];
+  __shared__ double sK;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwb = blockDim.x >> 5;
+  // load owned columns
+  for (int s = 0; s < ncpb; ++s) {
+    const int j = b + s * nb;
+    if (j >= n) break;
+    for (int r = threadIdx.x; r < n; r += blockDim.x) scol[(size_t)s * n + r] = A[r + (size_t)j * n];
+  }
+  __syncthreads();
+  // owner of column i builds reflector i from its shared copy and publishes it
+  auto reflector = [&](int i) {
+    double* col = scol + (size_t)(i / nb) * n;
+    const double alpha = col[i + 1];
+    double s = 0.0;
+    for (int r = i + 2 + threadIdx.x; r < n; r += blockDim.x) s += col[r] * col[r];
+    s = block_sum256(s, red);
+    double t = 0.0, beta = alpha;
+    if (s > 0.0) {
+      beta = -copysign(sqrt(alpha * alpha + s), alpha);
+      t = (beta - alpha) / beta;
+    }
+    const double sc = s > 0.0 ? 1.0 / (alpha - beta) : 0.0;
+    for (int r = i + 2 + threadIdx.x; r < n; r += blockDim.x) {
+      const double v = col[r] * sc;
+      col[r] = v;
+      vbuf[r] = v;
+      A[r + (size_t)i * n] = v;
+    }
+    if (threadIdx.x == 0) {
+      vbuf[i + 1] = 1.0;
+      tau[i] = t;
+      e[i] = beta;
+      d[i] = col[i];
+    }
+  };
+  if (n > 1 && b == 0) reflector(0);
+  if (n == 1 && b == 0 && threadIdx.x == 0) d[0] = scol[0];
+  grid.sync();
+  for (int i = 0; i < n - 1; ++i) {
+    const int m = n - i - 1;
+    const double t = tau[i];
+    // copy v (rows i+1..n-1) into shared memory
+    for (int r = i + 1 + threadIdx.x; r < n; r += blockDim.x) sv[r] = vbuf[r];
+    __syncthreads();
+    // p_j = t * A(i+1:n, j) . v for owned columns j > i
+    for (int s = wid; s < ncpb; s += nwb) {
+      const int j = b + s * nb;
+      if (j <= i || j >= n) continue;
+      const double* col = scol + (size_t)s * n;
+      double acc = 0.0;
+      for (int r = i + 1 + lane; r < n; r += 32) acc += col[r] * sv[r];
+      acc = wred(acc) * t;
+      if (lane == 0) {
+        pbuf[j] = acc;
+        pbuf[n + j] = acc * sv[j];
+      }
+    }
+    grid.sync();
+    // K = -1/2 t (p . v), same order in every block
+    {
+      double s = 0.0;
+      for (int r = i + 1 + threadIdx.x; r < n; r += blockDim.x) {
+        sp[r] = pbuf[r];
+        s += pbuf[n + r];
+      }
+      s = block_sum256(s, red);
+      if (threadIdx.x == 0) sK = -0.5 * t * s;
+      __syncthreads();
+    }
+    const double K = sK;
+    if (t != 0.0) {
+      for (int s = 0; s < ncpb; ++s) {
+        const int j = b + s * nb;
+        if (j <= i || j >= n) continue;
+        double* col = scol + (size_t)s * n;
+        const double vc = sv[j], wc = sp[j] + K * vc;
+        for (int r = i + 1 + threadIdx.x; r < n; r += blockDim.x) {
+          const double vr = sv[r];
+          col[r] -= vr * wc + (sp[r] + K * vr) * vc;
+        }
+      }
+    }
+    __syncthreads();
+    if ((i + 1) % nb == b) {
+      if (i + 1 < n - 1) reflector(i + 1);
+      else if (threadIdx.x == 0) d[n - 1] = scol[(size_t)((n - 1) / nb) * n + (n - 1)];
+    }
+    grid.sync();
+  }
+}
+
 // ------------------------------------------------------------------------------------------
 // eigenvalues of T by bisection on the Sturm count (one thread per eigenvalue, ascending)
 // ------------------------------------------------------------------------------------------
@@ -271,18 +385,34 @@ __global__ void __launch_bounds__(64) k_multisect(int n, const double* __restric
   for (int it = 0; it < 64; ++it) {
     const bool done = !active || hi - lo <= 2.0 * 2.220446049250313e-16 * fmax(fabs(lo), fabs(hi)) + 4.0 * pivmin;
     if (__all_sync(0xffffffffu, done)) break;
+    // four interior points per eigenvalue (a 5-way split).  Sturm count from the determinant
+    // recurrence p_i = (d_i - x) p_{i-1} - e_{i-1}^2 p_{i-2}: the number of sign changes equals
+    // the number of eigenvalues below x.  Division free; the pair (p_{i-1}, p_i) is rescaled by
+    // a power of two every 8 steps, and an exact zero takes the sign opposite to its
+    // predecessor (the limit of the quotient form with a negative pivot).
+    (void)pivmin;
     const double step = (hi - lo) * 0.2;
     const double x = lo + (sub + 1) * step;
     int cnt = 0;
     if (!done) {
-      double q = d[0] - x;
-      if (fabs(q) < pivmin) q = -pivmin;
-      cnt += q < 0.0;
+      double p0 = 1.0, p1 = d[0] - x;
+      if (p1 == 0.0) p1 = -0x1p-900;
+      cnt += p1 < 0.0;
       for (int i = 1; i < n; ++i) {
         const double ee = e[i - 1];
-        q = d[i] - x - (ee * ee) * frcp(q);
-        if (fabs(q) < pivmin) q = -pivmin;
-        cnt += q < 0.0;
+        double p2 = fma(d[i] - x, p1, -(ee * ee) * p0);
+        if (p2 == 0.0) p2 = -copysign(0x1p-900, p1);
+        cnt += (p2 < 0.0) != (p1 < 0.0);
+        p0 = p1;
+        p1 = p2;
+        if ((i & 7) == 0) {
+          const double a = fabs(p1);
+          if (a > 0x1p400 || a < 0x1p-400) {
+            const int ex = ilogb(a);
+            p1 = scalbn(p1, -ex);
+            p0 = scalbn(p0, -ex);
+          }
+        }
       }
     }
     // gather the four counts of this eigenvalue's group
@@ -526,19 +656,29 @@ __global__ void k_clusters(int n, int k, const double* __restrict__ d,
 constexpr int BT_WARPS = 4;
 constexpr int BT_CHUNK_MAX = 16;
 constexpr size_t BT_SMEM_MAX = 200 * 1024;
+// the columns live in shared memory too when at least two reflectors fit beside them
+static bool bt_ysmem(int n) {
+  return (int)(BT_SMEM_MAX / (sizeof(double) * (size_t)n)) - BT_WARPS >= 2;
+}
 static int bt_chunk(int n) {
-  int c = (int)(BT_SMEM_MAX / (sizeof(double) * (size_t)n));
+  int c = (int)(BT_SMEM_MAX / (sizeof(double) * (size_t)n)) - (bt_ysmem(n) ? BT_WARPS : 0);
   return c < 1 ? 1 : (c > BT_CHUNK_MAX ? BT_CHUNK_MAX : c);
 }
+static size_t bt_smem(int n) {
+  return sizeof(double) * (size_t)n * (bt_chunk(n) + (bt_ysmem(n) ? BT_WARPS : 0));
+}
 
-__global__ void __launch_bounds__(BT_WARPS * 32) k_backtransform(int n, int k, int chunk,
+__global__ void __launch_bounds__(BT_WARPS * 32) k_backtransform(int n, int k, int chunk, bool ysmem,
                                                                  const double* __restrict__ A,
                                                                  const double* __restrict__ tau,
                                                                  double* Y) {
-  extern __shared__ double smem[];  // [chunk][n]
+  extern __shared__ double smem[];  // [chunk][n] reflectors, then [BT_WARPS][n] columns
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int col = blockIdx.x * BT_WARPS + wid;
-  double* y = col < k ? Y + (size_t)col * n : nullptr;
+  double* yg = col < k ? Y + (size_t)col * n : nullptr;
+  double* y = !yg ? nullptr : (ysmem ? smem + (size_t)chunk * n + (size_t)wid * n : yg);
+  if (y && ysmem)
+    for (int r = lane; r < n; r += 32) y[r] = yg[r];
   // reflectors i = n-2 .. 0 ; reflector i acts on rows i+1..n-1, v[0] = 1
   for (int top = n - 2; top >= 0; top -= chunk) {
     const int bot = max(0, top - chunk + 1);
@@ -562,12 +702,15 @@ __global__ void __launch_bounds__(BT_WARPS * 32) k_backtransform(int n, int k, i
       }
     }
   }
+  if (y && ysmem)
+    for (int r = lane; r < n; r += 32) yg[r] = y[r];
 }
 
 // ------------------------------------------------------------------------------------------
 EigenSolver* eigen_create(int n, cudaStream_t s) {
   auto* e = new EigenSolver();
   e->n = n;
+  e->cap = n;
   e->stream = s;
   const size_t nn = (size_t)n * n;
   ck(cudaMalloc(&e->L, sizeof(double) * nn), "L");
@@ -580,7 +723,7 @@ EigenSolver* eigen_create(int n, cudaStream_t s) {
   ck(cudaMalloc(&e->e, sizeof(double) * (n + 1)), "e");
   ck(cudaMalloc(&e->tau, sizeof(double) * (n + 1)), "tau");
   ck(cudaMalloc(&e->w, sizeof(double) * (n + 1)), "w");
-  ck(cudaMalloc(&e->pv, sizeof(double) * 2 * (n + 1)), "pv");
+  ck(cudaMalloc(&e->pv, sizeof(double) * 4 * (n + 1)), "pv");
   ck(cudaMalloc(&e->scal, sizeof(double) * 8), "scal");
   ck(cudaMalloc(&e->status, sizeof(int)), "status");
   ck(cudaMallocHost(&e->hstatus, sizeof(int)), "hstatus");
@@ -591,8 +734,11 @@ EigenSolver* eigen_create(int n, cudaStream_t s) {
   (void)per_sm;
   e->coop_blocks = nsm;  // one block per SM keeps the grid barrier cheap
   // shared memory of the back-transformation
+  ck(cudaFuncSetAttribute(k_tridiag_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          (int)TRIDIAG_SMEM_MAX),
+     "smem attr tridiag");
   ck(cudaFuncSetAttribute(k_backtransform, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                          (int)(sizeof(double) * bt_chunk(n) * n)),
+                          (int)BT_SMEM_MAX + (int)(BT_WARPS * sizeof(double) * 64)),
      "smem attr");
   return e;
 }
@@ -627,9 +773,21 @@ int eigen_values(EigenSolver* es, const double* F, double* w_out) {
     int blocks = es->coop_blocks;
     const int need = (n * 32 + 255) / 256;
     if (blocks > need) blocks = need > 0 ? need : 1;
-    void* args[] = {&nn, &es->A, &es->d, &es->e, &es->tau, &es->pv, &es->scal};
-    ++g_kernel_launches;
-    ck(cudaLaunchCooperativeKernel((void*)k_tridiag, blocks, 256, args, 0, s), "tridiag");
+    // shared-memory resident path when every block can hold its columns
+    int nb = blocks;
+    const size_t ncpb = (n + nb - 1) / nb;
+    const size_t smem = sizeof(double) * (ncpb * n + 2 * (size_t)n);
+    if (smem <= TRIDIAG_SMEM_MAX) {
+      double* vbuf = es->pv;
+      double* pbuf = es->pv + (n + 1);
+      void* args[] = {&nn, &es->A, &es->d, &es->e, &es->tau, &vbuf, &pbuf};
+      ++g_kernel_launches;
+      ck(cudaLaunchCooperativeKernel((void*)k_tridiag_smem, nb, 256, args, smem, s), "tridiag_smem");
+    } else {
+      void* args[] = {&nn, &es->A, &es->d, &es->e, &es->tau, &es->pv, &es->scal};
+      ++g_kernel_launches;
+      ck(cudaLaunchCooperativeKernel((void*)k_tridiag, blocks, 256, args, 0, s), "tridiag");
+    }
   }
   ++g_kernel_launches;
   k_multisect<<<(4 * n + 63) / 64, 64, 0, s>>>(n, es->d, es->e, es->w, es->scal);
@@ -646,10 +804,9 @@ void eigen_vectors(EigenSolver* es, int k, double* C) {
   ++g_kernel_launches;
   k_clusters<<<k, 256, 0, s>>>(n, k, es->d, es->e, es->w, es->scal, 1e-5, es->Y);
   const int chunk = bt_chunk(n);
-  const size_t smem = sizeof(double) * chunk * n;
   ++g_kernel_launches;
-  k_backtransform<<<(k + BT_WARPS - 1) / BT_WARPS, BT_WARPS * 32, smem, s>>>(n, k, chunk, es->A,
-                                                                           es->tau, es->Y);
+  k_backtransform<<<(k + BT_WARPS - 1) / BT_WARPS, BT_WARPS * 32, bt_smem(n), s>>>(
+      n, k, chunk, bt_ysmem(n), es->A, es->tau, es->Y);
   // C = X Y (X upper triangular)
   gemm64(false, false, n, k, n, 1.0, es->X, n, es->Y, n, 0.0, C, n, KM_GE_ROWBEG, s);
 }

@@ -11,6 +11,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -18,7 +19,10 @@
 namespace tb {
 
 // number of engine kernels launched since library load (instrumentation)
-extern unsigned long long g_kernel_launches;
+extern std::atomic<unsigned long long> g_kernel_launches;
+
+// wait for the stream with a blocking-sync event (the host thread sleeps instead of spinning)
+void stream_wait(cudaStream_t s);
 
 constexpr int MAXG = 12;    // max primitives per shell
 constexpr int MAXL = 2;     // max angular momentum handled by the kernels
@@ -161,6 +165,9 @@ void launch_diff(int ndim, const double* vec_out, const double* q, double* dq, d
 struct EigenSolver;
 EigenSolver* eigen_create(int n, cudaStream_t s);
 void eigen_destroy(EigenSolver*);
+// largest order the solver's buffers hold; eigen_resize switches to any order up to it
+int eigen_capacity(const EigenSolver*);
+void eigen_resize(EigenSolver*, int n);
 // factorise S once per geometry; returns 0 on success, >0 if S is not positive definite
 int eigen_set_overlap(EigenSolver*, const double* S);
 // all eigenvalues (ascending) of F C = S C e; keeps the tridiagonal form for eigen_vectors

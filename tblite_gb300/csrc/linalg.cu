@@ -166,7 +166,89 @@ __global__ void k_tri_inv_t(int n, const double* __restrict__ L, double* X) {
   }
 }
 
+// Shared-memory resident Cholesky: column j lives in block j % nb for the whole factorisation.
+// Step j: the owner scales its column and publishes it (double-buffered by parity of j), one
+// grid barrier, every block updates its own trailing columns from the published column.
+constexpr size_t CHOL_SMEM_MAX = 200 * 1024;
+
+__global__ void __launch_bounds__(256) k_cholesky_smem(int n, double* A, double* buf, int* status) {
+  cg::grid_group grid = cg::this_grid();
+  extern __shared__ double sm[];
+  const int nb = gridDim.x, b = blockIdx.x;
+  const int ncpb = (n + nb - 1) / nb;
+  double* scol = sm;                   // [ncpb][n]
+  double* sl = sm + (size_t)ncpb * n;  // [n] published column
+  for (int s = 0; s < ncpb; ++s) {
+    const int j = b + s * nb;
+    if (j >= n) break;
+    for (int r = threadIdx.x; r < n; r += blockDim.x) scol[(size_t)s * n + r] = A[r + (size_t)j * n];
+  }
+  if (b == 0 && threadIdx.x == 0) *status = 0;
+  __syncthreads();
+  grid.sync();
+  for (int j = 0; j < n; ++j) {
+    double* pub = buf + (size_t)(j & 1) * n;
+    if (j % nb == b) {
+      double* col = scol + (size_t)(j / nb) * n;
+      const double piv = col[j];
+      if (!(piv > 0.0)) {
+        if (threadIdx.x == 0) *status = j + 1;
+      } else {
+        const double dd = sqrt(piv), inv = 1.0 / dd;
+        for (int r = j + threadIdx.x; r < n; r += blockDim.x) {
+          const double v = r == j ? dd : col[r] * inv;
+          col[r] = v;
+          pub[r] = v;
+          A[r + (size_t)j * n] = v;
+        }
+        for (int r = threadIdx.x; r < j; r += blockDim.x) A[r + (size_t)j * n] = 0.0;
+      }
+    }
+    grid.sync();
+    if (*(volatile int*)status != 0) return;  // every block sees the same flag
+    for (int r = j + 1 + threadIdx.x; r < n; r += blockDim.x) sl[r] = pub[r];
+    __syncthreads();
+    for (int s = 0; s < ncpb; ++s) {
+      const int c = b + s * nb;
+      if (c <= j || c >= n) continue;
+      double* col = scol + (size_t)s * n;
+      const double lcj = sl[c];
+      for (int r = c + threadIdx.x; r < n; r += blockDim.x) col[r] -= sl[r] * lcj;
+    }
+    __syncthreads();
+  }
+}
+
 int cholesky_inverse(int n, double* L, double* X, int* d_status, int* h_status, cudaStream_t s) {
+  {
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    int nb = nsm;
+    const int need = (n + 7) / 8;  // at least 8 columns per block
+    if (nb > need) nb = need > 0 ? need : 1;
+    const size_t ncpb = (n + nb - 1) / nb;
+    const size_t smem = sizeof(double) * (ncpb + 1) * (size_t)n;
+    if (smem <= CHOL_SMEM_MAX) {
+      static bool attr = false;
+      if (!attr) {
+        cudaFuncSetAttribute(k_cholesky_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)CHOL_SMEM_MAX);
+        attr = true;
+      }
+      double* buf = X;  // X is written after the factorisation; use it as the publish buffer
+      void* args[] = {&n, &L, &buf, &d_status};
+      ++g_kernel_launches;
+      cudaError_t e = cudaLaunchCooperativeKernel((void*)k_cholesky_smem, nb, 256, args, smem, s);
+      if (e != cudaSuccess) return -1;
+      cudaMemcpyAsync(h_status, d_status, sizeof(int), cudaMemcpyDeviceToHost, s);
+      stream_wait(s);
+      if (*h_status != 0) return *h_status;
+      ++g_kernel_launches;
+      k_tri_inv_t<<<(n * 32 + 255) / 256, 256, 0, s>>>(n, L, X);
+      return 0;
+    }
+  }
   int dev = 0, nsm = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -180,7 +262,7 @@ int cholesky_inverse(int n, double* L, double* X, int* d_status, int* h_status, 
   cudaError_t e = cudaLaunchCooperativeKernel((void*)k_cholesky, blocks, 256, args, 0, s);
   if (e != cudaSuccess) return -1;
   cudaMemcpyAsync(h_status, d_status, sizeof(int), cudaMemcpyDeviceToHost, s);
-  cudaStreamSynchronize(s);
+  stream_wait(s);
   if (*h_status != 0) return *h_status;
   ++g_kernel_launches;
   k_chol_scale<<<n, 256, 0, s>>>(n, L);

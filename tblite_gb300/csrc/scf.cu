@@ -21,7 +21,14 @@
 
 namespace tb {
 
-unsigned long long g_kernel_launches = 0;
+std::atomic<unsigned long long> g_kernel_launches{0};
+
+void stream_wait(cudaStream_t s) {
+  thread_local cudaEvent_t ev = nullptr;
+  if (!ev) cudaEventCreateWithFlags(&ev, cudaEventBlockingSync | cudaEventDisableTiming);
+  cudaEventRecord(ev, s);
+  cudaEventSynchronize(ev);
+}
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
