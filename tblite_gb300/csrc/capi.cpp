@@ -770,7 +770,13 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
                      w.dEdcn.p, s);
   launch_cn_grad(m, p, w.dEdcn.p, w.grad.p, w.sig_at.p, s);
   g_prof.end(s);
+  // the result carries every orbital (wavefunction/type.f90 coeff(nao, nao)): the SCF only
+  // needed the occupied ones, the empty ones come from the last tridiagonal form
+  g_prof.begin(PH_EIGEN, s);
+  eigen_vectors_range(w.eig, h_cnt[0], (int)n, w.C.p);
+  g_prof.end(s);
   g_prof.begin(PH_TRANSFER, s);
+  w.C.download(res->C, (size_t)n * n, s);
   w.grad.download(res->gradient, 3 * nat, s);
   std::vector<double> h_sig_at, h_sigma;
   w.sig_at.download(h_sig_at, 9 * nat, s);

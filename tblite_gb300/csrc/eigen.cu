@@ -451,10 +451,10 @@ __device__ __forceinline__ double hash_uniform(unsigned a, unsigned b) {
   return (double)h / 4294967296.0 * 2.0 - 1.0;
 }
 
-__global__ void k_invit(int n, int k, const double* __restrict__ d, const double* __restrict__ e,
-                        const double* __restrict__ w, const double* __restrict__ scal, double* lu,
-                        double* Y) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void k_invit(int n, int k0, int k, const double* __restrict__ d,
+                        const double* __restrict__ e, const double* __restrict__ w,
+                        const double* __restrict__ scal, double* lu, double* Y) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;  // vector k0 + j of the spectrum
   if (j >= k) return;
   const size_t nk = (size_t)n * k;
   double* U0 = lu;
@@ -463,7 +463,7 @@ __global__ void k_invit(int n, int k, const double* __restrict__ d, const double
   double* Lm = lu + 3 * nk;
   double* PV = lu + 4 * nk;  // pivot flag stored as double
 #define AT(arr, r) arr[(size_t)(r) * k + j]
-  const double lam = w[j];
+  const double lam = w[k0 + j];
   const double tnorm = scal[1] > 0 ? scal[1] : 1.0;
   const double tiny = 2.220446049250313e-16 * tnorm;
   // factorise T - lam I
@@ -489,8 +489,8 @@ __global__ void k_invit(int n, int k, const double* __restrict__ d, const double
   }
   if (fabs(u0) < tiny) u0 = copysign(tiny, u0 == 0.0 ? 1.0 : u0);
   AT(U0, n - 1) = u0; AT(U1, n - 1) = 0.0; AT(U2, n - 1) = 0.0;
-  double* y = Y + (size_t)j * n;
-  for (int r = 0; r < n; ++r) y[r] = hash_uniform(j + 1, r + 1);
+  double* y = Y + (size_t)(k0 + j) * n;
+  for (int r = 0; r < n; ++r) y[r] = hash_uniform(k0 + j + 1, r + 1);
   for (int iter = 0; iter < 2; ++iter) {
     // forward: apply row operations to the right-hand side
     for (int r = 0; r < n - 1; ++r) {
@@ -523,13 +523,13 @@ __global__ void k_invit(int n, int k, const double* __restrict__ d, const double
 // with T inside the cluster (Jacobi on the small projected matrix).  One block per cluster
 // start; vectors of a cluster are consecutive columns of Y.
 constexpr int MAXCL = 32;
-__global__ void k_clusters(int n, int k, const double* __restrict__ d,
+__global__ void k_clusters(int n, int k0, int k, const double* __restrict__ d,
                            const double* __restrict__ e, const double* __restrict__ w,
                            const double* __restrict__ scal, double tolrel, double* Y) {
-  const int j0 = blockIdx.x;
+  const int j0 = k0 + blockIdx.x;  // clusters are looked for among vectors k0 .. k-1
   if (j0 >= k) return;
   const double tol = tolrel * (scal[1] > 0 ? scal[1] : 1.0);
-  if (j0 > 0 && w[j0] - w[j0 - 1] < tol) return;  // not a cluster start
+  if (j0 > k0 && w[j0] - w[j0 - 1] < tol) return;  // not a cluster start
   int c = 1;
   while (j0 + c < k && w[j0 + c] - w[j0 + c - 1] < tol) ++c;
   if (c == 1) return;
@@ -795,21 +795,25 @@ int eigen_values(EigenSolver* es, const double* F, double* w_out) {
   return 0;
 }
 
-void eigen_vectors(EigenSolver* es, int k, double* C) {
+void eigen_vectors_range(EigenSolver* es, int k0, int k1, double* C) {
   const int n = es->n;
   cudaStream_t s = es->stream;
+  const int k = k1 - k0;
   if (k <= 0) return;
   ++g_kernel_launches;
-  k_invit<<<(k + 15) / 16, 16, 0, s>>>(n, k, es->d, es->e, es->w, es->scal, es->lu, es->Y);
+  k_invit<<<(k + 15) / 16, 16, 0, s>>>(n, k0, k, es->d, es->e, es->w, es->scal, es->lu, es->Y);
   ++g_kernel_launches;
-  k_clusters<<<k, 256, 0, s>>>(n, k, es->d, es->e, es->w, es->scal, 1e-5, es->Y);
+  k_clusters<<<k, 256, 0, s>>>(n, k0, k1, es->d, es->e, es->w, es->scal, 1e-5, es->Y);
   const int chunk = bt_chunk(n);
+  double* Yk = es->Y + (size_t)k0 * n;
   ++g_kernel_launches;
   k_backtransform<<<(k + BT_WARPS - 1) / BT_WARPS, BT_WARPS * 32, bt_smem(n), s>>>(
-      n, k, chunk, bt_ysmem(n), es->A, es->tau, es->Y);
+      n, k, chunk, bt_ysmem(n), es->A, es->tau, Yk);
   // C = X Y (X upper triangular)
-  gemm64(false, false, n, k, n, 1.0, es->X, n, es->Y, n, 0.0, C, n, KM_GE_ROWBEG, s);
+  gemm64(false, false, n, k, n, 1.0, es->X, n, Yk, n, 0.0, C + (size_t)k0 * n, n, KM_GE_ROWBEG, s);
 }
+
+void eigen_vectors(EigenSolver* es, int k, double* C) { eigen_vectors_range(es, 0, k, C); }
 
 // P = sum_{m<k} f_m C_m C_m^T: scale columns into work, then one GEMM
 __global__ void k_scale_cols(int n, int k, const double* C, const double* f, double* out) {

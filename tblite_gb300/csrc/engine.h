@@ -174,6 +174,8 @@ int eigen_set_overlap(EigenSolver*, const double* S);
 int eigen_values(EigenSolver*, const double* F, double* e);
 // the k lowest eigenvectors, C column-major [k][n] (S-orthonormal)
 void eigen_vectors(EigenSolver*, int k, double* C);
+// eigenvectors k0 .. k1-1 into columns k0 .. k1-1 of C (same tridiagonal form)
+void eigen_vectors_range(EigenSolver*, int k0, int k1, double* C);
 
 // dense FP64 GEMM (column-major, BLAS semantics); kmode skips zero triangles
 enum { KM_NONE = 0, KM_LT_COLEND = 1, KM_LT_ROWEND = 2, KM_GE_ROWBEG = 3 };
