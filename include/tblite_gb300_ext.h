@@ -24,6 +24,35 @@ void tblite_gb300_set_profiling(int enable);
 int tblite_gb300_get_profile(double* phase_ms, int* phase_count, int nphase, double* total_ms,
                              int* iterations);
 
+/* number of engine kernels launched since the library was loaded (all threads) */
+unsigned long long tblite_gb300_get_launch_count(void);
+
+/*
+ * Density matrix P = C diag(f) C^T that allocates no device memory.  No counterpart in the
+ * reference: it is the engine's density step (scf/diag.f90 get_density_matrix) for callers
+ * that cannot allocate device memory when they need it, because a pool allocator already
+ * owns the device or because cudaMalloc/cudaFree would synchronise the device on a
+ * latency-bound loop.
+ *
+ *   n       number of orbitals (rows of C and order of P)
+ *   k       number of leading columns of C that enter (0 <= k <= n)
+ *   C       device pointer, column-major [k][n]: C[m*n + r] = coefficient of AO r in orbital m
+ *   f       device pointer, occupations [k]
+ *   P       device pointer, output [n][n] (symmetric)
+ *   stream  cudaStream_t to launch on (NULL: the legacy default stream)
+ *
+ * Returns 0 on success, -1 for an invalid argument, -2 when n*k exceeds
+ * tblite_gb300_density_matrix_noalloc_max() (nothing is launched), -3 for a CUDA error.
+ * The workspace is one fixed device array per device inside the library (2^19 doubles,
+ * 4 MiB).  The first call on a device looks up its address with that device current; make
+ * that first call before starting any stream capture.  Calls that may overlap in time on
+ * one device (other streams or threads) race on the array and must be serialised.
+ */
+int tblite_gb300_density_matrix_noalloc(int n, int k, const double* C, const double* f, double* P,
+                                        void* stream);
+/* largest n*k the fixed workspace of tblite_gb300_density_matrix_noalloc holds */
+int tblite_gb300_density_matrix_noalloc_max(void);
+
 #ifdef __cplusplus
 }
 #endif
