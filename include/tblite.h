@@ -27,6 +27,10 @@ extern "C" {
 #include <stdbool.h>
 #endif
 
+#ifdef TBLITE_CFFI /* cffi parses the preprocessed header: plain declarations */
+#define TBLITE_API_ENTRY
+#define TBLITE_API_CALL
+#endif
 #ifndef TBLITE_API_ENTRY
 #define TBLITE_API_ENTRY extern
 #endif

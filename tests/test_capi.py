@@ -26,6 +26,28 @@ def test_header_symbols_exported(lib):
     assert not missing, missing
 
 
+def test_header_parses_with_cffi(lib):
+    """The reference's Python package binds the preprocessed header with cffi."""
+    import shutil
+    import subprocess
+
+    cffi = pytest.importorskip("cffi")
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C preprocessor")
+    src = subprocess.run([cc, "-E", "-P", "-DTBLITE_CFFI", str(ROOT / "include" / "tblite.h")],
+                         capture_output=True, text=True, check=True).stdout
+    ffi = cffi.FFI()
+    ffi.cdef(src)
+    clib = ffi.dlopen(str(library.library_path()))
+    assert clib.tblite_get_version() == lib.tblite_get_version()
+    err = clib.tblite_new_error()
+    assert clib.tblite_check_error(err) == 0
+    perr = ffi.new("tblite_error *", err)
+    clib.tblite_delete_error(perr)
+    assert perr[0] == ffi.NULL
+
+
 def test_error_roundtrip(lib):
     err = c_void_p(lib.tblite_new_error())
     assert lib.tblite_check_error(err) == 0
