@@ -35,7 +35,8 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "GFN2 energy+force evals/sec"
 WORKLOADS = {"c200h402": "C200H402 GFN2-xTB energy+gradient single point (602 atoms, 1202 AOs)",
-             "h2o32": "(H2O)32 GFN2-xTB energy+gradient single point (96 atoms, 192 AOs)"}
+             "h2o32": "(H2O)32 GFN2-xTB energy+gradient single point (96 atoms, 192 AOs)",
+             "c100h202": "C100H202 GFN2-xTB energy+gradient single point (302 atoms, 602 AOs)"}
 
 
 def _dist():
@@ -98,6 +99,70 @@ def _peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
+def _fp64_peak(torch):
+    """FP64 peak of this GPU, measured here: best of 5 cuBLAS DGEMMs (4096^3, CUDA events).
+    The generated peaks file holds HBM and bf16 figures only."""
+    a = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+    b = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+    c = a @ b
+    best = float("inf")
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        c = a @ b
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    del a, b, c
+    return 2.0 * 4096 ** 3 / (best / 1000.0) / 1e12
+
+
+def _profile_traffic(name):
+    """DRAM bytes per launch of a kernel from its committed ncu summary, or None."""
+    path = ROOT / "profiles" / name
+    try:
+        for line in path.read_text().splitlines():
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+def _roofline(kprof, n, ms_step, peaks, peak_kind, fp64_peak):
+    """Roofline of the dominant own kernel (largest summed event time in the step).
+
+    Algorithmic work per launch: Householder tridiagonalisation 4/3 n^3 flop; Fock assembly
+    reads H, S, D(3), Q(6) and writes F = 12 n^2 doubles; Mulliken column sums read P, S, H,
+    D(3), Q(6) = 12 n^2 doubles.  The other slots have data-dependent work and are listed
+    with their times only."""
+    kernels = {k: {"ms_per_launch": round(t / c, 4) if c else None, "launches": c,
+                   "share_of_step": round(t / ms_step, 4) if ms_step else None}
+               for k, (t, c) in kprof.items()}
+    work = {"tridiag": ("fp64", 4.0 / 3.0 * n ** 3, "tridiag_smem_c200h402.md"),
+            "fock": ("hbm", 12.0 * n * n * 8.0, None),
+            "mulliken": ("hbm", 12.0 * n * n * 8.0, None)}
+    dom = max(kprof, key=lambda k: kprof[k][0])
+    pick = dom if dom in work else max(work, key=lambda k: kprof[k][0])
+    t, c = kprof[pick]
+    if not c:
+        return None, kernels
+    bound, units, prof_file = work[pick]
+    ms = t / c
+    if bound == "fp64":
+        achieved = units / (ms / 1000.0) / 1e12
+        peak, unit, src = fp64_peak, "TFLOP/s", "measured in this run (cuBLAS DGEMM 4096^3)"
+    else:
+        achieved = units / (ms / 1000.0) / 1e9
+        peak, unit, src = peaks["hbm_gbs"], "GB/s", peak_kind
+    roof = {"kernel": pick, "dominant_kernel": dom, "bound": bound, "achieved": round(achieved, 4),
+            "peak": round(peak, 4), "unit": unit, "frac": round(achieved / peak, 4),
+            "traffic": _profile_traffic(prof_file) if (prof_file and n == 1202) else None,
+            "peak_source": src, "algorithmic_work_per_launch": units, "ms_per_launch": round(ms, 4),
+            "launches_per_step": c}
+    return roof, kernels
+
+
 def _cpu_baseline(numbers, positions, sample_evals=1):
     """Time the CPU oracle (all host threads) on the same molecule."""
     from oracle import gfn2
@@ -136,6 +201,7 @@ def run_gb300(args):
     numbers, positions = workloads.config(args.config)
     calc = Calculator("GFN2-xTB", numbers, positions)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
+    fp64_peak = _fp64_peak(torch)
     library.set_profiling(True)
     for _ in range(args.warmup):
         calc.singlepoint()
@@ -177,19 +243,8 @@ def run_gb300(args):
     iters = int(np.mean([p["iterations"] for p in profiles]))
     peaks, peak_kind = _peaks()
     n = nao
-    # algorithmic bytes per Fock launch: read H, S, D(3), Q(6) once (11 n^2) + write F (n^2)
-    fock_bytes = 12.0 * n * n * 8.0
-    # Mulliken: read P, S, H, D(3), Q(6) = 12 n^2
-    mull_bytes = 12.0 * n * n * 8.0
-    own = {"fock": (phases["fock"] / max(counts["fock"], 1), fock_bytes),
-           "mulliken": (phases["mulliken"] / max(counts["mulliken"], 1), mull_bytes)}
-    dom = max(own, key=lambda k: phases[k])
-    ms_per, bytes_per = own[dom]
-    achieved = bytes_per / (ms_per / 1000.0) / 1e9
-    roofline = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1),
-                "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4),
-                "traffic": None, "peak_source": peak_kind,
-                "algorithmic_bytes_per_launch": bytes_per, "ms_per_launch": round(ms_per, 4)}
+    kprof = [library.get_kernel_profile() for _ in range(1)]  # last step's per-kernel events
+    roofline, kernels = _roofline(kprof[0], n, dev_sum / args.steps, peaks, peak_kind, fp64_peak)
     cpu_val, cores = _cpu_baseline(numbers, positions) if not args.no_cpu else (None, None)
     h2d = positions.size * 8
     d2h = (1 + nat + 3 * nat + 9 + nat + 2 * n + n * n) * 8 + (res.get("norbitals") * 0)
@@ -205,6 +260,7 @@ def run_gb300(args):
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),
         "roofline": roofline,
+        "kernels": kernels,
         "phase_ms": {k: round(v, 3) for k, v in phases.items()},
         "phase_launches": counts,
         "cpu_baseline": None if cpu_val is None else {

@@ -24,6 +24,12 @@ void tblite_gb300_set_profiling(int enable);
 int tblite_gb300_get_profile(double* phase_ms, int* phase_count, int nphase, double* total_ms,
                              int* iterations);
 
+/* per-kernel device times (ms, summed) and launch counts of the last single point, from CUDA
+ * events around each launch on the engine stream (profiling enabled).  Slots: 0 Householder
+ * tridiagonalisation, 1 eigenvalue multisection, 2 inverse iteration, 3 back-transformation,
+ * 4 FP64 GEMM (all uses), 5 Fock assembly, 6 Mulliken column sums.  Returns the slot count. */
+int tblite_gb300_get_kernel_profile(double* kernel_ms, int* kernel_count, int nslot);
+
 /* number of engine kernels launched since the library was loaded (all threads) */
 unsigned long long tblite_gb300_get_launch_count(void);
 

@@ -517,6 +517,9 @@ struct Profiler {
   double total_ms = 0.0;
   int iterations = 0;
   int open_phase = -1, open_event = -1;
+  std::vector<std::pair<int, std::pair<int, int>>> kmarks;  // kernel slot, (event a, event b)
+  double kernel_ms[KS_COUNT] = {0};
+  int kernel_n[KS_COUNT] = {0};
   cudaEvent_t ev() {
     if (used == (int)pool.size()) {
       cudaEvent_t e;
@@ -528,9 +531,14 @@ struct Profiler {
   void reset() {
     used = 0;
     marks.clear();
+    kmarks.clear();
     for (int k = 0; k < PH_COUNT; ++k) {
       phase_ms[k] = 0.0;
       phase_n[k] = 0;
+    }
+    for (int k = 0; k < KS_COUNT; ++k) {
+      kernel_ms[k] = 0.0;
+      kernel_n[k] = 0;
     }
     total_ms = 0.0;
   }
@@ -548,8 +556,27 @@ struct Profiler {
     marks.push_back({open_phase, {open_event, b}});
     open_phase = -1;
   }
+  int kbegin(cudaStream_t s) {
+    if (!enabled) return -1;
+    const int a = used;
+    cuda_check(cudaEventRecord(ev(), s), "record");
+    return a;
+  }
+  void kend(int slot, int a, cudaStream_t s) {
+    if (!enabled || a < 0) return;
+    const int b = used;
+    cuda_check(cudaEventRecord(ev(), s), "record");
+    kmarks.push_back({slot, {a, b}});
+  }
   void collect() {
     if (!enabled || marks.empty()) return;
+    for (auto& mk : kmarks) {
+      float ms = 0.f;
+      cuda_check(cudaEventElapsedTime(&ms, pool[mk.second.first], pool[mk.second.second]),
+                 "elapsed");
+      kernel_ms[mk.first] += ms;
+      kernel_n[mk.first] += 1;
+    }
     for (auto& mk : marks) {
       float ms = 0.f;
       cuda_check(cudaEventElapsedTime(&ms, pool[mk.second.first], pool[mk.second.second]),
@@ -565,6 +592,10 @@ struct Profiler {
   }
 };
 static Profiler g_prof;
+namespace tb {
+int prof_kbegin(cudaStream_t s) { return g_prof.kbegin(s); }
+void prof_kend(int slot, int token, cudaStream_t s) { g_prof.kend(slot, token, s); }
+}  // namespace tb
 
 static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
                         _tblite_calculator* c, _tblite_result* res) {
@@ -846,6 +877,15 @@ int tblite_gb300_get_profile(double* phase_ms, int* phase_count, int nphase, dou
   if (total_ms) *total_ms = g_prof.total_ms;
   if (iterations) *iterations = g_prof.iterations;
   return PH_COUNT;
+}
+
+int tblite_gb300_get_kernel_profile(double* kernel_ms, int* kernel_count, int nslot) {
+  const int m = std::min(nslot, (int)KS_COUNT);
+  for (int k = 0; k < m; ++k) {
+    if (kernel_ms) kernel_ms[k] = g_prof.kernel_ms[k];
+    if (kernel_count) kernel_count[k] = g_prof.kernel_n[k];
+  }
+  return KS_COUNT;
 }
 
 unsigned long long tblite_gb300_get_launch_count(void) { return g_kernel_launches; }

@@ -32,7 +32,7 @@ __device__ __forceinline__ void d4_count(const DevD4& d, int i, int j, double r,
   dc = -den * d.kn / rc * exp(-arg * arg) * 0.5641895835477563;  // 1/sqrt(pi)
 }
 
-__global__ void k_d4_cn(DevMol m, DevD4 d, double* cn) {
+__device__ __forceinline__ void d4_cn_dev(DevMol m, DevD4 d, double* cn) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (warp >= m.nat) return;
   const int i = warp;
@@ -53,9 +53,12 @@ __global__ void k_d4_cn(DevMol m, DevD4 d, double* cn) {
   acc = wsum(acc);
   if (lane == 0) cn[i] = acc;
 }
+__global__ void k_d4_cn(DevMol m, DevD4 d, double* cn) {
+  d4_cn_dev(m, d, cn);
+}
 
 // Gaussian reference weights in CN and their CN derivative (charge independent part)
-__global__ void k_d4_weights(int nat, DevD4 d, const double* __restrict__ cn, double* gw,
+__device__ __forceinline__ void d4_weights_dev(int nat, DevD4 d, const double* __restrict__ cn, double* gw,
                              double* dgw) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nat) return;
@@ -79,9 +82,13 @@ __global__ void k_d4_weights(int nat, DevD4 d, const double* __restrict__ cn, do
     dgw[i * D4_MREF + r] = r < nr ? dnum[r] / norm - num[r] * dnorm / (norm * norm) : 0.0;
   }
 }
+__global__ void k_d4_weights(int nat, DevD4 d, const double* __restrict__ cn, double* gw,
+                             double* dgw) {
+  d4_weights_dev(nat, d, cn, gw, dgw);
+}
 
 // charge scaling: gwv = gw zeta(q), dgwdq = gw dzeta/dq, dgwv_cn = dgw/dcn zeta(q)
-__global__ void k_d4_zeta(int nat, DevD4 d, const double* __restrict__ q,
+__device__ __forceinline__ void d4_zeta_dev(int nat, DevD4 d, const double* __restrict__ q,
                           const double* __restrict__ gw, const double* __restrict__ dgw,
                           double* gwv, double* dgwdq, double* dgwv_cn) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -106,6 +113,11 @@ __global__ void k_d4_zeta(int nat, DevD4 d, const double* __restrict__ q,
     if (dgwv_cn) dgwv_cn[k] = dgw[k] * zeta;
   }
 }
+__global__ void k_d4_zeta(int nat, DevD4 d, const double* __restrict__ q,
+                          const double* __restrict__ gw, const double* __restrict__ dgw,
+                          double* gwv, double* dgwdq, double* dgwv_cn) {
+  d4_zeta_dev(nat, d, q, gw, dgw, gwv, dgwdq, dgwv_cn);
+}
 
 __device__ __forceinline__ double d4_de(double r2, double rrij, double r0, double s6, double s8,
                                         double& dd) {
@@ -120,7 +132,7 @@ __device__ __forceinline__ double d4_de(double r2, double rrij, double r0, doubl
 // MODE 0: vat += sum_r dgwdq_r u_r ; MODE 1: eat += 1/2 sum_r gwv_r u_r ;
 // MODE 2: gradient at fixed weights + dEdcn (own atom share), per-atom sigma partials
 template <int MODE>
-__global__ void k_d4_pair(DevMol m, DevD4 d, const double* __restrict__ gwv,
+__device__ __forceinline__ void d4_pair_dev(DevMol m, DevD4 d, const double* __restrict__ gwv,
                           const double* __restrict__ dgwdq, const double* __restrict__ dgwv_cn,
                           double* vat, double* eat, double* grad, double* sig_at, double* dEdcn) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
@@ -194,9 +206,15 @@ __global__ void k_d4_pair(DevMol m, DevD4 d, const double* __restrict__ gwv,
     }
   }
 }
+template <int MODE>
+__global__ void k_d4_pair(DevMol m, DevD4 d, const double* __restrict__ gwv,
+                          const double* __restrict__ dgwdq, const double* __restrict__ dgwv_cn,
+                          double* vat, double* eat, double* grad, double* sig_at, double* dEdcn) {
+  d4_pair_dev<MODE>(m, d, gwv, dgwdq, dgwv_cn, vat, eat, grad, sig_at, dEdcn);
+}
 
 // atomic C6 at the given weights and d c6_ij / d cn_i
-__global__ void k_d4_c6(int nat, DevD4 d, const double* __restrict__ gwv,
+__device__ __forceinline__ void d4_c6_dev(int nat, DevD4 d, const double* __restrict__ gwv,
                         const double* __restrict__ dgwv_cn, double* c6, double* dc6) {
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= (long long)nat * nat) return;
@@ -213,11 +231,15 @@ __global__ void k_d4_c6(int nat, DevD4 d, const double* __restrict__ gwv,
   c6[t] = c;
   dc6[t] = dc;
 }
+__global__ void k_d4_c6(int nat, DevD4 d, const double* __restrict__ gwv,
+                        const double* __restrict__ dgwv_cn, double* c6, double* dc6) {
+  d4_c6_dev(nat, d, gwv, dgwv_cn, c6, dc6);
+}
 
 // Axilrod-Teller-Muto term, one warp per atom i, triples (i, j, l) with j < l, both != i.
 // Atom i collects 1/3 of each triple energy, its own force, 1/3 of the virial and the
 // CN derivative through c6_ij and c6_il.
-__global__ void k_d4_atm(DevMol m, DevD4 d, const double* __restrict__ c6,
+__device__ __forceinline__ void d4_atm_dev(DevMol m, DevD4 d, const double* __restrict__ c6,
                          const double* __restrict__ dc6, double* eat, double* grad, double* sig_at,
                          double* dEdcn) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
@@ -295,8 +317,13 @@ __global__ void k_d4_atm(DevMol m, DevD4 d, const double* __restrict__ c6,
     }
   }
 }
+__global__ void k_d4_atm(DevMol m, DevD4 d, const double* __restrict__ c6,
+                         const double* __restrict__ dc6, double* eat, double* grad, double* sig_at,
+                         double* dEdcn) {
+  d4_atm_dev(m, d, c6, dc6, eat, grad, sig_at, dEdcn);
+}
 
-__global__ void k_d4_cn_grad(DevMol m, DevD4 d, const double* __restrict__ dEdcn, double* grad,
+__device__ __forceinline__ void d4_cn_grad_dev(DevMol m, DevD4 d, const double* __restrict__ dEdcn, double* grad,
                              double* sig_at) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (warp >= m.nat) return;
@@ -325,6 +352,10 @@ __global__ void k_d4_cn_grad(DevMol m, DevD4 d, const double* __restrict__ dEdcn
     for (int k = 0; k < 3; ++k) grad[3 * i + k] += g[k];
     for (int k = 0; k < 9; ++k) sig_at[9 * i + k] += sg[k];
   }
+}
+__global__ void k_d4_cn_grad(DevMol m, DevD4 d, const double* __restrict__ dEdcn, double* grad,
+                             double* sig_at) {
+  d4_cn_grad_dev(m, d, dEdcn, grad, sig_at);
 }
 
 static inline unsigned warps_grid(int nat) { return (unsigned)((nat * 32 + 63) / 64); }
@@ -379,5 +410,101 @@ void d4_gradient(const DevMol& m, const DevD4& d, D4Work& w, const double* qat, 
   ++g_kernel_launches;
   k_d4_cn_grad<<<warps_grid(m.nat), 64, 0, s>>>(m, d, w.dEdcn, grad, sig_at);
 }
+
+// ------------------------------------------------------------------------------------
+// batched launches: blockIdx.z walks the listed molecules (molecules without dispersion,
+// i.e. single atoms, leave at once); the D4 dEdcn accumulators start zeroed
+// ------------------------------------------------------------------------------------
+#define BMOL                                  \
+  const MolPtrs& q = mp[list[blockIdx.z]];    \
+  if (!q.has_d4) return
+#define BARGS const MolPtrs* __restrict__ mp, const int* __restrict__ list
+
+__global__ void kb_d4_cn(BARGS) {
+  BMOL;
+  d4_cn_dev(q.m, q.d4, q.d4w.cn);
+}
+__global__ void kb_d4_weights(BARGS) {
+  BMOL;
+  d4_weights_dev(q.m.nat, q.d4, q.d4w.cn, q.d4w.gw, q.d4w.dgw);
+}
+// mode 0: charge-free (setup), 1: potential, 2: energy, 3: gradient
+__global__ void kb_d4_zeta(BARGS, int mode) {
+  BMOL;
+  const D4Work& w = q.d4w;
+  if (mode == 0)
+    d4_zeta_dev(q.m.nat, q.d4, nullptr, w.gw, w.dgw, w.gwv, nullptr, w.dgwv_cn);
+  else if (mode == 1)
+    d4_zeta_dev(q.m.nat, q.d4, q.qat, w.gw, w.dgw, w.gwv, w.dgwdq, nullptr);
+  else if (mode == 2)
+    d4_zeta_dev(q.m.nat, q.d4, q.qat_o, w.gw, w.dgw, w.gwv, nullptr, nullptr);
+  else
+    d4_zeta_dev(q.m.nat, q.d4, q.qat_o, w.gw, w.dgw, w.gwv, nullptr, w.dgwv_cn);
+}
+__global__ void kb_d4_c6(BARGS) {
+  BMOL;
+  d4_c6_dev(q.m.nat, q.d4, q.d4w.gwv, q.d4w.dgwv_cn, q.d4w.c6, q.d4w.dc6);
+}
+__global__ void kb_d4_atm(BARGS) {
+  BMOL;
+  d4_atm_dev(q.m, q.d4, q.d4w.c6, q.d4w.dc6, q.d4w.e3, q.grad, q.sig_at, q.d4w.dEdcn);
+}
+__global__ void kb_d4_pair_pot(BARGS) {
+  BMOL;
+  d4_pair_dev<0>(q.m, q.d4, q.d4w.gwv, q.d4w.dgwdq, nullptr, q.vat, nullptr, nullptr, nullptr,
+                 nullptr);
+}
+__global__ void kb_d4_pair_energy(BARGS) {
+  BMOL;
+  d4_pair_dev<1>(q.m, q.d4, q.d4w.gwv, nullptr, nullptr, nullptr, q.eelec, nullptr, nullptr,
+                 nullptr);
+}
+__global__ void kb_d4_pair_grad(BARGS) {
+  BMOL;
+  d4_pair_dev<2>(q.m, q.d4, q.d4w.gwv, nullptr, q.d4w.dgwv_cn, nullptr, nullptr, q.grad,
+                 q.sig_at, q.d4w.dEdcn);
+}
+__global__ void kb_d4_cn_grad(BARGS) {
+  BMOL;
+  d4_cn_grad_dev(q.m, q.d4, q.d4w.dEdcn, q.grad, q.sig_at);
+}
+
+static inline dim3 bwarps(const BatchLaunch& b) { return dim3(warps_grid(b.nat_max), 1, b.count); }
+static inline dim3 batoms(const BatchLaunch& b) {
+  return dim3((b.nat_max + 127) / 128, 1, b.count);
+}
+
+void d4_setup_b(const BatchLaunch& b) {
+  if (!b.count) return;
+  g_kernel_launches += 5;
+  kb_d4_cn<<<bwarps(b), 64, 0, b.s>>>(b.mp, b.list);
+  kb_d4_weights<<<batoms(b), 128, 0, b.s>>>(b.mp, b.list);
+  kb_d4_zeta<<<batoms(b), 128, 0, b.s>>>(b.mp, b.list, 0);
+  const long long nn = (long long)b.nat_max * b.nat_max;
+  kb_d4_c6<<<dim3((unsigned)((nn + 255) / 256), 1, b.count), 256, 0, b.s>>>(b.mp, b.list);
+  kb_d4_atm<<<bwarps(b), 64, 0, b.s>>>(b.mp, b.list);
+}
+void d4_potential_b(const BatchLaunch& b) {
+  if (!b.count) return;
+  g_kernel_launches += 2;
+  kb_d4_zeta<<<batoms(b), 128, 0, b.s>>>(b.mp, b.list, 1);
+  kb_d4_pair_pot<<<bwarps(b), 64, 0, b.s>>>(b.mp, b.list);
+}
+void d4_energy_b(const BatchLaunch& b) {
+  if (!b.count) return;
+  g_kernel_launches += 2;
+  kb_d4_zeta<<<batoms(b), 128, 0, b.s>>>(b.mp, b.list, 2);
+  kb_d4_pair_energy<<<bwarps(b), 64, 0, b.s>>>(b.mp, b.list);
+}
+void d4_gradient_b(const BatchLaunch& b) {
+  if (!b.count) return;
+  g_kernel_launches += 3;
+  kb_d4_zeta<<<batoms(b), 128, 0, b.s>>>(b.mp, b.list, 3);
+  kb_d4_pair_grad<<<bwarps(b), 64, 0, b.s>>>(b.mp, b.list);
+  kb_d4_cn_grad<<<bwarps(b), 64, 0, b.s>>>(b.mp, b.list);
+}
+
+#undef BMOL
+#undef BARGS
 
 }  // namespace tb

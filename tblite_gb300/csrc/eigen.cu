@@ -358,7 +358,7 @@ __global__ void k_bisect(int n, const double* __restrict__ d, const double* __re
 // the current bracket (a 5-way split per round), so 8 eigenvalues fill a warp and the n
 // eigenvalues spread over all SMs.  The Sturm recurrence uses the correctly rounded FP64
 // reciprocal; the count stays backward stable.
-__global__ void __launch_bounds__(64) k_multisect(int n, const double* __restrict__ d,
+__device__ __forceinline__ void multisect_dev(int n, const double* __restrict__ d,
                                                   const double* __restrict__ e, double* w,
                                                   double* scal) {
   __shared__ double bounds[3];
@@ -434,6 +434,11 @@ __global__ void __launch_bounds__(64) k_multisect(int n, const double* __restric
   if (active && sub == 0) w[j] = 0.5 * (lo + hi);
   if (gt == 0) scal[1] = fmax(fabs(bounds[0]), fabs(bounds[1]));
 }
+__global__ void __launch_bounds__(64) k_multisect(int n, const double* __restrict__ d,
+                                                  const double* __restrict__ e, double* w,
+                                                  double* scal) {
+  multisect_dev(n, d, e, w, scal);
+}
 
 // ------------------------------------------------------------------------------------------
 // inverse iteration: one thread per eigenvector (column j < k), Gaussian elimination with
@@ -451,7 +456,7 @@ __device__ __forceinline__ double hash_uniform(unsigned a, unsigned b) {
   return (double)h / 4294967296.0 * 2.0 - 1.0;
 }
 
-__global__ void k_invit(int n, int k0, int k, const double* __restrict__ d,
+__device__ __forceinline__ void invit_dev(int n, int k0, int k, const double* __restrict__ d,
                         const double* __restrict__ e, const double* __restrict__ w,
                         const double* __restrict__ scal, double* lu, double* Y) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;  // vector k0 + j of the spectrum
@@ -518,12 +523,17 @@ __global__ void k_invit(int n, int k0, int k, const double* __restrict__ d,
   }
 #undef AT
 }
+__global__ void k_invit(int n, int k0, int k, const double* __restrict__ d,
+                        const double* __restrict__ e, const double* __restrict__ w,
+                        const double* __restrict__ scal, double* lu, double* Y) {
+  invit_dev(n, k0, k, d, e, w, scal, lu, Y);
+}
 
 // Clusters of close eigenvalues (gap < tol |T|): modified Gram-Schmidt, then Rayleigh-Ritz
 // with T inside the cluster (Jacobi on the small projected matrix).  One block per cluster
 // start; vectors of a cluster are consecutive columns of Y.
 constexpr int MAXCL = 32;
-__global__ void k_clusters(int n, int k0, int k, const double* __restrict__ d,
+__device__ __forceinline__ void clusters_dev(int n, int k0, int k, const double* __restrict__ d,
                            const double* __restrict__ e, const double* __restrict__ w,
                            const double* __restrict__ scal, double tolrel, double* Y) {
   const int j0 = k0 + blockIdx.x;  // clusters are looked for among vectors k0 .. k-1
@@ -648,6 +658,11 @@ __global__ void k_clusters(int n, int k0, int k, const double* __restrict__ d,
     }
   }
 }
+__global__ void k_clusters(int n, int k0, int k, const double* __restrict__ d,
+                           const double* __restrict__ e, const double* __restrict__ w,
+                           const double* __restrict__ scal, double tolrel, double* Y) {
+  clusters_dev(n, k0, k, d, e, w, scal, tolrel, Y);
+}
 
 // ------------------------------------------------------------------------------------------
 // back-transformation Z = Q Y = H_0 H_1 ... H_{n-2} Y  (apply H_{n-2} first).  Each block owns
@@ -668,7 +683,7 @@ static size_t bt_smem(int n) {
   return sizeof(double) * (size_t)n * (bt_chunk(n) + (bt_ysmem(n) ? BT_WARPS : 0));
 }
 
-__global__ void __launch_bounds__(BT_WARPS * 32) k_backtransform(int n, int k, int chunk, bool ysmem,
+__device__ __forceinline__ void backtransform_dev(int n, int k, int chunk, bool ysmem,
                                                                  const double* __restrict__ A,
                                                                  const double* __restrict__ tau,
                                                                  double* Y) {
@@ -704,6 +719,12 @@ __global__ void __launch_bounds__(BT_WARPS * 32) k_backtransform(int n, int k, i
   }
   if (y && ysmem)
     for (int r = lane; r < n; r += 32) yg[r] = y[r];
+}
+__global__ void __launch_bounds__(BT_WARPS * 32) k_backtransform(int n, int k, int chunk, bool ysmem,
+                                                                 const double* __restrict__ A,
+                                                                 const double* __restrict__ tau,
+                                                                 double* Y) {
+  backtransform_dev(n, k, chunk, ysmem, A, tau, Y);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -782,15 +803,21 @@ int eigen_values(EigenSolver* es, const double* F, double* w_out) {
       double* pbuf = es->pv + (n + 1);
       void* args[] = {&nn, &es->A, &es->d, &es->e, &es->tau, &vbuf, &pbuf};
       ++g_kernel_launches;
+      const int tk = prof_kbegin(s);
       ck(cudaLaunchCooperativeKernel((void*)k_tridiag_smem, nb, 256, args, smem, s), "tridiag_smem");
+      prof_kend(KS_TRIDIAG, tk, s);
     } else {
       void* args[] = {&nn, &es->A, &es->d, &es->e, &es->tau, &es->pv, &es->scal};
       ++g_kernel_launches;
+      const int tk = prof_kbegin(s);
       ck(cudaLaunchCooperativeKernel((void*)k_tridiag, blocks, 256, args, 0, s), "tridiag");
+      prof_kend(KS_TRIDIAG, tk, s);
     }
   }
   ++g_kernel_launches;
+  const int tm = prof_kbegin(s);
   k_multisect<<<(4 * n + 63) / 64, 64, 0, s>>>(n, es->d, es->e, es->w, es->scal);
+  prof_kend(KS_MULTISECT, tm, s);
   ck(cudaMemcpyAsync(w_out, es->w, sizeof(double) * n, cudaMemcpyDeviceToDevice, s), "w");
   return 0;
 }
@@ -801,14 +828,18 @@ void eigen_vectors_range(EigenSolver* es, int k0, int k1, double* C) {
   const int k = k1 - k0;
   if (k <= 0) return;
   ++g_kernel_launches;
+  const int ti = prof_kbegin(s);
   k_invit<<<(k + 15) / 16, 16, 0, s>>>(n, k0, k, es->d, es->e, es->w, es->scal, es->lu, es->Y);
+  prof_kend(KS_INVIT, ti, s);
   ++g_kernel_launches;
   k_clusters<<<k, 256, 0, s>>>(n, k0, k1, es->d, es->e, es->w, es->scal, 1e-5, es->Y);
   const int chunk = bt_chunk(n);
   double* Yk = es->Y + (size_t)k0 * n;
   ++g_kernel_launches;
+  const int tb_ = prof_kbegin(s);
   k_backtransform<<<(k + BT_WARPS - 1) / BT_WARPS, BT_WARPS * 32, bt_smem(n), s>>>(
       n, k, chunk, bt_ysmem(n), es->A, es->tau, Yk);
+  prof_kend(KS_BACKTRANSFORM, tb_, s);
   // C = X Y (X upper triangular)
   gemm64(false, false, n, k, n, 1.0, es->X, n, Yk, n, 0.0, C + (size_t)k0 * n, n, KM_GE_ROWBEG, s);
 }
@@ -816,10 +847,13 @@ void eigen_vectors_range(EigenSolver* es, int k0, int k1, double* C) {
 void eigen_vectors(EigenSolver* es, int k, double* C) { eigen_vectors_range(es, 0, k, C); }
 
 // P = sum_{m<k} f_m C_m C_m^T: scale columns into work, then one GEMM
-__global__ void k_scale_cols(int n, int k, const double* C, const double* f, double* out) {
+__device__ __forceinline__ void scale_cols_dev(int n, int k, const double* C, const double* f, double* out) {
   const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (t >= (size_t)n * k) return;
   out[t] = C[t] * f[t / n];
+}
+__global__ void k_scale_cols(int n, int k, const double* C, const double* f, double* out) {
+  scale_cols_dev(n, k, C, f, out);
 }
 
 void density_matrix(int n, int k, const double* C, const double* f, double* P, double* work,

@@ -24,6 +24,13 @@ extern std::atomic<unsigned long long> g_kernel_launches;
 // wait for the stream with a blocking-sync event (the host thread sleeps instead of spinning)
 void stream_wait(cudaStream_t s);
 
+// per-kernel CUDA-event timing (only while profiling is enabled): prof_kbegin records an event
+// on s and returns a token (-1 when disabled); prof_kend closes it for the given slot
+enum { KS_TRIDIAG = 0, KS_MULTISECT, KS_INVIT, KS_BACKTRANSFORM, KS_GEMM, KS_FOCK, KS_MULLIKEN,
+       KS_COUNT };
+int prof_kbegin(cudaStream_t s);
+void prof_kend(int slot, int token, cudaStream_t s);
+
 constexpr int MAXG = 12;    // max primitives per shell
 constexpr int MAXL = 2;     // max angular momentum handled by the kernels
 constexpr double INTCUT = 25.0;  // integral_cutoff(acc) is always 25 in the reference
@@ -191,5 +198,74 @@ void launch_fe(int n, const double* f, const double* e, double* out, cudaStream_
 // dense helpers
 void density_matrix(int n, int k, const double* C, const double* f, double* P, double* work,
                     cudaStream_t s);
+
+// ---------------------------------------------------------------------------------------------
+// Batched ensemble path: many molecules in one launch per step.  Every molecule owns a slice of
+// packed device arrays; MolPtrs (in device memory, one per molecule) holds the slice pointers.
+// A batched kernel walks a list of molecule indices with blockIdx.z and runs the same device
+// body as the one-molecule kernel, so both paths share their arithmetic.
+// ---------------------------------------------------------------------------------------------
+struct MolPtrs {
+  DevMol m;
+  DevD4 d4;
+  D4Work d4w;
+  int has_d4, nd, mull_chunks;
+  double nalp, nbet;
+  double *cn, *se, *mrad, *dmrdcn;
+  double *S, *H, *D, *Q, *F, *P, *C, *scratch;  // F doubles as W after the SCF
+  double *emo, *focc;                            // focc [3][n]: total, alpha, beta
+  double *qsh, *qat, *dpat, *qpat, *qsh_o, *qat_o, *dpat_o, *qpat_o;
+  double *vsh, *vat, *vdp, *vqp, *vao;
+  double *mull, *eband, *eelec, *erep, *vec_out, *scal;
+  int* icount;  // [0] number of orbitals with non-zero occupation
+  double *bq, *bqlast, *bdq, *bdqlast, *bdf, *bu, *ba, *bomega, *bwork;
+  int* bstatus;
+  double *grad, *sigma, *sig_at, *dEdcn;
+  // eigensolver: X = L^-T (L is built in T1), A reduced matrix / reflectors, Y vectors of T
+  double *X, *A, *T1, *Y, *lu, *ed, *ee, *etau, *ew, *epv, *escal;
+  int* estatus;
+  double* conv;  // [0] previous electronic energy, [1] current, [2] rms(dq)
+  int* flag;     // 1 converged, 0 running, <0 failed (Broyden or Cholesky), set on device
+};
+
+// one launch of a batched step: the molecules list[0..count) of one size bucket
+struct BatchLaunch {
+  const MolPtrs* mp;
+  const int* list;
+  int count;
+  int nat_max, nsh_max, nao_max, nd_max;
+  cudaStream_t s;
+};
+
+// batched counterparts of the launchers above (same arithmetic, per-molecule pointers)
+void launch_cn_b(const BatchLaunch& b, const Gfn2Scalars& p);
+void launch_setup_levels_b(const BatchLaunch& b, const Gfn2Scalars& p);
+void launch_build_h0_b(const BatchLaunch& b, const Gfn2Scalars& p);
+void launch_repulsion_b(const BatchLaunch& b, const Gfn2Scalars& p);
+void launch_coulomb_potential_b(const BatchLaunch& b, const Gfn2Scalars& p);
+void launch_coulomb_energy_b(const BatchLaunch& b, const Gfn2Scalars& p);
+void launch_coulomb_gradient_b(const BatchLaunch& b, const Gfn2Scalars& p);
+void launch_vao_b(const BatchLaunch& b);
+void launch_fock_b(const BatchLaunch& b);
+void launch_mulliken_b(const BatchLaunch& b);
+void launch_fermi_b(const BatchLaunch& b, double kt);
+void launch_pack_b(const BatchLaunch& b, bool output);  // output: *_o moments -> vec_out
+void launch_unpack_b(const BatchLaunch& b);
+void launch_diff_b(const BatchLaunch& b);
+void launch_broyden_b(const BatchLaunch& b, int iter, int memory, double damp);
+void launch_eelec_init_b(const BatchLaunch& b);
+void launch_converge_b(const BatchLaunch& b, double econv, double pconv, bool kt_final);
+void launch_fe_b(const BatchLaunch& b);
+void launch_h0_gradient_b(const BatchLaunch& b, const Gfn2Scalars& p);
+void launch_cn_grad_b(const BatchLaunch& b, const Gfn2Scalars& p);
+void d4_setup_b(const BatchLaunch& b);
+void d4_potential_b(const BatchLaunch& b);
+void d4_energy_b(const BatchLaunch& b);
+void d4_gradient_b(const BatchLaunch& b);
+// eigensolver steps for a bucket
+void cholesky_inverse_b(const BatchLaunch& b);          // S -> X (status into flag)
+void eigen_values_b(const BatchLaunch& b);              // F -> emo (tridiagonal form kept)
+void eigen_vectors_b(const BatchLaunch& b);             // icount lowest vectors into C
+void density_b(const BatchLaunch& b, bool weighted);   // P (or W into F) from C, focc (, emo)
 
 }  // namespace tb

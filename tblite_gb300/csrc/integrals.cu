@@ -66,7 +66,7 @@ __device__ __forceinline__ double hscale_of(const DevMol& m, const Gfn2Scalars& 
   return zij * p.kshell[m.sh_l[jsh]][m.sh_l[ish]] * (1.0 + p.enscale * den);
 }
 
-__global__ void k_build_h0(DevMol m, Gfn2Scalars p, const double* __restrict__ se, double* S,
+__device__ __forceinline__ void build_h0_dev(DevMol m, Gfn2Scalars p, const double* __restrict__ se, double* S,
                            double* H, double* D, double* Q, long long npair) {
   const long long gid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const long long t = gid / 3;
@@ -183,6 +183,10 @@ __global__ void k_build_h0(DevMol m, Gfn2Scalars p, const double* __restrict__ s
     }
   }
 }
+__global__ void k_build_h0(DevMol m, Gfn2Scalars p, const double* __restrict__ se, double* S,
+                           double* H, double* D, double* Q, long long npair) {
+  build_h0_dev(m, p, se, S, H, D, Q, npair);
+}
 
 void launch_build_h0(const DevMol& m, const Gfn2Scalars& p, const double* se, double* S,
                      double* H, double* D, double* Q, cudaStream_t s) {
@@ -206,7 +210,7 @@ void launch_build_h0(const DevMol& m, const Gfn2Scalars& p, const double* se, do
 // where O is the multipole potential operator of atoms A and B written as a polynomial in
 // (r - A).  The operator on A moves with A, which adds  P (vA_c S + sum_b (1+d_cb) wA_cb D_b).
 // ---------------------------------------------------------------------------------------
-__global__ void k_h0_gradient(DevMol m, Gfn2Scalars p, const double* __restrict__ se,
+__device__ __forceinline__ void h0_gradient_dev(DevMol m, Gfn2Scalars p, const double* __restrict__ se,
                               const double* __restrict__ P, const double* __restrict__ W,
                               const double* __restrict__ vao, const double* __restrict__ vdp,
                               const double* __restrict__ vqp, double* grad, double* sigma,
@@ -359,9 +363,16 @@ __global__ void k_h0_gradient(DevMol m, Gfn2Scalars p, const double* __restrict_
 #pragma unroll
     for (int c = 0; c < 3; ++c) atomicAdd(sigma + 3 * a + c, 0.5 * (vec[a] * dG[c] + dG[a] * vec[c]));
 }
+__global__ void k_h0_gradient(DevMol m, Gfn2Scalars p, const double* __restrict__ se,
+                              const double* __restrict__ P, const double* __restrict__ W,
+                              const double* __restrict__ vao, const double* __restrict__ vdp,
+                              const double* __restrict__ vqp, double* grad, double* sigma,
+                              double* dEdcn, long long npair) {
+  h0_gradient_dev(m, p, se, P, W, vao, vdp, vqp, grad, sigma, dEdcn, npair);
+}
 
 // on-site CN derivative of the diagonal levels: dEdcn_A += sum_{mu in A} dse/dcn P_mumu
-__global__ void k_h0_onsite_dcn(DevMol m, const double* __restrict__ P, double* dEdcn) {
+__device__ __forceinline__ void h0_onsite_dcn_dev(DevMol m, const double* __restrict__ P, double* dEdcn) {
   const int iat = blockIdx.x * blockDim.x + threadIdx.x;
   if (iat >= m.nat) return;
   double acc = 0.0;
@@ -371,6 +382,9 @@ __global__ void k_h0_onsite_dcn(DevMol m, const double* __restrict__ P, double* 
       acc += -m.sh_kcn[ish] * P[(size_t)(io + mi) * m.nao + io + mi];
   }
   dEdcn[iat] += acc;
+}
+__global__ void k_h0_onsite_dcn(DevMol m, const double* __restrict__ P, double* dEdcn) {
+  h0_onsite_dcn_dev(m, P, dEdcn);
 }
 
 void launch_h0_gradient(const DevMol& m, const Gfn2Scalars& p, const double* se, const double* P,
@@ -383,6 +397,41 @@ void launch_h0_gradient(const DevMol& m, const Gfn2Scalars& p, const double* se,
                                                                    grad, sigma, dEdcn, npair);
   ++g_kernel_launches;
   k_h0_onsite_dcn<<<(m.nat + 127) / 128, 128, 0, s>>>(m, P, dEdcn);
+}
+
+// batched launches (blockIdx.z walks the listed molecules; S, H, D, Q start zeroed)
+__global__ void kb_build_h0(const MolPtrs* __restrict__ mp, const int* __restrict__ list,
+                            Gfn2Scalars p) {
+  const MolPtrs& q = mp[list[blockIdx.z]];
+  const long long npair = (long long)q.m.nsh * (q.m.nsh + 1) / 2;
+  build_h0_dev(q.m, p, q.se, q.S, q.H, q.D, q.Q, npair);
+}
+void launch_build_h0_b(const BatchLaunch& b, const Gfn2Scalars& p) {
+  if (!b.count) return;
+  const long long nthr = (long long)b.nsh_max * (b.nsh_max + 1) / 2 * 3;
+  ++g_kernel_launches;
+  kb_build_h0<<<dim3((unsigned)((nthr + 127) / 128), 1, b.count), 128, 0, b.s>>>(b.mp, b.list, p);
+}
+
+// the energy-weighted density W sits in F once the SCF is done
+__global__ void kb_h0_gradient(const MolPtrs* __restrict__ mp, const int* __restrict__ list,
+                               Gfn2Scalars p) {
+  const MolPtrs& q = mp[list[blockIdx.z]];
+  const long long npair = (long long)q.m.nsh * (q.m.nsh + 1) / 2;
+  h0_gradient_dev(q.m, p, q.se, q.P, q.F, q.vao, q.vdp, q.vqp, q.grad, q.sigma, q.dEdcn, npair);
+}
+__global__ void kb_h0_onsite_dcn(const MolPtrs* __restrict__ mp, const int* __restrict__ list) {
+  const MolPtrs& q = mp[list[blockIdx.z]];
+  h0_onsite_dcn_dev(q.m, q.P, q.dEdcn);
+}
+void launch_h0_gradient_b(const BatchLaunch& b, const Gfn2Scalars& p) {
+  if (!b.count) return;
+  const long long npair = (long long)b.nsh_max * (b.nsh_max + 1) / 2;
+  ++g_kernel_launches;
+  kb_h0_gradient<<<dim3((unsigned)((npair + 127) / 128), 1, b.count), 128, 0, b.s>>>(b.mp, b.list,
+                                                                                     p);
+  ++g_kernel_launches;
+  kb_h0_onsite_dcn<<<dim3((b.nat_max + 127) / 128, 1, b.count), 128, 0, b.s>>>(b.mp, b.list);
 }
 
 }  // namespace tb

@@ -23,8 +23,7 @@ namespace tb {
 //   KM_GE_ROWBEG   k >= row tile begin    (op(A) upper triangular:  A(i,k) = 0 for k < i)
 // ------------------------------------------------------------------------------------------
 template <int BM, int BN, int BK, int TM, int TN>
-__global__ void __launch_bounds__((BM / TM) * (BN / TN))
-    k_gemm(int M, int N, int K, double alpha, const double* __restrict__ A, int lda, bool ta,
+__device__ __forceinline__ void gemm_dev(int M, int N, int K, double alpha, const double* __restrict__ A, int lda, bool ta,
            const double* __restrict__ B, int ldb, bool tb, double beta, double* __restrict__ C,
            int ldc, int kmode) {
   constexpr int NT = (BM / TM) * (BN / TN);
@@ -85,10 +84,18 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN))
     }
   }
 }
+template <int BM, int BN, int BK, int TM, int TN>
+__global__ void __launch_bounds__((BM / TM) * (BN / TN))
+    k_gemm(int M, int N, int K, double alpha, const double* __restrict__ A, int lda, bool ta,
+           const double* __restrict__ B, int ldb, bool tb, double beta, double* __restrict__ C,
+           int ldc, int kmode) {
+  gemm_dev<BM, BN, BK, TM, TN>(M, N, K, alpha, A, lda, ta, B, ldb, tb, beta, C, ldc, kmode);
+}
 
 void gemm64(bool ta, bool tb, int M, int N, int K, double alpha, const double* A, int lda,
             const double* B, int ldb, double beta, double* C, int ldc, int kmode, cudaStream_t s) {
   if (M <= 0 || N <= 0) return;
+  const int tk = prof_kbegin(s);
   // small problems: 16x16 tiles keep enough CTAs in flight on 152 SMs
   if ((long long)((M + 31) / 32) * ((N + 31) / 32) < 2 * 152) {
     dim3 grid((N + 15) / 16, (M + 15) / 16);
@@ -101,6 +108,7 @@ void gemm64(bool ta, bool tb, int M, int N, int K, double alpha, const double* A
     k_gemm<32, 32, 16, 4, 4><<<grid, 64, 0, s>>>(M, N, K, alpha, A, lda, ta, B, ldb, tb, beta, C,
                                                   ldc, kmode);
   }
+  prof_kend(KS_GEMM, tk, s);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -132,7 +140,7 @@ __global__ void k_cholesky(int n, double* A, int* status) {
 }
 
 // scale columns: L(i,j) = A(i,j)/sqrt(A(j,j)), zero the strict upper triangle
-__global__ void k_chol_scale(int n, double* A) {
+__device__ __forceinline__ void chol_scale_dev(int n, double* A) {
   const int j = blockIdx.x;
   const double d = sqrt(A[j + (size_t)j * n]);
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -143,10 +151,13 @@ __global__ void k_chol_scale(int n, double* A) {
   __syncthreads();
   if (threadIdx.x == 0) A[j + (size_t)j * n] = d;
 }
+__global__ void k_chol_scale(int n, double* A) {
+  chol_scale_dev(n, A);
+}
 
 // X = L^-T (upper triangular): column j solves L^T x = e_j by back substitution; the dot
 // products read columns of L, which are contiguous.  One warp per column.
-__global__ void k_tri_inv_t(int n, const double* __restrict__ L, double* X) {
+__device__ __forceinline__ void tri_inv_t_dev(int n, const double* __restrict__ L, double* X) {
   const int lane = threadIdx.x & 31;
   const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (j >= n) return;
@@ -164,6 +175,9 @@ __global__ void k_tri_inv_t(int n, const double* __restrict__ L, double* X) {
     if (lane == 0) x[i] = -s / li[i];
     __syncwarp();
   }
+}
+__global__ void k_tri_inv_t(int n, const double* __restrict__ L, double* X) {
+  tri_inv_t_dev(n, L, X);
 }
 
 // Shared-memory resident Cholesky: column j lives in block j % nb for the whole factorisation.

@@ -64,7 +64,7 @@ __device__ __forceinline__ void dexp_count(double r, double r0, const Gfn2Scalar
   dc = d1 * f2 + f1 * d2;
 }
 
-__global__ void k_cn(DevMol m, Gfn2Scalars p, double* cn) {
+__device__ __forceinline__ void cn_dev(DevMol m, Gfn2Scalars p, double* cn) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (warp >= m.nat) return;
   const int i = warp;
@@ -83,6 +83,9 @@ __global__ void k_cn(DevMol m, Gfn2Scalars p, double* cn) {
   acc = warp_sum(acc);
   if (lane == 0) cn[i] = acc;
 }
+__global__ void k_cn(DevMol m, Gfn2Scalars p, double* cn) {
+  cn_dev(m, p, cn);
+}
 
 void launch_cn(const DevMol& m, const Gfn2Scalars& p, double* cn, cudaStream_t s) {
   if (m.nat == 1) {
@@ -94,7 +97,7 @@ void launch_cn(const DevMol& m, const Gfn2Scalars& p, double* cn, cudaStream_t s
 }
 
 // grad_i += sum_j (dEdcn_i + dEdcn_j) dcount/dr (R_i - R_j)/r ; per-atom sigma partials
-__global__ void k_cn_grad(DevMol m, Gfn2Scalars p, const double* __restrict__ dEdcn, double* grad,
+__device__ __forceinline__ void cn_grad_dev(DevMol m, Gfn2Scalars p, const double* __restrict__ dEdcn, double* grad,
                           double* sig_at) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (warp >= m.nat) return;
@@ -126,6 +129,10 @@ __global__ void k_cn_grad(DevMol m, Gfn2Scalars p, const double* __restrict__ dE
     for (int k = 0; k < 9; ++k) sig_at[9 * i + k] += sg[k];
   }
 }
+__global__ void k_cn_grad(DevMol m, Gfn2Scalars p, const double* __restrict__ dEdcn, double* grad,
+                          double* sig_at) {
+  cn_grad_dev(m, p, dEdcn, grad, sig_at);
+}
 
 void launch_cn_grad(const DevMol& m, const Gfn2Scalars& p, const double* dEdcn, double* grad,
                     double* sig_at, cudaStream_t s) {
@@ -137,7 +144,7 @@ void launch_cn_grad(const DevMol& m, const Gfn2Scalars& p, const double* dEdcn, 
 // ------------------------------------------------------------------------------------
 // self energies and AES damping radii
 // ------------------------------------------------------------------------------------
-__global__ void k_levels(DevMol m, Gfn2Scalars p, const double* __restrict__ cn, double* se,
+__device__ __forceinline__ void levels_dev(DevMol m, Gfn2Scalars p, const double* __restrict__ cn, double* se,
                          double* mrad, double* dmrdcn) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t < m.nsh) se[t] = m.sh_se0[t] - m.sh_kcn[t] * cn[m.sh_atom[t]];
@@ -148,6 +155,10 @@ __global__ void k_levels(DevMol m, Gfn2Scalars p, const double* __restrict__ cn,
     mrad[t] = m.at_mprad[t] + t2;
     dmrdcn[t] = -t2 * p.mp_kexp * t1 / (1.0 + t1);
   }
+}
+__global__ void k_levels(DevMol m, Gfn2Scalars p, const double* __restrict__ cn, double* se,
+                         double* mrad, double* dmrdcn) {
+  levels_dev(m, p, cn, se, mrad, dmrdcn);
 }
 
 void launch_setup_levels(const DevMol& m, const Gfn2Scalars& p, const double* cn, double* se,
@@ -164,7 +175,7 @@ void launch_setup_levels(const DevMol& m, const Gfn2Scalars& p, const double* cn
 constexpr int MAXSH = 3;
 
 template <int MODE>
-__global__ void k_coulomb(DevMol m, Gfn2Scalars p, const double* __restrict__ mrad,
+__device__ __forceinline__ void coulomb_dev(DevMol m, Gfn2Scalars p, const double* __restrict__ mrad,
                           const double* __restrict__ qsh, const double* __restrict__ qat,
                           const double* __restrict__ dpat, const double* __restrict__ qpat,
                           double* vsh, double* vat, double* vdp, double* vqp, double* eat) {
@@ -267,6 +278,13 @@ __global__ void k_coulomb(DevMol m, Gfn2Scalars p, const double* __restrict__ mr
     eat[i] += e;
   }
 }
+template <int MODE>
+__global__ void k_coulomb(DevMol m, Gfn2Scalars p, const double* __restrict__ mrad,
+                          const double* __restrict__ qsh, const double* __restrict__ qat,
+                          const double* __restrict__ dpat, const double* __restrict__ qpat,
+                          double* vsh, double* vat, double* vdp, double* vqp, double* eat) {
+  coulomb_dev<MODE>(m, p, mrad, qsh, qat, dpat, qpat, vsh, vat, vdp, vqp, eat);
+}
 
 void launch_coulomb_potential(const DevMol& m, const Gfn2Scalars& p, const double* mrad,
                               const double* qsh, const double* qat, const double* dpat,
@@ -289,7 +307,7 @@ void launch_coulomb_energy(const DevMol& m, const Gfn2Scalars& p, const double* 
 // electrostatic gradient at fixed charges/moments (es2 + AES); dEdcn += dEdr dmrdcn
 // per-atom formulation: atom i sums its own share of every pair (no atomics)
 // ------------------------------------------------------------------------------------
-__global__ void k_coulomb_grad(DevMol m, Gfn2Scalars p, const double* __restrict__ mrad,
+__device__ __forceinline__ void coulomb_grad_dev(DevMol m, Gfn2Scalars p, const double* __restrict__ mrad,
                                const double* __restrict__ dmrdcn, const double* __restrict__ qsh,
                                const double* __restrict__ qat, const double* __restrict__ dpat,
                                const double* __restrict__ qpat, double* grad, double* sig_at,
@@ -380,6 +398,13 @@ __global__ void k_coulomb_grad(DevMol m, Gfn2Scalars p, const double* __restrict
     dEdcn[i] += dEdr * dmrdcn[i];
   }
 }
+__global__ void k_coulomb_grad(DevMol m, Gfn2Scalars p, const double* __restrict__ mrad,
+                               const double* __restrict__ dmrdcn, const double* __restrict__ qsh,
+                               const double* __restrict__ qat, const double* __restrict__ dpat,
+                               const double* __restrict__ qpat, double* grad, double* sig_at,
+                               double* dEdcn) {
+  coulomb_grad_dev(m, p, mrad, dmrdcn, qsh, qat, dpat, qpat, grad, sig_at, dEdcn);
+}
 
 void launch_coulomb_gradient(const DevMol& m, const Gfn2Scalars& p, const double* mrad,
                              const double* dmrdcn, const double* qsh, const double* qat,
@@ -394,7 +419,7 @@ void launch_coulomb_gradient(const DevMol& m, const Gfn2Scalars& p, const double
 // ------------------------------------------------------------------------------------
 // repulsion energy + gradient (per atom, each pair seen from both atoms)
 // ------------------------------------------------------------------------------------
-__global__ void k_repulsion(DevMol m, Gfn2Scalars p, double* erep, double* grad, double* sig_at) {
+__device__ __forceinline__ void repulsion_dev(DevMol m, Gfn2Scalars p, double* erep, double* grad, double* sig_at) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (warp >= m.nat) return;
   const int i = warp;
@@ -430,6 +455,9 @@ __global__ void k_repulsion(DevMol m, Gfn2Scalars p, double* erep, double* grad,
     }
   }
 }
+__global__ void k_repulsion(DevMol m, Gfn2Scalars p, double* erep, double* grad, double* sig_at) {
+  repulsion_dev(m, p, erep, grad, sig_at);
+}
 
 void launch_repulsion(const DevMol& m, const Gfn2Scalars& p, double* erep, double* grad,
                       double* sig_at, cudaStream_t s) {
@@ -440,10 +468,13 @@ void launch_repulsion(const DevMol& m, const Gfn2Scalars& p, double* erep, doubl
 // ------------------------------------------------------------------------------------
 // orbital potential: vao = vsh(ao) + vat(atom)
 // ------------------------------------------------------------------------------------
-__global__ void k_vao(DevMol m, const double* vsh, const double* vat, double* vao) {
+__device__ __forceinline__ void vao_dev(DevMol m, const double* vsh, const double* vat, double* vao) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= m.nao) return;
   vao[t] = vsh[m.ao_sh[t]] + vat[m.ao_at[t]];
+}
+__global__ void k_vao(DevMol m, const double* vsh, const double* vat, double* vao) {
+  vao_dev(m, vsh, vat, vao);
 }
 
 void launch_vao(const DevMol& m, const double* vsh, const double* vat, double* vao,
@@ -460,7 +491,7 @@ void launch_vao(const DevMol& m, const double* vsh, const double* vat, double* v
 // The two multipole products are summed in an order that depends only on min/max(r,c),
 // so F is exactly symmetric.
 // ------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_fock(int n, const int* __restrict__ ao_at,
+__device__ __forceinline__ void fock_dev(int n, const int* __restrict__ ao_at,
                                               const double* __restrict__ H,
                                               const double* __restrict__ S,
                                               const double* __restrict__ D,
@@ -530,13 +561,25 @@ __global__ void __launch_bounds__(256) k_fock(int n, const int* __restrict__ ao_
     if (rr < n && cc < n) F[(size_t)rr * n + cc] = sh[tx][ty + 8 * s];
   }
 }
+__global__ void __launch_bounds__(256) k_fock(int n, const int* __restrict__ ao_at,
+                                              const double* __restrict__ H,
+                                              const double* __restrict__ S,
+                                              const double* __restrict__ D,
+                                              const double* __restrict__ Q,
+                                              const double* __restrict__ vao,
+                                              const double* __restrict__ vdp,
+                                              const double* __restrict__ vqp, double* F) {
+  fock_dev(n, ao_at, H, S, D, Q, vao, vdp, vqp, F);
+}
 
 void launch_fock(int n, const int* ao_at, const double* H, const double* S, const double* D,
                  const double* Q, const double* vao, const double* vdp, const double* vqp, double* F,
                  cudaStream_t s) {
   const int nt = (n + 31) / 32;
   ++g_kernel_launches;
+  const int tk = prof_kbegin(s);
   k_fock<<<dim3(nt, nt), dim3(32, 8), 0, s>>>(n, ao_at, H, S, D, Q, vao, vdp, vqp, F);
+  prof_kend(KS_FOCK, tk, s);
 }
 
 // ------------------------------------------------------------------------------------
@@ -547,7 +590,7 @@ constexpr int MULL_ROWS = 64;
 
 int mulliken_chunks(int n) { return (n + MULL_ROWS - 1) / MULL_ROWS; }
 
-__global__ void __launch_bounds__(128) k_mull_partial(int n, const double* __restrict__ P,
+__device__ __forceinline__ void mull_partial_dev(int n, const double* __restrict__ P,
                                                       const double* __restrict__ S,
                                                       const double* __restrict__ H,
                                                       const double* __restrict__ D,
@@ -574,9 +617,17 @@ __global__ void __launch_bounds__(128) k_mull_partial(int n, const double* __res
 #pragma unroll
   for (int k = 0; k < 11; ++k) partial[((size_t)chunk * 11 + k) * n + c] = acc[k];
 }
+__global__ void __launch_bounds__(128) k_mull_partial(int n, const double* __restrict__ P,
+                                                      const double* __restrict__ S,
+                                                      const double* __restrict__ H,
+                                                      const double* __restrict__ D,
+                                                      const double* __restrict__ Q,
+                                                      double* partial) {
+  mull_partial_dev(n, P, S, H, D, Q, partial);
+}
 
 // one thread per atom: reduce chunks for its orbitals, fill shells/atoms
-__global__ void k_mull_reduce(DevMol m, const double* __restrict__ partial, int nchunk,
+__device__ __forceinline__ void mull_reduce_dev(DevMol m, const double* __restrict__ partial, int nchunk,
                               double* qsh, double* qat, double* dpat, double* qpat,
                               double* eband) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -604,13 +655,20 @@ __global__ void k_mull_reduce(DevMol m, const double* __restrict__ partial, int 
   for (int k = 0; k < 6; ++k) qpat[6 * i + k] = -q[k];
   eband[i] = e;
 }
+__global__ void k_mull_reduce(DevMol m, const double* __restrict__ partial, int nchunk,
+                              double* qsh, double* qat, double* dpat, double* qpat,
+                              double* eband) {
+  mull_reduce_dev(m, partial, nchunk, qsh, qat, dpat, qpat, eband);
+}
 
 void launch_mulliken(const DevMol& m, const double* P, const double* S, const double* H,
                      const double* D, const double* Q, double* partial, int nchunk, double* qsh,
                      double* qat, double* dpat, double* qpat, double* eband, cudaStream_t s) {
   const int n = m.nao;
   ++g_kernel_launches;
+  const int tk = prof_kbegin(s);
   k_mull_partial<<<dim3((n + 127) / 128, nchunk), 128, 0, s>>>(n, P, S, H, D, Q, partial);
+  prof_kend(KS_MULLIKEN, tk, s);
   ++g_kernel_launches;
   k_mull_reduce<<<(m.nat + 127) / 128, 128, 0, s>>>(m, partial, nchunk, qsh, qat, dpat, qpat,
                                                     eband);
@@ -682,7 +740,7 @@ __device__ void fermi_channel(int n, const double* emo, double nel, double kt, d
   __syncthreads();
 }
 
-__global__ void k_fermi(int n, const double* emo, double nalp, double nbet, double kt, double* fa,
+__device__ __forceinline__ void fermi_dev(int n, const double* emo, double nalp, double nbet, double kt, double* fa,
                         double* fb, double* focc, double* ts, int* ncols) {
   __shared__ double red[32];
   if (threadIdx.x == 0) *ts = 0.0;
@@ -703,6 +761,10 @@ __global__ void k_fermi(int n, const double* emo, double nalp, double nbet, doub
   __syncthreads();
   if (threadIdx.x == 0) *ncols = mx + 1;
 }
+__global__ void k_fermi(int n, const double* emo, double nalp, double nbet, double kt, double* fa,
+                        double* fb, double* focc, double* ts, int* ncols) {
+  fermi_dev(n, emo, nalp, nbet, kt, fa, fb, focc, ts, ncols);
+}
 
 void launch_fermi(int n, const double* emo, double nalp, double nbet, double kt, double* focc,
                   double* ts, int* ncols, cudaStream_t s) {
@@ -714,7 +776,7 @@ void launch_fermi(int n, const double* emo, double nalp, double nbet, double kt,
 // ------------------------------------------------------------------------------------
 // mixer vector packing  [qsh | dpat | qpat]
 // ------------------------------------------------------------------------------------
-__global__ void k_pack(int nsh, int nat, const double* qsh, const double* dpat, const double* qpat,
+__device__ __forceinline__ void pack_dev(int nsh, int nat, const double* qsh, const double* dpat, const double* qpat,
                        double* vec) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int nd = nsh + 9 * nat;
@@ -722,6 +784,10 @@ __global__ void k_pack(int nsh, int nat, const double* qsh, const double* dpat, 
   if (t < nsh) vec[t] = qsh[t];
   else if (t < nsh + 3 * nat) vec[t] = dpat[t - nsh];
   else vec[t] = qpat[t - nsh - 3 * nat];
+}
+__global__ void k_pack(int nsh, int nat, const double* qsh, const double* dpat, const double* qpat,
+                       double* vec) {
+  pack_dev(nsh, nat, qsh, dpat, qpat, vec);
 }
 
 void launch_pack(const DevMol& m, const double* qsh, const double* dpat, const double* qpat,
@@ -731,7 +797,7 @@ void launch_pack(const DevMol& m, const double* qsh, const double* dpat, const d
   k_pack<<<(nd + 255) / 256, 256, 0, s>>>(m.nsh, m.nat, qsh, dpat, qpat, vec);
 }
 
-__global__ void k_unpack(DevMol m, const double* vec, double* qsh, double* qat, double* dpat,
+__device__ __forceinline__ void unpack_dev(DevMol m, const double* vec, double* qsh, double* qat, double* dpat,
                          double* qpat) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int nsh = m.nsh, nat = m.nat;
@@ -744,6 +810,10 @@ __global__ void k_unpack(DevMol m, const double* vec, double* qsh, double* qat, 
     qat[t] = a;
   }
 }
+__global__ void k_unpack(DevMol m, const double* vec, double* qsh, double* qat, double* dpat,
+                         double* qpat) {
+  unpack_dev(m, vec, qsh, qat, dpat, qpat);
+}
 
 void launch_unpack(const DevMol& m, const double* vec, double* qsh, double* qat, double* dpat,
                    double* qpat, cudaStream_t s) {
@@ -752,7 +822,7 @@ void launch_unpack(const DevMol& m, const double* vec, double* qsh, double* qat,
   k_unpack<<<(nt + 255) / 256, 256, 0, s>>>(m, vec, qsh, qat, dpat, qpat);
 }
 
-__global__ void k_diff(int nd, const double* vout, const double* q, double* dq, double* err) {
+__device__ __forceinline__ void diff_dev(int nd, const double* vout, const double* q, double* dq, double* err) {
   __shared__ double red[32];
   double s = 0.0;
   for (int t = threadIdx.x; t < nd; t += blockDim.x) {
@@ -762,6 +832,9 @@ __global__ void k_diff(int nd, const double* vout, const double* q, double* dq, 
   }
   s = block_sum(s, red);
   if (threadIdx.x == 0) *err = sqrt(s);
+}
+__global__ void k_diff(int nd, const double* vout, const double* q, double* dq, double* err) {
+  diff_dev(nd, vout, q, dq, err);
 }
 
 void launch_diff(int nd, const double* vout, const double* q, double* dq, double* err,
@@ -781,7 +854,7 @@ __device__ double block_dot(int nd, const double* x, const double* y, double* re
   return block_sum(s, red);
 }
 
-__global__ void k_broyden(int nd, int memory, int iter, double alpha, double* q, double* qlast,
+__device__ __forceinline__ void broyden_dev(int nd, int memory, int iter, double alpha, double* q, double* qlast,
                           const double* dq, double* dqlast, double* df, double* u, double* a,
                           double* omega, double* work, int* status) {
   __shared__ double red[32];
@@ -918,10 +991,18 @@ __global__ void k_broyden(int nd, int memory, int iter, double alpha, double* q,
     q[t] = v;
   }
 }
+__global__ void k_broyden(int nd, int memory, int iter, double alpha, double* q, double* qlast,
+                          const double* dq, double* dqlast, double* df, double* u, double* a,
+                          double* omega, double* work, int* status) {
+  broyden_dev(nd, memory, iter, alpha, q, qlast, dq, dqlast, df, u, a, omega, work, status);
+}
 
-__global__ void k_eelec_init(int nat, const double* ts, const double* eband, double* eelec) {
+__device__ __forceinline__ void eelec_init_dev(int nat, const double* ts, const double* eband, double* eelec) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < nat) eelec[i] = *ts / nat + eband[i];
+}
+__global__ void k_eelec_init(int nat, const double* ts, const double* eband, double* eelec) {
+  eelec_init_dev(nat, ts, eband, eelec);
 }
 
 void launch_eelec_init(int nat, const double* ts, const double* eband, double* eelec,
@@ -930,9 +1011,12 @@ void launch_eelec_init(int nat, const double* ts, const double* eband, double* e
   k_eelec_init<<<(nat + 127) / 128, 128, 0, s>>>(nat, ts, eband, eelec);
 }
 
-__global__ void k_fe(int n, const double* f, const double* e, double* out) {
+__device__ __forceinline__ void fe_dev(int n, const double* f, const double* e, double* out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) out[i] = f[i] * e[i];
+}
+__global__ void k_fe(int n, const double* f, const double* e, double* out) {
+  fe_dev(n, f, e, out);
 }
 
 void launch_fe(int n, const double* f, const double* e, double* out, cudaStream_t s) {
@@ -946,5 +1030,236 @@ void launch_broyden_next(BroydenState& b, cudaStream_t s) {
   k_broyden<<<1, 1024, 0, s>>>(b.ndim, b.memory, b.iter, b.damp, b.q, b.qlast, b.dq, b.dqlast,
                                b.df, b.u, b.a, b.omega, b.work, b.status);
 }
+
+// ------------------------------------------------------------------------------------
+// Batched launches: blockIdx.z walks the listed molecules; each block runs the same body as
+// the one-molecule kernel on that molecule's slices.  Blocks past a molecule's own size exit
+// through the bodies' bounds checks (or the explicit tile checks below).
+// ------------------------------------------------------------------------------------
+#define BMOL const MolPtrs& q = mp[list[blockIdx.z]]
+#define BARGS const MolPtrs* __restrict__ mp, const int* __restrict__ list
+
+static inline dim3 bgrid(unsigned x, const BatchLaunch& b, unsigned y = 1) {
+  return dim3(x > 0 ? x : 1, y, (unsigned)b.count);
+}
+
+__global__ void kb_cn(BARGS, Gfn2Scalars p) {
+  BMOL;
+  cn_dev(q.m, p, q.cn);
+}
+void launch_cn_b(const BatchLaunch& b, const Gfn2Scalars& p) {
+  if (!b.count) return;
+  ++g_kernel_launches;
+  kb_cn<<<bgrid((b.nat_max * 32 + 63) / 64, b), 64, 0, b.s>>>(b.mp, b.list, p);
+}
+
+__global__ void kb_cn_grad(BARGS, Gfn2Scalars p) {
+  BMOL;
+  if (q.m.nat == 1) return;
+  cn_grad_dev(q.m, p, q.dEdcn, q.grad, q.sig_at);
+}
+void launch_cn_grad_b(const BatchLaunch& b, const Gfn2Scalars& p) {
+  if (!b.count) return;
+  ++g_kernel_launches;
+  kb_cn_grad<<<bgrid((b.nat_max * 32 + 63) / 64, b), 64, 0, b.s>>>(b.mp, b.list, p);
+}
+
+__global__ void kb_levels(BARGS, Gfn2Scalars p) {
+  BMOL;
+  levels_dev(q.m, p, q.cn, q.se, q.mrad, q.dmrdcn);
+}
+void launch_setup_levels_b(const BatchLaunch& b, const Gfn2Scalars& p) {
+  if (!b.count) return;
+  const int nt = b.nsh_max > b.nat_max ? b.nsh_max : b.nat_max;
+  ++g_kernel_launches;
+  kb_levels<<<bgrid((nt + 127) / 128, b), 128, 0, b.s>>>(b.mp, b.list, p);
+}
+
+template <int MODE>
+__global__ void kb_coulomb(BARGS, Gfn2Scalars p) {
+  BMOL;
+  if (MODE == 0)
+    coulomb_dev<0>(q.m, p, q.mrad, q.qsh, q.qat, q.dpat, q.qpat, q.vsh, q.vat, q.vdp, q.vqp,
+                   nullptr);
+  else
+    coulomb_dev<1>(q.m, p, q.mrad, q.qsh_o, q.qat_o, q.dpat_o, q.qpat_o, nullptr, nullptr,
+                   nullptr, nullptr, q.eelec);
+}
+void launch_coulomb_potential_b(const BatchLaunch& b, const Gfn2Scalars& p) {
+  if (!b.count) return;
+  ++g_kernel_launches;
+  kb_coulomb<0><<<bgrid((b.nat_max * 32 + 63) / 64, b), 64, 0, b.s>>>(b.mp, b.list, p);
+}
+void launch_coulomb_energy_b(const BatchLaunch& b, const Gfn2Scalars& p) {
+  if (!b.count) return;
+  ++g_kernel_launches;
+  kb_coulomb<1><<<bgrid((b.nat_max * 32 + 63) / 64, b), 64, 0, b.s>>>(b.mp, b.list, p);
+}
+
+__global__ void kb_coulomb_grad(BARGS, Gfn2Scalars p) {
+  BMOL;
+  if (q.m.nat == 1) return;
+  coulomb_grad_dev(q.m, p, q.mrad, q.dmrdcn, q.qsh_o, q.qat_o, q.dpat_o, q.qpat_o, q.grad,
+                   q.sig_at, q.dEdcn);
+}
+void launch_coulomb_gradient_b(const BatchLaunch& b, const Gfn2Scalars& p) {
+  if (!b.count) return;
+  ++g_kernel_launches;
+  kb_coulomb_grad<<<bgrid((b.nat_max * 32 + 63) / 64, b), 64, 0, b.s>>>(b.mp, b.list, p);
+}
+
+__global__ void kb_repulsion(BARGS, Gfn2Scalars p) {
+  BMOL;
+  repulsion_dev(q.m, p, q.erep, q.grad, q.sig_at);
+}
+void launch_repulsion_b(const BatchLaunch& b, const Gfn2Scalars& p) {
+  if (!b.count) return;
+  ++g_kernel_launches;
+  kb_repulsion<<<bgrid((b.nat_max * 32 + 63) / 64, b), 64, 0, b.s>>>(b.mp, b.list, p);
+}
+
+__global__ void kb_vao(BARGS) {
+  BMOL;
+  vao_dev(q.m, q.vsh, q.vat, q.vao);
+}
+void launch_vao_b(const BatchLaunch& b) {
+  if (!b.count) return;
+  ++g_kernel_launches;
+  kb_vao<<<bgrid((b.nao_max + 255) / 256, b), 256, 0, b.s>>>(b.mp, b.list);
+}
+
+__global__ void __launch_bounds__(256) kb_fock(BARGS) {
+  BMOL;
+  const int n = q.m.nao;
+  if ((int)blockIdx.x * 32 >= n || (int)blockIdx.y * 32 >= n) return;  // tile outside
+  fock_dev(n, q.m.ao_at, q.H, q.S, q.D, q.Q, q.vao, q.vdp, q.vqp, q.F);
+}
+void launch_fock_b(const BatchLaunch& b) {
+  if (!b.count) return;
+  const unsigned nt = (b.nao_max + 31) / 32;
+  ++g_kernel_launches;
+  kb_fock<<<bgrid(nt, b, nt), dim3(32, 8), 0, b.s>>>(b.mp, b.list);
+}
+
+__global__ void __launch_bounds__(128) kb_mull_partial(BARGS) {
+  BMOL;
+  if ((int)blockIdx.y >= q.mull_chunks) return;
+  mull_partial_dev(q.m.nao, q.P, q.S, q.H, q.D, q.Q, q.mull);
+}
+__global__ void kb_mull_reduce(BARGS) {
+  BMOL;
+  mull_reduce_dev(q.m, q.mull, q.mull_chunks, q.qsh_o, q.qat_o, q.dpat_o, q.qpat_o, q.eband);
+}
+void launch_mulliken_b(const BatchLaunch& b) {
+  if (!b.count) return;
+  ++g_kernel_launches;
+  kb_mull_partial<<<bgrid((b.nao_max + 127) / 128, b, mulliken_chunks(b.nao_max)), 128, 0,
+                    b.s>>>(b.mp, b.list);
+  ++g_kernel_launches;
+  kb_mull_reduce<<<bgrid((b.nat_max + 127) / 128, b), 128, 0, b.s>>>(b.mp, b.list);
+}
+
+__global__ void kb_fermi(BARGS, double kt) {
+  BMOL;
+  const int n = q.m.nao;
+  fermi_dev(n, q.emo, q.nalp, q.nbet, kt, q.focc + n, q.focc + 2 * n, q.focc, q.scal, q.icount);
+}
+void launch_fermi_b(const BatchLaunch& b, double kt) {
+  if (!b.count) return;
+  ++g_kernel_launches;
+  kb_fermi<<<bgrid(1, b), 1024, 0, b.s>>>(b.mp, b.list, kt);
+}
+
+__global__ void kb_pack(BARGS, int output) {
+  BMOL;
+  if (output)
+    pack_dev(q.m.nsh, q.m.nat, q.qsh_o, q.dpat_o, q.qpat_o, q.vec_out);
+  else
+    pack_dev(q.m.nsh, q.m.nat, q.qsh, q.dpat, q.qpat, q.bq);
+}
+void launch_pack_b(const BatchLaunch& b, bool output) {
+  if (!b.count) return;
+  ++g_kernel_launches;
+  kb_pack<<<bgrid((b.nd_max + 255) / 256, b), 256, 0, b.s>>>(b.mp, b.list, output ? 1 : 0);
+}
+
+__global__ void kb_unpack(BARGS) {
+  BMOL;
+  unpack_dev(q.m, q.bq, q.qsh, q.qat, q.dpat, q.qpat);
+}
+void launch_unpack_b(const BatchLaunch& b) {
+  if (!b.count) return;
+  const int nt = b.nsh_max > 6 * b.nat_max ? b.nsh_max : 6 * b.nat_max;
+  ++g_kernel_launches;
+  kb_unpack<<<bgrid((nt + 255) / 256, b), 256, 0, b.s>>>(b.mp, b.list);
+}
+
+__global__ void kb_diff(BARGS) {
+  BMOL;
+  diff_dev(q.nd, q.vec_out, q.bq, q.bdq, q.scal + 1);
+}
+void launch_diff_b(const BatchLaunch& b) {
+  if (!b.count) return;
+  ++g_kernel_launches;
+  kb_diff<<<bgrid(1, b), 1024, 0, b.s>>>(b.mp, b.list);
+}
+
+__global__ void kb_broyden(BARGS, int iter, int memory, double damp) {
+  BMOL;
+  broyden_dev(q.nd, memory, iter, damp, q.bq, q.bqlast, q.bdq, q.bdqlast, q.bdf, q.bu, q.ba,
+              q.bomega, q.bwork, q.bstatus);
+}
+void launch_broyden_b(const BatchLaunch& b, int iter, int memory, double damp) {
+  if (!b.count) return;
+  ++g_kernel_launches;
+  kb_broyden<<<bgrid(1, b), 1024, 0, b.s>>>(b.mp, b.list, iter, memory, damp);
+}
+
+__global__ void kb_eelec_init(BARGS) {
+  BMOL;
+  eelec_init_dev(q.m.nat, q.scal, q.eband, q.eelec);
+}
+void launch_eelec_init_b(const BatchLaunch& b) {
+  if (!b.count) return;
+  ++g_kernel_launches;
+  kb_eelec_init<<<bgrid((b.nat_max + 127) / 128, b), 128, 0, b.s>>>(b.mp, b.list);
+}
+
+// convergence test of the single-point driver (xtb/singlepoint.f90:300-304), one thread per
+// molecule: the electronic energy is summed in atom order, as the one-molecule driver does
+__global__ void kb_converge(BARGS, double econv, double pconv, int kt_final) {
+  BMOL;
+  if (threadIdx.x != 0) return;
+  double e = 0.0;
+  for (int i = 0; i < q.m.nat; ++i) e += q.eelec[i];
+  const double elast = q.conv[1];
+  q.conv[0] = elast;
+  q.conv[1] = e;
+  q.conv[2] = q.scal[1];
+  if (*q.bstatus != 0) {
+    *q.flag = -1;
+    return;
+  }
+  const bool ok = fabs(e - elast) < econv && q.scal[1] < pconv && kt_final;
+  *q.flag = ok ? 1 : 0;
+}
+void launch_converge_b(const BatchLaunch& b, double econv, double pconv, bool kt_final) {
+  if (!b.count) return;
+  ++g_kernel_launches;
+  kb_converge<<<bgrid(1, b), 32, 0, b.s>>>(b.mp, b.list, econv, pconv, kt_final ? 1 : 0);
+}
+
+__global__ void kb_fe(BARGS) {
+  BMOL;
+  fe_dev(q.m.nao, q.focc, q.emo, q.vec_out);
+}
+void launch_fe_b(const BatchLaunch& b) {
+  if (!b.count) return;
+  ++g_kernel_launches;
+  kb_fe<<<bgrid((b.nao_max + 255) / 256, b), 256, 0, b.s>>>(b.mp, b.list);
+}
+
+#undef BMOL
+#undef BARGS
 
 }  // namespace tb

@@ -76,6 +76,7 @@ _SIGNATURES = {
     "tblite_gb300_set_profiling": (None, [c_int]),
     "tblite_gb300_get_profile": (c_int, [_dbl_p, _int_p, c_int, _dbl_p, _int_p]),
     "tblite_gb300_get_launch_count": (ctypes.c_ulonglong, []),
+    "tblite_gb300_get_kernel_profile": (c_int, [_dbl_p, _int_p, c_int]),
     "tblite_gb300_density_matrix_noalloc": (
         c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
     "tblite_gb300_density_matrix_noalloc_max": (c_int, []),
@@ -123,6 +124,19 @@ def get_profile():
     lib.tblite_gb300_get_profile(_dp(ms), _ip(cnt), len(PHASES), byref(tot), byref(it))
     return {"phase_ms": dict(zip(PHASES, ms.tolist())), "phase_count": dict(zip(PHASES, cnt.tolist())),
             "total_ms": tot.value, "iterations": it.value}
+
+
+KERNEL_SLOTS = ("tridiag", "multisect", "invit", "backtransform", "gemm", "fock", "mulliken")
+
+
+def get_kernel_profile():
+    """Per-kernel device times (ms, summed over launches) and launch counts of the last single
+    point, from CUDA events around each launch on the engine stream."""
+    lib = load()
+    ms = np.zeros(len(KERNEL_SLOTS))
+    cnt = np.zeros(len(KERNEL_SLOTS), dtype=np.int32)
+    lib.tblite_gb300_get_kernel_profile(_dp(ms), _ip(cnt), len(KERNEL_SLOTS))
+    return {k: (float(t), int(c)) for k, t, c in zip(KERNEL_SLOTS, ms, cnt)}
 
 
 def launch_count() -> int:

@@ -139,6 +139,8 @@ def config(name):
         return water_cluster((4, 4, 2), seed=0)
     if name == "c200h402":
         return alkane(200, seed=1)
+    if name == "c100h202":  # half-size chain (602 AOs): small case for kernel captures
+        return alkane(100, seed=1)
     if name == "h2o1000":
         return water_cluster((10, 10, 10), seed=2)
     raise KeyError(name)
