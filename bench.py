@@ -1,17 +1,22 @@
-"""Benchmark: GFN2-xTB energy + analytic gradient single points per second on one GB300.
+"""Benchmark: GFN2-xTB energy + analytic gradient evaluations per second on one GB300.
 
-Workload (default): the plain one-molecule-per-call path on C200H402 (602 atoms, 1202 AOs),
-FP64, 300 K Fermi smearing, default SCF thresholds (accuracy 1), through the engine's
-C ABI (tblite_get_singlepoint) -- the reference's own single-point entry point.
+Workload (default, ``--config ensemble4096``): 4096 molecules of uneven size (50 % water
+clusters with k ~ log-uniform[1, 64] waters, 50 % alkanes CnH2n+2 with n ~ log-uniform[1, 60];
+3-192 atoms, up to 384 AOs), FP64, 300 K Fermi smearing, default SCF thresholds, all evaluated
+per step by one call of the batched entry point (tblite_gb300_batch_singlepoint).  The plain
+one-molecule-per-call path (tblite_get_singlepoint, the reference's entry point) is timed on an
+even sample of the same ensemble beside it.  ``--config c200h402`` / ``h2o32`` run the plain
+path on one molecule (C200H402: 602 atoms, 1202 AOs; (H2O)32: 96 atoms, 192 AOs).
 
-* value     evals/s of the device work of one single point (engine-internal CUDA events
-            on the engine stream, first to last event), geometry already on the device
-* e2e       evals/s of tblite_get_singlepoint called from host memory (host->device copy of
-            the geometry and device->host copy of energy, gradient, charges, orbital data
-            and density matrix inside the timed region)
-* roofline  for the engine's dominant own kernel phase, from its per-launch event times
-* cpu_baseline  the CPU oracle (plain C + numpy/LAPACK, all host threads) on one
-            evaluation of the same molecule
+* value     evals/s from device time (CUDA events on the engine streams; the batch's uploads,
+            read-back and host work excluded; for one molecule the events of the single point
+            minus its result transfer)
+* e2e       evals/s of the public call from host memory (geometry host->device, energies,
+            gradients, charges, orbital data device->host inside the timed region)
+* roofline  the dominant own kernel (Householder tridiagonalisation) against the FP64 peak
+            measured in the same run (cuBLAS DGEMM), from its CUDA-event times
+* cpu_baseline  the CPU oracle (plain C + numpy/LAPACK dsygvd, all host threads) on a bounded
+            sample of the same workload
 
 ``--impl reference`` times the CPU oracle instead (the reference itself cannot be built
 here: no Fortran compiler).  Multi-GPU runs are independent replicas (one process per GPU,
@@ -33,10 +38,15 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-METRIC = "GFN2 energy+force evals/sec"
+METRIC = "GFN2 energy+force evals/sec, batched vs plain GPU at |\u0394E|\u22641e-7 Eh, |\u0394F|\u22641e-6"
 WORKLOADS = {"c200h402": "C200H402 GFN2-xTB energy+gradient single point (602 atoms, 1202 AOs)",
              "h2o32": "(H2O)32 GFN2-xTB energy+gradient single point (96 atoms, 192 AOs)",
-             "c100h202": "C100H202 GFN2-xTB energy+gradient single point (302 atoms, 602 AOs)"}
+             "c100h202": "C100H202 GFN2-xTB energy+gradient single point (302 atoms, 602 AOs)",
+             "ensemble4096": "4096-molecule GFN2-xTB energy+gradient ensemble (50 % water clusters "
+                             "k ~ log-uniform[1, 64], 50 % alkanes n ~ log-uniform[1, 60]; "
+                             "3-192 atoms), batched",
+             "ensemble512": "512-molecule subset of the same ensemble generator, batched"}
+ENSEMBLE_SIZE = {"ensemble4096": 4096, "ensemble512": 512}
 
 
 def _dist():
@@ -271,25 +281,160 @@ def run_gb300(args):
     return line
 
 
+def _ensemble_flops(mols_nao, mols_nel, iters):
+    """Algorithmic FP64 work of the batched ensemble (per molecule: per SCF iteration the
+    Cholesky-reduced eigensolve 16/3 n^3 and the density 2 n^2 k; once the Cholesky n^3/3 and
+    the energy-weighted density 2 n^2 k; k = occupied orbitals)."""
+    tot = tri = 0.0
+    for n, nel, it in zip(mols_nao, mols_nel, iters):
+        k = min(n, (nel + 1) // 2)
+        tot += it * (16.0 / 3.0 * n ** 3 + 2.0 * n * n * k) + n ** 3 / 3.0 + 2.0 * n * n * k
+        tri += it * 4.0 / 3.0 * n ** 3
+    return tot, tri
+
+
+def run_batch(args):
+    """Batched ensemble: all molecules through tblite_gb300_batch_singlepoint per step."""
+    import torch
+
+    from tblite_gb300 import _build, library, workloads
+    from tblite_gb300.interface import Calculator, batch_fallbacks, batch_singlepoint
+
+    rank, ws = _dist()
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", dev))
+    _build.build()
+    count = ENSEMBLE_SIZE[args.config]
+    mols = workloads.mixed_ensemble(count, seed=4 + 1000 * rank)
+    calcs = [Calculator("GFN2-xTB", z, x) for z, x in mols]
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
+    fp64_peak = _fp64_peak(torch)
+    library.set_profiling(True)
+    for _ in range(args.warmup):
+        batch_singlepoint(calcs)
+    torch.cuda.synchronize()
+    n0 = library.launch_count()
+    if ws > 1:
+        torch.distributed.barrier()
+    wall = dev_ms = 0.0
+    with ClockSampler(dev) as clocks:
+        for _ in range(args.steps):
+            _flush_l2(flush)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            res = batch_singlepoint(calcs)  # host in, host out
+            energies = [r.get("energy") for r in res]
+            wall += time.perf_counter() - t0
+            dev_ms += library.load().tblite_gb300_batch_last_device_ms()
+    launches = library.launch_count() - n0
+    fallbacks = batch_fallbacks()
+    kprof = library.get_kernel_profile()
+    iters = np.zeros(count, dtype=np.int32)
+    library.load().tblite_gb300_batch_last_iterations(library._ip(iters), count)
+    if ws > 1:
+        t = torch.tensor([wall, dev_ms], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        wall, dev_ms = float(t[0]), float(t[1])
+        torch.distributed.barrier()
+    if rank != 0:
+        return None
+    evals = args.steps * count * ws
+    value = evals / (dev_ms / 1000.0)
+    e2e = evals / wall
+    nao = [c.get("orbital-map").size for c in calcs]
+    nel = [int(round(sum({1: 1, 6: 4, 8: 6}[int(q)] for q in z))) for z, _ in mols]
+    flops, tri_flops = _ensemble_flops(nao, nel, iters)
+    ms_step = dev_ms / args.steps
+    kernels = {k: {"ms_per_step": round(t, 3), "launches": c, "share_of_step": round(t / ms_step, 4)}
+               for k, (t, c) in kprof.items()}
+    t_tri, c_tri = kprof["tridiag"]
+    roofline = {"kernel": "tridiag (batched, one block cluster per molecule)", "bound": "fp64",
+                "achieved": round(tri_flops / (t_tri / 1000.0) / 1e12, 4) if t_tri else None,
+                "peak": round(fp64_peak, 4), "unit": "TFLOP/s",
+                "frac": round(tri_flops / (t_tri / 1000.0) / 1e12 / fp64_peak, 4) if t_tri else None,
+                "traffic": None, "peak_source": "measured in this run (cuBLAS DGEMM 4096^3)",
+                "algorithmic_work_per_step": tri_flops, "ms_per_step": round(t_tri, 3),
+                "launches_per_step": c_tri,
+                "whole_step": {"algorithmic_flops": flops,
+                               "achieved_tflops": round(flops / (ms_step / 1000.0) / 1e12, 4)}}
+    # the plain one-molecule GPU path on an even sample of the same ensemble
+    sample = list(range(0, count, max(1, count // 64)))
+    for i in sample:
+        calcs[i].singlepoint()  # per-calculator workspace
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in sample:
+        calcs[i].singlepoint()
+    plain = len(sample) / (time.perf_counter() - t0)
+    cpu = None
+    if not args.no_cpu:
+        from oracle import gfn2
+
+        gfn2.lib()
+        cs = sample[:16]
+        t0 = time.perf_counter()
+        for i in cs:
+            z, x = mols[i]
+            gfn2.singlepoint(gfn2.new_calc(gfn2.Molecule(np.asarray(z), np.asarray(x))), grad=True)
+        cpu = {"value": round(len(cs) / (time.perf_counter() - t0), 4), "unit": "evals/s",
+               "cores": os.cpu_count() or 1, "kind": "port",
+               "sample": f"{len(cs)} molecules evenly spaced through the ensemble, CPU oracle "
+                         "(C + numpy/LAPACK dsygvd), evals/s of the sample"}
+    h2d = sum(m[1].size * 8 + m[0].size * 4 for m in mols)
+    d2h = sum((1 + 5 * len(m[0]) + 9) * 8 for m in mols)
+    return {
+        "metric": METRIC, "value": round(value, 3), "unit": "evals/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded ensemble generator)",
+        "config": {"workload": WORKLOADS[args.config], "molecules": count,
+                   "max_orbitals": int(max(nao)), "mean_scf_iterations": float(np.mean(iters)),
+                   "path": "batched (tblite_gb300_batch_singlepoint)",
+                   "l2": "flushed (256 MB write) before every step", "parallelism": f"replicas x{ws}"},
+        "e2e": {"value": round(e2e, 3), "unit": "evals/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "batched_vs_plain": {"plain_gpu_evals_per_s": round(plain, 3),
+                             "sample": f"{len(sample)} molecules evenly spaced, one per call",
+                             "ratio_e2e": round(e2e / plain, 2)},
+        "fallbacks_to_plain": fallbacks,
+        "gpu_launches": int(launches),
+        "roofline": roofline,
+        "kernels": kernels,
+        "cpu_baseline": cpu,
+        "clocks": clocks.summary(),
+    }
+
+
 def run_reference(args):
     from tblite_gb300 import workloads
 
     rank, ws = _dist()
     if rank != 0:
         return None
-    numbers, positions = workloads.config(args.config)
-    for _ in range(args.warmup):
-        pass  # the oracle has no warm state worth priming beyond the first build
     from oracle import gfn2
 
     gfn2.lib()
     threads = os.cpu_count() or 1
+    if args.config in ENSEMBLE_SIZE:
+        # bounded sample per step: 16 molecules evenly spaced through the ensemble
+        count = ENSEMBLE_SIZE[args.config]
+        mols = workloads.mixed_ensemble(count, seed=4)
+        sample = [mols[i] for i in range(0, count, max(1, count // 16))][:16]
+        sample_desc = f"{len(sample)} molecules of the ensemble per step"
+    else:
+        sample = [workloads.config(args.config)]
+        sample_desc = "1 full evaluation per step"
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        calc = gfn2.new_calc(gfn2.Molecule(numbers, positions))
-        gfn2.singlepoint(calc, grad=True)
+        for numbers, positions in sample:
+            calc = gfn2.new_calc(gfn2.Molecule(np.asarray(numbers), np.asarray(positions)))
+            gfn2.singlepoint(calc, grad=True)
     dt = time.perf_counter() - t0
-    value = args.steps / dt
+    value = args.steps * len(sample) / dt
     return {
         "impl": "reference", "metric": METRIC, "value": round(value, 5), "unit": "evals/s",
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
@@ -297,7 +442,7 @@ def run_reference(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOADS[args.config]},
         "cpu_baseline": {"value": round(value, 5), "unit": "evals/s", "cores": threads,
-                         "kind": "port", "sample": f"{args.steps} full evaluations"},
+                         "kind": "port", "sample": sample_desc},
         "e2e": {"value": round(value, 5), "unit": "evals/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -309,14 +454,14 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", default="c200h402", choices=sorted(WORKLOADS))
+    ap.add_argument("--config", default="ensemble4096", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     args = ap.parse_args()
     if args.impl == "reference":
         args.steps = min(args.steps, 3)
         line = run_reference(args)
     else:
-        line = run_gb300(args)
+        line = run_batch(args) if args.config in ENSEMBLE_SIZE else run_gb300(args)
     if line is not None:
         print(json.dumps(line))
 

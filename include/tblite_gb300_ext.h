@@ -12,9 +12,39 @@
  */
 #ifndef TBLITE_GB300_EXT_H
 #define TBLITE_GB300_EXT_H
+#include "tblite.h"
 #ifdef __cplusplus
 extern "C" {
 #endif
+
+/*
+ * Batched single points.  No counterpart in the reference, which evaluates one molecule per
+ * tblite_get_singlepoint call.  Energy and analytic gradient of nmol independent molecules:
+ * mols[i] with calcs[i] (built by tblite_new_gfn2_calculator for that structure) into
+ * results[i].  The molecules run through the SCF together, one launch per step for every size
+ * bucket, each with its own calculator settings (accuracy, temperature, mixer damping and
+ * memory, iteration limit) and its own convergence test; a result that already holds a
+ * compatible wavefunction restarts that molecule, as in tblite_get_singlepoint.  A molecule
+ * that the batch cannot finish (temperature annealing, more than the batch's Broyden history,
+ * not converged, a failure) is evaluated by the one-molecule path afterwards, so every result
+ * and error is what tblite_get_singlepoint gives.  Batched results hold energies, gradient,
+ * virial, charges, multipoles, dipole, orbital energies and occupations; the density matrix
+ * and orbital coefficients are not kept.  status[i] (may be NULL) is 0 on success and 1 when
+ * molecule i failed; its message is pushed onto the context error log, prefixed with
+ * "Batch entry i:".  Returns the number of failed molecules.
+ */
+int tblite_gb300_batch_singlepoint(tblite_context ctx, int nmol, const tblite_structure* mols,
+                                   const tblite_calculator* calcs, const tblite_result* results,
+                                   int* status);
+/* molecules of the last batch call that took the one-molecule path */
+int tblite_gb300_batch_last_fallbacks(void);
+/* device time (ms, CUDA events) of the last batch call from the first setup kernel to the end
+ * of the gradient, summed over its memory chunks (uploads, read-back and the one-molecule
+ * path excluded) */
+double tblite_gb300_batch_last_device_ms(void);
+/* SCF iterations of each molecule of the last batch call (0 for molecules that took the
+ * one-molecule path); returns the number of molecules of that call */
+int tblite_gb300_batch_last_iterations(int* iterations, int nmol);
 
 /* enable (1) or disable (0) event timing for subsequent single points (process wide) */
 void tblite_gb300_set_profiling(int enable);
@@ -29,6 +59,11 @@ int tblite_gb300_get_profile(double* phase_ms, int* phase_count, int nphase, dou
  * tridiagonalisation, 1 eigenvalue multisection, 2 inverse iteration, 3 back-transformation,
  * 4 FP64 GEMM (all uses), 5 Fock assembly, 6 Mulliken column sums.  Returns the slot count. */
 int tblite_gb300_get_kernel_profile(double* kernel_ms, int* kernel_count, int nslot);
+
+/* channels of the bond orders tblite_get_result_bond_orders copies: 1 for a closed shell
+ * (nat x nat), 2 for a restricted open shell (total and magnetisation, nat x nat x 2 in the
+ * reference's column-major order), 0 when the result holds none (batched results) */
+int tblite_gb300_get_result_bond_order_channels(tblite_result res);
 
 /* number of engine kernels launched since the library was loaded (all threads) */
 unsigned long long tblite_gb300_get_launch_count(void);

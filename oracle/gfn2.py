@@ -549,6 +549,40 @@ def singlepoint(calc: Calc, grad=True, verbose=False, dispersion=None):
     energy = float(np.sum(energies))
     parts = dict(erep=float(np.sum(erep)), edisp_nonsc=float(np.sum(edisp)),
                  eelec=float(np.sum(eelec)), cn=st["cn"], vao=vao, vdp=vdp, vqp=vqp)
+    # post-processing: bond orders (post_processing/wbo.f90:60-115 ->
+    # wavefunction/mulliken.f90:176-235) and molecular moments (mulliken.f90:133-172)
+    if nalp != nbet:
+        spin_p = [(C * fa) @ C.T, (C * fb) @ C.T]
+        scale = 2.0
+    else:
+        spin_p = [P]
+        scale = 1.0
+    wbo = np.zeros((len(spin_p), nat, nat))
+    for s_, Ps in enumerate(spin_p):
+        PS_ = Ps @ st["S"]
+        prod = PS_ * PS_.T
+        for a in range(nat):
+            for b in range(nat):
+                if a != b:
+                    wbo[s_, a, b] = scale * np.sum(prod[np.ix_(ao2at == a, ao2at == b)])
+    if len(spin_p) == 2:
+        wbo = np.stack([wbo[0] + wbo[1], wbo[0] - wbo[1]])
+    parts["wbo"] = wbo
+    parts["dipole"] = np.sum(xyz * qat[:, None] + dpat, axis=0)
+    quad = np.zeros(6)
+    for a in range(nat):
+        x, d = xyz[a], dpat[a]
+        v = x * qat[a]
+        c = np.zeros(6)
+        c[[0, 2, 5]] = x * (v + 2 * d)
+        c[1] = x[0] * (v[1] + d[1]) + d[0] * x[1]
+        c[3] = x[0] * (v[2] + d[2]) + d[0] * x[2]
+        c[4] = x[1] * (v[2] + d[2]) + d[1] * x[2]
+        tr = 0.5 * (c[0] + c[2] + c[5])
+        c = np.array([1.5 * c[0] - tr, 3 * c[1], 1.5 * c[2] - tr, 3 * c[3], 3 * c[4],
+                      1.5 * c[5] - tr])
+        quad += qpat[a] + c
+    parts["quadrupole"] = quad
     if grad:
         gradient, sigma = _gradient(calc, st, gradient, sigma, C, emo, focc, P, qsh, qat, dpat,
                                     qpat, vao, vdp, vqp, disp)

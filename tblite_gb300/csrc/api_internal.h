@@ -1,0 +1,168 @@
+// Internal object layout of the C ABI (error, context, structure, calculator, result) and the
+// per-calculator device workspace; shared by the one-molecule driver (capi.cpp) and the batched
+// ensemble driver (batch.cpp).  Not part of the public interface.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/tblite.h"
+#include "engine.h"
+
+using namespace tb;
+
+// --------------------------------------------------------------------------------------
+// objects
+// --------------------------------------------------------------------------------------
+struct _tblite_error {
+  std::string msg;
+  bool set = false;
+};
+
+struct _tblite_context {
+  std::vector<std::string> errors;
+  tblite_logger_callback logger = nullptr;
+  void* userdata = nullptr;
+  int verbosity = 1;
+  int color = 0;
+  void push(const std::string& m) { errors.push_back(m); }
+  void message(const std::string& m) {
+    if (logger) {
+      std::string tmp = m;
+      logger(nullptr, tmp.data(), (int)tmp.size(), userdata);
+    } else if (verbosity > 0) {
+      printf("%s\n", m.c_str());
+    }
+  }
+};
+
+struct _tblite_structure {
+  int nat = 0;
+  std::vector<int> num;
+  std::vector<double> xyz;  // [nat][3] Bohr
+  double charge = 0.0;
+  int uhf = 0;
+};
+
+namespace {
+
+inline void cuda_check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess)
+    throw std::runtime_error(std::string("CUDA error '") + cudaGetErrorString(e) + "' in " + what);
+}
+
+template <class T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  void alloc(size_t count) {
+    if (count <= n && p) return;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cuda_check(cudaMalloc(&p, sizeof(T) * std::max<size_t>(count, 1)), "cudaMalloc");
+    n = count;
+  }
+  void upload(const std::vector<T>& h, cudaStream_t s) {
+    alloc(h.size());
+    if (!h.empty())
+      cuda_check(cudaMemcpyAsync(p, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice, s),
+                 "upload");
+  }
+  void download(std::vector<T>& h, size_t count, cudaStream_t s) const {
+    h.resize(count);
+    if (count)
+      cuda_check(cudaMemcpyAsync(h.data(), p, sizeof(T) * count, cudaMemcpyDeviceToHost, s),
+                 "download");
+  }
+  ~DBuf() {
+    if (p) cudaFree(p);
+  }
+};
+
+}  // namespace
+
+struct Workspace {
+  cudaStream_t stream = nullptr;
+  int nat = -1, nsh = -1, nao = -1, memory = -1;
+  // static molecule/basis data
+  DBuf<double> xyz, sh_alpha, sh_coeff, sh_se0, sh_kcn, sh_shpoly, sh_zeta, sh_hub, sh_gam3,
+      sh_refocc, at_en, at_rad, at_rcov, at_mprad, at_vcn, at_dkern, at_qkern, at_repa, at_repz;
+  DBuf<int> at_z, at_sh, sh_atom, sh_l, sh_nprim, sh_ao, ao_sh, ao_at;
+  // geometry dependent
+  DBuf<double> cn, se, mrad, dmrdcn, S, H, D, Q, F, C, P, W, emo, focc, scratch;
+  // SCF state
+  DBuf<double> qsh, qat, dpat, qpat, qsh_o, qat_o, dpat_o, qpat_o, vsh, vat, vdp, vqp, vao;
+  DBuf<double> mull, eband, eelec, erep, vec_out, scal;
+  DBuf<int> icount;
+  // Broyden
+  DBuf<double> b_q, b_qlast, b_dq, b_dqlast, b_df, b_u, b_a, b_omega, b_work;
+  DBuf<int> b_status;
+  // gradient
+  DBuf<double> grad, sigma, sig_at, dEdcn;
+  DBuf<double> wbo;
+  // D4 dispersion
+  DBuf<int> d4_sp, d4_nref, d4_ngw;
+  DBuf<double> d4_refcn, d4_refq, d4_zeff, d4_gam, d4_r4r2, d4_rcov, d4_en, d4_c6ref;
+  DBuf<double> d4_cn, d4_gw, d4_dgw, d4_gwv, d4_dgwdq, d4_dgwv_cn, d4_c6, d4_dc6, d4_e3, d4_dEdcn;
+  EigenSolver* eig = nullptr;
+  ~Workspace() {
+    if (eig) eigen_destroy(eig);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+struct _tblite_calculator {
+  // molecule-bound basis (built at construction)
+  int nat = 0, nsh = 0, nao = 0;
+  std::vector<int> at_z, at_sh, sh_atom, sh_l, sh_nprim, sh_ao, ao_sh, ao_at;
+  // D4 data per atom (empty for a single atom: no pairs, no dispersion)
+  bool has_d4 = false;
+  int d4_nsp = 0;
+  std::vector<int> d4_sp, d4_nref, d4_ngw;
+  std::vector<double> d4_refcn, d4_refq, d4_zeff, d4_gam, d4_r4r2, d4_rcov, d4_en, d4_c6ref;
+  std::vector<double> sh_alpha, sh_coeff, sh_se0, sh_kcn, sh_shpoly, sh_zeta, sh_hub, sh_gam3,
+      sh_refocc, at_en, at_rad, at_rcov, at_mprad, at_vcn, at_dkern, at_qkern, at_repa, at_repz;
+  double min_alpha = 1e300;
+  // settings (reference api/calculator.f90:78-89, scf/mixer/input.f90:28-34)
+  double accuracy = 1.0;
+  double etemp = 300.0 * 3.166808578545117e-06;
+  int max_iter = 250;
+  double damping = 0.4;
+  int memory = 0;
+  int guess = TBLITE_GUESS_SAD;
+  int save_integrals = 0;
+  bool anneal = false;
+  double anneal_kt = 0.0;
+  int anneal_hold = 50, anneal_cycles = 50;
+  std::unique_ptr<Workspace> ws;
+};
+
+struct _tblite_result {
+  int nat = 0, nsh = 0, nao = 0;
+  bool has_energy = false, has_wfn = false;
+  double energy = 0.0;
+  std::vector<double> energies, gradient, sigma, qat, qsh, dpat, qpat, emo, focc, P, C, S, H, wbo;
+  int wbo_channels = 0;  // 1 closed shell; 2 (total, magnetisation) for open shell
+  double dipole[3] = {0, 0, 0}, quadrupole[6] = {0, 0, 0, 0, 0, 0};
+};
+
+
+// D4 model constants (damping, counting function, cutoffs) of the element-data pack
+void d4_model_constants(DevD4& d);
+// GFN2 scalar parameters of a calculator
+Gfn2Scalars gfn2_scalars(const _tblite_calculator* c);
+// electrons per spin channel (reference xtb/singlepoint.f90:140-156); throws on an impossible
+// combination of charge and unpaired electrons
+void electron_counts(const _tblite_calculator* c, const _tblite_structure* mol, double* nalp,
+                     double* nbet);
+// molecular dipole and traceless quadrupole from the atomic charges and multipoles
+// (wavefunction/mulliken.f90 get_molecular_dipole_moment / get_molecular_quadrupole_moment)
+void molecular_moments(const _tblite_structure* mol, _tblite_result* res);
+// the one-molecule single point (energy + gradient) into res
+void run_singlepoint(_tblite_context* ctx, const _tblite_structure* mol, _tblite_calculator* c,
+                     _tblite_result* res);

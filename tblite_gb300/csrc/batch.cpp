@@ -1,0 +1,855 @@
+// Batched ensemble driver: GFN2-xTB energy + gradient of many independent molecules with one
+// launch per SCF step for a whole size bucket, instead of one launch per molecule.
+//
+// Layout.  Molecules are sorted by orbital count (largest first) and grouped into size buckets
+// whose largest member sets the launch shape.  Every per-molecule array lives in one device
+// arena, in three regions:
+//   zeroed   S, H, D, Q and accumulators; then the results, zeroed and read back (one D2H)
+//   scratch  matrices and vectors that the SCF writes before it reads them
+//   uploaded basis, parameters, geometry and the start charges (one H2D from a pinned stage)
+// MolPtrs (one per molecule, in device memory) holds the slice pointers; batched kernels walk a
+// list of molecule indices with blockIdx.z and run the one-molecule arithmetic.
+//
+// SCF.  All molecules iterate in lockstep (the same iteration index, so the Broyden history
+// index is shared); after each iteration one small D2H of the per-molecule flags drops the
+// converged molecules from the launch lists.  The convergence test, the Broyden update and the
+// Fermi filling run per molecule on the device with each molecule's own settings.
+//
+// A molecule leaves the batch for the one-molecule path (which then reproduces exactly what a
+// plain call does, including its errors) when it is larger than the batched
+// tridiagonalisation holds, uses temperature annealing, would need more Broyden history than
+// the batch keeps, does not converge within its iteration limit, or fails (overlap not
+// positive definite, singular Broyden system).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <numeric>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/tblite_gb300_ext.h"
+#include "api_internal.h"
+
+using namespace tb;
+
+namespace tb {
+int batch_tridiag_max_n();
+}
+
+namespace {
+
+constexpr int HCAP = 48;  // Broyden history kept per molecule in the batch
+
+struct Arena {
+  char* dev = nullptr;
+  size_t dev_cap = 0;
+  char* host = nullptr;  // pinned stage for uploads and read-back
+  size_t host_cap = 0;
+  cudaStream_t stream = nullptr;
+  // size buckets run concurrently on side streams, forked from and joined into `stream`
+  static constexpr int NSIDE = 8;
+  cudaStream_t side[NSIDE] = {};
+  cudaEvent_t fork = nullptr, join[NSIDE] = {};
+  void reserve(size_t dbytes, size_t hbytes) {
+    if (dbytes > dev_cap) {
+      if (dev) cudaFree(dev);
+      dev = nullptr;
+      cuda_check(cudaMalloc(&dev, dbytes), "batch arena");
+      dev_cap = dbytes;
+    }
+    if (hbytes > host_cap) {
+      if (host) cudaFreeHost(host);
+      host = nullptr;
+      cuda_check(cudaMallocHost(&host, hbytes), "batch stage");
+      host_cap = hbytes;
+    }
+    if (!stream) {
+      cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "stream");
+      cuda_check(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming), "event");
+      for (int k = 0; k < NSIDE; ++k) {
+        cuda_check(cudaStreamCreateWithFlags(&side[k], cudaStreamNonBlocking), "stream");
+        cuda_check(cudaEventCreateWithFlags(&join[k], cudaEventDisableTiming), "event");
+      }
+    }
+  }
+};
+std::mutex g_batch_mutex;
+Arena g_arena;
+int g_last_fallbacks = 0;
+double g_last_device_ms = 0.0;  // device time of the last call's batched steps (CUDA events)
+std::vector<int> g_last_iters;  // SCF iterations per molecule of the last call (0: not batched)
+
+// byte offsets of one region, 256-byte aligned pieces
+struct Region {
+  size_t size = 0;
+  size_t take(size_t bytes) {
+    const size_t o = size;
+    size += (bytes + 255) & ~(size_t)255;
+    return o;
+  }
+};
+
+enum { RZ = 0, RR = 1, RS = 2, RU = 3, NREG = 4 };  // zeroed, zeroed + read back, scratch, uploaded
+
+struct Piece {  // where a field of a molecule lives
+  int region;
+  size_t off, bytes;
+};
+
+struct Plan {
+  int idx;  // position in the caller's arrays
+  _tblite_calculator* c;
+  const _tblite_structure* mol;
+  _tblite_result* res;
+  int nat, nsh, nao, nd, memory, max_iter;
+  double nalp, nbet;
+  bool has_d4;
+  // offsets (region, offset) of every array
+  Piece xyz, at_z, at_sh, sh_atom, sh_l, sh_nprim, sh_alpha, sh_coeff, sh_ao, ao_sh, ao_at, sh_se0,
+      sh_kcn, sh_shpoly, sh_zeta, sh_hub, sh_gam3, sh_refocc, at_en, at_rad, at_rcov, at_mprad,
+      at_vcn, at_dkern, at_qkern, at_repa, at_repz;
+  Piece d4_sp, d4_nref, d4_ngw, d4_refcn, d4_refq, d4_zeff, d4_gam, d4_r4r2, d4_rcov, d4_en,
+      d4_c6ref;
+  Piece d4_cn, d4_gw, d4_dgw, d4_gwv, d4_dgwdq, d4_dgwv_cn, d4_c6, d4_dc6, d4_e3, d4_dEdcn;
+  Piece cn, se, mrad, dmrdcn, S, H, D, Q, F, P, C, scratch, emo, focc;
+  Piece qsh, qat, dpat, qpat, qsh_o, qat_o, dpat_o, qpat_o, vsh, vat, vdp, vqp, vao;
+  Piece mull, eband, eelec, erep, vec_out, scal, icount;
+  Piece bq, bqlast, bdq, bdqlast, bdf, bu, ba, bomega, bwork, bstatus;
+  Piece grad, sigma, sig_at, dEdcn;
+  Piece X, A, T1, Y, lu, ed, ee, etau, epv, escal, estatus, conv;
+};
+
+struct Bucket {
+  int first, last;  // range in the sorted plan
+  int nat_max = 0, nsh_max = 0, nao_max = 0, nd_max = 0;
+};
+
+template <class T>
+Piece piece(Region* regs, int r, size_t count) {
+  Piece p;
+  p.region = r;
+  p.bytes = sizeof(T) * std::max<size_t>(count, 1);
+  p.off = regs[r].take(p.bytes);
+  return p;
+}
+
+void layout(Plan& pl, Region* R) {
+  const size_t na = pl.nat, ns = pl.nsh, n = pl.nao, nn = n * n, nd = pl.nd;
+  const size_t hm = (size_t)std::min(pl.memory, HCAP);
+  // uploaded: basis, parameters, geometry, start charges
+  pl.xyz = piece<double>(R, RU, 3 * na);
+  pl.at_z = piece<int>(R, RU, na);
+  pl.at_sh = piece<int>(R, RU, na + 1);
+  pl.sh_atom = piece<int>(R, RU, ns);
+  pl.sh_l = piece<int>(R, RU, ns);
+  pl.sh_nprim = piece<int>(R, RU, ns);
+  pl.sh_alpha = piece<double>(R, RU, ns * MAXG);
+  pl.sh_coeff = piece<double>(R, RU, ns * MAXG);
+  pl.sh_ao = piece<int>(R, RU, ns);
+  pl.ao_sh = piece<int>(R, RU, n);
+  pl.ao_at = piece<int>(R, RU, n);
+  for (Piece* p : {&pl.sh_se0, &pl.sh_kcn, &pl.sh_shpoly, &pl.sh_zeta, &pl.sh_hub, &pl.sh_gam3,
+                   &pl.sh_refocc})
+    *p = piece<double>(R, RU, ns);
+  for (Piece* p : {&pl.at_en, &pl.at_rad, &pl.at_rcov, &pl.at_mprad, &pl.at_vcn, &pl.at_dkern,
+                   &pl.at_qkern, &pl.at_repa, &pl.at_repz})
+    *p = piece<double>(R, RU, na);
+  if (pl.has_d4) {
+    pl.d4_sp = piece<int>(R, RU, na);
+    pl.d4_nref = piece<int>(R, RU, na);
+    pl.d4_ngw = piece<int>(R, RU, na * D4_MREF);
+    pl.d4_refcn = piece<double>(R, RU, na * D4_MREF);
+    pl.d4_refq = piece<double>(R, RU, na * D4_MREF);
+    for (Piece* p : {&pl.d4_zeff, &pl.d4_gam, &pl.d4_r4r2, &pl.d4_rcov, &pl.d4_en})
+      *p = piece<double>(R, RU, na);
+    pl.d4_c6ref = piece<double>(R, RU, pl.c->d4_c6ref.size());
+  }
+  pl.qsh = piece<double>(R, RU, ns);
+  pl.qat = piece<double>(R, RU, na);
+  pl.dpat = piece<double>(R, RU, 3 * na);
+  pl.qpat = piece<double>(R, RU, 6 * na);
+  // zeroed: integrals (screened pairs stay zero), accumulators, results
+  pl.S = piece<double>(R, RZ, nn);
+  pl.H = piece<double>(R, RZ, nn);
+  pl.D = piece<double>(R, RZ, 3 * nn);
+  pl.Q = piece<double>(R, RZ, 6 * nn);
+  pl.dEdcn = piece<double>(R, RZ, na);
+  pl.conv = piece<double>(R, RZ, 3);
+  pl.bstatus = piece<int>(R, RZ, 1);
+  pl.estatus = piece<int>(R, RZ, 1);
+  if (pl.has_d4) pl.d4_dEdcn = piece<double>(R, RZ, na);
+  // zeroed and read back
+  pl.grad = piece<double>(R, RR, 3 * na);
+  pl.sig_at = piece<double>(R, RR, 9 * na);
+  pl.sigma = piece<double>(R, RR, 9);
+  pl.qsh_o = piece<double>(R, RR, ns);
+  pl.qat_o = piece<double>(R, RR, na);
+  pl.dpat_o = piece<double>(R, RR, 3 * na);
+  pl.qpat_o = piece<double>(R, RR, 6 * na);
+  pl.emo = piece<double>(R, RR, n);
+  pl.focc = piece<double>(R, RR, 3 * n);
+  pl.eelec = piece<double>(R, RR, na);
+  pl.erep = piece<double>(R, RR, na);
+  if (pl.has_d4) pl.d4_e3 = piece<double>(R, RR, na);
+  // scratch
+  pl.cn = piece<double>(R, RS, na);
+  pl.se = piece<double>(R, RS, ns);
+  pl.mrad = piece<double>(R, RS, na);
+  pl.dmrdcn = piece<double>(R, RS, na);
+  for (Piece* p : {&pl.F, &pl.P, &pl.C, &pl.scratch, &pl.X, &pl.A, &pl.T1, &pl.Y})
+    *p = piece<double>(R, RS, nn);
+  pl.lu = piece<double>(R, RS, 5 * nn);
+  pl.vsh = piece<double>(R, RS, ns);
+  pl.vat = piece<double>(R, RS, na);
+  pl.vdp = piece<double>(R, RS, 3 * na);
+  pl.vqp = piece<double>(R, RS, 6 * na);
+  pl.vao = piece<double>(R, RS, n);
+  pl.mull = piece<double>(R, RS, (size_t)mulliken_chunks((int)n) * 11 * n);
+  pl.eband = piece<double>(R, RS, na);
+  pl.vec_out = piece<double>(R, RS, std::max(nd, n));
+  pl.scal = piece<double>(R, RS, 8);
+  pl.icount = piece<int>(R, RS, 4);
+  for (Piece* p : {&pl.bq, &pl.bqlast, &pl.bdq, &pl.bdqlast}) *p = piece<double>(R, RS, nd);
+  pl.bdf = piece<double>(R, RS, nd * hm);
+  pl.bu = piece<double>(R, RS, nd * hm);
+  pl.ba = piece<double>(R, RS, hm * hm);
+  pl.bomega = piece<double>(R, RS, hm);
+  pl.bwork = piece<double>(R, RS, hm * hm + 2 * hm + 64);
+  pl.ed = piece<double>(R, RS, n + 1);
+  pl.ee = piece<double>(R, RS, n + 1);
+  pl.etau = piece<double>(R, RS, n + 1);
+  pl.epv = piece<double>(R, RS, 4 * (n + 1));
+  pl.escal = piece<double>(R, RS, 8);
+  if (pl.has_d4) {
+    pl.d4_cn = piece<double>(R, RS, na);
+    for (Piece* p : {&pl.d4_gw, &pl.d4_dgw, &pl.d4_gwv, &pl.d4_dgwdq, &pl.d4_dgwv_cn})
+      *p = piece<double>(R, RS, na * D4_MREF);
+    pl.d4_c6 = piece<double>(R, RS, na * na);
+    pl.d4_dc6 = piece<double>(R, RS, na * na);
+  }
+}
+
+struct Bases {
+  char* base[NREG];
+  template <class T>
+  T* at(const Piece& p) const {
+    return reinterpret_cast<T*>(base[p.region] + p.off);
+  }
+};
+
+template <class T>
+void stage(const Bases& hb, const Piece& p, const std::vector<T>& v) {
+  if (!v.empty()) std::memcpy(hb.at<T>(p), v.data(), sizeof(T) * v.size());
+}
+
+MolPtrs make_ptrs(const Plan& pl, const Bases& db) {
+  MolPtrs q{};
+  DevMol& m = q.m;
+  m.nat = pl.nat;
+  m.nsh = pl.nsh;
+  m.nao = pl.nao;
+  m.xyz = db.at<double>(pl.xyz);
+  m.at_z = db.at<int>(pl.at_z);
+  m.at_sh = db.at<int>(pl.at_sh);
+  m.sh_atom = db.at<int>(pl.sh_atom);
+  m.sh_l = db.at<int>(pl.sh_l);
+  m.sh_nprim = db.at<int>(pl.sh_nprim);
+  m.sh_alpha = db.at<double>(pl.sh_alpha);
+  m.sh_coeff = db.at<double>(pl.sh_coeff);
+  m.sh_ao = db.at<int>(pl.sh_ao);
+  m.ao_sh = db.at<int>(pl.ao_sh);
+  m.ao_at = db.at<int>(pl.ao_at);
+  m.sh_se0 = db.at<double>(pl.sh_se0);
+  m.sh_kcn = db.at<double>(pl.sh_kcn);
+  m.sh_shpoly = db.at<double>(pl.sh_shpoly);
+  m.sh_zeta = db.at<double>(pl.sh_zeta);
+  m.sh_hub = db.at<double>(pl.sh_hub);
+  m.sh_gam3 = db.at<double>(pl.sh_gam3);
+  m.sh_refocc = db.at<double>(pl.sh_refocc);
+  m.at_en = db.at<double>(pl.at_en);
+  m.at_rad = db.at<double>(pl.at_rad);
+  m.at_rcov = db.at<double>(pl.at_rcov);
+  m.at_mprad = db.at<double>(pl.at_mprad);
+  m.at_vcn = db.at<double>(pl.at_vcn);
+  m.at_dkern = db.at<double>(pl.at_dkern);
+  m.at_qkern = db.at<double>(pl.at_qkern);
+  m.at_repa = db.at<double>(pl.at_repa);
+  m.at_repz = db.at<double>(pl.at_repz);
+  q.has_d4 = pl.has_d4 ? 1 : 0;
+  if (pl.has_d4) {
+    DevD4& d = q.d4;
+    d.nsp = pl.c->d4_nsp;
+    d.sp = db.at<int>(pl.d4_sp);
+    d.nref = db.at<int>(pl.d4_nref);
+    d.ngw = db.at<int>(pl.d4_ngw);
+    d.refcn = db.at<double>(pl.d4_refcn);
+    d.refq = db.at<double>(pl.d4_refq);
+    d.zeff = db.at<double>(pl.d4_zeff);
+    d.gam = db.at<double>(pl.d4_gam);
+    d.r4r2 = db.at<double>(pl.d4_r4r2);
+    d.rcov = db.at<double>(pl.d4_rcov);
+    d.en = db.at<double>(pl.d4_en);
+    d.c6ref = db.at<double>(pl.d4_c6ref);
+    d4_model_constants(d);
+    D4Work& w = q.d4w;
+    w.cn = db.at<double>(pl.d4_cn);
+    w.gw = db.at<double>(pl.d4_gw);
+    w.dgw = db.at<double>(pl.d4_dgw);
+    w.gwv = db.at<double>(pl.d4_gwv);
+    w.dgwdq = db.at<double>(pl.d4_dgwdq);
+    w.dgwv_cn = db.at<double>(pl.d4_dgwv_cn);
+    w.c6 = db.at<double>(pl.d4_c6);
+    w.dc6 = db.at<double>(pl.d4_dc6);
+    w.e3 = db.at<double>(pl.d4_e3);
+    w.dEdcn = db.at<double>(pl.d4_dEdcn);
+  }
+  q.nd = pl.nd;
+  q.mull_chunks = mulliken_chunks(pl.nao);
+  q.memory = std::min(pl.memory, HCAP);
+  q.nalp = pl.nalp;
+  q.nbet = pl.nbet;
+  q.kt = pl.c->etemp;
+  q.damp = pl.c->damping;
+  q.econv = 1.0e-6 * pl.c->accuracy;
+  q.pconv = 2.0e-5 * pl.c->accuracy;
+  q.h0_cutoff = gfn2_scalars(pl.c).h0_cutoff;
+  q.cn = db.at<double>(pl.cn);
+  q.se = db.at<double>(pl.se);
+  q.mrad = db.at<double>(pl.mrad);
+  q.dmrdcn = db.at<double>(pl.dmrdcn);
+  q.S = db.at<double>(pl.S);
+  q.H = db.at<double>(pl.H);
+  q.D = db.at<double>(pl.D);
+  q.Q = db.at<double>(pl.Q);
+  q.F = db.at<double>(pl.F);
+  q.P = db.at<double>(pl.P);
+  q.C = db.at<double>(pl.C);
+  q.scratch = db.at<double>(pl.scratch);
+  q.emo = db.at<double>(pl.emo);
+  q.focc = db.at<double>(pl.focc);
+  q.qsh = db.at<double>(pl.qsh);
+  q.qat = db.at<double>(pl.qat);
+  q.dpat = db.at<double>(pl.dpat);
+  q.qpat = db.at<double>(pl.qpat);
+  q.qsh_o = db.at<double>(pl.qsh_o);
+  q.qat_o = db.at<double>(pl.qat_o);
+  q.dpat_o = db.at<double>(pl.dpat_o);
+  q.qpat_o = db.at<double>(pl.qpat_o);
+  q.vsh = db.at<double>(pl.vsh);
+  q.vat = db.at<double>(pl.vat);
+  q.vdp = db.at<double>(pl.vdp);
+  q.vqp = db.at<double>(pl.vqp);
+  q.vao = db.at<double>(pl.vao);
+  q.mull = db.at<double>(pl.mull);
+  q.eband = db.at<double>(pl.eband);
+  q.eelec = db.at<double>(pl.eelec);
+  q.erep = db.at<double>(pl.erep);
+  q.vec_out = db.at<double>(pl.vec_out);
+  q.scal = db.at<double>(pl.scal);
+  q.icount = db.at<int>(pl.icount);
+  q.bq = db.at<double>(pl.bq);
+  q.bqlast = db.at<double>(pl.bqlast);
+  q.bdq = db.at<double>(pl.bdq);
+  q.bdqlast = db.at<double>(pl.bdqlast);
+  q.bdf = db.at<double>(pl.bdf);
+  q.bu = db.at<double>(pl.bu);
+  q.ba = db.at<double>(pl.ba);
+  q.bomega = db.at<double>(pl.bomega);
+  q.bwork = db.at<double>(pl.bwork);
+  q.bstatus = db.at<int>(pl.bstatus);
+  q.grad = db.at<double>(pl.grad);
+  q.sigma = db.at<double>(pl.sigma);
+  q.sig_at = db.at<double>(pl.sig_at);
+  q.dEdcn = db.at<double>(pl.dEdcn);
+  q.X = db.at<double>(pl.X);
+  q.A = db.at<double>(pl.A);
+  q.T1 = db.at<double>(pl.T1);
+  q.Y = db.at<double>(pl.Y);
+  q.lu = db.at<double>(pl.lu);
+  q.ed = db.at<double>(pl.ed);
+  q.ee = db.at<double>(pl.ee);
+  q.etau = db.at<double>(pl.etau);
+  q.ew = nullptr;  // the batched eigenvalues go straight to emo
+  q.epv = db.at<double>(pl.epv);
+  q.escal = db.at<double>(pl.escal);
+  q.estatus = db.at<int>(pl.estatus);
+  q.conv = db.at<double>(pl.conv);
+  return q;
+}
+
+// start charges (wavefunction/guess.f90:51-120): restart from a compatible result, else SAD
+void start_charges(const Plan& pl, std::vector<double>& qsh, std::vector<double>& qat,
+                   std::vector<double>& dp, std::vector<double>& qp) {
+  const _tblite_calculator* c = pl.c;
+  const _tblite_result* res = pl.res;
+  const int nat = pl.nat, nsh = pl.nsh;
+  if (res->has_wfn && res->nat == nat && res->nsh == nsh && res->nao == pl.nao) {
+    qsh = res->qsh;
+    qat = res->qat;
+    dp = res->dpat;
+    qp = res->qpat;
+    return;
+  }
+  qsh.assign(nsh, 0.0);
+  qat.assign(nat, pl.mol->charge / nat);
+  dp.assign(3 * nat, 0.0);
+  qp.assign(6 * nat, 0.0);
+  std::vector<double> n0at(nat, 0.0);
+  for (int i = 0; i < nsh; ++i) n0at[c->sh_atom[i]] += c->sh_refocc[i];
+  for (int i = 0; i < nsh; ++i) qsh[i] = c->sh_refocc[i] / n0at[c->sh_atom[i]] * qat[c->sh_atom[i]];
+}
+
+// size buckets: consecutive molecules (sorted by orbital count, descending) while the count
+// stays above 3/4 of the bucket's largest
+std::vector<Bucket> make_buckets(const std::vector<Plan>& plans) {
+  std::vector<Bucket> out;
+  int i = 0;
+  const int np = (int)plans.size();
+  while (i < np) {
+    Bucket b;
+    b.first = i;
+    const int top = plans[i].nao;
+    int j = i;
+    while (j < np && 4 * plans[j].nao >= 3 * top && j - i < 65535) {
+      b.nat_max = std::max(b.nat_max, plans[j].nat);
+      b.nsh_max = std::max(b.nsh_max, plans[j].nsh);
+      b.nao_max = std::max(b.nao_max, plans[j].nao);
+      b.nd_max = std::max(b.nd_max, plans[j].nd);
+      ++j;
+    }
+    b.last = j;
+    out.push_back(b);
+    i = j;
+  }
+  return out;
+}
+
+struct Lists {
+  std::vector<int> host;           // molecule indices, grouped by bucket
+  std::vector<int> begin, count;   // per bucket
+};
+
+// one chunk of molecules through setup, SCF and gradient; fills results of the converged
+// ones, returns the plan indices that must take the one-molecule path
+std::vector<int> run_chunk(std::vector<Plan>& plans, Arena& ar, _tblite_context* ctx) {
+  const int np = (int)plans.size();
+  Region R[NREG];
+  for (auto& pl : plans) layout(pl, R);
+  // molecule tables and launch lists live after the three regions
+  Region tail;
+  const size_t off_ptrs = tail.take(sizeof(MolPtrs) * np);
+  const size_t off_list = tail.take(sizeof(int) * np);
+  const size_t off_flag = tail.take(sizeof(int) * np);
+  const size_t dbytes = R[RZ].size + R[RR].size + R[RS].size + R[RU].size + tail.size;
+  const size_t hbytes = std::max(R[RU].size, R[RR].size) + tail.size;
+  ar.reserve(dbytes, hbytes);
+  cudaStream_t s = ar.stream;
+  Bases db;
+  db.base[RZ] = ar.dev;
+  db.base[RR] = db.base[RZ] + R[RZ].size;
+  db.base[RS] = db.base[RR] + R[RR].size;
+  db.base[RU] = db.base[RS] + R[RS].size;
+  char* dtail = db.base[RU] + R[RU].size;
+  MolPtrs* d_ptrs = reinterpret_cast<MolPtrs*>(dtail + off_ptrs);
+  int* d_list = reinterpret_cast<int*>(dtail + off_list);
+  int* d_flag = reinterpret_cast<int*>(dtail + off_flag);
+  // host stage: uploaded region first, then the tables
+  Bases hb{{nullptr, nullptr, nullptr, ar.host}};
+  std::vector<double> qsh, qat, dp, qp;
+  for (auto& pl : plans) {
+    const _tblite_calculator* c = pl.c;
+    stage(hb, pl.xyz, pl.mol->xyz);
+    stage(hb, pl.at_z, c->at_z);
+    stage(hb, pl.at_sh, c->at_sh);
+    stage(hb, pl.sh_atom, c->sh_atom);
+    stage(hb, pl.sh_l, c->sh_l);
+    stage(hb, pl.sh_nprim, c->sh_nprim);
+    stage(hb, pl.sh_alpha, c->sh_alpha);
+    stage(hb, pl.sh_coeff, c->sh_coeff);
+    stage(hb, pl.sh_ao, c->sh_ao);
+    stage(hb, pl.ao_sh, c->ao_sh);
+    stage(hb, pl.ao_at, c->ao_at);
+    stage(hb, pl.sh_se0, c->sh_se0);
+    stage(hb, pl.sh_kcn, c->sh_kcn);
+    stage(hb, pl.sh_shpoly, c->sh_shpoly);
+    stage(hb, pl.sh_zeta, c->sh_zeta);
+    stage(hb, pl.sh_hub, c->sh_hub);
+    stage(hb, pl.sh_gam3, c->sh_gam3);
+    stage(hb, pl.sh_refocc, c->sh_refocc);
+    stage(hb, pl.at_en, c->at_en);
+    stage(hb, pl.at_rad, c->at_rad);
+    stage(hb, pl.at_rcov, c->at_rcov);
+    stage(hb, pl.at_mprad, c->at_mprad);
+    stage(hb, pl.at_vcn, c->at_vcn);
+    stage(hb, pl.at_dkern, c->at_dkern);
+    stage(hb, pl.at_qkern, c->at_qkern);
+    stage(hb, pl.at_repa, c->at_repa);
+    stage(hb, pl.at_repz, c->at_repz);
+    if (pl.has_d4) {
+      stage(hb, pl.d4_sp, c->d4_sp);
+      stage(hb, pl.d4_nref, c->d4_nref);
+      stage(hb, pl.d4_ngw, c->d4_ngw);
+      stage(hb, pl.d4_refcn, c->d4_refcn);
+      stage(hb, pl.d4_refq, c->d4_refq);
+      stage(hb, pl.d4_zeff, c->d4_zeff);
+      stage(hb, pl.d4_gam, c->d4_gam);
+      stage(hb, pl.d4_r4r2, c->d4_r4r2);
+      stage(hb, pl.d4_rcov, c->d4_rcov);
+      stage(hb, pl.d4_en, c->d4_en);
+      stage(hb, pl.d4_c6ref, c->d4_c6ref);
+    }
+    start_charges(pl, qsh, qat, dp, qp);
+    stage(hb, pl.qsh, qsh);
+    stage(hb, pl.qat, qat);
+    stage(hb, pl.dpat, dp);
+    stage(hb, pl.qpat, qp);
+  }
+  cuda_check(cudaMemcpyAsync(db.base[RU], ar.host, R[RU].size, cudaMemcpyHostToDevice, s),
+             "batch upload");
+  cuda_check(cudaMemsetAsync(db.base[RZ], 0, R[RZ].size + R[RR].size, s), "batch zero");
+  // molecule table (after the upload completes the stage can be reused)
+  stream_wait(s);
+  MolPtrs* h_ptrs = reinterpret_cast<MolPtrs*>(ar.host);
+  for (int i = 0; i < np; ++i) {
+    h_ptrs[i] = make_ptrs(plans[i], db);
+    h_ptrs[i].flag = d_flag + i;
+  }
+  cuda_check(cudaMemcpyAsync(d_ptrs, h_ptrs, sizeof(MolPtrs) * np, cudaMemcpyHostToDevice, s),
+             "batch table");
+  cuda_check(cudaMemsetAsync(d_flag, 0, sizeof(int) * np, s), "flags");
+  stream_wait(s);
+
+  const std::vector<Bucket> buckets = make_buckets(plans);
+  const int nb = (int)buckets.size();
+  std::vector<char> active(np, 1);
+  std::vector<int> h_flag(np, 0);
+  int* h_list = reinterpret_cast<int*>(ar.host);
+  std::vector<BatchLaunch> launch(nb);
+  auto upload_lists = [&](const std::vector<char>& sel) {
+    int pos = 0;
+    for (int bi = 0; bi < nb; ++bi) {
+      const Bucket& b = buckets[bi];
+      BatchLaunch& L = launch[bi];
+      L.mp = d_ptrs;
+      L.list = d_list + pos;
+      L.nat_max = b.nat_max;
+      L.nsh_max = b.nsh_max;
+      L.nao_max = b.nao_max;
+      L.nd_max = b.nd_max;
+      L.s = s;
+      int cnt = 0;
+      for (int i = b.first; i < b.last; ++i)
+        if (sel[i]) h_list[pos + cnt++] = i;
+      L.count = cnt;
+      pos += cnt;
+    }
+    if (pos)
+      cuda_check(cudaMemcpyAsync(d_list, h_list, sizeof(int) * pos, cudaMemcpyHostToDevice, s),
+                 "lists");
+    stream_wait(s);  // the host list buffer is rewritten next time
+    return pos;
+  };
+  // every bucket's steps on its own side stream (buckets touch disjoint molecules), ordered
+  // after the work already on the main stream and joined back into it
+  auto each = [&](auto&& fn) {
+    cuda_check(cudaEventRecord(ar.fork, s), "fork");
+    int k = 0;
+    for (auto& L : launch) {
+      if (!L.count) continue;
+      const int slot = k++ % Arena::NSIDE;
+      L.s = ar.side[slot];
+      cuda_check(cudaStreamWaitEvent(L.s, ar.fork, 0), "fork");
+      fn(L);
+      cuda_check(cudaEventRecord(ar.join[slot], L.s), "join");
+      cuda_check(cudaStreamWaitEvent(s, ar.join[slot], 0), "join");
+    }
+  };
+  const Gfn2Scalars p = gfn2_scalars(plans[0].c);  // h0_cutoff is taken per molecule
+
+  // geometry setup
+  upload_lists(active);
+  cudaEvent_t ev0, ev1;
+  cuda_check(cudaEventCreate(&ev0), "event");
+  cuda_check(cudaEventCreate(&ev1), "event");
+  cuda_check(cudaEventRecord(ev0, s), "event");
+  each([&](BatchLaunch& L) {
+    launch_cn_b(L, p);
+    launch_setup_levels_b(L, p);
+    launch_build_h0_b(L, p);
+    launch_repulsion_b(L, p);
+    d4_setup_b(L);
+    cholesky_inverse_b(L);
+  });
+  cuda_check(cudaMemcpyAsync(h_flag.data(), d_flag, sizeof(int) * np, cudaMemcpyDeviceToHost, s),
+             "flags");
+  stream_wait(s);
+  cuda_check(cudaGetLastError(), "batch setup");
+  std::vector<int> leave;
+  for (int i = 0; i < np; ++i)
+    if (h_flag[i] < 0) {
+      active[i] = 0;
+      leave.push_back(i);
+    }
+  std::vector<char> done(np, 0);
+  int max_iter = 0;
+  for (auto& pl : plans) max_iter = std::max(max_iter, pl.max_iter);
+  int iscf = 0;
+  int nactive = upload_lists(active);
+  auto t_iter = std::chrono::steady_clock::now();
+  while (nactive > 0 && iscf < max_iter) {
+    if (iscf > 0) {
+      each([&](BatchLaunch& L) {
+        launch_broyden_b(L, iscf);
+        launch_unpack_b(L);
+      });
+    }
+    ++iscf;
+    each([&](BatchLaunch& L) {
+      launch_coulomb_potential_b(L, p);
+      d4_potential_b(L);
+      launch_vao_b(L);
+      launch_fock_b(L);
+      launch_pack_b(L, false);
+      eigen_values_b(L);
+      launch_fermi_b(L);
+      eigen_vectors_b(L);
+      density_b(L, false);
+      launch_mulliken_b(L);
+      launch_pack_b(L, true);
+      launch_diff_b(L);
+      launch_eelec_init_b(L);
+      launch_coulomb_energy_b(L, p);
+      d4_energy_b(L);
+      launch_converge_b(L);
+    });
+    cuda_check(cudaMemcpyAsync(h_flag.data(), d_flag, sizeof(int) * np, cudaMemcpyDeviceToHost, s),
+               "flags");
+    stream_wait(s);
+    cuda_check(cudaGetLastError(), "batch scf");
+    for (int i = 0; i < np; ++i) {
+      if (!active[i]) continue;
+      const Plan& pl = plans[i];
+      if (h_flag[i] == 1) {
+        active[i] = 0;
+        done[i] = 1;
+        if (pl.idx < (int)g_last_iters.size()) g_last_iters[pl.idx] = iscf;
+      } else if (h_flag[i] < 0 || iscf >= pl.max_iter ||
+                 (iscf > HCAP && pl.memory > HCAP)) {
+        active[i] = 0;
+        leave.push_back(i);
+      }
+    }
+    const int nbefore = nactive;
+    nactive = upload_lists(active);
+    if (ctx->verbosity > 1) {
+      const auto now = std::chrono::steady_clock::now();
+      char buf[160];
+      snprintf(buf, sizeof(buf), "batch iteration %3d: %6d molecules, %6d still running, %9.3f ms",
+               iscf, nbefore, nactive,
+               std::chrono::duration<double, std::milli>(now - t_iter).count());
+      ctx->message(buf);
+      t_iter = now;
+    }
+  }
+  for (int i = 0; i < np; ++i)
+    if (active[i]) leave.push_back(i);
+  float scf_ms = 0.f;
+
+  // gradient of the converged molecules: Coulomb and D4 at the output moments, W into F,
+  // H0 gradient with the last potential, CN chain rule
+  if (upload_lists(done) > 0) {
+    each([&](BatchLaunch& L) {
+      launch_coulomb_gradient_b(L, p);
+      d4_gradient_b(L);
+      launch_fe_b(L);
+      density_b(L, true);
+      launch_h0_gradient_b(L, p);
+      launch_cn_grad_b(L, p);
+    });
+    cuda_check(cudaEventRecord(ev1, s), "event");
+    cuda_check(cudaMemcpyAsync(ar.host, db.base[RR], R[RR].size, cudaMemcpyDeviceToHost, s),
+               "batch results");
+    stream_wait(s);
+    cuda_check(cudaGetLastError(), "batch gradient");
+    cuda_check(cudaEventElapsedTime(&scf_ms, ev0, ev1), "event");
+    const Bases hz{{nullptr, ar.host, nullptr, nullptr}};
+    for (int i = 0; i < np; ++i) {
+      if (!done[i]) continue;
+      const Plan& pl = plans[i];
+      _tblite_result* res = pl.res;
+      const int nat = pl.nat, n = pl.nao;
+      auto get = [&](const Piece& pc, size_t count, std::vector<double>& out) {
+        const double* src = hz.at<double>(pc);
+        out.assign(src, src + count);
+      };
+      std::vector<double> eelec, erep, e3, sig_at, sigma;
+      get(pl.eelec, nat, eelec);
+      get(pl.erep, nat, erep);
+      if (pl.has_d4) get(pl.d4_e3, nat, e3);
+      res->nat = nat;
+      res->nsh = pl.nsh;
+      res->nao = n;
+      res->energies.assign(nat, 0.0);
+      res->energy = 0.0;
+      for (int a = 0; a < nat; ++a) {
+        double e = erep[a] + (pl.has_d4 ? e3[a] : 0.0);  // repulsion + three-body dispersion
+        e += eelec[a];
+        res->energies[a] = e;
+        res->energy += e;
+      }
+      res->has_energy = true;
+      get(pl.grad, 3 * nat, res->gradient);
+      get(pl.sig_at, 9 * nat, sig_at);
+      get(pl.sigma, 9, sigma);
+      res->sigma.assign(9, 0.0);
+      for (int k = 0; k < 9; ++k) {
+        double acc = sigma[k];
+        for (int a = 0; a < nat; ++a) acc += sig_at[9 * a + k];
+        res->sigma[k] = acc;
+      }
+      get(pl.qsh_o, pl.nsh, res->qsh);
+      get(pl.qat_o, nat, res->qat);
+      get(pl.dpat_o, 3 * nat, res->dpat);
+      get(pl.qpat_o, 6 * nat, res->qpat);
+      get(pl.emo, n, res->emo);
+      get(pl.focc, n, res->focc);
+      res->P.clear();
+      res->C.clear();
+      res->S.clear();
+      res->H.clear();
+      res->wbo.clear();
+      res->wbo_channels = 0;
+      res->has_wfn = true;
+      molecular_moments(pl.mol, res);
+    }
+  }
+  cudaEventDestroy(ev0);
+  cudaEventDestroy(ev1);
+  g_last_device_ms += scf_ms;
+  return leave;
+}
+
+// device bytes one molecule needs in the batch (for chunking)
+size_t molecule_bytes(const Plan& pl) {
+  Plan tmp = pl;
+  Region R[NREG];
+  layout(tmp, R);
+  return R[RZ].size + R[RR].size + R[RS].size + R[RU].size + sizeof(MolPtrs) + 64;
+}
+
+}  // namespace
+
+extern "C" int tblite_gb300_batch_singlepoint(tblite_context ctx, int nmol,
+                                              const tblite_structure* mols,
+                                              const tblite_calculator* calcs,
+                                              const tblite_result* results, int* status) {
+  if (!ctx) return nmol;
+  if (nmol <= 0) return 0;
+  if (!mols || !calcs || !results) {
+    ctx->push("Batch input arrays are missing");
+    return nmol;
+  }
+  std::vector<int> st(nmol, 0);
+  std::vector<Plan> plans;
+  std::vector<int> plain;  // molecules for the one-molecule path
+  const int tri_max = batch_tridiag_max_n();
+  for (int i = 0; i < nmol; ++i) {
+    _tblite_calculator* c = calcs[i];
+    const _tblite_structure* mol = mols[i];
+    _tblite_result* res = results[i];
+    if (!c || !mol || !res) {
+      ctx->push("Batch entry " + std::to_string(i) + ": structure, calculator or result missing");
+      st[i] = 1;
+      continue;
+    }
+    if (mol->nat != c->nat) {
+      ctx->push("Batch entry " + std::to_string(i) + ": structure does not match calculator");
+      st[i] = 1;
+      continue;
+    }
+    Plan pl{};
+    pl.idx = i;
+    pl.c = c;
+    pl.mol = mol;
+    pl.res = res;
+    pl.nat = c->nat;
+    pl.nsh = c->nsh;
+    pl.nao = c->nao;
+    pl.nd = c->nsh + 9 * c->nat;
+    pl.max_iter = c->max_iter;
+    pl.memory = c->memory > 0 ? std::min(c->memory, c->max_iter) : c->max_iter;
+    pl.has_d4 = c->has_d4;
+    try {
+      electron_counts(c, mol, &pl.nalp, &pl.nbet);
+    } catch (const std::exception& e) {
+      ctx->push("Batch entry " + std::to_string(i) + ": " + e.what());
+      st[i] = 1;
+      continue;
+    }
+    const bool anneal = c->anneal && c->anneal_kt > c->etemp;
+    if (pl.nao > tri_max || anneal || pl.max_iter < 1) {
+      plain.push_back(i);
+      continue;
+    }
+    plans.push_back(pl);
+  }
+  // largest first: the size buckets follow the sorted order
+  std::stable_sort(plans.begin(), plans.end(),
+                   [](const Plan& a, const Plan& b) { return a.nao > b.nao; });
+  try {
+    std::lock_guard<std::mutex> lock(g_batch_mutex);
+    g_last_device_ms = 0.0;
+    g_last_iters.assign(nmol, 0);
+    prof_reset();
+    // chunks of at most ~24 GB of device memory
+    const size_t budget = (size_t)24 << 30;
+    size_t i0 = 0;
+    while (i0 < plans.size()) {
+      size_t i1 = i0, bytes = 0;
+      while (i1 < plans.size() && (i1 == i0 || bytes + molecule_bytes(plans[i1]) <= budget)) {
+        bytes += molecule_bytes(plans[i1]);
+        ++i1;
+      }
+      std::vector<Plan> chunk(plans.begin() + i0, plans.begin() + i1);
+      const std::vector<int> leave = run_chunk(chunk, g_arena, ctx);
+      for (int k : leave) plain.push_back(chunk[k].idx);
+      i0 = i1;
+    }
+    prof_collect();
+  } catch (const std::exception& e) {
+    ctx->push(std::string("batched single points failed: ") + e.what());
+    for (int i = 0; i < nmol; ++i) st[i] = 1;
+    if (status)
+      for (int i = 0; i < nmol; ++i) status[i] = st[i];
+    return nmol;
+  }
+  // the one-molecule path for the rest (reproduces a plain call, errors included)
+  std::sort(plain.begin(), plain.end());
+  g_last_fallbacks = (int)plain.size();
+  for (int i : plain) {
+    try {
+      run_singlepoint(ctx, mols[i], calcs[i], results[i]);
+    } catch (const std::exception& e) {
+      ctx->push("Batch entry " + std::to_string(i) + ": " + e.what());
+      st[i] = 1;
+    }
+  }
+  int failed = 0;
+  for (int i = 0; i < nmol; ++i) failed += st[i];
+  if (status)
+    for (int i = 0; i < nmol; ++i) status[i] = st[i];
+  return failed;
+}
+
+extern "C" int tblite_gb300_batch_last_fallbacks(void) { return g_last_fallbacks; }
+extern "C" double tblite_gb300_batch_last_device_ms(void) { return g_last_device_ms; }
+extern "C" int tblite_gb300_batch_last_iterations(int* iterations, int nmol) {
+  const int m = std::min(nmol, (int)g_last_iters.size());
+  for (int i = 0; i < m && iterations; ++i) iterations[i] = g_last_iters[i];
+  return (int)g_last_iters.size();
+}

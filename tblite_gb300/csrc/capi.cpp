@@ -18,140 +18,9 @@
 #include "engine.h"
 #include "params_gfn2.inc"
 
+#include "api_internal.h"
+
 using namespace tb;
-
-// --------------------------------------------------------------------------------------
-// objects
-// --------------------------------------------------------------------------------------
-struct _tblite_error {
-  std::string msg;
-  bool set = false;
-};
-
-struct _tblite_context {
-  std::vector<std::string> errors;
-  tblite_logger_callback logger = nullptr;
-  void* userdata = nullptr;
-  int verbosity = 1;
-  int color = 0;
-  void push(const std::string& m) { errors.push_back(m); }
-  void message(const std::string& m) {
-    if (logger) {
-      std::string tmp = m;
-      logger(nullptr, tmp.data(), (int)tmp.size(), userdata);
-    } else if (verbosity > 0) {
-      printf("%s\n", m.c_str());
-    }
-  }
-};
-
-struct _tblite_structure {
-  int nat = 0;
-  std::vector<int> num;
-  std::vector<double> xyz;  // [nat][3] Bohr
-  double charge = 0.0;
-  int uhf = 0;
-};
-
-namespace {
-
-void cuda_check(cudaError_t e, const char* what) {
-  if (e != cudaSuccess)
-    throw std::runtime_error(std::string("CUDA error '") + cudaGetErrorString(e) + "' in " + what);
-}
-
-template <class T>
-struct DBuf {
-  T* p = nullptr;
-  size_t n = 0;
-  void alloc(size_t count) {
-    if (count <= n && p) return;
-    if (p) cudaFree(p);
-    p = nullptr;
-    cuda_check(cudaMalloc(&p, sizeof(T) * std::max<size_t>(count, 1)), "cudaMalloc");
-    n = count;
-  }
-  void upload(const std::vector<T>& h, cudaStream_t s) {
-    alloc(h.size());
-    if (!h.empty())
-      cuda_check(cudaMemcpyAsync(p, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice, s),
-                 "upload");
-  }
-  void download(std::vector<T>& h, size_t count, cudaStream_t s) const {
-    h.resize(count);
-    if (count)
-      cuda_check(cudaMemcpyAsync(h.data(), p, sizeof(T) * count, cudaMemcpyDeviceToHost, s),
-                 "download");
-  }
-  ~DBuf() {
-    if (p) cudaFree(p);
-  }
-};
-
-}  // namespace
-
-struct Workspace {
-  cudaStream_t stream = nullptr;
-  int nat = -1, nsh = -1, nao = -1, memory = -1;
-  // static molecule/basis data
-  DBuf<double> xyz, sh_alpha, sh_coeff, sh_se0, sh_kcn, sh_shpoly, sh_zeta, sh_hub, sh_gam3,
-      sh_refocc, at_en, at_rad, at_rcov, at_mprad, at_vcn, at_dkern, at_qkern, at_repa, at_repz;
-  DBuf<int> at_z, at_sh, sh_atom, sh_l, sh_nprim, sh_ao, ao_sh, ao_at;
-  // geometry dependent
-  DBuf<double> cn, se, mrad, dmrdcn, S, H, D, Q, F, C, P, W, emo, focc, scratch;
-  // SCF state
-  DBuf<double> qsh, qat, dpat, qpat, qsh_o, qat_o, dpat_o, qpat_o, vsh, vat, vdp, vqp, vao;
-  DBuf<double> mull, eband, eelec, erep, vec_out, scal;
-  DBuf<int> icount;
-  // Broyden
-  DBuf<double> b_q, b_qlast, b_dq, b_dqlast, b_df, b_u, b_a, b_omega, b_work;
-  DBuf<int> b_status;
-  // gradient
-  DBuf<double> grad, sigma, sig_at, dEdcn;
-  // D4 dispersion
-  DBuf<int> d4_sp, d4_nref, d4_ngw;
-  DBuf<double> d4_refcn, d4_refq, d4_zeff, d4_gam, d4_r4r2, d4_rcov, d4_en, d4_c6ref;
-  DBuf<double> d4_cn, d4_gw, d4_dgw, d4_gwv, d4_dgwdq, d4_dgwv_cn, d4_c6, d4_dc6, d4_e3, d4_dEdcn;
-  EigenSolver* eig = nullptr;
-  ~Workspace() {
-    if (eig) eigen_destroy(eig);
-    if (stream) cudaStreamDestroy(stream);
-  }
-};
-
-struct _tblite_calculator {
-  // molecule-bound basis (built at construction)
-  int nat = 0, nsh = 0, nao = 0;
-  std::vector<int> at_z, at_sh, sh_atom, sh_l, sh_nprim, sh_ao, ao_sh, ao_at;
-  // D4 data per atom (empty for a single atom: no pairs, no dispersion)
-  bool has_d4 = false;
-  int d4_nsp = 0;
-  std::vector<int> d4_sp, d4_nref, d4_ngw;
-  std::vector<double> d4_refcn, d4_refq, d4_zeff, d4_gam, d4_r4r2, d4_rcov, d4_en, d4_c6ref;
-  std::vector<double> sh_alpha, sh_coeff, sh_se0, sh_kcn, sh_shpoly, sh_zeta, sh_hub, sh_gam3,
-      sh_refocc, at_en, at_rad, at_rcov, at_mprad, at_vcn, at_dkern, at_qkern, at_repa, at_repz;
-  double min_alpha = 1e300;
-  // settings (reference api/calculator.f90:78-89, scf/mixer/input.f90:28-34)
-  double accuracy = 1.0;
-  double etemp = 300.0 * 3.166808578545117e-06;
-  int max_iter = 250;
-  double damping = 0.4;
-  int memory = 0;
-  int guess = TBLITE_GUESS_SAD;
-  int save_integrals = 0;
-  bool anneal = false;
-  double anneal_kt = 0.0;
-  int anneal_hold = 50, anneal_cycles = 50;
-  std::unique_ptr<Workspace> ws;
-};
-
-struct _tblite_result {
-  int nat = 0, nsh = 0, nao = 0;
-  bool has_energy = false, has_wfn = false;
-  double energy = 0.0;
-  std::vector<double> energies, gradient, sigma, qat, qsh, dpat, qpat, emo, focc, P, C, S, H, wbo;
-  double dipole[3] = {0, 0, 0}, quadrupole[6] = {0, 0, 0, 0, 0, 0};
-};
 
 // --------------------------------------------------------------------------------------
 // STO-nG expansion, reference src/tblite/basis/slater.f90:409-511
@@ -286,7 +155,7 @@ static void build_calculator(_tblite_calculator* c, const _tblite_structure* mol
   }
 }
 
-static Gfn2Scalars gfn2_scalars(const _tblite_calculator* c) {
+Gfn2Scalars gfn2_scalars(const _tblite_calculator* c) {
   Gfn2Scalars p{};
   p.wexp = GFN2_WEXP;
   p.enscale = GFN2_ENSCALE;
@@ -421,21 +290,7 @@ static void ensure_workspace(_tblite_calculator* c) {
   }
 }
 
-static DevD4 dev_d4(const _tblite_calculator* c, D4Work& wk) {
-  Workspace& w = *c->ws;
-  DevD4 d{};
-  d.nsp = c->d4_nsp;
-  d.sp = w.d4_sp.p;
-  d.nref = w.d4_nref.p;
-  d.ngw = w.d4_ngw.p;
-  d.refcn = w.d4_refcn.p;
-  d.refq = w.d4_refq.p;
-  d.zeff = w.d4_zeff.p;
-  d.gam = w.d4_gam.p;
-  d.r4r2 = w.d4_r4r2.p;
-  d.rcov = w.d4_rcov.p;
-  d.en = w.d4_en.p;
-  d.c6ref = w.d4_c6ref.p;
+void d4_model_constants(DevD4& d) {
   d.ga = EXT_D4_GA;
   d.gc = EXT_D4_GC;
   d.wf = EXT_D4_WF;
@@ -452,6 +307,24 @@ static DevD4 dev_d4(const _tblite_calculator* c, D4Work& wk) {
   d.a1 = GFN2_A1;
   d.a2 = GFN2_A2;
   d.s9 = GFN2_S9;
+}
+
+static DevD4 dev_d4(const _tblite_calculator* c, D4Work& wk) {
+  Workspace& w = *c->ws;
+  DevD4 d{};
+  d.nsp = c->d4_nsp;
+  d.sp = w.d4_sp.p;
+  d.nref = w.d4_nref.p;
+  d.ngw = w.d4_ngw.p;
+  d.refcn = w.d4_refcn.p;
+  d.refq = w.d4_refq.p;
+  d.zeff = w.d4_zeff.p;
+  d.gam = w.d4_gam.p;
+  d.r4r2 = w.d4_r4r2.p;
+  d.rcov = w.d4_rcov.p;
+  d.en = w.d4_en.p;
+  d.c6ref = w.d4_c6ref.p;
+  d4_model_constants(d);
   wk.cn = w.d4_cn.p;
   wk.gw = w.d4_gw.p;
   wk.dgw = w.d4_dgw.p;
@@ -569,7 +442,7 @@ struct Profiler {
     kmarks.push_back({slot, {a, b}});
   }
   void collect() {
-    if (!enabled || marks.empty()) return;
+    if (!enabled) return;
     for (auto& mk : kmarks) {
       float ms = 0.f;
       cuda_check(cudaEventElapsedTime(&ms, pool[mk.second.first], pool[mk.second.second]),
@@ -577,6 +450,8 @@ struct Profiler {
       kernel_ms[mk.first] += ms;
       kernel_n[mk.first] += 1;
     }
+    kmarks.clear();
+    if (marks.empty()) return;
     for (auto& mk : marks) {
       float ms = 0.f;
       cuda_check(cudaEventElapsedTime(&ms, pool[mk.second.first], pool[mk.second.second]),
@@ -595,22 +470,14 @@ static Profiler g_prof;
 namespace tb {
 int prof_kbegin(cudaStream_t s) { return g_prof.kbegin(s); }
 void prof_kend(int slot, int token, cudaStream_t s) { g_prof.kend(slot, token, s); }
+void prof_reset() { g_prof.reset(); }
+void prof_collect() { g_prof.collect(); }
 }  // namespace tb
 
-static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
-                        _tblite_calculator* c, _tblite_result* res) {
-  if (mol->nat != c->nat) throw std::runtime_error("structure does not match calculator");
-  ensure_workspace(c);
-  Workspace& w = *c->ws;
-  cudaStream_t s = w.stream;
-  const int nat = c->nat, nsh = c->nsh, n = c->nao;
-  const size_t nd = nsh + 9 * (size_t)nat;
-  const Gfn2Scalars p = gfn2_scalars(c);
-  cuda_check(cudaMemcpyAsync(w.xyz.p, mol->xyz.data(), sizeof(double) * 3 * nat,
-                             cudaMemcpyHostToDevice, s),
-             "xyz");
-  DevMol m = dev_mol(c);
-  // occupation, reference xtb/singlepoint.f90:140-156
+// occupation, reference xtb/singlepoint.f90:140-156
+void electron_counts(const _tblite_calculator* c, const _tblite_structure* mol, double* nalp_out,
+                     double* nbet_out) {
+  const int nsh = c->nsh;
   double nocc = -mol->charge, nel_ref = 0.0;
   for (int i = 0; i < nsh; ++i) nocc += c->sh_refocc[i];
   nel_ref = nocc;
@@ -626,7 +493,25 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
     nuhf = nel_i % 2;
   }
   const double diff = std::min((double)nuhf, nocc);
-  const double nalp = (nocc - diff) / 2 + diff, nbet = (nocc - diff) / 2;
+  *nalp_out = (nocc - diff) / 2 + diff;
+  *nbet_out = (nocc - diff) / 2;
+}
+
+static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
+                        _tblite_calculator* c, _tblite_result* res) {
+  if (mol->nat != c->nat) throw std::runtime_error("structure does not match calculator");
+  ensure_workspace(c);
+  Workspace& w = *c->ws;
+  cudaStream_t s = w.stream;
+  const int nat = c->nat, nsh = c->nsh, n = c->nao;
+  const size_t nd = nsh + 9 * (size_t)nat;
+  const Gfn2Scalars p = gfn2_scalars(c);
+  cuda_check(cudaMemcpyAsync(w.xyz.p, mol->xyz.data(), sizeof(double) * 3 * nat,
+                             cudaMemcpyHostToDevice, s),
+             "xyz");
+  DevMol m = dev_mol(c);
+  double nalp = 0.0, nbet = 0.0;
+  electron_counts(c, mol, &nalp, &nbet);
 
   g_prof.reset();
   // geometry-dependent setup
@@ -806,8 +691,27 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
   g_prof.begin(PH_EIGEN, s);
   eigen_vectors_range(w.eig, h_cnt[0], (int)n, w.C.p);
   g_prof.end(s);
+  // Wiberg/Mayer bond orders (post_processing/wbo.f90:60-115): closed shell from P; restricted
+  // open shell from the spin densities with the factor 2, then (up, down) -> (total, up-down)
+  g_prof.begin(PH_GRADIENT, s);
+  const bool open_shell = nalp != nbet;
+  const int nch = open_shell ? 2 : 1;
+  w.wbo.alloc((size_t)nch * nat * nat);
+  cuda_check(cudaMemsetAsync(w.wbo.p, 0, sizeof(double) * nch * nat * nat, s), "zero");
+  if (!open_shell) {
+    gemm64(false, false, n, n, n, 1.0, w.P.p, n, w.S.p, n, 0.0, w.scratch.p, n, KM_NONE, s);
+    launch_wbo(m, w.scratch.p, w.wbo.p, 1.0, s);
+  } else {
+    for (int sp = 0; sp < 2; ++sp) {  // W is free after the gradient: it holds the spin density
+      density_matrix(n, h_cnt[0], w.C.p, w.focc.p + (size_t)(1 + sp) * n, w.W.p, w.scratch.p, s);
+      gemm64(false, false, n, n, n, 1.0, w.W.p, n, w.S.p, n, 0.0, w.scratch.p, n, KM_NONE, s);
+      launch_wbo(m, w.scratch.p, w.wbo.p + (size_t)sp * nat * nat, 2.0, s);
+    }
+  }
+  g_prof.end(s);
   g_prof.begin(PH_TRANSFER, s);
   w.C.download(res->C, (size_t)n * n, s);
+  w.wbo.download(res->wbo, (size_t)nch * nat * nat, s);
   w.grad.download(res->gradient, 3 * nat, s);
   std::vector<double> h_sig_at, h_sigma;
   w.sig_at.download(h_sig_at, 9 * nat, s);
@@ -835,11 +739,16 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
     res->sigma[k] = acc;
   }
   res->has_wfn = true;
-  // molecular multipoles (post_processing/molmom.f90)
-  for (int k = 0; k < 3; ++k) res->dipole[k] = 0.0;
-  for (int i = 0; i < nat; ++i)
-    for (int k = 0; k < 3; ++k)
-      res->dipole[k] += mol->xyz[3 * i + k] * res->qat[i] + res->dpat[3 * i + k];
+  if (open_shell) {  // updown_to_magnet (wavefunction/spin.f90:130-140)
+    const size_t na2 = (size_t)nat * nat;
+    for (size_t t = 0; t < na2; ++t) {
+      const double up = res->wbo[t], dn = res->wbo[na2 + t];
+      res->wbo[t] = up + dn;
+      res->wbo[na2 + t] = up - dn;
+    }
+  }
+  res->wbo_channels = nch;
+  molecular_moments(mol, res);
   if (!converged)
     throw std::runtime_error("SCF not converged in " + std::to_string(iscf) + " cycles");
 }
@@ -847,6 +756,40 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
 // --------------------------------------------------------------------------------------
 // C ABI
 // --------------------------------------------------------------------------------------
+void molecular_moments(const _tblite_structure* mol, _tblite_result* res) {
+  const int nat = res->nat;
+  for (int k = 0; k < 3; ++k) res->dipole[k] = 0.0;
+  for (int k = 0; k < 6; ++k) res->quadrupole[k] = 0.0;
+  for (int i = 0; i < nat; ++i) {
+    const double* x = &mol->xyz[3 * i];
+    const double q = res->qat[i];
+    const double* d = &res->dpat[3 * i];
+    for (int k = 0; k < 3; ++k) res->dipole[k] += x[k] * q + d[k];
+    // cartesian second moment of the point charge and dipole, made traceless (xx xy yy xz yz zz)
+    const double v[3] = {x[0] * q, x[1] * q, x[2] * q};
+    double c[6];
+    c[0] = x[0] * (v[0] + 2 * d[0]);
+    c[2] = x[1] * (v[1] + 2 * d[1]);
+    c[5] = x[2] * (v[2] + 2 * d[2]);
+    c[1] = x[0] * (v[1] + d[1]) + d[0] * x[1];
+    c[3] = x[0] * (v[2] + d[2]) + d[0] * x[2];
+    c[4] = x[1] * (v[2] + d[2]) + d[1] * x[2];
+    const double tr = 0.5 * (c[0] + c[2] + c[5]);
+    c[0] = 1.5 * c[0] - tr;
+    c[1] = 3.0 * c[1];
+    c[2] = 1.5 * c[2] - tr;
+    c[3] = 3.0 * c[3];
+    c[4] = 3.0 * c[4];
+    c[5] = 1.5 * c[5] - tr;
+    for (int k = 0; k < 6; ++k) res->quadrupole[k] += res->qpat[6 * i + k] + c[k];
+  }
+}
+
+void run_singlepoint(_tblite_context* ctx, const _tblite_structure* mol, _tblite_calculator* c,
+                     _tblite_result* res) {
+  singlepoint(ctx, mol, c, res);
+}
+
 static void copy_msg(const std::string& msg, char* buffer, const int* buffersize) {
   if (!buffer) return;
   size_t cap = buffersize ? (size_t)std::max(*buffersize, 0) : msg.size() + 1;
@@ -889,6 +832,10 @@ int tblite_gb300_get_kernel_profile(double* kernel_ms, int* kernel_count, int ns
 }
 
 unsigned long long tblite_gb300_get_launch_count(void) { return g_kernel_launches; }
+
+int tblite_gb300_get_result_bond_order_channels(tblite_result res) {
+  return res ? res->wbo_channels : 0;
+}
 
 int tblite_get_version(void) { return 7 * 100 + 0; }  // 0.7.0 -> 700 (reference version.h)
 

@@ -192,11 +192,13 @@ constexpr size_t TRIDIAG_SMEM_MAX = 200 * 1024;
 // lives in block j % nb (slot j / nb) for the whole reduction, so the symmetric matrix-vector
 // product, the rank-2 update and the next reflector read and write shared memory only; just the
 // reflector v and the product p travel through L2.  Two grid barriers per column.
-__global__ void __launch_bounds__(256) k_tridiag_smem(int n, double* A, double* d, double* e,
-                                                      double* tau, double* vbuf, double* pbuf) {
-  cg::grid_group grid = cg::this_grid();
+template <class Sync>
+__device__ __forceinline__ void tridiag_smem_body(int n, double* A, double* d, double* e, double* tau,
+                                                  double* vbuf, double* pbuf, int nb, int b,
+                                                  Sync sync) {
+  // columns owned round-robin by the nb cooperating blocks; sync() is their common barrier
   extern __shared__ double sm[];
-  const int nb = gridDim.x, b = blockIdx.x;
+
   const int ncpb = (n + nb - 1) / nb;
   double* scol = sm;                    // [ncpb][n]
   double* sv = sm + (size_t)ncpb * n;   // [n]  reflector of the current step
@@ -239,7 +241,7 @@ __global__ void __launch_bounds__(256) k_tridiag_smem(int n, double* A, double* 
   };
   if (n > 1 && b == 0) reflector(0);
   if (n == 1 && b == 0 && threadIdx.x == 0) d[0] = scol[0];
-  grid.sync();
+  sync();
   for (int i = 0; i < n - 1; ++i) {
     const int m = n - i - 1;
     const double t = tau[i];
@@ -259,7 +261,7 @@ __global__ void __launch_bounds__(256) k_tridiag_smem(int n, double* A, double* 
         pbuf[n + j] = acc * sv[j];
       }
     }
-    grid.sync();
+    sync();
     // K = -1/2 t (p . v), same order in every block
     {
       double s = 0.0;
@@ -289,8 +291,14 @@ __global__ void __launch_bounds__(256) k_tridiag_smem(int n, double* A, double* 
       if (i + 1 < n - 1) reflector(i + 1);
       else if (threadIdx.x == 0) d[n - 1] = scol[(size_t)((n - 1) / nb) * n + (n - 1)];
     }
-    grid.sync();
+    sync();
   }
+}
+__global__ void __launch_bounds__(256) k_tridiag_smem(int n, double* A, double* d, double* e,
+                                                      double* tau, double* vbuf, double* pbuf) {
+  cg::grid_group grid = cg::this_grid();
+  tridiag_smem_body(n, A, d, e, tau, vbuf, pbuf, (int)gridDim.x, (int)blockIdx.x,
+                    [&] { grid.sync(); });
 }
 
 // ------------------------------------------------------------------------------------------
@@ -672,14 +680,14 @@ constexpr int BT_WARPS = 4;
 constexpr int BT_CHUNK_MAX = 16;
 constexpr size_t BT_SMEM_MAX = 200 * 1024;
 // the columns live in shared memory too when at least two reflectors fit beside them
-static bool bt_ysmem(int n) {
+__host__ __device__ static inline bool bt_ysmem(int n) {
   return (int)(BT_SMEM_MAX / (sizeof(double) * (size_t)n)) - BT_WARPS >= 2;
 }
-static int bt_chunk(int n) {
+__host__ __device__ static inline int bt_chunk(int n) {
   int c = (int)(BT_SMEM_MAX / (sizeof(double) * (size_t)n)) - (bt_ysmem(n) ? BT_WARPS : 0);
   return c < 1 ? 1 : (c > BT_CHUNK_MAX ? BT_CHUNK_MAX : c);
 }
-static size_t bt_smem(int n) {
+__host__ __device__ static inline size_t bt_smem(int n) {
   return sizeof(double) * (size_t)n * (bt_chunk(n) + (bt_ysmem(n) ? BT_WARPS : 0));
 }
 
@@ -867,5 +875,295 @@ void density_matrix(int n, int k, const double* C, const double* f, double* P, d
   k_scale_cols<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(n, k, C, f, work);
   gemm64(false, true, n, n, k, 1.0, work, n, C, n, 0.0, P, n, KM_NONE, s);
 }
+
+// ------------------------------------------------------------------------------------------
+// Batched eigensolver: one thread-block cluster per molecule for the tridiagonalisation (the
+// columns stay in the cluster's shared memory, the barrier is the cluster's hardware barrier
+// instead of a grid barrier), blockIdx.z over molecules for the other steps.  The eigenvalues
+// are written straight into emo; icount (from the Fermi filling) bounds the vectors.
+// ------------------------------------------------------------------------------------------
+#define BMOL const MolPtrs& q = mp[list[blockIdx.z]]
+#define BARGS const MolPtrs* __restrict__ mp, const int* __restrict__ list
+
+__global__ void __launch_bounds__(256) kb_tridiag(BARGS) {
+  cg::cluster_group cl = cg::this_cluster();
+  BMOL;
+  const int n = q.m.nao;
+  tridiag_smem_body(n, q.A, q.ed, q.ee, q.etau, q.epv, q.epv + (n + 1), (int)cl.num_blocks(),
+                    (int)cl.block_rank(), [&] { cl.sync(); });
+}
+// Small molecules (the whole n x n matrix in one CTA's shared memory): the same Householder
+// reduction with everything on chip.  Per column: warp 0 builds the reflector (no block
+// reduction), the warps form p = t A22 v column by column, every warp reduces K = -t/2 p.v
+// for itself, and all threads apply the symmetric rank-2 update as one 2-d loop over the
+// trailing block.  Three block barriers per column.  The reflectors and the diagonal go to
+// global memory at the end in the layout the back-transformation reads (column-major A,
+// v below the subdiagonal).
+constexpr int TRI_SMALL_MAX = 156;  // (n^2 + 2n) doubles <= 200 KB
+__global__ void __launch_bounds__(256) kb_tridiag_small(BARGS) {
+  BMOL;
+  const int n = q.m.nao;
+  extern __shared__ double sm[];
+  double* a = sm;            // [n][n] column-major, full symmetric storage
+  double* sv = sm + n * n;   // [n] reflector (sv[i+1] = 1)
+  double* sp = sv + n;       // [n] p, then w
+  __shared__ double s_t;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
+  const double* A0 = q.A;
+  for (int t = tid; t < n * n; t += blockDim.x) a[t] = A0[t];
+  __syncthreads();
+  for (int i = 0; i < n - 1; ++i) {
+    const int r0 = i + 1;  // trailing block rows/cols r0 .. n-1
+    if (wid == 0) {        // reflector of column i
+      double* col = a + (size_t)i * n;
+      const double alpha = col[r0];
+      double s = 0.0;
+      for (int r = r0 + 1 + lane; r < n; r += 32) s += col[r] * col[r];
+      s = wred(s);
+      double t = 0.0, beta = alpha;
+      if (s > 0.0) {
+        beta = -copysign(sqrt(alpha * alpha + s), alpha);
+        t = (beta - alpha) / beta;
+      }
+      const double sc = s > 0.0 ? 1.0 / (alpha - beta) : 0.0;
+      for (int r = r0 + 1 + lane; r < n; r += 32) {
+        const double v = col[r] * sc;
+        col[r] = v;
+        sv[r] = v;
+      }
+      if (lane == 0) {
+        sv[r0] = 1.0;
+        s_t = t;
+        q.etau[i] = t;
+        q.ee[i] = beta;
+        q.ed[i] = col[i];
+      }
+    }
+    __syncthreads();
+    const double t = s_t;
+    if (t != 0.0) {
+      // p_j = t * A22(:, j) . v  (warp per column)
+      for (int j = r0 + wid; j < n; j += nw) {
+        const double* col = a + (size_t)j * n;
+        double acc = 0.0;
+        for (int r = r0 + lane; r < n; r += 32) acc += col[r] * sv[r];
+        acc = wred(acc) * t;
+        if (lane == 0) sp[j] = acc;
+      }
+      __syncthreads();
+      // K = -1/2 t (p . v), each warp for itself; then w = p + K v is formed on the fly
+      double kk = 0.0;
+      for (int r = r0 + lane; r < n; r += 32) kk += sp[r] * sv[r];
+      const double K = -0.5 * t * wred(kk);
+      const int m = n - r0;
+      for (int e2 = tid; e2 < m * m; e2 += blockDim.x) {
+        const int c = r0 + e2 / m, r = r0 + e2 % m;
+        const double vr = sv[r], vc = sv[c];
+        a[(size_t)c * n + r] -= vr * (sp[c] + K * vc) + (sp[r] + K * vr) * vc;
+      }
+    }
+    __syncthreads();
+  }
+  if (tid == 0) q.ed[n - 1] = a[(size_t)(n - 1) * n + (n - 1)];
+  // reflectors (strictly below the subdiagonal of each column) for the back-transformation
+  double* Ag = q.A;
+  for (int t2 = tid; t2 < n * n; t2 += blockDim.x) Ag[t2] = a[t2];
+}
+
+// Eigenvalues for the batch: plain bisection, one thread per eigenvalue.  With thousands of
+// molecules the GPU is throughput bound, and bisection gains one bit per Sturm sequence
+// against the multisection's 2.3 bits per four sequences.  d and e^2 of the molecule are
+// staged in shared memory (every thread reads the same element at the same step).  Same
+// bracket, Sturm recurrence and stopping rule as the multisection.
+constexpr int BIS_MAXN = 448;
+__global__ void __launch_bounds__(128) kb_bisect(BARGS) {
+  BMOL;
+  const int n = q.m.nao;
+  if ((int)blockIdx.x * (int)blockDim.x >= n) return;
+  __shared__ double sd[BIS_MAXN], se2[BIS_MAXN];
+  __shared__ double bounds[3];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    sd[i] = q.ed[i];
+    se2[i] = i < n - 1 ? q.ee[i] * q.ee[i] : 0.0;
+  }
+  if (threadIdx.x == 0) {
+    double lo = 1e300, hi = -1e300, emax = 0.0;
+    for (int i = 0; i < n; ++i) {
+      const double r = (i > 0 ? fabs(q.ee[i - 1]) : 0.0) + (i < n - 1 ? fabs(q.ee[i]) : 0.0);
+      lo = fmin(lo, q.ed[i] - r);
+      hi = fmax(hi, q.ed[i] + r);
+      if (i < n - 1) emax = fmax(emax, q.ee[i] * q.ee[i]);
+    }
+    const double tnorm = fmax(fabs(lo), fabs(hi));
+    bounds[0] = lo - 8.9e-16 * tnorm - 1e-300;
+    bounds[1] = hi + 8.9e-16 * tnorm + 1e-300;
+    bounds[2] = fmax(2.2250738585072014e-308 * fmax(1.0, emax), 1e-300);
+    if (blockIdx.x == 0) q.escal[1] = fmax(fabs(bounds[0]), fabs(bounds[1]));
+  }
+  __syncthreads();
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = j < n;
+  double lo = bounds[0], hi = bounds[1];
+  const double pivmin = bounds[2];
+  for (int it = 0; it < 128; ++it) {
+    const bool done =
+        !active || hi - lo <= 2.0 * 2.220446049250313e-16 * fmax(fabs(lo), fabs(hi)) + 4.0 * pivmin;
+    if (__all_sync(0xffffffffu, done)) break;
+    if (done) continue;
+    const double x = 0.5 * (lo + hi);
+    double p0 = 1.0, p1 = sd[0] - x;
+    if (p1 == 0.0) p1 = -0x1p-900;
+    int cnt = p1 < 0.0;
+    for (int i = 1; i < n; ++i) {
+      double p2 = fma(sd[i] - x, p1, -se2[i - 1] * p0);
+      if (p2 == 0.0) p2 = -copysign(0x1p-900, p1);
+      cnt += (p2 < 0.0) != (p1 < 0.0);
+      p0 = p1;
+      p1 = p2;
+      if ((i & 7) == 0) {
+        const double a = fabs(p1);
+        if (a > 0x1p400 || a < 0x1p-400) {
+          const int ex = ilogb(a);
+          p1 = scalbn(p1, -ex);
+          p0 = scalbn(p0, -ex);
+        }
+      }
+    }
+    if (cnt > j) hi = x;
+    else lo = x;
+  }
+  if (active) q.emo[j] = 0.5 * (lo + hi);
+}
+
+__global__ void __launch_bounds__(64) kb_multisect(BARGS) {
+  BMOL;
+  multisect_dev(q.m.nao, q.ed, q.ee, q.emo, q.escal);
+}
+__global__ void kb_invit(BARGS) {
+  BMOL;
+  invit_dev(q.m.nao, 0, *q.icount, q.ed, q.ee, q.emo, q.escal, q.lu, q.Y);
+}
+__global__ void kb_clusters(BARGS) {
+  BMOL;
+  clusters_dev(q.m.nao, 0, *q.icount, q.ed, q.ee, q.emo, q.escal, 1e-5, q.Y);
+}
+__global__ void __launch_bounds__(BT_WARPS * 32) kb_backtransform(BARGS) {
+  BMOL;
+  const int n = q.m.nao, k = *q.icount;
+  if ((int)blockIdx.x * BT_WARPS >= k) return;  // no column of this molecule here
+  backtransform_dev(n, k, bt_chunk(n), bt_ysmem(n), q.A, q.etau, q.Y);
+}
+__global__ void kb_scale_cols(BARGS, int weighted) {
+  BMOL;
+  scale_cols_dev(q.m.nao, *q.icount, q.C, weighted ? q.vec_out : q.focc, q.scratch);
+}
+
+// smallest cluster (1, 2, 4, 8 blocks) whose shared memory holds the n x n matrix
+static int tridiag_cluster(int n, size_t* smem) {
+  for (int nb = 1; nb <= 8; nb *= 2) {
+    const size_t ncpb = (size_t)(n + nb - 1) / nb;
+    const size_t need = sizeof(double) * (ncpb * n + 2 * (size_t)n);
+    if (need <= TRIDIAG_SMEM_MAX) {
+      *smem = need;
+      return nb;
+    }
+  }
+  return 0;
+}
+int batch_tridiag_max_n() {
+  int n = 1;
+  size_t sm = 0;
+  while (tridiag_cluster(n + 1, &sm)) ++n;
+  return n;
+}
+
+static void batch_attributes() {
+  static bool done = false;
+  if (done) return;
+  ck(cudaFuncSetAttribute(kb_tridiag, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          (int)TRIDIAG_SMEM_MAX),
+     "smem attr batch tridiag");
+  ck(cudaFuncSetAttribute(kb_tridiag_small, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          (int)TRIDIAG_SMEM_MAX),
+     "smem attr batch tridiag small");
+  ck(cudaFuncSetAttribute(kb_backtransform, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          (int)BT_SMEM_MAX + (int)(BT_WARPS * sizeof(double) * 64)),
+     "smem attr batch backtransform");
+  done = true;
+}
+
+static void tridiag_cluster_b(const BatchLaunch& b);
+
+void eigen_values_b(const BatchLaunch& b) {
+  if (!b.count) return;
+  batch_attributes();
+  gemm_b(b, GS_FX);
+  gemm_b(b, GS_XTT);
+  if (b.nao_max <= TRI_SMALL_MAX) {
+    const size_t sm_small = sizeof(double) * ((size_t)b.nao_max * b.nao_max + 2 * b.nao_max);
+    ++g_kernel_launches;
+    const int tk = prof_kbegin(b.s);
+    kb_tridiag_small<<<dim3(1, 1, b.count), 256, sm_small, b.s>>>(b.mp, b.list);
+    prof_kend(KS_TRIDIAG, tk, b.s);
+  } else {
+    tridiag_cluster_b(b);
+  }
+  ++g_kernel_launches;
+  const int tm = prof_kbegin(b.s);
+  if (b.nao_max <= BIS_MAXN)
+    kb_bisect<<<dim3((b.nao_max + 127) / 128, 1, b.count), 128, 0, b.s>>>(b.mp, b.list);
+  else
+    kb_multisect<<<dim3((4 * b.nao_max + 63) / 64, 1, b.count), 64, 0, b.s>>>(b.mp, b.list);
+  prof_kend(KS_MULTISECT, tm, b.s);
+}
+
+static void tridiag_cluster_b(const BatchLaunch& b) {
+  size_t smem = 0;
+  const int nb = tridiag_cluster(b.nao_max, &smem);
+  if (!nb) throw std::runtime_error("batched tridiagonalisation: molecule too large");
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(nb, 1, b.count);
+  cfg.blockDim = dim3(256, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = b.s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = nb;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  ++g_kernel_launches;
+  const int tk = prof_kbegin(b.s);
+  ck(cudaLaunchKernelEx(&cfg, kb_tridiag, b.mp, b.list), "batch tridiag");
+  prof_kend(KS_TRIDIAG, tk, b.s);
+}
+
+void eigen_vectors_b(const BatchLaunch& b) {
+  if (!b.count) return;
+  batch_attributes();
+  g_kernel_launches += 3;
+  const int ti = prof_kbegin(b.s);
+  kb_invit<<<dim3((b.nao_max + 15) / 16, 1, b.count), 16, 0, b.s>>>(b.mp, b.list);
+  prof_kend(KS_INVIT, ti, b.s);
+  kb_clusters<<<dim3(b.nao_max, 1, b.count), 256, 0, b.s>>>(b.mp, b.list);
+  const int tb_ = prof_kbegin(b.s);
+  kb_backtransform<<<dim3((b.nao_max + BT_WARPS - 1) / BT_WARPS, 1, b.count), BT_WARPS * 32,
+                     bt_smem(b.nao_max), b.s>>>(b.mp, b.list);
+  prof_kend(KS_BACKTRANSFORM, tb_, b.s);
+  gemm_b(b, GS_XY);
+}
+
+void density_b(const BatchLaunch& b, bool weighted) {
+  if (!b.count) return;
+  const size_t tot = (size_t)b.nao_max * b.nao_max;
+  ++g_kernel_launches;
+  kb_scale_cols<<<dim3((unsigned)((tot + 255) / 256), 1, b.count), 256, 0, b.s>>>(
+      b.mp, b.list, weighted ? 1 : 0);
+  gemm_b(b, weighted ? GS_WDENS : GS_DENS);
+}
+
+#undef BMOL
+#undef BARGS
 
 }  // namespace tb

@@ -30,6 +30,8 @@ enum { KS_TRIDIAG = 0, KS_MULTISECT, KS_INVIT, KS_BACKTRANSFORM, KS_GEMM, KS_FOC
        KS_COUNT };
 int prof_kbegin(cudaStream_t s);
 void prof_kend(int slot, int token, cudaStream_t s);
+void prof_reset();    // clear the kernel and phase records
+void prof_collect();  // after a stream wait: turn the recorded events into times
 
 constexpr int MAXG = 12;    // max primitives per shell
 constexpr int MAXL = 2;     // max angular momentum handled by the kernels
@@ -198,6 +200,8 @@ void launch_fe(int n, const double* f, const double* e, double* out, cudaStream_
 // dense helpers
 void density_matrix(int n, int k, const double* C, const double* f, double* P, double* work,
                     cudaStream_t s);
+// wbo[A][B] += scale * sum (PS)_{nu mu} (PS)_{mu nu} over the orbitals of atoms A != B
+void launch_wbo(const DevMol& m, const double* PS, double* wbo, double scale, cudaStream_t s);
 
 // ---------------------------------------------------------------------------------------------
 // Batched ensemble path: many molecules in one launch per step.  Every molecule owns a slice of
@@ -209,8 +213,9 @@ struct MolPtrs {
   DevMol m;
   DevD4 d4;
   D4Work d4w;
-  int has_d4, nd, mull_chunks;
-  double nalp, nbet;
+  int has_d4, nd, mull_chunks, memory;
+  double nalp, nbet, kt, damp, econv, pconv;
+  double h0_cutoff;  // depends on the basis of the molecule (smallest exponent)
   double *cn, *se, *mrad, *dmrdcn;
   double *S, *H, *D, *Q, *F, *P, *C, *scratch;  // F doubles as W after the SCF
   double *emo, *focc;                            // focc [3][n]: total, alpha, beta
@@ -248,13 +253,13 @@ void launch_coulomb_gradient_b(const BatchLaunch& b, const Gfn2Scalars& p);
 void launch_vao_b(const BatchLaunch& b);
 void launch_fock_b(const BatchLaunch& b);
 void launch_mulliken_b(const BatchLaunch& b);
-void launch_fermi_b(const BatchLaunch& b, double kt);
+void launch_fermi_b(const BatchLaunch& b);  // temperature per molecule (no annealing)
 void launch_pack_b(const BatchLaunch& b, bool output);  // output: *_o moments -> vec_out
 void launch_unpack_b(const BatchLaunch& b);
 void launch_diff_b(const BatchLaunch& b);
-void launch_broyden_b(const BatchLaunch& b, int iter, int memory, double damp);
+void launch_broyden_b(const BatchLaunch& b, int iter);
 void launch_eelec_init_b(const BatchLaunch& b);
-void launch_converge_b(const BatchLaunch& b, double econv, double pconv, bool kt_final);
+void launch_converge_b(const BatchLaunch& b);  // thresholds per molecule
 void launch_fe_b(const BatchLaunch& b);
 void launch_h0_gradient_b(const BatchLaunch& b, const Gfn2Scalars& p);
 void launch_cn_grad_b(const BatchLaunch& b, const Gfn2Scalars& p);
@@ -262,6 +267,13 @@ void d4_setup_b(const BatchLaunch& b);
 void d4_potential_b(const BatchLaunch& b);
 void d4_energy_b(const BatchLaunch& b);
 void d4_gradient_b(const BatchLaunch& b);
+// batched FP64 GEMM at one of the fixed call sites of the SCF (operands from MolPtrs)
+enum { GS_FX = 0,  // T1 = F X            (X upper triangular)
+       GS_XTT,     // A = X^T T1
+       GS_XY,      // C = X Y, icount columns
+       GS_DENS,    // P = (C f) C^T over icount orbitals (scaled copy in scratch)
+       GS_WDENS }; // W (into F) = (C f e) C^T
+void gemm_b(const BatchLaunch& b, int site);
 // eigensolver steps for a bucket
 void cholesky_inverse_b(const BatchLaunch& b);          // S -> X (status into flag)
 void eigen_values_b(const BatchLaunch& b);              // F -> emo (tridiagonal form kept)

@@ -404,6 +404,7 @@ __global__ void kb_build_h0(const MolPtrs* __restrict__ mp, const int* __restric
                             Gfn2Scalars p) {
   const MolPtrs& q = mp[list[blockIdx.z]];
   const long long npair = (long long)q.m.nsh * (q.m.nsh + 1) / 2;
+  p.h0_cutoff = q.h0_cutoff;
   build_h0_dev(q.m, p, q.se, q.S, q.H, q.D, q.Q, npair);
 }
 void launch_build_h0_b(const BatchLaunch& b, const Gfn2Scalars& p) {
@@ -418,6 +419,7 @@ __global__ void kb_h0_gradient(const MolPtrs* __restrict__ mp, const int* __rest
                                Gfn2Scalars p) {
   const MolPtrs& q = mp[list[blockIdx.z]];
   const long long npair = (long long)q.m.nsh * (q.m.nsh + 1) / 2;
+  p.h0_cutoff = q.h0_cutoff;
   h0_gradient_dev(q.m, p, q.se, q.P, q.F, q.vao, q.vdp, q.vqp, q.grad, q.sigma, q.dEdcn, npair);
 }
 __global__ void kb_h0_onsite_dcn(const MolPtrs* __restrict__ mp, const int* __restrict__ list) {

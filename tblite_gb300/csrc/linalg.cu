@@ -285,4 +285,97 @@ int cholesky_inverse(int n, double* L, double* X, int* d_status, int* h_status, 
   return 0;
 }
 
+// ------------------------------------------------------------------------------------------
+// Batched launches (blockIdx.z walks the listed molecules)
+// ------------------------------------------------------------------------------------------
+#define BMOL const MolPtrs& q = mp[list[blockIdx.z]]
+#define BARGS const MolPtrs* __restrict__ mp, const int* __restrict__ list
+
+template <int BM, int BN, int BK, int TM, int TN>
+__global__ void __launch_bounds__((BM / TM) * (BN / TN)) kb_gemm(BARGS, int site) {
+  BMOL;
+  const int n = q.m.nao;
+  const int k = *q.icount;
+  int M = n, N = n, K = n, km = KM_NONE;
+  const double *A = nullptr, *B = nullptr;
+  double* C = nullptr;
+  bool ta = false, tb = false;
+  switch (site) {
+    case GS_FX: A = q.F; B = q.X; C = q.T1; km = KM_LT_COLEND; break;
+    case GS_XTT: A = q.X; ta = true; B = q.T1; C = q.A; km = KM_LT_ROWEND; break;
+    case GS_XY: A = q.X; B = q.Y; C = q.C; N = k; km = KM_GE_ROWBEG; break;
+    case GS_DENS: A = q.scratch; B = q.C; tb = true; C = q.P; K = k; break;
+    default: A = q.scratch; B = q.C; tb = true; C = q.F; K = k; break;  // GS_WDENS
+  }
+  if ((int)blockIdx.x * BN >= N || (int)blockIdx.y * BM >= M) return;  // tile outside
+  gemm_dev<BM, BN, BK, TM, TN>(M, N, K, 1.0, A, n, ta, B, n, tb, 0.0, C, n, km);
+}
+
+void gemm_b(const BatchLaunch& b, int site) {
+  if (!b.count) return;
+  const int tk = prof_kbegin(b.s);
+  ++g_kernel_launches;
+  if (b.nao_max <= 128) {
+    const unsigned t = (b.nao_max + 15) / 16;
+    kb_gemm<16, 16, 16, 2, 2><<<dim3(t, t, b.count), 64, 0, b.s>>>(b.mp, b.list, site);
+  } else {
+    const unsigned t = (b.nao_max + 31) / 32;
+    kb_gemm<32, 32, 16, 4, 4><<<dim3(t, t, b.count), 64, 0, b.s>>>(b.mp, b.list, site);
+  }
+  prof_kend(KS_GEMM, tk, b.s);
+}
+
+// Cholesky S = L L^T of one molecule per block, in T1 (column-major lower, L2 resident):
+// step j scales column j by 1/sqrt(pivot) and updates the trailing columns (warp per column).
+// The diagonal keeps the pivots until the end, then takes their square roots.  A pivot that
+// is not positive marks the molecule failed (flag -2); every thread reads the same pivot after
+// a barrier, so the whole block leaves together.
+__global__ void __launch_bounds__(256) kb_cholesky(BARGS) {
+  BMOL;
+  const int n = q.m.nao;
+  double* A = q.T1;
+  const size_t nn = (size_t)n * n;
+  for (size_t t = threadIdx.x; t < nn; t += blockDim.x) A[t] = q.S[t];  // S symmetric
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int j = 0; j < n; ++j) {
+    const double piv = A[j + (size_t)j * n];
+    if (!(piv > 0.0)) {
+      if (threadIdx.x == 0) *q.flag = -2;
+      return;
+    }
+    const double inv = 1.0 / sqrt(piv);
+    double* cj = A + (size_t)j * n;
+    for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x) cj[i] *= inv;
+    __syncthreads();
+    for (int c = j + 1 + warp; c < n; c += nw) {
+      const double lc = cj[c];
+      double* cc = A + (size_t)c * n;
+      for (int i = c + lane; i < n; i += 32) cc[i] -= cj[i] * lc;
+    }
+    __syncthreads();
+  }
+  for (size_t t = threadIdx.x; t < nn; t += blockDim.x) {
+    const int i = (int)(t % n), j = (int)(t / n);
+    if (i < j) A[t] = 0.0;
+    else if (i == j) A[t] = sqrt(A[t]);
+  }
+}
+
+__global__ void kb_tri_inv_t(BARGS) {
+  BMOL;
+  if (*q.flag < 0) return;
+  tri_inv_t_dev(q.m.nao, q.T1, q.X);
+}
+
+void cholesky_inverse_b(const BatchLaunch& b) {
+  if (!b.count) return;
+  g_kernel_launches += 2;
+  kb_cholesky<<<dim3(1, 1, b.count), 256, 0, b.s>>>(b.mp, b.list);
+  kb_tri_inv_t<<<dim3((b.nao_max * 32 + 255) / 256, 1, b.count), 256, 0, b.s>>>(b.mp, b.list);
+}
+
+#undef BMOL
+#undef BARGS
+
 }  // namespace tb

@@ -1032,6 +1032,34 @@ void launch_broyden_next(BroydenState& b, cudaStream_t s) {
 }
 
 // ------------------------------------------------------------------------------------
+// Wiberg/Mayer bond orders (wavefunction/mulliken.f90:176-235): for atoms A != B
+//   wbo(A, B) += scale * sum_{mu in A, nu in B} (PS)_{nu mu} (PS)_{mu nu}
+// one thread per atom pair; the orbitals of an atom are contiguous
+// ------------------------------------------------------------------------------------
+__device__ __forceinline__ void wbo_dev(DevMol m, const double* __restrict__ PS, double* wbo,
+                                        double scale) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int nat = m.nat, n = m.nao;
+  if (t >= (long long)nat * nat) return;
+  const int a = (int)(t / nat), b = (int)(t % nat);
+  if (a == b) return;
+  const int a0 = m.sh_ao[m.at_sh[a]], a1 = m.sh_ao[m.at_sh[a + 1] - 1] + 2 * m.sh_l[m.at_sh[a + 1] - 1] + 1;
+  const int b0 = m.sh_ao[m.at_sh[b]], b1 = m.sh_ao[m.at_sh[b + 1] - 1] + 2 * m.sh_l[m.at_sh[b + 1] - 1] + 1;
+  double s = 0.0;
+  for (int mu = a0; mu < a1; ++mu)
+    for (int nu = b0; nu < b1; ++nu) s += PS[(size_t)nu * n + mu] * PS[(size_t)mu * n + nu];
+  wbo[t] += scale * s;
+}
+__global__ void k_wbo(DevMol m, const double* __restrict__ PS, double* wbo, double scale) {
+  wbo_dev(m, PS, wbo, scale);
+}
+void launch_wbo(const DevMol& m, const double* PS, double* wbo, double scale, cudaStream_t s) {
+  const long long nn = (long long)m.nat * m.nat;
+  ++g_kernel_launches;
+  k_wbo<<<(unsigned)((nn + 255) / 256), 256, 0, s>>>(m, PS, wbo, scale);
+}
+
+// ------------------------------------------------------------------------------------
 // Batched launches: blockIdx.z walks the listed molecules; each block runs the same body as
 // the one-molecule kernel on that molecule's slices.  Blocks past a molecule's own size exit
 // through the bodies' bounds checks (or the explicit tile checks below).
@@ -1159,15 +1187,15 @@ void launch_mulliken_b(const BatchLaunch& b) {
   kb_mull_reduce<<<bgrid((b.nat_max + 127) / 128, b), 128, 0, b.s>>>(b.mp, b.list);
 }
 
-__global__ void kb_fermi(BARGS, double kt) {
+__global__ void kb_fermi(BARGS) {
   BMOL;
   const int n = q.m.nao;
-  fermi_dev(n, q.emo, q.nalp, q.nbet, kt, q.focc + n, q.focc + 2 * n, q.focc, q.scal, q.icount);
+  fermi_dev(n, q.emo, q.nalp, q.nbet, q.kt, q.focc + n, q.focc + 2 * n, q.focc, q.scal, q.icount);
 }
-void launch_fermi_b(const BatchLaunch& b, double kt) {
+void launch_fermi_b(const BatchLaunch& b) {
   if (!b.count) return;
   ++g_kernel_launches;
-  kb_fermi<<<bgrid(1, b), 1024, 0, b.s>>>(b.mp, b.list, kt);
+  kb_fermi<<<bgrid(1, b), 1024, 0, b.s>>>(b.mp, b.list);
 }
 
 __global__ void kb_pack(BARGS, int output) {
@@ -1204,15 +1232,15 @@ void launch_diff_b(const BatchLaunch& b) {
   kb_diff<<<bgrid(1, b), 1024, 0, b.s>>>(b.mp, b.list);
 }
 
-__global__ void kb_broyden(BARGS, int iter, int memory, double damp) {
+__global__ void kb_broyden(BARGS, int iter) {
   BMOL;
-  broyden_dev(q.nd, memory, iter, damp, q.bq, q.bqlast, q.bdq, q.bdqlast, q.bdf, q.bu, q.ba,
+  broyden_dev(q.nd, q.memory, iter, q.damp, q.bq, q.bqlast, q.bdq, q.bdqlast, q.bdf, q.bu, q.ba,
               q.bomega, q.bwork, q.bstatus);
 }
-void launch_broyden_b(const BatchLaunch& b, int iter, int memory, double damp) {
+void launch_broyden_b(const BatchLaunch& b, int iter) {
   if (!b.count) return;
   ++g_kernel_launches;
-  kb_broyden<<<bgrid(1, b), 1024, 0, b.s>>>(b.mp, b.list, iter, memory, damp);
+  kb_broyden<<<bgrid(1, b), 1024, 0, b.s>>>(b.mp, b.list, iter);
 }
 
 __global__ void kb_eelec_init(BARGS) {
@@ -1227,9 +1255,9 @@ void launch_eelec_init_b(const BatchLaunch& b) {
 
 // convergence test of the single-point driver (xtb/singlepoint.f90:300-304), one thread per
 // molecule: the electronic energy is summed in atom order, as the one-molecule driver does
-__global__ void kb_converge(BARGS, double econv, double pconv, int kt_final) {
+__global__ void kb_converge(BARGS) {
   BMOL;
-  if (threadIdx.x != 0) return;
+  if (threadIdx.x != 0 || *q.flag < 0) return;
   double e = 0.0;
   for (int i = 0; i < q.m.nat; ++i) e += q.eelec[i];
   const double elast = q.conv[1];
@@ -1240,13 +1268,13 @@ __global__ void kb_converge(BARGS, double econv, double pconv, int kt_final) {
     *q.flag = -1;
     return;
   }
-  const bool ok = fabs(e - elast) < econv && q.scal[1] < pconv && kt_final;
+  const bool ok = fabs(e - elast) < q.econv && q.scal[1] < q.pconv;
   *q.flag = ok ? 1 : 0;
 }
-void launch_converge_b(const BatchLaunch& b, double econv, double pconv, bool kt_final) {
+void launch_converge_b(const BatchLaunch& b) {
   if (!b.count) return;
   ++g_kernel_launches;
-  kb_converge<<<bgrid(1, b), 32, 0, b.s>>>(b.mp, b.list, econv, pconv, kt_final ? 1 : 0);
+  kb_converge<<<bgrid(1, b), 32, 0, b.s>>>(b.mp, b.list);
 }
 
 __global__ void kb_fe(BARGS) {

@@ -86,6 +86,11 @@ class Result:
             dims["nao"] = library.result_int(self._res, "number_of_orbitals")
         real = tuple(dims[s] if isinstance(s, str) else s for s in shape)
         name = attribute.replace("-", "_")
+        if attribute == "bond-orders":
+            nch = library.load().tblite_gb300_get_result_bond_order_channels(self._res)
+            if nch == 2:  # open shell: (nat, nat, 2) total and magnetisation, column-major
+                flat = library.result_array(self._res, name, (2 * real[0] * real[1],))
+                return flat.reshape((real[0], real[1], 2), order="F")
         if attribute == "energy":
             return float(library.result_array(self._res, name, (1,))[0])
         return library.result_array(self._res, name, real)
@@ -181,3 +186,37 @@ class Calculator(Structure):
         library.load().tblite_get_singlepoint(self._ctx, self._mol, self._calc, _res._res)
         library.context_check(self._ctx)
         return _res
+
+
+def batch_singlepoint(calculators, results=None, verbosity: int = 0):
+    """Energies and gradients of many molecules in one batched engine call.
+
+    No counterpart in the reference (one molecule per ``singlepoint`` there).  Each
+    ``Calculator`` keeps its own settings; ``results`` (optional, one per calculator) restart
+    the molecules like ``Calculator.singlepoint(res)`` does.  Returns the list of ``Result``
+    objects; density matrix and orbital coefficients are not kept by the batch.  Raises
+    ``TBLiteRuntimeError`` listing every molecule that failed (the others keep their results).
+    """
+    lib = library.load()
+    calcs = list(calculators)
+    n = len(calcs)
+    if results is None:
+        results = [Result() for _ in range(n)]
+    elif len(results) != n:
+        raise TBLiteValueError("One result per calculator is required")
+    mols = (c_void_p * n)(*[c._mol.value for c in calcs])
+    hcalc = (c_void_p * n)(*[c._calc.value for c in calcs])
+    hres = (c_void_p * n)(*[r._res.value for r in results])
+    status = np.zeros(n, dtype=np.int32)
+    ctx = library.new_context(verbosity=verbosity)
+    try:
+        lib.tblite_gb300_batch_singlepoint(ctx, n, mols, hcalc, hres, library._ip(status))
+        library.context_check(ctx)
+    finally:
+        lib.tblite_delete_context(byref(ctx))
+    return results
+
+
+def batch_fallbacks() -> int:
+    """Molecules of the last batch call that were evaluated by the one-molecule path."""
+    return int(library.load().tblite_gb300_batch_last_fallbacks())

@@ -76,10 +76,16 @@ _SIGNATURES = {
     "tblite_gb300_set_profiling": (None, [c_int]),
     "tblite_gb300_get_profile": (c_int, [_dbl_p, _int_p, c_int, _dbl_p, _int_p]),
     "tblite_gb300_get_launch_count": (ctypes.c_ulonglong, []),
+    "tblite_gb300_get_result_bond_order_channels": (c_int, [c_void_p]),
     "tblite_gb300_get_kernel_profile": (c_int, [_dbl_p, _int_p, c_int]),
     "tblite_gb300_density_matrix_noalloc": (
         c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
     "tblite_gb300_density_matrix_noalloc_max": (c_int, []),
+    "tblite_gb300_batch_singlepoint": (
+        c_int, [c_void_p, c_int, POINTER(c_void_p), POINTER(c_void_p), POINTER(c_void_p), _int_p]),
+    "tblite_gb300_batch_last_fallbacks": (c_int, []),
+    "tblite_gb300_batch_last_device_ms": (c_double, []),
+    "tblite_gb300_batch_last_iterations": (c_int, [_int_p, c_int]),
 }
 for _name in ("number_of_atoms", "number_of_shells", "number_of_orbitals", "number_of_spins"):
     _SIGNATURES[f"tblite_get_result_{_name}"] = (None, [c_void_p, c_void_p, _int_p])

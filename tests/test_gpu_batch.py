@@ -1,0 +1,107 @@
+"""Batched ensemble path vs the one-molecule path and the CPU oracle (needs a GPU).
+
+The batch runs the same per-molecule arithmetic as tblite_get_singlepoint, except the
+eigensolver's Cholesky and tridiagonalisation (one block cluster per molecule instead of a
+grid-wide kernel), so the results agree with the plain path to rounding; the bar is the one of
+the parity tests: |dE| <= 1e-7 Eh, charges <= 1e-6 e, gradient <= 1e-6 Eh/Bohr.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+E_TOL, Q_TOL, G_TOL, V_TOL = 1e-7, 1e-6, 1e-6, 1e-5
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    from tblite_gb300 import _build
+
+    _build.build()
+
+
+def _ensemble():
+    from tblite_gb300 import workloads
+
+    mols = []
+    for k in (1, 2, 3, 5, 8, 13):
+        mols.append(workloads.water_cluster_k(k, seed=100 + k))
+    for n in (1, 2, 4, 7, 12, 20):
+        mols.append(workloads.alkane(n, seed=200 + n))
+    return mols
+
+
+def _calc(z, x, **settings):
+    from tblite_gb300.interface import Calculator
+
+    calc = Calculator("GFN2-xTB", z, x)
+    for k, v in settings.items():
+        calc.set(k, v)
+    return calc
+
+
+def _compare(rb, rp):
+    assert abs(rb.get("energy") - rp.get("energy")) <= E_TOL
+    assert np.max(np.abs(rb.get("charges") - rp.get("charges"))) <= Q_TOL
+    assert np.max(np.abs(rb.get("gradient") - rp.get("gradient"))) <= G_TOL
+    assert np.max(np.abs(rb.get("virial") - rp.get("virial"))) <= V_TOL
+    assert np.max(np.abs(rb.get("energies") - rp.get("energies"))) <= E_TOL
+    assert np.max(np.abs(rb.get("dipole") - rp.get("dipole"))) <= 1e-6
+
+
+def test_batch_matches_plain_path():
+    from tblite_gb300.interface import batch_fallbacks, batch_singlepoint
+
+    mols = _ensemble()
+    calcs = [_calc(z, x) for z, x in mols]
+    res_b = batch_singlepoint(calcs)
+    assert batch_fallbacks() == 0
+    for (z, x), rb in zip(mols, res_b):
+        rp = _calc(z, x).singlepoint()
+        _compare(rb, rp)
+        occ_b, occ_p = rb.get("orbital-occupations"), rp.get("orbital-occupations")
+        assert np.max(np.abs(occ_b - occ_p)) <= 1e-6
+
+
+def test_batch_matches_oracle():
+    from oracle import gfn2
+    from tblite_gb300.interface import batch_singlepoint
+
+    mols = _ensemble()[::3]
+    res_b = batch_singlepoint([_calc(z, x) for z, x in mols])
+    for (z, x), rb in zip(mols, res_b):
+        ref = gfn2.singlepoint(gfn2.new_calc(gfn2.Molecule(np.asarray(z), np.asarray(x))), grad=True)
+        assert abs(rb.get("energy") - ref.energy) <= E_TOL
+        assert np.max(np.abs(rb.get("gradient") - ref.gradient)) <= G_TOL
+        assert np.max(np.abs(rb.get("charges") - ref.qat)) <= Q_TOL
+
+
+def test_batch_per_molecule_settings_and_single_atom():
+    from tblite_gb300 import workloads
+    from tblite_gb300.interface import batch_singlepoint
+
+    z, x = workloads.water_cluster_k(4, seed=7)
+    o_atom = (np.array([8]), np.zeros((1, 3)))
+    cases = [((z, x), {"accuracy": 0.01}), ((z, x), {"temperature": 3000 * 3.166808578545117e-6}),
+             ((z, x), {"mixer-damping": 0.2}), (o_atom, {})]
+    calcs = [_calc(mz, mx, **st) for (mz, mx), st in cases]
+    res_b = batch_singlepoint(calcs)
+    for ((mz, mx), st), rb in zip(cases, res_b):
+        _compare(rb, _calc(mz, mx, **st).singlepoint())
+
+
+def test_batch_restart_and_fallback():
+    from tblite_gb300 import workloads
+    from tblite_gb300.exceptions import TBLiteRuntimeError
+    from tblite_gb300.interface import Result, batch_fallbacks, batch_singlepoint
+
+    (z1, x1), (z2, x2) = workloads.water_cluster_k(6, seed=11), workloads.alkane(9, seed=12)
+    first = batch_singlepoint([_calc(z1, x1), _calc(z2, x2)])
+    again = batch_singlepoint([_calc(z1, x1), _calc(z2, x2)], [Result(r) for r in first])
+    for a, b in zip(first, again):
+        assert abs(a.get("energy") - b.get("energy")) <= E_TOL
+    # a molecule that cannot converge in 3 iterations leaves the batch and fails like a plain call
+    calcs = [_calc(z1, x1), _calc(z2, x2, **{"max-iter": 3})]
+    with pytest.raises(TBLiteRuntimeError, match="Batch entry 1"):
+        batch_singlepoint(calcs)
+    assert batch_fallbacks() == 1

@@ -127,3 +127,24 @@ def test_energy_is_deterministic():
     _, r2 = _gpu(z, x)
     assert r1.get("energy") == r2.get("energy")
     assert np.array_equal(r1.get("charges"), r2.get("charges"))
+
+
+@pytest.mark.parametrize("charge", [0.0, 1.0])
+def test_bond_orders_and_moments(charge):
+    """Wiberg/Mayer bond orders and molecular dipole/quadrupole vs the oracle's post-processing;
+    the cation is a restricted open shell (total and magnetisation channels)."""
+    from tblite_gb300 import workloads
+
+    z, x = workloads.water_cluster((2, 1, 1), seed=12)
+    res, ref = _compare(z, x, acc=1e-3, charge=charge)
+    wbo = res.get("bond-orders")
+    ref_wbo = ref.parts["wbo"]
+    if ref_wbo.shape[0] == 1:
+        assert wbo.shape == (len(z), len(z))
+        assert np.max(np.abs(wbo - ref_wbo[0])) < 1e-6
+    else:
+        assert wbo.shape == (len(z), len(z), 2)
+        for ch in range(2):
+            assert np.max(np.abs(wbo[:, :, ch] - ref_wbo[ch])) < 1e-6
+    assert np.max(np.abs(res.get("dipole") - ref.parts["dipole"])) < 1e-6
+    assert np.max(np.abs(res.get("quadrupole") - ref.parts["quadrupole"])) < 1e-5
