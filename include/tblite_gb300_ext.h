@@ -65,6 +65,29 @@ int tblite_gb300_get_kernel_profile(double* kernel_ms, int* kernel_count, int ns
  * reference's column-major order), 0 when the result holds none (batched results) */
 int tblite_gb300_get_result_bond_order_channels(tblite_result res);
 
+/*
+ * Shell parameters and the parameter gradient (no counterpart in the reference C API; the
+ * reference fits parameters through its Fortran parameter records).  Arrays are per shell of
+ * the calculator (tblite_get_calculator_shell_count): self energy se0 (Hartree), its
+ * coordination-number shift kcn (e_s = se0_s - kcn_s CN_A), chemical hardness eta and
+ * hardness derivative Gamma (third order).  NULL leaves an array untouched.
+ * With the parameter gradient enabled, tblite_get_singlepoint also stores dE/d(parameter) of
+ * the converged energy (explicit derivative at the final density, which the variational SCF
+ * makes exact).
+ */
+void tblite_gb300_set_calculator_parameter_gradient(tblite_context ctx, tblite_calculator calc,
+                                                    int enable);
+void tblite_gb300_get_calculator_shell_parameters(tblite_context ctx, tblite_calculator calc,
+                                                  double* selfenergy, double* kcn,
+                                                  double* hubbard, double* hubbard_deriv);
+void tblite_gb300_set_calculator_shell_parameters(tblite_context ctx, tblite_calculator calc,
+                                                  const double* selfenergy, const double* kcn,
+                                                  const double* hubbard,
+                                                  const double* hubbard_deriv);
+void tblite_gb300_get_result_parameter_gradient(tblite_error error, tblite_result res,
+                                                double* dselfenergy, double* dkcn,
+                                                double* dhubbard, double* dhubbard_deriv);
+
 /* number of engine kernels launched since the library was loaded (all threads) */
 unsigned long long tblite_gb300_get_launch_count(void);
 

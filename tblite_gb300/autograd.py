@@ -1,0 +1,130 @@
+"""``torch.autograd`` bridge: GFN2-xTB energies differentiable in positions and shell parameters.
+
+The energy is evaluated by the CUDA engine (``tblite_get_singlepoint``); the backward pass
+returns the engine's analytic nuclear gradient and its parameter gradient
+(``tblite_gb300_get_result_parameter_gradient``).  Because the SCF energy is stationary in
+the density, both are explicit derivatives at the converged density: no response equations
+are solved.
+
+Differentiable shell parameters (one entry per shell of the calculator, in the calculator's
+shell order): ``selfenergy`` (se0, Hartree), ``kcn`` (coordination-number shift of the self
+energy), ``hubbard`` (chemical hardness) and ``hubbard_deriv`` (third-order hardness
+derivative).  Slater exponents are not differentiable here.
+"""
+from __future__ import annotations
+
+from typing import Dict, Optional, Sequence
+
+import numpy as np
+
+from . import library
+from .interface import Calculator, Result
+
+PARAMETERS = ("selfenergy", "kcn", "hubbard", "hubbard_deriv")
+
+
+def shell_count(calc: Calculator) -> int:
+    return int(calc.get("shell-map").size)
+
+
+def shell_parameters(calc: Calculator) -> Dict[str, np.ndarray]:
+    """The calculator's current per-shell parameters."""
+    nsh = shell_count(calc)
+    out = {k: np.zeros(nsh) for k in PARAMETERS}
+    library.load().tblite_gb300_get_calculator_shell_parameters(
+        calc._ctx, calc._calc, *[library._dp(out[k]) for k in PARAMETERS])
+    library.context_check(calc._ctx)
+    return out
+
+
+def set_shell_parameters(calc: Calculator, **values) -> None:
+    """Replace per-shell parameters (keys of ``PARAMETERS``; missing keys stay unchanged)."""
+    nsh = shell_count(calc)
+    args = []
+    keep = []
+    for k in PARAMETERS:
+        v = values.get(k)
+        if v is None:
+            args.append(None)
+            continue
+        a = np.ascontiguousarray(np.asarray(v, dtype=np.float64).reshape(-1))
+        if a.size != nsh:
+            raise ValueError(f"{k}: expected {nsh} shell values, got {a.size}")
+        keep.append(a)
+        args.append(library._dp(a))
+    library.load().tblite_gb300_set_calculator_shell_parameters(calc._ctx, calc._calc, *args)
+    library.context_check(calc._ctx)
+
+
+def parameter_gradient(res: Result, nsh: int) -> Dict[str, np.ndarray]:
+    """dE/d(parameter) stored by a single point with the parameter gradient enabled."""
+    out = {k: np.zeros(nsh) for k in PARAMETERS}
+    err = library._Error()
+    library.load().tblite_gb300_get_result_parameter_gradient(
+        err.h, res._res, *[library._dp(out[k]) for k in PARAMETERS])
+    err.check()
+    return out
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+def _function():
+    torch = _torch()
+
+    class GFN2Energy(torch.autograd.Function):
+        """E(positions, selfenergy, kcn, hubbard, hubbard_deriv) for one calculator."""
+
+        @staticmethod
+        def forward(ctx, calc, positions, selfenergy, kcn, hubbard, hubbard_deriv):
+            pos = positions.detach().to("cpu", torch.float64).numpy()
+            calc.update(pos)
+            set_shell_parameters(
+                calc, **{k: t.detach().to("cpu", torch.float64).numpy()
+                         for k, t in zip(PARAMETERS, (selfenergy, kcn, hubbard, hubbard_deriv))})
+            library.load().tblite_gb300_set_calculator_parameter_gradient(calc._ctx, calc._calc, 1)
+            res = calc.singlepoint()
+            nsh = selfenergy.numel()
+            pg = parameter_gradient(res, nsh)
+            grads = [torch.from_numpy(res.get("gradient")).to(positions)]
+            grads += [torch.from_numpy(pg[k]).to(selfenergy) for k in PARAMETERS]
+            ctx.save_for_backward(*grads)
+            return torch.tensor(res.get("energy"), dtype=torch.float64, device=positions.device)
+
+        @staticmethod
+        def backward(ctx, grad_e):
+            g = ctx.saved_tensors
+            return (None,) + tuple(grad_e * t for t in g)
+
+    return GFN2Energy
+
+
+_FN = None
+
+
+def gfn2_energy(calc: Calculator, positions, selfenergy=None, kcn=None, hubbard=None,
+                hubbard_deriv=None):
+    """Differentiable GFN2-xTB energy (Hartree) of ``calc``'s molecule at ``positions`` (Bohr,
+    torch tensor [nat, 3]).  Parameters default to the calculator's current values."""
+    global _FN
+    torch = _torch()
+    if _FN is None:
+        _FN = _function()
+    cur = shell_parameters(calc)
+    vals = []
+    for k, v in zip(PARAMETERS, (selfenergy, kcn, hubbard, hubbard_deriv)):
+        vals.append(v if v is not None else torch.tensor(cur[k], dtype=torch.float64))
+    return _FN.apply(calc, positions, *vals)
+
+
+def gfn2_energies(calcs: Sequence[Calculator], positions: Sequence, parameters:
+                  Optional[Sequence[dict]] = None):
+    """Energies of several molecules (one engine call each) as a list of 0-d tensors."""
+    out = []
+    for i, (calc, pos) in enumerate(zip(calcs, positions)):
+        kw = parameters[i] if parameters is not None else {}
+        out.append(gfn2_energy(calc, pos, **kw))
+    return out

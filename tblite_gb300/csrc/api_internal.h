@@ -104,7 +104,7 @@ struct Workspace {
   DBuf<int> b_status;
   // gradient
   DBuf<double> grad, sigma, sig_at, dEdcn;
-  DBuf<double> wbo;
+  DBuf<double> wbo, ones, pgrad;
   // D4 dispersion
   DBuf<int> d4_sp, d4_nref, d4_ngw;
   DBuf<double> d4_refcn, d4_refq, d4_zeff, d4_gam, d4_r4r2, d4_rcov, d4_en, d4_c6ref;
@@ -139,6 +139,10 @@ struct _tblite_calculator {
   bool anneal = false;
   double anneal_kt = 0.0;
   int anneal_hold = 50, anneal_cycles = 50;
+  // shell parameters changed through the extension API: re-upload before the next single point
+  bool params_dirty = false;
+  // evaluate dE/d(shell parameters) with the single point
+  int param_grad = 0;
   std::unique_ptr<Workspace> ws;
 };
 
@@ -148,6 +152,8 @@ struct _tblite_result {
   double energy = 0.0;
   std::vector<double> energies, gradient, sigma, qat, qsh, dpat, qpat, emo, focc, P, C, S, H, wbo;
   int wbo_channels = 0;  // 1 closed shell; 2 (total, magnetisation) for open shell
+  // dE/d(per-shell parameters): self energy, its CN shift, hardness, hardness derivative
+  std::vector<double> dse, dkcn, dhub, dgam3;
   double dipole[3] = {0, 0, 0}, quadrupole[6] = {0, 0, 0, 0, 0, 0};
 };
 

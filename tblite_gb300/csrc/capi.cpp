@@ -191,6 +191,13 @@ static void ensure_workspace(_tblite_calculator* c) {
   Workspace& w = *c->ws;
   const int memory = c->memory > 0 ? std::min(c->memory, c->max_iter) : c->max_iter;
   cudaStream_t s = w.stream;
+  if (c->params_dirty && w.nat == c->nat && w.nao == c->nao && w.nsh == c->nsh) {
+    w.sh_se0.upload(c->sh_se0, s);
+    w.sh_kcn.upload(c->sh_kcn, s);
+    w.sh_hub.upload(c->sh_hub, s);
+    w.sh_gam3.upload(c->sh_gam3, s);
+  }
+  c->params_dirty = false;
   if (w.nat != c->nat || w.nao != c->nao || w.nsh != c->nsh) {
     const size_t n = c->nao, nn = n * n;
     w.sh_alpha.upload(c->sh_alpha, s);
@@ -708,6 +715,17 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
       launch_wbo(m, w.scratch.p, w.wbo.p + (size_t)sp * nat * nat, 2.0, s);
     }
   }
+  // parameter gradient (on request): H0 rebuilt with unit self energies into the scratch
+  // matrix (S, D and Q are rebuilt with identical values), then one thread per shell
+  std::vector<double> h_pgrad, h_cn;
+  if (c->param_grad) {
+    w.ones.upload(std::vector<double>(nsh, 1.0), s);
+    launch_build_h0(m, p, w.ones.p, w.S.p, w.scratch.p, w.D.p, w.Q.p, s);
+    w.pgrad.alloc((size_t)3 * nsh);
+    launch_param_grad(m, p, w.P.p, w.scratch.p, w.qsh_o.p, w.pgrad.p, s);
+    w.pgrad.download(h_pgrad, (size_t)3 * nsh, s);
+    w.cn.download(h_cn, nat, s);
+  }
   g_prof.end(s);
   g_prof.begin(PH_TRANSFER, s);
   w.C.download(res->C, (size_t)n * n, s);
@@ -749,6 +767,18 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
   }
   res->wbo_channels = nch;
   molecular_moments(mol, res);
+  if (c->param_grad) {  // self energy e_s = se0_s - kcn_s CN_A  =>  dE/dkcn_s = -CN_A dE/de_s
+    res->dse.assign(h_pgrad.begin(), h_pgrad.begin() + nsh);
+    res->dhub.assign(h_pgrad.begin() + nsh, h_pgrad.begin() + 2 * nsh);
+    res->dgam3.assign(h_pgrad.begin() + 2 * nsh, h_pgrad.end());
+    res->dkcn.resize(nsh);
+    for (int i = 0; i < nsh; ++i) res->dkcn[i] = -h_cn[c->sh_atom[i]] * res->dse[i];
+  } else {
+    res->dse.clear();
+    res->dhub.clear();
+    res->dgam3.clear();
+    res->dkcn.clear();
+  }
   if (!converged)
     throw std::runtime_error("SCF not converged in " + std::to_string(iscf) + " cycles");
 }
@@ -835,6 +865,71 @@ unsigned long long tblite_gb300_get_launch_count(void) { return g_kernel_launche
 
 int tblite_gb300_get_result_bond_order_channels(tblite_result res) {
   return res ? res->wbo_channels : 0;
+}
+
+void tblite_gb300_set_calculator_parameter_gradient(tblite_context ctx, tblite_calculator calc,
+                                                    int enable) {
+  if (!ctx) return;
+  if (!calc) {
+    ctx->push("Calculator object is missing");
+    return;
+  }
+  calc->param_grad = enable != 0;
+}
+
+void tblite_gb300_get_calculator_shell_parameters(tblite_context ctx, tblite_calculator calc,
+                                                  double* selfenergy, double* kcn,
+                                                  double* hubbard, double* hubbard_deriv) {
+  if (!ctx) return;
+  if (!calc) {
+    ctx->push("Calculator object is missing");
+    return;
+  }
+  const size_t nsh = calc->nsh;
+  if (selfenergy) std::copy(calc->sh_se0.begin(), calc->sh_se0.begin() + nsh, selfenergy);
+  if (kcn) std::copy(calc->sh_kcn.begin(), calc->sh_kcn.begin() + nsh, kcn);
+  if (hubbard) std::copy(calc->sh_hub.begin(), calc->sh_hub.begin() + nsh, hubbard);
+  if (hubbard_deriv) std::copy(calc->sh_gam3.begin(), calc->sh_gam3.begin() + nsh, hubbard_deriv);
+}
+
+void tblite_gb300_set_calculator_shell_parameters(tblite_context ctx, tblite_calculator calc,
+                                                  const double* selfenergy, const double* kcn,
+                                                  const double* hubbard,
+                                                  const double* hubbard_deriv) {
+  if (!ctx) return;
+  if (!calc) {
+    ctx->push("Calculator object is missing");
+    return;
+  }
+  const size_t nsh = calc->nsh;
+  if (hubbard)
+    for (size_t i = 0; i < nsh; ++i)
+      if (!(hubbard[i] > 0.0)) {
+        ctx->push("Shell hardness must be positive");
+        return;
+      }
+  if (selfenergy) std::copy(selfenergy, selfenergy + nsh, calc->sh_se0.begin());
+  if (kcn) std::copy(kcn, kcn + nsh, calc->sh_kcn.begin());
+  if (hubbard) std::copy(hubbard, hubbard + nsh, calc->sh_hub.begin());
+  if (hubbard_deriv) std::copy(hubbard_deriv, hubbard_deriv + nsh, calc->sh_gam3.begin());
+  calc->params_dirty = true;
+}
+
+void tblite_gb300_get_result_parameter_gradient(tblite_error error, tblite_result res,
+                                                double* dselfenergy, double* dkcn,
+                                                double* dhubbard, double* dhubbard_deriv) {
+  if (!res) {
+    set_err(error, "Result container is missing");
+    return;
+  }
+  if (res->dse.empty()) {
+    set_err(error, "Result does not contain a parameter gradient");
+    return;
+  }
+  if (dselfenergy) std::copy(res->dse.begin(), res->dse.end(), dselfenergy);
+  if (dkcn) std::copy(res->dkcn.begin(), res->dkcn.end(), dkcn);
+  if (dhubbard) std::copy(res->dhub.begin(), res->dhub.end(), dhubbard);
+  if (dhubbard_deriv) std::copy(res->dgam3.begin(), res->dgam3.end(), dhubbard_deriv);
 }
 
 int tblite_get_version(void) { return 7 * 100 + 0; }  // 0.7.0 -> 700 (reference version.h)

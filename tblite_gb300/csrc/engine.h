@@ -202,6 +202,10 @@ void density_matrix(int n, int k, const double* C, const double* f, double* P, d
                     cudaStream_t s);
 // wbo[A][B] += scale * sum (PS)_{nu mu} (PS)_{mu nu} over the orbitals of atoms A != B
 void launch_wbo(const DevMol& m, const double* PS, double* wbo, double scale, cudaStream_t s);
+// dE/d(shell self energy, hardness, hardness derivative) into out[3][nsh]; Hp is H0 built
+// with all self energies equal to one, qsh the output shell charges
+void launch_param_grad(const DevMol& m, const Gfn2Scalars& p, const double* P, const double* Hp,
+                       const double* qsh, double* out, cudaStream_t s);
 
 // ---------------------------------------------------------------------------------------------
 // Batched ensemble path: many molecules in one launch per step.  Every molecule owns a slice of

@@ -1060,6 +1060,57 @@ void launch_wbo(const DevMol& m, const double* PS, double* wbo, double scale, cu
 }
 
 // ------------------------------------------------------------------------------------
+// Parameter gradient of the converged energy (the SCF energy is stationary in the density,
+// so dE/dtheta is the explicit derivative at the final P and charges):
+//   self energies   H0_{mu nu} = (e_i + e_j)/2 * G_{mu nu}  =>  dE/de_s = sum_{mu in s, nu} P G'
+//                   with G' = H0 built with every self energy set to one (= 2 G)
+//   hardness        E2 = 1/2 sum_st q_s q_t gamma_st, gamma = (R^2 + eta_st^-2)^-1/2,
+//                   eta_st = (eta_s + eta_t)/2  =>  dgamma/deta_st = eta_st^-3 (R^2+eta_st^-2)^-3/2
+//   third order     E3 = sum_s Gamma_s q_s^3 / 3
+// one thread per shell
+// ------------------------------------------------------------------------------------
+__global__ void k_param_grad(DevMol m, Gfn2Scalars p, const double* __restrict__ P,
+                             const double* __restrict__ Hp, const double* __restrict__ qsh,
+                             double* out /* [3][nsh]: dse, dhub, dgam3 */) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= m.nsh) return;
+  const int n = m.nao, nsh = m.nsh;
+  const int o = m.sh_ao[s], no = 2 * m.sh_l[s] + 1;
+  double tr = 0.0;
+  for (int mu = o; mu < o + no; ++mu) {
+    const double* pr = P + (size_t)mu * n;
+    const double* hr = Hp + (size_t)mu * n;
+    for (int nu = 0; nu < n; ++nu) tr += pr[nu] * hr[nu];
+  }
+  const double qs = qsh[s], es = m.sh_hub[s];
+  const int ia = m.sh_atom[s];
+  double dh = 0.5 * qs * qs;  // gamma_ss = eta_s
+  for (int t = 0; t < nsh; ++t) {
+    if (t == s) continue;
+    const int ja = m.sh_atom[t];
+    double r2 = 0.0;
+    for (int k = 0; k < 3; ++k) {
+      const double d = m.xyz[3 * ia + k] - m.xyz[3 * ja + k];
+      r2 += d * d;
+    }
+    const double eta = 0.5 * (es + m.sh_hub[t]);
+    const double ie2 = 1.0 / (eta * eta);
+    const double den = r2 + ie2;
+    const double g = ie2 / eta / (den * sqrt(den));
+    dh += qs * qsh[t] * 0.5 * g;
+  }
+  out[s] = tr;
+  out[nsh + s] = dh;
+  out[2 * nsh + s] = qs * qs * qs / 3.0;
+  (void)p;
+}
+void launch_param_grad(const DevMol& m, const Gfn2Scalars& p, const double* P, const double* Hp,
+                       const double* qsh, double* out, cudaStream_t s) {
+  ++g_kernel_launches;
+  k_param_grad<<<(m.nsh + 127) / 128, 128, 0, s>>>(m, p, P, Hp, qsh, out);
+}
+
+// ------------------------------------------------------------------------------------
 // Batched launches: blockIdx.z walks the listed molecules; each block runs the same body as
 // the one-molecule kernel on that molecule's slices.  Blocks past a molecule's own size exit
 // through the bodies' bounds checks (or the explicit tile checks below).

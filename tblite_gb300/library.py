@@ -77,6 +77,13 @@ _SIGNATURES = {
     "tblite_gb300_get_profile": (c_int, [_dbl_p, _int_p, c_int, _dbl_p, _int_p]),
     "tblite_gb300_get_launch_count": (ctypes.c_ulonglong, []),
     "tblite_gb300_get_result_bond_order_channels": (c_int, [c_void_p]),
+    "tblite_gb300_set_calculator_parameter_gradient": (None, [c_void_p, c_void_p, c_int]),
+    "tblite_gb300_get_calculator_shell_parameters": (
+        None, [c_void_p, c_void_p, _dbl_p, _dbl_p, _dbl_p, _dbl_p]),
+    "tblite_gb300_set_calculator_shell_parameters": (
+        None, [c_void_p, c_void_p, _dbl_p, _dbl_p, _dbl_p, _dbl_p]),
+    "tblite_gb300_get_result_parameter_gradient": (
+        None, [c_void_p, c_void_p, _dbl_p, _dbl_p, _dbl_p, _dbl_p]),
     "tblite_gb300_get_kernel_profile": (c_int, [_dbl_p, _int_p, c_int]),
     "tblite_gb300_density_matrix_noalloc": (
         c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
