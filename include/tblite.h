@@ -202,6 +202,35 @@ TBLITE_API_ENTRY void TBLITE_API_CALL tblite_get_singlepoint(tblite_context ctx,
                                                             tblite_calculator calc,
                                                             tblite_result res);
 
+/* ---- interaction containers: include/tblite/container.h:31, 61-70 ---- */
+typedef struct _tblite_container* tblite_container;
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_calculator_push_back(tblite_context ctx,
+                                                                 tblite_calculator calc,
+                                                                 tblite_container* cont);
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_delete_container(tblite_container* cont);
+
+/* ---- implicit solvation: include/tblite/solvation.h:30-52, 104-109 ----
+ * Available here: ALPB with the GFN2 parameters (version tblite_solvation_alpb_gfn2) for the
+ * solvent "water", with its CDS and free-energy shift terms; other solvents and models report
+ * an error. */
+enum tblite_ref_solvation_state {
+  tblite_state_gsolv = 1,
+  tblite_state_bar1mol = 2,
+  tblite_state_reference = 3,
+};
+enum tblite_solvation_param {
+  tblite_solvation_gbe = 10,
+  tblite_solvation_alpb_gfn1 = 11,
+  tblite_solvation_alpb_gfn2 = 12,
+  tblite_solvation_gb = 20,
+  tblite_solvation_gbsa_gfn1 = 21,
+  tblite_solvation_gbsa_gfn2 = 22,
+};
+TBLITE_API_ENTRY tblite_container TBLITE_API_CALL
+tblite_new_alpb_solvation_solvent(tblite_error error, tblite_structure mol, char* solvent,
+                                  enum tblite_solvation_param version,
+                                  enum tblite_ref_solvation_state refstate);
+
 #ifdef __cplusplus
 }
 #endif

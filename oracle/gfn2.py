@@ -405,7 +405,7 @@ def setup(calc: Calc):
 MPSCALE = np.array([1.0, 2.0, 1.0, 2.0, 2.0, 1.0])
 
 
-def potentials(calc, st, qsh, qat, dpat, qpat, disp=None):
+def potentials(calc, st, qsh, qat, dpat, qpat, disp=None, solv=None):
     """vsh, vat, vdp, vqp; reference coulomb get_potential routines."""
     vsh = st["gamma"] @ qsh + qsh**2 * st["gam3"]
     vat = np.einsum("ijk,jk->i", st["asd"], dpat) + np.einsum("ijq,jq->i", st["asq"], qpat)
@@ -414,6 +414,8 @@ def potentials(calc, st, qsh, qat, dpat, qpat, disp=None):
     vqp = np.einsum("ijq,i->jq", st["asq"], qat) + 2 * st["qkernel"][:, None] * qpat * MPSCALE
     if disp is not None:
         vat = vat + disp.potential(qat)
+    if solv is not None:
+        vat = vat + solv.potential(qat)
     return vsh, vat, vdp, vqp
 
 
@@ -443,7 +445,7 @@ def fock(calc, st, vsh, vat, vdp, vqp):
     return F, vao, ao2at, ao2sh
 
 
-def singlepoint(calc: Calc, grad=True, verbose=False, dispersion=None):
+def singlepoint(calc: Calc, grad=True, verbose=False, dispersion=None, solvation=None):
     mol = calc.mol
     nat = len(mol.numbers)
     st = setup(calc)
@@ -489,6 +491,13 @@ def singlepoint(calc: Calc, grad=True, verbose=False, dispersion=None):
         disp = D4(calc, st)
         edisp = disp.energy_nonsc(gradient, sigma)
     energies += edisp
+    # implicit solvation (interactions container: ALPB + CDS + shift), geometry part
+    solv = solvation
+    esolv = np.zeros(nat)
+    if solv is not None:
+        solv.update(xyz)
+        esolv = solv.nonsc_energies()
+    energies += esolv
     # SAD guess, wavefunction/guess.f90:51-120
     qat = np.full(nat, mol.charge / nat)
     qsh = st["n0sh"] / st["n0at"][calc.sh_atom] * qat[calc.sh_atom]
@@ -511,7 +520,7 @@ def singlepoint(calc: Calc, grad=True, verbose=False, dispersion=None):
             qat = np.zeros(nat)
             np.add.at(qat, calc.sh_atom, qsh)
         iscf += 1
-        vsh, vat, vdp, vqp = potentials(calc, st, qsh, qat, dpat, qpat, disp)
+        vsh, vat, vdp, vqp = potentials(calc, st, qsh, qat, dpat, qpat, disp, solv)
         F, vao, ao2at, ao2sh = fock(calc, st, vsh, vat, vdp, vqp)
         mixer.set(np.concatenate([qsh, dpat.ravel(), qpat.ravel()]))
         emo, C = scipy.linalg.eigh(F, st["S"], type=1, driver="gvd", lower=False)
@@ -540,6 +549,8 @@ def singlepoint(calc: Calc, grad=True, verbose=False, dispersion=None):
         eelec += electrostatic_energies(calc, st, qsh, qat, dpat, qpat)
         if disp is not None:
             eelec += disp.energy_sc(qat)
+        if solv is not None:
+            eelec += solv.energies(qat)
         econverged = abs(float(np.sum(eelec)) - elast) < econv
         pconverged = mixer.error() < pconv
         converged = econverged and pconverged
@@ -586,6 +597,8 @@ def singlepoint(calc: Calc, grad=True, verbose=False, dispersion=None):
     if grad:
         gradient, sigma = _gradient(calc, st, gradient, sigma, C, emo, focc, P, qsh, qat, dpat,
                                     qpat, vao, vdp, vqp, disp)
+        if solv is not None:
+            gradient += solv.gradient(qat)
     return Result(energy=energy, energies=energies, gradient=gradient, sigma=sigma, qsh=qsh,
                   qat=qat, dpat=dpat, qpat=qpat, density=P, emo=emo, focc=focc, iterations=iscf,
                   converged=converged, parts=parts)

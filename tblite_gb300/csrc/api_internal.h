@@ -105,6 +105,10 @@ struct Workspace {
   // gradient
   DBuf<double> grad, sigma, sig_at, dEdcn;
   DBuf<double> wbo, ones, pgrad;
+  // implicit solvation: per-atom model arrays [9][nat], grid [230][4], work [4][nat]
+  DBuf<double> sv_atom, sv_grid, sv_work;
+  DBuf<int> sv_nbl, sv_nnb, sv_status;
+  int sv_nat = -1;
   // D4 dispersion
   DBuf<int> d4_sp, d4_nref, d4_ngw;
   DBuf<double> d4_refcn, d4_refq, d4_zeff, d4_gam, d4_r4r2, d4_rcov, d4_en, d4_c6ref;
@@ -114,6 +118,20 @@ struct Workspace {
     if (eig) eigen_destroy(eig);
     if (stream) cudaStreamDestroy(stream);
   }
+};
+
+// ALPB(water) + CDS + shift model for one molecule (reference solvation/alpb.f90, cds.f90,
+// shift.f90 with the gfn2 water parameters), built by tblite_new_alpb_solvation_solvent
+struct SolvModel {
+  int nat = 0, state = 1;
+  double keps = 0, alpbet = 0, born_scale = 0, lrcut = 0, srcut = 0, ah0 = 0, ah1 = 0, ah3 = 0;
+  double shift = 0;  // total free-energy shift (Hartree)
+  std::vector<double> vdwr, rho, svdw, vdwsa, wrp, trj2_lo, trj2_hi, tension, hbond;
+  std::vector<double> grid;  // [230][4]
+};
+
+struct _tblite_container {
+  std::unique_ptr<SolvModel> solv;
 };
 
 struct _tblite_calculator {
@@ -143,6 +161,8 @@ struct _tblite_calculator {
   bool params_dirty = false;
   // evaluate dE/d(shell parameters) with the single point
   int param_grad = 0;
+  // implicit solvation container moved in by tblite_calculator_push_back
+  std::unique_ptr<SolvModel> solv;
   std::unique_ptr<Workspace> ws;
 };
 
@@ -169,6 +189,9 @@ void electron_counts(const _tblite_calculator* c, const _tblite_structure* mol, 
 // molecular dipole and traceless quadrupole from the atomic charges and multipoles
 // (wavefunction/mulliken.f90 get_molecular_dipole_moment / get_molecular_quadrupole_moment)
 void molecular_moments(const _tblite_structure* mol, _tblite_result* res);
+// ALPB(water) + CDS + shift model for the molecule (reference state 1 gsolv, 2 bar1mol,
+// 3 reference)
+std::unique_ptr<SolvModel> build_solvation(const _tblite_structure* mol, int state);
 // the one-molecule single point (energy + gradient) into res
 void run_singlepoint(_tblite_context* ctx, const _tblite_structure* mol, _tblite_calculator* c,
                      _tblite_result* res);

@@ -17,9 +17,10 @@
 //
 // A molecule leaves the batch for the one-molecule path (which then reproduces exactly what a
 // plain call does, including its errors) when it is larger than the batched
-// tridiagonalisation holds, uses temperature annealing, would need more Broyden history than
-// the batch keeps, does not converge within its iteration limit, or fails (overlap not
-// positive definite, singular Broyden system).
+// tridiagonalisation holds, uses temperature annealing, carries an implicit solvation model or
+// asks for the parameter gradient, would need more Broyden history than the batch keeps, does
+// not converge within its iteration limit, or fails (overlap not positive definite, singular
+// Broyden system).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -792,7 +793,8 @@ extern "C" int tblite_gb300_batch_singlepoint(tblite_context ctx, int nmol,
       continue;
     }
     const bool anneal = c->anneal && c->anneal_kt > c->etemp;
-    if (pl.nao > tri_max || anneal || pl.max_iter < 1) {
+    // implicit solvation and the parameter gradient run on the one-molecule path
+    if (pl.nao > tri_max || anneal || pl.max_iter < 1 || c->solv || c->param_grad) {
       plain.push_back(i);
       continue;
     }

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -17,6 +18,7 @@
 #include "element_data.inc"
 #include "engine.h"
 #include "params_gfn2.inc"
+#include "params_solv.inc"
 
 #include "api_internal.h"
 
@@ -345,6 +347,65 @@ static DevD4 dev_d4(const _tblite_calculator* c, D4Work& wk) {
   return d;
 }
 
+static void alpb_shape(const SolvModel& sm, const double* xyz, double* adet, double cen[3],
+                       double I[3][3], double* vol_out);
+static void alpb_shape_gradient(const SolvModel& sm, const double* xyz, const double* qat,
+                                double* grad);
+
+// device view of the solvation model; uploads the per-atom arrays when the model is new
+static DevSolv dev_solv(_tblite_calculator* c, const _tblite_structure* mol) {
+  Workspace& w = *c->ws;
+  const SolvModel& sm = *c->solv;
+  const int nat = sm.nat;
+  cudaStream_t s = w.stream;
+  if (w.sv_nat != nat) {
+    std::vector<double> atom;
+    for (const auto* v : {&sm.vdwr, &sm.rho, &sm.svdw, &sm.vdwsa, &sm.wrp, &sm.trj2_lo,
+                          &sm.trj2_hi, &sm.tension, &sm.hbond})
+      atom.insert(atom.end(), v->begin(), v->end());
+    w.sv_atom.upload(atom, s);
+    w.sv_grid.upload(sm.grid, s);
+    w.sv_work.alloc((size_t)4 * nat);
+    w.sv_nbl.alloc((size_t)nat * SOLV_MAXNB);
+    w.sv_nnb.alloc(nat);
+    w.sv_status.alloc(1);
+    w.sv_nat = nat;
+  }
+  cuda_check(cudaMemsetAsync(w.sv_status.p, 0, sizeof(int), s), "zero");
+  DevSolv v{};
+  v.nat = nat;
+  v.lrcut = sm.lrcut;
+  v.srcut = sm.srcut;
+  v.keps = sm.keps;
+  v.alpbet = sm.alpbet;
+  v.born_scale = sm.born_scale;
+  v.ah0 = sm.ah0;
+  v.ah1 = sm.ah1;
+  v.ah3 = sm.ah3;
+  v.shift = sm.shift;
+  double cen[3], I[3][3], vol;
+  alpb_shape(sm, mol->xyz.data(), &v.adet, cen, I, &vol);
+  const double* a = w.sv_atom.p;
+  v.vdwr = a;
+  v.rho = a + nat;
+  v.svdw = a + 2 * nat;
+  v.vdwsa = a + 3 * nat;
+  v.wrp = a + 4 * nat;
+  v.trj2_lo = a + 5 * nat;
+  v.trj2_hi = a + 6 * nat;
+  v.tension = a + 7 * nat;
+  v.hbond = a + 8 * nat;
+  v.grid = w.sv_grid.p;
+  v.brad = w.sv_work.p;
+  v.dscale = w.sv_work.p + nat;
+  v.wbr = w.sv_work.p + 2 * nat;
+  v.surface = w.sv_work.p + 3 * nat;
+  v.nbl = w.sv_nbl.p;
+  v.nnb = w.sv_nnb.p;
+  v.status = w.sv_status.p;
+  return v;
+}
+
 static DevMol dev_mol(const _tblite_calculator* c) {
   const Workspace& w = *c->ws;
   DevMol m{};
@@ -534,6 +595,12 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
   D4Work d4w{};
   DevD4 d4 = c->has_d4 ? dev_d4(c, d4w) : DevD4{};
   if (c->has_d4) d4_setup(m, d4, d4w, true, w.grad.p, w.sig_at.p, s);
+  // implicit solvation: Born radii, surfaces, geometry-only energies into erep
+  DevSolv dsolv{};
+  if (c->solv) {
+    dsolv = dev_solv(c, mol);
+    solv_setup(dsolv, w.xyz.p, w.erep.p, s);
+  }
   const int chol = eigen_set_overlap(w.eig, w.S.p);
   g_prof.end(s);
   if (chol != 0) throw std::runtime_error("overlap matrix is not positive definite");
@@ -624,6 +691,7 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
     launch_coulomb_potential(m, p, w.mrad.p, w.qsh.p, w.qat.p, w.dpat.p, w.qpat.p, w.vsh.p, w.vat.p,
                              w.vdp.p, w.vqp.p, s);
     if (c->has_d4) d4_potential(m, d4, d4w, w.qat.p, w.vat.p, s);
+    if (c->solv) solv_potential(dsolv, w.xyz.p, w.qat.p, w.vat.p, s);
     launch_vao(m, w.vsh.p, w.vat.p, w.vao.p, s);
     g_prof.end(s);
     g_prof.begin(PH_FOCK, s);
@@ -652,6 +720,7 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
     launch_coulomb_energy(m, p, w.mrad.p, w.qsh_o.p, w.qat_o.p, w.dpat_o.p, w.qpat_o.p, w.eelec.p,
                           s);
     if (c->has_d4) d4_energy(m, d4, d4w, w.qat_o.p, w.eelec.p, s);
+    if (c->solv) solv_energy(dsolv, w.xyz.p, w.qat_o.p, w.eelec.p, s);
     g_prof.end(s);
     w.eelec.download(h_eelec, nat, s);
     w.scal.download(h_scal, 2, s);
@@ -686,6 +755,7 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
   launch_coulomb_gradient(m, p, w.mrad.p, w.dmrdcn.p, w.qsh_o.p, w.qat_o.p, w.dpat_o.p, w.qpat_o.p,
                           w.grad.p, w.sig_at.p, w.dEdcn.p, s);
   if (c->has_d4) d4_gradient(m, d4, d4w, w.qat_o.p, w.grad.p, w.sig_at.p, s);
+  if (c->solv) solv_gradient(dsolv, w.xyz.p, w.qat_o.p, w.grad.p, s);
   // W = C diag(f e) C^T  (scf/diag.f90:110-143)
   launch_fe(n, w.focc.p, w.emo.p, w.vec_out.p, s);
   density_matrix(n, h_cnt[0], w.C.p, w.vec_out.p, w.W.p, w.scratch.p, s);
@@ -745,11 +815,18 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
     w.S.download(res->S, (size_t)n * n, s);
     w.H.download(res->H, (size_t)n * n, s);
   }
+  std::vector<int> h_sv_status;
+  if (c->solv) w.sv_status.download(h_sv_status, 1, s);
   g_prof.end(s);
   stream_wait(s);
   cuda_check(cudaGetLastError(), "results");
   g_prof.collect();
   g_prof.iterations = iscf;
+  if (c->solv) {
+    if (h_sv_status[0] != 0)
+      throw std::runtime_error("solvent accessible surface: more neighbours than the GPU kernel holds");
+    alpb_shape_gradient(*c->solv, mol->xyz.data(), res->qat.data(), res->gradient.data());
+  }
   res->sigma.assign(9, 0.0);
   for (int k = 0; k < 9; ++k) {
     double acc = h_sigma[k];
@@ -786,6 +863,159 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
 // --------------------------------------------------------------------------------------
 // C ABI
 // --------------------------------------------------------------------------------------
+// --------------------------------------------------------------------------------------
+// ALPB(water) + CDS + shift model: parameters per atom (solvation/data/alpb.f90:227-249,
+// data/cds.f90:225-249, data/shift.f90:221-233; alpb.f90:173-206; cds.f90:166-184;
+// surface.f90:80-140; shift.f90:150-241) and the 230-point Lebedev grid from its orbits
+// --------------------------------------------------------------------------------------
+static std::vector<double> lebedev230() {
+  std::vector<double> g;
+  for (int o = 0; o < LEB230_NORB; ++o) {
+    const int t = LEB230_TYPE[o];
+    const double a = LEB230_A[o], b = LEB230_B[o], v = LEB230_V[o] * 4.0 * M_PI;
+    double base[3];
+    if (t == 1) {
+      base[0] = 1.0; base[1] = 0.0; base[2] = 0.0;
+    } else if (t == 3) {
+      const double s = sqrt(1.0 / 3.0);
+      base[0] = s; base[1] = s; base[2] = s;
+    } else if (t == 4) {
+      base[0] = a; base[1] = a; base[2] = sqrt(1.0 - 2.0 * a * a);
+    } else if (t == 5) {
+      base[0] = a; base[1] = sqrt(1.0 - a * a); base[2] = 0.0;
+    } else if (t == 6) {
+      base[0] = a; base[1] = b; base[2] = sqrt(1.0 - a * a - b * b);
+    } else {
+      throw std::runtime_error("unknown Lebedev orbit type");
+    }
+    // every distinct signed permutation of the generator
+    std::vector<std::array<double, 3>> pts;
+    const int perm[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+    for (auto& pm : perm)
+      for (int sg = 0; sg < 8; ++sg) {
+        std::array<double, 3> p;
+        for (int k = 0; k < 3; ++k) {
+          const double c = base[pm[k]];
+          p[k] = c == 0.0 ? 0.0 : ((sg >> k) & 1 ? -c : c);
+        }
+        if (std::find(pts.begin(), pts.end(), p) == pts.end()) pts.push_back(p);
+      }
+    std::sort(pts.begin(), pts.end());
+    for (auto& p : pts) {
+      g.push_back(p[0]);
+      g.push_back(p[1]);
+      g.push_back(p[2]);
+      g.push_back(v);
+    }
+  }
+  if (g.size() != 4 * 230) throw std::runtime_error("Lebedev grid has the wrong size");
+  return g;
+}
+
+std::unique_ptr<SolvModel> build_solvation(const _tblite_structure* mol, int state) {
+  auto m = std::make_unique<SolvModel>();
+  const int nat = mol->nat;
+  m->nat = nat;
+  m->state = state;
+  const double eps = ALPB_WATER_EPSV;
+  m->alpbet = 0.571412 / eps;
+  m->keps = (1.0 / eps - 1.0) / (1.0 + m->alpbet);
+  m->born_scale = ALPB_WATER_C1;
+  m->lrcut = 35.0 * SOLV_AATOAU;
+  const double probe = CDS_WATER_RPROBE * SOLV_AATOAU;
+  const double w = 0.3 * SOLV_AATOAU;
+  m->ah0 = 0.5;
+  m->ah1 = 3.0 / (4.0 * w);
+  m->ah3 = -1.0 / (4.0 * w * w * w);
+  double maxsa = 0.0;
+  for (int i = 0; i < nat; ++i) {
+    const int z = mol->num[i];
+    if (z < 1 || z > 94) throw std::runtime_error("No solvation parameters for Z > 94");
+    const double rv = SOLV_RVDW_D3[z - 1];
+    m->vdwr.push_back(rv);
+    m->rho.push_back(rv * ALPB_WATER_SX[z - 1]);
+    m->svdw.push_back(rv - ALPB_WATER_SOSET * 0.1 * SOLV_AATOAU);
+    const double vs = rv + probe;
+    maxsa = std::max(maxsa, vs);
+    m->vdwsa.push_back(vs);
+    m->trj2_lo.push_back((vs - w) * (vs - w));
+    m->trj2_hi.push_back((vs + w) * (vs + w));
+    auto part = [&](double r) {
+      return (0.25 / w + 3.0 * m->ah3 * (0.2 * r * r - 0.5 * r * vs + vs * vs / 3.0)) * r * r * r;
+    };
+    m->wrp.push_back(part(vs + w) - part(vs - w));
+    m->tension.push_back(CDS_WATER_GAMSCALE[z - 1] * 1.0e-5);
+    const double hb = -SOLV_KCALTOAU * CDS_WATER_SQRTGHB[z - 1] * CDS_WATER_SQRTGHB[z - 1];
+    m->hbond.push_back(hb / (4.0 * M_PI * vs * vs));
+  }
+  m->srcut = 2.0 * (w + maxsa) + 2.0 * SOLV_AATOAU;
+  // free-energy shift and reference state (shift.f90:191-241; CODATA 2018 constants)
+  const double kb_au = 1.380649e-23 / 4.3597447222071e-18, temp = 298.15, amb = 298.15;
+  const double vm = 8.314462618 * amb / 1.0e2;
+  double stateshift = 0.0;
+  if (state == 2) stateshift = temp * kb_au * log(vm * temp / amb);
+  if (state == 3)
+    stateshift = temp * kb_au *
+                 (log(vm * temp / amb) + log(SHIFT_WATER_RHOS / 1.0e-3 * 1.0 / SHIFT_WATER_SMASS));
+  m->shift = SHIFT_WATER_GSHIFT * SOLV_KCALTOAU + stateshift;
+  m->grid = lebedev230();
+  return m;
+}
+
+// shape descriptor of the ALPB term (alpb.f90:656-691) and its gradient (693-787)
+static void alpb_shape(const SolvModel& sm, const double* xyz, double* adet, double cen[3],
+                       double I[3][3], double* vol_out) {
+  double vol = 0.0;
+  cen[0] = cen[1] = cen[2] = 0.0;
+  for (int i = 0; i < sm.nat; ++i) {
+    const double r3 = sm.vdwr[i] * sm.vdwr[i] * sm.vdwr[i];
+    vol += r3;
+    for (int k = 0; k < 3; ++k) cen[k] += xyz[3 * i + k] * r3;
+  }
+  for (int k = 0; k < 3; ++k) cen[k] /= vol;
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) I[a][b] = 0.0;
+  for (int i = 0; i < sm.nat; ++i) {
+    const double r2 = sm.vdwr[i] * sm.vdwr[i], r3 = r2 * sm.vdwr[i];
+    double v[3], vv = 0.0;
+    for (int k = 0; k < 3; ++k) {
+      v[k] = xyz[3 * i + k] - cen[k];
+      vv += v[k] * v[k];
+    }
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) I[a][b] += r3 * ((a == b ? vv + 0.4 * r2 : 0.0) - v[a] * v[b]);
+  }
+  const double det = I[0][0] * (I[1][1] * I[2][2] - I[1][2] * I[2][1]) -
+                     I[0][1] * (I[1][0] * I[2][2] - I[1][2] * I[2][0]) +
+                     I[0][2] * (I[1][0] * I[2][1] - I[1][1] * I[2][0]);
+  *adet = sqrt(pow(det, 1.0 / 3.0) / (0.4 * vol));
+  *vol_out = vol;
+}
+
+static void alpb_shape_gradient(const SolvModel& sm, const double* xyz, const double* qat,
+                                double* grad) {
+  double adet, cen[3], I[3][3], vol;
+  alpb_shape(sm, xyz, &adet, cen, I, &vol);
+  double qt = 0.0;
+  for (int i = 0; i < sm.nat; ++i) qt += qat[i];
+  double d[3][3];
+  d[0][0] = I[0][0] * (I[1][1] + I[2][2]) - I[0][1] * I[0][1] - I[0][2] * I[0][2];
+  d[1][1] = I[1][1] * (I[0][0] + I[2][2]) - I[0][1] * I[0][1] - I[1][2] * I[1][2];
+  d[2][2] = I[2][2] * (I[0][0] + I[1][1]) - I[0][2] * I[0][2] - I[1][2] * I[1][2];
+  d[0][1] = d[1][0] = I[0][1] * I[2][2] - I[0][2] * I[1][2];
+  d[0][2] = d[2][0] = I[0][2] * I[1][1] - I[0][1] * I[2][1];
+  d[1][2] = d[2][1] = I[0][0] * I[1][2] - I[0][1] * I[0][2];
+  const double f = 250.0 / (48.0 * vol * vol * vol * pow(adet, 5)) *
+                   (-0.5 * sm.keps * sm.alpbet * qt * qt / (adet * adet));
+  for (int i = 0; i < sm.nat; ++i) {
+    const double r3 = sm.vdwr[i] * sm.vdwr[i] * sm.vdwr[i];
+    double v[3];
+    for (int k = 0; k < 3; ++k) v[k] = xyz[3 * i + k] - cen[k];
+    for (int a = 0; a < 3; ++a)
+      grad[3 * i + a] += r3 * f * (d[a][0] * v[0] + d[a][1] * v[1] + d[a][2] * v[2]);
+  }
+}
+
 void molecular_moments(const _tblite_structure* mol, _tblite_result* res) {
   const int nat = res->nat;
   for (int k = 0; k < 3; ++k) res->dipole[k] = 0.0;
@@ -1141,6 +1371,72 @@ void tblite_get_result_overlap_matrix(tblite_error error, tblite_result res, dou
 void tblite_get_result_hamiltonian_matrix(tblite_error error, tblite_result res, double* hmat) {
   RESULT_GUARD(!res->H.empty(), "Result does not contain Hamiltonian matrix");
   std::copy(res->H.begin(), res->H.end(), hmat);
+}
+
+void tblite_calculator_push_back(tblite_context ctx, tblite_calculator calc,
+                                 tblite_container* cont) {
+  if (!ctx) return;
+  if (!calc) {
+    ctx->push("Calculator object is missing");
+    return;
+  }
+  if (!cont || !*cont) {
+    ctx->push("Container object is missing");
+    return;
+  }
+  if ((*cont)->solv) {
+    if (calc->solv) {
+      ctx->push("Calculator already holds an implicit solvation model");
+      return;
+    }
+    if ((*cont)->solv->nat != calc->nat) {
+      ctx->push("Solvation model was built for a different structure");
+      return;
+    }
+    calc->solv = std::move((*cont)->solv);
+  }
+  delete *cont;  // the container moves into the calculator (api/container.f90:53-94)
+  *cont = nullptr;
+}
+
+void tblite_delete_container(tblite_container* cont) {
+  if (cont && *cont) {
+    delete *cont;
+    *cont = nullptr;
+  }
+}
+
+tblite_container tblite_new_alpb_solvation_solvent(tblite_error error, tblite_structure mol,
+                                                   char* solvent,
+                                                   enum tblite_solvation_param version,
+                                                   enum tblite_ref_solvation_state refstate) {
+  if (!error) return nullptr;
+  if (!mol) {
+    set_err(error, "Molecular structure data is missing");
+    return nullptr;
+  }
+  std::string name = solvent ? solvent : "";
+  for (auto& ch : name) ch = (char)tolower((unsigned char)ch);
+  if (name != "water" && name != "h2o") {
+    set_err(error, "Solvent '" + name + "' is not available: the GPU engine provides water only");
+    return nullptr;
+  }
+  if (version != tblite_solvation_alpb_gfn2) {
+    set_err(error, "Only the ALPB model with GFN2 parameters is available in the GPU engine");
+    return nullptr;
+  }
+  if (refstate < 1 || refstate > 3) {
+    set_err(error, "Unknown reference state for the solvation free energy");
+    return nullptr;
+  }
+  try {
+    auto* cont = new _tblite_container();
+    cont->solv = build_solvation(mol, (int)refstate);
+    return cont;
+  } catch (const std::exception& e) {
+    set_err(error, e.what());
+    return nullptr;
+  }
 }
 
 tblite_calculator tblite_new_gfn2_calculator(tblite_context ctx, tblite_structure mol,

@@ -111,6 +111,29 @@ void d4_energy(const DevMol& m, const DevD4& d, D4Work& w, const double* qat, do
 void d4_gradient(const DevMol& m, const DevD4& d, D4Work& w, const double* qat, double* grad,
                  double* sig_at, cudaStream_t s);
 
+// Implicit solvation (ALPB + CDS + shift), per atom device data + model constants
+constexpr int SOLV_MAXNB = 512;    // surface-grid neighbours per atom
+constexpr int SOLV_NGRID = 230;    // Lebedev points per atom
+constexpr int SOLV_MAXSHELL = 32;  // partners in the smoothing shell of one grid point
+struct DevSolv {
+  int nat;
+  double lrcut, srcut, keps, alpbet, adet, born_scale, ah0, ah1, ah3, shift;
+  const double *vdwr, *rho, *svdw, *vdwsa, *wrp, *trj2_lo, *trj2_hi, *tension, *hbond;
+  const double* grid;  // [230][4]: x, y, z, weight (x 4 pi)
+  double *brad, *dscale, *wbr, *surface;
+  int *nbl, *nnb;
+  int* status;  // 0 ok; 1 neighbour list overflow; 2 smoothing shell overflow
+};
+// Born radii, surface neighbour list, surfaces; adds surface tension + shift energies to eat
+void solv_setup(const DevSolv& v, const double* xyz, double* eat, cudaStream_t s);
+void solv_potential(const DevSolv& v, const double* xyz, const double* qat, double* vat,
+                    cudaStream_t s);
+void solv_energy(const DevSolv& v, const double* xyz, const double* qat, double* eat,
+                 cudaStream_t s);
+// ALPB pair + Born-radius chain rule + surface terms (the shape term is added on the host)
+void solv_gradient(const DevSolv& v, const double* xyz, const double* qat, double* grad,
+                   cudaStream_t s);
+
 // Kernel launchers (defined in the .cu files).  All run on `stream`.
 void launch_cn(const DevMol& m, const Gfn2Scalars& p, double* cn, cudaStream_t s);
 void launch_cn_grad(const DevMol& m, const Gfn2Scalars& p, const double* dEdcn, double* grad,

@@ -177,6 +177,13 @@ class Calculator(Structure):
         raise TBLiteValueError(f"Attribute '{attribute}' is not available in this calculator")
 
     def add(self, interaction: str, *args) -> None:
+        """Add an interaction (reference interface.py:588-637).  Available: ``"alpb-solvation"``
+        with the solvent ``"water"`` and an optional solution state ``"gsolv"`` (default),
+        ``"bar1mol"`` or ``"reference"``."""
+        if interaction == "alpb-solvation":
+            cont = library.new_alpb_solvation(self._mol, *args, version=2)
+            library.calculator_push_back(self._ctx, self._calc, cont)
+            return
         raise TBLiteValueError(f"Interaction '{interaction}' is not available in the GPU engine")
 
     def singlepoint(self, res: Optional[Result] = None, copy: bool = False) -> Result:

@@ -15,7 +15,7 @@ from pathlib import Path
 
 import numpy as np
 
-from .exceptions import TBLiteRuntimeError
+from .exceptions import TBLiteRuntimeError, TBLiteValueError
 
 _LIB = None
 _dbl_p = POINTER(c_double)
@@ -72,6 +72,9 @@ _SIGNATURES = {
     "tblite_get_calculator_orbital_count": (None, [c_void_p, c_void_p, _int_p]),
     "tblite_get_calculator_orbital_map": (None, [c_void_p, c_void_p, _int_p]),
     "tblite_get_singlepoint": (None, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    "tblite_new_alpb_solvation_solvent": (c_void_p, [c_void_p, c_void_p, c_char_p, c_int, c_int]),
+    "tblite_calculator_push_back": (None, [c_void_p, c_void_p, POINTER(c_void_p)]),
+    "tblite_delete_container": (None, [POINTER(c_void_p)]),
     # extensions (include/tblite_gb300_ext.h)
     "tblite_gb300_set_profiling": (None, [c_int]),
     "tblite_gb300_get_profile": (c_int, [_dbl_p, _int_p, c_int, _dbl_p, _int_p]),
@@ -249,3 +252,24 @@ def result_int(res, name):
     getattr(lib, f"tblite_get_result_{name}")(err.h, res, byref(v))
     err.check()
     return v.value
+
+
+SOLUTION_STATES = {"gsolv": 1, "bar1mol": 2, "reference": 3}
+
+
+def new_alpb_solvation(mol, solvent: str, state: str = "gsolv", version: int = 2):
+    """ALPB container for a named solvent (model code 10 + version, as the reference's
+    python/tblite/library.py:889-897 passes it)."""
+    lib = load()
+    if state not in SOLUTION_STATES:
+        raise TBLiteValueError(f"Unknown solution state '{state}'")
+    err = _Error()
+    cont = c_void_p(lib.tblite_new_alpb_solvation_solvent(
+        err.h, mol, solvent.encode("ascii"), 10 + int(version), SOLUTION_STATES[state]))
+    err.check()
+    return cont
+
+
+def calculator_push_back(ctx, calc, cont):
+    load().tblite_calculator_push_back(ctx, calc, byref(cont))
+    context_check(ctx)
