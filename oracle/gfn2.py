@@ -368,7 +368,8 @@ def setup(calc: Calc):
     sc = p["scalars"]
     L.orc_build_h0(ctypes.byref(b), _p(selfenergy), _p(shpoly), _p(calc.sh_zeta), _p(at_en),
                    _p(at_rad), _p(ksh), ctypes.c_double(sc["wexp"]), ctypes.c_double(sc["enscale"]),
-                   ctypes.c_double(intcut), ctypes.c_double(cutoff), _p(S), _p(D), _p(Q), _p(H))
+                   ctypes.c_double(intcut), ctypes.c_double(cutoff), _p(S), _p(D), _p(Q), _p(H),
+                   None)
     # shell hardness and Hubbard derivatives, xtb/gfn2.f90:717-763
     hub = np.array([p["hubbard_parameter"][z[calc.sh_atom[i]] - 1]
                     * p["shell_hubbard"][z[calc.sh_atom[i]] - 1][calc.sh_l[i]] for i in range(nsh)])
@@ -638,7 +639,7 @@ def _gradient(calc, st, gradient, sigma, C, emo, focc, P, qsh, qat, dpat, qpat, 
                       _p(st["ksh"]), ctypes.c_double(sc_["wexp"]), ctypes.c_double(sc_["enscale"]),
                       ctypes.c_double(st["intcut"]), ctypes.c_double(st["cutoff"]), _p(P_c), _p(W),
                       _p(np.ascontiguousarray(vao)), _p(vdp_c), _p(vqp_c), _p(gradient), _p(sigma),
-                      _p(dEdcn))
+                      _p(dEdcn), None)
     cnp = calc.edata["cn"]
     rcov = np.array([_elem(cnp, "rcov", zz) for zz in mol.numbers])
     L.orc_cn_dexp_grad(ctypes.c_int(nat), _p(xyz), _p(rcov), ctypes.c_double(cnp["ka"]),

@@ -322,11 +322,15 @@ int orc_shellpair_size(void) { return (int)(sizeof(shellpair_t) / sizeof(double)
  * hscale[nsh_j][nsh_i] is not materialised: it is rebuilt from per-shell data
  * as in src/tblite/xtb/gfn2.f90:767-797 (get_hscale):
  *   hscale = (2 sqrt(zi zj)/(zi+zj))^wexp * kshell(lj, li) * (1 + enscale (EN_i-EN_j)^2)
- * shpoly[nsh], sh_zeta[nsh], at_en[nat], at_rad[nat], selfenergy[nsh]. */
+ * shpoly[nsh], sh_zeta[nsh], at_en[nat], at_rad[nat], selfenergy[nsh].
+ * hspair[nsh][nsh] (optional): a precomputed shell-pair scale that replaces the GFN2 formula
+ * (GFN1: valence/polarisation shells and element-pair factors, xtb/gfn1.f90:797-828). */
 void orc_build_h0(const basis_t *b, const double *selfenergy, const double *shpoly,
                   const double *sh_zeta, const double *at_en, const double *at_rad,
                   const double *kshell /*[5][5]*/, double wexp, double enscale, double intcut,
-                  double cutoff, double *S, double *D, double *Q, double *H) {
+                  double cutoff, double *S, double *D, double *Q, double *H,
+                  const double *hspair) {
+    const int nshl = b->nsh;
     const int n = b->nao;
     const size_t nn = (size_t)n * n;
     memset(S, 0, nn * sizeof(double));
@@ -355,7 +359,8 @@ void orc_build_h0(const basis_t *b, const double *selfenergy, const double *shpo
                         const double zi = sh_zeta[ish], zj = sh_zeta[jsh];
                         const double zij = pow(2 * sqrt(zi * zj) / (zi + zj), wexp);
                         const double den = (at_en[iat] - at_en[jat]) * (at_en[iat] - at_en[jat]);
-                        const double hs = zij * kshell[cj.l * 5 + ci.l] * (1.0 + enscale * den);
+                        const double hs = hspair ? hspair[(size_t)jsh * nshl + ish]
+                                                 : zij * kshell[cj.l * 5 + ci.l] * (1.0 + enscale * den);
                         const double poly = (1.0 + shpoly[ish] * rr) * (1.0 + shpoly[jsh] * rr);
                         hij = 0.5 * (selfenergy[ish] + selfenergy[jsh]) * hs * poly;
                     } else {
@@ -394,8 +399,8 @@ void orc_h0_gradient(const basis_t *b, const double *selfenergy, const double *d
                      const double *at_rad, const double *kshell, double wexp, double enscale,
                      double intcut, double cutoff, const double *P, const double *W,
                      const double *vao, const double *vdp, const double *vqp, double *gradient,
-                     double *sigma, double *dEdcn) {
-    const int n = b->nao, nat = b->nat;
+                     double *sigma, double *dEdcn, const double *hspair) {
+    const int n = b->nao, nat = b->nat, nshl = b->nsh;
     const double cut2 = cutoff * cutoff;
     double *g_acc = (double *)calloc((size_t)nat * 3, sizeof(double));
     double *c_acc = (double *)calloc((size_t)nat, sizeof(double));
@@ -431,7 +436,8 @@ void orc_h0_gradient(const basis_t *b, const double *selfenergy, const double *d
                         const double zi = sh_zeta[ish], zj = sh_zeta[jsh];
                         const double zij = pow(2 * sqrt(zi * zj) / (zi + zj), wexp);
                         const double den = (at_en[iat] - at_en[jat]) * (at_en[iat] - at_en[jat]);
-                        const double hs = zij * kshell[cj.l * 5 + ci.l] * (1.0 + enscale * den) * poly;
+                        const double hs = (hspair ? hspair[(size_t)jsh * nshl + ish]
+                                                  : zij * kshell[cj.l * 5 + ci.l] * (1.0 + enscale * den)) * poly;
                         const double hij = 0.5 * (selfenergy[ish] + selfenergy[jsh]) * hs;
                         const double dhdcni = dsedcn[ish] * hs, dhdcnj = dsedcn[jsh] * hs;
                         const int io = b->sh_ao[ish], jo = b->sh_ao[jsh];

@@ -215,13 +215,75 @@ def write_inc(params, sto, path: Path):
     path.write_text("".join(lines))
 
 
+def extract_gfn1(root: Path):
+    """GFN1-xTB tables (reference src/tblite/xtb/gfn1.f90:47-496, kshell at :1056-1060)."""
+    d = _declarations((root / "src/tblite/xtb/gfn1.f90").read_text())
+    scalars = ["evtoau", "s6", "s8", "a1", "a2", "s9", "rep_kexp", "rep_rexp", "gexp",
+               "enscale", "kdiff", "halogen_radscale", "halogen_damping"]
+    env = {}
+    sc = evaluate(d, scalars, env)
+    env.update(sc)
+    tables = ["kdiag", "rep_alpha", "rep_zeff", "hubbard_parameter", "shell_hubbard",
+              "p_hubbard_derivs", "nshell", "ang_shell", "principal_quantum_number",
+              "number_of_primitives", "p_shpoly", "reference_occ", "slater_exponent",
+              "p_selfenergy", "p_kcn", "halogen_bond"]
+    tv = evaluate(d, tables, env)
+    max_elem = 86
+    shaped = {"shell_hubbard", "ang_shell", "principal_quantum_number", "number_of_primitives",
+              "p_shpoly", "reference_occ", "slater_exponent", "p_selfenergy", "p_kcn"}
+    out = {"scalars": {k: float(v) for k, v in sc.items()}}
+    for name, val in tv.items():
+        arr = np.asarray(val, dtype=float)
+        if name in shaped:
+            if arr.size != 3 * max_elem:
+                raise ValueError(f"{name}: {arr.size} values")
+            arr = arr.reshape((max_elem, 3))  # [element][slot]
+        out[name] = arr.tolist()
+    kdiag = np.asarray(tv["kdiag"])
+    ksh = np.zeros((3, 3))
+    for k in range(3):
+        for ll in range(3):
+            ksh[k, ll] = 2.08 if (k, ll) in ((0, 1), (1, 0)) else (kdiag[ll] + kdiag[k]) / 2
+    out["kshell"] = ksh.tolist()
+    return out
+
+
+def write_inc_gfn1(params, path: Path):
+    def arr1(name, ctype, vals):
+        body = ", ".join(repr(float(v)) if ctype == "double" else str(int(v)) for v in vals)
+        return f"static const {ctype} {name}[{len(vals)}] = {{{body}}};\n"
+
+    flat = lambda x: np.asarray(x).ravel().tolist()  # noqa: E731
+    lines = ["// Generated by tblite_gb300/data/extract_params.py -- do not edit.\n",
+             "// GFN1-xTB element tables (reference src/tblite/xtb/gfn1.f90:47-496).\n",
+             "#pragma once\n"]
+    for k, v in params["scalars"].items():
+        lines.append(f"static const double GFN1_{k.upper()} = {v!r};\n")
+    for name in ["rep_alpha", "rep_zeff", "hubbard_parameter", "p_hubbard_derivs",
+                 "halogen_bond"]:
+        lines.append(arr1("GFN1_" + name.upper(), "double", flat(params[name])))
+    lines.append("// [Z-1][slot]: slot = shell index (selfenergy, kcn, slater, ang, pqn, ngauss)\n")
+    lines.append("// or angular momentum (shell_hubbard, shpoly, reference_occ)\n")
+    for name in ["shell_hubbard", "p_shpoly", "reference_occ", "slater_exponent",
+                 "p_selfenergy", "p_kcn"]:
+        lines.append(arr1("GFN1_" + name.upper(), "double", flat(params[name])))
+    for name in ["ang_shell", "principal_quantum_number", "number_of_primitives"]:
+        lines.append(arr1("GFN1_" + name.upper(), "int", flat(params[name])))
+    lines.append(arr1("GFN1_NSHELL", "int", flat(params["nshell"])))
+    lines.append(arr1("GFN1_KSHELL", "double", flat(params["kshell"])))
+    path.write_text("".join(lines))
+
+
 def main():
     root = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
     params, sto = extract(root)
     (HERE / "gfn2.json").write_text(json.dumps(params, indent=0))
     (HERE / "sto_ng.json").write_text(json.dumps(sto, indent=0))
     write_inc(params, sto, HERE.parent / "csrc" / "params_gfn2.inc")
-    print("wrote gfn2.json, sto_ng.json, params_gfn2.inc")
+    g1 = extract_gfn1(root)
+    (HERE / "gfn1.json").write_text(json.dumps(g1, indent=0))
+    write_inc_gfn1(g1, HERE.parent / "csrc" / "params_gfn1.inc")
+    print("wrote gfn2.json, sto_ng.json, params_gfn2.inc, gfn1.json, params_gfn1.inc")
 
 
 if __name__ == "__main__":

@@ -1,8 +1,9 @@
 """Compile an element-data pack (JSON) into ``../csrc/element_data.inc``.
 
-The element-data pack carries the per-element numbers that GFN2-xTB takes from
-libraries outside the reference tree: mctc-lib covalent radii, Pauling
-electronegativities, atomic radii and coordination-number constants, and the
+The element-data pack carries the per-element numbers that GFN2-xTB and GFN1-xTB take
+from libraries outside the reference tree: mctc-lib covalent radii, Pauling
+electronegativities, atomic radii and coordination-number constants (double-exponential
+and exponential counting functions), the D3 model constants, and the
 dftd4 model data (reference coordination numbers and charges, Gaussian weight
 counts, reference C6 values, effective charges, hardnesses, <r4>/<r2> ratios).
 Elements absent from the pack are stored as NaN (nref = 0); the library rejects
@@ -74,6 +75,12 @@ def main():
               fmt("EXT_D4_ZEFF", table(d4["zeff"])), fmt("EXT_D4_GAM", table(d4["gam"])),
               fmt("EXT_D4_R4R2", table(d4["r4r2"])), fmt("EXT_D4_RCOV", table(d4["rcov"])),
               fmt("EXT_D4_EN", table(d4["en"]))]
+    cx = pack["cn_exp"]
+    lines += [f"static const double EXT_CNEXP_K = {float(cx['k'])!r};\n",
+              f"static const double EXT_CNEXP_CUTOFF = {float(cx['cutoff'])!r};\n"]
+    d3 = pack["d3"]
+    for key in ("k1", "k3", "cn_cutoff", "disp2_cutoff"):
+        lines.append(f"static const double EXT_D3_{key.upper()} = {float(d3[key])!r};\n")
     (HERE.parent / "csrc" / "element_data.inc").write_text("".join(lines))
     print("wrote element_data.inc from", src.name)
 
