@@ -155,6 +155,10 @@ typedef struct {
 } tblite_xtb_config;
 TBLITE_API_ENTRY tblite_calculator TBLITE_API_CALL
 tblite_new_gfn2_calculator(tblite_context ctx, tblite_structure mol, tblite_xtb_config* config);
+/* GFN1-xTB parametrisation (calculator.h:79-82); elements whose GFN1 parameters carry a
+   halogen-bond correction (Br, I, At) and d-shell elements are rejected */
+TBLITE_API_ENTRY tblite_calculator TBLITE_API_CALL
+tblite_new_gfn1_calculator(tblite_context ctx, tblite_structure mol, tblite_xtb_config* config);
 TBLITE_API_ENTRY void TBLITE_API_CALL tblite_delete_calculator(tblite_calculator* calc);
 TBLITE_API_ENTRY void TBLITE_API_CALL tblite_set_calculator_accuracy(tblite_context ctx,
                                                                     tblite_calculator calc,

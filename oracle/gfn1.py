@@ -30,9 +30,9 @@ from dataclasses import dataclass, field
 import numpy as np
 import scipy.linalg
 
-from oracle.gfn2 import (DATA, KT_300K, MAXG, Broyden, Molecule, _basis_struct, _elem, _p,
-                         entropy, fermi_filling, lib, load_element_data, load_sto,
-                         slater_to_gauss)
+from oracle.gfn2 import (DATA, KT_300K, MAXG, Broyden, Molecule, Result, _basis_struct, _elem,
+                         _p, entropy, fermi_filling, lib, load_element_data, load_sto,
+                         post_processing, slater_to_gauss)
 
 
 def load_params1():
@@ -411,6 +411,14 @@ def singlepoint(calc: Calc1, grad=True, verbose=False):
             print(iscf, float(np.sum(eelec + energies)), float(np.sum(eelec)) - elast, mixer.error())
     energies = energies + eelec
     energy = float(np.sum(energies))
+    # atomic multipoles of the final density (scf/iterator.f90:120-123 runs for every method)
+    dpat = np.zeros((nat, 3))
+    qpat = np.zeros((nat, 6))
+    np.add.at(dpat, ao2at, -np.einsum("krc,rc->ck", st["D"], P))
+    np.add.at(qpat, ao2at, -np.einsum("qrc,rc->cq", st["Q"], P))
+    parts = dict(erep=float(np.sum(erep)), edisp=float(np.sum(edisp)), eelec=float(np.sum(eelec)),
+                 cn=st["cn"], vao=vao)
+    parts.update(post_processing(st["S"], C, fa, fb, P, nalp, nbet, xyz, qat, dpat, qpat, ao2at))
     if grad:
         n = calc.nao
         dEdcn = np.zeros(nat)
@@ -432,8 +440,6 @@ def singlepoint(calc: Calc1, grad=True, verbose=False):
         for i in range(nat):
             for k in range(nat):
                 sigma += dEdcn[i] * np.outer(st["dcn"][i, k], xyz[k])
-    from oracle.gfn2 import Result
-
     return Result(energy=energy, energies=energies, gradient=gradient, sigma=sigma, qsh=qsh,
-                  qat=qat, dpat=np.zeros((nat, 3)), qpat=np.zeros((nat, 6)), density=P, emo=emo,
-                  focc=focc, iterations=iscf, converged=converged, parts={})
+                  qat=qat, dpat=dpat, qpat=qpat, density=P, emo=emo, focc=focc, iterations=iscf,
+                  converged=converged, parts=parts)

@@ -561,8 +561,23 @@ def singlepoint(calc: Calc, grad=True, verbose=False, dispersion=None, solvation
     energy = float(np.sum(energies))
     parts = dict(erep=float(np.sum(erep)), edisp_nonsc=float(np.sum(edisp)),
                  eelec=float(np.sum(eelec)), cn=st["cn"], vao=vao, vdp=vdp, vqp=vqp)
-    # post-processing: bond orders (post_processing/wbo.f90:60-115 ->
-    # wavefunction/mulliken.f90:176-235) and molecular moments (mulliken.f90:133-172)
+    parts.update(post_processing(st["S"], C, fa, fb, P, nalp, nbet, xyz, qat, dpat, qpat, ao2at))
+    if grad:
+        gradient, sigma = _gradient(calc, st, gradient, sigma, C, emo, focc, P, qsh, qat, dpat,
+                                    qpat, vao, vdp, vqp, disp)
+        if solv is not None:
+            gradient += solv.gradient(qat)
+    return Result(energy=energy, energies=energies, gradient=gradient, sigma=sigma, qsh=qsh,
+                  qat=qat, dpat=dpat, qpat=qpat, density=P, emo=emo, focc=focc, iterations=iscf,
+                  converged=converged, parts=parts)
+
+
+
+def post_processing(S, C, fa, fb, P, nalp, nbet, xyz, qat, dpat, qpat, ao2at):
+    """Wiberg/Mayer bond orders (post_processing/wbo.f90:60-115 ->
+    wavefunction/mulliken.f90:176-235) and molecular moments (mulliken.f90:133-172)."""
+    nat = len(qat)
+    parts = {}
     if nalp != nbet:
         spin_p = [(C * fa) @ C.T, (C * fb) @ C.T]
         scale = 2.0
@@ -571,7 +586,7 @@ def singlepoint(calc: Calc, grad=True, verbose=False, dispersion=None, solvation
         scale = 1.0
     wbo = np.zeros((len(spin_p), nat, nat))
     for s_, Ps in enumerate(spin_p):
-        PS_ = Ps @ st["S"]
+        PS_ = Ps @ S
         prod = PS_ * PS_.T
         for a in range(nat):
             for b in range(nat):
@@ -595,14 +610,7 @@ def singlepoint(calc: Calc, grad=True, verbose=False, dispersion=None, solvation
                       1.5 * c[5] - tr])
         quad += qpat[a] + c
     parts["quadrupole"] = quad
-    if grad:
-        gradient, sigma = _gradient(calc, st, gradient, sigma, C, emo, focc, P, qsh, qat, dpat,
-                                    qpat, vao, vdp, vqp, disp)
-        if solv is not None:
-            gradient += solv.gradient(qat)
-    return Result(energy=energy, energies=energies, gradient=gradient, sigma=sigma, qsh=qsh,
-                  qat=qat, dpat=dpat, qpat=qpat, density=P, emo=emo, focc=focc, iterations=iscf,
-                  converged=converged, parts=parts)
+    return parts
 
 
 def _gradient(calc, st, gradient, sigma, C, emo, focc, P, qsh, qat, dpat, qpat, vao, vdp, vqp, disp):

@@ -85,7 +85,7 @@ def _function():
             set_shell_parameters(
                 calc, **{k: t.detach().to("cpu", torch.float64).numpy()
                          for k, t in zip(PARAMETERS, (selfenergy, kcn, hubbard, hubbard_deriv))})
-            library.load().tblite_gb300_set_calculator_parameter_gradient(calc._ctx, calc._calc, 1)
+            library.set_parameter_gradient(calc._ctx, calc._calc)
             res = calc.singlepoint()
             nsh = selfenergy.numel()
             pg = parameter_gradient(res, nsh)

@@ -105,6 +105,9 @@ struct Workspace {
   // gradient
   DBuf<double> grad, sigma, sig_at, dEdcn;
   DBuf<double> wbo, ones, pgrad;
+  // GFN1 per-shell/atom data and D3 dispersion (data and work)
+  DBuf<int> sh_valence, d3_nref;
+  DBuf<double> at_gam3, d3_refcn, d3_sref, d3_r4r2, d3_rcov, d3_cn, d3_a, d3_da, d3_dEdcn;
   // implicit solvation: per-atom model arrays [9][nat], grid [230][4], work [4][nat]
   DBuf<double> sv_atom, sv_grid, sv_work;
   DBuf<int> sv_nbl, sv_nnb, sv_status;
@@ -138,6 +141,14 @@ struct _tblite_calculator {
   // molecule-bound basis (built at construction)
   int nat = 0, nsh = 0, nao = 0;
   std::vector<int> at_z, at_sh, sh_atom, sh_l, sh_nprim, sh_ao, ao_sh, ao_at;
+  // method: 2 GFN2-xTB, 1 GFN1-xTB
+  int method = 2;
+  std::vector<int> sh_valence;   // GFN1: first shell of its angular momentum on the atom
+  std::vector<double> at_gam3;   // GFN1: atom-resolved third-order hardness derivative
+  // D3 data per atom (GFN1, molecules with pairs)
+  bool has_d3 = false;
+  std::vector<int> d3_nref;
+  std::vector<double> d3_refcn, d3_sref, d3_r4r2, d3_rcov;
   // D4 data per atom (empty for a single atom: no pairs, no dispersion)
   bool has_d4 = false;
   int d4_nsp = 0;

@@ -310,6 +310,8 @@ MolPtrs make_ptrs(const Plan& pl, const Bases& db) {
     w.dEdcn = db.at<double>(pl.d4_dEdcn);
   }
   q.nd = pl.nd;
+  q.with_mp = 1;  // GFN2-xTB: the atomic multipoles are mixed with the shell charges
+  q.has_d3 = 0;
   q.mull_chunks = mulliken_chunks(pl.nao);
   q.memory = std::min(pl.memory, HCAP);
   q.nalp = pl.nalp;
@@ -793,8 +795,9 @@ extern "C" int tblite_gb300_batch_singlepoint(tblite_context ctx, int nmol,
       continue;
     }
     const bool anneal = c->anneal && c->anneal_kt > c->etemp;
-    // implicit solvation and the parameter gradient run on the one-molecule path
-    if (pl.nao > tri_max || anneal || pl.max_iter < 1 || c->solv || c->param_grad) {
+    // implicit solvation, the parameter gradient and GFN1-xTB run on the one-molecule path
+    if (pl.nao > tri_max || anneal || pl.max_iter < 1 || c->solv || c->param_grad ||
+        c->method != 2) {
       plain.push_back(i);
       continue;
     }

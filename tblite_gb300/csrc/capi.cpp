@@ -17,6 +17,7 @@
 #include "../../include/tblite_gb300_ext.h"
 #include "element_data.inc"
 #include "engine.h"
+#include "params_gfn1.inc"
 #include "params_gfn2.inc"
 #include "params_solv.inc"
 
@@ -95,6 +96,7 @@ static void build_calculator(_tblite_calculator* c, const _tblite_structure* mol
       c->sh_hub.push_back(GFN2_HUBBARD_PARAMETER[z - 1] * GFN2_SHELL_HUBBARD[(z - 1) * 3 + l]);
       c->sh_gam3.push_back(GFN2_P_HUBBARD_DERIVS[z - 1] * GFN2_SHELL_HUBBARD_DERIVS[l]);
       c->sh_refocc.push_back(GFN2_REFERENCE_OCC[(z - 1) * 3 + l]);
+      c->sh_valence.push_back(1);
       for (int m = 0; m < 2 * l + 1; ++m) {
         c->ao_sh.push_back(c->nsh);
         c->ao_at.push_back(i);
@@ -118,6 +120,7 @@ static void build_calculator(_tblite_calculator* c, const _tblite_structure* mol
     c->at_qkern.push_back(GFN2_P_QKERNEL[z - 1]);
     c->at_repa.push_back(GFN2_REP_ALPHA[z - 1]);
     c->at_repz.push_back(GFN2_REP_ZEFF[z - 1]);
+    c->at_gam3.push_back(0.0);
   }
   // D4 model data (element-data pack), only for molecules with pairs
   if (mol->nat > 1) {
@@ -157,8 +160,150 @@ static void build_calculator(_tblite_calculator* c, const _tblite_structure* mol
   }
 }
 
+// --------------------------------------------------------------------------------------
+// GFN1-xTB calculator data (reference xtb/gfn1.f90:556-905): basis with the second s shell
+// of hydrogen orthogonalised to the first (basis/ortho.f90:33-72), per-shell levels and CN
+// shifts, valence flags, harmonic-mean hardness, atom-resolved third order, D3 data.
+// --------------------------------------------------------------------------------------
+static void orthogonalize_s(int ni, const double* ai, const double* ci, int& nj, double* aj,
+                            double* cj) {
+  double ov = 0.0;
+  for (int p = 0; p < ni; ++p)
+    for (int q = 0; q < nj; ++q) ov += ci[p] * cj[q] * pow(sqrt(M_PI / (ai[p] + aj[q])), 3);
+  for (int p = 0; p < ni; ++p) {
+    aj[nj + p] = ai[p];
+    cj[nj + p] = -ov * ci[p];
+  }
+  nj += ni;
+  double norm = 0.0;
+  for (int p = 0; p < nj; ++p)
+    for (int q = 0; q < nj; ++q) norm += cj[p] * cj[q] * pow(sqrt(M_PI / (aj[p] + aj[q])), 3);
+  const double sc = 1.0 / sqrt(norm);
+  for (int p = 0; p < nj; ++p) cj[p] *= sc;
+}
+
+static void build_calculator_gfn1(_tblite_calculator* c, const _tblite_structure* mol) {
+  c->method = 1;
+  c->nat = mol->nat;
+  c->at_z = mol->num;
+  c->at_sh.assign(1, 0);
+  c->nsh = 0;
+  c->nao = 0;
+  for (int i = 0; i < mol->nat; ++i) {
+    const int z = mol->num[i];
+    if (z < 1 || z > 86) throw std::runtime_error("No support for elements with Z > 86.");
+    if (GFN1_HALOGEN_BOND[z - 1] > 0.0)
+      throw std::runtime_error("element Z=" + std::to_string(z) +
+                               " needs the GFN1 halogen-bond correction, which the GPU engine "
+                               "does not provide");
+    const int ns = GFN1_NSHELL[z - 1];
+    double a[3][MAXG] = {{0}}, cc[3][MAXG] = {{0}};
+    int np[3] = {0, 0, 0}, first[3] = {-1, -1, -1}, lsh[3] = {0, 0, 0};
+    bool val[3] = {false, false, false};
+    for (int s = 0; s < ns; ++s) {
+      const int l = GFN1_ANG_SHELL[(z - 1) * 3 + s];
+      if (l > 1)
+        throw std::runtime_error("element Z=" + std::to_string(z) +
+                                 " has d shells, which the CUDA integral kernels do not handle yet");
+      lsh[s] = l;
+      np[s] = GFN1_NUMBER_OF_PRIMITIVES[(z - 1) * 3 + s];
+      slater_to_gauss(np[s], GFN1_PRINCIPAL_QUANTUM_NUMBER[(z - 1) * 3 + s], l,
+                      GFN1_SLATER_EXPONENT[(z - 1) * 3 + s], a[s], cc[s]);
+      val[s] = first[l] < 0;
+      if (val[s]) first[l] = s;
+    }
+    for (int s = 0; s < ns; ++s)
+      if (!val[s]) {
+        const int r = first[lsh[s]];
+        if (np[s] + np[r] > MAXG) throw std::runtime_error("too many primitives");
+        orthogonalize_s(np[r], a[r], cc[r], np[s], a[s], cc[s]);
+      }
+    for (int s = 0; s < ns; ++s) {
+      const int l = lsh[s];
+      for (int k = 0; k < MAXG; ++k) {
+        c->sh_alpha.push_back(a[s][k]);
+        c->sh_coeff.push_back(cc[s][k]);
+        if (k < np[s]) c->min_alpha = std::min(c->min_alpha, a[s][k]);
+      }
+      c->sh_atom.push_back(i);
+      c->sh_l.push_back(l);
+      c->sh_nprim.push_back(np[s]);
+      c->sh_ao.push_back(c->nao);
+      c->sh_zeta.push_back(GFN1_SLATER_EXPONENT[(z - 1) * 3 + s]);
+      c->sh_se0.push_back(GFN1_P_SELFENERGY[(z - 1) * 3 + s]);
+      c->sh_kcn.push_back(GFN1_P_KCN[(z - 1) * 3 + s]);
+      c->sh_shpoly.push_back(GFN1_P_SHPOLY[(z - 1) * 3 + l]);
+      c->sh_hub.push_back(GFN1_HUBBARD_PARAMETER[z - 1] * GFN1_SHELL_HUBBARD[(z - 1) * 3 + l]);
+      c->sh_gam3.push_back(0.0);
+      c->sh_refocc.push_back(val[s] ? GFN1_REFERENCE_OCC[(z - 1) * 3 + l] : 0.0);
+      c->sh_valence.push_back(val[s] ? 1 : 0);
+      for (int m = 0; m < 2 * l + 1; ++m) {
+        c->ao_sh.push_back(c->nsh);
+        c->ao_at.push_back(i);
+      }
+      c->nao += 2 * l + 1;
+      c->nsh += 1;
+    }
+    c->at_sh.push_back(c->nsh);
+    const bool need = mol->nat > 1;
+    const double en = EXT_EN[z - 1], rad = EXT_RAD[z - 1], rcov = EXT_RCOV[z - 1];
+    if (need && (std::isnan(en) || std::isnan(rad) || std::isnan(rcov)))
+      throw std::runtime_error(std::string("element data pack '") + EXT_PACK_NAME +
+                               "' has no entry for Z=" + std::to_string(z));
+    c->at_en.push_back(need ? en : 0.0);
+    c->at_rad.push_back(need ? rad : 1.0);
+    c->at_rcov.push_back(need ? rcov : 1.0);
+    c->at_mprad.push_back(1.0);  // no anisotropic electrostatics in GFN1
+    c->at_vcn.push_back(0.0);
+    c->at_dkern.push_back(0.0);
+    c->at_qkern.push_back(0.0);
+    c->at_repa.push_back(GFN1_REP_ALPHA[z - 1]);
+    c->at_repz.push_back(GFN1_REP_ZEFF[z - 1]);
+    c->at_gam3.push_back(GFN1_P_HUBBARD_DERIVS[z - 1]);
+  }
+  if (mol->nat > 1) {  // D3 data (element-data pack)
+    c->has_d3 = true;
+    for (int i = 0; i < mol->nat; ++i) {
+      const int z = mol->num[i];
+      if (EXT_D4_NREF[z - 1] <= 0 || std::isnan(EXT_D4_R4R2[z - 1]) || std::isnan(EXT_D4_RCOV[z - 1]))
+        throw std::runtime_error(std::string("element data pack '") + EXT_PACK_NAME +
+                                 "' has no D3 data for Z=" + std::to_string(z));
+      c->d3_nref.push_back(EXT_D4_NREF[z - 1]);
+      for (int r = 0; r < D4_MREF; ++r) {
+        c->d3_refcn.push_back(EXT_D4_REFCN[(z - 1) * D4_MREF + r]);
+        c->d3_sref.push_back(sqrt(EXT_D4_REFC6[(z - 1) * D4_MREF + r]));
+      }
+      c->d3_r4r2.push_back(EXT_D4_R4R2[z - 1]);
+      c->d3_rcov.push_back(EXT_D4_RCOV[z - 1]);
+    }
+  }
+}
+
 Gfn2Scalars gfn2_scalars(const _tblite_calculator* c) {
+  if (c->method == 1) {
+    Gfn2Scalars p{};
+    p.method = 1;
+    p.wexp = 0.0;
+    p.enscale = GFN1_ENSCALE;
+    p.gexp = GFN1_GEXP;
+    for (int a = 0; a < 5; ++a)
+      for (int b = 0; b < 5; ++b) p.kshell[a][b] = (a < 3 && b < 3) ? GFN1_KSHELL[a * 3 + b] : 0.0;
+    p.kdiff = GFN1_KDIFF;
+    p.harmonic = 1;
+    p.third_atom = 1;
+    p.aes = 0;
+    p.rep_kexp = GFN1_REP_KEXP;
+    p.rep_kexp_light = GFN1_REP_KEXP;
+    p.rep_rexp = GFN1_REP_REXP;
+    p.rep_cutoff = 25.0;
+    p.cn_exp_k = EXT_CNEXP_K;
+    p.cn_cutoff = EXT_CNEXP_CUTOFF;
+    p.h0_cutoff = std::min(sqrt(2.0 * INTCUT / c->min_alpha), 40.0);
+    return p;
+  }
   Gfn2Scalars p{};
+  p.method = 2;
+  p.aes = 1;
   p.wexp = GFN2_WEXP;
   p.enscale = GFN2_ENSCALE;
   p.gexp = GFN2_GEXP;
@@ -220,6 +365,16 @@ static void ensure_workspace(_tblite_calculator* c) {
     w.at_qkern.upload(c->at_qkern, s);
     w.at_repa.upload(c->at_repa, s);
     w.at_repz.upload(c->at_repz, s);
+    w.sh_valence.upload(c->sh_valence, s);
+    w.at_gam3.upload(c->at_gam3, s);
+    if (c->has_d3) {
+      w.d3_nref.upload(c->d3_nref, s);
+      w.d3_refcn.upload(c->d3_refcn, s);
+      w.d3_sref.upload(c->d3_sref, s);
+      w.d3_r4r2.upload(c->d3_r4r2, s);
+      w.d3_rcov.upload(c->d3_rcov, s);
+      for (auto* b : {&w.d3_cn, &w.d3_a, &w.d3_da, &w.d3_dEdcn}) b->alloc(c->nat);
+    }
     if (c->has_d4) {
       w.d4_sp.upload(c->d4_sp, s);
       w.d4_nref.upload(c->d4_nref, s);
@@ -439,7 +594,32 @@ static DevMol dev_mol(const _tblite_calculator* c) {
   m.at_qkern = w.at_qkern.p;
   m.at_repa = w.at_repa.p;
   m.at_repz = w.at_repz.p;
+  m.sh_valence = w.sh_valence.p;
+  m.at_gam3 = w.at_gam3.p;
   return m;
+}
+
+static DevD3 dev_d3(const _tblite_calculator* c) {
+  const Workspace& w = *c->ws;
+  DevD3 d{};
+  d.nref = w.d3_nref.p;
+  d.refcn = w.d3_refcn.p;
+  d.sref = w.d3_sref.p;
+  d.r4r2 = w.d3_r4r2.p;
+  d.rcov = w.d3_rcov.p;
+  d.k1 = EXT_D3_K1;
+  d.k3 = EXT_D3_K3;
+  d.cn_cutoff = EXT_D3_CN_CUTOFF;
+  d.cutoff = EXT_D3_DISP2_CUTOFF;
+  d.s6 = GFN1_S6;
+  d.s8 = GFN1_S8;
+  d.a1 = GFN1_A1;
+  d.a2 = GFN1_A2;
+  d.cn = w.d3_cn.p;
+  d.a = w.d3_a.p;
+  d.da = w.d3_da.p;
+  d.dEdcn = w.d3_dEdcn.p;
+  return d;
 }
 
 // --------------------------------------------------------------------------------------
@@ -572,8 +752,11 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
   Workspace& w = *c->ws;
   cudaStream_t s = w.stream;
   const int nat = c->nat, nsh = c->nsh, n = c->nao;
-  const size_t nd = nsh + 9 * (size_t)nat;
   const Gfn2Scalars p = gfn2_scalars(c);
+  // mixed quantities: shell charges, plus the atomic multipoles where they enter the
+  // Hamiltonian (GFN2 anisotropic electrostatics)
+  const bool with_mp = p.aes != 0;
+  const size_t nd = nsh + (with_mp ? 9 * (size_t)nat : 0);
   cuda_check(cudaMemcpyAsync(w.xyz.p, mol->xyz.data(), sizeof(double) * 3 * nat,
                              cudaMemcpyHostToDevice, s),
              "xyz");
@@ -595,6 +778,7 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
   D4Work d4w{};
   DevD4 d4 = c->has_d4 ? dev_d4(c, d4w) : DevD4{};
   if (c->has_d4) d4_setup(m, d4, d4w, true, w.grad.p, w.sig_at.p, s);
+  if (c->has_d3) d3_energy_gradient(m, dev_d3(c), true, w.erep.p, w.grad.p, w.sig_at.p, s);
   // implicit solvation: Born radii, surfaces, geometry-only energies into erep
   DevSolv dsolv{};
   if (c->solv) {
@@ -683,7 +867,7 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
       cuda_check(cudaMemcpyAsync(&st, w.b_status.p, sizeof(int), cudaMemcpyDeviceToHost, s), "st");
       stream_wait(s);
       if (st != 0) throw std::runtime_error("Broyden mixing failed to obtain next iteration");
-      launch_unpack(m, w.b_q.p, w.qsh.p, w.qat.p, w.dpat.p, w.qpat.p, s);
+      launch_unpack(m, w.b_q.p, w.qsh.p, w.qat.p, w.dpat.p, w.qpat.p, s, with_mp);
       g_prof.end(s);
     }
     ++iscf;
@@ -695,8 +879,9 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
     launch_vao(m, w.vsh.p, w.vat.p, w.vao.p, s);
     g_prof.end(s);
     g_prof.begin(PH_FOCK, s);
-    launch_fock(n, w.ao_at.p, w.H.p, w.S.p, w.D.p, w.Q.p, w.vao.p, w.vdp.p, w.vqp.p, w.F.p, s);
-    launch_pack(m, w.qsh.p, w.dpat.p, w.qpat.p, w.b_q.p, s);  // mixer%set
+    launch_fock(n, w.ao_at.p, w.H.p, w.S.p, with_mp ? w.D.p : nullptr, w.Q.p, w.vao.p, w.vdp.p,
+                w.vqp.p, w.F.p, s);
+    launch_pack(m, w.qsh.p, w.dpat.p, w.qpat.p, w.b_q.p, s, with_mp);  // mixer%set
     g_prof.end(s);
     g_prof.begin(PH_EIGEN, s);
     const int info = eigen_values(w.eig, w.F.p, w.emo.p);
@@ -714,7 +899,7 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
     g_prof.begin(PH_MULLIKEN, s);
     launch_mulliken(m, w.P.p, w.S.p, w.H.p, w.D.p, w.Q.p, w.mull.p, mulliken_chunks(n), w.qsh_o.p,
                     w.qat_o.p, w.dpat_o.p, w.qpat_o.p, w.eband.p, s);
-    launch_pack(m, w.qsh_o.p, w.dpat_o.p, w.qpat_o.p, w.vec_out.p, s);
+    launch_pack(m, w.qsh_o.p, w.dpat_o.p, w.qpat_o.p, w.vec_out.p, s, with_mp);
     launch_diff((int)nd, w.vec_out.p, w.b_q.p, w.b_dq.p, w.scal.p + 1, s);  // mixer%diff
     launch_eelec_init(nat, w.scal.p, w.eband.p, w.eelec.p, s);
     launch_coulomb_energy(m, p, w.mrad.p, w.qsh_o.p, w.qat_o.p, w.dpat_o.p, w.qpat_o.p, w.eelec.p,
@@ -1104,6 +1289,10 @@ void tblite_gb300_set_calculator_parameter_gradient(tblite_context ctx, tblite_c
     ctx->push("Calculator object is missing");
     return;
   }
+  if (enable && calc->method != 2) {
+    ctx->push("parameter gradients are available for GFN2-xTB calculators only");
+    return;
+  }
   calc->param_grad = enable != 0;
 }
 
@@ -1450,6 +1639,24 @@ tblite_calculator tblite_new_gfn2_calculator(tblite_context ctx, tblite_structur
   auto* c = new _tblite_calculator();
   try {
     build_calculator(c, mol);
+  } catch (const std::exception& e) {
+    ctx->push(e.what());
+    delete c;
+    return nullptr;
+  }
+  return c;
+}
+tblite_calculator tblite_new_gfn1_calculator(tblite_context ctx, tblite_structure mol,
+                                            tblite_xtb_config* config) {
+  (void)config;
+  if (!ctx) return nullptr;
+  if (!mol) {
+    ctx->push("Molecular structure data is missing");
+    return nullptr;
+  }
+  auto* c = new _tblite_calculator();
+  try {
+    build_calculator_gfn1(c, mol);
   } catch (const std::exception& e) {
     ctx->push(e.what());
     delete c;

@@ -412,6 +412,146 @@ void d4_gradient(const DevMol& m, const DevD4& d, D4Work& w, const double* qat, 
 }
 
 // ------------------------------------------------------------------------------------
+// D3(BJ) two-body dispersion of GFN1-xTB (reference src/tblite/disp/d3.f90, which calls
+// s-dftd3 with s9 = 0): exponential coordination number over the D3 covalent radii,
+// Gaussian reference weights in CN, C6_ij = a_i a_j with a_i = sum_r w_ir sqrt(C6_r) / sum_r w_ir,
+// rational (BJ) damping.  Three kernels, one warp per atom each, every atom summing its own
+// share of each pair (deterministic, no atomics):
+//   setup:  CN_i, a_i, da_i/dCN_i
+//   pair:   E_i += 1/2 sum_j E_ij, the explicit pair gradient, dE/dCN_i
+//   cn:     CN chain rule  grad_i += sum_j (dE/dCN_i + dE/dCN_j) dc_ij/dr (R_i - R_j)/r
+// ------------------------------------------------------------------------------------
+__device__ __forceinline__ void d3_count(double r, double r0, double k1, double& c, double& dc) {
+  const double e = exp(-k1 * (r0 / r - 1.0));
+  c = 1.0 / (1.0 + e);
+  dc = -c * c * e * k1 * r0 / (r * r);
+}
+
+__global__ void k_d3_setup(DevMol m, DevD3 d) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= m.nat) return;
+  const int i = warp;
+  const double cut2 = d.cn_cutoff * d.cn_cutoff;
+  double acc = 0.0;
+  for (int j = lane; j < m.nat; j += 32) {
+    if (j == i) continue;
+    double r2 = 0.0;
+    for (int k = 0; k < 3; ++k) {
+      const double t = m.xyz[3 * i + k] - m.xyz[3 * j + k];
+      r2 += t * t;
+    }
+    if (r2 > cut2 || r2 < 1e-12) continue;
+    double c, dc;
+    d3_count(sqrt(r2), d.rcov[i] + d.rcov[j], d.k1, c, dc);
+    acc += c;
+  }
+  acc = wsum(acc);
+  if (lane != 0) return;
+  d.cn[i] = acc;
+  double norm = 0.0, dnorm = 0.0, ws = 0.0, dws = 0.0;
+  for (int r = 0; r < d.nref[i]; ++r) {
+    const double t = acc - d.refcn[i * D4_MREF + r];
+    const double w = exp(-d.k3 * t * t), dw = -2.0 * d.k3 * t * w;
+    const double sr = d.sref[i * D4_MREF + r];
+    norm += w;
+    dnorm += dw;
+    ws += w * sr;
+    dws += dw * sr;
+  }
+  d.a[i] = ws / norm;
+  d.da[i] = (dws * norm - ws * dnorm) / (norm * norm);
+}
+
+__global__ void k_d3_pair(DevMol m, DevD3 d, int grad, double* eat, double* grad_out,
+                          double* sig_at) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= m.nat) return;
+  const int i = warp;
+  const double cut2 = d.cutoff * d.cutoff;
+  const double ai = d.a[i], dai = d.da[i], ri = d.r4r2[i];
+  double e = 0.0, dcn = 0.0, g[3] = {0, 0, 0}, sg[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  for (int j = lane; j < m.nat; j += 32) {
+    if (j == i) continue;
+    double v[3], r2 = 0.0;
+    for (int k = 0; k < 3; ++k) {
+      v[k] = m.xyz[3 * i + k] - m.xyz[3 * j + k];
+      r2 += v[k] * v[k];
+    }
+    if (r2 > cut2) continue;
+    const double r = sqrt(r2);
+    const double qq = 3.0 * ri * d.r4r2[j];
+    const double r0 = d.a1 * sqrt(qq) + d.a2;
+    const double r02 = r0 * r0, r06 = r02 * r02 * r02, r08 = r06 * r02;
+    const double r6 = r2 * r2 * r2, r8 = r6 * r2;
+    const double t6 = 1.0 / (r6 + r06), t8 = 1.0 / (r8 + r08);
+    const double c6 = ai * d.a[j];
+    const double dedc6 = -(d.s6 * t6 + d.s8 * qq * t8);
+    e += 0.5 * dedc6 * c6;
+    if (grad) {
+      const double de = c6 * (d.s6 * 6.0 * r6 / r * t6 * t6 + d.s8 * qq * 8.0 * r8 / r * t8 * t8);
+      const double f = de / r;
+      for (int k = 0; k < 3; ++k) g[k] += f * v[k];
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) sg[3 * a + b] += 0.5 * f * v[a] * v[b];
+      dcn += dedc6 * dai * d.a[j];
+    }
+  }
+  e = wsum(e);
+  if (grad) {
+    dcn = wsum(dcn);
+    for (int k = 0; k < 3; ++k) g[k] = wsum(g[k]);
+    for (int k = 0; k < 9; ++k) sg[k] = wsum(sg[k]);
+  }
+  if (lane != 0) return;
+  eat[i] += e;
+  if (!grad) return;
+  d.dEdcn[i] = dcn;
+  for (int k = 0; k < 3; ++k) grad_out[3 * i + k] += g[k];
+  for (int k = 0; k < 9; ++k) sig_at[9 * i + k] += sg[k];
+}
+
+__global__ void k_d3_cn_grad(DevMol m, DevD3 d, double* grad, double* sig_at) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= m.nat) return;
+  const int i = warp;
+  const double cut2 = d.cn_cutoff * d.cn_cutoff;
+  double g[3] = {0, 0, 0}, sg[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  for (int j = lane; j < m.nat; j += 32) {
+    if (j == i) continue;
+    double v[3], r2 = 0.0;
+    for (int k = 0; k < 3; ++k) {
+      v[k] = m.xyz[3 * i + k] - m.xyz[3 * j + k];
+      r2 += v[k] * v[k];
+    }
+    if (r2 > cut2 || r2 < 1e-12) continue;
+    const double r = sqrt(r2);
+    double c, dc;
+    d3_count(r, d.rcov[i] + d.rcov[j], d.k1, c, dc);
+    const double f = (d.dEdcn[i] + d.dEdcn[j]) * dc / r;
+    for (int k = 0; k < 3; ++k) g[k] += f * v[k];
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) sg[3 * a + b] += 0.5 * f * v[a] * v[b];
+  }
+  for (int k = 0; k < 3; ++k) g[k] = wsum(g[k]);
+  for (int k = 0; k < 9; ++k) sg[k] = wsum(sg[k]);
+  if (lane == 0) {
+    for (int k = 0; k < 3; ++k) grad[3 * i + k] += g[k];
+    for (int k = 0; k < 9; ++k) sig_at[9 * i + k] += sg[k];
+  }
+}
+
+void d3_energy_gradient(const DevMol& m, const DevD3& d, bool grad, double* eat, double* grad_out,
+                        double* sig_at, cudaStream_t s) {
+  ++g_kernel_launches;
+  k_d3_setup<<<warps_grid(m.nat), 64, 0, s>>>(m, d);
+  ++g_kernel_launches;
+  k_d3_pair<<<warps_grid(m.nat), 64, 0, s>>>(m, d, grad ? 1 : 0, eat, grad_out, sig_at);
+  if (!grad) return;
+  ++g_kernel_launches;
+  k_d3_cn_grad<<<warps_grid(m.nat), 64, 0, s>>>(m, d, grad_out, sig_at);
+}
+
+// ------------------------------------------------------------------------------------
 // batched launches: blockIdx.z walks the listed molecules (molecules without dispersion,
 // i.e. single atoms, leave at once); the D4 dEdcn accumulators start zeroed
 // ------------------------------------------------------------------------------------

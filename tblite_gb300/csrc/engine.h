@@ -67,9 +67,18 @@ struct DevMol {
   const double* at_qkern;  // AES quadrupole kernel
   const double* at_repa;   // repulsion alpha
   const double* at_repz;   // repulsion zeff
+  const int* sh_valence;   // GFN1: 1 for the first shell of its angular momentum on the atom
+  const double* at_gam3;   // GFN1: atom-resolved third-order hardness derivative
 };
 
+// method constants of the tight-binding Hamiltonian (GFN2-xTB, or GFN1-xTB with method = 1)
 struct Gfn2Scalars {
+  int method;      // 2 GFN2-xTB, 1 GFN1-xTB
+  int harmonic;    // hardness average of shell pairs: 0 arithmetic (GFN2), 1 harmonic (GFN1)
+  int third_atom;  // third order on atomic charges (GFN1) instead of shell charges (GFN2)
+  int aes;         // anisotropic electrostatics (GFN2 only)
+  double kdiff;    // GFN1 H0 scale involving polarisation shells
+  double cn_exp_k; // GFN1 coordination number: exponential counting steepness
   double wexp, enscale, gexp;
   double kshell[5][5];
   double mp_dmp3, mp_dmp5, mp_shift, mp_kexp, mp_rmax;
@@ -110,6 +119,21 @@ void d4_energy(const DevMol& m, const DevD4& d, D4Work& w, const double* qat, do
 // two-body gradient at the final charges + the D4 CN chain rule (uses w.dEdcn from setup)
 void d4_gradient(const DevMol& m, const DevD4& d, D4Work& w, const double* qat, double* grad,
                  double* sig_at, cudaStream_t s);
+
+// D3(BJ) two-body dispersion of GFN1-xTB (no three-body term): per atom data, model
+// constants and scratch (device pointers)
+struct DevD3 {
+  const int* nref;      // [nat]
+  const double* refcn;  // [nat][D4_MREF]
+  const double* sref;   // [nat][D4_MREF] square roots of the reference C6
+  const double* r4r2;   // [nat]
+  const double* rcov;   // [nat]
+  double k1, k3, cn_cutoff, cutoff, s6, s8, a1, a2;
+  double *cn, *a, *da, *dEdcn;  // [nat] scratch
+};
+// energy (added to eat) and, with grad, gradient and per-atom virial partials
+void d3_energy_gradient(const DevMol& m, const DevD3& d, bool grad, double* eat, double* grad_out,
+                        double* sig_at, cudaStream_t s);
 
 // Implicit solvation (ALPB + CDS + shift), per atom device data + model constants
 constexpr int SOLV_MAXNB = 512;    // surface-grid neighbours per atom
@@ -185,10 +209,11 @@ struct BroydenState {
   int* status;    // device status word (0 ok, !=0 singular)
 };
 void launch_broyden_next(BroydenState& b, cudaStream_t s);
+// with_mp: the mixer vector holds the atomic multipoles too (GFN2); GFN1 mixes shell charges
 void launch_pack(const DevMol& m, const double* qsh, const double* dpat, const double* qpat,
-                 double* vec, cudaStream_t s);
+                 double* vec, cudaStream_t s, bool with_mp = true);
 void launch_unpack(const DevMol& m, const double* vec, double* qsh, double* qat, double* dpat,
-                   double* qpat, cudaStream_t s);
+                   double* qpat, cudaStream_t s, bool with_mp = true);
 // dq = vec_out - q ; err2 = sum(dq^2)/ndim (into *err)
 void launch_diff(int ndim, const double* vec_out, const double* q, double* dq, double* err,
                  cudaStream_t s);
@@ -240,7 +265,7 @@ struct MolPtrs {
   DevMol m;
   DevD4 d4;
   D4Work d4w;
-  int has_d4, nd, mull_chunks, memory;
+  int has_d4, nd, mull_chunks, memory, with_mp, has_d3;
   double nalp, nbet, kt, damp, econv, pconv;
   double h0_cutoff;  // depends on the basis of the molecule (smallest exponent)
   double *cn, *se, *mrad, *dmrdcn;

@@ -44,6 +44,11 @@ __device__ __forceinline__ double powe(double x, double e) {
   return pow(x, e);
 }
 
+// average hardness of a shell pair: arithmetic (GFN2) or harmonic (GFN1) mean
+__device__ __forceinline__ double eta_avg(double a, double b, int harmonic) {
+  return harmonic ? 2.0 / (1.0 / a + 1.0 / b) : 0.5 * (a + b);
+}
+
 // isotropic kernel 1/(r^g + eta^-g)^(1/g); g = 2 is the GFN2 case
 __device__ __forceinline__ double gam_kernel(double r1, double eta, double g) {
   if (g == 2.0) return rsqrt(r1 * r1 + 1.0 / (eta * eta));
@@ -55,6 +60,12 @@ __device__ __forceinline__ double gam_kernel(double r1, double eta, double g) {
 // ------------------------------------------------------------------------------------
 __device__ __forceinline__ void dexp_count(double r, double r0, const Gfn2Scalars& p, double& c,
                                            double& dc) {
+  if (p.method == 1) {  // GFN1: single exponential 1/(1 + exp(-k (r0/r - 1)))
+    const double e = exp(-p.cn_exp_k * (r0 / r - 1.0));
+    c = 1.0 / (1.0 + e);
+    dc = -c * c * e * p.cn_exp_k * r0 / (r * r);
+    return;
+  }
   const double e1 = exp(-p.cn_ka * (r0 / r - 1.0));
   const double e2 = exp(-p.cn_kb * ((r0 + p.cn_rshift) / r - 1.0));
   const double f1 = 1.0 / (1.0 + e1), f2 = 1.0 / (1.0 + e2);
@@ -207,12 +218,13 @@ __device__ __forceinline__ void coulomb_dev(DevMol m, Gfn2Scalars p, const doubl
       const double hi = m.sh_hub[is0 + a];
       double acc = 0.0;
       for (int b = 0; b < nsj; ++b) {
-        const double g = 0.5 * (hi + m.sh_hub[js0 + b]);
+        const double g = eta_avg(hi, m.sh_hub[js0 + b], p.harmonic);
         const double t = gam_kernel(r1, g, p.gexp);
         acc += t * qsh[js0 + b];
       }
       ush[a] += acc;
     }
+    if (!p.aes) continue;
     // AES (multipole.f90:488-535), amat(:, jat, iat) with vec = R_iat - R_jat
     const double g1 = 1.0 / r1, g3 = g1 * g1 * g1, g5 = g3 * g1 * g1;
     const double rr = 0.5 * (mrad[j] + ri) * g1;
@@ -251,23 +263,30 @@ __device__ __forceinline__ void coulomb_dev(DevMol m, Gfn2Scalars p, const doubl
   for (int a = 0; a < nsi; ++a) {
     double acc = ush[a];
     for (int b = 0; b < nsi; ++b)
-      acc += 0.5 * (m.sh_hub[is0 + a] + m.sh_hub[is0 + b]) * qsh[is0 + b];
+      acc += eta_avg(m.sh_hub[is0 + a], m.sh_hub[is0 + b], p.harmonic) * qsh[is0 + b];
     gsh[a] = acc;
   }
   const double mpscale[6] = {1, 2, 1, 2, 2, 1};
   if (MODE == 0) {
     for (int a = 0; a < nsi; ++a) {
       const double q = qsh[is0 + a];
-      vsh[is0 + a] = gsh[a] + q * q * m.sh_gam3[is0 + a];
+      vsh[is0 + a] = gsh[a] + (p.third_atom ? 0.0 : q * q * m.sh_gam3[is0 + a]);
     }
-    vat[i] = uat;
-    for (int k = 0; k < 3; ++k) vdp[3 * i + k] = ud[k] + udd[k] + 2.0 * m.at_dkern[i] * di[k];
-    for (int k = 0; k < 6; ++k) vqp[6 * i + k] = uq[k] + 2.0 * m.at_qkern[i] * qi[k] * mpscale[k];
+    vat[i] = uat + (p.third_atom ? qa_i * qa_i * m.at_gam3[i] : 0.0);
+    for (int k = 0; k < 3; ++k)
+      vdp[3 * i + k] = p.aes ? ud[k] + udd[k] + 2.0 * m.at_dkern[i] * di[k] : 0.0;
+    for (int k = 0; k < 6; ++k)
+      vqp[6 * i + k] = p.aes ? uq[k] + 2.0 * m.at_qkern[i] * qi[k] * mpscale[k] : 0.0;
   } else {
     double e = 0.0;
     for (int a = 0; a < nsi; ++a) {
       const double q = qsh[is0 + a];
-      e += 0.5 * gsh[a] * q + q * q * q * m.sh_gam3[is0 + a] / 3.0;
+      e += 0.5 * gsh[a] * q + (p.third_atom ? 0.0 : q * q * q * m.sh_gam3[is0 + a] / 3.0);
+    }
+    if (p.third_atom) e += qa_i * qa_i * qa_i * m.at_gam3[i] / 3.0;
+    if (!p.aes) {
+      eat[i] += e;
+      return;
     }
     for (int k = 0; k < 3; ++k) e += di[k] * (ud[k] + 0.5 * udd[k]);
     for (int k = 0; k < 6; ++k) e += qi[k] * uq[k];
@@ -329,7 +348,7 @@ __device__ __forceinline__ void coulomb_grad_dev(DevMol m, Gfn2Scalars p, const 
     double f = 0.0;
     for (int a = 0; a < nsi; ++a)
       for (int b = 0; b < nsj; ++b) {
-        const double gm = 0.5 * (m.sh_hub[is0 + a] + m.sh_hub[js0 + b]);
+        const double gm = eta_avg(m.sh_hub[is0 + a], m.sh_hub[js0 + b], p.harmonic);
         double d;
         if (p.gexp == 2.0) {
           d = 1.0 / (r2 + 1.0 / (gm * gm));
@@ -342,6 +361,12 @@ __device__ __forceinline__ void coulomb_grad_dev(DevMol m, Gfn2Scalars p, const 
       }
     double gp[3];
     for (int k = 0; k < 3; ++k) gp[k] = f * w[k];
+    if (!p.aes) {  // no anisotropic electrostatics (GFN1)
+      for (int k = 0; k < 3; ++k) g[k] += gp[k];
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) sg[3 * a + b] += 0.5 * gp[a] * w[b];
+      continue;
+    }
     // AES pair term written as in the reference with (iat, jat) = (i, j), vec = R_j - R_i
     const double* dj = dpat + 3 * j;
     const double* qj = qpat + 6 * j;
@@ -520,8 +545,8 @@ __device__ __forceinline__ void fock_dev(int n, const int* __restrict__ ao_at,
       acc[s] = H[rc] - 0.5 * S[rc] * (vao[r] + vc);
     }
   }
-  // multipole terms
-  for (int k = 0; k < 9; ++k) {
+  // multipole terms (absent, D == nullptr, for a Hamiltonian without anisotropic electrostatics)
+  for (int k = 0; D != nullptr && k < 9; ++k) {
     const double* M = k < 3 ? D + k * nn : Q + (k - 3) * nn;
     const double* u = k < 3 ? vdp : vqp;
     const int ku = k < 3 ? k : k - 3, su = k < 3 ? 3 : 6;
@@ -791,19 +816,20 @@ __global__ void k_pack(int nsh, int nat, const double* qsh, const double* dpat, 
 }
 
 void launch_pack(const DevMol& m, const double* qsh, const double* dpat, const double* qpat,
-                 double* vec, cudaStream_t s) {
-  const int nd = m.nsh + 9 * m.nat;
+                 double* vec, cudaStream_t s, bool with_mp) {
+  const int nmp = with_mp ? m.nat : 0;  // atoms whose multipoles enter the mixer
+  const int nd = m.nsh + 9 * nmp;
   ++g_kernel_launches;
-  k_pack<<<(nd + 255) / 256, 256, 0, s>>>(m.nsh, m.nat, qsh, dpat, qpat, vec);
+  k_pack<<<(nd + 255) / 256, 256, 0, s>>>(m.nsh, nmp, qsh, dpat, qpat, vec);
 }
 
 __device__ __forceinline__ void unpack_dev(DevMol m, const double* vec, double* qsh, double* qat, double* dpat,
-                         double* qpat) {
+                         double* qpat, int with_mp) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int nsh = m.nsh, nat = m.nat;
   if (t < nsh) qsh[t] = vec[t];
-  if (t < 3 * nat) dpat[t] = vec[nsh + t];
-  if (t < 6 * nat) qpat[t] = vec[nsh + 3 * nat + t];
+  if (with_mp && t < 3 * nat) dpat[t] = vec[nsh + t];
+  if (with_mp && t < 6 * nat) qpat[t] = vec[nsh + 3 * nat + t];
   if (t < nat) {
     double a = 0.0;
     for (int s = m.at_sh[t]; s < m.at_sh[t + 1]; ++s) a += vec[s];
@@ -811,15 +837,15 @@ __device__ __forceinline__ void unpack_dev(DevMol m, const double* vec, double* 
   }
 }
 __global__ void k_unpack(DevMol m, const double* vec, double* qsh, double* qat, double* dpat,
-                         double* qpat) {
-  unpack_dev(m, vec, qsh, qat, dpat, qpat);
+                         double* qpat, int with_mp) {
+  unpack_dev(m, vec, qsh, qat, dpat, qpat, with_mp);
 }
 
 void launch_unpack(const DevMol& m, const double* vec, double* qsh, double* qat, double* dpat,
-                   double* qpat, cudaStream_t s) {
+                   double* qpat, cudaStream_t s, bool with_mp) {
   const int nt = m.nsh > 6 * m.nat ? m.nsh : 6 * m.nat;
   ++g_kernel_launches;
-  k_unpack<<<(nt + 255) / 256, 256, 0, s>>>(m, vec, qsh, qat, dpat, qpat);
+  k_unpack<<<(nt + 255) / 256, 256, 0, s>>>(m, vec, qsh, qat, dpat, qpat, with_mp ? 1 : 0);
 }
 
 __device__ __forceinline__ void diff_dev(int nd, const double* vout, const double* q, double* dq, double* err) {
@@ -1251,10 +1277,11 @@ void launch_fermi_b(const BatchLaunch& b) {
 
 __global__ void kb_pack(BARGS, int output) {
   BMOL;
+  const int nmp = q.with_mp ? q.m.nat : 0;
   if (output)
-    pack_dev(q.m.nsh, q.m.nat, q.qsh_o, q.dpat_o, q.qpat_o, q.vec_out);
+    pack_dev(q.m.nsh, nmp, q.qsh_o, q.dpat_o, q.qpat_o, q.vec_out);
   else
-    pack_dev(q.m.nsh, q.m.nat, q.qsh, q.dpat, q.qpat, q.bq);
+    pack_dev(q.m.nsh, nmp, q.qsh, q.dpat, q.qpat, q.bq);
 }
 void launch_pack_b(const BatchLaunch& b, bool output) {
   if (!b.count) return;
@@ -1264,7 +1291,7 @@ void launch_pack_b(const BatchLaunch& b, bool output) {
 
 __global__ void kb_unpack(BARGS) {
   BMOL;
-  unpack_dev(q.m, q.bq, q.qsh, q.qat, q.dpat, q.qpat);
+  unpack_dev(q.m, q.bq, q.qsh, q.qat, q.dpat, q.qpat, q.with_mp);
 }
 void launch_unpack_b(const BatchLaunch& b) {
   if (!b.count) return;

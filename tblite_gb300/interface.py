@@ -109,16 +109,19 @@ class Result:
 class Calculator(Structure):
     """Single point calculator (reference interface.py:382-685)."""
 
-    _methods = ("GFN2-xTB",)
+    _loader = {
+        "GFN2-xTB": library.new_gfn2_calculator,
+        "GFN1-xTB": library.new_gfn1_calculator,
+    }
 
     def __init__(self, method: str, numbers, positions, charge: Optional[float] = None,
                  uhf: Optional[int] = None, lattice=None, periodic=None, xtb_config=None,
                  **context_kwargs):
         Structure.__init__(self, numbers, positions, charge, uhf, lattice, periodic)
-        if method not in self._methods:
+        if method not in self._loader:
             raise TBLiteValueError(f"Method '{method}' is not available for this calculator")
         self._ctx = library.new_context(**context_kwargs)
-        self._calc = library.new_gfn2_calculator(self._ctx, self._mol)
+        self._calc = self._loader[method](self._ctx, self._mol)
         self._method = method
 
     def __del__(self):

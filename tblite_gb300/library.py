@@ -55,6 +55,7 @@ _SIGNATURES = {
     "tblite_copy_result": (c_void_p, [c_void_p]),
     "tblite_delete_result": (None, [POINTER(c_void_p)]),
     "tblite_new_gfn2_calculator": (c_void_p, [c_void_p, c_void_p, c_void_p]),
+    "tblite_new_gfn1_calculator": (c_void_p, [c_void_p, c_void_p, c_void_p]),
     "tblite_delete_calculator": (None, [POINTER(c_void_p)]),
     "tblite_set_calculator_accuracy": (None, [c_void_p, c_void_p, c_double]),
     "tblite_set_calculator_max_iter": (None, [c_void_p, c_void_p, c_int]),
@@ -232,6 +233,19 @@ def update_geometry(mol, positions):
 def new_gfn2_calculator(ctx, mol):
     lib = load()
     calc = c_void_p(lib.tblite_new_gfn2_calculator(ctx, mol, None))
+    context_check(ctx)
+    return calc
+
+
+def set_parameter_gradient(ctx, calc, enable=True):
+    """Request dE/d(shell parameters) with the next single point (GFN2-xTB calculators)."""
+    load().tblite_gb300_set_calculator_parameter_gradient(ctx, calc, 1 if enable else 0)
+    context_check(ctx)
+
+
+def new_gfn1_calculator(ctx, mol):
+    lib = load()
+    calc = c_void_p(lib.tblite_new_gfn1_calculator(ctx, mol, None))
     context_check(ctx)
     return calc
 
