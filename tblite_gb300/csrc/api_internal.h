@@ -191,7 +191,9 @@ struct _tblite_result {
 
 // D4 model constants (damping, counting function, cutoffs) of the element-data pack
 void d4_model_constants(DevD4& d);
-// GFN2 scalar parameters of a calculator
+// D3 model constants (counting functions, cutoffs) and the GFN1-xTB damping parameters
+void d3_model_constants(DevD3& d);
+// scalar parameters of a calculator's Hamiltonian (GFN2-xTB or GFN1-xTB)
 Gfn2Scalars gfn2_scalars(const _tblite_calculator* c);
 // electrons per spin channel (reference xtb/singlepoint.f90:140-156); throws on an impossible
 // combination of charge and unpaired electrons

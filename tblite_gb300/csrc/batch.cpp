@@ -1,4 +1,4 @@
-// Batched ensemble driver: GFN2-xTB energy + gradient of many independent molecules with one
+// Batched ensemble driver: GFN2-xTB / GFN1-xTB energy + gradient of many independent molecules with one
 // launch per SCF step for a whole size bucket, instead of one launch per molecule.
 //
 // Layout.  Molecules are sorted by orbital count (largest first) and grouped into size buckets
@@ -107,13 +107,14 @@ struct Plan {
   _tblite_calculator* c;
   const _tblite_structure* mol;
   _tblite_result* res;
-  int nat, nsh, nao, nd, memory, max_iter;
+  int nat, nsh, nao, nd, memory, max_iter, method;
   double nalp, nbet;
-  bool has_d4;
+  bool has_d4, has_d3;
   // offsets (region, offset) of every array
   Piece xyz, at_z, at_sh, sh_atom, sh_l, sh_nprim, sh_alpha, sh_coeff, sh_ao, ao_sh, ao_at, sh_se0,
       sh_kcn, sh_shpoly, sh_zeta, sh_hub, sh_gam3, sh_refocc, at_en, at_rad, at_rcov, at_mprad,
-      at_vcn, at_dkern, at_qkern, at_repa, at_repz;
+      at_vcn, at_dkern, at_qkern, at_repa, at_repz, sh_valence, at_gam3;
+  Piece d3_nref, d3_refcn, d3_sref, d3_r4r2, d3_rcov, d3_cn, d3_a, d3_da, d3_dEdcn;
   Piece d4_sp, d4_nref, d4_ngw, d4_refcn, d4_refq, d4_zeff, d4_gam, d4_r4r2, d4_rcov, d4_en,
       d4_c6ref;
   Piece d4_cn, d4_gw, d4_dgw, d4_gwv, d4_dgwdq, d4_dgwv_cn, d4_c6, d4_dc6, d4_e3, d4_dEdcn;
@@ -158,8 +159,17 @@ void layout(Plan& pl, Region* R) {
                    &pl.sh_refocc})
     *p = piece<double>(R, RU, ns);
   for (Piece* p : {&pl.at_en, &pl.at_rad, &pl.at_rcov, &pl.at_mprad, &pl.at_vcn, &pl.at_dkern,
-                   &pl.at_qkern, &pl.at_repa, &pl.at_repz})
+                   &pl.at_qkern, &pl.at_repa, &pl.at_repz, &pl.at_gam3})
     *p = piece<double>(R, RU, na);
+  pl.sh_valence = piece<int>(R, RU, ns);
+  if (pl.has_d3) {
+    pl.d3_nref = piece<int>(R, RU, na);
+    pl.d3_refcn = piece<double>(R, RU, na * D4_MREF);
+    pl.d3_sref = piece<double>(R, RU, na * D4_MREF);
+    pl.d3_r4r2 = piece<double>(R, RU, na);
+    pl.d3_rcov = piece<double>(R, RU, na);
+    for (Piece* p : {&pl.d3_cn, &pl.d3_a, &pl.d3_da, &pl.d3_dEdcn}) *p = piece<double>(R, RS, na);
+  }
   if (pl.has_d4) {
     pl.d4_sp = piece<int>(R, RU, na);
     pl.d4_nref = piece<int>(R, RU, na);
@@ -281,7 +291,23 @@ MolPtrs make_ptrs(const Plan& pl, const Bases& db) {
   m.at_qkern = db.at<double>(pl.at_qkern);
   m.at_repa = db.at<double>(pl.at_repa);
   m.at_repz = db.at<double>(pl.at_repz);
+  m.sh_valence = db.at<int>(pl.sh_valence);
+  m.at_gam3 = db.at<double>(pl.at_gam3);
   q.has_d4 = pl.has_d4 ? 1 : 0;
+  q.has_d3 = pl.has_d3 ? 1 : 0;
+  if (pl.has_d3) {
+    DevD3& d = q.d3;
+    d3_model_constants(d);
+    d.nref = db.at<int>(pl.d3_nref);
+    d.refcn = db.at<double>(pl.d3_refcn);
+    d.sref = db.at<double>(pl.d3_sref);
+    d.r4r2 = db.at<double>(pl.d3_r4r2);
+    d.rcov = db.at<double>(pl.d3_rcov);
+    d.cn = db.at<double>(pl.d3_cn);
+    d.a = db.at<double>(pl.d3_a);
+    d.da = db.at<double>(pl.d3_da);
+    d.dEdcn = db.at<double>(pl.d3_dEdcn);
+  }
   if (pl.has_d4) {
     DevD4& d = q.d4;
     d.nsp = pl.c->d4_nsp;
@@ -310,8 +336,8 @@ MolPtrs make_ptrs(const Plan& pl, const Bases& db) {
     w.dEdcn = db.at<double>(pl.d4_dEdcn);
   }
   q.nd = pl.nd;
-  q.with_mp = 1;  // GFN2-xTB: the atomic multipoles are mixed with the shell charges
-  q.has_d3 = 0;
+  // GFN2-xTB mixes the atomic multipoles with the shell charges, GFN1-xTB the charges alone
+  q.with_mp = pl.method == 2 ? 1 : 0;
   q.mull_chunks = mulliken_chunks(pl.nao);
   q.memory = std::min(pl.memory, HCAP);
   q.nalp = pl.nalp;
@@ -493,6 +519,15 @@ std::vector<int> run_chunk(std::vector<Plan>& plans, Arena& ar, _tblite_context*
     stage(hb, pl.at_qkern, c->at_qkern);
     stage(hb, pl.at_repa, c->at_repa);
     stage(hb, pl.at_repz, c->at_repz);
+    stage(hb, pl.sh_valence, c->sh_valence);
+    stage(hb, pl.at_gam3, c->at_gam3);
+    if (pl.has_d3) {
+      stage(hb, pl.d3_nref, c->d3_nref);
+      stage(hb, pl.d3_refcn, c->d3_refcn);
+      stage(hb, pl.d3_sref, c->d3_sref);
+      stage(hb, pl.d3_r4r2, c->d3_r4r2);
+      stage(hb, pl.d3_rcov, c->d3_rcov);
+    }
     if (pl.has_d4) {
       stage(hb, pl.d4_sp, c->d4_sp);
       stage(hb, pl.d4_nref, c->d4_nref);
@@ -586,6 +621,7 @@ std::vector<int> run_chunk(std::vector<Plan>& plans, Arena& ar, _tblite_context*
     launch_build_h0_b(L, p);
     launch_repulsion_b(L, p);
     d4_setup_b(L);
+    d3_setup_b(L);
     cholesky_inverse_b(L);
   });
   cuda_check(cudaMemcpyAsync(h_flag.data(), d_flag, sizeof(int) * np, cudaMemcpyDeviceToHost, s),
@@ -783,10 +819,12 @@ extern "C" int tblite_gb300_batch_singlepoint(tblite_context ctx, int nmol,
     pl.nat = c->nat;
     pl.nsh = c->nsh;
     pl.nao = c->nao;
-    pl.nd = c->nsh + 9 * c->nat;
+    pl.method = c->method;
+    pl.nd = c->nsh + (c->method == 2 ? 9 * c->nat : 0);
     pl.max_iter = c->max_iter;
     pl.memory = c->memory > 0 ? std::min(c->memory, c->max_iter) : c->max_iter;
     pl.has_d4 = c->has_d4;
+    pl.has_d3 = c->has_d3;
     try {
       electron_counts(c, mol, &pl.nalp, &pl.nbet);
     } catch (const std::exception& e) {
@@ -795,17 +833,18 @@ extern "C" int tblite_gb300_batch_singlepoint(tblite_context ctx, int nmol,
       continue;
     }
     const bool anneal = c->anneal && c->anneal_kt > c->etemp;
-    // implicit solvation, the parameter gradient and GFN1-xTB run on the one-molecule path
-    if (pl.nao > tri_max || anneal || pl.max_iter < 1 || c->solv || c->param_grad ||
-        c->method != 2) {
+    // implicit solvation and the parameter gradient run on the one-molecule path
+    if (pl.nao > tri_max || anneal || pl.max_iter < 1 || c->solv || c->param_grad) {
       plain.push_back(i);
       continue;
     }
     plans.push_back(pl);
   }
-  // largest first: the size buckets follow the sorted order
-  std::stable_sort(plans.begin(), plans.end(),
-                   [](const Plan& a, const Plan& b) { return a.nao > b.nao; });
+  // by method (one chunk runs one Hamiltonian), then largest first: the size buckets follow
+  // the sorted order
+  std::stable_sort(plans.begin(), plans.end(), [](const Plan& a, const Plan& b) {
+    return a.method != b.method ? a.method > b.method : a.nao > b.nao;
+  });
   try {
     std::lock_guard<std::mutex> lock(g_batch_mutex);
     g_last_device_ms = 0.0;
@@ -816,7 +855,8 @@ extern "C" int tblite_gb300_batch_singlepoint(tblite_context ctx, int nmol,
     size_t i0 = 0;
     while (i0 < plans.size()) {
       size_t i1 = i0, bytes = 0;
-      while (i1 < plans.size() && (i1 == i0 || bytes + molecule_bytes(plans[i1]) <= budget)) {
+      while (i1 < plans.size() && plans[i1].method == plans[i0].method &&
+             (i1 == i0 || bytes + molecule_bytes(plans[i1]) <= budget)) {
         bytes += molecule_bytes(plans[i1]);
         ++i1;
       }

@@ -599,14 +599,7 @@ static DevMol dev_mol(const _tblite_calculator* c) {
   return m;
 }
 
-static DevD3 dev_d3(const _tblite_calculator* c) {
-  const Workspace& w = *c->ws;
-  DevD3 d{};
-  d.nref = w.d3_nref.p;
-  d.refcn = w.d3_refcn.p;
-  d.sref = w.d3_sref.p;
-  d.r4r2 = w.d3_r4r2.p;
-  d.rcov = w.d3_rcov.p;
+void d3_model_constants(DevD3& d) {
   d.k1 = EXT_D3_K1;
   d.k3 = EXT_D3_K3;
   d.cn_cutoff = EXT_D3_CN_CUTOFF;
@@ -615,6 +608,17 @@ static DevD3 dev_d3(const _tblite_calculator* c) {
   d.s8 = GFN1_S8;
   d.a1 = GFN1_A1;
   d.a2 = GFN1_A2;
+}
+
+static DevD3 dev_d3(const _tblite_calculator* c) {
+  const Workspace& w = *c->ws;
+  DevD3 d{};
+  d3_model_constants(d);
+  d.nref = w.d3_nref.p;
+  d.refcn = w.d3_refcn.p;
+  d.sref = w.d3_sref.p;
+  d.r4r2 = w.d3_r4r2.p;
+  d.rcov = w.d3_rcov.p;
   d.cn = w.d3_cn.p;
   d.a = w.d3_a.p;
   d.da = w.d3_da.p;

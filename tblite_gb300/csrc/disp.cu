@@ -427,7 +427,7 @@ __device__ __forceinline__ void d3_count(double r, double r0, double k1, double&
   dc = -c * c * e * k1 * r0 / (r * r);
 }
 
-__global__ void k_d3_setup(DevMol m, DevD3 d) {
+__device__ __forceinline__ void d3_setup_dev(const DevMol& m, const DevD3& d) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (warp >= m.nat) return;
   const int i = warp;
@@ -462,8 +462,8 @@ __global__ void k_d3_setup(DevMol m, DevD3 d) {
   d.da[i] = (dws * norm - ws * dnorm) / (norm * norm);
 }
 
-__global__ void k_d3_pair(DevMol m, DevD3 d, int grad, double* eat, double* grad_out,
-                          double* sig_at) {
+__device__ __forceinline__ void d3_pair_dev(const DevMol& m, const DevD3& d, int grad, double* eat,
+                                            double* grad_out, double* sig_at) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (warp >= m.nat) return;
   const int i = warp;
@@ -510,7 +510,8 @@ __global__ void k_d3_pair(DevMol m, DevD3 d, int grad, double* eat, double* grad
   for (int k = 0; k < 9; ++k) sig_at[9 * i + k] += sg[k];
 }
 
-__global__ void k_d3_cn_grad(DevMol m, DevD3 d, double* grad, double* sig_at) {
+__device__ __forceinline__ void d3_cn_grad_dev(const DevMol& m, const DevD3& d, double* grad,
+                                               double* sig_at) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (warp >= m.nat) return;
   const int i = warp;
@@ -538,6 +539,15 @@ __global__ void k_d3_cn_grad(DevMol m, DevD3 d, double* grad, double* sig_at) {
     for (int k = 0; k < 3; ++k) grad[3 * i + k] += g[k];
     for (int k = 0; k < 9; ++k) sig_at[9 * i + k] += sg[k];
   }
+}
+
+__global__ void k_d3_setup(DevMol m, DevD3 d) { d3_setup_dev(m, d); }
+__global__ void k_d3_pair(DevMol m, DevD3 d, int grad, double* eat, double* grad_out,
+                          double* sig_at) {
+  d3_pair_dev(m, d, grad, eat, grad_out, sig_at);
+}
+__global__ void k_d3_cn_grad(DevMol m, DevD3 d, double* grad, double* sig_at) {
+  d3_cn_grad_dev(m, d, grad, sig_at);
 }
 
 void d3_energy_gradient(const DevMol& m, const DevD3& d, bool grad, double* eat, double* grad_out,
@@ -609,6 +619,24 @@ __global__ void kb_d4_cn_grad(BARGS) {
   d4_cn_grad_dev(q.m, q.d4, q.d4w.dEdcn, q.grad, q.sig_at);
 }
 
+// D3 (GFN1-xTB): energy into erep, explicit and CN chain-rule gradient, all at setup
+#define BMOL3                                 \
+  const MolPtrs& q = mp[list[blockIdx.z]];    \
+  if (!q.has_d3) return
+__global__ void kb_d3_setup(BARGS) {
+  BMOL3;
+  d3_setup_dev(q.m, q.d3);
+}
+__global__ void kb_d3_pair(BARGS) {
+  BMOL3;
+  d3_pair_dev(q.m, q.d3, 1, q.erep, q.grad, q.sig_at);
+}
+__global__ void kb_d3_cn_grad(BARGS) {
+  BMOL3;
+  d3_cn_grad_dev(q.m, q.d3, q.grad, q.sig_at);
+}
+#undef BMOL3
+
 static inline dim3 bwarps(const BatchLaunch& b) { return dim3(warps_grid(b.nat_max), 1, b.count); }
 static inline dim3 batoms(const BatchLaunch& b) {
   return dim3((b.nat_max + 127) / 128, 1, b.count);
@@ -623,6 +651,13 @@ void d4_setup_b(const BatchLaunch& b) {
   const long long nn = (long long)b.nat_max * b.nat_max;
   kb_d4_c6<<<dim3((unsigned)((nn + 255) / 256), 1, b.count), 256, 0, b.s>>>(b.mp, b.list);
   kb_d4_atm<<<bwarps(b), 64, 0, b.s>>>(b.mp, b.list);
+}
+void d3_setup_b(const BatchLaunch& b) {
+  if (!b.count) return;
+  g_kernel_launches += 3;
+  kb_d3_setup<<<bwarps(b), 64, 0, b.s>>>(b.mp, b.list);
+  kb_d3_pair<<<bwarps(b), 64, 0, b.s>>>(b.mp, b.list);
+  kb_d3_cn_grad<<<bwarps(b), 64, 0, b.s>>>(b.mp, b.list);
 }
 void d4_potential_b(const BatchLaunch& b) {
   if (!b.count) return;

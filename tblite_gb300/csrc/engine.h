@@ -265,6 +265,7 @@ struct MolPtrs {
   DevMol m;
   DevD4 d4;
   D4Work d4w;
+  DevD3 d3;
   int has_d4, nd, mull_chunks, memory, with_mp, has_d3;
   double nalp, nbet, kt, damp, econv, pconv;
   double h0_cutoff;  // depends on the basis of the molecule (smallest exponent)
@@ -319,6 +320,7 @@ void d4_setup_b(const BatchLaunch& b);
 void d4_potential_b(const BatchLaunch& b);
 void d4_energy_b(const BatchLaunch& b);
 void d4_gradient_b(const BatchLaunch& b);
+void d3_setup_b(const BatchLaunch& b);  // D3 energy + gradient of the GFN1-xTB molecules
 // batched FP64 GEMM at one of the fixed call sites of the SCF (operands from MolPtrs)
 enum { GS_FX = 0,  // T1 = F X            (X upper triangular)
        GS_XTT,     // A = X^T T1

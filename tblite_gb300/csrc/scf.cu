@@ -1237,7 +1237,7 @@ __global__ void __launch_bounds__(256) kb_fock(BARGS) {
   BMOL;
   const int n = q.m.nao;
   if ((int)blockIdx.x * 32 >= n || (int)blockIdx.y * 32 >= n) return;  // tile outside
-  fock_dev(n, q.m.ao_at, q.H, q.S, q.D, q.Q, q.vao, q.vdp, q.vqp, q.F);
+  fock_dev(n, q.m.ao_at, q.H, q.S, q.with_mp ? q.D : nullptr, q.Q, q.vao, q.vdp, q.vqp, q.F);
 }
 void launch_fock_b(const BatchLaunch& b) {
   if (!b.count) return;

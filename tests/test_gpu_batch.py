@@ -31,10 +31,10 @@ def _ensemble():
     return mols
 
 
-def _calc(z, x, **settings):
+def _calc(z, x, method="GFN2-xTB", **settings):
     from tblite_gb300.interface import Calculator
 
-    calc = Calculator("GFN2-xTB", z, x)
+    calc = Calculator(method, z, x)
     for k, v in settings.items():
         calc.set(k, v)
     return calc
@@ -105,3 +105,23 @@ def test_batch_restart_and_fallback():
     with pytest.raises(TBLiteRuntimeError, match="Batch entry 1"):
         batch_singlepoint(calcs)
     assert batch_fallbacks() == 1
+
+
+def test_batch_mixed_methods():
+    """GFN1-xTB and GFN2-xTB molecules in one call: each method runs in its own chunk; both
+    agree with their plain paths, and the GFN1 molecules with the GFN1 oracle."""
+    from oracle import gfn1, gfn2
+    from tblite_gb300.interface import batch_fallbacks, batch_singlepoint
+
+    mols = _ensemble()
+    methods = ["GFN1-xTB" if i % 2 == 0 else "GFN2-xTB" for i in range(len(mols))]
+    res_b = batch_singlepoint([_calc(z, x, m) for (z, x), m in zip(mols, methods)])
+    assert batch_fallbacks() == 0
+    for (z, x), m, rb in zip(mols, methods, res_b):
+        _compare(rb, _calc(z, x, m).singlepoint())
+    for (z, x), m, rb in list(zip(mols, methods, res_b))[::4]:
+        if m != "GFN1-xTB":
+            continue
+        ref = gfn1.singlepoint(gfn1.new_calc(gfn2.Molecule(np.asarray(z), np.asarray(x))))
+        assert abs(rb.get("energy") - ref.energy) <= E_TOL
+        assert np.max(np.abs(rb.get("gradient") - ref.gradient)) <= G_TOL
