@@ -18,9 +18,9 @@
 // A molecule leaves the batch for the one-molecule path (which then reproduces exactly what a
 // plain call does, including its errors) when it is larger than the batched
 // tridiagonalisation holds, uses temperature annealing, carries an implicit solvation model or
-// asks for the parameter gradient, would need more Broyden history than the batch keeps, does
-// not converge within its iteration limit, or fails (overlap not positive definite, singular
-// Broyden system).
+// asks for the parameter gradient, would need more Broyden history than the batch keeps, has a
+// Fermi level within 51 kT of the highest eigenvalue the SCF computes, does not converge within
+// its iteration limit, or fails (overlap not positive definite, singular Broyden system).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -340,6 +340,7 @@ MolPtrs make_ptrs(const Plan& pl, const Bases& db) {
   q.with_mp = pl.method == 2 ? 1 : 0;
   q.mull_chunks = mulliken_chunks(pl.nao);
   q.memory = std::min(pl.memory, HCAP);
+  q.nev = scf_eigenvalue_count(pl.nao, std::max(pl.nalp, pl.nbet));
   q.nalp = pl.nalp;
   q.nbet = pl.nbet;
   q.kt = pl.c->etemp;
@@ -703,6 +704,7 @@ std::vector<int> run_chunk(std::vector<Plan>& plans, Arena& ar, _tblite_context*
   // H0 gradient with the last potential, CN chain rule
   if (upload_lists(done) > 0) {
     each([&](BatchLaunch& L) {
+      eigen_values_rest_b(L);  // the levels above the SCF's range, for the results
       launch_coulomb_gradient_b(L, p);
       d4_gradient_b(L);
       launch_fe_b(L);

@@ -854,7 +854,9 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
     stream_wait(s);
     for (int i = 0; i < nat; ++i) h_erep[i] += h_e3[i];
   }
-  std::vector<int> h_cnt(1);
+  std::vector<int> h_cnt(2);
+  // eigenvalues per iteration: the occupied levels and a margin (the rest once converged)
+  int nev = scf_eigenvalue_count(n, std::max(nalp, nbet));
   double kt = target_kt;
   while (!converged && iscf < c->max_iter) {
     const double elast = eelec_sum;
@@ -888,13 +890,20 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
     launch_pack(m, w.qsh.p, w.dpat.p, w.qpat.p, w.b_q.p, s, with_mp);  // mixer%set
     g_prof.end(s);
     g_prof.begin(PH_EIGEN, s);
-    const int info = eigen_values(w.eig, w.F.p, w.emo.p);
+    const int info = eigen_values(w.eig, w.F.p, w.emo.p, nev);
     if (info != 0)
       throw std::runtime_error("(sygvd) failed to solve eigenvalue problem. info=" +
                                std::to_string(info));
-    launch_fermi(n, w.emo.p, nalp, nbet, kt, w.focc.p, w.scal.p, w.icount.p, s);
-    w.icount.download(h_cnt, 1, s);
+    launch_fermi(n, w.emo.p, nalp, nbet, kt, w.focc.p, w.scal.p, w.icount.p, s, nev);
+    w.icount.download(h_cnt, 2, s);
     stream_wait(s);
+    if (h_cnt[1] != 0) {  // the Fermi level needs more levels: all of them from now on
+      eigen_values_rest(w.eig, nev, w.emo.p);
+      nev = n;
+      launch_fermi(n, w.emo.p, nalp, nbet, kt, w.focc.p, w.scal.p, w.icount.p, s, nev);
+      w.icount.download(h_cnt, 2, s);
+      stream_wait(s);
+    }
     eigen_vectors(w.eig, h_cnt[0], w.C.p);
     g_prof.end(s);
     g_prof.begin(PH_DENSITY, s);
@@ -955,6 +964,7 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
   // the result carries every orbital (wavefunction/type.f90 coeff(nao, nao)): the SCF only
   // needed the occupied ones, the empty ones come from the last tridiagonal form
   g_prof.begin(PH_EIGEN, s);
+  eigen_values_rest(w.eig, nev, w.emo.p);
   eigen_vectors_range(w.eig, h_cnt[0], (int)n, w.C.p);
   g_prof.end(s);
   // Wiberg/Mayer bond orders (post_processing/wbo.f90:60-115): closed shell from P; restricted

@@ -39,6 +39,7 @@ struct EigenSolver {
   double *L = nullptr, *X = nullptr, *A = nullptr, *T1 = nullptr;
   double *d = nullptr, *e = nullptr, *tau = nullptr, *w = nullptr, *pv = nullptr, *scal = nullptr;
   double *lu = nullptr;   // inverse iteration scratch [5][n][n]
+  double *tw = nullptr;   // eigenvalue scratch: e^2 [n] (double), d and e^2 [n] (float)
   double *Y = nullptr;    // eigenvectors of T, column-major [k][n]
   int* status = nullptr;  // device
   int* hstatus = nullptr; // pinned
@@ -275,15 +276,16 @@ __device__ __forceinline__ void tridiag_smem_body(int n, double* A, double* d, d
     }
     const double K = sK;
     if (t != 0.0) {
+      // w = p + K v once per row, then two FMAs per element: A -= v w^T + w v^T
+      for (int r = i + 1 + threadIdx.x; r < n; r += blockDim.x) sp[r] = fma(K, sv[r], sp[r]);
+      __syncthreads();
       for (int s = 0; s < ncpb; ++s) {
         const int j = b + s * nb;
         if (j <= i || j >= n) continue;
         double* col = scol + (size_t)s * n;
-        const double vc = sv[j], wc = sp[j] + K * vc;
-        for (int r = i + 1 + threadIdx.x; r < n; r += blockDim.x) {
-          const double vr = sv[r];
-          col[r] -= vr * wc + (sp[r] + K * vr) * vc;
-        }
+        const double vc = sv[j], wc = sp[j];
+        for (int r = i + 1 + threadIdx.x; r < n; r += blockDim.x)
+          col[r] = fma(-sv[r], wc, fma(-sp[r], vc, col[r]));
       }
     }
     __syncthreads();
@@ -302,150 +304,289 @@ __global__ void __launch_bounds__(256) k_tridiag_smem(int n, double* A, double* 
 }
 
 // ------------------------------------------------------------------------------------------
-// eigenvalues of T by bisection on the Sturm count (one thread per eigenvalue, ascending)
+// Eigenvalues of the tridiagonal T (one thread per eigenvalue, ascending order).
+//
+// GB300 executes FP32 about 60x faster than FP64, so each eigenvalue is found in three stages:
+//   1. FP32 bisection on the Sturm count of fl32(T) down to a bracket of 2^-21 |T|;
+//   2. the bracket is widened by 2^-16 |T| (the FP32 count is exact for a matrix within a few
+//      FP32 ulps of T, i.e. within ~1e-6 |T| in its eigenvalues) and both ends are checked
+//      with FP64 Sturm counts; a bracket that fails the check restarts from the Gershgorin
+//      interval;
+//   3. FP64: while the bracket holds exactly this eigenvalue, regula falsi with the Illinois
+//      modification on det(T - x I) (superlinear; a point at a converged end is moved half a
+//      tolerance inside); otherwise, and whenever three interpolation steps have not halved
+//      the bracket, bisection.  About 7 FP64 counts per isolated eigenvalue instead of ~55.
+// The stopping rule is the one of plain bisection (width <= 2 eps max(|lo|, |hi|) + 4 pivmin)
+// and the result is the midpoint of the final bracket.  The FP64 sweep is the determinant
+// recurrence p_i = (d_i - x) p_{i-1} - e_{i-1}^2 p_{i-2}: division free, the pair rescaled by
+// a power of two every 8 steps (the exponent is carried, so det(T - x I) = p * 2^E), an exact
+// zero takes the sign opposite to its predecessor; the number of sign changes is the number
+// of eigenvalues below x.
 // ------------------------------------------------------------------------------------------
-__device__ __forceinline__ int sturm(int n, const double* __restrict__ d,
-                                     const double* __restrict__ e2, double x, double pivmin) {
-  int cnt = 0;
-  double q = d[0] - x;
-  if (fabs(q) < pivmin) q = -pivmin;
-  cnt += q < 0.0;
-  for (int i = 1; i < n; ++i) {
-    q = d[i] - x - e2[i - 1] / q;
-    if (fabs(q) < pivmin) q = -pivmin;
-    cnt += q < 0.0;
+// One step of the FP64 recurrence.  FP64 issue slots are scarce on this GPU: the sign tests,
+// the zero test and the exponent test read the high word with integer instructions, so per
+// step the FP64 pipe sees one subtraction, one multiplication and one FMA.
+__device__ __forceinline__ void step64(double a, double ee, double& p0, double& p1, int& h1,
+                                       int& cnt) {
+  double p2 = fma(a, p1, -ee * p0);
+  const bool z = ((__double2hiint(p2) << 1) | __double2loint(p2)) == 0;
+  p2 = z ? (h1 < 0 ? 0x1p-900 : -0x1p-900) : p2;  // exact zero: opposite sign to p1
+  const int h2 = __double2hiint(p2);
+  cnt += (unsigned)(h2 ^ h1) >> 31;
+  p0 = p1;
+  p1 = p2;
+  h1 = h2;
+}
+__device__ __forceinline__ void rescale64(double& p0, double& p1, int& h1, int& E) {
+  const int be = (h1 >> 20) & 0x7ff;  // biased exponent of |p1|
+  if (be > 1023 + 400 || be < 1023 - 400) {
+    const double sc = __hiloint2double((2046 - be) << 20, 0);  // 2^-(be - 1023), exact
+    p1 *= sc;
+    p0 *= sc;
+    h1 = __double2hiint(p1);
+    E += be - 1023;
   }
+}
+// Sturm count below x and det(T - x I) = fm * 2^fe.  Blocks of 8 steps load their d and e^2
+// together, so the loads of a block overlap and the FMA chain runs back to back.
+__device__ __forceinline__ int sweep64(int n, const double* __restrict__ d,
+                                       const double* __restrict__ e2, double x, double& fm,
+                                       int& fe) {
+  double p0 = 1.0, p1 = d[0] - x;
+  if (p1 == 0.0) p1 = -0x1p-900;
+  int h1 = __double2hiint(p1);
+  int cnt = (unsigned)h1 >> 31, E = 0;
+  int i = 1;
+  for (; i + 8 <= n; i += 8) {
+    double dv[8], ev[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      dv[k] = d[i + k];
+      ev[k] = e2[i + k - 1];
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) step64(dv[k] - x, ev[k], p0, p1, h1, cnt);
+    rescale64(p0, p1, h1, E);
+  }
+  for (; i < n; ++i) step64(d[i] - x, e2[i - 1], p0, p1, h1, cnt);
+  fm = p1;
+  fe = E;
   return cnt;
 }
 
-__global__ void k_bisect(int n, const double* __restrict__ d, const double* __restrict__ e,
-                         double* e2, double* w, double* scal) {
-  __shared__ double bounds[3];
-  // Gershgorin bounds and pivmin (each block recomputes, O(n))
-  if (threadIdx.x == 0) {
-    double lo = 1e300, hi = -1e300, emax = 0.0;
-    for (int i = 0; i < n; ++i) {
-      const double r = (i > 0 ? fabs(e[i - 1]) : 0.0) + (i < n - 1 ? fabs(e[i]) : 0.0);
-      lo = fmin(lo, d[i] - r);
-      hi = fmax(hi, d[i] + r);
-      if (i < n - 1) emax = fmax(emax, e[i] * e[i]);
+__device__ __forceinline__ void step32(float a, float ee, float& p0, float& p1, int& cnt) {
+  float p2 = fmaf(a, p1, -ee * p0);
+  p2 = p2 == 0.f ? -copysignf(0x1p-100f, p1) : p2;
+  cnt += (unsigned)(__float_as_int(p2) ^ __float_as_int(p1)) >> 31;
+  const float m = fabsf(p2);
+  const float sc = m > 0x1p32f ? 0x1p-64f : (m < 0x1p-32f ? 0x1p64f : 1.f);
+  p0 = p1 * sc;
+  p1 = p2 * sc;
+}
+__device__ __forceinline__ int sweep32(int n, const float* __restrict__ d,
+                                       const float* __restrict__ e2, float x) {
+  float p0 = 1.f, p1 = d[0] - x;
+  if (p1 == 0.f) p1 = -0x1p-100f;
+  int cnt = p1 < 0.f;
+  int i = 1;
+  for (; i + 8 <= n; i += 8) {
+    float dv[8], ev[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      dv[k] = d[i + k];
+      ev[k] = e2[i + k - 1];
     }
-    const double tnorm = fmax(fabs(lo), fabs(hi));
-    bounds[0] = lo - 2.2e-16 * tnorm * 4 - 1e-300;
-    bounds[1] = hi + 2.2e-16 * tnorm * 4 + 1e-300;
-    bounds[2] = fmax(2.2250738585072014e-308 * fmax(1.0, emax), 1e-300);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) step32(dv[k] - x, ev[k], p0, p1, cnt);
   }
-  __syncthreads();
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  (void)e2;
-  if (j >= n) return;
-  double lo = bounds[0], hi = bounds[1];
-  const double pivmin = bounds[2];
-  for (int it = 0; it < 200; ++it) {
-    const double mid = 0.5 * (lo + hi);
-    if (hi - lo <= 2.0 * 2.220446049250313e-16 * fmax(fabs(lo), fabs(hi)) + 4.0 * pivmin ||
-        mid == lo || mid == hi)
-      break;
-    int cnt = 0;
-    double q = d[0] - mid;
-    if (fabs(q) < pivmin) q = -pivmin;
-    cnt += q < 0.0;
-    for (int i = 1; i < n; ++i) {
-      q = d[i] - mid - (e[i - 1] * e[i - 1]) / q;
-      if (fabs(q) < pivmin) q = -pivmin;
-      cnt += q < 0.0;
-    }
-    if (cnt > j) hi = mid;
-    else lo = mid;
-  }
-  w[j] = 0.5 * (lo + hi);
-  if (j == 0) scal[1] = fmax(fabs(bounds[0]), fabs(bounds[1]));  // |T| estimate
+  for (; i < n; ++i) step32(d[i] - x, e2[i - 1], p0, p1, cnt);
+  return cnt;
 }
 
-// Multisection: four lanes per eigenvalue evaluate the Sturm count at four interior points of
-// the current bracket (a 5-way split per round), so 8 eigenvalues fill a warp and the n
-// eigenvalues spread over all SMs.  The Sturm recurrence uses the correctly rounded FP64
-// reciprocal; the count stays backward stable.
-__device__ __forceinline__ void multisect_dev(int n, const double* __restrict__ d,
-                                                  const double* __restrict__ e, double* w,
-                                                  double* scal) {
-  __shared__ double bounds[3];
-  if (threadIdx.x == 0) {
-    double lo = 1e300, hi = -1e300, emax = 0.0;
-    for (int i = 0; i < n; ++i) {
-      const double r = (i > 0 ? fabs(e[i - 1]) : 0.0) + (i < n - 1 ? fabs(e[i]) : 0.0);
-      lo = fmin(lo, d[i] - r);
-      hi = fmax(hi, d[i] + r);
-      if (i < n - 1) emax = fmax(emax, e[i] * e[i]);
-    }
-    const double tnorm = fmax(fabs(lo), fabs(hi));
-    bounds[0] = lo - 8.9e-16 * tnorm - 1e-300;
-    bounds[1] = hi + 8.9e-16 * tnorm + 1e-300;
-    bounds[2] = fmax(2.2250738585072014e-308 * fmax(1.0, emax), 1e-300);
+// Gershgorin interval [lo, hi] (widened by 4 ulps) and pivmin of T, for every thread of the block
+struct TriBounds {
+  double lo, hi, tnorm, pivmin;
+};
+__device__ TriBounds tri_bounds(int n, const double* __restrict__ d,
+                                const double* __restrict__ e) {
+  __shared__ double red[3][32];
+  __shared__ TriBounds out;
+  double lo = 1e300, hi = -1e300, emax = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double r = (i > 0 ? fabs(e[i - 1]) : 0.0) + (i < n - 1 ? fabs(e[i]) : 0.0);
+    lo = fmin(lo, d[i] - r);
+    hi = fmax(hi, d[i] + r);
+    if (i < n - 1) emax = fmax(emax, e[i] * e[i]);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    emax = fmax(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  if (lane == 0) {
+    red[0][w] = lo;
+    red[1][w] = hi;
+    red[2][w] = emax;
   }
   __syncthreads();
-  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = gt >> 2, sub = gt & 3;
-  const unsigned grp = 0xFu << (threadIdx.x & 28);
-  const bool active = j < n;
-  double lo = bounds[0], hi = bounds[1];
-  const double pivmin = bounds[2];
-  for (int it = 0; it < 64; ++it) {
-    const bool done = !active || hi - lo <= 2.0 * 2.220446049250313e-16 * fmax(fabs(lo), fabs(hi)) + 4.0 * pivmin;
-    if (__all_sync(0xffffffffu, done)) break;
-    // four interior points per eigenvalue (a 5-way split).  Sturm count from the determinant
-    // recurrence p_i = (d_i - x) p_{i-1} - e_{i-1}^2 p_{i-2}: the number of sign changes equals
-    // the number of eigenvalues below x.  Division free; the pair (p_{i-1}, p_i) is rescaled by
-    // a power of two every 8 steps, and an exact zero takes the sign opposite to its
-    // predecessor (the limit of the quotient form with a negative pivot).
-    (void)pivmin;
-    const double step = (hi - lo) * 0.2;
-    const double x = lo + (sub + 1) * step;
-    int cnt = 0;
-    if (!done) {
-      double p0 = 1.0, p1 = d[0] - x;
-      if (p1 == 0.0) p1 = -0x1p-900;
-      cnt += p1 < 0.0;
-      for (int i = 1; i < n; ++i) {
-        const double ee = e[i - 1];
-        double p2 = fma(d[i] - x, p1, -(ee * ee) * p0);
-        if (p2 == 0.0) p2 = -copysign(0x1p-900, p1);
-        cnt += (p2 < 0.0) != (p1 < 0.0);
-        p0 = p1;
-        p1 = p2;
-        if ((i & 7) == 0) {
-          const double a = fabs(p1);
-          if (a > 0x1p400 || a < 0x1p-400) {
-            const int ex = ilogb(a);
-            p1 = scalbn(p1, -ex);
-            p0 = scalbn(p0, -ex);
-          }
-        }
-      }
+  if (threadIdx.x == 0) {
+    for (int k = 1; k < nw; ++k) {
+      lo = fmin(lo, red[0][k]);
+      hi = fmax(hi, red[1][k]);
+      emax = fmax(emax, red[2][k]);
     }
-    // gather the four counts of this eigenvalue's group
-    const int base = threadIdx.x & 28;
-    const int c0 = __shfl_sync(0xffffffffu, cnt, base + 0);
-    const int c1 = __shfl_sync(0xffffffffu, cnt, base + 1);
-    const int c2 = __shfl_sync(0xffffffffu, cnt, base + 2);
-    const int c3 = __shfl_sync(0xffffffffu, cnt, base + 3);
-    (void)grp;
-    if (!done) {
-      const double x0 = lo + step, x1 = lo + 2 * step, x2 = lo + 3 * step, x3 = lo + 4 * step;
-      if (c0 > j) hi = x0;
-      else if (c1 > j) { lo = x0; hi = x1; }
-      else if (c2 > j) { lo = x1; hi = x2; }
-      else if (c3 > j) { lo = x2; hi = x3; }
-      else lo = x3;
+    const double tnorm = fmax(fabs(lo), fabs(hi));
+    out.lo = lo - 8.9e-16 * tnorm - 1e-300;
+    out.hi = hi + 8.9e-16 * tnorm + 1e-300;
+    out.tnorm = fmax(fabs(out.lo), fabs(out.hi));
+    out.pivmin = fmax(2.2250738585072014e-308 * fmax(1.0, emax), 1e-300);
+  }
+  __syncthreads();
+  return out;
+}
+
+// eigenvalue j of T; warp-collective (every lane of the warp calls it, inactive lanes too)
+__device__ double tri_eigenvalue(int n, const double* __restrict__ d, const double* __restrict__ e2,
+                                 const float* __restrict__ fd, const float* __restrict__ fe2,
+                                 int j, bool active, const TriBounds& b) {
+  // 1. FP32 bisection
+  float flo = __double2float_rd(b.lo), fhi = __double2float_ru(b.hi);
+  const float ftol = (float)(b.tnorm * 0x1p-21);
+  for (int it = 0; it < 64; ++it) {
+    const float x = 0.5f * (flo + fhi);
+    const bool done = !active || fhi - flo <= ftol || x <= flo || x >= fhi;
+    if (__all_sync(0xffffffffu, done)) break;
+    if (done) continue;
+    if (sweep32(n, fd, fe2, x) > j) fhi = x;
+    else flo = x;
+  }
+  // 2. widened bracket, checked in FP64
+  const double wid = b.tnorm * 0x1p-16;
+  double lo = fmax(b.lo, (double)flo - wid), hi = fmin(b.hi, (double)fhi + wid);
+  double flm = 0.0, fhm = 0.0;
+  int fle = 0, fhe = 0, clo = 0, chi = n;
+  bool kl = false, kh = false;
+  if (active) {
+    clo = sweep64(n, d, e2, lo, flm, fle);
+    chi = sweep64(n, d, e2, hi, fhm, fhe);
+    kl = kh = true;
+    if (clo > j || chi <= j) {  // the FP32 stage missed: full interval
+      lo = b.lo;
+      hi = b.hi;
+      clo = 0;
+      chi = n;
+      kl = kh = false;
     }
   }
-  if (active && sub == 0) w[j] = 0.5 * (lo + hi);
-  if (gt == 0) scal[1] = fmax(fabs(bounds[0]), fabs(bounds[1]));
+  // 3. FP64 regula falsi (Illinois) / bisection
+  int last = 0, since = 0;
+  double wref = hi - lo;
+  for (int it = 0; it < 400; ++it) {
+    const double tol = 2.0 * 2.220446049250313e-16 * fmax(fabs(lo), fabs(hi)) + 4.0 * b.pivmin;
+    const bool done = !active || hi - lo <= tol;
+    if (__all_sync(0xffffffffu, done)) break;
+    if (done) continue;
+    double x = 0.5 * (lo + hi);
+    const bool iso = kl && kh && clo == j && chi == j + 1;  // only eigenvalue j inside
+    bool bis = !iso;
+    if (iso && since >= 3) {  // three interpolation steps must halve the bracket
+      if (hi - lo > 0.5 * wref) {
+        bis = true;
+      } else {
+        since = 0;
+        wref = hi - lo;
+      }
+    }
+    if (!bis) {
+      const int E = max(fle, fhe);
+      const double a = scalbn(flm, fle - E), c = scalbn(fhm, fhe - E);
+      double xr = lo + a / (a - c) * (hi - lo);
+      // a point at the converged end moves half a tolerance inside, so that the next count
+      // closes the bracket instead of leaving it to bisection
+      xr = fmin(fmax(xr, lo + 0.5 * tol), hi - 0.5 * tol);
+      if (xr > lo && xr < hi) x = xr;
+      else bis = true;
+    }
+    if (!(x > lo && x < hi)) {  // no representable point inside: the bracket is final
+      lo = hi = x;
+      continue;
+    }
+    if (bis) {
+      since = 0;
+      wref = 0.5 * (hi - lo);
+    } else {
+      ++since;
+    }
+    double fm;
+    int fe;
+    const int c = sweep64(n, d, e2, x, fm, fe);
+    if (c > j) {
+      hi = x;
+      chi = c;
+      fhm = fm;
+      fhe = fe;
+      kh = true;
+      if (last == 1) flm *= 0.5;  // Illinois: the stale end's value is halved
+      last = 1;
+    } else {
+      lo = x;
+      clo = c;
+      flm = fm;
+      fle = fe;
+      kl = true;
+      if (last == -1) fhm *= 0.5;
+      last = -1;
+    }
+  }
+  return 0.5 * (lo + hi);
 }
-__global__ void __launch_bounds__(64) k_multisect(int n, const double* __restrict__ d,
-                                                  const double* __restrict__ e, double* w,
-                                                  double* scal) {
-  multisect_dev(n, d, e, w, scal);
+
+// TRI_SENTINEL stands for eigenvalues above the computed range: (e - ef)/kT >= 50 for any
+// Fermi level, so their occupation is exactly zero
+constexpr double TRI_SENTINEL = 1e300;
+
+// one-molecule path, stage 0: e^2, FP32 copies and the Gershgorin data into scratch
+//   ws layout: e2[n] (double), then fd[n], fe2[n] (float)
+__global__ void k_tri_prep(int n, const double* __restrict__ d, const double* __restrict__ e,
+                           double* ws, double* scal) {
+  float* fd = reinterpret_cast<float*>(ws + n);
+  float* fe2 = fd + n;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double ee = i < n - 1 ? e[i] * e[i] : 0.0;
+    ws[i] = ee;
+    fd[i] = (float)d[i];
+    fe2[i] = (float)ee;
+  }
+  if (blockIdx.x == 0) {
+    const TriBounds b = tri_bounds(n, d, e);
+    if (threadIdx.x == 0) {
+      scal[1] = b.tnorm;  // |T| estimate for the inverse iteration
+      scal[2] = b.lo;
+      scal[3] = b.hi;
+      scal[4] = b.pivmin;
+    }
+  }
+}
+// one-molecule path: eigenvalues j0 <= j < j1; with fill, w[j1 .. n) = TRI_SENTINEL
+__global__ void __launch_bounds__(32) k_eigvals(int n, int j0, int j1, int fill,
+                                                 const double* __restrict__ d,
+                                                 const double* __restrict__ ws,
+                                                 const double* __restrict__ scal, double* w) {
+  const int j = j0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if ((int)(blockIdx.x * blockDim.x) + j0 >= n) return;  // whole warp beyond n
+  const float* fd = reinterpret_cast<const float*>(ws + n);
+  const float* fe2 = fd + n;
+  TriBounds b;
+  b.tnorm = scal[1];
+  b.lo = scal[2];
+  b.hi = scal[3];
+  b.pivmin = scal[4];
+  const bool active = j < j1;
+  const double v = tri_eigenvalue(n, d, ws, fd, fe2, j, active, b);
+  if (active) w[j] = v;
+  else if (fill && j < n) w[j] = TRI_SENTINEL;
 }
 
 // ------------------------------------------------------------------------------------------
@@ -753,6 +894,7 @@ EigenSolver* eigen_create(int n, cudaStream_t s) {
   ck(cudaMalloc(&e->tau, sizeof(double) * (n + 1)), "tau");
   ck(cudaMalloc(&e->w, sizeof(double) * (n + 1)), "w");
   ck(cudaMalloc(&e->pv, sizeof(double) * 4 * (n + 1)), "pv");
+  ck(cudaMalloc(&e->tw, sizeof(double) * 2 * (n + 1)), "tw");
   ck(cudaMalloc(&e->scal, sizeof(double) * 8), "scal");
   ck(cudaMalloc(&e->status, sizeof(int)), "status");
   ck(cudaMallocHost(&e->hstatus, sizeof(int)), "hstatus");
@@ -774,7 +916,8 @@ EigenSolver* eigen_create(int n, cudaStream_t s) {
 
 void eigen_destroy(EigenSolver* e) {
   if (!e) return;
-  for (double* p : {e->L, e->X, e->A, e->T1, e->Y, e->lu, e->d, e->e, e->tau, e->w, e->pv, e->scal})
+  for (double* p : {e->L, e->X, e->A, e->T1, e->Y, e->lu, e->d, e->e, e->tau, e->w, e->pv, e->tw,
+                    e->scal})
     cudaFree(p);
   cudaFree(e->status);
   cudaFreeHost(e->hstatus);
@@ -790,7 +933,7 @@ int eigen_set_overlap(EigenSolver* e, const double* S) {
   return cholesky_inverse(n, e->L, e->X, e->status, e->hstatus, e->stream);
 }
 
-int eigen_values(EigenSolver* es, const double* F, double* w_out) {
+int eigen_values(EigenSolver* es, const double* F, double* w_out, int nev) {
   const int n = es->n;
   cudaStream_t s = es->stream;
   // A = X^T (F X): X upper triangular
@@ -822,12 +965,28 @@ int eigen_values(EigenSolver* es, const double* F, double* w_out) {
       prof_kend(KS_TRIDIAG, tk, s);
     }
   }
-  ++g_kernel_launches;
+  if (nev <= 0 || nev > n) nev = n;
+  g_kernel_launches += 2;
   const int tm = prof_kbegin(s);
-  k_multisect<<<(4 * n + 63) / 64, 64, 0, s>>>(n, es->d, es->e, es->w, es->scal);
+  k_tri_prep<<<(n + 255) / 256, 256, 0, s>>>(n, es->d, es->e, es->tw, es->scal);
+  // one warp per block: the warps of a single molecule spread over as many SMs as possible
+  k_eigvals<<<(n + 31) / 32, 32, 0, s>>>(n, 0, nev, 1, es->d, es->tw, es->scal, es->w);
   prof_kend(KS_MULTISECT, tm, s);
   ck(cudaMemcpyAsync(w_out, es->w, sizeof(double) * n, cudaMemcpyDeviceToDevice, s), "w");
   return 0;
+}
+
+void eigen_values_rest(EigenSolver* es, int nev, double* w_out) {
+  const int n = es->n;
+  if (nev >= n) return;
+  cudaStream_t s = es->stream;
+  g_kernel_launches += 2;
+  const int tm = prof_kbegin(s);
+  k_tri_prep<<<(n + 255) / 256, 256, 0, s>>>(n, es->d, es->e, es->tw, es->scal);
+  k_eigvals<<<(n - nev + 31) / 32, 32, 0, s>>>(n, nev, n, 0, es->d, es->tw, es->scal, es->w);
+  prof_kend(KS_MULTISECT, tm, s);
+  ck(cudaMemcpyAsync(w_out + nev, es->w + nev, sizeof(double) * (n - nev), cudaMemcpyDeviceToDevice, s),
+     "w");
 }
 
 void eigen_vectors_range(EigenSolver* es, int k0, int k1, double* C) {
@@ -895,8 +1054,9 @@ __global__ void __launch_bounds__(256) kb_tridiag(BARGS) {
 // Small molecules (the whole n x n matrix in one CTA's shared memory): the same Householder
 // reduction with everything on chip.  Per column: warp 0 builds the reflector (no block
 // reduction), the warps form p = t A22 v column by column, every warp reduces K = -t/2 p.v
-// for itself, and all threads apply the symmetric rank-2 update as one 2-d loop over the
-// trailing block.  Three block barriers per column.  The reflectors and the diagonal go to
+// for itself, w = p + K v is formed once per row, and all threads apply the symmetric rank-2
+// update (two FMAs per element) as one 2-d loop over the trailing block.  Five block barriers
+// per column.  The reflectors and the diagonal go to
 // global memory at the end in the layout the back-transformation reads (column-major A,
 // v below the subdiagonal).
 constexpr int TRI_SMALL_MAX = 156;  // (n^2 + 2n) doubles <= 200 KB
@@ -951,15 +1111,19 @@ __global__ void __launch_bounds__(256) kb_tridiag_small(BARGS) {
         if (lane == 0) sp[j] = acc;
       }
       __syncthreads();
-      // K = -1/2 t (p . v), each warp for itself; then w = p + K v is formed on the fly
+      // K = -1/2 t (p . v), each warp for itself
       double kk = 0.0;
       for (int r = r0 + lane; r < n; r += 32) kk += sp[r] * sv[r];
       const double K = -0.5 * t * wred(kk);
+      __syncthreads();  // every warp has read p
+      // w = p + K v once per row, then two FMAs per element: A -= v w^T + w v^T
+      for (int r = r0 + tid; r < n; r += blockDim.x) sp[r] = fma(K, sv[r], sp[r]);
+      __syncthreads();
       const int m = n - r0;
       for (int e2 = tid; e2 < m * m; e2 += blockDim.x) {
         const int c = r0 + e2 / m, r = r0 + e2 % m;
-        const double vr = sv[r], vc = sv[c];
-        a[(size_t)c * n + r] -= vr * (sp[c] + K * vc) + (sp[r] + K * vr) * vc;
+        double* el = a + (size_t)c * n + r;
+        *el = fma(-sv[r], sp[c], fma(-sp[r], sv[c], *el));
       }
     }
     __syncthreads();
@@ -970,75 +1134,34 @@ __global__ void __launch_bounds__(256) kb_tridiag_small(BARGS) {
   for (int t2 = tid; t2 < n * n; t2 += blockDim.x) Ag[t2] = a[t2];
 }
 
-// Eigenvalues for the batch: plain bisection, one thread per eigenvalue.  With thousands of
-// molecules the GPU is throughput bound, and bisection gains one bit per Sturm sequence
-// against the multisection's 2.3 bits per four sequences.  d and e^2 of the molecule are
-// staged in shared memory (every thread reads the same element at the same step).  Same
-// bracket, Sturm recurrence and stopping rule as the multisection.
+// Eigenvalues for the batch, one thread per eigenvalue (tri_eigenvalue: FP32 bisection, FP64
+// check, FP64 Illinois / bisection).  d, e^2 and their FP32 copies are staged in shared memory
+// (every thread reads the same element at the same step).  rest = 0: eigenvalues j < nev and
+// the sentinel above them; rest = 1 (after the SCF): the eigenvalues nev <= j < n.
 constexpr int BIS_MAXN = 448;
-__global__ void __launch_bounds__(128) kb_bisect(BARGS) {
+__global__ void __launch_bounds__(128) kb_eigvals(BARGS, int rest) {
   BMOL;
   const int n = q.m.nao;
-  if ((int)blockIdx.x * (int)blockDim.x >= n) return;
+  const int j0 = rest ? q.nev : 0, j1 = rest ? n : q.nev;
+  if ((int)blockIdx.x * (int)blockDim.x + j0 >= n) return;
   __shared__ double sd[BIS_MAXN], se2[BIS_MAXN];
-  __shared__ double bounds[3];
+  __shared__ float fd[BIS_MAXN], fe2[BIS_MAXN];
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double ee = i < n - 1 ? q.ee[i] * q.ee[i] : 0.0;
     sd[i] = q.ed[i];
-    se2[i] = i < n - 1 ? q.ee[i] * q.ee[i] : 0.0;
+    se2[i] = ee;
+    fd[i] = (float)q.ed[i];
+    fe2[i] = (float)ee;
   }
-  if (threadIdx.x == 0) {
-    double lo = 1e300, hi = -1e300, emax = 0.0;
-    for (int i = 0; i < n; ++i) {
-      const double r = (i > 0 ? fabs(q.ee[i - 1]) : 0.0) + (i < n - 1 ? fabs(q.ee[i]) : 0.0);
-      lo = fmin(lo, q.ed[i] - r);
-      hi = fmax(hi, q.ed[i] + r);
-      if (i < n - 1) emax = fmax(emax, q.ee[i] * q.ee[i]);
-    }
-    const double tnorm = fmax(fabs(lo), fabs(hi));
-    bounds[0] = lo - 8.9e-16 * tnorm - 1e-300;
-    bounds[1] = hi + 8.9e-16 * tnorm + 1e-300;
-    bounds[2] = fmax(2.2250738585072014e-308 * fmax(1.0, emax), 1e-300);
-    if (blockIdx.x == 0) q.escal[1] = fmax(fabs(bounds[0]), fabs(bounds[1]));
-  }
-  __syncthreads();
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool active = j < n;
-  double lo = bounds[0], hi = bounds[1];
-  const double pivmin = bounds[2];
-  for (int it = 0; it < 128; ++it) {
-    const bool done =
-        !active || hi - lo <= 2.0 * 2.220446049250313e-16 * fmax(fabs(lo), fabs(hi)) + 4.0 * pivmin;
-    if (__all_sync(0xffffffffu, done)) break;
-    if (done) continue;
-    const double x = 0.5 * (lo + hi);
-    double p0 = 1.0, p1 = sd[0] - x;
-    if (p1 == 0.0) p1 = -0x1p-900;
-    int cnt = p1 < 0.0;
-    for (int i = 1; i < n; ++i) {
-      double p2 = fma(sd[i] - x, p1, -se2[i - 1] * p0);
-      if (p2 == 0.0) p2 = -copysign(0x1p-900, p1);
-      cnt += (p2 < 0.0) != (p1 < 0.0);
-      p0 = p1;
-      p1 = p2;
-      if ((i & 7) == 0) {
-        const double a = fabs(p1);
-        if (a > 0x1p400 || a < 0x1p-400) {
-          const int ex = ilogb(a);
-          p1 = scalbn(p1, -ex);
-          p0 = scalbn(p0, -ex);
-        }
-      }
-    }
-    if (cnt > j) hi = x;
-    else lo = x;
-  }
-  if (active) q.emo[j] = 0.5 * (lo + hi);
+  const TriBounds b = tri_bounds(n, q.ed, q.ee);  // ends with a block barrier
+  if (blockIdx.x == 0 && threadIdx.x == 0 && !rest) q.escal[1] = b.tnorm;
+  const int j = j0 + blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = j < j1;
+  const double v = tri_eigenvalue(n, sd, se2, fd, fe2, j, active, b);
+  if (active) q.emo[j] = v;
+  else if (!rest && j < n) q.emo[j] = TRI_SENTINEL;
 }
 
-__global__ void __launch_bounds__(64) kb_multisect(BARGS) {
-  BMOL;
-  multisect_dev(q.m.nao, q.ed, q.ee, q.emo, q.escal);
-}
 __global__ void kb_invit(BARGS) {
   BMOL;
   invit_dev(q.m.nao, 0, *q.icount, q.ed, q.ee, q.emo, q.escal, q.lu, q.Y);
@@ -1110,11 +1233,15 @@ void eigen_values_b(const BatchLaunch& b) {
   }
   ++g_kernel_launches;
   const int tm = prof_kbegin(b.s);
-  if (b.nao_max <= BIS_MAXN)
-    kb_bisect<<<dim3((b.nao_max + 127) / 128, 1, b.count), 128, 0, b.s>>>(b.mp, b.list);
-  else
-    kb_multisect<<<dim3((4 * b.nao_max + 63) / 64, 1, b.count), 64, 0, b.s>>>(b.mp, b.list);
+  if (b.nao_max > BIS_MAXN) throw std::runtime_error("batched eigenvalues: molecule too large");
+  kb_eigvals<<<dim3((b.nao_max + 127) / 128, 1, b.count), 128, 0, b.s>>>(b.mp, b.list, 0);
   prof_kend(KS_MULTISECT, tm, b.s);
+}
+
+void eigen_values_rest_b(const BatchLaunch& b) {
+  if (!b.count) return;
+  ++g_kernel_launches;
+  kb_eigvals<<<dim3((b.nao_max + 127) / 128, 1, b.count), 128, 0, b.s>>>(b.mp, b.list, 1);
 }
 
 static void tridiag_cluster_b(const BatchLaunch& b) {

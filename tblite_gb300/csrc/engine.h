@@ -197,8 +197,10 @@ void launch_mulliken(const DevMol& m, const double* P, const double* S, const do
 int mulliken_chunks(int n);
 
 // Fermi filling of both spin channels; writes focc (alpha+beta), ts (entropy term) to scal[0]
+// nocc_cols[0]: orbitals with non-zero occupation; nocc_cols[1] = 1 when the nev computed
+// eigenvalues do not reach 51 kT above the Fermi level (all n are then needed)
 void launch_fermi(int n, const double* emo, double nalp, double nbet, double kt, double* focc,
-                  double* ts, int* nocc_cols, cudaStream_t s);
+                  double* ts, int* nocc_cols, cudaStream_t s, int nev = 0);
 
 // Broyden mixer (reference scf/mixer/broyden.f90)
 struct BroydenState {
@@ -227,8 +229,17 @@ int eigen_capacity(const EigenSolver*);
 void eigen_resize(EigenSolver*, int n);
 // factorise S once per geometry; returns 0 on success, >0 if S is not positive definite
 int eigen_set_overlap(EigenSolver*, const double* S);
-// all eigenvalues (ascending) of F C = S C e; keeps the tridiagonal form for eigen_vectors
-int eigen_values(EigenSolver*, const double* F, double* e);
+// eigenvalues (ascending) of F C = S C e; keeps the tridiagonal form for eigen_vectors.
+// Only the nev lowest are computed (nev <= 0: all); e[nev..n) = 1e300, which the Fermi
+// filling treats as empty.  eigen_values_rest fills in e[nev..n) from the kept form.
+int eigen_values(EigenSolver*, const double* F, double* e, int nev = 0);
+void eigen_values_rest(EigenSolver*, int nev, double* e);
+// eigenvalues needed during the SCF: all occupied levels, the first empty one and a margin
+inline int scf_eigenvalue_count(int n, double nalp) {
+  const int occ = (int)nalp + 1;  // ceil(nalp) or more
+  const int m = occ + 1 + (n / 64 > 4 ? n / 64 : 4);
+  return m < n ? m : n;
+}
 // the k lowest eigenvectors, C column-major [k][n] (S-orthonormal)
 void eigen_vectors(EigenSolver*, int k, double* C);
 // eigenvectors k0 .. k1-1 into columns k0 .. k1-1 of C (same tridiagonal form)
@@ -267,6 +278,7 @@ struct MolPtrs {
   D4Work d4w;
   DevD3 d3;
   int has_d4, nd, mull_chunks, memory, with_mp, has_d3;
+  int nev;  // eigenvalues computed per SCF iteration (the rest after convergence)
   double nalp, nbet, kt, damp, econv, pconv;
   double h0_cutoff;  // depends on the basis of the molecule (smallest exponent)
   double *cn, *se, *mrad, *dmrdcn;
@@ -331,6 +343,7 @@ void gemm_b(const BatchLaunch& b, int site);
 // eigensolver steps for a bucket
 void cholesky_inverse_b(const BatchLaunch& b);          // S -> X (status into flag)
 void eigen_values_b(const BatchLaunch& b);              // F -> emo (tridiagonal form kept)
+void eigen_values_rest_b(const BatchLaunch& b);         // emo[nev..n) after convergence
 void eigen_vectors_b(const BatchLaunch& b);             // icount lowest vectors into C
 void density_b(const BatchLaunch& b, bool weighted);   // P (or W into F) from C, focc (, emo)
 

@@ -719,8 +719,10 @@ __device__ double block_sum(double v, double* red) {
   return r;
 }
 
-__device__ void fermi_channel(int n, const double* emo, double nel, double kt, double* occ,
-                              double* red, double* ts) {
+// returns the highest Fermi level at which occupations were evaluated (-1e300 if none)
+__device__ double fermi_channel(int n, const double* emo, double nel, double kt, double* occ,
+                                double* red, double* ts) {
+  double ef_max = -1e300;
   // Aufbau
   int homo = (int)floor(nel);
   const double frac = fmod(nel, 1.0);
@@ -734,6 +736,7 @@ __device__ void fermi_channel(int n, const double* emo, double nel, double kt, d
     const double thr = 1.4901161193847656e-08;      // sqrt(epsilon)
     const double sqrttiny = 1.4916681462400413e-154;  // sqrt(tiny)
     for (int cyc = 0; cyc < 200; ++cyc) {
+      ef_max = fmax(ef_max, ef);
       double tn = 0.0, td = 0.0;
       for (int k = threadIdx.x; k < n; k += blockDim.x) {
         const double x = (emo[k] - ef) / kt;
@@ -763,15 +766,21 @@ __device__ void fermi_channel(int n, const double* emo, double nel, double kt, d
   s = block_sum(s, red);
   if (threadIdx.x == 0) *ts += s * kt;
   __syncthreads();
+  return ef_max;
 }
 
+// emo[nev..n) may be placeholders (1e300) for levels that were not computed: valid as long as
+// the highest computed level lies 51 kT above every Fermi level used (the occupation is then
+// exactly zero above it, as for the true levels); otherwise ncols[1] = 1
 __device__ __forceinline__ void fermi_dev(int n, const double* emo, double nalp, double nbet, double kt, double* fa,
-                        double* fb, double* focc, double* ts, int* ncols) {
+                        double* fb, double* focc, double* ts, int* ncols, int nev) {
   __shared__ double red[32];
   if (threadIdx.x == 0) *ts = 0.0;
   __syncthreads();
-  fermi_channel(n, emo, nalp, kt, fa, red, ts);
-  fermi_channel(n, emo, nbet, kt, fb, red, ts);
+  const double efa = fermi_channel(n, emo, nalp, kt, fa, red, ts);
+  const double efb = fermi_channel(n, emo, nbet, kt, fb, red, ts);
+  if (threadIdx.x == 0)
+    ncols[1] = (nev < n && !(emo[nev - 1] >= fmax(efa, efb) + 51.0 * kt)) ? 1 : 0;
   int last = -1;
   for (int k = threadIdx.x; k < n; k += blockDim.x) {
     const double f = fa[k] + fb[k];
@@ -787,15 +796,16 @@ __device__ __forceinline__ void fermi_dev(int n, const double* emo, double nalp,
   if (threadIdx.x == 0) *ncols = mx + 1;
 }
 __global__ void k_fermi(int n, const double* emo, double nalp, double nbet, double kt, double* fa,
-                        double* fb, double* focc, double* ts, int* ncols) {
-  fermi_dev(n, emo, nalp, nbet, kt, fa, fb, focc, ts, ncols);
+                        double* fb, double* focc, double* ts, int* ncols, int nev) {
+  fermi_dev(n, emo, nalp, nbet, kt, fa, fb, focc, ts, ncols, nev);
 }
 
 void launch_fermi(int n, const double* emo, double nalp, double nbet, double kt, double* focc,
-                  double* ts, int* ncols, cudaStream_t s) {
+                  double* ts, int* ncols, cudaStream_t s, int nev) {
   // fa, fb scratch follow focc in memory: focc[n], fa[n], fb[n]
   ++g_kernel_launches;
-  k_fermi<<<1, 1024, 0, s>>>(n, emo, nalp, nbet, kt, focc + n, focc + 2 * n, focc, ts, ncols);
+  k_fermi<<<1, 1024, 0, s>>>(n, emo, nalp, nbet, kt, focc + n, focc + 2 * n, focc, ts, ncols,
+                             nev > 0 ? nev : n);
 }
 
 // ------------------------------------------------------------------------------------
@@ -1267,7 +1277,10 @@ void launch_mulliken_b(const BatchLaunch& b) {
 __global__ void kb_fermi(BARGS) {
   BMOL;
   const int n = q.m.nao;
-  fermi_dev(n, q.emo, q.nalp, q.nbet, q.kt, q.focc + n, q.focc + 2 * n, q.focc, q.scal, q.icount);
+  fermi_dev(n, q.emo, q.nalp, q.nbet, q.kt, q.focc + n, q.focc + 2 * n, q.focc, q.scal, q.icount,
+            q.nev);
+  // too few levels computed for this Fermi level: the molecule leaves for the one-molecule path
+  if (threadIdx.x == 0 && q.icount[1] != 0) *q.flag = -3;
 }
 void launch_fermi_b(const BatchLaunch& b) {
   if (!b.count) return;
