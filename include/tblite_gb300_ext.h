@@ -42,8 +42,10 @@ int tblite_gb300_batch_last_fallbacks(void);
  * of the gradient, summed over its memory chunks (uploads, read-back and the one-molecule
  * path excluded) */
 double tblite_gb300_batch_last_device_ms(void);
-/* SCF iterations of each molecule of the last batch call (0 for molecules that took the
- * one-molecule path); returns the number of molecules of that call */
+/* SCF iterations of each molecule of the last batch call; 0 for molecules routed to the
+ * one-molecule path up front, a negative code for molecules that left the batch (-1 singular
+ * Broyden system, -2 overlap not positive definite, -3 Fermi level above the eigenvalues the
+ * batch computes, -4 iteration limit or Broyden history); returns the number of molecules */
 int tblite_gb300_batch_last_iterations(int* iterations, int nmol);
 
 /* enable (1) or disable (0) event timing for subsequent single points (process wide) */

@@ -630,10 +630,17 @@ std::vector<int> run_chunk(std::vector<Plan>& plans, Arena& ar, _tblite_context*
   stream_wait(s);
   cuda_check(cudaGetLastError(), "batch setup");
   std::vector<int> leave;
+  // why a molecule left the batch (recorded as a negative iteration count): -2 overlap not
+  // positive definite, -1 singular Broyden system, -3 Fermi level above the computed levels,
+  // -4 iteration limit or Broyden history
+  auto record_leave = [&](int i, int code) {
+    leave.push_back(i);
+    if (plans[i].idx < (int)g_last_iters.size()) g_last_iters[plans[i].idx] = code;
+  };
   for (int i = 0; i < np; ++i)
     if (h_flag[i] < 0) {
       active[i] = 0;
-      leave.push_back(i);
+      record_leave(i, h_flag[i]);
     }
   std::vector<char> done(np, 0);
   int max_iter = 0;
@@ -681,7 +688,7 @@ std::vector<int> run_chunk(std::vector<Plan>& plans, Arena& ar, _tblite_context*
       } else if (h_flag[i] < 0 || iscf >= pl.max_iter ||
                  (iscf > HCAP && pl.memory > HCAP)) {
         active[i] = 0;
-        leave.push_back(i);
+        record_leave(i, h_flag[i] < 0 ? h_flag[i] : -4);
       }
     }
     const int nbefore = nactive;
@@ -697,7 +704,7 @@ std::vector<int> run_chunk(std::vector<Plan>& plans, Arena& ar, _tblite_context*
     }
   }
   for (int i = 0; i < np; ++i)
-    if (active[i]) leave.push_back(i);
+    if (active[i]) record_leave(i, -4);
   float scf_ms = 0.f;
 
   // gradient of the converged molecules: Coulomb and D4 at the output moments, W into F,

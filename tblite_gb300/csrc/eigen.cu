@@ -938,7 +938,7 @@ int eigen_values(EigenSolver* es, const double* F, double* w_out, int nev) {
   cudaStream_t s = es->stream;
   // A = X^T (F X): X upper triangular
   gemm64(false, false, n, n, n, 1.0, F, n, es->X, n, 0.0, es->T1, n, KM_LT_COLEND, s);
-  gemm64(true, false, n, n, n, 1.0, es->X, n, es->T1, n, 0.0, es->A, n, KM_LT_ROWEND, s);
+  gemm64(true, false, n, n, n, 1.0, es->X, n, es->T1, n, 0.0, es->A, n, KM_LT_ROWEND | KM_SYM, s);
   // tridiagonalise
   {
     int nn = n;
@@ -1032,7 +1032,7 @@ void density_matrix(int n, int k, const double* C, const double* f, double* P, d
   const size_t tot = (size_t)n * k;
   ++g_kernel_launches;
   k_scale_cols<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(n, k, C, f, work);
-  gemm64(false, true, n, n, k, 1.0, work, n, C, n, 0.0, P, n, KM_NONE, s);
+  gemm64(false, true, n, n, k, 1.0, work, n, C, n, 0.0, P, n, KM_NONE | KM_SYM, s);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -1044,12 +1044,140 @@ void density_matrix(int n, int k, const double* C, const double* f, double* P, d
 #define BMOL const MolPtrs& q = mp[list[blockIdx.z]]
 #define BARGS const MolPtrs* __restrict__ mp, const int* __restrict__ list
 
+// Householder tridiagonalisation of one molecule per thread-block cluster, lower-triangle
+// storage.  Column j lives in CTA j % nb of the cluster, packed (rows j .. n-1 only), so the
+// cluster holds n^2/2 doubles instead of n^2 and each element costs four FMAs per step
+// instead of six:
+//   p = A v   a column's dot product covers its rows r >= c; the rows above the diagonal are
+//             the same elements seen from their own columns, so every CTA also scatters
+//             A(r, c) v_c into a partial vector (one thread per row, no atomics), and each CTA
+//             sums the nb partial vectors through distributed shared memory;
+//   A -= v w^T + w v^T on the stored lower part only, w = t p + K v formed once per row.
+// Two cluster barriers per column, as in the full-storage form; v and tau of a step are read
+// from the owner CTA's shared memory.  The reflectors also go to global A (column-major, below
+// the subdiagonal) for the back-transformation.
+__device__ __forceinline__ size_t sym_off(int s, int n, int b, int nb) {
+  return (size_t)s * n - (size_t)s * b - (size_t)nb * s * (s - 1) / 2;
+}
+__host__ __device__ inline size_t sym_tridiag_doubles(int n, int nb) {
+  const size_t ncpb = (size_t)(n + nb - 1) / nb;  // CTA 0 owns the most columns
+  return ncpb * n - (size_t)nb * ncpb * (ncpb - 1) / 2 + 4 * (size_t)n + 1;
+}
 __global__ void __launch_bounds__(256) kb_tridiag(BARGS) {
   cg::cluster_group cl = cg::this_cluster();
   BMOL;
   const int n = q.m.nao;
-  tridiag_smem_body(n, q.A, q.ed, q.ee, q.etau, q.epv, q.epv + (n + 1), (int)cl.num_blocks(),
-                    (int)cl.block_rank(), [&] { cl.sync(); });
+  const int nb = (int)cl.num_blocks(), b = (int)cl.block_rank();
+  double* Ag = q.A;
+  double* d = q.ed;
+  double* e = q.ee;
+  double* tau = q.etau;
+  extern __shared__ double sm[];
+  const int ncpb = b < n ? (n - b + nb - 1) / nb : 0;
+  // the vectors first: other CTAs address spart and svpub at the same offset in their view
+  double* sv = sm;             // [n] v of the current step
+  double* sw = sv + n;         // [n] w = t p + K v
+  double* spart = sw + n;      // [n] this CTA's part of p (read by the others)
+  double* svpub = spart + n;   // [n + 1] v and tau published by the owner
+  double* scol = svpub + n + 1;  // packed columns (their total differs between CTAs)
+  __shared__ double red[32];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nwb = blockDim.x >> 5;
+  for (int s = 0; s < ncpb; ++s) {
+    const int j = b + s * nb;
+    double* col = scol + sym_off(s, n, b, nb) - j;
+    for (int r = j + tid; r < n; r += blockDim.x) col[r] = Ag[r + (size_t)j * n];
+  }
+  __syncthreads();
+  auto column = [&](int s) { return scol + sym_off(s, n, b, nb) - (b + s * nb); };  // col[r], r >= c
+  // owner of column i builds reflector i from its stored column and publishes v, tau
+  auto reflector = [&](int i) {
+    double* col = column(i / nb);
+    const double alpha = col[i + 1];
+    double ss = 0.0;
+    for (int r = i + 2 + tid; r < n; r += blockDim.x) ss += col[r] * col[r];
+    ss = block_sum256(ss, red);
+    double t = 0.0, beta = alpha;
+    if (ss > 0.0) {
+      beta = -copysign(sqrt(alpha * alpha + ss), alpha);
+      t = (beta - alpha) / beta;
+    }
+    const double sc = ss > 0.0 ? 1.0 / (alpha - beta) : 0.0;
+    for (int r = i + 2 + tid; r < n; r += blockDim.x) {
+      const double v = col[r] * sc;
+      col[r] = v;
+      svpub[r] = v;
+      Ag[r + (size_t)i * n] = v;
+    }
+    if (tid == 0) {
+      svpub[i + 1] = 1.0;
+      svpub[n] = t;
+      tau[i] = t;
+      e[i] = beta;
+      d[i] = col[i];
+    }
+  };
+  if (n == 1 && b == 0 && tid == 0) d[0] = scol[0];
+  if (n > 1 && b == 0) reflector(0);
+  cl.sync();
+  for (int i = 0; i < n - 1; ++i) {
+    // v_i and tau_i from the owner of column i
+    const double* pv = cl.map_shared_rank(svpub, i % nb);
+    for (int r = i + 1 + tid; r < n; r += blockDim.x) sv[r] = pv[r];
+    const double t = pv[n];
+    const int s0 = i < b ? 0 : (i - b) / nb + 1;  // first owned column > i
+    if (t != 0.0) {
+      __syncthreads();
+      // rows above the diagonal, from the owned columns c < r: spart_r = sum A(r, c) v_c
+      for (int r = i + 1 + tid; r < n; r += blockDim.x) {
+        double acc = 0.0;
+        for (int s2 = s0; s2 < ncpb; ++s2) {
+          const int c = b + s2 * nb;
+          if (c >= r) break;
+          acc = fma(scol[sym_off(s2, n, b, nb) + (r - c)], sv[c], acc);
+        }
+        spart[r] = acc;
+      }
+      __syncthreads();
+      // stored part of the owned columns: spart_c += sum_{r >= c} A(r, c) v_r (warp per column)
+      for (int s2 = s0 + wid; s2 < ncpb; s2 += nwb) {
+        const int c = b + s2 * nb;
+        const double* col = column(s2);
+        double acc = 0.0;
+        for (int r = c + lane; r < n; r += 32) acc = fma(col[r], sv[r], acc);
+        acc = wred(acc);
+        if (lane == 0) spart[c] += acc;
+      }
+    }
+    cl.sync();
+    if (t != 0.0) {
+      // p = t * (sum of the nb partial vectors), K = -t/2 p.v (same order in every CTA)
+      double kk = 0.0;
+      for (int r = i + 1 + tid; r < n; r += blockDim.x) {
+        double p = 0.0;
+        for (int q2 = 0; q2 < nb; ++q2) p += cl.map_shared_rank(spart, q2)[r];
+        p *= t;
+        sw[r] = p;
+        kk = fma(p, sv[r], kk);
+      }
+      kk = block_sum256(kk, red);
+      const double K = -0.5 * t * kk;
+      for (int r = i + 1 + tid; r < n; r += blockDim.x) sw[r] = fma(K, sv[r], sw[r]);
+      __syncthreads();
+      for (int s2 = s0; s2 < ncpb; ++s2) {
+        const int c = b + s2 * nb;
+        double* col = column(s2);
+        const double vc = sv[c], wc = sw[c];
+        for (int r = c + tid; r < n; r += blockDim.x)
+          col[r] = fma(-sv[r], wc, fma(-sw[r], vc, col[r]));
+      }
+    }
+    __syncthreads();
+    if ((i + 1) % nb == b) {
+      if (i + 1 < n - 1) reflector(i + 1);
+      else if (tid == 0) d[n - 1] = column((n - 1) / nb)[n - 1];
+    }
+    cl.sync();
+  }
 }
 // Small molecules (the whole n x n matrix in one CTA's shared memory): the same Householder
 // reduction with everything on chip.  Per column: warp 0 builds the reflector (no block
@@ -1138,7 +1266,7 @@ __global__ void __launch_bounds__(256) kb_tridiag_small(BARGS) {
 // check, FP64 Illinois / bisection).  d, e^2 and their FP32 copies are staged in shared memory
 // (every thread reads the same element at the same step).  rest = 0: eigenvalues j < nev and
 // the sentinel above them; rest = 1 (after the SCF): the eigenvalues nev <= j < n.
-constexpr int BIS_MAXN = 448;
+constexpr int BIS_MAXN = 1024;
 __global__ void __launch_bounds__(128) kb_eigvals(BARGS, int rest) {
   BMOL;
   const int n = q.m.nao;
@@ -1181,11 +1309,10 @@ __global__ void kb_scale_cols(BARGS, int weighted) {
   scale_cols_dev(q.m.nao, *q.icount, q.C, weighted ? q.vec_out : q.focc, q.scratch);
 }
 
-// smallest cluster (1, 2, 4, 8 blocks) whose shared memory holds the n x n matrix
+// smallest cluster (1, 2, 4, 8 blocks) whose shared memory holds the lower triangle
 static int tridiag_cluster(int n, size_t* smem) {
   for (int nb = 1; nb <= 8; nb *= 2) {
-    const size_t ncpb = (size_t)(n + nb - 1) / nb;
-    const size_t need = sizeof(double) * (ncpb * n + 2 * (size_t)n);
+    const size_t need = sizeof(double) * sym_tridiag_doubles(n, nb);
     if (need <= TRIDIAG_SMEM_MAX) {
       *smem = need;
       return nb;

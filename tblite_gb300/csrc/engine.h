@@ -246,7 +246,9 @@ void eigen_vectors(EigenSolver*, int k, double* C);
 void eigen_vectors_range(EigenSolver*, int k0, int k1, double* C);
 
 // dense FP64 GEMM (column-major, BLAS semantics); kmode skips zero triangles
-enum { KM_NONE = 0, KM_LT_COLEND = 1, KM_LT_ROWEND = 2, KM_GE_ROWBEG = 3 };
+// KM_SYM (or-ed with one of the others): the product is symmetric (M == N); only the tiles on
+// and below the diagonal are computed and each is also written to its mirror position
+enum { KM_NONE = 0, KM_LT_COLEND = 1, KM_LT_ROWEND = 2, KM_GE_ROWBEG = 3, KM_SYM = 8 };
 void gemm64(bool ta, bool tb, int M, int N, int K, double alpha, const double* A, int lda,
             const double* B, int ldb, double beta, double* C, int ldc, int kmode, cudaStream_t s);
 

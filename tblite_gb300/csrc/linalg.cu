@@ -21,6 +21,8 @@ namespace tb {
 //   KM_LT_COLEND   k <  column tile end   (op(B) upper triangular:  B(k,j) = 0 for k > j)
 //   KM_LT_ROWEND   k <  row tile end      (op(A) lower triangular:  A(i,k) = 0 for k > i)
 //   KM_GE_ROWBEG   k >= row tile begin    (op(A) upper triangular:  A(i,k) = 0 for k < i)
+// KM_SYM marks a symmetric product (M == N, square tiles): tiles above the diagonal are not
+// computed, the others are written twice (C(i,j) and C(j,i)), so C is exactly symmetric.
 // ------------------------------------------------------------------------------------------
 template <int BM, int BN, int BK, int TM, int TN>
 __device__ __forceinline__ void gemm_dev(int M, int N, int K, double alpha, const double* __restrict__ A, int lda, bool ta,
@@ -29,7 +31,11 @@ __device__ __forceinline__ void gemm_dev(int M, int N, int K, double alpha, cons
   constexpr int NT = (BM / TM) * (BN / TN);
   __shared__ double As[BK][BM + 1];
   __shared__ double Bs[BK][BN + 1];
+  static_assert(!(BM != BN), "square tiles");
   const int i0 = blockIdx.y * BM, j0 = blockIdx.x * BN;
+  const bool sym = (kmode & KM_SYM) != 0;
+  if (sym && i0 < j0) return;  // above the diagonal: written by the mirror tile
+  kmode &= 7;
   const int tid = threadIdx.x;
   const int tr = tid / (BN / TN), tc = tid % (BN / TN);
   int kbeg = 0, kend = K;
@@ -80,7 +86,9 @@ __device__ __forceinline__ void gemm_dev(int M, int N, int K, double alpha, cons
       const int gj = j0 + tc * TN + y;
       if (gj >= N) continue;
       double* c = C + gi + (size_t)gj * ldc;
-      *c = beta == 0.0 ? alpha * acc[x][y] : alpha * acc[x][y] + beta * *c;
+      const double v = beta == 0.0 ? alpha * acc[x][y] : alpha * acc[x][y] + beta * *c;
+      *c = v;
+      if (sym && i0 != j0) C[gj + (size_t)gi * ldc] = v;
     }
   }
 }
@@ -302,10 +310,10 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN)) kb_gemm(BARGS, int site
   bool ta = false, tb = false;
   switch (site) {
     case GS_FX: A = q.F; B = q.X; C = q.T1; km = KM_LT_COLEND; break;
-    case GS_XTT: A = q.X; ta = true; B = q.T1; C = q.A; km = KM_LT_ROWEND; break;
+    case GS_XTT: A = q.X; ta = true; B = q.T1; C = q.A; km = KM_LT_ROWEND | KM_SYM; break;
     case GS_XY: A = q.X; B = q.Y; C = q.C; N = k; km = KM_GE_ROWBEG; break;
-    case GS_DENS: A = q.scratch; B = q.C; tb = true; C = q.P; K = k; break;
-    default: A = q.scratch; B = q.C; tb = true; C = q.F; K = k; break;  // GS_WDENS
+    case GS_DENS: A = q.scratch; B = q.C; tb = true; C = q.P; K = k; km = KM_SYM; break;
+    default: A = q.scratch; B = q.C; tb = true; C = q.F; K = k; km = KM_SYM; break;  // GS_WDENS
   }
   if ((int)blockIdx.x * BN >= N || (int)blockIdx.y * BM >= M) return;  // tile outside
   gemm_dev<BM, BN, BK, TM, TN>(M, N, K, 1.0, A, n, ta, B, n, tb, 0.0, C, n, km);

@@ -85,7 +85,7 @@ extern "C" int tblite_gb300_density_matrix_noalloc(int n, int k, const double* C
     const size_t tot = (size_t)n * k;
     ++g_kernel_launches;
     k_scale_cols_fixed<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(n, k, C, f, work);
-    gemm64(false, true, n, n, k, 1.0, work, n, C, n, 0.0, P, n, KM_NONE, s);
+    gemm64(false, true, n, n, k, 1.0, work, n, C, n, 0.0, P, n, KM_SYM, s);
   }
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -3;
 }

@@ -125,3 +125,18 @@ def test_batch_mixed_methods():
         ref = gfn1.singlepoint(gfn1.new_calc(gfn2.Molecule(np.asarray(z), np.asarray(x))))
         assert abs(rb.get("energy") - ref.energy) <= E_TOL
         assert np.max(np.abs(rb.get("gradient") - ref.gradient)) <= G_TOL
+
+
+@pytest.mark.parametrize("method", ["GFN2-xTB", "GFN1-xTB"])
+def test_batch_large_molecules(method):
+    """Molecules above one CTA's shared memory (the cluster tridiagonalisation with packed
+    lower-triangle storage; GFN1 water 64-mers have 512 orbitals) against the plain path."""
+    from tblite_gb300 import workloads
+    from tblite_gb300.interface import batch_fallbacks, batch_singlepoint
+
+    mols = [workloads.water_cluster_k(40, seed=301), workloads.alkane(50, seed=302),
+            workloads.water_cluster_k(64, seed=303), workloads.alkane(30, seed=304)]
+    res_b = batch_singlepoint([_calc(z, x, method) for z, x in mols])
+    assert batch_fallbacks() == 0
+    for (z, x), rb in zip(mols, res_b):
+        _compare(rb, _calc(z, x, method).singlepoint())
