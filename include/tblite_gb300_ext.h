@@ -48,6 +48,10 @@ double tblite_gb300_batch_last_device_ms(void);
  * batch computes, -4 iteration limit or Broyden history); returns the number of molecules */
 int tblite_gb300_batch_last_iterations(int* iterations, int nmol);
 
+/* batched GEMMs of molecules with at least 128 orbitals on the BF16 tensor cores with
+ * FP64-accurate operand splitting (1, the default) or as FP64 tile GEMMs (0); process wide */
+void tblite_gb300_set_split_gemm(int enable);
+
 /* enable (1) or disable (0) event timing for subsequent single points (process wide) */
 void tblite_gb300_set_profiling(int enable);
 

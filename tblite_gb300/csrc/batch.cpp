@@ -901,6 +901,7 @@ extern "C" int tblite_gb300_batch_singlepoint(tblite_context ctx, int nmol,
 }
 
 extern "C" int tblite_gb300_batch_last_fallbacks(void) { return g_last_fallbacks; }
+extern "C" void tblite_gb300_set_split_gemm(int enable) { tb::g_split_gemm = enable != 0; }
 extern "C" double tblite_gb300_batch_last_device_ms(void) { return g_last_device_ms; }
 extern "C" int tblite_gb300_batch_last_iterations(int* iterations, int nmol) {
   const int m = std::min(nmol, (int)g_last_iters.size());

@@ -342,6 +342,10 @@ enum { GS_FX = 0,  // T1 = F X            (X upper triangular)
        GS_DENS,    // P = (C f) C^T over icount orbitals (scaled copy in scratch)
        GS_WDENS }; // W (into F) = (C f e) C^T
 void gemm_b(const BatchLaunch& b, int site);
+// the same sites on the BF16 tensor cores with FP64-accurate splitting (ozaki.cu); gemm_b
+// dispatches to it for buckets of at least 128 orbitals while split_gemm_enabled
+void ogemm_b(const BatchLaunch& b, int site);
+extern bool g_split_gemm;
 // eigensolver steps for a bucket
 void cholesky_inverse_b(const BatchLaunch& b);          // S -> X (status into flag)
 void eigen_values_b(const BatchLaunch& b);              // F -> emo (tridiagonal form kept)

@@ -319,8 +319,14 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN)) kb_gemm(BARGS, int site
   gemm_dev<BM, BN, BK, TM, TN>(M, N, K, 1.0, A, n, ta, B, n, tb, 0.0, C, n, km);
 }
 
+bool g_split_gemm = true;
+
 void gemm_b(const BatchLaunch& b, int site) {
   if (!b.count) return;
+  if (g_split_gemm && b.nao_max >= 128) {
+    ogemm_b(b, site);
+    return;
+  }
   const int tk = prof_kbegin(b.s);
   ++g_kernel_launches;
   if (b.nao_max <= 128) {

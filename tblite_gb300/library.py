@@ -89,6 +89,7 @@ _SIGNATURES = {
     "tblite_gb300_get_result_parameter_gradient": (
         None, [c_void_p, c_void_p, _dbl_p, _dbl_p, _dbl_p, _dbl_p]),
     "tblite_gb300_get_kernel_profile": (c_int, [_dbl_p, _int_p, c_int]),
+    "tblite_gb300_set_split_gemm": (None, [c_int]),
     "tblite_gb300_density_matrix_noalloc": (
         c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
     "tblite_gb300_density_matrix_noalloc_max": (c_int, []),
@@ -129,6 +130,11 @@ PHASES = ("setup", "potential", "fock", "eigensolve", "density", "mulliken", "mi
 
 def set_profiling(enable: bool) -> None:
     load().tblite_gb300_set_profiling(int(bool(enable)))
+
+
+def set_split_gemm(enable: bool) -> None:
+    """Batched GEMMs on the BF16 tensor cores with FP64-accurate splitting (default) or FP64."""
+    load().tblite_gb300_set_split_gemm(int(bool(enable)))
 
 
 def get_profile():

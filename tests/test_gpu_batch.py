@@ -140,3 +140,21 @@ def test_batch_large_molecules(method):
     assert batch_fallbacks() == 0
     for (z, x), rb in zip(mols, res_b):
         _compare(rb, _calc(z, x, method).singlepoint())
+
+
+def test_split_gemm_matches_fp64_gemm():
+    """The batched GEMMs on the BF16 tensor cores (FP64-accurate operand splitting) against the
+    FP64 tile GEMMs on the same molecules: results agree at the parity bar."""
+    from tblite_gb300 import library, workloads
+    from tblite_gb300.interface import batch_singlepoint
+
+    mols = [workloads.water_cluster_k(30, seed=401), workloads.alkane(40, seed=402),
+            workloads.water_cluster_k(64, seed=403)]
+    try:
+        library.set_split_gemm(False)
+        ref = batch_singlepoint([_calc(z, x) for z, x in mols])
+    finally:
+        library.set_split_gemm(True)
+    res = batch_singlepoint([_calc(z, x) for z, x in mols])
+    for a, b in zip(res, ref):
+        _compare(a, b)
