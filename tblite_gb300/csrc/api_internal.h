@@ -115,7 +115,8 @@ struct Workspace {
   // D4 dispersion
   DBuf<int> d4_sp, d4_nref, d4_ngw;
   DBuf<double> d4_refcn, d4_refq, d4_zeff, d4_gam, d4_r4r2, d4_rcov, d4_en, d4_c6ref;
-  DBuf<double> d4_cn, d4_gw, d4_dgw, d4_gwv, d4_dgwdq, d4_dgwv_cn, d4_c6, d4_dc6, d4_e3, d4_dEdcn;
+  DBuf<double> d4_cn, d4_gw, d4_dgw, d4_gwv, d4_dgwdq, d4_dgwv_cn, d4_c6, d4_dc6, d4_e3, d4_dEdcn,
+      d4_atm;
   EigenSolver* eig = nullptr;
   ~Workspace() {
     if (eig) eigen_destroy(eig);

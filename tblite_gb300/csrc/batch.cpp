@@ -117,7 +117,7 @@ struct Plan {
   Piece d3_nref, d3_refcn, d3_sref, d3_r4r2, d3_rcov, d3_cn, d3_a, d3_da, d3_dEdcn;
   Piece d4_sp, d4_nref, d4_ngw, d4_refcn, d4_refq, d4_zeff, d4_gam, d4_r4r2, d4_rcov, d4_en,
       d4_c6ref;
-  Piece d4_cn, d4_gw, d4_dgw, d4_gwv, d4_dgwdq, d4_dgwv_cn, d4_c6, d4_dc6, d4_e3, d4_dEdcn;
+  Piece d4_cn, d4_gw, d4_dgw, d4_gwv, d4_dgwdq, d4_dgwv_cn, d4_c6, d4_dc6, d4_e3, d4_dEdcn, d4_atm;
   Piece cn, se, mrad, dmrdcn, S, H, D, Q, F, P, C, scratch, emo, focc;
   Piece qsh, qat, dpat, qpat, qsh_o, qat_o, dpat_o, qpat_o, vsh, vat, vdp, vqp, vao;
   Piece mull, eband, eelec, erep, vec_out, scal, icount;
@@ -242,6 +242,7 @@ void layout(Plan& pl, Region* R) {
       *p = piece<double>(R, RS, na * D4_MREF);
     pl.d4_c6 = piece<double>(R, RS, na * na);
     pl.d4_dc6 = piece<double>(R, RS, na * na);
+    pl.d4_atm = piece<double>(R, RS, 5 * na * na);
   }
 }
 
@@ -334,6 +335,7 @@ MolPtrs make_ptrs(const Plan& pl, const Bases& db) {
     w.dc6 = db.at<double>(pl.d4_dc6);
     w.e3 = db.at<double>(pl.d4_e3);
     w.dEdcn = db.at<double>(pl.d4_dEdcn);
+    w.atm = db.at<double>(pl.d4_atm);
   }
   q.nd = pl.nd;
   // GFN2-xTB mixes the atomic multipoles with the shell charges, GFN1-xTB the charges alone

@@ -392,6 +392,7 @@ static void ensure_workspace(_tblite_calculator* c) {
       for (auto* b : {&w.d4_cn, &w.d4_e3, &w.d4_dEdcn}) b->alloc(na);
       w.d4_c6.alloc(na * na);
       w.d4_dc6.alloc(na * na);
+      w.d4_atm.alloc(5 * na * na);
     }
     w.at_z.upload(c->at_z, s);
     w.at_sh.upload(c->at_sh, s);
@@ -499,6 +500,7 @@ static DevD4 dev_d4(const _tblite_calculator* c, D4Work& wk) {
   wk.dc6 = w.d4_dc6.p;
   wk.e3 = w.d4_e3.p;
   wk.dEdcn = w.d4_dEdcn.p;
+  wk.atm = w.d4_atm.p;
   return d;
 }
 

@@ -236,72 +236,112 @@ __global__ void k_d4_c6(int nat, DevD4 d, const double* __restrict__ gwv,
   d4_c6_dev(nat, d, gwv, dgwv_cn, c6, dc6);
 }
 
-// Axilrod-Teller-Muto term, one warp per atom i, triples (i, j, l) with j < l, both != i.
-// Atom i collects 1/3 of each triple energy, its own force, 1/3 of the virial and the
-// CN derivative through c6_ij and c6_il.
-__device__ __forceinline__ void d4_atm_dev(DevMol m, DevD4 d, const double* __restrict__ c6,
-                         const double* __restrict__ dc6, double* eat, double* grad, double* sig_at,
-                         double* dEdcn) {
+// Axilrod-Teller-Muto term.  Every factor of a triple (i, j, l) that is a product over its
+// three pairs is tabulated per pair first (k_d4_atm_pairs): r^2, 1/r, the damping ratio
+// (r0/r)^(alpha/3), sqrt|C6| and dC6/dCN / (2 C6), so that (r0/r1)^(alpha/3) and
+// sqrt|C6_ij C6_il C6_jl| become products and no pow, sqrt or division but the damping's
+// remains per triple.  tab layout [5][nat][nat]; pairs beyond the cutoff hold r^2 = +inf.
+__device__ __forceinline__ void d4_atm_pairs_dev(DevMol m, DevD4 d, const double* __restrict__ c6,
+                                                 const double* __restrict__ dc6, double* tab) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int nat = m.nat;
+  const size_t nn = (size_t)nat * nat;
+  if (t >= (long long)nn) return;
+  const int i = (int)(t / nat), j = (int)(t % nat);
+  double r2 = 0.0;
+  for (int k = 0; k < 3; ++k) {
+    const double v = m.xyz[3 * j + k] - m.xyz[3 * i + k];
+    r2 += v * v;
+  }
+  const double cut2 = d.disp3_cutoff * d.disp3_cutoff;
+  double ir = 0.0, w = 0.0, sc = 0.0, dq = 0.0;
+  if (i == j || r2 > cut2 || r2 < 1e-12) {
+    r2 = __longlong_as_double(0x7ff0000000000000LL);  // +inf: never inside the cutoff
+  } else {
+    const double r = sqrt(r2);
+    ir = 1.0 / r;
+    const double r0 = d.a1 * sqrt(3.0 * d.r4r2[i] * d.r4r2[j]) + d.a2;
+    w = pow(r0 * ir, d.atm_alpha / 3.0);
+    const double c = c6[t];
+    sc = sqrt(fabs(c));
+    dq = c != 0.0 ? dc6[t] / (2.0 * c) : 0.0;
+  }
+  tab[t] = r2;
+  tab[nn + t] = ir;
+  tab[2 * nn + t] = w;
+  tab[3 * nn + t] = sc;
+  tab[4 * nn + t] = dq;
+}
+__global__ void k_d4_atm_pairs(DevMol m, DevD4 d, const double* __restrict__ c6,
+                               const double* __restrict__ dc6, double* tab) {
+  d4_atm_pairs_dev(m, d, c6, dc6, tab);
+}
+
+// one warp per atom i; for every partner j the lanes walk l > j, so the table rows i and j
+// are read contiguously.  Atom i collects 1/3 of each triple energy, its own force, 1/3 of the
+// virial and the CN derivative through C6_ij and C6_il.
+__device__ __forceinline__ void d4_atm_dev(DevMol m, DevD4 d, const double* __restrict__ tab,
+                                           double* eat, double* grad, double* sig_at,
+                                           double* dEdcn) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (warp >= m.nat) return;
   const int i = warp, nat = m.nat;
+  const size_t nn = (size_t)nat * nat;
+  const double* R2 = tab;
+  const double* IR = tab + nn;
+  const double* W = tab + 2 * nn;
+  const double* SC = tab + 3 * nn;
+  const double* DQ = tab + 4 * nn;
   const double cut2 = d.disp3_cutoff * d.disp3_cutoff;
-  const double alp3 = d.atm_alpha / 3.0;
+  const double a6 = d.atm_alpha / 6.0;
   double e = 0.0, g[3] = {0, 0, 0}, sg[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, dcn = 0.0;
   const double* xi = m.xyz + 3 * i;
-  for (int j = lane; j < nat; j += 32) {
-    if (j == i) continue;
-    double vij[3], r2ij = 0.0;
-    for (int k = 0; k < 3; ++k) {
-      vij[k] = m.xyz[3 * j + k] - xi[k];
-      r2ij += vij[k] * vij[k];
-    }
-    if (r2ij > cut2 || r2ij < 1e-12) continue;
-    const double r0ij = d.a1 * sqrt(3.0 * d.r4r2[i] * d.r4r2[j]) + d.a2;
-    const double c6ij = c6[(size_t)i * nat + j];
-    for (int l = j + 1; l < nat; ++l) {
-      if (l == i) continue;
-      double vil[3], vjl[3], r2il = 0.0, r2jl = 0.0;
-      for (int k = 0; k < 3; ++k) {
-        vil[k] = m.xyz[3 * l + k] - xi[k];
-        vjl[k] = m.xyz[3 * l + k] - m.xyz[3 * j + k];
-        r2il += vil[k] * vil[k];
-        r2jl += vjl[k] * vjl[k];
-      }
-      if (r2il > cut2 || r2jl > cut2 || r2il < 1e-12 || r2jl < 1e-12) continue;
-      const double r0il = d.a1 * sqrt(3.0 * d.r4r2[i] * d.r4r2[l]) + d.a2;
-      const double r0jl = d.a1 * sqrt(3.0 * d.r4r2[j] * d.r4r2[l]) + d.a2;
-      const double c6il = c6[(size_t)i * nat + l], c6jl = c6[(size_t)j * nat + l];
-      const double c9 = -d.s9 * sqrt(fabs(c6ij * c6il * c6jl));
-      const double r0 = r0ij * r0il * r0jl;
-      const double r2 = r2ij * r2il * r2jl, r1 = sqrt(r2), r3 = r2 * r1, r5 = r3 * r2;
-      const double t = pow(r0 / r1, alp3);
+  const size_t ri = (size_t)i * nat;
+  for (int j = 0; j < nat; ++j) {
+    const double r2ij = R2[ri + j];
+    if (!(r2ij <= cut2)) continue;  // j == i or beyond the cutoff (warp uniform)
+    const size_t rj = (size_t)j * nat;
+    const double irij = IR[ri + j], wij = W[ri + j], scij = SC[ri + j], dqij = DQ[ri + j];
+    double vij[3];
+    for (int k = 0; k < 3; ++k) vij[k] = m.xyz[3 * j + k] - xi[k];
+    for (int l = j + 1 + lane; l < nat; l += 32) {
+      const double r2il = R2[ri + l], r2jl = R2[rj + l];
+      if (!(r2il <= cut2) || !(r2jl <= cut2)) continue;
+      const double iril = IR[ri + l], irjl = IR[rj + l];
+      const double c9 = -d.s9 * scij * SC[ri + l] * SC[rj + l];
+      const double t = wij * W[ri + l] * W[rj + l];
+      const double ir1 = irij * iril * irjl;
+      const double ir2 = ir1 * ir1, ir3 = ir2 * ir1, ir5 = ir3 * ir2;
       const double fdmp = 1.0 / (1.0 + 6.0 * t);
       // angular factor in the squared distances a = r2ij, b = r2jl, c = r2il
       const double a = r2ij, b = r2jl, c = r2il;
-      const double P = (a + b - c) * (a - b + c) * (-a + b + c);
-      const double ang = 0.375 * P / r5 + 1.0 / r3;
+      const double ia = irij * irij, ib = irjl * irjl, ic = iril * iril;
+      const double pa = a - b + c, pb = -a + b + c, pc = a + b - c;
+      const double P = pc * pa * pb;
+      const double ang = 0.375 * P * ir5 + ir3;
       const double rr = ang * fdmp;
-      e += rr * c9 / 3.0;
-      const double dPa = (a - b + c) * (-a + b + c) + (a + b - c) * (-a + b + c) - (a + b - c) * (a - b + c);
-      const double dPc = -(a - b + c) * (-a + b + c) + (a + b - c) * (-a + b + c) + (a + b - c) * (a - b + c);
-      const double dPb = (a - b + c) * (-a + b + c) - (a + b - c) * (-a + b + c) + (a + b - c) * (a - b + c);
+      e += rr * c9 * (1.0 / 3.0);
+      const double dPa = pa * pb + pc * pb - pc * pa;
+      const double dPc = -pa * pb + pc * pb + pc * pa;
+      const double dPb = pa * pb - pc * pb + pc * pa;
       const double dfdt = -6.0 * fdmp * fdmp;
-      const double dEa = c9 * ((0.375 * (dPa / r5 - 2.5 * P / (r5 * a)) - 1.5 / (r3 * a)) * fdmp
-                               + ang * dfdt * (-(d.atm_alpha / 6.0) * t / a));
-      const double dEb = c9 * ((0.375 * (dPb / r5 - 2.5 * P / (r5 * b)) - 1.5 / (r3 * b)) * fdmp
-                               + ang * dfdt * (-(d.atm_alpha / 6.0) * t / b));
-      const double dEc = c9 * ((0.375 * (dPc / r5 - 2.5 * P / (r5 * c)) - 1.5 / (r3 * c)) * fdmp
-                               + ang * dfdt * (-(d.atm_alpha / 6.0) * t / c));
+      const double g0 = ang * dfdt * (-a6) * t;
+      const double dEa = c9 * ((0.375 * (dPa * ir5 - 2.5 * P * ir5 * ia) - 1.5 * ir3 * ia) * fdmp + g0 * ia);
+      const double dEb = c9 * ((0.375 * (dPb * ir5 - 2.5 * P * ir5 * ib) - 1.5 * ir3 * ib) * fdmp + g0 * ib);
+      const double dEc = c9 * ((0.375 * (dPc * ir5 - 2.5 * P * ir5 * ic) - 1.5 * ir3 * ic) * fdmp + g0 * ic);
+      double vil[3], vjl[3];
+      for (int k = 0; k < 3; ++k) {
+        vil[k] = m.xyz[3 * l + k] - xi[k];
+        vjl[k] = m.xyz[3 * l + k] - m.xyz[3 * j + k];
+      }
       // r2ij = |R_j - R_i|^2 -> d/dR_i = -2 vij ; r2il -> -2 vil
       for (int k = 0; k < 3; ++k) g[k] += -2.0 * dEa * vij[k] - 2.0 * dEc * vil[k];
       for (int p = 0; p < 3; ++p)
         for (int q = 0; q < 3; ++q)
           sg[3 * p + q] += 2.0 / 3.0 * (dEa * vij[p] * vij[q] + dEb * vjl[p] * vjl[q]
                                         + dEc * vil[p] * vil[q]);
-      // dE/dc6 = rr c9 / (2 c6)
-      dcn += rr * c9 / (2.0 * c6ij) * dc6[(size_t)i * nat + j]
-             + rr * c9 / (2.0 * c6il) * dc6[(size_t)i * nat + l];
+      // dE/dC6 = rr c9 / (2 C6)
+      dcn += rr * c9 * (dqij + DQ[ri + l]);
     }
   }
   e = wsum(e);
@@ -317,10 +357,9 @@ __device__ __forceinline__ void d4_atm_dev(DevMol m, DevD4 d, const double* __re
     }
   }
 }
-__global__ void k_d4_atm(DevMol m, DevD4 d, const double* __restrict__ c6,
-                         const double* __restrict__ dc6, double* eat, double* grad, double* sig_at,
-                         double* dEdcn) {
-  d4_atm_dev(m, d, c6, dc6, eat, grad, sig_at, dEdcn);
+__global__ void k_d4_atm(DevMol m, DevD4 d, const double* __restrict__ tab, double* eat,
+                         double* grad, double* sig_at, double* dEdcn) {
+  d4_atm_dev(m, d, tab, eat, grad, sig_at, dEdcn);
 }
 
 __device__ __forceinline__ void d4_cn_grad_dev(DevMol m, DevD4 d, const double* __restrict__ dEdcn, double* grad,
@@ -374,9 +413,10 @@ void d4_setup(const DevMol& m, const DevD4& d, D4Work& w, bool grad, double* gra
   ++g_kernel_launches;
   k_d4_c6<<<(unsigned)((nn + 255) / 256), 256, 0, s>>>(m.nat, d, w.gwv, w.dgwv_cn, w.c6, w.dc6);
   cudaMemsetAsync(w.dEdcn, 0, sizeof(double) * m.nat, s);
-  ++g_kernel_launches;
-  k_d4_atm<<<warps_grid(m.nat), 64, 0, s>>>(m, d, w.c6, w.dc6, w.e3, grad ? grad_out : nullptr,
-                                             sig_at, w.dEdcn);
+  g_kernel_launches += 2;
+  k_d4_atm_pairs<<<(unsigned)((nn + 255) / 256), 256, 0, s>>>(m, d, w.c6, w.dc6, w.atm);
+  k_d4_atm<<<warps_grid(m.nat), 64, 0, s>>>(m, d, w.atm, w.e3, grad ? grad_out : nullptr, sig_at,
+                                             w.dEdcn);
 }
 
 void d4_potential(const DevMol& m, const DevD4& d, D4Work& w, const double* qat, double* vat,
@@ -595,9 +635,13 @@ __global__ void kb_d4_c6(BARGS) {
   BMOL;
   d4_c6_dev(q.m.nat, q.d4, q.d4w.gwv, q.d4w.dgwv_cn, q.d4w.c6, q.d4w.dc6);
 }
+__global__ void kb_d4_atm_pairs(BARGS) {
+  BMOL;
+  d4_atm_pairs_dev(q.m, q.d4, q.d4w.c6, q.d4w.dc6, q.d4w.atm);
+}
 __global__ void kb_d4_atm(BARGS) {
   BMOL;
-  d4_atm_dev(q.m, q.d4, q.d4w.c6, q.d4w.dc6, q.d4w.e3, q.grad, q.sig_at, q.d4w.dEdcn);
+  d4_atm_dev(q.m, q.d4, q.d4w.atm, q.d4w.e3, q.grad, q.sig_at, q.d4w.dEdcn);
 }
 __global__ void kb_d4_pair_pot(BARGS) {
   BMOL;
@@ -644,12 +688,13 @@ static inline dim3 batoms(const BatchLaunch& b) {
 
 void d4_setup_b(const BatchLaunch& b) {
   if (!b.count) return;
-  g_kernel_launches += 5;
+  g_kernel_launches += 6;
   kb_d4_cn<<<bwarps(b), 64, 0, b.s>>>(b.mp, b.list);
   kb_d4_weights<<<batoms(b), 128, 0, b.s>>>(b.mp, b.list);
   kb_d4_zeta<<<batoms(b), 128, 0, b.s>>>(b.mp, b.list, 0);
   const long long nn = (long long)b.nat_max * b.nat_max;
   kb_d4_c6<<<dim3((unsigned)((nn + 255) / 256), 1, b.count), 256, 0, b.s>>>(b.mp, b.list);
+  kb_d4_atm_pairs<<<dim3((unsigned)((nn + 255) / 256), 1, b.count), 256, 0, b.s>>>(b.mp, b.list);
   kb_d4_atm<<<bwarps(b), 64, 0, b.s>>>(b.mp, b.list);
 }
 void d3_setup_b(const BatchLaunch& b) {
