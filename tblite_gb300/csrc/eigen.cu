@@ -1127,24 +1127,37 @@ __global__ void __launch_bounds__(256) kb_tridiag(BARGS) {
     const int s0 = i < b ? 0 : (i - b) / nb + 1;  // first owned column > i
     if (t != 0.0) {
       __syncthreads();
-      // rows above the diagonal, from the owned columns c < r: spart_r = sum A(r, c) v_c
-      for (int r = i + 1 + tid; r < n; r += blockDim.x) {
-        double acc = 0.0;
-        for (int s2 = s0; s2 < ncpb; ++s2) {
-          const int c = b + s2 * nb;
-          if (c >= r) break;
-          acc = fma(scol[sym_off(s2, n, b, nb) + (r - c)], sv[c], acc);
+      // rows above the diagonal, from the owned columns c < r: spart_r = sum A(r, c) v_c.
+      // A row's work grows with its index, so every thread takes one row from the top and one
+      // from the bottom of the trailing block.
+      const int m = n - i - 1;
+      for (int u = tid; 2 * u < m; u += blockDim.x) {
+#pragma unroll 1
+        for (int side = 0; side < 2; ++side) {
+          const int r = side ? n - 1 - u : i + 1 + u;
+          if (side && r == i + 1 + u) break;  // the middle row of an odd count
+          double acc = 0.0;
+          for (int s2 = s0; s2 < ncpb; ++s2) {
+            const int c = b + s2 * nb;
+            if (c >= r) break;
+            acc = fma(scol[sym_off(s2, n, b, nb) + (r - c)], sv[c], acc);
+          }
+          spart[r] = acc;
         }
-        spart[r] = acc;
       }
       __syncthreads();
       // stored part of the owned columns: spart_c += sum_{r >= c} A(r, c) v_r (warp per column)
       for (int s2 = s0 + wid; s2 < ncpb; s2 += nwb) {
         const int c = b + s2 * nb;
         const double* col = column(s2);
-        double acc = 0.0;
-        for (int r = c + lane; r < n; r += 32) acc = fma(col[r], sv[r], acc);
-        acc = wred(acc);
+        double a0 = 0.0, a1 = 0.0;
+        int r = c + lane;
+        for (; r + 32 < n; r += 64) {
+          a0 = fma(col[r], sv[r], a0);
+          a1 = fma(col[r + 32], sv[r + 32], a1);
+        }
+        if (r < n) a0 = fma(col[r], sv[r], a0);
+        const double acc = wred(a0 + a1);
         if (lane == 0) spart[c] += acc;
       }
     }
@@ -1163,12 +1176,22 @@ __global__ void __launch_bounds__(256) kb_tridiag(BARGS) {
       const double K = -0.5 * t * kk;
       for (int r = i + 1 + tid; r < n; r += blockDim.x) sw[r] = fma(K, sv[r], sw[r]);
       __syncthreads();
-      for (int s2 = s0; s2 < ncpb; ++s2) {
-        const int c = b + s2 * nb;
-        double* col = column(s2);
-        const double vc = sv[c], wc = sw[c];
-        for (int r = c + tid; r < n; r += blockDim.x)
-          col[r] = fma(-sv[r], wc, fma(-sw[r], vc, col[r]));
+      // the owned columns c > i are contiguous in the packed storage: one flat loop over their
+      // elements, each thread following its column with a cursor
+      if (s0 < ncpb) {
+        int s2 = s0;
+        size_t beg = sym_off(s0, n, b, nb);
+        size_t end = beg + (size_t)(n - (b + s0 * nb));
+        const size_t last = sym_off(ncpb, n, b, nb);
+        for (size_t e = beg + tid; e < last; e += blockDim.x) {
+          while (e >= end) {
+            ++s2;
+            beg = end;
+            end = beg + (size_t)(n - (b + s2 * nb));
+          }
+          const int c = b + s2 * nb, r = c + (int)(e - beg);
+          scol[e] = fma(-sv[r], sw[c], fma(-sw[r], sv[c], scol[e]));
+        }
       }
     }
     __syncthreads();
