@@ -909,7 +909,7 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
     eigen_vectors(w.eig, h_cnt[0], w.C.p);
     g_prof.end(s);
     g_prof.begin(PH_DENSITY, s);
-    density_matrix(n, h_cnt[0], w.C.p, w.focc.p, w.P.p, w.scratch.p, s);
+    density_matrix(n, h_cnt[0], w.C.p, w.focc.p, w.P.p, w.scratch.p, s, eigen_gemm_status(w.eig));
     g_prof.end(s);
     g_prof.begin(PH_MULLIKEN, s);
     launch_mulliken(m, w.P.p, w.S.p, w.H.p, w.D.p, w.Q.p, w.mull.p, mulliken_chunks(n), w.qsh_o.p,
@@ -958,7 +958,7 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
   if (c->solv) solv_gradient(dsolv, w.xyz.p, w.qat_o.p, w.grad.p, s);
   // W = C diag(f e) C^T  (scf/diag.f90:110-143)
   launch_fe(n, w.focc.p, w.emo.p, w.vec_out.p, s);
-  density_matrix(n, h_cnt[0], w.C.p, w.vec_out.p, w.W.p, w.scratch.p, s);
+  density_matrix(n, h_cnt[0], w.C.p, w.vec_out.p, w.W.p, w.scratch.p, s, eigen_gemm_status(w.eig));
   launch_h0_gradient(m, p, w.se.p, w.P.p, w.W.p, w.vao.p, w.vdp.p, w.vqp.p, w.grad.p, w.sigma.p,
                      w.dEdcn.p, s);
   launch_cn_grad(m, p, w.dEdcn.p, w.grad.p, w.sig_at.p, s);
@@ -981,7 +981,8 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
     launch_wbo(m, w.scratch.p, w.wbo.p, 1.0, s);
   } else {
     for (int sp = 0; sp < 2; ++sp) {  // W is free after the gradient: it holds the spin density
-      density_matrix(n, h_cnt[0], w.C.p, w.focc.p + (size_t)(1 + sp) * n, w.W.p, w.scratch.p, s);
+      density_matrix(n, h_cnt[0], w.C.p, w.focc.p + (size_t)(1 + sp) * n, w.W.p, w.scratch.p, s,
+                     eigen_gemm_status(w.eig));
       gemm64(false, false, n, n, n, 1.0, w.W.p, n, w.S.p, n, 0.0, w.scratch.p, n, KM_NONE, s);
       launch_wbo(m, w.scratch.p, w.wbo.p + (size_t)sp * nat * nat, 2.0, s);
     }
@@ -1021,6 +1022,8 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
   g_prof.end(s);
   stream_wait(s);
   cuda_check(cudaGetLastError(), "results");
+  if (eigen_gemm_failed(w.eig))
+    throw std::runtime_error("tensor-core matrix product did not complete (wait limit reached)");
   g_prof.collect();
   g_prof.iterations = iscf;
   if (c->solv) {

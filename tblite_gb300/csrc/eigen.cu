@@ -33,6 +33,9 @@ static void ck(cudaError_t e, const char* what) {
     throw std::runtime_error(std::string("CUDA error '") + cudaGetErrorString(e) + "' in " + what);
 }
 
+// GEMMs of the one-molecule path go to the tensor cores from 128 orbitals on
+static inline bool split_gemm(int n) { return g_split_gemm && n >= 128; }
+
 struct EigenSolver {
   int n = 0;
   cudaStream_t stream = nullptr;
@@ -42,6 +45,7 @@ struct EigenSolver {
   double *tw = nullptr;   // eigenvalue scratch: e^2 [n] (double), d and e^2 [n] (float)
   double *Y = nullptr;    // eigenvectors of T, column-major [k][n]
   int* status = nullptr;  // device
+  int* gstatus = nullptr; // device: 1 once a tensor-core GEMM did not answer
   int* hstatus = nullptr; // pinned
   int coop_blocks = 0;
   int cap = 0;  // buffers hold problems up to this order
@@ -897,6 +901,8 @@ EigenSolver* eigen_create(int n, cudaStream_t s) {
   ck(cudaMalloc(&e->tw, sizeof(double) * 2 * (n + 1)), "tw");
   ck(cudaMalloc(&e->scal, sizeof(double) * 8), "scal");
   ck(cudaMalloc(&e->status, sizeof(int)), "status");
+  ck(cudaMalloc(&e->gstatus, sizeof(int)), "gstatus");
+  ck(cudaMemsetAsync(e->gstatus, 0, sizeof(int), s), "gstatus");
   ck(cudaMallocHost(&e->hstatus, sizeof(int)), "hstatus");
   int dev = 0, nsm = 0, per_sm = 0;
   cudaGetDevice(&dev);
@@ -920,6 +926,7 @@ void eigen_destroy(EigenSolver* e) {
                     e->scal})
     cudaFree(p);
   cudaFree(e->status);
+  cudaFree(e->gstatus);
   cudaFreeHost(e->hstatus);
   delete e;
 }
@@ -937,8 +944,14 @@ int eigen_values(EigenSolver* es, const double* F, double* w_out, int nev) {
   const int n = es->n;
   cudaStream_t s = es->stream;
   // A = X^T (F X): X upper triangular
-  gemm64(false, false, n, n, n, 1.0, F, n, es->X, n, 0.0, es->T1, n, KM_LT_COLEND, s);
-  gemm64(true, false, n, n, n, 1.0, es->X, n, es->T1, n, 0.0, es->A, n, KM_LT_ROWEND | KM_SYM, s);
+  if (split_gemm(n)) {  // BF16 tensor cores, FP64-accurate splitting (exponents in tw)
+    int* ex = reinterpret_cast<int*>(es->tw);
+    ogemm(false, false, n, n, n, F, es->X, es->T1, n, KM_LT_COLEND, ex, es->gstatus, s);
+    ogemm(true, false, n, n, n, es->X, es->T1, es->A, n, KM_LT_ROWEND | KM_SYM, ex, es->gstatus, s);
+  } else {
+    gemm64(false, false, n, n, n, 1.0, F, n, es->X, n, 0.0, es->T1, n, KM_LT_COLEND, s);
+    gemm64(true, false, n, n, n, 1.0, es->X, n, es->T1, n, 0.0, es->A, n, KM_LT_ROWEND | KM_SYM, s);
+  }
   // tridiagonalise
   {
     int nn = n;
@@ -1008,7 +1021,12 @@ void eigen_vectors_range(EigenSolver* es, int k0, int k1, double* C) {
       n, k, chunk, bt_ysmem(n), es->A, es->tau, Yk);
   prof_kend(KS_BACKTRANSFORM, tb_, s);
   // C = X Y (X upper triangular)
-  gemm64(false, false, n, k, n, 1.0, es->X, n, Yk, n, 0.0, C + (size_t)k0 * n, n, KM_GE_ROWBEG, s);
+  if (split_gemm(n))
+    ogemm(false, false, n, k, n, es->X, Yk, C + (size_t)k0 * n, n, KM_GE_ROWBEG,
+          reinterpret_cast<int*>(es->tw), es->gstatus, s);
+  else
+    gemm64(false, false, n, k, n, 1.0, es->X, n, Yk, n, 0.0, C + (size_t)k0 * n, n, KM_GE_ROWBEG,
+           s);
 }
 
 void eigen_vectors(EigenSolver* es, int k, double* C) { eigen_vectors_range(es, 0, k, C); }
@@ -1024,7 +1042,7 @@ __global__ void k_scale_cols(int n, int k, const double* C, const double* f, dou
 }
 
 void density_matrix(int n, int k, const double* C, const double* f, double* P, double* work,
-                    cudaStream_t s) {
+                    cudaStream_t s, int* status) {
   if (k <= 0) {
     cudaMemsetAsync(P, 0, sizeof(double) * (size_t)n * n, s);
     return;
@@ -1032,7 +1050,20 @@ void density_matrix(int n, int k, const double* C, const double* f, double* P, d
   const size_t tot = (size_t)n * k;
   ++g_kernel_launches;
   k_scale_cols<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(n, k, C, f, work);
-  gemm64(false, true, n, n, k, 1.0, work, n, C, n, 0.0, P, n, KM_NONE | KM_SYM, s);
+  // the split GEMM keeps its 2n exponents behind the scaled columns (needs k < n)
+  if (status && split_gemm(n) && k < n)
+    ogemm(false, true, n, n, k, work, C, P, n, KM_NONE | KM_SYM,
+          reinterpret_cast<int*>(work + tot), status, s);
+  else
+    gemm64(false, true, n, n, k, 1.0, work, n, C, n, 0.0, P, n, KM_NONE | KM_SYM, s);
+}
+
+int* eigen_gemm_status(EigenSolver* es) { return es->gstatus; }
+bool eigen_gemm_failed(EigenSolver* es) {
+  int h = 0;
+  ck(cudaMemcpyAsync(&h, es->gstatus, sizeof(int), cudaMemcpyDeviceToHost, es->stream), "gstatus");
+  stream_wait(es->stream);
+  return h != 0;
 }
 
 // ------------------------------------------------------------------------------------------

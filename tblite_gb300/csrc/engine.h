@@ -260,8 +260,18 @@ void launch_eelec_init(int nat, const double* ts, const double* eband, double* e
 void launch_fe(int n, const double* f, const double* e, double* out, cudaStream_t s);
 
 // dense helpers
+// P = C diag(f) C^T over k columns; with status (a device int of the eigensolver) the product
+// may run on the tensor cores (split GEMM), which then keeps 2n ints behind the n*k scaled
+// columns in work
 void density_matrix(int n, int k, const double* C, const double* f, double* P, double* work,
-                    cudaStream_t s);
+                    cudaStream_t s, int* status = nullptr);
+// split GEMM of the one-molecule path (ozaki.cu): C = op(A) op(B), column-major, leading
+// dimension ld; ex: M + ld ints of device scratch; status set to 1 if it did not complete
+void ogemm(bool ta, bool tb, int M, int N, int K, const double* A, const double* B, double* C,
+           int ld, int kmode, int* ex, int* status, cudaStream_t s);
+// the eigensolver's tensor-core GEMM status word, and its check (synchronises the stream)
+int* eigen_gemm_status(EigenSolver*);
+bool eigen_gemm_failed(EigenSolver*);
 // wbo[A][B] += scale * sum (PS)_{nu mu} (PS)_{mu nu} over the orbitals of atoms A != B
 void launch_wbo(const DevMol& m, const double* PS, double* wbo, double scale, cudaStream_t s);
 // dE/d(shell self energy, hardness, hardness derivative) into out[3][nsh]; Hp is H0 built

@@ -46,7 +46,7 @@ constexpr int OZ_A_SLICE = OZ_M * OZ_KC;  // bf16 elements of one slice of the A
 constexpr int OZ_B_SLICE = OZ_N * OZ_KC;
 
 struct Site {
-  int M, N, K;
+  int M, N, K, ld;  // ld: leading dimension of A, B and C (column-major)
   const double* A;
   bool ta;  // op(A)(i, k) = ta ? A[k + i n] : A[i + k n]
   const double* B;
@@ -59,7 +59,7 @@ struct Site {
 // the operands of the GEMM sites (the same as the FP64 tile GEMM of linalg.cu)
 __device__ __forceinline__ Site site_of(const MolPtrs& q, int site) {
   const int n = q.m.nao, k = *q.icount;
-  Site s{n, n, n, nullptr, false, nullptr, false, nullptr, KM_NONE, false};
+  Site s{n, n, n, n, nullptr, false, nullptr, false, nullptr, KM_NONE, false};
   switch (site) {
     case GS_FX: s.A = q.F; s.B = q.X; s.C = q.T1; s.km = KM_LT_COLEND; break;
     case GS_XTT:
@@ -71,11 +71,11 @@ __device__ __forceinline__ Site site_of(const MolPtrs& q, int site) {
   }
   return s;
 }
-__device__ __forceinline__ double opA(const Site& s, int n, int i, int k) {
-  return s.ta ? s.A[k + (size_t)i * n] : s.A[i + (size_t)k * n];
+__device__ __forceinline__ double opA(const Site& s, int i, int k) {
+  return s.ta ? s.A[k + (size_t)i * s.ld] : s.A[i + (size_t)k * s.ld];
 }
-__device__ __forceinline__ double opB(const Site& s, int n, int k, int j) {
-  return s.tb ? s.B[j + (size_t)k * n] : s.B[k + (size_t)j * n];
+__device__ __forceinline__ double opB(const Site& s, int k, int j) {
+  return s.tb ? s.B[j + (size_t)k * s.ld] : s.B[k + (size_t)j * s.ld];
 }
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -130,36 +130,38 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
 
 }  // namespace
 
-// per molecule: exponent e = ilogb(max |x|) + 1 of every row of op(A) (into lu[0 .. M)) and of
-// every column of op(B) (into lu[n .. n + N)); one warp per vector
-__global__ void __launch_bounds__(256) kb_oexp(BARGS, int site) {
-  BMOL;
-  const Site s = site_of(q, site);
-  const int n = q.m.nao;
-  const int lane = threadIdx.x & 31, v = blockIdx.x * 8 + (threadIdx.x >> 5);
-  int* ex = reinterpret_cast<int*>(q.lu);
+// exponent e = ilogb(max |x|) + 1 of every row of op(A) (into ex[0 .. M)) and of every column
+// of op(B) (into ex[nb .. nb + N)); one warp per vector
+__device__ __forceinline__ void oexp_body(const Site& s, int* ex, int nb, int v, int lane) {
   if (v < s.M) {
     double mx = 0.0;
-    for (int k = lane; k < s.K; k += 32) mx = fmax(mx, fabs(opA(s, n, v, k)));
+    for (int k = lane; k < s.K; k += 32) mx = fmax(mx, fabs(opA(s, v, k)));
     for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if (lane == 0) ex[v] = mx > 0.0 ? ilogb(mx) + 1 : 0;
-  } else if (v - s.M < s.N && v - s.M < n) {
+  } else if (v - s.M < s.N && v - s.M < nb) {
     const int j = v - s.M;
     double mx = 0.0;
-    for (int k = lane; k < s.K; k += 32) mx = fmax(mx, fabs(opB(s, n, k, j)));
+    for (int k = lane; k < s.K; k += 32) mx = fmax(mx, fabs(opB(s, k, j)));
     for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    if (lane == 0) ex[n + j] = mx > 0.0 ? ilogb(mx) + 1 : 0;
+    if (lane == 0) ex[nb + j] = mx > 0.0 ? ilogb(mx) + 1 : 0;
   }
 }
-
-__global__ void __launch_bounds__(OZ_THREADS, 1) kb_ogemm(BARGS, int site) {
+// batched: per molecule, the exponents go to the inverse-iteration scratch lu (free at every
+// GEMM site), rows at lu[0 .. n), columns at lu[n .. 2n)
+__global__ void __launch_bounds__(256) kb_oexp(BARGS, int site) {
   BMOL;
-  const Site s = site_of(q, site);
-  const int n = q.m.nao;
-  const int i0 = blockIdx.y * OZ_M, j0 = blockIdx.x * OZ_N;
-  if (i0 >= s.M || j0 >= s.N) return;
-  if (s.sym && i0 + OZ_M - 1 < j0) return;  // strictly above the diagonal: the mirror writes it
-  if (*q.flag < 0) return;                  // the molecule has left the batch
+  oexp_body(site_of(q, site), reinterpret_cast<int*>(q.lu), q.m.nao,
+            blockIdx.x * 8 + (threadIdx.x >> 5), threadIdx.x & 31);
+}
+__global__ void __launch_bounds__(256) k_oexp(Site s, int* ex) {
+  oexp_body(s, ex, s.ld, blockIdx.x * 8 + (threadIdx.x >> 5), threadIdx.x & 31);
+}
+
+// one 128 x 64 output tile (i0, j0); the exponents ex: rows at ex[0 ..), columns at ex[n ..);
+// returns false if the tensor-core pipeline did not answer within the wait limit
+__device__ __forceinline__ bool ogemm_body(const Site& s, const int* __restrict__ ex, int i0,
+                                           int j0) {
+  const int n = s.ld;
   int kbeg = 0, kend = s.K;
   if (s.km == KM_LT_COLEND) kend = min(s.K, j0 + OZ_N);
   else if (s.km == KM_LT_ROWEND) kend = min(s.K, i0 + OZ_M);
@@ -171,7 +173,6 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) kb_ogemm(BARGS, int site) {
   __shared__ __align__(8) uint64_t mbar;
   __shared__ uint32_t tmem_base;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int* ex = reinterpret_cast<const int*>(q.lu);
 
   if (tid == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)));
@@ -220,7 +221,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) kb_ogemm(BARGS, int site) {
 #pragma unroll
       for (int t = 0; t < 8; ++t) {
         const int k = k0 + 8 * g8 + t;
-        const double x = (i < s.M && k < s.K) ? opA(s, n, i, k) : 0.0;
+        const double x = (i < s.M && k < s.K) ? opA(s, i, k) : 0.0;
         split_into(x, eA, t, w);
       }
       const int kk = 8 * g8;
@@ -238,7 +239,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) kb_ogemm(BARGS, int site) {
 #pragma unroll
       for (int t = 0; t < 8; ++t) {
         const int k = k0 + 8 * gb + t;
-        const double x = (j < s.N && k < s.K) ? opB(s, n, k, j) : 0.0;
+        const double x = (j < s.N && k < s.K) ? opB(s, k, j) : 0.0;
         split_into(x, eB, t, w);
       }
       const int kk = 8 * gb;
@@ -331,14 +332,33 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) kb_ogemm(BARGS, int site) {
         }
       }
     }
-  } else if (tid == 0) {
-    *q.flag = -5;  // the tensor-core pipeline did not answer: the molecule takes the plain path
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
   if (warp == 0)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                  "r"(OZ_TMEM_COLS));
+  return ok;
+}
+
+__global__ void __launch_bounds__(OZ_THREADS, 1) kb_ogemm(BARGS, int site) {
+  BMOL;
+  const Site s = site_of(q, site);
+  const int i0 = blockIdx.y * OZ_M, j0 = blockIdx.x * OZ_N;
+  if (i0 >= s.M || j0 >= s.N) return;
+  if (s.sym && i0 + OZ_M - 1 < j0) return;  // strictly above the diagonal: the mirror writes it
+  if (*q.flag < 0) return;                  // the molecule has left the batch
+  const bool ok = ogemm_body(s, reinterpret_cast<const int*>(q.lu), i0, j0);
+  // the tensor-core pipeline did not answer: the molecule takes the one-molecule path
+  if (!ok && threadIdx.x == 0) *q.flag = -5;
+}
+__global__ void __launch_bounds__(OZ_THREADS, 1) k_ogemm(Site s, const int* __restrict__ ex,
+                                                         int* status) {
+  const int i0 = blockIdx.y * OZ_M, j0 = blockIdx.x * OZ_N;
+  if (i0 >= s.M || j0 >= s.N) return;
+  if (s.sym && i0 + OZ_M - 1 < j0) return;
+  const bool ok = ogemm_body(s, ex, i0, j0);
+  if (!ok && threadIdx.x == 0) atomicExch(status, 1);
 }
 
 static void ck(cudaError_t e, const char* what) {
@@ -361,6 +381,27 @@ void ogemm_b(const BatchLaunch& b, int site) {
   kb_ogemm<<<dim3((n + OZ_N - 1) / OZ_N, (n + OZ_M - 1) / OZ_M, b.count), OZ_THREADS, OZ_SMEM,
              b.s>>>(b.mp, b.list, site);
   prof_kend(KS_GEMM, tk, b.s);
+}
+
+// one matrix product of the one-molecule path: C = op(A) op(B), all column-major with leading
+// dimension ld; ex holds M + ld ints of device scratch; status is set to 1 if the tensor-core
+// pipeline did not answer (checked by the caller once per single point)
+void ogemm(bool ta, bool tb, int M, int N, int K, const double* A, const double* B, double* C,
+           int ld, int kmode, int* ex, int* status, cudaStream_t st) {
+  if (M <= 0 || N <= 0) return;
+  static bool attr = false;
+  if (!attr) {
+    ck(cudaFuncSetAttribute(k_ogemm, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM),
+       "smem attr split gemm");
+    attr = true;
+  }
+  Site s{M, N, K, ld, A, ta, B, tb, C, kmode & 7, (kmode & KM_SYM) != 0};
+  const int tk = prof_kbegin(st);
+  g_kernel_launches += 2;
+  k_oexp<<<(M + ld + 7) / 8, 256, 0, st>>>(s, ex);
+  k_ogemm<<<dim3((N + OZ_N - 1) / OZ_N, (M + OZ_M - 1) / OZ_M, 1), OZ_THREADS, OZ_SMEM, st>>>(
+      s, ex, status);
+  prof_kend(KS_GEMM, tk, st);
 }
 
 #undef BMOL

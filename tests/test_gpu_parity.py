@@ -148,3 +148,21 @@ def test_bond_orders_and_moments(charge):
             assert np.max(np.abs(wbo[:, :, ch] - ref_wbo[ch])) < 1e-6
     assert np.max(np.abs(res.get("dipole") - ref.parts["dipole"])) < 1e-6
     assert np.max(np.abs(res.get("quadrupole") - ref.parts["quadrupole"])) < 1e-5
+
+
+def test_split_gemm_plain_path():
+    """One-molecule path: the tensor-core split GEMM (FP64-accurate operand splitting, used
+    from 128 orbitals on) against the FP64 tile GEMM on (H2O)32 (192 orbitals)."""
+    from tblite_gb300 import library, workloads
+
+    z, x = workloads.water_cluster((4, 4, 2), seed=0)
+    try:
+        library.set_split_gemm(False)
+        _, ref = _gpu(z, x, acc=0.01)
+    finally:
+        library.set_split_gemm(True)
+    _, res = _gpu(z, x, acc=0.01)
+    assert abs(res.get("energy") - ref.get("energy")) < E_TOL
+    assert np.max(np.abs(res.get("gradient") - ref.get("gradient"))) < G_TOL
+    assert np.max(np.abs(res.get("charges") - ref.get("charges"))) < Q_TOL
+    assert np.max(np.abs(res.get("bond-orders") - ref.get("bond-orders"))) < 1e-6
