@@ -51,6 +51,9 @@ int tblite_gb300_batch_last_iterations(int* iterations, int nmol);
 /* batched GEMMs of molecules with at least 128 orbitals on the BF16 tensor cores with
  * FP64-accurate operand splitting (1, the default) or as FP64 tile GEMMs (0); process wide */
 void tblite_gb300_set_split_gemm(int enable);
+/* number of streams (1..8, default 8) over which a batch call spreads its size buckets; 1 runs
+ * the buckets one after the other, so per-kernel event times bracket each kernel alone */
+void tblite_gb300_set_batch_streams(int count);
 
 /* enable (1) or disable (0) event timing for subsequent single points (process wide) */
 void tblite_gb300_set_profiling(int enable);

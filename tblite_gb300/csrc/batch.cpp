@@ -82,6 +82,7 @@ struct Arena {
 std::mutex g_batch_mutex;
 Arena g_arena;
 int g_last_fallbacks = 0;
+int g_batch_streams = 8;  // side streams the size buckets are spread over
 double g_last_device_ms = 0.0;  // device time of the last call's batched steps (CUDA events)
 std::vector<int> g_last_iters;  // SCF iterations per molecule of the last call (0: not batched)
 
@@ -602,7 +603,7 @@ std::vector<int> run_chunk(std::vector<Plan>& plans, Arena& ar, _tblite_context*
     int k = 0;
     for (auto& L : launch) {
       if (!L.count) continue;
-      const int slot = k++ % Arena::NSIDE;
+      const int slot = k++ % std::max(1, std::min(g_batch_streams, (int)Arena::NSIDE));
       L.s = ar.side[slot];
       cuda_check(cudaStreamWaitEvent(L.s, ar.fork, 0), "fork");
       fn(L);
@@ -904,6 +905,9 @@ extern "C" int tblite_gb300_batch_singlepoint(tblite_context ctx, int nmol,
 
 extern "C" int tblite_gb300_batch_last_fallbacks(void) { return g_last_fallbacks; }
 extern "C" void tblite_gb300_set_split_gemm(int enable) { tb::g_split_gemm = enable != 0; }
+extern "C" void tblite_gb300_set_batch_streams(int count) {
+  g_batch_streams = count < 1 ? 1 : (count > 8 ? 8 : count);
+}
 extern "C" double tblite_gb300_batch_last_device_ms(void) { return g_last_device_ms; }
 extern "C" int tblite_gb300_batch_last_iterations(int* iterations, int nmol) {
   const int m = std::min(nmol, (int)g_last_iters.size());

@@ -821,25 +821,86 @@ __global__ void k_clusters(int n, int k0, int k, const double* __restrict__ d,
 // back-transformation Z = Q Y = H_0 H_1 ... H_{n-2} Y  (apply H_{n-2} first).  Each block owns
 // a set of columns (one warp per column); reflectors are staged in shared memory in chunks.
 // ------------------------------------------------------------------------------------------
+// Back-transformation Z = Q Y of the eigenvectors of T.  The reflectors are taken in blocks of
+// four, [4g, 4g+3], from the top block down, each block as one compact-WY update
+//     y <- y - V (T (V^T y))      (V = the block's four reflectors, T upper triangular 4 x 4)
+// so that a column makes one pass for the four dot products and one for the update, and the
+// four warp reductions are independent.  T (LAPACK dlarft, forward, column-wise) is formed
+// once per block by k_bt_tmat.  One warp per column; the block's reflectors are staged in
+// shared memory (zero above each reflector's first row), the column too when it fits.
 constexpr int BT_WARPS = 4;
-constexpr int BT_CHUNK_MAX = 16;
+constexpr int BT_CHUNK_MAX = 16;  // reflectors staged per round (a multiple of 4)
 constexpr size_t BT_SMEM_MAX = 200 * 1024;
-// the columns live in shared memory too when at least two reflectors fit beside them
+// the columns live in shared memory too when at least one block of reflectors fits beside them
 __host__ __device__ static inline bool bt_ysmem(int n) {
-  return (int)(BT_SMEM_MAX / (sizeof(double) * (size_t)n)) - BT_WARPS >= 2;
+  return (int)(BT_SMEM_MAX / (sizeof(double) * (size_t)n)) - BT_WARPS >= 4;
 }
 __host__ __device__ static inline int bt_chunk(int n) {
   int c = (int)(BT_SMEM_MAX / (sizeof(double) * (size_t)n)) - (bt_ysmem(n) ? BT_WARPS : 0);
-  return c < 1 ? 1 : (c > BT_CHUNK_MAX ? BT_CHUNK_MAX : c);
+  c = c < 4 ? 4 : (c > BT_CHUNK_MAX ? BT_CHUNK_MAX : c);
+  return c & ~3;
 }
 __host__ __device__ static inline size_t bt_smem(int n) {
   return sizeof(double) * (size_t)n * (bt_chunk(n) + (bt_ysmem(n) ? BT_WARPS : 0));
 }
+// reflector j: v[j+1] = 1, v[r] = A[r + j n] for r > j+1; j > n-2 does not exist (zero)
+__device__ __forceinline__ double bt_v(int n, const double* __restrict__ A, int j, int r) {
+  if (j > n - 2 || r <= j) return 0.0;
+  return r == j + 1 ? 1.0 : A[r + (size_t)j * n];
+}
+// T of block g (reflectors 4g .. 4g+3), one warp: Tm[16 g + a + 4 b], upper triangular
+__device__ __forceinline__ void bt_tmat_dev(int n, const double* __restrict__ A,
+                                            const double* __restrict__ tau, double* Tm, int g,
+                                            int lane) {
+  const int j0 = 4 * g;
+  double dd[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) dd[a][b] = 0.0;
+#pragma unroll
+  for (int b = 1; b < 4; ++b) {
+    const int rb = j0 + b + 1;  // first row of reflector b (v = 1 there)
+#pragma unroll
+    for (int a = 0; a < b; ++a) {
+      double acc = 0.0;
+      for (int r = rb + lane; r < n; r += 32) acc += bt_v(n, A, j0 + a, r) * bt_v(n, A, j0 + b, r);
+      dd[a][b] = wred(acc);
+    }
+  }
+  if (lane != 0) return;
+  double t[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    const int j = j0 + a;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) t[a][b] = 0.0;
+    t[a][a] = j <= n - 2 ? tau[j] : 0.0;
+  }
+#pragma unroll
+  for (int b = 1; b < 4; ++b)
+#pragma unroll
+    for (int a = 0; a < b; ++a) {
+      double acc = 0.0;
+#pragma unroll
+      for (int c = a; c < b; ++c) acc += t[a][c] * dd[c][b];
+      t[a][b] = -t[b][b] * acc;
+    }
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) Tm[16 * g + a + 4 * b] = t[a][b];
+}
+__global__ void k_bt_tmat(int n, const double* __restrict__ A, const double* __restrict__ tau,
+                          double* Tm) {
+  const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (g * 4 > n - 2) return;
+  bt_tmat_dev(n, A, tau, Tm, g, threadIdx.x & 31);
+}
 
 __device__ __forceinline__ void backtransform_dev(int n, int k, int chunk, bool ysmem,
-                                                                 const double* __restrict__ A,
-                                                                 const double* __restrict__ tau,
-                                                                 double* Y) {
+                                                  const double* __restrict__ A,
+                                                  const double* __restrict__ Tm, double* Y) {
   extern __shared__ double smem[];  // [chunk][n] reflectors, then [BT_WARPS][n] columns
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int col = blockIdx.x * BT_WARPS + wid;
@@ -847,25 +908,42 @@ __device__ __forceinline__ void backtransform_dev(int n, int k, int chunk, bool 
   double* y = !yg ? nullptr : (ysmem ? smem + (size_t)chunk * n + (size_t)wid * n : yg);
   if (y && ysmem)
     for (int r = lane; r < n; r += 32) y[r] = yg[r];
-  // reflectors i = n-2 .. 0 ; reflector i acts on rows i+1..n-1, v[0] = 1
-  for (int top = n - 2; top >= 0; top -= chunk) {
-    const int bot = max(0, top - chunk + 1);
+  const int cb = chunk / 4;  // blocks per round
+  for (int gtop = (n - 2) / 4; gtop >= 0; gtop -= cb) {
+    const int gbot = max(0, gtop - cb + 1);
     __syncthreads();
-    for (int i = top; i >= bot; --i) {
-      double* sv = smem + (size_t)(top - i) * n;
-      for (int r = i + 1 + threadIdx.x; r < n; r += blockDim.x)
-        sv[r] = r == i + 1 ? 1.0 : A[r + (size_t)i * n];
-    }
+    for (int g = gtop; g >= gbot; --g)
+      for (int a = 0; a < 4; ++a) {
+        double* sv = smem + (size_t)((gtop - g) * 4 + a) * n;
+        for (int r = 4 * g + 1 + threadIdx.x; r < n; r += blockDim.x)
+          sv[r] = bt_v(n, A, 4 * g + a, r);
+      }
     __syncthreads();
     if (y) {
-      for (int i = top; i >= bot; --i) {
-        const double t = tau[i];
-        if (t == 0.0) continue;
-        const double* sv = smem + (size_t)(top - i) * n;
-        double s = 0.0;
-        for (int r = i + 1 + lane; r < n; r += 32) s += sv[r] * y[r];
-        s = wred(s) * t;
-        for (int r = i + 1 + lane; r < n; r += 32) y[r] -= s * sv[r];
+      for (int g = gtop; g >= gbot; --g) {
+        const double* v0 = smem + (size_t)((gtop - g) * 4) * n;
+        const double* v1 = v0 + n;
+        const double* v2 = v1 + n;
+        const double* v3 = v2 + n;
+        double w0 = 0.0, w1 = 0.0, w2 = 0.0, w3 = 0.0;
+        for (int r = 4 * g + 1 + lane; r < n; r += 32) {
+          const double yr = y[r];
+          w0 = fma(v0[r], yr, w0);
+          w1 = fma(v1[r], yr, w1);
+          w2 = fma(v2[r], yr, w2);
+          w3 = fma(v3[r], yr, w3);
+        }
+        w0 = wred(w0);
+        w1 = wred(w1);
+        w2 = wred(w2);
+        w3 = wred(w3);
+        const double* T = Tm + 16 * g;  // z = T w (upper triangular, column-major)
+        const double z0 = T[0] * w0 + T[4] * w1 + T[8] * w2 + T[12] * w3;
+        const double z1 = T[5] * w1 + T[9] * w2 + T[13] * w3;
+        const double z2 = T[10] * w2 + T[14] * w3;
+        const double z3 = T[15] * w3;
+        for (int r = 4 * g + 1 + lane; r < n; r += 32)
+          y[r] -= fma(v0[r], z0, fma(v1[r], z1, fma(v2[r], z2, v3[r] * z3)));
         __syncwarp();
       }
     }
@@ -875,9 +953,9 @@ __device__ __forceinline__ void backtransform_dev(int n, int k, int chunk, bool 
 }
 __global__ void __launch_bounds__(BT_WARPS * 32) k_backtransform(int n, int k, int chunk, bool ysmem,
                                                                  const double* __restrict__ A,
-                                                                 const double* __restrict__ tau,
+                                                                 const double* __restrict__ Tm,
                                                                  double* Y) {
-  backtransform_dev(n, k, chunk, ysmem, A, tau, Y);
+  backtransform_dev(n, k, chunk, ysmem, A, Tm, Y);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -1017,8 +1095,10 @@ void eigen_vectors_range(EigenSolver* es, int k0, int k1, double* C) {
   double* Yk = es->Y + (size_t)k0 * n;
   ++g_kernel_launches;
   const int tb_ = prof_kbegin(s);
+  ++g_kernel_launches;  // T of the blocks of four reflectors, into lu (free after the solves)
+  k_bt_tmat<<<(((n - 2) / 4 + 1) * 32 + 127) / 128, 128, 0, s>>>(n, es->A, es->tau, es->lu);
   k_backtransform<<<(k + BT_WARPS - 1) / BT_WARPS, BT_WARPS * 32, bt_smem(n), s>>>(
-      n, k, chunk, bt_ysmem(n), es->A, es->tau, Yk);
+      n, k, chunk, bt_ysmem(n), es->A, es->lu, Yk);
   prof_kend(KS_BACKTRANSFORM, tb_, s);
   // C = X Y (X upper triangular)
   if (split_gemm(n))
@@ -1356,7 +1436,14 @@ __global__ void __launch_bounds__(BT_WARPS * 32) kb_backtransform(BARGS) {
   BMOL;
   const int n = q.m.nao, k = *q.icount;
   if ((int)blockIdx.x * BT_WARPS >= k) return;  // no column of this molecule here
-  backtransform_dev(n, k, bt_chunk(n), bt_ysmem(n), q.A, q.etau, q.Y);
+  backtransform_dev(n, k, bt_chunk(n), bt_ysmem(n), q.A, q.lu, q.Y);
+}
+__global__ void kb_bt_tmat(BARGS) {
+  BMOL;
+  const int n = q.m.nao;
+  const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (g * 4 > n - 2) return;
+  bt_tmat_dev(n, q.A, q.etau, q.lu, g, threadIdx.x & 31);
 }
 __global__ void kb_scale_cols(BARGS, int weighted) {
   BMOL;
@@ -1456,6 +1543,9 @@ void eigen_vectors_b(const BatchLaunch& b) {
   prof_kend(KS_INVIT, ti, b.s);
   kb_clusters<<<dim3(b.nao_max, 1, b.count), 256, 0, b.s>>>(b.mp, b.list);
   const int tb_ = prof_kbegin(b.s);
+  ++g_kernel_launches;
+  kb_bt_tmat<<<dim3((((b.nao_max - 2) / 4 + 1) * 32 + 127) / 128, 1, b.count), 128, 0, b.s>>>(
+      b.mp, b.list);
   kb_backtransform<<<dim3((b.nao_max + BT_WARPS - 1) / BT_WARPS, 1, b.count), BT_WARPS * 32,
                      bt_smem(b.nao_max), b.s>>>(b.mp, b.list);
   prof_kend(KS_BACKTRANSFORM, tb_, b.s);

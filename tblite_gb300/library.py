@@ -90,6 +90,7 @@ _SIGNATURES = {
         None, [c_void_p, c_void_p, _dbl_p, _dbl_p, _dbl_p, _dbl_p]),
     "tblite_gb300_get_kernel_profile": (c_int, [_dbl_p, _int_p, c_int]),
     "tblite_gb300_set_split_gemm": (None, [c_int]),
+    "tblite_gb300_set_batch_streams": (None, [c_int]),
     "tblite_gb300_density_matrix_noalloc": (
         c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
     "tblite_gb300_density_matrix_noalloc_max": (c_int, []),
@@ -130,6 +131,11 @@ PHASES = ("setup", "potential", "fock", "eigensolve", "density", "mulliken", "mi
 
 def set_profiling(enable: bool) -> None:
     load().tblite_gb300_set_profiling(int(bool(enable)))
+
+
+def set_batch_streams(count: int) -> None:
+    """Streams a batch call spreads its size buckets over (1 serialises them)."""
+    load().tblite_gb300_set_batch_streams(int(count))
 
 
 def set_split_gemm(enable: bool) -> None:
