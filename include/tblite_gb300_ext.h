@@ -96,6 +96,14 @@ void tblite_gb300_set_calculator_shell_parameters(tblite_context ctx, tblite_cal
 void tblite_gb300_get_result_parameter_gradient(tblite_error error, tblite_result res,
                                                 double* dselfenergy, double* dkcn,
                                                 double* dhubbard, double* dhubbard_deriv);
+/* Slater exponent of every shell (calculator shell order); setting them redoes the STO-nG
+ * expansion of each shell (GFN2-xTB calculators) */
+void tblite_gb300_get_calculator_slater_exponents(tblite_context ctx, tblite_calculator calc,
+                                                   double* zeta);
+void tblite_gb300_set_calculator_slater_exponents(tblite_context ctx, tblite_calculator calc,
+                                                   const double* zeta);
+/* dE/d(Slater exponent) per shell, stored by a single point with the parameter gradient on */
+void tblite_gb300_get_result_slater_gradient(tblite_error error, tblite_result res, double* dzeta);
 
 /* number of engine kernels launched since the library was loaded (all threads) */
 unsigned long long tblite_gb300_get_launch_count(void);

@@ -8,8 +8,10 @@ are solved.
 
 Differentiable shell parameters (one entry per shell of the calculator, in the calculator's
 shell order): ``selfenergy`` (se0, Hartree), ``kcn`` (coordination-number shift of the self
-energy), ``hubbard`` (chemical hardness) and ``hubbard_deriv`` (third-order hardness
-derivative).  Slater exponents are not differentiable here.
+energy), ``hubbard`` (chemical hardness), ``hubbard_deriv`` (third-order hardness
+derivative) and ``slater`` (the shell's Slater exponent; the STO-nG expansion is redone for a
+new value, and dE/dzeta comes from the exponent derivative of the overlap, H0 and multipole
+integrals contracted with the converged densities).
 """
 from __future__ import annotations
 
@@ -20,7 +22,8 @@ import numpy as np
 from . import library
 from .interface import Calculator, Result
 
-PARAMETERS = ("selfenergy", "kcn", "hubbard", "hubbard_deriv")
+PARAMETERS = ("selfenergy", "kcn", "hubbard", "hubbard_deriv", "slater")
+_LEVELS = PARAMETERS[:4]  # set and read together by one C call
 
 
 def shell_count(calc: Calculator) -> int:
@@ -31,8 +34,11 @@ def shell_parameters(calc: Calculator) -> Dict[str, np.ndarray]:
     """The calculator's current per-shell parameters."""
     nsh = shell_count(calc)
     out = {k: np.zeros(nsh) for k in PARAMETERS}
-    library.load().tblite_gb300_get_calculator_shell_parameters(
-        calc._ctx, calc._calc, *[library._dp(out[k]) for k in PARAMETERS])
+    lib = library.load()
+    lib.tblite_gb300_get_calculator_shell_parameters(
+        calc._ctx, calc._calc, *[library._dp(out[k]) for k in _LEVELS])
+    lib.tblite_gb300_get_calculator_slater_exponents(calc._ctx, calc._calc,
+                                                     library._dp(out["slater"]))
     library.context_check(calc._ctx)
     return out
 
@@ -40,28 +46,35 @@ def shell_parameters(calc: Calculator) -> Dict[str, np.ndarray]:
 def set_shell_parameters(calc: Calculator, **values) -> None:
     """Replace per-shell parameters (keys of ``PARAMETERS``; missing keys stay unchanged)."""
     nsh = shell_count(calc)
-    args = []
-    keep = []
+    arrays = {}
     for k in PARAMETERS:
         v = values.get(k)
         if v is None:
-            args.append(None)
             continue
         a = np.ascontiguousarray(np.asarray(v, dtype=np.float64).reshape(-1))
         if a.size != nsh:
             raise ValueError(f"{k}: expected {nsh} shell values, got {a.size}")
-        keep.append(a)
-        args.append(library._dp(a))
-    library.load().tblite_gb300_set_calculator_shell_parameters(calc._ctx, calc._calc, *args)
+        arrays[k] = a
+    lib = library.load()
+    lib.tblite_gb300_set_calculator_shell_parameters(
+        calc._ctx, calc._calc,
+        *[library._dp(arrays[k]) if k in arrays else None for k in _LEVELS])
     library.context_check(calc._ctx)
+    if "slater" in arrays:
+        lib.tblite_gb300_set_calculator_slater_exponents(calc._ctx, calc._calc,
+                                                         library._dp(arrays["slater"]))
+        library.context_check(calc._ctx)
 
 
 def parameter_gradient(res: Result, nsh: int) -> Dict[str, np.ndarray]:
     """dE/d(parameter) stored by a single point with the parameter gradient enabled."""
     out = {k: np.zeros(nsh) for k in PARAMETERS}
     err = library._Error()
-    library.load().tblite_gb300_get_result_parameter_gradient(
-        err.h, res._res, *[library._dp(out[k]) for k in PARAMETERS])
+    lib = library.load()
+    lib.tblite_gb300_get_result_parameter_gradient(
+        err.h, res._res, *[library._dp(out[k]) for k in _LEVELS])
+    err.check()
+    lib.tblite_gb300_get_result_slater_gradient(err.h, res._res, library._dp(out["slater"]))
     err.check()
     return out
 
@@ -76,15 +89,16 @@ def _function():
     torch = _torch()
 
     class GFN2Energy(torch.autograd.Function):
-        """E(positions, selfenergy, kcn, hubbard, hubbard_deriv) for one calculator."""
+        """E(positions, selfenergy, kcn, hubbard, hubbard_deriv, slater) for one calculator."""
 
         @staticmethod
-        def forward(ctx, calc, positions, selfenergy, kcn, hubbard, hubbard_deriv):
+        def forward(ctx, calc, positions, selfenergy, kcn, hubbard, hubbard_deriv, slater):
             pos = positions.detach().to("cpu", torch.float64).numpy()
             calc.update(pos)
             set_shell_parameters(
                 calc, **{k: t.detach().to("cpu", torch.float64).numpy()
-                         for k, t in zip(PARAMETERS, (selfenergy, kcn, hubbard, hubbard_deriv))})
+                         for k, t in zip(PARAMETERS,
+                                         (selfenergy, kcn, hubbard, hubbard_deriv, slater))})
             library.set_parameter_gradient(calc._ctx, calc._calc)
             res = calc.singlepoint()
             nsh = selfenergy.numel()
@@ -106,7 +120,7 @@ _FN = None
 
 
 def gfn2_energy(calc: Calculator, positions, selfenergy=None, kcn=None, hubbard=None,
-                hubbard_deriv=None):
+                hubbard_deriv=None, slater=None):
     """Differentiable GFN2-xTB energy (Hartree) of ``calc``'s molecule at ``positions`` (Bohr,
     torch tensor [nat, 3]).  Parameters default to the calculator's current values."""
     global _FN
@@ -115,7 +129,7 @@ def gfn2_energy(calc: Calculator, positions, selfenergy=None, kcn=None, hubbard=
         _FN = _function()
     cur = shell_parameters(calc)
     vals = []
-    for k, v in zip(PARAMETERS, (selfenergy, kcn, hubbard, hubbard_deriv)):
+    for k, v in zip(PARAMETERS, (selfenergy, kcn, hubbard, hubbard_deriv, slater)):
         vals.append(v if v is not None else torch.tensor(cur[k], dtype=torch.float64))
     return _FN.apply(calc, positions, *vals)
 

@@ -104,7 +104,7 @@ struct Workspace {
   DBuf<int> b_status;
   // gradient
   DBuf<double> grad, sigma, sig_at, dEdcn;
-  DBuf<double> wbo, ones, pgrad;
+  DBuf<double> wbo, ones, pgrad, zgrad;
   // GFN1 per-shell/atom data and D3 dispersion (data and work)
   DBuf<int> sh_valence, d3_nref;
   DBuf<double> at_gam3, d3_refcn, d3_sref, d3_r4r2, d3_rcov, d3_cn, d3_a, d3_da, d3_dEdcn;
@@ -158,6 +158,7 @@ struct _tblite_calculator {
   std::vector<double> sh_alpha, sh_coeff, sh_se0, sh_kcn, sh_shpoly, sh_zeta, sh_hub, sh_gam3,
       sh_refocc, at_en, at_rad, at_rcov, at_mprad, at_vcn, at_dkern, at_qkern, at_repa, at_repz;
   double min_alpha = 1e300;
+  std::vector<int> sh_pqn;  // principal quantum number of each shell (STO-nG expansion)
   // settings (reference api/calculator.f90:78-89, scf/mixer/input.f90:28-34)
   double accuracy = 1.0;
   double etemp = 300.0 * 3.166808578545117e-06;
@@ -185,7 +186,7 @@ struct _tblite_result {
   std::vector<double> energies, gradient, sigma, qat, qsh, dpat, qpat, emo, focc, P, C, S, H, wbo;
   int wbo_channels = 0;  // 1 closed shell; 2 (total, magnetisation) for open shell
   // dE/d(per-shell parameters): self energy, its CN shift, hardness, hardness derivative
-  std::vector<double> dse, dkcn, dhub, dgam3;
+  std::vector<double> dse, dkcn, dhub, dgam3, dzeta;
   double dipole[3] = {0, 0, 0}, quadrupole[6] = {0, 0, 0, 0, 0, 0};
 };
 

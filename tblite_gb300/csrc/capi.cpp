@@ -90,6 +90,7 @@ static void build_calculator(_tblite_calculator* c, const _tblite_structure* mol
       c->sh_nprim.push_back(ng);
       c->sh_ao.push_back(c->nao);
       c->sh_zeta.push_back(zeta);
+      c->sh_pqn.push_back(pqn);
       c->sh_se0.push_back(GFN2_P_SELFENERGY[(z - 1) * 3 + s]);
       c->sh_kcn.push_back(GFN2_P_KCN[(z - 1) * 3 + l]);
       c->sh_shpoly.push_back(GFN2_P_SHPOLY[(z - 1) * 3 + l]);
@@ -339,6 +340,9 @@ static void ensure_workspace(_tblite_calculator* c) {
   const int memory = c->memory > 0 ? std::min(c->memory, c->max_iter) : c->max_iter;
   cudaStream_t s = w.stream;
   if (c->params_dirty && w.nat == c->nat && w.nao == c->nao && w.nsh == c->nsh) {
+    w.sh_alpha.upload(c->sh_alpha, s);
+    w.sh_coeff.upload(c->sh_coeff, s);
+    w.sh_zeta.upload(c->sh_zeta, s);
     w.sh_se0.upload(c->sh_se0, s);
     w.sh_kcn.upload(c->sh_kcn, s);
     w.sh_hub.upload(c->sh_hub, s);
@@ -962,6 +966,12 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
   launch_h0_gradient(m, p, w.se.p, w.P.p, w.W.p, w.vao.p, w.vdp.p, w.vqp.p, w.grad.p, w.sigma.p,
                      w.dEdcn.p, s);
   launch_cn_grad(m, p, w.dEdcn.p, w.grad.p, w.sig_at.p, s);
+  std::vector<double> h_zgrad;
+  if (c->param_grad) {  // dE/d(Slater exponent): needs W, so before W is reused below
+    w.zgrad.alloc(nsh);
+    launch_zeta_grad(m, p, w.se.p, w.P.p, w.W.p, w.vao.p, w.vdp.p, w.vqp.p, w.zgrad.p, s);
+    w.zgrad.download(h_zgrad, nsh, s);
+  }
   g_prof.end(s);
   // the result carries every orbital (wavefunction/type.f90 coeff(nao, nao)): the SCF only
   // needed the occupied ones, the empty ones come from the last tridiagonal form
@@ -1054,7 +1064,9 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
     res->dgam3.assign(h_pgrad.begin() + 2 * nsh, h_pgrad.end());
     res->dkcn.resize(nsh);
     for (int i = 0; i < nsh; ++i) res->dkcn[i] = -h_cn[c->sh_atom[i]] * res->dse[i];
+    res->dzeta = h_zgrad;
   } else {
+    res->dzeta.clear();
     res->dse.clear();
     res->dhub.clear();
     res->dgam3.clear();
@@ -1368,6 +1380,61 @@ void tblite_gb300_get_result_parameter_gradient(tblite_error error, tblite_resul
   if (dkcn) std::copy(res->dkcn.begin(), res->dkcn.end(), dkcn);
   if (dhubbard) std::copy(res->dhub.begin(), res->dhub.end(), dhubbard);
   if (dhubbard_deriv) std::copy(res->dgam3.begin(), res->dgam3.end(), dhubbard_deriv);
+}
+
+void tblite_gb300_get_calculator_slater_exponents(tblite_context ctx, tblite_calculator calc,
+                                                   double* zeta) {
+  if (!ctx) return;
+  if (!calc || !zeta) {
+    ctx->push("Calculator object or output array is missing");
+    return;
+  }
+  std::copy(calc->sh_zeta.begin(), calc->sh_zeta.begin() + calc->nsh, zeta);
+}
+
+// new Slater exponents: the STO-nG expansion of every shell is redone (slater.f90:409-511)
+void tblite_gb300_set_calculator_slater_exponents(tblite_context ctx, tblite_calculator calc,
+                                                   const double* zeta) {
+  if (!ctx) return;
+  if (!calc || !zeta) {
+    ctx->push("Calculator object or input array is missing");
+    return;
+  }
+  if (calc->method != 2 || (int)calc->sh_pqn.size() != calc->nsh) {
+    ctx->push("Slater exponents can be changed for GFN2-xTB calculators only");
+    return;
+  }
+  for (int i = 0; i < calc->nsh; ++i)
+    if (!(zeta[i] > 0.0)) {
+      ctx->push("Slater exponents must be positive");
+      return;
+    }
+  double min_alpha = 1e300;
+  for (int i = 0; i < calc->nsh; ++i) {
+    double a[MAXG] = {0}, cc[MAXG] = {0};
+    const int ng = calc->sh_nprim[i];
+    slater_to_gauss(ng, calc->sh_pqn[i], calc->sh_l[i], zeta[i], a, cc);
+    for (int k = 0; k < MAXG; ++k) {
+      calc->sh_alpha[(size_t)i * MAXG + k] = a[k];
+      calc->sh_coeff[(size_t)i * MAXG + k] = cc[k];
+      if (k < ng) min_alpha = std::min(min_alpha, a[k]);
+    }
+    calc->sh_zeta[i] = zeta[i];
+  }
+  calc->min_alpha = min_alpha;
+  calc->params_dirty = true;
+}
+
+void tblite_gb300_get_result_slater_gradient(tblite_error error, tblite_result res, double* dzeta) {
+  if (!res) {
+    set_err(error, "Result container is missing");
+    return;
+  }
+  if (res->dzeta.empty()) {
+    set_err(error, "Result does not contain a parameter gradient");
+    return;
+  }
+  if (dzeta) std::copy(res->dzeta.begin(), res->dzeta.end(), dzeta);
 }
 
 int tblite_get_version(void) { return 7 * 100 + 0; }  // 0.7.0 -> 700 (reference version.h)

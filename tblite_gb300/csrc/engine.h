@@ -278,6 +278,10 @@ void launch_wbo(const DevMol& m, const double* PS, double* wbo, double scale, cu
 // with all self energies equal to one, qsh the output shell charges
 void launch_param_grad(const DevMol& m, const Gfn2Scalars& p, const double* P, const double* Hp,
                        const double* qsh, double* out, cudaStream_t s);
+// dE/d(Slater exponent) per shell (GFN2-xTB) at the converged P, W and potentials (integrals.cu)
+void launch_zeta_grad(const DevMol& m, const Gfn2Scalars& p, const double* se, const double* P,
+                      const double* W, const double* vao, const double* vdp, const double* vqp,
+                      double* dz, cudaStream_t s);
 
 // ---------------------------------------------------------------------------------------------
 // Batched ensemble path: many molecules in one launch per step.  Every molecule owns a slice of

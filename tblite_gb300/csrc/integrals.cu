@@ -20,8 +20,8 @@ namespace tb {
 __device__ __forceinline__ int sph_of_cart_p(int c) { return c == 0 ? 2 : c - 1; }  // x->2,y->0,z->1
 __device__ __forceinline__ int cart_of_sph_p(int m) { return m == 2 ? 0 : m + 1; }
 
-struct Moments {  // per direction: m[0..5]
-  double m[3][6];
+struct Moments {  // per direction: m[0..6]
+  double m[3][7];
 };
 
 __device__ __forceinline__ void gauss_moments(const double pa[3], double eta, Moments& M) {
@@ -35,6 +35,7 @@ __device__ __forceinline__ void gauss_moments(const double pa[3], double eta, Mo
     M.m[k][3] = a3 + 3.0 * a * s2;
     M.m[k][4] = a2 * a2 + 6.0 * a2 * s2 + 3.0 * s2 * s2;
     M.m[k][5] = a3 * a2 + 10.0 * a3 * s2 + 15.0 * a * s2 * s2;
+    M.m[k][6] = a3 * a3 + 15.0 * a2 * a2 * s2 + 45.0 * a2 * s2 * s2 + 15.0 * s2 * s2 * s2;
   }
 }
 
@@ -429,6 +430,146 @@ void launch_h0_gradient(const DevMol& m, const Gfn2Scalars& p, const double* se,
                                                                    grad, sigma, dEdcn, npair);
   ++g_kernel_launches;
   k_h0_onsite_dcn<<<(m.nat + 127) / 128, 128, 0, s>>>(m, P, dEdcn);
+}
+
+// ---------------------------------------------------------------------------------------
+// dE/dzeta of the Slater exponents (GFN2-xTB), one thread per ordered shell pair (i, j): the
+// derivative acts on the i function only; pair (j, i) carries the one of zeta_j.  A primitive
+// of exponent alpha = alpha0 zeta^2 with its normalisation (2 alpha/pi)^(3/4) (4 alpha)^(l/2)
+// gives  d phi / d zeta = (2 / zeta) sum_k c_k [(3/4 + l/2) - alpha_k |r - A|^2] g_k ,  so the
+// derivative integrals are the pair's ordinary ones with (r - A)^2 inserted.  The SCF energy is
+// stationary, so (as for the nuclear gradient, h0.f90:528-560)
+//   dE/dzeta_i = sum_{mu in i, nu in j} [ (2 P h_ij - P (v_mu + v_nu) - 2 W) dS/dzeta_i
+//                                         + 2 P S dh_ij/dzeta_i - P dO/dzeta_i ],
+// O the multipole potential operator of both atoms, h_ij = (e_i + e_j)/2 hscale poly with
+// d ln hscale / d zeta_i = wexp (1/(2 zeta_i) - 1/(zeta_i + zeta_j)) off-site.  The same form
+// holds for on-site pairs (no H0 scaling there) and for i == j (bra and ket derivatives equal).
+// ---------------------------------------------------------------------------------------
+__global__ void k_zeta_grad(DevMol m, Gfn2Scalars p, const double* __restrict__ se,
+                            const double* __restrict__ P, const double* __restrict__ W,
+                            const double* __restrict__ vao, const double* __restrict__ vdp,
+                            const double* __restrict__ vqp, double* dz) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)m.nsh * m.nsh) return;
+  const int ish = (int)(t / m.nsh), jsh = (int)(t % m.nsh);
+  const int iat = m.sh_atom[ish], jat = m.sh_atom[jsh];
+  double vec[3];
+  double r2 = 0.0;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    vec[k] = m.xyz[3 * iat + k] - m.xyz[3 * jat + k];
+    r2 += vec[k] * vec[k];
+  }
+  const bool onsite = iat == jat;
+  if (!onsite && (r2 > p.h0_cutoff * p.h0_cutoff || r2 < 2.220446049250313e-16)) return;
+  const int li = m.sh_l[ish], lj = m.sh_l[jsh];
+  const int nci = 2 * li + 1, ncj = 2 * lj + 1;
+  double hij, dhij = 0.0;
+  if (onsite) {
+    hij = 0.5 * (se[ish] + se[jsh]);
+  } else {
+    const double rr = sqrt(sqrt(r2) / (m.at_rad[iat] + m.at_rad[jat]));
+    const double poly = (1.0 + m.sh_shpoly[ish] * rr) * (1.0 + m.sh_shpoly[jsh] * rr);
+    const double hs = hscale_of(m, p, ish, jsh, iat, jat);
+    const double zi = m.sh_zeta[ish], zj = m.sh_zeta[jsh];
+    hij = 0.5 * (se[ish] + se[jsh]) * hs * poly;
+    dhij = hij * p.wexp * (0.5 / zi - 1.0 / (zi + zj));
+  }
+  // potential operator of both atoms in (r - A) monomials (as in the nuclear gradient)
+  double c0 = 0.0, c1[3], c2[6];
+  {
+    double wA[6], wB[6];
+    const double* qa_ = vqp + 6 * iat;
+    const double* qb_ = vqp + 6 * jat;
+    const double tra = qa_[0] + qa_[2] + qa_[5], trb = qb_[0] + qb_[2] + qb_[5];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+      const bool diag = q == 0 || q == 2 || q == 5;
+      wA[q] = 1.5 * qa_[q] - (diag ? 0.5 * tra : 0.0);
+      wB[q] = 1.5 * qb_[q] - (diag ? 0.5 * trb : 0.0);
+    }
+    const int qa[6] = {0, 0, 1, 0, 1, 2}, qb[6] = {0, 1, 1, 2, 2, 2};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      c1[k] = vdp[3 * iat + k] + vdp[3 * jat + k];
+      c0 += vdp[3 * jat + k] * vec[k];
+    }
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+      c2[q] = wA[q] + wB[q];
+      c1[qa[q]] += wB[q] * vec[qb[q]];
+      c1[qb[q]] += wB[q] * vec[qa[q]];
+      c0 += wB[q] * vec[qa[q]] * vec[qb[q]];
+    }
+  }
+  const int n = m.nao;
+  const int io0 = m.sh_ao[ish], jo0 = m.sh_ao[jsh];
+  double ws[3][3], wp[3][3];
+  for (int cj = 0; cj < ncj; ++cj) {
+    const int ja = jo0 + (lj == 1 ? sph_of_cart_p(cj) : 0);
+    for (int ci = 0; ci < nci; ++ci) {
+      const int ia = io0 + (li == 1 ? sph_of_cart_p(ci) : 0);
+      const double pij = P[(size_t)ja * n + ia];
+      wp[cj][ci] = pij;
+      ws[cj][ci] = -pij * (vao[ja] + vao[ia]) + 2.0 * pij * hij - 2.0 * W[(size_t)ja * n + ia];
+    }
+  }
+  const double gl = 0.75 + 0.5 * li;
+  double accd = 0.0, accs = 0.0;
+  const int npi = m.sh_nprim[ish], npj = m.sh_nprim[jsh];
+  const double pi3 = 5.568327996831708;
+  for (int ip = 0; ip < npi; ++ip) {
+    const double ai = m.sh_alpha[ish * MAXG + ip];
+    const double ci_ = m.sh_coeff[ish * MAXG + ip];
+    for (int jp = 0; jp < npj; ++jp) {
+      const double aj = m.sh_alpha[jsh * MAXG + jp];
+      const double eta = ai + aj, oeta = 1.0 / eta;
+      const double est = ai * aj * r2 * oeta;
+      if (est > INTCUT) continue;
+      const double cc = ci_ * m.sh_coeff[jsh * MAXG + jp] * exp(-est) * pi3 * oeta * sqrt(oeta);
+      double pa[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) pa[k] = -vec[k] * aj * oeta;
+      Moments M;
+      gauss_moments(pa, eta, M);
+      for (int cj = 0; cj < ncj; ++cj) {
+        for (int ci = 0; ci < nci; ++ci) {
+          double V[3][5];  // (x-A)^(a+e) (x-B)^b, e = 0..4
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            const int a = cexp(li, ci, k), b = cexp(lj, cj, k);
+#pragma unroll
+            for (int e = 0; e < 5; ++e) V[k][e] = O1(M, k, a + e, b, vec[k]);
+          }
+          auto f = [&](int ex, int ey, int ez) { return V[0][ex] * V[1][ey] * V[2][ez]; };
+          // operator polynomial with the monomial (dx, dy, dz) multiplied in
+          auto op = [&](int dx, int dy, int dz) {
+            return c0 * f(dx, dy, dz) + c1[0] * f(dx + 1, dy, dz) + c1[1] * f(dx, dy + 1, dz) +
+                   c1[2] * f(dx, dy, dz + 1) + c2[0] * f(dx + 2, dy, dz) +
+                   c2[1] * f(dx + 1, dy + 1, dz) + c2[2] * f(dx, dy + 2, dz) +
+                   c2[3] * f(dx + 1, dy, dz + 1) + c2[4] * f(dx, dy + 1, dz + 1) +
+                   c2[5] * f(dx, dy, dz + 2);
+          };
+          const double s0 = f(0, 0, 0);
+          const double sd = gl * s0 - ai * (f(2, 0, 0) + f(0, 2, 0) + f(0, 0, 2));
+          const double od = gl * op(0, 0, 0) - ai * (op(2, 0, 0) + op(0, 2, 0) + op(0, 0, 2));
+          accd += cc * (ws[cj][ci] * sd - wp[cj][ci] * od);
+          accs += cc * wp[cj][ci] * s0;
+        }
+      }
+    }
+  }
+  const double val = 2.0 / m.sh_zeta[ish] * accd + 2.0 * dhij * accs;
+  atomicAdd(dz + ish, val);
+}
+
+void launch_zeta_grad(const DevMol& m, const Gfn2Scalars& p, const double* se, const double* P,
+                      const double* W, const double* vao, const double* vdp, const double* vqp,
+                      double* dz, cudaStream_t s) {
+  cudaMemsetAsync(dz, 0, sizeof(double) * m.nsh, s);
+  const long long np = (long long)m.nsh * m.nsh;
+  ++g_kernel_launches;
+  k_zeta_grad<<<(unsigned)((np + 127) / 128), 128, 0, s>>>(m, p, se, P, W, vao, vdp, vqp, dz);
 }
 
 // batched launches (blockIdx.z walks the listed molecules; S, H, D, Q start zeroed)

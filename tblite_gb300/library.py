@@ -91,6 +91,9 @@ _SIGNATURES = {
     "tblite_gb300_get_kernel_profile": (c_int, [_dbl_p, _int_p, c_int]),
     "tblite_gb300_set_split_gemm": (None, [c_int]),
     "tblite_gb300_set_batch_streams": (None, [c_int]),
+    "tblite_gb300_get_calculator_slater_exponents": (None, [c_void_p, c_void_p, _dbl_p]),
+    "tblite_gb300_set_calculator_slater_exponents": (None, [c_void_p, c_void_p, _dbl_p]),
+    "tblite_gb300_get_result_slater_gradient": (None, [c_void_p, c_void_p, _dbl_p]),
     "tblite_gb300_density_matrix_noalloc": (
         c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
     "tblite_gb300_density_matrix_noalloc_max": (c_int, []),

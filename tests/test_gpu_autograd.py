@@ -54,7 +54,7 @@ def test_position_gradient_matches_fd():
         assert abs(fd - g[a, k]) < 2e-6, (a, k, fd, g[a, k])
 
 
-@pytest.mark.parametrize("name", ["selfenergy", "kcn", "hubbard", "hubbard_deriv"])
+@pytest.mark.parametrize("name", ["selfenergy", "kcn", "hubbard", "hubbard_deriv", "slater"])
 def test_parameter_gradient_matches_fd(name):
     from tblite_gb300 import workloads
     from tblite_gb300.autograd import PARAMETERS, gfn2_energy, shell_parameters
