@@ -45,7 +45,10 @@ WORKLOADS = {"c200h402": "C200H402 GFN2-xTB energy+gradient single point (602 at
              "ensemble4096": "4096-molecule GFN2-xTB energy+gradient ensemble (50 % water clusters "
                              "k ~ log-uniform[1, 64], 50 % alkanes n ~ log-uniform[1, 60]; "
                              "3-192 atoms), batched",
-             "ensemble512": "512-molecule subset of the same ensemble generator, batched"}
+             "ensemble512": "512-molecule subset of the same ensemble generator, batched",
+             "autograd256": "256 alkanes CnH2n+2, n uniform in [4, 40] (seed 3), GFN2-xTB forces and "
+                            "dE/d(shell self energy, CN shift, hardness, third-order derivative, "
+                            "Slater exponent) through the torch.autograd bridge"}
 ENSEMBLE_SIZE = {"ensemble4096": 4096, "ensemble512": 512}
 
 
@@ -451,6 +454,89 @@ def run_batch(args):
     }
 
 
+def run_autograd(args):
+    """Differentiation: forces and parameter gradients of 256 alkanes through the
+    torch.autograd bridge; finite-difference check on a sample; adjoint time per molecule."""
+    import torch
+
+    from tblite_gb300 import _build, library, workloads
+    from tblite_gb300.autograd import PARAMETERS, gfn2_energy, shell_parameters
+    from tblite_gb300.interface import Calculator
+
+    rank, ws = _dist()
+    if rank != 0:
+        return None
+    _build.build()
+    mols = workloads.alkane_batch(256, seed=3, nmin=4, nmax=40)
+    calcs = [Calculator("GFN2-xTB", z, x) for z, x in mols]
+    base = [shell_parameters(c) for c in calcs]
+
+    def forward_backward(i):
+        pos = torch.tensor(mols[i][1], requires_grad=True)
+        prm = {k: torch.tensor(base[i][k], requires_grad=True) for k in PARAMETERS}
+        e = gfn2_energy(calcs[i], pos, **prm)
+        e.backward()
+        return pos.grad, prm
+
+    for i in range(min(args.warmup, 3)):
+        forward_backward(i)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for i in range(len(calcs)):
+            forward_backward(i)
+    t_grad = (time.perf_counter() - t0) / args.steps
+    # the same single points without the parameter gradient: the adjoint pass is the difference
+    for c in calcs:
+        library.set_parameter_gradient(c._ctx, c._calc, False)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for c in calcs:
+            c.singlepoint()
+    t_plain = (time.perf_counter() - t0) / args.steps
+    # central finite differences on three molecules (accuracy 1e-5): positions 0.5e-4 Bohr,
+    # parameters 1e-5 relative
+    errs = {"positions": 0.0, **{k: 0.0 for k in PARAMETERS}}
+    for i in (0, 1, 2):
+        c = calcs[i]
+        c.set("accuracy", 1e-5)
+        g, prm = forward_backward(i)
+        x = mols[i][1]
+
+        def energy(xx, **kw):
+            vals = {k: torch.tensor(kw.get(k, base[i][k])) for k in PARAMETERS}
+            return float(gfn2_energy(c, torch.tensor(xx), **vals))
+
+        for a, k in [(0, 0), (1, 2)]:
+            xp, xm = x.copy(), x.copy()
+            xp[a, k] += 0.5e-4
+            xm[a, k] -= 0.5e-4
+            fd = (energy(xp) - energy(xm)) / 1e-4
+            errs["positions"] = max(errs["positions"], abs(fd - float(g[a, k])))
+        for k in PARAMETERS:
+            v = base[i][k].copy()
+            h = 1e-5 * max(abs(v[0]), 1e-2)
+            v[0] += h
+            ep = energy(x, **{k: v})
+            v[0] -= 2 * h
+            em = energy(x, **{k: v})
+            errs[k] = max(errs[k], abs((ep - em) / (2 * h) - float(prm[k].grad[0])))
+        c.set("accuracy", 1.0)
+    count = len(calcs)
+    return {
+        "metric": "GFN2 energy+force+parameter-gradient evals/sec (torch.autograd bridge)",
+        "value": round(count / t_grad, 3), "unit": "evals/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(1000 * t_grad, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded alkanes)",
+        "config": {"workload": WORKLOADS[args.config], "molecules": count},
+        "adjoint_ms_per_molecule": round(1000 * (t_grad - t_plain) / count, 4),
+        "plain_ms_per_molecule": round(1000 * t_plain / count, 4),
+        "fd_max_abs_error": {k: float(f"{v:.3e}") for k, v in errs.items()},
+        "fd_sample": "molecules 0-2, accuracy 1e-5; positions 0.5e-4 Bohr, parameters 1e-5 relative "
+                     "(first shell)",
+    }
+
+
 def run_reference(args):
     from tblite_gb300 import workloads
 
@@ -467,6 +553,9 @@ def run_reference(args):
         mols = workloads.mixed_ensemble(count, seed=4)
         sample = [mols[i] for i in range(0, count, max(1, count // 16))][:16]
         sample_desc = f"{len(sample)} molecules of the ensemble per step"
+    elif args.config == "autograd256":
+        sample = workloads.alkane_batch(256, seed=3, nmin=4, nmax=40)[:16]
+        sample_desc = "16 of the 256 alkanes per step (energy + gradient)"
     else:
         sample = [workloads.config(args.config)]
         sample_desc = "1 full evaluation per step"
@@ -503,7 +592,10 @@ def main():
         args.steps = min(args.steps, 3)
         line = run_reference(args)
     else:
-        line = run_batch(args) if args.config in ENSEMBLE_SIZE else run_gb300(args)
+        if args.config == "autograd256":
+            line = run_autograd(args)
+        else:
+            line = run_batch(args) if args.config in ENSEMBLE_SIZE else run_gb300(args)
     if line is not None:
         print(json.dumps(line))
 
