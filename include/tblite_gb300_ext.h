@@ -105,8 +105,26 @@ void tblite_gb300_set_calculator_slater_exponents(tblite_context ctx, tblite_cal
 /* dE/d(Slater exponent) per shell, stored by a single point with the parameter gradient on */
 void tblite_gb300_get_result_slater_gradient(tblite_error error, tblite_result res, double* dzeta);
 
+/*
+ * Density solver of the calculator's next single points.  0 (default): the reference's
+ * diagonalisation (scf/diag.f90:62-143: generalised eigenproblem, Fermi filling,
+ * P = C f C^T).  1: spectral projection for large gapped closed-shell systems: Loewdin
+ * orthogonalisation by Newton-Schulz, second-order projection (SP2) of the orthogonalised
+ * Fock matrix, P = 2 Z X Z and W = P F P / 2, all products on the tensor cores.  It fills the
+ * reference's solver slot (scf/solver.f90:28-45, get_density / get_wdensity).  A single point
+ * with solver 1 fails for open shells and for a HOMO-LUMO gap below 80 kT (certified by
+ * Lanczos); its result has no orbital energies, occupations or coefficients.
+ */
+void tblite_gb300_set_calculator_density_solver(tblite_context ctx, tblite_calculator calc,
+                                                int solver);
+/* HOMO, LUMO (Hartree) and the bound on the sum of their errors, certified by solver 1 */
+void tblite_gb300_get_result_gap(tblite_error error, tblite_result res, double* gap);
+
 /* number of engine kernels launched since the library was loaded (all threads) */
 unsigned long long tblite_gb300_get_launch_count(void);
+/* algorithmic FP64 work (flop) of the one-molecule path's tensor-core split GEMMs since the
+ * library was loaded: 2 M N K per product, N (N + 1) K per symmetric product */
+unsigned long long tblite_gb300_get_split_gemm_flops(void);
 
 /*
  * Density matrix P = C diag(f) C^T that allocates no device memory.  No counterpart in the

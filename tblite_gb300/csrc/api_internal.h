@@ -118,8 +118,10 @@ struct Workspace {
   DBuf<double> d4_cn, d4_gw, d4_dgw, d4_gwv, d4_dgwdq, d4_dgwv_cn, d4_c6, d4_dc6, d4_e3, d4_dEdcn,
       d4_atm;
   EigenSolver* eig = nullptr;
+  Purifier* pur = nullptr;
   ~Workspace() {
     if (eig) eigen_destroy(eig);
+    if (pur) purify_destroy(pur);
     if (stream) cudaStreamDestroy(stream);
   }
 };
@@ -174,6 +176,8 @@ struct _tblite_calculator {
   bool params_dirty = false;
   // evaluate dE/d(shell parameters) with the single point
   int param_grad = 0;
+  // density solver: 0 diagonalisation (Fermi filling), 1 spectral projection (purify.cu)
+  int density_solver = 0;
   // implicit solvation container moved in by tblite_calculator_push_back
   std::unique_ptr<SolvModel> solv;
   std::unique_ptr<Workspace> ws;
@@ -187,6 +191,8 @@ struct _tblite_result {
   int wbo_channels = 0;  // 1 closed shell; 2 (total, magnetisation) for open shell
   // dE/d(per-shell parameters): self energy, its CN shift, hardness, hardness derivative
   std::vector<double> dse, dkcn, dhub, dgam3, dzeta;
+  // spectral projection: HOMO, LUMO, bound on their errors (empty after diagonalisation)
+  std::vector<double> gap;
   double dipole[3] = {0, 0, 0}, quadrupole[6] = {0, 0, 0, 0, 0, 0};
 };
 

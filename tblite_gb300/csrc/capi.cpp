@@ -773,6 +773,20 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
   DevMol m = dev_mol(c);
   double nalp = 0.0, nbet = 0.0;
   electron_counts(c, mol, &nalp, &nbet);
+  // spectral projection (purify.cu): closed shells with whole electron pairs only
+  const bool purify = c->density_solver == 1;
+  const int nocc = (int)llround(nalp);
+  if (purify) {
+    if (nalp != nbet)
+      throw std::runtime_error("the spectral-projection density solver needs a closed shell");
+    if (fabs(nalp - nocc) > 1e-10)
+      throw std::runtime_error("the spectral-projection density solver needs whole electron pairs");
+    if (w.pur && purify_capacity(w.pur) != n) {
+      purify_destroy(w.pur);
+      w.pur = nullptr;
+    }
+    if (!w.pur) w.pur = purify_create(n, s);
+  }
 
   g_prof.reset();
   // geometry-dependent setup
@@ -795,9 +809,13 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
     dsolv = dev_solv(c, mol);
     solv_setup(dsolv, w.xyz.p, w.erep.p, s);
   }
-  const int chol = eigen_set_overlap(w.eig, w.S.p);
+  int chol = 0;
+  if (purify) chol = purify_set_overlap(w.pur, w.S.p) < 0 ? 1 : 0;
+  else chol = eigen_set_overlap(w.eig, w.S.p);
   g_prof.end(s);
-  if (chol != 0) throw std::runtime_error("overlap matrix is not positive definite");
+  if (chol != 0)
+    throw std::runtime_error(purify ? "overlap orthogonalisation (Newton-Schulz) did not converge"
+                                    : "overlap matrix is not positive definite");
 
   // initial guess: restart from a compatible result, else SAD (wavefunction/guess.f90:51-120)
   std::vector<double> qsh0(nsh), dp0(3 * nat, 0.0), qp0(6 * nat, 0.0), qat0(nat);
@@ -895,26 +913,35 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
                 w.vqp.p, w.F.p, s);
     launch_pack(m, w.qsh.p, w.dpat.p, w.qpat.p, w.b_q.p, s, with_mp);  // mixer%set
     g_prof.end(s);
-    g_prof.begin(PH_EIGEN, s);
-    const int info = eigen_values(w.eig, w.F.p, w.emo.p, nev);
-    if (info != 0)
-      throw std::runtime_error("(sygvd) failed to solve eigenvalue problem. info=" +
-                               std::to_string(info));
-    launch_fermi(n, w.emo.p, nalp, nbet, kt, w.focc.p, w.scal.p, w.icount.p, s, nev);
-    w.icount.download(h_cnt, 2, s);
-    stream_wait(s);
-    if (h_cnt[1] != 0) {  // the Fermi level needs more levels: all of them from now on
-      eigen_values_rest(w.eig, nev, w.emo.p);
-      nev = n;
+    if (purify) {  // P from the Fock matrix by products alone; 0/1 occupations carry no entropy
+      g_prof.begin(PH_DENSITY, s);
+      if (purify_density(w.pur, w.F.p, nocc, w.P.p) < 0)
+        throw std::runtime_error("spectral projection (SP2) did not converge");
+      cuda_check(cudaMemsetAsync(w.scal.p, 0, sizeof(double), s), "ts");
+      g_prof.end(s);
+    } else {
+      g_prof.begin(PH_EIGEN, s);
+      const int info = eigen_values(w.eig, w.F.p, w.emo.p, nev);
+      if (info != 0)
+        throw std::runtime_error("(sygvd) failed to solve eigenvalue problem. info=" +
+                                 std::to_string(info));
       launch_fermi(n, w.emo.p, nalp, nbet, kt, w.focc.p, w.scal.p, w.icount.p, s, nev);
       w.icount.download(h_cnt, 2, s);
       stream_wait(s);
+      if (h_cnt[1] != 0) {  // the Fermi level needs more levels: all of them from now on
+        eigen_values_rest(w.eig, nev, w.emo.p);
+        nev = n;
+        launch_fermi(n, w.emo.p, nalp, nbet, kt, w.focc.p, w.scal.p, w.icount.p, s, nev);
+        w.icount.download(h_cnt, 2, s);
+        stream_wait(s);
+      }
+      eigen_vectors(w.eig, h_cnt[0], w.C.p);
+      g_prof.end(s);
+      g_prof.begin(PH_DENSITY, s);
+      density_matrix(n, h_cnt[0], w.C.p, w.focc.p, w.P.p, w.scratch.p, s,
+                     eigen_gemm_status(w.eig));
+      g_prof.end(s);
     }
-    eigen_vectors(w.eig, h_cnt[0], w.C.p);
-    g_prof.end(s);
-    g_prof.begin(PH_DENSITY, s);
-    density_matrix(n, h_cnt[0], w.C.p, w.focc.p, w.P.p, w.scratch.p, s, eigen_gemm_status(w.eig));
-    g_prof.end(s);
     g_prof.begin(PH_MULLIKEN, s);
     launch_mulliken(m, w.P.p, w.S.p, w.H.p, w.D.p, w.Q.p, w.mull.p, mulliken_chunks(n), w.qsh_o.p,
                     w.qat_o.p, w.dpat_o.p, w.qpat_o.p, w.eband.p, s);
@@ -953,6 +980,22 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
     res->energy += res->energies[i];
   }
   res->has_energy = true;
+  res->gap.clear();
+  if (purify) {  // the 0/1 occupations hold only with a gap of many kT
+    std::vector<double> gap(3);
+    g_prof.begin(PH_DENSITY, s);
+    purify_gap(w.pur, gap.data());
+    g_prof.end(s);
+    const double lower = gap[1] - gap[0] - gap[2];
+    if (!(lower >= purify_gap_kt() * kt)) {
+      char buf[200];
+      snprintf(buf, sizeof(buf),
+               "HOMO-LUMO gap %.3e Eh is below %.0f kT: the spectral-projection density solver "
+               "needs a gapped system (use diagonalisation)", gap[1] - gap[0], purify_gap_kt());
+      throw std::runtime_error(buf);
+    }
+    res->gap = gap;
+  }
 
   // gradient (singlepoint.f90:343-381): Coulomb at output moments, H0 with last potential
   g_prof.begin(PH_GRADIENT, s);
@@ -960,9 +1003,14 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
                           w.grad.p, w.sig_at.p, w.dEdcn.p, s);
   if (c->has_d4) d4_gradient(m, d4, d4w, w.qat_o.p, w.grad.p, w.sig_at.p, s);
   if (c->solv) solv_gradient(dsolv, w.xyz.p, w.qat_o.p, w.grad.p, s);
-  // W = C diag(f e) C^T  (scf/diag.f90:110-143)
-  launch_fe(n, w.focc.p, w.emo.p, w.vec_out.p, s);
-  density_matrix(n, h_cnt[0], w.C.p, w.vec_out.p, w.W.p, w.scratch.p, s, eigen_gemm_status(w.eig));
+  // W = C diag(f e) C^T  (scf/diag.f90:110-143); after projection W = P F P / 2
+  if (purify) {
+    purify_weighted(w.pur, w.F.p, w.P.p, w.W.p);
+  } else {
+    launch_fe(n, w.focc.p, w.emo.p, w.vec_out.p, s);
+    density_matrix(n, h_cnt[0], w.C.p, w.vec_out.p, w.W.p, w.scratch.p, s,
+                   eigen_gemm_status(w.eig));
+  }
   launch_h0_gradient(m, p, w.se.p, w.P.p, w.W.p, w.vao.p, w.vdp.p, w.vqp.p, w.grad.p, w.sigma.p,
                      w.dEdcn.p, s);
   launch_cn_grad(m, p, w.dEdcn.p, w.grad.p, w.sig_at.p, s);
@@ -975,10 +1023,12 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
   g_prof.end(s);
   // the result carries every orbital (wavefunction/type.f90 coeff(nao, nao)): the SCF only
   // needed the occupied ones, the empty ones come from the last tridiagonal form
-  g_prof.begin(PH_EIGEN, s);
-  eigen_values_rest(w.eig, nev, w.emo.p);
-  eigen_vectors_range(w.eig, h_cnt[0], (int)n, w.C.p);
-  g_prof.end(s);
+  if (!purify) {  // the projection has no orbitals
+    g_prof.begin(PH_EIGEN, s);
+    eigen_values_rest(w.eig, nev, w.emo.p);
+    eigen_vectors_range(w.eig, h_cnt[0], (int)n, w.C.p);
+    g_prof.end(s);
+  }
   // Wiberg/Mayer bond orders (post_processing/wbo.f90:60-115): closed shell from P; restricted
   // open shell from the spin densities with the factor 2, then (up, down) -> (total, up-down)
   g_prof.begin(PH_GRADIENT, s);
@@ -987,7 +1037,8 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
   w.wbo.alloc((size_t)nch * nat * nat);
   cuda_check(cudaMemsetAsync(w.wbo.p, 0, sizeof(double) * nch * nat * nat, s), "zero");
   if (!open_shell) {
-    gemm64(false, false, n, n, n, 1.0, w.P.p, n, w.S.p, n, 0.0, w.scratch.p, n, KM_NONE, s);
+    if (purify) purify_product(w.pur, w.P.p, w.S.p, w.scratch.p);
+    else gemm64(false, false, n, n, n, 1.0, w.P.p, n, w.S.p, n, 0.0, w.scratch.p, n, KM_NONE, s);
     launch_wbo(m, w.scratch.p, w.wbo.p, 1.0, s);
   } else {
     for (int sp = 0; sp < 2; ++sp) {  // W is free after the gradient: it holds the spin density
@@ -1010,7 +1061,7 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
   }
   g_prof.end(s);
   g_prof.begin(PH_TRANSFER, s);
-  w.C.download(res->C, (size_t)n * n, s);
+  if (!purify) w.C.download(res->C, (size_t)n * n, s);
   w.wbo.download(res->wbo, (size_t)nch * nat * nat, s);
   w.grad.download(res->gradient, 3 * nat, s);
   std::vector<double> h_sig_at, h_sigma;
@@ -1020,8 +1071,14 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
   w.qat_o.download(res->qat, nat, s);
   w.dpat_o.download(res->dpat, 3 * nat, s);
   w.qpat_o.download(res->qpat, 6 * nat, s);
-  w.emo.download(res->emo, n, s);
-  w.focc.download(res->focc, n, s);
+  if (purify) {
+    res->C.clear();
+    res->emo.clear();
+    res->focc.clear();
+  } else {
+    w.emo.download(res->emo, n, s);
+    w.focc.download(res->focc, n, s);
+  }
   w.P.download(res->P, (size_t)n * n, s);
   if (c->save_integrals) {
     w.S.download(res->S, (size_t)n * n, s);
@@ -1032,7 +1089,11 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
   g_prof.end(s);
   stream_wait(s);
   cuda_check(cudaGetLastError(), "results");
-  if (eigen_gemm_failed(w.eig))
+  int pur_status = 0;
+  if (purify)
+    cuda_check(cudaMemcpy(&pur_status, purify_status(w.pur), sizeof(int), cudaMemcpyDeviceToHost),
+               "purify status");
+  if (eigen_gemm_failed(w.eig) || pur_status != 0)
     throw std::runtime_error("tensor-core matrix product did not complete (wait limit reached)");
   g_prof.collect();
   g_prof.iterations = iscf;
@@ -1308,6 +1369,7 @@ int tblite_gb300_get_kernel_profile(double* kernel_ms, int* kernel_count, int ns
 }
 
 unsigned long long tblite_gb300_get_launch_count(void) { return g_kernel_launches; }
+unsigned long long tblite_gb300_get_split_gemm_flops(void) { return g_split_flops; }
 
 int tblite_gb300_get_result_bond_order_channels(tblite_result res) {
   return res ? res->wbo_channels : 0;
@@ -1325,6 +1387,32 @@ void tblite_gb300_set_calculator_parameter_gradient(tblite_context ctx, tblite_c
     return;
   }
   calc->param_grad = enable != 0;
+}
+
+void tblite_gb300_set_calculator_density_solver(tblite_context ctx, tblite_calculator calc,
+                                                int solver) {
+  if (!ctx) return;
+  if (!calc) {
+    ctx->push("Calculator object is missing");
+    return;
+  }
+  if (solver != 0 && solver != 1) {
+    ctx->push("density solver must be 0 (diagonalisation) or 1 (spectral projection)");
+    return;
+  }
+  calc->density_solver = solver;
+}
+
+void tblite_gb300_get_result_gap(tblite_error error, tblite_result res, double* gap) {
+  if (!res) {
+    set_err(error, "Result container is missing");
+    return;
+  }
+  if (res->gap.size() != 3) {
+    set_err(error, "Result does not contain a certified gap (spectral projection only)");
+    return;
+  }
+  if (gap) std::copy(res->gap.begin(), res->gap.end(), gap);
 }
 
 void tblite_gb300_get_calculator_shell_parameters(tblite_context ctx, tblite_calculator calc,
@@ -1624,11 +1712,11 @@ void tblite_get_result_quadrupole(tblite_error error, tblite_result res, double 
   for (int k = 0; k < 6; ++k) quadrupole[k] = res->quadrupole[k];
 }
 void tblite_get_result_orbital_energies(tblite_error error, tblite_result res, double* emo) {
-  RESULT_GUARD(res->has_wfn, "Result does not contain orbital energies");
+  RESULT_GUARD(res->has_wfn && !res->emo.empty(), "Result does not contain orbital energies");
   std::copy(res->emo.begin(), res->emo.end(), emo);
 }
 void tblite_get_result_orbital_occupations(tblite_error error, tblite_result res, double* occ) {
-  RESULT_GUARD(res->has_wfn, "Result does not contain orbital occupations");
+  RESULT_GUARD(res->has_wfn && !res->focc.empty(), "Result does not contain orbital occupations");
   std::copy(res->focc.begin(), res->focc.end(), occ);
 }
 void tblite_get_result_orbital_coefficients(tblite_error error, tblite_result res, double* cmat) {

@@ -20,6 +20,9 @@ namespace tb {
 
 // number of engine kernels launched since library load (instrumentation)
 extern std::atomic<unsigned long long> g_kernel_launches;
+// algorithmic FP64 work (flop) issued to the one-molecule split GEMM since library load:
+// 2 M N K per product, N (N + 1) K for a symmetric one (instrumentation)
+extern std::atomic<unsigned long long> g_split_flops;
 
 // wait for the stream with a blocking-sync event (the host thread sleeps instead of spinning)
 void stream_wait(cudaStream_t s);
@@ -245,6 +248,26 @@ inline int scf_eigenvalue_count(int n, double nalp) {
 void eigen_vectors(EigenSolver*, int k, double* C);
 // eigenvectors k0 .. k1-1 into columns k0 .. k1-1 of C (same tridiagonal form)
 void eigen_vectors_range(EigenSolver*, int k0, int k1, double* C);
+
+// density by spectral projection (purify.cu): closed-shell, gapped systems at large n
+struct Purifier;
+Purifier* purify_create(int n, cudaStream_t s);
+void purify_destroy(Purifier*);
+int purify_capacity(const Purifier*);
+// Loewdin orthogonaliser S^-1/2 once per geometry: Newton-Schulz iterations, -1 on failure
+int purify_set_overlap(Purifier*, const double* S);
+// P = 2 (projector on the nocc lowest orbitals of F C = S C e): SP2 iterations, -1 on failure
+int purify_density(Purifier*, const double* F, int nocc, double* P);
+// W = P F P / 2 after purify_density
+void purify_weighted(Purifier*, const double* F, const double* P, double* W);
+// C = A B on the split GEMM (n x n, column-major)
+void purify_product(Purifier*, const double* A, const double* B, double* C);
+// HOMO, LUMO and the bound on their errors (Lanczos) of the last purify_density call
+void purify_gap(Purifier*, double* gap3);
+// smallest certified gap in kT; the purifier's tensor-core GEMM status word
+double purify_gap_kt();
+int* purify_status(Purifier*);
+int purify_iterations(const Purifier*);
 
 // dense FP64 GEMM (column-major, BLAS semantics); kmode skips zero triangles
 // KM_SYM (or-ed with one of the others): the product is symmetric (M == N); only the tiles on

@@ -396,6 +396,7 @@ void ogemm(bool ta, bool tb, int M, int N, int K, const double* A, const double*
     attr = true;
   }
   Site s{M, N, K, ld, A, ta, B, tb, C, kmode & 7, (kmode & KM_SYM) != 0};
+  g_split_flops += s.sym ? (unsigned long long)N * (N + 1) * K : 2ull * M * N * K;
   const int tk = prof_kbegin(st);
   g_kernel_launches += 2;
   k_oexp<<<(M + ld + 7) / 8, 256, 0, st>>>(s, ex);

@@ -22,6 +22,7 @@
 namespace tb {
 
 std::atomic<unsigned long long> g_kernel_launches{0};
+std::atomic<unsigned long long> g_split_flops{0};
 
 void stream_wait(cudaStream_t s) {
   thread_local cudaEvent_t ev = nullptr;

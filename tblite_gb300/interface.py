@@ -74,6 +74,8 @@ class Result:
     def get(self, attribute: str):
         if attribute == "natoms":
             return library.result_int(self._res, "number_of_atoms")
+        if attribute == "gap":  # extension: HOMO, LUMO, error bound (spectral projection)
+            return library.result_gap(self._res)
         if attribute == "norbitals":
             return library.result_int(self._res, "number_of_orbitals")
         if attribute not in self._shapes:
@@ -153,6 +155,8 @@ class Calculator(Structure):
             "annealing": lambda v: lib.tblite_set_calculator_temperature_annealing(
                 self._ctx, self._calc, float(v[0]), int(v[1]), int(v[2])),
             "verbosity": lambda v: lib.tblite_set_context_verbosity(self._ctx, int(v)),
+            # extension: "diagonalization" (default) or "purification" (purify.cu)
+            "density-solver": lambda v: library.set_density_solver(self._ctx, self._calc, v),
         }
         if attribute not in setters:
             raise TBLiteValueError(f"Attribute '{attribute}' is not supported in this calculator")

@@ -80,6 +80,7 @@ _SIGNATURES = {
     "tblite_gb300_set_profiling": (None, [c_int]),
     "tblite_gb300_get_profile": (c_int, [_dbl_p, _int_p, c_int, _dbl_p, _int_p]),
     "tblite_gb300_get_launch_count": (ctypes.c_ulonglong, []),
+    "tblite_gb300_get_split_gemm_flops": (ctypes.c_ulonglong, []),
     "tblite_gb300_get_result_bond_order_channels": (c_int, [c_void_p]),
     "tblite_gb300_set_calculator_parameter_gradient": (None, [c_void_p, c_void_p, c_int]),
     "tblite_gb300_get_calculator_shell_parameters": (
@@ -94,6 +95,8 @@ _SIGNATURES = {
     "tblite_gb300_get_calculator_slater_exponents": (None, [c_void_p, c_void_p, _dbl_p]),
     "tblite_gb300_set_calculator_slater_exponents": (None, [c_void_p, c_void_p, _dbl_p]),
     "tblite_gb300_get_result_slater_gradient": (None, [c_void_p, c_void_p, _dbl_p]),
+    "tblite_gb300_set_calculator_density_solver": (None, [c_void_p, c_void_p, c_int]),
+    "tblite_gb300_get_result_gap": (None, [c_void_p, c_void_p, _dbl_p]),
     "tblite_gb300_density_matrix_noalloc": (
         c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
     "tblite_gb300_density_matrix_noalloc_max": (c_int, []),
@@ -173,6 +176,11 @@ def get_kernel_profile():
 
 def launch_count() -> int:
     return int(load().tblite_gb300_get_launch_count())
+
+
+def split_gemm_flops() -> int:
+    """Algorithmic FP64 flop issued to the one-molecule split GEMM since library load."""
+    return int(load().tblite_gb300_get_split_gemm_flops())
 
 
 def exported_symbols():
@@ -272,6 +280,30 @@ def result_array(res, name, shape):
     getattr(lib, f"tblite_get_result_{name}")(err.h, res, _dp(out))
     err.check()
     return out
+
+
+def result_gap(res):
+    """HOMO, LUMO and the bound on their errors certified by the spectral-projection solver."""
+    lib = load()
+    err = _Error()
+    out = np.zeros(3, dtype=np.float64)
+    lib.tblite_gb300_get_result_gap(err.h, res, _dp(out))
+    err.check()
+    return out
+
+
+DENSITY_SOLVERS = {"diagonalization": 0, "diagonalisation": 0, "purification": 1}
+
+
+def set_density_solver(ctx, calc, solver):
+    """Density solver of the next single points: "diagonalization" (default, Fermi filling of
+    the eigenvalues) or "purification" (spectral projection on the tensor cores, closed-shell
+    systems with a gap of at least 80 kT)."""
+    code = DENSITY_SOLVERS.get(solver, solver) if isinstance(solver, str) else int(solver)
+    if not isinstance(code, int):
+        raise ValueError(f"unknown density solver {solver!r}")
+    load().tblite_gb300_set_calculator_density_solver(ctx, calc, code)
+    context_check(ctx)
 
 
 def result_int(res, name):

@@ -109,3 +109,20 @@ def test_unsupported_element_message():
 
     with pytest.raises(TBLiteRuntimeError, match="d shells"):
         interface.Calculator("GFN2-xTB", [26, 1], [[0, 0, 0], [0, 0, 3.0]])
+
+
+def test_density_solver_setting():
+    """The density-solver key takes the two solver names; other codes are refused, and a result
+    without a spectral projection has no gap certificate."""
+    from tblite_gb300 import interface, workloads
+
+    z, x = workloads.water_cluster((2, 1, 1), seed=5)
+    calc = interface.Calculator("GFN2-xTB", z, x)
+    calc.set("density-solver", "purification")
+    calc.set("density-solver", "diagonalization")
+    with pytest.raises(TBLiteRuntimeError, match="density solver"):
+        calc.set("density-solver", 2)
+    with pytest.raises(ValueError):
+        calc.set("density-solver", "lanczos")
+    with pytest.raises(TBLiteRuntimeError, match="gap"):
+        interface.Result().get("gap")

@@ -1,0 +1,140 @@
+"""Spectral-projection density solver (purify.cu) against diagonalisation and the oracle
+(needs a GPU).
+
+For a closed shell with a HOMO-LUMO gap of many kT the Fermi occupations at 300 K are 0 or 1 to
+machine precision, so the projection P = 2 Z X Z (Z = S^-1/2 by Newton-Schulz, X by SP2) and
+W = P F P / 2 must reproduce the reference's diagonalisation path (scf/diag.f90:62-143): energy,
+atomic energies and charges, gradient, virial and bond orders at |dE| <= 1e-7 Eh,
+charges <= 1e-6 e, gradient <= 1e-6 Eh/Bohr.  The Lanczos gap certificate must bracket the
+HOMO and LUMO of the eigen solver, and the solver must refuse open shells, small gaps and the
+orbital getters.  The 1000-water cluster with ALPB(water) (6000 AOs) is checked against the
+oracle's result in tests/golden/water1000_alpb.npz (made by make_water1000.py).
+"""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+E_TOL, Q_TOL, G_TOL = 1e-7, 1e-6, 1e-6
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    from tblite_gb300 import _build
+
+    _build.build()
+
+
+def _run(method, z, x, solver, charge=None, uhf=None, acc=1.0, solvent=False, **settings):
+    from tblite_gb300.interface import Calculator
+
+    calc = Calculator(method, z, x, charge=charge, uhf=uhf)
+    calc.set("accuracy", acc)
+    calc.set("density-solver", solver)
+    for k, v in settings.items():
+        calc.set(k, v)
+    if solvent:
+        calc.add("alpb-solvation", "water")
+    return calc.singlepoint()
+
+
+def _compare(method, z, x, acc=1e-3, solvent=False):
+    pur = _run(method, z, x, "purification", acc=acc, solvent=solvent)
+    eig = _run(method, z, x, "diagonalization", acc=acc, solvent=solvent)
+    assert abs(pur.get("energy") - eig.get("energy")) < E_TOL
+    assert np.max(np.abs(pur.get("energies") - eig.get("energies"))) < E_TOL
+    assert np.max(np.abs(pur.get("charges") - eig.get("charges"))) < Q_TOL
+    assert np.max(np.abs(pur.get("gradient") - eig.get("gradient"))) < G_TOL
+    assert np.max(np.abs(pur.get("virial") - eig.get("virial"))) < 1e-5
+    assert np.max(np.abs(pur.get("bond-orders") - eig.get("bond-orders"))) < 1e-6
+    assert np.max(np.abs(pur.get("density-matrix") - eig.get("density-matrix"))) < 1e-6
+    # the certificate brackets the eigen solver's frontier orbitals (the two SCF runs stop at
+    # slightly different Fock matrices: 1e-5 Eh of slack)
+    homo, lumo, bound = pur.get("gap")
+    emo, occ = eig.get("orbital-energies"), eig.get("orbital-occupations")
+    k = int(round(occ.sum() / 2))
+    assert abs(homo - emo[k - 1]) <= bound + 1e-5
+    assert abs(lumo - emo[k]) <= bound + 1e-5
+    return pur, eig
+
+
+def test_water32_against_eigen_and_oracle():
+    from oracle import gfn2
+    from tblite_gb300 import workloads
+
+    z, x = workloads.config("h2o32")
+    pur, _ = _compare("GFN2-xTB", z, x, acc=1.0)
+    ref = gfn2.singlepoint(gfn2.new_calc(gfn2.Molecule(np.asarray(z), np.asarray(x))))
+    assert abs(pur.get("energy") - ref.energy) < E_TOL
+    assert np.max(np.abs(pur.get("charges") - ref.qat)) < Q_TOL
+    assert np.max(np.abs(pur.get("gradient") - ref.gradient)) < G_TOL
+
+
+def test_alkane():
+    from tblite_gb300 import workloads
+
+    z, x = workloads.alkane(30, seed=5)
+    _compare("GFN2-xTB", z, x)
+
+
+def test_gfn1_water_cluster():
+    from tblite_gb300 import workloads
+
+    z, x = workloads.water_cluster((3, 3, 2), seed=9)
+    _compare("GFN1-xTB", z, x)
+
+
+def test_solvated_water_cluster():
+    from tblite_gb300 import workloads
+
+    z, x = workloads.water_cluster((4, 4, 4), seed=12)
+    _compare("GFN2-xTB", z, x, solvent=True)
+
+
+def test_no_orbitals_in_result():
+    from tblite_gb300.exceptions import TBLiteRuntimeError
+    from tblite_gb300 import workloads
+
+    z, x = workloads.water_cluster((2, 1, 1), seed=11)
+    res = _run("GFN2-xTB", z, x, "purification")
+    for key in ("orbital-energies", "orbital-occupations", "orbital-coefficients"):
+        with pytest.raises(TBLiteRuntimeError):
+            res.get(key)
+
+
+def test_open_shell_refused():
+    from tblite_gb300.exceptions import TBLiteRuntimeError
+    from tblite_gb300 import workloads
+
+    z, x = workloads.water_cluster((2, 1, 1), seed=15)
+    with pytest.raises(TBLiteRuntimeError, match="closed shell"):
+        _run("GFN2-xTB", z, x, "purification", charge=1.0)
+
+
+def test_small_gap_refused():
+    """At kT = 0.0633 Eh (20000 K), 80 kT (5 Eh) exceeds any gap: the certificate fails."""
+    from tblite_gb300.exceptions import TBLiteRuntimeError
+    from tblite_gb300 import workloads
+
+    z, x = workloads.water_cluster((2, 1, 1), seed=11)
+    with pytest.raises(TBLiteRuntimeError, match="gap"):
+        _run("GFN2-xTB", z, x, "purification", temperature=20000.0 * 3.166808578545117e-06)
+
+
+@pytest.mark.skipif(not (GOLDEN / "water1000_alpb.npz").exists(), reason="fixture not generated")
+def test_water1000_alpb_against_oracle():
+    """1000 waters, ALPB(water), 6000 AOs: the full-size solvated cluster."""
+    from tblite_gb300 import workloads
+
+    ref = np.load(GOLDEN / "water1000_alpb.npz")
+    z, x = workloads.config("h2o1000")
+    res = _run("GFN2-xTB", z, x, "purification", solvent=True)
+    assert abs(res.get("energy") - float(ref["energy"])) < E_TOL
+    assert np.max(np.abs(res.get("charges") - ref["charges"])) < Q_TOL
+    assert np.max(np.abs(res.get("gradient") - ref["gradient"])) < G_TOL
+    homo, lumo, bound = res.get("gap")
+    assert abs(homo - float(ref["homo"])) <= bound + 1e-5
+    assert abs(lumo - float(ref["lumo"])) <= bound + 1e-5
