@@ -120,6 +120,20 @@ void tblite_gb300_set_calculator_density_solver(tblite_context ctx, tblite_calcu
 /* HOMO, LUMO (Hartree) and the bound on the sum of their errors, certified by solver 1 */
 void tblite_gb300_get_result_gap(tblite_error error, tblite_result res, double* gap);
 
+/*
+ * C = A B on the pipelined FP64-accurate split GEMM (BF16 tensor cores), device pointers,
+ * column-major: A m x k (leading dimension m), B k x n (leading dimension k), C m x n (leading
+ * dimension m); sym != 0: C is symmetric (m == n), its lower tiles are computed and mirrored.
+ * stream: a cudaStream_t (NULL: the default stream); the call synchronises it.  Returns 0, 1 if
+ * the tensor-core pipeline did not answer within its wait limit, -1 on bad arguments, -2 on a
+ * CUDA error.  No counterpart in the reference (its products are BLAS dgemm calls).
+ */
+int tblite_gb300_split_gemm(int m, int n, int k, const double* a, const double* b, double* c,
+                            int sym, void* stream);
+/* products of the spectral-projection solver: 1 (default) pipelined split GEMM from slice
+ * images, 0 the per-tile split GEMM */
+void tblite_gb300_set_pipelined_gemm(int enable);
+
 /* number of engine kernels launched since the library was loaded (all threads) */
 unsigned long long tblite_gb300_get_launch_count(void);
 /* algorithmic FP64 work (flop) of the one-molecule path's tensor-core split GEMMs since the

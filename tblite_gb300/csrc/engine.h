@@ -249,6 +249,23 @@ void eigen_vectors(EigenSolver*, int k, double* C);
 // eigenvectors k0 .. k1-1 into columns k0 .. k1-1 of C (same tridiagonal form)
 void eigen_vectors_range(EigenSolver*, int k0, int k1, double* C);
 
+// pipelined split GEMM (ozaki_pipe.cu): a matrix is split once into a slice image (per line a
+// power-of-two exponent and eight BF16 slices in the tensor cores' shared-memory layout), then
+// C = op(A) op(B) runs from two images
+struct PImage {
+  int lines = 0, K = 0;
+  uint16_t* data = nullptr;  // pimage_bytes(lines, K) bytes
+  int* e = nullptr;          // pimage_lines(lines) ints
+};
+size_t pimage_bytes(int lines, int K);
+int pimage_lines(int lines);
+// line i, position k: M[i + k ld] (kcontig 0) or M[k + i ld] (kcontig 1)
+void psplit(const double* M, int ld, int kcontig, int lines, int K, PImage& img, cudaStream_t s);
+// C = 2^eshiftA op(A) op(B); sym: symmetric product (lower tiles computed, mirrored); status
+// set to 1 if a wait of the tensor-core pipeline ran out
+void pgemm(const PImage& A, const PImage& B, double* C, int ldc, bool sym, int* status,
+           cudaStream_t s, int eshiftA = 0);
+
 // density by spectral projection (purify.cu): closed-shell, gapped systems at large n
 struct Purifier;
 Purifier* purify_create(int n, cudaStream_t s);

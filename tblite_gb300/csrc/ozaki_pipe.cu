@@ -1,0 +1,516 @@
+// Pipelined FP64-accurate split GEMM on the BF16 tensor cores for the one-molecule path.
+//
+// Same arithmetic as ozaki.cu (eight 7-bit slices per FP64 value, 36 exact BF16 slice products
+// per FP64 product, exact integer level sums moved to int64 every 192 values of k), but the
+// operands are split once per matrix instead of once per tile pair:
+//
+//   psplit   turns a matrix into a slice image: per line (row of op(A) or column of op(B)) a
+//            power-of-two exponent, and the eight BF16 slices laid out exactly as the tensor
+//            cores read them from shared memory (K-major core matrices of 8 lines x 16 bytes),
+//            image[k chunk of 32][slice][k step of 16][line block of 64][8 x 256 bytes];
+//   pgemm    (kernel k_opipe) one 128 x 64 output tile per CTA, 10 warps: warp 0 streams the slices of each
+//            k chunk (96 KB: A 64 KB, B 32 KB) with cp.async.bulk into a two-stage shared
+//            memory ring (mbarrier complete_tx); warp 1 issues the 72 tcgen05.mma of a chunk
+//            (M 128, N 64, K 16, FP32 accumulators in TMEM: levels 2..6 exact, 7..9 shared)
+//            and commits them to the stage's "empty" barrier; warps 2..9 move the exact levels
+//            out of TMEM into int64 registers after every 6 chunks and write C at the end.
+//
+// Every wait is bounded; a wait that runs out sets a CTA-wide abort flag, the other roles leave
+// their loops, copies and MMAs still in flight are waited for (bounded), TMEM is freed and the
+// status word is set.  Tiles are visited in groups of 8 row blocks so that the slices a wave of
+// CTAs reads stay in L2.  Symmetric products compute the tiles on and below the diagonal and
+// write each element also to its mirror position.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+
+#include "engine.h"
+
+namespace tb {
+
+namespace {
+
+constexpr int PP_M = 128, PP_N = 64, PP_KC = 32, PP_FLUSH = 6, PP_THREADS = 320;
+constexpr int PP_STAGES = 2;  // the producer's bookkeeping below assumes two
+constexpr int PP_A_BYTES = 8 * 2 * 4096;  // 8 slices x 2 k steps x (128 lines x 16 k x 2 B)
+constexpr int PP_B_BYTES = 8 * 2 * 2048;  // 8 slices x 2 k steps x (64 lines x 16 k x 2 B)
+constexpr int PP_STAGE_BYTES = PP_A_BYTES + PP_B_BYTES;
+constexpr int PP_SMEM = PP_STAGES * PP_STAGE_BYTES + 1024;
+constexpr int PP_TMEM_COLS = 512;
+constexpr int PP_GROUP = 8;  // row blocks per tile group
+constexpr int PP_WAIT = 1 << 22;
+
+void ck(cudaError_t e, const char* what) {
+  if (e != cudaSuccess)
+    throw std::runtime_error(std::string("CUDA error '") + cudaGetErrorString(e) + "' in " + what);
+}
+
+__device__ __forceinline__ uint32_t su32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr) {
+  return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)(128 >> 4) << 16) |
+         ((uint64_t)(256 >> 4) << 32) | ((uint64_t)1 << 46);
+}
+__device__ __forceinline__ bool try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait; gives up early once another role has aborted (abort != nullptr)
+__device__ __forceinline__ bool wait_bar(uint32_t bar, uint32_t parity, volatile int* abort) {
+  for (int it = 0; it < PP_WAIT; ++it) {
+    if (try_wait(bar, parity)) return true;
+    if (abort && *abort) return false;
+  }
+  return false;
+}
+
+// BF16 bits of (-1)^sign a 2^-7p for an integer 0 <= a < 128 (exact: at most 7 significant bits)
+__device__ __forceinline__ uint32_t slice_bits(uint32_t a, int p, uint32_t sign) {
+  if (a == 0) return 0u;
+  const uint32_t u = __float_as_uint((float)a) - ((uint32_t)(7 * p) << 23);
+  return (u >> 16) | (sign << 15);
+}
+
+// ---- exponents: e = ilogb(max |x|) + 1 of every line ------------------------------------------
+// lines contiguous in memory (element (i, k) at M[i + k ld]): 32 lines per block, the 8 warps
+// take every 8th k (coalesced 256-byte rows), then a shared-memory reduction
+__global__ void __launch_bounds__(256) k_pexp_rows(const double* __restrict__ M, int ld,
+                                                   int lines, int K, int Lp, int* e) {
+  __shared__ double part[8][33];
+  const int li = threadIdx.x & 31, kg = threadIdx.x >> 5;
+  const int i = blockIdx.x * 32 + li;
+  double mx = 0.0;
+  if (i < lines)
+    for (int k = kg; k < K; k += 8) mx = fmax(mx, fabs(M[i + (size_t)k * ld]));
+  part[kg][li] = mx;
+  __syncthreads();
+  if (kg == 0 && i < Lp) {
+    for (int g = 1; g < 8; ++g) mx = fmax(mx, part[g][li]);
+    e[i] = mx > 0.0 ? ilogb(mx) + 1 : 0;
+  }
+}
+// k contiguous (element (i, k) at M[k + i ld]): one warp per line
+__global__ void k_pexp_cols(const double* __restrict__ M, int ld, int lines, int K, int Lp,
+                            int* e) {
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (i >= Lp) return;
+  double mx = 0.0;
+  if (i < lines)
+    for (int k = lane; k < K; k += 32) mx = fmax(mx, fabs(M[k + (size_t)i * ld]));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if (lane == 0) e[i] = mx > 0.0 ? ilogb(mx) + 1 : 0;
+}
+
+// ---- slice image: one block per (64 lines, 32 k); the FP64 tile goes through shared memory so
+// both memory orders read coalesced; each thread splits 8 consecutive k of one line
+__global__ void __launch_bounds__(256) k_psplit(const double* __restrict__ M, int ld, int kcontig,
+                                                int lines, int K, int nlb,
+                                                const int* __restrict__ e, uint16_t* img) {
+  __shared__ double tile[64][33];
+  const int lb = blockIdx.x, kc = blockIdx.y, t = threadIdx.x;
+  const int l0 = lb * 64, k0 = kc * PP_KC;
+  if (!kcontig) {
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      const int li = t & 63, kk = (t >> 6) + 4 * r;
+      const int i = l0 + li, k = k0 + kk;
+      tile[li][kk] = (i < lines && k < K) ? M[i + (size_t)k * ld] : 0.0;
+    }
+  } else {
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      const int kk = t & 31, li = (t >> 5) + 8 * r;
+      const int i = l0 + li, k = k0 + kk;
+      tile[li][kk] = (i < lines && k < K) ? M[k + (size_t)i * ld] : 0.0;
+    }
+  }
+  __syncthreads();
+  const int li = t & 63, g = t >> 6;  // k group of 8: 0..3
+  const int i = l0 + li;
+  const int ei = e[i];
+  uint32_t w[8][4];
+#pragma unroll
+  for (int p = 0; p < 8; ++p) w[p][0] = w[p][1] = w[p][2] = w[p][3] = 0u;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    const double x = tile[li][8 * g + c];
+    const uint64_t bits = (uint64_t)__double_as_longlong(x);
+    const uint32_t sign = (uint32_t)(bits >> 63);
+    const int ex = (int)((bits >> 52) & 0x7FF);
+    uint64_t Y = 0;
+    if (ex != 0) {  // zero and subnormals give zero slices
+      const uint64_t m = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+      const int sh = ex - ei - 1019;  // Y = |x| 2^(56 - e) < 2^56
+      if (sh >= 0) Y = m << sh;
+      else if (sh > -64) Y = m >> (-sh);
+    }
+#pragma unroll
+    for (int p = 0; p < 8; ++p) {
+      const uint32_t a = (uint32_t)(Y >> (49 - 7 * p)) & 0x7Fu;
+      w[p][c >> 1] |= slice_bits(a, p, sign) << ((c & 1) * 16);
+    }
+  }
+  const int ks = g >> 1, half = g & 1;
+  const int rg = li >> 3, r = li & 7;
+#pragma unroll
+  for (int p = 0; p < 8; ++p) {
+    const size_t off = ((((size_t)kc * 8 + p) * 2 + ks) * nlb + lb) * 1024 + rg * 128 + half * 64 +
+                       r * 8;
+    *reinterpret_cast<uint4*>(img + off) = make_uint4(w[p][0], w[p][1], w[p][2], w[p][3]);
+  }
+}
+
+struct PipeArgs {
+  const uint16_t* A;  // slice image of op(A) (lines = rows, nlbA line blocks of 64)
+  const uint16_t* B;  // slice image of op(B) (lines = columns)
+  const int* eA;
+  const int* eB;
+  int eshiftA;  // added to every exponent of A (scaling A by a power of two)
+  int nlbA, nlbB;
+  int M, N, nkc;  // nkc: k chunks of 32
+  double* C;
+  int ldc;
+  int sym;
+  int* status;
+};
+
+__global__ void __launch_bounds__(PP_THREADS, 1) k_opipe(PipeArgs a) {
+  // ---- tile of this CTA: groups of PP_GROUP row blocks, column blocks inside a group
+  const int mt = (a.M + PP_M - 1) / PP_M, nt = (a.N + PP_N - 1) / PP_N;
+  const int b = blockIdx.x;
+  const int gid = b / (PP_GROUP * nt);
+  const int first = gid * PP_GROUP;
+  const int gsize = min(mt - first, PP_GROUP);
+  const int inner = b - gid * PP_GROUP * nt;
+  const int tm = first + inner % gsize, tn = inner / gsize;
+  const int i0 = tm * PP_M, j0 = tn * PP_N;
+  if (a.sym && i0 + PP_M - 1 < j0) return;  // strictly above the diagonal: mirrored
+
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem =
+      smem_raw + ((1024 - (su32(smem_raw) & 1023)) & 1023);  // 1 KB aligned stages
+  __shared__ __align__(8) uint64_t full[PP_STAGES], empty[PP_STAGES], accf, accfree, fin;
+  __shared__ uint32_t tmem_base;
+  __shared__ int abort_flag;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  volatile int* abort = &abort_flag;
+
+  if (tid == 0) {
+    for (int s = 0; s < PP_STAGES; ++s) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&full[s])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&empty[s])));
+    }
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&accf)));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 256;" ::"r"(su32(&accfree)));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&fin)));
+    asm volatile("fence.mbarrier_init.release.cluster;");
+    abort_flag = 0;
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                 ::"r"(su32(&tmem_base)), "r"(PP_TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = tmem_base;
+  const int nkc = a.nkc;
+  const int nwin = (nkc + PP_FLUSH - 1) / PP_FLUSH;
+
+  if (warp == 0) {
+    // ---- producer: one elected lane streams the slices of every k chunk
+    if (lane == 0) {
+      const int lbA = i0 / 64, lbB = j0 / 64;
+      int last0 = -1, last1 = -1;  // last chunk issued into stage 0 / 1
+      for (int c = 0; c < nkc; ++c) {
+        const int s = c % PP_STAGES;
+        if (c >= PP_STAGES &&
+            !wait_bar(su32(&empty[s]), (uint32_t)(((c - PP_STAGES) / PP_STAGES) & 1), abort)) {
+          if (!*abort) atomicExch(&abort_flag, 1);
+          break;
+        }
+        const uint32_t bar = su32(&full[s]);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
+                     "r"(PP_STAGE_BYTES)
+                     : "memory");
+        unsigned char* st = smem + (size_t)s * PP_STAGE_BYTES;
+#pragma unroll 1
+        for (int p = 0; p < 8; ++p)
+#pragma unroll 1
+          for (int ks = 0; ks < 2; ++ks) {
+            const size_t blk = ((size_t)c * 8 + p) * 2 + ks;
+            const uint16_t* srcA = a.A + (blk * a.nlbA + lbA) * 1024;
+            const uint16_t* srcB = a.B + (blk * a.nlbB + lbB) * 1024;
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], "
+                "%2, [%3];" ::"r"(su32(st + (p * 2 + ks) * 4096)),
+                "l"(srcA), "r"(4096), "r"(bar)
+                : "memory");
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], "
+                "%2, [%3];" ::"r"(su32(st + PP_A_BYTES + (p * 2 + ks) * 2048)),
+                "l"(srcB), "r"(2048), "r"(bar)
+                : "memory");
+          }
+        if (s == 0) last0 = c;
+        else last1 = c;
+      }
+      // copies still in flight complete on their own; wait for them before the CTA ends
+      if (last0 >= 0) wait_bar(su32(&full[0]), (uint32_t)((last0 / PP_STAGES) & 1), nullptr);
+      if (last1 >= 0) wait_bar(su32(&full[1]), (uint32_t)((last1 / PP_STAGES) & 1), nullptr);
+    }
+  } else if (warp == 1) {
+    // ---- MMA issuer
+    if (lane == 0) {
+      const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) |
+                             ((uint32_t)(PP_N >> 3) << 17) | ((uint32_t)(PP_M >> 4) << 24);
+      for (int c = 0; c < nkc; ++c) {
+        const int s = c % PP_STAGES;
+        const int win = c / PP_FLUSH;
+        const bool win_start = (c % PP_FLUSH) == 0;
+        if (win_start && win > 0 &&
+            !wait_bar(su32(&accfree), (uint32_t)((win - 1) & 1), abort)) {
+          atomicExch(&abort_flag, 1);
+          break;
+        }
+        if (!wait_bar(su32(&full[s]), (uint32_t)((c / PP_STAGES) & 1), abort)) {
+          atomicExch(&abort_flag, 1);
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const uint32_t stA = su32(smem + (size_t)s * PP_STAGE_BYTES);
+        const uint32_t stB = stA + PP_A_BYTES;
+        uint32_t fresh = win_start ? 0x1Fu : 0u;  // exact levels restart every window
+        if (c == 0) fresh |= 0x20u;               // the shared level only at the start
+#pragma unroll 1
+        for (int ks = 0; ks < 2; ++ks)
+#pragma unroll 1
+          for (int p = 0; p < 8; ++p)
+#pragma unroll 1
+            for (int q = 0; q + p < 8; ++q) {
+              const int lv = min(p + q, 5);
+              const uint32_t acc = ((fresh >> lv) & 1u) ? 0u : 1u;
+              fresh &= ~(1u << lv);
+              const uint64_t da = sdesc(stA + (uint32_t)((p * 2 + ks) * 4096));
+              const uint64_t db = sdesc(stB + (uint32_t)((q * 2 + ks) * 2048));
+              asm volatile(
+                  "{\n\t.reg .pred pd;\n\tsetp.ne.b32 pd, %4, 0;\n\t"
+                  "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, pd;\n\t}" ::"r"(
+                      tmem + (uint32_t)(lv * PP_N)),
+                  "l"(da), "l"(db), "r"(idesc), "r"(acc));
+            }
+        asm volatile(
+            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                su32(&empty[s]))
+            : "memory");
+        if ((c % PP_FLUSH) == PP_FLUSH - 1 || c == nkc - 1)
+          asm volatile(
+              "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                  su32(&accf))
+              : "memory");
+      }
+      // every MMA issued so far has completed before TMEM is read for the last time or freed
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+              su32(&fin))
+          : "memory");
+      wait_bar(su32(&fin), 0u, nullptr);
+    }
+  } else {
+    // ---- epilogue warps 2..9: TMEM lane quarter warp % 4, column half (warp - 2) / 4
+    const int quarter = warp & 3, half = (warp - 2) >> 2;
+    const int row = 32 * quarter + lane;
+    long long T[32];
+#pragma unroll
+    for (int c = 0; c < 32; ++c) T[c] = 0;
+    const uint32_t lane_base = tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(32 * half);
+    bool ok = true;
+    for (int w = 0; w < nwin; ++w) {
+      // warp-uniform decision: the TMEM loads below are .sync.aligned
+      const bool got = wait_bar(su32(&accf), (uint32_t)(w & 1), abort);
+      if (!__all_sync(0xffffffffu, got ? 1 : 0)) {
+        atomicExch(&abort_flag, 1);
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;");
+#pragma unroll
+      for (int lv = 0; lv < 5; ++lv) {
+#pragma unroll
+        for (int c0 = 0; c0 < 32; c0 += 8) {
+          uint32_t v[8];
+          asm volatile(
+              "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+              : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
+                "=r"(v[6]), "=r"(v[7])
+              : "r"(lane_base + (uint32_t)(lv * PP_N + c0)));
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+          for (int t = 0; t < 8; ++t) {
+            const float f = __uint_as_float(v[t]);
+            const long long iv =
+                (long long)__float2int_rn(f * __uint_as_float((uint32_t)(127 + 7 * lv) << 23));
+            T[c0 + t] += iv * (1LL << (7 * (4 - lv)));
+          }
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(&accfree)) : "memory");
+    }
+    if (__all_sync(0xffffffffu, (ok && !*abort) ? 1 : 0)) {
+      // levels 7..9 (accumulated over all of k) and the output
+      const int i = i0 + row;
+      const int ei = i < a.M ? a.eA[i] + a.eshiftA : 0;
+#pragma unroll
+      for (int c0 = 0; c0 < 32; c0 += 8) {
+        uint32_t v[8];
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
+              "=r"(v[6]), "=r"(v[7])
+            : "r"(lane_base + (uint32_t)(5 * PP_N + c0)));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (i < a.M) {
+#pragma unroll
+          for (int t = 0; t < 8; ++t) {
+            const int j = j0 + 32 * half + c0 + t;
+            if (j < a.N && !(a.sym && i < j)) {
+              const int sc = ei + a.eB[j] - 14;
+              const double scale =
+                  (sc > -1022 && sc < 1023) ? __hiloint2double((sc + 1023) << 20, 0) : 0.0;
+              const double val =
+                  fma((double)T[c0 + t], 0x1p-28, (double)__uint_as_float(v[t])) * scale;
+              a.C[i + (size_t)j * a.ldc] = val;
+              if (a.sym && i != j) a.C[j + (size_t)i * a.ldc] = val;
+            }
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (tid == 0 && abort_flag) atomicExch(a.status, 1);
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(PP_TMEM_COLS));
+}
+
+}  // namespace
+
+size_t pimage_bytes(int lines, int K) {
+  const size_t lp = (size_t)((lines + PP_M - 1) / PP_M) * PP_M;
+  const size_t kp = (size_t)((K + PP_KC - 1) / PP_KC) * PP_KC;
+  return lp * kp * 8 * sizeof(uint16_t);
+}
+int pimage_lines(int lines) { return ((lines + PP_M - 1) / PP_M) * PP_M; }
+
+// slice image of a matrix: line i, position k is M[i + k ld] (kcontig = 0: the rows of M) or
+// M[k + i ld] (kcontig = 1: the columns of M); img holds pimage_bytes(lines, K) bytes and e
+// pimage_lines(lines) ints
+void psplit(const double* M, int ld, int kcontig, int lines, int K, PImage& img, cudaStream_t s) {
+  img.lines = lines;
+  img.K = K;
+  const int lp = pimage_lines(lines);
+  const int nkc = (K + PP_KC - 1) / PP_KC;
+  g_kernel_launches += 2;
+  if (kcontig) k_pexp_cols<<<(lp * 32 + 255) / 256, 256, 0, s>>>(M, ld, lines, K, lp, img.e);
+  else k_pexp_rows<<<lp / 32, 256, 0, s>>>(M, ld, lines, K, lp, img.e);
+  k_psplit<<<dim3(lp / 64, nkc), 256, 0, s>>>(M, ld, kcontig, lines, K, lp / 64, img.e,
+                                              img.data);
+}
+
+// C = 2^eshiftA op(A) op(B) from two slice images (A.K == B.K); sym: the product is symmetric
+void pgemm(const PImage& A, const PImage& B, double* C, int ldc, bool sym, int* status,
+           cudaStream_t s, int eshiftA) {
+  if (A.lines <= 0 || B.lines <= 0) return;
+  if (A.K != B.K) throw std::runtime_error("split GEMM: inner dimensions differ");
+  static bool attr = false;
+  if (!attr) {
+    ck(cudaFuncSetAttribute(k_opipe, cudaFuncAttributeMaxDynamicSharedMemorySize, PP_SMEM),
+       "smem attr pipelined split gemm");
+    attr = true;
+  }
+  PipeArgs a{};
+  a.A = A.data;
+  a.B = B.data;
+  a.eA = A.e;
+  a.eB = B.e;
+  a.eshiftA = eshiftA;
+  a.nlbA = pimage_lines(A.lines) / 64;
+  a.nlbB = pimage_lines(B.lines) / 64;
+  a.M = A.lines;
+  a.N = B.lines;
+  a.nkc = (A.K + PP_KC - 1) / PP_KC;
+  a.C = C;
+  a.ldc = ldc;
+  a.sym = sym ? 1 : 0;
+  a.status = status;
+  const int mt = (a.M + PP_M - 1) / PP_M, nt = (a.N + PP_N - 1) / PP_N;
+  g_split_flops += sym ? (unsigned long long)a.N * (a.N + 1) * A.K
+                       : 2ull * a.M * a.N * A.K;
+  const int tk = prof_kbegin(s);
+  ++g_kernel_launches;
+  k_opipe<<<mt * nt, PP_THREADS, PP_SMEM, s>>>(a);
+  prof_kend(KS_GEMM, tk, s);
+}
+
+}  // namespace tb
+
+namespace tb {
+extern bool g_pipe_gemm;
+}
+
+// C = A B on the pipelined split GEMM from device pointers (column-major: A m x k with leading
+// dimension m, B k x n with leading dimension k, C m x n with leading dimension m; sym: C is
+// symmetric, m == n).  Allocates the two slice images for the call and synchronises the
+// stream.  0 on success, 1 if a wait of the tensor-core pipeline ran out, -1 on bad arguments,
+// -2 on a CUDA error.
+extern "C" int tblite_gb300_split_gemm(int m, int n, int k, const double* a, const double* b,
+                                       double* c, int sym, void* stream) {
+  using namespace tb;
+  if (m <= 0 || n <= 0 || k <= 0 || !a || !b || !c || (sym && m != n)) return -1;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  PImage ia, ib;
+  int* st = nullptr;
+  int hst = 0;
+  int rc = 0;
+  if (cudaMalloc(&ia.data, pimage_bytes(m, k)) != cudaSuccess ||
+      cudaMalloc(&ia.e, sizeof(int) * pimage_lines(m)) != cudaSuccess ||
+      cudaMalloc(&ib.data, pimage_bytes(n, k)) != cudaSuccess ||
+      cudaMalloc(&ib.e, sizeof(int) * pimage_lines(n)) != cudaSuccess ||
+      cudaMalloc(&st, sizeof(int)) != cudaSuccess) {
+    rc = -2;
+  } else {
+    try {
+      cudaMemsetAsync(st, 0, sizeof(int), s);
+      psplit(a, m, 0, m, k, ia, s);
+      psplit(b, k, 1, n, k, ib, s);
+      pgemm(ia, ib, c, m, sym != 0, st, s);
+      cudaMemcpyAsync(&hst, st, sizeof(int), cudaMemcpyDeviceToHost, s);
+      if (cudaStreamSynchronize(s) != cudaSuccess) rc = -2;
+      else rc = hst != 0 ? 1 : 0;
+    } catch (...) {
+      rc = -2;
+    }
+  }
+  cudaFree(ia.data);
+  cudaFree(ia.e);
+  cudaFree(ib.data);
+  cudaFree(ib.e);
+  cudaFree(st);
+  return rc;
+}
+
+extern "C" void tblite_gb300_set_pipelined_gemm(int enable) { tb::g_pipe_gemm = enable != 0; }

@@ -349,8 +349,13 @@ struct Purifier {
   int* ex = nullptr;      // split-GEMM exponents [2n]
   int* status = nullptr;  // split-GEMM wait limit
   double* hsc = nullptr;  // pinned copy of sc
+  PImage img[3];          // slice images: 0, 1 operands; 2 the orthogonaliser Z
   int last_iterations = 0;
 };
+
+// the products of the projection run on the pipelined split GEMM (ozaki_pipe.cu); switched off,
+// on the per-tile split GEMM (ozaki.cu)
+bool g_pipe_gemm = true;
 
 Purifier* purify_create(int n, cudaStream_t s) {
   auto* p = new Purifier();
@@ -366,6 +371,10 @@ Purifier* purify_create(int n, cudaStream_t s) {
   ck(cudaMalloc(&p->status, sizeof(int)), "purify status");
   ck(cudaMemsetAsync(p->status, 0, sizeof(int), s), "purify status");
   ck(cudaMallocHost(&p->hsc, sizeof(double) * 16), "purify hsc");
+  for (PImage& im : p->img) {
+    ck(cudaMalloc(&im.data, pimage_bytes(n, n)), "purify image");
+    ck(cudaMalloc(&im.e, sizeof(int) * pimage_lines(n)), "purify image e");
+  }
   return p;
 }
 
@@ -375,6 +384,10 @@ void purify_destroy(Purifier* p) {
   cudaFree(p->ex);
   cudaFree(p->status);
   cudaFreeHost(p->hsc);
+  for (PImage& im : p->img) {
+    cudaFree(im.data);
+    cudaFree(im.e);
+  }
   delete p;
 }
 
@@ -385,12 +398,20 @@ static void read_scalars(Purifier* p, int count) {
   ck(cudaMemcpyAsync(p->hsc, p->sc, sizeof(double) * count, cudaMemcpyDeviceToHost, p->s), "sc");
   stream_wait(p->s);
 }
-// symmetric product C = A B (tiles on and below the diagonal, mirrored)
-static void sym_product(Purifier* p, const double* A, const double* B, double* C) {
-  ogemm(false, false, p->n, p->n, p->n, A, B, C, p->n, KM_NONE | KM_SYM, p->ex, p->status, p->s);
-}
-static void gen_product(Purifier* p, const double* A, const double* B, double* C) {
-  ogemm(false, false, p->n, p->n, p->n, A, B, C, p->n, KM_NONE, p->ex, p->status, p->s);
+// C = A B (n x n, column-major; sym: C is symmetric, the tiles on and below the diagonal are
+// computed and mirrored).  The pipelined GEMM first splits A into image slot sa (its rows) and
+// B into slot sb (its columns), unless keep_a / keep_b say the slot already holds that image.
+static void product(Purifier* p, const double* A, int sa, bool keep_a, const double* B, int sb,
+                    bool keep_b, double* C, bool sym) {
+  const int n = p->n;
+  if (!g_pipe_gemm) {
+    ogemm(false, false, n, n, n, A, B, C, n, KM_NONE | (sym ? KM_SYM : 0), p->ex, p->status,
+          p->s);
+    return;
+  }
+  if (!keep_a) psplit(A, n, 0, n, n, p->img[sa], p->s);
+  if (!keep_b && !(sb == sa && B == A)) psplit(B, n, 1, n, n, p->img[sb], p->s);
+  pgemm(p->img[sa], p->img[sb], C, n, sym, p->status, p->s);
 }
 static void bounds(Purifier* p, const double* M) {
   const int n = p->n;
@@ -411,7 +432,7 @@ int purify_set_overlap(Purifier* p, const double* S) {
   int it = 0;
   bool done = false;
   for (; it < PU_NS_MAX && !done; ++it) {
-    sym_product(p, Z, Y, p->T);
+    product(p, Z, 0, false, Y, 1, false, p->T, true);
     ck(cudaMemsetAsync(p->sc + 3, 0, sizeof(double), p->s), "err");
     ++g_kernel_launches;
     k_ns_mid<<<eb, 256, 0, p->s>>>(n, p->T, p->sc + 3);
@@ -424,8 +445,8 @@ int purify_set_overlap(Purifier* p, const double* S) {
     }
     // quadratic convergence (||I - T'||_F^2 <= 0.6 ||I - T||_F^4): one more update after 1e-12
     done = err < 1e-12;
-    sym_product(p, Y, p->T, Yn);
-    sym_product(p, p->T, Z, Zn);
+    product(p, Y, 1, true, p->T, 2, false, Yn, true);   // M = T into slot 2
+    product(p, p->T, 2, true, Z, 0, true, Zn, true);
     std::swap(Y, Yn);
     std::swap(Z, Zn);
   }
@@ -433,6 +454,7 @@ int purify_set_overlap(Purifier* p, const double* S) {
   ++g_kernel_launches;
   k_scale_dev<<<eb, 256, 0, p->s>>>(nn, Z, p->sc + 2);
   if (Z != p->Z) ck(cudaMemcpyAsync(p->Z, Z, sizeof(double) * nn, cudaMemcpyDeviceToDevice, p->s), "Z");
+  if (g_pipe_gemm) psplit(p->Z, n, 0, n, n, p->img[2], p->s);  // Z stays split (symmetric)
   return it;
 }
 
@@ -443,8 +465,8 @@ int purify_density(Purifier* p, const double* F, int nocc, double* P) {
   const int n = p->n;
   const size_t nn = (size_t)n * n;
   const int eb = ew_blocks(nn);
-  gen_product(p, F, p->Z, p->T);
-  sym_product(p, p->Z, p->T, p->A);
+  product(p, F, 0, false, p->Z, 2, true, p->T, false);
+  product(p, p->Z, 2, true, p->T, 1, false, p->A, true);
   bounds(p, p->A);
   ++g_kernel_launches;
   k_sp2_init<<<eb, 256, 0, p->s>>>(n, p->A, p->sc, p->X);
@@ -452,7 +474,7 @@ int purify_density(Purifier* p, const double* F, int nocc, double* P) {
   int it = 0;
   bool done = false;
   for (; it < PU_SP2_MAX; ++it) {
-    sym_product(p, p->X, p->X, p->X2);
+    product(p, p->X, 0, false, p->X, 0, true, p->X2, true);
     ++g_kernel_launches;
     k_sp2_traces<<<1, 1024, 0, p->s>>>(n, p->X, p->X2, p->sc + 4);
     read_scalars(p, 6);
@@ -476,22 +498,26 @@ int purify_density(Purifier* p, const double* F, int nocc, double* P) {
   }
   p->last_iterations = it + 1;
   if (!done) return -1;
-  g_kernel_launches += 1;
-  k_scale_to<<<eb, 256, 0, p->s>>>(nn, p->X, 2.0, p->X2);
-  gen_product(p, p->X2, p->Z, p->T);
-  sym_product(p, p->Z, p->T, P);
+  if (g_pipe_gemm) {  // T = 2 X Z: slot 0 holds X, the factor 2 goes into its exponents
+    pgemm(p->img[0], p->img[2], p->T, n, false, p->status, p->s, 1);
+  } else {
+    ++g_kernel_launches;
+    k_scale_to<<<eb, 256, 0, p->s>>>(nn, p->X, 2.0, p->X2);
+    product(p, p->X2, 0, false, p->Z, 2, true, p->T, false);
+  }
+  product(p, p->Z, 2, true, p->T, 1, false, P, true);
   return it + 1;
 }
 
 void purify_product(Purifier* p, const double* A, const double* B, double* C) {
-  gen_product(p, A, B, C);
+  product(p, A, 0, false, B, 1, false, C, false);
 }
 
 // W = P F P / 2 (the energy-weighted density of the last purify_density call)
 void purify_weighted(Purifier* p, const double* F, const double* P, double* W) {
   const size_t nn = (size_t)p->n * p->n;
-  gen_product(p, F, P, p->T);
-  sym_product(p, P, p->T, W);
+  product(p, F, 0, false, P, 1, false, p->T, false);
+  product(p, P, 1, true, p->T, 0, false, W, true);  // slot 1 holds P (symmetric)
   ++g_kernel_launches;
   k_scale_to<<<ew_blocks(nn), 256, 0, p->s>>>(nn, W, 0.5, W);
 }

@@ -96,6 +96,9 @@ _SIGNATURES = {
     "tblite_gb300_set_calculator_slater_exponents": (None, [c_void_p, c_void_p, _dbl_p]),
     "tblite_gb300_get_result_slater_gradient": (None, [c_void_p, c_void_p, _dbl_p]),
     "tblite_gb300_set_calculator_density_solver": (None, [c_void_p, c_void_p, c_int]),
+    "tblite_gb300_split_gemm": (
+        c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
+    "tblite_gb300_set_pipelined_gemm": (None, [c_int]),
     "tblite_gb300_get_result_gap": (None, [c_void_p, c_void_p, _dbl_p]),
     "tblite_gb300_density_matrix_noalloc": (
         c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
