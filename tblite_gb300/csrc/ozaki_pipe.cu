@@ -1,8 +1,12 @@
 // Pipelined FP64-accurate split GEMM on the BF16 tensor cores for the one-molecule path.
 //
-// Same arithmetic as ozaki.cu (eight 7-bit slices per FP64 value, 36 exact BF16 slice products
-// per FP64 product, exact integer level sums moved to int64 every 192 values of k), but the
-// operands are split once per matrix instead of once per tile pair:
+// Same splitting as ozaki.cu (eight 7-bit slices per FP64 value, 36 exact BF16 slice products
+// per FP64 product), with one more exact level: the levels p + q = 2..7 each own a TMEM
+// accumulator whose sums stay exact integers (at most 6 products of < 2^14 over 160 values of k:
+// < 2^24) and move to one int64 per element every 160 values of k; only levels 8 and 9 (< 2^-42
+// of the leading level) share an FP32 accumulator over the whole of k, so its rounding stays
+// below 2^-60 of the result.  The operands are split once per matrix instead of once per tile
+// pair:
 //
 //   psplit   turns a matrix into a slice image: per line (row of op(A) or column of op(B)) a
 //            power-of-two exponent, and the eight BF16 slices laid out exactly as the tensor
@@ -11,9 +15,9 @@
 //   pgemm    (kernel k_opipe) one 128 x 64 output tile per CTA, 10 warps: warp 0 streams the slices of each
 //            k chunk (96 KB: A 64 KB, B 32 KB) with cp.async.bulk into a two-stage shared
 //            memory ring (mbarrier complete_tx); warp 1 issues the 72 tcgen05.mma of a chunk
-//            (M 128, N 64, K 16, FP32 accumulators in TMEM: levels 2..6 exact, 7..9 shared)
+//            (M 128, N 64, K 16, FP32 accumulators in TMEM: levels 2..7 exact, 8..9 shared)
 //            and commits them to the stage's "empty" barrier; warps 2..9 move the exact levels
-//            out of TMEM into int64 registers after every 6 chunks and write C at the end.
+//            out of TMEM into int64 registers after every 5 chunks and write C at the end.
 //
 // Every wait is bounded; a wait that runs out sets a CTA-wide abort flag, the other roles leave
 // their loops, copies and MMAs still in flight are waited for (bounded), TMEM is freed and the
@@ -32,7 +36,9 @@ namespace tb {
 
 namespace {
 
-constexpr int PP_M = 128, PP_N = 64, PP_KC = 32, PP_FLUSH = 6, PP_THREADS = 320;
+constexpr int PP_M = 128, PP_N = 64, PP_KC = 32, PP_FLUSH = 5, PP_THREADS = 320;
+constexpr int PP_EXACT = 6;    // exact level accumulators (levels 2..7); one more for 8..9
+constexpr int PP_KMAX = 16384;  // |int64 level sum| < 2^49 K
 constexpr int PP_STAGES = 2;  // the producer's bookkeeping below assumes two
 constexpr int PP_A_BYTES = 8 * 2 * 4096;  // 8 slices x 2 k steps x (128 lines x 16 k x 2 B)
 constexpr int PP_B_BYTES = 8 * 2 * 2048;  // 8 slices x 2 k steps x (64 lines x 16 k x 2 B)
@@ -291,15 +297,15 @@ __global__ void __launch_bounds__(PP_THREADS, 1) k_opipe(PipeArgs a) {
         asm volatile("tcgen05.fence::after_thread_sync;");
         const uint32_t stA = su32(smem + (size_t)s * PP_STAGE_BYTES);
         const uint32_t stB = stA + PP_A_BYTES;
-        uint32_t fresh = win_start ? 0x1Fu : 0u;  // exact levels restart every window
-        if (c == 0) fresh |= 0x20u;               // the shared level only at the start
+        uint32_t fresh = win_start ? 0x3Fu : 0u;  // exact levels restart every window
+        if (c == 0) fresh |= 0x40u;               // the shared level only at the start
 #pragma unroll 1
         for (int ks = 0; ks < 2; ++ks)
 #pragma unroll 1
           for (int p = 0; p < 8; ++p)
 #pragma unroll 1
             for (int q = 0; q + p < 8; ++q) {
-              const int lv = min(p + q, 5);
+              const int lv = min(p + q, PP_EXACT);
               const uint32_t acc = ((fresh >> lv) & 1u) ? 0u : 1u;
               fresh &= ~(1u << lv);
               const uint64_t da = sdesc(stA + (uint32_t)((p * 2 + ks) * 4096));
@@ -346,7 +352,7 @@ __global__ void __launch_bounds__(PP_THREADS, 1) k_opipe(PipeArgs a) {
       }
       asm volatile("tcgen05.fence::after_thread_sync;");
 #pragma unroll
-      for (int lv = 0; lv < 5; ++lv) {
+      for (int lv = 0; lv < PP_EXACT; ++lv) {
 #pragma unroll
         for (int c0 = 0; c0 < 32; c0 += 8) {
           uint32_t v[8];
@@ -361,7 +367,7 @@ __global__ void __launch_bounds__(PP_THREADS, 1) k_opipe(PipeArgs a) {
             const float f = __uint_as_float(v[t]);
             const long long iv =
                 (long long)__float2int_rn(f * __uint_as_float((uint32_t)(127 + 7 * lv) << 23));
-            T[c0 + t] += iv * (1LL << (7 * (4 - lv)));
+            T[c0 + t] += iv * (1LL << (7 * (PP_EXACT - 1 - lv)));
           }
         }
       }
@@ -369,7 +375,7 @@ __global__ void __launch_bounds__(PP_THREADS, 1) k_opipe(PipeArgs a) {
       asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(&accfree)) : "memory");
     }
     if (__all_sync(0xffffffffu, (ok && !*abort) ? 1 : 0)) {
-      // levels 7..9 (accumulated over all of k) and the output
+      // levels 8..9 (accumulated over all of k) and the output
       const int i = i0 + row;
       const int ei = i < a.M ? a.eA[i] + a.eshiftA : 0;
 #pragma unroll
@@ -379,7 +385,7 @@ __global__ void __launch_bounds__(PP_THREADS, 1) k_opipe(PipeArgs a) {
             "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
             : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
               "=r"(v[6]), "=r"(v[7])
-            : "r"(lane_base + (uint32_t)(5 * PP_N + c0)));
+            : "r"(lane_base + (uint32_t)(PP_EXACT * PP_N + c0)));
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
         if (i < a.M) {
 #pragma unroll
@@ -390,7 +396,7 @@ __global__ void __launch_bounds__(PP_THREADS, 1) k_opipe(PipeArgs a) {
               const double scale =
                   (sc > -1022 && sc < 1023) ? __hiloint2double((sc + 1023) << 20, 0) : 0.0;
               const double val =
-                  fma((double)T[c0 + t], 0x1p-28, (double)__uint_as_float(v[t])) * scale;
+                  fma((double)T[c0 + t], 0x1p-35, (double)__uint_as_float(v[t])) * scale;
               a.C[i + (size_t)j * a.ldc] = val;
               if (a.sym && i != j) a.C[j + (size_t)i * a.ldc] = val;
             }
@@ -436,6 +442,7 @@ void pgemm(const PImage& A, const PImage& B, double* C, int ldc, bool sym, int* 
            cudaStream_t s, int eshiftA) {
   if (A.lines <= 0 || B.lines <= 0) return;
   if (A.K != B.K) throw std::runtime_error("split GEMM: inner dimensions differ");
+  if (A.K > PP_KMAX) throw std::runtime_error("split GEMM: inner dimension above 12288");
   static bool attr = false;
   if (!attr) {
     ck(cudaFuncSetAttribute(k_opipe, cudaFuncAttributeMaxDynamicSharedMemorySize, PP_SMEM),
