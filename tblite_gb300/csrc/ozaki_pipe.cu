@@ -38,7 +38,7 @@ namespace {
 
 constexpr int PP_M = 128, PP_N = 64, PP_KC = 32, PP_FLUSH = 5, PP_THREADS = 320;
 constexpr int PP_EXACT = 6;    // exact level accumulators (levels 2..7); one more for 8..9
-constexpr int PP_KMAX = 16384;  // |int64 level sum| < 2^49 K
+constexpr int PP_KMAX = 12288;  // |int64 level sums| < 1.02 * 2^49 K < 2^63
 constexpr int PP_STAGES = 2;  // the producer's bookkeeping below assumes two
 constexpr int PP_A_BYTES = 8 * 2 * 4096;  // 8 slices x 2 k steps x (128 lines x 16 k x 2 B)
 constexpr int PP_B_BYTES = 8 * 2 * 2048;  // 8 slices x 2 k steps x (64 lines x 16 k x 2 B)
