@@ -10,11 +10,12 @@
 //
 //   psplit   turns a matrix into a slice image: per line (row of op(A) or column of op(B)) a
 //            power-of-two exponent, and the eight BF16 slices laid out exactly as the tensor
-//            cores read them from shared memory (K-major core matrices of 8 lines x 16 bytes),
-//            image[k chunk of 32][slice][k step of 16][line block of 64][8 x 256 bytes];
-//   pgemm    (kernel k_opipe) one 128 x 64 output tile per CTA, 10 warps: warp 0 streams the slices of each
-//            k chunk (96 KB: A 64 KB, B 32 KB) with cp.async.bulk into a two-stage shared
-//            memory ring (mbarrier complete_tx); warp 1 issues the 72 tcgen05.mma of a chunk
+//            cores read them from shared memory: K-major lines of 64 bytes with the 64-byte
+//            swizzle, image[k chunk of 32][slice][line block of 64][64 x 64 bytes] (or the
+//            interleaved layout of ozaki.cu, 8-line x 16-byte core matrices);
+//   pgemm    (kernel k_opipe) one 128 x 64 output tile per CTA, 10 warps: warp 0 streams the
+//            slices of each k chunk (96 KB: A 64 KB, B 32 KB) with cp.async.bulk into a two-stage
+//            shared-memory ring (mbarrier complete_tx); warp 1 issues the 72 tcgen05.mma of a chunk
 //            (M 128, N 64, K 16, FP32 accumulators in TMEM: levels 2..7 exact, 8..9 shared)
 //            and commits them to the stage's "empty" barrier; warps 2..9 move the exact levels
 //            out of TMEM into int64 registers after every 5 chunks and write C at the end.
@@ -56,9 +57,17 @@ void ck(cudaError_t e, const char* what) {
 __device__ __forceinline__ uint32_t su32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
+// shared-memory matrix descriptors (K-major, descriptor version 1).  Interleaved: core matrices
+// of 8 lines x 16 bytes, 128 B apart along K and 256 B apart along the lines.  Swizzled: lines of
+// 64 bytes (32 BF16 of k), 8-line atoms 512 B apart, the 16-byte chunks of line r permuted by
+// chunk ^ ((r >> 1) & 3) (the 64-byte swizzle); a k step of 16 moves the start by 32 bytes.
 __device__ __forceinline__ uint64_t sdesc(uint32_t addr) {
   return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)(128 >> 4) << 16) |
          ((uint64_t)(256 >> 4) << 32) | ((uint64_t)1 << 46);
+}
+__device__ __forceinline__ uint64_t sdesc_sw64(uint32_t addr) {
+  return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)1 << 16) | ((uint64_t)(512 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)4 << 61);
 }
 __device__ __forceinline__ bool try_wait(uint32_t bar, uint32_t parity) {
   uint32_t ok;
@@ -77,6 +86,18 @@ __device__ __forceinline__ bool wait_bar(uint32_t bar, uint32_t parity, volatile
     if (abort && *abort) return false;
   }
   return false;
+}
+
+// 16 consecutive TMEM columns of this thread's lane (one row of the tile) into v
+__device__ __forceinline__ void tmem_ld16(uint32_t addr, uint32_t (&v)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+      "%14,%15}, [%16];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+        "=r"(v[14]), "=r"(v[15])
+      : "r"(addr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
 // BF16 bits of (-1)^sign a 2^-7p for an integer 0 <= a < 128 (exact: at most 7 significant bits)
@@ -119,6 +140,7 @@ __global__ void k_pexp_cols(const double* __restrict__ M, int ld, int lines, int
 
 // ---- slice image: one block per (64 lines, 32 k); the FP64 tile goes through shared memory so
 // both memory orders read coalesced; each thread splits 8 consecutive k of one line
+template <bool SW>
 __global__ void __launch_bounds__(256) k_psplit(const double* __restrict__ M, int ld, int kcontig,
                                                 int lines, int K, int nlb,
                                                 const int* __restrict__ e, uint16_t* img) {
@@ -166,13 +188,22 @@ __global__ void __launch_bounds__(256) k_psplit(const double* __restrict__ M, in
       w[p][c >> 1] |= slice_bits(a, p, sign) << ((c & 1) * 16);
     }
   }
-  const int ks = g >> 1, half = g & 1;
-  const int rg = li >> 3, r = li & 7;
+  if (SW) {  // [k chunk][slice][line block][64 lines x 64 B, 16-byte chunks swizzled]
 #pragma unroll
-  for (int p = 0; p < 8; ++p) {
-    const size_t off = ((((size_t)kc * 8 + p) * 2 + ks) * nlb + lb) * 1024 + rg * 128 + half * 64 +
-                       r * 8;
-    *reinterpret_cast<uint4*>(img + off) = make_uint4(w[p][0], w[p][1], w[p][2], w[p][3]);
+    for (int p = 0; p < 8; ++p) {
+      const size_t off = (((size_t)kc * 8 + p) * nlb + lb) * 2048 + li * 32 +
+                         ((g ^ ((li >> 1) & 3)) << 3);
+      *reinterpret_cast<uint4*>(img + off) = make_uint4(w[p][0], w[p][1], w[p][2], w[p][3]);
+    }
+  } else {  // [k chunk][slice][k step][line block][8 x (2 core matrices of 8 lines x 16 B)]
+    const int ks = g >> 1, half = g & 1;
+    const int rg = li >> 3, r = li & 7;
+#pragma unroll
+    for (int p = 0; p < 8; ++p) {
+      const size_t off = ((((size_t)kc * 8 + p) * 2 + ks) * nlb + lb) * 1024 + rg * 128 +
+                         half * 64 + r * 8;
+      *reinterpret_cast<uint4*>(img + off) = make_uint4(w[p][0], w[p][1], w[p][2], w[p][3]);
+    }
   }
 }
 
@@ -190,6 +221,7 @@ struct PipeArgs {
   int* status;
 };
 
+template <bool SW>
 __global__ void __launch_bounds__(PP_THREADS, 1) k_opipe(PipeArgs a) {
   // ---- tile of this CTA: groups of PP_GROUP row blocks, column blocks inside a group
   const int mt = (a.M + PP_M - 1) / PP_M, nt = (a.N + PP_N - 1) / PP_N;
@@ -251,6 +283,24 @@ __global__ void __launch_bounds__(PP_THREADS, 1) k_opipe(PipeArgs a) {
                      "r"(PP_STAGE_BYTES)
                      : "memory");
         unsigned char* st = smem + (size_t)s * PP_STAGE_BYTES;
+        if (SW) {  // per slice: A 8 KB (two line blocks), B 4 KB
+#pragma unroll 1
+          for (int p = 0; p < 8; ++p) {
+            const size_t blk = (size_t)c * 8 + p;
+            const uint16_t* srcA = a.A + (blk * a.nlbA + lbA) * 2048;
+            const uint16_t* srcB = a.B + (blk * a.nlbB + lbB) * 2048;
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], "
+                "%2, [%3];" ::"r"(su32(st + p * 8192)),
+                "l"(srcA), "r"(8192), "r"(bar)
+                : "memory");
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], "
+                "%2, [%3];" ::"r"(su32(st + PP_A_BYTES + p * 4096)),
+                "l"(srcB), "r"(4096), "r"(bar)
+                : "memory");
+          }
+        } else {
 #pragma unroll 1
         for (int p = 0; p < 8; ++p)
 #pragma unroll 1
@@ -269,6 +319,7 @@ __global__ void __launch_bounds__(PP_THREADS, 1) k_opipe(PipeArgs a) {
                 "l"(srcB), "r"(2048), "r"(bar)
                 : "memory");
           }
+        }
         if (s == 0) last0 = c;
         else last1 = c;
       }
@@ -308,8 +359,10 @@ __global__ void __launch_bounds__(PP_THREADS, 1) k_opipe(PipeArgs a) {
               const int lv = min(p + q, PP_EXACT);
               const uint32_t acc = ((fresh >> lv) & 1u) ? 0u : 1u;
               fresh &= ~(1u << lv);
-              const uint64_t da = sdesc(stA + (uint32_t)((p * 2 + ks) * 4096));
-              const uint64_t db = sdesc(stB + (uint32_t)((q * 2 + ks) * 2048));
+              const uint64_t da = SW ? sdesc_sw64(stA + (uint32_t)(p * 8192 + ks * 32))
+                                     : sdesc(stA + (uint32_t)((p * 2 + ks) * 4096));
+              const uint64_t db = SW ? sdesc_sw64(stB + (uint32_t)(q * 4096 + ks * 32))
+                                     : sdesc(stB + (uint32_t)((q * 2 + ks) * 2048));
               asm volatile(
                   "{\n\t.reg .pred pd;\n\tsetp.ne.b32 pd, %4, 0;\n\t"
                   "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, pd;\n\t}" ::"r"(
@@ -354,20 +407,15 @@ __global__ void __launch_bounds__(PP_THREADS, 1) k_opipe(PipeArgs a) {
 #pragma unroll
       for (int lv = 0; lv < PP_EXACT; ++lv) {
 #pragma unroll
-        for (int c0 = 0; c0 < 32; c0 += 8) {
-          uint32_t v[8];
-          asm volatile(
-              "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-              : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
-                "=r"(v[6]), "=r"(v[7])
-              : "r"(lane_base + (uint32_t)(lv * PP_N + c0)));
-          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        for (int h = 0; h < 2; ++h) {
+          uint32_t v[16];
+          tmem_ld16(lane_base + (uint32_t)(lv * PP_N + 16 * h), v);
 #pragma unroll
-          for (int t = 0; t < 8; ++t) {
+          for (int t = 0; t < 16; ++t) {
             const float f = __uint_as_float(v[t]);
             const long long iv =
                 (long long)__float2int_rn(f * __uint_as_float((uint32_t)(127 + 7 * lv) << 23));
-            T[c0 + t] += iv * (1LL << (7 * (PP_EXACT - 1 - lv)));
+            T[16 * h + t] += iv * (1LL << (7 * (PP_EXACT - 1 - lv)));
           }
         }
       }
@@ -379,24 +427,19 @@ __global__ void __launch_bounds__(PP_THREADS, 1) k_opipe(PipeArgs a) {
       const int i = i0 + row;
       const int ei = i < a.M ? a.eA[i] + a.eshiftA : 0;
 #pragma unroll
-      for (int c0 = 0; c0 < 32; c0 += 8) {
-        uint32_t v[8];
-        asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
-              "=r"(v[6]), "=r"(v[7])
-            : "r"(lane_base + (uint32_t)(PP_EXACT * PP_N + c0)));
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      for (int h = 0; h < 2; ++h) {
+        uint32_t v[16];
+        tmem_ld16(lane_base + (uint32_t)(PP_EXACT * PP_N + 16 * h), v);
         if (i < a.M) {
 #pragma unroll
-          for (int t = 0; t < 8; ++t) {
-            const int j = j0 + 32 * half + c0 + t;
+          for (int t = 0; t < 16; ++t) {
+            const int j = j0 + 32 * half + 16 * h + t;
             if (j < a.N && !(a.sym && i < j)) {
               const int sc = ei + a.eB[j] - 14;
               const double scale =
                   (sc > -1022 && sc < 1023) ? __hiloint2double((sc + 1023) << 20, 0) : 0.0;
               const double val =
-                  fma((double)T[c0 + t], 0x1p-35, (double)__uint_as_float(v[t])) * scale;
+                  fma((double)T[16 * h + t], 0x1p-35, (double)__uint_as_float(v[t])) * scale;
               a.C[i + (size_t)j * a.ldc] = val;
               if (a.sym && i != j) a.C[j + (size_t)i * a.ldc] = val;
             }
@@ -425,16 +468,24 @@ int pimage_lines(int lines) { return ((lines + PP_M - 1) / PP_M) * PP_M; }
 // slice image of a matrix: line i, position k is M[i + k ld] (kcontig = 0: the rows of M) or
 // M[k + i ld] (kcontig = 1: the columns of M); img holds pimage_bytes(lines, K) bytes and e
 // pimage_lines(lines) ints
+// layout of the slice images made from now on: 64-byte swizzled (default) or interleaved
+static bool g_pipe_swizzle = true;
+
 void psplit(const double* M, int ld, int kcontig, int lines, int K, PImage& img, cudaStream_t s) {
   img.lines = lines;
   img.K = K;
+  img.swz = g_pipe_swizzle ? 1 : 0;
   const int lp = pimage_lines(lines);
   const int nkc = (K + PP_KC - 1) / PP_KC;
   g_kernel_launches += 2;
   if (kcontig) k_pexp_cols<<<(lp * 32 + 255) / 256, 256, 0, s>>>(M, ld, lines, K, lp, img.e);
   else k_pexp_rows<<<lp / 32, 256, 0, s>>>(M, ld, lines, K, lp, img.e);
-  k_psplit<<<dim3(lp / 64, nkc), 256, 0, s>>>(M, ld, kcontig, lines, K, lp / 64, img.e,
-                                              img.data);
+  if (img.swz)
+    k_psplit<true><<<dim3(lp / 64, nkc), 256, 0, s>>>(M, ld, kcontig, lines, K, lp / 64, img.e,
+                                                      img.data);
+  else
+    k_psplit<false><<<dim3(lp / 64, nkc), 256, 0, s>>>(M, ld, kcontig, lines, K, lp / 64, img.e,
+                                                       img.data);
 }
 
 // C = 2^eshiftA op(A) op(B) from two slice images (A.K == B.K); sym: the product is symmetric
@@ -443,9 +494,12 @@ void pgemm(const PImage& A, const PImage& B, double* C, int ldc, bool sym, int* 
   if (A.lines <= 0 || B.lines <= 0) return;
   if (A.K != B.K) throw std::runtime_error("split GEMM: inner dimensions differ");
   if (A.K > PP_KMAX) throw std::runtime_error("split GEMM: inner dimension above 12288");
+  if (A.swz != B.swz) throw std::runtime_error("split GEMM: slice images of different layouts");
   static bool attr = false;
   if (!attr) {
-    ck(cudaFuncSetAttribute(k_opipe, cudaFuncAttributeMaxDynamicSharedMemorySize, PP_SMEM),
+    ck(cudaFuncSetAttribute(k_opipe<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, PP_SMEM),
+       "smem attr pipelined split gemm");
+    ck(cudaFuncSetAttribute(k_opipe<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, PP_SMEM),
        "smem attr pipelined split gemm");
     attr = true;
   }
@@ -469,7 +523,8 @@ void pgemm(const PImage& A, const PImage& B, double* C, int ldc, bool sym, int* 
                        : 2ull * a.M * a.N * A.K;
   const int tk = prof_kbegin(s);
   ++g_kernel_launches;
-  k_opipe<<<mt * nt, PP_THREADS, PP_SMEM, s>>>(a);
+  if (A.swz) k_opipe<true><<<mt * nt, PP_THREADS, PP_SMEM, s>>>(a);
+  else k_opipe<false><<<mt * nt, PP_THREADS, PP_SMEM, s>>>(a);
   prof_kend(KS_GEMM, tk, s);
 }
 
@@ -477,6 +532,7 @@ void pgemm(const PImage& A, const PImage& B, double* C, int ldc, bool sym, int* 
 
 namespace tb {
 extern bool g_pipe_gemm;
+void set_pipe_swizzle(bool on) { g_pipe_swizzle = on; }
 }
 
 // C = A B on the pipelined split GEMM from device pointers (column-major: A m x k with leading
@@ -520,4 +576,7 @@ extern "C" int tblite_gb300_split_gemm(int m, int n, int k, const double* a, con
   return rc;
 }
 
-extern "C" void tblite_gb300_set_pipelined_gemm(int enable) { tb::g_pipe_gemm = enable != 0; }
+extern "C" void tblite_gb300_set_pipelined_gemm(int mode) {
+  tb::g_pipe_gemm = mode != 0;
+  tb::set_pipe_swizzle(mode != 1);
+}
