@@ -130,10 +130,9 @@ void tblite_gb300_get_result_gap(tblite_error error, tblite_result res, double* 
  */
 int tblite_gb300_split_gemm(int m, int n, int k, const double* a, const double* b, double* c,
                             int sym, void* stream);
-/* products of the spectral-projection solver and of tblite_gb300_split_gemm: 2 (default)
- * pipelined split GEMM from 64-byte-swizzled slice images, 1 the same from interleaved images,
- * 0 the per-tile split GEMM (the projection solver only) */
-void tblite_gb300_set_pipelined_gemm(int mode);
+/* products of the spectral-projection solver: 1 (default) pipelined split GEMM from slice
+ * images, 0 the per-tile split GEMM */
+void tblite_gb300_set_pipelined_gemm(int enable);
 
 /* number of engine kernels launched since the library was loaded (all threads) */
 unsigned long long tblite_gb300_get_launch_count(void);

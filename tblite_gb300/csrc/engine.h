@@ -254,7 +254,6 @@ void eigen_vectors_range(EigenSolver*, int k0, int k1, double* C);
 // C = op(A) op(B) runs from two images
 struct PImage {
   int lines = 0, K = 0;
-  int swz = 0;               // 1: 64-byte swizzled layout, 0: interleaved core matrices
   uint16_t* data = nullptr;  // pimage_bytes(lines, K) bytes
   int* e = nullptr;          // pimage_lines(lines) ints
 };

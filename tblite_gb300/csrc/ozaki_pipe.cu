@@ -1,24 +1,25 @@
 // Pipelined FP64-accurate split GEMM on the BF16 tensor cores for the one-molecule path.
 //
-// Same splitting as ozaki.cu (eight 7-bit slices per FP64 value, 36 exact BF16 slice products
-// per FP64 product), with one more exact level: the levels p + q = 2..7 each own a TMEM
-// accumulator whose sums stay exact integers (at most 6 products of < 2^14 over 160 values of k:
-// < 2^24) and move to one int64 per element every 160 values of k; only levels 8 and 9 (< 2^-42
-// of the leading level) share an FP32 accumulator over the whole of k, so its rounding stays
-// below 2^-60 of the result.  The operands are split once per matrix instead of once per tile
-// pair:
+// Same splitting as ozaki.cu: eight 7-bit slices per FP64 value, x = 2^e sum_p a_p 2^-7p, stored
+// pre-scaled in BF16, and the 36 exact slice products a_p b_q with p + q <= 7 (zero based).  The
+// operands are split once per matrix instead of once per tile pair, and the products are grouped
+// so that each tensor-core instruction is wide:
 //
 //   psplit   turns a matrix into a slice image: per line (row of op(A) or column of op(B)) a
 //            power-of-two exponent, and the eight BF16 slices laid out exactly as the tensor
-//            cores read them from shared memory: K-major lines of 64 bytes with the 64-byte
-//            swizzle, image[k chunk of 32][slice][line block of 64][64 x 64 bytes] (or the
-//            interleaved layout of ozaki.cu, 8-line x 16-byte core matrices);
-//   pgemm    (kernel k_opipe) one 128 x 64 output tile per CTA, 10 warps: warp 0 streams the
-//            slices of each k chunk (96 KB: A 64 KB, B 32 KB) with cp.async.bulk into a two-stage
-//            shared-memory ring (mbarrier complete_tx); warp 1 issues the 72 tcgen05.mma of a chunk
-//            (M 128, N 64, K 16, FP32 accumulators in TMEM: levels 2..7 exact, 8..9 shared)
-//            and commits them to the stage's "empty" barrier; warps 2..9 move the exact levels
-//            out of TMEM into int64 registers after every 5 chunks and write C at the end.
+//            cores read them from shared memory, K-major lines of 64 bytes with the 64-byte
+//            swizzle: image[k chunk of 32][slice][line block of 64][64 x 64 bytes];
+//   pgemm    (kernel k_opipe) one 128 x 64 output tile per CTA, 10 warps.  Warp 0 streams the
+//            slices of each k chunk (96 KB: A 64 KB, B 32 KB) with cp.async.bulk into a
+//            two-stage shared-memory ring (mbarrier complete_tx).  Warp 1 issues the MMAs: the B
+//            slices of a stage lie one after another, so a_p times [b_q0 .. b_q0+3] is a single
+//            M 128 x N 256 x K 16 tcgen05.mma whose four 64-column blocks land in the TMEM
+//            accumulators of the levels p + q0 .. p + q0 + 3 (one accumulator of 64 columns per
+//            level 0..7, 512 columns); 13 MMAs per k step instead of 36.  Warps 2..9 drain the
+//            levels 0..5 every 5 chunks (160 values of k): they hold exact integers (at most 6
+//            products of < 2^14 each per k: < 2^24) that go into one int64 per element.  The
+//            levels 6..7 (< 2^-42 of the leading level) stay in FP32 over the whole of k (their
+//            rounding is < 2^-56 of the result) and are read with the output at the end.
 //
 // Every wait is bounded; a wait that runs out sets a CTA-wide abort flag, the other roles leave
 // their loops, copies and MMAs still in flight are waited for (bounded), TMEM is freed and the
@@ -38,14 +39,16 @@ namespace tb {
 namespace {
 
 constexpr int PP_M = 128, PP_N = 64, PP_KC = 32, PP_FLUSH = 5, PP_THREADS = 320;
-constexpr int PP_EXACT = 6;    // exact level accumulators (levels 2..7); one more for 8..9
+constexpr int PP_LEVELS = 8;    // TMEM accumulators, one per level p + q = 0..7
+constexpr int PP_EXACT = 6;     // levels 0..5 are drained as exact integers
 constexpr int PP_KMAX = 12288;  // |int64 level sums| < 1.02 * 2^49 K < 2^63
-constexpr int PP_STAGES = 2;  // the producer's bookkeeping below assumes two
-constexpr int PP_A_BYTES = 8 * 2 * 4096;  // 8 slices x 2 k steps x (128 lines x 16 k x 2 B)
-constexpr int PP_B_BYTES = 8 * 2 * 2048;  // 8 slices x 2 k steps x (64 lines x 16 k x 2 B)
+constexpr int PP_STAGES = 2;    // the producer's bookkeeping below assumes two
+constexpr int PP_A_BYTES = 8 * 8192;  // 8 slices x 128 lines x 64 B
+constexpr int PP_B_BYTES = 8 * 4096;  // 8 slices x 64 lines x 64 B
 constexpr int PP_STAGE_BYTES = PP_A_BYTES + PP_B_BYTES;
 constexpr int PP_SMEM = PP_STAGES * PP_STAGE_BYTES + 1024;
 constexpr int PP_TMEM_COLS = 512;
+static_assert(PP_LEVELS * PP_N == PP_TMEM_COLS, "one 64-column accumulator per level");
 constexpr int PP_GROUP = 8;  // row blocks per tile group
 constexpr int PP_WAIT = 1 << 22;
 
@@ -57,14 +60,9 @@ void ck(cudaError_t e, const char* what) {
 __device__ __forceinline__ uint32_t su32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
-// shared-memory matrix descriptors (K-major, descriptor version 1).  Interleaved: core matrices
-// of 8 lines x 16 bytes, 128 B apart along K and 256 B apart along the lines.  Swizzled: lines of
-// 64 bytes (32 BF16 of k), 8-line atoms 512 B apart, the 16-byte chunks of line r permuted by
-// chunk ^ ((r >> 1) & 3) (the 64-byte swizzle); a k step of 16 moves the start by 32 bytes.
-__device__ __forceinline__ uint64_t sdesc(uint32_t addr) {
-  return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)(128 >> 4) << 16) |
-         ((uint64_t)(256 >> 4) << 32) | ((uint64_t)1 << 46);
-}
+// shared-memory matrix descriptor (K-major, descriptor version 1): lines of 64 bytes (32 BF16 of
+// k), 8-line atoms 512 B apart, the 16-byte chunks of line r permuted by chunk ^ ((r >> 1) & 3)
+// (the 64-byte swizzle); a k step of 16 moves the start by 32 bytes
 __device__ __forceinline__ uint64_t sdesc_sw64(uint32_t addr) {
   return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)1 << 16) | ((uint64_t)(512 >> 4) << 32) |
          ((uint64_t)1 << 46) | ((uint64_t)4 << 61);
@@ -140,7 +138,6 @@ __global__ void k_pexp_cols(const double* __restrict__ M, int ld, int lines, int
 
 // ---- slice image: one block per (64 lines, 32 k); the FP64 tile goes through shared memory so
 // both memory orders read coalesced; each thread splits 8 consecutive k of one line
-template <bool SW>
 __global__ void __launch_bounds__(256) k_psplit(const double* __restrict__ M, int ld, int kcontig,
                                                 int lines, int K, int nlb,
                                                 const int* __restrict__ e, uint16_t* img) {
@@ -188,22 +185,12 @@ __global__ void __launch_bounds__(256) k_psplit(const double* __restrict__ M, in
       w[p][c >> 1] |= slice_bits(a, p, sign) << ((c & 1) * 16);
     }
   }
-  if (SW) {  // [k chunk][slice][line block][64 lines x 64 B, 16-byte chunks swizzled]
+  // [k chunk][slice][line block][64 lines x 64 B, 16-byte chunks swizzled]
 #pragma unroll
-    for (int p = 0; p < 8; ++p) {
-      const size_t off = (((size_t)kc * 8 + p) * nlb + lb) * 2048 + li * 32 +
-                         ((g ^ ((li >> 1) & 3)) << 3);
-      *reinterpret_cast<uint4*>(img + off) = make_uint4(w[p][0], w[p][1], w[p][2], w[p][3]);
-    }
-  } else {  // [k chunk][slice][k step][line block][8 x (2 core matrices of 8 lines x 16 B)]
-    const int ks = g >> 1, half = g & 1;
-    const int rg = li >> 3, r = li & 7;
-#pragma unroll
-    for (int p = 0; p < 8; ++p) {
-      const size_t off = ((((size_t)kc * 8 + p) * 2 + ks) * nlb + lb) * 1024 + rg * 128 +
-                         half * 64 + r * 8;
-      *reinterpret_cast<uint4*>(img + off) = make_uint4(w[p][0], w[p][1], w[p][2], w[p][3]);
-    }
+  for (int p = 0; p < 8; ++p) {
+    const size_t off = (((size_t)kc * 8 + p) * nlb + lb) * 2048 + li * 32 +
+                       ((g ^ ((li >> 1) & 3)) << 3);
+    *reinterpret_cast<uint4*>(img + off) = make_uint4(w[p][0], w[p][1], w[p][2], w[p][3]);
   }
 }
 
@@ -221,7 +208,6 @@ struct PipeArgs {
   int* status;
 };
 
-template <bool SW>
 __global__ void __launch_bounds__(PP_THREADS, 1) k_opipe(PipeArgs a) {
   // ---- tile of this CTA: groups of PP_GROUP row blocks, column blocks inside a group
   const int mt = (a.M + PP_M - 1) / PP_M, nt = (a.N + PP_N - 1) / PP_N;
@@ -283,7 +269,7 @@ __global__ void __launch_bounds__(PP_THREADS, 1) k_opipe(PipeArgs a) {
                      "r"(PP_STAGE_BYTES)
                      : "memory");
         unsigned char* st = smem + (size_t)s * PP_STAGE_BYTES;
-        if (SW) {  // per slice: A 8 KB (two line blocks), B 4 KB
+        {  // per slice: A 8 KB (two line blocks), B 4 KB
 #pragma unroll 1
           for (int p = 0; p < 8; ++p) {
             const size_t blk = (size_t)c * 8 + p;
@@ -300,25 +286,6 @@ __global__ void __launch_bounds__(PP_THREADS, 1) k_opipe(PipeArgs a) {
                 "l"(srcB), "r"(4096), "r"(bar)
                 : "memory");
           }
-        } else {
-#pragma unroll 1
-        for (int p = 0; p < 8; ++p)
-#pragma unroll 1
-          for (int ks = 0; ks < 2; ++ks) {
-            const size_t blk = ((size_t)c * 8 + p) * 2 + ks;
-            const uint16_t* srcA = a.A + (blk * a.nlbA + lbA) * 1024;
-            const uint16_t* srcB = a.B + (blk * a.nlbB + lbB) * 1024;
-            asm volatile(
-                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], "
-                "%2, [%3];" ::"r"(su32(st + (p * 2 + ks) * 4096)),
-                "l"(srcA), "r"(4096), "r"(bar)
-                : "memory");
-            asm volatile(
-                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], "
-                "%2, [%3];" ::"r"(su32(st + PP_A_BYTES + (p * 2 + ks) * 2048)),
-                "l"(srcB), "r"(2048), "r"(bar)
-                : "memory");
-          }
         }
         if (s == 0) last0 = c;
         else last1 = c;
@@ -330,8 +297,8 @@ __global__ void __launch_bounds__(PP_THREADS, 1) k_opipe(PipeArgs a) {
   } else if (warp == 1) {
     // ---- MMA issuer
     if (lane == 0) {
-      const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) |
-                             ((uint32_t)(PP_N >> 3) << 17) | ((uint32_t)(PP_M >> 4) << 24);
+      // instruction descriptor: FP32 accumulator, BF16 A and B (K-major), M 128, N set below
+      const uint32_t idesc0 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(PP_M >> 4) << 24);
       for (int c = 0; c < nkc; ++c) {
         const int s = c % PP_STAGES;
         const int win = c / PP_FLUSH;
@@ -348,26 +315,27 @@ __global__ void __launch_bounds__(PP_THREADS, 1) k_opipe(PipeArgs a) {
         asm volatile("tcgen05.fence::after_thread_sync;");
         const uint32_t stA = su32(smem + (size_t)s * PP_STAGE_BYTES);
         const uint32_t stB = stA + PP_A_BYTES;
-        uint32_t fresh = win_start ? 0x3Fu : 0u;  // exact levels restart every window
-        if (c == 0) fresh |= 0x40u;               // the shared level only at the start
+        // slice 0 goes in three MMAs (levels 0..3, 4..5, 6..7), the others in groups of four
+        // B slices; a window starts with the first two overwriting the exact levels, the
+        // levels 6..7 are overwritten only by the very first MMA of the tile
 #pragma unroll 1
         for (int ks = 0; ks < 2; ++ks)
 #pragma unroll 1
           for (int p = 0; p < 8; ++p)
 #pragma unroll 1
-            for (int q = 0; q + p < 8; ++q) {
-              const int lv = min(p + q, PP_EXACT);
-              const uint32_t acc = ((fresh >> lv) & 1u) ? 0u : 1u;
-              fresh &= ~(1u << lv);
-              const uint64_t da = SW ? sdesc_sw64(stA + (uint32_t)(p * 8192 + ks * 32))
-                                     : sdesc(stA + (uint32_t)((p * 2 + ks) * 4096));
-              const uint64_t db = SW ? sdesc_sw64(stB + (uint32_t)(q * 4096 + ks * 32))
-                                     : sdesc(stB + (uint32_t)((q * 2 + ks) * 2048));
+            for (int q0 = 0; q0 < 8 - p;) {
+              const int nq = p == 0 ? (q0 == 0 ? 4 : 2) : min(4, 8 - p - q0);
+              const bool first = ks == 0 && p == 0 && (q0 < PP_EXACT ? win_start : c == 0);
+              const uint32_t acc = first ? 0u : 1u;
+              const uint32_t idesc = idesc0 | ((uint32_t)((nq * PP_N) >> 3) << 17);
+              const uint64_t da = sdesc_sw64(stA + (uint32_t)(p * 8192 + ks * 32));
+              const uint64_t db = sdesc_sw64(stB + (uint32_t)(q0 * 4096 + ks * 32));
               asm volatile(
                   "{\n\t.reg .pred pd;\n\tsetp.ne.b32 pd, %4, 0;\n\t"
                   "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, pd;\n\t}" ::"r"(
-                      tmem + (uint32_t)(lv * PP_N)),
+                      tmem + (uint32_t)((p + q0) * PP_N)),
                   "l"(da), "l"(db), "r"(idesc), "r"(acc));
+              q0 += nq;
             }
         asm volatile(
             "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
@@ -419,17 +387,19 @@ __global__ void __launch_bounds__(PP_THREADS, 1) k_opipe(PipeArgs a) {
           }
         }
       }
+
       asm volatile("tcgen05.fence::before_thread_sync;");
       asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(&accfree)) : "memory");
     }
     if (__all_sync(0xffffffffu, (ok && !*abort) ? 1 : 0)) {
-      // levels 8..9 (accumulated over all of k) and the output
+      // C = 2^(eA + eB - 14) (T 2^-35 + F), F = levels 6 + 7
       const int i = i0 + row;
       const int ei = i < a.M ? a.eA[i] + a.eshiftA : 0;
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
-        uint32_t v[16];
-        tmem_ld16(lane_base + (uint32_t)(PP_EXACT * PP_N + 16 * h), v);
+        uint32_t v6[16], v7[16];
+        tmem_ld16(lane_base + (uint32_t)(6 * PP_N + 16 * h), v6);
+        tmem_ld16(lane_base + (uint32_t)(7 * PP_N + 16 * h), v7);
         if (i < a.M) {
 #pragma unroll
           for (int t = 0; t < 16; ++t) {
@@ -438,8 +408,8 @@ __global__ void __launch_bounds__(PP_THREADS, 1) k_opipe(PipeArgs a) {
               const int sc = ei + a.eB[j] - 14;
               const double scale =
                   (sc > -1022 && sc < 1023) ? __hiloint2double((sc + 1023) << 20, 0) : 0.0;
-              const double val =
-                  fma((double)T[16 * h + t], 0x1p-35, (double)__uint_as_float(v[t])) * scale;
+              const double f = (double)__uint_as_float(v6[t]) + (double)__uint_as_float(v7[t]);
+              const double val = fma((double)T[16 * h + t], 0x1p-35, f) * scale;
               a.C[i + (size_t)j * a.ldc] = val;
               if (a.sym && i != j) a.C[j + (size_t)i * a.ldc] = val;
             }
@@ -468,24 +438,16 @@ int pimage_lines(int lines) { return ((lines + PP_M - 1) / PP_M) * PP_M; }
 // slice image of a matrix: line i, position k is M[i + k ld] (kcontig = 0: the rows of M) or
 // M[k + i ld] (kcontig = 1: the columns of M); img holds pimage_bytes(lines, K) bytes and e
 // pimage_lines(lines) ints
-// layout of the slice images made from now on: 64-byte swizzled (default) or interleaved
-static bool g_pipe_swizzle = true;
-
 void psplit(const double* M, int ld, int kcontig, int lines, int K, PImage& img, cudaStream_t s) {
   img.lines = lines;
   img.K = K;
-  img.swz = g_pipe_swizzle ? 1 : 0;
   const int lp = pimage_lines(lines);
   const int nkc = (K + PP_KC - 1) / PP_KC;
   g_kernel_launches += 2;
   if (kcontig) k_pexp_cols<<<(lp * 32 + 255) / 256, 256, 0, s>>>(M, ld, lines, K, lp, img.e);
   else k_pexp_rows<<<lp / 32, 256, 0, s>>>(M, ld, lines, K, lp, img.e);
-  if (img.swz)
-    k_psplit<true><<<dim3(lp / 64, nkc), 256, 0, s>>>(M, ld, kcontig, lines, K, lp / 64, img.e,
-                                                      img.data);
-  else
-    k_psplit<false><<<dim3(lp / 64, nkc), 256, 0, s>>>(M, ld, kcontig, lines, K, lp / 64, img.e,
-                                                       img.data);
+  k_psplit<<<dim3(lp / 64, nkc), 256, 0, s>>>(M, ld, kcontig, lines, K, lp / 64, img.e,
+                                              img.data);
 }
 
 // C = 2^eshiftA op(A) op(B) from two slice images (A.K == B.K); sym: the product is symmetric
@@ -494,12 +456,9 @@ void pgemm(const PImage& A, const PImage& B, double* C, int ldc, bool sym, int* 
   if (A.lines <= 0 || B.lines <= 0) return;
   if (A.K != B.K) throw std::runtime_error("split GEMM: inner dimensions differ");
   if (A.K > PP_KMAX) throw std::runtime_error("split GEMM: inner dimension above 12288");
-  if (A.swz != B.swz) throw std::runtime_error("split GEMM: slice images of different layouts");
   static bool attr = false;
   if (!attr) {
-    ck(cudaFuncSetAttribute(k_opipe<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, PP_SMEM),
-       "smem attr pipelined split gemm");
-    ck(cudaFuncSetAttribute(k_opipe<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, PP_SMEM),
+    ck(cudaFuncSetAttribute(k_opipe, cudaFuncAttributeMaxDynamicSharedMemorySize, PP_SMEM),
        "smem attr pipelined split gemm");
     attr = true;
   }
@@ -523,8 +482,7 @@ void pgemm(const PImage& A, const PImage& B, double* C, int ldc, bool sym, int* 
                        : 2ull * a.M * a.N * A.K;
   const int tk = prof_kbegin(s);
   ++g_kernel_launches;
-  if (A.swz) k_opipe<true><<<mt * nt, PP_THREADS, PP_SMEM, s>>>(a);
-  else k_opipe<false><<<mt * nt, PP_THREADS, PP_SMEM, s>>>(a);
+  k_opipe<<<mt * nt, PP_THREADS, PP_SMEM, s>>>(a);
   prof_kend(KS_GEMM, tk, s);
 }
 
@@ -532,7 +490,6 @@ void pgemm(const PImage& A, const PImage& B, double* C, int ldc, bool sym, int* 
 
 namespace tb {
 extern bool g_pipe_gemm;
-void set_pipe_swizzle(bool on) { g_pipe_swizzle = on; }
 }
 
 // C = A B on the pipelined split GEMM from device pointers (column-major: A m x k with leading
@@ -576,7 +533,4 @@ extern "C" int tblite_gb300_split_gemm(int m, int n, int k, const double* a, con
   return rc;
 }
 
-extern "C" void tblite_gb300_set_pipelined_gemm(int mode) {
-  tb::g_pipe_gemm = mode != 0;
-  tb::set_pipe_swizzle(mode != 1);
-}
+extern "C" void tblite_gb300_set_pipelined_gemm(int enable) { tb::g_pipe_gemm = enable != 0; }

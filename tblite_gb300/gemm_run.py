@@ -1,6 +1,6 @@
 """Products of two seeded random FP64 matrices on the pipelined split GEMM.
 
-    python -m tblite_gb300.gemm_run [--n 4096] [--calls 2] [--sym] [--mode 2]
+    python -m tblite_gb300.gemm_run [--n 4096] [--calls 2] [--sym]
 
 Each call computes C = A B (or, with --sym, C = X X for a symmetric X) through
 ``tblite_gb300_split_gemm`` with n x n operands on the current GPU and prints the largest
@@ -20,8 +20,6 @@ def main(argv=None) -> int:
     ap.add_argument("--n", type=int, default=4096)
     ap.add_argument("--calls", type=int, default=2)
     ap.add_argument("--sym", action="store_true")
-    ap.add_argument("--mode", type=int, default=2,
-                    help="2: swizzled slice images (default), 1: interleaved")
     args = ap.parse_args(argv)
     root = Path(__file__).resolve().parents[1]
     if str(root) not in sys.path:
@@ -32,7 +30,6 @@ def main(argv=None) -> int:
 
     _build.build()
     lib = library.load()
-    lib.tblite_gb300_set_pipelined_gemm(args.mode)
     n = args.n
     g = torch.Generator(device="cuda").manual_seed(7)
     a = torch.randn(n, n, dtype=torch.float64, device="cuda", generator=g)
@@ -63,7 +60,7 @@ def main(argv=None) -> int:
     err = ((c.T - ref).abs() / (a.abs() @ b.abs())).max().item()
     flop = (n * (n + 1) * n if args.sym else 2 * n ** 3)
     best = min(times)
-    print(f"n {n} calls {args.calls} sym {args.sym} mode {args.mode} max relative deviation "
+    print(f"n {n} calls {args.calls} sym {args.sym} max relative deviation "
           f"{err:.3e} best call {best:.3f} ms (split, allocation and product) "
           f"{flop / best / 1e9:.2f} TFLOP/s FP64-equivalent")
     return 0

@@ -85,19 +85,6 @@ def test_zero_and_tiny(lib):
     assert np.all(np.abs(c - ref) <= bound + 1e-290)
 
 
-def test_interleaved_layout(lib):
-    """The interleaved slice layout (mode 1) gives the same products."""
-    lib.tblite_gb300_set_pipelined_gemm(1)
-    try:
-        rng = np.random.default_rng(11)
-        a = rng.standard_normal((300, 420))
-        b = rng.standard_normal((420, 200))
-        c, ref, bound = _run(lib, a, b)
-        assert np.all(np.abs(c - ref) <= bound)
-    finally:
-        lib.tblite_gb300_set_pipelined_gemm(2)
-
-
 def test_bad_arguments(lib):
     assert lib.tblite_gb300_split_gemm(0, 4, 4, None, None, None, 0, None) == -1
     assert lib.tblite_gb300_split_gemm(4, 5, 4, ctypes.c_void_p(1), ctypes.c_void_p(1),
