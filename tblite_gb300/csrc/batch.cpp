@@ -243,7 +243,7 @@ void layout(Plan& pl, Region* R) {
       *p = piece<double>(R, RS, na * D4_MREF);
     pl.d4_c6 = piece<double>(R, RS, na * na);
     pl.d4_dc6 = piece<double>(R, RS, na * na);
-    pl.d4_atm = piece<double>(R, RS, 5 * na * na);
+    pl.d4_atm = piece<double>(R, RS, 8 * na * na);
   }
 }
 

@@ -396,7 +396,7 @@ static void ensure_workspace(_tblite_calculator* c) {
       for (auto* b : {&w.d4_cn, &w.d4_e3, &w.d4_dEdcn}) b->alloc(na);
       w.d4_c6.alloc(na * na);
       w.d4_dc6.alloc(na * na);
-      w.d4_atm.alloc(5 * na * na);
+      w.d4_atm.alloc(8 * na * na);
     }
     w.at_z.upload(c->at_z, s);
     w.at_sh.upload(c->at_sh, s);

@@ -12,6 +12,8 @@
 // triple, so all reductions are deterministic (no atomics).
 #include <cuda_runtime.h>
 
+#include <stdexcept>
+
 #include "engine.h"
 
 namespace tb {
@@ -236,17 +238,26 @@ __global__ void k_d4_c6(int nat, DevD4 d, const double* __restrict__ gwv,
   d4_c6_dev(nat, d, gwv, dgwv_cn, c6, dc6);
 }
 
-// Axilrod-Teller-Muto term.  Every factor of a triple (i, j, l) that is a product over its
-// three pairs is tabulated per pair first (k_d4_atm_pairs): r^2, 1/r, the damping ratio
-// (r0/r)^(alpha/3), sqrt|C6| and dC6/dCN / (2 C6), so that (r0/r1)^(alpha/3) and
-// sqrt|C6_ij C6_il C6_jl| become products and no pow, sqrt or division but the damping's
-// remains per triple.  tab layout [5][nat][nat]; pairs beyond the cutoff hold r^2 = +inf.
+// Axilrod-Teller-Muto term (disp/d4.f90 three-body part, d4 get_atm_dispersion).  Every factor
+// of a triple (i, j, l) that is a product over its three pairs is tabulated per pair first
+// (k_d4_atm_pairs): r^2, 1/r, the damping ratio (r0/r)^(alpha/3), sqrt|C6| and
+// dC6_ij/dCN_i / (2 C6_ij) in both index orders, so that no pow or sqrt and a single division
+// remain per triple.  Each triple i < j < l is then evaluated once (k_d4_atm): its energy goes
+// 1/3 to each atom, its CN derivatives to the three atoms, and its derivatives with respect to
+// the three squared distances into a pair matrix Gamma (upper triangle); the forces and the
+// virial follow from Gamma in one pass over the pairs (k_d4_atm_grad):
+//   dE/dR_i = sum_j 2 Gamma_ij (R_i - R_j),  sigma = sum_{i<j} 2 Gamma_ij v_ij v_ij^T.
+// tab layout [8][nat][nat]: r^2 (+inf beyond the cutoff), 1/r, ratio, sqrt|C6|, dq, dq^T,
+// Gamma rows written by their owner atom, Gamma of the (j, l) pairs accumulated atomically.
+constexpr int ATM_TABLES = 8;
 __device__ __forceinline__ void d4_atm_pairs_dev(DevMol m, DevD4 d, const double* __restrict__ c6,
-                                                 const double* __restrict__ dc6, double* tab) {
+                                                 const double* __restrict__ dc6, double* tab,
+                                                 double* eat) {
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const int nat = m.nat;
   const size_t nn = (size_t)nat * nat;
   if (t >= (long long)nn) return;
+  if (t < nat) eat[t] = 0.0;
   const int i = (int)(t / nat), j = (int)(t % nat);
   double r2 = 0.0;
   for (int k = 0; k < 3; ++k) {
@@ -254,7 +265,7 @@ __device__ __forceinline__ void d4_atm_pairs_dev(DevMol m, DevD4 d, const double
     r2 += v * v;
   }
   const double cut2 = d.disp3_cutoff * d.disp3_cutoff;
-  double ir = 0.0, w = 0.0, sc = 0.0, dq = 0.0;
+  double ir = 0.0, w = 0.0, sc = 0.0, dq = 0.0, dqt = 0.0;
   if (i == j || r2 > cut2 || r2 < 1e-12) {
     r2 = __longlong_as_double(0x7ff0000000000000LL);  // +inf: never inside the cutoff
   } else {
@@ -265,48 +276,64 @@ __device__ __forceinline__ void d4_atm_pairs_dev(DevMol m, DevD4 d, const double
     const double c = c6[t];
     sc = sqrt(fabs(c));
     dq = c != 0.0 ? dc6[t] / (2.0 * c) : 0.0;
+    dqt = c != 0.0 ? dc6[(size_t)j * nat + i] / (2.0 * c) : 0.0;
   }
   tab[t] = r2;
   tab[nn + t] = ir;
   tab[2 * nn + t] = w;
   tab[3 * nn + t] = sc;
   tab[4 * nn + t] = dq;
+  tab[5 * nn + t] = dqt;
+  tab[7 * nn + t] = 0.0;
 }
 __global__ void k_d4_atm_pairs(DevMol m, DevD4 d, const double* __restrict__ c6,
-                               const double* __restrict__ dc6, double* tab) {
-  d4_atm_pairs_dev(m, d, c6, dc6, tab);
+                               const double* __restrict__ dc6, double* tab, double* eat) {
+  d4_atm_pairs_dev(m, d, c6, dc6, tab, eat);
 }
 
-// one warp per atom i; for every partner j the lanes walk l > j, so the table rows i and j
-// are read contiguously.  Atom i collects 1/3 of each triple energy, its own force, 1/3 of the
-// virial and the CN derivative through C6_ij and C6_il.
-__device__ __forceinline__ void d4_atm_dev(DevMol m, DevD4 d, const double* __restrict__ tab,
-                                           double* eat, double* grad, double* sig_at,
-                                           double* dEdcn) {
+// one warp per atom i, triples i < j < l: j warp-uniform, the lanes walk l > j.  The warp keeps
+// three rows in shared memory (3 nat doubles): Gamma_i. (roles (i, j) and (i, l)), the energy
+// thirds and the CN derivatives of the partners; Gamma of the (j, l) pairs goes to global memory
+// with coalesced atomics.  eat and dEdcn are accumulated (eat is zeroed by the pairs kernel).
+__device__ __forceinline__ void d4_atm_dev(DevMol m, DevD4 d, double* tab, double* eat,
+                                           double* dEdcn, double* srow) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (warp >= m.nat) return;
-  const int i = warp, nat = m.nat;
+  const int nat = m.nat;
+  if (warp >= nat) return;
+  const int i = warp;
   const size_t nn = (size_t)nat * nat;
   const double* R2 = tab;
   const double* IR = tab + nn;
   const double* W = tab + 2 * nn;
   const double* SC = tab + 3 * nn;
   const double* DQ = tab + 4 * nn;
+  const double* DQT = tab + 5 * nn;
+  double* GO = tab + 6 * nn;
+  double* GB = tab + 7 * nn;
+  double* sG = srow;
+  double* sE = srow + nat;
+  double* sD = srow + 2 * nat;
+  for (int l = lane; l < nat; l += 32) {
+    sG[l] = 0.0;
+    sE[l] = 0.0;
+    sD[l] = 0.0;
+  }
+  __syncwarp();
   const double cut2 = d.disp3_cutoff * d.disp3_cutoff;
   const double a6 = d.atm_alpha / 6.0;
-  double e = 0.0, g[3] = {0, 0, 0}, sg[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, dcn = 0.0;
-  const double* xi = m.xyz + 3 * i;
   const size_t ri = (size_t)i * nat;
-  for (int j = 0; j < nat; ++j) {
-    const double r2ij = R2[ri + j];
-    if (!(r2ij <= cut2)) continue;  // j == i or beyond the cutoff (warp uniform)
+  double ei = 0.0, di = 0.0;
+  for (int j = i + 1; j < nat; ++j) {
+    const double a = R2[ri + j];
+    if (!(a <= cut2)) continue;  // beyond the cutoff (warp uniform)
     const size_t rj = (size_t)j * nat;
-    const double irij = IR[ri + j], wij = W[ri + j], scij = SC[ri + j], dqij = DQ[ri + j];
-    double vij[3];
-    for (int k = 0; k < 3; ++k) vij[k] = m.xyz[3 * j + k] - xi[k];
+    const double irij = IR[ri + j], wij = W[ri + j], scij = SC[ri + j];
+    const double dqij = DQ[ri + j], dqji = DQT[ri + j];
+    const double ia = irij * irij;
+    double gA = 0.0, eJ = 0.0, dJ = 0.0;
     for (int l = j + 1 + lane; l < nat; l += 32) {
-      const double r2il = R2[ri + l], r2jl = R2[rj + l];
-      if (!(r2il <= cut2) || !(r2jl <= cut2)) continue;
+      const double c = R2[ri + l], b = R2[rj + l];
+      if (!(c <= cut2) || !(b <= cut2)) continue;
       const double iril = IR[ri + l], irjl = IR[rj + l];
       const double c9 = -d.s9 * scij * SC[ri + l] * SC[rj + l];
       const double t = wij * W[ri + l] * W[rj + l];
@@ -314,52 +341,107 @@ __device__ __forceinline__ void d4_atm_dev(DevMol m, DevD4 d, const double* __re
       const double ir2 = ir1 * ir1, ir3 = ir2 * ir1, ir5 = ir3 * ir2;
       const double fdmp = 1.0 / (1.0 + 6.0 * t);
       // angular factor in the squared distances a = r2ij, b = r2jl, c = r2il
-      const double a = r2ij, b = r2jl, c = r2il;
-      const double ia = irij * irij, ib = irjl * irjl, ic = iril * iril;
+      const double ib = irjl * irjl, ic = iril * iril;
       const double pa = a - b + c, pb = -a + b + c, pc = a + b - c;
       const double P = pc * pa * pb;
       const double ang = 0.375 * P * ir5 + ir3;
-      const double rr = ang * fdmp;
-      e += rr * c9 * (1.0 / 3.0);
+      const double E = ang * fdmp * c9;
       const double dPa = pa * pb + pc * pb - pc * pa;
       const double dPc = -pa * pb + pc * pb + pc * pa;
       const double dPb = pa * pb - pc * pb + pc * pa;
-      const double dfdt = -6.0 * fdmp * fdmp;
-      const double g0 = ang * dfdt * (-a6) * t;
-      const double dEa = c9 * ((0.375 * (dPa * ir5 - 2.5 * P * ir5 * ia) - 1.5 * ir3 * ia) * fdmp + g0 * ia);
-      const double dEb = c9 * ((0.375 * (dPb * ir5 - 2.5 * P * ir5 * ib) - 1.5 * ir3 * ib) * fdmp + g0 * ib);
-      const double dEc = c9 * ((0.375 * (dPc * ir5 - 2.5 * P * ir5 * ic) - 1.5 * ir3 * ic) * fdmp + g0 * ic);
-      double vil[3], vjl[3];
-      for (int k = 0; k < 3; ++k) {
-        vil[k] = m.xyz[3 * l + k] - xi[k];
-        vjl[k] = m.xyz[3 * l + k] - m.xyz[3 * j + k];
-      }
-      // r2ij = |R_j - R_i|^2 -> d/dR_i = -2 vij ; r2il -> -2 vil
-      for (int k = 0; k < 3; ++k) g[k] += -2.0 * dEa * vij[k] - 2.0 * dEc * vil[k];
-      for (int p = 0; p < 3; ++p)
-        for (int q = 0; q < 3; ++q)
-          sg[3 * p + q] += 2.0 / 3.0 * (dEa * vij[p] * vij[q] + dEb * vjl[p] * vjl[q]
-                                        + dEc * vil[p] * vil[q]);
-      // dE/dC6 = rr c9 / (2 C6)
-      dcn += rr * c9 * (dqij + DQ[ri + l]);
+      const double g0 = ang * (-6.0 * fdmp * fdmp) * (-a6) * t;
+      const double h = 0.375 * ir5, q = 2.5 * P * h, s = 1.5 * ir3;
+      const double dEa = c9 * ((dPa * h - (q + s) * ia) * fdmp + g0 * ia);
+      const double dEb = c9 * ((dPb * h - (q + s) * ib) * fdmp + g0 * ib);
+      const double dEc = c9 * ((dPc * h - (q + s) * ic) * fdmp + g0 * ic);
+      const double e3 = E * (1.0 / 3.0);
+      ei += e3;
+      eJ += e3;
+      sE[l] += e3;
+      gA += dEa;
+      sG[l] += dEc;
+      atomicAdd(GB + rj + l, dEb);
+      // dE/dCN through C6_pq = sqrt: E dC6_pq/dCN_p / (2 C6_pq)
+      di += E * (dqij + DQ[ri + l]);
+      dJ += E * (dqji + DQ[rj + l]);
+      sD[l] += E * (DQT[ri + l] + DQT[rj + l]);
+    }
+    gA = wsum(gA);
+    eJ = wsum(eJ);
+    dJ = wsum(dJ);
+    if (lane == 0) {
+      sG[j] += gA;
+      sE[j] += eJ;
+      sD[j] += dJ;
+    }
+    __syncwarp();
+  }
+  ei = wsum(ei);
+  di = wsum(di);
+  for (int l = lane; l < nat; l += 32) {
+    if (l > i) GO[ri + l] = sG[l];
+    if (l != i) {
+      if (sE[l] != 0.0) atomicAdd(eat + l, sE[l]);
+      if (sD[l] != 0.0) atomicAdd(dEdcn + l, sD[l]);
     }
   }
-  e = wsum(e);
-  for (int k = 0; k < 3; ++k) g[k] = wsum(g[k]);
-  for (int k = 0; k < 9; ++k) sg[k] = wsum(sg[k]);
-  dcn = wsum(dcn);
   if (lane == 0) {
-    eat[i] = e;
-    if (grad) {
-      for (int k = 0; k < 3; ++k) grad[3 * i + k] += g[k];
-      for (int k = 0; k < 9; ++k) sig_at[9 * i + k] += sg[k];
-      dEdcn[i] += dcn;
-    }
+    atomicAdd(eat + i, ei);
+    atomicAdd(dEdcn + i, di);
   }
 }
-__global__ void k_d4_atm(DevMol m, DevD4 d, const double* __restrict__ tab, double* eat,
-                         double* grad, double* sig_at, double* dEdcn) {
-  d4_atm_dev(m, d, tab, eat, grad, sig_at, dEdcn);
+__global__ void k_d4_atm(DevMol m, DevD4 d, double* tab, double* eat, double* dEdcn) {
+  extern __shared__ double atm_rows[];
+  d4_atm_dev(m, d, tab, eat, dEdcn, atm_rows + (size_t)(threadIdx.x >> 5) * 3 * m.nat);
+}
+
+// forces and virial from Gamma: one warp per atom, half of each pair's virial to each atom
+__device__ __forceinline__ void d4_atm_grad_dev(DevMol m, const double* __restrict__ tab,
+                                                double* grad, double* sig_at) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  const int nat = m.nat;
+  if (warp >= nat) return;
+  const int i = warp;
+  const size_t nn = (size_t)nat * nat;
+  const double* GO = tab + 6 * nn;
+  const double* GB = tab + 7 * nn;
+  double g[3] = {0, 0, 0}, sg[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  for (int j = lane; j < nat; j += 32) {
+    if (j == i) continue;
+    const size_t u = i < j ? (size_t)i * nat + j : (size_t)j * nat + i;
+    const double G = GO[u] + GB[u];
+    if (G == 0.0) continue;
+    double v[3];
+    for (int k = 0; k < 3; ++k) v[k] = m.xyz[3 * j + k] - m.xyz[3 * i + k];
+    for (int k = 0; k < 3; ++k) g[k] += -2.0 * G * v[k];
+    for (int p = 0; p < 3; ++p)
+      for (int q = 0; q < 3; ++q) sg[3 * p + q] += G * v[p] * v[q];
+  }
+  for (int k = 0; k < 3; ++k) g[k] = wsum(g[k]);
+  for (int k = 0; k < 9; ++k) sg[k] = wsum(sg[k]);
+  if (lane == 0) {
+    for (int k = 0; k < 3; ++k) grad[3 * i + k] += g[k];
+    for (int k = 0; k < 9; ++k) sig_at[9 * i + k] += sg[k];
+  }
+}
+__global__ void k_d4_atm_grad(DevMol m, const double* __restrict__ tab, double* grad,
+                              double* sig_at) {
+  d4_atm_grad_dev(m, tab, grad, sig_at);
+}
+
+// warps per block of k_d4_atm: its shared memory holds 3 nat doubles per warp
+static inline int atm_warps(int nat) {
+  const size_t per = (size_t)3 * nat * sizeof(double);
+  if (per * 2 <= 200 * 1024) return 2;
+  if (per <= 200 * 1024) return 1;
+  return 0;
+}
+static void atm_attr(size_t smem) {
+  static size_t set = 0;
+  if (smem > 48 * 1024 && smem > set) {
+    cudaFuncSetAttribute(k_d4_atm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    set = smem;
+  }
 }
 
 __device__ __forceinline__ void d4_cn_grad_dev(DevMol m, DevD4 d, const double* __restrict__ dEdcn, double* grad,
@@ -414,9 +496,16 @@ void d4_setup(const DevMol& m, const DevD4& d, D4Work& w, bool grad, double* gra
   k_d4_c6<<<(unsigned)((nn + 255) / 256), 256, 0, s>>>(m.nat, d, w.gwv, w.dgwv_cn, w.c6, w.dc6);
   cudaMemsetAsync(w.dEdcn, 0, sizeof(double) * m.nat, s);
   g_kernel_launches += 2;
-  k_d4_atm_pairs<<<(unsigned)((nn + 255) / 256), 256, 0, s>>>(m, d, w.c6, w.dc6, w.atm);
-  k_d4_atm<<<warps_grid(m.nat), 64, 0, s>>>(m, d, w.atm, w.e3, grad ? grad_out : nullptr, sig_at,
-                                             w.dEdcn);
+  k_d4_atm_pairs<<<(unsigned)((nn + 255) / 256), 256, 0, s>>>(m, d, w.c6, w.dc6, w.atm, w.e3);
+  const int wpb = atm_warps(m.nat);
+  if (!wpb) throw std::runtime_error("three-body dispersion: more atoms than the GPU kernel holds");
+  const size_t smem = (size_t)wpb * 3 * m.nat * sizeof(double);
+  atm_attr(smem);
+  k_d4_atm<<<(m.nat + wpb - 1) / wpb, 32 * wpb, smem, s>>>(m, d, w.atm, w.e3, w.dEdcn);
+  if (grad) {
+    ++g_kernel_launches;
+    k_d4_atm_grad<<<warps_grid(m.nat), 64, 0, s>>>(m, w.atm, grad_out, sig_at);
+  }
 }
 
 void d4_potential(const DevMol& m, const DevD4& d, D4Work& w, const double* qat, double* vat,
@@ -637,11 +726,17 @@ __global__ void kb_d4_c6(BARGS) {
 }
 __global__ void kb_d4_atm_pairs(BARGS) {
   BMOL;
-  d4_atm_pairs_dev(q.m, q.d4, q.d4w.c6, q.d4w.dc6, q.d4w.atm);
+  d4_atm_pairs_dev(q.m, q.d4, q.d4w.c6, q.d4w.dc6, q.d4w.atm, q.d4w.e3);
 }
 __global__ void kb_d4_atm(BARGS) {
   BMOL;
-  d4_atm_dev(q.m, q.d4, q.d4w.atm, q.d4w.e3, q.grad, q.sig_at, q.d4w.dEdcn);
+  extern __shared__ double atm_rows_b[];
+  d4_atm_dev(q.m, q.d4, q.d4w.atm, q.d4w.e3, q.d4w.dEdcn,
+             atm_rows_b + (size_t)(threadIdx.x >> 5) * 3 * q.m.nat);
+}
+__global__ void kb_d4_atm_grad(BARGS) {
+  BMOL;
+  d4_atm_grad_dev(q.m, q.d4w.atm, q.grad, q.sig_at);
 }
 __global__ void kb_d4_pair_pot(BARGS) {
   BMOL;
@@ -688,14 +783,15 @@ static inline dim3 batoms(const BatchLaunch& b) {
 
 void d4_setup_b(const BatchLaunch& b) {
   if (!b.count) return;
-  g_kernel_launches += 6;
+  g_kernel_launches += 7;
   kb_d4_cn<<<bwarps(b), 64, 0, b.s>>>(b.mp, b.list);
   kb_d4_weights<<<batoms(b), 128, 0, b.s>>>(b.mp, b.list);
   kb_d4_zeta<<<batoms(b), 128, 0, b.s>>>(b.mp, b.list, 0);
   const long long nn = (long long)b.nat_max * b.nat_max;
   kb_d4_c6<<<dim3((unsigned)((nn + 255) / 256), 1, b.count), 256, 0, b.s>>>(b.mp, b.list);
   kb_d4_atm_pairs<<<dim3((unsigned)((nn + 255) / 256), 1, b.count), 256, 0, b.s>>>(b.mp, b.list);
-  kb_d4_atm<<<bwarps(b), 64, 0, b.s>>>(b.mp, b.list);
+  kb_d4_atm<<<bwarps(b), 64, (size_t)2 * 3 * b.nat_max * sizeof(double), b.s>>>(b.mp, b.list);
+  kb_d4_atm_grad<<<bwarps(b), 64, 0, b.s>>>(b.mp, b.list);
 }
 void d3_setup_b(const BatchLaunch& b) {
   if (!b.count) return;

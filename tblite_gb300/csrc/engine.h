@@ -110,7 +110,7 @@ struct DevD4 {
 };
 struct D4Work {  // device scratch
   double *cn, *gw, *dgw, *gwv, *dgwdq, *dgwv_cn, *c6, *dc6, *e3, *dEdcn;
-  double* atm;  // [5][nat][nat] pair tables of the three-body term
+  double* atm;  // [8][nat][nat] pair tables and pair derivatives of the three-body term
 };
 // geometry setup: CN, weights, atomic C6 at q = 0, three-body energy (e3) and, with grad,
 // its gradient and dEdcn (w.dEdcn is reset here)
