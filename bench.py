@@ -48,13 +48,16 @@ WORKLOADS = {"c200h402": "C200H402 GFN2-xTB energy+gradient single point (602 at
              "ensemble512": "512-molecule subset of the same ensemble generator, batched",
              "h2o1000_alpb": "(H2O)1000 GFN2-xTB + ALPB(water) energy+gradient single point "
                              "(3000 atoms, 6000 AOs), density by spectral projection",
+             "c200h402_sp2": "C200H402 GFN2-xTB energy+gradient single point (602 atoms, 1202 "
+                             "AOs), density by spectral projection instead of diagonalisation",
              "autograd256": "256 alkanes CnH2n+2, n uniform in [4, 40] (seed 3), GFN2-xTB forces and "
                             "dE/d(shell self energy, CN shift, hardness, third-order derivative, "
                             "Slater exponent) through the torch.autograd bridge"}
 ENSEMBLE_SIZE = {"ensemble4096": 4096, "ensemble512": 512}
-GEOMETRY = {"h2o1000_alpb": "h2o1000"}  # workload -> workloads.config name
+GEOMETRY = {"h2o1000_alpb": "h2o1000", "c200h402_sp2": "c200h402"}  # -> workloads.config
 SOLVATED = {"h2o1000_alpb"}
-PURIFIED = {"h2o1000_alpb"}
+PURIFIED = {"h2o1000_alpb", "c200h402_sp2"}
+LARGE = {"h2o1000_alpb"}  # one oracle evaluation takes tens of minutes: bounded CPU samples
 SPLIT_SLICE_PRODUCTS = 36  # BF16 slice products per FP64 product in the split GEMM
 
 
@@ -316,7 +319,7 @@ def run_gb300(args):
                                   split_flops)
     if args.no_cpu:
         cpu_val, cores, cpu_sample = None, None, None
-    elif purified:
+    elif args.config in LARGE:
         cpu_val, cores, cpu_sample = _cpu_baseline_eigensolve(numbers, positions, iters)
     else:
         cpu_val, cores = _cpu_baseline(numbers, positions)
@@ -626,7 +629,7 @@ def run_reference(args):
     elif args.config == "autograd256":
         sample = workloads.alkane_batch(256, seed=3, nmin=4, nmax=40)[:16]
         sample_desc = "16 of the 256 alkanes per step (energy + gradient)"
-    elif args.config in PURIFIED:
+    elif args.config in LARGE:
         # one oracle evaluation takes tens of minutes: each step times one generalised
         # eigensolve, scaled by the oracle's own SCF iteration count for this system
         numbers, positions = workloads.config(GEOMETRY[args.config])
@@ -650,7 +653,7 @@ def run_reference(args):
                     "d2h_bytes_per_step": 0},
         }
     else:
-        sample = [workloads.config(args.config)]
+        sample = [workloads.config(GEOMETRY.get(args.config, args.config))]
         sample_desc = "1 full evaluation per step"
     t0 = time.perf_counter()
     for _ in range(args.steps):
