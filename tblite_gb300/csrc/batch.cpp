@@ -905,6 +905,12 @@ extern "C" int tblite_gb300_batch_singlepoint(tblite_context ctx, int nmol,
 
 extern "C" int tblite_gb300_batch_last_fallbacks(void) { return g_last_fallbacks; }
 extern "C" void tblite_gb300_set_split_gemm(int enable) { tb::g_split_gemm = enable != 0; }
+namespace tb {
+void set_tridiag_ctas_per_sm(int k);
+}
+extern "C" void tblite_gb300_set_tridiag_ctas_per_sm(int count) {
+  tb::set_tridiag_ctas_per_sm(count);
+}
 extern "C" void tblite_gb300_set_batch_streams(int count) {
   g_batch_streams = count < 1 ? 1 : (count > 8 ? 8 : count);
 }

@@ -1450,21 +1450,30 @@ __global__ void kb_scale_cols(BARGS, int weighted) {
   scale_cols_dev(q.m.nao, *q.icount, q.C, weighted ? q.vec_out : q.focc, q.scratch);
 }
 
-// smallest cluster (1, 2, 4, 8 blocks) whose shared memory holds the lower triangle
+// CTAs of the batched tridiagonalisation that should fit on one SM (1 or 2): with 2 the
+// clusters are made wide enough that each CTA holds at most ~110 KB, so a second molecule's CTA
+// computes while the first waits at a cluster barrier
+static int g_tridiag_ctas_per_sm = 1;
+// smallest cluster (1, 2, 4, 8 blocks) whose shared memory holds the lower triangle, within the
+// per-CTA budget of the chosen residency when possible
 static int tridiag_cluster(int n, size_t* smem) {
-  for (int nb = 1; nb <= 8; nb *= 2) {
-    const size_t need = sizeof(double) * sym_tridiag_doubles(n, nb);
-    if (need <= TRIDIAG_SMEM_MAX) {
-      *smem = need;
-      return nb;
+  const size_t caps[2] = {g_tridiag_ctas_per_sm >= 2 ? (size_t)110 * 1024 : TRIDIAG_SMEM_MAX,
+                          TRIDIAG_SMEM_MAX};
+  for (size_t cap : caps)
+    for (int nb = 1; nb <= 8; nb *= 2) {
+      const size_t need = sizeof(double) * sym_tridiag_doubles(n, nb);
+      if (need <= cap) {
+        *smem = need;
+        return nb;
+      }
     }
-  }
   return 0;
 }
+void set_tridiag_ctas_per_sm(int k) { g_tridiag_ctas_per_sm = k >= 2 ? 2 : 1; }
 int batch_tridiag_max_n() {
   int n = 1;
   size_t sm = 0;
-  while (tridiag_cluster(n + 1, &sm)) ++n;
+  while (tridiag_cluster(n + 1, &sm)) ++n;  // the second cap is the residency-independent one
   return n;
 }
 

@@ -92,6 +92,7 @@ _SIGNATURES = {
     "tblite_gb300_get_kernel_profile": (c_int, [_dbl_p, _int_p, c_int]),
     "tblite_gb300_set_split_gemm": (None, [c_int]),
     "tblite_gb300_set_batch_streams": (None, [c_int]),
+    "tblite_gb300_set_tridiag_ctas_per_sm": (None, [c_int]),
     "tblite_gb300_get_calculator_slater_exponents": (None, [c_void_p, c_void_p, _dbl_p]),
     "tblite_gb300_set_calculator_slater_exponents": (None, [c_void_p, c_void_p, _dbl_p]),
     "tblite_gb300_get_result_slater_gradient": (None, [c_void_p, c_void_p, _dbl_p]),
@@ -145,6 +146,11 @@ def set_profiling(enable: bool) -> None:
 def set_batch_streams(count: int) -> None:
     """Streams a batch call spreads its size buckets over (1 serialises them)."""
     load().tblite_gb300_set_batch_streams(int(count))
+
+
+def set_tridiag_ctas_per_sm(count: int) -> None:
+    """Schedule of the batched tridiagonalisation: 1 or 2 CTAs per SM."""
+    load().tblite_gb300_set_tridiag_ctas_per_sm(int(count))
 
 
 def set_split_gemm(enable: bool) -> None:
