@@ -54,8 +54,9 @@ void tblite_gb300_set_split_gemm(int enable);
 /* number of streams (1..8, default 8) over which a batch call spreads its size buckets; 1 runs
  * the buckets one after the other, so per-kernel event times bracket each kernel alone */
 void tblite_gb300_set_batch_streams(int count);
-/* schedule of the batched tridiagonalisation: 1 (default) the narrowest cluster whose CTAs fit
- * the shared memory of one SM each, 2 clusters wide enough that two CTAs share an SM */
+/* schedule of the batched tridiagonalisation: 2 (default) clusters wide enough that two CTAs
+ * share an SM (one computes while the other waits at a cluster barrier), 1 the narrowest
+ * cluster whose CTAs fit the shared memory of one SM each */
 void tblite_gb300_set_tridiag_ctas_per_sm(int count);
 
 /* enable (1) or disable (0) event timing for subsequent single points (process wide) */

@@ -1453,7 +1453,7 @@ __global__ void kb_scale_cols(BARGS, int weighted) {
 // CTAs of the batched tridiagonalisation that should fit on one SM (1 or 2): with 2 the
 // clusters are made wide enough that each CTA holds at most ~110 KB, so a second molecule's CTA
 // computes while the first waits at a cluster barrier
-static int g_tridiag_ctas_per_sm = 1;
+static int g_tridiag_ctas_per_sm = 2;
 // smallest cluster (1, 2, 4, 8 blocks) whose shared memory holds the lower triangle, within the
 // per-CTA budget of the chosen residency when possible
 static int tridiag_cluster(int n, size_t* smem) {
