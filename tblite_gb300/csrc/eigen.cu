@@ -49,31 +49,12 @@ struct EigenSolver {
   int* hstatus = nullptr; // pinned
   int coop_blocks = 0;
   int cap = 0;  // buffers hold problems up to this order
-  // the solver's buffers seen as a one-molecule batch (the cluster tridiagonalisation)
-  MolPtrs* dmp = nullptr;
-  int* dlist = nullptr;
 };
-
-// up to this order the one-molecule path tridiagonalises in one cluster of 8 CTAs (cluster
-// barriers) instead of a cooperative grid (grid barriers: ~4.5 us per column pair)
-constexpr int TRI_PLAIN_CLUSTER_MAX = 384;
-static void plain_molptrs(EigenSolver* e) {
-  MolPtrs h{};
-  h.m.nao = e->n;
-  h.A = e->A;
-  h.ed = e->d;
-  h.ee = e->e;
-  h.etau = e->tau;
-  ck(cudaMemcpy(e->dmp, &h, sizeof(MolPtrs), cudaMemcpyHostToDevice), "plain molptrs");
-}
 
 int eigen_capacity(const EigenSolver* e) { return e ? e->cap : 0; }
 void eigen_resize(EigenSolver* e, int n) {
   if (n > e->cap) throw std::runtime_error("eigen solver capacity exceeded");
-  if (n != e->n) {
-    e->n = n;
-    plain_molptrs(e);
-  }
+  e->n = n;
 }
 
 // ------------------------------------------------------------------------------------------
@@ -1001,10 +982,6 @@ EigenSolver* eigen_create(int n, cudaStream_t s) {
   ck(cudaMalloc(&e->gstatus, sizeof(int)), "gstatus");
   ck(cudaMemsetAsync(e->gstatus, 0, sizeof(int), s), "gstatus");
   ck(cudaMallocHost(&e->hstatus, sizeof(int)), "hstatus");
-  ck(cudaMalloc(&e->dmp, sizeof(MolPtrs)), "plain molptrs");
-  ck(cudaMalloc(&e->dlist, sizeof(int)), "plain list");
-  ck(cudaMemset(e->dlist, 0, sizeof(int)), "plain list");
-  plain_molptrs(e);
   int dev = 0, nsm = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -1029,8 +1006,6 @@ void eigen_destroy(EigenSolver* e) {
   cudaFree(e->status);
   cudaFree(e->gstatus);
   cudaFreeHost(e->hstatus);
-  cudaFree(e->dmp);
-  cudaFree(e->dlist);
   delete e;
 }
 
@@ -1042,11 +1017,6 @@ int eigen_set_overlap(EigenSolver* e, const double* S) {
      "copy S");
   return cholesky_inverse(n, e->L, e->X, e->status, e->hstatus, e->stream);
 }
-
-__global__ void __launch_bounds__(256) kb_tridiag(const MolPtrs* __restrict__ mp,
-                                                  const int* __restrict__ list);
-__host__ __device__ inline size_t sym_tridiag_doubles(int n, int nb);
-static void batch_attributes();
 
 int eigen_values(EigenSolver* es, const double* F, double* w_out, int nev) {
   const int n = es->n;
@@ -1061,26 +1031,7 @@ int eigen_values(EigenSolver* es, const double* F, double* w_out, int nev) {
     gemm64(true, false, n, n, n, 1.0, es->X, n, es->T1, n, 0.0, es->A, n, KM_LT_ROWEND | KM_SYM, s);
   }
   // tridiagonalise
-  if (n >= 2 && n <= TRI_PLAIN_CLUSTER_MAX) {
-    batch_attributes();
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(8, 1, 1);
-    cfg.blockDim = dim3(256, 1, 1);
-    cfg.dynamicSmemBytes = sizeof(double) * sym_tridiag_doubles(n, 8);
-    cfg.stream = s;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = 8;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    ++g_kernel_launches;
-    const int tk = prof_kbegin(s);
-    ck(cudaLaunchKernelEx(&cfg, kb_tridiag, (const MolPtrs*)es->dmp, (const int*)es->dlist),
-       "tridiag cluster");
-    prof_kend(KS_TRIDIAG, tk, s);
-  } else {
+  {
     int nn = n;
     int blocks = es->coop_blocks;
     const int need = (n * 32 + 255) / 256;
