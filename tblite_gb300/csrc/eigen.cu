@@ -1170,9 +1170,11 @@ bool eigen_gemm_failed(EigenSolver* es) {
 __device__ __forceinline__ size_t sym_off(int s, int n, int b, int nb) {
   return (size_t)s * n - (size_t)s * b - (size_t)nb * s * (s - 1) / 2;
 }
+constexpr int TRI_WARPS = 8;  // warps of a kb_tridiag CTA (256 threads)
 __host__ __device__ inline size_t sym_tridiag_doubles(int n, int nb) {
   const size_t ncpb = (size_t)(n + nb - 1) / nb;  // CTA 0 owns the most columns
-  return ncpb * n - (size_t)nb * ncpb * (ncpb - 1) / 2 + 4 * (size_t)n + 1;
+  // packed columns, four vectors (+1) and one row accumulator per warp
+  return ncpb * n - (size_t)nb * ncpb * (ncpb - 1) / 2 + (4 + TRI_WARPS) * (size_t)n + 1;
 }
 __global__ void __launch_bounds__(256) kb_tridiag(BARGS) {
   cg::cluster_group cl = cg::this_cluster();
@@ -1190,7 +1192,8 @@ __global__ void __launch_bounds__(256) kb_tridiag(BARGS) {
   double* sw = sv + n;         // [n] w = t p + K v
   double* spart = sw + n;      // [n] this CTA's part of p (read by the others)
   double* svpub = spart + n;   // [n + 1] v and tau published by the owner
-  double* scol = svpub + n + 1;  // packed columns (their total differs between CTAs)
+  double* wrow = svpub + n + 1;  // [TRI_WARPS][n] per-warp row accumulators of p, kept zero
+  double* scol = wrow + (size_t)TRI_WARPS * n;  // packed columns (their total differs by CTA)
   __shared__ double red[32];
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nwb = blockDim.x >> 5;
   for (int s = 0; s < ncpb; ++s) {
@@ -1198,6 +1201,7 @@ __global__ void __launch_bounds__(256) kb_tridiag(BARGS) {
     double* col = scol + sym_off(s, n, b, nb) - j;
     for (int r = j + tid; r < n; r += blockDim.x) col[r] = Ag[r + (size_t)j * n];
   }
+  for (size_t u = tid; u < (size_t)TRI_WARPS * n; u += blockDim.x) wrow[u] = 0.0;
   __syncthreads();
   auto column = [&](int s) { return scol + sym_off(s, n, b, nb) - (b + s * nb); };  // col[r], r >= c
   // owner of column i builds reflector i from its stored column and publishes v, tau
@@ -1238,38 +1242,39 @@ __global__ void __launch_bounds__(256) kb_tridiag(BARGS) {
     const int s0 = i < b ? 0 : (i - b) / nb + 1;  // first owned column > i
     if (t != 0.0) {
       __syncthreads();
-      // rows above the diagonal, from the owned columns c < r: spart_r = sum A(r, c) v_c.
-      // A row's work grows with its index, so every thread takes one row from the top and one
-      // from the bottom of the trailing block.
-      const int m = n - i - 1;
-      for (int u = tid; 2 * u < m; u += blockDim.x) {
-#pragma unroll 1
-        for (int side = 0; side < 2; ++side) {
-          const int r = side ? n - 1 - u : i + 1 + u;
-          if (side && r == i + 1 + u) break;  // the middle row of an odd count
-          double acc = 0.0;
-          for (int s2 = s0; s2 < ncpb; ++s2) {
-            const int c = b + s2 * nb;
-            if (c >= r) break;
-            acc = fma(scol[sym_off(s2, n, b, nb) + (r - c)], sv[c], acc);
-          }
-          spart[r] = acc;
-        }
-      }
-      __syncthreads();
-      // stored part of the owned columns: spart_c += sum_{r >= c} A(r, c) v_r (warp per column)
+      // p from the owned columns c > i, one warp per column and one pass over its stored rows
+      // r >= c: the column's dot product sum_r A(r, c) v_r goes to p_c, and A(r, c) v_c (r > c,
+      // the elements above the diagonal seen from their rows) into the warp's row accumulator
+      double* acc = wrow + (size_t)wid * n;
       for (int s2 = s0 + wid; s2 < ncpb; s2 += nwb) {
         const int c = b + s2 * nb;
         const double* col = column(s2);
-        double a0 = 0.0, a1 = 0.0;
+        const double vc = sv[c];
+        double dot = 0.0;
         int r = c + lane;
-        for (; r + 32 < n; r += 64) {
-          a0 = fma(col[r], sv[r], a0);
-          a1 = fma(col[r + 32], sv[r + 32], a1);
+        if (r == c) {  // the diagonal: dot only
+          dot = col[r] * sv[r];
+          r += 32;
         }
-        if (r < n) a0 = fma(col[r], sv[r], a0);
-        const double acc = wred(a0 + a1);
-        if (lane == 0) spart[c] += acc;
+        for (; r < n; r += 32) {
+          const double a = col[r];
+          dot = fma(a, sv[r], dot);
+          acc[r] = fma(a, vc, acc[r]);
+        }
+        dot = wred(dot);
+        if (lane == 0) acc[c] += dot;
+        __syncwarp();
+      }
+      __syncthreads();
+      // this CTA's part of p: the sum of the warp accumulators, which are zeroed again
+      for (int r = i + 1 + tid; r < n; r += blockDim.x) {
+        double s = 0.0;
+#pragma unroll
+        for (int w = 0; w < TRI_WARPS; ++w) {
+          s += wrow[(size_t)w * n + r];
+          wrow[(size_t)w * n + r] = 0.0;
+        }
+        spart[r] = s;
       }
     }
     cl.sync();
@@ -1287,22 +1292,12 @@ __global__ void __launch_bounds__(256) kb_tridiag(BARGS) {
       const double K = -0.5 * t * kk;
       for (int r = i + 1 + tid; r < n; r += blockDim.x) sw[r] = fma(K, sv[r], sw[r]);
       __syncthreads();
-      // the owned columns c > i are contiguous in the packed storage: one flat loop over their
-      // elements, each thread following its column with a cursor
-      if (s0 < ncpb) {
-        int s2 = s0;
-        size_t beg = sym_off(s0, n, b, nb);
-        size_t end = beg + (size_t)(n - (b + s0 * nb));
-        const size_t last = sym_off(ncpb, n, b, nb);
-        for (size_t e = beg + tid; e < last; e += blockDim.x) {
-          while (e >= end) {
-            ++s2;
-            beg = end;
-            end = beg + (size_t)(n - (b + s2 * nb));
-          }
-          const int c = b + s2 * nb, r = c + (int)(e - beg);
-          scol[e] = fma(-sv[r], sw[c], fma(-sw[r], sv[c], scol[e]));
-        }
+      // rank-2 update of the owned columns c > i, one warp per column
+      for (int s2 = s0 + wid; s2 < ncpb; s2 += nwb) {
+        const int c = b + s2 * nb;
+        double* col = column(s2);
+        const double vc = sv[c], wc = sw[c];
+        for (int r = c + lane; r < n; r += 32) col[r] = fma(-sv[r], wc, fma(-sw[r], vc, col[r]));
       }
     }
     __syncthreads();
