@@ -1094,7 +1094,7 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
     cuda_check(cudaMemcpy(&pur_status, purify_status(w.pur), sizeof(int), cudaMemcpyDeviceToHost),
                "purify status");
   if (eigen_gemm_failed(w.eig) || pur_status != 0)
-    throw std::runtime_error("a device wait ran out (tensor-core product or tridiagonalisation)");
+    throw std::runtime_error("tensor-core matrix product did not complete (wait limit reached)");
   g_prof.collect();
   g_prof.iterations = iscf;
   if (c->solv) {

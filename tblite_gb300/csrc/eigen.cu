@@ -45,8 +45,7 @@ struct EigenSolver {
   double *tw = nullptr;   // eigenvalue scratch: e^2 [n] (double), d and e^2 [n] (float)
   double *Y = nullptr;    // eigenvectors of T, column-major [k][n]
   int* status = nullptr;  // device
-  int* gstatus = nullptr; // device: 1 once a tensor-core GEMM did not answer, 2 a flag wait
-  int* tflag = nullptr;   // device: reflectors published by the shared-memory tridiagonalisation
+  int* gstatus = nullptr; // device: 1 once a tensor-core GEMM did not answer
   int* hstatus = nullptr; // pinned
   int coop_blocks = 0;
   int cap = 0;  // buffers hold problems up to this order
@@ -197,34 +196,29 @@ constexpr size_t TRIDIAG_SMEM_MAX = 200 * 1024;
 // Shared-memory resident variant for n where every block can hold its columns: global column j
 // lives in block j % nb (slot j / nb) for the whole reduction, so the symmetric matrix-vector
 // product, the rank-2 update and the next reflector read and write shared memory only; just the
-// reflector v and the product p travel through L2.  One grid barrier per column (for p): the
-// owner of column i+1 applies step i to that column first, builds reflector i+1 and publishes it
-// behind a release flag (tflag = i + 2) before it updates its other columns, and the other
-// blocks wait for the flag instead of a second barrier.  p goes through a buffer per step
-// parity, so a block that has seen the next reflector never overwrites a p another block still
-// reads.  A flag wait that runs out (it cannot while all blocks are resident, which the
-// cooperative launch guarantees) sets *wstat = 2 and the block goes on, so no block is left at
-// the barrier.
-constexpr int TRI_FLAG_WAIT = 1 << 24;
-__device__ __forceinline__ void tridiag_smem_body(int n, double* A, double* d, double* e,
-                                                  double* tau, double* vbuf, double* pbuf,
-                                                  int* tflag, int* wstat, int nb, int b,
-                                                  cg::grid_group grid) {
+// reflector v and the product p travel through L2.  Two grid barriers per column.
+template <class Sync>
+__device__ __forceinline__ void tridiag_smem_body(int n, double* A, double* d, double* e, double* tau,
+                                                  double* vbuf, double* pbuf, int nb, int b,
+                                                  Sync sync) {
+  // columns owned round-robin by the nb cooperating blocks; sync() is their common barrier
   extern __shared__ double sm[];
+
   const int ncpb = (n + nb - 1) / nb;
   double* scol = sm;                    // [ncpb][n]
   double* sv = sm + (size_t)ncpb * n;   // [n]  reflector of the current step
-  double* sp = sv + n;                  // [n]  p, then w, of the current step
+  double* sp = sv + n;                  // [n]  p of the current step
   __shared__ double red[32];
   __shared__ double sK;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwb = blockDim.x >> 5;
+  // load owned columns
   for (int s = 0; s < ncpb; ++s) {
     const int j = b + s * nb;
     if (j >= n) break;
     for (int r = threadIdx.x; r < n; r += blockDim.x) scol[(size_t)s * n + r] = A[r + (size_t)j * n];
   }
   __syncthreads();
-  // owner of column i builds reflector i from its shared copy, publishes it, raises the flag
+  // owner of column i builds reflector i from its shared copy and publishes it
   auto reflector = [&](int i) {
     double* col = scol + (size_t)(i / nb) * n;
     const double alpha = col[i + 1];
@@ -249,32 +243,15 @@ __device__ __forceinline__ void tridiag_smem_body(int n, double* A, double* d, d
       e[i] = beta;
       d[i] = col[i];
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      __threadfence();
-      asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(tflag), "r"(i + 1) : "memory");
-    }
-  };
-  // wait until reflector i is published (thread 0 polls, the block follows)
-  auto await = [&](int i) {
-    if (threadIdx.x == 0) {
-      int it = 0, f = 0;
-      for (; it < TRI_FLAG_WAIT; ++it) {
-        asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(f) : "l"(tflag) : "memory");
-        if (f >= i + 1) break;
-      }
-      if (it == TRI_FLAG_WAIT) atomicExch(wstat, 2);
-    }
-    __syncthreads();
   };
   if (n > 1 && b == 0) reflector(0);
   if (n == 1 && b == 0 && threadIdx.x == 0) d[0] = scol[0];
+  sync();
   for (int i = 0; i < n - 1; ++i) {
-    await(i);
-    double* pb = pbuf + (size_t)(i & 1) * 2 * n;
-    // published by another block after the previous barrier: read past L1
-    const double t = __ldcg(tau + i);
-    for (int r = i + 1 + threadIdx.x; r < n; r += blockDim.x) sv[r] = __ldcg(vbuf + r);
+    const int m = n - i - 1;
+    const double t = tau[i];
+    // copy v (rows i+1..n-1) into shared memory
+    for (int r = i + 1 + threadIdx.x; r < n; r += blockDim.x) sv[r] = vbuf[r];
     __syncthreads();
     // p_j = t * A(i+1:n, j) . v for owned columns j > i
     for (int s = wid; s < ncpb; s += nwb) {
@@ -285,17 +262,17 @@ __device__ __forceinline__ void tridiag_smem_body(int n, double* A, double* d, d
       for (int r = i + 1 + lane; r < n; r += 32) acc += col[r] * sv[r];
       acc = wred(acc) * t;
       if (lane == 0) {
-        pb[j] = acc;
-        pb[n + j] = acc * sv[j];
+        pbuf[j] = acc;
+        pbuf[n + j] = acc * sv[j];
       }
     }
-    grid.sync();
-    // K = -1/2 t (p . v), same order in every block; w = p + K v
+    sync();
+    // K = -1/2 t (p . v), same order in every block
     {
       double s = 0.0;
       for (int r = i + 1 + threadIdx.x; r < n; r += blockDim.x) {
-        sp[r] = pb[r];
-        s += pb[n + r];
+        sp[r] = pbuf[r];
+        s += pbuf[n + r];
       }
       s = block_sum256(s, red);
       if (threadIdx.x == 0) sK = -0.5 * t * s;
@@ -303,39 +280,31 @@ __device__ __forceinline__ void tridiag_smem_body(int n, double* A, double* d, d
     }
     const double K = sK;
     if (t != 0.0) {
+      // w = p + K v once per row, then two FMAs per element: A -= v w^T + w v^T
       for (int r = i + 1 + threadIdx.x; r < n; r += blockDim.x) sp[r] = fma(K, sv[r], sp[r]);
       __syncthreads();
-    }
-    // A -= v w^T + w v^T on the owned columns j > i, column i+1 first (look-ahead)
-    auto update = [&](int s) {
-      const int j = b + s * nb;
-      double* col = scol + (size_t)s * n;
-      const double vc = sv[j], wc = sp[j];
-      for (int r = i + 1 + threadIdx.x; r < n; r += blockDim.x)
-        col[r] = fma(-sv[r], wc, fma(-sp[r], vc, col[r]));
-    };
-    const bool owner = (i + 1) % nb == b;
-    const int snext = (i + 1) / nb;
-    if (owner) {
-      if (t != 0.0) update(snext);
-      __syncthreads();
-      if (i + 1 < n - 1) reflector(i + 1);
-      else if (threadIdx.x == 0) d[n - 1] = scol[(size_t)snext * n + (n - 1)];
-    }
-    if (t != 0.0)
       for (int s = 0; s < ncpb; ++s) {
         const int j = b + s * nb;
-        if (j <= i + 1 || j >= n) continue;
-        update(s);
+        if (j <= i || j >= n) continue;
+        double* col = scol + (size_t)s * n;
+        const double vc = sv[j], wc = sp[j];
+        for (int r = i + 1 + threadIdx.x; r < n; r += blockDim.x)
+          col[r] = fma(-sv[r], wc, fma(-sp[r], vc, col[r]));
       }
+    }
     __syncthreads();
+    if ((i + 1) % nb == b) {
+      if (i + 1 < n - 1) reflector(i + 1);
+      else if (threadIdx.x == 0) d[n - 1] = scol[(size_t)((n - 1) / nb) * n + (n - 1)];
+    }
+    sync();
   }
 }
 __global__ void __launch_bounds__(256) k_tridiag_smem(int n, double* A, double* d, double* e,
-                                                      double* tau, double* vbuf, double* pbuf,
-                                                      int* tflag, int* wstat) {
-  tridiag_smem_body(n, A, d, e, tau, vbuf, pbuf, tflag, wstat, (int)gridDim.x, (int)blockIdx.x,
-                    cg::this_grid());
+                                                      double* tau, double* vbuf, double* pbuf) {
+  cg::grid_group grid = cg::this_grid();
+  tridiag_smem_body(n, A, d, e, tau, vbuf, pbuf, (int)gridDim.x, (int)blockIdx.x,
+                    [&] { grid.sync(); });
 }
 
 // ------------------------------------------------------------------------------------------
@@ -1006,8 +975,7 @@ EigenSolver* eigen_create(int n, cudaStream_t s) {
   ck(cudaMalloc(&e->e, sizeof(double) * (n + 1)), "e");
   ck(cudaMalloc(&e->tau, sizeof(double) * (n + 1)), "tau");
   ck(cudaMalloc(&e->w, sizeof(double) * (n + 1)), "w");
-  ck(cudaMalloc(&e->pv, sizeof(double) * 6 * (n + 1)), "pv");
-  ck(cudaMalloc(&e->tflag, sizeof(int)), "tflag");
+  ck(cudaMalloc(&e->pv, sizeof(double) * 4 * (n + 1)), "pv");
   ck(cudaMalloc(&e->tw, sizeof(double) * 2 * (n + 1)), "tw");
   ck(cudaMalloc(&e->scal, sizeof(double) * 8), "scal");
   ck(cudaMalloc(&e->status, sizeof(int)), "status");
@@ -1037,7 +1005,6 @@ void eigen_destroy(EigenSolver* e) {
     cudaFree(p);
   cudaFree(e->status);
   cudaFree(e->gstatus);
-  cudaFree(e->tflag);
   cudaFreeHost(e->hstatus);
   delete e;
 }
@@ -1075,9 +1042,8 @@ int eigen_values(EigenSolver* es, const double* F, double* w_out, int nev) {
     const size_t smem = sizeof(double) * (ncpb * n + 2 * (size_t)n);
     if (smem <= TRIDIAG_SMEM_MAX) {
       double* vbuf = es->pv;
-      double* pbuf = es->pv + (n + 1);  // [2][2n]: p and p v per step parity
-      ck(cudaMemsetAsync(es->tflag, 0, sizeof(int), s), "tflag");
-      void* args[] = {&nn, &es->A, &es->d, &es->e, &es->tau, &vbuf, &pbuf, &es->tflag, &es->gstatus};
+      double* pbuf = es->pv + (n + 1);
+      void* args[] = {&nn, &es->A, &es->d, &es->e, &es->tau, &vbuf, &pbuf};
       ++g_kernel_launches;
       const int tk = prof_kbegin(s);
       ck(cudaLaunchCooperativeKernel((void*)k_tridiag_smem, nb, 256, args, smem, s), "tridiag_smem");
