@@ -142,3 +142,68 @@ def gfn2_energies(calcs: Sequence[Calculator], positions: Sequence, parameters:
         kw = parameters[i] if parameters is not None else {}
         out.append(gfn2_energy(calc, pos, **kw))
     return out
+
+
+def _batch_function():
+    torch = _torch()
+    k = 1 + len(PARAMETERS)
+
+    class GFN2EnergyBatch(torch.autograd.Function):
+        """E_i(positions_i, parameters_i) for many calculators in one batched engine call
+        (tblite_gb300_batch_singlepoint); the forces and dE/dtheta of every molecule come from
+        the same call."""
+
+        @staticmethod
+        def forward(ctx, calcs, *tensors):
+            from .interface import batch_singlepoint
+
+            for i, calc in enumerate(calcs):
+                pos, *prm = tensors[k * i:k * (i + 1)]
+                calc.update(pos.detach().to("cpu", torch.float64).numpy())
+                set_shell_parameters(
+                    calc, **{name: t.detach().to("cpu", torch.float64).numpy()
+                             for name, t in zip(PARAMETERS, prm)})
+                library.set_parameter_gradient(calc._ctx, calc._calc)
+            results = batch_singlepoint(list(calcs))
+            grads, energies = [], []
+            for i, res in enumerate(results):
+                pos, sel = tensors[k * i], tensors[k * i + 1]
+                pg = parameter_gradient(res, sel.numel())
+                grads.append(torch.from_numpy(res.get("gradient")).to(pos))
+                grads += [torch.from_numpy(pg[name]).to(sel) for name in PARAMETERS]
+                energies.append(res.get("energy"))
+            ctx.save_for_backward(*grads)
+            ctx.nmol = len(results)
+            return torch.tensor(energies, dtype=torch.float64, device=tensors[0].device)
+
+        @staticmethod
+        def backward(ctx, grad_e):
+            g = ctx.saved_tensors
+            out = [None]
+            for i in range(ctx.nmol):
+                out += [grad_e[i] * t for t in g[k * i:k * (i + 1)]]
+            return tuple(out)
+
+    return GFN2EnergyBatch
+
+
+_FNB = None
+
+
+def gfn2_energies_batch(calcs: Sequence[Calculator], positions: Sequence,
+                        parameters: Optional[Sequence[dict]] = None):
+    """Differentiable GFN2-xTB energies of many molecules, evaluated in one batched engine call;
+    returns a tensor [nmol] whose backward pass gives every molecule's forces and dE/dtheta."""
+    global _FNB
+    torch = _torch()
+    if _FNB is None:
+        _FNB = _batch_function()
+    flat = []
+    for i, (calc, pos) in enumerate(zip(calcs, positions)):
+        kw = parameters[i] if parameters is not None else {}
+        cur = shell_parameters(calc)
+        flat.append(pos)
+        for name in PARAMETERS:
+            v = kw.get(name)
+            flat.append(v if v is not None else torch.tensor(cur[name], dtype=torch.float64))
+    return _FNB.apply(tuple(calcs), *flat)

@@ -17,10 +17,11 @@
 //
 // A molecule leaves the batch for the one-molecule path (which then reproduces exactly what a
 // plain call does, including its errors) when it is larger than the batched
-// tridiagonalisation holds, uses temperature annealing, carries an implicit solvation model or
-// asks for the parameter gradient, would need more Broyden history than the batch keeps, has a
+// tridiagonalisation holds, uses temperature annealing, carries an implicit solvation model,
+// would need more Broyden history than the batch keeps, has a
 // Fermi level within 51 kT of the highest eigenvalue the SCF computes, does not converge within
 // its iteration limit, or fails (overlap not positive definite, singular Broyden system).
+// Molecules that ask for the parameter gradient get it in the batch, after the nuclear gradient.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -111,6 +112,7 @@ struct Plan {
   int nat, nsh, nao, nd, memory, max_iter, method;
   double nalp, nbet;
   bool has_d4, has_d3;
+  bool param_grad;  // dE/d(shell parameters) with the single point
   // offsets (region, offset) of every array
   Piece xyz, at_z, at_sh, sh_atom, sh_l, sh_nprim, sh_alpha, sh_coeff, sh_ao, ao_sh, ao_at, sh_se0,
       sh_kcn, sh_shpoly, sh_zeta, sh_hub, sh_gam3, sh_refocc, at_en, at_rad, at_rcov, at_mprad,
@@ -125,6 +127,7 @@ struct Plan {
   Piece bq, bqlast, bdq, bdqlast, bdf, bu, ba, bomega, bwork, bstatus;
   Piece grad, sigma, sig_at, dEdcn;
   Piece X, A, T1, Y, lu, ed, ee, etau, epv, escal, estatus, conv;
+  Piece pgrad, zgrad;  // [4][nsh], [nsh] (param_grad only)
 };
 
 struct Bucket {
@@ -208,6 +211,10 @@ void layout(Plan& pl, Region* R) {
   pl.eelec = piece<double>(R, RR, na);
   pl.erep = piece<double>(R, RR, na);
   if (pl.has_d4) pl.d4_e3 = piece<double>(R, RR, na);
+  if (pl.param_grad) {
+    pl.pgrad = piece<double>(R, RR, 4 * ns);
+    pl.zgrad = piece<double>(R, RR, ns);
+  }
   // scratch
   pl.cn = piece<double>(R, RS, na);
   pl.se = piece<double>(R, RS, ns);
@@ -412,6 +419,9 @@ MolPtrs make_ptrs(const Plan& pl, const Bases& db) {
   q.escal = db.at<double>(pl.escal);
   q.estatus = db.at<int>(pl.estatus);
   q.conv = db.at<double>(pl.conv);
+  q.param_grad = pl.param_grad ? 1 : 0;
+  q.pgrad = pl.param_grad ? db.at<double>(pl.pgrad) : nullptr;
+  q.zgrad = pl.param_grad ? db.at<double>(pl.zgrad) : nullptr;
   return q;
 }
 
@@ -612,6 +622,8 @@ std::vector<int> run_chunk(std::vector<Plan>& plans, Arena& ar, _tblite_context*
     }
   };
   const Gfn2Scalars p = gfn2_scalars(plans[0].c);  // h0_cutoff is taken per molecule
+  bool any_param_grad = false;
+  for (const Plan& pl : plans) any_param_grad = any_param_grad || pl.param_grad;
 
   // geometry setup
   upload_lists(active);
@@ -721,6 +733,10 @@ std::vector<int> run_chunk(std::vector<Plan>& plans, Arena& ar, _tblite_context*
       density_b(L, true);
       launch_h0_gradient_b(L, p);
       launch_cn_grad_b(L, p);
+      if (any_param_grad) {  // dE/d(shell parameters), Slater exponents (GFN2)
+        launch_param_grad_b(L);
+        launch_zeta_grad_b(L, p);
+      }
     });
     cuda_check(cudaEventRecord(ev1, s), "event");
     cuda_check(cudaMemcpyAsync(ar.host, db.base[RR], R[RR].size, cudaMemcpyDeviceToHost, s),
@@ -777,6 +793,22 @@ std::vector<int> run_chunk(std::vector<Plan>& plans, Arena& ar, _tblite_context*
       res->wbo_channels = 0;
       res->has_wfn = true;
       molecular_moments(pl.mol, res);
+      if (pl.param_grad) {
+        std::vector<double> pg;
+        get(pl.pgrad, 4 * (size_t)pl.nsh, pg);
+        const size_t ns = pl.nsh;
+        res->dse.assign(pg.begin(), pg.begin() + ns);
+        res->dhub.assign(pg.begin() + ns, pg.begin() + 2 * ns);
+        res->dgam3.assign(pg.begin() + 2 * ns, pg.begin() + 3 * ns);
+        res->dkcn.assign(pg.begin() + 3 * ns, pg.end());
+        get(pl.zgrad, ns, res->dzeta);
+      } else {
+        res->dse.clear();
+        res->dhub.clear();
+        res->dgam3.clear();
+        res->dkcn.clear();
+        res->dzeta.clear();
+      }
     }
   }
   cudaEventDestroy(ev0);
@@ -845,8 +877,9 @@ extern "C" int tblite_gb300_batch_singlepoint(tblite_context ctx, int nmol,
       continue;
     }
     const bool anneal = c->anneal && c->anneal_kt > c->etemp;
-    // implicit solvation and the parameter gradient run on the one-molecule path
-    if (pl.nao > tri_max || anneal || pl.max_iter < 1 || c->solv || c->param_grad) {
+    // implicit solvation runs on the one-molecule path
+    pl.param_grad = c->param_grad != 0;
+    if (pl.nao > tri_max || anneal || pl.max_iter < 1 || c->solv) {
       plain.push_back(i);
       continue;
     }

@@ -353,6 +353,10 @@ struct MolPtrs {
   int* estatus;
   double* conv;  // [0] previous electronic energy, [1] current, [2] rms(dq)
   int* flag;     // 1 converged, 0 running, <0 failed (Broyden or Cholesky), set on device
+  // parameter gradient (param_grad != 0): [4][nsh] dE/d(self energy, hardness, hardness
+  // derivative, CN shift) and [nsh] dE/d(Slater exponent)
+  int param_grad;
+  double *pgrad, *zgrad;
 };
 
 // one launch of a batched step: the molecules list[0..count) of one size bucket
@@ -363,6 +367,12 @@ struct BatchLaunch {
   int nat_max, nsh_max, nao_max, nd_max;
   cudaStream_t s;
 };
+// batched parameter gradient of the molecules that ask for it (after the gradient phase: P, W in
+// F, the last potentials): self energies from H0 / ((e_s + e_t)/2), hardness, third order, CN
+// shift, Slater exponents
+void launch_param_grad_b(const BatchLaunch& b);
+void launch_zeta_grad_b(const BatchLaunch& b, const Gfn2Scalars& p);
+
 
 // batched counterparts of the launchers above (same arithmetic, per-molecule pointers)
 void launch_cn_b(const BatchLaunch& b, const Gfn2Scalars& p);

@@ -445,11 +445,14 @@ void launch_h0_gradient(const DevMol& m, const Gfn2Scalars& p, const double* se,
 // d ln hscale / d zeta_i = wexp (1/(2 zeta_i) - 1/(zeta_i + zeta_j)) off-site.  The same form
 // holds for on-site pairs (no H0 scaling there) and for i == j (bra and ket derivatives equal).
 // ---------------------------------------------------------------------------------------
-__global__ void k_zeta_grad(DevMol m, Gfn2Scalars p, const double* __restrict__ se,
-                            const double* __restrict__ P, const double* __restrict__ W,
-                            const double* __restrict__ vao, const double* __restrict__ vdp,
-                            const double* __restrict__ vqp, double* dz) {
-  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+__device__ __forceinline__ void zeta_grad_dev(const DevMol& m, const Gfn2Scalars& p,
+                                              const double* __restrict__ se,
+                                              const double* __restrict__ P,
+                                              const double* __restrict__ W,
+                                              const double* __restrict__ vao,
+                                              const double* __restrict__ vdp,
+                                              const double* __restrict__ vqp, double* dz,
+                                              long long t) {
   if (t >= (long long)m.nsh * m.nsh) return;
   const int ish = (int)(t / m.nsh), jsh = (int)(t % m.nsh);
   const int iat = m.sh_atom[ish], jat = m.sh_atom[jsh];
@@ -562,6 +565,13 @@ __global__ void k_zeta_grad(DevMol m, Gfn2Scalars p, const double* __restrict__ 
   const double val = 2.0 / m.sh_zeta[ish] * accd + 2.0 * dhij * accs;
   atomicAdd(dz + ish, val);
 }
+__global__ void k_zeta_grad(DevMol m, Gfn2Scalars p, const double* __restrict__ se,
+                            const double* __restrict__ P, const double* __restrict__ W,
+                            const double* __restrict__ vao, const double* __restrict__ vdp,
+                            const double* __restrict__ vqp, double* dz) {
+  zeta_grad_dev(m, p, se, P, W, vao, vdp, vqp, dz,
+                blockIdx.x * (long long)blockDim.x + threadIdx.x);
+}
 
 void launch_zeta_grad(const DevMol& m, const Gfn2Scalars& p, const double* se, const double* P,
                       const double* W, const double* vao, const double* vdp, const double* vqp,
@@ -599,6 +609,22 @@ __global__ void kb_h0_onsite_dcn(const MolPtrs* __restrict__ mp, const int* __re
   const MolPtrs& q = mp[list[blockIdx.z]];
   h0_onsite_dcn_dev(q.m, q.P, q.dEdcn);
 }
+// W is in F after the gradient phase; zgrad was zeroed by kb_param_grad
+__global__ void kb_zeta_grad(const MolPtrs* __restrict__ mp, const int* __restrict__ list,
+                             Gfn2Scalars p) {
+  const MolPtrs& q = mp[list[blockIdx.z]];
+  if (!q.param_grad) return;
+  p.h0_cutoff = q.h0_cutoff;
+  zeta_grad_dev(q.m, p, q.se, q.P, q.F, q.vao, q.vdp, q.vqp, q.zgrad,
+                blockIdx.x * (long long)blockDim.x + threadIdx.x);
+}
+void launch_zeta_grad_b(const BatchLaunch& b, const Gfn2Scalars& p) {
+  if (!b.count) return;
+  const long long np = (long long)b.nsh_max * b.nsh_max;
+  ++g_kernel_launches;
+  kb_zeta_grad<<<dim3((unsigned)((np + 127) / 128), 1, b.count), 128, 0, b.s>>>(b.mp, b.list, p);
+}
+
 void launch_h0_gradient_b(const BatchLaunch& b, const Gfn2Scalars& p) {
   if (!b.count) return;
   const long long npair = (long long)b.nsh_max * (b.nsh_max + 1) / 2;

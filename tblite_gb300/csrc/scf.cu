@@ -1106,18 +1106,29 @@ void launch_wbo(const DevMol& m, const double* PS, double* wbo, double scale, cu
 //   third order     E3 = sum_s Gamma_s q_s^3 / 3
 // one thread per shell
 // ------------------------------------------------------------------------------------
-__global__ void k_param_grad(DevMol m, Gfn2Scalars p, const double* __restrict__ P,
-                             const double* __restrict__ Hp, const double* __restrict__ qsh,
-                             double* out /* [3][nsh]: dse, dhub, dgam3 */) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= m.nsh) return;
+// Hp: H0 built with unit self energies; or nullptr, and then the same elements come from H0
+// and the self energies se, Hp = H0 / ((e_s + e_t) / 2) (H0 is linear in the pair's mean self
+// energy, which is never zero).  cn != nullptr: also out[3 nsh + s] = dE/dkcn_s = -CN_A dE/de_s
+__device__ __forceinline__ void param_grad_dev(const DevMol& m, const double* __restrict__ P,
+                                               const double* __restrict__ Hp,
+                                               const double* __restrict__ H,
+                                               const double* __restrict__ se,
+                                               const double* __restrict__ cn,
+                                               const double* __restrict__ qsh, double* out,
+                                               double* zgrad, int s) {
   const int n = m.nao, nsh = m.nsh;
   const int o = m.sh_ao[s], no = 2 * m.sh_l[s] + 1;
   double tr = 0.0;
   for (int mu = o; mu < o + no; ++mu) {
     const double* pr = P + (size_t)mu * n;
-    const double* hr = Hp + (size_t)mu * n;
-    for (int nu = 0; nu < n; ++nu) tr += pr[nu] * hr[nu];
+    if (Hp) {
+      const double* hr = Hp + (size_t)mu * n;
+      for (int nu = 0; nu < n; ++nu) tr += pr[nu] * hr[nu];
+    } else {
+      const double* hr = H + (size_t)mu * n;
+      const double es = se[s];
+      for (int nu = 0; nu < n; ++nu) tr += pr[nu] * hr[nu] * (2.0 / (es + se[m.ao_sh[nu]]));
+    }
   }
   const double qs = qsh[s], es = m.sh_hub[s];
   const int ia = m.sh_atom[s];
@@ -1139,6 +1150,15 @@ __global__ void k_param_grad(DevMol m, Gfn2Scalars p, const double* __restrict__
   out[s] = tr;
   out[nsh + s] = dh;
   out[2 * nsh + s] = qs * qs * qs / 3.0;
+  if (cn) out[3 * nsh + s] = -cn[ia] * tr;
+  if (zgrad) zgrad[s] = 0.0;  // accumulated by the Slater-exponent kernel that follows
+}
+__global__ void k_param_grad(DevMol m, Gfn2Scalars p, const double* __restrict__ P,
+                             const double* __restrict__ Hp, const double* __restrict__ qsh,
+                             double* out /* [3][nsh]: dse, dhub, dgam3 */) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= m.nsh) return;
+  param_grad_dev(m, P, Hp, nullptr, nullptr, nullptr, qsh, out, nullptr, s);
   (void)p;
 }
 void launch_param_grad(const DevMol& m, const Gfn2Scalars& p, const double* P, const double* Hp,
@@ -1155,7 +1175,19 @@ void launch_param_grad(const DevMol& m, const Gfn2Scalars& p, const double* P, c
 #define BMOL const MolPtrs& q = mp[list[blockIdx.z]]
 #define BARGS const MolPtrs* __restrict__ mp, const int* __restrict__ list
 
-static inline dim3 bgrid(unsigned x, const BatchLaunch& b, unsigned y = 1) {
+__global__ void kb_param_grad(BARGS) {
+  BMOL;
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (!q.param_grad || s >= q.m.nsh) return;
+  param_grad_dev(q.m, q.P, nullptr, q.H, q.se, q.cn, q.qsh_o, q.pgrad, q.zgrad, s);
+}
+static inline dim3 bgrid(unsigned x, const BatchLaunch& b, unsigned y = 1);
+void launch_param_grad_b(const BatchLaunch& b) {
+  if (!b.count) return;
+  ++g_kernel_launches;
+  kb_param_grad<<<bgrid((b.nsh_max + 127) / 128, b), 128, 0, b.s>>>(b.mp, b.list);
+}
+static inline dim3 bgrid(unsigned x, const BatchLaunch& b, unsigned y) {
   return dim3(x > 0 ? x : 1, y, (unsigned)b.count);
 }
 

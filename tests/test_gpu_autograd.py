@@ -80,3 +80,34 @@ def test_parameter_gradient_matches_fd(name):
     from tblite_gb300.autograd import set_shell_parameters
 
     set_shell_parameters(calc, **base)
+
+
+def test_batched_bridge_matches_one_molecule_path():
+    """gfn2_energies_batch (one tblite_gb300_batch_singlepoint call, parameter gradient on the
+    batched path) against gfn2_energy per molecule: energies, forces and all five parameter
+    gradients at the parity bar."""
+    from tblite_gb300 import workloads
+    from tblite_gb300.autograd import (PARAMETERS, gfn2_energies_batch, gfn2_energy,
+                                       shell_parameters)
+    from tblite_gb300.interface import Calculator
+
+    mols = workloads.alkane_batch(6, seed=7, nmin=3, nmax=14)
+    single, batch_calcs = [], []
+    for z, x in mols:
+        calc = Calculator("GFN2-xTB", z, x)
+        prm = {k: torch.tensor(v, requires_grad=True) for k, v in shell_parameters(calc).items()}
+        pos = torch.tensor(x, requires_grad=True)
+        e = gfn2_energy(calc, pos, **prm)
+        e.backward()
+        single.append((float(e), pos.grad.numpy(), {k: prm[k].grad.numpy() for k in PARAMETERS}))
+        batch_calcs.append(Calculator("GFN2-xTB", z, x))
+    pos = [torch.tensor(x, requires_grad=True) for _, x in mols]
+    prm = [{k: torch.tensor(v, requires_grad=True) for k, v in shell_parameters(c).items()}
+           for c in batch_calcs]
+    e = gfn2_energies_batch(batch_calcs, pos, prm)
+    e.sum().backward()
+    for i, (e1, g1, p1) in enumerate(single):
+        assert abs(float(e[i]) - e1) < 1e-7
+        assert np.max(np.abs(pos[i].grad.numpy() - g1)) < 1e-6
+        for k in PARAMETERS:
+            assert np.max(np.abs(prm[i][k].grad.numpy() - p1[k])) < 1e-6, k
