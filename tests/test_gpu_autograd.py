@@ -99,7 +99,7 @@ def test_batched_bridge_matches_one_molecule_path():
         pos = torch.tensor(x, requires_grad=True)
         e = gfn2_energy(calc, pos, **prm)
         e.backward()
-        single.append((float(e), pos.grad.numpy(), {k: prm[k].grad.numpy() for k in PARAMETERS}))
+        single.append((e.item(), pos.grad.numpy(), {k: prm[k].grad.numpy() for k in PARAMETERS}))
         batch_calcs.append(Calculator("GFN2-xTB", z, x))
     pos = [torch.tensor(x, requires_grad=True) for _, x in mols]
     prm = [{k: torch.tensor(v, requires_grad=True) for k, v in shell_parameters(c).items()}
@@ -107,7 +107,7 @@ def test_batched_bridge_matches_one_molecule_path():
     e = gfn2_energies_batch(batch_calcs, pos, prm)
     e.sum().backward()
     for i, (e1, g1, p1) in enumerate(single):
-        assert abs(float(e[i]) - e1) < 1e-7
+        assert abs(e[i].item() - e1) < 1e-7
         assert np.max(np.abs(pos[i].grad.numpy() - g1)) < 1e-6
         for k in PARAMETERS:
             assert np.max(np.abs(prm[i][k].grad.numpy() - p1[k])) < 1e-6, k
