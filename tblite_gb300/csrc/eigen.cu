@@ -828,20 +828,23 @@ __global__ void k_clusters(int n, int k0, int k, const double* __restrict__ d,
 // four warp reductions are independent.  T (LAPACK dlarft, forward, column-wise) is formed
 // once per block by k_bt_tmat.  One warp per column; the block's reflectors are staged in
 // shared memory (zero above each reflector's first row), the column too when it fits.
-constexpr int BT_WARPS = 4;
+// warps (columns) per block: 4 on the one-molecule path (more blocks for small k), 8 in the batch
+// (the reflectors staged per block serve twice the columns; measured 2131 -> 2104 ms on the
+// 4096-molecule ensemble, while 8 slowed the 192-orbital single point)
+constexpr int BT_WARPS = 4, BT_WARPS_B = 8;
 constexpr int BT_CHUNK_MAX = 16;  // reflectors staged per round (a multiple of 4)
 constexpr size_t BT_SMEM_MAX = 200 * 1024;
 // the columns live in shared memory too when at least one block of reflectors fits beside them
-__host__ __device__ static inline bool bt_ysmem(int n) {
-  return (int)(BT_SMEM_MAX / (sizeof(double) * (size_t)n)) - BT_WARPS >= 4;
+__host__ __device__ static inline bool bt_ysmem(int n, int w = BT_WARPS) {
+  return (int)(BT_SMEM_MAX / (sizeof(double) * (size_t)n)) - w >= 4;
 }
-__host__ __device__ static inline int bt_chunk(int n) {
-  int c = (int)(BT_SMEM_MAX / (sizeof(double) * (size_t)n)) - (bt_ysmem(n) ? BT_WARPS : 0);
+__host__ __device__ static inline int bt_chunk(int n, int w = BT_WARPS) {
+  int c = (int)(BT_SMEM_MAX / (sizeof(double) * (size_t)n)) - (bt_ysmem(n, w) ? w : 0);
   c = c < 4 ? 4 : (c > BT_CHUNK_MAX ? BT_CHUNK_MAX : c);
   return c & ~3;
 }
-__host__ __device__ static inline size_t bt_smem(int n) {
-  return sizeof(double) * (size_t)n * (bt_chunk(n) + (bt_ysmem(n) ? BT_WARPS : 0));
+__host__ __device__ static inline size_t bt_smem(int n, int w = BT_WARPS) {
+  return sizeof(double) * (size_t)n * (bt_chunk(n, w) + (bt_ysmem(n, w) ? w : 0));
 }
 // reflector j: v[j+1] = 1, v[r] = A[r + j n] for r > j+1; j > n-2 does not exist (zero)
 __device__ __forceinline__ double bt_v(int n, const double* __restrict__ A, int j, int r) {
@@ -898,12 +901,13 @@ __global__ void k_bt_tmat(int n, const double* __restrict__ A, const double* __r
   bt_tmat_dev(n, A, tau, Tm, g, threadIdx.x & 31);
 }
 
+template <int W>
 __device__ __forceinline__ void backtransform_dev(int n, int k, int chunk, bool ysmem,
                                                   const double* __restrict__ A,
                                                   const double* __restrict__ Tm, double* Y) {
-  extern __shared__ double smem[];  // [chunk][n] reflectors, then [BT_WARPS][n] columns
+  extern __shared__ double smem[];  // [chunk][n] reflectors, then [W][n] columns
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int col = blockIdx.x * BT_WARPS + wid;
+  const int col = blockIdx.x * W + wid;
   double* yg = col < k ? Y + (size_t)col * n : nullptr;
   double* y = !yg ? nullptr : (ysmem ? smem + (size_t)chunk * n + (size_t)wid * n : yg);
   if (y && ysmem)
@@ -955,7 +959,7 @@ __global__ void __launch_bounds__(BT_WARPS * 32) k_backtransform(int n, int k, i
                                                                  const double* __restrict__ A,
                                                                  const double* __restrict__ Tm,
                                                                  double* Y) {
-  backtransform_dev(n, k, chunk, ysmem, A, Tm, Y);
+  backtransform_dev<BT_WARPS>(n, k, chunk, ysmem, A, Tm, Y);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -1427,11 +1431,12 @@ __global__ void kb_clusters(BARGS) {
   BMOL;
   clusters_dev(q.m.nao, 0, *q.icount, q.ed, q.ee, q.emo, q.escal, 1e-5, q.Y);
 }
-__global__ void __launch_bounds__(BT_WARPS * 32) kb_backtransform(BARGS) {
+__global__ void __launch_bounds__(BT_WARPS_B * 32) kb_backtransform(BARGS) {
   BMOL;
   const int n = q.m.nao, k = *q.icount;
-  if ((int)blockIdx.x * BT_WARPS >= k) return;  // no column of this molecule here
-  backtransform_dev(n, k, bt_chunk(n), bt_ysmem(n), q.A, q.lu, q.Y);
+  if ((int)blockIdx.x * BT_WARPS_B >= k) return;  // no column of this molecule here
+  backtransform_dev<BT_WARPS_B>(n, k, bt_chunk(n, BT_WARPS_B), bt_ysmem(n, BT_WARPS_B), q.A, q.lu,
+                                q.Y);
 }
 __global__ void kb_bt_tmat(BARGS) {
   BMOL;
@@ -1482,7 +1487,7 @@ static void batch_attributes() {
                           (int)TRIDIAG_SMEM_MAX),
      "smem attr batch tridiag small");
   ck(cudaFuncSetAttribute(kb_backtransform, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                          (int)BT_SMEM_MAX + (int)(BT_WARPS * sizeof(double) * 64)),
+                          (int)BT_SMEM_MAX + (int)(BT_WARPS_B * sizeof(double) * 64)),
      "smem attr batch backtransform");
   done = true;
 }
@@ -1550,8 +1555,8 @@ void eigen_vectors_b(const BatchLaunch& b) {
   ++g_kernel_launches;
   kb_bt_tmat<<<dim3((((b.nao_max - 2) / 4 + 1) * 32 + 127) / 128, 1, b.count), 128, 0, b.s>>>(
       b.mp, b.list);
-  kb_backtransform<<<dim3((b.nao_max + BT_WARPS - 1) / BT_WARPS, 1, b.count), BT_WARPS * 32,
-                     bt_smem(b.nao_max), b.s>>>(b.mp, b.list);
+  kb_backtransform<<<dim3((b.nao_max + BT_WARPS_B - 1) / BT_WARPS_B, 1, b.count),
+                     BT_WARPS_B * 32, bt_smem(b.nao_max, BT_WARPS_B), b.s>>>(b.mp, b.list);
   prof_kend(KS_BACKTRANSFORM, tb_, b.s);
   gemm_b(b, GS_XY);
 }
