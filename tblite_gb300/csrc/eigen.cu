@@ -1548,7 +1548,9 @@ void eigen_vectors_b(const BatchLaunch& b) {
   batch_attributes();
   g_kernel_launches += 3;
   const int ti = prof_kbegin(b.s);
-  kb_invit<<<dim3((b.nao_max + 15) / 16, 1, b.count), 16, 0, b.s>>>(b.mp, b.list);
+  // one thread per vector; full warps (the one-molecule path keeps 16-thread blocks so that a
+  // single molecule's vectors spread over more SMs)
+  kb_invit<<<dim3((b.nao_max + 31) / 32, 1, b.count), 32, 0, b.s>>>(b.mp, b.list);
   prof_kend(KS_INVIT, ti, b.s);
   kb_clusters<<<dim3(b.nao_max, 1, b.count), 256, 0, b.s>>>(b.mp, b.list);
   const int tb_ = prof_kbegin(b.s);
