@@ -1380,11 +1380,10 @@ __global__ void __launch_bounds__(256) kb_tridiag_small(BARGS) {
       // w = p + K v once per row, then two FMAs per element: A -= v w^T + w v^T
       for (int r = r0 + tid; r < n; r += blockDim.x) sp[r] = fma(K, sv[r], sp[r]);
       __syncthreads();
-      const int m = n - r0;
-      for (int e2 = tid; e2 < m * m; e2 += blockDim.x) {
-        const int c = r0 + e2 / m, r = r0 + e2 % m;
-        double* el = a + (size_t)c * n + r;
-        *el = fma(-sv[r], sp[c], fma(-sp[r], sv[c], *el));
+      for (int c = r0 + wid; c < n; c += nw) {  // warp per column, v_c and w_c in registers
+        double* col = a + (size_t)c * n;
+        const double vc = sv[c], wc = sp[c];
+        for (int r = r0 + lane; r < n; r += 32) col[r] = fma(-sv[r], wc, fma(-sp[r], vc, col[r]));
       }
     }
     __syncthreads();
