@@ -80,6 +80,14 @@ def test_alkane():
     _compare("GFN2-xTB", z, x)
 
 
+def test_c100h202_against_eigen():
+    """602 orbitals: products over several 128 x 64 tiles and 160-wide k windows."""
+    from tblite_gb300 import workloads
+
+    z, x = workloads.config("c100h202")
+    _compare("GFN2-xTB", z, x, acc=1.0)
+
+
 def test_gfn1_water_cluster():
     from tblite_gb300 import workloads
 
