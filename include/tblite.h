@@ -91,6 +91,14 @@ typedef struct _tblite_result* tblite_result;
 TBLITE_API_ENTRY tblite_result TBLITE_API_CALL tblite_new_result(void);
 TBLITE_API_ENTRY tblite_result TBLITE_API_CALL tblite_copy_result(tblite_result res);
 TBLITE_API_ENTRY void TBLITE_API_CALL tblite_delete_result(tblite_result* res);
+/* Save / load the wavefunction of a result (NumPy .npz restart file with the reference's
+ * member names; replaces include/tblite/result.h:253-265) */
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_save_result_wavefunction(tblite_error error,
+                                                                      tblite_result res,
+                                                                      const char* filename);
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_load_result_wavefunction(tblite_error error,
+                                                                      tblite_result res,
+                                                                      const char* filename);
 TBLITE_API_ENTRY void TBLITE_API_CALL tblite_get_result_number_of_atoms(tblite_error error,
                                                                        tblite_result res, int* nat);
 TBLITE_API_ENTRY void TBLITE_API_CALL tblite_get_result_number_of_shells(tblite_error error,

@@ -193,6 +193,9 @@ struct _tblite_result {
   std::vector<double> dse, dkcn, dhub, dgam3, dzeta;
   // spectral projection: HOMO, LUMO, bound on their errors (empty after diagonalisation)
   std::vector<double> gap;
+  // wavefunction data of the restart file: reference occupations, electrons per spin, kT
+  std::vector<double> n0at, n0sh;
+  double nel[2] = {0.0, 0.0}, kt = 0.0;
   double dipole[3] = {0, 0, 0}, quadrupole[6] = {0, 0, 0, 0, 0, 0};
 };
 

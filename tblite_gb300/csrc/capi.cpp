@@ -22,6 +22,7 @@
 #include "params_solv.inc"
 
 #include "api_internal.h"
+#include "npz.h"
 
 using namespace tb;
 
@@ -1109,6 +1110,12 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
     res->sigma[k] = acc;
   }
   res->has_wfn = true;
+  res->n0sh.assign(c->sh_refocc.begin(), c->sh_refocc.begin() + nsh);
+  res->n0at.assign(nat, 0.0);
+  for (int i = 0; i < nsh; ++i) res->n0at[c->sh_atom[i]] += c->sh_refocc[i];
+  res->nel[0] = nalp;
+  res->nel[1] = nbet;
+  res->kt = c->etemp;
   if (open_shell) {  // updown_to_magnet (wavefunction/spin.f90:130-140)
     const size_t na2 = (size_t)nat * nat;
     for (size_t t = 0; t < na2; ++t) {
@@ -1646,6 +1653,105 @@ void tblite_update_structure_uhf(tblite_error error, tblite_structure m, const i
 
 tblite_result tblite_new_result(void) { return new _tblite_result(); }
 tblite_result tblite_copy_result(tblite_result r) { return r ? new _tblite_result(*r) : nullptr; }
+
+// wavefunction restart files (api/result.f90:597-642, wavefunction/restart.f90): a NumPy .npz
+// archive with the members tblite0_{kt, nel, n0at, n0sh, density, coeff, emo, focc, qat, qsh,
+// dpat, qpat}, Fortran order, one spin channel (the closed-shell / total representation)
+void tblite_save_result_wavefunction(tblite_error error, tblite_result res, const char* filename) {
+  if (!res) {
+    set_err(error, "Result container is missing");
+    return;
+  }
+  const size_t nat = res->nat, nsh = res->nsh, nao = res->nao;
+  if (!res->has_wfn || res->P.size() != nao * nao || res->C.size() != nao * nao ||
+      res->emo.size() < nao || res->focc.size() < nao || res->n0at.size() != nat) {
+    set_err(error, "Result does not contain wavefunction");
+    return;
+  }
+  auto arr = [](std::vector<size_t> shape, const double* p) {
+    tb::NpyArray a;
+    size_t count = 1;
+    for (size_t d : shape) count *= d;
+    a.shape = std::move(shape);
+    a.data.assign(p, p + count);
+    return a;
+  };
+  const std::string pre = "tblite0_";
+  std::vector<std::pair<std::string, tb::NpyArray>> out = {
+      {pre + "kt", arr({1}, &res->kt)},
+      {pre + "nel", arr({2}, res->nel)},
+      {pre + "n0at", arr({nat}, res->n0at.data())},
+      {pre + "n0sh", arr({nsh}, res->n0sh.data())},
+      {pre + "density", arr({nao, nao, 1}, res->P.data())},
+      {pre + "coeff", arr({nao, nao, 1}, res->C.data())},
+      {pre + "emo", arr({nao, 1}, res->emo.data())},
+      {pre + "focc", arr({nao, 1}, res->focc.data())},
+      {pre + "qat", arr({nat, 1}, res->qat.data())},
+      {pre + "qsh", arr({nsh, 1}, res->qsh.data())},
+      {pre + "dpat", arr({3, nat, 1}, res->dpat.data())},
+      {pre + "qpat", arr({6, nat, 1}, res->qpat.data())}};
+  try {
+    tb::npz_write(filename ? filename : "", out);
+  } catch (const std::exception& e) {
+    set_err(error, e.what());
+  }
+}
+
+void tblite_load_result_wavefunction(tblite_error error, tblite_result res, const char* filename) {
+  if (!res) {
+    set_err(error, "Result container is missing");
+    return;
+  }
+  const std::string file = filename ? filename : "";
+  try {
+    const auto m = tb::npz_read(file);
+    auto get = [&](const char* key) -> const tb::NpyArray& {
+      const auto it = m.find(std::string("tblite0_") + key);
+      if (it == m.end()) throw std::runtime_error(std::string("'") + file + "' has no " + key);
+      return it->second;
+    };
+    const auto &n0at = get("n0at"), &n0sh = get("n0sh"), &emo = get("emo"), &qat = get("qat"),
+               &qsh = get("qsh"), &dpat = get("dpat"), &qpat = get("qpat"), &den = get("density"),
+               &coeff = get("coeff"), &focc = get("focc"), &nel = get("nel"), &kt = get("kt");
+    auto dim = [](const tb::NpyArray& a, size_t k) { return k < a.shape.size() ? a.shape[k] : 1; };
+    const size_t nat = n0at.data.size(), nsh = n0sh.data.size(), nao = dim(emo, 0);
+    if (dim(qat, 0) != nat || dim(dpat, 1) != nat || dim(qpat, 1) != nat || dim(dpat, 0) != 3 ||
+        dim(qpat, 0) != 6)
+      throw std::runtime_error("Dimension mismatch in '" + file + "' for number of atoms");
+    if (dim(qsh, 0) != nsh)
+      throw std::runtime_error("Dimension mismatch in '" + file + "' for number of shells");
+    if (dim(den, 0) != nao || dim(den, 1) != nao || dim(coeff, 0) != nao ||
+        dim(coeff, 1) != nao || dim(focc, 0) != nao)
+      throw std::runtime_error("Dimension mismatch in '" + file + "' for number of orbitals");
+    if (nel.data.size() < 2 || kt.data.empty())
+      throw std::runtime_error("Dimension mismatch in '" + file + "' for number of spins");
+    // first spin channel: the total (closed shell) or charge part of the restart data
+    auto first = [](const tb::NpyArray& a, size_t count) {
+      return std::vector<double>(a.data.begin(), a.data.begin() + count);
+    };
+    res->nat = (int)nat;
+    res->nsh = (int)nsh;
+    res->nao = (int)nao;
+    res->n0at = n0at.data;
+    res->n0sh = n0sh.data;
+    res->nel[0] = nel.data[0];
+    res->nel[1] = nel.data[1];
+    res->kt = kt.data[0];
+    res->qat = first(qat, nat);
+    res->qsh = first(qsh, nsh);
+    res->dpat = first(dpat, 3 * nat);
+    res->qpat = first(qpat, 6 * nat);
+    res->P = first(den, nao * nao);
+    res->C = first(coeff, nao * nao);
+    res->emo = first(emo, nao);
+    res->focc = first(focc, nao);
+    res->has_wfn = true;
+    res->has_energy = false;
+    res->gap.clear();
+  } catch (const std::exception& e) {
+    set_err(error, e.what());
+  }
+}
 void tblite_delete_result(tblite_result* r) {
   if (r && *r) {
     delete *r;

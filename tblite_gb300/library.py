@@ -101,6 +101,8 @@ _SIGNATURES = {
         c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
     "tblite_gb300_set_pipelined_gemm": (None, [c_int]),
     "tblite_gb300_get_result_gap": (None, [c_void_p, c_void_p, _dbl_p]),
+    "tblite_save_result_wavefunction": (None, [c_void_p, c_void_p, c_char_p]),
+    "tblite_load_result_wavefunction": (None, [c_void_p, c_void_p, c_char_p]),
     "tblite_gb300_density_matrix_noalloc": (
         c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
     "tblite_gb300_density_matrix_noalloc_max": (c_int, []),
