@@ -694,6 +694,100 @@ def run_reference(args):
     }
 
 
+# --------------------------------------------------------------------------------------------
+# Fixed commands behind the kernel profiles (``--run``): one kind of engine call, no timing
+# contract, no JSON line.
+# --------------------------------------------------------------------------------------------
+def profile_run_ensemble(args):
+    """Batched energy + gradient calls over ``workloads.mixed_ensemble(molecules, seed=4)``;
+    prints the molecules, the fallbacks to the one-molecule path and the energy sum."""
+    from tblite_gb300 import _build, library, workloads
+    from tblite_gb300.interface import Calculator, batch_fallbacks, batch_singlepoint
+
+    _build.build()
+    if args.tridiag_ctas:
+        library.set_tridiag_ctas_per_sm(args.tridiag_ctas)
+    mols = workloads.mixed_ensemble(args.molecules, seed=4)
+    calcs = [Calculator(args.method, z, x) for z, x in mols]
+    for _ in range(args.calls):
+        res = batch_singlepoint(calcs)
+        print(f"molecules {len(res)} fallbacks {batch_fallbacks()} "
+              f"energy_sum {sum(r.get('energy') for r in res):.10f} "
+              f"device_ms {library.load().tblite_gb300_batch_last_device_ms():.1f}")
+    return 0
+
+
+def profile_run_gemm(args):
+    """Products of two seeded random FP64 n x n matrices (or X X for a symmetric X with
+    ``--sym``) through ``tblite_gb300_split_gemm``; prints the largest deviation from torch's
+    FP64 product relative to |A| |B| and the best call time."""
+    import ctypes
+
+    import torch
+
+    from tblite_gb300 import _build, library
+
+    _build.build()
+    lib = library.load()
+    n = args.n
+    g = torch.Generator(device="cuda").manual_seed(7)
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda", generator=g)
+    if args.sym:
+        a = 0.5 * (a + a.T)
+        b = a
+    else:
+        b = torch.randn(n, n, dtype=torch.float64, device="cuda", generator=g)
+    c = torch.empty(n, n, dtype=torch.float64, device="cuda")
+    at, bt = a.T.contiguous(), b.T.contiguous()  # column-major views for the C ABI
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(args.calls):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(torch.cuda.default_stream())
+        rc = lib.tblite_gb300_split_gemm(n, n, n, ctypes.c_void_p(at.data_ptr()),
+                                         ctypes.c_void_p(bt.data_ptr()),
+                                         ctypes.c_void_p(c.data_ptr()), 1 if args.sym else 0,
+                                         None)
+        e1.record(torch.cuda.default_stream())
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+        if rc != 0:
+            print(f"split gemm returned {rc}")
+            return 1
+    ref = a @ b
+    err = ((c.T - ref).abs() / (a.abs() @ b.abs())).max().item()
+    flop = (n * (n + 1) * n if args.sym else 2 * n ** 3)
+    best = min(times)
+    print(f"n {n} calls {args.calls} sym {args.sym} max relative deviation {err:.3e} best call "
+          f"{best:.3f} ms (split, allocation and product) {flop / best / 1e9:.2f} TFLOP/s "
+          "FP64-equivalent")
+    return 0
+
+
+def profile_run_single(args):
+    """Plain-path single points (energy + gradient) of ``workloads.config(geometry)``, with
+    ALPB(water) for ``--solvent`` and the density solver of ``--solver``."""
+    from tblite_gb300 import _build, library, workloads
+    from tblite_gb300.interface import Calculator
+
+    _build.build()
+    z, x = workloads.config(args.geometry)
+    calc = Calculator(args.method, z, x)
+    if args.solvent:
+        calc.add("alpb-solvation", "water")
+    calc.set("density-solver", args.solver)
+    library.set_profiling(True)
+    for _ in range(args.calls):
+        res = calc.singlepoint()
+        prof = library.get_profile()
+        print(f"atoms {len(z)} energy {res.get('energy'):.10f} iterations {prof['iterations']}")
+    return 0
+
+
+PROFILE_RUNS = {"ensemble": profile_run_ensemble, "gemm": profile_run_gemm,
+                "single": profile_run_single}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -702,7 +796,23 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="ensemble4096", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    prof = ap.add_argument_group("fixed profiling commands (--run)")
+    prof.add_argument("--run", choices=sorted(PROFILE_RUNS),
+                      help="run one kind of engine call for a profiler instead of the benchmark")
+    prof.add_argument("--molecules", type=int, default=512)
+    prof.add_argument("--method", default="GFN2-xTB", choices=["GFN2-xTB", "GFN1-xTB"])
+    prof.add_argument("--calls", type=int, default=1)
+    prof.add_argument("--tridiag-ctas", type=int, default=0,
+                      help="CTAs per SM of the batched tridiagonalisation (0: library default)")
+    prof.add_argument("--n", type=int, default=4096)
+    prof.add_argument("--sym", action="store_true")
+    prof.add_argument("--geometry", default="h2o1000")
+    prof.add_argument("--solvent", action="store_true")
+    prof.add_argument("--solver", default="diagonalization",
+                      choices=["diagonalization", "purification"])
     args = ap.parse_args()
+    if args.run:
+        raise SystemExit(PROFILE_RUNS[args.run](args))
     if args.impl == "reference":
         args.steps = min(args.steps, 3)
         line = run_reference(args)

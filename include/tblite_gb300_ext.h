@@ -161,8 +161,9 @@ unsigned long long tblite_gb300_get_split_gemm_flops(void);
  * Returns 0 on success, -1 for an invalid argument, -2 when n*k exceeds
  * tblite_gb300_density_matrix_noalloc_max() (nothing is launched), -3 for a CUDA error.
  * The workspace is one fixed device array per device inside the library (2^19 doubles,
- * 4 MiB).  The first call on a device looks up its address with that device current; make
- * that first call before starting any stream capture.  Calls that may overlap in time on
+ * 4 MiB).  Every call looks up its address with the caller's device current; the first
+ * call on a device can load the library's device code there, so make that first call before
+ * starting any stream capture.  P is exactly symmetric.  Calls that may overlap in time on
  * one device (other streams or threads) race on the array and must be serialised.
  */
 int tblite_gb300_density_matrix_noalloc(int n, int k, const double* C, const double* f, double* P,

@@ -1726,7 +1726,9 @@ void tblite_load_result_wavefunction(tblite_error error, tblite_result res, cons
     if (nel.data.size() < 2 || kt.data.empty())
       throw std::runtime_error("Dimension mismatch in '" + file + "' for number of spins");
     // first spin channel: the total (closed shell) or charge part of the restart data
-    auto first = [](const tb::NpyArray& a, size_t count) {
+    auto first = [&file](const tb::NpyArray& a, size_t count) {
+      if (a.data.size() < count)  // e.g. a trailing dimension of 0
+        throw std::runtime_error("Dimension mismatch in '" + file + "'");
       return std::vector<double>(a.data.begin(), a.data.begin() + count);
     };
     res->nat = (int)nat;

@@ -27,6 +27,9 @@ extern std::atomic<unsigned long long> g_split_flops;
 // wait for the stream with a blocking-sync event (the host thread sleeps instead of spinning)
 void stream_wait(cudaStream_t s);
 
+// streaming multiprocessors of the current device (cached per device)
+int device_sm_count();
+
 // per-kernel CUDA-event timing (only while profiling is enabled): prof_kbegin records an event
 // on s and returns a token (-1 when disabled); prof_kend closes it for the given slot
 enum { KS_TRIDIAG = 0, KS_MULTISECT, KS_INVIT, KS_BACKTRANSFORM, KS_GEMM, KS_FOCK, KS_MULLIKEN,
@@ -289,8 +292,9 @@ int purify_iterations(const Purifier*);
 // dense FP64 GEMM (column-major, BLAS semantics); kmode skips zero triangles
 // KM_SYM (or-ed with one of the others): the product is symmetric (M == N); only the tiles on
 // and below the diagonal are computed and each is also written to its mirror position
+// returns the status of its own launch (not an earlier error of another launch)
 enum { KM_NONE = 0, KM_LT_COLEND = 1, KM_LT_ROWEND = 2, KM_GE_ROWBEG = 3, KM_SYM = 8 };
-void gemm64(bool ta, bool tb, int M, int N, int K, double alpha, const double* A, int lda,
+cudaError_t gemm64(bool ta, bool tb, int M, int N, int K, double alpha, const double* A, int lda,
             const double* B, int ldb, double beta, double* C, int ldc, int kmode, cudaStream_t s);
 
 // eelec[i] = ts/nat + eband[i]

@@ -22,7 +22,8 @@ namespace tb {
 //   KM_LT_ROWEND   k <  row tile end      (op(A) lower triangular:  A(i,k) = 0 for k > i)
 //   KM_GE_ROWBEG   k >= row tile begin    (op(A) upper triangular:  A(i,k) = 0 for k < i)
 // KM_SYM marks a symmetric product (M == N, square tiles): tiles above the diagonal are not
-// computed, the others are written twice (C(i,j) and C(j,i)), so C is exactly symmetric.
+// computed, the others (and the lower half of a diagonal tile) are written twice (C(i,j) and
+// C(j,i)), so C is exactly symmetric.
 // ------------------------------------------------------------------------------------------
 template <int BM, int BN, int BK, int TM, int TN>
 __device__ __forceinline__ void gemm_dev(int M, int N, int K, double alpha, const double* __restrict__ A, int lda, bool ta,
@@ -85,10 +86,11 @@ __device__ __forceinline__ void gemm_dev(int M, int N, int K, double alpha, cons
     for (int y = 0; y < TN; ++y) {
       const int gj = j0 + tc * TN + y;
       if (gj >= N) continue;
+      if (sym && gi < gj) continue;  // diagonal tile: the upper entries are mirrors too
       double* c = C + gi + (size_t)gj * ldc;
       const double v = beta == 0.0 ? alpha * acc[x][y] : alpha * acc[x][y] + beta * *c;
       *c = v;
-      if (sym && i0 != j0) C[gj + (size_t)gi * ldc] = v;
+      if (sym && gi != gj) C[gj + (size_t)gi * ldc] = v;
     }
   }
 }
@@ -100,23 +102,41 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN))
   gemm_dev<BM, BN, BK, TM, TN>(M, N, K, alpha, A, lda, ta, B, ldb, tb, beta, C, ldc, kmode);
 }
 
-void gemm64(bool ta, bool tb, int M, int N, int K, double alpha, const double* A, int lda,
-            const double* B, int ldb, double beta, double* C, int ldc, int kmode, cudaStream_t s) {
-  if (M <= 0 || N <= 0) return;
+int device_sm_count() {
+  constexpr int kMaxDevices = 64;
+  static std::atomic<int> cache[kMaxDevices];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return 1;
+  int nsm = cache[dev].load(std::memory_order_relaxed);
+  if (nsm <= 0) {
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        nsm <= 0)
+      nsm = 1;
+    cache[dev].store(nsm, std::memory_order_relaxed);
+  }
+  return nsm;
+}
+
+cudaError_t gemm64(bool ta, bool tb, int M, int N, int K, double alpha, const double* A,
+                   int lda, const double* B, int ldb, double beta, double* C, int ldc, int kmode,
+                   cudaStream_t s) {
+  if (M <= 0 || N <= 0) return cudaSuccess;
   const int tk = prof_kbegin(s);
-  // small problems: 16x16 tiles keep enough CTAs in flight on 152 SMs
-  if ((long long)((M + 31) / 32) * ((N + 31) / 32) < 2 * 152) {
+  void* args[] = {&M, &N, &K, &alpha, (void*)&A, &lda, &ta, (void*)&B, &ldb, &tb, &beta, &C,
+                  &ldc, &kmode};
+  cudaError_t e;
+  // small problems: 16x16 tiles keep enough CTAs in flight (two 32x32 tiles per SM or fewer)
+  if ((long long)((M + 31) / 32) * ((N + 31) / 32) < 2LL * device_sm_count()) {
     dim3 grid((N + 15) / 16, (M + 15) / 16);
     ++g_kernel_launches;
-    k_gemm<16, 16, 16, 2, 2><<<grid, 64, 0, s>>>(M, N, K, alpha, A, lda, ta, B, ldb, tb, beta, C,
-                                                 ldc, kmode);
+    e = cudaLaunchKernel((const void*)k_gemm<16, 16, 16, 2, 2>, grid, dim3(64), args, 0, s);
   } else {
     dim3 grid((N + 31) / 32, (M + 31) / 32);
     ++g_kernel_launches;
-    k_gemm<32, 32, 16, 4, 4><<<grid, 64, 0, s>>>(M, N, K, alpha, A, lda, ta, B, ldb, tb, beta, C,
-                                                  ldc, kmode);
+    e = cudaLaunchKernel((const void*)k_gemm<32, 32, 16, 4, 4>, grid, dim3(64), args, 0, s);
   }
   prof_kend(KS_GEMM, tk, s);
+  return e;
 }
 
 // ------------------------------------------------------------------------------------------

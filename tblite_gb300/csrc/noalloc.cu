@@ -13,9 +13,9 @@
 // Limits and rules:
 //   * n * k must not exceed TBLITE_GB300_NOALLOC_DENSITY_MAX (2^19 doubles = 4 MiB); larger
 //     problems are rejected before anything is launched.
-//   * The first call on a device looks up the device address of the array with that device
-//     current (cudaGetSymbolAddress, which can load the module).  Make that first call before
-//     any stream capture is started on the device.
+//   * Every call looks up the device address of the array with the caller's device current
+//     (cudaGetSymbolAddress); the first call on a device can load the module there.  Make that
+//     first call before any stream capture is started on the device.
 //   * The array is shared by every call on a device: two calls that can run at the same time
 //     (different streams, or different host threads) race on it.  Serialise them.
 //   * Nothing in the array has to start at zero: the scale kernel writes all n*k entries that
@@ -33,24 +33,17 @@ namespace {
 
 __device__ __align__(256) double g_density_scratch[TBLITE_GB300_NOALLOC_DENSITY_MAX];
 
-constexpr int kMaxDevices = 64;
+// The device address of the fixed scratch array in the current device's context.  It is looked
+// up on every call (cheap once the module is loaded), so a context that was torn down and
+// created again (cudaDeviceReset) never sees a stale address.  The first lookup on a device can
+// load the module; the mutex keeps concurrent first calls from different host threads apart.
 std::mutex g_setup_mutex;
-double* g_scratch_ptr[kMaxDevices] = {nullptr};
-
-// one-time per device: the device address of the fixed scratch array
 cudaError_t scratch_for_current_device(double** out) {
-  int dev = 0;
-  cudaError_t rc = cudaGetDevice(&dev);
-  if (rc != cudaSuccess) return rc;
-  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
   std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_scratch_ptr[dev]) {
-    void* p = nullptr;
-    rc = cudaGetSymbolAddress(&p, g_density_scratch);
-    if (rc != cudaSuccess) return rc;
-    g_scratch_ptr[dev] = static_cast<double*>(p);
-  }
-  *out = g_scratch_ptr[dev];
+  void* p = nullptr;
+  const cudaError_t rc = cudaGetSymbolAddress(&p, g_density_scratch);
+  if (rc != cudaSuccess) return rc;
+  *out = static_cast<double*>(p);
   return cudaSuccess;
 }
 
@@ -77,17 +70,26 @@ extern "C" int tblite_gb300_density_matrix_noalloc(int n, int k, const double* C
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   double* work = nullptr;
   if (scratch_for_current_device(&work) != cudaSuccess) return -3;
+  // every launch is checked through its own return code, so an error left behind by an
+  // earlier, unrelated launch is not reported as this call's failure
   if (k == 0) {  // no occupied orbital: P = 0
-    const size_t nn = (size_t)n * n;
+    size_t nn = (size_t)n * n;
+    void* args[] = {&nn, &P};
     ++g_kernel_launches;
-    k_zero<<<(unsigned)((nn + 255) / 256), 256, 0, s>>>(nn, P);
+    if (cudaLaunchKernel((const void*)k_zero, dim3((unsigned)((nn + 255) / 256)), dim3(256), args,
+                         0, s) != cudaSuccess)
+      return -3;
   } else {
     const size_t tot = (size_t)n * k;
+    void* args[] = {&n, &k, (void*)&C, (void*)&f, &work};
     ++g_kernel_launches;
-    k_scale_cols_fixed<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(n, k, C, f, work);
-    gemm64(false, true, n, n, k, 1.0, work, n, C, n, 0.0, P, n, KM_SYM, s);
+    if (cudaLaunchKernel((const void*)k_scale_cols_fixed, dim3((unsigned)((tot + 255) / 256)),
+                         dim3(256), args, 0, s) != cudaSuccess)
+      return -3;
+    if (gemm64(false, true, n, n, k, 1.0, work, n, C, n, 0.0, P, n, KM_SYM, s) != cudaSuccess)
+      return -3;
   }
-  return cudaPeekAtLastError() == cudaSuccess ? 0 : -3;
+  return 0;
 }
 
 extern "C" int tblite_gb300_density_matrix_noalloc_max(void) {

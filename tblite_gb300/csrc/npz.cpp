@@ -96,17 +96,26 @@ NpyArray npy_parse(const unsigned char* p, size_t n, const std::string& name) {
   const size_t lp = hdr.find('(', sp), rp = hdr.find(')', sp);
   if (lp == std::string::npos || rp == std::string::npos) bad("bad shape");
   NpyArray a;
+  // every element must fit in the member: count stays <= n / 8, so the products below cannot
+  // overflow (each factor is checked against that bound before multiplying)
+  const size_t max_count = n / sizeof(double);
   size_t count = 1;
   for (size_t i = lp + 1; i < rp;) {
     while (i < rp && (hdr[i] == ' ' || hdr[i] == ',')) ++i;
     if (i >= rp) break;
+    if (hdr[i] < '0' || hdr[i] > '9') bad("bad shape");
     size_t v = 0;
-    while (i < rp && hdr[i] >= '0' && hdr[i] <= '9') v = 10 * v + (size_t)(hdr[i++] - '0');
+    while (i < rp && hdr[i] >= '0' && hdr[i] <= '9') {
+      v = 10 * v + (size_t)(hdr[i++] - '0');
+      if (v > max_count) bad("truncated data");
+    }
+    if (i < rp && hdr[i] != ' ' && hdr[i] != ',') bad("bad shape");
     a.shape.push_back(v);
+    if (v != 0 && count > max_count / v) bad("truncated data");
     count *= v;
   }
   const size_t data = off + hlen;
-  if (data + count * sizeof(double) > n) bad("truncated data");
+  if (data > n || count > (n - data) / sizeof(double)) bad("truncated data");
   std::vector<double> raw(count);
   std::memcpy(raw.data(), p + data, count * sizeof(double));
   if (fortran || a.shape.size() < 2) {
@@ -222,16 +231,18 @@ std::map<std::string, NpyArray> npz_read(const std::string& file) {
     const uint32_t csize = get32(&buf[cd + 20]);
     const uint32_t nlen = get16(&buf[cd + 28]), xlen = get16(&buf[cd + 30]),
                    clen = get16(&buf[cd + 32]);
-    const uint32_t loc = get32(&buf[cd + 42]);
-    if (cd + 46 + nlen > n) throw std::runtime_error("'" + file + "': damaged central directory");
+    const size_t loc = get32(&buf[cd + 42]);  // offsets widened before any addition
+    if (cd + 46 + (size_t)nlen > n)
+      throw std::runtime_error("'" + file + "': damaged central directory");
     std::string name(reinterpret_cast<const char*>(&buf[cd + 46]), nlen);
-    cd += 46 + nlen + xlen + clen;
+    cd += 46 + (size_t)nlen + (size_t)xlen + (size_t)clen;
     if (loc + 30 > n || get32(&buf[loc]) != 0x04034b50u)
       throw std::runtime_error("'" + file + "': damaged member '" + name + "'");
-    const size_t data = loc + 30 + get16(&buf[loc + 26]) + get16(&buf[loc + 28]);
+    const size_t data = loc + 30 + (size_t)get16(&buf[loc + 26]) + (size_t)get16(&buf[loc + 28]);
     if (method != 0)
       throw std::runtime_error("'" + file + "': member '" + name + "' is compressed");
-    if (data + csize > n) throw std::runtime_error("'" + file + "': truncated member '" + name + "'");
+    if (data > n || (size_t)csize > n - data)
+      throw std::runtime_error("'" + file + "': truncated member '" + name + "'");
     if (crc32_of(&buf[data], csize) != crc)
       throw std::runtime_error("'" + file + "': CRC mismatch in member '" + name + "'");
     if (name.size() > 4 && name.compare(name.size() - 4, 4, ".npy") == 0)

@@ -51,8 +51,8 @@ void ck(cudaError_t e, const char* what) {
 }
 
 int ew_blocks(size_t count) {
-  const size_t b = (count + 255) / 256;
-  return (int)(b < 152 * 16 ? b : 152 * 16);
+  const size_t b = (count + 255) / 256, cap = 16 * (size_t)device_sm_count();
+  return (int)(b < cap ? b : cap);
 }
 
 __device__ __forceinline__ double warp_sum(double v) {

@@ -20,7 +20,7 @@ which reproduces the compile-time folding of the reference bit for bit.
 
 Usage::
 
-    python tblite_gb300/data/extract_params.py [REFERENCE_ROOT]
+    python tblite_gb300/data/extract_params.py REFERENCE_ROOT
 
 It is only needed when regenerating the committed outputs.
 """
@@ -275,7 +275,9 @@ def write_inc_gfn1(params, path: Path):
 
 
 def main():
-    root = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+    if len(sys.argv) < 2:
+        raise SystemExit(f"usage: python {Path(__file__).name} <tblite source tree>")
+    root = Path(sys.argv[1])
     params, sto = extract(root)
     (HERE / "gfn2.json").write_text(json.dumps(params, indent=0))
     (HERE / "sto_ng.json").write_text(json.dumps(sto, indent=0))

@@ -23,7 +23,7 @@ Hartree 2625.4996394799 kJ/mol, 1 kcal = 4.184 kJ), the values of the reference'
 
 Usage::
 
-    python tblite_gb300/data/extract_solvation.py [REFERENCE_ROOT]
+    python tblite_gb300/data/extract_solvation.py REFERENCE_ROOT
 """
 from __future__ import annotations
 
@@ -121,7 +121,9 @@ def write_inc(d: dict, path: Path) -> None:
 
 
 if __name__ == "__main__":
-    root = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+    if len(sys.argv) < 2:
+        raise SystemExit(f"usage: python {Path(__file__).name} <tblite source tree>")
+    root = Path(sys.argv[1])
     d = extract(root)
     (HERE / "solvation_water.json").write_text(json.dumps(d, indent=1))
     write_inc(d, HERE.parent / "csrc" / "params_solv.inc")

@@ -13,7 +13,7 @@ energies pin the basis, the on-site integrals, the self energies, the
 shell-resolved Coulomb / third-order terms, Fermi smearing, the entropy term
 and the Broyden-mixed SCF of the oracle and of the CUDA engine.
 
-Usage: ``python tests/golden/make_golden.py [REFERENCE_ROOT]``
+Usage: ``python tests/golden/make_golden.py REFERENCE_ROOT``
 """
 from __future__ import annotations
 
@@ -30,7 +30,9 @@ def _array(block: str, name: str):
 
 
 def main():
-    root = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+    if len(sys.argv) < 2:
+        raise SystemExit(f"usage: python {Path(__file__).name} <tblite source tree>")
+    root = Path(sys.argv[1])
     for method, src in (("gfn2", "test/unit/test_gfn2_xtb.f90:61-272"),
                         ("gfn1", "test/unit/test_gfn1_xtb.f90:135-349")):
         extract(root, method, src)

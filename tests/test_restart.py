@@ -78,6 +78,57 @@ def test_refuses_bad_files(tmp_path):
         lib.tblite_delete_result(res)
 
 
+def _npy_bytes(header_shape, payload):
+    """A .npy 1.0 member with the given shape text in its header (not checked by numpy)."""
+    hdr = "{'descr': '<f8', 'fortran_order': True, 'shape': %s, }" % header_shape
+    hdr = hdr + " " * (63 - (10 + len(hdr)) % 64) + "\n"
+    return b"\x93NUMPY\x01\x00" + len(hdr).to_bytes(2, "little") + hdr.encode() + payload
+
+
+def _archive_with(tmp_path, name, member, data):
+    import zipfile
+
+    ref = _arrays()
+    path = tmp_path / name
+    with zipfile.ZipFile(path, "w", compression=zipfile.ZIP_STORED) as zf:
+        for k, v in ref.items():
+            if k == member:
+                zf.writestr(k + ".npy", data)
+            else:
+                import io
+
+                buf = io.BytesIO()
+                np.save(buf, v)
+                zf.writestr(k + ".npy", buf.getvalue())
+    return path
+
+
+def test_refuses_malformed_headers_and_offsets(tmp_path):
+    """Malformed shapes, empty trailing dimensions and wrapped offsets give an error, never a
+    hang or a read outside the file."""
+    lib = library.load()
+    res = c_void_p(lib.tblite_new_result())
+    payload = np.zeros(3).tobytes()
+    try:
+        for i, (shape, match) in enumerate([("(3L,)", "bad shape"), ("(3,x)", "bad shape"),
+                                            ("(99999999999999999999,)", "truncated"),
+                                            ("(4611686018427387904, 4)", "truncated"),
+                                            ("(3, 0)", "Dimension mismatch")]):
+            path = _archive_with(tmp_path, f"shape{i}.npz", "tblite0_qat",
+                                 _npy_bytes(shape, payload))
+            with pytest.raises(TBLiteRuntimeError, match=match):
+                _call("tblite_load_result_wavefunction", res, path)
+        np.savez(tmp_path / "good.npz", **_arrays())
+        raw = bytearray((tmp_path / "good.npz").read_bytes())
+        cd = raw.index(b"PK\x01\x02")
+        raw[cd + 42:cd + 46] = (0xFFFFFFF0).to_bytes(4, "little")  # local header offset
+        (tmp_path / "offset.npz").write_bytes(bytes(raw))
+        with pytest.raises(TBLiteRuntimeError, match="damaged member"):
+            _call("tblite_load_result_wavefunction", res, tmp_path / "offset.npz")
+    finally:
+        lib.tblite_delete_result(res)
+
+
 @pytest.mark.gpu
 def test_restart_from_file(tmp_path):
     from tblite_gb300 import _build, workloads

@@ -74,6 +74,7 @@ def test_matches_singlepoint_density_twice(lib):
             outs.append(p_dev.cpu().numpy())
         for p in outs:
             assert np.max(np.abs(p - pmat)) <= P_TOL
+            assert np.array_equal(p, p.T)  # mirrored, not two roundings of one sum
         assert np.array_equal(outs[0], outs[1])
     # independent check: P = C^T diag(f) C in the row-major view of the column-major buffer
     ref = (cmat.T * occ) @ cmat
