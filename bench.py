@@ -59,6 +59,42 @@ SOLVATED = {"h2o1000_alpb"}
 PURIFIED = {"h2o1000_alpb", "c200h402_sp2"}
 LARGE = {"h2o1000_alpb"}  # one oracle evaluation takes tens of minutes: bounded CPU samples
 SPLIT_SLICE_PRODUCTS = 36  # BF16 slice products per FP64 product in the split GEMM
+# comparison legs of the ensemble: one seeded random order of the ensemble's molecules; the
+# plain GPU leg takes its first 64, the CPU baseline its first 256 (with the accuracy check of
+# the GPU results), the reference arm consecutive slices of REF_PER_STEP per step
+SAMPLE_SEED = 4242
+PLAIN_SAMPLE, CPU_SAMPLE, REF_PER_STEP = 64, 256, 128
+BARS = {"energy_eh": 1e-7, "force_eh_per_bohr": 1e-6, "shell_charge_e": 1e-6}
+
+
+def ensemble_order(count):
+    """The seeded random order of the ensemble's molecules shared by the comparison legs."""
+    return [int(i) for i in np.random.default_rng(SAMPLE_SEED).permutation(count)]
+
+
+def _kinds(idx):
+    """water clusters / alkanes among ensemble indices (the generator alternates them)."""
+    w = sum(1 for i in idx if i % 2 == 0)
+    return {"water_clusters": w, "alkanes": len(idx) - w}
+
+
+def _accuracy(gpu_results, oracle_results, idx):
+    """max |dE|, |dF|, |dq_sh|, |dq_at| of GPU results against the oracle's on the same
+    molecules (ensemble indices idx)."""
+    de = df = dqs = dqa = 0.0
+    for i, ref in zip(idx, oracle_results):
+        r = gpu_results[i]
+        de = max(de, abs(r.get("energy") - ref["energy"]))
+        df = max(df, float(np.max(np.abs(r.get("gradient") - ref["gradient"]))))
+        dqs = max(dqs, float(np.max(np.abs(r.get("shell-charges") - ref["qsh"]))))
+        dqa = max(dqa, float(np.max(np.abs(r.get("charges") - ref["qat"]))))
+    out = {"molecules": len(idx), **_kinds(idx), "max_abs_dE_eh": float(f"{de:.3e}"),
+           "max_abs_dF_eh_per_bohr": float(f"{df:.3e}"), "max_abs_dq_shell_e": float(f"{dqs:.3e}"),
+           "max_abs_dq_atom_e": float(f"{dqa:.3e}"), "bars": BARS,
+           "within_bars": bool(de <= BARS["energy_eh"] and df <= BARS["force_eh_per_bohr"]
+                               and dqs <= BARS["shell_charge_e"]),
+           "against": "CPU oracle (FP64, LAPACK dsygvd), same molecules and settings"}
+    return out
 
 
 def _dist():
@@ -454,8 +490,9 @@ def run_batch(args):
                 "ms_per_launch": round(t_tri / c_tri, 4) if c_tri else None,
                 "whole_step": {"algorithmic_flops": flops,
                                "achieved_tflops": round(flops / (ms_step / 1000.0) / 1e12, 4)}}
-    # the plain one-molecule GPU path on an even sample of the same ensemble
-    sample = list(range(0, count, max(1, count // 64)))
+    # the plain one-molecule GPU path on the first molecules of the seeded random order
+    order = ensemble_order(count)
+    sample = order[:PLAIN_SAMPLE]
     for i in sample:
         calcs[i].singlepoint()  # per-calculator workspace
     torch.cuda.synchronize()
@@ -484,20 +521,26 @@ def run_batch(args):
             "fallback_reasons": leave1,
             "mean_scf_iterations": float(np.mean(iters1[iters1 > 0])) if np.any(iters1 > 0) else 0.0,
             "note": "same molecules and timing as the headline, GFN1-xTB Hamiltonian (D3 dispersion)"}
-    cpu = None
+    cpu = accuracy = None
     if not args.no_cpu:
-        from oracle import gfn2
+        # the CPU oracle on all host cores (a spawn pool: this process already uses the GPU),
+        # on the first CPU_SAMPLE molecules of the same order; its results also check the GPU
+        # results of those molecules from the last timed step (and of the GFN1 leg)
+        from oracle.parallel import OraclePool
 
-        gfn2.lib()
-        cs = sample[:16]
-        t0 = time.perf_counter()
-        for i in cs:
-            z, x = mols[i]
-            gfn2.singlepoint(gfn2.new_calc(gfn2.Molecule(np.asarray(z), np.asarray(x))), grad=True)
-        cpu = {"value": round(len(cs) / (time.perf_counter() - t0), 4), "unit": "evals/s",
-               "cores": os.cpu_count() or 1, "kind": "port",
-               "sample": f"{len(cs)} molecules evenly spaced through the ensemble, CPU oracle "
-                         "(C + numpy/LAPACK dsygvd), evals/s of the sample"}
+        cs = order[:CPU_SAMPLE]
+        with OraclePool() as pool:
+            refs, wall_cpu = pool.run([mols[i] for i in cs])
+            refs1, _ = pool.run([mols[i] for i in cs[:PLAIN_SAMPLE]], method="GFN1-xTB")
+            cores = pool.processes
+        cpu = {"value": round(len(cs) / wall_cpu, 4), "unit": "evals/s", "cores": cores,
+               "kind": "port",
+               "sample": f"{len(cs)} molecules of the ensemble in a seeded random order "
+                         f"(numpy default_rng({SAMPLE_SEED}).permutation; {_kinds(cs)}), CPU "
+                         f"oracle (C + numpy/LAPACK dsygvd), one molecule per process on "
+                         f"{cores} processes, evals/s of the sample"}
+        accuracy = _accuracy(res, refs, cs)
+        gfn1["accuracy"] = _accuracy(res1, refs1, cs[:PLAIN_SAMPLE])
     h2d = sum(m[1].size * 8 + m[0].size * 4 for m in mols)
     d2h = sum((1 + 5 * len(m[0]) + 9) * 8 for m in mols)
     return {
@@ -513,8 +556,10 @@ def run_batch(args):
         "e2e": {"value": round(e2e, 3), "unit": "evals/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "batched_vs_plain": {"plain_gpu_evals_per_s": round(plain, 3),
-                             "sample": f"{len(sample)} molecules evenly spaced, one per call",
+                             "sample": f"first {len(sample)} molecules of the seeded random "
+                                       f"order ({_kinds(sample)}), one per call",
                              "ratio_e2e": round(e2e / plain, 2)},
+        "accuracy": accuracy,
         "fallbacks_to_plain": fallbacks,
         "gfn1": gfn1,
         "gpu_launches": int(launches),
@@ -639,15 +684,48 @@ def run_reference(args):
 
     gfn2.lib()
     threads = os.cpu_count() or 1
-    if args.config in ENSEMBLE_SIZE:
-        # bounded sample per step: 16 molecules evenly spaced through the ensemble
-        count = ENSEMBLE_SIZE[args.config]
-        mols = workloads.mixed_ensemble(count, seed=4)
-        sample = [mols[i] for i in range(0, count, max(1, count // 16))][:16]
-        sample_desc = f"{len(sample)} molecules of the ensemble per step"
-    elif args.config == "autograd256":
-        sample = workloads.alkane_batch(256, seed=3, nmin=4, nmax=40)[:16]
-        sample_desc = "16 of the 256 alkanes per step (energy + gradient)"
+    if args.config in ENSEMBLE_SIZE or args.config == "autograd256":
+        # a bounded sample per step on all host cores (one molecule per process): for the
+        # ensemble, consecutive slices of the seeded random order the GPU arm's comparison legs
+        # use (warm-up steps first, then the timed steps); for the alkanes, all 256 per step
+        from oracle.parallel import OraclePool
+
+        if args.config == "autograd256":
+            mols = workloads.alkane_batch(256, seed=3, nmin=4, nmax=40)
+            slices = [list(range(len(mols)))] * (args.warmup + args.steps)
+            desc = "all 256 alkanes per step (energy + gradient)"
+        else:
+            count = ENSEMBLE_SIZE[args.config]
+            mols = workloads.mixed_ensemble(count, seed=4)
+            order = ensemble_order(count)
+            slices = [[order[(s * REF_PER_STEP + j) % count] for j in range(REF_PER_STEP)]
+                      for s in range(args.warmup + args.steps)]
+            timed = [i for sl in slices[args.warmup:] for i in sl]
+            desc = (f"{REF_PER_STEP} molecules of the ensemble per step, consecutive slices of "
+                    f"its seeded random order (numpy default_rng({SAMPLE_SEED}).permutation) after "
+                    f"{args.warmup} warm-up slices; timed: {len(set(timed))} distinct molecules, "
+                    f"{_kinds(timed)}")
+        with OraclePool() as pool:
+            for sl in slices[:args.warmup]:
+                pool.run([mols[i] for i in sl])
+            wall = 0.0
+            for sl in slices[args.warmup:]:
+                _, w = pool.run([mols[i] for i in sl])
+                wall += w
+            cores = pool.processes
+        evals = sum(len(sl) for sl in slices[args.warmup:])
+        value = evals / wall
+        return {
+            "impl": "reference", "metric": METRIC, "value": round(value, 5), "unit": "evals/s",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(1000 * wall / args.steps, 2), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOADS[args.config]},
+            "cpu_baseline": {"value": round(value, 5), "unit": "evals/s", "cores": cores,
+                             "kind": "port", "sample": desc + f", {cores} processes"},
+            "e2e": {"value": round(value, 5), "unit": "evals/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+        }
     elif args.config in LARGE:
         # one oracle evaluation takes tens of minutes: each step times one generalised
         # eigensolve, scaled by the oracle's own SCF iteration count for this system
@@ -814,7 +892,6 @@ def main():
     if args.run:
         raise SystemExit(PROFILE_RUNS[args.run](args))
     if args.impl == "reference":
-        args.steps = min(args.steps, 3)
         line = run_reference(args)
     else:
         if args.config == "autograd256":

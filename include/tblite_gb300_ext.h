@@ -78,6 +78,11 @@ int tblite_gb300_get_kernel_profile(double* kernel_ms, int* kernel_count, int ns
  * reference's column-major order), 0 when the result holds none (batched results) */
 int tblite_gb300_get_result_bond_order_channels(tblite_result res);
 
+/* Mulliken shell charges q_sh [nsh] of the last single point (the reference keeps them in its
+ * wavefunction, wavefunction/type.f90 qsh, and writes them to restart files, but its C API has
+ * no getter for them) */
+void tblite_gb300_get_result_shell_charges(tblite_error error, tblite_result res, double* qsh);
+
 /*
  * Shell parameters and the parameter gradient (no counterpart in the reference C API; the
  * reference fits parameters through its Fortran parameter records).  Arrays are per shell of

@@ -584,31 +584,29 @@ def post_processing(S, C, fa, fb, P, nalp, nbet, xyz, qat, dpat, qpat, ao2at):
     else:
         spin_p = [P]
         scale = 1.0
+    # atom blocks of P S (P S)^T summed with np.add.reduceat over the atom-sorted AOs
+    starts = np.flatnonzero(np.r_[True, ao2at[1:] != ao2at[:-1]])
     wbo = np.zeros((len(spin_p), nat, nat))
     for s_, Ps in enumerate(spin_p):
         PS_ = Ps @ S
         prod = PS_ * PS_.T
-        for a in range(nat):
-            for b in range(nat):
-                if a != b:
-                    wbo[s_, a, b] = scale * np.sum(prod[np.ix_(ao2at == a, ao2at == b)])
+        blk = np.add.reduceat(np.add.reduceat(prod, starts, axis=0), starts, axis=1)
+        wbo[s_] = scale * blk
+        np.fill_diagonal(wbo[s_], 0.0)
     if len(spin_p) == 2:
         wbo = np.stack([wbo[0] + wbo[1], wbo[0] - wbo[1]])
     parts["wbo"] = wbo
     parts["dipole"] = np.sum(xyz * qat[:, None] + dpat, axis=0)
-    quad = np.zeros(6)
-    for a in range(nat):
-        x, d = xyz[a], dpat[a]
-        v = x * qat[a]
-        c = np.zeros(6)
-        c[[0, 2, 5]] = x * (v + 2 * d)
-        c[1] = x[0] * (v[1] + d[1]) + d[0] * x[1]
-        c[3] = x[0] * (v[2] + d[2]) + d[0] * x[2]
-        c[4] = x[1] * (v[2] + d[2]) + d[1] * x[2]
-        tr = 0.5 * (c[0] + c[2] + c[5])
-        c = np.array([1.5 * c[0] - tr, 3 * c[1], 1.5 * c[2] - tr, 3 * c[3], 3 * c[4],
-                      1.5 * c[5] - tr])
-        quad += qpat[a] + c
+    v = xyz * qat[:, None]
+    c = np.zeros((nat, 6))
+    c[:, [0, 2, 5]] = xyz * (v + 2 * dpat)
+    c[:, 1] = xyz[:, 0] * (v[:, 1] + dpat[:, 1]) + dpat[:, 0] * xyz[:, 1]
+    c[:, 3] = xyz[:, 0] * (v[:, 2] + dpat[:, 2]) + dpat[:, 0] * xyz[:, 2]
+    c[:, 4] = xyz[:, 1] * (v[:, 2] + dpat[:, 2]) + dpat[:, 1] * xyz[:, 2]
+    tr = 0.5 * (c[:, 0] + c[:, 2] + c[:, 5])
+    cq = np.stack([1.5 * c[:, 0] - tr, 3 * c[:, 1], 1.5 * c[:, 2] - tr, 3 * c[:, 3], 3 * c[:, 4],
+                   1.5 * c[:, 5] - tr], axis=1)
+    quad = np.sum(qpat + cq, axis=0)
     parts["quadrupole"] = quad
     return parts
 

@@ -1807,6 +1807,11 @@ void tblite_get_result_charges(tblite_error error, tblite_result res, double* ch
   RESULT_GUARD(res->has_wfn, "Result does not contain atomic charges");
   std::copy(res->qat.begin(), res->qat.end(), charges);
 }
+void tblite_gb300_get_result_shell_charges(tblite_error error, tblite_result res, double* qsh) {
+  RESULT_GUARD(res->has_wfn && (int)res->qsh.size() == res->nsh,
+               "Result does not contain shell charges");
+  std::copy(res->qsh.begin(), res->qsh.end(), qsh);
+}
 void tblite_get_result_bond_orders(tblite_error error, tblite_result res, double* mbo) {
   RESULT_GUARD(!res->wbo.empty(), "Result does not contain bond orders");
   std::copy(res->wbo.begin(), res->wbo.end(), mbo);

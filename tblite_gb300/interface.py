@@ -78,6 +78,8 @@ class Result:
             return library.result_gap(self._res)
         if attribute == "norbitals":
             return library.result_int(self._res, "number_of_orbitals")
+        if attribute == "shell-charges":  # extension: Mulliken shell charges
+            return library.result_shell_charges(self._res)
         if attribute not in self._shapes:
             raise TBLiteValueError(f"Attribute '{attribute}' is not available in this container")
         dims = {"nat": None, "nao": None}

@@ -101,6 +101,7 @@ _SIGNATURES = {
         c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
     "tblite_gb300_set_pipelined_gemm": (None, [c_int]),
     "tblite_gb300_get_result_gap": (None, [c_void_p, c_void_p, _dbl_p]),
+    "tblite_gb300_get_result_shell_charges": (None, [c_void_p, c_void_p, _dbl_p]),
     "tblite_save_result_wavefunction": (None, [c_void_p, c_void_p, c_char_p]),
     "tblite_load_result_wavefunction": (None, [c_void_p, c_void_p, c_char_p]),
     "tblite_gb300_density_matrix_noalloc": (
@@ -289,6 +290,17 @@ def result_array(res, name, shape):
     err = _Error()
     out = np.zeros(shape, dtype=np.float64)
     getattr(lib, f"tblite_get_result_{name}")(err.h, res, _dp(out))
+    err.check()
+    return out
+
+
+def result_shell_charges(res):
+    """Mulliken shell charges of the last single point (extension getter)."""
+    lib = load()
+    nsh = result_int(res, "number_of_shells")
+    err = _Error()
+    out = np.zeros(nsh, dtype=np.float64)
+    lib.tblite_gb300_get_result_shell_charges(err.h, res, _dp(out))
     err.check()
     return out
 

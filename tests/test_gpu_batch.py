@@ -43,6 +43,7 @@ def _calc(z, x, method="GFN2-xTB", **settings):
 def _compare(rb, rp):
     assert abs(rb.get("energy") - rp.get("energy")) <= E_TOL
     assert np.max(np.abs(rb.get("charges") - rp.get("charges"))) <= Q_TOL
+    assert np.max(np.abs(rb.get("shell-charges") - rp.get("shell-charges"))) <= Q_TOL
     assert np.max(np.abs(rb.get("gradient") - rp.get("gradient"))) <= G_TOL
     assert np.max(np.abs(rb.get("virial") - rp.get("virial"))) <= V_TOL
     assert np.max(np.abs(rb.get("energies") - rp.get("energies"))) <= E_TOL
@@ -74,6 +75,7 @@ def test_batch_matches_oracle():
         assert abs(rb.get("energy") - ref.energy) <= E_TOL
         assert np.max(np.abs(rb.get("gradient") - ref.gradient)) <= G_TOL
         assert np.max(np.abs(rb.get("charges") - ref.qat)) <= Q_TOL
+        assert np.max(np.abs(rb.get("shell-charges") - ref.qsh)) <= Q_TOL
 
 
 def test_batch_per_molecule_settings_and_single_atom():

@@ -58,6 +58,7 @@ def _compare(z, x, acc, charge=0.0):
     ref = _oracle(z, x, charge=charge, acc=acc)
     assert abs(res.get("energy") - ref.energy) < E_TOL
     assert np.max(np.abs(res.get("charges") - ref.qat)) < Q_TOL
+    assert np.max(np.abs(res.get("shell-charges") - ref.qsh)) < Q_TOL
     assert np.max(np.abs(res.get("gradient") - ref.gradient)) < G_TOL
     assert np.max(np.abs(res.get("energies") - ref.energies)) < E_TOL
     assert np.max(np.abs(res.get("virial") - ref.sigma)) < 1e-5
