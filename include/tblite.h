@@ -22,9 +22,11 @@
 
 #ifdef __cplusplus
 #include <cstdbool>
+#include <cstdint>
 extern "C" {
-#else
+#elif !defined(TBLITE_CFFI) /* cffi knows bool and int64_t itself: no system headers */
 #include <stdbool.h>
+#include <stdint.h>
 #endif
 
 #ifdef TBLITE_CFFI /* cffi parses the preprocessed header: plain declarations */
@@ -56,6 +58,10 @@ TBLITE_API_ENTRY void TBLITE_API_CALL tblite_set_error(tblite_error error, char*
 /* ---- calculation context: include/tblite/context.h:32-100 ---- */
 typedef struct _tblite_context* tblite_context;
 typedef void (*tblite_logger_callback)(tblite_error, char*, int, void*);
+#ifdef TBLITE_CFFI /* the callback the reference's Python package defines (context.h:42-45) */
+extern "Python" void TBLITE_API_CALL logger_callback(tblite_error error, char* msg, int len,
+                                                     void* user_data);
+#endif
 TBLITE_API_ENTRY tblite_context TBLITE_API_CALL tblite_new_context(void);
 TBLITE_API_ENTRY void TBLITE_API_CALL tblite_delete_context(tblite_context* ctx);
 TBLITE_API_ENTRY int TBLITE_API_CALL tblite_check_context(tblite_context ctx);
@@ -148,6 +154,141 @@ TBLITE_API_ENTRY void TBLITE_API_CALL tblite_get_result_hamiltonian_matrix(tblit
                                                                           tblite_result res,
                                                                           double* hmat);
 
+/* ---- post-processing dictionary: include/tblite/double_dictionary.h:28-110, result.h:243-246
+ * A snapshot of a result's post-processing arrays ("bond-orders" [nat][nat][channels],
+ * "molecular-dipole" [3], "molecular-quadrupole" [6]); indices are 1-based as in the
+ * reference; arrays come out in Fortran order, unused trailing dimensions reported as 0. */
+typedef struct _tblite_double_dictionary* tblite_double_dictionary;
+TBLITE_API_ENTRY tblite_double_dictionary TBLITE_API_CALL
+tblite_get_post_processing_dict(tblite_error error, tblite_result res);
+TBLITE_API_ENTRY int TBLITE_API_CALL tblite_get_n_entries_dict(tblite_error error,
+                                                              tblite_double_dictionary dict);
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_get_array_entry_index(tblite_error error,
+                                                                  tblite_double_dictionary dict,
+                                                                  const int* index, double* array);
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_get_array_size_index(tblite_error error,
+                                                                 tblite_double_dictionary dict,
+                                                                 const int* index, int* dim1,
+                                                                 int* dim2, int* dim3);
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_get_array_entry_label(tblite_error error,
+                                                                  tblite_double_dictionary dict,
+                                                                  char* label, double* array);
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_get_array_size_label(tblite_error error,
+                                                                 tblite_double_dictionary dict,
+                                                                 char* label, int* dim1,
+                                                                 int* dim2, int* dim3);
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_get_label_entry_index(tblite_error error,
+                                                                  tblite_double_dictionary dict,
+                                                                  const int* index, char* label,
+                                                                  const int* buffersize);
+TBLITE_API_ENTRY void TBLITE_API_CALL
+tblite_delete_double_dictionary(tblite_double_dictionary* dict);
+
+/* ---- data tables: include/tblite/table.h:26-316 ----
+ * Nested key/value tables (booleans, 64-bit integers, doubles, strings, arrays of those,
+ * sub-tables), e.g. parameter sets in the reference's TOML layout.  Handles returned by
+ * add_table / get_table / get_array refer to the parent's entry and stay valid on their own;
+ * every handle is released with its delete call.  Array and key indices are 1-based. */
+typedef struct _tblite_table* tblite_table;
+typedef struct _tblite_array* tblite_array;
+enum tblite_table_value_type {
+  TBLITE_TABLE_VALUE_TYPE_NONE = 0,
+  TBLITE_TABLE_VALUE_TYPE_BOOL = 1,
+  TBLITE_TABLE_VALUE_TYPE_INT = 2,
+  TBLITE_TABLE_VALUE_TYPE_DOUBLE = 3,
+  TBLITE_TABLE_VALUE_TYPE_CHAR = 4,
+  TBLITE_TABLE_VALUE_TYPE_ARRAY = 5,
+  TBLITE_TABLE_VALUE_TYPE_TABLE = 6
+};
+TBLITE_API_ENTRY tblite_table TBLITE_API_CALL tblite_new_table(tblite_table* table);
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_delete_table(tblite_table* table);
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_table_set_double(tblite_error error,
+                                                             tblite_table table, char key[],
+                                                             double* value, int n);
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_table_set_int64_t(tblite_error error,
+                                                              tblite_table table, char key[],
+                                                              int64_t* value, int n);
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_table_set_bool(tblite_error error, tblite_table table,
+                                                           char key[], bool* value, int n);
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_table_set_char(tblite_error error, tblite_table table,
+                                                           char key[], char (*value)[], int n);
+TBLITE_API_ENTRY tblite_table TBLITE_API_CALL tblite_table_add_table(tblite_error error,
+                                                                    tblite_table table,
+                                                                    char key[]);
+TBLITE_API_ENTRY tblite_array TBLITE_API_CALL tblite_new_array(void);
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_delete_array(tblite_array* array);
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_array_push_back_double(tblite_error error,
+                                                                   tblite_array array,
+                                                                   double value);
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_array_push_back_int64_t(tblite_error error,
+                                                                    tblite_array array,
+                                                                    int64_t value);
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_array_push_back_bool(tblite_error error,
+                                                                 tblite_array array, bool value);
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_array_push_back_char(tblite_error error,
+                                                                 tblite_array array,
+                                                                 char value[]);
+TBLITE_API_ENTRY int TBLITE_API_CALL tblite_array_size(tblite_error error, tblite_array array);
+TBLITE_API_ENTRY int TBLITE_API_CALL tblite_array_get_type(tblite_error error, tblite_array array,
+                                                          int index);
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_array_get_double(tblite_error error,
+                                                             tblite_array array, int index,
+                                                             double* value);
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_array_get_int64_t(tblite_error error,
+                                                              tblite_array array, int index,
+                                                              int64_t* value);
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_array_get_bool(tblite_error error, tblite_array array,
+                                                           int index, bool* value);
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_array_get_char(tblite_error error, tblite_array array,
+                                                           int index, char value[], int n);
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_table_set_array(tblite_error error,
+                                                            tblite_table table, char key[],
+                                                            tblite_array array);
+TBLITE_API_ENTRY int TBLITE_API_CALL tblite_table_get_type(tblite_error error, tblite_table table,
+                                                          char key[]);
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_table_get_bool(tblite_error error, tblite_table table,
+                                                           char key[], bool* value);
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_table_get_int64_t(tblite_error error,
+                                                              tblite_table table, char key[],
+                                                              int64_t* value);
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_table_get_double(tblite_error error,
+                                                             tblite_table table, char key[],
+                                                             double* value);
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_table_get_char(tblite_error error, tblite_table table,
+                                                           char key[], char value[], int n);
+TBLITE_API_ENTRY tblite_table TBLITE_API_CALL tblite_table_get_table(tblite_error error,
+                                                                    tblite_table table,
+                                                                    char key[]);
+TBLITE_API_ENTRY tblite_array TBLITE_API_CALL tblite_table_get_array(tblite_error error,
+                                                                    tblite_table table,
+                                                                    char key[]);
+TBLITE_API_ENTRY int TBLITE_API_CALL tblite_table_get_n_keys(tblite_error error,
+                                                            tblite_table table);
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_table_get_key(tblite_error error, tblite_table table,
+                                                          int index, char key[], int n);
+/* write the table as TOML text to a file */
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_dump_table(tblite_error error, tblite_table table,
+                                                       char filename[]);
+
+/* ---- parametrisation records: include/tblite/param.h:26-80 ----
+ * The global constants and element records of an xTB method.  export_* fill a record with a
+ * built-in method's parameters; load / dump read and write it as a data table in the
+ * reference's TOML layout (levels and CN shifts in eV there); tblite_new_xtb_calculator makes
+ * a calculator from it.  IPEA1-xTB is not available (an error). */
+typedef struct _tblite_param* tblite_param;
+TBLITE_API_ENTRY tblite_param TBLITE_API_CALL tblite_new_param(void);
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_delete_param(tblite_param* param);
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_load_param(tblite_error error, tblite_param param,
+                                                       tblite_table table);
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_dump_param(tblite_error error, tblite_param param,
+                                                       tblite_table table);
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_export_gfn2_param(tblite_error error,
+                                                              tblite_param param);
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_export_gfn1_param(tblite_error error,
+                                                              tblite_param param);
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_export_ipea1_param(tblite_error error,
+                                                               tblite_param param);
+
 /* ---- calculator: include/tblite/calculator.h:36-291 ---- */
 typedef enum {
   TBLITE_GUESS_SAD = 0,
@@ -167,6 +308,17 @@ tblite_new_gfn2_calculator(tblite_context ctx, tblite_structure mol, tblite_xtb_
    halogen-bond correction (Br, I, At) and d-shell elements are rejected */
 TBLITE_API_ENTRY tblite_calculator TBLITE_API_CALL
 tblite_new_gfn1_calculator(tblite_context ctx, tblite_structure mol, tblite_xtb_config* config);
+/* calculator from a parametrisation record (calculator.h:92-107).  The GFN2-xTB form (CN
+ * "dexp", self-consistent D4, arithmetic hardness average, shell-resolved third order, damped
+ * multipoles) and the GFN1-xTB form (CN "exp", D3, harmonic average, atom-resolved third order,
+ * its own element-pair factors) are available, with any element records and global constants;
+ * other forms, d shells and the halogen-bond correction are refused with an error. */
+TBLITE_API_ENTRY tblite_calculator TBLITE_API_CALL
+tblite_new_xtb_calculator(tblite_context ctx, tblite_structure mol, tblite_param param,
+                          tblite_xtb_config* config);
+/* IPEA1-xTB (calculator.h:84-89): not available, reports an error and returns NULL */
+TBLITE_API_ENTRY tblite_calculator TBLITE_API_CALL
+tblite_new_ipea1_calculator(tblite_context ctx, tblite_structure mol, tblite_xtb_config* config);
 TBLITE_API_ENTRY void TBLITE_API_CALL tblite_delete_calculator(tblite_calculator* calc);
 TBLITE_API_ENTRY void TBLITE_API_CALL tblite_set_calculator_accuracy(tblite_context ctx,
                                                                     tblite_calculator calc,
@@ -213,6 +365,17 @@ TBLITE_API_ENTRY void TBLITE_API_CALL tblite_get_singlepoint(tblite_context ctx,
                                                             tblite_structure mol,
                                                             tblite_calculator calc,
                                                             tblite_result res);
+/* post-processing of every single point (calculator.h:270-279): "bond-orders" or "molmom"
+ * (molecular dipole and quadrupole), in the order added; without any, the first single point
+ * adds both (the reference's default).  "xtbml" descriptors and TOML files report an error. */
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_push_back_post_processing_str(tblite_context ctx,
+                                                                          tblite_calculator calc,
+                                                                          tblite_structure mol,
+                                                                          char* charptr);
+/* post-processing from a parametrisation record (calculator.h:281-291): the records here carry
+ * none, so this reports an error */
+TBLITE_API_ENTRY void TBLITE_API_CALL tblite_push_back_post_processing_param(
+    tblite_context ctx, tblite_calculator calc, tblite_structure mol, tblite_param param);
 
 /* ---- interaction containers: include/tblite/container.h:31, 61-70 ---- */
 typedef struct _tblite_container* tblite_container;
@@ -245,6 +408,26 @@ tblite_new_alpb_solvation_solvent(tblite_error error, tblite_structure mol, char
 
 #ifdef __cplusplus
 }
+#endif
+
+#if !defined(__cplusplus) && !defined(TBLITE_CFFI)
+/* Generic macro to free an object handle (include/tblite.h:45-58) */
+#define tblite_delete(ptr) _Generic((ptr), \
+                       tblite_error: tblite_delete_error, \
+                   tblite_container: tblite_delete_container, \
+                     tblite_context: tblite_delete_context, \
+                   tblite_structure: tblite_delete_structure, \
+           tblite_double_dictionary: tblite_delete_double_dictionary, \
+                  tblite_calculator: tblite_delete_calculator, \
+                      tblite_result: tblite_delete_result, \
+                       tblite_table: tblite_delete_table, \
+                       tblite_param: tblite_delete_param \
+                                   )(&ptr)
+/* Generic macro to check for error status (include/tblite.h:60-67) */
+#define tblite_check(ptr) _Generic((ptr), \
+                      tblite_error: tblite_check_error, \
+                    tblite_context: tblite_check_context \
+                                  )(ptr)
 #endif
 
 #endif /* TBLITE_GB300_H */

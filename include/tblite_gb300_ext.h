@@ -38,6 +38,15 @@ int tblite_gb300_batch_singlepoint(tblite_context ctx, int nmol, const tblite_st
                                    int* status);
 /* molecules of the last batch call that took the one-molecule path */
 int tblite_gb300_batch_last_fallbacks(void);
+/* Density solver of the batched SCF for closed shells of at least 128 orbitals: 1 (default)
+ * spectral projection (SP2 squarings on the tensor cores, P = 2 X D X^T; a molecule whose
+ * HOMO-LUMO gap of the converged Fock matrix is below 80 kT, or whose projection does not
+ * converge, is re-run by the one-molecule path), 0 diagonalisation for every molecule.  The
+ * results are the same to the parity bar either way; orbital energies and occupations come
+ * from a diagonalisation of the final Fock matrix. */
+void tblite_gb300_set_batch_density_solver(int mode);
+/* molecules of the last batch call whose SCF density came from the spectral projection */
+int tblite_gb300_batch_last_projected(void);
 /* device time (ms, CUDA events) of the last batch call from the first setup kernel to the end
  * of the gradient, summed over its memory chunks (uploads, read-back and the one-molecule
  * path excluded) */

@@ -19,8 +19,9 @@ OBJ = PKG / "_build"
 LIBNAME = "libtblite_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 UNITS = ["integrals.cu", "scf.cu", "disp.cu", "linalg.cu", "eigen.cu", "noalloc.cu", "solv.cu",
-         "ozaki.cu", "ozaki_pipe.cu", "purify.cu", "capi.cpp", "batch.cpp", "npz.cpp"]
-HEADERS = ["engine.h", "api_internal.h", "npz.h", "params_solv.inc", "params_gfn1.inc", "params_gfn2.inc",
+         "ozaki.cu", "ozaki_pipe.cu", "purify.cu", "capi.cpp", "batch.cpp", "npz.cpp",
+         "dictionary.cpp", "sp2.cu", "table.cpp", "param.cpp"]
+HEADERS = ["engine.h", "api_internal.h", "npz.h", "table.h", "param.h", "params_solv.inc", "params_gfn1.inc", "params_gfn2.inc",
            "element_data.inc"]
 
 

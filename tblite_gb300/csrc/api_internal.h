@@ -140,12 +140,23 @@ struct _tblite_container {
   std::unique_ptr<SolvModel> solv;
 };
 
+// global constants of the calculator's Hamiltonian, from its parametrisation record
+struct ModelConstants {
+  double wexp = 0.0, enscale = 0.0, kpol = 2.0;
+  double ksh[5][5] = {};
+  double gexp = 0.0;
+  double rep_kexp = 0.0, rep_klight = 0.0;
+  double dmp3 = 0.0, dmp5 = 0.0, mp_kexp = 0.0, mp_shift = 0.0, mp_rmax = 0.0;
+  double s6 = 1.0, s8 = 0.0, a1 = 0.0, a2 = 0.0, s9 = 0.0;
+};
+
 struct _tblite_calculator {
   // molecule-bound basis (built at construction)
   int nat = 0, nsh = 0, nao = 0;
   std::vector<int> at_z, at_sh, sh_atom, sh_l, sh_nprim, sh_ao, ao_sh, ao_at;
-  // method: 2 GFN2-xTB, 1 GFN1-xTB
+  // method form: 2 GFN2-xTB, 1 GFN1-xTB
   int method = 2;
+  ModelConstants model;
   std::vector<int> sh_valence;   // GFN1: first shell of its angular momentum on the atom
   std::vector<double> at_gam3;   // GFN1: atom-resolved third-order hardness derivative
   // D3 data per atom (GFN1, molecules with pairs)
@@ -178,6 +189,16 @@ struct _tblite_calculator {
   int param_grad = 0;
   // density solver: 0 diagonalisation (Fermi filling), 1 spectral projection (purify.cu)
   int density_solver = 0;
+  // post-processing of every single point, in order ("bond-orders", "molmom"); an empty list
+  // becomes the reference's default (bond orders and molecular moments) at the first single
+  // point (api/calculator.f90:668-675)
+  std::vector<std::string> post_proc;
+  bool wants(const char* name) const {
+    return std::find(post_proc.begin(), post_proc.end(), name) != post_proc.end();
+  }
+  void default_post_processing() {
+    if (post_proc.empty()) post_proc = {"bond-orders", "molmom"};
+  }
   // implicit solvation container moved in by tblite_calculator_push_back
   std::unique_ptr<SolvModel> solv;
   std::unique_ptr<Workspace> ws;
@@ -189,6 +210,23 @@ struct _tblite_result {
   double energy = 0.0;
   std::vector<double> energies, gradient, sigma, qat, qsh, dpat, qpat, emo, focc, P, C, S, H, wbo;
   int wbo_channels = 0;  // 1 closed shell; 2 (total, magnetisation) for open shell
+  // labels of the post-processing dictionary of the last single point, in order
+  // ("bond-orders" [nat][nat][channels], "molecular-dipole" [3], "molecular-quadrupole" [6])
+  std::vector<std::string> pp;
+  bool has_pp(const char* label) const {
+    return std::find(pp.begin(), pp.end(), label) != pp.end();
+  }
+  // fill pp from the calculator's post-processing list
+  void set_post_processing(const std::vector<std::string>& list) {
+    pp.clear();
+    for (const auto& e : list) {
+      if (e == "bond-orders") pp.push_back("bond-orders");
+      if (e == "molmom") {
+        pp.push_back("molecular-dipole");
+        pp.push_back("molecular-quadrupole");
+      }
+    }
+  }
   // dE/d(per-shell parameters): self energy, its CN shift, hardness, hardness derivative
   std::vector<double> dse, dkcn, dhub, dgam3, dzeta;
   // spectral projection: HOMO, LUMO, bound on their errors (empty after diagonalisation)
@@ -200,10 +238,12 @@ struct _tblite_result {
 };
 
 
-// D4 model constants (damping, counting function, cutoffs) of the element-data pack
-void d4_model_constants(DevD4& d);
-// D3 model constants (counting functions, cutoffs) and the GFN1-xTB damping parameters
-void d3_model_constants(DevD3& d);
+// D4 model constants (counting function, cutoffs of the element-data pack; damping parameters
+// of the calculator)
+void d4_model_constants(DevD4& d, const _tblite_calculator* c);
+// D3 model constants (counting functions, cutoffs of the element-data pack; damping parameters
+// of the calculator)
+void d3_model_constants(DevD3& d, const _tblite_calculator* c);
 // scalar parameters of a calculator's Hamiltonian (GFN2-xTB or GFN1-xTB)
 Gfn2Scalars gfn2_scalars(const _tblite_calculator* c);
 // electrons per spin channel (reference xtb/singlepoint.f90:140-156); throws on an impossible

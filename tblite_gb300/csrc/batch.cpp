@@ -84,6 +84,8 @@ std::mutex g_batch_mutex;
 Arena g_arena;
 int g_last_fallbacks = 0;
 int g_batch_streams = 8;  // side streams the size buckets are spread over
+bool g_batch_sp2 = true;  // closed shells of >= SP2_MIN_NAO orbitals: density by projection
+int g_last_projected = 0;  // molecules of the last call whose SCF density came from projection
 double g_last_device_ms = 0.0;  // device time of the last call's batched steps (CUDA events)
 std::vector<int> g_last_iters;  // SCF iterations per molecule of the last call (0: not batched)
 
@@ -113,6 +115,9 @@ struct Plan {
   double nalp, nbet;
   bool has_d4, has_d3;
   bool param_grad;  // dE/d(shell parameters) with the single point
+  int wbo_ch;       // bond-order channels: 0 not requested, 1 closed shell, 2 open shell
+  bool molmom;      // molecular moments requested
+  bool sp2;         // density by spectral projection during the SCF (sp2.cu)
   // offsets (region, offset) of every array
   Piece xyz, at_z, at_sh, sh_atom, sh_l, sh_nprim, sh_alpha, sh_coeff, sh_ao, ao_sh, ao_at, sh_se0,
       sh_kcn, sh_shpoly, sh_zeta, sh_hub, sh_gam3, sh_refocc, at_en, at_rad, at_rcov, at_mprad,
@@ -128,11 +133,15 @@ struct Plan {
   Piece grad, sigma, sig_at, dEdcn;
   Piece X, A, T1, Y, lu, ed, ee, etau, epv, escal, estatus, conv;
   Piece pgrad, zgrad;  // [4][nsh], [nsh] (param_grad only)
+  Piece wbo;           // [wbo_ch][nat][nat] (bond orders requested only)
+  Piece img, iexp, sp2s, sp2i;  // spectral projection (sp2 only)
 };
 
 struct Bucket {
   int first, last;  // range in the sorted plan
   int nat_max = 0, nsh_max = 0, nao_max = 0, nd_max = 0;
+  bool sp2 = false;
+  int sp2_steps = SP2_MAX_STEPS;  // step budget of the next projection
 };
 
 template <class T>
@@ -214,6 +223,13 @@ void layout(Plan& pl, Region* R) {
   if (pl.param_grad) {
     pl.pgrad = piece<double>(R, RR, 4 * ns);
     pl.zgrad = piece<double>(R, RR, ns);
+  }
+  if (pl.wbo_ch > 0) pl.wbo = piece<double>(R, RR, (size_t)pl.wbo_ch * na * na);
+  if (pl.sp2) {
+    pl.img = piece<uint16_t>(R, RS, pimage_bytes((int)n, (int)n) / sizeof(uint16_t));
+    pl.iexp = piece<int>(R, RS, pimage_lines((int)n));
+    pl.sp2s = piece<double>(R, RS, 8);
+    pl.sp2i = piece<int>(R, RS, 8);
   }
   // scratch
   pl.cn = piece<double>(R, RS, na);
@@ -306,7 +322,7 @@ MolPtrs make_ptrs(const Plan& pl, const Bases& db) {
   q.has_d3 = pl.has_d3 ? 1 : 0;
   if (pl.has_d3) {
     DevD3& d = q.d3;
-    d3_model_constants(d);
+    d3_model_constants(d, pl.c);
     d.nref = db.at<int>(pl.d3_nref);
     d.refcn = db.at<double>(pl.d3_refcn);
     d.sref = db.at<double>(pl.d3_sref);
@@ -331,7 +347,7 @@ MolPtrs make_ptrs(const Plan& pl, const Bases& db) {
     d.rcov = db.at<double>(pl.d4_rcov);
     d.en = db.at<double>(pl.d4_en);
     d.c6ref = db.at<double>(pl.d4_c6ref);
-    d4_model_constants(d);
+    d4_model_constants(d, pl.c);
     D4Work& w = q.d4w;
     w.cn = db.at<double>(pl.d4_cn);
     w.gw = db.at<double>(pl.d4_gw);
@@ -422,6 +438,13 @@ MolPtrs make_ptrs(const Plan& pl, const Bases& db) {
   q.param_grad = pl.param_grad ? 1 : 0;
   q.pgrad = pl.param_grad ? db.at<double>(pl.pgrad) : nullptr;
   q.zgrad = pl.param_grad ? db.at<double>(pl.zgrad) : nullptr;
+  q.wbo_ch = pl.wbo_ch;
+  q.wbo = pl.wbo_ch > 0 ? db.at<double>(pl.wbo) : nullptr;
+  q.img = pl.sp2 ? db.at<uint16_t>(pl.img) : nullptr;
+  q.iexp = pl.sp2 ? db.at<int>(pl.iexp) : nullptr;
+  q.sp2s = pl.sp2 ? db.at<double>(pl.sp2s) : nullptr;
+  q.sp2i = pl.sp2 ? db.at<int>(pl.sp2i) : nullptr;
+  if (pl.sp2) q.nev = pl.nao;  // the projection needs no levels during the SCF; all after it
   return q;
 }
 
@@ -456,9 +479,10 @@ std::vector<Bucket> make_buckets(const std::vector<Plan>& plans) {
   while (i < np) {
     Bucket b;
     b.first = i;
+    b.sp2 = plans[i].sp2;
     const int top = plans[i].nao;
     int j = i;
-    while (j < np && 4 * plans[j].nao >= 3 * top && j - i < 65535) {
+    while (j < np && 4 * plans[j].nao >= 3 * top && j - i < 65535 && plans[j].sp2 == b.sp2) {
       b.nat_max = std::max(b.nat_max, plans[j].nat);
       b.nsh_max = std::max(b.nsh_max, plans[j].nsh);
       b.nao_max = std::max(b.nao_max, plans[j].nao);
@@ -488,6 +512,7 @@ std::vector<int> run_chunk(std::vector<Plan>& plans, Arena& ar, _tblite_context*
   const size_t off_ptrs = tail.take(sizeof(MolPtrs) * np);
   const size_t off_list = tail.take(sizeof(int) * np);
   const size_t off_flag = tail.take(sizeof(int) * np);
+  const size_t off_steps = tail.take(sizeof(int) * np);
   const size_t dbytes = R[RZ].size + R[RR].size + R[RS].size + R[RU].size + tail.size;
   const size_t hbytes = std::max(R[RU].size, R[RR].size) + tail.size;
   ar.reserve(dbytes, hbytes);
@@ -501,6 +526,7 @@ std::vector<int> run_chunk(std::vector<Plan>& plans, Arena& ar, _tblite_context*
   MolPtrs* d_ptrs = reinterpret_cast<MolPtrs*>(dtail + off_ptrs);
   int* d_list = reinterpret_cast<int*>(dtail + off_list);
   int* d_flag = reinterpret_cast<int*>(dtail + off_flag);
+  int* d_steps = reinterpret_cast<int*>(dtail + off_steps);
   // host stage: uploaded region first, then the tables
   Bases hb{{nullptr, nullptr, nullptr, ar.host}};
   std::vector<double> qsh, qat, dp, qp;
@@ -570,13 +596,14 @@ std::vector<int> run_chunk(std::vector<Plan>& plans, Arena& ar, _tblite_context*
   for (int i = 0; i < np; ++i) {
     h_ptrs[i] = make_ptrs(plans[i], db);
     h_ptrs[i].flag = d_flag + i;
+    h_ptrs[i].sp2steps = d_steps + i;
   }
   cuda_check(cudaMemcpyAsync(d_ptrs, h_ptrs, sizeof(MolPtrs) * np, cudaMemcpyHostToDevice, s),
              "batch table");
   cuda_check(cudaMemsetAsync(d_flag, 0, sizeof(int) * np, s), "flags");
   stream_wait(s);
 
-  const std::vector<Bucket> buckets = make_buckets(plans);
+  std::vector<Bucket> buckets = make_buckets(plans);
   const int nb = (int)buckets.size();
   std::vector<char> active(np, 1);
   std::vector<int> h_flag(np, 0);
@@ -593,6 +620,8 @@ std::vector<int> run_chunk(std::vector<Plan>& plans, Arena& ar, _tblite_context*
       L.nsh_max = b.nsh_max;
       L.nao_max = b.nao_max;
       L.nd_max = b.nd_max;
+      L.sp2 = b.sp2 ? 1 : 0;
+      L.sp2_steps = b.sp2_steps;
       L.s = s;
       int cnt = 0;
       for (int i = b.first; i < b.last; ++i)
@@ -622,6 +651,9 @@ std::vector<int> run_chunk(std::vector<Plan>& plans, Arena& ar, _tblite_context*
     }
   };
   const Gfn2Scalars p = gfn2_scalars(plans[0].c);  // h0_cutoff is taken per molecule
+  bool any_sp2 = false;
+  for (const Plan& pl : plans) any_sp2 = any_sp2 || pl.sp2;
+  std::vector<int> h_steps(np, 0);
   bool any_param_grad = false;
   for (const Plan& pl : plans) any_param_grad = any_param_grad || pl.param_grad;
 
@@ -677,10 +709,14 @@ std::vector<int> run_chunk(std::vector<Plan>& plans, Arena& ar, _tblite_context*
       launch_vao_b(L);
       launch_fock_b(L);
       launch_pack_b(L, false);
-      eigen_values_b(L);
-      launch_fermi_b(L);
-      eigen_vectors_b(L);
-      density_b(L, false);
+      if (L.sp2) {
+        sp2_density_b(L, L.sp2_steps);
+      } else {
+        eigen_values_b(L);
+        launch_fermi_b(L);
+        eigen_vectors_b(L);
+        density_b(L, false);
+      }
       launch_mulliken_b(L);
       launch_pack_b(L, true);
       launch_diff_b(L);
@@ -691,8 +727,20 @@ std::vector<int> run_chunk(std::vector<Plan>& plans, Arena& ar, _tblite_context*
     });
     cuda_check(cudaMemcpyAsync(h_flag.data(), d_flag, sizeof(int) * np, cudaMemcpyDeviceToHost, s),
                "flags");
+    if (any_sp2)
+      cuda_check(cudaMemcpyAsync(h_steps.data(), d_steps, sizeof(int) * np, cudaMemcpyDeviceToHost,
+                                 s),
+                 "projection steps");
     stream_wait(s);
     cuda_check(cudaGetLastError(), "batch scf");
+    // step budget of each projection bucket: the most steps its molecules took, plus a margin
+    for (Bucket& b : buckets) {
+      if (!b.sp2) continue;
+      int most = 0;
+      for (int i = b.first; i < b.last; ++i)
+        if (active[i]) most = std::max(most, h_steps[i]);
+      b.sp2_steps = std::min(SP2_MAX_STEPS, most + 10);
+    }
     for (int i = 0; i < np; ++i) {
       if (!active[i]) continue;
       const Plan& pl = plans[i];
@@ -722,15 +770,44 @@ std::vector<int> run_chunk(std::vector<Plan>& plans, Arena& ar, _tblite_context*
     if (active[i]) record_leave(i, -4);
   float scf_ms = 0.f;
 
+  // projection buckets: every eigenvalue of the last Fock matrix (for the results) and the gap
+  // check that makes their 0/2 occupations exact; a molecule below 80 kT leaves the batch
+  if (any_sp2) {
+    std::vector<char> sel(np, 0);
+    for (int i = 0; i < np; ++i) sel[i] = done[i] && plans[i].sp2;
+    if (upload_lists(sel) > 0) {
+      each([&](BatchLaunch& L) {
+        if (!L.sp2) return;
+        eigen_values_b(L);
+        launch_fermi_b(L);
+        sp2_gap_b(L);
+      });
+      cuda_check(
+          cudaMemcpyAsync(h_flag.data(), d_flag, sizeof(int) * np, cudaMemcpyDeviceToHost, s),
+          "flags");
+      stream_wait(s);
+      cuda_check(cudaGetLastError(), "batch projection gap");
+      for (int i = 0; i < np; ++i)
+        if (sel[i] && h_flag[i] < 0) {
+          done[i] = 0;
+          record_leave(i, h_flag[i]);
+        }
+    }
+  }
+
   // gradient of the converged molecules: Coulomb and D4 at the output moments, W into F,
   // H0 gradient with the last potential, CN chain rule
   if (upload_lists(done) > 0) {
     each([&](BatchLaunch& L) {
-      eigen_values_rest_b(L);  // the levels above the SCF's range, for the results
+      if (!L.sp2) eigen_values_rest_b(L);  // the levels above the SCF's range, for the results
       launch_coulomb_gradient_b(L, p);
       d4_gradient_b(L);
-      launch_fe_b(L);
-      density_b(L, true);
+      if (L.sp2) {
+        sp2_weighted_b(L);  // W = P F P / 2
+      } else {
+        launch_fe_b(L);
+        density_b(L, true);
+      }
       launch_h0_gradient_b(L, p);
       launch_cn_grad_b(L, p);
       if (any_param_grad) {  // dE/d(shell parameters), Slater exponents (GFN2)
@@ -738,6 +815,13 @@ std::vector<int> run_chunk(std::vector<Plan>& plans, Arena& ar, _tblite_context*
         launch_zeta_grad_b(L, p);
       }
     });
+    // bond orders (post_processing/wbo.f90:60-115): closed shells from the total density,
+    // restricted open shells per spin channel with the factor 2
+    for (int ch = 0; ch < 2; ++ch) {
+      std::vector<char> sel(np, 0);
+      for (int i = 0; i < np; ++i) sel[i] = done[i] && plans[i].wbo_ch > ch;
+      if (upload_lists(sel) > 0) each([&](BatchLaunch& L) { wbo_b(L, ch); });
+    }
     cuda_check(cudaEventRecord(ev1, s), "event");
     cuda_check(cudaMemcpyAsync(ar.host, db.base[RR], R[RR].size, cudaMemcpyDeviceToHost, s),
                "batch results");
@@ -790,9 +874,21 @@ std::vector<int> run_chunk(std::vector<Plan>& plans, Arena& ar, _tblite_context*
       res->S.clear();
       res->H.clear();
       res->wbo.clear();
-      res->wbo_channels = 0;
+      res->wbo_channels = pl.wbo_ch;
+      if (pl.wbo_ch > 0) {
+        get(pl.wbo, (size_t)pl.wbo_ch * nat * nat, res->wbo);
+        if (pl.wbo_ch == 2) {  // (up, down) -> (total, magnetisation), wavefunction/spin.f90
+          const size_t na2 = (size_t)nat * nat;
+          for (size_t t = 0; t < na2; ++t) {
+            const double up = res->wbo[t], dn = res->wbo[na2 + t];
+            res->wbo[t] = up + dn;
+            res->wbo[na2 + t] = up - dn;
+          }
+        }
+      }
       res->has_wfn = true;
       molecular_moments(pl.mol, res);
+      res->set_post_processing(pl.c->post_proc);
       if (pl.param_grad) {
         std::vector<double> pg;
         get(pl.pgrad, 4 * (size_t)pl.nsh, pg);
@@ -879,6 +975,12 @@ extern "C" int tblite_gb300_batch_singlepoint(tblite_context ctx, int nmol,
     const bool anneal = c->anneal && c->anneal_kt > c->etemp;
     // implicit solvation runs on the one-molecule path
     pl.param_grad = c->param_grad != 0;
+    c->default_post_processing();  // as a plain single point does
+    pl.wbo_ch = c->wants("bond-orders") ? (pl.nalp != pl.nbet ? 2 : 1) : 0;
+    pl.molmom = c->wants("molmom");
+    // the projection needs a closed shell with a whole number of electron pairs
+    pl.sp2 = g_batch_sp2 && pl.nao >= SP2_MIN_NAO && pl.nalp == pl.nbet &&
+             pl.nalp == std::floor(pl.nalp) && pl.nalp >= 1.0;
     if (pl.nao > tri_max || anneal || pl.max_iter < 1 || c->solv) {
       plain.push_back(i);
       continue;
@@ -888,11 +990,14 @@ extern "C" int tblite_gb300_batch_singlepoint(tblite_context ctx, int nmol,
   // by method (one chunk runs one Hamiltonian), then largest first: the size buckets follow
   // the sorted order
   std::stable_sort(plans.begin(), plans.end(), [](const Plan& a, const Plan& b) {
-    return a.method != b.method ? a.method > b.method : a.nao > b.nao;
+    if (a.method != b.method) return a.method > b.method;
+    if (a.sp2 != b.sp2) return a.sp2;
+    return a.nao > b.nao;
   });
   try {
     std::lock_guard<std::mutex> lock(g_batch_mutex);
     g_last_device_ms = 0.0;
+    g_last_projected = 0;
     g_last_iters.assign(nmol, 0);
     prof_reset();
     // chunks of at most ~24 GB of device memory
@@ -908,6 +1013,9 @@ extern "C" int tblite_gb300_batch_singlepoint(tblite_context ctx, int nmol,
       std::vector<Plan> chunk(plans.begin() + i0, plans.begin() + i1);
       const std::vector<int> leave = run_chunk(chunk, g_arena, ctx);
       for (int k : leave) plain.push_back(chunk[k].idx);
+      std::vector<char> left(chunk.size(), 0);
+      for (int k : leave) left[k] = 1;
+      for (size_t k = 0; k < chunk.size(); ++k) g_last_projected += chunk[k].sp2 && !left[k];
       i0 = i1;
     }
     prof_collect();
@@ -944,6 +1052,8 @@ void set_tridiag_ctas_per_sm(int k);
 extern "C" void tblite_gb300_set_tridiag_ctas_per_sm(int count) {
   tb::set_tridiag_ctas_per_sm(count);
 }
+extern "C" void tblite_gb300_set_batch_density_solver(int mode) { g_batch_sp2 = mode != 0; }
+extern "C" int tblite_gb300_batch_last_projected(void) { return g_last_projected; }
 extern "C" void tblite_gb300_set_batch_streams(int count) {
   g_batch_streams = count < 1 ? 1 : (count > 8 ? 8 : count);
 }

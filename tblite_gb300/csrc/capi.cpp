@@ -16,6 +16,7 @@
 #include "../../include/tblite.h"
 #include "../../include/tblite_gb300_ext.h"
 #include "element_data.inc"
+#include "param.h"
 #include "engine.h"
 #include "params_gfn1.inc"
 #include "params_gfn2.inc"
@@ -61,7 +62,122 @@ static void slater_to_gauss(int ng, int n, int l, double zeta, double* alpha, do
     coeff[k] = coeff[k] * pow(top * alpha[k], 0.75) * pow(sqrt(4 * alpha[k]), l) / sqrt(dfac[l]);
 }
 
-static void build_calculator(_tblite_calculator* c, const _tblite_structure* mol) {
+// D4 model data of the molecule's species (element-data pack)
+static void build_d4_data(_tblite_calculator* c, const _tblite_structure* mol) {
+  std::vector<int> species;
+  for (int z : mol->num)
+    if (std::find(species.begin(), species.end(), z) == species.end()) species.push_back(z);
+  c->has_d4 = true;
+  c->d4_nsp = (int)species.size();
+  for (int z : species)
+    if (EXT_D4_NREF[z - 1] <= 0 || std::isnan(EXT_D4_ZEFF[z - 1]))
+      throw std::runtime_error(std::string("element data pack '") + EXT_PACK_NAME +
+                               "' has no D4 data for Z=" + std::to_string(z));
+  for (int i = 0; i < mol->nat; ++i) {
+    const int z = mol->num[i];
+    c->d4_sp.push_back((int)(std::find(species.begin(), species.end(), z) - species.begin()));
+    c->d4_nref.push_back(EXT_D4_NREF[z - 1]);
+    for (int r = 0; r < D4_MREF; ++r) {
+      c->d4_ngw.push_back(EXT_D4_NGW[(z - 1) * D4_MREF + r]);
+      c->d4_refcn.push_back(EXT_D4_REFCN[(z - 1) * D4_MREF + r]);
+      c->d4_refq.push_back(EXT_D4_REFQ[(z - 1) * D4_MREF + r]);
+    }
+    c->d4_zeff.push_back(EXT_D4_ZEFF[z - 1]);
+    c->d4_gam.push_back(EXT_D4_GAM[z - 1]);
+    c->d4_r4r2.push_back(EXT_D4_R4R2[z - 1]);
+    c->d4_rcov.push_back(EXT_D4_RCOV[z - 1]);
+    c->d4_en.push_back(EXT_D4_EN[z - 1]);
+  }
+  const int nsp = c->d4_nsp, ld = nsp * D4_MREF;
+  c->d4_c6ref.assign((size_t)ld * ld, 0.0);
+  for (int a = 0; a < nsp; ++a)
+    for (int r = 0; r < EXT_D4_NREF[species[a] - 1]; ++r)
+      for (int b = 0; b < nsp; ++b)
+        for (int q = 0; q < EXT_D4_NREF[species[b] - 1]; ++q)
+          c->d4_c6ref[(size_t)(a * D4_MREF + r) * ld + b * D4_MREF + q] =
+              sqrt(EXT_D4_REFC6[(species[a] - 1) * D4_MREF + r] *
+                   EXT_D4_REFC6[(species[b] - 1) * D4_MREF + q]);
+}
+
+// D3 data of the molecule's atoms (element-data pack)
+static void build_d3_data(_tblite_calculator* c, const _tblite_structure* mol) {
+  c->has_d3 = true;
+  for (int i = 0; i < mol->nat; ++i) {
+    const int z = mol->num[i];
+    if (EXT_D4_NREF[z - 1] <= 0 || std::isnan(EXT_D4_R4R2[z - 1]) || std::isnan(EXT_D4_RCOV[z - 1]))
+      throw std::runtime_error(std::string("element data pack '") + EXT_PACK_NAME +
+                               "' has no D3 data for Z=" + std::to_string(z));
+    c->d3_nref.push_back(EXT_D4_NREF[z - 1]);
+    for (int r = 0; r < D4_MREF; ++r) {
+      c->d3_refcn.push_back(EXT_D4_REFCN[(z - 1) * D4_MREF + r]);
+      c->d3_sref.push_back(sqrt(EXT_D4_REFC6[(z - 1) * D4_MREF + r]));
+    }
+    c->d3_r4r2.push_back(EXT_D4_R4R2[z - 1]);
+    c->d3_rcov.push_back(EXT_D4_RCOV[z - 1]);
+  }
+}
+
+static void orthogonalize_s(int ni, const double* ai, const double* ci, int& nj, double* aj,
+                            double* cj);
+
+// The calculator of a molecule from a parametrisation record (reference
+// xtb/calculator.f90:new_xtb_calculator with the records of param/*.f90; the built-in methods
+// pass their exported records, xtb/gfn2.f90:914-1022 and xtb/gfn1.f90:931-1054).  Two model
+// forms are available on the GPU: the GFN2-xTB form (CN "dexp", D4 dispersion, arithmetic
+// hardness average, shell-resolved third order, damped multipoles) and the GFN1-xTB form (CN
+// "exp", D3 dispersion, harmonic average, atom-resolved third order, no multipoles; valence and
+// polarisation shells, the second shell of an angular momentum orthogonalised to the first).
+// Within a form every element record entry and every global constant of the record is used;
+// anything else (another form, d shells, the halogen-bond correction, element-pair factors
+// other than the form's own) is refused with an error.
+static void build_calculator(_tblite_calculator* c, const _tblite_structure* mol,
+                             const ParamRecord& rec) {
+  int method = 0;
+  if (rec.cn == "dexp") method = 2;
+  else if (rec.cn == "exp") method = 1;
+  else throw std::runtime_error("coordination number '" + rec.cn + "' of the parameter set is "
+                                "not available in the GPU engine (\"dexp\" or \"exp\")");
+  const char* form = method == 2 ? "GFN2-xTB" : "GFN1-xTB";
+  auto need = [&](bool ok, const std::string& what) {
+    if (!ok)
+      throw std::runtime_error(std::string("parameter set of the ") + form +
+                               " form not supported by the GPU engine: " + what);
+  };
+  need(rec.has_repulsion && rec.has_charge && rec.has_thirdorder && rec.has_dispersion,
+       "repulsion, charge, thirdorder and dispersion entries are required");
+  if (method == 2) {
+    need(!rec.d3 && rec.sc && !rec.smooth, "self-consistent D4 dispersion required");
+    need(rec.average == "arithmetic", "arithmetic hardness average required");
+    need(rec.third_shell, "shell-resolved third order required");
+    need(rec.has_multipole, "damped multipole electrostatics required");
+    need(rec.kpair.empty(), "element-pair scaling factors must be 1");
+  } else {
+    need(rec.d3, "D3 dispersion required");
+    need(rec.average == "harmonic", "harmonic hardness average required");
+    need(!rec.third_shell, "atom-resolved third order required");
+    need(!rec.has_multipole, "no multipole electrostatics in this form");
+    need(rec.wexp == 0.0, "Slater-exponent weighting must be 0");
+  }
+  ModelConstants& k = c->model;
+  k.wexp = rec.wexp;
+  k.enscale = rec.enscale;
+  k.kpol = rec.kpol;
+  for (int a = 0; a < 5; ++a)
+    for (int b = 0; b < 5; ++b) k.ksh[a][b] = rec.ksh[a][b];
+  k.gexp = rec.gexp;
+  k.rep_kexp = rec.kexp;
+  k.rep_klight = rec.klight;
+  k.dmp3 = rec.dmp3;
+  k.dmp5 = rec.dmp5;
+  k.mp_kexp = rec.mp_kexp;
+  k.mp_shift = rec.mp_shift;
+  k.mp_rmax = rec.mp_rmax;
+  k.s6 = rec.s6;
+  k.s8 = rec.s8;
+  k.a1 = rec.a1;
+  k.a2 = rec.a2;
+  k.s9 = rec.s9;
+  c->method = method;
   c->nat = mol->nat;
   c->at_z = mol->num;
   c->at_sh.assign(1, 0);
@@ -70,35 +186,61 @@ static void build_calculator(_tblite_calculator* c, const _tblite_structure* mol
   for (int i = 0; i < mol->nat; ++i) {
     const int z = mol->num[i];
     if (z < 1 || z > 86) throw std::runtime_error("No support for elements with Z > 86.");
-    const int ns = GFN2_NSHELL[z - 1];
+    const ElementRecord* e = rec.get(z);
+    if (!e) throw std::runtime_error("No parameters for element " + element_symbol(z));
+    if (method == 1 && e->xbond > 0.0)
+      throw std::runtime_error("element Z=" + std::to_string(z) +
+                               " needs the GFN1 halogen-bond correction, which the GPU engine "
+                               "does not provide");
+    if (method == 1)
+      for (int j = 0; j <= i; ++j)
+        need(rec.pair(z, mol->num[j]) == gfn1_pair_factor(z, mol->num[j]),
+             "element-pair scaling factors other than GFN1-xTB's");
+    const int ns = e->nsh;
+    if (ns > 3 || (int)e->levels.size() != ns)
+      throw std::runtime_error("element record of " + e->sym + " is inconsistent");
+    double a[3][MAXG] = {{0}}, cc[3][MAXG] = {{0}};
+    int np[3] = {0, 0, 0}, first[5] = {-1, -1, -1, -1, -1};
+    bool val[3] = {true, true, true};
     for (int s = 0; s < ns; ++s) {
-      const int l = GFN2_ANG_SHELL[(z - 1) * 3 + s];
+      const int l = e->lsh[s];
       if (l > 1)
         throw std::runtime_error("element Z=" + std::to_string(z) +
                                  " has d shells, which the CUDA integral kernels do not handle yet");
-      const int pqn = GFN2_PRINCIPAL_QUANTUM_NUMBER[(z - 1) * 3 + s];
-      const int ng = GFN2_NUMBER_OF_PRIMITIVES[(z - 1) * 3 + s];
-      const double zeta = GFN2_SLATER_EXPONENT[(z - 1) * 3 + s];
-      double a[MAXG] = {0}, cc[MAXG] = {0};
-      slater_to_gauss(ng, pqn, l, zeta, a, cc);
-      for (int k = 0; k < MAXG; ++k) {
-        c->sh_alpha.push_back(a[k]);
-        c->sh_coeff.push_back(cc[k]);
-        if (k < ng) c->min_alpha = std::min(c->min_alpha, a[k]);
+      np[s] = e->ngauss[s];
+      if (np[s] < 1 || np[s] > 6) throw std::runtime_error("invalid number of primitives");
+      slater_to_gauss(np[s], e->pqn[s], l, e->slater[s], a[s], cc[s]);
+      if (method == 1) {  // valence: the first shell of its angular momentum
+        val[s] = first[l] < 0;
+        if (val[s]) first[l] = s;
+      }
+    }
+    for (int s = 0; s < ns; ++s)
+      if (!val[s]) {
+        const int r = first[e->lsh[s]];
+        if (np[s] + np[r] > MAXG) throw std::runtime_error("too many primitives");
+        orthogonalize_s(np[r], a[r], cc[r], np[s], a[s], cc[s]);
+      }
+    for (int s = 0; s < ns; ++s) {
+      const int l = e->lsh[s];
+      for (int q = 0; q < MAXG; ++q) {
+        c->sh_alpha.push_back(a[s][q]);
+        c->sh_coeff.push_back(cc[s][q]);
+        if (q < np[s]) c->min_alpha = std::min(c->min_alpha, a[s][q]);
       }
       c->sh_atom.push_back(i);
       c->sh_l.push_back(l);
-      c->sh_nprim.push_back(ng);
+      c->sh_nprim.push_back(np[s]);
       c->sh_ao.push_back(c->nao);
-      c->sh_zeta.push_back(zeta);
-      c->sh_pqn.push_back(pqn);
-      c->sh_se0.push_back(GFN2_P_SELFENERGY[(z - 1) * 3 + s]);
-      c->sh_kcn.push_back(GFN2_P_KCN[(z - 1) * 3 + l]);
-      c->sh_shpoly.push_back(GFN2_P_SHPOLY[(z - 1) * 3 + l]);
-      c->sh_hub.push_back(GFN2_HUBBARD_PARAMETER[z - 1] * GFN2_SHELL_HUBBARD[(z - 1) * 3 + l]);
-      c->sh_gam3.push_back(GFN2_P_HUBBARD_DERIVS[z - 1] * GFN2_SHELL_HUBBARD_DERIVS[l]);
-      c->sh_refocc.push_back(GFN2_REFERENCE_OCC[(z - 1) * 3 + l]);
-      c->sh_valence.push_back(1);
+      c->sh_zeta.push_back(e->slater[s]);
+      c->sh_pqn.push_back(e->pqn[s]);
+      c->sh_se0.push_back(e->levels[s]);
+      c->sh_kcn.push_back(e->kcn[s]);
+      c->sh_shpoly.push_back(e->shpoly[s]);
+      c->sh_hub.push_back(e->gam * e->lgam[s]);
+      c->sh_gam3.push_back(method == 2 ? e->gam3 * rec.third_ksh[l] : 0.0);
+      c->sh_refocc.push_back(val[s] ? e->refocc[s] : 0.0);
+      c->sh_valence.push_back(val[s] ? 1 : 0);
       for (int m = 0; m < 2 * l + 1; ++m) {
         c->ao_sh.push_back(c->nsh);
         c->ao_at.push_back(i);
@@ -108,57 +250,25 @@ static void build_calculator(_tblite_calculator* c, const _tblite_structure* mol
     }
     c->at_sh.push_back(c->nsh);
     // external element data: needed only when the molecule has pairs
-    const bool need = mol->nat > 1;
-    const double en = EXT_EN[z - 1], rad = EXT_RAD[z - 1], rcov = EXT_RCOV[z - 1];
-    if (need && (std::isnan(en) || std::isnan(rad) || std::isnan(rcov)))
+    const bool pairs = mol->nat > 1;
+    const double en = e->en, rad = EXT_RAD[z - 1], rcov = EXT_RCOV[z - 1];
+    if (pairs && (std::isnan(en) || std::isnan(rad) || std::isnan(rcov)))
       throw std::runtime_error(std::string("element data pack '") + EXT_PACK_NAME +
                                "' has no entry for Z=" + std::to_string(z));
-    c->at_en.push_back(need ? en : 0.0);
-    c->at_rad.push_back(need ? rad : 1.0);
-    c->at_rcov.push_back(need ? rcov : 1.0);
-    c->at_mprad.push_back(GFN2_P_RAD[z - 1]);
-    c->at_vcn.push_back(GFN2_P_VCN[z - 1]);
-    c->at_dkern.push_back(GFN2_P_DKERNEL[z - 1]);
-    c->at_qkern.push_back(GFN2_P_QKERNEL[z - 1]);
-    c->at_repa.push_back(GFN2_REP_ALPHA[z - 1]);
-    c->at_repz.push_back(GFN2_REP_ZEFF[z - 1]);
-    c->at_gam3.push_back(0.0);
+    c->at_en.push_back(pairs ? en : 0.0);
+    c->at_rad.push_back(pairs ? rad : 1.0);
+    c->at_rcov.push_back(pairs ? rcov : 1.0);
+    c->at_mprad.push_back(method == 2 ? e->mprad : 1.0);  // no multipoles in the GFN1 form
+    c->at_vcn.push_back(method == 2 ? e->mpvcn : 0.0);
+    c->at_dkern.push_back(method == 2 ? e->dkernel : 0.0);
+    c->at_qkern.push_back(method == 2 ? e->qkernel : 0.0);
+    c->at_repa.push_back(e->arep);
+    c->at_repz.push_back(e->zeff);
+    c->at_gam3.push_back(method == 1 ? e->gam3 : 0.0);
   }
-  // D4 model data (element-data pack), only for molecules with pairs
   if (mol->nat > 1) {
-    std::vector<int> species;
-    for (int z : mol->num)
-      if (std::find(species.begin(), species.end(), z) == species.end()) species.push_back(z);
-    c->has_d4 = true;
-    c->d4_nsp = (int)species.size();
-    for (int z : species)
-      if (EXT_D4_NREF[z - 1] <= 0 || std::isnan(EXT_D4_ZEFF[z - 1]))
-        throw std::runtime_error(std::string("element data pack '") + EXT_PACK_NAME +
-                                 "' has no D4 data for Z=" + std::to_string(z));
-    for (int i = 0; i < mol->nat; ++i) {
-      const int z = mol->num[i];
-      c->d4_sp.push_back((int)(std::find(species.begin(), species.end(), z) - species.begin()));
-      c->d4_nref.push_back(EXT_D4_NREF[z - 1]);
-      for (int r = 0; r < D4_MREF; ++r) {
-        c->d4_ngw.push_back(EXT_D4_NGW[(z - 1) * D4_MREF + r]);
-        c->d4_refcn.push_back(EXT_D4_REFCN[(z - 1) * D4_MREF + r]);
-        c->d4_refq.push_back(EXT_D4_REFQ[(z - 1) * D4_MREF + r]);
-      }
-      c->d4_zeff.push_back(EXT_D4_ZEFF[z - 1]);
-      c->d4_gam.push_back(EXT_D4_GAM[z - 1]);
-      c->d4_r4r2.push_back(EXT_D4_R4R2[z - 1]);
-      c->d4_rcov.push_back(EXT_D4_RCOV[z - 1]);
-      c->d4_en.push_back(EXT_D4_EN[z - 1]);
-    }
-    const int nsp = c->d4_nsp, ld = nsp * D4_MREF;
-    c->d4_c6ref.assign((size_t)ld * ld, 0.0);
-    for (int a = 0; a < nsp; ++a)
-      for (int r = 0; r < EXT_D4_NREF[species[a] - 1]; ++r)
-        for (int b = 0; b < nsp; ++b)
-          for (int q = 0; q < EXT_D4_NREF[species[b] - 1]; ++q)
-            c->d4_c6ref[(size_t)(a * D4_MREF + r) * ld + b * D4_MREF + q] =
-                sqrt(EXT_D4_REFC6[(species[a] - 1) * D4_MREF + r] *
-                     EXT_D4_REFC6[(species[b] - 1) * D4_MREF + q]);
+    if (method == 2) build_d4_data(c, mol);
+    else build_d3_data(c, mol);
   }
 }
 
@@ -184,148 +294,40 @@ static void orthogonalize_s(int ni, const double* ai, const double* ci, int& nj,
   for (int p = 0; p < nj; ++p) cj[p] *= sc;
 }
 
-static void build_calculator_gfn1(_tblite_calculator* c, const _tblite_structure* mol) {
-  c->method = 1;
-  c->nat = mol->nat;
-  c->at_z = mol->num;
-  c->at_sh.assign(1, 0);
-  c->nsh = 0;
-  c->nao = 0;
-  for (int i = 0; i < mol->nat; ++i) {
-    const int z = mol->num[i];
-    if (z < 1 || z > 86) throw std::runtime_error("No support for elements with Z > 86.");
-    if (GFN1_HALOGEN_BOND[z - 1] > 0.0)
-      throw std::runtime_error("element Z=" + std::to_string(z) +
-                               " needs the GFN1 halogen-bond correction, which the GPU engine "
-                               "does not provide");
-    const int ns = GFN1_NSHELL[z - 1];
-    double a[3][MAXG] = {{0}}, cc[3][MAXG] = {{0}};
-    int np[3] = {0, 0, 0}, first[3] = {-1, -1, -1}, lsh[3] = {0, 0, 0};
-    bool val[3] = {false, false, false};
-    for (int s = 0; s < ns; ++s) {
-      const int l = GFN1_ANG_SHELL[(z - 1) * 3 + s];
-      if (l > 1)
-        throw std::runtime_error("element Z=" + std::to_string(z) +
-                                 " has d shells, which the CUDA integral kernels do not handle yet");
-      lsh[s] = l;
-      np[s] = GFN1_NUMBER_OF_PRIMITIVES[(z - 1) * 3 + s];
-      slater_to_gauss(np[s], GFN1_PRINCIPAL_QUANTUM_NUMBER[(z - 1) * 3 + s], l,
-                      GFN1_SLATER_EXPONENT[(z - 1) * 3 + s], a[s], cc[s]);
-      val[s] = first[l] < 0;
-      if (val[s]) first[l] = s;
-    }
-    for (int s = 0; s < ns; ++s)
-      if (!val[s]) {
-        const int r = first[lsh[s]];
-        if (np[s] + np[r] > MAXG) throw std::runtime_error("too many primitives");
-        orthogonalize_s(np[r], a[r], cc[r], np[s], a[s], cc[s]);
-      }
-    for (int s = 0; s < ns; ++s) {
-      const int l = lsh[s];
-      for (int k = 0; k < MAXG; ++k) {
-        c->sh_alpha.push_back(a[s][k]);
-        c->sh_coeff.push_back(cc[s][k]);
-        if (k < np[s]) c->min_alpha = std::min(c->min_alpha, a[s][k]);
-      }
-      c->sh_atom.push_back(i);
-      c->sh_l.push_back(l);
-      c->sh_nprim.push_back(np[s]);
-      c->sh_ao.push_back(c->nao);
-      c->sh_zeta.push_back(GFN1_SLATER_EXPONENT[(z - 1) * 3 + s]);
-      c->sh_se0.push_back(GFN1_P_SELFENERGY[(z - 1) * 3 + s]);
-      c->sh_kcn.push_back(GFN1_P_KCN[(z - 1) * 3 + s]);
-      c->sh_shpoly.push_back(GFN1_P_SHPOLY[(z - 1) * 3 + l]);
-      c->sh_hub.push_back(GFN1_HUBBARD_PARAMETER[z - 1] * GFN1_SHELL_HUBBARD[(z - 1) * 3 + l]);
-      c->sh_gam3.push_back(0.0);
-      c->sh_refocc.push_back(val[s] ? GFN1_REFERENCE_OCC[(z - 1) * 3 + l] : 0.0);
-      c->sh_valence.push_back(val[s] ? 1 : 0);
-      for (int m = 0; m < 2 * l + 1; ++m) {
-        c->ao_sh.push_back(c->nsh);
-        c->ao_at.push_back(i);
-      }
-      c->nao += 2 * l + 1;
-      c->nsh += 1;
-    }
-    c->at_sh.push_back(c->nsh);
-    const bool need = mol->nat > 1;
-    const double en = EXT_EN[z - 1], rad = EXT_RAD[z - 1], rcov = EXT_RCOV[z - 1];
-    if (need && (std::isnan(en) || std::isnan(rad) || std::isnan(rcov)))
-      throw std::runtime_error(std::string("element data pack '") + EXT_PACK_NAME +
-                               "' has no entry for Z=" + std::to_string(z));
-    c->at_en.push_back(need ? en : 0.0);
-    c->at_rad.push_back(need ? rad : 1.0);
-    c->at_rcov.push_back(need ? rcov : 1.0);
-    c->at_mprad.push_back(1.0);  // no anisotropic electrostatics in GFN1
-    c->at_vcn.push_back(0.0);
-    c->at_dkern.push_back(0.0);
-    c->at_qkern.push_back(0.0);
-    c->at_repa.push_back(GFN1_REP_ALPHA[z - 1]);
-    c->at_repz.push_back(GFN1_REP_ZEFF[z - 1]);
-    c->at_gam3.push_back(GFN1_P_HUBBARD_DERIVS[z - 1]);
-  }
-  if (mol->nat > 1) {  // D3 data (element-data pack)
-    c->has_d3 = true;
-    for (int i = 0; i < mol->nat; ++i) {
-      const int z = mol->num[i];
-      if (EXT_D4_NREF[z - 1] <= 0 || std::isnan(EXT_D4_R4R2[z - 1]) || std::isnan(EXT_D4_RCOV[z - 1]))
-        throw std::runtime_error(std::string("element data pack '") + EXT_PACK_NAME +
-                                 "' has no D3 data for Z=" + std::to_string(z));
-      c->d3_nref.push_back(EXT_D4_NREF[z - 1]);
-      for (int r = 0; r < D4_MREF; ++r) {
-        c->d3_refcn.push_back(EXT_D4_REFCN[(z - 1) * D4_MREF + r]);
-        c->d3_sref.push_back(sqrt(EXT_D4_REFC6[(z - 1) * D4_MREF + r]));
-      }
-      c->d3_r4r2.push_back(EXT_D4_R4R2[z - 1]);
-      c->d3_rcov.push_back(EXT_D4_RCOV[z - 1]);
-    }
-  }
-}
-
 Gfn2Scalars gfn2_scalars(const _tblite_calculator* c) {
+  const ModelConstants& k = c->model;
+  Gfn2Scalars p{};
+  p.method = c->method;
+  p.wexp = k.wexp;
+  p.enscale = k.enscale;
+  p.gexp = k.gexp;
+  for (int a = 0; a < 5; ++a)
+    for (int b = 0; b < 5; ++b) p.kshell[a][b] = k.ksh[a][b];
+  p.rep_kexp = k.rep_kexp;
+  p.rep_kexp_light = k.rep_klight;
+  p.rep_rexp = 1.0;  // repulsion/effective.f90: 1/R
+  p.rep_cutoff = 25.0;
+  // get_cutoff, reference basis/type.f90:227-247
+  p.h0_cutoff = std::min(sqrt(2.0 * INTCUT / c->min_alpha), 40.0);
   if (c->method == 1) {
-    Gfn2Scalars p{};
-    p.method = 1;
-    p.wexp = 0.0;
-    p.enscale = GFN1_ENSCALE;
-    p.gexp = GFN1_GEXP;
-    for (int a = 0; a < 5; ++a)
-      for (int b = 0; b < 5; ++b) p.kshell[a][b] = (a < 3 && b < 3) ? GFN1_KSHELL[a * 3 + b] : 0.0;
-    p.kdiff = GFN1_KDIFF;
+    p.kdiff = k.kpol;
     p.harmonic = 1;
     p.third_atom = 1;
     p.aes = 0;
-    p.rep_kexp = GFN1_REP_KEXP;
-    p.rep_kexp_light = GFN1_REP_KEXP;
-    p.rep_rexp = GFN1_REP_REXP;
-    p.rep_cutoff = 25.0;
     p.cn_exp_k = EXT_CNEXP_K;
     p.cn_cutoff = EXT_CNEXP_CUTOFF;
-    p.h0_cutoff = std::min(sqrt(2.0 * INTCUT / c->min_alpha), 40.0);
     return p;
   }
-  Gfn2Scalars p{};
-  p.method = 2;
   p.aes = 1;
-  p.wexp = GFN2_WEXP;
-  p.enscale = GFN2_ENSCALE;
-  p.gexp = GFN2_GEXP;
-  for (int a = 0; a < 5; ++a)
-    for (int b = 0; b < 5; ++b) p.kshell[a][b] = GFN2_KSHELL[a * 5 + b];
-  p.mp_dmp3 = GFN2_MP_DMP3;
-  p.mp_dmp5 = GFN2_MP_DMP5;
-  p.mp_shift = GFN2_MP_SHIFT;
-  p.mp_kexp = GFN2_MP_KEXP;
-  p.mp_rmax = GFN2_MP_RMAX;
-  p.rep_kexp = GFN2_REP_KEXP;
-  p.rep_kexp_light = GFN2_REP_KEXP_LIGHT;
-  p.rep_rexp = GFN2_REP_REXP;
-  p.rep_cutoff = 25.0;
+  p.mp_dmp3 = k.dmp3;
+  p.mp_dmp5 = k.dmp5;
+  p.mp_shift = k.mp_shift;
+  p.mp_kexp = k.mp_kexp;
+  p.mp_rmax = k.mp_rmax;
   p.cn_ka = EXT_CN_KA;
   p.cn_kb = EXT_CN_KB;
   p.cn_rshift = EXT_CN_RSHIFT;
   p.cn_cutoff = EXT_CN_CUTOFF;
-  // get_cutoff, reference basis/type.f90:227-247
-  p.h0_cutoff = std::min(sqrt(2.0 * INTCUT / c->min_alpha), 40.0);
   return p;
 }
 
@@ -460,7 +462,7 @@ static void ensure_workspace(_tblite_calculator* c) {
   }
 }
 
-void d4_model_constants(DevD4& d) {
+void d4_model_constants(DevD4& d, const _tblite_calculator* c) {
   d.ga = EXT_D4_GA;
   d.gc = EXT_D4_GC;
   d.wf = EXT_D4_WF;
@@ -472,11 +474,11 @@ void d4_model_constants(DevD4& d) {
   d.disp2_cutoff = EXT_D4_DISP2_CUTOFF;
   d.disp3_cutoff = EXT_D4_DISP3_CUTOFF;
   d.atm_alpha = EXT_D4_ATM_ALPHA;
-  d.s6 = GFN2_S6;
-  d.s8 = GFN2_S8;
-  d.a1 = GFN2_A1;
-  d.a2 = GFN2_A2;
-  d.s9 = GFN2_S9;
+  d.s6 = c->model.s6;
+  d.s8 = c->model.s8;
+  d.a1 = c->model.a1;
+  d.a2 = c->model.a2;
+  d.s9 = c->model.s9;
 }
 
 static DevD4 dev_d4(const _tblite_calculator* c, D4Work& wk) {
@@ -494,7 +496,7 @@ static DevD4 dev_d4(const _tblite_calculator* c, D4Work& wk) {
   d.rcov = w.d4_rcov.p;
   d.en = w.d4_en.p;
   d.c6ref = w.d4_c6ref.p;
-  d4_model_constants(d);
+  d4_model_constants(d, c);
   wk.cn = w.d4_cn.p;
   wk.gw = w.d4_gw.p;
   wk.dgw = w.d4_dgw.p;
@@ -606,21 +608,21 @@ static DevMol dev_mol(const _tblite_calculator* c) {
   return m;
 }
 
-void d3_model_constants(DevD3& d) {
+void d3_model_constants(DevD3& d, const _tblite_calculator* c) {
   d.k1 = EXT_D3_K1;
   d.k3 = EXT_D3_K3;
   d.cn_cutoff = EXT_D3_CN_CUTOFF;
   d.cutoff = EXT_D3_DISP2_CUTOFF;
-  d.s6 = GFN1_S6;
-  d.s8 = GFN1_S8;
-  d.a1 = GFN1_A1;
-  d.a2 = GFN1_A2;
+  d.s6 = c->model.s6;
+  d.s8 = c->model.s8;
+  d.a1 = c->model.a1;
+  d.a2 = c->model.a2;
 }
 
 static DevD3 dev_d3(const _tblite_calculator* c) {
   const Workspace& w = *c->ws;
   DevD3 d{};
-  d3_model_constants(d);
+  d3_model_constants(d, c);
   d.nref = w.d3_nref.p;
   d.refcn = w.d3_refcn.p;
   d.sref = w.d3_sref.p;
@@ -1034,10 +1036,14 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
   // open shell from the spin densities with the factor 2, then (up, down) -> (total, up-down)
   g_prof.begin(PH_GRADIENT, s);
   const bool open_shell = nalp != nbet;
-  const int nch = open_shell ? 2 : 1;
-  w.wbo.alloc((size_t)nch * nat * nat);
-  cuda_check(cudaMemsetAsync(w.wbo.p, 0, sizeof(double) * nch * nat * nat, s), "zero");
-  if (!open_shell) {
+  const bool want_wbo = c->wants("bond-orders");
+  const int nch = want_wbo ? (open_shell ? 2 : 1) : 0;
+  w.wbo.alloc((size_t)std::max(nch, 1) * nat * nat);
+  cuda_check(cudaMemsetAsync(w.wbo.p, 0, sizeof(double) * std::max(nch, 1) * nat * nat, s),
+             "zero");
+  if (!want_wbo) {
+    // bond orders not requested (post-processing list without "bond-orders")
+  } else if (!open_shell) {
     if (purify) purify_product(w.pur, w.P.p, w.S.p, w.scratch.p);
     else gemm64(false, false, n, n, n, 1.0, w.P.p, n, w.S.p, n, 0.0, w.scratch.p, n, KM_NONE, s);
     launch_wbo(m, w.scratch.p, w.wbo.p, 1.0, s);
@@ -1116,7 +1122,7 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
   res->nel[0] = nalp;
   res->nel[1] = nbet;
   res->kt = c->etemp;
-  if (open_shell) {  // updown_to_magnet (wavefunction/spin.f90:130-140)
+  if (nch == 2) {  // updown_to_magnet (wavefunction/spin.f90:130-140)
     const size_t na2 = (size_t)nat * nat;
     for (size_t t = 0; t < na2; ++t) {
       const double up = res->wbo[t], dn = res->wbo[na2 + t];
@@ -1126,6 +1132,7 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
   }
   res->wbo_channels = nch;
   molecular_moments(mol, res);
+  res->set_post_processing(c->post_proc);
   if (c->param_grad) {  // self energy e_s = se0_s - kcn_s CN_A  =>  dE/dkcn_s = -CN_A dE/de_s
     res->dse.assign(h_pgrad.begin(), h_pgrad.begin() + nsh);
     res->dhub.assign(h_pgrad.begin() + nsh, h_pgrad.begin() + 2 * nsh);
@@ -1813,15 +1820,17 @@ void tblite_gb300_get_result_shell_charges(tblite_error error, tblite_result res
   std::copy(res->qsh.begin(), res->qsh.end(), qsh);
 }
 void tblite_get_result_bond_orders(tblite_error error, tblite_result res, double* mbo) {
-  RESULT_GUARD(!res->wbo.empty(), "Result does not contain bond orders");
+  RESULT_GUARD(res->has_energy || res->has_wfn, "Result does not contain bond orders");
+  RESULT_GUARD(res->has_pp("bond-orders") && !res->wbo.empty(),
+               "Could not find bond orders in results dictionary");
   std::copy(res->wbo.begin(), res->wbo.end(), mbo);
 }
 void tblite_get_result_dipole(tblite_error error, tblite_result res, double dipole[3]) {
-  RESULT_GUARD(res->has_wfn, "Result does not contain dipole moment");
+  RESULT_GUARD(res->has_pp("molecular-dipole"), "Result does not contain dipole moment");
   for (int k = 0; k < 3; ++k) dipole[k] = res->dipole[k];
 }
 void tblite_get_result_quadrupole(tblite_error error, tblite_result res, double quadrupole[6]) {
-  RESULT_GUARD(res->has_wfn, "Result does not contain quadrupole moment");
+  RESULT_GUARD(res->has_pp("molecular-quadrupole"), "Result does not contain quadrupole moment");
   for (int k = 0; k < 6; ++k) quadrupole[k] = res->quadrupole[k];
 }
 void tblite_get_result_orbital_energies(tblite_error error, tblite_result res, double* emo) {
@@ -1925,7 +1934,9 @@ tblite_calculator tblite_new_gfn2_calculator(tblite_context ctx, tblite_structur
   }
   auto* c = new _tblite_calculator();
   try {
-    build_calculator(c, mol);
+    ParamRecord rec;
+    export_gfn2(rec);
+    build_calculator(c, mol, rec);
   } catch (const std::exception& e) {
     ctx->push(e.what());
     delete c;
@@ -1943,13 +1954,48 @@ tblite_calculator tblite_new_gfn1_calculator(tblite_context ctx, tblite_structur
   }
   auto* c = new _tblite_calculator();
   try {
-    build_calculator_gfn1(c, mol);
+    ParamRecord rec;
+    export_gfn1(rec);
+    build_calculator(c, mol, rec);
   } catch (const std::exception& e) {
     ctx->push(e.what());
     delete c;
     return nullptr;
   }
   return c;
+}
+tblite_calculator tblite_new_xtb_calculator(tblite_context ctx, tblite_structure mol,
+                                           tblite_param param, tblite_xtb_config* config) {
+  (void)config;
+  if (!ctx) return nullptr;
+  if (!mol) {
+    ctx->push("Molecular structure data is missing");
+    return nullptr;
+  }
+  if (!param) {
+    ctx->push("Parametrization record is missing");
+    return nullptr;
+  }
+  if (!param->set) {
+    ctx->push("Parametrization record is empty");
+    return nullptr;
+  }
+  auto* c = new _tblite_calculator();
+  try {
+    build_calculator(c, mol, param->rec);
+  } catch (const std::exception& e) {
+    ctx->push(e.what());
+    delete c;
+    return nullptr;
+  }
+  return c;
+}
+tblite_calculator tblite_new_ipea1_calculator(tblite_context ctx, tblite_structure mol,
+                                             tblite_xtb_config* config) {
+  (void)mol;
+  (void)config;
+  if (ctx) ctx->push("IPEA1-xTB is not available in the GPU engine");
+  return nullptr;
 }
 void tblite_delete_calculator(tblite_calculator* c) {
   if (c && *c) {
@@ -2045,6 +2091,7 @@ void tblite_get_singlepoint(tblite_context ctx, tblite_structure mol, tblite_cal
     ctx->push("Result container is missing");
     return;
   }
+  calc->default_post_processing();  // bond orders and molecular moments unless asked otherwise
   try {
     singlepoint(ctx, mol, calc, res);
   } catch (const std::exception& e) {

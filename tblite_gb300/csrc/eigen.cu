@@ -1444,9 +1444,14 @@ __global__ void kb_bt_tmat(BARGS) {
   if (g * 4 > n - 2) return;
   bt_tmat_dev(n, q.A, q.etau, q.lu, g, threadIdx.x & 31);
 }
-__global__ void kb_scale_cols(BARGS, int weighted) {
+// mode 0: occupations (total), 1: occupations x energies (vec_out), 2 + c: spin channel c of
+// the bond orders (a closed shell's channel 0 is the total occupation)
+__global__ void kb_scale_cols(BARGS, int mode) {
   BMOL;
-  scale_cols_dev(q.m.nao, *q.icount, q.C, weighted ? q.vec_out : q.focc, q.scratch);
+  const int n = q.m.nao;
+  const double* f = mode == 0 ? q.focc : mode == 1 ? q.vec_out
+                  : q.wbo_ch == 2 ? q.focc + (size_t)(mode - 1) * n : q.focc;
+  scale_cols_dev(n, *q.icount, q.C, f, q.scratch);
 }
 
 // CTAs of the batched tridiagonalisation that should fit on one SM (1 or 2): with 2 the
@@ -1569,6 +1574,22 @@ void density_b(const BatchLaunch& b, bool weighted) {
   kb_scale_cols<<<dim3((unsigned)((tot + 255) / 256), 1, b.count), 256, 0, b.s>>>(
       b.mp, b.list, weighted ? 1 : 0);
   gemm_b(b, weighted ? GS_WDENS : GS_DENS);
+}
+
+void wbo_b(const BatchLaunch& b, int channel) {
+  if (!b.count) return;
+  if (b.sp2) {  // closed shells without orbitals: P S directly
+    gemm_b(b, GS_PS);
+    launch_wbo_b(b, channel);
+    return;
+  }
+  const size_t tot = (size_t)b.nao_max * b.nao_max;
+  ++g_kernel_launches;
+  kb_scale_cols<<<dim3((unsigned)((tot + 255) / 256), 1, b.count), 256, 0, b.s>>>(
+      b.mp, b.list, 2 + channel);
+  gemm_b(b, GS_WDENS);  // the channel's density into F (W is no longer needed)
+  gemm_b(b, GS_FS);
+  launch_wbo_b(b, channel);
 }
 
 #undef BMOL

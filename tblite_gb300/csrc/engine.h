@@ -361,6 +361,18 @@ struct MolPtrs {
   // derivative, CN shift) and [nsh] dE/d(Slater exponent)
   int param_grad;
   double *pgrad, *zgrad;
+  // Wiberg/Mayer bond orders: channels (0 none, 1 closed shell, 2 spin up/down for a restricted
+  // open shell) and the output [channels][nat][nat]
+  int wbo_ch;
+  double* wbo;
+  // density by spectral projection (closed shells of a projection bucket, sp2.cu): slice image
+  // of the iterate (in Y) and its line exponents, state doubles [8] and ints [8], and the steps
+  // of the last projection for the host
+  uint16_t* img;
+  int* iexp;
+  double* sp2s;
+  int* sp2i;
+  int* sp2steps;
 };
 
 // one launch of a batched step: the molecules list[0..count) of one size bucket
@@ -369,6 +381,8 @@ struct BatchLaunch {
   const int* list;
   int count;
   int nat_max, nsh_max, nao_max, nd_max;
+  int sp2;        // the bucket's density comes from the spectral projection (sp2.cu)
+  int sp2_steps;  // its step budget in this SCF iteration
   cudaStream_t s;
 };
 // batched parameter gradient of the molecules that ask for it (after the gradient phase: P, W in
@@ -397,6 +411,7 @@ void launch_broyden_b(const BatchLaunch& b, int iter);
 void launch_eelec_init_b(const BatchLaunch& b);
 void launch_converge_b(const BatchLaunch& b);  // thresholds per molecule
 void launch_fe_b(const BatchLaunch& b);
+void launch_wbo_b(const BatchLaunch& b, int channel);  // atom-pair sums of scratch = P_c S
 void launch_h0_gradient_b(const BatchLaunch& b, const Gfn2Scalars& p);
 void launch_cn_grad_b(const BatchLaunch& b, const Gfn2Scalars& p);
 void d4_setup_b(const BatchLaunch& b);
@@ -409,7 +424,13 @@ enum { GS_FX = 0,  // T1 = F X            (X upper triangular)
        GS_XTT,     // A = X^T T1
        GS_XY,      // C = X Y, icount columns
        GS_DENS,    // P = (C f) C^T over icount orbitals (scaled copy in scratch)
-       GS_WDENS }; // W (into F) = (C f e) C^T
+       GS_WDENS,   // W (into F) = (C f e) C^T
+       GS_FS,      // scratch = F S (bond orders: F holds a spin density after the gradient)
+       GS_PS,      // scratch = P S (bond orders of a closed shell without orbitals)
+       GS_XD,      // T1 = 2 X D (spectral projection: D, the occupied projector of A, in Y)
+       GS_PXT,     // P = T1 X^T
+       GS_PF,      // T1 = P F / 2
+       GS_WPFP };  // W (into F) = T1 P
 void gemm_b(const BatchLaunch& b, int site);
 // the same sites on the BF16 tensor cores with FP64-accurate splitting (ozaki.cu); gemm_b
 // dispatches to it for buckets of at least 128 orbitals while split_gemm_enabled
@@ -421,5 +442,17 @@ void eigen_values_b(const BatchLaunch& b);              // F -> emo (tridiagonal
 void eigen_values_rest_b(const BatchLaunch& b);         // emo[nev..n) after convergence
 void eigen_vectors_b(const BatchLaunch& b);             // icount lowest vectors into C
 void density_b(const BatchLaunch& b, bool weighted);   // P (or W into F) from C, focc (, emo)
+// bond orders of one spin channel (0: closed shell or spin up, 1: spin down) into MolPtrs.wbo:
+// the channel's density into F, F S into scratch, then the atom-pair sums (after the gradient)
+void wbo_b(const BatchLaunch& b, int channel);
+// batched spectral projection (sp2.cu): P = 2 X D X^T with D the SP2 projector of A = X^T F X
+// after at most `steps` squarings; the gap check after the SCF (all eigenvalues of the last
+// Fock matrix in emo); W = P F P / 2 into F
+void sp2_density_b(const BatchLaunch& b, int steps);
+void sp2_gap_b(const BatchLaunch& b);
+void sp2_weighted_b(const BatchLaunch& b);
+void sp2_square_b(const BatchLaunch& b);  // ozaki_pipe.cu: C = Y Y of the iterating molecules
+constexpr int SP2_MIN_NAO = 128;   // smallest orbital count that takes the projection
+constexpr int SP2_MAX_STEPS = 64;  // squarings per projection at most
 
 }  // namespace tb

@@ -325,6 +325,7 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN)) kb_gemm(BARGS, int site
   const int n = q.m.nao;
   const int k = *q.icount;
   int M = n, N = n, K = n, km = KM_NONE;
+  double alpha = 1.0;
   const double *A = nullptr, *B = nullptr;
   double* C = nullptr;
   bool ta = false, tb = false;
@@ -333,10 +334,17 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN)) kb_gemm(BARGS, int site
     case GS_XTT: A = q.X; ta = true; B = q.T1; C = q.A; km = KM_LT_ROWEND | KM_SYM; break;
     case GS_XY: A = q.X; B = q.Y; C = q.C; N = k; km = KM_GE_ROWBEG; break;
     case GS_DENS: A = q.scratch; B = q.C; tb = true; C = q.P; K = k; km = KM_SYM; break;
-    default: A = q.scratch; B = q.C; tb = true; C = q.F; K = k; km = KM_SYM; break;  // GS_WDENS
+    case GS_WDENS: A = q.scratch; B = q.C; tb = true; C = q.F; K = k; km = KM_SYM; break;
+    case GS_FS: A = q.F; B = q.S; C = q.scratch; break;
+    case GS_PS: A = q.P; B = q.S; C = q.scratch; break;
+    case GS_XD: A = q.X; B = q.Y; C = q.T1; km = KM_GE_ROWBEG; alpha = 2.0; break;
+    case GS_PXT: A = q.T1; B = q.X; tb = true; C = q.P; km = KM_SYM; break;
+    case GS_PF: A = q.P; B = q.F; C = q.T1; alpha = 0.5; break;
+    default: A = q.T1; B = q.P; C = q.F; km = KM_SYM; break;  // GS_WPFP
   }
   if ((int)blockIdx.x * BN >= N || (int)blockIdx.y * BM >= M) return;  // tile outside
-  gemm_dev<BM, BN, BK, TM, TN>(M, N, K, 1.0, A, n, ta, B, n, tb, 0.0, C, n, km);
+  if (*q.flag < 0) return;  // the molecule has left the batch
+  gemm_dev<BM, BN, BK, TM, TN>(M, N, K, alpha, A, n, ta, B, n, tb, 0.0, C, n, km);
 }
 
 bool g_split_gemm = true;

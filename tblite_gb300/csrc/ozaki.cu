@@ -54,12 +54,13 @@ struct Site {
   double* C;
   int km;
   bool sym;
+  double alpha;  // power of two applied to the product (exact)
 };
 
 // the operands of the GEMM sites (the same as the FP64 tile GEMM of linalg.cu)
 __device__ __forceinline__ Site site_of(const MolPtrs& q, int site) {
   const int n = q.m.nao, k = *q.icount;
-  Site s{n, n, n, n, nullptr, false, nullptr, false, nullptr, KM_NONE, false};
+  Site s{n, n, n, n, nullptr, false, nullptr, false, nullptr, KM_NONE, false, 1.0};
   switch (site) {
     case GS_FX: s.A = q.F; s.B = q.X; s.C = q.T1; s.km = KM_LT_COLEND; break;
     case GS_XTT:
@@ -67,7 +68,13 @@ __device__ __forceinline__ Site site_of(const MolPtrs& q, int site) {
       break;
     case GS_XY: s.A = q.X; s.B = q.Y; s.C = q.C; s.N = k; s.km = KM_GE_ROWBEG; break;
     case GS_DENS: s.A = q.scratch; s.B = q.C; s.tb = true; s.C = q.P; s.K = k; s.sym = true; break;
-    default: s.A = q.scratch; s.B = q.C; s.tb = true; s.C = q.F; s.K = k; s.sym = true; break;
+    case GS_WDENS: s.A = q.scratch; s.B = q.C; s.tb = true; s.C = q.F; s.K = k; s.sym = true; break;
+    case GS_FS: s.A = q.F; s.B = q.S; s.C = q.scratch; break;
+    case GS_PS: s.A = q.P; s.B = q.S; s.C = q.scratch; break;
+    case GS_XD: s.A = q.X; s.B = q.Y; s.C = q.T1; s.km = KM_GE_ROWBEG; s.alpha = 2.0; break;
+    case GS_PXT: s.A = q.T1; s.B = q.X; s.tb = true; s.C = q.P; s.sym = true; break;
+    case GS_PF: s.A = q.P; s.B = q.F; s.C = q.T1; s.alpha = 0.5; break;
+    default: s.A = q.T1; s.B = q.P; s.C = q.F; s.sym = true; break;  // GS_WPFP
   }
   return s;
 }
@@ -326,7 +333,7 @@ __device__ __forceinline__ bool ogemm_body(const Site& s, const int* __restrict_
           const int sc = ei + ex[n + j] - 14;
           const double scale =
               (sc > -1022 && sc < 1023) ? __hiloint2double((sc + 1023) << 20, 0) : 0.0;
-          const double v = fma((double)T[c], 0x1p-28, (double)F[c]) * scale;
+          const double v = fma((double)T[c], 0x1p-28, (double)F[c]) * scale * s.alpha;
           s.C[i + (size_t)j * n] = v;
           if (s.sym && i != j) s.C[j + (size_t)i * n] = v;
         }
@@ -395,7 +402,7 @@ void ogemm(bool ta, bool tb, int M, int N, int K, const double* A, const double*
        "smem attr split gemm");
     attr = true;
   }
-  Site s{M, N, K, ld, A, ta, B, tb, C, kmode & 7, (kmode & KM_SYM) != 0};
+  Site s{M, N, K, ld, A, ta, B, tb, C, kmode & 7, (kmode & KM_SYM) != 0, 1.0};
   g_split_flops += s.sym ? (unsigned long long)N * (N + 1) * K : 2ull * M * N * K;
   const int tk = prof_kbegin(st);
   g_kernel_launches += 2;

@@ -108,11 +108,11 @@ __device__ __forceinline__ uint32_t slice_bits(uint32_t a, int p, uint32_t sign)
 // ---- exponents: e = ilogb(max |x|) + 1 of every line ------------------------------------------
 // lines contiguous in memory (element (i, k) at M[i + k ld]): 32 lines per block, the 8 warps
 // take every 8th k (coalesced 256-byte rows), then a shared-memory reduction
-__global__ void __launch_bounds__(256) k_pexp_rows(const double* __restrict__ M, int ld,
-                                                   int lines, int K, int Lp, int* e) {
+__device__ __forceinline__ void pexp_rows_dev(const double* __restrict__ M, int ld, int lines,
+                                              int K, int Lp, int* e, int blk) {
   __shared__ double part[8][33];
   const int li = threadIdx.x & 31, kg = threadIdx.x >> 5;
-  const int i = blockIdx.x * 32 + li;
+  const int i = blk * 32 + li;
   double mx = 0.0;
   if (i < lines)
     for (int k = kg; k < K; k += 8) mx = fmax(mx, fabs(M[i + (size_t)k * ld]));
@@ -122,6 +122,10 @@ __global__ void __launch_bounds__(256) k_pexp_rows(const double* __restrict__ M,
     for (int g = 1; g < 8; ++g) mx = fmax(mx, part[g][li]);
     e[i] = mx > 0.0 ? ilogb(mx) + 1 : 0;
   }
+}
+__global__ void __launch_bounds__(256) k_pexp_rows(const double* __restrict__ M, int ld,
+                                                   int lines, int K, int Lp, int* e) {
+  pexp_rows_dev(M, ld, lines, K, Lp, e, blockIdx.x);
 }
 // k contiguous (element (i, k) at M[k + i ld]): one warp per line
 __global__ void k_pexp_cols(const double* __restrict__ M, int ld, int lines, int K, int Lp,
@@ -138,11 +142,11 @@ __global__ void k_pexp_cols(const double* __restrict__ M, int ld, int lines, int
 
 // ---- slice image: one block per (64 lines, 32 k); the FP64 tile goes through shared memory so
 // both memory orders read coalesced; each thread splits 8 consecutive k of one line
-__global__ void __launch_bounds__(256) k_psplit(const double* __restrict__ M, int ld, int kcontig,
-                                                int lines, int K, int nlb,
-                                                const int* __restrict__ e, uint16_t* img) {
+__device__ __forceinline__ void psplit_dev(const double* __restrict__ M, int ld, int kcontig,
+                                           int lines, int K, int nlb, const int* __restrict__ e,
+                                           uint16_t* img, int lb, int kc) {
   __shared__ double tile[64][33];
-  const int lb = blockIdx.x, kc = blockIdx.y, t = threadIdx.x;
+  const int t = threadIdx.x;
   const int l0 = lb * 64, k0 = kc * PP_KC;
   if (!kcontig) {
 #pragma unroll
@@ -193,6 +197,11 @@ __global__ void __launch_bounds__(256) k_psplit(const double* __restrict__ M, in
     *reinterpret_cast<uint4*>(img + off) = make_uint4(w[p][0], w[p][1], w[p][2], w[p][3]);
   }
 }
+__global__ void __launch_bounds__(256) k_psplit(const double* __restrict__ M, int ld, int kcontig,
+                                                int lines, int K, int nlb,
+                                                const int* __restrict__ e, uint16_t* img) {
+  psplit_dev(M, ld, kcontig, lines, K, nlb, e, img, blockIdx.x, blockIdx.y);
+}
 
 struct PipeArgs {
   const uint16_t* A;  // slice image of op(A) (lines = rows, nlbA line blocks of 64)
@@ -208,10 +217,10 @@ struct PipeArgs {
   int* status;
 };
 
-__global__ void __launch_bounds__(PP_THREADS, 1) k_opipe(PipeArgs a) {
+// one 128 x 64 output tile (number b in the grouped order) of the product a
+__device__ __forceinline__ void opipe_tile(const PipeArgs& a, int b) {
   // ---- tile of this CTA: groups of PP_GROUP row blocks, column blocks inside a group
   const int mt = (a.M + PP_M - 1) / PP_M, nt = (a.N + PP_N - 1) / PP_N;
-  const int b = blockIdx.x;
   const int gid = b / (PP_GROUP * nt);
   const int first = gid * PP_GROUP;
   const int gsize = min(mt - first, PP_GROUP);
@@ -425,8 +434,74 @@ __global__ void __launch_bounds__(PP_THREADS, 1) k_opipe(PipeArgs a) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                  "r"(PP_TMEM_COLS));
 }
+__global__ void __launch_bounds__(PP_THREADS, 1) k_opipe(PipeArgs a) { opipe_tile(a, blockIdx.x); }
+
+// ---- batched squaring X <- X X of the spectral projection: one symmetric product per molecule
+// of the list (blockIdx.z / blockIdx.y walks the molecules).  The iterate lives in Y, its slice
+// image in img (exponents iexp), the square goes to C.  Molecules that left the batch or whose
+// projection has converged (sp2i[0] != 0) launch nothing.
+__device__ __forceinline__ int lines_padded(int n) { return ((n + PP_M - 1) / PP_M) * PP_M; }
+__device__ __forceinline__ bool sq_skip(const MolPtrs& q) {
+  return *q.flag < 0 || q.sp2i[0] != 0;
+}
+__global__ void __launch_bounds__(256) kb_pexp_sq(const MolPtrs* __restrict__ mp,
+                                                  const int* __restrict__ list) {
+  const MolPtrs& q = mp[list[blockIdx.z]];
+  const int n = q.m.nao, lp = lines_padded(n);
+  if (sq_skip(q) || (int)blockIdx.x * 32 >= lp) return;
+  pexp_rows_dev(q.Y, n, n, n, lp, q.iexp, blockIdx.x);
+}
+__global__ void __launch_bounds__(256) kb_psplit_sq(const MolPtrs* __restrict__ mp,
+                                                    const int* __restrict__ list) {
+  const MolPtrs& q = mp[list[blockIdx.z]];
+  const int n = q.m.nao, lp = lines_padded(n), nkc = (n + PP_KC - 1) / PP_KC;
+  if (sq_skip(q) || (int)blockIdx.x >= lp / 64 || (int)blockIdx.y >= nkc) return;
+  psplit_dev(q.Y, n, 0, n, n, lp / 64, q.iexp, q.img, blockIdx.x, blockIdx.y);
+}
+__global__ void __launch_bounds__(PP_THREADS, 1) kb_opipe_sq(const MolPtrs* __restrict__ mp,
+                                                            const int* __restrict__ list) {
+  const MolPtrs& q = mp[list[blockIdx.y]];
+  const int n = q.m.nao;
+  const int tiles = ((n + PP_M - 1) / PP_M) * ((n + PP_N - 1) / PP_N);
+  if (sq_skip(q) || (int)blockIdx.x >= tiles) return;
+  PipeArgs a{};
+  a.A = q.img;
+  a.B = q.img;  // a symmetric matrix: its rows are its columns
+  a.eA = q.iexp;
+  a.eB = q.iexp;
+  a.eshiftA = 0;
+  a.nlbA = a.nlbB = lines_padded(n) / 64;
+  a.M = a.N = n;
+  a.nkc = (n + PP_KC - 1) / PP_KC;
+  a.C = q.C;
+  a.ldc = n;
+  a.sym = 1;
+  a.status = q.sp2i + 3;
+  opipe_tile(a, blockIdx.x);
+}
 
 }  // namespace
+
+// one squaring step of the batched spectral projection: slice image of Y, then C = Y Y on the
+// tensor cores, for every listed molecule still iterating
+void sp2_square_b(const BatchLaunch& b) {
+  if (!b.count) return;
+  static bool attr = false;
+  if (!attr) {
+    ck(cudaFuncSetAttribute(kb_opipe_sq, cudaFuncAttributeMaxDynamicSharedMemorySize, PP_SMEM),
+       "smem attr batched pipelined split gemm");
+    attr = true;
+  }
+  const int n = b.nao_max;
+  const int lp = pimage_lines(n), nkc = (n + PP_KC - 1) / PP_KC;
+  const int tiles = ((n + PP_M - 1) / PP_M) * ((n + PP_N - 1) / PP_N);
+  const int tk = prof_kbegin(b.s);
+  g_kernel_launches += 3;
+  kb_pexp_sq<<<dim3(lp / 32, 1, b.count), 256, 0, b.s>>>(b.mp, b.list);
+  kb_psplit_sq<<<dim3(lp / 64, nkc, b.count), 256, 0, b.s>>>(b.mp, b.list);
+  kb_opipe_sq<<<dim3(tiles, b.count), PP_THREADS, PP_SMEM, b.s>>>(b.mp, b.list);
+  prof_kend(KS_GEMM, tk, b.s);
+}
 
 size_t pimage_bytes(int lines, int K) {
   const size_t lp = (size_t)((lines + PP_M - 1) / PP_M) * PP_M;

@@ -1405,6 +1405,18 @@ __global__ void kb_fe(BARGS) {
   BMOL;
   fe_dev(q.m.nao, q.focc, q.emo, q.vec_out);
 }
+__global__ void kb_wbo(BARGS, int channel) {
+  BMOL;
+  if (q.wbo_ch <= channel) return;
+  wbo_dev(q.m, q.scratch, q.wbo + (size_t)channel * q.m.nat * q.m.nat, q.wbo_ch == 2 ? 2.0 : 1.0);
+}
+void launch_wbo_b(const BatchLaunch& b, int channel) {
+  if (!b.count) return;
+  ++g_kernel_launches;
+  kb_wbo<<<bgrid((unsigned)(((long long)b.nat_max * b.nat_max + 255) / 256), b), 256, 0, b.s>>>(
+      b.mp, b.list, channel);
+}
+
 void launch_fe_b(const BatchLaunch& b) {
   if (!b.count) return;
   ++g_kernel_launches;

@@ -1,0 +1,227 @@
+// Density matrix by spectral projection for the batched ensemble path (closed shells with a
+// gap), beside the batched eigensolver.
+//
+// The reference reaches the density through its solver slot (src/tblite/scf/solver.f90:28-45),
+// filled by diagonalisation (scf/diag.f90:62-143: sygvd, Fermi filling, P = C f C^T).  For a
+// closed shell whose HOMO-LUMO gap spans many kT the Fermi occupations are 0 or 2 to ~e^-80, so
+// P = 2 X D X^T with X = L^-T (the Cholesky factor of S, X^T S X = I) and D the spectral
+// projector onto the lowest nocc eigenvectors of A = X^T F X.  D comes from matrix squarings
+// alone (SP2, Niklasson, Phys. Rev. B 66, 155115 (2002)):
+//
+//   D0 = (emax I - A) / (emax - emin) with Gershgorin bounds [emin, emax] of A,
+//   D <- D^2 or 2D - D^2, whichever brings tr D closer to nocc,
+//   until the idempotency error tr(D - D^2) stops falling over two steps (Kruchinin, Rubensson,
+//   Niklasson, J. Chem. Phys. 145, 204106 (2016)) or reaches the rounding floor.
+//
+// Per molecule and SCF iteration the eigensolver's tridiagonalisation, eigenvalues, inverse
+// iteration and back-transformation (FP64 cores) become ~25 symmetric squarings on the BF16
+// tensor cores with FP64-accurate operand splitting (ozaki_pipe.cu, kb_opipe_sq).  Every
+// molecule of a size bucket iterates in lockstep; each decides its own step on the device and
+// stops on its own (its later launches return at once).  The host launches a step budget per
+// bucket (the most steps any of its molecules took in the previous SCF iteration plus a margin);
+// a molecule that has not converged within it, or whose final gap is below 80 kT (checked after
+// the SCF with all eigenvalues of the last Fock matrix), leaves the batch for the one-molecule
+// path, which reproduces the reference's diagonalisation exactly.
+//
+// The energy-weighted density of the gradient is W = P F P / 2 (the reference's C f e C^T for
+// 0/2 occupations); bond orders use P S.
+#include <cuda_runtime.h>
+
+#include "engine.h"
+
+namespace tb {
+
+namespace {
+
+#define BMOL const MolPtrs& q = mp[list[blockIdx.z]]
+#define BARGS const MolPtrs* __restrict__ mp, const int* __restrict__ list
+
+constexpr double SP2_GAP_KT = 80.0;
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// block-wide sum and min/max; the results are valid in every thread
+__device__ double block_sum(double v, double* red) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  double s = 0.0;
+  for (int w = 0; w < nw; ++w) s += red[w];
+  return s;
+}
+
+// Gershgorin bounds of A and a fresh projection state (one block per molecule)
+__global__ void __launch_bounds__(256) kb_sp2_start(BARGS) {
+  BMOL;
+  if (*q.flag < 0) return;
+  __shared__ double smin[8], smax[8];
+  const int n = q.m.nao, lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  double lo = 1e300, hi = -1e300;
+  for (int j = wid; j < n; j += 8) {
+    const double* col = q.A + (size_t)j * n;
+    double r = 0.0;
+    for (int i = lane; i < n; i += 32)
+      if (i != j) r += fabs(col[i]);
+    r = warp_sum(r);
+    lo = fmin(lo, col[j] - r);
+    hi = fmax(hi, col[j] + r);
+  }
+  if (lane == 0) {
+    smin[wid] = lo;
+    smax[wid] = hi;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < 8; ++w) {
+      lo = fmin(lo, smin[w]);
+      hi = fmax(hi, smax[w]);
+    }
+    lo = fmin(lo, smin[0]);
+    hi = fmax(hi, smax[0]);
+    if (!(hi > lo)) hi = lo + 1.0;  // a 1 x 1 or scalar A: any positive width
+    q.sp2s[0] = lo;
+    q.sp2s[1] = hi;
+    q.sp2s[2] = q.sp2s[3] = q.sp2s[4] = 1e300;  // idempotency errors e(k-2), e(k-1), e(k)
+    q.sp2i[0] = 0;   // converged
+    q.sp2i[1] = 0;   // steps taken
+    q.sp2i[2] = -1;  // update of the current step: 1 square, 0 2D - D^2, -1 none
+    q.sp2i[3] = 0;   // tensor-core pipeline status (set by the squaring kernel)
+    q.scal[0] = 0.0;  // no Fermi entropy: the occupations are 0/2 (checked after the SCF)
+  }
+}
+
+// D0 = (emax I - A) / (emax - emin) into Y
+__global__ void kb_sp2_init(BARGS) {
+  BMOL;
+  if (*q.flag < 0) return;
+  const int n = q.m.nao;
+  const size_t nn = (size_t)n * n;
+  const double emin = q.sp2s[0], emax = q.sp2s[1];
+  const double f = 1.0 / (emax - emin);
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < nn;
+       t += (size_t)gridDim.x * blockDim.x)
+    q.Y[t] = (((t % (n + 1)) == 0 ? emax : 0.0) - q.A[t]) * f;
+}
+
+// traces of D (Y) and D^2 (C), idempotency error, convergence and the next update (one block
+// per molecule)
+__global__ void __launch_bounds__(256) kb_sp2_decide(BARGS) {
+  BMOL;
+  if (*q.flag < 0 || q.sp2i[0] != 0) return;
+  __shared__ double red[8];
+  const int n = q.m.nao;
+  double a = 0.0, b = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    a += q.Y[i + (size_t)i * n];
+    b += q.C[i + (size_t)i * n];
+  }
+  const double tx = block_sum(a, red);
+  const double tx2 = block_sum(b, red);
+  if (threadIdx.x != 0) return;
+  if (q.sp2i[3] != 0) {  // a tensor-core wait ran out: the molecule takes the one-molecule path
+    *q.flag = -5;
+    return;
+  }
+  const double e = tx - tx2;
+  if (!(e == e)) {
+    *q.flag = -6;
+    return;
+  }
+  const int k = q.sp2i[1];
+  const double ekm2 = q.sp2s[3];  // after the shift below: e(k-2)
+  q.sp2s[2] = q.sp2s[3];
+  q.sp2s[3] = q.sp2s[4];
+  q.sp2s[4] = e;
+  // noise floor reached: the error no longer falls over two steps (one of each kind)
+  const bool done = (k >= 2 && ekm2 < 1e-4 * n && e >= ekm2) || e <= 1e-15 * n;
+  if (done) {
+    q.sp2i[0] = 1;
+    q.sp2i[2] = -1;
+    return;
+  }
+  const double nocc = q.nalp;
+  q.sp2i[2] = fabs(tx2 - nocc) <= fabs(2.0 * tx - tx2 - nocc) ? 1 : 0;
+  q.sp2i[1] = k + 1;
+}
+
+// D <- D^2 or 2D - D^2
+__global__ void kb_sp2_update(BARGS) {
+  BMOL;
+  if (*q.flag < 0) return;
+  const int u = q.sp2i[2];
+  if (u < 0) return;
+  const size_t nn = (size_t)q.m.nao * q.m.nao;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < nn;
+       t += (size_t)gridDim.x * blockDim.x)
+    q.Y[t] = u ? q.C[t] : 2.0 * q.Y[t] - q.C[t];
+}
+
+// after the step budget: a projection that has not converged sends the molecule to the
+// one-molecule path; the steps taken go to the host (budget of the next SCF iteration)
+__global__ void kb_sp2_finish(BARGS) {
+  BMOL;
+  if (threadIdx.x != 0) return;
+  *q.sp2steps = q.sp2i[1];
+  if (*q.flag < 0) return;
+  if (q.sp2i[0] == 0) *q.flag = -6;
+}
+
+// after the SCF, with every eigenvalue of the last Fock matrix: the occupations are 0/2 only
+// if the HOMO-LUMO gap spans at least 80 kT; otherwise the molecule leaves the batch
+__global__ void kb_sp2_gap(BARGS) {
+  BMOL;
+  if (threadIdx.x != 0 || *q.flag < 0) return;
+  const int nocc = (int)q.nalp, n = q.m.nao;
+  if (nocc <= 0 || nocc >= n) return;  // no gap to speak of: all levels empty or full
+  if (q.emo[nocc] - q.emo[nocc - 1] < SP2_GAP_KT * q.kt) *q.flag = -7;
+}
+
+inline unsigned ew_blocks(const BatchLaunch& b) {
+  const size_t nn = (size_t)b.nao_max * b.nao_max;
+  const size_t blocks = (nn + 255) / 256;
+  return (unsigned)(blocks < 64 ? blocks : 64);
+}
+
+}  // namespace
+
+void sp2_density_b(const BatchLaunch& b, int steps) {
+  if (!b.count) return;
+  gemm_b(b, GS_FX);
+  gemm_b(b, GS_XTT);
+  g_kernel_launches += 2;
+  kb_sp2_start<<<dim3(1, 1, b.count), 256, 0, b.s>>>(b.mp, b.list);
+  kb_sp2_init<<<dim3(ew_blocks(b), 1, b.count), 256, 0, b.s>>>(b.mp, b.list);
+  for (int k = 0; k < steps; ++k) {
+    sp2_square_b(b);
+    g_kernel_launches += 2;
+    kb_sp2_decide<<<dim3(1, 1, b.count), 256, 0, b.s>>>(b.mp, b.list);
+    kb_sp2_update<<<dim3(ew_blocks(b), 1, b.count), 256, 0, b.s>>>(b.mp, b.list);
+  }
+  ++g_kernel_launches;
+  kb_sp2_finish<<<dim3(1, 1, b.count), 32, 0, b.s>>>(b.mp, b.list);
+  gemm_b(b, GS_XD);   // T1 = 2 X D
+  gemm_b(b, GS_PXT);  // P = T1 X^T
+}
+
+void sp2_gap_b(const BatchLaunch& b) {
+  if (!b.count) return;
+  ++g_kernel_launches;
+  kb_sp2_gap<<<dim3(1, 1, b.count), 32, 0, b.s>>>(b.mp, b.list);
+}
+
+void sp2_weighted_b(const BatchLaunch& b) {
+  if (!b.count) return;
+  gemm_b(b, GS_PF);    // T1 = P F / 2
+  gemm_b(b, GS_WPFP);  // W = T1 P, into F
+}
+
+#undef BMOL
+#undef BARGS
+
+}  // namespace tb

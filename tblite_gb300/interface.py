@@ -80,6 +80,8 @@ class Result:
             return library.result_int(self._res, "number_of_orbitals")
         if attribute == "shell-charges":  # extension: Mulliken shell charges
             return library.result_shell_charges(self._res)
+        if attribute == "post-processing-dict":
+            return library.post_processing_dict(self._res)
         if attribute not in self._shapes:
             raise TBLiteValueError(f"Attribute '{attribute}' is not available in this container")
         dims = {"nat": None, "nao": None}
@@ -122,6 +124,12 @@ class Calculator(Structure):
                  uhf: Optional[int] = None, lattice=None, periodic=None, xtb_config=None,
                  **context_kwargs):
         Structure.__init__(self, numbers, positions, charge, uhf, lattice, periodic)
+        if isinstance(method, dict):  # a parameter set in the reference's TOML layout
+            self._param = library.param_from_dict(method)
+            self._ctx = library.new_context(**context_kwargs)
+            self._calc = library.new_xtb_calculator(self._ctx, self._mol, self._param.h)
+            self._method = "xTB"
+            return
         if method not in self._loader:
             raise TBLiteValueError(f"Method '{method}' is not available for this calculator")
         self._ctx = library.new_context(**context_kwargs)
@@ -185,13 +193,22 @@ class Calculator(Structure):
             return out
         raise TBLiteValueError(f"Attribute '{attribute}' is not available in this calculator")
 
+    _post_processing = {"bond-orders": "bond-orders", "molecular-multipoles": "molmom"}
+
     def add(self, interaction: str, *args) -> None:
-        """Add an interaction (reference interface.py:588-637).  Available: ``"alpb-solvation"``
-        with the solvent ``"water"`` and an optional solution state ``"gsolv"`` (default),
-        ``"bar1mol"`` or ``"reference"``."""
+        """Add an interaction or a post-processing step (reference interface.py:588-637).
+
+        Interactions: ``"alpb-solvation"`` with the solvent ``"water"`` and an optional
+        solution state ``"gsolv"`` (default), ``"bar1mol"`` or ``"reference"``.
+        Post-processing: ``"bond-orders"`` and ``"molecular-multipoles"`` (computed with every
+        single point in the order added; without any, both are computed)."""
         if interaction == "alpb-solvation":
             cont = library.new_alpb_solvation(self._mol, *args, version=2)
             library.calculator_push_back(self._ctx, self._calc, cont)
+            return
+        if interaction in self._post_processing:
+            library.post_processing_push_back(self._ctx, self._calc, self._mol,
+                                              self._post_processing[interaction])
             return
         raise TBLiteValueError(f"Interaction '{interaction}' is not available in the GPU engine")
 

@@ -102,6 +102,16 @@ _SIGNATURES = {
     "tblite_gb300_set_pipelined_gemm": (None, [c_int]),
     "tblite_gb300_get_result_gap": (None, [c_void_p, c_void_p, _dbl_p]),
     "tblite_gb300_get_result_shell_charges": (None, [c_void_p, c_void_p, _dbl_p]),
+    "tblite_get_post_processing_dict": (c_void_p, [c_void_p, c_void_p]),
+    "tblite_get_n_entries_dict": (c_int, [c_void_p, c_void_p]),
+    "tblite_get_array_size_index": (None, [c_void_p, c_void_p, _int_p, _int_p, _int_p, _int_p]),
+    "tblite_get_array_entry_index": (None, [c_void_p, c_void_p, _int_p, _dbl_p]),
+    "tblite_get_array_size_label": (None, [c_void_p, c_void_p, c_char_p, _int_p, _int_p,
+                                           _int_p]),
+    "tblite_get_array_entry_label": (None, [c_void_p, c_void_p, c_char_p, _dbl_p]),
+    "tblite_get_label_entry_index": (None, [c_void_p, c_void_p, _int_p, c_char_p, _int_p]),
+    "tblite_delete_double_dictionary": (None, [POINTER(c_void_p)]),
+    "tblite_push_back_post_processing_str": (None, [c_void_p, c_void_p, c_void_p, c_char_p]),
     "tblite_save_result_wavefunction": (None, [c_void_p, c_void_p, c_char_p]),
     "tblite_load_result_wavefunction": (None, [c_void_p, c_void_p, c_char_p]),
     "tblite_gb300_density_matrix_noalloc": (
@@ -110,9 +120,55 @@ _SIGNATURES = {
     "tblite_gb300_batch_singlepoint": (
         c_int, [c_void_p, c_int, POINTER(c_void_p), POINTER(c_void_p), POINTER(c_void_p), _int_p]),
     "tblite_gb300_batch_last_fallbacks": (c_int, []),
+    "tblite_gb300_set_batch_density_solver": (None, [c_int]),
+    "tblite_gb300_batch_last_projected": (c_int, []),
     "tblite_gb300_batch_last_device_ms": (c_double, []),
     "tblite_gb300_batch_last_iterations": (c_int, [_int_p, c_int]),
 }
+_c64p = POINTER(ctypes.c_int64)
+_bp = POINTER(c_bool)
+_SIGNATURES.update({
+    "tblite_new_param": (c_void_p, []),
+    "tblite_delete_param": (None, [POINTER(c_void_p)]),
+    "tblite_load_param": (None, [c_void_p, c_void_p, c_void_p]),
+    "tblite_dump_param": (None, [c_void_p, c_void_p, c_void_p]),
+    "tblite_export_gfn2_param": (None, [c_void_p, c_void_p]),
+    "tblite_export_gfn1_param": (None, [c_void_p, c_void_p]),
+    "tblite_export_ipea1_param": (None, [c_void_p, c_void_p]),
+    "tblite_new_xtb_calculator": (c_void_p, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    "tblite_new_ipea1_calculator": (c_void_p, [c_void_p, c_void_p, c_void_p]),
+    "tblite_push_back_post_processing_param": (None, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    "tblite_new_table": (c_void_p, [c_void_p]),
+    "tblite_delete_table": (None, [POINTER(c_void_p)]),
+    "tblite_table_set_double": (None, [c_void_p, c_void_p, c_char_p, _dbl_p, c_int]),
+    "tblite_table_set_int64_t": (None, [c_void_p, c_void_p, c_char_p, _c64p, c_int]),
+    "tblite_table_set_bool": (None, [c_void_p, c_void_p, c_char_p, _bp, c_int]),
+    "tblite_table_set_char": (None, [c_void_p, c_void_p, c_char_p, c_char_p, c_int]),
+    "tblite_table_add_table": (c_void_p, [c_void_p, c_void_p, c_char_p]),
+    "tblite_new_array": (c_void_p, []),
+    "tblite_delete_array": (None, [POINTER(c_void_p)]),
+    "tblite_array_push_back_double": (None, [c_void_p, c_void_p, c_double]),
+    "tblite_array_push_back_int64_t": (None, [c_void_p, c_void_p, ctypes.c_int64]),
+    "tblite_array_push_back_bool": (None, [c_void_p, c_void_p, c_bool]),
+    "tblite_array_push_back_char": (None, [c_void_p, c_void_p, c_char_p]),
+    "tblite_array_size": (c_int, [c_void_p, c_void_p]),
+    "tblite_array_get_type": (c_int, [c_void_p, c_void_p, c_int]),
+    "tblite_array_get_double": (None, [c_void_p, c_void_p, c_int, _dbl_p]),
+    "tblite_array_get_int64_t": (None, [c_void_p, c_void_p, c_int, _c64p]),
+    "tblite_array_get_bool": (None, [c_void_p, c_void_p, c_int, _bp]),
+    "tblite_array_get_char": (None, [c_void_p, c_void_p, c_int, c_char_p, c_int]),
+    "tblite_table_set_array": (None, [c_void_p, c_void_p, c_char_p, c_void_p]),
+    "tblite_table_get_type": (c_int, [c_void_p, c_void_p, c_char_p]),
+    "tblite_table_get_bool": (None, [c_void_p, c_void_p, c_char_p, _bp]),
+    "tblite_table_get_int64_t": (None, [c_void_p, c_void_p, c_char_p, _c64p]),
+    "tblite_table_get_double": (None, [c_void_p, c_void_p, c_char_p, _dbl_p]),
+    "tblite_table_get_char": (None, [c_void_p, c_void_p, c_char_p, c_char_p, c_int]),
+    "tblite_table_get_table": (c_void_p, [c_void_p, c_void_p, c_char_p]),
+    "tblite_table_get_array": (c_void_p, [c_void_p, c_void_p, c_char_p]),
+    "tblite_table_get_n_keys": (c_int, [c_void_p, c_void_p]),
+    "tblite_table_get_key": (None, [c_void_p, c_void_p, c_int, c_char_p, c_int]),
+    "tblite_dump_table": (None, [c_void_p, c_void_p, c_char_p]),
+})
 for _name in ("number_of_atoms", "number_of_shells", "number_of_orbitals", "number_of_spins"):
     _SIGNATURES[f"tblite_get_result_{_name}"] = (None, [c_void_p, c_void_p, _int_p])
 for _name in ("energy", "energies", "gradient", "virial", "charges", "bond_orders", "dipole",
@@ -144,6 +200,20 @@ PHASES = ("setup", "potential", "fock", "eigensolve", "density", "mulliken", "mi
 
 def set_profiling(enable: bool) -> None:
     load().tblite_gb300_set_profiling(int(bool(enable)))
+
+
+def set_batch_density_solver(solver: str) -> None:
+    """Density solver of the batched SCF for closed shells of >= 128 orbitals: "purification"
+    (default, spectral projection on the tensor cores) or "diagonalization"."""
+    code = DENSITY_SOLVERS.get(solver, solver) if isinstance(solver, str) else int(solver)
+    if not isinstance(code, int):
+        raise TBLiteValueError(f"Unknown density solver '{solver}'")
+    load().tblite_gb300_set_batch_density_solver(code)
+
+
+def batch_projected() -> int:
+    """Molecules of the last batch call whose SCF density came from the spectral projection."""
+    return int(load().tblite_gb300_batch_last_projected())
 
 
 def set_batch_streams(count: int) -> None:
@@ -278,6 +348,176 @@ def set_parameter_gradient(ctx, calc, enable=True):
     context_check(ctx)
 
 
+def new_xtb_calculator(ctx, mol, param):
+    """Calculator from a parametrisation record handle (tblite_new_xtb_calculator)."""
+    lib = load()
+    calc = c_void_p(lib.tblite_new_xtb_calculator(ctx, mol, param, None))
+    context_check(ctx)
+    return calc
+
+
+class Param:
+    """A parametrisation record handle (tblite_param), freed with the object."""
+
+    def __init__(self):
+        self.h = c_void_p(load().tblite_new_param())
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h is not None and h.value:
+            load().tblite_delete_param(byref(h))
+
+
+class Table:
+    """A data table handle (tblite_table), freed with the object."""
+
+    def __init__(self, handle=None):
+        self.h = c_void_p(handle if handle is not None else load().tblite_new_table(None))
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h is not None and h.value:
+            load().tblite_delete_table(byref(h))
+
+
+def _set_entry(lib, err, table, key: bytes, value):
+    if isinstance(value, dict):
+        sub = Table(lib.tblite_table_add_table(err.h, table, key))
+        err.check()
+        for k, v in value.items():
+            _set_entry(lib, err, sub.h, str(k).encode(), v)
+    elif isinstance(value, (list, tuple, np.ndarray)):
+        arr = c_void_p(lib.tblite_new_array())
+        try:
+            for v in (value.tolist() if isinstance(value, np.ndarray) else value):
+                if isinstance(v, (bool, np.bool_)):
+                    lib.tblite_array_push_back_bool(err.h, arr, bool(v))
+                elif isinstance(v, (int, np.integer)):
+                    lib.tblite_array_push_back_int64_t(err.h, arr, int(v))
+                elif isinstance(v, (float, np.floating)):
+                    lib.tblite_array_push_back_double(err.h, arr, float(v))
+                elif isinstance(v, str):
+                    lib.tblite_array_push_back_char(err.h, arr, v.encode())
+                else:
+                    raise TBLiteValueError(f"Unsupported array entry {v!r}")
+            lib.tblite_table_set_array(err.h, table, key, arr)
+        finally:
+            lib.tblite_delete_array(byref(arr))
+    elif isinstance(value, (bool, np.bool_)):
+        lib.tblite_table_set_bool(err.h, table, key, byref(c_bool(bool(value))), 0)
+    elif isinstance(value, (int, np.integer)):
+        lib.tblite_table_set_int64_t(err.h, table, key, byref(ctypes.c_int64(int(value))), 0)
+    elif isinstance(value, (float, np.floating)):
+        lib.tblite_table_set_double(err.h, table, key, byref(c_double(float(value))), 0)
+    elif isinstance(value, str):
+        lib.tblite_table_set_char(err.h, table, key, value.encode(), 0)
+    else:
+        raise TBLiteValueError(f"Unsupported value type {type(value)!r} for '{key.decode()}'")
+    err.check()
+
+
+def dict_to_table(data) -> Table:
+    """A data table from a nested mapping (reference library.py dict_to_table)."""
+    if not isinstance(data, dict):
+        raise TBLiteValueError("Expected a dictionary for parametrization data")
+    lib = load()
+    err = _Error()
+    table = Table()
+    for k, v in data.items():
+        _set_entry(lib, err, table.h, str(k).encode(), v)
+    return table
+
+
+def table_to_dict(table) -> dict:
+    """A nested mapping from a data table handle."""
+    lib = load()
+    err = _Error()
+    h = table.h if isinstance(table, Table) else table
+    out = {}
+    key = ctypes.create_string_buffer(512)
+    for i in range(1, lib.tblite_table_get_n_keys(err.h, h) + 1):
+        lib.tblite_table_get_key(err.h, h, i, key, 512)
+        err.check()
+        k = key.value
+        kind = lib.tblite_table_get_type(err.h, h, k)
+        if kind == 1:
+            v = c_bool()
+            lib.tblite_table_get_bool(err.h, h, k, byref(v))
+            value = bool(v.value)
+        elif kind == 2:
+            v = ctypes.c_int64()
+            lib.tblite_table_get_int64_t(err.h, h, k, byref(v))
+            value = int(v.value)
+        elif kind == 3:
+            v = c_double()
+            lib.tblite_table_get_double(err.h, h, k, byref(v))
+            value = float(v.value)
+        elif kind == 4:
+            buf = ctypes.create_string_buffer(4096)
+            lib.tblite_table_get_char(err.h, h, k, buf, 4096)
+            value = buf.value.decode()
+        elif kind == 5:
+            arr = c_void_p(lib.tblite_table_get_array(err.h, h, k))
+            try:
+                value = []
+                for j in range(1, lib.tblite_array_size(err.h, arr) + 1):
+                    t = lib.tblite_array_get_type(err.h, arr, j)
+                    if t == 1:
+                        v = c_bool()
+                        lib.tblite_array_get_bool(err.h, arr, j, byref(v))
+                        value.append(bool(v.value))
+                    elif t == 2:
+                        v = ctypes.c_int64()
+                        lib.tblite_array_get_int64_t(err.h, arr, j, byref(v))
+                        value.append(int(v.value))
+                    elif t == 3:
+                        v = c_double()
+                        lib.tblite_array_get_double(err.h, arr, j, byref(v))
+                        value.append(float(v.value))
+                    else:
+                        buf = ctypes.create_string_buffer(4096)
+                        lib.tblite_array_get_char(err.h, arr, j, buf, 4096)
+                        value.append(buf.value.decode())
+            finally:
+                lib.tblite_delete_array(byref(arr))
+        elif kind == 6:
+            sub = Table(lib.tblite_table_get_table(err.h, h, k))
+            value = table_to_dict(sub)
+        else:
+            raise TBLiteValueError(f"Unsupported table entry for key {k!r}")
+        err.check()
+        out[k.decode()] = value
+    return out
+
+
+def export_param(method: str) -> dict:
+    """The parameters of a built-in method ("GFN2-xTB" or "GFN1-xTB") as a nested mapping in
+    the reference's TOML layout (tblite_export_*_param, tblite_dump_param)."""
+    fn = {"GFN2-xTB": "tblite_export_gfn2_param", "GFN1-xTB": "tblite_export_gfn1_param"}
+    if method not in fn:
+        raise TBLiteValueError(f"No parameters for method '{method}'")
+    lib = load()
+    err = _Error()
+    p = Param()
+    getattr(lib, fn[method])(err.h, p.h)
+    err.check()
+    t = Table()
+    lib.tblite_dump_param(err.h, p.h, t.h)
+    err.check()
+    return table_to_dict(t)
+
+
+def param_from_dict(data) -> Param:
+    """A parametrisation record loaded from a nested mapping (tblite_load_param)."""
+    lib = load()
+    table = dict_to_table(data)
+    err = _Error()
+    p = Param()
+    lib.tblite_load_param(err.h, p.h, table.h)
+    err.check()
+    return p
+
+
 def new_gfn1_calculator(ctx, mol):
     lib = load()
     calc = c_void_p(lib.tblite_new_gfn1_calculator(ctx, mol, None))
@@ -291,6 +531,39 @@ def result_array(res, name, shape):
     out = np.zeros(shape, dtype=np.float64)
     getattr(lib, f"tblite_get_result_{name}")(err.h, res, _dp(out))
     err.check()
+    return out
+
+
+def post_processing_push_back(ctx, calc, mol, name: str):
+    """Add a post-processing step ("bond-orders" or "molmom") to a calculator."""
+    load().tblite_push_back_post_processing_str(ctx, calc, mol, name.encode("ascii"))
+    context_check(ctx)
+
+
+def post_processing_dict(res):
+    """The post-processing arrays of a result by label (reference library.py:744-774); arrays
+    keep the dictionary's dimensions in Fortran order."""
+    lib = load()
+    err = _Error()
+    d = c_void_p(lib.tblite_get_post_processing_dict(err.h, res))
+    err.check()
+    out = {}
+    try:
+        for i in range(1, lib.tblite_get_n_entries_dict(err.h, d) + 1):
+            idx = c_int(i)
+            dims = [c_int(0), c_int(0), c_int(0)]
+            lib.tblite_get_array_size_index(err.h, d, byref(idx), *[byref(x) for x in dims])
+            err.check()
+            shape = tuple(x.value for x in dims if x.value > 0)
+            arr = np.zeros(int(np.prod(shape)), dtype=np.float64)
+            lib.tblite_get_array_entry_index(err.h, d, byref(idx), _dp(arr))
+            label = ctypes.create_string_buffer(512)
+            size = c_int(512)
+            lib.tblite_get_label_entry_index(err.h, d, byref(idx), label, byref(size))
+            err.check()
+            out[label.value.decode()] = arr.reshape(shape, order="F")
+    finally:
+        lib.tblite_delete_double_dictionary(byref(d))
     return out
 
 

@@ -20,7 +20,8 @@ def lib():
 
 def test_header_symbols_exported(lib):
     header = "".join(p.read_text() for p in sorted((ROOT / "include").glob("*.h")))
-    names = sorted(set(re.findall(r"\b(tblite_[a-z0-9_]+)\s*\(", header)))
+    macros = set(re.findall(r"#define\s+(tblite_[a-z0-9_]+)\(", header))
+    names = sorted(set(re.findall(r"\b(tblite_[a-z0-9_]+)\s*\(", header)) - macros)
     assert len(names) > 50
     missing = [n for n in names if not hasattr(lib, n)]
     assert not missing, missing

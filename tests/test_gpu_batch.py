@@ -160,3 +160,46 @@ def test_split_gemm_matches_fp64_gemm():
     res = batch_singlepoint([_calc(z, x) for z, x in mols])
     for a, b in zip(res, ref):
         _compare(a, b)
+
+
+def test_projection_matches_diagonalisation():
+    """Closed shells of >= 128 orbitals take the spectral projection in the batch (SP2 squarings
+    on the tensor cores); the same molecules with the batched diagonalisation, and with the
+    one-molecule path, agree at the parity bar, bond orders and orbital energies included."""
+    from tblite_gb300 import library, workloads
+    from tblite_gb300.interface import batch_fallbacks, batch_singlepoint
+
+    mols = [workloads.water_cluster_k(k, seed=500 + k) for k in (22, 31, 45, 64)]
+    mols += [workloads.alkane(n, seed=520 + n) for n in (21, 33, 47, 60)]
+    res_p = batch_singlepoint([_calc(z, x) for z, x in mols])
+    assert batch_fallbacks() == 0
+    assert library.batch_projected() == len(mols)
+    try:
+        library.set_batch_density_solver("diagonalization")
+        res_d = batch_singlepoint([_calc(z, x) for z, x in mols])
+        assert library.batch_projected() == 0
+    finally:
+        library.set_batch_density_solver("purification")
+    for (z, x), rp_, rd in zip(mols, res_p, res_d):
+        _compare(rp_, rd)
+        assert np.max(np.abs(rp_.get("bond-orders") - rd.get("bond-orders"))) <= 1e-6
+        assert np.max(np.abs(rp_.get("orbital-energies") - rd.get("orbital-energies"))) <= 1e-6
+        assert np.max(np.abs(rp_.get("orbital-occupations")
+                             - rd.get("orbital-occupations"))) <= 1e-6
+    for (z, x), rp_ in list(zip(mols, res_p))[::3]:
+        _compare(rp_, _calc(z, x).singlepoint())
+
+
+def test_projection_small_gap_leaves_the_batch():
+    """A molecule whose final HOMO-LUMO gap is below 80 kT (here: a very high electronic
+    temperature makes kT large) cannot use 0/2 occupations; it leaves the batch and the
+    one-molecule path gives the reference's Fermi-smeared result."""
+    from tblite_gb300 import library, workloads
+    from tblite_gb300.interface import batch_fallbacks, batch_singlepoint
+
+    z, x = workloads.alkane(30, seed=540)
+    hot = {"temperature": 20000 * 3.166808578545117e-6}
+    res = batch_singlepoint([_calc(z, x, **hot), _calc(z, x)])
+    assert batch_fallbacks() == 1 and library.batch_projected() == 1
+    _compare(res[0], _calc(z, x, **hot).singlepoint())
+    _compare(res[1], _calc(z, x).singlepoint())
