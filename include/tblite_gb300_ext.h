@@ -47,6 +47,25 @@ int tblite_gb300_batch_last_fallbacks(void);
 void tblite_gb300_set_batch_density_solver(int mode);
 /* molecules of the last batch call whose SCF density came from the spectral projection */
 int tblite_gb300_batch_last_projected(void);
+/* Autotuner of the batch schedule: coordinate descent over the projection threshold (128, 160,
+ * 224 orbitals or off), the bucket cut (3/4, 2/3, 4/5 of the largest orbital count), the CTAs
+ * per SM of the cluster tridiagonalisation (1, 2) and the side streams (4, 8), each candidate
+ * timed as the wall time of a batch call (best of two) on a fixed pseudo-random sample of
+ * `sample` of the given molecules (256 if <= 0).  The fastest schedule stays set.  Returns the
+ * number of timed calls, -1 if the sample could not be evaluated. */
+int tblite_gb300_batch_autotune(tblite_context ctx, int nmol, const tblite_structure* mols,
+                                const tblite_calculator* calcs, int sample);
+/* the current batch schedule as text (written up to n - 1 characters); returns its length */
+int tblite_gb300_batch_schedule(char* buf, int n);
+/* back to the default batch schedule */
+void tblite_gb300_batch_reset_schedule(void);
+/* SCF iterations of a batch call as CUDA graphs (default 1): each iteration of a memory chunk
+ * (every bucket on every side stream) is captured, instantiated once and updated in place while
+ * its launch structure stays the same, and launched with one call.  Calls with the per-kernel
+ * profiler enabled launch directly.  _last_graphs reports the instantiations and graph launches
+ * of the last call (returns whether graphs are enabled). */
+void tblite_gb300_set_batch_graphs(int enable);
+int tblite_gb300_batch_last_graphs(int* builds, int* launches);
 /* device time (ms, CUDA events) of the last batch call from the first setup kernel to the end
  * of the gradient, summed over its memory chunks (uploads, read-back and the one-molecule
  * path excluded) */
@@ -182,6 +201,17 @@ unsigned long long tblite_gb300_get_split_gemm_flops(void);
  */
 int tblite_gb300_density_matrix_noalloc(int n, int k, const double* C, const double* f, double* P,
                                         void* stream);
+/* Test hooks of the failure paths (no GPU fault is caused by either):
+ * tblite_gb300_set_calculator_fault(ctx, calc, 1) makes every overlap factorisation of the
+ * calculator report a pivot that is not positive, as a singular overlap (coincident atoms)
+ * does: the single point fails with the reference's "(sygvd) failed to solve eigenvalue
+ * problem. info=<n+1>", a batch entry leaves the batch and fails the same way (0 clears it).
+ * tblite_gb300_set_pipeline_wait_limit(polls) sets how often a pipeline wait of the
+ * pipelined split GEMM polls before it aborts the tile (0: the default 2^22); a wait that runs
+ * out sets the status word (projection single point: an error; batch: the molecule takes the
+ * one-molecule path).  Returns 0, or -1 on a CUDA error. */
+void tblite_gb300_set_calculator_fault(tblite_context ctx, tblite_calculator calc, int kind);
+int tblite_gb300_set_pipeline_wait_limit(int polls);
 /* largest n*k the fixed workspace of tblite_gb300_density_matrix_noalloc holds */
 int tblite_gb300_density_matrix_noalloc_max(void);
 

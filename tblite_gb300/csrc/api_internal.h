@@ -189,6 +189,9 @@ struct _tblite_calculator {
   int param_grad = 0;
   // density solver: 0 diagonalisation (Fermi filling), 1 spectral projection (purify.cu)
   int density_solver = 0;
+  // fault injected on the host for tests: 1 = the overlap factorisation reports a pivot that is
+  // not positive (what a singular overlap, e.g. from coincident atoms, produces)
+  int fault = 0;
   // post-processing of every single point, in order ("bond-orders", "molmom"); an empty list
   // becomes the reference's default (bond orders and molecular moments) at the first single
   // point (api/calculator.f90:668-675)

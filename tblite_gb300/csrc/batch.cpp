@@ -84,8 +84,15 @@ std::mutex g_batch_mutex;
 Arena g_arena;
 int g_last_fallbacks = 0;
 int g_batch_streams = 8;  // side streams the size buckets are spread over
-bool g_batch_sp2 = true;  // closed shells of >= SP2_MIN_NAO orbitals: density by projection
+bool g_batch_sp2 = true;  // closed shells of >= g_sp2_min_nao orbitals: density by projection
+// schedule of the batch (set by hand or by tblite_gb300_batch_autotune): smallest orbital count
+// of the projection, and the bucket cut (a bucket ends below cut_num/cut_den of its largest)
+int g_sp2_min_nao = SP2_MIN_NAO;
+int g_cut_num = 3, g_cut_den = 4;
+std::string g_schedule_note = "defaults";
 int g_last_projected = 0;  // molecules of the last call whose SCF density came from projection
+bool g_batch_graphs = true;  // SCF iterations as CUDA graphs
+int g_last_graph_builds = 0, g_last_graph_launches = 0;  // of the last call
 double g_last_device_ms = 0.0;  // device time of the last call's batched steps (CUDA events)
 std::vector<int> g_last_iters;  // SCF iterations per molecule of the last call (0: not batched)
 
@@ -482,7 +489,8 @@ std::vector<Bucket> make_buckets(const std::vector<Plan>& plans) {
     b.sp2 = plans[i].sp2;
     const int top = plans[i].nao;
     int j = i;
-    while (j < np && 4 * plans[j].nao >= 3 * top && j - i < 65535 && plans[j].sp2 == b.sp2) {
+    while (j < np && g_cut_den * plans[j].nao >= g_cut_num * top && j - i < 65535 &&
+           plans[j].sp2 == b.sp2) {
       b.nat_max = std::max(b.nat_max, plans[j].nat);
       b.nsh_max = std::max(b.nsh_max, plans[j].nsh);
       b.nao_max = std::max(b.nao_max, plans[j].nao);
@@ -684,25 +692,68 @@ std::vector<int> run_chunk(std::vector<Plan>& plans, Arena& ar, _tblite_context*
     leave.push_back(i);
     if (plans[i].idx < (int)g_last_iters.size()) g_last_iters[plans[i].idx] = code;
   };
-  for (int i = 0; i < np; ++i)
+  for (int i = 0; i < np; ++i) {
+    if (plans[i].c->fault == 1) h_flag[i] = -2;  // injected: overlap not positive definite
     if (h_flag[i] < 0) {
       active[i] = 0;
       record_leave(i, h_flag[i]);
     }
+  }
   std::vector<char> done(np, 0);
   int max_iter = 0;
   for (auto& pl : plans) max_iter = std::max(max_iter, pl.max_iter);
   int iscf = 0;
   int nactive = upload_lists(active);
   auto t_iter = std::chrono::steady_clock::now();
+  // every SCF iteration of the whole chunk (all buckets, all side streams) as one CUDA graph:
+  // captured from the launch sequence, instantiated once and updated in place while the launch
+  // structure stays the same (lists and step budgets change only as molecules converge), then
+  // launched with one call; the per-kernel profiler's events are not captured, so a profiled
+  // call launches the kernels directly
+  const bool graphs = g_batch_graphs && !prof_enabled();
+  cudaGraphExec_t gexec = nullptr;
+  struct GraphGuard {
+    cudaGraphExec_t* e;
+    ~GraphGuard() {
+      if (*e) cudaGraphExecDestroy(*e);
+    }
+  } gguard{&gexec};
+  auto iteration = [&](auto&& body) {
+    if (!graphs) {
+      body();
+      return;
+    }
+    cuda_check(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed), "capture");
+    try {
+      body();
+    } catch (...) {
+      cudaGraph_t dropped = nullptr;
+      cudaStreamEndCapture(s, &dropped);
+      if (dropped) cudaGraphDestroy(dropped);
+      throw;
+    }
+    cudaGraph_t graph = nullptr;
+    cuda_check(cudaStreamEndCapture(s, &graph), "capture");
+    cudaGraphExecUpdateResultInfo info;
+    if (!gexec || cudaGraphExecUpdate(gexec, graph, &info) != cudaSuccess) {
+      cudaGetLastError();  // an update that does not fit is not an error: instantiate anew
+      if (gexec) cudaGraphExecDestroy(gexec);
+      gexec = nullptr;
+      cuda_check(cudaGraphInstantiate(&gexec, graph, 0), "graph instantiate");
+      ++g_last_graph_builds;
+    }
+    cudaGraphDestroy(graph);
+    cuda_check(cudaGraphLaunch(gexec, s), "graph launch");
+    ++g_last_graph_launches;
+  };
   while (nactive > 0 && iscf < max_iter) {
+    iteration([&]() {
     if (iscf > 0) {
       each([&](BatchLaunch& L) {
         launch_broyden_b(L, iscf);
         launch_unpack_b(L);
       });
     }
-    ++iscf;
     each([&](BatchLaunch& L) {
       launch_coulomb_potential_b(L, p);
       d4_potential_b(L);
@@ -725,6 +776,8 @@ std::vector<int> run_chunk(std::vector<Plan>& plans, Arena& ar, _tblite_context*
       d4_energy_b(L);
       launch_converge_b(L);
     });
+    });
+    ++iscf;
     cuda_check(cudaMemcpyAsync(h_flag.data(), d_flag, sizeof(int) * np, cudaMemcpyDeviceToHost, s),
                "flags");
     if (any_sp2)
@@ -979,7 +1032,7 @@ extern "C" int tblite_gb300_batch_singlepoint(tblite_context ctx, int nmol,
     pl.wbo_ch = c->wants("bond-orders") ? (pl.nalp != pl.nbet ? 2 : 1) : 0;
     pl.molmom = c->wants("molmom");
     // the projection needs a closed shell with a whole number of electron pairs
-    pl.sp2 = g_batch_sp2 && pl.nao >= SP2_MIN_NAO && pl.nalp == pl.nbet &&
+    pl.sp2 = g_batch_sp2 && pl.nao >= g_sp2_min_nao && pl.nalp == pl.nbet &&
              pl.nalp == std::floor(pl.nalp) && pl.nalp >= 1.0;
     if (pl.nao > tri_max || anneal || pl.max_iter < 1 || c->solv) {
       plain.push_back(i);
@@ -998,6 +1051,7 @@ extern "C" int tblite_gb300_batch_singlepoint(tblite_context ctx, int nmol,
     std::lock_guard<std::mutex> lock(g_batch_mutex);
     g_last_device_ms = 0.0;
     g_last_projected = 0;
+    g_last_graph_builds = g_last_graph_launches = 0;
     g_last_iters.assign(nmol, 0);
     prof_reset();
     // chunks of at most ~24 GB of device memory
@@ -1054,6 +1108,12 @@ extern "C" void tblite_gb300_set_tridiag_ctas_per_sm(int count) {
 }
 extern "C" void tblite_gb300_set_batch_density_solver(int mode) { g_batch_sp2 = mode != 0; }
 extern "C" int tblite_gb300_batch_last_projected(void) { return g_last_projected; }
+extern "C" void tblite_gb300_set_batch_graphs(int enable) { g_batch_graphs = enable != 0; }
+extern "C" int tblite_gb300_batch_last_graphs(int* builds, int* launches) {
+  if (builds) *builds = g_last_graph_builds;
+  if (launches) *launches = g_last_graph_launches;
+  return g_batch_graphs ? 1 : 0;
+}
 extern "C" void tblite_gb300_set_batch_streams(int count) {
   g_batch_streams = count < 1 ? 1 : (count > 8 ? 8 : count);
 }
@@ -1062,4 +1122,107 @@ extern "C" int tblite_gb300_batch_last_iterations(int* iterations, int nmol) {
   const int m = std::min(nmol, (int)g_last_iters.size());
   for (int i = 0; i < m && iterations; ++i) iterations[i] = g_last_iters[i];
   return (int)g_last_iters.size();
+}
+
+namespace tb {
+int get_tridiag_ctas_per_sm();
+}
+
+// back to the default schedule (projection from 128 orbitals, bucket cut 3/4, two CTAs per SM,
+// 8 streams)
+extern "C" void tblite_gb300_batch_reset_schedule(void) {
+  g_sp2_min_nao = SP2_MIN_NAO;
+  g_cut_num = 3;
+  g_cut_den = 4;
+  tb::set_tridiag_ctas_per_sm(2);
+  g_batch_streams = 8;
+  g_schedule_note = "defaults";
+}
+
+// The batch schedule: projection threshold, bucket cut, CTAs per SM of the cluster
+// tridiagonalisation and side streams, as a short text for logs and benchmark records.
+extern "C" int tblite_gb300_batch_schedule(char* buf, int n) {
+  char tmp[256];
+  const int len = std::snprintf(
+      tmp, sizeof(tmp),
+      "projection from %d orbitals%s; bucket cut %d/%d; tridiagonalisation %d CTA(s) per SM; "
+      "%d streams; %s",
+      g_sp2_min_nao, g_batch_sp2 ? "" : " (off)", g_cut_num, g_cut_den,
+      tb::get_tridiag_ctas_per_sm(), g_batch_streams, g_schedule_note.c_str());
+  if (buf && n > 0) {
+    std::strncpy(buf, tmp, (size_t)n - 1);
+    buf[n - 1] = '\0';
+  }
+  return len;
+}
+
+// Autotuner of the batch schedule (no counterpart in the reference): coordinate descent over the
+// projection threshold, the bucket cut, the CTAs per SM of the tridiagonalisation and the side
+// streams, each candidate timed (wall time of the call, best of two) on a seeded sample of the given
+// molecules; the fastest schedule stays set.  Returns the number of timed calls, or -1 if the
+// sample could not be evaluated (the schedule is then left as it was).
+extern "C" int tblite_gb300_batch_autotune(tblite_context ctx, int nmol,
+                                           const tblite_structure* mols,
+                                           const tblite_calculator* calcs, int sample) {
+  if (!ctx || nmol <= 0 || !mols || !calcs) return -1;
+  std::vector<int> idx(nmol);
+  std::iota(idx.begin(), idx.end(), 0);
+  unsigned long long state = 0x9E3779B97F4A7C15ull;  // fixed seed: the same sample every time
+  for (int i = nmol - 1; i > 0; --i) {             // Fisher-Yates with a 64-bit LCG
+    state = state * 6364136223846793005ull + 1442695040888963407ull;
+    std::swap(idx[i], idx[(int)((state >> 33) % (unsigned long long)(i + 1))]);
+  }
+  const int k = std::max(1, std::min(nmol, sample > 0 ? sample : 256));
+  std::vector<tblite_structure> sm(k);
+  std::vector<tblite_calculator> sc(k);
+  std::vector<_tblite_result> rs(k);
+  std::vector<tblite_result> sr(k);
+  for (int i = 0; i < k; ++i) {
+    sm[i] = mols[idx[i]];
+    sc[i] = calcs[idx[i]];
+    sr[i] = &rs[i];
+  }
+  _tblite_context quiet;
+  quiet.verbosity = 0;
+  int calls = 0;
+  auto time_it = [&]() {
+    double best = 1e300;
+    for (int r = 0; r < 2; ++r) {
+      quiet.errors.clear();
+      // wall time of the whole call: molecules handed to the one-molecule path count too
+      const auto t0 = std::chrono::steady_clock::now();
+      if (tblite_gb300_batch_singlepoint(&quiet, k, sm.data(), sc.data(), sr.data(), nullptr) != 0)
+        return -1.0;
+      const auto t1 = std::chrono::steady_clock::now();
+      ++calls;
+      best = std::min(best, std::chrono::duration<double, std::milli>(t1 - t0).count());
+    }
+    return best;
+  };
+  const int sp2_keep = g_sp2_min_nao, num_keep = g_cut_num, den_keep = g_cut_den,
+            ctas_keep = tb::get_tridiag_ctas_per_sm(), streams_keep = g_batch_streams;
+  double best = time_it();
+  if (best < 0) return -1;
+  auto try_values = [&](auto set, const std::vector<int>& values, int& keep) {
+    for (int v : values) {
+      if (v == keep) continue;
+      set(v);
+      const double t = time_it();
+      if (t >= 0 && t < best) {
+        best = t;
+        keep = v;
+      }
+    }
+    set(keep);
+  };
+  int sp2 = sp2_keep, cut = num_keep * 10 + den_keep, ctas = ctas_keep, streams = streams_keep;
+  try_values([](int v) { g_sp2_min_nao = v; }, {128, 160, 224, 100000}, sp2);
+  try_values([](int v) { g_cut_num = v / 10; g_cut_den = v % 10; }, {34, 23, 45}, cut);
+  try_values([](int v) { tb::set_tridiag_ctas_per_sm(v); }, {1, 2}, ctas);
+  try_values([](int v) { g_batch_streams = v; }, {4, 8}, streams);
+  char note[96];
+  std::snprintf(note, sizeof(note), "autotuned on %d molecules (%d calls, %.1f ms)", k, calls,
+                best);
+  g_schedule_note = note;
+  return calls;
 }

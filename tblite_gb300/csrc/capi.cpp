@@ -334,6 +334,18 @@ Gfn2Scalars gfn2_scalars(const _tblite_calculator* c) {
 // --------------------------------------------------------------------------------------
 // single point driver
 // --------------------------------------------------------------------------------------
+// a failed projection step: report a tensor-core wait that ran out (the status word of the
+// split GEMMs) before the numerical failure it caused
+static void pipeline_check(Workspace& w) {
+  if (!w.pur) return;
+  stream_wait(w.stream);
+  int st = 0;
+  cuda_check(cudaMemcpy(&st, purify_status(w.pur), sizeof(int), cudaMemcpyDeviceToHost),
+             "purify status");
+  if (st != 0)
+    throw std::runtime_error("tensor-core matrix product did not complete (wait limit reached)");
+}
+
 static void ensure_workspace(_tblite_calculator* c) {
   if (!c->ws) {
     c->ws.reset(new Workspace());
@@ -730,6 +742,7 @@ struct Profiler {
 static Profiler g_prof;
 namespace tb {
 int prof_kbegin(cudaStream_t s) { return g_prof.kbegin(s); }
+bool prof_enabled() { return g_prof.enabled; }
 void prof_kend(int slot, int token, cudaStream_t s) { g_prof.kend(slot, token, s); }
 void prof_reset() { g_prof.reset(); }
 void prof_collect() { g_prof.collect(); }
@@ -816,9 +829,17 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
   if (purify) chol = purify_set_overlap(w.pur, w.S.p) < 0 ? 1 : 0;
   else chol = eigen_set_overlap(w.eig, w.S.p);
   g_prof.end(s);
-  if (chol != 0)
-    throw std::runtime_error(purify ? "overlap orthogonalisation (Newton-Schulz) did not converge"
-                                    : "overlap matrix is not positive definite");
+  if (c->fault == 1) chol = 1;  // injected: the first pivot is not positive
+  if (chol != 0) {
+    if (purify) {
+      pipeline_check(w);
+      throw std::runtime_error("overlap orthogonalisation (Newton-Schulz) did not converge");
+    }
+    // LAPACK's convention for sygvd (lapack/sygvd.f90:153-161): info = n + i when the leading
+    // minor of order i of the overlap is not positive definite
+    throw std::runtime_error("(sygvd) failed to solve eigenvalue problem. info=" +
+                             std::to_string((long long)n + chol));
+  }
 
   // initial guess: restart from a compatible result, else SAD (wavefunction/guess.f90:51-120)
   std::vector<double> qsh0(nsh), dp0(3 * nat, 0.0), qp0(6 * nat, 0.0), qat0(nat);
@@ -918,8 +939,10 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
     g_prof.end(s);
     if (purify) {  // P from the Fock matrix by products alone; 0/1 occupations carry no entropy
       g_prof.begin(PH_DENSITY, s);
-      if (purify_density(w.pur, w.F.p, nocc, w.P.p) < 0)
+      if (purify_density(w.pur, w.F.p, nocc, w.P.p) < 0) {
+        pipeline_check(w);
         throw std::runtime_error("spectral projection (SP2) did not converge");
+      }
       cuda_check(cudaMemsetAsync(w.scal.p, 0, sizeof(double), s), "ts");
       g_prof.end(s);
     } else {
@@ -1989,6 +2012,18 @@ tblite_calculator tblite_new_xtb_calculator(tblite_context ctx, tblite_structure
     return nullptr;
   }
   return c;
+}
+void tblite_gb300_set_calculator_fault(tblite_context ctx, tblite_calculator calc, int kind) {
+  if (!ctx) return;
+  if (!calc) {
+    ctx->push("Calculator object is missing");
+    return;
+  }
+  if (kind < 0 || kind > 1) {
+    ctx->push("fault kind must be 0 (none) or 1 (overlap not positive definite)");
+    return;
+  }
+  calc->fault = kind;
 }
 tblite_calculator tblite_new_ipea1_calculator(tblite_context ctx, tblite_structure mol,
                                              tblite_xtb_config* config) {

@@ -1017,6 +1017,8 @@ int cholesky_inverse(int n, double* L, double* X, int* d_status, int* h_status, 
 
 int eigen_set_overlap(EigenSolver* e, const double* S) {
   const int n = e->n;
+  // a new geometry: the tensor-core status word starts clear
+  ck(cudaMemsetAsync(e->gstatus, 0, sizeof(int), e->stream), "gstatus");
   ck(cudaMemcpyAsync(e->L, S, sizeof(double) * (size_t)n * n, cudaMemcpyDeviceToDevice, e->stream),
      "copy S");
   return cholesky_inverse(n, e->L, e->X, e->status, e->hstatus, e->stream);
@@ -1474,6 +1476,7 @@ static int tridiag_cluster(int n, size_t* smem) {
   return 0;
 }
 void set_tridiag_ctas_per_sm(int k) { g_tridiag_ctas_per_sm = k >= 2 ? 2 : 1; }
+int get_tridiag_ctas_per_sm() { return g_tridiag_ctas_per_sm; }
 int batch_tridiag_max_n() {
   int n = 1;
   size_t sm = 0;

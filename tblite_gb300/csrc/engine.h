@@ -37,6 +37,7 @@ enum { KS_TRIDIAG = 0, KS_MULTISECT, KS_INVIT, KS_BACKTRANSFORM, KS_GEMM, KS_FOC
 int prof_kbegin(cudaStream_t s);
 void prof_kend(int slot, int token, cudaStream_t s);
 void prof_reset();    // clear the kernel and phase records
+bool prof_enabled();  // per-kernel events are being recorded
 void prof_collect();  // after a stream wait: turn the recorded events into times
 
 constexpr int MAXG = 12;    // max primitives per shell

@@ -284,9 +284,15 @@ __device__ __forceinline__ bool ogemm_body(const Site& s, const int* __restrict_
                    ::"r"(smem_u32(&mbar)) : "memory");
     }
     ok = __syncthreads_and(mbar_wait(smem_u32(&mbar), phase) ? 1 : 0) != 0;
+    if (!ok) {
+      // the MMAs of this chunk have not reported back: wait for them once more (bounded) so
+      // that TMEM is not released under MMAs still in flight, then give up on the tile
+      __syncthreads_and(mbar_wait(smem_u32(&mbar), phase) ? 1 : 0);
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      break;
+    }
     phase ^= 1u;
     asm volatile("tcgen05.fence::after_thread_sync;");
-    if (!ok) break;
     ++nchunk;
     const bool flush = (nchunk % OZ_FLUSH) == 0 || k0 + OZ_KC >= kend;
     if (flush) {

@@ -51,6 +51,11 @@ constexpr int PP_TMEM_COLS = 512;
 static_assert(PP_LEVELS * PP_N == PP_TMEM_COLS, "one 64-column accumulator per level");
 constexpr int PP_GROUP = 8;  // row blocks per tile group
 constexpr int PP_WAIT = 1 << 22;
+// polls of a pipeline wait (stage full / empty, accumulators ready / free) before it gives up
+// and aborts the tile; the drains of copies and MMAs in flight after an abort always use
+// PP_WAIT.  Settable for tests (tblite_gb300_set_pipeline_wait_limit) so that a wait runs out
+// and the abort path, the status word and the hand-off can be checked.
+__device__ int g_pipe_wait_limit = PP_WAIT;
 
 void ck(cudaError_t e, const char* what) {
   if (e != cudaSuccess)
@@ -79,7 +84,8 @@ __device__ __forceinline__ bool try_wait(uint32_t bar, uint32_t parity) {
 }
 // bounded wait; gives up early once another role has aborted (abort != nullptr)
 __device__ __forceinline__ bool wait_bar(uint32_t bar, uint32_t parity, volatile int* abort) {
-  for (int it = 0; it < PP_WAIT; ++it) {
+  const int limit = abort ? g_pipe_wait_limit : PP_WAIT;
+  for (int it = 0; it < limit; ++it) {
     if (try_wait(bar, parity)) return true;
     if (abort && *abort) return false;
   }
@@ -609,3 +615,10 @@ extern "C" int tblite_gb300_split_gemm(int m, int n, int k, const double* a, con
 }
 
 extern "C" void tblite_gb300_set_pipelined_gemm(int enable) { tb::g_pipe_gemm = enable != 0; }
+
+// test setting: polls of the pipelined split GEMM's pipeline waits on the current device (0:
+// the default 2^22).  0 on success, -1 on a CUDA error.
+extern "C" int tblite_gb300_set_pipeline_wait_limit(int polls) {
+  const int v = polls > 0 ? polls : tb::PP_WAIT;
+  return cudaMemcpyToSymbol(tb::g_pipe_wait_limit, &v, sizeof(int)) == cudaSuccess ? 0 : -1;
+}

@@ -425,6 +425,9 @@ int purify_set_overlap(Purifier* p, const double* S) {
   const int n = p->n;
   const size_t nn = (size_t)n * n;
   const int eb = ew_blocks(nn);
+  // a new geometry: the status word of the split GEMMs starts clear (a wait that ran out in an
+  // earlier single point was reported there)
+  ck(cudaMemsetAsync(p->status, 0, sizeof(int), p->s), "purify status");
   bounds(p, S);
   double *Y = p->A, *Z = p->Z, *Yn = p->X, *Zn = p->X2;
   ++g_kernel_launches;

@@ -121,7 +121,15 @@ _SIGNATURES = {
         c_int, [c_void_p, c_int, POINTER(c_void_p), POINTER(c_void_p), POINTER(c_void_p), _int_p]),
     "tblite_gb300_batch_last_fallbacks": (c_int, []),
     "tblite_gb300_set_batch_density_solver": (None, [c_int]),
+    "tblite_gb300_set_calculator_fault": (None, [c_void_p, c_void_p, c_int]),
+    "tblite_gb300_set_pipeline_wait_limit": (c_int, [c_int]),
     "tblite_gb300_batch_last_projected": (c_int, []),
+    "tblite_gb300_batch_autotune": (c_int, [c_void_p, c_int, POINTER(c_void_p), POINTER(c_void_p),
+                                            c_int]),
+    "tblite_gb300_batch_schedule": (c_int, [c_char_p, c_int]),
+    "tblite_gb300_batch_reset_schedule": (None, []),
+    "tblite_gb300_set_batch_graphs": (None, [c_int]),
+    "tblite_gb300_batch_last_graphs": (c_int, [_int_p, _int_p]),
     "tblite_gb300_batch_last_device_ms": (c_double, []),
     "tblite_gb300_batch_last_iterations": (c_int, [_int_p, c_int]),
 }
@@ -209,6 +217,43 @@ def set_batch_density_solver(solver: str) -> None:
     if not isinstance(code, int):
         raise TBLiteValueError(f"Unknown density solver '{solver}'")
     load().tblite_gb300_set_batch_density_solver(code)
+
+
+def batch_autotune(calculators, sample: int = 256) -> int:
+    """Tune the batch schedule on a sample of these calculators' molecules (see
+    tblite_gb300_batch_autotune); returns the number of timed calls."""
+    lib = load()
+    calcs = list(calculators)
+    n = len(calcs)
+    mols = (c_void_p * n)(*[c._mol.value for c in calcs])
+    hcalc = (c_void_p * n)(*[c._calc.value for c in calcs])
+    ctx = new_context(verbosity=0)
+    try:
+        rc = lib.tblite_gb300_batch_autotune(ctx, n, mols, hcalc, int(sample))
+    finally:
+        lib.tblite_delete_context(byref(ctx))
+    if rc < 0:
+        raise TBLiteRuntimeError("batch autotuning failed on its sample")
+    return rc
+
+
+def batch_schedule() -> str:
+    """The current batch schedule as text."""
+    buf = ctypes.create_string_buffer(512)
+    load().tblite_gb300_batch_schedule(buf, 512)
+    return buf.value.decode()
+
+
+def set_batch_graphs(enable: bool) -> None:
+    """Run the batched SCF iterations as CUDA graphs (default) or launch kernels directly."""
+    load().tblite_gb300_set_batch_graphs(1 if enable else 0)
+
+
+def batch_graphs():
+    """(instantiations, graph launches) of the last batch call."""
+    b, n = c_int(0), c_int(0)
+    load().tblite_gb300_batch_last_graphs(byref(b), byref(n))
+    return b.value, n.value
 
 
 def batch_projected() -> int:

@@ -203,3 +203,48 @@ def test_projection_small_gap_leaves_the_batch():
     assert batch_fallbacks() == 1 and library.batch_projected() == 1
     _compare(res[0], _calc(z, x, **hot).singlepoint())
     _compare(res[1], _calc(z, x).singlepoint())
+
+
+def test_autotuned_schedule_keeps_results():
+    """The autotuner times candidate schedules on a sample and keeps the fastest; results
+    under the tuned schedule agree with the one-molecule path."""
+    from tblite_gb300 import library, workloads
+    from tblite_gb300.interface import batch_singlepoint
+
+    mols = workloads.mixed_ensemble(48, seed=77)
+    calcs = [_calc(z, x) for z, x in mols]
+    before = library.batch_schedule()
+    try:
+        assert library.batch_autotune(calcs, sample=24) > 0
+        assert "autotuned on 24 molecules" in library.batch_schedule()
+        res = batch_singlepoint(calcs)
+        for (z, x), r in list(zip(mols, res))[::6]:
+            _compare(r, _calc(z, x).singlepoint())
+    finally:
+        # back to the defaults for the other tests
+        library.set_batch_streams(8)
+        library.set_tridiag_ctas_per_sm(2)
+        library.load().tblite_gb300_batch_reset_schedule()
+    assert library.batch_schedule() == before
+
+
+def test_scf_iterations_as_cuda_graphs():
+    """The batched SCF iterations run as CUDA graphs (captured, updated in place, one launch
+    per iteration and memory chunk); launching the kernels directly gives the same results."""
+    from tblite_gb300 import library, workloads
+    from tblite_gb300.interface import batch_singlepoint
+
+    mols = workloads.mixed_ensemble(40, seed=88)
+    library.set_profiling(False)
+    res_g = batch_singlepoint([_calc(z, x) for z, x in mols])
+    builds, launches = library.batch_graphs()
+    assert launches > 0 and 0 < builds <= launches
+    try:
+        library.set_batch_graphs(False)
+        res_d = batch_singlepoint([_calc(z, x) for z, x in mols])
+        assert library.batch_graphs() == (0, 0)
+    finally:
+        library.set_batch_graphs(True)
+    for a, b in zip(res_g, res_d):
+        assert abs(a.get("energy") - b.get("energy")) <= 1e-12
+        assert np.max(np.abs(a.get("gradient") - b.get("gradient"))) <= 1e-12
