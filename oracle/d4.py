@@ -26,6 +26,24 @@ from oracle.gfn2 import _elem, _p, lib
 MREF = 7
 
 
+def pair_c6(d4, za, zb):
+    """nref(za) x nref(zb) reference C6 matrix of an element pair from the pack (stored once
+    per unordered pair as "Za-Zb", Za <= Zb)."""
+    if za <= zb:
+        return np.array(d4["c6"][f"{za}-{zb}"], dtype=float)
+    return np.array(d4["c6"][f"{zb}-{za}"], dtype=float).T
+
+
+def species_c6(d4, species, nref):
+    """[nsp, MREF, nsp, MREF] reference C6 of the species pairs, zero beyond nref."""
+    nsp = len(species)
+    out = np.zeros((nsp, MREF, nsp, MREF))
+    for a, za in enumerate(species):
+        for b, zb in enumerate(species):
+            out[a, :nref[a], b, :nref[b]] = pair_c6(d4, za, zb)
+    return out
+
+
 class D4:
     def __init__(self, calc, st):
         self.calc = calc
@@ -44,18 +62,16 @@ class D4:
         self.refcn = np.zeros((nsp, MREF))
         self.refq = np.zeros((nsp, MREF))
         self.ngw = np.zeros((nsp, MREF), dtype=int)
-        c6b = np.zeros((nsp, MREF))
         for k, s in enumerate(species):
             nr = self.nref[k]
             self.refcn[k, :nr] = _elem(d4, "refcn", s)
             self.refq[k, :nr] = _elem(d4, "refq", s)
             self.ngw[k, :nr] = _elem(d4, "ngw", s)
-            c6b[k, :nr] = _elem(d4, "refc6", s)
-        # reference C6 table: synthetic combining rule sqrt(c6_r c6_s)
-        self.c6ref = np.zeros((nsp, MREF, nsp, MREF))
-        for a in range(nsp):
-            for b in range(nsp):
-                self.c6ref[a, :, b, :] = np.sqrt(np.outer(c6b[a], c6b[b]))
+        if d4.get("width2", 0.0) != 0.0 or d4.get("width3", 0.0) != 0.0:
+            raise ValueError("smooth dispersion cutoffs are not restated (widths must be 0)")
+        # reference C6 per species pair from the pack's per-element-pair table, the layout of
+        # dftd4's c6(iref, jref, izp, jzp) read by disp/d4.f90:410-413
+        self.c6ref = species_c6(d4, species, self.nref)
         self.zeff = np.array([_elem(d4, "zeff", s) for s in species])[self.sp]
         self.gam = np.array([_elem(d4, "gam", s) for s in species])[self.sp]
         self.r4r2 = np.array([_elem(d4, "r4r2", s) for s in species])[self.sp]

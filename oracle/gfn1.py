@@ -227,19 +227,28 @@ class D3:
         self.cut = d3["disp2_cutoff"]
         self.xyz = xyz
         nat = len(z)
-        self.a = np.zeros(nat)
-        self.da = np.zeros(nat)
+        self.z = [int(v) for v in z]
+        self.d4 = d4
+        # normalised Gaussian weights of the reference CNs and their CN derivatives
+        self.w, self.dw = [], []
         for i in range(nat):
             refcn = np.array(d4["refcn"][str(z[i])])
-            s = np.sqrt(np.array(d4["refc6"][str(z[i])]))
             w = np.exp(-d3["k3"] * (self.cn[i] - refcn) ** 2)
             dw = -2.0 * d3["k3"] * (self.cn[i] - refcn) * w
             norm = w.sum()
-            self.a[i] = (w * s).sum() / norm
-            self.da[i] = ((dw * s).sum() * norm - (w * s).sum() * dw.sum()) / norm ** 2
+            self.w.append(w / norm)
+            self.dw.append((dw * norm - w * dw.sum()) / norm ** 2)
+
+    def _c6(self, i, j):
+        """C6 of the pair (i, j) = sum_rs w_ir w_js C6ref(r, s) and its CN_i, CN_j derivatives"""
+        from oracle.d4 import pair_c6
+
+        t = pair_c6(self.d4, self.z[i], self.z[j])
+        return (self.w[i] @ t @ self.w[j], self.dw[i] @ t @ self.w[j],
+                self.w[i] @ t @ self.dw[j])
 
     def energy_gradient(self, gradient=None, sigma=None):
-        nat = len(self.a)
+        nat = len(self.w)
         e = np.zeros(nat)
         dedcn = np.zeros(nat)
         xyz = self.xyz
@@ -249,7 +258,7 @@ class D3:
                 r = np.linalg.norm(v)
                 if r > self.cut:
                     continue
-                c6 = self.a[i] * self.a[j]
+                c6, dc6i, dc6j = self._c6(i, j)
                 q = 3.0 * self.r4r2[i] * self.r4r2[j]
                 r0 = self.a1 * math.sqrt(q) + self.a2
                 t6 = 1.0 / (r ** 6 + r0 ** 6)
@@ -265,8 +274,8 @@ class D3:
                     if sigma is not None:
                         sigma += np.outer(g, v)
                     dedc6 = -(self.s6 * t6 + self.s8 * q * t8)
-                    dedcn[i] += dedc6 * self.da[i] * self.a[j]
-                    dedcn[j] += dedc6 * self.a[i] * self.da[j]
+                    dedcn[i] += dedc6 * dc6i
+                    dedcn[j] += dedc6 * dc6j
         if gradient is not None:
             gradient += np.einsum("i,ikx->kx", dedcn, self.dcn)
             if sigma is not None:

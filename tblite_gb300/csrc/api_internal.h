@@ -107,7 +107,8 @@ struct Workspace {
   DBuf<double> wbo, ones, pgrad, zgrad;
   // GFN1 per-shell/atom data and D3 dispersion (data and work)
   DBuf<int> sh_valence, d3_nref;
-  DBuf<double> at_gam3, d3_refcn, d3_sref, d3_r4r2, d3_rcov, d3_cn, d3_a, d3_da, d3_dEdcn;
+  DBuf<double> at_gam3, d3_refcn, d3_c6ref, d3_r4r2, d3_rcov, d3_cn, d3_w, d3_dw, d3_dEdcn;
+  DBuf<int> d3_sp;
   // implicit solvation: per-atom model arrays [9][nat], grid [230][4], work [4][nat]
   DBuf<double> sv_atom, sv_grid, sv_work;
   DBuf<int> sv_nbl, sv_nnb, sv_status;
@@ -162,7 +163,9 @@ struct _tblite_calculator {
   // D3 data per atom (GFN1, molecules with pairs)
   bool has_d3 = false;
   std::vector<int> d3_nref;
-  std::vector<double> d3_refcn, d3_sref, d3_r4r2, d3_rcov;
+  int d3_nsp = 0;
+  std::vector<int> d3_sp;
+  std::vector<double> d3_refcn, d3_c6ref, d3_r4r2, d3_rcov;
   // D4 data per atom (empty for a single atom: no pairs, no dispersion)
   bool has_d4 = false;
   int d4_nsp = 0;

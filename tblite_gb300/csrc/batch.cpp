@@ -129,7 +129,7 @@ struct Plan {
   Piece xyz, at_z, at_sh, sh_atom, sh_l, sh_nprim, sh_alpha, sh_coeff, sh_ao, ao_sh, ao_at, sh_se0,
       sh_kcn, sh_shpoly, sh_zeta, sh_hub, sh_gam3, sh_refocc, at_en, at_rad, at_rcov, at_mprad,
       at_vcn, at_dkern, at_qkern, at_repa, at_repz, sh_valence, at_gam3;
-  Piece d3_nref, d3_refcn, d3_sref, d3_r4r2, d3_rcov, d3_cn, d3_a, d3_da, d3_dEdcn;
+  Piece d3_sp, d3_nref, d3_refcn, d3_c6ref, d3_r4r2, d3_rcov, d3_cn, d3_w, d3_dw, d3_dEdcn;
   Piece d4_sp, d4_nref, d4_ngw, d4_refcn, d4_refq, d4_zeff, d4_gam, d4_r4r2, d4_rcov, d4_en,
       d4_c6ref;
   Piece d4_cn, d4_gw, d4_dgw, d4_gwv, d4_dgwdq, d4_dgwv_cn, d4_c6, d4_dc6, d4_e3, d4_dEdcn, d4_atm;
@@ -185,10 +185,12 @@ void layout(Plan& pl, Region* R) {
   if (pl.has_d3) {
     pl.d3_nref = piece<int>(R, RU, na);
     pl.d3_refcn = piece<double>(R, RU, na * D4_MREF);
-    pl.d3_sref = piece<double>(R, RU, na * D4_MREF);
+    pl.d3_sp = piece<int>(R, RU, na);
+    pl.d3_c6ref = piece<double>(R, RU, pl.c->d3_c6ref.size());
     pl.d3_r4r2 = piece<double>(R, RU, na);
     pl.d3_rcov = piece<double>(R, RU, na);
-    for (Piece* p : {&pl.d3_cn, &pl.d3_a, &pl.d3_da, &pl.d3_dEdcn}) *p = piece<double>(R, RS, na);
+    for (Piece* p : {&pl.d3_cn, &pl.d3_dEdcn}) *p = piece<double>(R, RS, na);
+    for (Piece* p : {&pl.d3_w, &pl.d3_dw}) *p = piece<double>(R, RS, na * D4_MREF);
   }
   if (pl.has_d4) {
     pl.d4_sp = piece<int>(R, RU, na);
@@ -330,14 +332,16 @@ MolPtrs make_ptrs(const Plan& pl, const Bases& db) {
   if (pl.has_d3) {
     DevD3& d = q.d3;
     d3_model_constants(d, pl.c);
+    d.nsp = pl.c->d3_nsp;
+    d.sp = db.at<int>(pl.d3_sp);
     d.nref = db.at<int>(pl.d3_nref);
     d.refcn = db.at<double>(pl.d3_refcn);
-    d.sref = db.at<double>(pl.d3_sref);
+    d.c6ref = db.at<double>(pl.d3_c6ref);
     d.r4r2 = db.at<double>(pl.d3_r4r2);
     d.rcov = db.at<double>(pl.d3_rcov);
     d.cn = db.at<double>(pl.d3_cn);
-    d.a = db.at<double>(pl.d3_a);
-    d.da = db.at<double>(pl.d3_da);
+    d.w = db.at<double>(pl.d3_w);
+    d.dw = db.at<double>(pl.d3_dw);
     d.dEdcn = db.at<double>(pl.d3_dEdcn);
   }
   if (pl.has_d4) {
@@ -572,7 +576,8 @@ std::vector<int> run_chunk(std::vector<Plan>& plans, Arena& ar, _tblite_context*
     if (pl.has_d3) {
       stage(hb, pl.d3_nref, c->d3_nref);
       stage(hb, pl.d3_refcn, c->d3_refcn);
-      stage(hb, pl.d3_sref, c->d3_sref);
+      stage(hb, pl.d3_sp, c->d3_sp);
+      stage(hb, pl.d3_c6ref, c->d3_c6ref);
       stage(hb, pl.d3_r4r2, c->d3_r4r2);
       stage(hb, pl.d3_rcov, c->d3_rcov);
     }

@@ -62,8 +62,44 @@ static void slater_to_gauss(int ng, int n, int l, double zeta, double* alpha, do
     coeff[k] = coeff[k] * pow(top * alpha[k], 0.75) * pow(sqrt(4 * alpha[k]), l) / sqrt(dfac[l]);
 }
 
+// reference C6 of reference r of element za with reference q of element zb, from the pack's
+// per-pair table (stored once per unordered pair); NaN if the pack has no entry for the pair
+static double pack_c6(int za, int r, int zb, int q) {
+  if (za > zb) {
+    std::swap(za, zb);
+    std::swap(r, q);
+  }
+  const int off = EXT_D4_C6OFF[(za - 1) * 86 + zb - 1];
+  return off < 0 ? NAN : EXT_D4_C6PAIR[off + r * EXT_D4_NREF[zb - 1] + q];
+}
+
+// the dispersion models' species tables: per-species-pair reference C6 [nsp][MREF][nsp][MREF]
+// from the pack (zero outside the species' reference counts); throws if a pair is missing
+static void species_c6(const std::vector<int>& species, std::vector<double>& c6ref) {
+  const int nsp = (int)species.size(), ld = nsp * D4_MREF;
+  c6ref.assign((size_t)ld * ld, 0.0);
+  for (int a = 0; a < nsp; ++a)
+    for (int b = 0; b < nsp; ++b)
+      for (int r = 0; r < EXT_D4_NREF[species[a] - 1]; ++r)
+        for (int q = 0; q < EXT_D4_NREF[species[b] - 1]; ++q) {
+          const double v = pack_c6(species[a], r, species[b], q);
+          if (std::isnan(v))
+            throw std::runtime_error(std::string("element data pack '") + EXT_PACK_NAME +
+                                     "' has no reference C6 for the element pair Z=" +
+                                     std::to_string(species[a]) + ", Z=" +
+                                     std::to_string(species[b]));
+          c6ref[(size_t)(a * D4_MREF + r) * ld + b * D4_MREF + q] = v;
+        }
+}
+
 // D4 model data of the molecule's species (element-data pack)
 static void build_d4_data(_tblite_calculator* c, const _tblite_structure* mol) {
+  // the reference builds its D4 model with the default smooth-cutoff widths of 0 (hard cutoffs,
+  // disp/d4.f90:71-72); a pack asking for smooth cutoffs needs dftd4's switching function
+  if (EXT_D4_WIDTH2 != 0.0 || EXT_D4_WIDTH3 != 0.0)
+    throw std::runtime_error(std::string("element data pack '") + EXT_PACK_NAME +
+                             "' asks for smooth dispersion cutoffs, which the GPU engine does "
+                             "not provide");
   std::vector<int> species;
   for (int z : mol->num)
     if (std::find(species.begin(), species.end(), z) == species.end()) species.push_back(z);
@@ -88,33 +124,28 @@ static void build_d4_data(_tblite_calculator* c, const _tblite_structure* mol) {
     c->d4_rcov.push_back(EXT_D4_RCOV[z - 1]);
     c->d4_en.push_back(EXT_D4_EN[z - 1]);
   }
-  const int nsp = c->d4_nsp, ld = nsp * D4_MREF;
-  c->d4_c6ref.assign((size_t)ld * ld, 0.0);
-  for (int a = 0; a < nsp; ++a)
-    for (int r = 0; r < EXT_D4_NREF[species[a] - 1]; ++r)
-      for (int b = 0; b < nsp; ++b)
-        for (int q = 0; q < EXT_D4_NREF[species[b] - 1]; ++q)
-          c->d4_c6ref[(size_t)(a * D4_MREF + r) * ld + b * D4_MREF + q] =
-              sqrt(EXT_D4_REFC6[(species[a] - 1) * D4_MREF + r] *
-                   EXT_D4_REFC6[(species[b] - 1) * D4_MREF + q]);
+  species_c6(species, c->d4_c6ref);
 }
 
 // D3 data of the molecule's atoms (element-data pack)
 static void build_d3_data(_tblite_calculator* c, const _tblite_structure* mol) {
   c->has_d3 = true;
+  std::vector<int> species;
+  for (int z : mol->num)
+    if (std::find(species.begin(), species.end(), z) == species.end()) species.push_back(z);
+  c->d3_nsp = (int)species.size();
   for (int i = 0; i < mol->nat; ++i) {
     const int z = mol->num[i];
     if (EXT_D4_NREF[z - 1] <= 0 || std::isnan(EXT_D4_R4R2[z - 1]) || std::isnan(EXT_D4_RCOV[z - 1]))
       throw std::runtime_error(std::string("element data pack '") + EXT_PACK_NAME +
                                "' has no D3 data for Z=" + std::to_string(z));
+    c->d3_sp.push_back((int)(std::find(species.begin(), species.end(), z) - species.begin()));
     c->d3_nref.push_back(EXT_D4_NREF[z - 1]);
-    for (int r = 0; r < D4_MREF; ++r) {
-      c->d3_refcn.push_back(EXT_D4_REFCN[(z - 1) * D4_MREF + r]);
-      c->d3_sref.push_back(sqrt(EXT_D4_REFC6[(z - 1) * D4_MREF + r]));
-    }
+    for (int r = 0; r < D4_MREF; ++r) c->d3_refcn.push_back(EXT_D4_REFCN[(z - 1) * D4_MREF + r]);
     c->d3_r4r2.push_back(EXT_D4_R4R2[z - 1]);
     c->d3_rcov.push_back(EXT_D4_RCOV[z - 1]);
   }
+  species_c6(species, c->d3_c6ref);
 }
 
 static void orthogonalize_s(int ni, const double* ai, const double* ci, int& nj, double* aj,
@@ -389,10 +420,12 @@ static void ensure_workspace(_tblite_calculator* c) {
     if (c->has_d3) {
       w.d3_nref.upload(c->d3_nref, s);
       w.d3_refcn.upload(c->d3_refcn, s);
-      w.d3_sref.upload(c->d3_sref, s);
+      w.d3_sp.upload(c->d3_sp, s);
+      w.d3_c6ref.upload(c->d3_c6ref, s);
       w.d3_r4r2.upload(c->d3_r4r2, s);
       w.d3_rcov.upload(c->d3_rcov, s);
-      for (auto* b : {&w.d3_cn, &w.d3_a, &w.d3_da, &w.d3_dEdcn}) b->alloc(c->nat);
+      for (auto* b : {&w.d3_cn, &w.d3_dEdcn}) b->alloc(c->nat);
+      for (auto* b : {&w.d3_w, &w.d3_dw}) b->alloc((size_t)c->nat * D4_MREF);
     }
     if (c->has_d4) {
       w.d4_sp.upload(c->d4_sp, s);
@@ -635,14 +668,16 @@ static DevD3 dev_d3(const _tblite_calculator* c) {
   const Workspace& w = *c->ws;
   DevD3 d{};
   d3_model_constants(d, c);
+  d.nsp = c->d3_nsp;
+  d.sp = w.d3_sp.p;
   d.nref = w.d3_nref.p;
   d.refcn = w.d3_refcn.p;
-  d.sref = w.d3_sref.p;
+  d.c6ref = w.d3_c6ref.p;
   d.r4r2 = w.d3_r4r2.p;
   d.rcov = w.d3_rcov.p;
   d.cn = w.d3_cn.p;
-  d.a = w.d3_a.p;
-  d.da = w.d3_da.p;
+  d.w = w.d3_w.p;
+  d.dw = w.d3_dw.p;
   d.dEdcn = w.d3_dEdcn.p;
   return d;
 }

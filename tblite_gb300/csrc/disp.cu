@@ -542,11 +542,11 @@ void d4_gradient(const DevMol& m, const DevD4& d, D4Work& w, const double* qat, 
 
 // ------------------------------------------------------------------------------------
 // D3(BJ) two-body dispersion of GFN1-xTB (reference src/tblite/disp/d3.f90, which calls
-// s-dftd3 with s9 = 0): exponential coordination number over the D3 covalent radii,
-// Gaussian reference weights in CN, C6_ij = a_i a_j with a_i = sum_r w_ir sqrt(C6_r) / sum_r w_ir,
-// rational (BJ) damping.  Three kernels, one warp per atom each, every atom summing its own
-// share of each pair (deterministic, no atomics):
-//   setup:  CN_i, a_i, da_i/dCN_i
+// s-dftd3 with s9 = 0): exponential coordination number over the covalent radii, normalised
+// Gaussian reference weights w_ir in CN, C6_ij = sum_rs w_ir w_js C6ref(r, s, Z_i, Z_j) from the
+// per-element-pair reference table, rational (BJ) damping.  Three kernels, one warp per atom
+// each, every atom summing its own share of each pair (deterministic, no atomics):
+//   setup:  CN_i, w_ir and dw_ir/dCN_i
 //   pair:   E_i += 1/2 sum_j E_ij, the explicit pair gradient, dE/dCN_i
 //   cn:     CN chain rule  grad_i += sum_j (dE/dCN_i + dE/dCN_j) dc_ij/dr (R_i - R_j)/r
 // ------------------------------------------------------------------------------------
@@ -577,18 +577,40 @@ __device__ __forceinline__ void d3_setup_dev(const DevMol& m, const DevD3& d) {
   acc = wsum(acc);
   if (lane != 0) return;
   d.cn[i] = acc;
-  double norm = 0.0, dnorm = 0.0, ws = 0.0, dws = 0.0;
-  for (int r = 0; r < d.nref[i]; ++r) {
+  double w[D4_MREF], dw[D4_MREF], norm = 0.0, dnorm = 0.0;
+  const int nr = d.nref[i];
+  for (int r = 0; r < nr; ++r) {
     const double t = acc - d.refcn[i * D4_MREF + r];
-    const double w = exp(-d.k3 * t * t), dw = -2.0 * d.k3 * t * w;
-    const double sr = d.sref[i * D4_MREF + r];
-    norm += w;
-    dnorm += dw;
-    ws += w * sr;
-    dws += dw * sr;
+    w[r] = exp(-d.k3 * t * t);
+    dw[r] = -2.0 * d.k3 * t * w[r];
+    norm += w[r];
+    dnorm += dw[r];
   }
-  d.a[i] = ws / norm;
-  d.da[i] = (dws * norm - ws * dnorm) / (norm * norm);
+  for (int r = 0; r < D4_MREF; ++r) {
+    d.w[i * D4_MREF + r] = r < nr ? w[r] / norm : 0.0;
+    d.dw[i * D4_MREF + r] = r < nr ? (dw[r] * norm - w[r] * dnorm) / (norm * norm) : 0.0;
+  }
+}
+
+// C6 of the pair (i, j) and its derivatives in CN_i and CN_j
+__device__ __forceinline__ void d3_c6(const DevD3& d, int i, int j, double& c6, double& dc6i,
+                                      double& dc6j) {
+  const int ld = d.nsp * D4_MREF;
+  const double* tab = d.c6ref + (size_t)d.sp[i] * D4_MREF * ld + d.sp[j] * D4_MREF;
+  const double *wi = d.w + i * D4_MREF, *wj = d.w + j * D4_MREF;
+  const double *dwi = d.dw + i * D4_MREF, *dwj = d.dw + j * D4_MREF;
+  c6 = dc6i = dc6j = 0.0;
+  for (int r = 0; r < d.nref[i]; ++r) {
+    double s = 0.0, ds = 0.0;
+    for (int q = 0; q < d.nref[j]; ++q) {
+      const double c = tab[(size_t)r * ld + q];
+      s += wj[q] * c;
+      ds += dwj[q] * c;
+    }
+    c6 += wi[r] * s;
+    dc6i += dwi[r] * s;
+    dc6j += wi[r] * ds;
+  }
 }
 
 __device__ __forceinline__ void d3_pair_dev(const DevMol& m, const DevD3& d, int grad, double* eat,
@@ -597,7 +619,7 @@ __device__ __forceinline__ void d3_pair_dev(const DevMol& m, const DevD3& d, int
   if (warp >= m.nat) return;
   const int i = warp;
   const double cut2 = d.cutoff * d.cutoff;
-  const double ai = d.a[i], dai = d.da[i], ri = d.r4r2[i];
+  const double ri = d.r4r2[i];
   double e = 0.0, dcn = 0.0, g[3] = {0, 0, 0}, sg[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   for (int j = lane; j < m.nat; j += 32) {
     if (j == i) continue;
@@ -613,7 +635,8 @@ __device__ __forceinline__ void d3_pair_dev(const DevMol& m, const DevD3& d, int
     const double r02 = r0 * r0, r06 = r02 * r02 * r02, r08 = r06 * r02;
     const double r6 = r2 * r2 * r2, r8 = r6 * r2;
     const double t6 = 1.0 / (r6 + r06), t8 = 1.0 / (r8 + r08);
-    const double c6 = ai * d.a[j];
+    double c6, dc6i, dc6j;
+    d3_c6(d, i, j, c6, dc6i, dc6j);
     const double dedc6 = -(d.s6 * t6 + d.s8 * qq * t8);
     e += 0.5 * dedc6 * c6;
     if (grad) {
@@ -622,7 +645,7 @@ __device__ __forceinline__ void d3_pair_dev(const DevMol& m, const DevD3& d, int
       for (int k = 0; k < 3; ++k) g[k] += f * v[k];
       for (int a = 0; a < 3; ++a)
         for (int b = 0; b < 3; ++b) sg[3 * a + b] += 0.5 * f * v[a] * v[b];
-      dcn += dedc6 * dai * d.a[j];
+      dcn += dedc6 * dc6i;
     }
   }
   e = wsum(e);

@@ -131,13 +131,16 @@ void d4_gradient(const DevMol& m, const DevD4& d, D4Work& w, const double* qat, 
 // D3(BJ) two-body dispersion of GFN1-xTB (no three-body term): per atom data, model
 // constants and scratch (device pointers)
 struct DevD3 {
+  int nsp;
+  const int* sp;        // [nat] species index
   const int* nref;      // [nat]
   const double* refcn;  // [nat][D4_MREF]
-  const double* sref;   // [nat][D4_MREF] square roots of the reference C6
+  const double* c6ref;  // [nsp][D4_MREF][nsp][D4_MREF] reference C6 per species pair
   const double* r4r2;   // [nat]
   const double* rcov;   // [nat]
   double k1, k3, cn_cutoff, cutoff, s6, s8, a1, a2;
-  double *cn, *a, *da, *dEdcn;  // [nat] scratch
+  double *cn, *dEdcn;   // [nat] scratch
+  double *w, *dw;       // [nat][D4_MREF] scratch: normalised weights and their CN derivatives
 };
 // energy (added to eat) and, with grad, gradient and per-atom virial partials
 void d3_energy_gradient(const DevMol& m, const DevD3& d, bool grad, double* eat, double* grad_out,

@@ -9,8 +9,9 @@ counts, reference C6 values, effective charges, hardnesses, <r4>/<r2> ratios).
 Elements absent from the pack are stored as NaN (nref = 0); the library rejects
 molecules that need them with an error naming the element.
 
-Reference C6 values for a pair of references (r of element A, s of element B)
-are formed as sqrt(c6_A[r] * c6_B[s]) -- the combining rule of the pack format.
+Reference C6 values come per element pair (the pack's d4.c6["Za-Zb"], Za <= Zb, an
+nref(Za) x nref(Zb) matrix): EXT_D4_C6OFF[(Za-1)*86 + Zb-1] is the offset of that matrix
+(row-major) in EXT_D4_C6PAIR, -1 when the pack has no entry for the pair.
 
 Usage: ``python tblite_gb300/data/gen_element_data.py [PACK.json]``
 (default: ``element_data_synthetic.json``).
@@ -55,13 +56,12 @@ def main():
              fmt("EXT_RAD", table(pack["atomic_rad"])),
              f"static const int EXT_D4_MREF = {MREF};\n"]
     for key in ("ga", "gc", "wf", "cn_kn", "cn_k4", "cn_k5", "cn_k6", "cn_cutoff", "disp2_cutoff",
-                "disp3_cutoff", "atm_alpha"):
-        lines.append(f"static const double EXT_D4_{key.upper()} = {float(d4[key])!r};\n")
+                "disp3_cutoff", "atm_alpha", "width2", "width3"):
+        lines.append(f"static const double EXT_D4_{key.upper()} = {float(d4.get(key, 0.0))!r};\n")
     nref = [0] * 86
     refcn = [0.0] * (86 * MREF)
     refq = [0.0] * (86 * MREF)
     ngw = [0] * (86 * MREF)
-    refc6 = [0.0] * (86 * MREF)
     for k, v in d4["refcn"].items():
         z = int(k) - 1
         nref[z] = len(v)
@@ -69,9 +69,17 @@ def main():
             refcn[z * MREF + r] = v[r]
             refq[z * MREF + r] = d4["refq"][k][r]
             ngw[z * MREF + r] = d4["ngw"][k][r]
-            refc6[z * MREF + r] = d4["refc6"][k][r]
+    c6off = [-1] * (86 * 86)
+    c6pair = []
+    for key, mat in sorted(d4["c6"].items(), key=lambda kv: tuple(map(int, kv[0].split("-")))):
+        za, zb = map(int, key.split("-"))
+        if za > zb or len(mat) != nref[za - 1] or any(len(row) != nref[zb - 1] for row in mat):
+            raise SystemExit(f"pack: C6 pair {key} does not match the reference counts")
+        c6off[(za - 1) * 86 + zb - 1] = len(c6pair)
+        c6pair += [float(x) for row in mat for x in row]
     lines += [fmt("EXT_D4_NREF", nref, "int"), fmt("EXT_D4_REFCN", refcn), fmt("EXT_D4_REFQ", refq),
-              fmt("EXT_D4_NGW", ngw, "int"), fmt("EXT_D4_REFC6", refc6),
+              fmt("EXT_D4_NGW", ngw, "int"), fmt("EXT_D4_C6OFF", c6off, "int"),
+              fmt("EXT_D4_C6PAIR", c6pair or [0.0]),
               fmt("EXT_D4_ZEFF", table(d4["zeff"])), fmt("EXT_D4_GAM", table(d4["gam"])),
               fmt("EXT_D4_R4R2", table(d4["r4r2"])), fmt("EXT_D4_RCOV", table(d4["rcov"])),
               fmt("EXT_D4_EN", table(d4["en"]))]
