@@ -393,16 +393,35 @@ def run_gb300(args):
     return line
 
 
-def _ensemble_flops(mols_nao, mols_nel, iters):
-    """Algorithmic FP64 work of the batched ensemble (per molecule: per SCF iteration the
-    Cholesky-reduced eigensolve 16/3 n^3 and the density 2 n^2 k; once the Cholesky n^3/3 and
-    the energy-weighted density 2 n^2 k; k = occupied orbitals)."""
+def _ensemble_flops(mols_nao, mols_nel, iters, modes=None, pipe_flops=0.0):
+    """Algorithmic FP64 work of the batched ensemble and of its tridiagonalisations.
+
+    Diagonalised molecules: per SCF iteration the Cholesky-reduced eigensolve 16/3 n^3 and the
+    density 2 n^2 k; once the Cholesky n^3/3 and the energy-weighted density 2 n^2 k; the
+    tridiagonalisation 4/3 n^3 per iteration.  Projected molecules (mode 1): per iteration the
+    reduction X^T F X (n^3 + n^3) and P = 2 X D X^T (n^3 + n^3), the squarings as counted on
+    the device (pipe_flops, FP64-equivalent); once the Cholesky n^3/3, the final
+    diagonalisation for the orbital energies 4/3 n^3 and W = P F P / 2 (4 n^3); k = occupied
+    orbitals."""
     tot = tri = 0.0
-    for n, nel, it in zip(mols_nao, mols_nel, iters):
+    modes = modes if modes is not None else [0] * len(mols_nao)
+    for n, nel, it, mode in zip(mols_nao, mols_nel, iters, modes):
         k = min(n, (nel + 1) // 2)
-        tot += it * (16.0 / 3.0 * n ** 3 + 2.0 * n * n * k) + n ** 3 / 3.0 + 2.0 * n * n * k
-        tri += it * 4.0 / 3.0 * n ** 3
-    return tot, tri
+        if mode == 1:
+            tot += it * 4.0 * n ** 3 + n ** 3 / 3.0 + 4.0 / 3.0 * n ** 3 + 4.0 * n ** 3
+            tri += 4.0 / 3.0 * n ** 3
+        else:
+            tot += it * (16.0 / 3.0 * n ** 3 + 2.0 * n * n * k) + n ** 3 / 3.0 + 2.0 * n * n * k
+            tri += it * 4.0 / 3.0 * n ** 3
+    return tot + pipe_flops, tri
+
+
+def _modes(count):
+    from tblite_gb300 import library
+
+    m = np.zeros(count, dtype=np.int32)
+    library.load().tblite_gb300_batch_last_modes(library._ip(m), count)
+    return m
 
 
 def run_batch(args):
@@ -425,6 +444,7 @@ def run_batch(args):
     calcs = [Calculator("GFN2-xTB", z, x) for z, x in mols]
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
     fp64_peak = _fp64_peak(torch)
+    library.set_batch_graphs(not args.no_graphs)
     batch_singlepoint(calcs)  # first use: device memory, module loading
     tuned_calls = library.batch_autotune(calcs, sample=256) if not args.no_tune else 0
     schedule = library.batch_schedule()
@@ -433,6 +453,7 @@ def run_batch(args):
         batch_singlepoint(calcs)
     torch.cuda.synchronize()
     n0 = library.launch_count()
+    pf0 = library.pipe_batch_flops()
     if ws > 1:
         torch.distributed.barrier()
     wall = dev_ms = 0.0
@@ -448,6 +469,8 @@ def run_batch(args):
     launches = library.launch_count() - n0
     fallbacks = batch_fallbacks()
     projected = library.batch_projected()
+    modes = _modes(count)
+    pipe_flops_step = (library.pipe_batch_flops() - pf0) / args.steps
     graph_builds, graph_launches = library.batch_graphs()
     # per-kernel CUDA events: one more (untimed) call with the profiler on (kernels launched
     # directly, buckets on the side streams as in the timed calls)
@@ -468,7 +491,7 @@ def run_batch(args):
     e2e = evals / wall
     nao = [c.get("orbital-map").size for c in calcs]
     nel = [int(round(sum({1: 1, 6: 4, 8: 6}[int(q)] for q in z))) for z, _ in mols]
-    flops, tri_flops = _ensemble_flops(nao, nel, np.maximum(iters, 0))
+    flops, tri_flops = _ensemble_flops(nao, nel, np.maximum(iters, 0), modes, pipe_flops_step)
     ms_step = dev_ms / args.steps
     kernels = {k: {"ms_per_step": round(t, 3), "launches": c, "share_of_step": round(t / ms_step, 4)}
                for k, (t, c) in kprof.items()}
@@ -476,29 +499,54 @@ def run_batch(args):
     # steps, so an event pair there also spans other buckets' kernels; one more (untimed) call
     # with the buckets on one stream brackets every tridiagonalisation launch alone
     library.set_batch_streams(1)
+    pf1 = library.pipe_batch_flops()
     batch_singlepoint(calcs)
+    pipe_flops_s = library.pipe_batch_flops() - pf1
     kser = library.get_kernel_profile()
     library.set_batch_streams(8)
     iters_s = np.zeros(count, dtype=np.int32)
     library.load().tblite_gb300_batch_last_iterations(library._ip(iters_s), count)
-    _, tri_flops_s = _ensemble_flops(nao, nel, np.maximum(iters_s, 0))
+    _, tri_flops_s = _ensemble_flops(nao, nel, np.maximum(iters_s, 0), _modes(count))
     t_tri, c_tri = kser["tridiag"]
-    roofline = {"kernel": "tridiag (batched, one block cluster per molecule)", "bound": "fp64",
+    t_pipe, c_pipe = kser["projection_squaring"]
+    peaks, peak_kind = _peaks()
+    bf16 = peaks.get("bf16_tflops_sustained", peaks["bf16_tflops"])
+    timing = ("CUDA events around each launch on its stream, one untimed call with the size "
+              "buckets serialised on one stream")
+    tri_roof = {"kernel": "tridiag (batched, one block cluster per molecule)", "bound": "fp64",
                 "achieved": round(tri_flops_s / (t_tri / 1000.0) / 1e12, 4) if t_tri else None,
                 "peak": round(fp64_peak, 4), "unit": "TFLOP/s",
                 "frac": round(tri_flops_s / (t_tri / 1000.0) / 1e12 / fp64_peak, 4) if t_tri else None,
-                "timing": "CUDA events around each launch on its stream, one untimed call with "
-                          "the size buckets serialised on one stream",
-                "traffic": 17577984,
+                "timing": timing, "traffic": 17577984,
                 "traffic_note": "dram__bytes_read+write of one kb_tridiag launch (38 molecules, "
                                 "288-384 orbitals; profiles/tridiag_cluster_ensemble512.md): each "
                                 "matrix is read once, n^2 x 8 B per molecule",
                 "peak_source": "measured in this run (cuBLAS DGEMM 4096^3)",
                 "algorithmic_work_per_call": tri_flops_s, "ms_per_call": round(t_tri, 3),
                 "launches_per_call": c_tri,
-                "ms_per_launch": round(t_tri / c_tri, 4) if c_tri else None,
-                "whole_step": {"algorithmic_flops": flops,
-                               "achieved_tflops": round(flops / (ms_step / 1000.0) / 1e12, 4)}}
+                "ms_per_launch": round(t_tri / c_tri, 4) if c_tri else None}
+    pipe_roof = None
+    if t_pipe and pipe_flops_s:
+        ach = SPLIT_SLICE_PRODUCTS * pipe_flops_s / (t_pipe / 1000.0) / 1e12
+        pipe_roof = {"kernel": "projection squarings (slice images + pipelined split GEMM on "
+                               "tcgen05, batched: kb_pexp_sq, kb_psplit_sq, kb_opipe_sq)",
+                     "bound": "tensor", "achieved": round(ach, 4), "peak": round(bf16, 4),
+                     "unit": "TFLOP/s", "frac": round(ach / bf16, 4), "timing": timing,
+                     "traffic": _profile_traffic("pipe_sq_ensemble512.md"),
+                     "peak_source": f"{peak_kind} (bf16 sustained)",
+                     "algorithmic_work_per_call": SPLIT_SLICE_PRODUCTS * pipe_flops_s,
+                     "work_note": "36 BF16 slice products per FP64-equivalent flop; FP64-"
+                                  "equivalent flop counted on the device (2 m n K per tile)",
+                     "fp64_equivalent_tflops": round(pipe_flops_s / (t_pipe / 1000.0) / 1e12, 4),
+                     "ms_per_call": round(t_pipe, 3), "launches_per_call": c_pipe}
+    if pipe_roof is not None and t_pipe >= t_tri:
+        roofline, other = pipe_roof, tri_roof
+    else:
+        roofline, other = tri_roof, pipe_roof
+    roofline = dict(roofline)
+    roofline["secondary"] = other
+    roofline["whole_step"] = {"algorithmic_flops": flops,
+                              "achieved_tflops": round(flops / (ms_step / 1000.0) / 1e12, 4)}
     # the plain one-molecule GPU path on the first molecules of the seeded random order
     order = ensemble_order(count)
     sample = order[:PLAIN_SAMPLE]
@@ -889,6 +937,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="ensemble4096", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-graphs", action="store_true",
+                    help="launch the batched SCF kernels directly instead of as CUDA graphs")
     ap.add_argument("--no-tune", action="store_true",
                     help="keep the default batch schedule (no autotuning before the warm-up)")
     prof = ap.add_argument_group("fixed profiling commands (--run)")

@@ -400,11 +400,35 @@ enum tblite_solvation_param {
   tblite_solvation_gb = 20,
   tblite_solvation_gbsa_gfn1 = 21,
   tblite_solvation_gbsa_gfn2 = 22,
+  tblite_solvation_ddcosmo = 100,
+  tblite_solvation_ddcpcm = 101,
+  tblite_solvation_ddpcm = 200
 };
 TBLITE_API_ENTRY tblite_container TBLITE_API_CALL
 tblite_new_alpb_solvation_solvent(tblite_error error, tblite_structure mol, char* solvent,
                                   enum tblite_solvation_param version,
                                   enum tblite_ref_solvation_state refstate);
+/* Interactions of the reference that the GPU engine does not provide; each reports an error
+ * (the electric field, whose reference signature has no error handle, returns NULL):
+ * container.h:36-45 (electric field, spin polarisation), solvation.h:54-95 (GB with a
+ * dielectric constant, ddX). */
+enum tblite_born_kernel {
+  tblite_born_still = 1,
+  tblite_born_p16 = 2,
+};
+TBLITE_API_ENTRY tblite_container TBLITE_API_CALL tblite_new_electric_field(double* efield);
+TBLITE_API_ENTRY tblite_container TBLITE_API_CALL
+tblite_new_spin_polarization(tblite_context ctx, tblite_structure mol, tblite_calculator calc,
+                             double wscale);
+TBLITE_API_ENTRY tblite_container TBLITE_API_CALL
+tblite_new_gb_solvation_epsilon(tblite_error error, tblite_structure mol, double eps,
+                                enum tblite_solvation_param version, enum tblite_born_kernel born);
+TBLITE_API_ENTRY tblite_container TBLITE_API_CALL
+tblite_new_ddx_solvation_epsilon(tblite_error error, tblite_structure mol, double eps,
+                                 enum tblite_solvation_param model);
+TBLITE_API_ENTRY tblite_container TBLITE_API_CALL
+tblite_new_ddx_solvation_solvent(tblite_error error, tblite_structure mol, char* solvent,
+                                 enum tblite_solvation_param model);
 
 #ifdef __cplusplus
 }

@@ -47,6 +47,9 @@ int tblite_gb300_batch_last_fallbacks(void);
 void tblite_gb300_set_batch_density_solver(int mode);
 /* molecules of the last batch call whose SCF density came from the spectral projection */
 int tblite_gb300_batch_last_projected(void);
+/* density path of each molecule of the last batch call: 1 spectral projection, 0 batched
+ * diagonalisation, -1 the one-molecule path; returns the number of molecules recorded */
+int tblite_gb300_batch_last_modes(int* modes, int nmol);
 /* Autotuner of the batch schedule: coordinate descent over the projection threshold (128, 160,
  * 224 orbitals or off), the bucket cut (3/4, 2/3, 4/5 of the largest orbital count), the CTAs
  * per SM of the cluster tridiagonalisation (1, 2) and the side streams (4, 8), each candidate
@@ -212,6 +215,9 @@ int tblite_gb300_density_matrix_noalloc(int n, int k, const double* C, const dou
  * one-molecule path).  Returns 0, or -1 on a CUDA error. */
 void tblite_gb300_set_calculator_fault(tblite_context ctx, tblite_calculator calc, int kind);
 int tblite_gb300_set_pipeline_wait_limit(int polls);
+/* FP64-equivalent flop (2 m n K per output tile that ran) of the batched spectral projection's
+ * squarings on the tensor cores since library load, counted on the device */
+unsigned long long tblite_gb300_get_pipe_batch_flops(void);
 /* largest n*k the fixed workspace of tblite_gb300_density_matrix_noalloc holds */
 int tblite_gb300_density_matrix_noalloc_max(void);
 

@@ -95,6 +95,7 @@ bool g_batch_graphs = true;  // SCF iterations as CUDA graphs
 int g_last_graph_builds = 0, g_last_graph_launches = 0;  // of the last call
 double g_last_device_ms = 0.0;  // device time of the last call's batched steps (CUDA events)
 std::vector<int> g_last_iters;  // SCF iterations per molecule of the last call (0: not batched)
+std::vector<int> g_last_modes;  // 1 projection, 0 diagonalisation, -1 one-molecule path
 
 // byte offsets of one region, 256-byte aligned pieces
 struct Region {
@@ -791,14 +792,17 @@ std::vector<int> run_chunk(std::vector<Plan>& plans, Arena& ar, _tblite_context*
                  "projection steps");
     stream_wait(s);
     cuda_check(cudaGetLastError(), "batch scf");
-    // step budget of each projection bucket: the most steps its molecules took, plus a margin
-    for (Bucket& b : buckets) {
-      if (!b.sp2) continue;
-      int most = 0;
-      for (int i = b.first; i < b.last; ++i)
-        if (active[i]) most = std::max(most, h_steps[i]);
-      b.sp2_steps = std::min(SP2_MAX_STEPS, most + 10);
-    }
+    // step budget of each projection bucket, set once after the first iteration: the most
+    // steps its molecules took there plus a margin (the first, from the SAD guess, takes the
+    // most); a fixed budget keeps the launch structure of the iteration graphs unchanged
+    if (iscf == 1)
+      for (Bucket& b : buckets) {
+        if (!b.sp2) continue;
+        int most = 0;
+        for (int i = b.first; i < b.last; ++i)
+          if (active[i]) most = std::max(most, h_steps[i]);
+        b.sp2_steps = std::min(SP2_MAX_STEPS, most + 10);
+      }
     for (int i = 0; i < np; ++i) {
       if (!active[i]) continue;
       const Plan& pl = plans[i];
@@ -1058,6 +1062,7 @@ extern "C" int tblite_gb300_batch_singlepoint(tblite_context ctx, int nmol,
     g_last_projected = 0;
     g_last_graph_builds = g_last_graph_launches = 0;
     g_last_iters.assign(nmol, 0);
+    g_last_modes.assign(nmol, -1);
     prof_reset();
     // chunks of at most ~24 GB of device memory
     const size_t budget = (size_t)24 << 30;
@@ -1074,7 +1079,10 @@ extern "C" int tblite_gb300_batch_singlepoint(tblite_context ctx, int nmol,
       for (int k : leave) plain.push_back(chunk[k].idx);
       std::vector<char> left(chunk.size(), 0);
       for (int k : leave) left[k] = 1;
-      for (size_t k = 0; k < chunk.size(); ++k) g_last_projected += chunk[k].sp2 && !left[k];
+      for (size_t k = 0; k < chunk.size(); ++k) {
+        g_last_projected += chunk[k].sp2 && !left[k];
+        if (!left[k]) g_last_modes[chunk[k].idx] = chunk[k].sp2 ? 1 : 0;
+      }
       i0 = i1;
     }
     prof_collect();
@@ -1113,6 +1121,11 @@ extern "C" void tblite_gb300_set_tridiag_ctas_per_sm(int count) {
 }
 extern "C" void tblite_gb300_set_batch_density_solver(int mode) { g_batch_sp2 = mode != 0; }
 extern "C" int tblite_gb300_batch_last_projected(void) { return g_last_projected; }
+extern "C" int tblite_gb300_batch_last_modes(int* modes, int nmol) {
+  const int m = std::min(nmol, (int)g_last_modes.size());
+  for (int i = 0; i < m && modes; ++i) modes[i] = g_last_modes[i];
+  return (int)g_last_modes.size();
+}
 extern "C" void tblite_gb300_set_batch_graphs(int enable) { g_batch_graphs = enable != 0; }
 extern "C" int tblite_gb300_batch_last_graphs(int* builds, int* launches) {
   if (builds) *builds = g_last_graph_builds;

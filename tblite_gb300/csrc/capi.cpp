@@ -1949,6 +1949,51 @@ void tblite_delete_container(tblite_container* cont) {
   }
 }
 
+// interactions of the reference that the GPU engine does not provide: each reports an error and
+// returns NULL (include/tblite/container.h:31-45, solvation.h:54-95)
+tblite_container tblite_new_electric_field(double* efield) {
+  (void)efield;
+  return nullptr;  // the reference's signature has no error handle: NULL is the report
+}
+tblite_container tblite_new_spin_polarization(tblite_context ctx, tblite_structure mol,
+                                              tblite_calculator calc, double wscale) {
+  (void)mol;
+  (void)calc;
+  (void)wscale;
+  if (ctx) ctx->push("Spin polarization is not available in the GPU engine");
+  return nullptr;
+}
+tblite_container tblite_new_gb_solvation_epsilon(tblite_error error, tblite_structure mol,
+                                                 double eps, enum tblite_solvation_param version,
+                                                 enum tblite_born_kernel born) {
+  (void)eps;
+  (void)born;
+  if (!mol) {
+    set_err(error, "Molecular structure data is missing");
+    return nullptr;
+  }
+  set_err(error, version == tblite_solvation_gbe || version == tblite_solvation_gb
+                     ? "Generalized Born solvation with a dielectric constant is not available in "
+                       "the GPU engine (ALPB water only)"
+                     : "Unknown solvation model requested");
+  return nullptr;
+}
+tblite_container tblite_new_ddx_solvation_epsilon(tblite_error error, tblite_structure mol,
+                                                  double eps, enum tblite_solvation_param model) {
+  (void)mol;
+  (void)eps;
+  (void)model;
+  set_err(error, "ddX solvation is not available in the GPU engine");
+  return nullptr;
+}
+tblite_container tblite_new_ddx_solvation_solvent(tblite_error error, tblite_structure mol,
+                                                  char* solvent, enum tblite_solvation_param model) {
+  (void)mol;
+  (void)solvent;
+  (void)model;
+  set_err(error, "ddX solvation is not available in the GPU engine");
+  return nullptr;
+}
 tblite_container tblite_new_alpb_solvation_solvent(tblite_error error, tblite_structure mol,
                                                    char* solvent,
                                                    enum tblite_solvation_param version,

@@ -56,6 +56,8 @@ constexpr int PP_WAIT = 1 << 22;
 // PP_WAIT.  Settable for tests (tblite_gb300_set_pipeline_wait_limit) so that a wait runs out
 // and the abort path, the status word and the hand-off can be checked.
 __device__ int g_pipe_wait_limit = PP_WAIT;
+// FP64-equivalent flop (2 m n K per output tile that ran) of the batched squarings since load
+__device__ unsigned long long g_pipe_batch_flops = 0;
 
 void ck(cudaError_t e, const char* what) {
   if (e != cudaSuccess)
@@ -483,6 +485,15 @@ __global__ void __launch_bounds__(PP_THREADS, 1) kb_opipe_sq(const MolPtrs* __re
   a.ldc = n;
   a.sym = 1;
   a.status = q.sp2i + 3;
+  if (threadIdx.x == 0) {  // the tile's useful area (the upper tiles of the symmetric product exit)
+    const int mt = (n + PP_M - 1) / PP_M, nt = (n + PP_N - 1) / PP_N;
+    const int b = blockIdx.x, gid = b / (PP_GROUP * nt), first = gid * PP_GROUP;
+    const int gsize = min(mt - first, PP_GROUP), inner = b - gid * PP_GROUP * nt;
+    const int i0 = (first + inner % gsize) * PP_M, j0 = (inner / gsize) * PP_N;
+    if (!(i0 + PP_M - 1 < j0))
+      atomicAdd(&g_pipe_batch_flops, 2ull * (unsigned long long)min(PP_M, n - i0) *
+                                         (unsigned long long)min(PP_N, n - j0) * (unsigned)n);
+  }
   opipe_tile(a, blockIdx.x);
 }
 
@@ -506,7 +517,7 @@ void sp2_square_b(const BatchLaunch& b) {
   kb_pexp_sq<<<dim3(lp / 32, 1, b.count), 256, 0, b.s>>>(b.mp, b.list);
   kb_psplit_sq<<<dim3(lp / 64, nkc, b.count), 256, 0, b.s>>>(b.mp, b.list);
   kb_opipe_sq<<<dim3(tiles, b.count), PP_THREADS, PP_SMEM, b.s>>>(b.mp, b.list);
-  prof_kend(KS_GEMM, tk, b.s);
+  prof_kend(KS_PIPE, tk, b.s);
 }
 
 size_t pimage_bytes(int lines, int K) {
@@ -618,6 +629,12 @@ extern "C" void tblite_gb300_set_pipelined_gemm(int enable) { tb::g_pipe_gemm = 
 
 // test setting: polls of the pipelined split GEMM's pipeline waits on the current device (0:
 // the default 2^22).  0 on success, -1 on a CUDA error.
+extern "C" unsigned long long tblite_gb300_get_pipe_batch_flops(void) {
+  unsigned long long v = 0;
+  if (cudaMemcpyFromSymbol(&v, tb::g_pipe_batch_flops, sizeof(v)) != cudaSuccess) return 0;
+  return v;
+}
+
 extern "C" int tblite_gb300_set_pipeline_wait_limit(int polls) {
   const int v = polls > 0 ? polls : tb::PP_WAIT;
   return cudaMemcpyToSymbol(tb::g_pipe_wait_limit, &v, sizeof(int)) == cudaSuccess ? 0 : -1;

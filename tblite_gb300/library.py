@@ -123,7 +123,9 @@ _SIGNATURES = {
     "tblite_gb300_set_batch_density_solver": (None, [c_int]),
     "tblite_gb300_set_calculator_fault": (None, [c_void_p, c_void_p, c_int]),
     "tblite_gb300_set_pipeline_wait_limit": (c_int, [c_int]),
+    "tblite_gb300_get_pipe_batch_flops": (ctypes.c_ulonglong, []),
     "tblite_gb300_batch_last_projected": (c_int, []),
+    "tblite_gb300_batch_last_modes": (c_int, [_int_p, c_int]),
     "tblite_gb300_batch_autotune": (c_int, [c_void_p, c_int, POINTER(c_void_p), POINTER(c_void_p),
                                             c_int]),
     "tblite_gb300_batch_schedule": (c_int, [c_char_p, c_int]),
@@ -288,7 +290,8 @@ def get_profile():
             "total_ms": tot.value, "iterations": it.value}
 
 
-KERNEL_SLOTS = ("tridiag", "multisect", "invit", "backtransform", "gemm", "fock", "mulliken")
+KERNEL_SLOTS = ("tridiag", "multisect", "invit", "backtransform", "gemm", "fock", "mulliken",
+                "projection_squaring")
 
 
 def get_kernel_profile():
@@ -303,6 +306,12 @@ def get_kernel_profile():
 
 def launch_count() -> int:
     return int(load().tblite_gb300_get_launch_count())
+
+
+def pipe_batch_flops() -> int:
+    """FP64-equivalent flop (2 m n K per output tile) of the batched projection squarings on the
+    tensor cores since library load (counted on the device)."""
+    return int(load().tblite_gb300_get_pipe_batch_flops())
 
 
 def split_gemm_flops() -> int:

@@ -154,7 +154,8 @@ def test_exported_record_is_bitwise_the_builtin(method):
     calc._calc = library.new_xtb_calculator(calc._ctx, calc._mol, p.h)
     res = calc.singlepoint()
     assert res.get("energy") == ref.get("energy")
-    assert np.array_equal(res.get("gradient"), ref.get("gradient"))
+    # the gradient kernels sum some pair terms with atomics: equal to the last bits
+    assert np.max(np.abs(res.get("gradient") - ref.get("gradient"))) < 1e-14
     # through the table in the TOML layout (levels in eV and back)
     res2 = Calculator(library.export_param(method), z, x).singlepoint()
     assert abs(res2.get("energy") - ref.get("energy")) < 1e-10

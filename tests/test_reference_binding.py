@@ -121,3 +121,13 @@ def test_gpu_calls_fail_loudly_and_results_need_a_single_point(tblite):
     if not torch.cuda.is_available():
         with pytest.raises(tblite.exceptions.TBLiteRuntimeError, match="CUDA"):
             calc.singlepoint()
+
+
+def test_unavailable_interactions_report_errors(tblite):
+    numbers, positions = _water_dimer()
+    calc = tblite.interface.Calculator("GFN2-xTB", numbers, positions)
+    with pytest.raises(tblite.exceptions.TBLiteRuntimeError, match="not available"):
+        calc.add("gb-solvation", 78.4, "still")
+    with pytest.raises(tblite.exceptions.TBLiteRuntimeError, match="not available"):
+        calc.add("spin-polarization", 1.0)
+    calc.add("alpb-solvation", "water")  # ALPB(water) is available
