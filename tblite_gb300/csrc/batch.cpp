@@ -142,7 +142,7 @@ struct Plan {
   Piece X, A, T1, Y, lu, ed, ee, etau, epv, escal, estatus, conv;
   Piece pgrad, zgrad;  // [4][nsh], [nsh] (param_grad only)
   Piece wbo;           // [wbo_ch][nat][nat] (bond orders requested only)
-  Piece img, iexp, sp2s, sp2i;  // spectral projection (sp2 only)
+  Piece img, iexp, img2, iexp2, sp2s, sp2i;  // spectral projection (sp2 only)
 };
 
 struct Bucket {
@@ -238,8 +238,10 @@ void layout(Plan& pl, Region* R) {
   if (pl.sp2) {
     pl.img = piece<uint16_t>(R, RS, pimage_bytes((int)n, (int)n) / sizeof(uint16_t));
     pl.iexp = piece<int>(R, RS, pimage_lines((int)n));
+    pl.img2 = piece<uint16_t>(R, RS, pimage_bytes((int)n, (int)n) / sizeof(uint16_t));
+    pl.iexp2 = piece<int>(R, RS, pimage_lines((int)n));
     pl.sp2s = piece<double>(R, RS, 8);
-    pl.sp2i = piece<int>(R, RS, 8);
+    pl.sp2i = piece<int>(R, RZ, 8);  // zeroed: the pipeline status starts clear
   }
   // scratch
   pl.cn = piece<double>(R, RS, na);
@@ -454,6 +456,8 @@ MolPtrs make_ptrs(const Plan& pl, const Bases& db) {
   q.wbo = pl.wbo_ch > 0 ? db.at<double>(pl.wbo) : nullptr;
   q.img = pl.sp2 ? db.at<uint16_t>(pl.img) : nullptr;
   q.iexp = pl.sp2 ? db.at<int>(pl.iexp) : nullptr;
+  q.img2 = pl.sp2 ? db.at<uint16_t>(pl.img2) : nullptr;
+  q.iexp2 = pl.sp2 ? db.at<int>(pl.iexp2) : nullptr;
   q.sp2s = pl.sp2 ? db.at<double>(pl.sp2s) : nullptr;
   q.sp2i = pl.sp2 ? db.at<int>(pl.sp2i) : nullptr;
   if (pl.sp2) q.nev = pl.nao;  // the projection needs no levels during the SCF; all after it
@@ -884,11 +888,25 @@ std::vector<int> run_chunk(std::vector<Plan>& plans, Arena& ar, _tblite_context*
       for (int i = 0; i < np; ++i) sel[i] = done[i] && plans[i].wbo_ch > ch;
       if (upload_lists(sel) > 0) each([&](BatchLaunch& L) { wbo_b(L, ch); });
     }
+    if (any_sp2) {  // a pipelined product of the gradient phase whose wait ran out
+      std::vector<char> sel(np, 0);
+      for (int i = 0; i < np; ++i) sel[i] = done[i] && plans[i].sp2;
+      if (upload_lists(sel) > 0) each([&](BatchLaunch& L) { sp2_pipe_check_b(L); });
+    }
     cuda_check(cudaEventRecord(ev1, s), "event");
     cuda_check(cudaMemcpyAsync(ar.host, db.base[RR], R[RR].size, cudaMemcpyDeviceToHost, s),
                "batch results");
+    cuda_check(cudaMemcpyAsync(h_flag.data(), d_flag, sizeof(int) * np, cudaMemcpyDeviceToHost, s),
+               "flags");
     stream_wait(s);
     cuda_check(cudaGetLastError(), "batch gradient");
+    // a split GEMM of the gradient phase that did not answer: the molecule is re-run by the
+    // one-molecule path instead of reporting these results
+    for (int i = 0; i < np; ++i)
+      if (done[i] && h_flag[i] < 0) {
+        done[i] = 0;
+        record_leave(i, h_flag[i]);
+      }
     cuda_check(cudaEventElapsedTime(&scf_ms, ev0, ev1), "event");
     const Bases hz{{nullptr, ar.host, nullptr, nullptr}};
     for (int i = 0; i < np; ++i) {

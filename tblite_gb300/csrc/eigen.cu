@@ -1582,7 +1582,7 @@ void density_b(const BatchLaunch& b, bool weighted) {
 void wbo_b(const BatchLaunch& b, int channel) {
   if (!b.count) return;
   if (b.sp2) {  // closed shells without orbitals: P S directly
-    gemm_b(b, GS_PS);
+    pipe_site_b(b, GS_PS);
     launch_wbo_b(b, channel);
     return;
   }

@@ -375,6 +375,8 @@ struct MolPtrs {
   // of the last projection for the host
   uint16_t* img;
   int* iexp;
+  uint16_t* img2;  // second image (the columns of op(B) of a pipelined GEMM site)
+  int* iexp2;
   double* sp2s;
   int* sp2i;
   int* sp2steps;
@@ -437,6 +439,46 @@ enum { GS_FX = 0,  // T1 = F X            (X upper triangular)
        GS_PF,      // T1 = P F / 2
        GS_WPFP };  // W (into F) = T1 P
 void gemm_b(const BatchLaunch& b, int site);
+
+// one GEMM site of a molecule: C = alpha op(A) op(B), column-major, leading dimension ld (the
+// orbital count); op(A)(i, k) = ta ? A[k + i ld] : A[i + k ld], op(B)(k, j) = tb ? B[j + k ld]
+// : B[k + j ld]; km restricts k for a triangular operand, sym marks a symmetric product
+struct Site {
+  int M, N, K, ld;
+  const double* A;
+  bool ta;
+  const double* B;
+  bool tb;
+  double* C;
+  int km;
+  bool sym;
+  double alpha;  // power of two applied to the product (exact)
+};
+#ifdef __CUDACC__
+__device__ __forceinline__ Site site_of(const MolPtrs& q, int site) {
+  const int n = q.m.nao, k = *q.icount;
+  Site s{n, n, n, n, nullptr, false, nullptr, false, nullptr, KM_NONE, false, 1.0};
+  switch (site) {
+    case GS_FX: s.A = q.F; s.B = q.X; s.C = q.T1; s.km = KM_LT_COLEND; break;
+    case GS_XTT:
+      s.A = q.X; s.ta = true; s.B = q.T1; s.C = q.A; s.km = KM_LT_ROWEND; s.sym = true;
+      break;
+    case GS_XY: s.A = q.X; s.B = q.Y; s.C = q.C; s.N = k; s.km = KM_GE_ROWBEG; break;
+    case GS_DENS: s.A = q.scratch; s.B = q.C; s.tb = true; s.C = q.P; s.K = k; s.sym = true; break;
+    case GS_WDENS: s.A = q.scratch; s.B = q.C; s.tb = true; s.C = q.F; s.K = k; s.sym = true; break;
+    case GS_FS: s.A = q.F; s.B = q.S; s.C = q.scratch; break;
+    case GS_PS: s.A = q.P; s.B = q.S; s.C = q.scratch; break;
+    case GS_XD: s.A = q.X; s.B = q.Y; s.C = q.T1; s.km = KM_GE_ROWBEG; s.alpha = 2.0; break;
+    case GS_PXT: s.A = q.T1; s.B = q.X; s.tb = true; s.C = q.P; s.sym = true; break;
+    case GS_PF: s.A = q.P; s.B = q.F; s.C = q.T1; s.alpha = 0.5; break;
+    default: s.A = q.T1; s.B = q.P; s.C = q.F; s.sym = true; break;  // GS_WPFP
+  }
+  return s;
+}
+#endif
+// the same sites on the pipelined split GEMM (ozaki_pipe.cu; projection buckets: operands split
+// into the molecule's two slice images, then one batched product), n x n sites only
+void pipe_site_b(const BatchLaunch& b, int site);
 // the same sites on the BF16 tensor cores with FP64-accurate splitting (ozaki.cu); gemm_b
 // dispatches to it for buckets of at least 128 orbitals while split_gemm_enabled
 void ogemm_b(const BatchLaunch& b, int site);
@@ -456,6 +498,7 @@ void wbo_b(const BatchLaunch& b, int channel);
 void sp2_density_b(const BatchLaunch& b, int steps);
 void sp2_gap_b(const BatchLaunch& b);
 void sp2_weighted_b(const BatchLaunch& b);
+void sp2_pipe_check_b(const BatchLaunch& b);  // flag -5 for a molecule whose pipe wait ran out
 void sp2_square_b(const BatchLaunch& b);  // ozaki_pipe.cu: C = Y Y of the iterating molecules
 constexpr int SP2_MIN_NAO = 128;   // smallest orbital count that takes the projection
 constexpr int SP2_MAX_STEPS = 64;  // squarings per projection at most

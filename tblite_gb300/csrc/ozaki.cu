@@ -45,39 +45,6 @@ constexpr int OZ_SMEM = 120 * 1024;  // 96 KB of slices; the rest only limits re
 constexpr int OZ_A_SLICE = OZ_M * OZ_KC;  // bf16 elements of one slice of the A tile
 constexpr int OZ_B_SLICE = OZ_N * OZ_KC;
 
-struct Site {
-  int M, N, K, ld;  // ld: leading dimension of A, B and C (column-major)
-  const double* A;
-  bool ta;  // op(A)(i, k) = ta ? A[k + i n] : A[i + k n]
-  const double* B;
-  bool tb;  // op(B)(k, j) = tb ? B[j + k n] : B[k + j n]
-  double* C;
-  int km;
-  bool sym;
-  double alpha;  // power of two applied to the product (exact)
-};
-
-// the operands of the GEMM sites (the same as the FP64 tile GEMM of linalg.cu)
-__device__ __forceinline__ Site site_of(const MolPtrs& q, int site) {
-  const int n = q.m.nao, k = *q.icount;
-  Site s{n, n, n, n, nullptr, false, nullptr, false, nullptr, KM_NONE, false, 1.0};
-  switch (site) {
-    case GS_FX: s.A = q.F; s.B = q.X; s.C = q.T1; s.km = KM_LT_COLEND; break;
-    case GS_XTT:
-      s.A = q.X; s.ta = true; s.B = q.T1; s.C = q.A; s.km = KM_LT_ROWEND; s.sym = true;
-      break;
-    case GS_XY: s.A = q.X; s.B = q.Y; s.C = q.C; s.N = k; s.km = KM_GE_ROWBEG; break;
-    case GS_DENS: s.A = q.scratch; s.B = q.C; s.tb = true; s.C = q.P; s.K = k; s.sym = true; break;
-    case GS_WDENS: s.A = q.scratch; s.B = q.C; s.tb = true; s.C = q.F; s.K = k; s.sym = true; break;
-    case GS_FS: s.A = q.F; s.B = q.S; s.C = q.scratch; break;
-    case GS_PS: s.A = q.P; s.B = q.S; s.C = q.scratch; break;
-    case GS_XD: s.A = q.X; s.B = q.Y; s.C = q.T1; s.km = KM_GE_ROWBEG; s.alpha = 2.0; break;
-    case GS_PXT: s.A = q.T1; s.B = q.X; s.tb = true; s.C = q.P; s.sym = true; break;
-    case GS_PF: s.A = q.P; s.B = q.F; s.C = q.T1; s.alpha = 0.5; break;
-    default: s.A = q.T1; s.B = q.P; s.C = q.F; s.sym = true; break;  // GS_WPFP
-  }
-  return s;
-}
 __device__ __forceinline__ double opA(const Site& s, int i, int k) {
   return s.ta ? s.A[k + (size_t)i * s.ld] : s.A[i + (size_t)k * s.ld];
 }

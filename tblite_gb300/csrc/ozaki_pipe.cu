@@ -497,7 +497,108 @@ __global__ void __launch_bounds__(PP_THREADS, 1) kb_opipe_sq(const MolPtrs* __re
   opipe_tile(a, blockIdx.x);
 }
 
+// ---- batched GEMM sites on the pipe (projection buckets): the rows of op(A) go into img,
+// the columns of op(B) into img2, then one product per molecule
+struct SiteLines {
+  const double* M;
+  int ld, kcontig, lines, K;
+};
+__device__ __forceinline__ SiteLines site_lines(const Site& s, int which) {
+  if (which == 0) return {s.A, s.ld, s.ta ? 1 : 0, s.M, s.K};
+  return {s.B, s.ld, s.tb ? 0 : 1, s.N, s.K};
+}
+// exponents of the lines: 32 lines per block (lines strided in memory) or one warp per line
+// (k contiguous); grid.x covers lines_padded / 8 blocks for the widest molecule
+__global__ void __launch_bounds__(256) kb_pexp_site(const MolPtrs* __restrict__ mp,
+                                                    const int* __restrict__ list, int site,
+                                                    int which) {
+  const MolPtrs& q = mp[list[blockIdx.z]];
+  if (*q.flag < 0) return;
+  const SiteLines L = site_lines(site_of(q, site), which);
+  const int lp = lines_padded(L.lines);
+  int* e = which ? q.iexp2 : q.iexp;
+  if (!L.kcontig) {
+    if ((int)blockIdx.x * 32 >= lp) return;
+    pexp_rows_dev(L.M, L.ld, L.lines, L.K, lp, e, blockIdx.x);
+    return;
+  }
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (i >= lp) return;
+  double mx = 0.0;
+  if (i < L.lines)
+    for (int k = lane; k < L.K; k += 32) mx = fmax(mx, fabs(L.M[k + (size_t)i * L.ld]));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if (lane == 0) e[i] = mx > 0.0 ? ilogb(mx) + 1 : 0;
+}
+__global__ void __launch_bounds__(256) kb_psplit_site(const MolPtrs* __restrict__ mp,
+                                                      const int* __restrict__ list, int site,
+                                                      int which) {
+  const MolPtrs& q = mp[list[blockIdx.z]];
+  if (*q.flag < 0) return;
+  const SiteLines L = site_lines(site_of(q, site), which);
+  const int lp = lines_padded(L.lines), nkc = (L.K + PP_KC - 1) / PP_KC;
+  if ((int)blockIdx.x >= lp / 64 || (int)blockIdx.y >= nkc) return;
+  psplit_dev(L.M, L.ld, L.kcontig, L.lines, L.K, lp / 64, which ? q.iexp2 : q.iexp,
+             which ? q.img2 : q.img, blockIdx.x, blockIdx.y);
+}
+__global__ void __launch_bounds__(PP_THREADS, 1) kb_opipe_site(const MolPtrs* __restrict__ mp,
+                                                              const int* __restrict__ list,
+                                                              int site) {
+  const MolPtrs& q = mp[list[blockIdx.y]];
+  if (*q.flag < 0) return;
+  const Site s = site_of(q, site);
+  const int tiles = ((s.M + PP_M - 1) / PP_M) * ((s.N + PP_N - 1) / PP_N);
+  if ((int)blockIdx.x >= tiles) return;
+  PipeArgs a{};
+  a.A = q.img;
+  a.B = q.img2;
+  a.eA = q.iexp;
+  a.eB = q.iexp2;
+  a.eshiftA = s.alpha == 2.0 ? 1 : s.alpha == 0.5 ? -1 : 0;
+  a.nlbA = lines_padded(s.M) / 64;
+  a.nlbB = lines_padded(s.N) / 64;
+  a.M = s.M;
+  a.N = s.N;
+  a.nkc = (s.K + PP_KC - 1) / PP_KC;
+  a.C = s.C;
+  a.ldc = s.ld;
+  a.sym = s.sym ? 1 : 0;
+  a.status = q.sp2i + 3;
+  if (threadIdx.x == 0) {
+    const int mt = (s.M + PP_M - 1) / PP_M, nt = (s.N + PP_N - 1) / PP_N;
+    const int b = blockIdx.x, gid = b / (PP_GROUP * nt), first = gid * PP_GROUP;
+    const int gsize = min(mt - first, PP_GROUP), inner = b - gid * PP_GROUP * nt;
+    const int i0 = (first + inner % gsize) * PP_M, j0 = (inner / gsize) * PP_N;
+    if (!(s.sym && i0 + PP_M - 1 < j0))
+      atomicAdd(&g_pipe_batch_flops, 2ull * (unsigned long long)min(PP_M, s.M - i0) *
+                                         (unsigned long long)min(PP_N, s.N - j0) * (unsigned)s.K);
+  }
+  opipe_tile(a, blockIdx.x);
+}
+
 }  // namespace
+
+void pipe_site_b(const BatchLaunch& b, int site) {
+  if (!b.count) return;
+  static bool attr = false;
+  if (!attr) {
+    ck(cudaFuncSetAttribute(kb_opipe_site, cudaFuncAttributeMaxDynamicSharedMemorySize, PP_SMEM),
+       "smem attr batched pipelined split gemm");
+    attr = true;
+  }
+  const int n = b.nao_max;
+  const int lp = pimage_lines(n), nkc = (n + PP_KC - 1) / PP_KC;
+  const int tiles = ((n + PP_M - 1) / PP_M) * ((n + PP_N - 1) / PP_N);
+  const int tk = prof_kbegin(b.s);
+  g_kernel_launches += 5;
+  for (int which = 0; which < 2; ++which) {
+    kb_pexp_site<<<dim3(lp / 8, 1, b.count), 256, 0, b.s>>>(b.mp, b.list, site, which);
+    kb_psplit_site<<<dim3(lp / 64, nkc, b.count), 256, 0, b.s>>>(b.mp, b.list, site, which);
+  }
+  kb_opipe_site<<<dim3(tiles, b.count), PP_THREADS, PP_SMEM, b.s>>>(b.mp, b.list, site);
+  prof_kend(KS_PIPE, tk, b.s);
+}
 
 // one squaring step of the batched spectral projection: slice image of Y, then C = Y Y on the
 // tensor cores, for every listed molecule still iterating

@@ -91,7 +91,8 @@ __global__ void __launch_bounds__(256) kb_sp2_start(BARGS) {
     q.sp2i[0] = 0;   // converged
     q.sp2i[1] = 0;   // steps taken
     q.sp2i[2] = -1;  // update of the current step: 1 square, 0 2D - D^2, -1 none
-    q.sp2i[3] = 0;   // tensor-core pipeline status (set by the squaring kernel)
+    // sp2i[3]: tensor-core pipeline status, set by any pipelined product of the molecule; it
+    // starts zeroed with the batch and is never cleared (a failure sends the molecule away)
     q.scal[0] = 0.0;  // no Fermi entropy: the occupations are 0/2 (checked after the SCF)
   }
 }
@@ -192,8 +193,8 @@ inline unsigned ew_blocks(const BatchLaunch& b) {
 
 void sp2_density_b(const BatchLaunch& b, int steps) {
   if (!b.count) return;
-  gemm_b(b, GS_FX);
-  gemm_b(b, GS_XTT);
+  pipe_site_b(b, GS_FX);   // T1 = F X
+  pipe_site_b(b, GS_XTT);  // A = X^T T1
   g_kernel_launches += 2;
   kb_sp2_start<<<dim3(1, 1, b.count), 256, 0, b.s>>>(b.mp, b.list);
   kb_sp2_init<<<dim3(ew_blocks(b), 1, b.count), 256, 0, b.s>>>(b.mp, b.list);
@@ -205,8 +206,20 @@ void sp2_density_b(const BatchLaunch& b, int steps) {
   }
   ++g_kernel_launches;
   kb_sp2_finish<<<dim3(1, 1, b.count), 32, 0, b.s>>>(b.mp, b.list);
-  gemm_b(b, GS_XD);   // T1 = 2 X D
-  gemm_b(b, GS_PXT);  // P = T1 X^T
+  pipe_site_b(b, GS_XD);   // T1 = 2 X D
+  pipe_site_b(b, GS_PXT);  // P = T1 X^T
+}
+
+// a pipelined product after the SCF (W, bond orders) whose wait ran out: the molecule leaves
+__global__ void kb_pipe_check(BARGS) {
+  BMOL;
+  if (threadIdx.x == 0 && *q.flag >= 0 && q.sp2i[3] != 0) *q.flag = -5;
+}
+
+void sp2_pipe_check_b(const BatchLaunch& b) {
+  if (!b.count) return;
+  ++g_kernel_launches;
+  kb_pipe_check<<<dim3(1, 1, b.count), 32, 0, b.s>>>(b.mp, b.list);
 }
 
 void sp2_gap_b(const BatchLaunch& b) {
@@ -217,8 +230,8 @@ void sp2_gap_b(const BatchLaunch& b) {
 
 void sp2_weighted_b(const BatchLaunch& b) {
   if (!b.count) return;
-  gemm_b(b, GS_PF);    // T1 = P F / 2
-  gemm_b(b, GS_WPFP);  // W = T1 P, into F
+  pipe_site_b(b, GS_PF);    // T1 = P F / 2
+  pipe_site_b(b, GS_WPFP);  // W = T1 P, into F
 }
 
 #undef BMOL
