@@ -50,7 +50,8 @@ int tblite_gb300_batch_last_projected(void);
 /* density path of each molecule of the last batch call: 1 spectral projection, 0 batched
  * diagonalisation, -1 the one-molecule path; returns the number of molecules recorded */
 int tblite_gb300_batch_last_modes(int* modes, int nmol);
-/* Autotuner of the batch schedule: coordinate descent over the projection threshold (128, 160,
+/* Autotuner of the batch schedule: coordinate descent over CUDA graphs (kept, or switched off;
+ * never switched on against tblite_gb300_set_batch_graphs), the projection threshold (128, 160,
  * 224 orbitals or off), the bucket cut (3/4, 2/3, 4/5 of the largest orbital count), the CTAs
  * per SM of the cluster tridiagonalisation (1, 2) and the side streams (4, 8), each candidate
  * timed as the wall time of a batch call (best of two) on a fixed pseudo-random sample of
@@ -60,7 +61,7 @@ int tblite_gb300_batch_autotune(tblite_context ctx, int nmol, const tblite_struc
                                 const tblite_calculator* calcs, int sample);
 /* the current batch schedule as text (written up to n - 1 characters); returns its length */
 int tblite_gb300_batch_schedule(char* buf, int n);
-/* back to the default batch schedule */
+/* back to the default batch schedule (CUDA graphs on) */
 void tblite_gb300_batch_reset_schedule(void);
 /* SCF iterations of a batch call as CUDA graphs (default 1): each iteration of a memory chunk
  * (every bucket on every side stream) is captured, instantiated once and updated in place while

@@ -1164,9 +1164,10 @@ namespace tb {
 int get_tridiag_ctas_per_sm();
 }
 
-// back to the default schedule (projection from 128 orbitals, bucket cut 3/4, two CTAs per SM,
-// 8 streams)
+// back to the default schedule (CUDA graphs, projection from 128 orbitals, bucket cut 3/4, two
+// CTAs per SM, 8 streams)
 extern "C" void tblite_gb300_batch_reset_schedule(void) {
+  g_batch_graphs = true;
   g_sp2_min_nao = SP2_MIN_NAO;
   g_cut_num = 3;
   g_cut_den = 4;
@@ -1178,7 +1179,7 @@ extern "C" void tblite_gb300_batch_reset_schedule(void) {
 // The batch schedule: projection threshold, bucket cut, CTAs per SM of the cluster
 // tridiagonalisation and side streams, as a short text for logs and benchmark records.
 extern "C" int tblite_gb300_batch_schedule(char* buf, int n) {
-  char tmp[256];
+  char tmp[384];
   const int len = std::snprintf(
       tmp, sizeof(tmp),
       "projection from %d orbitals%s; bucket cut %d/%d; tridiagonalisation %d CTA(s) per SM; "
@@ -1192,8 +1193,8 @@ extern "C" int tblite_gb300_batch_schedule(char* buf, int n) {
   return len;
 }
 
-// Autotuner of the batch schedule (no counterpart in the reference): coordinate descent over the
-// projection threshold, the bucket cut, the CTAs per SM of the tridiagonalisation and the side
+// Autotuner of the batch schedule (no counterpart in the reference): coordinate descent over
+// CUDA graphs on/off, the projection threshold, the bucket cut, the CTAs per SM of the tridiagonalisation and the side
 // streams, each candidate timed (wall time of the call, best of two) on a seeded sample of the given
 // molecules; the fastest schedule stays set.  Returns the number of timed calls, or -1 if the
 // sample could not be evaluated (the schedule is then left as it was).
@@ -1252,13 +1253,18 @@ extern "C" int tblite_gb300_batch_autotune(tblite_context ctx, int nmol,
     set(keep);
   };
   int sp2 = sp2_keep, cut = num_keep * 10 + den_keep, ctas = ctas_keep, streams = streams_keep;
+  // CUDA graphs first (only switched off, never on against the caller's setting): a projection
+  // iteration is a long launch sequence whose graph is instantiated again whenever its step
+  // budget changes, which can cost more than the launches it saves
+  int graphs = g_batch_graphs ? 1 : 0;
+  if (graphs) try_values([](int v) { g_batch_graphs = v != 0; }, {0}, graphs);
   try_values([](int v) { g_sp2_min_nao = v; }, {128, 160, 224, 100000}, sp2);
   try_values([](int v) { g_cut_num = v / 10; g_cut_den = v % 10; }, {34, 23, 45}, cut);
   try_values([](int v) { tb::set_tridiag_ctas_per_sm(v); }, {1, 2}, ctas);
   try_values([](int v) { g_batch_streams = v; }, {4, 8}, streams);
-  char note[96];
-  std::snprintf(note, sizeof(note), "autotuned on %d molecules (%d calls, %.1f ms)", k, calls,
-                best);
+  char note[160];
+  std::snprintf(note, sizeof(note), "autotuned on %d molecules (%d calls, %.1f ms)%s", k, calls,
+                best, g_batch_graphs ? "" : "; SCF iterations launched directly");
   g_schedule_note = note;
   return calls;
 }

@@ -258,6 +258,11 @@ def batch_graphs():
     return b.value, n.value
 
 
+def batch_graphs_enabled() -> bool:
+    """Whether batched SCF iterations run as CUDA graphs (the autotuner may switch them off)."""
+    return bool(load().tblite_gb300_batch_last_graphs(None, None))
+
+
 def batch_projected() -> int:
     """Molecules of the last batch call whose SCF density came from the spectral projection."""
     return int(load().tblite_gb300_batch_last_projected())
