@@ -92,6 +92,14 @@ static void species_c6(const std::vector<int>& species, std::vector<double>& c6r
         }
 }
 
+// An element the element-data pack does not cover: the error names the library whose tables
+// hold the real values (none of them ships with the reference's source tree)
+[[noreturn]] static void pack_missing(const char* what, const char* origin, int z) {
+  throw std::runtime_error(std::string("element data pack '") + EXT_PACK_NAME + "' has no " +
+                           what + " for Z=" + std::to_string(z) + " (" + origin +
+                           " data, not part of this build)");
+}
+
 // D4 model data of the molecule's species (element-data pack)
 static void build_d4_data(_tblite_calculator* c, const _tblite_structure* mol) {
   // the reference builds its D4 model with the default smooth-cutoff widths of 0 (hard cutoffs,
@@ -107,8 +115,7 @@ static void build_d4_data(_tblite_calculator* c, const _tblite_structure* mol) {
   c->d4_nsp = (int)species.size();
   for (int z : species)
     if (EXT_D4_NREF[z - 1] <= 0 || std::isnan(EXT_D4_ZEFF[z - 1]))
-      throw std::runtime_error(std::string("element data pack '") + EXT_PACK_NAME +
-                               "' has no D4 data for Z=" + std::to_string(z));
+      pack_missing("D4 reference data", "dftd4 v4.2.0", z);
   for (int i = 0; i < mol->nat; ++i) {
     const int z = mol->num[i];
     c->d4_sp.push_back((int)(std::find(species.begin(), species.end(), z) - species.begin()));
@@ -137,8 +144,7 @@ static void build_d3_data(_tblite_calculator* c, const _tblite_structure* mol) {
   for (int i = 0; i < mol->nat; ++i) {
     const int z = mol->num[i];
     if (EXT_D4_NREF[z - 1] <= 0 || std::isnan(EXT_D4_R4R2[z - 1]) || std::isnan(EXT_D4_RCOV[z - 1]))
-      throw std::runtime_error(std::string("element data pack '") + EXT_PACK_NAME +
-                               "' has no D3 data for Z=" + std::to_string(z));
+      pack_missing("D3 reference data", "s-dftd3 v1.4.0", z);
     c->d3_sp.push_back((int)(std::find(species.begin(), species.end(), z) - species.begin()));
     c->d3_nref.push_back(EXT_D4_NREF[z - 1]);
     for (int r = 0; r < D4_MREF; ++r) c->d3_refcn.push_back(EXT_D4_REFCN[(z - 1) * D4_MREF + r]);
@@ -284,8 +290,7 @@ static void build_calculator(_tblite_calculator* c, const _tblite_structure* mol
     const bool pairs = mol->nat > 1;
     const double en = e->en, rad = EXT_RAD[z - 1], rcov = EXT_RCOV[z - 1];
     if (pairs && (std::isnan(en) || std::isnan(rad) || std::isnan(rcov)))
-      throw std::runtime_error(std::string("element data pack '") + EXT_PACK_NAME +
-                               "' has no entry for Z=" + std::to_string(z));
+      pack_missing("covalent radius, electronegativity or atomic radius", "mctc-lib v0.5.2", z);
     c->at_en.push_back(pairs ? en : 0.0);
     c->at_rad.push_back(pairs ? rad : 1.0);
     c->at_rcov.push_back(pairs ? rcov : 1.0);

@@ -110,6 +110,12 @@ def test_unsupported_element_message():
 
     with pytest.raises(TBLiteRuntimeError, match="d shells"):
         interface.Calculator("GFN2-xTB", [26, 1], [[0, 0, 0], [0, 0, 3.0]])
+    # fluorine has no d shell, but the element-data pack covers H, C, N, O only: the error names
+    # the library whose tables are missing
+    with pytest.raises(TBLiteRuntimeError, match=r"Z=9 \(mctc-lib v0\.5\.2 data"):
+        interface.Calculator("GFN2-xTB", [9, 1], [[0, 0, 0], [0, 0, 1.7]])
+    with pytest.raises(TBLiteRuntimeError, match=r"Z=9 \(mctc-lib v0\.5\.2 data"):
+        interface.Calculator("GFN1-xTB", [9, 1], [[0, 0, 0], [0, 0, 1.7]])
 
 
 def test_density_solver_setting():
