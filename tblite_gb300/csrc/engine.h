@@ -500,6 +500,9 @@ void sp2_gap_b(const BatchLaunch& b);
 void sp2_weighted_b(const BatchLaunch& b);
 void sp2_pipe_check_b(const BatchLaunch& b);  // flag -5 for a molecule whose pipe wait ran out
 void sp2_square_b(const BatchLaunch& b);  // ozaki_pipe.cu: C = Y Y of the iterating molecules
+// ozaki_pipe.cu: the next iterate into Y (init: D0 from A and the Gershgorin bounds; else D^2
+// or 2D - D^2 as decided), its line exponents and slice image
+void sp2_step_b(const BatchLaunch& b, bool init);
 constexpr int SP2_MIN_NAO = 128;   // smallest orbital count that takes the projection
 constexpr int SP2_MAX_STEPS = 64;  // squarings per projection at most
 

@@ -452,20 +452,6 @@ __device__ __forceinline__ int lines_padded(int n) { return ((n + PP_M - 1) / PP
 __device__ __forceinline__ bool sq_skip(const MolPtrs& q) {
   return *q.flag < 0 || q.sp2i[0] != 0;
 }
-__global__ void __launch_bounds__(256) kb_pexp_sq(const MolPtrs* __restrict__ mp,
-                                                  const int* __restrict__ list) {
-  const MolPtrs& q = mp[list[blockIdx.z]];
-  const int n = q.m.nao, lp = lines_padded(n);
-  if (sq_skip(q) || (int)blockIdx.x * 32 >= lp) return;
-  pexp_rows_dev(q.Y, n, n, n, lp, q.iexp, blockIdx.x);
-}
-__global__ void __launch_bounds__(256) kb_psplit_sq(const MolPtrs* __restrict__ mp,
-                                                    const int* __restrict__ list) {
-  const MolPtrs& q = mp[list[blockIdx.z]];
-  const int n = q.m.nao, lp = lines_padded(n), nkc = (n + PP_KC - 1) / PP_KC;
-  if (sq_skip(q) || (int)blockIdx.x >= lp / 64 || (int)blockIdx.y >= nkc) return;
-  psplit_dev(q.Y, n, 0, n, n, lp / 64, q.iexp, q.img, blockIdx.x, blockIdx.y);
-}
 __global__ void __launch_bounds__(PP_THREADS, 1) kb_opipe_sq(const MolPtrs* __restrict__ mp,
                                                             const int* __restrict__ list) {
   const MolPtrs& q = mp[list[blockIdx.y]];
@@ -495,6 +481,72 @@ __global__ void __launch_bounds__(PP_THREADS, 1) kb_opipe_sq(const MolPtrs* __re
                                          (unsigned long long)min(PP_N, n - j0) * (unsigned)n);
   }
   opipe_tile(a, blockIdx.x);
+}
+
+// ---- one projection step per molecule without a separate exponent or split pass: each warp
+// owns one line i of the symmetric iterate (column i in memory, which equals row i), forms
+// the new iterate there (init: D0 = (emax I - A) / (emax - emin); else D^2 or 2D - D^2 as
+// kb_sp2_decide chose), writes it back, takes the line's exponent from its largest element and
+// writes the line's slices (the same bits as pexp_rows_dev + psplit_dev on the row, since the
+// iterate is exactly symmetric).  Padding lines and k positions get zero slices.
+__global__ void __launch_bounds__(256) kb_sp2_step(const MolPtrs* __restrict__ mp,
+                                                   const int* __restrict__ list, int init) {
+  const MolPtrs& q = mp[list[blockIdx.z]];
+  const int n = q.m.nao, lp = lines_padded(n);
+  const int i = (int)blockIdx.x * 8 + (int)(threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (i >= lp || *q.flag < 0) return;
+  int u = 2;  // 2: the start D0 from A
+  double emax = 0.0, f = 0.0;
+  if (init) {
+    emax = q.sp2s[1];
+    f = 1.0 / (emax - q.sp2s[0]);
+  } else {
+    u = q.sp2i[2];  // -1 once converged
+    if (u < 0) return;
+  }
+  double mx = 0.0;
+  if (i < n) {
+    double* y = q.Y + (size_t)i * n;
+    const double* c = q.C + (size_t)i * n;
+    const double* am = q.A + (size_t)i * n;
+    for (int k = lane; k < n; k += 32) {
+      const double v =
+          u == 2 ? ((k == i ? emax : 0.0) - am[k]) * f : (u ? c[k] : 2.0 * y[k] - c[k]);
+      y[k] = v;
+      mx = fmax(mx, fabs(v));
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  const int ei = mx > 0.0 ? ilogb(mx) + 1 : 0;
+  if (lane == 0) q.iexp[i] = ei;
+  const int nkc = (n + PP_KC - 1) / PP_KC, nlb = lp / 64, lb = i >> 6, li = i & 63;
+  // this lane's element of every k chunk: position c = lane & 7 of 16-byte chunk g = lane >> 3
+  const size_t lane_off =
+      (size_t)li * 32 + (size_t)(((lane >> 3) ^ ((li >> 1) & 3)) << 3) + (size_t)(lane & 7);
+  const double* y = q.Y + (size_t)i * n;
+  for (int kc = 0; kc < nkc; ++kc) {
+    const int k = kc * PP_KC + lane;
+    const double x = (i < n && k < n) ? y[k] : 0.0;  // this lane wrote y[k] above
+    const uint64_t bits = (uint64_t)__double_as_longlong(x);
+    const uint32_t sign = (uint32_t)(bits >> 63);
+    const int ex = (int)((bits >> 52) & 0x7FF);
+    uint64_t Y = 0;
+    if (ex != 0) {  // zero and subnormals give zero slices
+      const uint64_t m = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+      const int sh = ex - ei - 1019;  // Y = |x| 2^(56 - e) < 2^56
+      if (sh >= 0) Y = m << sh;
+      else if (sh > -64) Y = m >> (-sh);
+    }
+#pragma unroll
+    for (int p = 0; p < 8; ++p) {
+      const uint32_t sb = slice_bits((uint32_t)(Y >> (49 - 7 * p)) & 0x7Fu, p, sign);
+      const uint32_t hi = __shfl_xor_sync(0xffffffffu, sb, 1);
+      if (!(lane & 1))  // even k in the low half, odd k in the high half of a 32-bit word
+        *reinterpret_cast<uint32_t*>(q.img + (((size_t)kc * 8 + p) * nlb + lb) * 2048 +
+                                     lane_off) = sb | (hi << 16);
+    }
+  }
 }
 
 // ---- batched GEMM sites on the pipe (projection buckets): the rows of op(A) go into img,
@@ -600,8 +652,19 @@ void pipe_site_b(const BatchLaunch& b, int site) {
   prof_kend(KS_PIPE, tk, b.s);
 }
 
-// one squaring step of the batched spectral projection: slice image of Y, then C = Y Y on the
-// tensor cores, for every listed molecule still iterating
+// the new iterate with its exponents and slice image (init: D0 from A), for every listed
+// molecule still iterating
+void sp2_step_b(const BatchLaunch& b, bool init) {
+  if (!b.count) return;
+  const int lp = pimage_lines(b.nao_max);
+  const int tk = prof_kbegin(b.s);
+  ++g_kernel_launches;
+  kb_sp2_step<<<dim3(lp / 8, 1, b.count), 256, 0, b.s>>>(b.mp, b.list, init ? 1 : 0);
+  prof_kend(KS_PIPE, tk, b.s);
+}
+
+// one squaring of the batched spectral projection: C = Y Y on the tensor cores from the slice
+// image that sp2_step_b wrote, for every listed molecule still iterating
 void sp2_square_b(const BatchLaunch& b) {
   if (!b.count) return;
   static bool attr = false;
@@ -611,12 +674,9 @@ void sp2_square_b(const BatchLaunch& b) {
     attr = true;
   }
   const int n = b.nao_max;
-  const int lp = pimage_lines(n), nkc = (n + PP_KC - 1) / PP_KC;
   const int tiles = ((n + PP_M - 1) / PP_M) * ((n + PP_N - 1) / PP_N);
   const int tk = prof_kbegin(b.s);
-  g_kernel_launches += 3;
-  kb_pexp_sq<<<dim3(lp / 32, 1, b.count), 256, 0, b.s>>>(b.mp, b.list);
-  kb_psplit_sq<<<dim3(lp / 64, nkc, b.count), 256, 0, b.s>>>(b.mp, b.list);
+  ++g_kernel_launches;
   kb_opipe_sq<<<dim3(tiles, b.count), PP_THREADS, PP_SMEM, b.s>>>(b.mp, b.list);
   prof_kend(KS_PIPE, tk, b.s);
 }

@@ -15,7 +15,9 @@
 //
 // Per molecule and SCF iteration the eigensolver's tridiagonalisation, eigenvalues, inverse
 // iteration and back-transformation (FP64 cores) become ~25 symmetric squarings on the BF16
-// tensor cores with FP64-accurate operand splitting (ozaki_pipe.cu, kb_opipe_sq).  Every
+// tensor cores with FP64-accurate operand splitting (ozaki_pipe.cu: kb_opipe_sq squares from
+// the slice image; kb_sp2_step forms the next iterate, its exponents and its image in one pass
+// over the matrix, so a step is three launches: square, decide, step).  Every
 // molecule of a size bucket iterates in lockstep; each decides its own step on the device and
 // stops on its own (its later launches return at once).  The host launches a step budget per
 // bucket (the most steps any of its molecules took in the previous SCF iteration plus a margin);
@@ -97,19 +99,6 @@ __global__ void __launch_bounds__(256) kb_sp2_start(BARGS) {
   }
 }
 
-// D0 = (emax I - A) / (emax - emin) into Y
-__global__ void kb_sp2_init(BARGS) {
-  BMOL;
-  if (*q.flag < 0) return;
-  const int n = q.m.nao;
-  const size_t nn = (size_t)n * n;
-  const double emin = q.sp2s[0], emax = q.sp2s[1];
-  const double f = 1.0 / (emax - emin);
-  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < nn;
-       t += (size_t)gridDim.x * blockDim.x)
-    q.Y[t] = (((t % (n + 1)) == 0 ? emax : 0.0) - q.A[t]) * f;
-}
-
 // traces of D (Y) and D^2 (C), idempotency error, convergence and the next update (one block
 // per molecule)
 __global__ void __launch_bounds__(256) kb_sp2_decide(BARGS) {
@@ -151,18 +140,6 @@ __global__ void __launch_bounds__(256) kb_sp2_decide(BARGS) {
   q.sp2i[1] = k + 1;
 }
 
-// D <- D^2 or 2D - D^2
-__global__ void kb_sp2_update(BARGS) {
-  BMOL;
-  if (*q.flag < 0) return;
-  const int u = q.sp2i[2];
-  if (u < 0) return;
-  const size_t nn = (size_t)q.m.nao * q.m.nao;
-  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < nn;
-       t += (size_t)gridDim.x * blockDim.x)
-    q.Y[t] = u ? q.C[t] : 2.0 * q.Y[t] - q.C[t];
-}
-
 // after the step budget: a projection that has not converged sends the molecule to the
 // one-molecule path; the steps taken go to the host (budget of the next SCF iteration)
 __global__ void kb_sp2_finish(BARGS) {
@@ -183,26 +160,20 @@ __global__ void kb_sp2_gap(BARGS) {
   if (q.emo[nocc] - q.emo[nocc - 1] < SP2_GAP_KT * q.kt) *q.flag = -7;
 }
 
-inline unsigned ew_blocks(const BatchLaunch& b) {
-  const size_t nn = (size_t)b.nao_max * b.nao_max;
-  const size_t blocks = (nn + 255) / 256;
-  return (unsigned)(blocks < 64 ? blocks : 64);
-}
-
 }  // namespace
 
 void sp2_density_b(const BatchLaunch& b, int steps) {
   if (!b.count) return;
   pipe_site_b(b, GS_FX);   // T1 = F X
   pipe_site_b(b, GS_XTT);  // A = X^T T1
-  g_kernel_launches += 2;
+  ++g_kernel_launches;
   kb_sp2_start<<<dim3(1, 1, b.count), 256, 0, b.s>>>(b.mp, b.list);
-  kb_sp2_init<<<dim3(ew_blocks(b), 1, b.count), 256, 0, b.s>>>(b.mp, b.list);
+  sp2_step_b(b, true);  // D0 and its slice image
   for (int k = 0; k < steps; ++k) {
     sp2_square_b(b);
-    g_kernel_launches += 2;
+    ++g_kernel_launches;
     kb_sp2_decide<<<dim3(1, 1, b.count), 256, 0, b.s>>>(b.mp, b.list);
-    kb_sp2_update<<<dim3(ew_blocks(b), 1, b.count), 256, 0, b.s>>>(b.mp, b.list);
+    sp2_step_b(b, false);  // the update and its slice image for the next squaring
   }
   ++g_kernel_launches;
   kb_sp2_finish<<<dim3(1, 1, b.count), 32, 0, b.s>>>(b.mp, b.list);
