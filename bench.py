@@ -508,7 +508,8 @@ def run_batch(args):
     library.load().tblite_gb300_batch_last_iterations(library._ip(iters_s), count)
     _, tri_flops_s = _ensemble_flops(nao, nel, np.maximum(iters_s, 0), _modes(count))
     t_tri, c_tri = kser["tridiag"]
-    t_pipe, c_pipe = kser["projection_squaring"]
+    t_pipe, c_pipe = kser["pipe_products"]
+    t_prep, c_prep = kser["pipe_operands"]
     peaks, peak_kind = _peaks()
     bf16 = peaks.get("bf16_tflops_sustained", peaks["bf16_tflops"])
     timing = ("CUDA events around each launch on its stream, one untimed call with the size "
@@ -528,8 +529,8 @@ def run_batch(args):
     pipe_roof = None
     if t_pipe and pipe_flops_s:
         ach = SPLIT_SLICE_PRODUCTS * pipe_flops_s / (t_pipe / 1000.0) / 1e12
-        pipe_roof = {"kernel": "projection squarings (slice images + pipelined split GEMM on "
-                               "tcgen05, batched: kb_pexp_sq, kb_psplit_sq, kb_opipe_sq)",
+        pipe_roof = {"kernel": "batched pipelined split GEMM on tcgen05 (projection squarings "
+                               "kb_opipe_sq and product sites kb_opipe_site)",
                      "bound": "tensor", "achieved": round(ach, 4), "peak": round(bf16, 4),
                      "unit": "TFLOP/s", "frac": round(ach / bf16, 4), "timing": timing,
                      "traffic": _profile_traffic("pipe_sq_ensemble512.md"),
@@ -538,7 +539,11 @@ def run_batch(args):
                      "work_note": "36 BF16 slice products per FP64-equivalent flop; FP64-"
                                   "equivalent flop counted on the device (2 m n K per tile)",
                      "fp64_equivalent_tflops": round(pipe_flops_s / (t_pipe / 1000.0) / 1e12, 4),
-                     "ms_per_call": round(t_pipe, 3), "launches_per_call": c_pipe}
+                     "ms_per_call": round(t_pipe, 3), "launches_per_call": c_pipe,
+                     "ms_per_launch": round(t_pipe / c_pipe, 4) if c_pipe else None,
+                     "operands": {"kernels": "kb_sp2_step, kb_pexp_site, kb_psplit_site "
+                                             "(HBM-bound: new iterate, exponents, slice images)",
+                                  "ms_per_call": round(t_prep, 3), "launches_per_call": c_prep}}
     if pipe_roof is not None and t_pipe >= t_tri:
         roofline, other = pipe_roof, tri_roof
     else:

@@ -102,7 +102,10 @@ int tblite_gb300_get_profile(double* phase_ms, int* phase_count, int nphase, dou
 /* per-kernel device times (ms, summed) and launch counts of the last single point, from CUDA
  * events around each launch on the engine stream (profiling enabled).  Slots: 0 Householder
  * tridiagonalisation, 1 eigenvalue multisection, 2 inverse iteration, 3 back-transformation,
- * 4 FP64 GEMM (all uses), 5 Fock assembly, 6 Mulliken column sums.  Returns the slot count. */
+ * 4 GEMM (all uses outside the pipelined split GEMM), 5 Fock assembly, 6 Mulliken column sums,
+ * 7 pipelined split GEMM products of the batch (kb_opipe_sq, kb_opipe_site), 8 their operand
+ * preparation (projection steps kb_sp2_step, exponents and slice images of the GEMM sites).
+ * Returns the slot count. */
 int tblite_gb300_get_kernel_profile(double* kernel_ms, int* kernel_count, int nslot);
 
 /* channels of the bond orders tblite_get_result_bond_orders copies: 1 for a closed shell

@@ -33,7 +33,8 @@ int device_sm_count();
 // per-kernel CUDA-event timing (only while profiling is enabled): prof_kbegin records an event
 // on s and returns a token (-1 when disabled); prof_kend closes it for the given slot
 enum { KS_TRIDIAG = 0, KS_MULTISECT, KS_INVIT, KS_BACKTRANSFORM, KS_GEMM, KS_FOCK, KS_MULLIKEN,
-       KS_PIPE,  // squarings of the batched spectral projection on the pipelined split GEMM
+       KS_PIPE,       // batched products on the pipelined split GEMM (squarings and sites)
+       KS_PIPE_PREP,  // their operands: projection steps, exponents and slice images
        KS_COUNT };
 int prof_kbegin(cudaStream_t s);
 void prof_kend(int slot, int token, cudaStream_t s);

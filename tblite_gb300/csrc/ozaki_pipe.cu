@@ -642,12 +642,14 @@ void pipe_site_b(const BatchLaunch& b, int site) {
   const int n = b.nao_max;
   const int lp = pimage_lines(n), nkc = (n + PP_KC - 1) / PP_KC;
   const int tiles = ((n + PP_M - 1) / PP_M) * ((n + PP_N - 1) / PP_N);
-  const int tk = prof_kbegin(b.s);
+  int tk = prof_kbegin(b.s);
   g_kernel_launches += 5;
   for (int which = 0; which < 2; ++which) {
     kb_pexp_site<<<dim3(lp / 8, 1, b.count), 256, 0, b.s>>>(b.mp, b.list, site, which);
     kb_psplit_site<<<dim3(lp / 64, nkc, b.count), 256, 0, b.s>>>(b.mp, b.list, site, which);
   }
+  prof_kend(KS_PIPE_PREP, tk, b.s);
+  tk = prof_kbegin(b.s);
   kb_opipe_site<<<dim3(tiles, b.count), PP_THREADS, PP_SMEM, b.s>>>(b.mp, b.list, site);
   prof_kend(KS_PIPE, tk, b.s);
 }
@@ -660,7 +662,7 @@ void sp2_step_b(const BatchLaunch& b, bool init) {
   const int tk = prof_kbegin(b.s);
   ++g_kernel_launches;
   kb_sp2_step<<<dim3(lp / 8, 1, b.count), 256, 0, b.s>>>(b.mp, b.list, init ? 1 : 0);
-  prof_kend(KS_PIPE, tk, b.s);
+  prof_kend(KS_PIPE_PREP, tk, b.s);
 }
 
 // one squaring of the batched spectral projection: C = Y Y on the tensor cores from the slice

@@ -296,7 +296,7 @@ def get_profile():
 
 
 KERNEL_SLOTS = ("tridiag", "multisect", "invit", "backtransform", "gemm", "fock", "mulliken",
-                "projection_squaring")
+                "pipe_products", "pipe_operands")
 
 
 def get_kernel_profile():
