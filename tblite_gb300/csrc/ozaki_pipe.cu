@@ -422,11 +422,21 @@ __device__ __forceinline__ void opipe_tile(const PipeArgs& a, int b) {
           for (int t = 0; t < 16; ++t) {
             const int j = j0 + 32 * half + 16 * h + t;
             if (j < a.N && !(a.sym && i < j)) {
-              const int sc = ei + a.eB[j] - 14;
-              const double scale =
-                  (sc > -1022 && sc < 1023) ? __hiloint2double((sc + 1023) << 20, 0) : 0.0;
-              const double f = (double)__uint_as_float(v6[t]) + (double)__uint_as_float(v7[t]);
-              const double val = fma((double)T[16 * h + t], 0x1p-35, f) * scale;
+              // C = (T + F 2^35) 2^(sc - 35), F = levels 6 + 7 summed in FP32 (F < 2^-42 of
+              // the result, so its rounding is below 2^-66); the power of two goes into the
+              // exponent field by an integer add where the result stays normal: three FP64
+              // operations per element (two conversions and an add) instead of six
+              const int sc = ei + a.eB[j] - 14 - 35;
+              const float ff = (__uint_as_float(v6[t]) + __uint_as_float(v7[t])) * 0x1p35f;
+              const double sum = (double)T[16 * h + t] + (double)ff;
+              const long long sb = __double_as_longlong(sum);
+              const int se = (int)((sb >> 52) & 0x7FF);
+              double val;
+              if (sum == 0.0) val = 0.0;
+              else if (se > 0 && se + sc > 0 && se + sc < 2047)
+                val = __longlong_as_double(sb + ((long long)sc << 52));
+              else
+                val = ldexp(sum, sc);  // subnormal or out-of-range result: the general path
               a.C[i + (size_t)j * a.ldc] = val;
               if (a.sym && i != j) a.C[j + (size_t)i * a.ldc] = val;
             }
@@ -504,7 +514,10 @@ __global__ void __launch_bounds__(256) kb_sp2_step(const MolPtrs* __restrict__ m
     u = q.sp2i[2];  // -1 once converged
     if (u < 0) return;
   }
-  double mx = 0.0;
+  // the largest |v| of the line as bits: for non-negative doubles the unsigned order of the
+  // bit patterns is the numeric order (integer instructions instead of FP64 ones, which this
+  // GPU issues at 1/64 of the FP32 rate)
+  unsigned long long mb = 0ull;
   if (i < n) {
     double* y = q.Y + (size_t)i * n;
     const double* c = q.C + (size_t)i * n;
@@ -513,12 +526,18 @@ __global__ void __launch_bounds__(256) kb_sp2_step(const MolPtrs* __restrict__ m
       const double v =
           u == 2 ? ((k == i ? emax : 0.0) - am[k]) * f : (u ? c[k] : 2.0 * y[k] - c[k]);
       y[k] = v;
-      mx = fmax(mx, fabs(v));
+      const unsigned long long b = (unsigned long long)__double_as_longlong(v) & ~(1ull << 63);
+      mb = b > mb ? b : mb;
     }
   }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  const int ei = mx > 0.0 ? ilogb(mx) + 1 : 0;
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long b = __shfl_xor_sync(0xffffffffu, mb, o);
+    mb = b > mb ? b : mb;
+  }
+  // e = ilogb(max) + 1: the biased exponent field minus 1022 for a normal maximum
+  const int mexp = (int)(mb >> 52);
+  const int ei = mb == 0ull ? 0 : mexp > 0 ? mexp - 1022 : ilogb(__longlong_as_double((long long)mb)) + 1;
   if (lane == 0) q.iexp[i] = ei;
   const int nkc = (n + PP_KC - 1) / PP_KC, nlb = lp / 64, lb = i >> 6, li = i & 63;
   // this lane's element of every k chunk: position c = lane & 7 of 16-byte chunk g = lane >> 3
