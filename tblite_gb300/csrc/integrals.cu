@@ -249,19 +249,25 @@ __device__ __forceinline__ void h0_gradient_dev(DevMol m, Gfn2Scalars p, const d
                               const double* __restrict__ vqp, double* grad, double* sigma,
                               double* dEdcn, long long npair) {
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= npair) return;
+  // every thread reaches the warp-wide virial sum at the end: pairs that contribute nothing
+  // (outside the list, on one atom, beyond the cutoff) skip the work, not the sum
+  double vec[3] = {0.0, 0.0, 0.0}, dG[3] = {0.0, 0.0, 0.0};
+  do {
+  if (t >= npair) break;
   int ish, jsh;
   tri_index(t, ish, jsh);
   const int iat = m.sh_atom[ish], jat = m.sh_atom[jsh];
-  if (iat == jat) return;
-  double vec[3];
+  if (iat == jat) break;
   double r2 = 0.0;
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     vec[k] = m.xyz[3 * iat + k] - m.xyz[3 * jat + k];
     r2 += vec[k] * vec[k];
   }
-  if (r2 > p.h0_cutoff * p.h0_cutoff || r2 < 2.220446049250313e-16) return;
+  if (r2 > p.h0_cutoff * p.h0_cutoff || r2 < 2.220446049250313e-16) {
+    vec[0] = vec[1] = vec[2] = 0.0;
+    break;
+  }
   const int li = m.sh_l[ish], lj = m.sh_l[jsh];
   const int nci = 2 * li + 1, ncj = 2 * lj + 1;
   const double rr = sqrt(sqrt(r2) / (m.at_rad[iat] + m.at_rad[jat]));
@@ -316,7 +322,7 @@ __device__ __forceinline__ void h0_gradient_dev(DevMol m, Gfn2Scalars p, const d
       ws[cj][ci] = -pij * (vao[ja] + vao[ia]) + 2.0 * pij * hij - 2.0 * wij;
     }
   }
-  double dG[3] = {0, 0, 0}, PS = 0.0, PD[3] = {0, 0, 0};
+  double PS = 0.0, PD[3] = {0, 0, 0};
   const int npi = m.sh_nprim[ish], npj = m.sh_nprim[jsh];
   const double pi3 = 5.568327996831708;
   for (int ip = 0; ip < npi; ++ip) {
@@ -391,10 +397,20 @@ __device__ __forceinline__ void h0_gradient_dev(DevMol m, Gfn2Scalars p, const d
     atomicAdd(grad + 3 * iat + c, dG[c]);
     atomicAdd(grad + 3 * jat + c, -dG[c]);
   }
+  } while (false);
+  // virial: the six distinct elements of the symmetric 3 x 3 summed over the warp, then one
+  // atomic per element and warp (every pair of a molecule adds to the same nine numbers)
+  const int va[6] = {0, 0, 1, 0, 1, 2}, vb[6] = {0, 1, 1, 2, 2, 2};
 #pragma unroll
-  for (int a = 0; a < 3; ++a)
+  for (int e = 0; e < 6; ++e) {
+    double v = 0.5 * (vec[va[e]] * dG[vb[e]] + dG[va[e]] * vec[vb[e]]);
 #pragma unroll
-    for (int c = 0; c < 3; ++c) atomicAdd(sigma + 3 * a + c, 0.5 * (vec[a] * dG[c] + dG[a] * vec[c]));
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0 && v != 0.0) {
+      atomicAdd(sigma + 3 * va[e] + vb[e], v);
+      if (va[e] != vb[e]) atomicAdd(sigma + 3 * vb[e] + va[e], v);
+    }
+  }
 }
 __global__ void k_h0_gradient(DevMol m, Gfn2Scalars p, const double* __restrict__ se,
                               const double* __restrict__ P, const double* __restrict__ W,
