@@ -235,6 +235,79 @@ void launch_build_h0(const DevMol& m, const Gfn2Scalars& p, const double* se, do
   k_build_h0<<<(unsigned)((nthr + bs - 1) / bs), bs, 0, s>>>(m, p, se, S, H, D, Q, npair);
 }
 
+// One primitive pair of the H0 gradient for shells of angular momenta LI (bra, A) and LJ
+// (ket, B): for every component pair the overlap, the dipole moments about A (PS, PD) and the
+// derivative of the multipole-potential integral and of the overlap with respect to A.  The
+// 1-d factors O(p, b) come from one table per direction; the derivative of the product along
+// c is written as sum_e G_c[e] T_c(e), with T_c(e) the polynomial's coefficients times the
+// products of the other two directions' factors (fewer FP64 operations than expanding the ten
+// monomials per direction).
+template <int LI, int LJ>
+__device__ __forceinline__ void h0g_prim(const Moments& M, const double (&vec)[3], double ai,
+                                         double cc, const double (&wp)[3][3],
+                                         const double (&ws)[3][3], double c0,
+                                         const double (&c1)[3], const double (&c2)[6],
+                                         double (&dG)[3], double& PS, double (&PD)[3]) {
+  double T[3][2][5];  // O(p, b) of direction k, p = 0..4
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+#pragma unroll
+    for (int p = 0; p < 5; ++p) {
+      T[k][0][p] = M.m[k][p];
+      T[k][1][p] = LJ ? M.m[k][p + 1] + vec[k] * M.m[k][p] : 0.0;
+    }
+  const double a2 = 2.0 * ai;
+#pragma unroll
+  for (int cj = 0; cj < 2 * LJ + 1; ++cj)
+#pragma unroll
+    for (int ci = 0; ci < 2 * LI + 1; ++ci) {
+      double V[3][3], G[3][3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const int a = (LI == 1 && ci == k) ? 1 : 0, b = (LJ == 1 && cj == k) ? 1 : 0;
+#pragma unroll
+        for (int e = 0; e < 3; ++e) {
+          V[k][e] = T[k][b][a + e];
+          G[k][e] = a ? a2 * T[k][b][a + 1 + e] - T[k][b][a - 1 + e] : a2 * T[k][b][1 + e];
+        }
+      }
+      const double w_p = wp[cj][ci] * cc, w_s = ws[cj][ci] * cc;
+      // products of the two other directions' factors, (e1, e2) = 00, 10, 01, 20, 11, 02
+      const double p12[6] = {V[1][0] * V[2][0], V[1][1] * V[2][0], V[1][0] * V[2][1],
+                             V[1][2] * V[2][0], V[1][1] * V[2][1], V[1][0] * V[2][2]};
+      const double p02[6] = {V[0][0] * V[2][0], V[0][1] * V[2][0], V[0][0] * V[2][1],
+                             V[0][2] * V[2][0], V[0][1] * V[2][1], V[0][0] * V[2][2]};
+      const double p01[6] = {V[0][0] * V[1][0], V[0][1] * V[1][0], V[0][0] * V[1][1],
+                             V[0][2] * V[1][0], V[0][1] * V[1][1], V[0][0] * V[1][2]};
+      PS += w_p * (V[0][0] * p12[0]);
+      PD[0] += w_p * (V[0][1] * p12[0]);
+      PD[1] += w_p * (V[0][0] * p12[1]);
+      PD[2] += w_p * (V[0][0] * p12[2]);
+      // monomial coefficients: 1 c0; x, y, z c1[0..2]; xx, xy, yy, xz, yz, zz c2[0..5]
+      {  // derivative along x: the other directions are y (first) and z (second)
+        const double t0 = c0 * p12[0] + c1[1] * p12[1] + c1[2] * p12[2] + c2[2] * p12[3] +
+                          c2[4] * p12[4] + c2[5] * p12[5];
+        const double t1 = c1[0] * p12[0] + c2[1] * p12[1] + c2[3] * p12[2];
+        const double t2 = c2[0] * p12[0];
+        dG[0] += w_s * (G[0][0] * p12[0]) - w_p * (G[0][0] * t0 + G[0][1] * t1 + G[0][2] * t2);
+      }
+      {  // along y: the others are x and z
+        const double t0 = c0 * p02[0] + c1[0] * p02[1] + c1[2] * p02[2] + c2[0] * p02[3] +
+                          c2[3] * p02[4] + c2[5] * p02[5];
+        const double t1 = c1[1] * p02[0] + c2[1] * p02[1] + c2[4] * p02[2];
+        const double t2 = c2[2] * p02[0];
+        dG[1] += w_s * (G[1][0] * p02[0]) - w_p * (G[1][0] * t0 + G[1][1] * t1 + G[1][2] * t2);
+      }
+      {  // along z: the others are x and y
+        const double t0 = c0 * p01[0] + c1[0] * p01[1] + c1[1] * p01[2] + c2[0] * p01[3] +
+                          c2[1] * p01[4] + c2[2] * p01[5];
+        const double t1 = c1[2] * p01[0] + c2[3] * p01[1] + c2[4] * p01[2];
+        const double t2 = c2[5] * p01[0];
+        dG[2] += w_s * (G[2][0] * p01[0]) - w_p * (G[2][0] * t0 + G[2][1] * t1 + G[2][2] * t2);
+      }
+    }
+}
+
 // ---------------------------------------------------------------------------------------
 // H0 gradient: one thread per cross-atom shell pair (ish > jsh).  The reference formula
 // (h0.f90:528-560) is contracted on the fly:
@@ -339,43 +412,19 @@ __device__ __forceinline__ void h0_gradient_dev(DevMol m, Gfn2Scalars p, const d
       for (int k = 0; k < 3; ++k) pa[k] = -vec[k] * aj * oeta;
       Moments M;
       gauss_moments(pa, eta, M);
-      for (int cj = 0; cj < ncj; ++cj) {
-        for (int ci = 0; ci < nci; ++ci) {
-          double V[3][3], G[3][3];
-#pragma unroll
-          for (int k = 0; k < 3; ++k) {
-            const int a = cexp(li, ci, k), b = cexp(lj, cj, k);
-#pragma unroll
-            for (int e = 0; e < 3; ++e) {
-              V[k][e] = O1(M, k, a + e, b, vec[k]);
-              double g = 2.0 * ai * O1(M, k, a + 1 + e, b, vec[k]);
-              if (a > 0) g -= a * O1(M, k, a - 1 + e, b, vec[k]);
-              G[k][e] = g;
-            }
-          }
-          const double s = V[0][0] * V[1][0] * V[2][0];
-          const double w_p = wp[cj][ci] * cc, w_s = ws[cj][ci] * cc;
-          PS += w_p * s;
-          PD[0] += w_p * V[0][1] * V[1][0] * V[2][0];
-          PD[1] += w_p * V[0][0] * V[1][1] * V[2][0];
-          PD[2] += w_p * V[0][0] * V[1][0] * V[2][1];
-#pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            // product of 1-d factors with exponents (ex,ey,ez); the ket derivative acts on c
-            auto f = [&](int ex, int ey, int ez) {
-              const int e[3] = {ex, ey, ez};
-              double r = 1.0;
-#pragma unroll
-              for (int k = 0; k < 3; ++k) r *= (k == c) ? G[k][e[k]] : V[k][e[k]];
-              return r;
-            };
-            const double dS = f(0, 0, 0);
-            double dO = c0 * dS + c1[0] * f(1, 0, 0) + c1[1] * f(0, 1, 0) + c1[2] * f(0, 0, 1)
-                        + c2[0] * f(2, 0, 0) + c2[1] * f(1, 1, 0) + c2[2] * f(0, 2, 0)
-                        + c2[3] * f(1, 0, 1) + c2[4] * f(0, 1, 1) + c2[5] * f(0, 0, 2);
-            dG[c] += w_s * dS - w_p * dO;
-          }
-        }
+      switch (2 * li + lj) {  // shell kinds as template arguments: the 1-d factors of all
+        case 0:               // angular components are shared by the compiler
+          h0g_prim<0, 0>(M, vec, ai, cc, wp, ws, c0, c1, c2, dG, PS, PD);
+          break;
+        case 1:
+          h0g_prim<0, 1>(M, vec, ai, cc, wp, ws, c0, c1, c2, dG, PS, PD);
+          break;
+        case 2:
+          h0g_prim<1, 0>(M, vec, ai, cc, wp, ws, c0, c1, c2, dG, PS, PD);
+          break;
+        default:
+          h0g_prim<1, 1>(M, vec, ai, cc, wp, ws, c0, c1, c2, dG, PS, PD);
+          break;
       }
     }
   }
