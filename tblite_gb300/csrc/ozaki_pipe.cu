@@ -592,13 +592,20 @@ __global__ void __launch_bounds__(256) kb_sp2_step(const MolPtrs* __restrict__ m
     double* y = q.Y + (size_t)i * n;
     const double* c = q.C + (size_t)i * n;
     const double* am = q.A + (size_t)i * n;
-    for (int k = lane; k < n; k += 32) {
-      const double v =
-          u == 2 ? ((k == i ? emax : 0.0) - am[k]) * f : (u ? c[k] : 2.0 * y[k] - c[k]);
+    // one loop per kind of update (u is uniform over the warp), so no FP64 operation is
+    // evaluated for a branch that is not taken: D^2 is a copy, 2D - D^2 one FMA per element
+    auto put = [&](int k, double v) {
       y[k] = v;
       if (k == i) yd_next[i] = v;
       const unsigned long long b = (unsigned long long)__double_as_longlong(v) & ~(1ull << 63);
       mb = b > mb ? b : mb;
+    };
+    if (u == 1) {
+      for (int k = lane; k < n; k += 32) put(k, c[k]);
+    } else if (u == 0) {
+      for (int k = lane; k < n; k += 32) put(k, 2.0 * y[k] - c[k]);
+    } else {
+      for (int k = lane; k < n; k += 32) put(k, ((k == i ? emax : 0.0) - am[k]) * f);
     }
   }
 #pragma unroll
