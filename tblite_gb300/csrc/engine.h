@@ -456,17 +456,6 @@ struct Site {
   double alpha;  // power of two applied to the product (exact)
 };
 #ifdef __CUDACC__
-// State of a molecule's spectral projection in two slots by step parity: the step launch of
-// index k reads slot k & 1 and writes slot (k + 1) & 1, so no launch writes what its own blocks
-// still read.  Slot s: converged flag sp2i[4 + 2s], steps taken sp2i[5 + 2s], idempotency errors
-// e(k-1) sp2s[2 + 2s] and e(k-2) sp2s[3 + 2s], diagonal of the iterate T1[s n, s n + n) (T1 is
-// free between the reduction and P = 2 X D X^T).
-__device__ __forceinline__ int* sp2_conv(const MolPtrs& q, int s) { return q.sp2i + 4 + 2 * s; }
-__device__ __forceinline__ int* sp2_nstep(const MolPtrs& q, int s) { return q.sp2i + 5 + 2 * s; }
-__device__ __forceinline__ double* sp2_err(const MolPtrs& q, int s) { return q.sp2s + 2 + 2 * s; }
-__device__ __forceinline__ double* sp2_ydiag(const MolPtrs& q, int s) {
-  return q.T1 + (size_t)s * q.m.nao;
-}
 __device__ __forceinline__ Site site_of(const MolPtrs& q, int site) {
   const int n = q.m.nao, k = *q.icount;
   Site s{n, n, n, n, nullptr, false, nullptr, false, nullptr, KM_NONE, false, 1.0};
@@ -511,12 +500,10 @@ void sp2_density_b(const BatchLaunch& b, int steps);
 void sp2_gap_b(const BatchLaunch& b);
 void sp2_weighted_b(const BatchLaunch& b);
 void sp2_pipe_check_b(const BatchLaunch& b);  // flag -5 for a molecule whose pipe wait ran out
-// ozaki_pipe.cu: C = Y Y of the molecules still iterating before step launch `step`
-void sp2_square_b(const BatchLaunch& b, int step);
-// ozaki_pipe.cu: step launch `step` (-1: the start D0 from A and the Gershgorin bounds): traces,
-// stop test and choice of D^2 or 2D - D^2, then the next iterate into Y with its line exponents
-// and slice image
-void sp2_step_b(const BatchLaunch& b, int step);
+void sp2_square_b(const BatchLaunch& b);  // ozaki_pipe.cu: C = Y Y of the iterating molecules
+// ozaki_pipe.cu: the next iterate into Y (init: D0 from A and the Gershgorin bounds; else D^2
+// or 2D - D^2 as decided), its line exponents and slice image
+void sp2_step_b(const BatchLaunch& b, bool init);
 constexpr int SP2_MIN_NAO = 128;   // smallest orbital count that takes the projection
 constexpr int SP2_MAX_STEPS = 64;  // squarings per projection at most
 

@@ -457,15 +457,17 @@ __global__ void __launch_bounds__(PP_THREADS, 1) k_opipe(PipeArgs a) { opipe_til
 // ---- batched squaring X <- X X of the spectral projection: one symmetric product per molecule
 // of the list (blockIdx.z / blockIdx.y walks the molecules).  The iterate lives in Y, its slice
 // image in img (exponents iexp), the square goes to C.  Molecules that left the batch or whose
-// projection has converged (slot step & 1 of the projection state) launch nothing.
+// projection has converged (sp2i[0] != 0) launch nothing.
 __device__ __forceinline__ int lines_padded(int n) { return ((n + PP_M - 1) / PP_M) * PP_M; }
+__device__ __forceinline__ bool sq_skip(const MolPtrs& q) {
+  return *q.flag < 0 || q.sp2i[0] != 0;
+}
 __global__ void __launch_bounds__(PP_THREADS, 1) kb_opipe_sq(const MolPtrs* __restrict__ mp,
-                                                            const int* __restrict__ list,
-                                                            int step) {
+                                                            const int* __restrict__ list) {
   const MolPtrs& q = mp[list[blockIdx.y]];
   const int n = q.m.nao;
   const int tiles = ((n + PP_M - 1) / PP_M) * ((n + PP_N - 1) / PP_N);
-  if (*q.flag < 0 || *sp2_conv(q, step & 1) != 0 || (int)blockIdx.x >= tiles) return;
+  if (sq_skip(q) || (int)blockIdx.x >= tiles) return;
   PipeArgs a{};
   a.A = q.img;
   a.B = q.img;  // a symmetric matrix: its rows are its columns
@@ -491,99 +493,27 @@ __global__ void __launch_bounds__(PP_THREADS, 1) kb_opipe_sq(const MolPtrs* __re
   opipe_tile(a, blockIdx.x);
 }
 
-// ---- one projection step per molecule, decision included, without a separate exponent or
-// split pass.  Every block first takes the traces of D (its diagonal, kept by the launch that
-// formed D) and of D^2 (the diagonal of C) in the same fixed order, so all blocks reach the
-// same decision: the idempotency error tr(D - D^2), the stop test (the error no longer falls
-// over two steps, Kruchinin, Rubensson, Niklasson 2016, or reaches the rounding floor) and the
-// update D^2 or 2D - D^2 whose trace is closer to the occupied count (Niklasson 2002); the
-// first block records it in the next state slot.  Then each warp owns one line i of the
-// symmetric iterate (column i in memory, which equals row i), forms the new iterate there
-// (step -1: D0 = (emax I - A) / (emax - emin)), writes it back with its diagonal element,
-// takes the line's exponent from its largest element and writes the line's slices (the same
-// bits as pexp_rows_dev + psplit_dev on the row, since the iterate is exactly symmetric).
-// Padding lines and k positions get zero slices.
+// ---- one projection step per molecule without a separate exponent or split pass: each warp
+// owns one line i of the symmetric iterate (column i in memory, which equals row i), forms
+// the new iterate there (init: D0 = (emax I - A) / (emax - emin); else D^2 or 2D - D^2 as
+// kb_sp2_decide chose), writes it back, takes the line's exponent from its largest element and
+// writes the line's slices (the same bits as pexp_rows_dev + psplit_dev on the row, since the
+// iterate is exactly symmetric).  Padding lines and k positions get zero slices.
 __global__ void __launch_bounds__(256) kb_sp2_step(const MolPtrs* __restrict__ mp,
-                                                   const int* __restrict__ list, int step) {
+                                                   const int* __restrict__ list, int init) {
   const MolPtrs& q = mp[list[blockIdx.z]];
   const int n = q.m.nao, lp = lines_padded(n);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if ((int)blockIdx.x * 8 >= lp) return;
-  // the flag is read once per block: the first block may set it during this launch, and every
-  // thread of a block must take the same branch to the barrier below
-  __shared__ int leave;
-  if (threadIdx.x == 0) leave = *q.flag < 0;
-  __syncthreads();
-  if (leave) return;
-  const bool lead = blockIdx.x == 0 && threadIdx.x == 0;
-  const int rs = step & 1, ws = (step + 1) & 1;  // slot read, slot written
+  const int i = (int)blockIdx.x * 8 + (int)(threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (i >= lp || *q.flag < 0) return;
   int u = 2;  // 2: the start D0 from A
   double emax = 0.0, f = 0.0;
-  if (step < 0) {
+  if (init) {
     emax = q.sp2s[1];
     f = 1.0 / (emax - q.sp2s[0]);
-    if (lead) {
-      *sp2_conv(q, 0) = 0;
-      *sp2_nstep(q, 0) = 0;
-      sp2_err(q, 0)[0] = sp2_err(q, 0)[1] = 1e300;
-    }
   } else {
-    const int conv = *sp2_conv(q, rs), ks = *sp2_nstep(q, rs);
-    const double e1 = sp2_err(q, rs)[0], e2 = sp2_err(q, rs)[1];
-    if (conv) {  // carried forward, so the next launch reads a current slot
-      if (lead) {
-        *sp2_conv(q, ws) = 1;
-        *sp2_nstep(q, ws) = ks;
-        sp2_err(q, ws)[0] = e1;
-        sp2_err(q, ws)[1] = e2;
-      }
-      return;
-    }
-    if (q.sp2i[3] != 0) {  // a tensor-core wait ran out: the molecule takes the one-molecule path
-      if (lead) *q.flag = -5;
-      return;
-    }
-    __shared__ double red[2][8];
-    const double* yd = sp2_ydiag(q, rs);
-    double a = 0.0, b = 0.0;
-    for (int t = threadIdx.x; t < n; t += 256) {
-      a += yd[t];
-      b += q.C[t + (size_t)t * n];
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      a += __shfl_xor_sync(0xffffffffu, a, o);
-      b += __shfl_xor_sync(0xffffffffu, b, o);
-    }
-    if (lane == 0) {
-      red[0][warp] = a;
-      red[1][warp] = b;
-    }
-    __syncthreads();
-    double tx = 0.0, tx2 = 0.0;
-    for (int w = 0; w < 8; ++w) {
-      tx += red[0][w];
-      tx2 += red[1][w];
-    }
-    const double e = tx - tx2;
-    if (!(e == e)) {
-      if (lead) *q.flag = -6;
-      return;
-    }
-    const bool done = (ks >= 2 && e2 < 1e-4 * n && e >= e2) || e <= 1e-15 * n;
-    if (lead) {
-      *sp2_conv(q, ws) = done ? 1 : 0;
-      *sp2_nstep(q, ws) = done ? ks : ks + 1;
-      sp2_err(q, ws)[0] = e;
-      sp2_err(q, ws)[1] = e1;
-    }
-    if (done) return;
-    const double nocc = q.nalp;
-    u = fabs(tx2 - nocc) <= fabs(2.0 * tx - tx2 - nocc) ? 1 : 0;
+    u = q.sp2i[2];  // -1 once converged
+    if (u < 0) return;
   }
-  const int i = (int)blockIdx.x * 8 + warp;
-  if (i >= lp) return;  // after the block's barriers
-  double* yd_next = sp2_ydiag(q, ws);
   // the largest |v| of the line as bits: for non-negative doubles the unsigned order of the
   // bit patterns is the numeric order (integer instructions instead of FP64 ones, which this
   // GPU issues at 1/64 of the FP32 rate)
@@ -596,7 +526,6 @@ __global__ void __launch_bounds__(256) kb_sp2_step(const MolPtrs* __restrict__ m
     // evaluated for a branch that is not taken: D^2 is a copy, 2D - D^2 one FMA per element
     auto put = [&](int k, double v) {
       y[k] = v;
-      if (k == i) yd_next[i] = v;
       const unsigned long long b = (unsigned long long)__double_as_longlong(v) & ~(1ull << 63);
       mb = b > mb ? b : mb;
     };
@@ -753,18 +682,18 @@ void pipe_site_b(const BatchLaunch& b, int site) {
 
 // the new iterate with its exponents and slice image (init: D0 from A), for every listed
 // molecule still iterating
-void sp2_step_b(const BatchLaunch& b, int step) {
+void sp2_step_b(const BatchLaunch& b, bool init) {
   if (!b.count) return;
   const int lp = pimage_lines(b.nao_max);
   const int tk = prof_kbegin(b.s);
   ++g_kernel_launches;
-  kb_sp2_step<<<dim3(lp / 8, 1, b.count), 256, 0, b.s>>>(b.mp, b.list, step);
+  kb_sp2_step<<<dim3(lp / 8, 1, b.count), 256, 0, b.s>>>(b.mp, b.list, init ? 1 : 0);
   prof_kend(KS_PIPE_PREP, tk, b.s);
 }
 
 // one squaring of the batched spectral projection: C = Y Y on the tensor cores from the slice
 // image that sp2_step_b wrote, for every listed molecule still iterating
-void sp2_square_b(const BatchLaunch& b, int step) {
+void sp2_square_b(const BatchLaunch& b) {
   if (!b.count) return;
   static bool attr = false;
   if (!attr) {
@@ -776,7 +705,7 @@ void sp2_square_b(const BatchLaunch& b, int step) {
   const int tiles = ((n + PP_M - 1) / PP_M) * ((n + PP_N - 1) / PP_N);
   const int tk = prof_kbegin(b.s);
   ++g_kernel_launches;
-  kb_opipe_sq<<<dim3(tiles, b.count), PP_THREADS, PP_SMEM, b.s>>>(b.mp, b.list, step);
+  kb_opipe_sq<<<dim3(tiles, b.count), PP_THREADS, PP_SMEM, b.s>>>(b.mp, b.list);
   prof_kend(KS_PIPE, tk, b.s);
 }
 

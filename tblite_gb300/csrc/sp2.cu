@@ -16,8 +16,8 @@
 // Per molecule and SCF iteration the eigensolver's tridiagonalisation, eigenvalues, inverse
 // iteration and back-transformation (FP64 cores) become ~25 symmetric squarings on the BF16
 // tensor cores with FP64-accurate operand splitting (ozaki_pipe.cu: kb_opipe_sq squares from
-// the slice image; kb_sp2_step decides the step and forms the next iterate, its exponents and
-// its image in one pass over the matrix, so a step is two launches).  Every
+// the slice image; kb_sp2_step forms the next iterate, its exponents and its image in one pass
+// over the matrix, so a step is three launches: square, decide, step).  Every
 // molecule of a size bucket iterates in lockstep; each decides its own step on the device and
 // stops on its own (its later launches return at once).  The host launches a step budget per
 // bucket (the most steps any of its molecules took in the previous SCF iteration plus a margin);
@@ -46,7 +46,19 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-// Gershgorin bounds of A (one block per molecule); the step launch -1 starts the state
+// block-wide sum and min/max; the results are valid in every thread
+__device__ double block_sum(double v, double* red) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  double s = 0.0;
+  for (int w = 0; w < nw; ++w) s += red[w];
+  return s;
+}
+
+// Gershgorin bounds of A and a fresh projection state (one block per molecule)
 __global__ void __launch_bounds__(256) kb_sp2_start(BARGS) {
   BMOL;
   if (*q.flag < 0) return;
@@ -77,20 +89,65 @@ __global__ void __launch_bounds__(256) kb_sp2_start(BARGS) {
     if (!(hi > lo)) hi = lo + 1.0;  // a 1 x 1 or scalar A: any positive width
     q.sp2s[0] = lo;
     q.sp2s[1] = hi;
+    q.sp2s[2] = q.sp2s[3] = q.sp2s[4] = 1e300;  // idempotency errors e(k-2), e(k-1), e(k)
+    q.sp2i[0] = 0;   // converged
+    q.sp2i[1] = 0;   // steps taken
+    q.sp2i[2] = -1;  // update of the current step: 1 square, 0 2D - D^2, -1 none
     // sp2i[3]: tensor-core pipeline status, set by any pipelined product of the molecule; it
     // starts zeroed with the batch and is never cleared (a failure sends the molecule away)
     q.scal[0] = 0.0;  // no Fermi entropy: the occupations are 0/2 (checked after the SCF)
   }
 }
 
+// traces of D (Y) and D^2 (C), idempotency error, convergence and the next update (one block
+// per molecule)
+__global__ void __launch_bounds__(256) kb_sp2_decide(BARGS) {
+  BMOL;
+  if (*q.flag < 0 || q.sp2i[0] != 0) return;
+  __shared__ double red[8];
+  const int n = q.m.nao;
+  double a = 0.0, b = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    a += q.Y[i + (size_t)i * n];
+    b += q.C[i + (size_t)i * n];
+  }
+  const double tx = block_sum(a, red);
+  const double tx2 = block_sum(b, red);
+  if (threadIdx.x != 0) return;
+  if (q.sp2i[3] != 0) {  // a tensor-core wait ran out: the molecule takes the one-molecule path
+    *q.flag = -5;
+    return;
+  }
+  const double e = tx - tx2;
+  if (!(e == e)) {
+    *q.flag = -6;
+    return;
+  }
+  const int k = q.sp2i[1];
+  const double ekm2 = q.sp2s[3];  // after the shift below: e(k-2)
+  q.sp2s[2] = q.sp2s[3];
+  q.sp2s[3] = q.sp2s[4];
+  q.sp2s[4] = e;
+  // noise floor reached: the error no longer falls over two steps (one of each kind)
+  const bool done = (k >= 2 && ekm2 < 1e-4 * n && e >= ekm2) || e <= 1e-15 * n;
+  if (done) {
+    q.sp2i[0] = 1;
+    q.sp2i[2] = -1;
+    return;
+  }
+  const double nocc = q.nalp;
+  q.sp2i[2] = fabs(tx2 - nocc) <= fabs(2.0 * tx - tx2 - nocc) ? 1 : 0;
+  q.sp2i[1] = k + 1;
+}
+
 // after the step budget: a projection that has not converged sends the molecule to the
 // one-molecule path; the steps taken go to the host (budget of the next SCF iteration)
-__global__ void kb_sp2_finish(BARGS, int steps) {
+__global__ void kb_sp2_finish(BARGS) {
   BMOL;
   if (threadIdx.x != 0) return;
-  *q.sp2steps = *sp2_nstep(q, steps & 1);
+  *q.sp2steps = q.sp2i[1];
   if (*q.flag < 0) return;
-  if (*sp2_conv(q, steps & 1) == 0) *q.flag = -6;
+  if (q.sp2i[0] == 0) *q.flag = -6;
 }
 
 // after the SCF, with every eigenvalue of the last Fock matrix: the occupations are 0/2 only
@@ -111,13 +168,15 @@ void sp2_density_b(const BatchLaunch& b, int steps) {
   pipe_site_b(b, GS_XTT);  // A = X^T T1
   ++g_kernel_launches;
   kb_sp2_start<<<dim3(1, 1, b.count), 256, 0, b.s>>>(b.mp, b.list);
-  sp2_step_b(b, -1);  // D0 and its slice image
+  sp2_step_b(b, true);  // D0 and its slice image
   for (int k = 0; k < steps; ++k) {
-    sp2_square_b(b, k);  // C = D^2
-    sp2_step_b(b, k);    // stop test and update, the slice image for the next squaring
+    sp2_square_b(b);
+    ++g_kernel_launches;
+    kb_sp2_decide<<<dim3(1, 1, b.count), 256, 0, b.s>>>(b.mp, b.list);
+    sp2_step_b(b, false);  // the update and its slice image for the next squaring
   }
   ++g_kernel_launches;
-  kb_sp2_finish<<<dim3(1, 1, b.count), 32, 0, b.s>>>(b.mp, b.list, steps);
+  kb_sp2_finish<<<dim3(1, 1, b.count), 32, 0, b.s>>>(b.mp, b.list);
   pipe_site_b(b, GS_XD);   // T1 = 2 X D
   pipe_site_b(b, GS_PXT);  // P = T1 X^T
 }
