@@ -459,6 +459,62 @@ __global__ void __launch_bounds__(PP_THREADS, 1) k_opipe(PipeArgs a) { opipe_til
 // image in img (exponents iexp), the square goes to C.  Molecules that left the batch or whose
 // projection has converged (sp2i[0] != 0) launch nothing.
 __device__ __forceinline__ int lines_padded(int n) { return ((n + PP_M - 1) / PP_M) * PP_M; }
+
+// The decision of a projection step, taken by one CTA after C = D^2 is complete: traces of D (Y)
+// and D^2 (C) in a fixed order, read past L1 since other CTAs and kernels wrote them, the idempotency error
+// tr(D - D^2), the stop test (the error no longer falls over two steps, Kruchinin, Rubensson,
+// Niklasson 2016, or reaches the rounding floor) and the update D^2 or 2D - D^2 whose trace is
+// closer to the occupied count (Niklasson 2002).  State: sp2i[0] converged, [1] steps taken,
+// [2] update of this step (1 square, 0 2D - D^2, -1 none), [3] pipeline status; sp2s[2..4]
+// the last three idempotency errors.
+__device__ void sp2_decide_cta(const MolPtrs& q) {
+  __shared__ double red[2][PP_THREADS / 32];
+  const int n = q.m.nao, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  double a = 0.0, b = 0.0;
+  for (int t = threadIdx.x; t < n; t += PP_THREADS) {
+    a += __ldcg(q.Y + t + (size_t)t * n);
+    b += __ldcg(q.C + t + (size_t)t * n);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+  }
+  if (lane == 0) {
+    red[0][warp] = a;
+    red[1][warp] = b;
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  double tx = 0.0, tx2 = 0.0;
+  for (int w = 0; w < PP_THREADS / 32; ++w) {
+    tx += red[0][w];
+    tx2 += red[1][w];
+  }
+  if (q.sp2i[3] != 0) {  // a tensor-core wait ran out: the molecule takes the one-molecule path
+    *q.flag = -5;
+    return;
+  }
+  const double e = tx - tx2;
+  if (!(e == e)) {
+    *q.flag = -6;
+    return;
+  }
+  const int k = q.sp2i[1];
+  const double ekm2 = q.sp2s[3];  // after the shift below: e(k-2)
+  q.sp2s[2] = q.sp2s[3];
+  q.sp2s[3] = q.sp2s[4];
+  q.sp2s[4] = e;
+  const bool done = (k >= 2 && ekm2 < 1e-4 * n && e >= ekm2) || e <= 1e-15 * n;
+  if (done) {
+    q.sp2i[0] = 1;
+    q.sp2i[2] = -1;
+    return;
+  }
+  const double nocc = q.nalp;
+  q.sp2i[2] = fabs(tx2 - nocc) <= fabs(2.0 * tx - tx2 - nocc) ? 1 : 0;
+  q.sp2i[1] = k + 1;
+}
 __device__ __forceinline__ bool sq_skip(const MolPtrs& q) {
   return *q.flag < 0 || q.sp2i[0] != 0;
 }
@@ -491,6 +547,18 @@ __global__ void __launch_bounds__(PP_THREADS, 1) kb_opipe_sq(const MolPtrs* __re
                                          (unsigned long long)min(PP_N, n - j0) * (unsigned)n);
   }
   opipe_tile(a, blockIdx.x);
+  // the last CTA of the molecule to finish takes the step's decision (no separate launch): every
+  // thread fences its stores of C, one atomic counts the finished tiles, and the CTA that
+  // completes the count reads the diagonals of D and D^2 and resets the count
+  __shared__ int last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(q.sp2i + 5, 1) == tiles - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  sp2_decide_cta(q);
+  if (threadIdx.x == 0) q.sp2i[5] = 0;
 }
 
 // ---- one projection step per molecule without a separate exponent or split pass: each warp

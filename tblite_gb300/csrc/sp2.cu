@@ -16,8 +16,9 @@
 // Per molecule and SCF iteration the eigensolver's tridiagonalisation, eigenvalues, inverse
 // iteration and back-transformation (FP64 cores) become ~25 symmetric squarings on the BF16
 // tensor cores with FP64-accurate operand splitting (ozaki_pipe.cu: kb_opipe_sq squares from
-// the slice image; kb_sp2_step forms the next iterate, its exponents and its image in one pass
-// over the matrix, so a step is three launches: square, decide, step).  Every
+// the slice image, and its last CTA per molecule takes the step's decision; kb_sp2_step forms
+// the next iterate, its exponents and its image in one pass over the matrix, so a step is two
+// launches).  Every
 // molecule of a size bucket iterates in lockstep; each decides its own step on the device and
 // stops on its own (its later launches return at once).  The host launches a step budget per
 // bucket (the most steps any of its molecules took in the previous SCF iteration plus a margin);
@@ -44,18 +45,6 @@ __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
-}
-
-// block-wide sum and min/max; the results are valid in every thread
-__device__ double block_sum(double v, double* red) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  v = warp_sum(v);
-  __syncthreads();
-  if (lane == 0) red[wid] = v;
-  __syncthreads();
-  double s = 0.0;
-  for (int w = 0; w < nw; ++w) s += red[w];
-  return s;
 }
 
 // Gershgorin bounds of A and a fresh projection state (one block per molecule)
@@ -93,51 +82,11 @@ __global__ void __launch_bounds__(256) kb_sp2_start(BARGS) {
     q.sp2i[0] = 0;   // converged
     q.sp2i[1] = 0;   // steps taken
     q.sp2i[2] = -1;  // update of the current step: 1 square, 0 2D - D^2, -1 none
+    q.sp2i[5] = 0;   // tiles of the current squaring finished (the last one decides)
     // sp2i[3]: tensor-core pipeline status, set by any pipelined product of the molecule; it
     // starts zeroed with the batch and is never cleared (a failure sends the molecule away)
     q.scal[0] = 0.0;  // no Fermi entropy: the occupations are 0/2 (checked after the SCF)
   }
-}
-
-// traces of D (Y) and D^2 (C), idempotency error, convergence and the next update (one block
-// per molecule)
-__global__ void __launch_bounds__(256) kb_sp2_decide(BARGS) {
-  BMOL;
-  if (*q.flag < 0 || q.sp2i[0] != 0) return;
-  __shared__ double red[8];
-  const int n = q.m.nao;
-  double a = 0.0, b = 0.0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    a += q.Y[i + (size_t)i * n];
-    b += q.C[i + (size_t)i * n];
-  }
-  const double tx = block_sum(a, red);
-  const double tx2 = block_sum(b, red);
-  if (threadIdx.x != 0) return;
-  if (q.sp2i[3] != 0) {  // a tensor-core wait ran out: the molecule takes the one-molecule path
-    *q.flag = -5;
-    return;
-  }
-  const double e = tx - tx2;
-  if (!(e == e)) {
-    *q.flag = -6;
-    return;
-  }
-  const int k = q.sp2i[1];
-  const double ekm2 = q.sp2s[3];  // after the shift below: e(k-2)
-  q.sp2s[2] = q.sp2s[3];
-  q.sp2s[3] = q.sp2s[4];
-  q.sp2s[4] = e;
-  // noise floor reached: the error no longer falls over two steps (one of each kind)
-  const bool done = (k >= 2 && ekm2 < 1e-4 * n && e >= ekm2) || e <= 1e-15 * n;
-  if (done) {
-    q.sp2i[0] = 1;
-    q.sp2i[2] = -1;
-    return;
-  }
-  const double nocc = q.nalp;
-  q.sp2i[2] = fabs(tx2 - nocc) <= fabs(2.0 * tx - tx2 - nocc) ? 1 : 0;
-  q.sp2i[1] = k + 1;
 }
 
 // after the step budget: a projection that has not converged sends the molecule to the
@@ -170,9 +119,7 @@ void sp2_density_b(const BatchLaunch& b, int steps) {
   kb_sp2_start<<<dim3(1, 1, b.count), 256, 0, b.s>>>(b.mp, b.list);
   sp2_step_b(b, true);  // D0 and its slice image
   for (int k = 0; k < steps; ++k) {
-    sp2_square_b(b);
-    ++g_kernel_launches;
-    kb_sp2_decide<<<dim3(1, 1, b.count), 256, 0, b.s>>>(b.mp, b.list);
+    sp2_square_b(b);       // C = D^2, and the step's decision by the last CTA of each molecule
     sp2_step_b(b, false);  // the update and its slice image for the next squaring
   }
   ++g_kernel_launches;
