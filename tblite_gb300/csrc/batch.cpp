@@ -133,8 +133,9 @@ struct Plan {
   Piece d3_sp, d3_nref, d3_refcn, d3_c6ref, d3_r4r2, d3_rcov, d3_cn, d3_w, d3_dw, d3_dEdcn;
   Piece d4_sp, d4_nref, d4_ngw, d4_refcn, d4_refq, d4_zeff, d4_gam, d4_r4r2, d4_rcov, d4_en,
       d4_c6ref;
-  Piece d4_cn, d4_gw, d4_dgw, d4_gwv, d4_dgwdq, d4_dgwv_cn, d4_c6, d4_dc6, d4_e3, d4_dEdcn, d4_atm;
-  Piece cn, se, mrad, dmrdcn, S, H, D, Q, F, P, C, scratch, emo, focc;
+  Piece d4_cn, d4_gw, d4_dgw, d4_gwv, d4_dgwdq, d4_dgwv_cn, d4_c6, d4_dc6, d4_e3, d4_dEdcn, d4_atm,
+      d4_de;
+  Piece cn, se, mrad, dmrdcn, ctab, S, H, D, Q, F, P, C, scratch, emo, focc;
   Piece qsh, qat, dpat, qpat, qsh_o, qat_o, dpat_o, qpat_o, vsh, vat, vdp, vqp, vao;
   Piece mull, eband, eelec, erep, vec_out, scal, icount;
   Piece bq, bqlast, bdq, bdqlast, bdf, bu, ba, bomega, bwork, bstatus;
@@ -247,6 +248,7 @@ void layout(Plan& pl, Region* R) {
   pl.cn = piece<double>(R, RS, na);
   pl.se = piece<double>(R, RS, ns);
   pl.mrad = piece<double>(R, RS, na);
+  pl.ctab = piece<double>(R, RS, ns * ns + 3 * na * na);
   pl.dmrdcn = piece<double>(R, RS, na);
   for (Piece* p : {&pl.F, &pl.P, &pl.C, &pl.scratch, &pl.X, &pl.A, &pl.T1, &pl.Y})
     *p = piece<double>(R, RS, nn);
@@ -279,6 +281,7 @@ void layout(Plan& pl, Region* R) {
     pl.d4_c6 = piece<double>(R, RS, na * na);
     pl.d4_dc6 = piece<double>(R, RS, na * na);
     pl.d4_atm = piece<double>(R, RS, 8 * na * na);
+    pl.d4_de = piece<double>(R, RS, na * na);
   }
 }
 
@@ -374,6 +377,7 @@ MolPtrs make_ptrs(const Plan& pl, const Bases& db) {
     w.e3 = db.at<double>(pl.d4_e3);
     w.dEdcn = db.at<double>(pl.d4_dEdcn);
     w.atm = db.at<double>(pl.d4_atm);
+    w.de = db.at<double>(pl.d4_de);
   }
   q.nd = pl.nd;
   // GFN2-xTB mixes the atomic multipoles with the shell charges, GFN1-xTB the charges alone
@@ -391,6 +395,7 @@ MolPtrs make_ptrs(const Plan& pl, const Bases& db) {
   q.cn = db.at<double>(pl.cn);
   q.se = db.at<double>(pl.se);
   q.mrad = db.at<double>(pl.mrad);
+  q.ctab = db.at<double>(pl.ctab);
   q.dmrdcn = db.at<double>(pl.dmrdcn);
   q.S = db.at<double>(pl.S);
   q.H = db.at<double>(pl.H);
@@ -684,6 +689,7 @@ std::vector<int> run_chunk(std::vector<Plan>& plans, Arena& ar, _tblite_context*
   each([&](BatchLaunch& L) {
     launch_cn_b(L, p);
     launch_setup_levels_b(L, p);
+    launch_coulomb_table_b(L, p);  // needs the multipole radii of the levels kernel
     launch_build_h0_b(L, p);
     launch_repulsion_b(L, p);
     d4_setup_b(L);

@@ -133,10 +133,36 @@ __device__ __forceinline__ double d4_de(double r2, double rrij, double r0, doubl
 
 // MODE 0: vat += sum_r dgwdq_r u_r ; MODE 1: eat += 1/2 sum_r gwv_r u_r ;
 // MODE 2: gradient at fixed weights + dEdcn (own atom share), per-atom sigma partials
+// two-body damping kernel of every ordered pair (i, j), once per geometry: the pair kernels of
+// the SCF iterations read it instead of evaluating the powers and divisions of d4_de
+__device__ __forceinline__ void d4_de_table_dev(DevMol m, DevD4 d, double* tab) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int nat = m.nat;
+  if (t >= (long long)nat * nat) return;
+  const int i = (int)(t / nat), j = (int)(t % nat);
+  double de = 0.0;
+  if (i != j) {
+    double r2 = 0.0;
+    for (int k = 0; k < 3; ++k) {
+      const double v = m.xyz[3 * i + k] - m.xyz[3 * j + k];
+      r2 += v * v;
+    }
+    if (!(r2 > d.disp2_cutoff * d.disp2_cutoff || r2 < 1e-12)) {
+      const double rrij = 3.0 * d.r4r2[i] * d.r4r2[j];
+      const double r0 = d.a1 * sqrt(rrij) + d.a2;
+      double dd;
+      de = d4_de(r2, rrij, r0, d.s6, d.s8, dd);
+    }
+  }
+  tab[t] = de;
+}
+
+// detab (MODE 0, 1): the table of d4_de_table_dev, or nullptr to evaluate the kernel here
 template <int MODE>
 __device__ __forceinline__ void d4_pair_dev(DevMol m, DevD4 d, const double* __restrict__ gwv,
                           const double* __restrict__ dgwdq, const double* __restrict__ dgwv_cn,
-                          double* vat, double* eat, double* grad, double* sig_at, double* dEdcn) {
+                          double* vat, double* eat, double* grad, double* sig_at, double* dEdcn,
+                          const double* __restrict__ detab = nullptr) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (warp >= m.nat) return;
   const int i = warp;
@@ -144,6 +170,8 @@ __device__ __forceinline__ void d4_pair_dev(DevMol m, DevD4 d, const double* __r
   const int ld = d.nsp * D4_MREF;
   const double* tab_i = d.c6ref + (size_t)d.sp[i] * D4_MREF * ld;
   double gi[D4_MREF], dci[D4_MREF];
+  const int nri = d.nref[i];
+#pragma unroll
   for (int r = 0; r < D4_MREF; ++r) {
     gi[r] = gwv[i * D4_MREF + r];
     dci[r] = MODE == 2 ? dgwv_cn[i * D4_MREF + r] : 0.0;
@@ -152,29 +180,44 @@ __device__ __forceinline__ void d4_pair_dev(DevMol m, DevD4 d, const double* __r
   double g[3] = {0, 0, 0}, sg[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, dcn = 0.0;
   for (int j = lane; j < m.nat; j += 32) {
     if (j == i) continue;
-    double v[3], r2 = 0.0;
-    for (int k = 0; k < 3; ++k) {
-      v[k] = m.xyz[3 * i + k] - m.xyz[3 * j + k];
-      r2 += v[k] * v[k];
+    double v[3] = {0.0, 0.0, 0.0}, r2 = 0.0, dd = 0.0, de;
+    if (MODE < 2 && detab) {
+      de = detab[(size_t)i * m.nat + j];
+      if (de == 0.0) continue;  // beyond the cutoff
+    } else {
+      for (int k = 0; k < 3; ++k) {
+        v[k] = m.xyz[3 * i + k] - m.xyz[3 * j + k];
+        r2 += v[k] * v[k];
+      }
+      if (r2 > cut2 || r2 < 1e-12) continue;
+      const double rrij = 3.0 * d.r4r2[i] * d.r4r2[j];
+      const double r0 = d.a1 * sqrt(rrij) + d.a2;
+      de = d4_de(r2, rrij, r0, d.s6, d.s8, dd);
     }
-    if (r2 > cut2 || r2 < 1e-12) continue;
-    const double rrij = 3.0 * d.r4r2[i] * d.r4r2[j];
-    const double r0 = d.a1 * sqrt(rrij) + d.a2;
-    double dd;
-    const double de = d4_de(r2, rrij, r0, d.s6, d.s8, dd);
     const double* tab = tab_i + d.sp[j] * D4_MREF;
     const double* gj = gwv + j * D4_MREF;
+    // only the atoms' own reference points (weights and C6 entries beyond them are zero):
+    // unrolled to the maximum with guards so the accumulators stay in registers
+    const int nrj = d.nref[j];
     if (MODE < 2) {
+#pragma unroll
       for (int r = 0; r < D4_MREF; ++r) {
+        if (r >= nri) break;
         double acc = 0.0;
-        for (int s = 0; s < D4_MREF; ++s) acc += tab[(size_t)r * ld + s] * gj[s];
+#pragma unroll
+        for (int s = 0; s < D4_MREF; ++s)
+          if (s < nrj) acc += tab[(size_t)r * ld + s] * gj[s];
         u[r] += de * acc;
       }
     } else {
       double c6 = 0.0, dc6 = 0.0;
+#pragma unroll
       for (int r = 0; r < D4_MREF; ++r) {
+        if (r >= nri) break;
         double acc = 0.0;
-        for (int s = 0; s < D4_MREF; ++s) acc += tab[(size_t)r * ld + s] * gj[s];
+#pragma unroll
+        for (int s = 0; s < D4_MREF; ++s)
+          if (s < nrj) acc += tab[(size_t)r * ld + s] * gj[s];
         c6 += gi[r] * acc;
         dc6 += dci[r] * acc;
       }
@@ -743,6 +786,10 @@ __global__ void kb_d4_zeta(BARGS, int mode) {
   else
     d4_zeta_dev(q.m.nat, q.d4, q.qat_o, w.gw, w.dgw, w.gwv, nullptr, w.dgwv_cn);
 }
+__global__ void kb_d4_de(BARGS) {
+  BMOL;
+  d4_de_table_dev(q.m, q.d4, q.d4w.de);
+}
 __global__ void kb_d4_c6(BARGS) {
   BMOL;
   d4_c6_dev(q.m.nat, q.d4, q.d4w.gwv, q.d4w.dgwv_cn, q.d4w.c6, q.d4w.dc6);
@@ -764,12 +811,12 @@ __global__ void kb_d4_atm_grad(BARGS) {
 __global__ void kb_d4_pair_pot(BARGS) {
   BMOL;
   d4_pair_dev<0>(q.m, q.d4, q.d4w.gwv, q.d4w.dgwdq, nullptr, q.vat, nullptr, nullptr, nullptr,
-                 nullptr);
+                 nullptr, q.d4w.de);
 }
 __global__ void kb_d4_pair_energy(BARGS) {
   BMOL;
   d4_pair_dev<1>(q.m, q.d4, q.d4w.gwv, nullptr, nullptr, nullptr, q.eelec, nullptr, nullptr,
-                 nullptr);
+                 nullptr, q.d4w.de);
 }
 __global__ void kb_d4_pair_grad(BARGS) {
   BMOL;
@@ -812,6 +859,8 @@ void d4_setup_b(const BatchLaunch& b) {
   kb_d4_zeta<<<batoms(b), 128, 0, b.s>>>(b.mp, b.list, 0);
   const long long nn = (long long)b.nat_max * b.nat_max;
   kb_d4_c6<<<dim3((unsigned)((nn + 255) / 256), 1, b.count), 256, 0, b.s>>>(b.mp, b.list);
+  ++g_kernel_launches;
+  kb_d4_de<<<dim3((unsigned)((nn + 255) / 256), 1, b.count), 256, 0, b.s>>>(b.mp, b.list);
   kb_d4_atm_pairs<<<dim3((unsigned)((nn + 255) / 256), 1, b.count), 256, 0, b.s>>>(b.mp, b.list);
   kb_d4_atm<<<bwarps(b), 64, (size_t)2 * 3 * b.nat_max * sizeof(double), b.s>>>(b.mp, b.list);
   kb_d4_atm_grad<<<bwarps(b), 64, 0, b.s>>>(b.mp, b.list);

@@ -117,6 +117,8 @@ struct DevD4 {
 struct D4Work {  // device scratch
   double *cn, *gw, *dgw, *gwv, *dgwdq, *dgwv_cn, *c6, *dc6, *e3, *dEdcn;
   double* atm;  // [8][nat][nat] pair tables and pair derivatives of the three-body term
+  double* de;   // [nat][nat] two-body damping kernel of each ordered pair (0 beyond the cutoff),
+                // or nullptr: the pair kernels evaluate it
 };
 // geometry setup: CN, weights, atomic C6 at q = 0, three-body energy (e3) and, with grad,
 // its gradient and dEdcn (w.dEdcn is reset here)
@@ -349,6 +351,10 @@ struct MolPtrs {
   double nalp, nbet, kt, damp, econv, pconv;
   double h0_cutoff;  // depends on the basis of the molecule (smallest exponent)
   double *cn, *se, *mrad, *dmrdcn;
+  // per-geometry pair table of the electrostatics: gamma of every shell pair (nsh x nsh, row
+  // = shell of the potential's atom), then the AES pair scalars g3 f3, g5 f5, g3 f5 of every
+  // ordered atom pair (three nat x nat planes)
+  double* ctab;
   double *S, *H, *D, *Q, *F, *P, *C, *scratch;  // F doubles as W after the SCF
   double *emo, *focc;                            // focc [3][n]: total, alpha, beta
   double *qsh, *qat, *dpat, *qpat, *qsh_o, *qat_o, *dpat_o, *qpat_o;
@@ -406,6 +412,7 @@ void launch_setup_levels_b(const BatchLaunch& b, const Gfn2Scalars& p);
 void launch_build_h0_b(const BatchLaunch& b, const Gfn2Scalars& p);
 void launch_repulsion_b(const BatchLaunch& b, const Gfn2Scalars& p);
 void launch_coulomb_potential_b(const BatchLaunch& b, const Gfn2Scalars& p);
+void launch_coulomb_table_b(const BatchLaunch& b, const Gfn2Scalars& p);  // once per geometry
 void launch_coulomb_energy_b(const BatchLaunch& b, const Gfn2Scalars& p);
 void launch_coulomb_gradient_b(const BatchLaunch& b, const Gfn2Scalars& p);
 void launch_vao_b(const BatchLaunch& b);

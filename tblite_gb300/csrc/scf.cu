@@ -186,11 +186,62 @@ void launch_setup_levels(const DevMol& m, const Gfn2Scalars& p, const double* cn
 // ------------------------------------------------------------------------------------
 constexpr int MAXSH = 3;
 
+// AES pair scalars of atoms i, j at distance r1: g3 f3, g5 f5, g3 f5 with g = 1/r and the
+// damping f_n = 1/(1 + 6 (rr)^dmp_n), rr = (mrad_i + mrad_j) / (2 r)
+__device__ __forceinline__ void aes_pair(double r1, double mri, double mrj, const Gfn2Scalars& p,
+                                         double& g3f3, double& g5f5, double& g3f5) {
+  const double g1 = 1.0 / r1, g3 = g1 * g1 * g1, g5 = g3 * g1 * g1;
+  const double rr = 0.5 * (mrj + mri) * g1;
+  const double f3 = 1.0 / (1.0 + 6.0 * powe(rr, p.mp_dmp3));
+  const double f5 = 1.0 / (1.0 + 6.0 * powe(rr, p.mp_dmp5));
+  g3f3 = g3 * f3;
+  g5f5 = g5 * f5;
+  g3f5 = g3 * f5;
+}
+
+// Pair table of the electrostatics, once per geometry (one warp per atom i, partners over the
+// lanes): gamma of every shell pair of different atoms and the AES pair scalars.  The kernels
+// below then read instead of evaluating square roots, divisions and powers per pair in every
+// SCF iteration (FP64 arithmetic is the scarce resource of this GPU; the table costs 8 bytes of
+// HBM traffic per entry and iteration).
+__device__ __forceinline__ void coulomb_table_dev(DevMol m, Gfn2Scalars p,
+                                                  const double* __restrict__ mrad, double* tab) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= m.nat) return;
+  const int i = warp, nsh = m.nsh, nat = m.nat;
+  const int is0 = m.at_sh[i], nsi = m.at_sh[i + 1] - is0;
+  double* aes = tab + (size_t)nsh * nsh;
+  const size_t plane = (size_t)nat * nat;
+  for (int j = lane; j < nat; j += 32) {
+    if (j == i) continue;
+    double r2 = 0.0;
+    for (int k = 0; k < 3; ++k) {
+      const double d = m.xyz[3 * i + k] - m.xyz[3 * j + k];
+      r2 += d * d;
+    }
+    const double r1 = sqrt(r2);
+    const int js0 = m.at_sh[j], nsj = m.at_sh[j + 1] - js0;
+    for (int a = 0; a < nsi; ++a)
+      for (int b = 0; b < nsj; ++b)
+        tab[(size_t)(is0 + a) * nsh + js0 + b] =
+            gam_kernel(r1, eta_avg(m.sh_hub[is0 + a], m.sh_hub[js0 + b], p.harmonic), p.gexp);
+    if (!p.aes) continue;
+    double g3f3, g5f5, g3f5;
+    aes_pair(r1, mrad[i], mrad[j], p, g3f3, g5f5, g3f5);
+    const size_t ij = (size_t)i * nat + j;
+    aes[ij] = g3f3;
+    aes[plane + ij] = g5f5;
+    aes[2 * plane + ij] = g3f5;
+  }
+}
+
+// tab: the pair table of coulomb_table_dev, or nullptr to evaluate the pair terms here
 template <int MODE>
 __device__ __forceinline__ void coulomb_dev(DevMol m, Gfn2Scalars p, const double* __restrict__ mrad,
                           const double* __restrict__ qsh, const double* __restrict__ qat,
                           const double* __restrict__ dpat, const double* __restrict__ qpat,
-                          double* vsh, double* vat, double* vdp, double* vqp, double* eat) {
+                          double* vsh, double* vat, double* vdp, double* vqp, double* eat,
+                          const double* __restrict__ tab = nullptr) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (warp >= m.nat) return;
   const int i = warp;
@@ -207,46 +258,50 @@ __device__ __forceinline__ void coulomb_dev(DevMol m, Gfn2Scalars p, const doubl
   double ud[3] = {0, 0, 0};          // vdp_i: sd + dd parts
   double udd[3] = {0, 0, 0};         // dd part only (energy needs 1/2 of it)
   double uq[6] = {0, 0, 0, 0, 0, 0};  // vqp_i
-  for (int j = lane; j < m.nat; j += 32) {
+  const int nsh = m.nsh, nat = m.nat;
+  const double* aes = tab + (size_t)nsh * nsh;
+  const size_t plane = (size_t)nat * nat;
+  for (int j = lane; j < nat; j += 32) {
     if (j == i) continue;
     double v[3];
     for (int k = 0; k < 3; ++k) v[k] = xi[k] - m.xyz[3 * j + k];  // R_i - R_j
-    const double r2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
-    const double r1 = sqrt(r2);
+    const double r1 = tab ? 0.0 : sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
     // isotropic: gamma = 1/sqrt(r^2 + eta^-2) for gexp = 2; general form kept
     const int js0 = m.at_sh[j], nsj = m.at_sh[j + 1] - js0;
     for (int a = 0; a < nsi; ++a) {
       const double hi = m.sh_hub[is0 + a];
       double acc = 0.0;
       for (int b = 0; b < nsj; ++b) {
-        const double g = eta_avg(hi, m.sh_hub[js0 + b], p.harmonic);
-        const double t = gam_kernel(r1, g, p.gexp);
+        const double t = tab ? tab[(size_t)(is0 + a) * nsh + js0 + b]
+                             : gam_kernel(r1, eta_avg(hi, m.sh_hub[js0 + b], p.harmonic), p.gexp);
         acc += t * qsh[js0 + b];
       }
       ush[a] += acc;
     }
     if (!p.aes) continue;
     // AES (multipole.f90:488-535), amat(:, jat, iat) with vec = R_iat - R_jat
-    const double g1 = 1.0 / r1, g3 = g1 * g1 * g1, g5 = g3 * g1 * g1;
-    const double rr = 0.5 * (mrad[j] + ri) * g1;
-    const double rr3 = rr * rr * rr;
-    const double f3 = 1.0 / (1.0 + 6.0 * powe(rr, p.mp_dmp3));
-    const double f5 = 1.0 / (1.0 + 6.0 * powe(rr, p.mp_dmp5));
-    (void)rr3;
+    double g3f3, g5f5, g3f5;
+    if (tab) {
+      const size_t ij = (size_t)i * nat + j;
+      g3f3 = aes[ij];
+      g5f5 = aes[plane + ij];
+      g3f5 = aes[2 * plane + ij];
+    } else {
+      aes_pair(r1, ri, mrad[j], p, g3f3, g5f5, g3f5);
+    }
     const double* dj = dpat + 3 * j;
     const double* qj = qpat + 6 * j;
     const double qa_j = qat[j];
     // vat_i += sum_j amat_sd(:, j, i) . dpat_j + amat_sq(:, j, i) . qpat_j   (v = R_i - R_j)
-    const double sq[6] = {v[0] * v[0] * g5 * f5, 2 * v[0] * v[1] * g5 * f5, v[1] * v[1] * g5 * f5,
-                          2 * v[0] * v[2] * g5 * f5, 2 * v[1] * v[2] * g5 * f5,
-                          v[2] * v[2] * g5 * f5};
-    uat += (v[0] * dj[0] + v[1] * dj[1] + v[2] * dj[2]) * g3 * f3;
+    const double sq[6] = {v[0] * v[0] * g5f5, 2 * v[0] * v[1] * g5f5, v[1] * v[1] * g5f5,
+                          2 * v[0] * v[2] * g5f5, 2 * v[1] * v[2] * g5f5, v[2] * v[2] * g5f5};
+    uat += (v[0] * dj[0] + v[1] * dj[1] + v[2] * dj[2]) * g3f3;
     for (int k = 0; k < 6; ++k) uat += sq[k] * qj[k];
     // vdp_i += sum_j amat_sd(:, i, j) q_j + amat_dd(:, i, :, j) dpat_j ; amat_sd(:, i, j) = -v g3 f3
     const double vd = v[0] * dj[0] + v[1] * dj[1] + v[2] * dj[2];
     for (int k = 0; k < 3; ++k) {
-      ud[k] += -v[k] * g3 * f3 * qa_j;
-      const double dd = dj[k] * g3 * f5 - v[k] * vd * 3.0 * g5 * f5;
+      ud[k] += -v[k] * g3f3 * qa_j;
+      const double dd = dj[k] * g3f5 - v[k] * vd * 3.0 * g5f5;
       udd[k] += dd;
     }
     for (int k = 0; k < 6; ++k) uq[k] += sq[k] * qa_j;
@@ -1223,15 +1278,25 @@ void launch_setup_levels_b(const BatchLaunch& b, const Gfn2Scalars& p) {
   kb_levels<<<bgrid((nt + 127) / 128, b), 128, 0, b.s>>>(b.mp, b.list, p);
 }
 
+__global__ void kb_coulomb_table(BARGS, Gfn2Scalars p) {
+  BMOL;
+  coulomb_table_dev(q.m, p, q.mrad, q.ctab);
+}
+void launch_coulomb_table_b(const BatchLaunch& b, const Gfn2Scalars& p) {
+  if (!b.count) return;
+  ++g_kernel_launches;
+  kb_coulomb_table<<<bgrid((b.nat_max * 32 + 63) / 64, b), 64, 0, b.s>>>(b.mp, b.list, p);
+}
+
 template <int MODE>
 __global__ void kb_coulomb(BARGS, Gfn2Scalars p) {
   BMOL;
   if (MODE == 0)
     coulomb_dev<0>(q.m, p, q.mrad, q.qsh, q.qat, q.dpat, q.qpat, q.vsh, q.vat, q.vdp, q.vqp,
-                   nullptr);
+                   nullptr, q.ctab);
   else
     coulomb_dev<1>(q.m, p, q.mrad, q.qsh_o, q.qat_o, q.dpat_o, q.qpat_o, nullptr, nullptr,
-                   nullptr, nullptr, q.eelec);
+                   nullptr, nullptr, q.eelec, q.ctab);
 }
 void launch_coulomb_potential_b(const BatchLaunch& b, const Gfn2Scalars& p) {
   if (!b.count) return;
