@@ -547,13 +547,16 @@ __global__ void __launch_bounds__(PP_THREADS, 1) kb_opipe_sq(const MolPtrs* __re
                                          (unsigned long long)min(PP_N, n - j0) * (unsigned)n);
   }
   opipe_tile(a, blockIdx.x);
-  // the last CTA of the molecule to finish takes the step's decision (no separate launch): every
-  // thread fences its stores of C, one atomic counts the finished tiles, and the CTA that
-  // completes the count reads the diagonals of D and D^2 and resets the count
+  // the last CTA of the molecule to finish takes the step's decision (no separate launch): after
+  // the CTA's barrier one thread fences (cumulatively, the stores of C its barrier ordered
+  // before it) and counts the finished tiles; the CTA that completes the count reads the
+  // diagonals of D and D^2 and resets the count
   __shared__ int last;
-  __threadfence();
   __syncthreads();
-  if (threadIdx.x == 0) last = atomicAdd(q.sp2i + 5, 1) == tiles - 1;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(q.sp2i + 5, 1) == tiles - 1;
+  }
   __syncthreads();
   if (!last) return;
   __threadfence();
