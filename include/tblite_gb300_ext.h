@@ -53,7 +53,7 @@ int tblite_gb300_batch_last_modes(int* modes, int nmol);
 /* Autotuner of the batch schedule: coordinate descent over CUDA graphs (kept, or switched off;
  * never switched on against tblite_gb300_set_batch_graphs), the projection threshold (128, 144,
  * 157, 176, 224 orbitals or off), the bucket cut (3/4, 2/3, 4/5 of the largest orbital count), the CTAs
- * per SM of the cluster tridiagonalisation (1, 2) and the side streams (4, 8), each candidate
+ * per SM of the cluster tridiagonalisation (1, 2) and the side streams (4, 8, 16), each candidate
  * timed as the wall time of a batch call (best of two) on a fixed pseudo-random sample of
  * `sample` of the given molecules (256 if <= 0).  The fastest schedule stays set.  Returns the
  * number of timed calls, -1 if the sample could not be evaluated. */
@@ -83,7 +83,7 @@ int tblite_gb300_batch_last_iterations(int* iterations, int nmol);
 /* batched GEMMs of molecules with at least 128 orbitals on the BF16 tensor cores with
  * FP64-accurate operand splitting (1, the default) or as FP64 tile GEMMs (0); process wide */
 void tblite_gb300_set_split_gemm(int enable);
-/* number of streams (1..8, default 8) over which a batch call spreads its size buckets; 1 runs
+/* number of streams (1..16, default 8) over which a batch call spreads its size buckets; 1 runs
  * the buckets one after the other, so per-kernel event times bracket each kernel alone */
 void tblite_gb300_set_batch_streams(int count);
 /* schedule of the batched tridiagonalisation: 2 (default) clusters wide enough that two CTAs

@@ -54,7 +54,7 @@ struct Arena {
   size_t host_cap = 0;
   cudaStream_t stream = nullptr;
   // size buckets run concurrently on side streams, forked from and joined into `stream`
-  static constexpr int NSIDE = 8;
+  static constexpr int NSIDE = 16;
   cudaStream_t side[NSIDE] = {};
   cudaEvent_t fork = nullptr, join[NSIDE] = {};
   void reserve(size_t dbytes, size_t hbytes) {
@@ -1157,7 +1157,7 @@ extern "C" int tblite_gb300_batch_last_graphs(int* builds, int* launches) {
   return g_batch_graphs ? 1 : 0;
 }
 extern "C" void tblite_gb300_set_batch_streams(int count) {
-  g_batch_streams = count < 1 ? 1 : (count > 8 ? 8 : count);
+  g_batch_streams = count < 1 ? 1 : (count > Arena::NSIDE ? Arena::NSIDE : count);
 }
 extern "C" double tblite_gb300_batch_last_device_ms(void) { return g_last_device_ms; }
 extern "C" int tblite_gb300_batch_last_iterations(int* iterations, int nmol) {
@@ -1267,7 +1267,7 @@ extern "C" int tblite_gb300_batch_autotune(tblite_context ctx, int nmol,
   try_values([](int v) { g_sp2_min_nao = v; }, {128, 144, 157, 176, 224, 100000}, sp2);
   try_values([](int v) { g_cut_num = v / 10; g_cut_den = v % 10; }, {34, 23, 45}, cut);
   try_values([](int v) { tb::set_tridiag_ctas_per_sm(v); }, {1, 2}, ctas);
-  try_values([](int v) { g_batch_streams = v; }, {4, 8}, streams);
+  try_values([](int v) { g_batch_streams = v; }, {4, 8, 16}, streams);
   char note[160];
   std::snprintf(note, sizeof(note), "autotuned on %d molecules (%d calls, %.1f ms)%s", k, calls,
                 best, g_batch_graphs ? "" : "; SCF iterations launched directly");
