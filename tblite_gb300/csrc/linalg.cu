@@ -6,6 +6,8 @@
 // the zero triangles of triangular operands.  All matrices are column-major
 // (element (i, j) at p[i + j*ld]) as in BLAS.
 #include <cooperative_groups.h>
+#include <stdexcept>
+#include <string>
 #include <cuda_runtime.h>
 
 #include "engine.h"
@@ -367,40 +369,99 @@ void gemm_b(const BatchLaunch& b, int site) {
   prof_kend(KS_GEMM, tk, b.s);
 }
 
-// Cholesky S = L L^T of one molecule per block, in T1 (column-major lower, L2 resident):
-// step j scales column j by 1/sqrt(pivot) and updates the trailing columns (warp per column).
-// The diagonal keeps the pivots until the end, then takes their square roots.  A pivot that
-// is not positive marks the molecule failed (flag -2); every thread reads the same pivot after
-// a barrier, so the whole block leaves together.
+// Cholesky S = L L^T of one molecule per block, in T1 (column-major lower, L2 resident),
+// blocked by panels of CHOL_NB columns.  The panel (rows j0..n-1) is factorised in shared
+// memory (per column: scale by 1/sqrt(pivot), rank-1 update of the panel's later columns),
+// written back, and the trailing lower triangle takes the panel's CHOL_NB rank-1 updates at
+// once: 64 x 64 tiles, a 4 x 4 register block per thread, the panel rows from shared memory.
+// Each trailing element is read and written once per panel instead of once per column, so the
+// update runs on the FP64 pipe instead of waiting on L2.  A pivot that is not positive marks
+// the molecule failed (flag -2); it is read after a barrier, so the whole block leaves together.
+constexpr int CHOL_NB = 16;
 __global__ void __launch_bounds__(256) kb_cholesky(BARGS) {
   BMOL;
   const int n = q.m.nao;
   double* A = q.T1;
+  extern __shared__ double pan[];  // [CHOL_NB][m] panel, column-major (m = n - j0 rows)
+  __shared__ int bad;
+  const int tid = threadIdx.x;
   const size_t nn = (size_t)n * n;
-  for (size_t t = threadIdx.x; t < nn; t += blockDim.x) A[t] = q.S[t];  // S symmetric
+  for (size_t t = tid; t < nn; t += blockDim.x) A[t] = q.S[t];  // S symmetric
+  if (tid == 0) bad = 0;
   __syncthreads();
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int j = 0; j < n; ++j) {
-    const double piv = A[j + (size_t)j * n];
-    if (!(piv > 0.0)) {
-      if (threadIdx.x == 0) *q.flag = -2;
+  for (int j0 = 0; j0 < n; j0 += CHOL_NB) {
+    const int nb = min(CHOL_NB, n - j0), m = n - j0;
+    for (int t = tid; t < nb * m; t += blockDim.x) {
+      const int c = t / m, r = t % m;
+      pan[(size_t)c * m + r] = A[(size_t)(j0 + c) * n + j0 + r];
+    }
+    __syncthreads();
+    for (int jj = 0; jj < nb; ++jj) {
+      double* cj = pan + (size_t)jj * m;
+      const double piv = cj[jj];
+      if (!(piv > 0.0)) {
+        if (tid == 0) bad = 1;
+        break;
+      }
+      const double d = sqrt(piv), inv = 1.0 / d;
+      for (int r = jj + 1 + tid; r < m; r += blockDim.x) cj[r] *= inv;
+      __syncthreads();
+      if (tid == 0) cj[jj] = d;
+      for (int t = tid; t < (nb - jj - 1) * m; t += blockDim.x) {  // later panel columns
+        const int c = jj + 1 + t / m, r = t % m;
+        if (r >= c) pan[(size_t)c * m + r] -= cj[r] * cj[c];
+      }
+      __syncthreads();
+    }
+    __syncthreads();
+    if (bad) {
+      if (tid == 0) *q.flag = -2;
       return;
     }
-    const double inv = 1.0 / sqrt(piv);
-    double* cj = A + (size_t)j * n;
-    for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x) cj[i] *= inv;
-    __syncthreads();
-    for (int c = j + 1 + warp; c < n; c += nw) {
-      const double lc = cj[c];
-      double* cc = A + (size_t)c * n;
-      for (int i = c + lane; i < n; i += 32) cc[i] -= cj[i] * lc;
+    for (int t = tid; t < nb * m; t += blockDim.x) {
+      const int c = t / m, r = t % m;
+      if (r >= c) A[(size_t)(j0 + c) * n + j0 + r] = pan[(size_t)c * m + r];
+    }
+    // trailing update of rows and columns j0 + nb .. n-1 (lower triangle)
+    const int m2 = m - nb, nt = (m2 + 63) / 64;
+    const int tr = tid & 15, tc = tid >> 4;
+    for (int tile = 0; tile < nt * (nt + 1) / 2; ++tile) {
+      int ti = 0;
+      while ((ti + 1) * (ti + 2) / 2 <= tile) ++ti;
+      const int tj = tile - ti * (ti + 1) / 2;  // tile row ti >= tile column tj
+      const int r0 = nb + 64 * ti, c0 = nb + 64 * tj;  // panel-relative rows / columns
+      double acc[4][4];
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = 0.0;
+      for (int k = 0; k < nb; ++k) {
+        const double* pk = pan + (size_t)k * m;
+        double pr[4], pc[4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+          const int r = r0 + tr + 16 * a, c = c0 + tc + 16 * a;
+          pr[a] = r < m ? pk[r] : 0.0;
+          pc[a] = c < m ? pk[c] : 0.0;
+        }
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+          for (int b = 0; b < 4; ++b) acc[a][b] = fma(pr[a], pc[b], acc[a][b]);
+      }
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+          const int r = r0 + tr + 16 * a, c = c0 + tc + 16 * b;
+          if (r < m && c < m && r >= c) A[(size_t)(j0 + c) * n + j0 + r] -= acc[a][b];
+        }
     }
     __syncthreads();
   }
-  for (size_t t = threadIdx.x; t < nn; t += blockDim.x) {
+  for (size_t t = tid; t < nn; t += blockDim.x) {
     const int i = (int)(t % n), j = (int)(t / n);
     if (i < j) A[t] = 0.0;
-    else if (i == j) A[t] = sqrt(A[t]);
   }
 }
 
@@ -413,7 +474,17 @@ __global__ void kb_tri_inv_t(BARGS) {
 void cholesky_inverse_b(const BatchLaunch& b) {
   if (!b.count) return;
   g_kernel_launches += 2;
-  kb_cholesky<<<dim3(1, 1, b.count), 256, 0, b.s>>>(b.mp, b.list);
+  const size_t smem = (size_t)CHOL_NB * b.nao_max * sizeof(double);
+  static size_t attr = 0;
+  if (smem > 48 * 1024 && smem > attr) {
+    const cudaError_t e = cudaFuncSetAttribute(
+        kb_cholesky, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess)
+      throw std::runtime_error(std::string("CUDA error '") + cudaGetErrorString(e) +
+                               "' in batched Cholesky shared memory");
+    attr = smem;
+  }
+  kb_cholesky<<<dim3(1, 1, b.count), 256, smem, b.s>>>(b.mp, b.list);
   kb_tri_inv_t<<<dim3((b.nao_max * 32 + 255) / 256, 1, b.count), 256, 0, b.s>>>(b.mp, b.list);
 }
 
