@@ -532,8 +532,8 @@ void cholesky_inverse_b(const BatchLaunch& b) {
   if (!b.count) return;
   g_kernel_launches += 2;
   const size_t smem = (size_t)CHOL_NB * b.nao_max * sizeof(double);
-  static size_t attr = 0;
-  if (smem > 48 * 1024 && smem > attr) {
+  static size_t attr = 0;  // the kernel's static shared memory comes on top of smem
+  if (smem > attr) {
     const cudaError_t e = cudaFuncSetAttribute(
         kb_cholesky, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess)
