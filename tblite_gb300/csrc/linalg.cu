@@ -467,9 +467,10 @@ __global__ void __launch_bounds__(256) kb_cholesky(BARGS) {
 
 // X = L^-T of the batch, one warp per column j of X (back substitution x_i = -(sum_{i<k<=j}
 // L_ki x_k) / L_ii for i = j-1 .. 0).  The column stays in registers across the warp (element k
-// on lane k % 32), so the chain of j steps waits only on a warp sum and a division; the column
-// of L that the next step reads is loaded one step ahead.  Orders beyond 32 TRI_INV_R take the
-// general form.
+// on lane k % 32), so the chain of j steps waits only on a warp sum and a multiplication; the
+// column of L and the reciprocal of the diagonal element that the next step needs are formed
+// one step ahead, and only the registers holding rows i+1 .. j take part in a step's sum.
+// Orders beyond 32 TRI_INV_R take the general form.
 constexpr int TRI_INV_R = 18;
 __device__ __forceinline__ void tri_col_load(const double* __restrict__ L, int n, int i, int j,
                                              int lane, double (&v)[TRI_INV_R]) {
@@ -496,28 +497,32 @@ __global__ void kb_tri_inv_t(BARGS) {
 #pragma unroll
   for (int t = 0; t < TRI_INV_R; ++t) xr[t] = (lane + 32 * t == j) ? xjj : 0.0;
   double cur[TRI_INV_R];
-  double dcur = j > 0 ? L[(j - 1) + (size_t)(j - 1) * n] : 1.0;
+  // reciprocal of the diagonal element of the current step, formed a step ahead (off the chain)
+  double rcur = j > 0 ? 1.0 / L[(j - 1) + (size_t)(j - 1) * n] : 1.0;
   if (j > 0) tri_col_load(L, n, j - 1, j, lane, cur);
+  const int thi = j >> 5;
   for (int i = j - 1; i >= 0; --i) {
     double nxt[TRI_INV_R];
-    double dnxt = 1.0;
+    double rnxt = 1.0;
     if (i > 0) {
       tri_col_load(L, n, i - 1, j, lane, nxt);
-      dnxt = L[(i - 1) + (size_t)(i - 1) * n];
+      rnxt = 1.0 / L[(i - 1) + (size_t)(i - 1) * n];
     }
+    const int tlo = (i + 1) >> 5;  // registers that hold rows i+1 .. j (a warp-uniform range)
     double s = 0.0;
 #pragma unroll
-    for (int t = 0; t < TRI_INV_R; ++t) s = fma(cur[t], xr[t], s);
+    for (int t = 0; t < TRI_INV_R; ++t)
+      if (t >= tlo && t <= thi) s = fma(cur[t], xr[t], s);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    const double xi = -s / dcur;
+    const double xi = -s * rcur;
 #pragma unroll
     for (int t = 0; t < TRI_INV_R; ++t)
       if (lane + 32 * t == i) xr[t] = xi;
     if (i > 0) {
 #pragma unroll
       for (int t = 0; t < TRI_INV_R; ++t) cur[t] = nxt[t];
-      dcur = dnxt;
+      rcur = rnxt;
     }
   }
   double* x = q.X + (size_t)j * n;
