@@ -54,7 +54,7 @@ int tblite_gb300_batch_last_modes(int* modes, int nmol);
  * never switched on against tblite_gb300_set_batch_graphs), the projection threshold (128, 144,
  * 157, 176, 224 orbitals or off), the bucket cut (3/4, 2/3, 4/5 of the largest orbital count), the CTAs
  * per SM of the cluster tridiagonalisation (1, 2) and the side streams (4, 8, 16), each candidate
- * timed as the wall time of a batch call (best of two) on a fixed pseudo-random sample of
+ * timed as the wall time of a batch call (best of three) on a fixed pseudo-random sample of
  * `sample` of the given molecules (256 if <= 0).  The fastest schedule stays set.  Returns the
  * number of timed calls, -1 if the sample could not be evaluated. */
 int tblite_gb300_batch_autotune(tblite_context ctx, int nmol, const tblite_structure* mols,

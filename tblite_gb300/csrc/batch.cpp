@@ -1201,7 +1201,7 @@ extern "C" int tblite_gb300_batch_schedule(char* buf, int n) {
 
 // Autotuner of the batch schedule (no counterpart in the reference): coordinate descent over
 // CUDA graphs on/off, the projection threshold, the bucket cut, the CTAs per SM of the tridiagonalisation and the side
-// streams, each candidate timed (wall time of the call, best of two) on a seeded sample of the given
+// streams, each candidate timed (wall time of the call, best of three) on a seeded sample of the given
 // molecules; the fastest schedule stays set.  Returns the number of timed calls, or -1 if the
 // sample could not be evaluated (the schedule is then left as it was).
 extern "C" int tblite_gb300_batch_autotune(tblite_context ctx, int nmol,
@@ -1230,7 +1230,7 @@ extern "C" int tblite_gb300_batch_autotune(tblite_context ctx, int nmol,
   int calls = 0;
   auto time_it = [&]() {
     double best = 1e300;
-    for (int r = 0; r < 2; ++r) {
+    for (int r = 0; r < 3; ++r) {
       quiet.errors.clear();
       // wall time of the whole call: molecules handed to the one-molecule path count too
       const auto t0 = std::chrono::steady_clock::now();
