@@ -53,7 +53,8 @@ int tblite_gb300_batch_last_modes(int* modes, int nmol);
 /* Autotuner of the batch schedule: coordinate descent over CUDA graphs (kept, or switched off;
  * never switched on against tblite_gb300_set_batch_graphs), the projection threshold (128, 144,
  * 157, 176, 224 orbitals or off), the bucket cut (3/4, 2/3, 4/5 of the largest orbital count), the CTAs
- * per SM of the cluster tridiagonalisation (1, 2) and the side streams (4, 8, 16), each candidate
+ * per SM of the cluster tridiagonalisation (1, 2), the small-bucket tridiagonalisation (full
+ * storage or packed) and the side streams (4, 8, 16), each candidate
  * timed as the wall time of a batch call (best of three) on a fixed pseudo-random sample of
  * `sample` of the given molecules (256 if <= 0).  The fastest schedule stays set.  Returns the
  * number of timed calls, -1 if the sample could not be evaluated. */
@@ -86,6 +87,10 @@ void tblite_gb300_set_split_gemm(int enable);
 /* number of streams (1..16, default 8) over which a batch call spreads its size buckets; 1 runs
  * the buckets one after the other, so per-kernel event times bracket each kernel alone */
 void tblite_gb300_set_batch_streams(int count);
+/* tridiagonalisation of batch buckets of at most 156 orbitals: 1 (default) the one-CTA kernel
+ * with the full matrix in shared memory, 0 the packed lower-triangle kernel (a cluster of one or
+ * two CTAs; two thirds of the FMAs) */
+void tblite_gb300_set_small_tridiag(int full_storage);
 /* schedule of the batched tridiagonalisation: 2 (default) clusters wide enough that two CTAs
  * share an SM (one computes while the other waits at a cluster barrier), 1 the narrowest
  * cluster whose CTAs fit the shared memory of one SM each */

@@ -1139,6 +1139,10 @@ extern "C" int tblite_gb300_batch_last_fallbacks(void) { return g_last_fallbacks
 extern "C" void tblite_gb300_set_split_gemm(int enable) { tb::g_split_gemm = enable != 0; }
 namespace tb {
 void set_tridiag_ctas_per_sm(int k);
+void set_tridiag_small(int k);
+}
+extern "C" void tblite_gb300_set_small_tridiag(int full_storage) {
+  tb::set_tridiag_small(full_storage);
 }
 extern "C" void tblite_gb300_set_tridiag_ctas_per_sm(int count) {
   tb::set_tridiag_ctas_per_sm(count);
@@ -1168,16 +1172,18 @@ extern "C" int tblite_gb300_batch_last_iterations(int* iterations, int nmol) {
 
 namespace tb {
 int get_tridiag_ctas_per_sm();
+int get_tridiag_small();
 }
 
 // back to the default schedule (CUDA graphs, projection from 128 orbitals, bucket cut 3/4, two
-// CTAs per SM, 8 streams)
+// CTAs per SM, full-storage small tridiagonalisation, 8 streams)
 extern "C" void tblite_gb300_batch_reset_schedule(void) {
   g_batch_graphs = true;
   g_sp2_min_nao = SP2_MIN_NAO;
   g_cut_num = 3;
   g_cut_den = 4;
   tb::set_tridiag_ctas_per_sm(2);
+  tb::set_tridiag_small(1);
   g_batch_streams = 8;
   g_schedule_note = "defaults";
 }
@@ -1188,10 +1194,11 @@ extern "C" int tblite_gb300_batch_schedule(char* buf, int n) {
   char tmp[384];
   const int len = std::snprintf(
       tmp, sizeof(tmp),
-      "projection from %d orbitals%s; bucket cut %d/%d; tridiagonalisation %d CTA(s) per SM; "
-      "%d streams; %s",
+      "projection from %d orbitals%s; bucket cut %d/%d; tridiagonalisation %d CTA(s) per SM, "
+      "%s below 157 orbitals; %d streams; %s",
       g_sp2_min_nao, g_batch_sp2 ? "" : " (off)", g_cut_num, g_cut_den,
-      tb::get_tridiag_ctas_per_sm(), g_batch_streams, g_schedule_note.c_str());
+      tb::get_tridiag_ctas_per_sm(), tb::get_tridiag_small() ? "full storage" : "packed",
+      g_batch_streams, g_schedule_note.c_str());
   if (buf && n > 0) {
     std::strncpy(buf, tmp, (size_t)n - 1);
     buf[n - 1] = '\0';
@@ -1267,6 +1274,8 @@ extern "C" int tblite_gb300_batch_autotune(tblite_context ctx, int nmol,
   try_values([](int v) { g_sp2_min_nao = v; }, {128, 144, 157, 176, 224, 100000}, sp2);
   try_values([](int v) { g_cut_num = v / 10; g_cut_den = v % 10; }, {34, 23, 45}, cut);
   try_values([](int v) { tb::set_tridiag_ctas_per_sm(v); }, {1, 2}, ctas);
+  int small = tb::get_tridiag_small();
+  try_values([](int v) { tb::set_tridiag_small(v); }, {0, 1}, small);
   try_values([](int v) { g_batch_streams = v; }, {4, 8, 16}, streams);
   char note[160];
   std::snprintf(note, sizeof(note), "autotuned on %d molecules (%d calls, %.1f ms)%s", k, calls,

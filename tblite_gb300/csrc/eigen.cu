@@ -1477,6 +1477,12 @@ static int tridiag_cluster(int n, size_t* smem) {
 }
 void set_tridiag_ctas_per_sm(int k) { g_tridiag_ctas_per_sm = k >= 2 ? 2 : 1; }
 int get_tridiag_ctas_per_sm() { return g_tridiag_ctas_per_sm; }
+// buckets of at most TRI_SMALL_MAX orbitals: the one-CTA full-storage kernel (1, default) or the
+// packed lower-triangle kernel as a cluster of one CTA (0: two thirds of the FMAs, half the
+// shared memory, but row accumulators summed per column)
+static int g_tridiag_small = 1;
+void set_tridiag_small(int k) { g_tridiag_small = k ? 1 : 0; }
+int get_tridiag_small() { return g_tridiag_small; }
 int batch_tridiag_max_n() {
   int n = 1;
   size_t sm = 0;
@@ -1506,7 +1512,7 @@ void eigen_values_b(const BatchLaunch& b) {
   batch_attributes();
   gemm_b(b, GS_FX);
   gemm_b(b, GS_XTT);
-  if (b.nao_max <= TRI_SMALL_MAX) {
+  if (b.nao_max <= TRI_SMALL_MAX && g_tridiag_small) {
     const size_t sm_small = sizeof(double) * ((size_t)b.nao_max * b.nao_max + 2 * b.nao_max);
     ++g_kernel_launches;
     const int tk = prof_kbegin(b.s);

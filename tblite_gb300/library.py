@@ -92,6 +92,7 @@ _SIGNATURES = {
     "tblite_gb300_get_kernel_profile": (c_int, [_dbl_p, _int_p, c_int]),
     "tblite_gb300_set_split_gemm": (None, [c_int]),
     "tblite_gb300_set_batch_streams": (None, [c_int]),
+    "tblite_gb300_set_small_tridiag": (None, [c_int]),
     "tblite_gb300_set_tridiag_ctas_per_sm": (None, [c_int]),
     "tblite_gb300_get_calculator_slater_exponents": (None, [c_void_p, c_void_p, _dbl_p]),
     "tblite_gb300_set_calculator_slater_exponents": (None, [c_void_p, c_void_p, _dbl_p]),
@@ -266,6 +267,12 @@ def batch_graphs_enabled() -> bool:
 def batch_projected() -> int:
     """Molecules of the last batch call whose SCF density came from the spectral projection."""
     return int(load().tblite_gb300_batch_last_projected())
+
+
+def set_small_tridiag(full_storage: bool) -> None:
+    """Small batch buckets: one-CTA full-storage tridiagonalisation (default) or the packed
+    lower-triangle kernel."""
+    load().tblite_gb300_set_small_tridiag(1 if full_storage else 0)
 
 
 def set_batch_streams(count: int) -> None:

@@ -248,3 +248,24 @@ def test_scf_iterations_as_cuda_graphs():
     for a, b in zip(res_g, res_d):
         assert abs(a.get("energy") - b.get("energy")) <= 1e-12
         assert np.max(np.abs(a.get("gradient") - b.get("gradient"))) <= 1e-12
+
+
+def test_packed_small_tridiagonalisation():
+    """Small buckets tridiagonalised by the packed lower-triangle kernel (a cluster of one or two
+    CTAs) instead of the one-CTA full-storage kernel: same results as the one-molecule path,
+    from the smallest molecules (3 orbitals) up to the largest bucket the small kernel takes."""
+    from tblite_gb300 import library, workloads
+    from tblite_gb300.interface import batch_fallbacks, batch_singlepoint
+
+    mols = _ensemble() + [workloads.water_cluster_k(26, seed=411),
+                          workloads.alkane(25, seed=412)]  # 156 and 152 orbitals
+    try:
+        library.set_batch_density_solver("diagonalization")  # every bucket diagonalises
+        library.set_small_tridiag(False)
+        res = batch_singlepoint([_calc(z, x) for z, x in mols])
+        assert batch_fallbacks() == 0
+    finally:
+        library.set_small_tridiag(True)
+        library.set_batch_density_solver("purification")
+    for (z, x), rb in zip(mols, res):
+        _compare(rb, _calc(z, x).singlepoint())
