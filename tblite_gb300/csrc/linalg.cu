@@ -468,8 +468,9 @@ __global__ void __launch_bounds__(256) kb_cholesky(BARGS) {
 // X = L^-T of the batch, one warp per column j of X (back substitution x_i = -(sum_{i<k<=j}
 // L_ki x_k) / L_ii for i = j-1 .. 0).  The column stays in registers across the warp (element k
 // on lane k % 32), so the chain of j steps waits only on a warp sum and a multiplication; the
-// column of L and the reciprocal of the diagonal element that the next step needs are formed
-// one step ahead, and only the registers holding rows i+1 .. j take part in a step's sum.
+// column of L that the next step needs is loaded one step ahead, the reciprocals of the
+// diagonal are formed once per warp (spread over its lanes), and only the registers holding
+// rows i+1 .. j take part in a step's sum.
 // Orders beyond 32 TRI_INV_R take the general form.
 constexpr int TRI_INV_R = 18;
 __device__ __forceinline__ void tri_col_load(const double* __restrict__ L, int n, int i, int j,
@@ -496,18 +497,25 @@ __global__ void kb_tri_inv_t(BARGS) {
   const double xjj = 1.0 / L[j + (size_t)j * n];
 #pragma unroll
   for (int t = 0; t < TRI_INV_R; ++t) xr[t] = (lane + 32 * t == j) ? xjj : 0.0;
+  // reciprocals of the diagonal elements L_kk, k < j, one per lane and register (a few
+  // divisions per warp instead of one per step); step i takes its own by a shuffle
+  double rd[TRI_INV_R];
+#pragma unroll
+  for (int t = 0; t < TRI_INV_R; ++t) {
+    const int k = lane + 32 * t;
+    rd[t] = k < j ? 1.0 / L[k + (size_t)k * n] : 1.0;
+  }
   double cur[TRI_INV_R];
-  // reciprocal of the diagonal element of the current step, formed a step ahead (off the chain)
-  double rcur = j > 0 ? 1.0 / L[(j - 1) + (size_t)(j - 1) * n] : 1.0;
   if (j > 0) tri_col_load(L, n, j - 1, j, lane, cur);
   const int thi = j >> 5;
   for (int i = j - 1; i >= 0; --i) {
     double nxt[TRI_INV_R];
-    double rnxt = 1.0;
-    if (i > 0) {
-      tri_col_load(L, n, i - 1, j, lane, nxt);
-      rnxt = 1.0 / L[(i - 1) + (size_t)(i - 1) * n];
-    }
+    if (i > 0) tri_col_load(L, n, i - 1, j, lane, nxt);
+    double rsel = 1.0;
+#pragma unroll
+    for (int t = 0; t < TRI_INV_R; ++t)
+      if (t == (i >> 5)) rsel = rd[t];
+    const double rcur = __shfl_sync(0xffffffffu, rsel, i & 31);
     const int tlo = (i + 1) >> 5;  // registers that hold rows i+1 .. j (a warp-uniform range)
     double s = 0.0;
 #pragma unroll
@@ -522,7 +530,6 @@ __global__ void kb_tri_inv_t(BARGS) {
     if (i > 0) {
 #pragma unroll
       for (int t = 0; t < TRI_INV_R; ++t) cur[t] = nxt[t];
-      rcur = rnxt;
     }
   }
   double* x = q.X + (size_t)j * n;
