@@ -534,6 +534,10 @@ def run_batch(args):
                      "bound": "tensor", "achieved": round(ach, 4), "peak": round(bf16, 4),
                      "unit": "TFLOP/s", "frac": round(ach / bf16, 4), "timing": timing,
                      "traffic": _profile_traffic("pipe_sq_ensemble512.md"),
+                     "traffic_note": "dram__bytes_read+write of one captured kb_opipe_sq launch "
+                                     "(38 molecules of 288-384 orbitals; "
+                                     "profiles/pipe_sq_ensemble512.md): each slice image read "
+                                     "about once from DRAM, the tile re-reads served by L2",
                      "peak_source": f"{peak_kind} (bf16 sustained)",
                      "algorithmic_work_per_call": SPLIT_SLICE_PRODUCTS * pipe_flops_s,
                      "work_note": "36 BF16 slice products per FP64-equivalent flop; FP64-"
