@@ -1318,27 +1318,34 @@ __global__ void __launch_bounds__(256) kb_tridiag(BARGS) {
 // reduction with everything on chip.  Per column: warp 0 builds the reflector (no block
 // reduction), the warps form p = t A22 v column by column, every warp reduces K = -t/2 p.v
 // for itself, w = p + K v is formed once per row, and all threads apply the symmetric rank-2
-// update (two FMAs per element) as one 2-d loop over the trailing block.  Five block barriers
-// per column.  The reflectors and the diagonal go to
-// global memory at the end in the layout the back-transformation reads (column-major A,
-// v below the subdiagonal).
-constexpr int TRI_SMALL_MAX = 156;  // (n^2 + 2n) doubles <= 200 KB
+// update to the lower triangle only (two FMAs per stored element, half the elements of the
+// full block).  p_j then reads column j from the diagonal down and the rest of it, above the
+// diagonal, as row j of the lower triangle (the same elements by symmetry); the columns are
+// ld = n | 1 doubles apart, so those row reads hit distinct banks.  Five block barriers per
+// column.  The reflectors and the diagonal go to global memory at the end in the layout the
+// back-transformation reads (column-major A, v below the subdiagonal).
+constexpr int TRI_SMALL_MAX = 156;  // n (n | 1) + 2n doubles <= 200 KB
+__host__ __device__ constexpr size_t tri_small_doubles(int n) {
+  return (size_t)n * (size_t)(n | 1) + 2 * (size_t)n;
+}
+static_assert(sizeof(double) * tri_small_doubles(TRI_SMALL_MAX) <= TRIDIAG_SMEM_MAX,
+              "the largest small tridiagonalisation fits the shared-memory attribute");
 __global__ void __launch_bounds__(256) kb_tridiag_small(BARGS) {
   BMOL;
-  const int n = q.m.nao;
+  const int n = q.m.nao, ld = n | 1;
   extern __shared__ double sm[];
-  double* a = sm;            // [n][n] column-major, full symmetric storage
-  double* sv = sm + n * n;   // [n] reflector (sv[i+1] = 1)
-  double* sp = sv + n;       // [n] p, then w
+  double* a = sm;                    // [n][ld] column-major; the lower triangle is kept current
+  double* sv = sm + (size_t)n * ld;  // [n] reflector (sv[i+1] = 1)
+  double* sp = sv + n;               // [n] p, then w
   __shared__ double s_t;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
   const double* A0 = q.A;
-  for (int t = tid; t < n * n; t += blockDim.x) a[t] = A0[t];
+  for (int t = tid; t < n * n; t += blockDim.x) a[(size_t)(t / n) * ld + t % n] = A0[t];
   __syncthreads();
   for (int i = 0; i < n - 1; ++i) {
     const int r0 = i + 1;  // trailing block rows/cols r0 .. n-1
     if (wid == 0) {        // reflector of column i
-      double* col = a + (size_t)i * n;
+      double* col = a + (size_t)i * ld;
       const double alpha = col[r0];
       double s = 0.0;
       for (int r = r0 + 1 + lane; r < n; r += 32) s += col[r] * col[r];
@@ -1365,11 +1372,13 @@ __global__ void __launch_bounds__(256) kb_tridiag_small(BARGS) {
     __syncthreads();
     const double t = s_t;
     if (t != 0.0) {
-      // p_j = t * A22(:, j) . v  (warp per column)
+      // p_j = t * A22(:, j) . v  (warp per column): rows j .. n-1 from column j, rows
+      // r0 .. j-1 from row j
       for (int j = r0 + wid; j < n; j += nw) {
-        const double* col = a + (size_t)j * n;
+        const double* col = a + (size_t)j * ld;
         double acc = 0.0;
-        for (int r = r0 + lane; r < n; r += 32) acc += col[r] * sv[r];
+        for (int r = j + lane; r < n; r += 32) acc += col[r] * sv[r];
+        for (int r = r0 + lane; r < j; r += 32) acc += a[(size_t)r * ld + j] * sv[r];
         acc = wred(acc) * t;
         if (lane == 0) sp[j] = acc;
       }
@@ -1379,21 +1388,21 @@ __global__ void __launch_bounds__(256) kb_tridiag_small(BARGS) {
       for (int r = r0 + lane; r < n; r += 32) kk += sp[r] * sv[r];
       const double K = -0.5 * t * wred(kk);
       __syncthreads();  // every warp has read p
-      // w = p + K v once per row, then two FMAs per element: A -= v w^T + w v^T
+      // w = p + K v once per row, then two FMAs per element: A -= v w^T + w v^T (lower part)
       for (int r = r0 + tid; r < n; r += blockDim.x) sp[r] = fma(K, sv[r], sp[r]);
       __syncthreads();
       for (int c = r0 + wid; c < n; c += nw) {  // warp per column, v_c and w_c in registers
-        double* col = a + (size_t)c * n;
+        double* col = a + (size_t)c * ld;
         const double vc = sv[c], wc = sp[c];
-        for (int r = r0 + lane; r < n; r += 32) col[r] = fma(-sv[r], wc, fma(-sp[r], vc, col[r]));
+        for (int r = c + lane; r < n; r += 32) col[r] = fma(-sv[r], wc, fma(-sp[r], vc, col[r]));
       }
     }
     __syncthreads();
   }
-  if (tid == 0) q.ed[n - 1] = a[(size_t)(n - 1) * n + (n - 1)];
+  if (tid == 0) q.ed[n - 1] = a[(size_t)(n - 1) * ld + (n - 1)];
   // reflectors (strictly below the subdiagonal of each column) for the back-transformation
   double* Ag = q.A;
-  for (int t2 = tid; t2 < n * n; t2 += blockDim.x) Ag[t2] = a[t2];
+  for (int t2 = tid; t2 < n * n; t2 += blockDim.x) Ag[t2] = a[(size_t)(t2 / n) * ld + t2 % n];
 }
 
 // Eigenvalues for the batch, one thread per eigenvalue (tri_eigenvalue: FP32 bisection, FP64
@@ -1513,7 +1522,7 @@ void eigen_values_b(const BatchLaunch& b) {
   gemm_b(b, GS_FX);
   gemm_b(b, GS_XTT);
   if (b.nao_max <= TRI_SMALL_MAX && g_tridiag_small) {
-    const size_t sm_small = sizeof(double) * ((size_t)b.nao_max * b.nao_max + 2 * b.nao_max);
+    const size_t sm_small = sizeof(double) * tri_small_doubles(b.nao_max);
     ++g_kernel_launches;
     const int tk = prof_kbegin(b.s);
     kb_tridiag_small<<<dim3(1, 1, b.count), 256, sm_small, b.s>>>(b.mp, b.list);
