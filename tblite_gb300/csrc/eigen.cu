@@ -1410,6 +1410,9 @@ __global__ void __launch_bounds__(256) kb_tridiag_small(BARGS) {
 // (every thread reads the same element at the same step).  rest = 0: eigenvalues j < nev and
 // the sentinel above them; rest = 1 (after the SCF): the eigenvalues nev <= j < n.
 constexpr int BIS_MAXN = 1024;
+// one warp per block: the Sturm counts are FP64-bound (a division per element), so spreading a
+// molecule's eigenvalues over more SMs shortens the kernel; each block stages d and e^2 again
+constexpr int EIG_BLOCK = 32;
 __global__ void __launch_bounds__(128) kb_eigvals(BARGS, int rest) {
   BMOL;
   const int n = q.m.nao;
@@ -1533,14 +1536,16 @@ void eigen_values_b(const BatchLaunch& b) {
   ++g_kernel_launches;
   const int tm = prof_kbegin(b.s);
   if (b.nao_max > BIS_MAXN) throw std::runtime_error("batched eigenvalues: molecule too large");
-  kb_eigvals<<<dim3((b.nao_max + 127) / 128, 1, b.count), 128, 0, b.s>>>(b.mp, b.list, 0);
+  kb_eigvals<<<dim3((b.nao_max + EIG_BLOCK - 1) / EIG_BLOCK, 1, b.count), EIG_BLOCK, 0, b.s>>>(
+      b.mp, b.list, 0);
   prof_kend(KS_MULTISECT, tm, b.s);
 }
 
 void eigen_values_rest_b(const BatchLaunch& b) {
   if (!b.count) return;
   ++g_kernel_launches;
-  kb_eigvals<<<dim3((b.nao_max + 127) / 128, 1, b.count), 128, 0, b.s>>>(b.mp, b.list, 1);
+  kb_eigvals<<<dim3((b.nao_max + EIG_BLOCK - 1) / EIG_BLOCK, 1, b.count), EIG_BLOCK, 0, b.s>>>(
+      b.mp, b.list, 1);
 }
 
 static void tridiag_cluster_b(const BatchLaunch& b) {
