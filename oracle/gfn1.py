@@ -336,7 +336,7 @@ def setup(calc):
                 hs=hs, ksh=ksh, hub=hub, gamma=gamma, gam3=gam3, n0sh=refocc, n0at=n0at)
 
 
-def singlepoint(calc: Calc1, grad=True, verbose=False):
+def singlepoint(calc: Calc1, grad=True, verbose=False, solvation=None):
     mol = calc.mol
     nat = len(mol.numbers)
     st = setup(calc)
@@ -374,6 +374,12 @@ def singlepoint(calc: Calc1, grad=True, verbose=False):
         disp = D3(calc, xyz)
         edisp = disp.energy_gradient(gradient, sigma)
     energies += edisp
+    # implicit solvation (the dielectric-constant GB models take atomic Mulliken charges for
+    # every method), geometry part
+    solv = solvation
+    if solv is not None:
+        solv.update(xyz)
+        energies += solv.nonsc_energies()
     ao2sh = np.repeat(np.arange(nsh), 2 * calc.sh_l + 1)
     ao2at = calc.sh_atom[ao2sh]
     qat = np.full(nat, mol.charge / nat)
@@ -393,6 +399,8 @@ def singlepoint(calc: Calc1, grad=True, verbose=False):
         iscf += 1
         vsh = st["gamma"] @ qsh
         vat = st["gam3"] * qat ** 2
+        if solv is not None:
+            vat = vat + solv.potential(qat)
         vao = (vsh + vat[calc.sh_atom])[ao2sh]
         F = st["H"] - 0.5 * st["S"] * (vao[:, None] + vao[None, :])
         mixer.set(qsh.copy())
@@ -415,6 +423,8 @@ def singlepoint(calc: Calc1, grad=True, verbose=False):
         e2sh = 0.5 * (st["gamma"] @ qsh) * qsh
         np.add.at(eelec, calc.sh_atom, e2sh)
         eelec += st["gam3"] * qat ** 3 / 3.0
+        if solv is not None:
+            eelec += solv.energies(qat)
         converged = abs(float(np.sum(eelec)) - elast) < econv and mixer.error() < pconv
         if verbose:
             print(iscf, float(np.sum(eelec + energies)), float(np.sum(eelec)) - elast, mixer.error())
@@ -446,6 +456,8 @@ def singlepoint(calc: Calc1, grad=True, verbose=False):
                          ctypes.c_double(sc["gexp"]), ctypes.c_int(1), _p(qsh), _p(gradient),
                          _p(sigma))
         gradient += np.einsum("i,ikx->kx", dEdcn, st["dcn"])
+        if solv is not None:
+            gradient += solv.gradient(qat)
         for i in range(nat):
             for k in range(nat):
                 sigma += dEdcn[i] * np.outer(st["dcn"][i, k], xyz[k])

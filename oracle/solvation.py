@@ -1,4 +1,6 @@
-"""CPU oracle: ALPB implicit solvation with CDS and free-energy shift (GFN2 parameters, water).
+"""CPU oracle: generalized Born implicit solvation -- ALPB(water) and GBSA(water) with CDS and
+free-energy shift (GFN2 parameters), and the dielectric-constant GB models (GB-epsilon with or
+without the ALPB shape term, Still or P16 kernel).
 
 TEST INFRASTRUCTURE ONLY -- a CPU restatement of the reference's solvation containers used to
 check the CUDA engine.  Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU legs of
@@ -8,8 +10,10 @@ Follows (reference tblite 0.7.0):
   Born radii        src/tblite/solvation/born.f90:135-454 (compute_bornr, compute_psi; GBOBC
                     integrator, 35 Angstrom pair cutoff)
   ALPB kernel       src/tblite/solvation/alpb.f90:173-206 (new_alpb), 218-256 (update),
-                    426-535 (add_born_mat_p16, add_born_deriv_p16), 656-787 (get_adet,
-                    get_adet_deriv); energy/potential/gradient 260-365
+                    426-535 (add_born_mat_p16, add_born_deriv_p16), 562-684 (add_born_mat_still,
+                    add_born_deriv_still), 656-787 (get_adet, get_adet_deriv); energy/potential/
+                    gradient 260-365; dielectric-constant models api/solvation.f90:185-229 with
+                    the COSMO radii of data.f90:103-130 and born.f90:52-107 defaults
   CDS               src/tblite/solvation/cds.f90:166-365; surface.f90:80-387 (SASA with the
                     230-point Lebedev grid, smoothed step function)
   shift             src/tblite/solvation/shift.f90:150-241
@@ -67,17 +71,21 @@ def lebedev230(orbits):
 
 
 class ALPBWater:
-    """ALPB(water) + CDS + shift for GFN2 (tblite_new_alpb_solvation_solvent(..., 12, state))."""
+    """ALPB(water) + CDS + shift for GFN2 (tblite_new_alpb_solvation_solvent(..., 12, state));
+    with model="gbsa" the GBSA(water) tables and the Still kernel (version 22)."""
 
-    def __init__(self, numbers, state=1):
+    def __init__(self, numbers, state=1, model="alpb"):
         d = json.loads(DATA.read_text())
         aatoau, kcaltoau = d["constants"]["aatoau"], d["constants"]["kcaltoau"]
         z = np.asarray(numbers) - 1
         self.nat = len(z)
-        # ALPB (load_alpb_param, new_alpb, new_born_integrator)
-        a = d["alpb"]
+        gbsa = model == "gbsa"
+        self.kernel = "still" if gbsa else "p16"
+        self.cds = True
+        # ALPB / GBSA (load_alpb_param, new_alpb, new_born_integrator)
+        a = d["gbsa" if gbsa else "alpb"]
         eps = a["epsv"]
-        self.alpbet = ALPHA_ALPB / eps
+        self.alpbet = 0.0 if gbsa else ALPHA_ALPB / eps
         self.keps = (1.0 / eps - 1.0) / (1.0 + self.alpbet)
         self.vdwr = np.array(d["rvdw_d3"])[z]
         self.rho = self.vdwr * np.array(a["sx"])[z]
@@ -85,7 +93,7 @@ class ALPBWater:
         self.born_scale = a["c1"]
         self.lrcut = 35.0 * aatoau
         # CDS (load_cds_param, new_cds, new_surface_integrator)
-        c = d["cds"]
+        c = d["gbsa_cds" if gbsa else "cds"]
         probe = c["rprobe"] * aatoau
         rad = np.array(d["rvdw_d3"])[z]
         self.tension = np.array(c["gamscale"])[z] * 1.0e-5
@@ -103,7 +111,7 @@ class ALPBWater:
         self.srcut = 2.0 * (w + self.vdwsa.max()) + 2.0 * aatoau
         self.grid, self.gw = lebedev230(d["lebedev230"])
         # shift (load_shift_param, new_shift, get_stateshift)
-        s = d["shift"]
+        s = d["gbsa_shift" if gbsa else "shift"]
         gshift = s["gshift"] * kcaltoau
         temp, amb = 298.15, 298.15
         vm = R_GAS * amb / 1.0e2  # ideal-gas molar volume, reference units (L/mol)
@@ -122,7 +130,10 @@ class ALPBWater:
         self.xyz = xyz
         self.brad, self.dbrad = self._born(xyz)
         self.adet = self._adet(xyz)
-        self.surface, self.dsdr = self._sasa(xyz)
+        if self.cds:
+            self.surface, self.dsdr = self._sasa(xyz)
+        else:
+            self.surface, self.dsdr = np.zeros(self.nat), np.zeros((self.nat, self.nat, 3))
 
     def _born(self, xyz):
         nat = self.nat
@@ -232,6 +243,10 @@ class ALPBWater:
         for i in range(nat):
             for j in range(i):
                 r = np.linalg.norm(xyz[i] - xyz[j])
+                if self.kernel == "still":
+                    aa = self.brad[i] * self.brad[j]
+                    J[i, j] = J[j, i] = self.keps / math.sqrt(r * r + aa * math.exp(-0.25 * r * r / aa))
+                    continue
                 ab = math.sqrt(self.brad[i] * self.brad[j])
                 arg = ab / (ab + ZETA_P16 / 16.0 * r)
                 arg = arg ** 16
@@ -264,6 +279,19 @@ class ALPBWater:
                 vec = xyz[i] - xyz[j]
                 r = np.linalg.norm(vec)
                 qq = qat[i] * qat[j]
+                if self.kernel == "still":  # add_born_deriv_still
+                    aa = self.brad[i] * self.brad[j]
+                    dd = 0.25 * r * r / aa
+                    expd = math.exp(-dd)
+                    dfgb2 = 1.0 / (r * r + aa * expd)
+                    dfgb3 = dfgb2 * math.sqrt(dfgb2) * keps
+                    dG = (1.0 - 0.25 * expd) * dfgb3 * vec * qq
+                    g[i] -= dG
+                    g[j] += dG
+                    bp = -0.5 * expd * (1.0 + dd) * dfgb3
+                    dedbr[i] += self.brad[j] * bp * qq
+                    dedbr[j] += self.brad[i] * bp * qq
+                    continue
                 ab = math.sqrt(self.brad[i] * self.brad[j])
                 arg1 = ab / (ab + ZETA_P16 / 16.0 * r)
                 arg16 = arg1 ** 16
@@ -304,3 +332,28 @@ class ALPBWater:
         for i in range(nat):
             g[i] += rad3[i] * (ad @ (xyz[i] - center))
         return g
+
+
+class GBEpsilon(ALPBWater):
+    """Generalized Born model with a dielectric constant (tblite_new_gb_solvation_epsilon):
+    alpb=True is version 10 (GB-epsilon with the ALPB shape term), False version 20; kernel
+    "still" or "p16".  COSMO radii, descreening 0.8, Born scale 1, no offset, no surface term
+    and no free-energy shift."""
+
+    def __init__(self, numbers, eps, alpb=True, kernel="p16"):
+        d = json.loads(DATA.read_text())
+        aatoau = d["constants"]["aatoau"]
+        z = np.asarray(numbers) - 1
+        self.nat = len(z)
+        self.kernel = kernel
+        self.cds = False
+        self.alpbet = ALPHA_ALPB / eps if alpb else 0.0
+        self.keps = (1.0 / eps - 1.0) / (1.0 + self.alpbet)
+        self.vdwr = np.array(d["rvdw_cosmo"])[z]
+        self.rho = self.vdwr * 0.8
+        self.svdw = self.vdwr.copy()
+        self.born_scale = 1.0
+        self.lrcut = 35.0 * aatoau
+        self.tension = np.zeros(self.nat)
+        self.hbond = np.zeros(self.nat)
+        self.total_shift = 0.0

@@ -131,6 +131,8 @@ struct Workspace {
 // shift.f90 with the gfn2 water parameters), built by tblite_new_alpb_solvation_solvent
 struct SolvModel {
   int nat = 0, state = 1;
+  int kernel = 2;    // Born interaction kernel: 1 Still, 2 P16 (alpb.f90:45-51)
+  bool cds = true;   // surface (CDS) term present; the dielectric-constant models have none
   double keps = 0, alpbet = 0, born_scale = 0, lrcut = 0, srcut = 0, ah0 = 0, ah1 = 0, ah3 = 0;
   double shift = 0;  // total free-energy shift (Hartree)
   std::vector<double> vdwr, rho, svdw, vdwsa, wrp, trj2_lo, trj2_hi, tension, hbond;
@@ -259,9 +261,12 @@ void electron_counts(const _tblite_calculator* c, const _tblite_structure* mol, 
 // molecular dipole and traceless quadrupole from the atomic charges and multipoles
 // (wavefunction/mulliken.f90 get_molecular_dipole_moment / get_molecular_quadrupole_moment)
 void molecular_moments(const _tblite_structure* mol, _tblite_result* res);
-// ALPB(water) + CDS + shift model for the molecule (reference state 1 gsolv, 2 bar1mol,
-// 3 reference)
-std::unique_ptr<SolvModel> build_solvation(const _tblite_structure* mol, int state);
+// ALPB(water) or, with gbsa, GBSA(water) + CDS + shift model for the molecule (reference state
+// 1 gsolv, 2 bar1mol, 3 reference); the generalized Born model with a dielectric constant
+// (alpb: with the ALPB shape term; kernel 1 Still, 2 P16)
+std::unique_ptr<SolvModel> build_solvation(const _tblite_structure* mol, int state, bool gbsa);
+std::unique_ptr<SolvModel> build_gb_epsilon(const _tblite_structure* mol, double eps, bool alpb,
+                                            int kernel);
 // the one-molecule single point (energy + gradient) into res
 void run_singlepoint(_tblite_context* ctx, const _tblite_structure* mol, _tblite_calculator* c,
                      _tblite_result* res);

@@ -588,6 +588,8 @@ static DevSolv dev_solv(_tblite_calculator* c, const _tblite_structure* mol) {
   cuda_check(cudaMemsetAsync(w.sv_status.p, 0, sizeof(int), s), "zero");
   DevSolv v{};
   v.nat = nat;
+  v.kernel = sm.kernel;
+  v.cds = sm.cds ? 1 : 0;
   v.lrcut = sm.lrcut;
   v.srcut = sm.srcut;
   v.keps = sm.keps;
@@ -1266,17 +1268,24 @@ static std::vector<double> lebedev230() {
   return g;
 }
 
-std::unique_ptr<SolvModel> build_solvation(const _tblite_structure* mol, int state) {
+// gbsa: the GBSA(water) tables and the Still kernel without the ALPB shape term
+// (api/solvation.f90:272-283, data/alpb.f90:92-249), else ALPB(water) with the P16 kernel
+std::unique_ptr<SolvModel> build_solvation(const _tblite_structure* mol, int state, bool gbsa) {
   auto m = std::make_unique<SolvModel>();
   const int nat = mol->nat;
   m->nat = nat;
   m->state = state;
-  const double eps = ALPB_WATER_EPSV;
-  m->alpbet = 0.571412 / eps;
+  m->kernel = gbsa ? 1 : 2;
+  const double eps = gbsa ? GBSA_WATER_EPSV : ALPB_WATER_EPSV;
+  m->alpbet = gbsa ? 0.0 : 0.571412 / eps;
   m->keps = (1.0 / eps - 1.0) / (1.0 + m->alpbet);
-  m->born_scale = ALPB_WATER_C1;
+  m->born_scale = gbsa ? GBSA_WATER_C1 : ALPB_WATER_C1;
   m->lrcut = 35.0 * SOLV_AATOAU;
-  const double probe = CDS_WATER_RPROBE * SOLV_AATOAU;
+  const double* sx = gbsa ? GBSA_WATER_SX : ALPB_WATER_SX;
+  const double soset = gbsa ? GBSA_WATER_SOSET : ALPB_WATER_SOSET;
+  const double* gamscale = gbsa ? CDS_GBSA_WATER_GAMSCALE : CDS_WATER_GAMSCALE;
+  const double* sqrtghb = gbsa ? CDS_GBSA_WATER_SQRTGHB : CDS_WATER_SQRTGHB;
+  const double probe = (gbsa ? CDS_GBSA_WATER_RPROBE : CDS_WATER_RPROBE) * SOLV_AATOAU;
   const double w = 0.3 * SOLV_AATOAU;
   m->ah0 = 0.5;
   m->ah1 = 3.0 / (4.0 * w);
@@ -1287,8 +1296,8 @@ std::unique_ptr<SolvModel> build_solvation(const _tblite_structure* mol, int sta
     if (z < 1 || z > 94) throw std::runtime_error("No solvation parameters for Z > 94");
     const double rv = SOLV_RVDW_D3[z - 1];
     m->vdwr.push_back(rv);
-    m->rho.push_back(rv * ALPB_WATER_SX[z - 1]);
-    m->svdw.push_back(rv - ALPB_WATER_SOSET * 0.1 * SOLV_AATOAU);
+    m->rho.push_back(rv * sx[z - 1]);
+    m->svdw.push_back(rv - soset * 0.1 * SOLV_AATOAU);
     const double vs = rv + probe;
     maxsa = std::max(maxsa, vs);
     m->vdwsa.push_back(vs);
@@ -1298,8 +1307,8 @@ std::unique_ptr<SolvModel> build_solvation(const _tblite_structure* mol, int sta
       return (0.25 / w + 3.0 * m->ah3 * (0.2 * r * r - 0.5 * r * vs + vs * vs / 3.0)) * r * r * r;
     };
     m->wrp.push_back(part(vs + w) - part(vs - w));
-    m->tension.push_back(CDS_WATER_GAMSCALE[z - 1] * 1.0e-5);
-    const double hb = -SOLV_KCALTOAU * CDS_WATER_SQRTGHB[z - 1] * CDS_WATER_SQRTGHB[z - 1];
+    m->tension.push_back(gamscale[z - 1] * 1.0e-5);
+    const double hb = -SOLV_KCALTOAU * sqrtghb[z - 1] * sqrtghb[z - 1];
     m->hbond.push_back(hb / (4.0 * M_PI * vs * vs));
   }
   m->srcut = 2.0 * (w + maxsa) + 2.0 * SOLV_AATOAU;
@@ -1308,10 +1317,44 @@ std::unique_ptr<SolvModel> build_solvation(const _tblite_structure* mol, int sta
   const double vm = 8.314462618 * amb / 1.0e2;
   double stateshift = 0.0;
   if (state == 2) stateshift = temp * kb_au * log(vm * temp / amb);
+  const double rhos = gbsa ? SHIFT_GBSA_WATER_RHOS : SHIFT_WATER_RHOS;
+  const double smass = gbsa ? SHIFT_GBSA_WATER_SMASS : SHIFT_WATER_SMASS;
   if (state == 3)
-    stateshift = temp * kb_au *
-                 (log(vm * temp / amb) + log(SHIFT_WATER_RHOS / 1.0e-3 * 1.0 / SHIFT_WATER_SMASS));
-  m->shift = SHIFT_WATER_GSHIFT * SOLV_KCALTOAU + stateshift;
+    stateshift = temp * kb_au * (log(vm * temp / amb) + log(rhos / 1.0e-3 * 1.0 / smass));
+  m->shift = (gbsa ? SHIFT_GBSA_WATER_GSHIFT : SHIFT_WATER_GSHIFT) * SOLV_KCALTOAU + stateshift;
+  m->grid = lebedev230();
+  return m;
+}
+
+// generalized Born model with a dielectric constant (api/solvation.f90:185-229, alpb.f90:146-204,
+// born.f90:60-107): COSMO radii, descreening 0.8, Born scale 1, no offset; alpb adds the ALPB
+// shape term (version 10), kernel 1 Still or 2 P16; no surface term and no free-energy shift
+std::unique_ptr<SolvModel> build_gb_epsilon(const _tblite_structure* mol, double eps, bool alpb,
+                                            int kernel) {
+  auto m = std::make_unique<SolvModel>();
+  const int nat = mol->nat;
+  m->nat = nat;
+  m->kernel = kernel;
+  m->cds = false;
+  m->alpbet = alpb ? 0.571412 / eps : 0.0;
+  m->keps = (1.0 / eps - 1.0) / (1.0 + m->alpbet);
+  m->born_scale = 1.0;
+  m->lrcut = 35.0 * SOLV_AATOAU;
+  for (int i = 0; i < nat; ++i) {
+    const int z = mol->num[i];
+    if (z < 1 || z > 94) throw std::runtime_error("No solvation parameters for Z > 94");
+    const double rv = SOLV_RVDW_COSMO[z - 1];
+    m->vdwr.push_back(rv);
+    m->rho.push_back(rv * 0.8);
+    m->svdw.push_back(rv);
+    // no surface: the surface arrays only keep the device layout
+    m->vdwsa.push_back(rv);
+    m->wrp.push_back(0.0);
+    m->trj2_lo.push_back(0.0);
+    m->trj2_hi.push_back(0.0);
+    m->tension.push_back(0.0);
+    m->hbond.push_back(0.0);
+  }
   m->grid = lebedev230();
   return m;
 }
@@ -1971,17 +2014,31 @@ tblite_container tblite_new_spin_polarization(tblite_context ctx, tblite_structu
 tblite_container tblite_new_gb_solvation_epsilon(tblite_error error, tblite_structure mol,
                                                  double eps, enum tblite_solvation_param version,
                                                  enum tblite_born_kernel born) {
-  (void)eps;
-  (void)born;
+  if (!error) return nullptr;
   if (!mol) {
     set_err(error, "Molecular structure data is missing");
     return nullptr;
   }
-  set_err(error, version == tblite_solvation_gbe || version == tblite_solvation_gb
-                     ? "Generalized Born solvation with a dielectric constant is not available in "
-                       "the GPU engine (ALPB water only)"
-                     : "Unknown solvation model requested");
-  return nullptr;
+  if (version != tblite_solvation_gbe && version != tblite_solvation_gb) {
+    set_err(error, "Unknown solvation model requested");
+    return nullptr;
+  }
+  if (born != tblite_born_still && born != tblite_born_p16) {
+    set_err(error, "Unknown Born interaction kernel requested");
+    return nullptr;
+  }
+  if (!(eps > 0.0)) {
+    set_err(error, "Dielectric constant must be positive");
+    return nullptr;
+  }
+  try {
+    auto* cont = new _tblite_container();
+    cont->solv = build_gb_epsilon(mol, eps, version == tblite_solvation_gbe, (int)born);
+    return cont;
+  } catch (const std::exception& e) {
+    set_err(error, e.what());
+    return nullptr;
+  }
 }
 tblite_container tblite_new_ddx_solvation_epsilon(tblite_error error, tblite_structure mol,
                                                   double eps, enum tblite_solvation_param model) {
@@ -2014,8 +2071,9 @@ tblite_container tblite_new_alpb_solvation_solvent(tblite_error error, tblite_st
     set_err(error, "Solvent '" + name + "' is not available: the GPU engine provides water only");
     return nullptr;
   }
-  if (version != tblite_solvation_alpb_gfn2) {
-    set_err(error, "Only the ALPB model with GFN2 parameters is available in the GPU engine");
+  if (version != tblite_solvation_alpb_gfn2 && version != tblite_solvation_gbsa_gfn2) {
+    set_err(error, "Only the ALPB and GBSA models with GFN2 parameters are available in the GPU "
+                   "engine");
     return nullptr;
   }
   if (refstate < 1 || refstate > 3) {
@@ -2024,7 +2082,7 @@ tblite_container tblite_new_alpb_solvation_solvent(tblite_error error, tblite_st
   }
   try {
     auto* cont = new _tblite_container();
-    cont->solv = build_solvation(mol, (int)refstate);
+    cont->solv = build_solvation(mol, (int)refstate, version == tblite_solvation_gbsa_gfn2);
     return cont;
   } catch (const std::exception& e) {
     set_err(error, e.what());

@@ -156,6 +156,8 @@ constexpr int SOLV_NGRID = 230;    // Lebedev points per atom
 constexpr int SOLV_MAXSHELL = 32;  // partners in the smoothing shell of one grid point
 struct DevSolv {
   int nat;
+  int kernel;  // Born interaction kernel: 1 Still, 2 P16
+  int cds;     // surface term present (else the surface kernels do not run, surfaces are 0)
   double lrcut, srcut, keps, alpbet, adet, born_scale, ah0, ah1, ah3, shift;
   const double *vdwr, *rho, *svdw, *vdwsa, *wrp, *trj2_lo, *trj2_hi, *tension, *hbond;
   const double* grid;  // [230][4]: x, y, z, weight (x 4 pi)

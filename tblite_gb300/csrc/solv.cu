@@ -1,9 +1,11 @@
-// Implicit solvation: ALPB reaction field (P16 Born kernel, GBOBC Born radii), CDS surface
-// term with hydrogen-bond correction, free-energy shift.
+// Implicit solvation: generalized Born reaction field (P16 or Still kernel, GBOBC Born radii,
+// optional ALPB shape term), CDS surface term with hydrogen-bond correction, free-energy shift:
+// ALPB(water), GBSA(water) and the dielectric-constant GB models.
 //
 // Restated from the reference:
 //   Born radii           src/tblite/solvation/born.f90:135-454 (compute_bornr, compute_psi)
-//   ALPB matrix/energy   src/tblite/solvation/alpb.f90:218-365, 426-535 (P16 kernel), 656-787
+//   ALPB matrix/energy   src/tblite/solvation/alpb.f90:218-365, 426-535 (P16 kernel), 562-684
+//                        (Still kernel), 656-787 (shape term)
 //   CDS and SASA         src/tblite/solvation/cds.f90:247-365, surface.f90:80-387
 //   shift                src/tblite/solvation/shift.f90:185-241
 //
@@ -192,6 +194,12 @@ __device__ __forceinline__ double p16(double r, double bi, double bj, double kep
   return keps / (r + ab * arg);
 }
 
+// Still kernel (alpb.f90:562-601): keps / sqrt(r^2 + a exp(-r^2 / (4 a))), a = R_i R_j
+__device__ __forceinline__ double still(double r2, double bi, double bj, double keps) {
+  const double aa = bi * bj;
+  return keps / sqrt(r2 + aa * exp(-0.25 * r2 / aa));
+}
+
 // MODE 0: vat += J q + 2 hbond S q ;  MODE 1: eat += 1/2 q (J q) + hbond S q^2
 template <int MODE>
 __global__ void k_solv_jq(DevSolv v, const double* __restrict__ xyz, const double* __restrict__ q,
@@ -210,7 +218,8 @@ __global__ void k_solv_jq(DevSolv v, const double* __restrict__ xyz, const doubl
         const double d = xyz[3 * i + k] - xyz[3 * j + k];
         r2 += d * d;
       }
-      jij = p16(sqrt(r2), v.brad[i], v.brad[j], v.keps);
+      jij = v.kernel == 1 ? still(r2, v.brad[i], v.brad[j], v.keps)
+                          : p16(sqrt(r2), v.brad[i], v.brad[j], v.keps);
     }
     s += (jij + kconst) * q[j];
   }
@@ -222,7 +231,8 @@ __global__ void k_solv_jq(DevSolv v, const double* __restrict__ xyz, const doubl
   }
 }
 
-// ALPB pair gradient (P16 kernel, explicit part) and dE/dR_born, one warp per atom
+// Born pair gradient (explicit part) and dE/dR_born, one warp per atom: P16 kernel
+// (alpb.f90:470-535) or Still kernel (alpb.f90:604-684)
 __global__ void k_solv_pair_grad(DevSolv v, const double* __restrict__ xyz,
                                  const double* __restrict__ q, double* grad) {
   const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
@@ -236,7 +246,17 @@ __global__ void k_solv_pair_grad(DevSolv v, const double* __restrict__ xyz,
       d[k] = xyz[3 * i + k] - xyz[3 * j + k];
       r2 += d[k] * d[k];
     }
-    const double r1 = sqrt(r2), bj = v.brad[j], qq = qi * q[j];
+    const double bj = v.brad[j], qq = qi * q[j];
+    if (v.kernel == 1) {
+      const double aa = bi * bj, dd = 0.25 * r2 / aa, expd = exp(-dd);
+      const double dfgb2 = 1.0 / (r2 + aa * expd);
+      const double dfgb3 = dfgb2 * sqrt(dfgb2) * keps;
+      const double f = (1.0 - 0.25 * expd) * dfgb3 * qq;
+      for (int k = 0; k < 3; ++k) g[k] -= f * d[k];
+      dedbr += bj * (-0.5 * expd * (1.0 + dd) * dfgb3) * qq;
+      continue;
+    }
+    const double r1 = sqrt(r2);
     const double ab = sqrt(bi * bj);
     const double arg1 = ab / (ab + ZETA_P16 / 16.0 * r1);
     double a16 = arg1 * arg1;
@@ -357,8 +377,13 @@ __global__ void __launch_bounds__(256) k_sasa_grad(DevSolv v, const double* __re
 static inline unsigned warps(int nat) { return (unsigned)((nat * 32 + 127) / 128); }
 
 void solv_setup(const DevSolv& v, const double* xyz, double* eat, cudaStream_t s) {
-  g_kernel_launches += 4;
+  ++g_kernel_launches;
   k_born<<<warps(v.nat), 128, 0, s>>>(v, xyz);
+  if (!v.cds) {  // no surface term: zero surfaces (read by the potential kernels), no shift
+    cudaMemsetAsync(v.surface, 0, sizeof(double) * v.nat, s);
+    return;
+  }
+  g_kernel_launches += 3;
   k_sasa_nbl<<<warps(v.nat), 128, 0, s>>>(v, xyz);
   k_sasa<<<v.nat, 256, 0, s>>>(v, xyz);
   k_solv_nonsc<<<(v.nat + 127) / 128, 128, 0, s>>>(v, eat);
@@ -375,9 +400,11 @@ void solv_energy(const DevSolv& v, const double* xyz, const double* qat, double*
 }
 void solv_gradient(const DevSolv& v, const double* xyz, const double* qat, double* grad,
                    cudaStream_t s) {
-  g_kernel_launches += 3;
+  g_kernel_launches += 2;
   k_solv_pair_grad<<<warps(v.nat), 128, 0, s>>>(v, xyz, qat, grad);
   k_born_grad<<<warps(v.nat), 128, 0, s>>>(v, xyz, grad);
+  if (!v.cds) return;
+  ++g_kernel_launches;
   k_sasa_grad<<<v.nat, 256, 0, s>>>(v, xyz, qat, grad);
 }
 

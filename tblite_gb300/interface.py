@@ -198,12 +198,21 @@ class Calculator(Structure):
     def add(self, interaction: str, *args) -> None:
         """Add an interaction or a post-processing step (reference interface.py:588-637).
 
-        Interactions: ``"alpb-solvation"`` with the solvent ``"water"`` and an optional
-        solution state ``"gsolv"`` (default), ``"bar1mol"`` or ``"reference"``.
+        Interactions: ``"alpb-solvation"`` and ``"gbsa-solvation"`` with the solvent
+        ``"water"`` and an optional solution state ``"gsolv"`` (default), ``"bar1mol"`` or
+        ``"reference"`` (GFN2 parameters); ``"gbe-solvation"`` and ``"gb-solvation"`` with a
+        dielectric constant and the Born kernel ``"still"`` or ``"p16"``.
         Post-processing: ``"bond-orders"`` and ``"molecular-multipoles"`` (computed with every
         single point in the order added; without any, both are computed)."""
+        cont = None
         if interaction == "alpb-solvation":
             cont = library.new_alpb_solvation(self._mol, *args, version=2)
+        elif interaction == "gbsa-solvation":
+            cont = library.new_gbsa_solvation(self._mol, *args, version=2)
+        elif interaction in ("gbe-solvation", "gb-solvation"):
+            cont = library.new_gb_solvation_epsilon(self._mol, *args,
+                                                    alpb=interaction == "gbe-solvation")
+        if cont is not None:
             library.calculator_push_back(self._ctx, self._calc, cont)
             return
         if interaction in self._post_processing:

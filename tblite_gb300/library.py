@@ -74,6 +74,7 @@ _SIGNATURES = {
     "tblite_get_calculator_orbital_map": (None, [c_void_p, c_void_p, _int_p]),
     "tblite_get_singlepoint": (None, [c_void_p, c_void_p, c_void_p, c_void_p]),
     "tblite_new_alpb_solvation_solvent": (c_void_p, [c_void_p, c_void_p, c_char_p, c_int, c_int]),
+    "tblite_new_gb_solvation_epsilon": (c_void_p, [c_void_p, c_void_p, c_double, c_int, c_int]),
     "tblite_calculator_push_back": (None, [c_void_p, c_void_p, POINTER(c_void_p)]),
     "tblite_delete_container": (None, [POINTER(c_void_p)]),
     # extensions (include/tblite_gb300_ext.h)
@@ -689,6 +690,29 @@ def new_alpb_solvation(mol, solvent: str, state: str = "gsolv", version: int = 2
     err = _Error()
     cont = c_void_p(lib.tblite_new_alpb_solvation_solvent(
         err.h, mol, solvent.encode("ascii"), 10 + int(version), SOLUTION_STATES[state]))
+    err.check()
+    return cont
+
+
+def new_gbsa_solvation(mol, solvent: str, state: str = "gsolv", version: int = 2):
+    """GBSA container for a named solvent (model code 20 + version, as the reference's
+    python/tblite/library.py:900-908 passes it)."""
+    return new_alpb_solvation(mol, solvent, state, version=10 + int(version))
+
+
+BORN_KERNELS = {"still": 1, "p16": 2}
+
+
+def new_gb_solvation_epsilon(mol, epsilon: float, born: str, alpb: bool):
+    """Generalized Born container for a dielectric constant: model code 10 (GB-epsilon with
+    the ALPB shape term, "gbe-solvation") or 20 ("gb-solvation"), Born kernel "still" or "p16"
+    (python/tblite/library.py:911-922)."""
+    lib = load()
+    if born not in BORN_KERNELS:
+        raise TBLiteValueError(f"Unknown Born kernel '{born}'")
+    err = _Error()
+    cont = c_void_p(lib.tblite_new_gb_solvation_epsilon(err.h, mol, float(epsilon),
+                                                        10 if alpb else 20, BORN_KERNELS[born]))
     err.check()
     return cont
 

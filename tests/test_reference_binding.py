@@ -123,11 +123,15 @@ def test_gpu_calls_fail_loudly_and_results_need_a_single_point(tblite):
             calc.singlepoint()
 
 
-def test_unavailable_interactions_report_errors(tblite):
+def test_interactions_through_the_reference_package(tblite):
     numbers, positions = _water_dimer()
     calc = tblite.interface.Calculator("GFN2-xTB", numbers, positions)
     with pytest.raises(tblite.exceptions.TBLiteRuntimeError, match="not available"):
-        calc.add("gb-solvation", 78.4, "still")
-    with pytest.raises(tblite.exceptions.TBLiteRuntimeError, match="not available"):
         calc.add("spin-polarization", 1.0)
+    with pytest.raises(tblite.exceptions.TBLiteRuntimeError, match="water only"):
+        calc.add("alpb-solvation", "benzene")
     calc.add("alpb-solvation", "water")  # ALPB(water) is available
+    for interaction, args in (("gbsa-solvation", ("water",)), ("gbe-solvation", (7.0, "p16")),
+                              ("gb-solvation", (78.4, "still"))):
+        other = tblite.interface.Calculator("GFN2-xTB", numbers, positions)
+        other.add(interaction, *args)
