@@ -274,7 +274,7 @@ TBLITE_API_ENTRY void TBLITE_API_CALL tblite_dump_table(tblite_error error, tbli
  * The global constants and element records of an xTB method.  export_* fill a record with a
  * built-in method's parameters; load / dump read and write it as a data table in the
  * reference's TOML layout (levels and CN shifts in eV there); tblite_new_xtb_calculator makes
- * a calculator from it.  IPEA1-xTB is not available (an error). */
+ * a calculator from it (the GFN2-xTB form, or the GFN1-xTB form to which IPEA1-xTB belongs). */
 typedef struct _tblite_param* tblite_param;
 TBLITE_API_ENTRY tblite_param TBLITE_API_CALL tblite_new_param(void);
 TBLITE_API_ENTRY void TBLITE_API_CALL tblite_delete_param(tblite_param* param);
@@ -316,7 +316,7 @@ tblite_new_gfn1_calculator(tblite_context ctx, tblite_structure mol, tblite_xtb_
 TBLITE_API_ENTRY tblite_calculator TBLITE_API_CALL
 tblite_new_xtb_calculator(tblite_context ctx, tblite_structure mol, tblite_param param,
                           tblite_xtb_config* config);
-/* IPEA1-xTB (calculator.h:84-89): not available, reports an error and returns NULL */
+/* IPEA1-xTB (calculator.h:84-89): the GFN1 form with IPEA1-xTB's parameters */
 TBLITE_API_ENTRY tblite_calculator TBLITE_API_CALL
 tblite_new_ipea1_calculator(tblite_context ctx, tblite_structure mol, tblite_xtb_config* config);
 TBLITE_API_ENTRY void TBLITE_API_CALL tblite_delete_calculator(tblite_calculator* calc);

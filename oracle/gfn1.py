@@ -35,8 +35,10 @@ from oracle.gfn2 import (DATA, KT_300K, MAXG, Broyden, Molecule, Result, _basis_
                          post_processing, slater_to_gauss)
 
 
-def load_params1():
-    return json.loads((DATA / "gfn1.json").read_text())
+def load_params1(method="gfn1"):
+    """GFN1-xTB tables, or with method="ipea1" the IPEA1-xTB tables of the same form
+    (xtb/ipea1.f90:47-490, extracted into ipea1.json)."""
+    return json.loads((DATA / f"{method}.json").read_text())
 
 
 def orthogonalize(ai, ci, aj, cj):
@@ -77,8 +79,12 @@ class Calc1:
     include_dispersion: bool = True
 
 
-def new_calc(mol: Molecule, edata=None, **kw):
-    p = load_params1()
+def new_calc(mol: Molecule, edata=None, method="gfn1", **kw):
+    """Calculator of the GFN1 form: GFN1-xTB, or IPEA1-xTB with method="ipea1" (its own tables,
+    the s-p H0 scale 2.25 and element-pair factors from the d-block rule only,
+    xtb/ipea1.f90:752-765, 1037-1041)."""
+    p = load_params1(method)
+    p["ipea1"] = method == "ipea1"
     sto = load_sto()
     nat = len(mol.numbers)
     if edata is None and nat > 1:
@@ -136,12 +142,13 @@ def new_calc(mol: Molecule, edata=None, **kw):
     return calc
 
 
-def pair_param(zi, zj):
-    """get_pair_param, xtb/gfn1.f90:734-772."""
+def pair_param(zi, zj, ipea1=False):
+    """get_pair_param, xtb/gfn1.f90:734-772 (IPEA1-xTB: xtb/ipea1.f90:752-765, the d-block
+    rule only)."""
     pairs = {(1, 1): 0.96, (1, 5): 0.95, (1, 7): 1.04, (1, 28): 0.90, (1, 75): 0.80,
              (1, 78): 0.80, (5, 15): 0.97, (7, 14): 1.01}
     key = (min(zi, zj), max(zi, zj))
-    if key in pairs:
+    if key in pairs and not ipea1:
         return pairs[key]
 
     def row(z):
@@ -176,7 +183,7 @@ def hscale_pairs(calc, at_en):
             vi, vj = calc.sh_valence[i], calc.sh_valence[j]
             if vi and vj:
                 den = (at_en[ai] - at_en[aj]) ** 2
-                km = pair_param(z[aj], z[ai]) * ksh[lj][li] * (1.0 + enscale * den)
+                km = pair_param(z[aj], z[ai], p.get("ipea1", False)) * ksh[lj][li] * (1.0 + enscale * den)
             elif vi:
                 km = 0.5 * (ksh[li][li] + kdiff)
             elif vj:

@@ -151,6 +151,7 @@ struct ModelConstants {
   double rep_kexp = 0.0, rep_klight = 0.0;
   double dmp3 = 0.0, dmp5 = 0.0, mp_kexp = 0.0, mp_shift = 0.0, mp_rmax = 0.0;
   double s6 = 1.0, s8 = 0.0, a1 = 0.0, a2 = 0.0, s9 = 0.0;
+  int pair_mode = 1;  // GFN1 form: 1 GFN1-xTB element-pair factors, 0 the d-block rule only
 };
 
 struct _tblite_calculator {

@@ -83,6 +83,21 @@ struct Arena {
 std::mutex g_batch_mutex;
 Arena g_arena;
 int g_last_fallbacks = 0;
+// two calculators run in one chunk only with the same global model constants
+static bool same_model(const ModelConstants& a, const ModelConstants& b) {
+  if (a.pair_mode != b.pair_mode) return false;
+  const double va[] = {a.wexp, a.enscale, a.kpol, a.gexp, a.rep_kexp, a.rep_klight, a.dmp3,
+                       a.dmp5, a.mp_kexp, a.mp_shift, a.mp_rmax, a.s6, a.s8, a.a1, a.a2, a.s9};
+  const double vb[] = {b.wexp, b.enscale, b.kpol, b.gexp, b.rep_kexp, b.rep_klight, b.dmp3,
+                       b.dmp5, b.mp_kexp, b.mp_shift, b.mp_rmax, b.s6, b.s8, b.a1, b.a2, b.s9};
+  for (size_t k = 0; k < sizeof(va) / sizeof(va[0]); ++k)
+    if (!(va[k] == vb[k])) return false;
+  for (int l = 0; l < 5; ++l)
+    for (int m = 0; m < 5; ++m)
+      if (!(a.ksh[l][m] == b.ksh[l][m])) return false;
+  return true;
+}
+
 int g_batch_streams = 8;  // side streams the size buckets are spread over
 bool g_batch_sp2 = true;  // closed shells of >= g_sp2_min_nao orbitals: density by projection
 // schedule of the batch (set by hand or by tblite_gb300_batch_autotune): smallest orbital count
@@ -120,6 +135,7 @@ struct Plan {
   const _tblite_structure* mol;
   _tblite_result* res;
   int nat, nsh, nao, nd, memory, max_iter, method;
+  int model = 0;  // index of the calculator's global model constants among the call's
   double nalp, nbet;
   bool has_d4, has_d3;
   bool param_grad;  // dE/d(shell parameters) with the single point
@@ -1073,10 +1089,25 @@ extern "C" int tblite_gb300_batch_singlepoint(tblite_context ctx, int nmol,
     }
     plans.push_back(pl);
   }
-  // by method (one chunk runs one Hamiltonian), then largest first: the size buckets follow
-  // the sorted order
+  // one chunk runs one Hamiltonian: the plans are grouped by their global model constants
+  // (GFN2-xTB, GFN1-xTB, IPEA1-xTB or a custom record of either form), then largest first;
+  // the size buckets follow the sorted order
+  {
+    std::vector<std::pair<int, const ModelConstants*>> models;  // (method, constants)
+    for (Plan& pl : plans) {
+      const ModelConstants& m = pl.c->model;
+      int id = -1;
+      for (size_t k = 0; k < models.size() && id < 0; ++k)
+        if (models[k].first == pl.method && same_model(*models[k].second, m)) id = (int)k;
+      if (id < 0) {
+        id = (int)models.size();
+        models.push_back({pl.method, &m});
+      }
+      pl.model = id;
+    }
+  }
   std::stable_sort(plans.begin(), plans.end(), [](const Plan& a, const Plan& b) {
-    if (a.method != b.method) return a.method > b.method;
+    if (a.model != b.model) return a.model < b.model;
     if (a.sp2 != b.sp2) return a.sp2;
     return a.nao > b.nao;
   });
@@ -1093,7 +1124,7 @@ extern "C" int tblite_gb300_batch_singlepoint(tblite_context ctx, int nmol,
     size_t i0 = 0;
     while (i0 < plans.size()) {
       size_t i1 = i0, bytes = 0;
-      while (i1 < plans.size() && plans[i1].method == plans[i0].method &&
+      while (i1 < plans.size() && plans[i1].model == plans[i0].model &&
              (i1 == i0 || bytes + molecule_bytes(plans[i1]) <= budget)) {
         bytes += molecule_bytes(plans[i1]);
         ++i1;

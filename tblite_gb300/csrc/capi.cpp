@@ -220,6 +220,7 @@ static void build_calculator(_tblite_calculator* c, const _tblite_structure* mol
   c->at_sh.assign(1, 0);
   c->nsh = 0;
   c->nao = 0;
+  bool pairs_gfn1 = true, pairs_dblock = true;  // which pair-factor rule the record follows
   for (int i = 0; i < mol->nat; ++i) {
     const int z = mol->num[i];
     if (z < 1 || z > 86) throw std::runtime_error("No support for elements with Z > 86.");
@@ -230,9 +231,13 @@ static void build_calculator(_tblite_calculator* c, const _tblite_structure* mol
                                " needs the GFN1 halogen-bond correction, which the GPU engine "
                                "does not provide");
     if (method == 1)
-      for (int j = 0; j <= i; ++j)
-        need(rec.pair(z, mol->num[j]) == gfn1_pair_factor(z, mol->num[j]),
-             "element-pair scaling factors other than GFN1-xTB's");
+      for (int j = 0; j <= i; ++j) {
+        const double f = rec.pair(z, mol->num[j]);
+        pairs_gfn1 = pairs_gfn1 && f == gfn1_pair_factor(z, mol->num[j]);
+        pairs_dblock = pairs_dblock && f == dblock_pair_factor(z, mol->num[j]);
+        need(pairs_gfn1 || pairs_dblock,
+             "element-pair scaling factors other than GFN1-xTB's or IPEA1-xTB's");
+      }
     const int ns = e->nsh;
     if (ns > 3 || (int)e->levels.size() != ns)
       throw std::runtime_error("element record of " + e->sym + " is inconsistent");
@@ -302,6 +307,7 @@ static void build_calculator(_tblite_calculator* c, const _tblite_structure* mol
     c->at_repz.push_back(e->zeff);
     c->at_gam3.push_back(method == 1 ? e->gam3 : 0.0);
   }
+  c->model.pair_mode = pairs_gfn1 ? 1 : 0;
   if (mol->nat > 1) {
     if (method == 2) build_d4_data(c, mol);
     else build_d3_data(c, mol);
@@ -334,6 +340,7 @@ Gfn2Scalars gfn2_scalars(const _tblite_calculator* c) {
   const ModelConstants& k = c->model;
   Gfn2Scalars p{};
   p.method = c->method;
+  p.pair_mode = c->model.pair_mode;
   p.wexp = k.wexp;
   p.enscale = k.enscale;
   p.gexp = k.gexp;
@@ -2170,10 +2177,23 @@ void tblite_gb300_set_calculator_fault(tblite_context ctx, tblite_calculator cal
 }
 tblite_calculator tblite_new_ipea1_calculator(tblite_context ctx, tblite_structure mol,
                                              tblite_xtb_config* config) {
-  (void)mol;
   (void)config;
-  if (ctx) ctx->push("IPEA1-xTB is not available in the GPU engine");
-  return nullptr;
+  if (!ctx) return nullptr;
+  if (!mol) {
+    ctx->push("Molecular structure data is missing");
+    return nullptr;
+  }
+  auto* c = new _tblite_calculator();
+  try {
+    ParamRecord rec;
+    export_ipea1(rec);  // the GFN1 form with IPEA1-xTB's tables (xtb/ipea1.f90:529-564)
+    build_calculator(c, mol, rec);
+  } catch (const std::exception& e) {
+    ctx->push(e.what());
+    delete c;
+    return nullptr;
+  }
+  return c;
 }
 void tblite_delete_calculator(tblite_calculator* c) {
   if (c && *c) {

@@ -86,6 +86,8 @@ struct Gfn2Scalars {
   int harmonic;    // hardness average of shell pairs: 0 arithmetic (GFN2), 1 harmonic (GFN1)
   int third_atom;  // third order on atomic charges (GFN1) instead of shell charges (GFN2)
   int aes;         // anisotropic electrostatics (GFN2 only)
+  int pair_mode;   // GFN1 form: 1 the GFN1-xTB element-pair factors, 0 the d-block rule only
+                   // (IPEA1-xTB)
   double kdiff;    // GFN1 H0 scale involving polarisation shells
   double cn_exp_k; // GFN1 coordination number: exponential counting steepness
   double wexp, enscale, gexp;

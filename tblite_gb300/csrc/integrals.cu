@@ -63,8 +63,9 @@ __device__ __forceinline__ void tri_index(long long t, int& i, int& j) {
 __device__ __forceinline__ int dblock_row(int z) {
   return (z > 20 && z < 30) ? 1 : (z > 38 && z < 48) ? 2 : (z > 56 && z < 80) ? 3 : 0;
 }
-__device__ __forceinline__ double gfn1_pair(int zi, int zj) {
+__device__ __forceinline__ double gfn1_pair(int zi, int zj, int mode) {
   const int a = zi < zj ? zi : zj, b = zi < zj ? zj : zi;
+  if (mode == 1) {  // mode 0 (IPEA1-xTB): only the d-block rule below
   if (a == 1 && b == 1) return 0.96;
   if (a == 1 && b == 5) return 0.95;
   if (a == 1 && b == 7) return 1.04;
@@ -72,6 +73,7 @@ __device__ __forceinline__ double gfn1_pair(int zi, int zj) {
   if (a == 1 && (b == 75 || b == 78)) return 0.80;
   if (a == 5 && b == 15) return 0.97;
   if (a == 7 && b == 14) return 1.01;
+  }
   const int ti = dblock_row(zi), tj = dblock_row(zj);
   if (ti > 0 && tj > 0) {
     const double kp[3] = {1.1, 1.2, 1.2};
@@ -87,7 +89,8 @@ __device__ __forceinline__ double hscale_of(const DevMol& m, const Gfn2Scalars& 
     const bool vi = m.sh_valence[ish] != 0, vj = m.sh_valence[jsh] != 0;
     if (vi && vj) {
       const double den = (m.at_en[iat] - m.at_en[jat]) * (m.at_en[iat] - m.at_en[jat]);
-      return gfn1_pair(m.at_z[iat], m.at_z[jat]) * p.kshell[lj][li] * (1.0 + p.enscale * den);
+      return gfn1_pair(m.at_z[iat], m.at_z[jat], p.pair_mode) * p.kshell[lj][li] *
+             (1.0 + p.enscale * den);
     }
     if (vi) return 0.5 * (p.kshell[li][li] + p.kdiff);
     if (vj) return 0.5 * (p.kshell[lj][lj] + p.kdiff);

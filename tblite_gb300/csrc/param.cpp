@@ -26,6 +26,7 @@
 #include "api_internal.h"
 #include "element_data.inc"
 #include "params_gfn1.inc"
+#include "params_ipea1.inc"
 #include "params_gfn2.inc"
 
 namespace tb {
@@ -66,6 +67,17 @@ double gfn1_pair_factor(int zi, int zj) {
   if (a == 1 && (b == 75 || b == 78)) return 0.80;
   if (a == 5 && b == 15) return 0.97;
   if (a == 7 && b == 14) return 1.01;
+  const int ti = dblock_row(zi), tj = dblock_row(zj);
+  if (ti > 0 && tj > 0) {
+    const double kp[3] = {1.1, 1.2, 1.2};
+    return 0.5 * (kp[ti - 1] + kp[tj - 1]);
+  }
+  return 1.0;
+}
+
+// IPEA1-xTB pair factors (xtb/ipea1.f90:752-765): the mean of the d-block row factors for two
+// transition metals, 1 otherwise
+double dblock_pair_factor(int zi, int zj) {
   const int ti = dblock_row(zi), tj = dblock_row(zj);
   if (ti > 0 && tj > 0) {
     const double kp[3] = {1.1, 1.2, 1.2};
@@ -269,75 +281,120 @@ void export_gfn2(ParamRecord& r) {
   }
 }
 
-void export_gfn1(ParamRecord& r) {
+// element tables of the two GFN1-form parametrisations, as types for export_xtb1
+#define XTB1_TABLES(P)                                                                      \
+  static constexpr const double& ENSCALE = P##_ENSCALE;                                    \
+  static constexpr const double& KDIFF = P##_KDIFF;                                        \
+  static constexpr const double& S6 = P##_S6;                                              \
+  static constexpr const double& S8 = P##_S8;                                              \
+  static constexpr const double& A1 = P##_A1;                                              \
+  static constexpr const double& A2 = P##_A2;                                              \
+  static constexpr const double& S9 = P##_S9;                                              \
+  static constexpr const double& REP_KEXP = P##_REP_KEXP;                                  \
+  static constexpr const double& GEXP = P##_GEXP;                                          \
+  static constexpr const double& HALOGEN_DAMPING = P##_HALOGEN_DAMPING;                    \
+  static constexpr const double& HALOGEN_RADSCALE = P##_HALOGEN_RADSCALE;                  \
+  static constexpr const double* KSHELL = P##_KSHELL;                                      \
+  static constexpr const double* REP_ZEFF = P##_REP_ZEFF;                                  \
+  static constexpr const double* REP_ALPHA = P##_REP_ALPHA;                                \
+  static constexpr const int* NSHELL = P##_NSHELL;                                         \
+  static constexpr const int* ANG_SHELL = P##_ANG_SHELL;                                   \
+  static constexpr const int* PRINCIPAL_QUANTUM_NUMBER = P##_PRINCIPAL_QUANTUM_NUMBER;     \
+  static constexpr const int* NUMBER_OF_PRIMITIVES = P##_NUMBER_OF_PRIMITIVES;             \
+  static constexpr const double* P_SELFENERGY = P##_P_SELFENERGY;                          \
+  static constexpr const double* SLATER_EXPONENT = P##_SLATER_EXPONENT;                    \
+  static constexpr const double* REFERENCE_OCC = P##_REFERENCE_OCC;                        \
+  static constexpr const double* P_KCN = P##_P_KCN;                                        \
+  static constexpr const double* P_SHPOLY = P##_P_SHPOLY;                                  \
+  static constexpr const double* SHELL_HUBBARD = P##_SHELL_HUBBARD;                        \
+  static constexpr const double* HUBBARD_PARAMETER = P##_HUBBARD_PARAMETER;                \
+  static constexpr const double* P_HUBBARD_DERIVS = P##_P_HUBBARD_DERIVS;                  \
+  static constexpr const double* HALOGEN_BOND = P##_HALOGEN_BOND;
+struct Gfn1Tables {
+  XTB1_TABLES(GFN1)
+};
+struct Ipea1Tables {
+  XTB1_TABLES(IPEA1)
+};
+#undef XTB1_TABLES
+
+template <class T>
+static void export_xtb1(ParamRecord& r, bool ipea1) {
   r = ParamRecord();
   r.version = 1;
-  r.name = "GFN1-xTB";
+  r.name = ipea1 ? "IPEA1-xTB" : "GFN1-xTB";
   r.reference =
-      "S. Grimme, C. Bannwarth, P. Shushkov, J. Chem. Theory Comput., 2017, 13, 1989-2009. "
-      "DOI: 10.1021/acs.jctc.7b00118";
+      ipea1 ? "V. Asgeirsson, C. Bauer and S. Grimme, Chem. Sci., 2017, 8, 4879. DOI: "
+              "10.1039/c7sc00601b"
+            : "S. Grimme, C. Bannwarth, P. Shushkov, J. Chem. Theory Comput., 2017, 13, "
+              "1989-2009. DOI: 10.1021/acs.jctc.7b00118";
   r.cn = "exp";
-  r.enscale = GFN1_ENSCALE;
+  r.enscale = T::ENSCALE;
   r.wexp = 0.0;
   r.lmax = 2;
   for (int l = 0; l < 5; ++l)
-    for (int k = 0; k < 5; ++k) r.ksh[l][k] = (l < 3 && k < 3) ? GFN1_KSHELL[l * 3 + k] : 0.0;
-  r.kpol = GFN1_KDIFF;
+    for (int k = 0; k < 5; ++k) r.ksh[l][k] = (l < 3 && k < 3) ? T::KSHELL[l * 3 + k] : 0.0;
+  r.kpol = T::KDIFF;
   for (int zi = 1; zi <= MAX_ELEM; ++zi)
     for (int zj = 1; zj <= zi; ++zj) {
-      const double k = gfn1_pair_factor(zi, zj);
+      const double k = ipea1 ? dblock_pair_factor(zi, zj) : gfn1_pair_factor(zi, zj);
       if (k != 1.0) r.kpair[{zi, zj}] = k;
     }
   r.has_dispersion = true;
   r.d3 = true;
   r.sc = false;
   r.smooth = false;
-  r.s6 = GFN1_S6;
-  r.s8 = GFN1_S8;
-  r.a1 = GFN1_A1;
-  r.a2 = GFN1_A2;
-  r.s9 = GFN1_S9;
+  r.s6 = T::S6;
+  r.s8 = T::S8;
+  r.a1 = T::A1;
+  r.a2 = T::A2;
+  r.s9 = T::S9;
   r.has_repulsion = true;
-  r.kexp = GFN1_REP_KEXP;
-  r.klight = GFN1_REP_KEXP;
+  r.kexp = T::REP_KEXP;
+  r.klight = T::REP_KEXP;
   r.has_charge = true;
-  r.gexp = GFN1_GEXP;
+  r.gexp = T::GEXP;
   r.average = "harmonic";
   r.has_thirdorder = true;
   r.third_shell = false;
   r.third_lmax = 0;
   r.has_halogen = true;
-  r.hal_damping = GFN1_HALOGEN_DAMPING;
-  r.hal_rscale = GFN1_HALOGEN_RADSCALE;
+  r.hal_damping = T::HALOGEN_DAMPING;
+  r.hal_rscale = T::HALOGEN_RADSCALE;
   for (int z = 1; z <= MAX_ELEM; ++z) {
     ElementRecord e;
     e.sym = element_symbol(z);
     e.num = z;
-    e.zeff = GFN1_REP_ZEFF[z - 1];
-    e.arep = GFN1_REP_ALPHA[z - 1];
-    e.nsh = GFN1_NSHELL[z - 1];
+    e.zeff = T::REP_ZEFF[z - 1];
+    e.arep = T::REP_ALPHA[z - 1];
+    e.nsh = T::NSHELL[z - 1];
     bool seen[5] = {false, false, false, false, false};
     for (int s = 0; s < e.nsh; ++s) {
-      const int l = GFN1_ANG_SHELL[(z - 1) * 3 + s];
+      const int l = T::ANG_SHELL[(z - 1) * 3 + s];
       const bool valence = !seen[l];
       seen[l] = true;
       e.lsh.push_back(l);
-      e.pqn.push_back(GFN1_PRINCIPAL_QUANTUM_NUMBER[(z - 1) * 3 + s]);
-      e.ngauss.push_back(GFN1_NUMBER_OF_PRIMITIVES[(z - 1) * 3 + s]);
-      e.levels.push_back(GFN1_P_SELFENERGY[(z - 1) * 3 + s]);
-      e.slater.push_back(GFN1_SLATER_EXPONENT[(z - 1) * 3 + s]);
-      e.refocc.push_back(valence ? GFN1_REFERENCE_OCC[(z - 1) * 3 + l] : 0.0);
-      e.kcn.push_back(GFN1_P_KCN[(z - 1) * 3 + s]);
-      e.shpoly.push_back(GFN1_P_SHPOLY[(z - 1) * 3 + l]);
-      e.lgam.push_back(GFN1_SHELL_HUBBARD[(z - 1) * 3 + l]);
+      e.pqn.push_back(T::PRINCIPAL_QUANTUM_NUMBER[(z - 1) * 3 + s]);
+      e.ngauss.push_back(T::NUMBER_OF_PRIMITIVES[(z - 1) * 3 + s]);
+      e.levels.push_back(T::P_SELFENERGY[(z - 1) * 3 + s]);
+      e.slater.push_back(T::SLATER_EXPONENT[(z - 1) * 3 + s]);
+      // the reference's IPEA1 export keeps the occupation of polarisation shells too
+      // (xtb/ipea1.f90:1015); calculators take occupations of valence shells only
+      e.refocc.push_back(valence || ipea1 ? T::REFERENCE_OCC[(z - 1) * 3 + l] : 0.0);
+      e.kcn.push_back(T::P_KCN[(z - 1) * 3 + s]);
+      e.shpoly.push_back(T::P_SHPOLY[(z - 1) * 3 + l]);
+      e.lgam.push_back(T::SHELL_HUBBARD[(z - 1) * 3 + l]);
     }
-    e.gam = GFN1_HUBBARD_PARAMETER[z - 1];
-    e.gam3 = GFN1_P_HUBBARD_DERIVS[z - 1];
-    e.xbond = GFN1_HALOGEN_BOND[z - 1];
+    e.gam = T::HUBBARD_PARAMETER[z - 1];
+    e.gam3 = T::P_HUBBARD_DERIVS[z - 1];
+    e.xbond = T::HALOGEN_BOND[z - 1];
     e.en = EXT_EN[z - 1];
     r.element.push_back(std::move(e));
   }
 }
+
+void export_gfn1(ParamRecord& r) { export_xtb1<Gfn1Tables>(r, false); }
+void export_ipea1(ParamRecord& r) { export_xtb1<Ipea1Tables>(r, true); }
 
 // ---- table <-> record ---------------------------------------------------------------------
 void param_load(ParamRecord& r, const TTable& t) {
@@ -633,8 +690,9 @@ void tblite_export_gfn1_param(tblite_error error, tblite_param param) {
 
 void tblite_export_ipea1_param(tblite_error error, tblite_param param) {
   if (!error) return;
-  (void)param;
-  set_error(error, "IPEA1-xTB parameters are not available in the GPU engine");
+  if (!param) return set_error(error, "Parametrization record is missing");
+  tb::export_ipea1(param->rec);
+  param->set = true;
 }
 
 // post-processing named in a parametrisation record: none is kept by the records here (the

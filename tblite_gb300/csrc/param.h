@@ -70,12 +70,15 @@ struct ParamRecord {
 
 void export_gfn2(ParamRecord& r);
 void export_gfn1(ParamRecord& r);
+void export_ipea1(ParamRecord& r);
 // reference layout: meta, hamiltonian, dispersion, repulsion, charge, thirdorder, multipole,
 // halogen, element.<symbol>; throws std::runtime_error with the reference's messages
 void param_load(ParamRecord& r, const TTable& t);
 void param_dump(const ParamRecord& r, TTable& t);
 // element-pair factor of the GFN1-xTB valence Hamiltonian (the GPU kernel applies the same)
 double gfn1_pair_factor(int zi, int zj);
+// element-pair factor of IPEA1-xTB (the d-block rule of the GFN1 form only)
+double dblock_pair_factor(int zi, int zj);
 // element symbol of Z (1..118) and the inverse (0 for an unknown symbol)
 std::string element_symbol(int z);
 int element_number(const std::string& sym);

@@ -215,9 +215,14 @@ def write_inc(params, sto, path: Path):
     path.write_text("".join(lines))
 
 
-def extract_gfn1(root: Path):
-    """GFN1-xTB tables (reference src/tblite/xtb/gfn1.f90:47-496, kshell at :1056-1060)."""
-    d = _declarations((root / "src/tblite/xtb/gfn1.f90").read_text())
+def extract_gfn1(root: Path, method: str = "gfn1"):
+    """GFN1-xTB tables (reference src/tblite/xtb/gfn1.f90:47-496, kshell at :1056-1060); with
+    method="ipea1" the IPEA1-xTB tables of the same form (src/tblite/xtb/ipea1.f90:47-490,
+    kshell at :1037-1041; its hardnesses are named chemical_hardness / shell_hardness)."""
+    d = _declarations((root / f"src/tblite/xtb/{method}.f90").read_text())
+    if method == "ipea1":
+        d["hubbard_parameter"] = d["chemical_hardness"]
+        d["shell_hubbard"] = d["shell_hardness"]
     scalars = ["evtoau", "s6", "s8", "a1", "a2", "s9", "rep_kexp", "rep_rexp", "gexp",
                "enscale", "kdiff", "halogen_radscale", "halogen_damping"]
     env = {}
@@ -243,34 +248,36 @@ def extract_gfn1(root: Path):
     ksh = np.zeros((3, 3))
     for k in range(3):
         for ll in range(3):
-            ksh[k, ll] = 2.08 if (k, ll) in ((0, 1), (1, 0)) else (kdiag[ll] + kdiag[k]) / 2
+            sp = 2.25 if method == "ipea1" else 2.08
+            ksh[k, ll] = sp if (k, ll) in ((0, 1), (1, 0)) else (kdiag[ll] + kdiag[k]) / 2
     out["kshell"] = ksh.tolist()
     return out
 
 
-def write_inc_gfn1(params, path: Path):
+def write_inc_gfn1(params, path: Path, prefix: str = "GFN1"):
     def arr1(name, ctype, vals):
         body = ", ".join(repr(float(v)) if ctype == "double" else str(int(v)) for v in vals)
         return f"static const {ctype} {name}[{len(vals)}] = {{{body}}};\n"
 
     flat = lambda x: np.asarray(x).ravel().tolist()  # noqa: E731
+    src = "gfn1.f90:47-496" if prefix == "GFN1" else "ipea1.f90:47-490"
     lines = ["// Generated by tblite_gb300/data/extract_params.py -- do not edit.\n",
-             "// GFN1-xTB element tables (reference src/tblite/xtb/gfn1.f90:47-496).\n",
+             f"// {prefix} element tables (reference src/tblite/xtb/{src}).\n",
              "#pragma once\n"]
     for k, v in params["scalars"].items():
-        lines.append(f"static const double GFN1_{k.upper()} = {v!r};\n")
+        lines.append(f"static const double {prefix}_{k.upper()} = {v!r};\n")
     for name in ["rep_alpha", "rep_zeff", "hubbard_parameter", "p_hubbard_derivs",
                  "halogen_bond"]:
-        lines.append(arr1("GFN1_" + name.upper(), "double", flat(params[name])))
+        lines.append(arr1(prefix + "_" + name.upper(), "double", flat(params[name])))
     lines.append("// [Z-1][slot]: slot = shell index (selfenergy, kcn, slater, ang, pqn, ngauss)\n")
     lines.append("// or angular momentum (shell_hubbard, shpoly, reference_occ)\n")
     for name in ["shell_hubbard", "p_shpoly", "reference_occ", "slater_exponent",
                  "p_selfenergy", "p_kcn"]:
-        lines.append(arr1("GFN1_" + name.upper(), "double", flat(params[name])))
+        lines.append(arr1(prefix + "_" + name.upper(), "double", flat(params[name])))
     for name in ["ang_shell", "principal_quantum_number", "number_of_primitives"]:
-        lines.append(arr1("GFN1_" + name.upper(), "int", flat(params[name])))
-    lines.append(arr1("GFN1_NSHELL", "int", flat(params["nshell"])))
-    lines.append(arr1("GFN1_KSHELL", "double", flat(params["kshell"])))
+        lines.append(arr1(prefix + "_" + name.upper(), "int", flat(params[name])))
+    lines.append(arr1(prefix + "_NSHELL", "int", flat(params["nshell"])))
+    lines.append(arr1(prefix + "_KSHELL", "double", flat(params["kshell"])))
     path.write_text("".join(lines))
 
 
@@ -285,7 +292,11 @@ def main():
     g1 = extract_gfn1(root)
     (HERE / "gfn1.json").write_text(json.dumps(g1, indent=0))
     write_inc_gfn1(g1, HERE.parent / "csrc" / "params_gfn1.inc")
-    print("wrote gfn2.json, sto_ng.json, params_gfn2.inc, gfn1.json, params_gfn1.inc")
+    i1 = extract_gfn1(root, "ipea1")
+    (HERE / "ipea1.json").write_text(json.dumps(i1, indent=0))
+    write_inc_gfn1(i1, HERE.parent / "csrc" / "params_ipea1.inc", "IPEA1")
+    print("wrote gfn2.json, sto_ng.json, params_gfn2.inc, gfn1.json, params_gfn1.inc, "
+          "ipea1.json, params_ipea1.inc")
 
 
 if __name__ == "__main__":

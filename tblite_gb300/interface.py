@@ -118,6 +118,7 @@ class Calculator(Structure):
     _loader = {
         "GFN2-xTB": library.new_gfn2_calculator,
         "GFN1-xTB": library.new_gfn1_calculator,
+        "IPEA1-xTB": library.new_ipea1_calculator,
     }
 
     def __init__(self, method: str, numbers, positions, charge: Optional[float] = None,

@@ -558,9 +558,10 @@ def table_to_dict(table) -> dict:
 
 
 def export_param(method: str) -> dict:
-    """The parameters of a built-in method ("GFN2-xTB" or "GFN1-xTB") as a nested mapping in
-    the reference's TOML layout (tblite_export_*_param, tblite_dump_param)."""
-    fn = {"GFN2-xTB": "tblite_export_gfn2_param", "GFN1-xTB": "tblite_export_gfn1_param"}
+    """The parameters of a built-in method ("GFN2-xTB", "GFN1-xTB" or "IPEA1-xTB") as a nested
+    mapping in the reference's TOML layout (tblite_export_*_param, tblite_dump_param)."""
+    fn = {"GFN2-xTB": "tblite_export_gfn2_param", "GFN1-xTB": "tblite_export_gfn1_param",
+          "IPEA1-xTB": "tblite_export_ipea1_param"}
     if method not in fn:
         raise TBLiteValueError(f"No parameters for method '{method}'")
     lib = load()
@@ -588,6 +589,13 @@ def param_from_dict(data) -> Param:
 def new_gfn1_calculator(ctx, mol):
     lib = load()
     calc = c_void_p(lib.tblite_new_gfn1_calculator(ctx, mol, None))
+    context_check(ctx)
+    return calc
+
+
+def new_ipea1_calculator(ctx, mol):
+    lib = load()
+    calc = c_void_p(lib.tblite_new_ipea1_calculator(ctx, mol, None))
     context_check(ctx)
     return calc
 

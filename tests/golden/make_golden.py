@@ -1,12 +1,12 @@
 """Extract golden vectors from the reference's own unit tests.
 
-Reads ``test/unit/test_gfn2_xtb.f90`` and ``test/unit/test_gfn1_xtb.f90`` of
-the reference repository (as text; nothing is compiled or run) and writes
-``atoms_gfn2.json`` / ``atoms_gfn1.json`` next to this file: total energies of isolated atoms Z = 1..86 for the neutral,
-cation and anion cases, with the unpaired-electron counts the reference
-uses, the accuracy (0.01) and the tolerance (10*sqrt(eps)) of that test
-(reference ``test/unit/test_gfn2_xtb.f90:34-36,61-272``,
-``test/unit/test_gfn1_xtb.f90:135-349``).
+Reads ``test/unit/test_gfn2_xtb.f90``, ``test/unit/test_gfn1_xtb.f90`` and
+``test/unit/test_ipea1_xtb.f90`` of the reference repository (as text; nothing is compiled or
+run) and writes ``atoms_gfn2.json`` / ``atoms_gfn1.json`` / ``atoms_ipea1.json`` next to this
+file: total energies of isolated atoms Z = 1..86 for the neutral, cation and anion cases, with
+the unpaired-electron counts the reference uses, the accuracy (0.01) and the tolerance of that
+test (reference ``test/unit/test_gfn2_xtb.f90:34-36,61-272``,
+``test/unit/test_gfn1_xtb.f90:135-349``, ``test/unit/test_ipea1_xtb.f90:33-36,133-347``).
 
 Isolated atoms need no coordination-number or dispersion data, so these
 energies pin the basis, the on-site integrals, the self energies, the
@@ -34,7 +34,8 @@ def main():
         raise SystemExit(f"usage: python {Path(__file__).name} <tblite source tree>")
     root = Path(sys.argv[1])
     for method, src in (("gfn2", "test/unit/test_gfn2_xtb.f90:61-272"),
-                        ("gfn1", "test/unit/test_gfn1_xtb.f90:135-349")):
+                        ("gfn1", "test/unit/test_gfn1_xtb.f90:135-349"),
+                        ("ipea1", "test/unit/test_ipea1_xtb.f90:133-347")):
         extract(root, method, src)
 
 
@@ -42,7 +43,7 @@ def extract(root: Path, method: str, src: str):
     text = (root / f"test/unit/test_{method}_xtb.f90").read_text()
     out = {"source": "reference " + src, "accuracy": 0.01,
            "kt": 300.0 * 3.166808578545117e-06,
-           # thresholds of the two reference tests: 10 sqrt(eps) (gfn2), sqrt(eps) (gfn1)
+           # thresholds of the reference tests: 10 sqrt(eps) (gfn2), sqrt(eps) (gfn1, ipea1)
            "thr": (10.0 if method == "gfn2" else 1.0) * (2.220446049250313e-16) ** 0.5,
            "cases": {}}
     for key, sub, charge in (("neutral", "test_e_pse(", 0), ("cation", "test_e_pse_cation(", 1),

@@ -110,11 +110,15 @@ def test_refusals():
     bad["element"] = {"O": {k: v for k, v in d["element"]["O"].items() if k != "levels"}}
     with pytest.raises(TBLiteRuntimeError, match="No atomic levels specified for O"):
         library.param_from_dict(bad)
-    err = library._Error()
-    p = library.Param()
-    library.load().tblite_export_ipea1_param(err.h, p.h)
-    with pytest.raises(TBLiteRuntimeError, match="IPEA1"):
-        err.check()
+    # a GFN1-form record whose element-pair factors follow neither GFN1-xTB nor IPEA1-xTB
+    from tblite_gb300 import workloads
+    from tblite_gb300.interface import Calculator
+
+    g1 = library.export_param("GFN1-xTB")
+    g1["hamiltonian"]["xtb"]["kpair"]["H-H"] = 0.5
+    z, x = workloads.water_cluster((2, 1, 1), seed=11)
+    with pytest.raises(TBLiteRuntimeError, match="element-pair scaling factors"):
+        Calculator(g1, z, x)
 
 
 def test_xtb_calculator_basis_matches_builtin():
@@ -122,7 +126,7 @@ def test_xtb_calculator_basis_matches_builtin():
     from tblite_gb300.interface import Calculator
 
     z, x = workloads.water_cluster((2, 1, 1), seed=11)
-    for method in ("GFN2-xTB", "GFN1-xTB"):
+    for method in ("GFN2-xTB", "GFN1-xTB", "IPEA1-xTB"):
         a = Calculator(method, z, x)
         b = Calculator(library.export_param(method), z, x)
         for key in ("shell-map", "angular-momenta", "orbital-map"):
