@@ -408,10 +408,11 @@ TBLITE_API_ENTRY tblite_container TBLITE_API_CALL
 tblite_new_alpb_solvation_solvent(tblite_error error, tblite_structure mol, char* solvent,
                                   enum tblite_solvation_param version,
                                   enum tblite_ref_solvation_state refstate);
-/* Interactions of the reference that the GPU engine does not provide; each reports an error
- * (the electric field, whose reference signature has no error handle, returns NULL):
- * container.h:36-45 (electric field, spin polarisation), solvation.h:54-95 (GB with a
- * dielectric constant, ddX). */
+/* Further interactions (container.h:36-45, solvation.h:54-95): the homogeneous electric
+ * field (three components, atomic units; NULL for a NULL argument; pushed into a GFN2-form
+ * calculator), generalized Born with a dielectric constant (version 10 GB-epsilon with the ALPB
+ * shape term or 20, Born kernel Still or P16); spin polarisation and ddX are not provided and
+ * report an error. */
 enum tblite_born_kernel {
   tblite_born_still = 1,
   tblite_born_p16 = 2,

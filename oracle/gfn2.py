@@ -406,8 +406,9 @@ def setup(calc: Calc):
 MPSCALE = np.array([1.0, 2.0, 1.0, 2.0, 2.0, 1.0])
 
 
-def potentials(calc, st, qsh, qat, dpat, qpat, disp=None, solv=None):
-    """vsh, vat, vdp, vqp; reference coulomb get_potential routines."""
+def potentials(calc, st, qsh, qat, dpat, qpat, disp=None, solv=None, efield=None):
+    """vsh, vat, vdp, vqp; reference coulomb get_potential routines (and the homogeneous
+    electric field of external/field.f90:77-86: vat -= E.R, vdp -= E)."""
     vsh = st["gamma"] @ qsh + qsh**2 * st["gam3"]
     vat = np.einsum("ijk,jk->i", st["asd"], dpat) + np.einsum("ijq,jq->i", st["asq"], qpat)
     vdp = np.einsum("ijk,i->jk", st["asd"], qat) + np.einsum("ijac,ic->ja", st["add"], dpat)
@@ -417,6 +418,9 @@ def potentials(calc, st, qsh, qat, dpat, qpat, disp=None, solv=None):
         vat = vat + disp.potential(qat)
     if solv is not None:
         vat = vat + solv.potential(qat)
+    if efield is not None:
+        vat = vat - st["xyz"] @ efield
+        vdp = vdp - efield[None, :]
     return vsh, vat, vdp, vqp
 
 
@@ -446,7 +450,8 @@ def fock(calc, st, vsh, vat, vdp, vqp):
     return F, vao, ao2at, ao2sh
 
 
-def singlepoint(calc: Calc, grad=True, verbose=False, dispersion=None, solvation=None):
+def singlepoint(calc: Calc, grad=True, verbose=False, dispersion=None, solvation=None,
+                efield=None):
     mol = calc.mol
     nat = len(mol.numbers)
     st = setup(calc)
@@ -492,6 +497,7 @@ def singlepoint(calc: Calc, grad=True, verbose=False, dispersion=None, solvation
         disp = D4(calc, st)
         edisp = disp.energy_nonsc(gradient, sigma)
     energies += edisp
+    field = None if efield is None else np.asarray(efield, dtype=float).reshape(3)
     # implicit solvation (interactions container: ALPB + CDS + shift), geometry part
     solv = solvation
     esolv = np.zeros(nat)
@@ -521,7 +527,7 @@ def singlepoint(calc: Calc, grad=True, verbose=False, dispersion=None, solvation
             qat = np.zeros(nat)
             np.add.at(qat, calc.sh_atom, qsh)
         iscf += 1
-        vsh, vat, vdp, vqp = potentials(calc, st, qsh, qat, dpat, qpat, disp, solv)
+        vsh, vat, vdp, vqp = potentials(calc, st, qsh, qat, dpat, qpat, disp, solv, field)
         F, vao, ao2at, ao2sh = fock(calc, st, vsh, vat, vdp, vqp)
         mixer.set(np.concatenate([qsh, dpat.ravel(), qpat.ravel()]))
         emo, C = scipy.linalg.eigh(F, st["S"], type=1, driver="gvd", lower=False)
@@ -552,6 +558,8 @@ def singlepoint(calc: Calc, grad=True, verbose=False, dispersion=None, solvation
             eelec += disp.energy_sc(qat)
         if solv is not None:
             eelec += solv.energies(qat)
+        if field is not None:  # external/field.f90:64-75, with the output moments
+            eelec -= (xyz @ field) * qat + dpat @ field
         econverged = abs(float(np.sum(eelec)) - elast) < econv
         pconverged = mixer.error() < pconv
         converged = econverged and pconverged
@@ -567,6 +575,10 @@ def singlepoint(calc: Calc, grad=True, verbose=False, dispersion=None, solvation
                                     qpat, vao, vdp, vqp, disp)
         if solv is not None:
             gradient += solv.gradient(qat)
+        if field is not None:  # external/field.f90:100-113
+            gradient -= field[None, :]
+            stmp = np.outer(field, xyz.sum(0))
+            sigma -= 0.5 * (stmp + stmp.T)
     return Result(energy=energy, energies=energies, gradient=gradient, sigma=sigma, qsh=qsh,
                   qat=qat, dpat=dpat, qpat=qpat, density=P, emo=emo, focc=focc, iterations=iscf,
                   converged=converged, parts=parts)

@@ -141,6 +141,8 @@ struct SolvModel {
 
 struct _tblite_container {
   std::unique_ptr<SolvModel> solv;
+  bool field = false;  // a homogeneous electric field (tblite_new_electric_field)
+  double efield[3] = {0.0, 0.0, 0.0};
 };
 
 // global constants of the calculator's Hamiltonian, from its parametrisation record
@@ -210,6 +212,9 @@ struct _tblite_calculator {
   }
   // implicit solvation container moved in by tblite_calculator_push_back
   std::unique_ptr<SolvModel> solv;
+  // homogeneous electric field (atomic units) moved in by tblite_calculator_push_back
+  bool has_field = false;
+  double efield[3] = {0.0, 0.0, 0.0};
   std::unique_ptr<Workspace> ws;
 };
 

@@ -1075,7 +1075,7 @@ extern "C" int tblite_gb300_batch_singlepoint(tblite_context ctx, int nmol,
       continue;
     }
     const bool anneal = c->anneal && c->anneal_kt > c->etemp;
-    // implicit solvation runs on the one-molecule path
+    // implicit solvation and an electric field run on the one-molecule path
     pl.param_grad = c->param_grad != 0;
     c->default_post_processing();  // as a plain single point does
     pl.wbo_ch = c->wants("bond-orders") ? (pl.nalp != pl.nbet ? 2 : 1) : 0;
@@ -1083,7 +1083,7 @@ extern "C" int tblite_gb300_batch_singlepoint(tblite_context ctx, int nmol,
     // the projection needs a closed shell with a whole number of electron pairs
     pl.sp2 = g_batch_sp2 && pl.nao >= g_sp2_min_nao && pl.nalp == pl.nbet &&
              pl.nalp == std::floor(pl.nalp) && pl.nalp >= 1.0;
-    if (pl.nao > tri_max || anneal || pl.max_iter < 1 || c->solv) {
+    if (pl.nao > tri_max || anneal || pl.max_iter < 1 || c->solv || c->has_field) {
       plain.push_back(i);
       continue;
     }

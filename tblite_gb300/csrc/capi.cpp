@@ -979,6 +979,7 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
                              w.vdp.p, w.vqp.p, s);
     if (c->has_d4) d4_potential(m, d4, d4w, w.qat.p, w.vat.p, s);
     if (c->solv) solv_potential(dsolv, w.xyz.p, w.qat.p, w.vat.p, s);
+    if (c->has_field) launch_field_potential(nat, w.xyz.p, c->efield, w.vat.p, w.vdp.p, s);
     launch_vao(m, w.vsh.p, w.vat.p, w.vao.p, s);
     g_prof.end(s);
     g_prof.begin(PH_FOCK, s);
@@ -1027,6 +1028,8 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
                           s);
     if (c->has_d4) d4_energy(m, d4, d4w, w.qat_o.p, w.eelec.p, s);
     if (c->solv) solv_energy(dsolv, w.xyz.p, w.qat_o.p, w.eelec.p, s);
+    if (c->has_field)
+      launch_field_energy(nat, w.xyz.p, c->efield, w.qat_o.p, w.dpat_o.p, w.eelec.p, s);
     g_prof.end(s);
     w.eelec.download(h_eelec, nat, s);
     w.scal.download(h_scal, 2, s);
@@ -1186,6 +1189,16 @@ static void singlepoint(_tblite_context* ctx, const _tblite_structure* mol,
     double acc = h_sigma[k];
     for (int i = 0; i < nat; ++i) acc += h_sig_at[9 * i + k];
     res->sigma[k] = acc;
+  }
+  if (c->has_field) {  // external/field.f90 get_gradient: gradient -= E, sigma -= sym(E R^T)
+    double st[3][3] = {};
+    for (int i = 0; i < nat; ++i)
+      for (int a = 0; a < 3; ++a) {
+        res->gradient[3 * i + a] -= c->efield[a];
+        for (int b = 0; b < 3; ++b) st[a][b] += c->efield[a] * mol->xyz[3 * i + b];
+      }
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) res->sigma[3 * a + b] -= 0.5 * (st[a][b] + st[b][a]);
   }
   res->has_wfn = true;
   res->n0sh.assign(c->sh_refocc.begin(), c->sh_refocc.begin() + nsh);
@@ -1993,6 +2006,19 @@ void tblite_calculator_push_back(tblite_context ctx, tblite_calculator calc,
     }
     calc->solv = std::move((*cont)->solv);
   }
+  if ((*cont)->field) {
+    if (calc->method != 2) {
+      ctx->push("An electric field needs the atomic dipole moments of the GFN2-xTB form in the "
+                "GPU engine");
+      return;
+    }
+    if (calc->has_field) {
+      ctx->push("Calculator already holds an electric field");
+      return;
+    }
+    calc->has_field = true;
+    for (int k = 0; k < 3; ++k) calc->efield[k] = (*cont)->efield[k];
+  }
   delete *cont;  // the container moves into the calculator (api/container.f90:53-94)
   *cont = nullptr;
 }
@@ -2006,9 +2032,14 @@ void tblite_delete_container(tblite_container* cont) {
 
 // interactions of the reference that the GPU engine does not provide: each reports an error and
 // returns NULL (include/tblite/container.h:31-45, solvation.h:54-95)
+// homogeneous electric field (external/field.f90): vat -= E.R_A, vdp -= E; the container
+// moves into a calculator of the GFN2 form (its dipole moments enter the SCF)
 tblite_container tblite_new_electric_field(double* efield) {
-  (void)efield;
-  return nullptr;  // the reference's signature has no error handle: NULL is the report
+  if (!efield) return nullptr;  // the reference's signature has no error handle
+  auto* cont = new _tblite_container();
+  cont->field = true;
+  for (int k = 0; k < 3; ++k) cont->efield[k] = efield[k];
+  return cont;
 }
 tblite_container tblite_new_spin_polarization(tblite_context ctx, tblite_structure mol,
                                               tblite_calculator calc, double wscale) {

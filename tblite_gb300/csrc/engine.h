@@ -192,6 +192,12 @@ void launch_h0_gradient(const DevMol& m, const Gfn2Scalars& p, const double* sel
 void launch_repulsion(const DevMol& m, const Gfn2Scalars& p, double* erep, double* grad,
                       double* sigma, cudaStream_t s);
 // electrostatics: potentials from (qsh, qat, dpat, qpat)
+// homogeneous electric field E (host array of 3): vat -= E.R_A, vdp -= E; energies
+// eat -= E.R_A q_A + E.mu_A (external/field.f90)
+void launch_field_potential(int nat, const double* xyz, const double* efield, double* vat,
+                            double* vdp, cudaStream_t s);
+void launch_field_energy(int nat, const double* xyz, const double* efield, const double* qat,
+                         const double* dpat, double* eat, cudaStream_t s);
 void launch_coulomb_potential(const DevMol& m, const Gfn2Scalars& p, const double* mrad,
                               const double* qsh, const double* qat, const double* dpat,
                               const double* qpat, double* vsh, double* vat, double* vdp,

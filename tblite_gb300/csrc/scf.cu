@@ -181,6 +181,41 @@ void launch_setup_levels(const DevMol& m, const Gfn2Scalars& p, const double* cn
 }
 
 // ------------------------------------------------------------------------------------
+// homogeneous external electric field (external/field.f90:64-90): atomic and dipole
+// potentials of the constant field, and its energy with the output moments
+// ------------------------------------------------------------------------------------
+struct Field3 {
+  double e[3];
+};
+__global__ void k_field_potential(int nat, const double* __restrict__ xyz, Field3 f, double* vat,
+                                  double* vdp) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nat) return;
+  vat[i] -= f.e[0] * xyz[3 * i] + f.e[1] * xyz[3 * i + 1] + f.e[2] * xyz[3 * i + 2];
+  for (int k = 0; k < 3; ++k) vdp[3 * i + k] -= f.e[k];
+}
+__global__ void k_field_energy(int nat, const double* __restrict__ xyz, Field3 f,
+                               const double* __restrict__ qat, const double* __restrict__ dpat,
+                               double* eat) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nat) return;
+  const double v = f.e[0] * xyz[3 * i] + f.e[1] * xyz[3 * i + 1] + f.e[2] * xyz[3 * i + 2];
+  eat[i] -= v * qat[i] + f.e[0] * dpat[3 * i] + f.e[1] * dpat[3 * i + 1] + f.e[2] * dpat[3 * i + 2];
+}
+void launch_field_potential(int nat, const double* xyz, const double* efield, double* vat,
+                            double* vdp, cudaStream_t s) {
+  const Field3 f{{efield[0], efield[1], efield[2]}};
+  ++g_kernel_launches;
+  k_field_potential<<<(nat + 127) / 128, 128, 0, s>>>(nat, xyz, f, vat, vdp);
+}
+void launch_field_energy(int nat, const double* xyz, const double* efield, const double* qat,
+                         const double* dpat, double* eat, cudaStream_t s) {
+  const Field3 f{{efield[0], efield[1], efield[2]}};
+  ++g_kernel_launches;
+  k_field_energy<<<(nat + 127) / 128, 128, 0, s>>>(nat, xyz, f, qat, dpat, eat);
+}
+
+// ------------------------------------------------------------------------------------
 // electrostatics: one warp per atom i, partners j strided over lanes
 // MODE 0: potentials (vsh, vat, vdp, vqp);  MODE 1: per-atom energy (added to eat)
 // ------------------------------------------------------------------------------------

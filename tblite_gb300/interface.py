@@ -202,7 +202,8 @@ class Calculator(Structure):
         Interactions: ``"alpb-solvation"`` and ``"gbsa-solvation"`` with the solvent
         ``"water"`` and an optional solution state ``"gsolv"`` (default), ``"bar1mol"`` or
         ``"reference"`` (GFN2 parameters); ``"gbe-solvation"`` and ``"gb-solvation"`` with a
-        dielectric constant and the Born kernel ``"still"`` or ``"p16"``.
+        dielectric constant and the Born kernel ``"still"`` or ``"p16"``; ``"electric-field"``
+        with the three components of a homogeneous field (atomic units, GFN2-xTB form).
         Post-processing: ``"bond-orders"`` and ``"molecular-multipoles"`` (computed with every
         single point in the order added; without any, both are computed)."""
         cont = None
@@ -210,6 +211,8 @@ class Calculator(Structure):
             cont = library.new_alpb_solvation(self._mol, *args, version=2)
         elif interaction == "gbsa-solvation":
             cont = library.new_gbsa_solvation(self._mol, *args, version=2)
+        elif interaction == "electric-field":
+            cont = library.new_electric_field(*args)
         elif interaction in ("gbe-solvation", "gb-solvation"):
             cont = library.new_gb_solvation_epsilon(self._mol, *args,
                                                     alpb=interaction == "gbe-solvation")

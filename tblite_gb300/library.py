@@ -75,6 +75,7 @@ _SIGNATURES = {
     "tblite_get_singlepoint": (None, [c_void_p, c_void_p, c_void_p, c_void_p]),
     "tblite_new_alpb_solvation_solvent": (c_void_p, [c_void_p, c_void_p, c_char_p, c_int, c_int]),
     "tblite_new_gb_solvation_epsilon": (c_void_p, [c_void_p, c_void_p, c_double, c_int, c_int]),
+    "tblite_new_electric_field": (c_void_p, [_dbl_p]),
     "tblite_calculator_push_back": (None, [c_void_p, c_void_p, POINTER(c_void_p)]),
     "tblite_delete_container": (None, [POINTER(c_void_p)]),
     # extensions (include/tblite_gb300_ext.h)
@@ -722,6 +723,16 @@ def new_gb_solvation_epsilon(mol, epsilon: float, born: str, alpb: bool):
     cont = c_void_p(lib.tblite_new_gb_solvation_epsilon(err.h, mol, float(epsilon),
                                                         10 if alpb else 20, BORN_KERNELS[born]))
     err.check()
+    return cont
+
+
+def new_electric_field(efield):
+    """Container of a homogeneous electric field (three components, atomic units;
+    tblite_new_electric_field)."""
+    e = np.ascontiguousarray(efield, dtype=np.float64).reshape(3)
+    cont = c_void_p(load().tblite_new_electric_field(_dp(e)))
+    if not cont.value:
+        raise TBLiteRuntimeError("Could not create the electric field container")
     return cont
 
 
