@@ -457,15 +457,22 @@ def run_batch(args):
     if ws > 1:
         torch.distributed.barrier()
     wall = dev_ms = 0.0
+    host = dict.fromkeys(library.BATCH_HOST_PHASES + ("python_call", "python_results"), 0.0)
     with ClockSampler(dev) as clocks:
         for _ in range(args.steps):
             _flush_l2(flush)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             res = batch_singlepoint(calcs)  # host in, host out
+            t1 = time.perf_counter()
             energies = [r.get("energy") for r in res]
-            wall += time.perf_counter() - t0
+            t2 = time.perf_counter()
+            wall += t2 - t0
             dev_ms += library.load().tblite_gb300_batch_last_device_ms()
+            for k, v in library.batch_host_ms().items():
+                host[k] += v
+            host["python_call"] += 1e3 * (t1 - t0)
+            host["python_results"] += 1e3 * (t2 - t1)
     launches = library.launch_count() - n0
     fallbacks = batch_fallbacks()
     projected = library.batch_projected()
@@ -627,7 +634,11 @@ def run_batch(args):
                                                     "memory chunk is one CUDA graph launch"},
                    "l2": "flushed (256 MB write) before every step", "parallelism": f"replicas x{ws}"},
         "e2e": {"value": round(e2e, 3), "unit": "evals/s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h)},
+                "d2h_bytes_per_step": int(d2h),
+                "host_ms_per_step": {k: round(v / args.steps, 2) for k, v in host.items()},
+                "host_note": "plans .. call: phases of the C call (host wall); python_call: "
+                             "batch_singlepoint as Python sees it; python_results: the "
+                             "energy getter over all results"},
         "batched_vs_plain": {"plain_gpu_evals_per_s": round(plain, 3),
                              "sample": f"first {len(sample)} molecules of the seeded random "
                                        f"order ({_kinds(sample)}), one per call",

@@ -75,6 +75,10 @@ int tblite_gb300_batch_last_graphs(int* builds, int* launches);
  * of the gradient, summed over its memory chunks (uploads, read-back and the one-molecule
  * path excluded) */
 double tblite_gb300_batch_last_device_ms(void);
+/* host wall time (ms) of the last batch call by phase, in this order: building the molecule
+ * plans, chunking, staging and uploading the inputs, unpacking the results, the one-molecule
+ * path, the whole call; fills up to n entries and returns the number of phases */
+int tblite_gb300_batch_last_host_ms(double* ms, int n);
 /* SCF iterations of each molecule of the last batch call; 0 for molecules routed to the
  * one-molecule path up front, a negative code for molecules that left the batch (-1 singular
  * Broyden system, -2 overlap not positive definite, -3 Fermi level above the eigenvalues the

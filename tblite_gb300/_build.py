@@ -34,7 +34,7 @@ def nvcc() -> str:
 
 def _compile(src: Path, obj: Path) -> None:
     cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-           "-Xcompiler", "-fvisibility=default", "-c", str(src), "-o", str(obj)]
+           "-Xcompiler", "-fvisibility=default", "-Xcompiler", "-pthread", "-c", str(src), "-o", str(obj)]
     if src.suffix == ".cu":
         cmd[1:1] = ["-Xptxas", "-O3"]
     res = subprocess.run(cmd, capture_output=True, text=True)
@@ -64,8 +64,8 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     newest = max(o.stat().st_mtime for _, o, _ in jobs)
     if force or not lib.exists() or lib.stat().st_mtime < newest:
         tmp = OUT / f".{LIBNAME}.{os.getpid()}"
-        cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *[str(o) for _, o, _ in jobs],
-               "-lcudart"]
+        cmd = [nvcc(), *ARCH, "-shared", "-Xcompiler", "-pthread", "-o", str(tmp),
+               *[str(o) for _, o, _ in jobs], "-lcudart"]
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")

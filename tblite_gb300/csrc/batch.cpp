@@ -28,10 +28,12 @@
 #include <chrono>
 #include <cstdio>
 #include <cstring>
+#include <exception>
 #include <mutex>
 #include <numeric>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/tblite_gb300_ext.h"
@@ -109,6 +111,41 @@ int g_last_projected = 0;  // molecules of the last call whose SCF density came 
 bool g_batch_graphs = true;  // SCF iterations as CUDA graphs
 int g_last_graph_builds = 0, g_last_graph_launches = 0;  // of the last call
 double g_last_device_ms = 0.0;  // device time of the last call's batched steps (CUDA events)
+// host wall time of the last call by phase (ms): plans, chunking, staging and upload, result
+// unpacking, one-molecule path, whole call
+enum { HP_PLAN, HP_CHUNK, HP_STAGE, HP_UNPACK, HP_PLAIN, HP_TOTAL, HP_N };
+double g_last_host_ms[HP_N] = {};
+using host_clock = std::chrono::steady_clock;
+double ms_since(host_clock::time_point t0) {
+  return std::chrono::duration<double, std::milli>(host_clock::now() - t0).count();
+}
+
+// fn(i) for i in [0, n) on up to 16 host threads in contiguous ranges (one thread below 256
+// molecules); fn touches only molecule i's host data.  The first exception is rethrown.
+template <class F>
+void host_parallel(int n, F&& fn) {
+  const int hw = std::max(1u, std::thread::hardware_concurrency());
+  const int nt = std::max(1, std::min({hw, 16, n / 128}));
+  if (nt == 1) {
+    for (int i = 0; i < n; ++i) fn(i);
+    return;
+  }
+  std::vector<std::exception_ptr> err(nt);
+  auto work = [&](int t) {
+    try {
+      for (int i = (int)((long)n * t / nt), e = (int)((long)n * (t + 1) / nt); i < e; ++i) fn(i);
+    } catch (...) {
+      err[t] = std::current_exception();
+    }
+  };
+  std::vector<std::thread> pool;
+  pool.reserve(nt - 1);
+  for (int t = 1; t < nt; ++t) pool.emplace_back(work, t);
+  work(0);
+  for (auto& th : pool) th.join();
+  for (auto& e : err)
+    if (e) std::rethrow_exception(e);
+}
 std::vector<int> g_last_iters;  // SCF iterations per molecule of the last call (0: not batched)
 std::vector<int> g_last_modes;  // 1 projection, 0 diagonalisation, -1 one-molecule path
 
@@ -542,6 +579,7 @@ struct Lists {
 // one chunk of molecules through setup, SCF and gradient; fills results of the converged
 // ones, returns the plan indices that must take the one-molecule path
 std::vector<int> run_chunk(std::vector<Plan>& plans, Arena& ar, _tblite_context* ctx) {
+  const auto t_stage = host_clock::now();
   const int np = (int)plans.size();
   Region R[NREG];
   for (auto& pl : plans) layout(pl, R);
@@ -567,8 +605,9 @@ std::vector<int> run_chunk(std::vector<Plan>& plans, Arena& ar, _tblite_context*
   int* d_steps = reinterpret_cast<int*>(dtail + off_steps);
   // host stage: uploaded region first, then the tables
   Bases hb{{nullptr, nullptr, nullptr, ar.host}};
-  std::vector<double> qsh, qat, dp, qp;
-  for (auto& pl : plans) {
+  host_parallel(np, [&](int i) {
+    const Plan& pl = plans[i];
+    std::vector<double> qsh, qat, dp, qp;
     const _tblite_calculator* c = pl.c;
     stage(hb, pl.xyz, pl.mol->xyz);
     stage(hb, pl.at_z, c->at_z);
@@ -625,7 +664,7 @@ std::vector<int> run_chunk(std::vector<Plan>& plans, Arena& ar, _tblite_context*
     stage(hb, pl.qat, qat);
     stage(hb, pl.dpat, dp);
     stage(hb, pl.qpat, qp);
-  }
+  });
   cuda_check(cudaMemcpyAsync(db.base[RU], ar.host, R[RU].size, cudaMemcpyHostToDevice, s),
              "batch upload");
   cuda_check(cudaMemsetAsync(db.base[RZ], 0, R[RZ].size + R[RR].size, s), "batch zero");
@@ -702,6 +741,7 @@ std::vector<int> run_chunk(std::vector<Plan>& plans, Arena& ar, _tblite_context*
   cuda_check(cudaEventCreate(&ev0), "event");
   cuda_check(cudaEventCreate(&ev1), "event");
   cuda_check(cudaEventRecord(ev0, s), "event");
+  g_last_host_ms[HP_STAGE] += ms_since(t_stage);
   each([&](BatchLaunch& L) {
     launch_cn_b(L, p);
     launch_setup_levels_b(L, p);
@@ -930,9 +970,10 @@ std::vector<int> run_chunk(std::vector<Plan>& plans, Arena& ar, _tblite_context*
         record_leave(i, h_flag[i]);
       }
     cuda_check(cudaEventElapsedTime(&scf_ms, ev0, ev1), "event");
+    const auto t_unpack = host_clock::now();
     const Bases hz{{nullptr, ar.host, nullptr, nullptr}};
-    for (int i = 0; i < np; ++i) {
-      if (!done[i]) continue;
+    host_parallel(np, [&](int i) {
+      if (!done[i]) return;
       const Plan& pl = plans[i];
       _tblite_result* res = pl.res;
       const int nat = pl.nat, n = pl.nao;
@@ -1007,7 +1048,8 @@ std::vector<int> run_chunk(std::vector<Plan>& plans, Arena& ar, _tblite_context*
         res->dkcn.clear();
         res->dzeta.clear();
       }
-    }
+    });
+    g_last_host_ms[HP_UNPACK] += ms_since(t_unpack);
   }
   cudaEventDestroy(ev0);
   cudaEventDestroy(ev1);
@@ -1035,8 +1077,10 @@ extern "C" int tblite_gb300_batch_singlepoint(tblite_context ctx, int nmol,
     ctx->push("Batch input arrays are missing");
     return nmol;
   }
+  const auto t_call = host_clock::now();
   std::vector<int> st(nmol, 0);
   std::vector<Plan> plans;
+  plans.reserve(nmol);
   std::vector<int> plain;  // molecules for the one-molecule path
   const int tri_max = batch_tridiag_max_n();
   for (int i = 0; i < nmol; ++i) {
@@ -1106,13 +1150,25 @@ extern "C" int tblite_gb300_batch_singlepoint(tblite_context ctx, int nmol,
       pl.model = id;
     }
   }
-  std::stable_sort(plans.begin(), plans.end(), [](const Plan& a, const Plan& b) {
-    if (a.model != b.model) return a.model < b.model;
-    if (a.sp2 != b.sp2) return a.sp2;
-    return a.nao > b.nao;
-  });
+  {  // sorted through an index permutation: a plan holds ~140 array offsets
+    std::vector<int> order(plans.size());
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int i, int j) {
+      const Plan& a = plans[i];
+      const Plan& b = plans[j];
+      if (a.model != b.model) return a.model < b.model;
+      if (a.sp2 != b.sp2) return a.sp2;
+      return a.nao > b.nao;
+    });
+    std::vector<Plan> sorted;
+    sorted.reserve(plans.size());
+    for (int k : order) sorted.push_back(plans[k]);
+    plans.swap(sorted);
+  }
   try {
     std::lock_guard<std::mutex> lock(g_batch_mutex);
+    for (double& t : g_last_host_ms) t = 0.0;
+    g_last_host_ms[HP_PLAN] = ms_since(t_call);
     g_last_device_ms = 0.0;
     g_last_projected = 0;
     g_last_graph_builds = g_last_graph_launches = 0;
@@ -1122,11 +1178,17 @@ extern "C" int tblite_gb300_batch_singlepoint(tblite_context ctx, int nmol,
     // chunks of at most ~24 GB of device memory
     const size_t budget = (size_t)24 << 30;
     size_t i0 = 0;
+    std::vector<size_t> mbytes(plans.size());
+    {
+      const auto t_chunk = host_clock::now();
+      for (size_t k = 0; k < plans.size(); ++k) mbytes[k] = molecule_bytes(plans[k]);
+      g_last_host_ms[HP_CHUNK] = ms_since(t_chunk);
+    }
     while (i0 < plans.size()) {
       size_t i1 = i0, bytes = 0;
       while (i1 < plans.size() && plans[i1].model == plans[i0].model &&
-             (i1 == i0 || bytes + molecule_bytes(plans[i1]) <= budget)) {
-        bytes += molecule_bytes(plans[i1]);
+             (i1 == i0 || bytes + mbytes[i1] <= budget)) {
+        bytes += mbytes[i1];
         ++i1;
       }
       std::vector<Plan> chunk(plans.begin() + i0, plans.begin() + i1);
@@ -1151,6 +1213,7 @@ extern "C" int tblite_gb300_batch_singlepoint(tblite_context ctx, int nmol,
   // the one-molecule path for the rest (reproduces a plain call, errors included)
   std::sort(plain.begin(), plain.end());
   g_last_fallbacks = (int)plain.size();
+  const auto t_plain = host_clock::now();
   for (int i : plain) {
     try {
       run_singlepoint(ctx, mols[i], calcs[i], results[i]);
@@ -1159,6 +1222,8 @@ extern "C" int tblite_gb300_batch_singlepoint(tblite_context ctx, int nmol,
       st[i] = 1;
     }
   }
+  g_last_host_ms[HP_PLAIN] = ms_since(t_plain);
+  g_last_host_ms[HP_TOTAL] = ms_since(t_call);
   int failed = 0;
   for (int i = 0; i < nmol; ++i) failed += st[i];
   if (status)
@@ -1195,6 +1260,11 @@ extern "C" void tblite_gb300_set_batch_streams(int count) {
   g_batch_streams = count < 1 ? 1 : (count > Arena::NSIDE ? Arena::NSIDE : count);
 }
 extern "C" double tblite_gb300_batch_last_device_ms(void) { return g_last_device_ms; }
+extern "C" int tblite_gb300_batch_last_host_ms(double* ms, int n) {
+  const int m = std::min(n, (int)HP_N);
+  for (int k = 0; k < m && ms; ++k) ms[k] = g_last_host_ms[k];
+  return HP_N;
+}
 extern "C" int tblite_gb300_batch_last_iterations(int* iterations, int nmol) {
   const int m = std::min(nmol, (int)g_last_iters.size());
   for (int i = 0; i < m && iterations; ++i) iterations[i] = g_last_iters[i];

@@ -98,7 +98,7 @@ class Result:
                 flat = library.result_array(self._res, name, (2 * real[0] * real[1],))
                 return flat.reshape((real[0], real[1], 2), order="F")
         if attribute == "energy":
-            return float(library.result_array(self._res, name, (1,))[0])
+            return library.result_double(self._res, name)
         return library.result_array(self._res, name, real)
 
     def dict(self):

@@ -10,6 +10,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+import threading
 from ctypes import POINTER, byref, c_bool, c_char_p, c_double, c_int, c_void_p
 from pathlib import Path
 
@@ -136,6 +137,7 @@ _SIGNATURES = {
     "tblite_gb300_set_batch_graphs": (None, [c_int]),
     "tblite_gb300_batch_last_graphs": (c_int, [_int_p, _int_p]),
     "tblite_gb300_batch_last_device_ms": (c_double, []),
+    "tblite_gb300_batch_last_host_ms": (c_int, [POINTER(c_double), c_int]),
     "tblite_gb300_batch_last_iterations": (c_int, [_int_p, c_int]),
 }
 _c64p = POINTER(ctypes.c_int64)
@@ -266,6 +268,17 @@ def batch_graphs_enabled() -> bool:
     return bool(load().tblite_gb300_batch_last_graphs(None, None))
 
 
+BATCH_HOST_PHASES = ("plans", "chunking", "staging", "unpacking", "one_molecule_path", "call")
+
+
+def batch_host_ms() -> dict:
+    """Host wall time (ms) of the last batch call by phase (the device time is
+    ``tblite_gb300_batch_last_device_ms``)."""
+    out = np.zeros(len(BATCH_HOST_PHASES), dtype=np.float64)
+    load().tblite_gb300_batch_last_host_ms(_dp(out), out.size)
+    return {k: float(v) for k, v in zip(BATCH_HOST_PHASES, out)}
+
+
 def batch_projected() -> int:
     """Molecules of the last batch call whose SCF density came from the spectral projection."""
     return int(load().tblite_gb300_batch_last_projected())
@@ -362,6 +375,17 @@ class _Error:
     def __del__(self):
         if getattr(self, "h", None) and self.h.value:
             self.lib.tblite_delete_error(byref(self.h))
+
+
+_tls = threading.local()
+
+
+def _thread_error() -> _Error:
+    """One error handle per thread, reused by the result getters (``check`` clears it)."""
+    err = getattr(_tls, "err", None)
+    if err is None:
+        err = _tls.err = _Error()
+    return err
 
 
 def context_check(ctx):
@@ -603,7 +627,7 @@ def new_ipea1_calculator(ctx, mol):
 
 def result_array(res, name, shape):
     lib = load()
-    err = _Error()
+    err = _thread_error()
     out = np.zeros(shape, dtype=np.float64)
     getattr(lib, f"tblite_get_result_{name}")(err.h, res, _dp(out))
     err.check()
@@ -678,9 +702,18 @@ def set_density_solver(ctx, calc, solver):
     context_check(ctx)
 
 
+def result_double(res, name):
+    lib = load()
+    err = _thread_error()
+    v = c_double(0.0)
+    getattr(lib, f"tblite_get_result_{name}")(err.h, res, byref(v))
+    err.check()
+    return v.value
+
+
 def result_int(res, name):
     lib = load()
-    err = _Error()
+    err = _thread_error()
     v = c_int(0)
     getattr(lib, f"tblite_get_result_{name}")(err.h, res, byref(v))
     err.check()
