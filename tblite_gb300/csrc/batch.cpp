@@ -196,7 +196,7 @@ struct Plan {
   Piece X, A, T1, Y, lu, ed, ee, etau, epv, escal, estatus, conv;
   Piece pgrad, zgrad;  // [4][nsh], [nsh] (param_grad only)
   Piece wbo;           // [wbo_ch][nat][nat] (bond orders requested only)
-  Piece img, iexp, img2, iexp2, sp2s, sp2i;  // spectral projection (sp2 only)
+  Piece img, iexp, img2, iexp2, sp2s, sp2i, sp2p;  // spectral projection (sp2 only)
 };
 
 struct Bucket {
@@ -296,6 +296,7 @@ void layout(Plan& pl, Region* R) {
     pl.iexp2 = piece<int>(R, RS, pimage_lines((int)n));
     pl.sp2s = piece<double>(R, RS, 8);
     pl.sp2i = piece<int>(R, RZ, 8);  // zeroed: the pipeline status starts clear
+    pl.sp2p = piece<unsigned long long>(R, RS, 3 * (size_t)sp2_slot_count((int)n));
   }
   // scratch
   pl.cn = piece<double>(R, RS, na);
@@ -518,6 +519,7 @@ MolPtrs make_ptrs(const Plan& pl, const Bases& db) {
   q.iexp2 = pl.sp2 ? db.at<int>(pl.iexp2) : nullptr;
   q.sp2s = pl.sp2 ? db.at<double>(pl.sp2s) : nullptr;
   q.sp2i = pl.sp2 ? db.at<int>(pl.sp2i) : nullptr;
+  q.sp2p = pl.sp2 ? db.at<unsigned long long>(pl.sp2p) : nullptr;
   if (pl.sp2) q.nev = pl.nao;  // the projection needs no levels during the SCF; all after it
   return q;
 }

@@ -387,15 +387,18 @@ struct MolPtrs {
   // open shell) and the output [channels][nat][nat]
   int wbo_ch;
   double* wbo;
-  // density by spectral projection (closed shells of a projection bucket, sp2.cu): slice image
-  // of the iterate (in Y) and its line exponents, state doubles [8] and ints [8], and the steps
-  // of the last projection for the host
+  // density by spectral projection (closed shells of a projection bucket, sp2.cu): the slice
+  // image of the iterate (in Y) and its line exponents, a second image (the columns of op(B) of
+  // a pipelined GEMM site), state doubles [8] and ints [8], partial sums of the iterate
+  // [3 sp2_slot_count(nao)] (trace and the 128-bit sum of squares per block of 8 lines), and the
+  // steps of the last projection for the host
   uint16_t* img;
   int* iexp;
-  uint16_t* img2;  // second image (the columns of op(B) of a pipelined GEMM site)
+  uint16_t* img2;
   int* iexp2;
   double* sp2s;
   int* sp2i;
+  unsigned long long* sp2p;
   int* sp2steps;
 };
 
@@ -517,10 +520,13 @@ void sp2_density_b(const BatchLaunch& b, int steps);
 void sp2_gap_b(const BatchLaunch& b);
 void sp2_weighted_b(const BatchLaunch& b);
 void sp2_pipe_check_b(const BatchLaunch& b);  // flag -5 for a molecule whose pipe wait ran out
-void sp2_square_b(const BatchLaunch& b);  // ozaki_pipe.cu: C = Y Y of the iterating molecules
-// ozaki_pipe.cu: the next iterate into Y (init: D0 from A and the Gershgorin bounds; else D^2
-// or 2D - D^2 as decided), its line exponents and slice image
-void sp2_step_b(const BatchLaunch& b, bool init);
+// ozaki_pipe.cu: the squaring of a projection step of the iterating molecules (D^2 on the
+// tensor cores from the slice image; the next iterate D^2 or 2D - D^2 over D in Y)
+void sp2_square_b(const BatchLaunch& b);
+// ozaki_pipe.cu: the slice image of the iterate in Y with its exact partial sums, and the next
+// decision (init: D0 from A and the Gershgorin bounds into Y first)
+void sp2_slice_b(const BatchLaunch& b, bool init);
+int sp2_slot_count(int n);  // partial-sum slots of a molecule of n orbitals (3 words each)
 constexpr int SP2_MIN_NAO = 128;   // smallest orbital count that takes the projection
 constexpr int SP2_MAX_STEPS = 64;  // squarings per projection at most
 

@@ -105,12 +105,14 @@ __device__ __forceinline__ void tmem_ld16(uint32_t addr, uint32_t (&v)[16]) {
       : "r"(addr));
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
-
-// BF16 bits of (-1)^sign a 2^-7p for an integer 0 <= a < 128 (exact: at most 7 significant bits)
+// BF16 bits of (-1)^sign a 2^-7p for an integer 0 <= a < 128 (exact: at most 7 significant bits).
+// a becomes a float by the 2^23 bias trick: the float with exponent 2^23 and mantissa field a is
+// 2^23 + a exactly, and subtracting 2^23 leaves a (one FP32 add on the FMA pipe instead of an
+// integer-to-float conversion); the power of two then goes into the exponent field.
 __device__ __forceinline__ uint32_t slice_bits(uint32_t a, int p, uint32_t sign) {
-  if (a == 0) return 0u;
-  const uint32_t u = __float_as_uint((float)a) - ((uint32_t)(7 * p) << 23);
-  return (u >> 16) | (sign << 15);
+  const float fa = __uint_as_float(0x4B000000u | a) - 8388608.0f;
+  const uint32_t u = __float_as_uint(fa) - ((uint32_t)(7 * p) << 23);
+  return a ? ((u >> 16) | (sign << 15)) : 0u;
 }
 
 // ---- exponents: e = ilogb(max |x|) + 1 of every line ------------------------------------------
@@ -223,7 +225,47 @@ struct PipeArgs {
   int ldc;
   int sym;
   int* status;
+  // a projection step applied in the epilogue: C <- 2 C - product (the old C read first); with
+  // C the iterate D this turns D^2 into 2D - D^2 in place
+  int sub2;
 };
+
+// line exponent of every projection iterate: the spectrum of D stays in [0, 1], so every element
+// has |x| <= 1 < 2^SP2_E and the slices hold x to an absolute 2^-55 (the iterate's own rounding
+// is 2^-53 relative to its O(1) diagonal); an element at or above 2^SP2_E stops the molecule
+constexpr int SP2_E = 1;
+
+__device__ __forceinline__ int slice_off(int line, int k, int nlb) {
+  // image[k chunk][slice][line block][64 lines x 32 k], 16-byte groups swizzled (slice 0)
+  const int li = line & 63, g = (k >> 3) & 3;
+  return (((k >> 5) * 8) * nlb + (line >> 6)) * 2048 + li * 32 + ((g ^ ((li >> 1) & 3)) << 3) +
+         (k & 7);
+}
+
+// |x| 2^(56 - e) as an integer (< 2^56 for |x| < 2^e): zero and subnormals give zero
+__device__ __forceinline__ uint64_t fixed_bits(uint64_t bits, int e) {
+  const int ex = (int)((bits >> 52) & 0x7FF);
+  if (ex == 0) return 0ull;
+  const uint64_t m = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+  const int sh = ex - e - 1019;
+  return sh >= 0 ? m << sh : (sh > -64 ? m >> (-sh) : 0ull);
+}
+
+// C element (i, j) of a finished tile from the exact levels T, the FP32 levels v6 + v7 and the
+// scale 2^sc: C = (T + F 2^35) 2^(sc - 35), F = levels 6 + 7 summed in FP32 (F < 2^-42 of the
+// result, so its rounding is below 2^-66); the power of two goes into the exponent field by an
+// integer add where the result stays normal: three FP64 operations per element (two conversions
+// and an add) instead of six
+__device__ __forceinline__ double tile_value(long long T, uint32_t v6, uint32_t v7, int sc) {
+  const float ff = (__uint_as_float(v6) + __uint_as_float(v7)) * 0x1p35f;
+  const double sum = (double)T + (double)ff;
+  const long long sb = __double_as_longlong(sum);
+  const int se = (int)((sb >> 52) & 0x7FF);
+  if (sum == 0.0) return 0.0;
+  if (se > 0 && se + (sc - 35) > 0 && se + (sc - 35) < 2047)
+    return __longlong_as_double(sb + ((long long)(sc - 35) << 52));
+  return ldexp(sum, sc - 35);  // subnormal or out-of-range result: the general path
+}
 
 // one 128 x 64 output tile (number b in the grouped order) of the product a
 __device__ __forceinline__ void opipe_tile(const PipeArgs& a, int b) {
@@ -419,26 +461,24 @@ __device__ __forceinline__ void opipe_tile(const PipeArgs& a, int b) {
         tmem_ld16(lane_base + (uint32_t)(7 * PP_N + 16 * h), v7);
         if (i < a.M) {
 #pragma unroll
-          for (int t = 0; t < 16; ++t) {
-            const int j = j0 + 32 * half + 16 * h + t;
-            if (j < a.N && !(a.sym && i < j)) {
-              // C = (T + F 2^35) 2^(sc - 35), F = levels 6 + 7 summed in FP32 (F < 2^-42 of
-              // the result, so its rounding is below 2^-66); the power of two goes into the
-              // exponent field by an integer add where the result stays normal: three FP64
-              // operations per element (two conversions and an add) instead of six
-              const int sc = ei + a.eB[j] - 14 - 35;
-              const float ff = (__uint_as_float(v6[t]) + __uint_as_float(v7[t])) * 0x1p35f;
-              const double sum = (double)T[16 * h + t] + (double)ff;
-              const long long sb = __double_as_longlong(sum);
-              const int se = (int)((sb >> 52) & 0x7FF);
-              double val;
-              if (sum == 0.0) val = 0.0;
-              else if (se > 0 && se + sc > 0 && se + sc < 2047)
-                val = __longlong_as_double(sb + ((long long)sc << 52));
-              else
-                val = ldexp(sum, sc);  // subnormal or out-of-range result: the general path
-              a.C[i + (size_t)j * a.ldc] = val;
-              if (a.sym && i != j) a.C[j + (size_t)i * a.ldc] = val;
+          for (int t8 = 0; t8 < 16; t8 += 8) {
+            // the old elements of C first (sub2), so their loads are in flight together
+            double old[8];
+#pragma unroll
+            for (int t = 0; t < 8; ++t) {
+              const int j = j0 + 32 * half + 16 * h + t8 + t;
+              old[t] = (a.sub2 && j < a.N && !(a.sym && i < j)) ? a.C[i + (size_t)j * a.ldc] : 0.0;
+            }
+#pragma unroll
+            for (int t = 0; t < 8; ++t) {
+              const int j = j0 + 32 * half + 16 * h + t8 + t;
+              if (j < a.N && !(a.sym && i < j)) {
+                double val =
+                    tile_value(T[16 * h + t8 + t], v6[t8 + t], v7[t8 + t], ei + a.eB[j] - 14);
+                if (a.sub2) val = 2.0 * old[t] - val;
+                a.C[i + (size_t)j * a.ldc] = val;
+                if (a.sym && i != j) a.C[j + (size_t)i * a.ldc] = val;
+              }
             }
           }
         }
@@ -454,43 +494,43 @@ __device__ __forceinline__ void opipe_tile(const PipeArgs& a, int b) {
 }
 __global__ void __launch_bounds__(PP_THREADS, 1) k_opipe(PipeArgs a) { opipe_tile(a, blockIdx.x); }
 
-// ---- batched squaring X <- X X of the spectral projection: one symmetric product per molecule
-// of the list (blockIdx.z / blockIdx.y walks the molecules).  The iterate lives in Y, its slice
-// image in img (exponents iexp), the square goes to C.  Molecules that left the batch or whose
-// projection has converged (sp2i[0] != 0) launch nothing.
+// ---- batched spectral projection on the pipe, two launches per step for every molecule of the
+// list still iterating (blockIdx.y / blockIdx.z walks the molecules): kb_opipe_sq squares the
+// iterate D_k from its slice image and writes D_(k+1) = D_k^2, or 2 D_k - D_k^2 (the old element
+// read first), over D_k in Y; kb_sp2_slice then writes the slice image of D_(k+1) (every line
+// exponent SP2_E) with the partial sums of its trace and of its squared elements, and its last
+// block takes the next decision.  Molecules that left the batch or whose projection has
+// converged (sp2i[0] != 0) launch nothing.
 __device__ __forceinline__ int lines_padded(int n) { return ((n + PP_M - 1) / PP_M) * PP_M; }
+__device__ __forceinline__ int sq_tiles(int n) {
+  return ((n + PP_M - 1) / PP_M) * ((n + PP_N - 1) / PP_N);
+}
+// partial-sum slots of a molecule: one per block of kb_sp2_slice (8 lines)
+__host__ __device__ __forceinline__ int sp2_slots(int n) {
+  return ((n + PP_M - 1) / PP_M) * PP_M / 8;
+}
 
-// The decision of a projection step, taken by one CTA after C = D^2 is complete: traces of D (Y)
-// and D^2 (C) in a fixed order, read past L1 since other CTAs and kernels wrote them, the idempotency error
+// The decision at a new iterate D, taken by one thread after every partial sum of D is written:
+// tr D in a fixed order, tr D^2 = sum of the squares of D's elements (D is symmetric) exactly in
+// 128-bit integers, read past L1 since other CTAs wrote them; then the idempotency error
 // tr(D - D^2), the stop test (the error no longer falls over two steps, Kruchinin, Rubensson,
 // Niklasson 2016, or reaches the rounding floor) and the update D^2 or 2D - D^2 whose trace is
 // closer to the occupied count (Niklasson 2002).  State: sp2i[0] converged, [1] steps taken,
-// [2] update of this step (1 square, 0 2D - D^2, -1 none), [3] pipeline status; sp2s[2..4]
-// the last three idempotency errors.
-__device__ void sp2_decide_cta(const MolPtrs& q) {
-  __shared__ double red[2][PP_THREADS / 32];
-  const int n = q.m.nao, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  double a = 0.0, b = 0.0;
-  for (int t = threadIdx.x; t < n; t += PP_THREADS) {
-    a += __ldcg(q.Y + t + (size_t)t * n);
-    b += __ldcg(q.C + t + (size_t)t * n);
+// [2] update of the next step (1 square, 0 2D - D^2, -1 none), [3] pipeline status; sp2s[2..4]
+// the last three idempotency errors.  A partial sum that is not a number (an element outside
+// the fixed-exponent range, or not finite) sends the molecule away.
+__device__ void sp2_decide(const MolPtrs& q, int nslots) {
+  double tx = 0.0;
+  unsigned long long lo = 0ull, hi = 0ull;
+  for (int t = 0; t < nslots; ++t) {
+    const unsigned long long* pt = q.sp2p + 3 * t;
+    tx += __longlong_as_double((long long)__ldcg(pt));
+    const unsigned long long l = __ldcg(pt + 1);
+    lo += l;
+    hi += __ldcg(pt + 2) + (lo < l ? 1ull : 0ull);
   }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    a += __shfl_xor_sync(0xffffffffu, a, o);
-    b += __shfl_xor_sync(0xffffffffu, b, o);
-  }
-  if (lane == 0) {
-    red[0][warp] = a;
-    red[1][warp] = b;
-  }
-  __syncthreads();
-  if (threadIdx.x != 0) return;
-  double tx = 0.0, tx2 = 0.0;
-  for (int w = 0; w < PP_THREADS / 32; ++w) {
-    tx += red[0][w];
-    tx2 += red[1][w];
-  }
+  const double tx2 = ((double)hi * 0x1p64 + (double)lo) * 0x1p-110;
+  const int n = q.m.nao;
   if (q.sp2i[3] != 0) {  // a tensor-core wait ran out: the molecule takes the one-molecule path
     *q.flag = -5;
     return;
@@ -515,6 +555,22 @@ __device__ void sp2_decide_cta(const MolPtrs& q) {
   q.sp2i[2] = fabs(tx2 - nocc) <= fabs(2.0 * tx - tx2 - nocc) ? 1 : 0;
   q.sp2i[1] = k + 1;
 }
+// the last of `units` CTAs of a molecule to finish takes the decision (no separate launch):
+// after the CTA's barrier one thread fences (cumulatively, the stores its barrier ordered before
+// it) and counts the finished units; the CTA that completes the count decides and resets it
+__device__ __forceinline__ void sp2_last_decides(const MolPtrs& q, int units) {
+  __shared__ int last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(q.sp2i + 5, 1) == units - 1;
+  }
+  __syncthreads();
+  if (!last || threadIdx.x != 0) return;
+  __threadfence();
+  sp2_decide(q, units);  // one partial sum per unit
+  q.sp2i[5] = 0;
+}
 __device__ __forceinline__ bool sq_skip(const MolPtrs& q) {
   return *q.flag < 0 || q.sp2i[0] != 0;
 }
@@ -522,21 +578,20 @@ __global__ void __launch_bounds__(PP_THREADS, 1) kb_opipe_sq(const MolPtrs* __re
                                                             const int* __restrict__ list) {
   const MolPtrs& q = mp[list[blockIdx.y]];
   const int n = q.m.nao;
-  const int tiles = ((n + PP_M - 1) / PP_M) * ((n + PP_N - 1) / PP_N);
+  const int tiles = sq_tiles(n);
   if (sq_skip(q) || (int)blockIdx.x >= tiles) return;
   PipeArgs a{};
-  a.A = q.img;
-  a.B = q.img;  // a symmetric matrix: its rows are its columns
-  a.eA = q.iexp;
-  a.eB = q.iexp;
+  a.A = a.B = q.img;  // a symmetric matrix: its rows are its columns
+  a.eA = a.eB = q.iexp;
   a.eshiftA = 0;
   a.nlbA = a.nlbB = lines_padded(n) / 64;
   a.M = a.N = n;
   a.nkc = (n + PP_KC - 1) / PP_KC;
-  a.C = q.C;
+  a.C = q.Y;  // D_(k+1) over D_k
   a.ldc = n;
   a.sym = 1;
   a.status = q.sp2i + 3;
+  a.sub2 = q.sp2i[2] == 0 ? 1 : 0;
   if (threadIdx.x == 0) {  // the tile's useful area (the upper tiles of the symmetric product exit)
     const int mt = (n + PP_M - 1) / PP_M, nt = (n + PP_N - 1) / PP_N;
     const int b = blockIdx.x, gid = b / (PP_GROUP * nt), first = gid * PP_GROUP;
@@ -547,103 +602,134 @@ __global__ void __launch_bounds__(PP_THREADS, 1) kb_opipe_sq(const MolPtrs* __re
                                          (unsigned long long)min(PP_N, n - j0) * (unsigned)n);
   }
   opipe_tile(a, blockIdx.x);
-  // the last CTA of the molecule to finish takes the step's decision (no separate launch): after
-  // the CTA's barrier one thread fences (cumulatively, the stores of C its barrier ordered
-  // before it) and counts the finished tiles; the CTA that completes the count reads the
-  // diagonals of D and D^2 and resets the count
-  __shared__ int last;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    last = atomicAdd(q.sp2i + 5, 1) == tiles - 1;
-  }
-  __syncthreads();
-  if (!last) return;
-  __threadfence();
-  sp2_decide_cta(q);
-  if (threadIdx.x == 0) q.sp2i[5] = 0;
 }
 
-// ---- one projection step per molecule without a separate exponent or split pass: each warp
-// owns one line i of the symmetric iterate (column i in memory, which equals row i), forms
-// the new iterate there (init: D0 = (emax I - A) / (emax - emin); else D^2 or 2D - D^2 as
-// kb_sp2_decide chose), writes it back, takes the line's exponent from its largest element and
-// writes the line's slices (the same bits as pexp_rows_dev + psplit_dev on the row, since the
-// iterate is exactly symmetric).  Padding lines and k positions get zero slices.
-__global__ void __launch_bounds__(256) kb_sp2_step(const MolPtrs* __restrict__ mp,
-                                                   const int* __restrict__ list, int init) {
+// ---- the slice image of the iterate and the decision: each warp owns one line i of D (column i
+// in memory, which equals row i); at the start (init) the line is D0 = (emax I - A) /
+// (emax - emin), written to Y, else it is read from Y.  Its slices (exponent SP2_E) go to img,
+// and the line's diagonal element and the exact squares of its elements to the block's partial
+// sums; the last block of the molecule takes the decision.  A lane holds two neighbouring
+// elements k, k + 1 of a 64-element segment (coalesced loads), so each slice plane gets one
+// 32-bit word per lane.  Padding lines and positions get zero slices.
+//
+// Slice p of a fixed-point value Y < 2^56 is the 7-bit field a = (Y >> (49 - 7p)) & 127; its
+// BF16 value a 2^-7p is read off the float whose exponent field is 150 - 7p and mantissa field
+// a: that float is 2^(23 - 7p) + a 2^-7p exactly, and subtracting 2^(23 - 7p) leaves a 2^-7p
+// (exact: at most 7 significant bits), whose low 16 bits are zero.  The byte permute packs the
+// high halves of the two elements' floats into one word, and the signs go in with one OR (a
+// zero slice of a negative element becomes -0, which adds nothing to a product).
+__device__ __forceinline__ uint32_t slice7(uint64_t Y, int p) {
+  return (uint32_t)(Y >> (49 - 7 * p)) & 0x7Fu;
+}
+__device__ __forceinline__ float slice_value(uint32_t a, int p) {
+  return __uint_as_float(((uint32_t)(150 - 7 * p) << 23) | a) -
+         __uint_as_float((uint32_t)(150 - 7 * p) << 23);
+}
+// the square of Y < 2^56 as a (2^56, 2^28, 1) limb triple: Y = h 2^28 + l, Y^2 = h^2 2^56 +
+// 2 h l 2^28 + l^2 (every partial product below 2^56, so per-lane sums of up to 256 stay exact)
+struct Sq3 {
+  unsigned long long hh = 0ull, hl = 0ull, ll = 0ull;
+  __device__ __forceinline__ void add(uint64_t Y) {
+    const uint32_t h = (uint32_t)(Y >> 28), l = (uint32_t)Y & 0xFFFFFFFu;
+    hh += (unsigned long long)h * h;
+    hl += (unsigned long long)h * l;
+    ll += (unsigned long long)l * l;
+  }
+  // the 128-bit value hh 2^56 + hl 2^29 + ll
+  __device__ __forceinline__ void value(unsigned long long& lo, unsigned long long& hi) const {
+    lo = hh << 56;
+    hi = hh >> 8;
+    const unsigned long long m = hl << 29, mh = hl >> 35;
+    lo += m;
+    hi += mh + (lo < m ? 1ull : 0ull);
+    lo += ll;
+    hi += (lo < ll ? 1ull : 0ull);
+  }
+};
+__device__ __forceinline__ void add128(unsigned long long& lo, unsigned long long& hi,
+                                       unsigned long long l, unsigned long long h) {
+  lo += l;
+  hi += h + (lo < l ? 1ull : 0ull);
+}
+
+__global__ void __launch_bounds__(256) kb_sp2_slice(const MolPtrs* __restrict__ mp,
+                                                    const int* __restrict__ list, int init) {
   const MolPtrs& q = mp[list[blockIdx.z]];
   const int n = q.m.nao, lp = lines_padded(n);
+  // uniform over the block; sp2i[0] changes only in the last block, after every block started
+  if ((int)blockIdx.x * 8 >= lp || *q.flag < 0 || (!init && q.sp2i[0] != 0)) return;
   const int i = (int)blockIdx.x * 8 + (int)(threadIdx.x >> 5), lane = threadIdx.x & 31;
-  if (i >= lp || *q.flag < 0) return;
-  int u = 2;  // 2: the start D0 from A
-  double emax = 0.0, f = 0.0;
-  if (init) {
-    emax = q.sp2s[1];
-    f = 1.0 / (emax - q.sp2s[0]);
-  } else {
-    u = q.sp2i[2];  // -1 once converged
-    if (u < 0) return;
-  }
-  // the largest |v| of the line as bits: for non-negative doubles the unsigned order of the
-  // bit patterns is the numeric order (integer instructions instead of FP64 ones, which this
-  // GPU issues at 1/64 of the FP32 rate)
-  unsigned long long mb = 0ull;
-  if (i < n) {
-    double* y = q.Y + (size_t)i * n;
-    const double* c = q.C + (size_t)i * n;
-    const double* am = q.A + (size_t)i * n;
-    // one loop per kind of update (u is uniform over the warp), so no FP64 operation is
-    // evaluated for a branch that is not taken: D^2 is a copy, 2D - D^2 one FMA per element
-    auto put = [&](int k, double v) {
-      y[k] = v;
-      const unsigned long long b = (unsigned long long)__double_as_longlong(v) & ~(1ull << 63);
-      mb = b > mb ? b : mb;
-    };
-    if (u == 1) {
-      for (int k = lane; k < n; k += 32) put(k, c[k]);
-    } else if (u == 0) {
-      for (int k = lane; k < n; k += 32) put(k, 2.0 * y[k] - c[k]);
-    } else {
-      for (int k = lane; k < n; k += 32) put(k, ((k == i ? emax : 0.0) - am[k]) * f);
+  const double emax = init ? q.sp2s[1] : 0.0, f = init ? 1.0 / (emax - q.sp2s[0]) : 0.0;
+  const int nkc = (n + PP_KC - 1) / PP_KC, nlb = lp / 64;
+  const size_t plane = (size_t)nlb * 2048;
+  double tr = 0.0;
+  Sq3 sq;
+  bool over = false;
+  const double* __restrict__ am = q.A + (size_t)i * n;
+  double* __restrict__ y = q.Y + (size_t)i * n;
+  const bool real = i < n;
+  for (int seg = 0; seg * 64 < nkc * PP_KC; ++seg) {
+    const int k = seg * 64 + 2 * lane;
+    if ((k >> 5) >= nkc) continue;  // the last segment may hold one chunk only
+    double x0 = 0.0, x1 = 0.0;
+    if (real) {
+      if (init) {
+        if (k < n) y[k] = x0 = ((k == i ? emax : 0.0) - am[k]) * f;
+        if (k + 1 < n) y[k + 1] = x1 = ((k + 1 == i ? emax : 0.0) - am[k + 1]) * f;
+      } else {
+        if (k < n) x0 = y[k];
+        if (k + 1 < n) x1 = y[k + 1];
+      }
+      if (k == i) tr += x0;
+      if (k + 1 == i) tr += x1;
+    }
+    const uint64_t b0 = (uint64_t)__double_as_longlong(x0), b1 = (uint64_t)__double_as_longlong(x1);
+    over = over || ((b0 >> 52) & 0x7FF) >= (uint64_t)(1023 + SP2_E) ||
+           ((b1 >> 52) & 0x7FF) >= (uint64_t)(1023 + SP2_E);
+    const uint64_t Y0 = fixed_bits(b0, SP2_E), Y1 = fixed_bits(b1, SP2_E);
+    sq.add(Y0);
+    sq.add(Y1);
+    const uint32_t signs = ((uint32_t)(b0 >> 63) << 15) | ((uint32_t)(b1 >> 63) << 31);
+    const size_t off = (size_t)slice_off(i, k, nlb);
+#pragma unroll
+    for (int pp = 0; pp < 8; ++pp) {
+      const uint32_t w = __byte_perm(__float_as_uint(slice_value(slice7(Y0, pp), pp)),
+                                     __float_as_uint(slice_value(slice7(Y1, pp), pp)), 0x7632);
+      *reinterpret_cast<uint32_t*>(q.img + off + pp * plane) = w | signs;
     }
   }
+  if (init && lane == 0) q.iexp[i] = SP2_E;
+  // block partial sums: warp trees, then the warps in order
+  __shared__ double s_tr[8];
+  __shared__ unsigned long long s_lo[8], s_hi[8];
+  unsigned long long flo, fhi;
+  sq.value(flo, fhi);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    const unsigned long long b = __shfl_xor_sync(0xffffffffu, mb, o);
-    mb = b > mb ? b : mb;
+    tr += __shfl_xor_sync(0xffffffffu, tr, o);
+    add128(flo, fhi, __shfl_xor_sync(0xffffffffu, flo, o), __shfl_xor_sync(0xffffffffu, fhi, o));
   }
-  // e = ilogb(max) + 1: the biased exponent field minus 1022 for a normal maximum
-  const int mexp = (int)(mb >> 52);
-  const int ei = mb == 0ull ? 0 : mexp > 0 ? mexp - 1022 : ilogb(__longlong_as_double((long long)mb)) + 1;
-  if (lane == 0) q.iexp[i] = ei;
-  const int nkc = (n + PP_KC - 1) / PP_KC, nlb = lp / 64, lb = i >> 6, li = i & 63;
-  // this lane's element of every k chunk: position c = lane & 7 of 16-byte chunk g = lane >> 3
-  const size_t lane_off =
-      (size_t)li * 32 + (size_t)(((lane >> 3) ^ ((li >> 1) & 3)) << 3) + (size_t)(lane & 7);
-  const double* y = q.Y + (size_t)i * n;
-  for (int kc = 0; kc < nkc; ++kc) {
-    const int k = kc * PP_KC + lane;
-    const double x = (i < n && k < n) ? y[k] : 0.0;  // this lane wrote y[k] above
-    const uint64_t bits = (uint64_t)__double_as_longlong(x);
-    const uint32_t sign = (uint32_t)(bits >> 63);
-    const int ex = (int)((bits >> 52) & 0x7FF);
-    uint64_t Y = 0;
-    if (ex != 0) {  // zero and subnormals give zero slices
-      const uint64_t m = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-      const int sh = ex - ei - 1019;  // Y = |x| 2^(56 - e) < 2^56
-      if (sh >= 0) Y = m << sh;
-      else if (sh > -64) Y = m >> (-sh);
-    }
-#pragma unroll
-    for (int p = 0; p < 8; ++p) {
-      const uint32_t sb = slice_bits((uint32_t)(Y >> (49 - 7 * p)) & 0x7Fu, p, sign);
-      const uint32_t hi = __shfl_xor_sync(0xffffffffu, sb, 1);
-      if (!(lane & 1))  // even k in the low half, odd k in the high half of a 32-bit word
-        *reinterpret_cast<uint32_t*>(q.img + (((size_t)kc * 8 + p) * nlb + lb) * 2048 +
-                                     lane_off) = sb | (hi << 16);
-    }
+  over = __any_sync(0xffffffffu, over ? 1 : 0) != 0;
+  const int w = threadIdx.x >> 5;
+  if (lane == 0) {
+    s_tr[w] = over ? __longlong_as_double(0x7FF8000000000000ll) : tr;
+    s_lo[w] = flo;
+    s_hi[w] = fhi;
   }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    unsigned long long lo = 0ull, hi = 0ull;
+    for (int u = 0; u < 8; ++u) {
+      t += s_tr[u];
+      add128(lo, hi, s_lo[u], s_hi[u]);
+    }
+    unsigned long long* pt = q.sp2p + 3 * blockIdx.x;
+    pt[0] = (unsigned long long)__double_as_longlong(t);
+    pt[1] = lo;
+    pt[2] = hi;
+  }
+  sp2_last_decides(q, lp / 8);
 }
 
 // ---- batched GEMM sites on the pipe (projection buckets): the rows of op(A) go into img,
@@ -751,19 +837,20 @@ void pipe_site_b(const BatchLaunch& b, int site) {
   prof_kend(KS_PIPE, tk, b.s);
 }
 
-// the new iterate with its exponents and slice image (init: D0 from A), for every listed
-// molecule still iterating
-void sp2_step_b(const BatchLaunch& b, bool init) {
+// the slice image of the iterate and the next decision for every listed molecule still
+// iterating (init: D0 from A and the Gershgorin bounds into Y first)
+void sp2_slice_b(const BatchLaunch& b, bool init) {
   if (!b.count) return;
   const int lp = pimage_lines(b.nao_max);
   const int tk = prof_kbegin(b.s);
   ++g_kernel_launches;
-  kb_sp2_step<<<dim3(lp / 8, 1, b.count), 256, 0, b.s>>>(b.mp, b.list, init ? 1 : 0);
+  kb_sp2_slice<<<dim3(lp / 8, 1, b.count), 256, 0, b.s>>>(b.mp, b.list, init ? 1 : 0);
   prof_kend(KS_PIPE_PREP, tk, b.s);
 }
 
-// one squaring of the batched spectral projection: C = Y Y on the tensor cores from the slice
-// image that sp2_step_b wrote, for every listed molecule still iterating
+// the squaring of a projection step for every listed molecule still iterating: D^2 on the
+// tensor cores from the iterate's slice image, and the next iterate (D^2 or 2D - D^2 as decided)
+// over D in Y
 void sp2_square_b(const BatchLaunch& b) {
   if (!b.count) return;
   static bool attr = false;
@@ -786,6 +873,7 @@ size_t pimage_bytes(int lines, int K) {
   return lp * kp * 8 * sizeof(uint16_t);
 }
 int pimage_lines(int lines) { return ((lines + PP_M - 1) / PP_M) * PP_M; }
+int sp2_slot_count(int n) { return sp2_slots(n); }
 
 // slice image of a matrix: line i, position k is M[i + k ld] (kcontig = 0: the rows of M) or
 // M[k + i ld] (kcontig = 1: the columns of M); img holds pimage_bytes(lines, K) bytes and e

@@ -15,10 +15,11 @@
 //
 // Per molecule and SCF iteration the eigensolver's tridiagonalisation, eigenvalues, inverse
 // iteration and back-transformation (FP64 cores) become ~25 symmetric squarings on the BF16
-// tensor cores with FP64-accurate operand splitting (ozaki_pipe.cu: kb_opipe_sq squares from
-// the slice image, and its last CTA per molecule takes the step's decision; kb_sp2_step forms
-// the next iterate, its exponents and its image in one pass over the matrix, so a step is two
-// launches).  Every
+// tensor cores with FP64-accurate operand splitting (ozaki_pipe.cu: kb_opipe_sq squares the
+// iterate from its slice image and writes the next iterate over it in the epilogue; kb_sp2_slice
+// writes the new iterate's slice image with one exponent for every line, sums its trace and,
+// exactly in integers, tr D^2 = sum of its squared elements, and its last block per molecule
+// takes the next decision, so a step is two launches and the decision needs no product).  Every
 // molecule of a size bucket iterates in lockstep; each decides its own step on the device and
 // stops on its own (its later launches return at once).  The host launches a step budget per
 // bucket (the most steps any of its molecules took in the previous SCF iteration plus a margin);
@@ -117,10 +118,10 @@ void sp2_density_b(const BatchLaunch& b, int steps) {
   pipe_site_b(b, GS_XTT);  // A = X^T T1
   ++g_kernel_launches;
   kb_sp2_start<<<dim3(1, 1, b.count), 256, 0, b.s>>>(b.mp, b.list);
-  sp2_step_b(b, true);  // D0 and its slice image
+  sp2_slice_b(b, true);  // D0, its slice image and the first decision
   for (int k = 0; k < steps; ++k) {
-    sp2_square_b(b);       // C = D^2, and the step's decision by the last CTA of each molecule
-    sp2_step_b(b, false);  // the update and its slice image for the next squaring
+    sp2_square_b(b);         // D^2 and the next iterate over D
+    sp2_slice_b(b, false);  // its slice image and the next decision
   }
   ++g_kernel_launches;
   kb_sp2_finish<<<dim3(1, 1, b.count), 32, 0, b.s>>>(b.mp, b.list);
