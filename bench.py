@@ -552,8 +552,9 @@ def run_batch(args):
                      "fp64_equivalent_tflops": round(pipe_flops_s / (t_pipe / 1000.0) / 1e12, 4),
                      "ms_per_call": round(t_pipe, 3), "launches_per_call": c_pipe,
                      "ms_per_launch": round(t_pipe / c_pipe, 4) if c_pipe else None,
-                     "operands": {"kernels": "kb_sp2_step, kb_pexp_site, kb_psplit_site "
-                                             "(HBM-bound: new iterate, exponents, slice images)",
+                     "operands": {"kernels": "kb_sp2_slice, kb_pexp_site, kb_psplit_site "
+                                             "(HBM-bound: slice images, exponents, partial "
+                                             "sums)",
                                   "ms_per_call": round(t_prep, 3), "launches_per_call": c_prep}}
     if pipe_roof is not None and t_pipe >= t_tri:
         roofline, other = pipe_roof, tri_roof

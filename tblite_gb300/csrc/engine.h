@@ -521,11 +521,14 @@ void sp2_gap_b(const BatchLaunch& b);
 void sp2_weighted_b(const BatchLaunch& b);
 void sp2_pipe_check_b(const BatchLaunch& b);  // flag -5 for a molecule whose pipe wait ran out
 // ozaki_pipe.cu: the squaring of a projection step of the iterating molecules (D^2 on the
-// tensor cores from the slice image; the next iterate D^2 or 2D - D^2 over D in Y)
+// tensor cores from the slice image; the next iterate D^2 or 2D - D^2 over D in Y, as signed
+// 64-bit fixed point in units of 2^-55 during the projection)
 void sp2_square_b(const BatchLaunch& b);
 // ozaki_pipe.cu: the slice image of the iterate in Y with its exact partial sums, and the next
 // decision (init: D0 from A and the Gershgorin bounds into Y first)
 void sp2_slice_b(const BatchLaunch& b, bool init);
+// ozaki_pipe.cu: the converged iterate (fixed point during the projection) back to FP64 in Y
+void sp2_unfix_b(const BatchLaunch& b);
 int sp2_slot_count(int n);  // partial-sum slots of a molecule of n orbitals (3 words each)
 constexpr int SP2_MIN_NAO = 128;   // smallest orbital count that takes the projection
 constexpr int SP2_MAX_STEPS = 64;  // squarings per projection at most

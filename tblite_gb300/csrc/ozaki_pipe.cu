@@ -28,6 +28,7 @@
 // write each element also to its mirror position.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <stdexcept>
 #include <string>
@@ -228,12 +229,20 @@ struct PipeArgs {
   // a projection step applied in the epilogue: C <- 2 C - product (the old C read first); with
   // C the iterate D this turns D^2 into 2D - D^2 in place
   int sub2;
+  // C holds signed 64-bit fixed-point values in units of 2^-SP2_FRAC instead of doubles (the
+  // projection iterate, |D_ij| <= 1): the epilogue needs no FP64 operation
+  int fixed;
 };
 
 // line exponent of every projection iterate: the spectrum of D stays in [0, 1], so every element
-// has |x| <= 1 < 2^SP2_E and the slices hold x to an absolute 2^-55 (the iterate's own rounding
-// is 2^-53 relative to its O(1) diagonal); an element at or above 2^SP2_E stops the molecule
+// has |x| <= 1 < 2^SP2_E and the slices hold x to an absolute 2^-55 (an FP64 iterate's own
+// rounding is 2^-53 relative to its O(1) diagonal); an element at or above 2^SP2_E stops the
+// molecule.  During the projection the iterate lives in Y as signed 64-bit integers W = x 2^55
+// (SP2_FRAC fractional bits): |W| < 2^56, and the magnitude's two 28-bit halves are the slices'
+// source directly.
 constexpr int SP2_E = 1;
+constexpr int SP2_FRAC = 56 - SP2_E;
+constexpr long long SP2_BAD = (long long)0x8000000000000000ull;  // an element out of range
 
 __device__ __forceinline__ int slice_off(int line, int k, int nlb) {
   // image[k chunk][slice][line block][64 lines x 32 k], 16-byte groups swizzled (slice 0)
@@ -267,7 +276,9 @@ __device__ __forceinline__ double tile_value(long long T, uint32_t v6, uint32_t 
   return ldexp(sum, sc - 35);  // subnormal or out-of-range result: the general path
 }
 
-// one 128 x 64 output tile (number b in the grouped order) of the product a
+// one 128 x 64 output tile (number b in the grouped order) of the product a (FIXED: the
+// projection's fixed-point epilogue, a.fixed set)
+template <bool FIXED = false>
 __device__ __forceinline__ void opipe_tile(const PipeArgs& a, int b) {
   // ---- tile of this CTA: groups of PP_GROUP row blocks, column blocks inside a group
   const int mt = (a.M + PP_M - 1) / PP_M, nt = (a.N + PP_N - 1) / PP_N;
@@ -459,7 +470,44 @@ __device__ __forceinline__ void opipe_tile(const PipeArgs& a, int b) {
         uint32_t v6[16], v7[16];
         tmem_ld16(lane_base + (uint32_t)(6 * PP_N + 16 * h), v6);
         tmem_ld16(lane_base + (uint32_t)(7 * PP_N + 16 * h), v7);
-        if (i < a.M) {
+        if constexpr (FIXED) {
+          if (i < a.M) {
+          // the projection iterate in fixed point: the product is (T + F 2^35) 2^(sc - 35) with
+          // sc = 2 SP2_E - 14, i.e. W = T 2^8 + F 2^43 in units of 2^-55 (F rounded to an
+          // integer there: an absolute 2^-56); |T| < 2^54 keeps T 2^8 exact, else the element is
+          // marked out of range
+          long long* W = reinterpret_cast<long long*>(a.C);
+          static_assert(2 * SP2_E - 14 - 35 + SP2_FRAC == 8, "fixed-point scale of the product");
+#pragma unroll
+          for (int t8 = 0; t8 < 16; t8 += 8) {
+            long long old[8];
+#pragma unroll
+            for (int t = 0; t < 8; ++t) {
+              const int j = j0 + 32 * half + 16 * h + t8 + t;
+              old[t] = (a.sub2 && j < a.N && i >= j) ? W[i + (size_t)j * a.ldc] : 0ll;
+            }
+#pragma unroll
+            for (int t = 0; t < 8; ++t) {
+              const int j = j0 + 32 * half + 16 * h + t8 + t;
+              if (j < a.N && i >= j) {
+                const long long tv = T[16 * h + t8 + t];
+                const float ff = (__uint_as_float(v6[t8 + t]) + __uint_as_float(v7[t8 + t])) *
+                                 0x1p43f;
+                // unsigned arithmetic: wrap-around instead of undefined overflow, and the
+                // out-of-range cases are replaced below
+                unsigned long long w =
+                    ((unsigned long long)tv << 8) + (unsigned long long)(long long)__float2int_rn(ff);
+                if (a.sub2) w = 2ull * (unsigned long long)old[t] - w;
+                if (tv >= (1ll << 54) || tv <= -(1ll << 54) || fabsf(ff) >= 0x1p30f ||
+                    old[t] == SP2_BAD)
+                  w = (unsigned long long)SP2_BAD;
+                W[i + (size_t)j * a.ldc] = (long long)w;
+                if (i != j) W[j + (size_t)i * a.ldc] = (long long)w;
+              }
+            }
+          }
+          }
+        } else if (i < a.M) {
 #pragma unroll
           for (int t8 = 0; t8 < 16; t8 += 8) {
             // the old elements of C first (sub2), so their loads are in flight together
@@ -517,29 +565,33 @@ __host__ __device__ __forceinline__ int sp2_slots(int n) {
 // Niklasson 2016, or reaches the rounding floor) and the update D^2 or 2D - D^2 whose trace is
 // closer to the occupied count (Niklasson 2002).  State: sp2i[0] converged, [1] steps taken,
 // [2] update of the next step (1 square, 0 2D - D^2, -1 none), [3] pipeline status; sp2s[2..4]
-// the last three idempotency errors.  A partial sum that is not a number (an element outside
-// the fixed-exponent range, or not finite) sends the molecule away.
+// the last three idempotency errors, [4] set by a block that met an element outside the
+// fixed-point range (the molecule leaves).
 __device__ void sp2_decide(const MolPtrs& q, int nslots) {
-  double tx = 0.0;
-  unsigned long long lo = 0ull, hi = 0ull;
+  // tr D 2^55 as a signed 128-bit sum of the blocks' int64 sums, tr D^2 2^110 unsigned
+  unsigned long long tlo = 0ull, slo = 0ull, shi = 0ull;
+  long long thi = 0;
   for (int t = 0; t < nslots; ++t) {
     const unsigned long long* pt = q.sp2p + 3 * t;
-    tx += __longlong_as_double((long long)__ldcg(pt));
+    const long long tv = (long long)__ldcg(pt);
+    tlo += (unsigned long long)tv;
+    thi += (tv < 0 ? -1 : 0) + (tlo < (unsigned long long)tv ? 1 : 0);
     const unsigned long long l = __ldcg(pt + 1);
-    lo += l;
-    hi += __ldcg(pt + 2) + (lo < l ? 1ull : 0ull);
+    slo += l;
+    shi += __ldcg(pt + 2) + (slo < l ? 1ull : 0ull);
   }
-  const double tx2 = ((double)hi * 0x1p64 + (double)lo) * 0x1p-110;
+  const double tx = ((double)thi * 0x1p64 + (double)tlo) * 0x1p-55;
+  const double tx2 = ((double)shi * 0x1p64 + (double)slo) * 0x1p-110;
   const int n = q.m.nao;
   if (q.sp2i[3] != 0) {  // a tensor-core wait ran out: the molecule takes the one-molecule path
     *q.flag = -5;
     return;
   }
-  const double e = tx - tx2;
-  if (!(e == e)) {
+  if (q.sp2i[4] != 0) {  // an element outside the fixed-point range
     *q.flag = -6;
     return;
   }
+  const double e = tx - tx2;
   const int k = q.sp2i[1];
   const double ekm2 = q.sp2s[3];  // after the shift below: e(k-2)
   q.sp2s[2] = q.sp2s[3];
@@ -587,11 +639,12 @@ __global__ void __launch_bounds__(PP_THREADS, 1) kb_opipe_sq(const MolPtrs* __re
   a.nlbA = a.nlbB = lines_padded(n) / 64;
   a.M = a.N = n;
   a.nkc = (n + PP_KC - 1) / PP_KC;
-  a.C = q.Y;  // D_(k+1) over D_k
+  a.C = q.Y;  // D_(k+1) over D_k, fixed point
   a.ldc = n;
   a.sym = 1;
   a.status = q.sp2i + 3;
   a.sub2 = q.sp2i[2] == 0 ? 1 : 0;
+  a.fixed = 1;
   if (threadIdx.x == 0) {  // the tile's useful area (the upper tiles of the symmetric product exit)
     const int mt = (n + PP_M - 1) / PP_M, nt = (n + PP_N - 1) / PP_N;
     const int b = blockIdx.x, gid = b / (PP_GROUP * nt), first = gid * PP_GROUP;
@@ -601,25 +654,28 @@ __global__ void __launch_bounds__(PP_THREADS, 1) kb_opipe_sq(const MolPtrs* __re
       atomicAdd(&g_pipe_batch_flops, 2ull * (unsigned long long)min(PP_M, n - i0) *
                                          (unsigned long long)min(PP_N, n - j0) * (unsigned)n);
   }
-  opipe_tile(a, blockIdx.x);
+  opipe_tile<true>(a, blockIdx.x);
 }
 
 // ---- the slice image of the iterate and the decision: each warp owns one line i of D (column i
-// in memory, which equals row i); at the start (init) the line is D0 = (emax I - A) /
-// (emax - emin), written to Y, else it is read from Y.  Its slices (exponent SP2_E) go to img,
-// and the line's diagonal element and the exact squares of its elements to the block's partial
-// sums; the last block of the molecule takes the decision.  A lane holds two neighbouring
+// in memory, which equals row i), held in Y as fixed-point integers W = x 2^55; at the start
+// (init) the line is D0 = (emax I - A) / (emax - emin), computed in FP64 and written to Y in
+// fixed point, else it is read from Y.  Its slices (exponent SP2_E) go to img, and the line's
+// diagonal element and the exact squares of its elements to the block's partial sums (exact
+// integers); the last block of the molecule takes the decision.  A lane holds two neighbouring
 // elements k, k + 1 of a 64-element segment (coalesced loads), so each slice plane gets one
 // 32-bit word per lane.  Padding lines and positions get zero slices.
 //
-// Slice p of a fixed-point value Y < 2^56 is the 7-bit field a = (Y >> (49 - 7p)) & 127; its
+// Slice p of a fixed-point value Y < 2^56 is the 7-bit field a = (Y >> (49 - 7p)) & 127 (read
+// from the 28-bit half that holds it); its
 // BF16 value a 2^-7p is read off the float whose exponent field is 150 - 7p and mantissa field
 // a: that float is 2^(23 - 7p) + a 2^-7p exactly, and subtracting 2^(23 - 7p) leaves a 2^-7p
 // (exact: at most 7 significant bits), whose low 16 bits are zero.  The byte permute packs the
 // high halves of the two elements' floats into one word, and the signs go in with one OR (a
 // zero slice of a negative element becomes -0, which adds nothing to a product).
-__device__ __forceinline__ uint32_t slice7(uint64_t Y, int p) {
-  return (uint32_t)(Y >> (49 - 7 * p)) & 0x7Fu;
+// slice p (0..7) of Y: the 7-bit field (Y >> (49 - 7p)) & 127, from the half that holds it
+__device__ __forceinline__ uint32_t slice7(uint32_t h, uint32_t l, int p) {
+  return ((p < 4 ? h : l) >> (21 - 7 * (p & 3))) & 0x7Fu;
 }
 __device__ __forceinline__ float slice_value(uint32_t a, int p) {
   return __uint_as_float(((uint32_t)(150 - 7 * p) << 23) | a) -
@@ -629,8 +685,7 @@ __device__ __forceinline__ float slice_value(uint32_t a, int p) {
 // 2 h l 2^28 + l^2 (every partial product below 2^56, so per-lane sums of up to 256 stay exact)
 struct Sq3 {
   unsigned long long hh = 0ull, hl = 0ull, ll = 0ull;
-  __device__ __forceinline__ void add(uint64_t Y) {
-    const uint32_t h = (uint32_t)(Y >> 28), l = (uint32_t)Y & 0xFFFFFFFu;
+  __device__ __forceinline__ void add(uint32_t h, uint32_t l) {
     hh += (unsigned long long)h * h;
     hl += (unsigned long long)h * l;
     ll += (unsigned long long)l * l;
@@ -662,74 +717,101 @@ __global__ void __launch_bounds__(256) kb_sp2_slice(const MolPtrs* __restrict__ 
   const double emax = init ? q.sp2s[1] : 0.0, f = init ? 1.0 / (emax - q.sp2s[0]) : 0.0;
   const int nkc = (n + PP_KC - 1) / PP_KC, nlb = lp / 64;
   const size_t plane = (size_t)nlb * 2048;
-  double tr = 0.0;
+  long long dw = 0;  // the line's diagonal element (an integer select per element)
   Sq3 sq;
   bool over = false;
   const double* __restrict__ am = q.A + (size_t)i * n;
-  double* __restrict__ y = q.Y + (size_t)i * n;
+  long long* __restrict__ y = reinterpret_cast<long long*>(q.Y) + (size_t)i * n;
   const bool real = i < n;
   for (int seg = 0; seg * 64 < nkc * PP_KC; ++seg) {
     const int k = seg * 64 + 2 * lane;
     if ((k >> 5) >= nkc) continue;  // the last segment may hold one chunk only
-    double x0 = 0.0, x1 = 0.0;
+    long long w0 = 0, w1 = 0;
     if (real) {
-      if (init) {
-        if (k < n) y[k] = x0 = ((k == i ? emax : 0.0) - am[k]) * f;
-        if (k + 1 < n) y[k + 1] = x1 = ((k + 1 == i ? emax : 0.0) - am[k + 1]) * f;
+      if (init) {  // D0 in FP64, then to fixed point (once per projection)
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+          if (k + e >= n) continue;
+          const double x = ((k + e == i ? emax : 0.0) - am[k + e]) * f;
+          const uint64_t bits = (uint64_t)__double_as_longlong(x);
+          const long long m = (long long)fixed_bits(bits, SP2_E);
+          const long long w =
+              ((bits >> 52) & 0x7FF) >= (uint64_t)(1023 + SP2_E) ? SP2_BAD : ((bits >> 63) ? -m : m);
+          y[k + e] = w;
+          (e ? w1 : w0) = w;
+        }
       } else {
-        if (k < n) x0 = y[k];
-        if (k + 1 < n) x1 = y[k + 1];
+        if (k < n) w0 = y[k];
+        if (k + 1 < n) w1 = y[k + 1];
       }
-      if (k == i) tr += x0;
-      if (k + 1 == i) tr += x1;
     }
-    const uint64_t b0 = (uint64_t)__double_as_longlong(x0), b1 = (uint64_t)__double_as_longlong(x1);
-    over = over || ((b0 >> 52) & 0x7FF) >= (uint64_t)(1023 + SP2_E) ||
-           ((b1 >> 52) & 0x7FF) >= (uint64_t)(1023 + SP2_E);
-    const uint64_t Y0 = fixed_bits(b0, SP2_E), Y1 = fixed_bits(b1, SP2_E);
-    sq.add(Y0);
-    sq.add(Y1);
-    const uint32_t signs = ((uint32_t)(b0 >> 63) << 15) | ((uint32_t)(b1 >> 63) << 31);
+    dw = k == i ? w0 : (k + 1 == i ? w1 : dw);
+    // magnitudes (an out-of-range element, including the marker, counts as zero and stops the
+    // molecule) and their 28-bit halves
+    const unsigned long long a0 = w0 < 0 ? 0ull - (unsigned long long)w0 : (unsigned long long)w0;
+    const unsigned long long a1 = w1 < 0 ? 0ull - (unsigned long long)w1 : (unsigned long long)w1;
+    const bool bad0 = a0 >= (1ull << 56), bad1 = a1 >= (1ull << 56);
+    over = over || bad0 || bad1;
+    const unsigned long long m0 = bad0 ? 0ull : a0, m1 = bad1 ? 0ull : a1;
+    const uint32_t h0 = (uint32_t)(m0 >> 28), l0 = (uint32_t)m0 & 0xFFFFFFFu;
+    const uint32_t h1 = (uint32_t)(m1 >> 28), l1 = (uint32_t)m1 & 0xFFFFFFFu;
+    sq.add(h0, l0);
+    sq.add(h1, l1);
+    const uint32_t signs = (w0 < 0 ? 0x8000u : 0u) | (w1 < 0 ? 0x80000000u : 0u);
     const size_t off = (size_t)slice_off(i, k, nlb);
 #pragma unroll
     for (int pp = 0; pp < 8; ++pp) {
-      const uint32_t w = __byte_perm(__float_as_uint(slice_value(slice7(Y0, pp), pp)),
-                                     __float_as_uint(slice_value(slice7(Y1, pp), pp)), 0x7632);
+      const uint32_t w = __byte_perm(__float_as_uint(slice_value(slice7(h0, l0, pp), pp)),
+                                     __float_as_uint(slice_value(slice7(h1, l1, pp), pp)), 0x7632);
       *reinterpret_cast<uint32_t*>(q.img + off + pp * plane) = w | signs;
     }
   }
   if (init && lane == 0) q.iexp[i] = SP2_E;
-  // block partial sums: warp trees, then the warps in order
-  __shared__ double s_tr[8];
+  // block partial sums (exact integers): warp trees, then the warps in order
+  __shared__ long long s_tr[8];
   __shared__ unsigned long long s_lo[8], s_hi[8];
   unsigned long long flo, fhi;
   sq.value(flo, fhi);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    tr += __shfl_xor_sync(0xffffffffu, tr, o);
+    dw += __shfl_xor_sync(0xffffffffu, dw, o);  // one lane holds the diagonal, the others 0
     add128(flo, fhi, __shfl_xor_sync(0xffffffffu, flo, o), __shfl_xor_sync(0xffffffffu, fhi, o));
   }
   over = __any_sync(0xffffffffu, over ? 1 : 0) != 0;
+  if (over && lane == 0) q.sp2i[4] = 1;
   const int w = threadIdx.x >> 5;
   if (lane == 0) {
-    s_tr[w] = over ? __longlong_as_double(0x7FF8000000000000ll) : tr;
+    s_tr[w] = dw;
     s_lo[w] = flo;
     s_hi[w] = fhi;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    double t = 0.0;
+    long long t = 0;  // 8 lines of |W| < 2^56: no overflow
     unsigned long long lo = 0ull, hi = 0ull;
     for (int u = 0; u < 8; ++u) {
       t += s_tr[u];
       add128(lo, hi, s_lo[u], s_hi[u]);
     }
     unsigned long long* pt = q.sp2p + 3 * blockIdx.x;
-    pt[0] = (unsigned long long)__double_as_longlong(t);
+    pt[0] = (unsigned long long)t;
     pt[1] = lo;
     pt[2] = hi;
   }
   sp2_last_decides(q, lp / 8);
+}
+
+// after a projection: the converged iterate from fixed point back to FP64 in place (the products
+// P = 2 X D X^T read it as doubles); every listed molecule of the projection bucket
+__global__ void __launch_bounds__(256) kb_sp2_unfix(const MolPtrs* __restrict__ mp,
+                                                    const int* __restrict__ list) {
+  const MolPtrs& q = mp[list[blockIdx.z]];
+  if (*q.flag < 0) return;
+  const size_t nn = (size_t)q.m.nao * q.m.nao;
+  long long* w = reinterpret_cast<long long*>(q.Y);
+  for (size_t e = (size_t)blockIdx.x * 256 + threadIdx.x; e < nn; e += (size_t)gridDim.x * 256)
+    q.Y[e] = w[e] == SP2_BAD ? __longlong_as_double(0x7FF8000000000000ll)
+                             : (double)w[e] * 0x1p-55;
 }
 
 // ---- batched GEMM sites on the pipe (projection buckets): the rows of op(A) go into img,
@@ -846,6 +928,15 @@ void sp2_slice_b(const BatchLaunch& b, bool init) {
   ++g_kernel_launches;
   kb_sp2_slice<<<dim3(lp / 8, 1, b.count), 256, 0, b.s>>>(b.mp, b.list, init ? 1 : 0);
   prof_kend(KS_PIPE_PREP, tk, b.s);
+}
+
+// the projection iterate back to FP64 for every listed molecule (after the last step)
+void sp2_unfix_b(const BatchLaunch& b) {
+  if (!b.count) return;
+  const size_t nn = (size_t)b.nao_max * b.nao_max;
+  const int blocks = (int)std::min<size_t>((nn + 1023) / 1024, 4096);
+  ++g_kernel_launches;
+  kb_sp2_unfix<<<dim3(blocks, 1, b.count), 256, 0, b.s>>>(b.mp, b.list);
 }
 
 // the squaring of a projection step for every listed molecule still iterating: D^2 on the

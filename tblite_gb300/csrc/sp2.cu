@@ -83,7 +83,8 @@ __global__ void __launch_bounds__(256) kb_sp2_start(BARGS) {
     q.sp2i[0] = 0;   // converged
     q.sp2i[1] = 0;   // steps taken
     q.sp2i[2] = -1;  // update of the current step: 1 square, 0 2D - D^2, -1 none
-    q.sp2i[5] = 0;   // tiles of the current squaring finished (the last one decides)
+    q.sp2i[4] = 0;   // an element outside the fixed-point range
+    q.sp2i[5] = 0;   // blocks of the current slice pass finished (the last one decides)
     // sp2i[3]: tensor-core pipeline status, set by any pipelined product of the molecule; it
     // starts zeroed with the batch and is never cleared (a failure sends the molecule away)
     q.scal[0] = 0.0;  // no Fermi entropy: the occupations are 0/2 (checked after the SCF)
@@ -125,6 +126,7 @@ void sp2_density_b(const BatchLaunch& b, int steps) {
   }
   ++g_kernel_launches;
   kb_sp2_finish<<<dim3(1, 1, b.count), 32, 0, b.s>>>(b.mp, b.list);
+  sp2_unfix_b(b);          // D from fixed point to FP64
   pipe_site_b(b, GS_XD);   // T1 = 2 X D
   pipe_site_b(b, GS_PXT);  // P = T1 X^T
 }
