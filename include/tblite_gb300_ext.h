@@ -51,8 +51,8 @@ int tblite_gb300_batch_last_projected(void);
  * diagonalisation, -1 the one-molecule path; returns the number of molecules recorded */
 int tblite_gb300_batch_last_modes(int* modes, int nmol);
 /* Autotuner of the batch schedule: coordinate descent over CUDA graphs (kept, or switched off;
- * never switched on against tblite_gb300_set_batch_graphs), the projection threshold (128, 144,
- * 157, 176, 224 orbitals or off), the bucket cut (3/4, 2/3, 4/5 of the largest orbital count), the CTAs
+ * never switched on against tblite_gb300_set_batch_graphs), the projection threshold (96, 112,
+ * 128, 144, 157, 176, 224 orbitals or off), the bucket cut (3/4, 2/3, 4/5 of the largest orbital count), the CTAs
  * per SM of the cluster tridiagonalisation (1, 2), the small-bucket tridiagonalisation (full
  * storage or packed) and the side streams (4, 8, 16), each candidate
  * timed as the wall time of a batch call (best of three) on a fixed pseudo-random sample of

@@ -1374,7 +1374,7 @@ extern "C" int tblite_gb300_batch_autotune(tblite_context ctx, int nmol,
   // budget changes, which can cost more than the launches it saves
   int graphs = g_batch_graphs ? 1 : 0;
   if (graphs) try_values([](int v) { g_batch_graphs = v != 0; }, {0}, graphs);
-  try_values([](int v) { g_sp2_min_nao = v; }, {128, 144, 157, 176, 224, 100000}, sp2);
+  try_values([](int v) { g_sp2_min_nao = v; }, {96, 112, 128, 144, 157, 176, 224, 100000}, sp2);
   try_values([](int v) { g_cut_num = v / 10; g_cut_den = v % 10; }, {34, 23, 45}, cut);
   try_values([](int v) { tb::set_tridiag_ctas_per_sm(v); }, {1, 2}, ctas);
   int small = tb::get_tridiag_small();

@@ -116,22 +116,34 @@ __device__ __forceinline__ uint32_t slice_bits(uint32_t a, int p, uint32_t sign)
   return a ? ((u >> 16) | (sign << 15)) : 0u;
 }
 
+// |x| as bits: for non-negative doubles the unsigned order of the bit patterns is the numeric
+// order, so line maxima are integer maxima (no FP64 instruction, which this GPU issues at 1/64
+// of the FP32 rate); e = ilogb(max) + 1 is the biased exponent field minus 1022 for a normal
+// maximum
+__device__ __forceinline__ unsigned long long abs_bits(double x) {
+  return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+}
+__device__ __forceinline__ int exp_of_max(unsigned long long mb) {
+  const int mexp = (int)(mb >> 52);
+  return mb == 0ull ? 0 : mexp > 0 ? mexp - 1022 : ilogb(__longlong_as_double((long long)mb)) + 1;
+}
+
 // ---- exponents: e = ilogb(max |x|) + 1 of every line ------------------------------------------
 // lines contiguous in memory (element (i, k) at M[i + k ld]): 32 lines per block, the 8 warps
 // take every 8th k (coalesced 256-byte rows), then a shared-memory reduction
 __device__ __forceinline__ void pexp_rows_dev(const double* __restrict__ M, int ld, int lines,
                                               int K, int Lp, int* e, int blk) {
-  __shared__ double part[8][33];
+  __shared__ unsigned long long part[8][33];
   const int li = threadIdx.x & 31, kg = threadIdx.x >> 5;
   const int i = blk * 32 + li;
-  double mx = 0.0;
+  unsigned long long mx = 0ull;
   if (i < lines)
-    for (int k = kg; k < K; k += 8) mx = fmax(mx, fabs(M[i + (size_t)k * ld]));
+    for (int k = kg; k < K; k += 8) mx = max(mx, abs_bits(M[i + (size_t)k * ld]));
   part[kg][li] = mx;
   __syncthreads();
   if (kg == 0 && i < Lp) {
-    for (int g = 1; g < 8; ++g) mx = fmax(mx, part[g][li]);
-    e[i] = mx > 0.0 ? ilogb(mx) + 1 : 0;
+    for (int g = 1; g < 8; ++g) mx = max(mx, part[g][li]);
+    e[i] = exp_of_max(mx);
   }
 }
 __global__ void __launch_bounds__(256) k_pexp_rows(const double* __restrict__ M, int ld,
@@ -143,12 +155,12 @@ __global__ void k_pexp_cols(const double* __restrict__ M, int ld, int lines, int
                             int* e) {
   const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (i >= Lp) return;
-  double mx = 0.0;
+  unsigned long long mx = 0ull;
   if (i < lines)
-    for (int k = lane; k < K; k += 32) mx = fmax(mx, fabs(M[k + (size_t)i * ld]));
+    for (int k = lane; k < K; k += 32) mx = max(mx, abs_bits(M[k + (size_t)i * ld]));
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  if (lane == 0) e[i] = mx > 0.0 ? ilogb(mx) + 1 : 0;
+  for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if (lane == 0) e[i] = exp_of_max(mx);
 }
 
 // ---- slice image: one block per (64 lines, 32 k); the FP64 tile goes through shared memory so
@@ -841,12 +853,12 @@ __global__ void __launch_bounds__(256) kb_pexp_site(const MolPtrs* __restrict__ 
   }
   const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (i >= lp) return;
-  double mx = 0.0;
+  unsigned long long mx = 0ull;
   if (i < L.lines)
-    for (int k = lane; k < L.K; k += 32) mx = fmax(mx, fabs(L.M[k + (size_t)i * L.ld]));
+    for (int k = lane; k < L.K; k += 32) mx = max(mx, abs_bits(L.M[k + (size_t)i * L.ld]));
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  if (lane == 0) e[i] = mx > 0.0 ? ilogb(mx) + 1 : 0;
+  for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if (lane == 0) e[i] = exp_of_max(mx);
 }
 __global__ void __launch_bounds__(256) kb_psplit_site(const MolPtrs* __restrict__ mp,
                                                       const int* __restrict__ list, int site,
