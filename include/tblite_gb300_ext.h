@@ -38,7 +38,8 @@ int tblite_gb300_batch_singlepoint(tblite_context ctx, int nmol, const tblite_st
                                    int* status);
 /* molecules of the last batch call that took the one-molecule path */
 int tblite_gb300_batch_last_fallbacks(void);
-/* Density solver of the batched SCF for closed shells of at least 128 orbitals: 1 (default)
+/* Density solver of the batched SCF for closed shells of at least 96 orbitals (the projection
+ * threshold): 1 (default)
  * spectral projection (SP2 squarings on the tensor cores, P = 2 X D X^T; a molecule whose
  * HOMO-LUMO gap of the converged Fock matrix is below 80 kT, or whose projection does not
  * converge, is re-run by the one-molecule path), 0 diagonalisation for every molecule.  The
@@ -51,12 +52,13 @@ int tblite_gb300_batch_last_projected(void);
  * diagonalisation, -1 the one-molecule path; returns the number of molecules recorded */
 int tblite_gb300_batch_last_modes(int* modes, int nmol);
 /* Autotuner of the batch schedule: coordinate descent over CUDA graphs (kept, or switched off;
- * never switched on against tblite_gb300_set_batch_graphs), the projection threshold (96, 112,
- * 128, 144, 157, 176, 224 orbitals or off), the bucket cut (3/4, 2/3, 4/5 of the largest orbital count), the CTAs
+ * never switched on against tblite_gb300_set_batch_graphs), the projection threshold (64, 80, 96,
+ * 112, 128, 144, 176 orbitals or off), the bucket cut (3/4, 2/3, 4/5 of the largest orbital count), the CTAs
  * per SM of the cluster tridiagonalisation (1, 2), the small-bucket tridiagonalisation (full
  * storage or packed) and the side streams (4, 8, 16), each candidate
  * timed as the wall time of a batch call (best of three) on a fixed pseudo-random sample of
- * `sample` of the given molecules (256 if <= 0).  The fastest schedule stays set.  Returns the
+ * `sample` of the given molecules (256 if <= 0); a candidate replaces the current choice only
+ * when more than 1 % faster.  The fastest schedule stays set.  Returns the
  * number of timed calls, -1 if the sample could not be evaluated. */
 int tblite_gb300_batch_autotune(tblite_context ctx, int nmol, const tblite_structure* mols,
                                 const tblite_calculator* calcs, int sample);
@@ -91,6 +93,9 @@ void tblite_gb300_set_split_gemm(int enable);
 /* number of streams (1..16, default 8) over which a batch call spreads its size buckets; 1 runs
  * the buckets one after the other, so per-kernel event times bracket each kernel alone */
 void tblite_gb300_set_batch_streams(int count);
+/* smallest orbital count of a closed shell that takes the spectral projection in the batch (the
+ * autotuner's threshold); a value <= 0 only queries.  Returns the previous value. */
+int tblite_gb300_set_projection_threshold(int nao);
 /* tridiagonalisation of batch buckets of at most 156 orbitals: 1 (default) the one-CTA kernel
  * with the full matrix in shared memory, 0 the packed lower-triangle kernel (a cluster of one or
  * two CTAs; two thirds of the FMAs) */

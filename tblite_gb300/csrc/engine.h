@@ -530,7 +530,7 @@ void sp2_slice_b(const BatchLaunch& b, bool init);
 // ozaki_pipe.cu: the converged iterate (fixed point during the projection) back to FP64 in Y
 void sp2_unfix_b(const BatchLaunch& b);
 int sp2_slot_count(int n);  // partial-sum slots of a molecule of n orbitals (3 words each)
-constexpr int SP2_MIN_NAO = 128;   // smallest orbital count that takes the projection
+constexpr int SP2_MIN_NAO = 96;    // smallest orbital count that takes the projection
 constexpr int SP2_MAX_STEPS = 64;  // squarings per projection at most
 
 }  // namespace tb

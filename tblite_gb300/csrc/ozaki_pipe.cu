@@ -238,11 +238,10 @@ struct PipeArgs {
   int ldc;
   int sym;
   int* status;
-  // a projection step applied in the epilogue: C <- 2 C - product (the old C read first); with
-  // C the iterate D this turns D^2 into 2D - D^2 in place
+  // the projection iterate (opipe_tile<true>): C holds signed 64-bit fixed-point values in units
+  // of 2^-SP2_FRAC instead of doubles (|D_ij| <= 1); sub2: C <- 2 C - product (the old element
+  // read first), which turns D^2 into 2D - D^2 in place
   int sub2;
-  // C holds signed 64-bit fixed-point values in units of 2^-SP2_FRAC instead of doubles (the
-  // projection iterate, |D_ij| <= 1): the epilogue needs no FP64 operation
   int fixed;
 };
 
@@ -521,24 +520,12 @@ __device__ __forceinline__ void opipe_tile(const PipeArgs& a, int b) {
           }
         } else if (i < a.M) {
 #pragma unroll
-          for (int t8 = 0; t8 < 16; t8 += 8) {
-            // the old elements of C first (sub2), so their loads are in flight together
-            double old[8];
-#pragma unroll
-            for (int t = 0; t < 8; ++t) {
-              const int j = j0 + 32 * half + 16 * h + t8 + t;
-              old[t] = (a.sub2 && j < a.N && !(a.sym && i < j)) ? a.C[i + (size_t)j * a.ldc] : 0.0;
-            }
-#pragma unroll
-            for (int t = 0; t < 8; ++t) {
-              const int j = j0 + 32 * half + 16 * h + t8 + t;
-              if (j < a.N && !(a.sym && i < j)) {
-                double val =
-                    tile_value(T[16 * h + t8 + t], v6[t8 + t], v7[t8 + t], ei + a.eB[j] - 14);
-                if (a.sub2) val = 2.0 * old[t] - val;
-                a.C[i + (size_t)j * a.ldc] = val;
-                if (a.sym && i != j) a.C[j + (size_t)i * a.ldc] = val;
-              }
+          for (int t = 0; t < 16; ++t) {
+            const int j = j0 + 32 * half + 16 * h + t;
+            if (j < a.N && !(a.sym && i < j)) {
+              const double val = tile_value(T[16 * h + t], v6[t], v7[t], ei + a.eB[j] - 14);
+              a.C[i + (size_t)j * a.ldc] = val;
+              if (a.sym && i != j) a.C[j + (size_t)i * a.ldc] = val;
             }
           }
         }

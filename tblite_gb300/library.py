@@ -95,6 +95,7 @@ _SIGNATURES = {
     "tblite_gb300_get_kernel_profile": (c_int, [_dbl_p, _int_p, c_int]),
     "tblite_gb300_set_split_gemm": (None, [c_int]),
     "tblite_gb300_set_batch_streams": (None, [c_int]),
+    "tblite_gb300_set_projection_threshold": (c_int, [c_int]),
     "tblite_gb300_set_small_tridiag": (None, [c_int]),
     "tblite_gb300_set_tridiag_ctas_per_sm": (None, [c_int]),
     "tblite_gb300_get_calculator_slater_exponents": (None, [c_void_p, c_void_p, _dbl_p]),
@@ -218,7 +219,8 @@ def set_profiling(enable: bool) -> None:
 
 
 def set_batch_density_solver(solver: str) -> None:
-    """Density solver of the batched SCF for closed shells of >= 128 orbitals: "purification"
+    """Density solver of the batched SCF for closed shells of >= 96 orbitals (the projection
+    threshold): "purification"
     (default, spectral projection on the tensor cores) or "diagonalization"."""
     code = DENSITY_SOLVERS.get(solver, solver) if isinstance(solver, str) else int(solver)
     if not isinstance(code, int):
@@ -293,6 +295,12 @@ def set_small_tridiag(full_storage: bool) -> None:
 def set_batch_streams(count: int) -> None:
     """Streams a batch call spreads its size buckets over (1 serialises them)."""
     load().tblite_gb300_set_batch_streams(int(count))
+
+
+def set_projection_threshold(nao: int) -> int:
+    """Smallest orbital count of a closed shell that takes the spectral projection in the
+    batch (0 only queries); returns the previous value."""
+    return int(load().tblite_gb300_set_projection_threshold(int(nao)))
 
 
 def set_tridiag_ctas_per_sm(count: int) -> None:

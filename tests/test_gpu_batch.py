@@ -163,7 +163,7 @@ def test_split_gemm_matches_fp64_gemm():
 
 
 def test_projection_matches_diagonalisation():
-    """Closed shells of >= 128 orbitals take the spectral projection in the batch (SP2 squarings
+    """Closed shells of >= 96 orbitals take the spectral projection in the batch (SP2 squarings
     on the tensor cores); the same molecules with the batched diagonalisation, and with the
     one-molecule path, agree at the parity bar, bond orders and orbital energies included."""
     from tblite_gb300 import library, workloads
