@@ -398,26 +398,30 @@ __device__ __forceinline__ void opipe_tile(const PipeArgs& a, int b) {
         const uint32_t stB = stA + PP_A_BYTES;
         // slice 0 goes in three MMAs (levels 0..3, 4..5, 6..7), the others in groups of four
         // B slices; a window starts with the first two overwriting the exact levels, the
-        // levels 6..7 are overwritten only by the very first MMA of the tile
-#pragma unroll 1
+        // levels 6..7 are overwritten only by the very first MMA of the tile.  The 13 groups
+        // (A slice p, first B slice q0, B slices nq) are a compile-time table, so the issue is
+        // a straight sequence: descriptors are the stage's base descriptors plus constants
+        // (the start-address field holds address / 16; every address stays inside the stage)
+        constexpr int GP[13] = {0, 0, 0, 1, 1, 2, 2, 3, 3, 4, 5, 6, 7};
+        constexpr int GQ[13] = {0, 4, 6, 0, 4, 0, 4, 0, 4, 0, 0, 0, 0};
+        constexpr int GN[13] = {4, 2, 2, 4, 3, 4, 2, 4, 1, 4, 3, 2, 1};
+        const uint64_t dA = sdesc_sw64(stA), dB = sdesc_sw64(stB);
+#pragma unroll
         for (int ks = 0; ks < 2; ++ks)
-#pragma unroll 1
-          for (int p = 0; p < 8; ++p)
-#pragma unroll 1
-            for (int q0 = 0; q0 < 8 - p;) {
-              const int nq = p == 0 ? (q0 == 0 ? 4 : 2) : min(4, 8 - p - q0);
-              const bool first = ks == 0 && p == 0 && (q0 < PP_EXACT ? win_start : c == 0);
-              const uint32_t acc = first ? 0u : 1u;
-              const uint32_t idesc = idesc0 | ((uint32_t)((nq * PP_N) >> 3) << 17);
-              const uint64_t da = sdesc_sw64(stA + (uint32_t)(p * 8192 + ks * 32));
-              const uint64_t db = sdesc_sw64(stB + (uint32_t)(q0 * 4096 + ks * 32));
-              asm volatile(
-                  "{\n\t.reg .pred pd;\n\tsetp.ne.b32 pd, %4, 0;\n\t"
-                  "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, pd;\n\t}" ::"r"(
-                      tmem + (uint32_t)((p + q0) * PP_N)),
-                  "l"(da), "l"(db), "r"(idesc), "r"(acc));
-              q0 += nq;
-            }
+#pragma unroll
+          for (int g = 0; g < 13; ++g) {
+            const int pg = GP[g], q0 = GQ[g], nq = GN[g];
+            const bool first = ks == 0 && pg == 0 && (q0 < PP_EXACT ? win_start : c == 0);
+            const uint32_t acc = first ? 0u : 1u;
+            const uint32_t idesc = idesc0 | ((uint32_t)((nq * PP_N) >> 3) << 17);
+            const uint64_t da = dA + (uint64_t)((pg * 8192 + ks * 32) >> 4);
+            const uint64_t db = dB + (uint64_t)((q0 * 4096 + ks * 32) >> 4);
+            asm volatile(
+                "{\n\t.reg .pred pd;\n\tsetp.ne.b32 pd, %4, 0;\n\t"
+                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, pd;\n\t}" ::"r"(
+                    tmem + (uint32_t)((pg + q0) * PP_N)),
+                "l"(da), "l"(db), "r"(idesc), "r"(acc));
+          }
         asm volatile(
             "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                 su32(&empty[s]))
