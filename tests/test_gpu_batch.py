@@ -169,8 +169,10 @@ def test_projection_matches_diagonalisation():
     from tblite_gb300 import library, workloads
     from tblite_gb300.interface import batch_fallbacks, batch_singlepoint
 
-    mols = [workloads.water_cluster_k(k, seed=500 + k) for k in (22, 31, 45, 64)]
+    # 96-126 orbitals (from the default threshold on) and 132-384
+    mols = [workloads.water_cluster_k(k, seed=500 + k) for k in (16, 19, 21, 22, 31, 45, 64)]
     mols += [workloads.alkane(n, seed=520 + n) for n in (21, 33, 47, 60)]
+    assert min(_calc(z, x).get("orbital-map").size for z, x in mols) >= 96
     res_p = batch_singlepoint([_calc(z, x) for z, x in mols])
     assert batch_fallbacks() == 0
     assert library.batch_projected() == len(mols)
@@ -269,3 +271,30 @@ def test_packed_small_tridiagonalisation():
         library.set_batch_density_solver("purification")
     for (z, x), rb in zip(mols, res):
         _compare(rb, _calc(z, x).singlepoint())
+
+
+def test_host_phases_and_projection_threshold():
+    """The host phases of the last batch call add up to at most the whole call; the projection
+    threshold setter returns the previous value and moves molecules between the solvers
+    without changing their results beyond the parity bar."""
+    from tblite_gb300 import library, workloads
+    from tblite_gb300.interface import batch_singlepoint
+
+    mols = [workloads.water_cluster_k(k, seed=560 + k) for k in (17, 20)]  # 102, 120 orbitals
+    calcs = [_calc(z, x) for z, x in mols]
+    old = library.set_projection_threshold(96)
+    try:
+        assert library.set_projection_threshold(0) == 96  # query only
+        res_p = batch_singlepoint(calcs)
+        host = library.batch_host_ms()
+        assert set(host) == set(library.BATCH_HOST_PHASES)
+        parts = sum(v for k, v in host.items() if k != "call")
+        assert all(v >= 0.0 for v in host.values()) and parts <= host["call"] + 1e-6
+        assert library.batch_projected() == 2
+        assert library.set_projection_threshold(128) == 96
+        res_d = batch_singlepoint(calcs)
+        assert library.batch_projected() == 0
+        for a, b in zip(res_p, res_d):
+            _compare(a, b)
+    finally:
+        library.set_projection_threshold(old)
