@@ -446,7 +446,7 @@ def run_batch(args):
     fp64_peak = _fp64_peak(torch)
     library.set_batch_graphs(not args.no_graphs)
     batch_singlepoint(calcs)  # first use: device memory, module loading
-    tuned_calls = library.batch_autotune(calcs, sample=512) if not args.no_tune else 0
+    tuned_calls = library.batch_autotune(calcs, sample=2048) if not args.no_tune else 0
     schedule = library.batch_schedule()
     library.set_profiling(False)  # the timed calls run their SCF iterations as CUDA graphs
     for _ in range(args.warmup):
