@@ -197,6 +197,7 @@ struct Plan {
   Piece pgrad, zgrad;  // [4][nsh], [nsh] (param_grad only)
   Piece wbo;           // [wbo_ch][nat][nat] (bond orders requested only)
   Piece img, iexp, img2, iexp2, sp2s, sp2i, sp2p;  // spectral projection (sp2 only)
+  Piece ximg0, ximg1, xexp0, xexp1;                 // X's slice images (sp2 only)
 };
 
 struct Bucket {
@@ -297,6 +298,10 @@ void layout(Plan& pl, Region* R) {
     pl.sp2s = piece<double>(R, RS, 8);
     pl.sp2i = piece<int>(R, RZ, 8);  // zeroed: the pipeline status starts clear
     pl.sp2p = piece<unsigned long long>(R, RS, 3 * (size_t)sp2_slot_count((int)n));
+    pl.ximg0 = piece<uint16_t>(R, RS, pimage_bytes((int)n, (int)n) / sizeof(uint16_t));
+    pl.ximg1 = piece<uint16_t>(R, RS, pimage_bytes((int)n, (int)n) / sizeof(uint16_t));
+    pl.xexp0 = piece<int>(R, RS, pimage_lines((int)n));
+    pl.xexp1 = piece<int>(R, RS, pimage_lines((int)n));
   }
   // scratch
   pl.cn = piece<double>(R, RS, na);
@@ -520,6 +525,10 @@ MolPtrs make_ptrs(const Plan& pl, const Bases& db) {
   q.sp2s = pl.sp2 ? db.at<double>(pl.sp2s) : nullptr;
   q.sp2i = pl.sp2 ? db.at<int>(pl.sp2i) : nullptr;
   q.sp2p = pl.sp2 ? db.at<unsigned long long>(pl.sp2p) : nullptr;
+  q.ximg[0] = pl.sp2 ? db.at<uint16_t>(pl.ximg0) : nullptr;
+  q.ximg[1] = pl.sp2 ? db.at<uint16_t>(pl.ximg1) : nullptr;
+  q.xexp[0] = pl.sp2 ? db.at<int>(pl.xexp0) : nullptr;
+  q.xexp[1] = pl.sp2 ? db.at<int>(pl.xexp1) : nullptr;
   if (pl.sp2) q.nev = pl.nao;  // the projection needs no levels during the SCF; all after it
   return q;
 }
@@ -753,6 +762,7 @@ std::vector<int> run_chunk(std::vector<Plan>& plans, Arena& ar, _tblite_context*
     d4_setup_b(L);
     d3_setup_b(L);
     cholesky_inverse_b(L);
+    if (L.sp2) pipe_x_images_b(L);  // X's slice images for the projection's products
   });
   cuda_check(cudaMemcpyAsync(h_flag.data(), d_flag, sizeof(int) * np, cudaMemcpyDeviceToHost, s),
              "flags");

@@ -400,6 +400,10 @@ struct MolPtrs {
   int* sp2i;
   unsigned long long* sp2p;
   int* sp2steps;
+  // slice images of X = L^-T, split once per geometry (projection buckets): [0] its rows (the
+  // lines of op(A) = X and of op(B) = X^T), [1] its columns (op(A) = X^T, op(B) = X)
+  uint16_t* ximg[2];
+  int* xexp[2];
 };
 
 // one launch of a batched step: the molecules list[0..count) of one size bucket
@@ -500,6 +504,9 @@ __device__ __forceinline__ Site site_of(const MolPtrs& q, int site) {
 // the same sites on the pipelined split GEMM (ozaki_pipe.cu; projection buckets: operands split
 // into the molecule's two slice images, then one batched product), n x n sites only
 void pipe_site_b(const BatchLaunch& b, int site);
+// the two slice images of X (after cholesky_inverse_b), read by the sites F X, X^T T1, X D and
+// T1 X^T instead of splitting X again
+void pipe_x_images_b(const BatchLaunch& b);
 // the same sites on the BF16 tensor cores with FP64-accurate splitting (ozaki.cu); gemm_b
 // dispatches to it for buckets of at least 128 orbitals while split_gemm_enabled
 void ogemm_b(const BatchLaunch& b, int site);

@@ -829,14 +829,24 @@ __device__ __forceinline__ SiteLines site_lines(const Site& s, int which) {
 }
 // exponents of the lines: 32 lines per block (lines strided in memory) or one warp per line
 // (k contiguous); grid.x covers lines_padded / 8 blocks for the widest molecule
+// which operand image of a site is one of X's two cached images: -1 none, else its index
+// (0 rows of X, 1 columns of X)
+__host__ __device__ __forceinline__ int site_ximage(int site, int which) {
+  if (site == GS_FX) return which ? 1 : -1;   // B = X: its columns
+  if (site == GS_XTT) return which ? -1 : 1;  // A = X^T: rows of X^T are columns of X
+  if (site == GS_XD) return which ? -1 : 0;   // A = X: its rows
+  if (site == GS_PXT) return which ? 0 : -1;  // B = X^T: columns of X^T are rows of X
+  return -1;
+}
+// xdst >= 0: the image goes to X's cached image xdst instead of img (which 0) / img2 (which 1)
 __global__ void __launch_bounds__(256) kb_pexp_site(const MolPtrs* __restrict__ mp,
                                                     const int* __restrict__ list, int site,
-                                                    int which) {
+                                                    int which, int xdst) {
   const MolPtrs& q = mp[list[blockIdx.z]];
   if (*q.flag < 0) return;
   const SiteLines L = site_lines(site_of(q, site), which);
   const int lp = lines_padded(L.lines);
-  int* e = which ? q.iexp2 : q.iexp;
+  int* e = xdst >= 0 ? q.xexp[xdst] : which ? q.iexp2 : q.iexp;
   if (!L.kcontig) {
     if ((int)blockIdx.x * 32 >= lp) return;
     pexp_rows_dev(L.M, L.ld, L.lines, L.K, lp, e, blockIdx.x);
@@ -853,14 +863,15 @@ __global__ void __launch_bounds__(256) kb_pexp_site(const MolPtrs* __restrict__ 
 }
 __global__ void __launch_bounds__(256) kb_psplit_site(const MolPtrs* __restrict__ mp,
                                                       const int* __restrict__ list, int site,
-                                                      int which) {
+                                                      int which, int xdst) {
   const MolPtrs& q = mp[list[blockIdx.z]];
   if (*q.flag < 0) return;
   const SiteLines L = site_lines(site_of(q, site), which);
   const int lp = lines_padded(L.lines), nkc = (L.K + PP_KC - 1) / PP_KC;
   if ((int)blockIdx.x >= lp / 64 || (int)blockIdx.y >= nkc) return;
-  psplit_dev(L.M, L.ld, L.kcontig, L.lines, L.K, lp / 64, which ? q.iexp2 : q.iexp,
-             which ? q.img2 : q.img, blockIdx.x, blockIdx.y);
+  psplit_dev(L.M, L.ld, L.kcontig, L.lines, L.K, lp / 64,
+             xdst >= 0 ? q.xexp[xdst] : which ? q.iexp2 : q.iexp,
+             xdst >= 0 ? q.ximg[xdst] : which ? q.img2 : q.img, blockIdx.x, blockIdx.y);
 }
 __global__ void __launch_bounds__(PP_THREADS, 1) kb_opipe_site(const MolPtrs* __restrict__ mp,
                                                               const int* __restrict__ list,
@@ -871,10 +882,11 @@ __global__ void __launch_bounds__(PP_THREADS, 1) kb_opipe_site(const MolPtrs* __
   const int tiles = ((s.M + PP_M - 1) / PP_M) * ((s.N + PP_N - 1) / PP_N);
   if ((int)blockIdx.x >= tiles) return;
   PipeArgs a{};
-  a.A = q.img;
-  a.B = q.img2;
-  a.eA = q.iexp;
-  a.eB = q.iexp2;
+  const int xa = site_ximage(site, 0), xb = site_ximage(site, 1);
+  a.A = xa >= 0 ? q.ximg[xa] : q.img;
+  a.B = xb >= 0 ? q.ximg[xb] : q.img2;
+  a.eA = xa >= 0 ? q.xexp[xa] : q.iexp;
+  a.eB = xb >= 0 ? q.xexp[xb] : q.iexp2;
   a.eshiftA = s.alpha == 2.0 ? 1 : s.alpha == 0.5 ? -1 : 0;
   a.nlbA = lines_padded(s.M) / 64;
   a.nlbB = lines_padded(s.N) / 64;
@@ -911,15 +923,34 @@ void pipe_site_b(const BatchLaunch& b, int site) {
   const int lp = pimage_lines(n), nkc = (n + PP_KC - 1) / PP_KC;
   const int tiles = ((n + PP_M - 1) / PP_M) * ((n + PP_N - 1) / PP_N);
   int tk = prof_kbegin(b.s);
-  g_kernel_launches += 5;
   for (int which = 0; which < 2; ++which) {
-    kb_pexp_site<<<dim3(lp / 8, 1, b.count), 256, 0, b.s>>>(b.mp, b.list, site, which);
-    kb_psplit_site<<<dim3(lp / 64, nkc, b.count), 256, 0, b.s>>>(b.mp, b.list, site, which);
+    if (site_ximage(site, which) >= 0) continue;  // X's image was split with the geometry
+    g_kernel_launches += 2;
+    kb_pexp_site<<<dim3(lp / 8, 1, b.count), 256, 0, b.s>>>(b.mp, b.list, site, which, -1);
+    kb_psplit_site<<<dim3(lp / 64, nkc, b.count), 256, 0, b.s>>>(b.mp, b.list, site, which,
+                                                                   -1);
   }
   prof_kend(KS_PIPE_PREP, tk, b.s);
+  ++g_kernel_launches;
   tk = prof_kbegin(b.s);
   kb_opipe_site<<<dim3(tiles, b.count), PP_THREADS, PP_SMEM, b.s>>>(b.mp, b.list, site);
   prof_kend(KS_PIPE, tk, b.s);
+}
+
+void pipe_x_images_b(const BatchLaunch& b) {
+  if (!b.count) return;
+  const int n = b.nao_max;
+  const int lp = pimage_lines(n), nkc = (n + 31) / 32;  // split blocks of 32 k
+  const int tk = prof_kbegin(b.s);
+  // rows of X as op(A) of X D, columns of X as op(B) of F X
+  const int src[2][2] = {{GS_XD, 0}, {GS_FX, 1}};
+  for (int x = 0; x < 2; ++x) {
+    g_kernel_launches += 2;
+    kb_pexp_site<<<dim3(lp / 8, 1, b.count), 256, 0, b.s>>>(b.mp, b.list, src[x][0], src[x][1], x);
+    kb_psplit_site<<<dim3(lp / 64, nkc, b.count), 256, 0, b.s>>>(b.mp, b.list, src[x][0],
+                                                                   src[x][1], x);
+  }
+  prof_kend(KS_PIPE_PREP, tk, b.s);
 }
 
 // the slice image of the iterate and the next decision for every listed molecule still
