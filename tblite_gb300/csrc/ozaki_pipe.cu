@@ -829,12 +829,13 @@ __device__ __forceinline__ SiteLines site_lines(const Site& s, int which) {
 }
 // exponents of the lines: 32 lines per block (lines strided in memory) or one warp per line
 // (k contiguous); grid.x covers lines_padded / 8 blocks for the widest molecule
-// which operand image of a site is one of X's two cached images: -1 none, else its index
-// (0 rows of X, 1 columns of X)
+// which operand image of a site is already split: -1 none (split it), 0 / 1 one of X's two
+// cached images (rows / columns of X), 2 the projection's last iterate image in img (op(B) = D
+// of X D: D is symmetric, so its columns are the lines img holds, exact for the fixed-point D)
 __host__ __device__ __forceinline__ int site_ximage(int site, int which) {
   if (site == GS_FX) return which ? 1 : -1;   // B = X: its columns
   if (site == GS_XTT) return which ? -1 : 1;  // A = X^T: rows of X^T are columns of X
-  if (site == GS_XD) return which ? -1 : 0;   // A = X: its rows
+  if (site == GS_XD) return which ? 2 : 0;    // A = X: its rows; B = D
   if (site == GS_PXT) return which ? 0 : -1;  // B = X^T: columns of X^T are rows of X
   return -1;
 }
@@ -883,10 +884,10 @@ __global__ void __launch_bounds__(PP_THREADS, 1) kb_opipe_site(const MolPtrs* __
   if ((int)blockIdx.x >= tiles) return;
   PipeArgs a{};
   const int xa = site_ximage(site, 0), xb = site_ximage(site, 1);
-  a.A = xa >= 0 ? q.ximg[xa] : q.img;
-  a.B = xb >= 0 ? q.ximg[xb] : q.img2;
+  a.A = xa >= 0 ? q.ximg[xa] : q.img;  // (xa is never 2)
+  a.B = xb == 2 ? q.img : xb >= 0 ? q.ximg[xb] : q.img2;
   a.eA = xa >= 0 ? q.xexp[xa] : q.iexp;
-  a.eB = xb >= 0 ? q.xexp[xb] : q.iexp2;
+  a.eB = xb == 2 ? q.iexp : xb >= 0 ? q.xexp[xb] : q.iexp2;
   a.eshiftA = s.alpha == 2.0 ? 1 : s.alpha == 0.5 ? -1 : 0;
   a.nlbA = lines_padded(s.M) / 64;
   a.nlbB = lines_padded(s.N) / 64;
@@ -924,7 +925,7 @@ void pipe_site_b(const BatchLaunch& b, int site) {
   const int tiles = ((n + PP_M - 1) / PP_M) * ((n + PP_N - 1) / PP_N);
   int tk = prof_kbegin(b.s);
   for (int which = 0; which < 2; ++which) {
-    if (site_ximage(site, which) >= 0) continue;  // X's image was split with the geometry
+    if (site_ximage(site, which) >= 0) continue;  // already split (X's images, the iterate)
     g_kernel_launches += 2;
     kb_pexp_site<<<dim3(lp / 8, 1, b.count), 256, 0, b.s>>>(b.mp, b.list, site, which, -1);
     kb_psplit_site<<<dim3(lp / 64, nkc, b.count), 256, 0, b.s>>>(b.mp, b.list, site, which,
