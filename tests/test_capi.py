@@ -133,3 +133,20 @@ def test_density_solver_setting():
         calc.set("density-solver", "lanczos")
     with pytest.raises(TBLiteRuntimeError, match="gap"):
         interface.Result().get("gap")
+
+
+def test_batch_host_settings_without_a_gpu(lib):
+    """Host-side batch settings need no device: the projection threshold setter returns the
+    previous value (0 only queries), and the host phases of the last batch call are reported
+    by name (zeros before any call in this process)."""
+    old = library.set_projection_threshold(0)
+    assert old > 0
+    try:
+        assert library.set_projection_threshold(120) == old
+        assert library.set_projection_threshold(0) == 120
+    finally:
+        library.set_projection_threshold(old)
+    assert library.set_projection_threshold(0) == old
+    host = library.batch_host_ms()
+    assert tuple(host) == library.BATCH_HOST_PHASES
+    assert all(v >= 0.0 for v in host.values())
