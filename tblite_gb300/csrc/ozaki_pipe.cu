@@ -26,6 +26,7 @@
 // status word is set.  Tiles are visited in groups of 8 row blocks so that the slices a wave of
 // CTAs reads stay in L2.  Symmetric products compute the tiles on and below the diagonal and
 // write each element also to its mirror position.
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -670,19 +671,22 @@ __global__ void __launch_bounds__(PP_THREADS, 1) kb_opipe_sq(const MolPtrs* __re
 // 32-bit word per lane.  Padding lines and positions get zero slices.
 //
 // Slice p of a fixed-point value Y < 2^56 is the 7-bit field a = (Y >> (49 - 7p)) & 127 (read
-// from the 28-bit half that holds it); its
-// BF16 value a 2^-7p is read off the float whose exponent field is 150 - 7p and mantissa field
-// a: that float is 2^(23 - 7p) + a 2^-7p exactly, and subtracting 2^(23 - 7p) leaves a 2^-7p
-// (exact: at most 7 significant bits), whose low 16 bits are zero.  The byte permute packs the
-// high halves of the two elements' floats into one word, and the signs go in with one OR (a
-// zero slice of a negative element becomes -0, which adds nothing to a product).
-// slice p (0..7) of Y: the 7-bit field (Y >> (49 - 7p)) & 127, from the half that holds it
-__device__ __forceinline__ uint32_t slice7(uint32_t h, uint32_t l, int p) {
-  return ((p < 4 ? h : l) >> (21 - 7 * (p & 3))) & 0x7Fu;
-}
-__device__ __forceinline__ float slice_value(uint32_t a, int p) {
-  return __uint_as_float(((uint32_t)(150 - 7 * p) << 23) | a) -
-         __uint_as_float((uint32_t)(150 - 7 * p) << 23);
+// from the 28-bit half that holds it); its BF16 value a 2^-7p is read off the BF16 number whose
+// exponent field is 134 - 7p and mantissa field a: that number is 2^(7 - 7p) + a 2^-7p exactly,
+// and subtracting 2^(7 - 7p) leaves a 2^-7p (exact: at most 7 significant bits).  Two
+// elements go through one BF16x2 subtraction, and the signs go in with one OR (a zero slice of
+// a negative element becomes -0, which adds nothing to a product).
+
+// a - b of two packed BF16 pairs (the bits of both), one BF16x2 instruction
+__device__ __forceinline__ uint32_t bf16x2_sub(uint32_t a, uint32_t b) {
+  union {
+    uint32_t u;
+    __nv_bfloat162 v;
+  } x, y, r;
+  x.u = a;
+  y.u = b;
+  r.v = __hsub2(x.v, y.v);
+  return r.u;
 }
 // the square of Y < 2^56 as a (2^56, 2^28, 1) limb triple: Y = h 2^28 + l, Y^2 = h^2 2^56 +
 // 2 h l 2^28 + l^2 (every partial product below 2^56, so per-lane sums of up to 256 stay exact)
@@ -762,10 +766,18 @@ __global__ void __launch_bounds__(256) kb_sp2_slice(const MolPtrs* __restrict__ 
     sq.add(h1, l1);
     const uint32_t signs = (w0 < 0 ? 0x8000u : 0u) | (w1 < 0 ? 0x80000000u : 0u);
     const size_t off = (size_t)slice_off(i, k, nlb);
+    // both elements at once: 16-bit lanes hold the two elements' bits 0..15 of a half (slices
+    // 3 and 2 of h, 7 and 6 of l) or its bits 14..29 (slices 1 and 0, 5 and 4); a shift and a
+    // mask put a slice's 7-bit field of both elements in the lanes' mantissa fields, the
+    // exponent field 134 - 7p makes each lane 2^(7-7p) + a 2^-7p exactly, and one BF16x2
+    // subtraction of 2^(7-7p) leaves the packed pair of slices (exact: a has 7 bits)
+    const uint32_t R[4] = {__byte_perm(h0 >> 14, h1 >> 14, 0x5410), __byte_perm(h0, h1, 0x5410),
+                           __byte_perm(l0 >> 14, l1 >> 14, 0x5410), __byte_perm(l0, l1, 0x5410)};
 #pragma unroll
     for (int pp = 0; pp < 8; ++pp) {
-      const uint32_t w = __byte_perm(__float_as_uint(slice_value(slice7(h0, l0, pp), pp)),
-                                     __float_as_uint(slice_value(slice7(h1, l1, pp), pp)), 0x7632);
+      const uint32_t bias = ((uint32_t)(134 - 7 * pp) << 7) * 0x10001u;
+      const uint32_t mag = ((R[pp >> 1] >> ((pp & 1) ? 0 : 7)) & 0x007F007Fu) | bias;
+      const uint32_t w = bf16x2_sub(mag, bias);
       *reinterpret_cast<uint32_t*>(q.img + off + pp * plane) = w | signs;
     }
   }
