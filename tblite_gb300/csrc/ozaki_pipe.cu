@@ -107,14 +107,26 @@ __device__ __forceinline__ void tmem_ld16(uint32_t addr, uint32_t (&v)[16]) {
       : "r"(addr));
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
-// BF16 bits of (-1)^sign a 2^-7p for an integer 0 <= a < 128 (exact: at most 7 significant bits).
-// a becomes a float by the 2^23 bias trick: the float with exponent 2^23 and mantissa field a is
-// 2^23 + a exactly, and subtracting 2^23 leaves a (one FP32 add on the FMA pipe instead of an
-// integer-to-float conversion); the power of two then goes into the exponent field.
-__device__ __forceinline__ uint32_t slice_bits(uint32_t a, int p, uint32_t sign) {
-  const float fa = __uint_as_float(0x4B000000u | a) - 8388608.0f;
-  const uint32_t u = __float_as_uint(fa) - ((uint32_t)(7 * p) << 23);
-  return a ? ((u >> 16) | (sign << 15)) : 0u;
+
+// |x| 2^(56 - e) as an integer (< 2^56 for |x| < 2^e): zero and subnormals give zero
+__device__ __forceinline__ uint64_t fixed_bits(uint64_t bits, int e) {
+  const int ex = (int)((bits >> 52) & 0x7FF);
+  if (ex == 0) return 0ull;
+  const uint64_t m = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+  const int sh = ex - e - 1019;
+  return sh >= 0 ? m << sh : (sh > -64 ? m >> (-sh) : 0ull);
+}
+
+// a - b of two packed BF16 pairs (the bits of both), one BF16x2 instruction
+__device__ __forceinline__ uint32_t bf16x2_sub(uint32_t a, uint32_t b) {
+  union {
+    uint32_t u;
+    __nv_bfloat162 v;
+  } x, y, r;
+  x.u = a;
+  y.u = b;
+  r.v = __hsub2(x.v, y.v);
+  return r.u;
 }
 
 // |x| as bits: for non-negative doubles the unsigned order of the bit patterns is the numeric
@@ -193,24 +205,25 @@ __device__ __forceinline__ void psplit_dev(const double* __restrict__ M, int ld,
   const int ei = e[i];
   uint32_t w[8][4];
 #pragma unroll
-  for (int p = 0; p < 8; ++p) w[p][0] = w[p][1] = w[p][2] = w[p][3] = 0u;
+  for (int c = 0; c < 8; c += 2) {  // two neighbouring k per step, as in kb_sp2_slice
+    uint32_t hh[2], ll[2], signs = 0u;
 #pragma unroll
-  for (int c = 0; c < 8; ++c) {
-    const double x = tile[li][8 * g + c];
-    const uint64_t bits = (uint64_t)__double_as_longlong(x);
-    const uint32_t sign = (uint32_t)(bits >> 63);
-    const int ex = (int)((bits >> 52) & 0x7FF);
-    uint64_t Y = 0;
-    if (ex != 0) {  // zero and subnormals give zero slices
-      const uint64_t m = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-      const int sh = ex - ei - 1019;  // Y = |x| 2^(56 - e) < 2^56
-      if (sh >= 0) Y = m << sh;
-      else if (sh > -64) Y = m >> (-sh);
+    for (int d = 0; d < 2; ++d) {
+      const uint64_t bits = (uint64_t)__double_as_longlong(tile[li][8 * g + c + d]);
+      signs |= (uint32_t)(bits >> 63) << (15 + 16 * d);
+      const uint64_t Y = fixed_bits(bits, ei);  // |x| 2^(56 - e) < 2^56; zero and subnormals: 0
+      hh[d] = (uint32_t)(Y >> 28);
+      ll[d] = (uint32_t)Y & 0xFFFFFFFu;
     }
+    const uint32_t R[4] = {__byte_perm(hh[0] >> 14, hh[1] >> 14, 0x5410),
+                           __byte_perm(hh[0], hh[1], 0x5410),
+                           __byte_perm(ll[0] >> 14, ll[1] >> 14, 0x5410),
+                           __byte_perm(ll[0], ll[1], 0x5410)};
 #pragma unroll
     for (int p = 0; p < 8; ++p) {
-      const uint32_t a = (uint32_t)(Y >> (49 - 7 * p)) & 0x7Fu;
-      w[p][c >> 1] |= slice_bits(a, p, sign) << ((c & 1) * 16);
+      const uint32_t bias = ((uint32_t)(134 - 7 * p) << 7) * 0x10001u;
+      const uint32_t mag = ((R[p >> 1] >> ((p & 1) ? 0 : 7)) & 0x007F007Fu) | bias;
+      w[p][c >> 1] = bf16x2_sub(mag, bias) | signs;
     }
   }
   // [k chunk][slice][line block][64 lines x 64 B, 16-byte chunks swizzled]
@@ -263,14 +276,6 @@ __device__ __forceinline__ int slice_off(int line, int k, int nlb) {
          (k & 7);
 }
 
-// |x| 2^(56 - e) as an integer (< 2^56 for |x| < 2^e): zero and subnormals give zero
-__device__ __forceinline__ uint64_t fixed_bits(uint64_t bits, int e) {
-  const int ex = (int)((bits >> 52) & 0x7FF);
-  if (ex == 0) return 0ull;
-  const uint64_t m = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-  const int sh = ex - e - 1019;
-  return sh >= 0 ? m << sh : (sh > -64 ? m >> (-sh) : 0ull);
-}
 
 // C element (i, j) of a finished tile from the exact levels T, the FP32 levels v6 + v7 and the
 // scale 2^sc: C = (T + F 2^35) 2^(sc - 35), F = levels 6 + 7 summed in FP32 (F < 2^-42 of the
@@ -677,17 +682,6 @@ __global__ void __launch_bounds__(PP_THREADS, 1) kb_opipe_sq(const MolPtrs* __re
 // elements go through one BF16x2 subtraction, and the signs go in with one OR (a zero slice of
 // a negative element becomes -0, which adds nothing to a product).
 
-// a - b of two packed BF16 pairs (the bits of both), one BF16x2 instruction
-__device__ __forceinline__ uint32_t bf16x2_sub(uint32_t a, uint32_t b) {
-  union {
-    uint32_t u;
-    __nv_bfloat162 v;
-  } x, y, r;
-  x.u = a;
-  y.u = b;
-  r.v = __hsub2(x.v, y.v);
-  return r.u;
-}
 // the square of Y < 2^56 as a (2^56, 2^28, 1) limb triple: Y = h 2^28 + l, Y^2 = h^2 2^56 +
 // 2 h l 2^28 + l^2 (every partial product below 2^56, so per-lane sums of up to 256 stay exact)
 struct Sq3 {
