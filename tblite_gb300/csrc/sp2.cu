@@ -48,21 +48,28 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-// Gershgorin bounds of A and a fresh projection state (one block per molecule)
+// Gershgorin bounds of A and a fresh projection state: one block per 8 columns (a warp per
+// column) writes its columns' lowest and highest bound into its partial-sum slot (the slots of
+// the later slice passes, free here); the last block of the molecule to finish (a fence and the
+// block count sp2i[5], zero between passes) takes the minimum and maximum over the slots in a
+// fixed order and resets the state
 __global__ void __launch_bounds__(256) kb_sp2_start(BARGS) {
   BMOL;
-  if (*q.flag < 0) return;
+  const int n = q.m.nao, lp = ((n + 127) / 128) * 128, nblk = lp / 8;
+  if ((int)blockIdx.x >= nblk || *q.flag < 0) return;  // uniform over the block
   __shared__ double smin[8], smax[8];
-  const int n = q.m.nao, lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __shared__ int last;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int j = (int)blockIdx.x * 8 + wid;
   double lo = 1e300, hi = -1e300;
-  for (int j = wid; j < n; j += 8) {
+  if (j < n) {
     const double* col = q.A + (size_t)j * n;
     double r = 0.0;
     for (int i = lane; i < n; i += 32)
       if (i != j) r += fabs(col[i]);
     r = warp_sum(r);
-    lo = fmin(lo, col[j] - r);
-    hi = fmax(hi, col[j] + r);
+    lo = col[j] - r;
+    hi = col[j] + r;
   }
   if (lane == 0) {
     smin[wid] = lo;
@@ -74,21 +81,33 @@ __global__ void __launch_bounds__(256) kb_sp2_start(BARGS) {
       lo = fmin(lo, smin[w]);
       hi = fmax(hi, smax[w]);
     }
-    lo = fmin(lo, smin[0]);
-    hi = fmax(hi, smax[0]);
-    if (!(hi > lo)) hi = lo + 1.0;  // a 1 x 1 or scalar A: any positive width
-    q.sp2s[0] = lo;
-    q.sp2s[1] = hi;
-    q.sp2s[2] = q.sp2s[3] = q.sp2s[4] = 1e300;  // idempotency errors e(k-2), e(k-1), e(k)
-    q.sp2i[0] = 0;   // converged
-    q.sp2i[1] = 0;   // steps taken
-    q.sp2i[2] = -1;  // update of the current step: 1 square, 0 2D - D^2, -1 none
-    q.sp2i[4] = 0;   // an element outside the fixed-point range
-    q.sp2i[5] = 0;   // blocks of the current slice pass finished (the last one decides)
-    // sp2i[3]: tensor-core pipeline status, set by any pipelined product of the molecule; it
-    // starts zeroed with the batch and is never cleared (a failure sends the molecule away)
-    q.scal[0] = 0.0;  // no Fermi entropy: the occupations are 0/2 (checked after the SCF)
+    unsigned long long* pt = q.sp2p + 3 * blockIdx.x;
+    pt[0] = (unsigned long long)__double_as_longlong(lo);
+    pt[1] = (unsigned long long)__double_as_longlong(hi);
+    __threadfence();
+    last = atomicAdd(q.sp2i + 5, 1) == nblk - 1;
   }
+  __syncthreads();
+  if (!last || threadIdx.x != 0) return;
+  __threadfence();
+  lo = 1e300;
+  hi = -1e300;
+  for (int t = 0; t < nblk; ++t) {
+    lo = fmin(lo, __longlong_as_double((long long)__ldcg(q.sp2p + 3 * t)));
+    hi = fmax(hi, __longlong_as_double((long long)__ldcg(q.sp2p + 3 * t + 1)));
+  }
+  if (!(hi > lo)) hi = lo + 1.0;  // a 1 x 1 or scalar A: any positive width
+  q.sp2s[0] = lo;
+  q.sp2s[1] = hi;
+  q.sp2s[2] = q.sp2s[3] = q.sp2s[4] = 1e300;  // idempotency errors e(k-2), e(k-1), e(k)
+  q.sp2i[0] = 0;   // converged
+  q.sp2i[1] = 0;   // steps taken
+  q.sp2i[2] = -1;  // update of the current step: 1 square, 0 2D - D^2, -1 none
+  q.sp2i[4] = 0;   // an element outside the fixed-point range
+  q.sp2i[5] = 0;   // blocks of the current pass finished (the last one decides)
+  // sp2i[3]: tensor-core pipeline status, set by any pipelined product of the molecule; it
+  // starts zeroed with the batch and is never cleared (a failure sends the molecule away)
+  q.scal[0] = 0.0;  // no Fermi entropy: the occupations are 0/2 (checked after the SCF)
 }
 
 // after the step budget: a projection that has not converged sends the molecule to the
@@ -118,7 +137,7 @@ void sp2_density_b(const BatchLaunch& b, int steps) {
   pipe_site_b(b, GS_FX);   // T1 = F X
   pipe_site_b(b, GS_XTT);  // A = X^T T1
   ++g_kernel_launches;
-  kb_sp2_start<<<dim3(1, 1, b.count), 256, 0, b.s>>>(b.mp, b.list);
+  kb_sp2_start<<<dim3(pimage_lines(b.nao_max) / 8, 1, b.count), 256, 0, b.s>>>(b.mp, b.list);
   sp2_slice_b(b, true);  // D0, its slice image and the first decision
   for (int k = 0; k < steps; ++k) {
     sp2_square_b(b);         // D^2 and the next iterate over D
